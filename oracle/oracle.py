@@ -1,0 +1,210 @@
+"""ctypes wrapper of the FP64 CPU oracle (oracle/_build/libswm_oracle.so).
+
+TEST INFRASTRUCTURE ONLY.  The oracle restates the reference Fortran
+shallow-water hot path (vvshashkin/cubedsphere_sbp_swm) in C++; see
+swm_oracle.cpp for the file:line each routine follows.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg import this module,
+and only as the checker or as the timed CPU baseline.
+
+Arrays use the reference layout: shape (6, N+1, N+1) = (panel, j, i), FP64,
+C-contiguous (i fastest).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libswm_oracle.so")
+_lib = None
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (portable flags, a few seconds)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < max(
+            os.path.getmtime(os.path.join(_HERE, f))
+            for f in ("swm_oracle.cpp", "swm_oracle.h", "Makefile")
+        )
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        vp = ctypes.c_void_p
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, _D]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_npts.argtypes = [vp]
+        L.orc_npts.restype = ctypes.c_int
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_get_threads.restype = ctypes.c_int
+        L.orc_geometry.argtypes = [vp] + [_D] * 8
+        L.orc_bases.argtypes = [vp] + [_D] * 4
+        L.orc_sync_weights.argtypes = [vp] + [_D] * 4
+        for name, n in (("orc_co2contra", 4), ("orc_contra2co", 4), ("orc_grad", 3),
+                        ("orc_div", 3), ("orc_curl", 3), ("orc_sync_scalar", 1),
+                        ("orc_sync_vector_cov", 2), ("orc_coriolis", 6),
+                        ("orc_apply", 7), ("orc_diagnostics", 5)):
+            getattr(L, name).argtypes = [vp] + [_D] * n
+        L.orc_rk4.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int]
+        L.orc_l2norm.argtypes = [vp, _D]
+        L.orc_l2norm.restype = ctypes.c_double
+        L.orc_mass.argtypes = [vp, _D]
+        L.orc_mass.restype = ctypes.c_double
+        for name in ("orc_golden_div", "orc_golden_grad", "orc_golden_curl"):
+            getattr(L, name).argtypes = [ctypes.c_int, ctypes.c_int, _D]
+            getattr(L, name).restype = ctypes.c_int
+        for name in ("orc_golden_co2contra", "orc_golden_contra2co"):
+            getattr(L, name).argtypes = [ctypes.c_int, _D]
+            getattr(L, name).restype = ctypes.c_int
+        L.orc_golden_quadrature.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_golden_quadrature.restype = ctypes.c_double
+        L.orc_golden_rk4_iomega.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_D)
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+class OracleDomain:
+    """FP64 oracle domain: geometry + SBP operator of one configuration."""
+
+    def __init__(self, N, sbp_order=42, radius=6.371e6, grav=9.80616,
+                 omega=7.292e-5, axis=(0.0, 0.0, 1.0)):
+        L = lib()
+        ax = np.asarray(axis, dtype=np.float64)
+        self._h = L.orc_create(int(N), int(sbp_order), float(radius), float(grav),
+                               float(omega), _p(ax))
+        if not self._h:
+            raise ValueError(f"oracle: unsupported N={N} / sbp_order={sbp_order}")
+        self.N, self.n, self.sbp_order = int(N), int(N) + 1, int(sbp_order)
+        self.shape = (6, self.n, self.n)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def zeros(self):
+        return np.zeros(self.shape)
+
+    def geometry(self):
+        out = {k: self.zeros() for k in ("J", "Qi1", "Qi2", "Qi3", "f", "rx", "ry", "rz")}
+        lib().orc_geometry(self._h, *(_p(out[k]) for k in
+                                      ("J", "Qi1", "Qi2", "Qi3", "f", "rx", "ry", "rz")))
+        return out
+
+    def bases(self):
+        out = {k: np.zeros(self.shape + (3,)) for k in ("a1", "a2", "b1", "b2")}
+        lib().orc_bases(self._h, *(_p(out[k]) for k in ("a1", "a2", "b1", "b2")))
+        return out
+
+    def sync_weights(self):
+        out = [np.zeros(self.n) for _ in range(4)]
+        lib().orc_sync_weights(self._h, *(_p(o) for o in out))
+        return dict(zip(("qb", "qt", "ql", "qr"), out))
+
+    def co2contra(self, u, v):
+        ut, vt = self.zeros(), self.zeros()
+        lib().orc_co2contra(self._h, _p(u), _p(v), _p(ut), _p(vt))
+        return ut, vt
+
+    def grad(self, f):
+        gx, gy = self.zeros(), self.zeros()
+        lib().orc_grad(self._h, _p(f), _p(gx), _p(gy))
+        return gx, gy
+
+    def div(self, u, v):
+        out = self.zeros()
+        lib().orc_div(self._h, _p(u), _p(v), _p(out))
+        return out
+
+    def curl(self, u, v):
+        out = self.zeros()
+        lib().orc_curl(self._h, _p(u), _p(v), _p(out))
+        return out
+
+    def sync_scalar(self, f):
+        f = np.array(f, dtype=np.float64, order="C")
+        lib().orc_sync_scalar(self._h, _p(f))
+        return f
+
+    def sync_vector_cov(self, gx, gy):
+        gx = np.array(gx, dtype=np.float64, order="C")
+        gy = np.array(gy, dtype=np.float64, order="C")
+        lib().orc_sync_vector_cov(self._h, _p(gx), _p(gy))
+        return gx, gy
+
+    def coriolis(self, hu, hv, h, curl):
+        cu, cv = self.zeros(), self.zeros()
+        lib().orc_coriolis(self._h, _p(hu), _p(hv), _p(h), _p(curl), _p(cu), _p(cv))
+        return cu, cv
+
+    def apply(self, h, u, v, hs=None):
+        th, tu, tv = self.zeros(), self.zeros(), self.zeros()
+        lib().orc_apply(self._h, _p(hs), _p(h), _p(u), _p(v), _p(th), _p(tu), _p(tv))
+        return th, tu, tv
+
+    def rk4(self, h, u, v, dt, nsteps=1, hs=None):
+        h, u, v = (np.array(a, dtype=np.float64, order="C") for a in (h, u, v))
+        lib().orc_rk4(self._h, _p(hs), _p(h), _p(u), _p(v), float(dt), int(nsteps))
+        return h, u, v
+
+    def diagnostics(self, h, u, v, hs=None):
+        out = np.zeros(7)
+        lib().orc_diagnostics(self._h, _p(hs), _p(h), _p(u), _p(v), _p(out))
+        return out
+
+    def l2norm(self, f):
+        return lib().orc_l2norm(self._h, _p(np.ascontiguousarray(f, dtype=np.float64)))
+
+    def mass(self, f):
+        return lib().orc_mass(self._h, _p(np.ascontiguousarray(f, dtype=np.float64)))
+
+
+def golden(kind: str, N: int = 32, sbp_order: int = 42):
+    """Values printed by the reference known-answer test at (N, nz=3)."""
+    L = lib()
+    if kind in ("div", "curl"):
+        out = np.zeros(4)
+        rc = getattr(L, f"orc_golden_{kind}")(int(N), int(sbp_order), _p(out))
+    elif kind == "grad":
+        out = np.zeros(2)
+        rc = L.orc_golden_grad(int(N), int(sbp_order), _p(out))
+    elif kind in ("co2contra", "contra2co"):
+        out = np.zeros(2)
+        rc = getattr(L, f"orc_golden_{kind}")(int(N), _p(out))
+    else:
+        raise ValueError(kind)
+    if rc != 0:
+        raise ValueError(f"oracle golden {kind} failed for order {sbp_order}")
+    return out
+
+
+def quadrature_error(N: int, sbp_order: int, max_order: int) -> float:
+    return lib().orc_golden_quadrature(int(N), int(sbp_order), int(max_order))
+
+
+def rk4_iomega_error() -> float:
+    return lib().orc_golden_rk4_iomega()

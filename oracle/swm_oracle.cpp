@@ -1,0 +1,960 @@
+// swm_oracle.cpp -- FP64 CPU oracle for the shallow-water hot path.
+//
+// TEST INFRASTRUCTURE ONLY (see swm_oracle.h).  This file restates, in plain
+// C++, the algorithms of the reference Fortran code (vvshashkin/
+// cubedsphere_sbp_swm); every routine names the reference file:line it
+// follows.  It keeps the reference's evaluation order where that is cheap
+// (SBP row sums left to right, the corner "/3" averages, the two-part RK4
+// update) so that the oracle reproduces the reference's printed golden
+// numbers.  OpenMP parallelises the field loops over panel rows for the timed
+// CPU baseline; every result is independent of the thread count (no parallel
+// floating-point reductions).
+
+#include "swm_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const double PI = 3.141592653589793238462643383279502884;  // acos(-1._8)
+
+// ---------------------------------------------------------------------------
+// Cube topology: panel frames ex, ey, inward normal n and integer origin r.
+// topology/cubed_sphere_topology_mod.f90:29-55 (same six frames).
+// ---------------------------------------------------------------------------
+const int TEX[6][3] = {{-1, 0, 0}, {0, 0, -1}, {1, 0, 0}, {0, 0, 1}, {1, 0, 0}, {1, 0, 0}};
+const int TEY[6][3] = {{0, 1, 0}, {0, 1, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, -1}};
+const int TN[6][3]  = {{0, 0, 1}, {-1, 0, 0}, {0, 0, -1}, {1, 0, 0}, {0, 1, 0}, {0, -1, 0}};
+const int TR[6][3]  = {{1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 1, 1}};
+
+int dot3i(const int* a, const int* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Unfolded frame of target panel pt extended across the edge it shares with
+// source panel ps (cubed_sphere_topology_mod.f90:80-148 and 180-239).
+struct Unfold {
+  int exl[3], eyl[3], rl[3], shift[2];
+};
+
+Unfold unfold(int ps, int pt, int nx, int ny) {
+  Unfold u{};
+  const int d_right = dot3i(TEX[pt], TN[ps]);
+  const int d_bt = dot3i(TEY[pt], TN[ps]);
+  const int d_opp = dot3i(TN[pt], TN[ps]);
+  for (int c = 0; c < 3; ++c) {
+    if (d_right == -1) {  // source lies right of target
+      u.exl[c] = TN[pt][c]; u.eyl[c] = TEY[pt][c]; u.rl[c] = TR[pt][c] + TEX[pt][c];
+    } else if (d_right == 1) {  // left
+      u.exl[c] = -TN[pt][c]; u.eyl[c] = TEY[pt][c]; u.rl[c] = TR[pt][c] + TN[pt][c];
+    } else if (d_bt == 1) {  // bottom
+      u.exl[c] = TEX[pt][c]; u.eyl[c] = -TN[pt][c]; u.rl[c] = TR[pt][c] + TN[pt][c];
+    } else if (d_bt == -1) {  // top
+      u.exl[c] = TEX[pt][c]; u.eyl[c] = TN[pt][c]; u.rl[c] = TR[pt][c] + TEY[pt][c];
+    } else if (d_opp == -1) {  // opposite
+      u.exl[c] = -TEX[pt][c]; u.eyl[c] = TEY[pt][c];
+      u.rl[c] = TR[pt][c] + TEX[pt][c] + TN[pt][c];
+    }
+  }
+  if (d_right == -1) { u.shift[0] = nx; u.shift[1] = 0; }
+  else if (d_right == 1) { u.shift[0] = -nx; u.shift[1] = 0; }
+  else if (d_bt == 1) { u.shift[0] = 0; u.shift[1] = -ny; }
+  else if (d_bt == -1) { u.shift[0] = 0; u.shift[1] = ny; }
+  else { u.shift[0] = 2 * nx; u.shift[1] = 0; }
+  return u;
+}
+
+// transform_index: 1-based node of panel ps -> (possibly halo) index of pt.
+void transform_index(int ps, int is, int js, int pt, int nx, int ny, int& it, int& jt) {
+  if (ps == pt) { it = is; jt = js; return; }
+  Unfold u = unfold(ps, pt, nx, ny);
+  int dr[3];
+  for (int c = 0; c < 3; ++c) dr[c] = TR[ps][c] - u.rl[c];
+  const int ex_ex = dot3i(TEX[ps], u.exl), ex_ey = dot3i(TEY[ps], u.exl), ex_r = dot3i(dr, u.exl);
+  const int ey_ex = dot3i(TEX[ps], u.eyl), ey_ey = dot3i(TEY[ps], u.eyl), ey_r = dot3i(dr, u.eyl);
+  it = (is - 1) * ex_ex + (js - 1) * ex_ey + (nx - 1) * ex_r + 1 + u.shift[0];
+  jt = (is - 1) * ey_ex + (js - 1) * ey_ey + (ny - 1) * ey_r + 1 + u.shift[1];
+}
+
+// find_basis_orientation(pn_source, pn_target): loop direction and the
+// swapped/negated component order used when packing vectors.
+void basis_orientation(int ps, int pt, int& istep, int& jstep, bool& dim_i) {
+  if (ps == pt) { istep = 1; jstep = 1; dim_i = true; return; }
+  Unfold u = unfold(ps, pt, 2, 2);
+  const int ex_ex = dot3i(TEX[ps], u.exl), ex_ey = dot3i(TEY[ps], u.exl);
+  const int ey_ex = dot3i(TEX[ps], u.eyl), ey_ey = dot3i(TEY[ps], u.eyl);
+  if (ex_ex != 0) { dim_i = true; istep = ex_ex; jstep = ey_ey; }
+  else { dim_i = false; istep = ex_ey; jstep = ey_ex; }
+}
+
+// ---------------------------------------------------------------------------
+// SBP first-derivative operators (sbp_operators_collection_mod.f90:15-85,
+// sbp_factory_mod.f90:38-179).  Ql[r][m] multiplies f[m] for left closure row
+// r (0-based); the right block is the sign-flipped mirror.
+// ---------------------------------------------------------------------------
+struct Sbp {
+  int ne = 0, nw = 0;
+  std::vector<double> Ql;   // ne*nw
+  std::vector<int> last;    // nonzero count per closure row
+  std::vector<double> Qin;  // interior stencil
+  int inshift = 0;
+  std::vector<double> A;    // diagonal norm (quadrature) edge weights
+};
+
+Sbp make_sbp(int order) {
+  Sbp s;
+  if (order == 21) {
+    s.ne = 1; s.nw = 2;
+    s.Ql = {-1.0, 1.0};
+    s.last = {2};
+    s.Qin = {-0.5, 0.0, 0.5}; s.inshift = -1;
+    s.A = {0.5, 1.0};
+  } else if (order == 42) {
+    s.ne = 4; s.nw = 6;
+    s.Ql = {-1.4117647058823528, 1.7352941176470589, -0.2352941176470588, -0.08823529411764705, 0.0, 0.0,
+            -0.5, 0.0, 0.5, 0.0, 0.0, 0.0,
+            0.09302325581395347, -0.686046511627907, 0.0, 0.686046511627907, -0.09302325581395347, 0.0,
+            0.030612244897959186, -0.0, -0.6020408163265307, 0.0, 0.653061224489796, -0.0816326530612245};
+    s.last = {4, 3, 5, 6};
+    s.Qin = {1.0 / 12.0, -2.0 / 3.0, 0.0, 2.0 / 3.0, -1.0 / 12.0}; s.inshift = -2;
+    s.A = {17.0 / 48.0, 59.0 / 48.0, 43.0 / 48.0, 49.0 / 48.0};
+  } else if (order == 43) {
+    s.ne = 4; s.nw = 6;
+    s.Ql = {-1.8280236842718398, 2.978054584697369, -1.4653148294044123, 0.3078538227474199, 0.008136925288119662, -0.0007068190566565205,
+            -0.37814159126691327, -0.31480210500706657, 0.707290999364066, 0.04835554461933453, -0.06866771096803422, 0.005964863258613564,
+            0.1162478575921292, -0.8028500807354999, 0.21558841368737428, 0.5078566674295846, -0.03231754093993847, -0.004525317033649745,
+            -0.010287398573128293, 0.12592344801071614, -0.7341531396449149, 0.04979271660173103, 0.6506171865540596, -0.08189281294846368};
+    s.last = {6, 6, 6, 6};
+    s.Qin = {1.0 / 12.0, -2.0 / 3.0, 0.0, 2.0 / 3.0, -1.0 / 12.0}; s.inshift = -2;
+    s.A = {17.0 / 48.0, 59.0 / 48.0, 43.0 / 48.0, 49.0 / 48.0};
+  } else if (order == 63) {
+    // Sixth-order interior / third-order boundary closure with one free
+    // parameter q56, assembled from its rational entries exactly as the
+    // reference parameter block does.
+    const double A1 = 13649.0 / 43200.0, A2 = 12013.0 / 8640.0, A3 = 2711.0 / 4320.0,
+                 A4 = 5359.0 / 4320.0, A5 = 7877.0 / 8640.0, A6 = 43801.0 / 43200.0;
+    const double q56 = 5591070156686698065364559.0 / 7931626489314500743872000.0;
+    const double q11 = -1.0 / 2.0;
+    const double q12 = -953.0 / 16200.0 + q56;
+    const double q13 = 715489.0 / 259200.0 - (4.0 * q56);
+    const double q14 = -62639.0 / 14400.0 + (6.0 * q56);
+    const double q15 = 147127.0 / 51840.0 - (4.0 * q56);
+    const double q16 = -89387.0 / 129600.0 + q56;
+    const double q23 = -57139.0 / 8640.0 + (10.0 * q56);
+    const double q24 = 745733.0 / 51840.0 - (20.0 * q56);
+    const double q25 = -18343.0 / 1728.0 + (15.0 * q56);
+    const double q26 = 240569.0 / 86400.0 - (4.0 * q56);
+    const double q34 = -176839.0 / 12960.0 + (20.0 * q56);
+    const double q35 = 242111.0 / 17280.0 - (20.0 * q56);
+    const double q36 = -182261.0 / 43200.0 + (6.0 * q56);
+    const double q45 = -165041.0 / 25920.0 + (10.0 * q56);
+    const double q46 = 710473.0 / 259200.0 - (4.0 * q56);
+    const double q47 = 1.0 / 60.0, q57 = -3.0 / 20.0, q58 = 1.0 / 60.0;
+    const double q67 = 3.0 / 4.0, q68 = -3.0 / 20.0, q69 = 1.0 / 60.0;
+    s.ne = 6; s.nw = 9;
+    s.Ql = {q11 / A1, q12 / A1, q13 / A1, q14 / A1, q15 / A1, q16 / A1, 0.0, 0.0, 0.0,
+            -q12 / A2, 0.0, q23 / A2, q24 / A2, q25 / A2, q26 / A2, 0.0, 0.0, 0.0,
+            -q13 / A3, -q23 / A3, 0.0, q34 / A3, q35 / A3, q36 / A3, 0.0, 0.0, 0.0,
+            -q14 / A4, -q24 / A4, -q34 / A4, 0.0, q45 / A4, q46 / A4, q47 / A4, 0.0, 0.0,
+            -q15 / A5, -q25 / A5, -q35 / A5, -q45 / A5, 0.0, q56 / A5, q57 / A5, q58 / A5, 0.0,
+            -q16 / A6, -q26 / A6, -q36 / A6, -q46 / A6, -q56 / A6, 0.0, q67 / A6, q68 / A6, q69 / A6};
+    s.last = {6, 6, 6, 7, 8, 9};
+    s.Qin = {-1.0 / 60.0, 3.0 / 20.0, -3.0 / 4.0, 0.0, 3.0 / 4.0, -3.0 / 20.0, 1.0 / 60.0};
+    s.inshift = -3;
+    s.A = {A1, A2, A3, A4, A5, A6};
+  }
+  return s;
+}
+
+// sbp_apply (sbp_operator_mod.f90:152-228) along one line of n values with
+// stride st: out[k] for k in [0,n).
+inline double sbp_point(const Sbp& s, const double* f, int n, int st, int k) {
+  double acc = 0.0;
+  if (k < s.ne) {
+    const double* q = &s.Ql[k * s.nw];
+    for (int m = 0; m < s.last[k]; ++m) acc += q[m] * f[m * st];
+  } else if (k < n - s.ne) {
+    const int w = (int)s.Qin.size();
+    for (int t = 0; t < w; ++t) acc += s.Qin[t] * f[(k + s.inshift + t) * st];
+  } else {
+    // mirrored right block, summed from the outermost tap inwards like the
+    // reference's Qr(nwst:nw) * f(mx:n)
+    const int r = n - 1 - k;
+    const double* q = &s.Ql[r * s.nw];
+    for (int m = s.last[r] - 1; m >= 0; --m) acc += (-q[m]) * f[(n - 1 - m) * st];
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// ECS metric on the prototype face (equiang_cs/ecs_metric_mod.f90:326-478).
+// ---------------------------------------------------------------------------
+void r_proto(double a, double b, double r[3]) {
+  const double ta = std::tan(a), tb = std::tan(b);
+  const double d = std::sqrt(1.0 + ta * ta + tb * tb);
+  r[0] = ta / d; r[1] = tb / d; r[2] = 1.0 / d;
+}
+void a1_proto(double a, double b, double v[3]) {
+  const double ta = std::tan(a), tb = std::tan(b);
+  const double p = std::pow(1.0 + ta * ta + tb * tb, 1.5);
+  v[0] = (1.0 + ta * ta) * (1.0 + tb * tb) / p;
+  v[1] = -ta * tb * (1.0 + ta * ta) / p;
+  v[2] = -ta * (1.0 + ta * ta) / p;
+}
+void a2_proto(double a, double b, double v[3]) {
+  const double ta = std::tan(a), tb = std::tan(b);
+  const double p = std::pow(1.0 + ta * ta + tb * tb, 1.5);
+  v[0] = -ta * tb * (1.0 + tb * tb) / p;
+  v[1] = (1.0 + ta * ta) * (1.0 + tb * tb) / p;
+  v[2] = -tb * (1.0 + tb * tb) / p;
+}
+void b1_proto(double a, double b, double v[3]) {
+  const double ta = std::tan(a), tb = std::tan(b);
+  const double s = std::sqrt(1.0 + ta * ta + tb * tb);
+  v[0] = (1.0 + tb * tb - (ta * tb) * (ta * tb) / (1.0 + ta * ta)) / s;
+  v[1] = 0.0;
+  v[2] = -ta * (1.0 + tb * tb / (1.0 + ta * ta)) / s;
+}
+void b2_proto(double a, double b, double v[3]) {
+  const double ta = std::tan(a), tb = std::tan(b);
+  const double s = std::sqrt(1.0 + ta * ta + tb * tb);
+  v[0] = 0.0;
+  v[1] = ((1.0 + ta * ta) - (ta * tb) * (ta * tb) / (1.0 + tb * tb)) / s;
+  v[2] = -tb * (ta * ta / (1.0 + tb * tb) + 1.0) / s;
+}
+// ecs_proto2realface with the identity rotation matrix.
+void to_face(int p, const double v[3], double out[3]) {
+  for (int c = 0; c < 3; ++c) out[c] = TEX[p][c] * v[0] + TEY[p][c] * v[1] - TN[p][c] * v[2];
+}
+
+// Halo ring slot: side 0 = i=0 (left), 1 = i=n+1 (right), 2 = j=0 (bottom),
+// 3 = j=n+1 (top); position k = 0..n-1 along the side.
+struct RingSrc {
+  int q;            // sender panel
+  int node;         // sender node index within its panel (j*n+i)
+  int istep, jstep;
+  bool dim_i;
+};
+
+}  // namespace
+
+struct orc_domain {
+  int N = 0, n = 0, order = 42;
+  double hx = 0.0, scale = 1.0, grav = 9.80616, omega = 1.0, axis[3] = {0, 0, 1};
+  Sbp sbp;
+  std::vector<double> A;                // quadrature weights per line index (n)
+  std::vector<double> J, Qi1, Qi2, Qi3, Q1, Q2, Q3, f, rx, ry, rz;
+  std::vector<double> a1, a2, b1, b2;   // 3 per node
+  std::vector<double> qb, qt, ql, qr;   // covariant sync weights
+  std::vector<RingSrc> ring;            // [p][side][k]
+  int npts() const { return 6 * n * n; }
+};
+
+namespace {
+
+int g_threads = 1;
+
+double alpha_of(const orc_domain& d, int i0) { return -0.25 * PI + i0 * d.hx; }
+
+void build_ring(orc_domain& d) {
+  const int n = d.n;
+  d.ring.assign(6 * 4 * n, RingSrc{-1, -1, 0, 0, true});
+  for (int p = 0; p < 6; ++p) {
+    for (int q = 0; q < 6; ++q) {
+      if (q == p) continue;
+      int istep, jstep; bool dim_i;
+      basis_orientation(p, q, istep, jstep, dim_i);
+      for (int js = 1; js <= n; ++js)
+        for (int is = 1; is <= n; ++is) {
+          if (is != 1 && is != n && js != 1 && js != n) continue;
+          int it, jt;
+          transform_index(q, is, js, p, n, n, it, jt);
+          int side = -1, k = -1;
+          if (it == 0 && jt >= 1 && jt <= n) { side = 0; k = jt - 1; }
+          else if (it == n + 1 && jt >= 1 && jt <= n) { side = 1; k = jt - 1; }
+          else if (jt == 0 && it >= 1 && it <= n) { side = 2; k = it - 1; }
+          else if (jt == n + 1 && it >= 1 && it <= n) { side = 3; k = it - 1; }
+          if (side < 0) continue;
+          d.ring[(p * 4 + side) * n + k] = RingSrc{q, (js - 1) * n + (is - 1), istep, jstep, dim_i};
+        }
+    }
+  }
+  for (const RingSrc& r : d.ring)
+    if (r.q < 0) std::abort();  // every ring slot has exactly one sender
+}
+
+void build(orc_domain& d, int N, int order, double radius, double grav, double omega,
+           const double axis[3]) {
+  d.N = N; d.n = N + 1; d.order = order;
+  d.scale = radius; d.grav = grav; d.omega = omega;
+  const double an = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+  for (int c = 0; c < 3; ++c) d.axis[c] = axis[c] / an;
+  d.hx = (0.25 * PI - (-0.25 * PI)) / (double)N;
+  d.sbp = make_sbp(order);
+  // quadrature edge weights: Ah21 / Ah42 / Ah63 (d43 has no norm of its own
+  // in the reference and is paired with SBP_Ah42_quadrature)
+  Sbp qs = make_sbp(order == 43 ? 42 : order);
+  const int n = d.n, ne = (int)qs.A.size();
+  d.A.assign(n, 1.0);
+  for (int i = 0; i < std::min(ne, n); ++i) d.A[i] = qs.A[i];
+  for (int i = std::max(n - ne, 0); i < n; ++i) d.A[i] = qs.A[n - 1 - i];
+
+  const int np = d.npts();
+  for (auto* v : {&d.J, &d.Qi1, &d.Qi2, &d.Qi3, &d.Q1, &d.Q2, &d.Q3, &d.f, &d.rx, &d.ry, &d.rz}) v->assign(np, 0.0);
+  for (auto* v : {&d.a1, &d.a2, &d.b1, &d.b2}) v->assign(3 * np, 0.0);
+  for (int p = 0; p < 6; ++p)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const int id = p * n * n + j * n + i;
+        const double al = alpha_of(d, i), be = alpha_of(d, j);
+        const double ta = std::tan(al), tb = std::tan(be);
+        const double sg = std::sqrt(1.0 + ta * ta + tb * tb);
+        d.J[id] = (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
+        d.Qi1[id] = sg * sg / (1.0 + ta * ta);
+        d.Qi2[id] = sg * sg * ta * tb / ((1.0 + ta * ta) * (1.0 + tb * tb));
+        d.Qi3[id] = sg * sg / (1.0 + tb * tb);
+        const double s4 = (sg * sg) * (sg * sg);
+        d.Q1[id] = (1.0 + ta * ta) * (1.0 + ta * ta) * (1.0 + tb * tb) / s4;
+        d.Q2[id] = -(1.0 + ta * ta) * (1.0 + tb * tb) * ta * tb / s4;
+        d.Q3[id] = (1.0 + ta * ta) * (1.0 + tb * tb) * (1.0 + tb * tb) / s4;
+        double v[3], w[3];
+        r_proto(al, be, v); to_face(p, v, w);
+        d.rx[id] = w[0]; d.ry[id] = w[1]; d.rz[id] = w[2];
+        const double nn = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        const double pr = (d.axis[0] * w[0] + d.axis[1] * w[1] + d.axis[2] * w[2]) / nn;
+        d.f[id] = 2.0 * d.omega * pr;
+        a1_proto(al, be, v); to_face(p, v, &d.a1[3 * id]);
+        a2_proto(al, be, v); to_face(p, v, &d.a2[3 * id]);
+        b1_proto(al, be, v); to_face(p, v, &d.b1[3 * id]);
+        b2_proto(al, be, v); to_face(p, v, &d.b2[3 * id]);
+      }
+
+  // covariant sync weights (ecs_Ah_vec_sync_factory_mod.f90:97-144)
+  d.qb.assign(n, 0.0); d.qt.assign(n, 0.0); d.ql.assign(n, 0.0); d.qr.assign(n, 0.0);
+  for (int k = 0; k < n; ++k) {
+    const double c = -0.25 * PI + k * d.hx;
+    double a[3], b[3];
+    a2_proto(c, -0.25 * PI, a); b1_proto(c, 0.25 * PI, b);
+    d.qb[k] = a[0] * b[0] + a[1] * (-b[2]) + a[2] * b[1];
+    a2_proto(c, 0.25 * PI, a); b1_proto(c, -0.25 * PI, b);
+    d.qt[k] = a[0] * b[0] + a[1] * b[2] + a[2] * (-b[1]);
+    a1_proto(-0.25 * PI, c, a); b2_proto(0.25 * PI, c, b);
+    d.ql[k] = a[0] * (-b[2]) + a[1] * b[1] + a[2] * b[0];
+    a1_proto(0.25 * PI, c, a); b2_proto(-0.25 * PI, c, b);
+    d.qr[k] = a[0] * b[2] + a[1] * b[1] + a[2] * (-b[0]);
+  }
+  build_ring(d);
+}
+
+// ---------------------------------------------------------------------------
+// Halo exchange of the 1-wide ring (parallel/exchange_halo_mod.f90:42-167,
+// parallel/buffer_mod.f90:48-277): scalar copy, or the vector copy with the
+// component swap/negation of pack_to_buf_vec.
+// ---------------------------------------------------------------------------
+void exchange_scalar(const orc_domain& d, const double* f, std::vector<double>& ring) {
+  const int n = d.n;
+  ring.assign(6 * 4 * n, 0.0);
+  for (int s = 0; s < 6 * 4 * n; ++s) {
+    const RingSrc& r = d.ring[s];
+    ring[s] = f[r.q * n * n + r.node];
+  }
+}
+
+void exchange_vector(const orc_domain& d, const double* u, const double* v,
+                     std::vector<double>& ru, std::vector<double>& rv) {
+  const int n = d.n;
+  ru.assign(6 * 4 * n, 0.0); rv.assign(6 * 4 * n, 0.0);
+  for (int s = 0; s < 6 * 4 * n; ++s) {
+    const RingSrc& r = d.ring[s];
+    const double uq = u[r.q * n * n + r.node], vq = v[r.q * n * n + r.node];
+    if (r.dim_i) { ru[s] = r.istep * uq; rv[s] = r.jstep * vq; }
+    else { ru[s] = r.jstep * vq; rv[s] = r.istep * uq; }
+  }
+}
+
+// Scalar edge/corner averaging (halo/halo_Ah_scalar_sync_mod.f90:38-93).
+void sync_scalar(const orc_domain& d, double* f) {
+  const int n = d.n;
+  std::vector<double> ring;
+  exchange_scalar(d, f, ring);
+  for (int p = 0; p < 6; ++p) {
+    double* F = f + p * n * n;
+    const double* L = &ring[(p * 4 + 0) * n];
+    const double* R = &ring[(p * 4 + 1) * n];
+    const double* B = &ring[(p * 4 + 2) * n];
+    const double* T = &ring[(p * 4 + 3) * n];
+    auto at = [&](int i, int j) -> double& { return F[j * n + i]; };
+    const int e = n - 1;
+    at(0, 0) = (at(0, 0) + L[0] + B[0]) / 3.0;
+    for (int j = 1; j < e; ++j) at(0, j) = 0.5 * (L[j] + at(0, j));
+    at(0, e) = (at(0, e) + L[e] + T[0]) / 3.0;
+    at(e, 0) = (at(e, 0) + R[0] + B[e]) / 3.0;
+    for (int j = 1; j < e; ++j) at(e, j) = 0.5 * (at(e, j) + R[j]);
+    at(e, e) = (at(e, e) + R[e] + T[e]) / 3.0;
+    for (int i = 1; i < e; ++i) at(i, 0) = 0.5 * (at(i, 0) + B[i]);
+    for (int i = 1; i < e; ++i) at(i, e) = 0.5 * (at(i, e) + T[i]);
+  }
+}
+
+// Covariant vector edge sync: syncronize_grad_on_edges called with the
+// components swapped (ecs_Ah_vec_sync_mod.f90:34-125): U = gy, V = gx.
+void sync_vector_cov(const orc_domain& d, double* gx, double* gy) {
+  const int n = d.n;
+  std::vector<double> rgx, rgy;
+  exchange_vector(d, gx, gy, rgx, rgy);
+  const double* qb = d.qb.data(); const double* qt = d.qt.data();
+  const double* ql = d.ql.data(); const double* qr = d.qr.data();
+  for (int p = 0; p < 6; ++p) {
+    double* U = gy + p * n * n;
+    double* V = gx + p * n * n;
+    const double* UL = &rgy[(p * 4 + 0) * n]; const double* VL = &rgx[(p * 4 + 0) * n];
+    const double* UR = &rgy[(p * 4 + 1) * n]; const double* VR = &rgx[(p * 4 + 1) * n];
+    const double* UB = &rgy[(p * 4 + 2) * n]; const double* VB = &rgx[(p * 4 + 2) * n];
+    const double* UT = &rgy[(p * 4 + 3) * n]; const double* VT = &rgx[(p * 4 + 3) * n];
+    auto u = [&](int i, int j) -> double& { return U[j * n + i]; };
+    auto v = [&](int i, int j) -> double& { return V[j * n + i]; };
+    const int e = n - 1;
+    u(0, 0) = (u(0, 0) + UL[0] + UB[0] + qb[0] * VB[0]) / 3.0;
+    v(0, 0) = (v(0, 0) + VL[0] + VB[0] + ql[0] * UL[0]) / 3.0;
+    u(e, 0) = (u(e, 0) + UR[0] + UB[e] + qb[e] * VB[e]) / 3.0;
+    v(e, 0) = (v(e, 0) + VR[0] + VB[e] + qr[0] * UR[0]) / 3.0;
+    u(0, e) = (u(0, e) + UL[e] + UT[0] + qt[0] * VT[0]) / 3.0;
+    v(0, e) = (v(0, e) + VL[e] + VT[0] + ql[e] * UL[e]) / 3.0;
+    u(e, e) = (u(e, e) + UR[e] + UT[e] + qt[e] * VT[e]) / 3.0;
+    v(e, e) = (v(e, e) + VR[e] + VT[e] + qr[e] * UR[e]) / 3.0;
+    for (int j = 1; j < e; ++j) {
+      u(0, j) = 0.5 * (UL[j] + u(0, j));
+      v(0, j) = 0.5 * (v(0, j) + VL[j] + ql[j] * UL[j]);
+      u(e, j) = 0.5 * (u(e, j) + UR[j]);
+      v(e, j) = 0.5 * (v(e, j) + VR[j] + qr[j] * UR[j]);
+    }
+    for (int i = 1; i < e; ++i) {
+      v(i, 0) = 0.5 * (VB[i] + v(i, 0));
+      u(i, 0) = 0.5 * (UB[i] + u(i, 0) + qb[i] * VB[i]);
+      v(i, e) = 0.5 * (v(i, e) + VT[i]);
+      u(i, e) = 0.5 * (u(i, e) + UT[i] + qt[i] * VT[i]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Horizontal operators on the Ah grid.
+// ---------------------------------------------------------------------------
+// grad_ah_sbp: calc_grad_on_tile (gradient/grad_ah_sbp_mod.f90:51-88), then
+// the covariant sync.
+void grad(const orc_domain& d, const double* f, double* gx, double* gy) {
+  const int n = d.n;
+  const double hs = d.hx * d.scale;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int pj = 0; pj < 6 * n; ++pj) {
+    const int p = pj / n, j = pj % n;
+    const double* F = f + p * n * n;
+    for (int i = 0; i < n; ++i) {
+      const double dx = sbp_point(d.sbp, F + j * n, n, 1, i);
+      const double dy = sbp_point(d.sbp, F + i, n, n, j);
+      gx[p * n * n + j * n + i] = dx / hs;
+      gy[p * n * n + j * n + i] = dy / hs;
+    }
+  }
+  sync_vector_cov(d, gx, gy);
+}
+
+// div_ah_sbp: calc_div_on_tile (divergence/div_ah_sbp_mod.f90:46-96), then
+// the scalar sync.  u, v are contravariant components.
+void div(const orc_domain& d, const double* u, const double* v, double* out) {
+  const int n = d.n, np = d.npts();
+  std::vector<double> Gu(np), Gv(np);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) { Gu[k] = d.J[k] * u[k]; Gv[k] = d.J[k] * v[k]; }
+  const double hx = d.hx, sc = d.scale;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int pj = 0; pj < 6 * n; ++pj) {
+    const int p = pj / n, j = pj % n;
+    const double* GU = &Gu[p * n * n];
+    const double* GV = &Gv[p * n * n];
+    for (int i = 0; i < n; ++i) {
+      const int id = p * n * n + j * n + i;
+      const double dx = sbp_point(d.sbp, GU + j * n, n, 1, i);
+      const double dy = sbp_point(d.sbp, GV + i, n, n, j);
+      out[id] = (dx + dy) / (d.J[id] * hx * sc);
+    }
+  }
+  sync_scalar(d, out);
+}
+
+// curl_div_based (curl/curl_div_based_mod.f90:26-66): div(v/J, -u/J).
+void curl(const orc_domain& d, const double* u, const double* v, double* out) {
+  const int np = d.npts();
+  std::vector<double> ut(np), vt(np);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) { ut[k] = v[k] / d.J[k]; vt[k] = -u[k] / d.J[k]; }
+  div(d, ut.data(), vt.data(), out);
+}
+
+// co2contra_colocated (co2contra/co2contra_colocated_mod.f90:36-60, 78-102)
+void co2contra(const orc_domain& d, const double* u, const double* v, double* ut, double* vt) {
+  const int np = d.npts();
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) {
+    const double a = d.Qi1[k] * u[k] + d.Qi2[k] * v[k];
+    const double b = d.Qi2[k] * u[k] + d.Qi3[k] * v[k];
+    ut[k] = a; vt[k] = b;
+  }
+}
+void contra2co(const orc_domain& d, const double* ut, const double* vt, double* u, double* v) {
+  const int np = d.npts();
+  for (int k = 0; k < np; ++k) {
+    const double a = d.Q1[k] * ut[k] + d.Q2[k] * vt[k];
+    const double b = d.Q2[k] * ut[k] + d.Q3[k] * vt[k];
+    u[k] = a; v[k] = b;
+  }
+}
+
+// calc_coriolis_vec_inv_tile (coriolis/coriolis_colocated_mod.f90:79-103)
+void coriolis(const orc_domain& d, const double* hu, const double* hv, const double* h,
+              const double* cu, double* cor_u, double* cor_v) {
+  const int np = d.npts();
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) {
+    const double fz = d.f[k] + cu[k];
+    cor_u[k] = fz * hv[k] / h[k] * d.J[k];
+    cor_v[k] = -(fz * hu[k] / h[k] * d.J[k]);
+  }
+}
+
+// operator_swm_t%apply (models/shallow_water/operator/operator_swm_mod.f90:61-113)
+void apply(const orc_domain& d, const double* hs, const double* h, const double* u,
+           const double* v, double* th, double* tu, double* tv) {
+  const int np = d.npts();
+  std::vector<double> ut(np), vt(np), hu(np), hv(np), KE(np), gx(np), gy(np), cu(np),
+      cor_u(np), cor_v(np), dv(np);
+  co2contra(d, u, v, ut.data(), vt.data());
+  const double g = d.grav;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) {
+    hu[k] = 1.0 * h[k] * ut[k];                       // massflux_colocated_mod.f90:19-29
+    hv[k] = 1.0 * h[k] * vt[k];
+    KE[k] = (u[k] * ut[k] + v[k] * vt[k]) / 2.0;      // KE_colocated_mod.f90:41-47
+    KE[k] = KE[k] + g * h[k] + g * (hs ? hs[k] : 0.0);  // operator_swm_mod.f90:85
+  }
+  grad(d, KE.data(), gx.data(), gy.data());
+  curl(d, u, v, cu.data());
+  coriolis(d, hu.data(), hv.data(), h, cu.data(), cor_u.data(), cor_v.data());
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) {
+    tu[k] = -1.0 * gx[k] + 1.0 * cor_u[k];
+    tv[k] = -1.0 * gy[k] + 1.0 * cor_v[k];
+  }
+  div(d, hu.data(), hv.data(), dv.data());
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) th[k] = -1.0 * dv[k];
+}
+
+// rk4_t%step (time_schemes/rk4_mod.f90:20-42)
+void rk4(const orc_domain& d, const double* hs, double* h, double* u, double* v, double dt,
+         int nsteps) {
+  const int np = d.npts();
+  std::vector<double> k1(3 * np), k2(3 * np), k3(3 * np), k4(3 * np), y(3 * np);
+  double* F0[3] = {h, u, v};
+  auto A = [&](std::vector<double>& out, const double* yh, const double* yu, const double* yv) {
+    apply(d, hs, yh, yu, yv, &out[0], &out[np], &out[2 * np]);
+  };
+  auto assign = [&](double s2, const std::vector<double>& kk) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int k = 0; k < np; ++k)
+      for (int c = 0; c < 3; ++c) y[c * np + k] = 1.0 * F0[c][k] + s2 * kk[c * np + k];
+  };
+  for (int s = 0; s < nsteps; ++s) {
+    A(k1, h, u, v);
+    assign(0.5 * dt, k1);
+    A(k2, &y[0], &y[np], &y[2 * np]);
+    assign(0.5 * dt, k2);
+    A(k3, &y[0], &y[np], &y[2 * np]);
+    assign(dt, k3);
+    A(k4, &y[0], &y[np], &y[2 * np]);
+    const double c6 = dt / 6.0, c3 = dt / 3.0;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int k = 0; k < np; ++k)
+      for (int c = 0; c < 3; ++c) {
+        double x = F0[c][k];
+        x = x + c6 * k1[c * np + k] + c3 * k2[c * np + k];
+        x = x + c3 * k3[c * np + k] + c6 * k4[c * np + k];
+        F0[c][k] = x;
+      }
+  }
+}
+
+// SBP quadrature mass (quadrature/sbp_quadrature_mod.f90:21-40 summed over
+// tiles as abstract_quadrature_mod.f90:27-44).
+double mass(const orc_domain& d, const double* f) {
+  const int n = d.n;
+  double tot = 0.0;
+  for (int p = 0; p < 6; ++p) {
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const int id = p * n * n + j * n + i;
+        acc = acc + f[id] * d.J[id] * d.hx * d.hx * d.A[i] * d.A[j];
+      }
+    tot = tot + acc;
+  }
+  return tot;
+}
+
+// l2norm (vec_math_mod.f90:50-90), one level.
+double l2sq(const orc_domain& d, const double* f) {
+  const int n = d.n;
+  double tot = 0.0;
+  for (int p = 0; p < 6; ++p) {
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const int id = p * n * n + j * n + i;
+        acc = acc + f[id] * f[id] * d.J[id] * d.hx * d.hx;
+      }
+    tot = tot + acc;
+  }
+  return tot;
+}
+
+double maxabs(const std::vector<double>& f) {
+  double m = 0.0;
+  for (double x : f) m = std::max(m, std::fabs(x));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// Analytic test fields (test_fields/test_fields_mod.f90, latlon_functions_mod,
+// sph_coords_mod).  Level k (0,1,2) matters for the fields that cycle axes.
+// ---------------------------------------------------------------------------
+void field_solid_rotation(int k, double x, double y, double z, double v[3]) {
+  const double ax[3] = {k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0};
+  v[0] = ax[1] * z - ax[2] * y;
+  v[1] = -ax[0] * z + ax[2] * x;
+  v[2] = ax[0] * y - ax[1] * x;
+}
+void field_cross_polar(double x, double y, double z, double v[3]) {
+  const double r2 = x * x + y * y + z * z;
+  const double cphi = std::sqrt((x * x + y * y) / r2);
+  const double sphi = z / std::sqrt(r2);
+  const double rho = std::max(std::sqrt(x * x + y * y), (double)1e-14f);
+  const double clam = x / rho;
+  double slam = y / rho;
+  if (x * x + y * y == 0.0) slam = 1.0;
+  const double u = sphi * (sphi * sphi - 3.0 * cphi * cphi) * slam - 0.5 * cphi;
+  const double w = sphi * sphi * clam;
+  v[0] = -slam * u - sphi * clam * w;
+  v[1] = clam * u - sphi * slam * w;
+  v[2] = cphi * w;
+}
+double field_cross_polar_div(double x, double y, double z) { return -x * z / (x * x + y * y + z * z); }
+double field_cross_polar_zeta(double x, double y, double z) {
+  return (16.0 * (1 - z * z) * y - 13.0 * y - z) / (x * x + y * y + z * z);
+}
+double field_xyz(int k, double x, double y, double z) {
+  return (k == 0 ? 1.0 : 0.0) * x + (k == 1 ? 1.0 : 0.0) * y + (k == 2 ? 1.0 : 0.0) * z;
+}
+void field_xyz_grad(int k, double x, double y, double z, double v[3]) {
+  const double e[3] = {k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0};
+  const double r = std::sqrt(x * x + y * y + z * z);
+  const double nv[3] = {x / r, y / r, z / r};
+  const double s = nv[0] * e[0] + nv[1] * e[1] + nv[2] * e[2];
+  for (int c = 0; c < 3; ++c) v[c] = e[c] - nv[c] * s;
+}
+void field_vsh_curl_free_10(double x, double y, double z, double v[3]) {
+  double lam = std::atan2(y, x);
+  const double phi = std::atan2(z, std::sqrt(x * x + y * y));
+  lam = lam + PI * (1.0 - (lam >= 0.0 ? 1.0 : -1.0));
+  const double vl = 0.0, vp = -std::cos(phi);
+  v[0] = -std::sin(lam) * vl - std::sin(phi) * std::cos(lam) * vp;
+  v[1] = std::cos(lam) * vl - std::sin(phi) * std::sin(lam) * vp;
+  v[2] = std::cos(phi) * vp;
+}
+
+template <class Gen>
+void set_vector(const orc_domain& d, Gen gen, bool contravariant, std::vector<double>& u,
+                std::vector<double>& v) {
+  const int np = d.npts();
+  u.assign(np, 0.0); v.assign(np, 0.0);
+  const std::vector<double>& e1 = contravariant ? d.b1 : d.a1;
+  const std::vector<double>& e2 = contravariant ? d.b2 : d.a2;
+  for (int k = 0; k < np; ++k) {
+    double w[3];
+    gen(d.rx[k], d.ry[k], d.rz[k], w);
+    u[k] = w[0] * e1[3 * k] + w[1] * e1[3 * k + 1] + w[2] * e1[3 * k + 2];
+    v[k] = w[0] * e2[3 * k] + w[1] * e2[3 * k + 1] + w[2] * e2[3 * k + 2];
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+// C interface
+// ===========================================================================
+extern "C" {
+
+orc_domain* orc_create(int N, int sbp_order, double radius, double grav, double omega,
+                       const double axis[3]) {
+  if (N < 8 || (sbp_order != 21 && sbp_order != 42 && sbp_order != 43 && sbp_order != 63))
+    return nullptr;
+  orc_domain* d = new orc_domain();
+  const double def_axis[3] = {0.0, 0.0, 1.0};
+  build(*d, N, sbp_order, radius, grav, omega, axis ? axis : def_axis);
+  return d;
+}
+
+void orc_destroy(orc_domain* d) { delete d; }
+int orc_npts(const orc_domain* d) { return d->npts(); }
+void orc_set_threads(int t) { g_threads = t < 1 ? 1 : t; }
+int orc_get_threads(void) { return g_threads; }
+
+void orc_geometry(const orc_domain* d, double* J, double* Qi1, double* Qi2, double* Qi3,
+                  double* f, double* rx, double* ry, double* rz) {
+  const size_t b = sizeof(double) * d->npts();
+  if (J) std::memcpy(J, d->J.data(), b);
+  if (Qi1) std::memcpy(Qi1, d->Qi1.data(), b);
+  if (Qi2) std::memcpy(Qi2, d->Qi2.data(), b);
+  if (Qi3) std::memcpy(Qi3, d->Qi3.data(), b);
+  if (f) std::memcpy(f, d->f.data(), b);
+  if (rx) std::memcpy(rx, d->rx.data(), b);
+  if (ry) std::memcpy(ry, d->ry.data(), b);
+  if (rz) std::memcpy(rz, d->rz.data(), b);
+}
+
+void orc_bases(const orc_domain* d, double* a1, double* a2, double* b1, double* b2) {
+  const size_t b = sizeof(double) * 3 * d->npts();
+  if (a1) std::memcpy(a1, d->a1.data(), b);
+  if (a2) std::memcpy(a2, d->a2.data(), b);
+  if (b1) std::memcpy(b1, d->b1.data(), b);
+  if (b2) std::memcpy(b2, d->b2.data(), b);
+}
+
+void orc_sync_weights(const orc_domain* d, double* qb, double* qt, double* ql, double* qr) {
+  const size_t b = sizeof(double) * d->n;
+  std::memcpy(qb, d->qb.data(), b); std::memcpy(qt, d->qt.data(), b);
+  std::memcpy(ql, d->ql.data(), b); std::memcpy(qr, d->qr.data(), b);
+}
+
+void orc_co2contra(const orc_domain* d, const double* u, const double* v, double* ut, double* vt) { co2contra(*d, u, v, ut, vt); }
+void orc_contra2co(const orc_domain* d, const double* ut, const double* vt, double* u, double* v) { contra2co(*d, ut, vt, u, v); }
+void orc_grad(const orc_domain* d, const double* f, double* gx, double* gy) { grad(*d, f, gx, gy); }
+void orc_div(const orc_domain* d, const double* u, const double* v, double* o) { div(*d, u, v, o); }
+void orc_curl(const orc_domain* d, const double* u, const double* v, double* o) { curl(*d, u, v, o); }
+void orc_sync_scalar(const orc_domain* d, double* f) { sync_scalar(*d, f); }
+void orc_sync_vector_cov(const orc_domain* d, double* gx, double* gy) { sync_vector_cov(*d, gx, gy); }
+void orc_coriolis(const orc_domain* d, const double* hu, const double* hv, const double* h,
+                  const double* cu, double* cor_u, double* cor_v) { coriolis(*d, hu, hv, h, cu, cor_u, cor_v); }
+
+void orc_apply(const orc_domain* d, const double* hs, const double* h, const double* u,
+               const double* v, double* th, double* tu, double* tv) { apply(*d, hs, h, u, v, th, tu, tv); }
+void orc_rk4(const orc_domain* d, const double* hs, double* h, double* u, double* v, double dt,
+             int nsteps) { rk4(*d, hs, h, u, v, dt, nsteps); }
+
+// get_diagnostics (operator_swm_mod.f90:115-155) with calc_energy 211-236 and
+// calc_enstrophy 238-260.
+void orc_diagnostics(const orc_domain* d, const double* hs, const double* h, const double* u,
+                     const double* v, double out[7]) {
+  const int np = d->npts();
+  double hmin = h[0], hmax = h[0];
+  for (int k = 0; k < np; ++k) { hmin = std::min(hmin, h[k]); hmax = std::max(hmax, h[k]); }
+  std::vector<double> ut(np), vt(np), hu(np), hv(np), ku(np), kv(np), pe(np), cu(np);
+  co2contra(*d, u, v, ut.data(), vt.data());
+  for (int k = 0; k < np; ++k) {
+    hu[k] = 1.0 * h[k] * ut[k]; hv[k] = 1.0 * h[k] * vt[k];
+    ku[k] = 0.5 * hu[k] * u[k]; kv[k] = 0.5 * hv[k] * v[k];
+    pe[k] = 1.0 * h[k] + 1.0 * (hs ? hs[k] : 0.0);
+    pe[k] = 0.5 * d->grav * pe[k] * pe[k];
+  }
+  const double ke = mass(*d, ku.data()) + mass(*d, kv.data());
+  const double pen = mass(*d, pe.data());
+  curl(*d, u, v, cu.data());
+  for (int k = 0; k < np; ++k) {
+    double c = cu[k] + 1.0 * d->f[k];
+    c = 0.5 * c * c;
+    cu[k] = 1.0 * c / h[k];
+  }
+  out[0] = hmin; out[1] = hmax; out[2] = mass(*d, h);
+  out[3] = ke + pen; out[4] = ke; out[5] = pen; out[6] = mass(*d, cu.data());
+}
+
+double orc_l2norm(const orc_domain* d, const double* f) { return std::sqrt(l2sq(*d, f)); }
+double orc_mass(const orc_domain* d, const double* f) { return mass(*d, f); }
+
+// test_div (test_diff_ops/test_diffops_mod.f90:71-125), nz = 3
+int orc_golden_div(int N, int order, double out[4]) {
+  const double ax[3] = {0, 0, 1};
+  orc_domain* d = orc_create(N, order, 1.0, 9.80616, 1.0, ax);
+  if (!d) return -1;
+  const int np = d->npts();
+  std::vector<double> u, v, dv(np), all;
+  double l2 = 0.0;
+  for (int lev = 0; lev < 3; ++lev) {
+    set_vector(*d, [lev](double x, double y, double z, double w[3]) { field_solid_rotation(lev, x, y, z, w); }, true, u, v);
+    div(*d, u.data(), v.data(), dv.data());
+    for (int k = 0; k < np; ++k) dv[k] = d->scale * dv[k];
+    all.insert(all.end(), dv.begin(), dv.end());
+    l2 += l2sq(*d, dv.data());
+  }
+  out[0] = maxabs(all); out[1] = std::sqrt(l2);
+  all.clear(); l2 = 0.0;
+  for (int lev = 0; lev < 3; ++lev) {
+    set_vector(*d, field_cross_polar, true, u, v);
+    div(*d, u.data(), v.data(), dv.data());
+    for (int k = 0; k < np; ++k)
+      dv[k] = d->scale * dv[k] - 1.0 * field_cross_polar_div(d->rx[k], d->ry[k], d->rz[k]);
+    all.insert(all.end(), dv.begin(), dv.end());
+    l2 += l2sq(*d, dv.data());
+  }
+  out[2] = maxabs(all); out[3] = std::sqrt(l2);
+  orc_destroy(d);
+  return 0;
+}
+
+// test_grad (test_diffops_mod.f90:127-178), nz = 3
+int orc_golden_grad(int N, int order, double out[2]) {
+  const double ax[3] = {0, 0, 1};
+  orc_domain* d = orc_create(N, order, 1.0, 9.80616, 1.0, ax);
+  if (!d) return -1;
+  const int np = d->npts();
+  std::vector<double> f(np), gx(np), gy(np), tx, ty, ex_all, ey_all;
+  double l2x = 0.0, l2y = 0.0;
+  for (int lev = 0; lev < 3; ++lev) {
+    for (int k = 0; k < np; ++k) f[k] = field_xyz(lev, d->rx[k], d->ry[k], d->rz[k]);
+    set_vector(*d, [lev](double x, double y, double z, double w[3]) { field_xyz_grad(lev, x, y, z, w); }, false, tx, ty);
+    grad(*d, f.data(), gx.data(), gy.data());
+    for (int k = 0; k < np; ++k) {
+      gx[k] = d->scale * gx[k] - 1.0 * tx[k];
+      gy[k] = d->scale * gy[k] - 1.0 * ty[k];
+    }
+    ex_all.insert(ex_all.end(), gx.begin(), gx.end());
+    ey_all.insert(ey_all.end(), gy.begin(), gy.end());
+    l2x += l2sq(*d, gx.data()); l2y += l2sq(*d, gy.data());
+  }
+  out[0] = maxabs(ex_all) + maxabs(ey_all);
+  out[1] = std::sqrt(l2x) + std::sqrt(l2y);
+  orc_destroy(d);
+  return 0;
+}
+
+// test_curl (test_diffops_mod.f90:466-522), nz = 3
+int orc_golden_curl(int N, int order, double out[4]) {
+  const double ax[3] = {0, 0, 1};
+  orc_domain* d = orc_create(N, order, 1.0, 9.80616, 1.0, ax);
+  if (!d) return -1;
+  const int np = d->npts();
+  std::vector<double> u, v, c(np), all;
+  double l2 = 0.0;
+  for (int lev = 0; lev < 3; ++lev) {
+    set_vector(*d, field_vsh_curl_free_10, false, u, v);
+    curl(*d, u.data(), v.data(), c.data());
+    for (int k = 0; k < np; ++k) c[k] = d->scale * c[k];
+    all.insert(all.end(), c.begin(), c.end());
+    l2 += l2sq(*d, c.data());
+  }
+  out[0] = maxabs(all); out[1] = std::sqrt(l2);
+  all.clear(); l2 = 0.0;
+  for (int lev = 0; lev < 3; ++lev) {
+    set_vector(*d, field_cross_polar, false, u, v);
+    curl(*d, u.data(), v.data(), c.data());
+    for (int k = 0; k < np; ++k)
+      c[k] = d->scale * c[k] - 1.0 * field_cross_polar_zeta(d->rx[k], d->ry[k], d->rz[k]);
+    all.insert(all.end(), c.begin(), c.end());
+    l2 += l2sq(*d, c.data());
+  }
+  out[2] = maxabs(all); out[3] = std::sqrt(l2);
+  orc_destroy(d);
+  return 0;
+}
+
+static int golden_transform(int N, bool to_contra, double out[2]) {
+  const double ax[3] = {0, 0, 1};
+  orc_domain* d = orc_create(N, 42, 1.0, 9.80616, 1.0, ax);
+  if (!d) return -1;
+  const int np = d->npts();
+  std::vector<double> ui, vi, ut, vt, uo(np), vo(np), eu, ev;
+  double l2u = 0.0, l2v = 0.0;
+  for (int lev = 0; lev < 3; ++lev) {
+    set_vector(*d, field_cross_polar, !to_contra, ui, vi);
+    set_vector(*d, field_cross_polar, to_contra, ut, vt);
+    if (to_contra) co2contra(*d, ui.data(), vi.data(), uo.data(), vo.data());
+    else contra2co(*d, ui.data(), vi.data(), uo.data(), vo.data());
+    for (int k = 0; k < np; ++k) { uo[k] = uo[k] + (-1.0) * ut[k]; vo[k] = vo[k] + (-1.0) * vt[k]; }
+    eu.insert(eu.end(), uo.begin(), uo.end());
+    ev.insert(ev.end(), vo.begin(), vo.end());
+    l2u += l2sq(*d, uo.data()); l2v += l2sq(*d, vo.data());
+  }
+  out[0] = maxabs(eu) + maxabs(ev);
+  out[1] = std::sqrt(l2u) + std::sqrt(l2v);
+  orc_destroy(d);
+  return 0;
+}
+int orc_golden_co2contra(int N, double out[2]) { return golden_transform(N, true, out); }
+int orc_golden_contra2co(int N, double out[2]) { return golden_transform(N, false, out); }
+
+// test_quadrature (test_quadrature/test_quadrature_mod.f90:18-80)
+double orc_golden_quadrature(int N, int order, int max_order) {
+  const double ax[3] = {0, 0, 1};
+  orc_domain* d = orc_create(N, order, 1.0, 9.80616, 1.0, ax);
+  if (!d) return -1.0;
+  const int n = d->n, np = d->npts();
+  std::vector<double> fu(np);
+  double worst = 0.0;
+  for (int o = 0; o <= max_order; ++o) {
+    for (int p = 0; p < 6; ++p)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int id = p * n * n + j * n + i;
+          const double a = alpha_of(*d, i), b = alpha_of(*d, j);
+          fu[id] = 1.0 / d->J[id] * std::pow(a, o) * std::pow(b, o);
+        }
+    const int pw = o + 1;
+    const double t = std::pow(0.25 * PI, pw) - std::pow(-0.25 * PI, pw);
+    const double exact = 6.0 * t * t / (double)(pw * pw);
+    worst = std::max(worst, std::fabs(exact - mass(*d, fu.data())));
+  }
+  orc_destroy(d);
+  return worst;
+}
+
+// RK4 amplification on the diagonal test operator dv/dt = i*omega*v
+// (test/test_time_steping/test_ts_mod.f90:7-73 with models/iomega_model):
+// one rk4_mod.f90:20-42 step from v=1 must equal 1+z+z^2/2+z^3/6+z^4/24,
+// z = dt*omega.  Returns sum |numeric - analytic| over the 10 modes.
+double orc_golden_rk4_iomega(void) {
+  typedef std::complex<double> C;
+  const int n = 10;
+  const double day = 24.0 * 3600.0, dt = 6.0 * 3600.0;
+  std::vector<C> om(n), v0(n, C(1.0, 0.0)), k1(n), k2(n), k3(n), k4(n), y(n);
+  // cmplx() without a kind argument yields default (single precision) parts
+  for (int i = 0; i < n; ++i)
+    om[i] = C((double)(float)(1.0 / (day * (i + 1))), (double)(float)(2.0 * PI * (i + 1) / day));
+  auto A = [&](std::vector<C>& out, const std::vector<C>& in) {
+    for (int i = 0; i < n; ++i) out[i] = om[i] * in[i];
+  };
+  A(k1, v0);
+  for (int i = 0; i < n; ++i) y[i] = 1.0 * v0[i] + (0.5 * dt) * k1[i];
+  A(k2, y);
+  for (int i = 0; i < n; ++i) y[i] = 1.0 * v0[i] + (0.5 * dt) * k2[i];
+  A(k3, y);
+  for (int i = 0; i < n; ++i) y[i] = 1.0 * v0[i] + dt * k3[i];
+  A(k4, y);
+  double err = 0.0;
+  for (int i = 0; i < n; ++i) {
+    C x = v0[i];
+    x = x + (dt / 6.0) * k1[i] + (dt / 3.0) * k2[i];
+    x = x + (dt / 3.0) * k3[i] + (dt / 6.0) * k4[i];
+    const C z = dt * om[i];
+    const C z2 = z * z, z3 = z2 * z, z4 = z3 * z;
+    const C tr = 1.0 + z + 0.5 * z2 + z3 / 6.0 + z4 / 24.0;
+    err += std::abs(x - tr);
+  }
+  return err;
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+/*
+ * swm_oracle.h -- C interface of the FP64 CPU oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The oracle is a plain C++ restatement of the
+ * reference's shallow-water hot path (vvshashkin/cubedsphere_sbp_swm, Fortran).
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load it, and only as the checker or as the timed CPU baseline.  The product
+ * path (cubedsphere_sbp_swm_gb300) never links, loads or calls it.
+ *
+ * Layout of every field passed through this interface: 6 panels, each panel
+ * (N+1) x (N+1) FP64 nodes, i (alpha direction) fastest, then j, then panel:
+ *     index(p, i, j) = p*(N+1)*(N+1) + j*(N+1) + i      (all 0-based)
+ * which is the reference's per-tile array p(1:N+1, 1:N+1, 1) with one tile per
+ * panel (parallel/partition_mod.f90:69-95), flattened panel after panel.
+ *
+ * Parity pins: orc_golden_* reproduce the reference's own known-answer test
+ * src/test/test_diff_ops/test_diffops_mod.f90 (test_div 71-125, test_grad
+ * 127-178, test_curl 466-522, test_co2contra 231-278, test_contra2co 279-324)
+ * whose printed values are checked in at src/test/test_diff_ops/
+ * reference_results.txt.
+ */
+#ifndef SWM_ORACLE_H
+#define SWM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_domain orc_domain;
+
+/* sbp_order: 21, 42, 43 or 63 (names d21/d42/d43/d63 of
+ * differential_operators/sbp_operators/sbp_factory_mod.f90:38-179).
+ * radius/omega/axis as config_metric_t (metric/config_metric_mod.f90:7-63);
+ * the axis is normalised as config_metric_mod.f90:57 does. */
+orc_domain* orc_create(int N, int sbp_order, double radius, double grav,
+                       double omega, const double axis[3]);
+void orc_destroy(orc_domain* d);
+int  orc_npts(const orc_domain* d);          /* 6*(N+1)^2 */
+void orc_set_threads(int nthreads);           /* OpenMP threads (CPU baseline) */
+int  orc_get_threads(void);
+
+/* Geometry export (mesh_factory_mod.f90:85-133, coriolis_factory_mod.f90:151-172). */
+void orc_geometry(const orc_domain* d, double* J, double* Qi1, double* Qi2,
+                  double* Qi3, double* f, double* rx, double* ry, double* rz);
+/* Covariant basis a1,a2 and contravariant basis b1,b2 (3 comps each, xyz
+ * interleaved per node: out[3*node + c]). */
+void orc_bases(const orc_domain* d, double* a1, double* a2, double* b1,
+               double* b2);
+/* Edge-sync weights qb, qt, ql, qr (n each), covariant case
+ * (equiang_cs/ecs_Ah_vec_sync_factory_mod.f90:97-144). */
+void orc_sync_weights(const orc_domain* d, double* qb, double* qt, double* ql,
+                      double* qr);
+
+/* Single-field operators, each including its cube-edge sync. */
+void orc_co2contra(const orc_domain* d, const double* u, const double* v,
+                   double* ut, double* vt);
+void orc_contra2co(const orc_domain* d, const double* ut, const double* vt,
+                   double* u, double* v);
+void orc_grad(const orc_domain* d, const double* f, double* gx, double* gy);
+void orc_div(const orc_domain* d, const double* u, const double* v, double* div);
+void orc_curl(const orc_domain* d, const double* u, const double* v, double* curl);
+void orc_sync_scalar(const orc_domain* d, double* f);
+void orc_sync_vector_cov(const orc_domain* d, double* gx, double* gy);
+void orc_coriolis(const orc_domain* d, const double* hu, const double* hv,
+                  const double* h, const double* curl, double* cor_u,
+                  double* cor_v);
+
+/* Model operator, RK4 and diagnostics.  hs (orography) may be NULL (zero). */
+void orc_apply(const orc_domain* d, const double* hs, const double* h,
+               const double* u, const double* v, double* th, double* tu,
+               double* tv);
+void orc_rk4(const orc_domain* d, const double* hs, double* h, double* u,
+             double* v, double dt, int nsteps);
+/* out[7] = hmin, hmax, mass, TE, KE, PE, Enstrophy (operator_swm_mod.f90:115-155) */
+void orc_diagnostics(const orc_domain* d, const double* hs, const double* h,
+                     const double* u, const double* v, double out[7]);
+double orc_l2norm(const orc_domain* d, const double* f);   /* vec_math_mod.f90:50-90 */
+double orc_mass(const orc_domain* d, const double* f);     /* SBP quadrature */
+
+/* Known-answer tests at (N, nz=3, unit sphere); out receives the values
+ * printed by the reference test (4 for div/curl, 2 for grad/co2contra). */
+int orc_golden_div(int N, int sbp_order, double out[4]);
+int orc_golden_grad(int N, int sbp_order, double out[2]);
+int orc_golden_curl(int N, int sbp_order, double out[4]);
+int orc_golden_co2contra(int N, double out[2]);
+int orc_golden_contra2co(int N, double out[2]);
+/* SBP quadrature exactness (test_quadrature_mod.f90:18-80): returns the
+ * largest |exact - numeric| over orders 0..max_order at N. */
+double orc_golden_quadrature(int N, int sbp_order, int max_order);
+/* RK4 amplification test (test_time_steping/test_ts_mod.f90:7-73). */
+double orc_golden_rk4_iomega(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

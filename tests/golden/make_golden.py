@@ -1,0 +1,47 @@
+"""Regenerate tests/golden/diffops_ah_n32.json from the reference's own
+known-answer file src/test/test_diff_ops/reference_results.txt.
+
+Run once in a container that has the reference checked out:
+    python tests/golden/make_golden.py /root/reference
+The JSON keeps only the Ah-grid (colocated, SBP) entries that pin the hot
+path, each with the line number of the reference file it came from.  The
+values were printed by the reference test with format "(A,4E15.7)", i.e. to
+7 significant digits, from test_diffops_all.f90 at N=32, nz=3.
+"""
+import json
+import os
+import sys
+
+KEEP = {
+    "divergence_ah42_sbp": ("div", 42),
+    "divergence_ah43_sbp": ("div", 43),
+    "gradient_ah21_sbp_ecs": ("grad", 21),
+    "gradient_ah42_sbp_ecs": ("grad", 42),
+    "gradient_ah43_sbp_ecs": ("grad", 43),
+    "curl_divergence_ah42_sbp": ("curl", 42),
+    "curl_divergence_ah43_sbp": ("curl", 43),
+    "co2contra_colocated Ah grid": ("co2contra", 42),
+    "contra2co_colocated": ("contra2co", 42),
+}
+
+
+def main(ref_root):
+    path = os.path.join(ref_root, "src/test/test_diff_ops/reference_results.txt")
+    lines = open(path).read().splitlines()
+    out = []
+    for k, line in enumerate(lines):
+        name = line.strip()
+        if name in KEEP and k + 1 < len(lines) and lines[k + 1].startswith("Err:"):
+            vals = [float(x) for x in lines[k + 1].split()[1:]]
+            kind, order = KEEP[name]
+            out.append({"name": name, "kind": kind, "sbp_order": order, "N": 32,
+                        "nz": 3, "values": vals,
+                        "source": f"src/test/test_diff_ops/reference_results.txt:{k + 1}-{k + 2}"})
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "diffops_ah_n32.json")
+    with open(dst, "w") as f:
+        json.dump(out, f, indent=1)
+    print(f"wrote {len(out)} entries to {dst}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
