@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark of the shallow-water RK4 hot path on GB300.
+
+Workload: 6 panels x 385^2 nodes (N=384), SBP 4/2 operators, RK4 with
+dt = 120 s, seeded balanced zonal flow plus a degree<=64 spherical-harmonic
+height perturbation (synthetic; the reference's own test cases are analytic
+and produce no checked-in data).  One "step" is one RK4 step of the whole
+state.  The headline value is the FP32 fused form (compensated stage sums,
+FP64 metric precompute); the FP64 plain path is measured beside it.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+Multi-GPU runs (torchrun) are independent replicas, one per GPU: the path
+does not shard across GPUs here (all six panels live on one GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("RK4 steps/s at 6×384² (FP32 form vs FP64 plain), "
+          "adjoint/forward time ratio")
+N_BENCH, ORDER, DT = 384, 42, 120.0
+L2_FLUSH_BYTES = 256 << 20          # > 129 MB L2
+# Algorithmic HBM bytes per node per RK4 step (4 stage launches), see DESIGN:
+#  FP32 compensated: 77 words x 4 B; FP64 plain: 68 + 4 (rJ) words x 8 B.
+BYTES_PER_NODE_STEP = {"fp32": 77 * 4, "fp64": 72 * 8}
+KERNELS_PER_STEP = 8                # 4 x (stage kernel + cube-edge kernel)
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profile_traffic():
+    """Per-launch DRAM traffic of the stage kernel from the committed ncu
+    summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "stage_kernel_fp32_n384.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                      text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out, _ = self.p.communicate()
+
+    def summary(self):
+        if not getattr(self, "out", ""):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            if self.uuid and self.uuid not in f[0]:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _state(cfg_N):
+    from cubedsphere_sbp_swm_gb300 import initial
+    h, u, v, info = initial.balanced_zonal(cfg_N, 2, 64)
+    return h, u, v, info
+
+
+def run_gpu_arm(args):
+    import numpy as np
+    import torch
+
+    import cubedsphere_sbp_swm_gb300 as swm
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    h, u, v, info = _state(N_BENCH)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def time_steps(prec, steps, warmup, kernel_timing=False):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N_BENCH, sbp_order=ORDER, precision=prec, device=local))
+        s = op.create_stvec()
+        s.upload(h, u, v)
+        ts = swm.RK4()
+        stream = torch.cuda.ExternalStream(op.stream, device=dev)
+        for _ in range(warmup):
+            ts.step(s, op, DT, 1)
+        op.synchronize()
+        if kernel_timing:
+            op.timing_enable(True)
+            op.timing_read()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        torch.cuda.synchronize(dev)
+        for a, b in evs:
+            with torch.cuda.stream(stream):
+                flush.zero_()                         # evict L2 between timed steps
+            a.record(stream)
+            ts.step(s, op, DT, 1)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = [a.elapsed_time(b) for a, b in evs]
+        kt = op.timing_read() if kernel_timing else None
+        if kernel_timing:
+            op.timing_enable(False)
+        return op, s, ms, kt
+
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+
+    # headline: FP32 fused form, graph-replayed steps
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(uuid) as clk:
+        op32, s32, ms32, _ = time_steps("fp32", args.steps, args.warmup)
+    clocks = clk.summary()
+    total_ms = sum(ms32)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = ws * args.steps / (total_ms / 1e3)
+
+    # dominant kernel timing (stage kernel), events around every launch
+    _, _, _, kt = time_steps("fp32", max(8, min(args.steps, 40)), 2, kernel_timing=True)
+    stage_ms, stage_n, edge_ms, edge_n = kt
+    npts = 6 * (N_BENCH + 1) ** 2
+    bytes_per_launch = BYTES_PER_NODE_STEP["fp32"] * npts / 4.0
+    achieved = bytes_per_launch / (stage_ms / stage_n / 1e3) / 1e9
+    peak, peak_kind = _measured_peak()
+    traffic = _profile_traffic()
+
+    # FP64 plain path beside it
+    op64, s64, ms64, _ = time_steps("fp64", max(10, args.steps // 2), args.warmup)
+    fp64_ms = sum(ms64) / len(ms64)
+    _, _, _, kt64 = time_steps("fp64", 10, 2, kernel_timing=True)
+
+    # end to end through the C-ABI with host (pinned) buffers
+    pin = [torch.empty((6, N_BENCH + 1, N_BENCH + 1), dtype=torch.float64, pin_memory=True) for _ in range(6)]
+    for t_, a_ in zip(pin[:3], (h, u, v)):
+        t_.numpy()[...] = a_
+    hin = [t_.numpy() for t_ in pin[:3]]
+    hout = [t_.numpy() for t_ in pin[3:]]
+    ts = swm.RK4()
+    e2e_steps = max(10, args.steps // 2)
+    for _ in range(2):
+        s32.upload_async(*hin)
+        ts.step(s32, op32, DT, 1)
+        s32.download(out=hout)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s32.upload_async(*hin)
+        ts.step(s32, op32, DT, 1)
+        s32.download(out=hout)
+    e2e_s = time.perf_counter() - t0
+    e2e_val = ws * e2e_steps / e2e_s
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_val = ws * e2e_steps / float(t.item())
+
+    # CPU baseline: the oracle (C++ restatement) on the host cores, rank 0
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline_sample(h, u, v, budget_s=args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded balanced zonal flow u0=%.2f m/s + Y_lm (l<=64) height "
+                    "perturbation, 10 m RMS" % info["u0"],
+            "config": {"workload": "6 panels x 385^2 nodes (N=384), SBP 4/2 (d42), RK4 dt=120 s, "
+                                   "FP32 fused form (compensated stage sums, FP64 metric precompute)",
+                       "N": N_BENCH, "sbp": "d42", "dt_s": DT, "nodes_per_field": npts,
+                       "l2": "256 MB buffer written between timed steps",
+                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "e2e": {"value": round(e2e_val, 3), "unit": "steps/s",
+                    "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,
+                    "path": "swm_state_upload (pinned FP64 host) + swm_rk4_step + swm_state_download"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "kernel": "stage_kernel<float,42>", "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "avg_launch_us": round(stage_ms / stage_n * 1e3, 3),
+                         "edge_kernel_avg_us": round(edge_ms / max(edge_n, 1) * 1e3, 3)},
+            "fp64_plain": {"value": round(1e3 / fp64_ms, 3), "unit": "steps/s",
+                           "ms_per_step": round(fp64_ms, 5),
+                           "stage_kernel_avg_us": round(kt64[0] / kt64[1] * 1e3, 3)},
+            "fp32_over_fp64": round((1e3 / ms_per_step) / (1e3 / fp64_ms), 3),
+            "clocks": clocks,
+            "gpu_launches": KERNELS_PER_STEP * args.steps,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_sample(h, u, v, budget_s=15.0, min_steps=1, max_steps=50):
+    """Time RK4 steps of the FP64 oracle with all host threads on a bounded
+    sample (whole N=384 steps until the time budget is used)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU restatement of the reference (checker / baseline)
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    od = oracle.OracleDomain(N_BENCH, ORDER)
+    hh, uu, vv = h.copy(), u.copy(), v.copy()
+    hh, uu, vv = od.rk4(hh, uu, vv, DT, 1)            # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps and (steps < min_steps or time.perf_counter() - t0 < budget_s):
+        hh, uu, vv = od.rk4(hh, uu, vv, DT, 1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(steps / dt, 4), "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} RK4 steps of the N=384 FP64 oracle (C++ restatement of the reference), "
+                      f"OpenMP over panel rows"}
+
+
+def run_reference_arm(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    h, u, v, info = _state(N_BENCH)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    od = oracle.OracleDomain(N_BENCH, ORDER)
+    for _ in range(args.warmup):
+        h, u, v = od.rk4(h, u, v, DT, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        h, u, v = od.rk4(h, u, v, DT, 1)
+    el = time.perf_counter() - t0
+    val = args.steps / el
+    line = {
+        "metric": METRIC, "value": round(val, 4), "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic: seeded balanced zonal flow + Y_lm (l<=64) height perturbation",
+        "config": {"workload": "6 panels x 385^2 nodes (N=384), SBP 4/2 (d42), RK4 dt=120 s, FP64",
+                   "N": N_BENCH, "sbp": "d42", "dt_s": DT},
+        "cpu_baseline": {"value": round(val, 4), "unit": "steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} RK4 steps of the FP64 C++ restatement of the reference "
+                                   "(the Fortran/MPI reference has no compiler on this image)"},
+        "e2e": {"value": round(val, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

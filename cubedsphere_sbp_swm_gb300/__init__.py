@@ -1,0 +1,353 @@
+"""GB300-native shallow-water time-stepping hot path (cubed sphere, Ah-grid SBP).
+
+Host-side mirror of the reference's plugin surface
+(vvshashkin/cubedsphere_sbp_swm), over the C-ABI of include/swm_gpu.h:
+
+  OperatorSWM      operator_t / operator_swm_t  (apply, get_diagnostics)
+  StvecSWM         stvec_t / stvec_swm_t        (assign/update/dot/norm2)
+  RK4              timescheme_t / rk4_t         (step)
+  HaloAhScalarSync, EcsAhVecSyncCovariant       halo_t / halo_vec_t
+  GridField        grid_field_t (FP64 field; single operators)
+
+Host arrays are float64 with shape (6, N+1, N+1) = (panel, j, i): one tile
+per panel as in the reference Ah grid, edge nodes duplicated on both panels.
+All compute runs in libswm_gb300.so on the GPU; nothing here falls back to
+the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from ._abi import SWM_FP32_FUSED, SWM_FP64_PLAIN, SwmError
+
+__all__ = [
+    "ModelConfig", "OperatorSWM", "StvecSWM", "GridField", "RK4", "HaloAhScalarSync",
+    "EcsAhVecSyncCovariant", "create_timescheme", "create_halo_procedure",
+    "create_vector_halo_procedure", "SwmError", "EARTH",
+]
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+# constants of the benchmark configurations (not the reference's const_mod)
+EARTH = dict(radius=6.371e6, grav=9.80616, omega=7.292e-5)
+
+_PREC = {"fp64": SWM_FP64_PLAIN, "fp64_plain": SWM_FP64_PLAIN,
+         "fp32": SWM_FP32_FUSED, "fp32_fused": SWM_FP32_FUSED}
+
+DIAG_KEYS = ("hmin", "hmax", "mass", "TE", "KE", "PE", "Enstrophy")
+
+
+@dataclass
+class ModelConfig:
+    """&domain / &metric / &shallow_water_model keys of the hot path."""
+    N: int
+    sbp_order: int = 42
+    radius: float = EARTH["radius"]
+    grav: float = EARTH["grav"]
+    omega: float = EARTH["omega"]
+    rotation_axis: tuple = (0.0, 0.0, 1.0)
+    precision: str = "fp64"
+    device: int = 0
+    # operator names of the &shallow_water_model namelist (None: derived
+    # from sbp_order)
+    names: dict | None = field(default=None)
+
+    def c_struct(self) -> _abi.SwmConfig:
+        c = _abi.SwmConfig()
+        c.N = int(self.N)
+        c.sbp_order = int(self.sbp_order)
+        c.radius, c.grav, c.omega = float(self.radius), float(self.grav), float(self.omega)
+        for k in range(3):
+            c.rotation_axis[k] = float(self.rotation_axis[k])
+        if self.precision not in _PREC:
+            raise ValueError(f"unknown precision {self.precision!r}")
+        c.precision = _PREC[self.precision]
+        c.device = int(self.device)
+        return c
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _host(a, shape) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+class OperatorSWM:
+    """operator_swm_t on one GPU: domain geometry, the vector-invariant RHS,
+    its cube-edge syncs, the fused RK4 driver and FP64 diagnostics."""
+
+    def __init__(self, config: ModelConfig | None = None, **kw):
+        if config is None:
+            config = ModelConfig(**kw)
+        self.config = config
+        self._L = _abi.load()
+        c = config.c_struct()
+        h = ctypes.c_void_p()
+        if config.names:
+            nm = config.names
+            keys = ("div_op_name", "grad_op_name", "curl_op_name", "coriolis_op_name",
+                    "KE_op_name", "co2contra_op_name", "massflux_op_name", "quadrature_name")
+            args = [(nm.get(k) or "").encode() for k in keys]
+            rc = self._L.swm_ctx_create_named(ctypes.byref(c), *args, ctypes.byref(h))
+        else:
+            rc = self._L.swm_ctx_create(ctypes.byref(c), ctypes.byref(h))
+        _abi.check(rc, None)
+        self._h = h
+        self.N = config.N
+        self.n = config.N + 1
+        self.shape = (6, self.n, self.n)
+
+    # lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.swm_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        _abi.check(rc, self._h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return self._L.swm_ctx_stream(self._h) or 0
+
+    def synchronize(self):
+        self._check(self._L.swm_ctx_synchronize(self._h))
+
+    @property
+    def npts(self) -> int:
+        return int(self._L.swm_ctx_npts(self._h))
+
+    # factories ----------------------------------------------------------
+    def create_stvec(self) -> "StvecSWM":
+        return StvecSWM(self)
+
+    def create_field(self) -> "GridField":
+        return GridField(self)
+
+    def set_orography(self, hs):
+        hs = _host(hs, self.shape)
+        self._check(self._L.swm_set_orography(self._h, _ptr(hs)))
+
+    # operator_t ---------------------------------------------------------
+    def apply(self, vout: "StvecSWM", vin: "StvecSWM"):
+        """vout = A(vin) (operator_mod.f90:18-25)."""
+        self._check(self._L.swm_apply(self._h, vout._h, vin._h))
+
+    def apply_unfused(self, vout: "StvecSWM", vin: "StvecSWM"):
+        self._check(self._L.swm_apply_unfused(self._h, vout._h, vin._h))
+
+    def get_diagnostics(self, v: "StvecSWM") -> dict:
+        out = np.zeros(7)
+        self._check(self._L.swm_diagnostics(self._h, v._h, _ptr(out)))
+        return dict(zip(DIAG_KEYS, out.tolist()))
+
+    # single operators on GridFields ------------------------------------
+    def co2contra(self, ut, vt, u, v):
+        self._check(self._L.swm_op_co2contra(self._h, ut._h, vt._h, u._h, v._h))
+
+    def massflux(self, hu, hv, h, ut, vt):
+        self._check(self._L.swm_op_massflux(self._h, hu._h, hv._h, h._h, ut._h, vt._h))
+
+    def calc_KE(self, ke, u, v, ut, vt):
+        self._check(self._L.swm_op_ke(self._h, ke._h, u._h, v._h, ut._h, vt._h))
+
+    def calc_grad(self, gx, gy, f):
+        self._check(self._L.swm_op_grad(self._h, gx._h, gy._h, f._h))
+
+    def calc_div(self, div, u, v):
+        self._check(self._L.swm_op_div(self._h, div._h, u._h, v._h))
+
+    def calc_curl(self, curl, u, v):
+        self._check(self._L.swm_op_curl(self._h, curl._h, u._h, v._h))
+
+    def calc_coriolis_vec_inv(self, cor_u, cor_v, hu, hv, h, curl):
+        self._check(self._L.swm_op_coriolis(self._h, cor_u._h, cor_v._h, hu._h, hv._h,
+                                            h._h, curl._h))
+
+    def quadrature_mass(self, f) -> float:
+        out = ctypes.c_double()
+        self._check(self._L.swm_quadrature_mass(self._h, f._h, ctypes.byref(out)))
+        return out.value
+
+    # measurement --------------------------------------------------------
+    def timing_enable(self, on: bool = True):
+        self._check(self._L.swm_timing_enable(self._h, 1 if on else 0))
+
+    def timing_read(self):
+        sm, em = ctypes.c_double(), ctypes.c_double()
+        sl, el = ctypes.c_long(), ctypes.c_long()
+        self._check(self._L.swm_timing_read(self._h, ctypes.byref(sm), ctypes.byref(sl),
+                                            ctypes.byref(em), ctypes.byref(el)))
+        return sm.value, sl.value, em.value, el.value
+
+
+class StvecSWM:
+    """stvec_swm_t: the (h, u, v) state on the device (covariant u, v)."""
+
+    def __init__(self, op: OperatorSWM, _similar_to: "StvecSWM" | None = None):
+        self.op = op
+        h = ctypes.c_void_p()
+        if _similar_to is None:
+            rc = op._L.swm_state_create(op._h, ctypes.byref(h))
+        else:
+            rc = op._L.swm_state_create_similar(op._h, _similar_to._h, ctypes.byref(h))
+        op._check(rc)
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.op._L.swm_state_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def create_similar(self) -> "StvecSWM":
+        return StvecSWM(self.op, _similar_to=self)
+
+    def upload(self, h, u, v):
+        sh = self.op.shape
+        h, u, v = (_host(a, sh) for a in (h, u, v))
+        self.op._check(self.op._L.swm_state_upload(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
+        self.op.synchronize()
+
+    def upload_async(self, h, u, v):
+        """Upload from caller-owned (ideally pinned) C-contiguous float64 arrays
+        without synchronising; the arrays must stay alive until the stream
+        reaches the copy."""
+        self.op._check(self.op._L.swm_state_upload(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
+
+    def download(self, out=None):
+        sh = self.op.shape
+        if out is None:
+            out = tuple(np.empty(sh) for _ in range(3))
+        self.op._check(self.op._L.swm_state_download(self.op._h, self._h, *(_ptr(a) for a in out)))
+        return out
+
+    def assign_s1(self, s1):
+        self.op._check(self.op._L.swm_assign_s1(self.op._h, self._h, float(s1)))
+
+    def assign_s1v1(self, s1, v1):
+        self.op._check(self.op._L.swm_assign_s1v1(self.op._h, self._h, float(s1), v1._h))
+
+    def assign_s1v1s2v2(self, s1, v1, s2, v2):
+        self.op._check(self.op._L.swm_assign_s1v1s2v2(self.op._h, self._h, float(s1), v1._h,
+                                                       float(s2), v2._h))
+
+    def update_s1v1(self, s1, v1):
+        self.op._check(self.op._L.swm_update_s1v1(self.op._h, self._h, float(s1), v1._h))
+
+    def update_s1v1s2v2(self, s1, v1, s2, v2):
+        self.op._check(self.op._L.swm_update_s1v1s2v2(self.op._h, self._h, float(s1), v1._h,
+                                                       float(s2), v2._h))
+
+    def algebraic_dot(self, other) -> float:
+        out = ctypes.c_double()
+        self.op._check(self.op._L.swm_dot(self.op._h, self._h, other._h, ctypes.byref(out)))
+        return out.value
+
+    def algebraic_norm2(self) -> float:
+        out = ctypes.c_double()
+        self.op._check(self.op._L.swm_norm2(self.op._h, self._h, ctypes.byref(out)))
+        return out.value
+
+
+class GridField:
+    """grid_field_t: one FP64 field on the device."""
+
+    def __init__(self, op: OperatorSWM):
+        self.op = op
+        h = ctypes.c_void_p()
+        op._check(op._L.swm_field_create(op._h, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.op._L.swm_field_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, a):
+        a = _host(a, self.op.shape)
+        self.op._check(self.op._L.swm_field_upload(self.op._h, self._h, _ptr(a)))
+        self.op.synchronize()
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.op.shape)
+        self.op._check(self.op._L.swm_field_download(self.op._h, self._h, _ptr(out)))
+        return out
+
+
+class RK4:
+    """rk4_t (time_schemes/rk4_mod.f90:12-42): classic RK4 with the stage
+    combinations fused into the RHS kernels, replayed as a CUDA graph."""
+
+    def step(self, v0: StvecSWM, operator: OperatorSWM, dt: float, nsteps: int = 1):
+        operator._check(operator._L.swm_rk4_step(operator._h, v0._h, float(dt), int(nsteps)))
+
+
+class HaloAhScalarSync:
+    """halo_t "Ah_scalar_sync" (halo/halo_Ah_scalar_sync_mod.f90)."""
+
+    def __init__(self, op: OperatorSWM):
+        self.op = op
+
+    def get_halo_scalar(self, f: GridField, halo_width: int = 1):
+        self.op._check(self.op._L.swm_sync_scalar(self.op._h, f._h))
+
+
+class EcsAhVecSyncCovariant:
+    """halo_vec_t "ecs_Ah_vec_sync_covariant" (equiang_cs/ecs_Ah_vec_sync_mod.f90)."""
+
+    def __init__(self, op: OperatorSWM):
+        self.op = op
+
+    def get_halo_vector(self, u: GridField, v: GridField, halo_width: int = 0):
+        self.op._check(self.op._L.swm_sync_vector_cov(self.op._h, u._h, v._h))
+
+
+def create_timescheme(name: str) -> RK4:
+    """timescheme factory (time_schemes/timescheme_factory_mod.f90:13-59);
+    the GPU hot path provides "rk4"."""
+    if name == "rk4":
+        return RK4()
+    raise SwmError(_abi.SWM_E_UNSUPPORTED, f"unsupported time scheme: {name}")
+
+
+def create_halo_procedure(op: OperatorSWM, name: str):
+    if name == "Ah_scalar_sync":
+        return HaloAhScalarSync(op)
+    raise SwmError(_abi.SWM_E_UNSUPPORTED, f"unsupported halo procedure: {name}")
+
+
+def create_vector_halo_procedure(op: OperatorSWM, name: str):
+    if name == "ecs_Ah_vec_sync_covariant":
+        return EcsAhVecSyncCovariant(op)
+    raise SwmError(_abi.SWM_E_UNSUPPORTED, f"unsupported vector halo procedure: {name}")

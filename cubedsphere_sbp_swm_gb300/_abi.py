@@ -1,0 +1,133 @@
+"""ctypes binding of libswm_gb300.so (the C-ABI of include/swm_gpu.h).
+
+The library is built in-tree by cubedsphere_sbp_swm_gb300.build; loading
+fails loudly when it is missing (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+SWM_OK = 0
+SWM_E_INVALID = -1
+SWM_E_UNSUPPORTED = -2
+SWM_E_CUDA = -3
+SWM_E_NOMEM = -4
+SWM_E_DEVICE = -5
+
+SWM_FP64_PLAIN = 0
+SWM_FP32_FUSED = 1
+
+# every entry point of include/swm_gpu.h
+EXPORTS = (
+    "swm_ctx_create", "swm_ctx_create_named", "swm_ctx_destroy", "swm_last_error",
+    "swm_ctx_synchronize", "swm_ctx_stream", "swm_ctx_npts", "swm_set_orography",
+    "swm_state_create", "swm_state_create_similar", "swm_state_free", "swm_state_upload",
+    "swm_state_download", "swm_assign_s1", "swm_assign_s1v1", "swm_assign_s1v1s2v2",
+    "swm_update_s1v1", "swm_update_s1v1s2v2", "swm_dot", "swm_norm2", "swm_apply",
+    "swm_apply_unfused", "swm_rk4_step", "swm_diagnostics", "swm_field_create",
+    "swm_field_free", "swm_field_upload", "swm_field_download", "swm_op_co2contra",
+    "swm_op_massflux", "swm_op_ke", "swm_op_grad", "swm_op_div", "swm_op_curl",
+    "swm_op_coriolis", "swm_sync_scalar", "swm_sync_vector_cov", "swm_quadrature_mass",
+    "swm_timing_enable", "swm_timing_read",
+)
+
+
+class SwmConfig(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int),
+        ("sbp_order", ctypes.c_int),
+        ("radius", ctypes.c_double),
+        ("grav", ctypes.c_double),
+        ("omega", ctypes.c_double),
+        ("rotation_axis", ctypes.c_double * 3),
+        ("precision", ctypes.c_int),
+        ("device", ctypes.c_int),
+    ]
+
+
+class SwmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+_D = ctypes.POINTER(ctypes.c_double)
+_VP = ctypes.c_void_p
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libswm_gb300.so, compiling it first when it is absent or stale."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(path):
+        raise OSError(f"libswm_gb300.so not found at {path}: build the CUDA library first")
+    L = ctypes.CDLL(path)
+    I, D, VP, C = ctypes.c_int, ctypes.c_double, _VP, ctypes.c_char_p
+    PP = ctypes.POINTER(ctypes.c_void_p)
+
+    def sig(name, res, *args):
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = list(args)
+
+    sig("swm_ctx_create", I, ctypes.POINTER(SwmConfig), PP)
+    sig("swm_ctx_create_named", I, ctypes.POINTER(SwmConfig), C, C, C, C, C, C, C, C, PP)
+    sig("swm_ctx_destroy", None, VP)
+    sig("swm_last_error", C, VP)
+    sig("swm_ctx_synchronize", I, VP)
+    sig("swm_ctx_stream", VP, VP)
+    sig("swm_ctx_npts", ctypes.c_size_t, VP)
+    sig("swm_set_orography", I, VP, _D)
+    sig("swm_state_create", I, VP, PP)
+    sig("swm_state_create_similar", I, VP, VP, PP)
+    sig("swm_state_free", None, VP)
+    sig("swm_state_upload", I, VP, VP, _D, _D, _D)
+    sig("swm_state_download", I, VP, VP, _D, _D, _D)
+    sig("swm_assign_s1", I, VP, VP, D)
+    sig("swm_assign_s1v1", I, VP, VP, D, VP)
+    sig("swm_assign_s1v1s2v2", I, VP, VP, D, VP, D, VP)
+    sig("swm_update_s1v1", I, VP, VP, D, VP)
+    sig("swm_update_s1v1s2v2", I, VP, VP, D, VP, D, VP)
+    sig("swm_dot", I, VP, VP, VP, _D)
+    sig("swm_norm2", I, VP, VP, _D)
+    sig("swm_apply", I, VP, VP, VP)
+    sig("swm_apply_unfused", I, VP, VP, VP)
+    sig("swm_rk4_step", I, VP, VP, D, I)
+    sig("swm_diagnostics", I, VP, VP, _D)
+    sig("swm_field_create", I, VP, PP)
+    sig("swm_field_free", None, VP)
+    sig("swm_field_upload", I, VP, VP, _D)
+    sig("swm_field_download", I, VP, VP, _D)
+    sig("swm_op_co2contra", I, VP, VP, VP, VP, VP)
+    sig("swm_op_massflux", I, VP, VP, VP, VP, VP, VP)
+    sig("swm_op_ke", I, VP, VP, VP, VP, VP, VP)
+    sig("swm_op_grad", I, VP, VP, VP, VP)
+    sig("swm_op_div", I, VP, VP, VP, VP)
+    sig("swm_op_curl", I, VP, VP, VP, VP)
+    sig("swm_op_coriolis", I, VP, VP, VP, VP, VP, VP, VP)
+    sig("swm_sync_scalar", I, VP, VP)
+    sig("swm_sync_vector_cov", I, VP, VP, VP)
+    sig("swm_quadrature_mass", I, VP, VP, _D)
+    sig("swm_timing_enable", I, VP, I)
+    sig("swm_timing_read", I, VP, _D, ctypes.POINTER(ctypes.c_long), _D,
+        ctypes.POINTER(ctypes.c_long))
+    _lib = L
+    return L
+
+
+def check(rc: int, ctx=None) -> None:
+    if rc != SWM_OK:
+        msg = load().swm_last_error(ctx)
+        raise SwmError(rc, msg.decode() if msg else "")

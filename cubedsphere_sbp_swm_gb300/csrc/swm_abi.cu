@@ -1,0 +1,988 @@
+// swm_abi.cu -- the C-ABI of include/swm_gpu.h: context (domain + operator +
+// RK4 time scheme), device states and fields, the fused RK4 driver replayed
+// as a CUDA graph, the unfused FP64 operator path and FP64 diagnostics.
+#include "../../include/swm_gpu.h"
+#include "swm_launch.h"
+#include "swm_ops.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <utility>
+#include <vector>
+
+using namespace swm;
+
+namespace {
+
+thread_local std::string g_err;  // errors without a context
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// ---------------------------------------------------------------------------
+// Cube topology on the host: which neighbour side holds the duplicated nodes
+// of each panel side, and the component map of the vector exchange.  Follows
+// transform_index / find_basis_orientation of the reference
+// (topology/cubed_sphere_topology_mod.f90:80-239) and the halo placement of
+// parallel/exchange_factory_mod.f90:157-299 (the neighbour's copy of a shared
+// node sits in the 1-wide halo ring).
+// ---------------------------------------------------------------------------
+const int kEX[6][3] = {{-1, 0, 0}, {0, 0, -1}, {1, 0, 0}, {0, 0, 1}, {1, 0, 0}, {1, 0, 0}};
+const int kEY[6][3] = {{0, 1, 0}, {0, 1, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, -1}};
+const int kN[6][3] = {{0, 0, 1}, {-1, 0, 0}, {0, 0, -1}, {1, 0, 0}, {0, 1, 0}, {0, -1, 0}};
+const int kR[6][3] = {{1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 1, 1}};
+
+int dot3(const int* a, const int* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// frame of target panel pt unfolded across its edge with source panel ps
+void unfolded_frame(int ps, int pt, int nx, int exl[3], int eyl[3], int rl[3], int sh[2]) {
+  const int dr = dot3(kEX[pt], kN[ps]), db = dot3(kEY[pt], kN[ps]);
+  for (int c = 0; c < 3; ++c) {
+    if (dr == -1) { exl[c] = kN[pt][c]; eyl[c] = kEY[pt][c]; rl[c] = kR[pt][c] + kEX[pt][c]; }
+    else if (dr == 1) { exl[c] = -kN[pt][c]; eyl[c] = kEY[pt][c]; rl[c] = kR[pt][c] + kN[pt][c]; }
+    else if (db == 1) { exl[c] = kEX[pt][c]; eyl[c] = -kN[pt][c]; rl[c] = kR[pt][c] + kN[pt][c]; }
+    else if (db == -1) { exl[c] = kEX[pt][c]; eyl[c] = kN[pt][c]; rl[c] = kR[pt][c] + kEY[pt][c]; }
+    else { exl[c] = -kEX[pt][c]; eyl[c] = kEY[pt][c]; rl[c] = kR[pt][c] + kEX[pt][c] + kN[pt][c]; }
+  }
+  if (dr == -1) { sh[0] = nx; sh[1] = 0; }
+  else if (dr == 1) { sh[0] = -nx; sh[1] = 0; }
+  else if (db == 1) { sh[0] = 0; sh[1] = -nx; }
+  else if (db == -1) { sh[0] = 0; sh[1] = nx; }
+  else { sh[0] = 2 * nx; sh[1] = 0; }
+}
+
+void map_index(int ps, int is, int js, int pt, int n, int& it, int& jt) {
+  int exl[3], eyl[3], rl[3], sh[2], d[3];
+  unfolded_frame(ps, pt, n, exl, eyl, rl, sh);
+  for (int c = 0; c < 3; ++c) d[c] = kR[ps][c] - rl[c];
+  it = (is - 1) * dot3(kEX[ps], exl) + (js - 1) * dot3(kEY[ps], exl) + (n - 1) * dot3(d, exl) + 1 + sh[0];
+  jt = (is - 1) * dot3(kEX[ps], eyl) + (js - 1) * dot3(kEY[ps], eyl) + (n - 1) * dot3(d, eyl) + 1 + sh[1];
+}
+
+void orientation(int ps, int pt, int& istep, int& jstep, int& dim_i) {
+  int exl[3], eyl[3], rl[3], sh[2];
+  unfolded_frame(ps, pt, 2, exl, eyl, rl, sh);
+  const int ex_ex = dot3(kEX[ps], exl), ex_ey = dot3(kEY[ps], exl);
+  const int ey_ex = dot3(kEX[ps], eyl), ey_ey = dot3(kEY[ps], eyl);
+  if (ex_ex != 0) { dim_i = 1; istep = ex_ex; jstep = ey_ey; }
+  else { dim_i = 0; istep = ex_ey; jstep = ey_ex; }
+}
+
+bool build_topology(Topology& tp, std::string& why) {
+  const int n = 9;  // the map is linear along a side; any size resolves it
+  for (int p = 0; p < 6; ++p)
+    for (int s = 0; s < 4; ++s) tp.link[p][s].q = -1;
+  for (int p = 0; p < 6; ++p) {
+    for (int q = 0; q < 6; ++q) {
+      if (q == p) continue;
+      int istep, jstep, dim_i;
+      orientation(p, q, istep, jstep, dim_i);  // (receiver, sender)
+      int k_first[4] = {-1, -1, -1, -1}, kq_first[4], kq_mid[4], sq_mid[4];
+      for (int js = 1; js <= n; ++js)
+        for (int is = 1; is <= n; ++is) {
+          if (is != 1 && is != n && js != 1 && js != n) continue;
+          int it, jt;
+          map_index(q, is, js, p, n, it, jt);
+          int side = -1, k = -1;
+          if (it == 0 && jt >= 1 && jt <= n) { side = SIDE_L; k = jt - 1; }
+          else if (it == n + 1 && jt >= 1 && jt <= n) { side = SIDE_R; k = jt - 1; }
+          else if (jt == 0 && it >= 1 && it <= n) { side = SIDE_B; k = it - 1; }
+          else if (jt == n + 1 && it >= 1 && it <= n) { side = SIDE_T; k = it - 1; }
+          if (side < 0) continue;
+          // side of q holding the node, and its along-side index
+          int sq, kq;
+          if (k == n / 2) {
+            if (is == 1) { sq = SIDE_L; kq = js - 1; }
+            else if (is == n) { sq = SIDE_R; kq = js - 1; }
+            else if (js == 1) { sq = SIDE_B; kq = is - 1; }
+            else { sq = SIDE_T; kq = is - 1; }
+            sq_mid[side] = sq;
+            kq_mid[side] = kq;
+          }
+          if (k == 0) {
+            k_first[side] = 0;
+            // remember q-node of k=0 (along-side index resolved below)
+            kq_first[side] = (js - 1) * n + (is - 1);
+          }
+        }
+      for (int s = 0; s < 4; ++s) {
+        if (k_first[s] < 0) continue;
+        EdgeLink L;
+        L.q = q;
+        L.side_q = sq_mid[s];
+        const int node0 = kq_first[s];
+        const int is0 = node0 % n, js0 = node0 / n;
+        const int k0 = (L.side_q == SIDE_L || L.side_q == SIDE_R) ? js0 : is0;
+        L.rev = (k0 == 0) ? 0 : 1;
+        if (L.rev && k0 != n - 1) { why = "topology: non-linear side map"; return false; }
+        if ((L.rev ? n - 1 - n / 2 : n / 2) != kq_mid[s]) { why = "topology: inconsistent side map"; return false; }
+        L.dim_i = dim_i;
+        L.istep = istep;
+        L.jstep = jstep;
+        tp.link[p][s] = L;
+      }
+    }
+  }
+  for (int p = 0; p < 6; ++p)
+    for (int s = 0; s < 4; ++s)
+      if (tp.link[p][s].q < 0) { why = "topology: panel side without neighbour"; return false; }
+  return true;
+}
+
+const SbpC kTables[4] = SWM_SBP_TABLES;
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// handles
+// ---------------------------------------------------------------------------
+struct swm_state {
+  swm_ctx* ctx;
+  void* hi;     // 3 fields of the context precision
+  float* lo;    // FP32 contexts: low parts of the compensated state
+};
+
+struct swm_field {
+  swm_ctx* ctx;
+  double* p;
+};
+
+struct GraphEntry {
+  cudaGraphExec_t exec;
+  long use;
+};
+
+struct swm_ctx {
+  swm_config cfg{};
+  int N = 0, n = 0, P = 0, order = 42, prec = SWM_FP64_PLAIN, elt = 8;
+  long long ps = 0, fs = 0;
+  double hx = 0.0, ghs = 0.0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  Topology topo{};
+  FieldGeom g{};      // geometry of the context-precision fields
+  FieldGeom g64{};    // geometry of FP64 fields (pitch for doubles)
+  double* m64 = nullptr;   // FP64 metric, NMETRIC fields (g64)
+  float* m32 = nullptr;    // FP32 metric copy (FP32 contexts)
+  double* qw = nullptr;    // sync weights 4n
+  double* Aw = nullptr;    // quadrature weights per line index (n)
+  void* edge = nullptr;    // stage edge buffer (context precision)
+  double* edge64 = nullptr;
+  void* ya = nullptr; void* yb = nullptr; void* acc = nullptr;  // RK work (3 fields)
+  double* tmp = nullptr;   // 14 FP64 work fields (g64)
+  double* hs64 = nullptr; void* hsT = nullptr;
+  double* partial = nullptr; double* dres = nullptr; double* hres = nullptr;
+  WorkUnit* units = nullptr; int nunits = 0;
+  std::map<std::pair<void*, double>, GraphEntry> graphs;
+  long graph_clock = 0;
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_stage, ev_edge;
+  // live children: destroying the context releases their device memory and
+  // detaches them, so a later swm_state_free / swm_field_free stays safe
+  std::set<swm_state*> states;
+  std::set<swm_field*> fields;
+};
+
+namespace {
+
+int fail(swm_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg; else g_err = msg;
+  return code;
+}
+int cuda_fail(swm_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, SWM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call, where)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, where); \
+  } while (0)
+
+long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+// Work units of the fused stage kernel: column strips x row segments.
+bool make_units(const SbpC& s, int n, int threads, std::vector<WorkUnit>& out, std::string& why) {
+  auto need_lo = [&](int k) {
+    if (k < s.ne) return 0;
+    if (k >= n - s.ne) return n - s.last[n - 1 - k];
+    return k - s.H;
+  };
+  auto need_hi = [&](int k) {
+    if (k < s.ne) return s.last[k] - 1;
+    if (k >= n - s.ne) return n - 1;
+    return k + s.H;
+  };
+  int nstrip = (n + (threads - 2 * s.rmax) - 1) / (threads - 2 * s.rmax);
+  std::vector<int> cs;
+  for (;; ++nstrip) {
+    cs.assign(nstrip + 1, 0);
+    for (int k = 0; k <= nstrip; ++k) cs[k] = (int)((long long)n * k / nstrip);
+    bool ok = true;
+    for (int k = 0; k < nstrip && ok; ++k) {
+      int lo = n, hi = 0;
+      for (int c = cs[k]; c < cs[k + 1]; ++c) { lo = std::min(lo, need_lo(c)); hi = std::max(hi, need_hi(c)); }
+      ok = (hi + 1 - lo) <= threads && (cs[k + 1] - cs[k]) >= 1;
+    }
+    if (ok) break;
+    if (nstrip > n) { why = "work split failed"; return false; }
+  }
+  const int seg = 16;
+  const int nseg = (n + seg - 1) / seg;
+  for (int p = 0; p < 6; ++p)
+    for (int k = 0; k < nstrip; ++k)
+      for (int r = 0; r < nseg; ++r) {
+        WorkUnit w;
+        w.inst = 0; w.panel = (int16_t)p;
+        w.i0 = (int16_t)cs[k]; w.i1 = (int16_t)cs[k + 1];
+        w.j0 = (int16_t)((long long)n * r / nseg); w.j1 = (int16_t)((long long)n * (r + 1) / nseg);
+        if (w.j1 <= w.j0) continue;
+        int lo = n, hi = 0;
+        for (int c = w.i0; c < w.i1; ++c) { lo = std::min(lo, need_lo(c)); hi = std::max(hi, need_hi(c)); }
+        w.cl0 = (int16_t)lo; w.cl1 = (int16_t)(hi + 1);
+        lo = n; hi = 0;
+        for (int c = w.j0; c < w.j1; ++c) { lo = std::min(lo, need_lo(c)); hi = std::max(hi, need_hi(c)); }
+        w.rl0 = (int16_t)lo; w.rl1 = (int16_t)(hi + 1);
+        out.push_back(w);
+      }
+  return true;
+}
+
+bool name_order(const std::string& nm, const char* prefix, const char* suffix, int& order) {
+  const std::string pre(prefix), suf(suffix);
+  if (nm.size() < pre.size() + suf.size() + 2) return false;
+  if (nm.compare(0, pre.size(), pre) != 0) return false;
+  if (nm.compare(nm.size() - suf.size(), suf.size(), suf) != 0) return false;
+  const std::string mid = nm.substr(pre.size(), nm.size() - pre.size() - suf.size());
+  if (mid == "21") order = 21;
+  else if (mid == "42") order = 42;
+  else if (mid == "43") order = 43;
+  else if (mid == "63") order = 63;
+  else return false;
+  return true;
+}
+
+template <class T>
+InstDev<T> base_inst(swm_ctx* c) {
+  InstDev<T> I{};
+  I.n = c->n; I.P = c->P; I.ps = c->ps; I.fs = c->fs;
+  I.metric = (c->prec == SWM_FP32_FUSED) ? (const T*)(const void*)c->m32 : (const T*)(const void*)c->m64;
+  I.qw = c->qw;
+  I.hs = (const T*)c->hsT;
+  I.edge = (T*)c->edge;
+  I.ghs = (T)c->ghs;
+  I.grav = (T)c->cfg.grav;
+  return I;
+}
+
+template <class T>
+int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (ctx->timing) {
+    CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
+    CK(cudaEventRecord(a, ctx->st), "event record");
+  }
+  CK(launch_stage<T>(ctx->order, I, nullptr, ctx->units, ctx->nunits, mode, ctx->st), "stage kernel");
+  if (ctx->timing) {
+    CK(cudaEventRecord(b, ctx->st), "event record");
+    ctx->ev_stage.emplace_back(a, b);
+    CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
+    CK(cudaEventRecord(a, ctx->st), "event record");
+  }
+  CK(launch_edge<T>(I, nullptr, 1, ctx->n, ctx->topo, mode, ctx->st), "edge kernel");
+  if (ctx->timing) {
+    CK(cudaEventRecord(b, ctx->st), "event record");
+    ctx->ev_edge.emplace_back(a, b);
+  }
+  return SWM_OK;
+}
+
+// One RK4 step of the fused path on state s (see rk4_mod.f90:20-42).
+template <class T>
+int enqueue_rk4(swm_ctx* ctx, swm_state* s, double dt) {
+  T* v0 = (T*)s->hi;
+  T* ya = (T*)ctx->ya;
+  T* yb = (T*)ctx->yb;
+  T* acc = (T*)ctx->acc;
+  InstDev<T> I = base_inst<T>(ctx);
+  int rc;
+  // stage 1: k1 = A(v0); y = v0 + dt/2 k1; running sum from v0 + dt/6 k1
+  I.in = v0; I.base = v0; I.out = ya; I.acc = acc;
+  I.c_in = (T)(0.5 * dt); I.c_acc = (T)(dt / 6.0);
+  if ((rc = run_stage<T>(ctx, I, MODE_RK1))) return rc;
+  // stage 2: k2 = A(y); y = v0 + dt/2 k2; sum += dt/3 k2
+  I.in = ya; I.out = yb; I.c_in = (T)(0.5 * dt); I.c_acc = (T)(dt / 3.0);
+  if ((rc = run_stage<T>(ctx, I, MODE_RK2))) return rc;
+  // stage 3: k3 = A(y); y = v0 + dt k3; sum += dt/3 k3
+  I.in = yb; I.out = ya; I.c_in = (T)dt; I.c_acc = (T)(dt / 3.0);
+  if ((rc = run_stage<T>(ctx, I, MODE_RK3))) return rc;
+  // stage 4: k4 = A(y); v0 = sum + dt/6 k4
+  I.in = ya; I.out = nullptr; I.base_out = v0; I.base_lo = s->lo ? (T*)(void*)s->lo : nullptr;
+  I.c_acc = (T)(dt / 6.0);
+  return run_stage<T>(ctx, I, MODE_RK4);
+}
+
+int check_state(swm_ctx* ctx, const swm_state* s) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  if (!s || s->ctx != ctx) return fail(ctx, SWM_E_INVALID, "state does not belong to this context");
+  return SWM_OK;
+}
+int check_field(swm_ctx* ctx, const swm_field* f) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  if (!f || f->ctx != ctx) return fail(ctx, SWM_E_INVALID, "field does not belong to this context");
+  return SWM_OK;
+}
+
+double* tmpf(swm_ctx* c, int k) { return c->tmp + (long long)k * c->g64.fs; }
+
+// FP64 view of a state: the state itself (FP64) or its joined copy in the
+// work fields 11..13 (FP32).
+int state64(swm_ctx* ctx, const swm_state* s, const double** h, const double** u, const double** v) {
+  if (ctx->prec == SWM_FP64_PLAIN) {
+    const double* b = (const double*)s->hi;
+    *h = b; *u = b + ctx->fs; *v = b + 2 * ctx->fs;
+    return SWM_OK;
+  }
+  // FP32 fields share the FP64 geometry (same n, pitch in elements differs)
+  double* d = tmpf(ctx, 11);
+  for (int c = 0; c < 3; ++c) {
+    // join row by row through a pitched 2D copy: same element pitch needed,
+    // so the FP32 pitch is kept equal to the FP64 pitch (see ctx creation)
+    CK(launch_join_f32pair(ctx->fs, (const float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs,
+                           d + c * ctx->g64.fs, ctx->st), "join");
+  }
+  *h = d; *u = d + ctx->g64.fs; *v = d + 2 * ctx->g64.fs;
+  return SWM_OK;
+}
+
+int reduce(swm_ctx* ctx, int kind, const double* a, const double* b, int slot) {
+  CK(launch_reduce(ctx->g64, kind, a, b, ctx->m64 + MJ * ctx->g64.fs, ctx->Aw, ctx->hx * ctx->hx,
+                   ctx->partial, REDUCE_BLOCKS, ctx->dres + slot, ctx->st), "reduce");
+  return SWM_OK;
+}
+
+int fetch_results(swm_ctx* ctx, int count, double* out) {
+  CK(cudaMemcpyAsync(ctx->hres, ctx->dres, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->st), "copy results");
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  std::memcpy(out, ctx->hres, sizeof(double) * count);
+  return SWM_OK;
+}
+
+// unfused operator helpers on FP64 fields
+int op_curl(swm_ctx* ctx, const double* u, const double* v, double* out) {
+  CK(launch_div_presync(ctx->g64, ctx->order, ctx->hx * ctx->cfg.radius, ctx->m64, u, v, 1, out, ctx->st), "curl");
+  CK(launch_sync_scalar(ctx->g64, ctx->topo, out, ctx->edge64, ctx->st), "sync");
+  return SWM_OK;
+}
+int op_div(swm_ctx* ctx, const double* u, const double* v, double* out) {
+  CK(launch_div_presync(ctx->g64, ctx->order, ctx->hx * ctx->cfg.radius, ctx->m64, u, v, 0, out, ctx->st), "div");
+  CK(launch_sync_scalar(ctx->g64, ctx->topo, out, ctx->edge64, ctx->st), "sync");
+  return SWM_OK;
+}
+int op_grad(swm_ctx* ctx, const double* f, double* gx, double* gy) {
+  CK(launch_grad_presync(ctx->g64, ctx->order, ctx->ghs, f, gx, gy, ctx->st), "grad");
+  CK(launch_sync_vector(ctx->g64, ctx->topo, ctx->qw, gx, gy, ctx->edge64, ctx->st), "sync");
+  return SWM_OK;
+}
+
+void free_ctx(swm_ctx* c) {
+  if (!c) return;
+  for (swm_state* s : c->states) {
+    if (s->hi) cudaFree(s->hi);
+    if (s->lo) cudaFree(s->lo);
+    s->hi = nullptr; s->lo = nullptr; s->ctx = nullptr;
+  }
+  for (swm_field* f : c->fields) {
+    if (f->p) cudaFree(f->p);
+    f->p = nullptr; f->ctx = nullptr;
+  }
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
+  for (auto& e : c->ev_stage) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& e : c->ev_edge) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
+                  c->tmp, c->hs64, c->hsT, c->partial, c->dres, c->units};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  if (c->hres) cudaFreeHost(c->hres);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+const char* swm_last_error(const swm_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+
+int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const char* grad_op_name,
+                         const char* curl_op_name, const char* coriolis_op_name,
+                         const char* KE_op_name, const char* co2contra_op_name,
+                         const char* massflux_op_name, const char* quadrature_name,
+                         swm_ctx** out) {
+  swm_ctx* ctx = nullptr;
+  if (!cfg || !out) return fail(nullptr, SWM_E_INVALID, "null argument");
+  *out = nullptr;
+  int od = 0, og = 0, oc = 0, oq = 0;
+  if (!div_op_name || !name_order(div_op_name, "divergence_ah", "_sbp", od))
+    return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported div operator: ") + (div_op_name ? div_op_name : "(null)"));
+  if (!grad_op_name || !name_order(grad_op_name, "gradient_ah", "_sbp_ecs", og))
+    return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported grad operator: ") + (grad_op_name ? grad_op_name : "(null)"));
+  if (!curl_op_name || !name_order(curl_op_name, "curl_divergence_ah", "_sbp", oc))
+    return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported curl operator: ") + (curl_op_name ? curl_op_name : "(null)"));
+  if (od == 21 || oc == 21)
+    return fail(nullptr, SWM_E_UNSUPPORTED, "divergence_ah21_sbp does not exist in the operator family");
+  if (od != og || od != oc)
+    return fail(nullptr, SWM_E_UNSUPPORTED, "fused path needs div, grad and curl of one SBP order");
+  auto eq = [](const char* a, const char* b) { return a && std::strcmp(a, b) == 0; };
+  if (!eq(coriolis_op_name, "coriolis_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported coriolis operator");
+  if (!eq(KE_op_name, "KE_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported KE operator");
+  if (!eq(co2contra_op_name, "co2contra_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported co2contra operator");
+  if (!eq(massflux_op_name, "massflux_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported massflux operator");
+  if (!quadrature_name || !name_order(quadrature_name, "SBP_Ah", "_quadrature", oq) || oq == 43)
+    return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported quadrature");
+  if (cfg->N < 16 || cfg->N > 8190) return fail(nullptr, SWM_E_INVALID, "N must be in [16, 8190]");
+  if (cfg->precision != SWM_FP64_PLAIN && cfg->precision != SWM_FP32_FUSED)
+    return fail(nullptr, SWM_E_UNSUPPORTED, "unknown precision");
+  if (!(cfg->radius > 0.0) || !std::isfinite(cfg->grav) || !std::isfinite(cfg->omega))
+    return fail(nullptr, SWM_E_INVALID, "bad physical constants");
+  const double an = std::sqrt(cfg->rotation_axis[0] * cfg->rotation_axis[0] +
+                              cfg->rotation_axis[1] * cfg->rotation_axis[1] +
+                              cfg->rotation_axis[2] * cfg->rotation_axis[2]);
+  if (!(an > 0.0)) return fail(nullptr, SWM_E_INVALID, "rotation axis must be non-zero");
+
+  ctx = new swm_ctx();
+  ctx->cfg = *cfg;
+  ctx->N = cfg->N; ctx->n = cfg->N + 1; ctx->order = od; ctx->prec = cfg->precision;
+  ctx->elt = ctx->prec == SWM_FP32_FUSED ? 4 : 8;
+  // One element pitch for both precisions (a 128-byte multiple for doubles
+  // and a 64-byte multiple for floats) so FP32 and FP64 fields share indexing.
+  ctx->P = (int)round_up(ctx->n, 16);
+  ctx->ps = (long long)ctx->n * ctx->P;
+  ctx->fs = 6 * ctx->ps;
+  ctx->hx = (0.25 * kPi - (-0.25 * kPi)) / (double)ctx->N;
+  ctx->ghs = 1.0 / (ctx->hx * cfg->radius);
+  ctx->g = FieldGeom{ctx->n, ctx->P, ctx->ps, ctx->fs};
+  ctx->g64 = ctx->g;
+  std::string why;
+  if (!build_topology(ctx->topo, why)) { free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why); }
+  std::vector<WorkUnit> units;
+  if (!make_units(kTables[sbp_index(od)], ctx->n, kStageThreads, units, why)) {
+    free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
+  }
+  ctx->nunits = (int)units.size();
+
+  cudaError_t e;
+#define CKC(call, where)                                                              \
+  do {                                                                                \
+    e = (call);                                                                       \
+    if (e != cudaSuccess) {                                                           \
+      std::string m = std::string(where) + ": " + cudaGetErrorString(e);             \
+      free_ctx(ctx);                                                                  \
+      return fail(nullptr, e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA, m); \
+    }                                                                                 \
+  } while (0)
+  CKC(cudaSetDevice(cfg->device), "cudaSetDevice");
+  CKC(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking), "stream");
+  const size_t fbytes = sizeof(double) * ctx->fs;
+  CKC(cudaMalloc(&ctx->m64, NMETRIC * fbytes), "alloc metric");
+  CKC(cudaMemsetAsync(ctx->m64, 0, NMETRIC * fbytes, ctx->st), "memset");
+  CKC(cudaMalloc(&ctx->qw, sizeof(double) * 4 * ctx->n), "alloc");
+  CKC(cudaMalloc(&ctx->Aw, sizeof(double) * ctx->n), "alloc");
+  CKC(cudaMalloc(&ctx->edge64, sizeof(double) * 16 * 6 * ctx->n), "alloc");
+  CKC(cudaMalloc(&ctx->edge, (size_t)ctx->elt * 16 * 6 * ctx->n), "alloc");
+  CKC(cudaMalloc(&ctx->ya, (size_t)ctx->elt * 3 * ctx->fs), "alloc");
+  CKC(cudaMalloc(&ctx->yb, (size_t)ctx->elt * 3 * ctx->fs), "alloc");
+  CKC(cudaMalloc(&ctx->acc, (size_t)ctx->elt * 3 * ctx->fs), "alloc");
+  CKC(cudaMemsetAsync(ctx->ya, 0, (size_t)ctx->elt * 3 * ctx->fs, ctx->st), "memset");
+  CKC(cudaMemsetAsync(ctx->yb, 0, (size_t)ctx->elt * 3 * ctx->fs, ctx->st), "memset");
+  CKC(cudaMemsetAsync(ctx->acc, 0, (size_t)ctx->elt * 3 * ctx->fs, ctx->st), "memset");
+  CKC(cudaMalloc(&ctx->tmp, 14 * fbytes), "alloc work fields");
+  CKC(cudaMemsetAsync(ctx->tmp, 0, 14 * fbytes, ctx->st), "memset");
+  CKC(cudaMalloc(&ctx->partial, sizeof(double) * REDUCE_BLOCKS), "alloc");
+  CKC(cudaMalloc(&ctx->dres, sizeof(double) * 16), "alloc");
+  CKC(cudaMallocHost(&ctx->hres, sizeof(double) * 16), "alloc host");
+  CKC(cudaMalloc(&ctx->units, sizeof(WorkUnit) * units.size()), "alloc");
+  CKC(cudaMemcpyAsync(ctx->units, units.data(), sizeof(WorkUnit) * units.size(), cudaMemcpyHostToDevice, ctx->st), "copy");
+  CKC(launch_geometry(ctx->g64, ctx->N, cfg->radius, cfg->omega, cfg->rotation_axis, ctx->m64, ctx->qw, ctx->st), "geometry");
+  CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od) : prepare_stage<double>(od), "stage kernel attributes");
+  if (ctx->prec == SWM_FP32_FUSED) {
+    CKC(cudaMalloc(&ctx->m32, sizeof(float) * NMETRIC * ctx->fs), "alloc");
+    CKC(launch_to_f32(ctx->m64, ctx->m32, NMETRIC * ctx->fs, ctx->st), "metric to f32");
+  }
+  // SBP quadrature weights (quadrature_factory_mod.f90:158-177)
+  {
+    const SbpC& q = kTables[sbp_index(oq)];
+    std::vector<double> A(ctx->n, 1.0);
+    for (int i = 0; i < std::min(q.nA, ctx->n); ++i) A[i] = q.A[i];
+    for (int i = std::max(ctx->n - q.nA, 0); i < ctx->n; ++i) A[i] = q.A[ctx->n - 1 - i];
+    CKC(cudaMemcpy(ctx->Aw, A.data(), sizeof(double) * ctx->n, cudaMemcpyHostToDevice), "copy");
+  }
+  CKC(cudaStreamSynchronize(ctx->st), "sync");
+#undef CKC
+  *out = ctx;
+  return SWM_OK;
+}
+
+int swm_ctx_create(const swm_config* cfg, swm_ctx** out) {
+  if (!cfg) return fail(nullptr, SWM_E_INVALID, "null config");
+  const int o = cfg->sbp_order;
+  if (o != 42 && o != 43 && o != 63)
+    return fail(nullptr, SWM_E_UNSUPPORTED, "sbp_order must be 42, 43 or 63 for the model operator");
+  char dn[64], gn[64], cn[64], qn[64];
+  std::snprintf(dn, sizeof dn, "divergence_ah%d_sbp", o);
+  std::snprintf(gn, sizeof gn, "gradient_ah%d_sbp_ecs", o);
+  std::snprintf(cn, sizeof cn, "curl_divergence_ah%d_sbp", o);
+  std::snprintf(qn, sizeof qn, "SBP_Ah%d_quadrature", o == 43 ? 42 : o);
+  return swm_ctx_create_named(cfg, dn, gn, cn, "coriolis_colocated", "KE_colocated",
+                              "co2contra_colocated", "massflux_colocated", qn, out);
+}
+
+void swm_ctx_destroy(swm_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->cfg.device);
+  cudaStreamSynchronize(ctx->st);
+  free_ctx(ctx);
+}
+
+int swm_ctx_synchronize(swm_ctx* ctx) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  CK(cudaStreamSynchronize(ctx->st), "synchronize");
+  return SWM_OK;
+}
+
+void* swm_ctx_stream(swm_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
+size_t swm_ctx_npts(const swm_ctx* ctx) { return ctx ? (size_t)6 * ctx->n * ctx->n : 0; }
+
+int swm_set_orography(swm_ctx* ctx, const double* hs) {
+  if (!ctx || !hs) return fail(ctx, SWM_E_INVALID, "null argument");
+  cudaSetDevice(ctx->cfg.device);
+  if (!ctx->hs64) {
+    CK(cudaMalloc(&ctx->hs64, sizeof(double) * ctx->fs), "alloc");
+    CK(cudaMemsetAsync(ctx->hs64, 0, sizeof(double) * ctx->fs, ctx->st), "memset");
+  }
+  CK(cudaMemcpy2DAsync(ctx->hs64, sizeof(double) * ctx->P, hs, sizeof(double) * ctx->n,
+                       sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyHostToDevice, ctx->st), "upload");
+  if (ctx->prec == SWM_FP32_FUSED) {
+    if (!ctx->hsT) CK(cudaMalloc(&ctx->hsT, sizeof(float) * ctx->fs), "alloc");
+    CK(launch_to_f32(ctx->hs64, (float*)ctx->hsT, ctx->fs, ctx->st), "to f32");
+  } else {
+    ctx->hsT = nullptr;  // FP64 uses hs64 directly
+  }
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+  ctx->graphs.clear();
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  if (ctx->prec == SWM_FP64_PLAIN) ctx->hsT = ctx->hs64;
+  return SWM_OK;
+}
+
+// ---------------------------------------------------------------- states
+int swm_state_create(swm_ctx* ctx, swm_state** out) {
+  if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
+  cudaSetDevice(ctx->cfg.device);
+  swm_state* s = new swm_state{ctx, nullptr, nullptr};
+  const size_t b = (size_t)ctx->elt * 3 * ctx->fs;
+  cudaError_t e = cudaMalloc(&s->hi, b);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->hi, 0, b, ctx->st);
+  if (e == cudaSuccess && ctx->prec == SWM_FP32_FUSED) {
+    e = cudaMalloc((void**)&s->lo, sizeof(float) * 3 * ctx->fs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->lo, 0, sizeof(float) * 3 * ctx->fs, ctx->st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  if (e != cudaSuccess) {
+    if (s->hi) cudaFree(s->hi);
+    if (s->lo) cudaFree(s->lo);
+    delete s;
+    return fail(ctx, e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
+                std::string("state alloc: ") + cudaGetErrorString(e));
+  }
+  ctx->states.insert(s);
+  *out = s;
+  return SWM_OK;
+}
+
+int swm_state_create_similar(swm_ctx* ctx, const swm_state* src, swm_state** out) {
+  if (int rc = check_state(ctx, src)) return rc;
+  return swm_state_create(ctx, out);
+}
+
+void swm_state_free(swm_state* s) {
+  if (!s) return;
+  swm_ctx* c = s->ctx;
+  if (c) {  // a state whose context is gone was already released
+    cudaSetDevice(c->cfg.device);
+    cudaStreamSynchronize(c->st);
+    for (auto it = c->graphs.begin(); it != c->graphs.end();) {
+      if (it->first.first == (void*)s) { cudaGraphExecDestroy(it->second.exec); it = c->graphs.erase(it); }
+      else ++it;
+    }
+    if (s->hi) cudaFree(s->hi);
+    if (s->lo) cudaFree(s->lo);
+    c->states.erase(s);
+  }
+  delete s;
+}
+
+int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* u, const double* v) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
+  cudaSetDevice(ctx->cfg.device);
+  const double* src[3] = {h, u, v};
+  for (int c = 0; c < 3; ++c) {
+    double* dst = ctx->prec == SWM_FP64_PLAIN ? (double*)s->hi + c * ctx->fs : tmpf(ctx, 11 + c);
+    CK(cudaMemcpy2DAsync(dst, sizeof(double) * ctx->P, src[c], sizeof(double) * ctx->n,
+                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyHostToDevice, ctx->st), "upload");
+    if (ctx->prec == SWM_FP32_FUSED)
+      CK(launch_split_f64(ctx->fs, dst, (float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs, ctx->st), "split");
+  }
+  return SWM_OK;
+}
+
+int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
+  cudaSetDevice(ctx->cfg.device);
+  double* dst[3] = {h, u, v};
+  const double *dh, *du, *dv;
+  if (int rc = state64(ctx, s, &dh, &du, &dv)) return rc;
+  const double* src[3] = {dh, du, dv};
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpy2DAsync(dst[c], sizeof(double) * ctx->n, src[c], sizeof(double) * ctx->P,
+                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToHost, ctx->st), "download");
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  return SWM_OK;
+}
+
+static int combine(swm_ctx* ctx, swm_state* s, double s1, const swm_state* a, double s2,
+                   const swm_state* b, bool update) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (a && check_state(ctx, a)) return SWM_E_INVALID;
+  if (b && check_state(ctx, b)) return SWM_E_INVALID;
+  cudaSetDevice(ctx->cfg.device);
+  const long long cnt = 3 * ctx->fs;
+  if (ctx->prec == SWM_FP64_PLAIN) {
+    double* o = (double*)s->hi;
+    if (update) {
+      // this = this + s1*a (+ s2*b), evaluated as (this + s1*a) + s2*b
+      CK(launch_axpby(cnt, 1.0, o, s1, (const double*)a->hi, o, ctx->st), "update");
+      if (b) CK(launch_axpby(cnt, 1.0, o, s2, (const double*)b->hi, o, ctx->st), "update");
+    } else if (!a) {
+      CK(launch_fill(cnt, s1, o, ctx->st), "assign");
+    } else {
+      CK(launch_axpby(cnt, s1, (const double*)a->hi, s2, b ? (const double*)b->hi : nullptr, o, ctx->st), "assign");
+    }
+  } else {
+    float* ohi = (float*)s->hi;
+    float* olo = s->lo;
+    if (update) {
+      CK(launch_axpby_f32pair(cnt, 1.0, ohi, olo, s1, (const float*)a->hi, a->lo, ohi, olo, ctx->st), "update");
+      if (b) CK(launch_axpby_f32pair(cnt, 1.0, ohi, olo, s2, (const float*)b->hi, b->lo, ohi, olo, ctx->st), "update");
+    } else if (!a) {
+      double* d = tmpf(ctx, 11);  // 3 work fields = 3*fs doubles
+      CK(launch_fill(cnt, s1, d, ctx->st), "fill");
+      CK(launch_split_f64(cnt, d, ohi, olo, ctx->st), "split");
+    } else {
+      CK(launch_axpby_f32pair(cnt, s1, (const float*)a->hi, a->lo, s2,
+                              b ? (const float*)b->hi : nullptr, b ? b->lo : nullptr, ohi, olo, ctx->st), "assign");
+    }
+  }
+  return SWM_OK;
+}
+
+int swm_assign_s1(swm_ctx* ctx, swm_state* s, double s1) { return combine(ctx, s, s1, nullptr, 0.0, nullptr, false); }
+int swm_assign_s1v1(swm_ctx* ctx, swm_state* s, double s1, const swm_state* v1) {
+  if (!v1) return fail(ctx, SWM_E_INVALID, "null state");
+  return combine(ctx, s, s1, v1, 0.0, nullptr, false);
+}
+int swm_assign_s1v1s2v2(swm_ctx* ctx, swm_state* s, double s1, const swm_state* v1, double s2, const swm_state* v2) {
+  if (!v1 || !v2) return fail(ctx, SWM_E_INVALID, "null state");
+  return combine(ctx, s, s1, v1, s2, v2, false);
+}
+int swm_update_s1v1(swm_ctx* ctx, swm_state* s, double s1, const swm_state* v1) {
+  if (!v1) return fail(ctx, SWM_E_INVALID, "null state");
+  return combine(ctx, s, s1, v1, 0.0, nullptr, true);
+}
+int swm_update_s1v1s2v2(swm_ctx* ctx, swm_state* s, double s1, const swm_state* v1, double s2, const swm_state* v2) {
+  if (!v1 || !v2) return fail(ctx, SWM_E_INVALID, "null state");
+  return combine(ctx, s, s1, v1, s2, v2, true);
+}
+
+int swm_dot(swm_ctx* ctx, const swm_state* a, const swm_state* b, double* out) {
+  if (int rc = check_state(ctx, a)) return rc;
+  if (int rc = check_state(ctx, b)) return rc;
+  if (!out) return fail(ctx, SWM_E_INVALID, "null output");
+  cudaSetDevice(ctx->cfg.device);
+  const double *ah, *au, *av, *bh, *bu, *bv;
+  if (ctx->prec == SWM_FP32_FUSED) {
+    // join a into 11..13 and b into 8..10
+    if (int rc = state64(ctx, a, &ah, &au, &av)) return rc;
+    double* d = tmpf(ctx, 8);
+    for (int c = 0; c < 3; ++c)
+      CK(launch_join_f32pair(ctx->fs, (const float*)b->hi + c * ctx->fs, b->lo + c * ctx->fs, d + c * ctx->fs, ctx->st), "join");
+    bh = d; bu = d + ctx->fs; bv = d + 2 * ctx->fs;
+  } else {
+    if (int rc = state64(ctx, a, &ah, &au, &av)) return rc;
+    if (int rc = state64(ctx, b, &bh, &bu, &bv)) return rc;
+  }
+  if (int rc = reduce(ctx, 0, ah, bh, 0)) return rc;
+  if (int rc = reduce(ctx, 0, au, bu, 1)) return rc;
+  if (int rc = reduce(ctx, 0, av, bv, 2)) return rc;
+  double r[3];
+  if (int rc = fetch_results(ctx, 3, r)) return rc;
+  *out = r[0] + r[1] + r[2];
+  return SWM_OK;
+}
+
+int swm_norm2(swm_ctx* ctx, const swm_state* a, double* out) {
+  double d;
+  if (int rc = swm_dot(ctx, a, a, &d)) return rc;
+  *out = std::sqrt(d);
+  return SWM_OK;
+}
+
+// ------------------------------------------------------------- operator
+int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  if (int rc = check_state(ctx, vout)) return rc;
+  if (int rc = check_state(ctx, vin)) return rc;
+  if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->prec == SWM_FP64_PLAIN) {
+    InstDev<double> I = base_inst<double>(ctx);
+    I.in = (const double*)vin->hi; I.out = (double*)vout->hi;
+    return run_stage<double>(ctx, I, MODE_APPLY);
+  }
+  InstDev<float> I = base_inst<float>(ctx);
+  I.in = (const float*)vin->hi; I.out = (float*)vout->hi;
+  CK(cudaMemsetAsync(vout->lo, 0, sizeof(float) * 3 * ctx->fs, ctx->st), "memset");
+  return run_stage<float>(ctx, I, MODE_APPLY);
+}
+
+int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  if (int rc = check_state(ctx, vout)) return rc;
+  if (int rc = check_state(ctx, vin)) return rc;
+  if (ctx->prec != SWM_FP64_PLAIN) return fail(ctx, SWM_E_UNSUPPORTED, "unfused apply is FP64 only");
+  cudaSetDevice(ctx->cfg.device);
+  const long long fs = ctx->fs;
+  const double* h = (const double*)vin->hi;
+  const double* u = h + fs;
+  const double* v = h + 2 * fs;
+  double* oh = (double*)vout->hi;
+  double* ou = oh + fs;
+  double* ov = oh + 2 * fs;
+  double *ut = tmpf(ctx, 0), *vt = tmpf(ctx, 1), *hu = tmpf(ctx, 2), *hv = tmpf(ctx, 3),
+         *ke = tmpf(ctx, 4), *gx = tmpf(ctx, 5), *gy = tmpf(ctx, 6), *cu = tmpf(ctx, 7),
+         *cor_u = tmpf(ctx, 8), *cor_v = tmpf(ctx, 9), *dv = tmpf(ctx, 10);
+  const FieldGeom& g = ctx->g64;
+  cudaStream_t st = ctx->st;
+  CK(launch_co2contra(g, ctx->m64, u, v, ut, vt, st), "co2contra");
+  CK(launch_massflux(g, h, ut, vt, hu, hv, st), "massflux");
+  CK(launch_ke(g, u, v, ut, vt, ke, st), "KE");
+  CK(launch_ke_update(g, ctx->cfg.grav, h, ctx->hs64, ke, st), "KE update");
+  if (int rc = op_grad(ctx, ke, gx, gy)) return rc;
+  if (int rc = op_curl(ctx, u, v, cu)) return rc;
+  CK(launch_coriolis(g, ctx->m64, hu, hv, h, cu, cor_u, cor_v, st), "coriolis");
+  CK(launch_axpby(fs, -1.0, gx, 1.0, cor_u, ou, st), "assign");
+  CK(launch_axpby(fs, -1.0, gy, 1.0, cor_v, ov, st), "assign");
+  if (int rc = op_div(ctx, hu, hv, dv)) return rc;
+  CK(launch_axpby(fs, -1.0, dv, 0.0, nullptr, oh, st), "assign");
+  return SWM_OK;
+}
+
+int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  if (int rc = check_state(ctx, v0)) return rc;
+  if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
+  if (nsteps == 0) return SWM_OK;
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->timing) {
+    for (int k = 0; k < nsteps; ++k) {
+      int rc = ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);
+      if (rc) return rc;
+    }
+    return SWM_OK;
+  }
+  const auto key = std::make_pair((void*)v0, dt);
+  auto it = ctx->graphs.find(key);
+  if (it == ctx->graphs.end()) {
+    if (ctx->graphs.size() >= 8) {
+      auto old = ctx->graphs.begin();
+      for (auto jt = ctx->graphs.begin(); jt != ctx->graphs.end(); ++jt)
+        if (jt->second.use < old->second.use) old = jt;
+      cudaGraphExecDestroy(old->second.exec);
+      ctx->graphs.erase(old);
+    }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int rc = ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);
+    cudaError_t ec = cudaStreamEndCapture(ctx->st, &graph);
+    if (rc) { if (ec == cudaSuccess) cudaGraphDestroy(graph); return rc; }
+    CK(ec, "end capture");
+    GraphEntry ge{};
+    cudaError_t ei = cudaGraphInstantiate(&ge.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei, "graph instantiate");
+    it = ctx->graphs.emplace(key, ge).first;
+  }
+  it->second.use = ++ctx->graph_clock;
+  for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(it->second.exec, ctx->st), "graph launch");
+  return SWM_OK;
+}
+
+int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!out) return fail(ctx, SWM_E_INVALID, "null output");
+  cudaSetDevice(ctx->cfg.device);
+  const double *h, *u, *v;
+  if (int rc = state64(ctx, s, &h, &u, &v)) return rc;
+  double* z = tmpf(ctx, 0);
+  double *ku = tmpf(ctx, 1), *kv = tmpf(ctx, 2), *pe = tmpf(ctx, 3), *en = tmpf(ctx, 4);
+  if (int rc = op_curl(ctx, u, v, z)) return rc;
+  CK(launch_diag_integrands(ctx->g64, ctx->m64, ctx->cfg.grav, h, u, v, ctx->hs64, z, ku, kv, pe, en, ctx->st), "diag");
+  if (int rc = reduce(ctx, 2, h, nullptr, 0)) return rc;
+  if (int rc = reduce(ctx, 3, h, nullptr, 1)) return rc;
+  if (int rc = reduce(ctx, 1, h, nullptr, 2)) return rc;
+  if (int rc = reduce(ctx, 1, ku, nullptr, 3)) return rc;
+  if (int rc = reduce(ctx, 1, kv, nullptr, 4)) return rc;
+  if (int rc = reduce(ctx, 1, pe, nullptr, 5)) return rc;
+  if (int rc = reduce(ctx, 1, en, nullptr, 6)) return rc;
+  double r[7];
+  if (int rc = fetch_results(ctx, 7, r)) return rc;
+  const double ke = r[3] + r[4];
+  out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+  out[3] = ke + r[5]; out[4] = ke; out[5] = r[5]; out[6] = r[6];
+  return SWM_OK;
+}
+
+// ---------------------------------------------------------------- fields
+int swm_field_create(swm_ctx* ctx, swm_field** out) {
+  if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
+  cudaSetDevice(ctx->cfg.device);
+  swm_field* f = new swm_field{ctx, nullptr};
+  cudaError_t e = cudaMalloc(&f->p, sizeof(double) * ctx->fs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(f->p, 0, sizeof(double) * ctx->fs, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  if (e != cudaSuccess) {
+    if (f->p) cudaFree(f->p);
+    delete f;
+    return fail(ctx, SWM_E_NOMEM, std::string("field alloc: ") + cudaGetErrorString(e));
+  }
+  ctx->fields.insert(f);
+  *out = f;
+  return SWM_OK;
+}
+
+void swm_field_free(swm_field* f) {
+  if (!f) return;
+  if (swm_ctx* c = f->ctx) {
+    cudaSetDevice(c->cfg.device);
+    cudaStreamSynchronize(c->st);
+    if (f->p) cudaFree(f->p);
+    c->fields.erase(f);
+  }
+  delete f;
+}
+
+int swm_field_upload(swm_ctx* ctx, swm_field* f, const double* host) {
+  if (int rc = check_field(ctx, f)) return rc;
+  if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
+  cudaSetDevice(ctx->cfg.device);
+  CK(cudaMemcpy2DAsync(f->p, sizeof(double) * ctx->P, host, sizeof(double) * ctx->n, sizeof(double) * ctx->n,
+                       (size_t)6 * ctx->n, cudaMemcpyHostToDevice, ctx->st), "upload");
+  return SWM_OK;
+}
+
+int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
+  if (int rc = check_field(ctx, f)) return rc;
+  if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
+  cudaSetDevice(ctx->cfg.device);
+  CK(cudaMemcpy2DAsync(host, sizeof(double) * ctx->n, f->p, sizeof(double) * ctx->P, sizeof(double) * ctx->n,
+                       (size_t)6 * ctx->n, cudaMemcpyDeviceToHost, ctx->st), "download");
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  return SWM_OK;
+}
+
+#define CHECK_FIELDS(...)                                       \
+  do {                                                          \
+    const swm_field* fl_[] = {__VA_ARGS__};                     \
+    for (const swm_field* f_ : fl_)                             \
+      if (int rc_ = check_field(ctx, f_)) return rc_;           \
+    cudaSetDevice(ctx->cfg.device);                             \
+  } while (0)
+
+int swm_op_co2contra(swm_ctx* ctx, swm_field* ut, swm_field* vt, const swm_field* u, const swm_field* v) {
+  CHECK_FIELDS(ut, vt, u, v);
+  CK(launch_co2contra(ctx->g64, ctx->m64, u->p, v->p, ut->p, vt->p, ctx->st), "co2contra");
+  return SWM_OK;
+}
+int swm_op_massflux(swm_ctx* ctx, swm_field* hu, swm_field* hv, const swm_field* h, const swm_field* ut, const swm_field* vt) {
+  CHECK_FIELDS(hu, hv, h, ut, vt);
+  CK(launch_massflux(ctx->g64, h->p, ut->p, vt->p, hu->p, hv->p, ctx->st), "massflux");
+  return SWM_OK;
+}
+int swm_op_ke(swm_ctx* ctx, swm_field* ke, const swm_field* u, const swm_field* v, const swm_field* ut, const swm_field* vt) {
+  CHECK_FIELDS(ke, u, v, ut, vt);
+  CK(launch_ke(ctx->g64, u->p, v->p, ut->p, vt->p, ke->p, ctx->st), "KE");
+  return SWM_OK;
+}
+int swm_op_grad(swm_ctx* ctx, swm_field* gx, swm_field* gy, const swm_field* f) {
+  CHECK_FIELDS(gx, gy, f);
+  return op_grad(ctx, f->p, gx->p, gy->p);
+}
+int swm_op_div(swm_ctx* ctx, swm_field* div, const swm_field* u, const swm_field* v) {
+  CHECK_FIELDS(div, u, v);
+  return op_div(ctx, u->p, v->p, div->p);
+}
+int swm_op_curl(swm_ctx* ctx, swm_field* curl, const swm_field* u, const swm_field* v) {
+  CHECK_FIELDS(curl, u, v);
+  return op_curl(ctx, u->p, v->p, curl->p);
+}
+int swm_op_coriolis(swm_ctx* ctx, swm_field* cor_u, swm_field* cor_v, const swm_field* hu, const swm_field* hv,
+                    const swm_field* h, const swm_field* curl) {
+  CHECK_FIELDS(cor_u, cor_v, hu, hv, h, curl);
+  CK(launch_coriolis(ctx->g64, ctx->m64, hu->p, hv->p, h->p, curl->p, cor_u->p, cor_v->p, ctx->st), "coriolis");
+  return SWM_OK;
+}
+int swm_sync_scalar(swm_ctx* ctx, swm_field* f) {
+  CHECK_FIELDS(f);
+  CK(launch_sync_scalar(ctx->g64, ctx->topo, f->p, ctx->edge64, ctx->st), "sync");
+  return SWM_OK;
+}
+int swm_sync_vector_cov(swm_ctx* ctx, swm_field* gx, swm_field* gy) {
+  CHECK_FIELDS(gx, gy);
+  CK(launch_sync_vector(ctx->g64, ctx->topo, ctx->qw, gx->p, gy->p, ctx->edge64, ctx->st), "sync");
+  return SWM_OK;
+}
+int swm_quadrature_mass(swm_ctx* ctx, const swm_field* f, double* out) {
+  CHECK_FIELDS(f);
+  if (!out) return fail(ctx, SWM_E_INVALID, "null output");
+  if (int rc = reduce(ctx, 1, f->p, nullptr, 0)) return rc;
+  return fetch_results(ctx, 1, out);
+}
+
+// ---------------------------------------------------------------- timing
+int swm_timing_enable(swm_ctx* ctx, int on) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  ctx->timing = on != 0;
+  return SWM_OK;
+}
+
+int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches, double* edge_ms, long* edge_launches) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  double ts = 0.0, te = 0.0;
+  for (auto& e : ctx->ev_stage) { float ms; CK(cudaEventElapsedTime(&ms, e.first, e.second), "elapsed"); ts += ms; }
+  for (auto& e : ctx->ev_edge) { float ms; CK(cudaEventElapsedTime(&ms, e.first, e.second), "elapsed"); te += ms; }
+  if (stage_ms) *stage_ms = ts;
+  if (stage_launches) *stage_launches = (long)ctx->ev_stage.size();
+  if (edge_ms) *edge_ms = te;
+  if (edge_launches) *edge_launches = (long)ctx->ev_edge.size();
+  for (auto& e : ctx->ev_stage) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& e : ctx->ev_edge) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  ctx->ev_stage.clear();
+  ctx->ev_edge.clear();
+  return SWM_OK;
+}
+
+}  // extern "C"

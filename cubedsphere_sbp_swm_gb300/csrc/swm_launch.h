@@ -1,0 +1,24 @@
+// swm_launch.h -- host launchers of the fused stage and cube-edge kernels,
+// one instantiation per precision (swm_stage_f64.cu / swm_stage_f32.cu).
+#pragma once
+
+#include "swm_device.cuh"
+
+namespace swm {
+
+// Fused stage kernel over nunits work units (one CTA each).
+template <class T>
+cudaError_t launch_stage(int order, const InstDev<T>& one, const InstDev<T>* many,
+                         const WorkUnit* units, int nunits, int mode, cudaStream_t st);
+// Sets the launch attributes of the stage kernel of one SBP order; called at
+// context creation, outside any stream capture.
+template <class T>
+cudaError_t prepare_stage(int order);
+// Cube-edge kernel over ninst instances whose largest edge has max_n nodes.
+template <class T>
+cudaError_t launch_edge(const InstDev<T>& one, const InstDev<T>* many, int ninst, int max_n,
+                        const Topology& tp, int mode, cudaStream_t st);
+
+constexpr int kStageThreads = 128;
+
+}  // namespace swm

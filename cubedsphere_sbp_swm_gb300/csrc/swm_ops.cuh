@@ -1,0 +1,82 @@
+// swm_ops.cuh -- host-callable launchers of the per-operator (unfused) FP64
+// kernels, the FP64 geometry precompute, state linear combinations and the
+// deterministic FP64 reductions.  Implemented in swm_ops.cu.
+#pragma once
+
+#include "swm_device.cuh"
+
+namespace swm {
+
+struct FieldGeom {
+  int n, P;
+  long long ps, fs;   // panel stride, field stride (elements)
+};
+
+// Geometry (FP64): metric fields J, Qi1, Qi2, Qi3, f, rJ into m64 (NMETRIC
+// fields of fs doubles) and sync weights qb|qt|ql|qr into qw (4n doubles).
+cudaError_t launch_geometry(const FieldGeom& g, int N, double radius, double omega,
+                            const double axis[3], double* m64, double* qw, cudaStream_t st);
+// FP64 -> FP32 copy of nfields fields
+cudaError_t launch_to_f32(const double* src, float* dst, long long count, cudaStream_t st);
+
+// Per-operator FP64 kernels on (pitched) fields.
+cudaError_t launch_co2contra(const FieldGeom& g, const double* m64, const double* u,
+                             const double* v, double* ut, double* vt, cudaStream_t st);
+cudaError_t launch_massflux(const FieldGeom& g, const double* h, const double* ut,
+                            const double* vt, double* hu, double* hv, cudaStream_t st);
+cudaError_t launch_ke(const FieldGeom& g, const double* u, const double* v, const double* ut,
+                      const double* vt, double* ke, cudaStream_t st);
+// ke += grav*h + grav*hs (hs nullable)
+cudaError_t launch_ke_update(const FieldGeom& g, double grav, const double* h, const double* hs,
+                             double* ke, cudaStream_t st);
+// pre-sync SBP gradient: gx = Dx f / (hx a), gy = Dy f / (hx a)
+cudaError_t launch_grad_presync(const FieldGeom& g, int order, double ghs, const double* f,
+                                double* gx, double* gy, cudaStream_t st);
+// pre-sync SBP divergence (Dx(J u) + Dy(J v)) / (J hx a); curl_form: the
+// input is covariant and the operator uses (v/J, -u/J).
+cudaError_t launch_div_presync(const FieldGeom& g, int order, double hx_a, const double* m64,
+                               const double* u, const double* v, int curl_form, double* out,
+                               cudaStream_t st);
+cudaError_t launch_coriolis(const FieldGeom& g, const double* m64, const double* hu,
+                            const double* hv, const double* h, const double* curl,
+                            double* cor_u, double* cor_v, cudaStream_t st);
+// out[k] = value for k < count
+cudaError_t launch_fill(long long count, double value, double* out, cudaStream_t st);
+// out = s1*a + s2*b over count elements (b nullable)
+cudaError_t launch_axpby(long long count, double s1, const double* a, double s2, const double* b,
+                         double* out, cudaStream_t st);
+// Cube-edge syncs of pitched FP64 fields: gather the boundary values into
+// the edge buffer, then apply the reference's averaging.
+cudaError_t launch_sync_scalar(const FieldGeom& g, const Topology& tp, double* f, double* edge,
+                               cudaStream_t st);
+cudaError_t launch_sync_vector(const FieldGeom& g, const Topology& tp, const double* qw,
+                               double* gx, double* gy, double* edge, cudaStream_t st);
+
+// Deterministic FP64 reductions over the valid nodes of a field.
+// kind: 0 sum(a*b), 1 SBP mass sum(a*J*hx^2*Ax*Ay), 2 min(a), 3 max(a),
+//       4 SBP mass of a*b.
+cudaError_t launch_reduce(const FieldGeom& g, int kind, const double* a, const double* b,
+                          const double* J, const double* Aw, double hx2, double* partial,
+                          int nblocks, double* result, cudaStream_t st);
+constexpr int REDUCE_BLOCKS = 264;
+
+// Per-node integrands of the SWM diagnostics (operator_swm_mod.f90:211-260):
+// ke_u = 0.5*(h*ut)*u, ke_v = 0.5*(h*vt)*v, pe = 0.5*g*(h+hs)^2,
+// ens = 0.5*(zeta+f)^2/h.
+cudaError_t launch_diag_integrands(const FieldGeom& g, const double* m64, double grav,
+                                   const double* h, const double* u, const double* v,
+                                   const double* hs, const double* zeta, double* ke_u,
+                                   double* ke_v, double* pe, double* ens, cudaStream_t st);
+
+// State combinations for the FP32 compensated representation: out = s1*(a_hi
+// + a_lo) + s2*(b_hi + b_lo) evaluated in FP64 and split into (hi, lo).
+cudaError_t launch_axpby_f32pair(long long count, double s1, const float* ahi, const float* alo,
+                                 double s2, const float* bhi, const float* blo, float* ohi,
+                                 float* olo, cudaStream_t st);
+// FP64 <-> (hi, lo) FP32 pair conversions
+cudaError_t launch_split_f64(long long count, const double* src, float* hi, float* lo,
+                             cudaStream_t st);
+cudaError_t launch_join_f32pair(long long count, const float* hi, const float* lo, double* dst,
+                                cudaStream_t st);
+
+}  // namespace swm

@@ -1,0 +1,411 @@
+// swm_stage.cuh -- fused vector-invariant RHS + RK4 stage epilogue, and the
+// cube-edge pass that finishes the panel-boundary nodes.
+//
+// One RK stage is two launches:
+//   stage_kernel  every node: co2contra, mass flux, KE, SBP grad(KE),
+//                 curl = div(v/J, -u/J) and div(h u) with their one-sided
+//                 boundary closures; interior nodes then get Coriolis, the
+//                 tendency and the RK stage combination; panel-boundary nodes
+//                 write their pre-sync (gx, gy, zeta, div) to the edge buffer.
+//   edge_kernel   every panel-boundary node: the reference's cube-edge syncs
+//                 (2-way average on edges, 3-way at cube corners, metric-
+//                 weighted for the covariant gradient), then the same
+//                 Coriolis / tendency / RK epilogue.
+// Reference: operator_swm_mod.f90:61-113, rk4_mod.f90:20-42,
+// sbp_operator_mod.f90:152-228, div_ah_sbp_mod.f90:46-96,
+// grad_ah_sbp_mod.f90:51-88, curl_div_based_mod.f90:26-66,
+// coriolis_colocated_mod.f90:79-103, halo_Ah_scalar_sync_mod.f90:38-93,
+// ecs_Ah_vec_sync_mod.f90:62-125.
+#pragma once
+
+#include "swm_device.cuh"
+
+namespace swm {
+
+template <int ORD> struct Ord;
+template <> struct Ord<21> { static constexpr int idx = 0, NE = 1, NW = 2, H = 1, RMAX = 1; };
+template <> struct Ord<42> { static constexpr int idx = 1, NE = 4, NW = 6, H = 2, RMAX = 3; };
+template <> struct Ord<43> { static constexpr int idx = 2, NE = 4, NW = 6, H = 2, RMAX = 5; };
+template <> struct Ord<63> { static constexpr int idx = 3, NE = 6, NW = 9, H = 3, RMAX = 5; };
+
+constexpr int STAGE_BW = 128;   // threads per CTA = max columns a unit reads
+enum { RF_KE = 0, RF_U, RF_V, RF_GU, RF_GV, RF_UT, RF_VT, RF_J, RF_N };
+
+// Interior central difference with the antisymmetric coefficients of the
+// order's interior stencil; fm(o) returns the value at offset o.
+template <int ORD, class T, class F>
+__device__ __forceinline__ T d_interior(F fm) {
+  if constexpr (Ord<ORD>::H == 1) {
+    return T(0.5) * (fm(1) - fm(-1));
+  } else if constexpr (Ord<ORD>::H == 2) {
+    return T(2.0 / 3.0) * (fm(1) - fm(-1)) + T(-1.0 / 12.0) * (fm(2) - fm(-2));
+  } else {
+    return T(3.0 / 4.0) * (fm(1) - fm(-1)) + T(-3.0 / 20.0) * (fm(2) - fm(-2)) +
+           T(1.0 / 60.0) * (fm(3) - fm(-3));
+  }
+}
+
+// SBP derivative at line index k of a line of n nodes; fa(m) returns the value
+// at absolute line index m.
+template <int ORD, class T, class FA>
+__device__ __forceinline__ T d_line(int k, int n, FA fa) {
+  constexpr int NE = Ord<ORD>::NE, NW = Ord<ORD>::NW, ID = Ord<ORD>::idx;
+  if (k < NE) {
+    T acc = T(0);
+    const int last = c_sbp[ID].last[k];
+#pragma unroll
+    for (int m = 0; m < NW; ++m)
+      if (m < last) acc += T(c_sbp[ID].Ql[k * MAXNW + m]) * fa(m);
+    return acc;
+  } else if (k >= n - NE) {
+    const int r = n - 1 - k;
+    const int last = c_sbp[ID].last[r];
+    T acc = T(0);
+#pragma unroll
+    for (int m = NW - 1; m >= 0; --m)
+      if (m < last) acc += T(-c_sbp[ID].Ql[r * MAXNW + m]) * fa(n - 1 - m);
+    return acc;
+  }
+  return d_interior<ORD, T>([&](int o) { return fa(k + o); });
+}
+
+// Tendency at one node from its (synced) derivative terms and the RK stage
+// epilogue.  kk = (k_h, k_u, k_v).
+template <class T>
+__device__ __forceinline__ void stage_epilogue(const InstDev<T>& I, int mode, long long idx,
+                                               T kh, T ku, T kv) {
+  const long long fs = I.fs;
+  const T kk[3] = {kh, ku, kv};
+  if (mode == MODE_APPLY) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) I.out[c * fs + idx] = kk[c];
+    return;
+  }
+  if constexpr (sizeof(T) == 8) {
+    // FP64: the reference's order.  y = 1*v0 + c*k; w = v0 + dt/6 k1,
+    // w += dt/3 k2, w += dt/3 k3, v0 = w + dt/6 k4 (rk4_mod.f90:28-40).
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long o = c * fs + idx;
+      if (mode == MODE_RK1) {
+        const T b = I.base[o];
+        I.out[o] = T(1.0) * b + I.c_in * kk[c];
+        I.acc[o] = b + I.c_acc * kk[c];
+      } else if (mode == MODE_RK4) {
+        I.base_out[o] = I.acc[o] + I.c_acc * kk[c];
+      } else {
+        I.out[o] = T(1.0) * I.base[o] + I.c_in * kk[c];
+        I.acc[o] = I.acc[o] + I.c_acc * kk[c];
+      }
+    }
+  } else {
+    // FP32 compensated form: the stage increments accumulate separately from
+    // the state (dacc = dt/6 k1 + dt/3 k2 + dt/3 k3), and the final stage adds
+    // dacc + dt/6 k4 to the (hi, lo) state pair with an exact two-sum, so the
+    // FP32 state keeps the low-order bits across steps.
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long o = c * fs + idx;
+      if (mode == MODE_RK1) {
+        I.out[o] = I.base[o] + I.c_in * kk[c];
+        I.acc[o] = I.c_acc * kk[c];
+      } else if (mode == MODE_RK4) {
+        const T d = I.acc[o] + I.c_acc * kk[c];
+        const T hi = I.base_out[o], lo = I.base_lo[o];
+        const T t = lo + d;
+        const T s = hi + t;
+        const T bb = s - hi;
+        const T err = (hi - (s - bb)) + (t - bb);
+        I.base_out[o] = s;
+        I.base_lo[o] = err;
+      } else {
+        I.out[o] = I.base[o] + I.c_in * kk[c];
+        I.acc[o] = I.acc[o] + I.c_acc * kk[c];
+      }
+    }
+  }
+}
+
+// Coriolis + tendency at a node, given the synced gx, gy, zeta, div.
+// cor_u = (f+zeta)*hv/h*J with hv/h = vt (coriolis_colocated_mod.f90:93-100).
+template <class T>
+__device__ __forceinline__ void node_tendency(T gx, T gy, T zeta, T dv, T f, T J, T ut, T vt,
+                                              T& kh, T& ku, T& kv) {
+  const T fz = f + zeta;
+  ku = -gx + fz * (J * vt);
+  kv = -gy - fz * (J * ut);
+  kh = -dv;
+}
+
+// ---------------------------------------------------------------------------
+// Fused stage kernel.  One CTA = one work unit (panel strip x row segment);
+// thread t owns column cl0+t.  Rows stream through a shared-memory ring of
+// 2*RMAX+1 rows holding the derived fields, so every input node is read from
+// global memory once per unit.
+// ---------------------------------------------------------------------------
+template <class T, int ORD>
+__global__ void __launch_bounds__(STAGE_BW)
+    stage_kernel(InstDev<T> one, const InstDev<T>* many, const WorkUnit* units, int mode) {
+  constexpr int RMAX = Ord<ORD>::RMAX, RB = 2 * RMAX + 1, NE = Ord<ORD>::NE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T(*ring)[RF_N][STAGE_BW] = reinterpret_cast<T(*)[RF_N][STAGE_BW]>(smem_raw);
+
+  const WorkUnit wu = units[blockIdx.x];
+  const InstDev<T>& I = many ? many[wu.inst] : one;
+  const int n = I.n, P = I.P;
+  const long long pbase = (long long)wu.panel * I.ps;
+  const long long fs = I.fs;
+  const int t = threadIdx.x;
+  const int col = wu.cl0 + t;
+  const bool load_col = col < wu.cl1;
+  const T grav = I.grav;
+
+  auto load_row = [&](int r) {
+    if (!load_col) return;
+    const long long idx = pbase + (long long)r * P + col;
+    const T h = I.in[idx], u = I.in[fs + idx], v = I.in[2 * fs + idx];
+    const T J = I.metric[MJ * fs + idx];
+    const T q1 = I.metric[MQI1 * fs + idx], q2 = I.metric[MQI2 * fs + idx],
+            q3 = I.metric[MQI3 * fs + idx];
+    const T ut = q1 * u + q2 * v;
+    const T vt = q2 * u + q3 * v;
+    T ke = (u * ut + v * vt) / T(2.0);
+    ke = ke + grav * h;
+    if (I.hs) ke = ke + grav * I.hs[idx];
+    const int s = r % RB;
+    ring[s][RF_KE][t] = ke;
+    ring[s][RF_U][t] = u;
+    ring[s][RF_V][t] = v;
+    ring[s][RF_GU][t] = J * (h * ut);
+    ring[s][RF_GV][t] = J * (h * vt);
+    ring[s][RF_UT][t] = ut;
+    ring[s][RF_VT][t] = vt;
+    ring[s][RF_J][t] = J;
+  };
+
+  int loaded = wu.rl0;
+  {
+    const int target = min((int)wu.rl1, wu.j0 + RMAX + 1);
+    for (; loaded < target; ++loaded) load_row(loaded);
+  }
+  for (int j = wu.j0; j < wu.j1; ++j) {
+    if (j > wu.j0) {
+      __syncthreads();
+      const int target = min((int)wu.rl1, j + RMAX + 1);
+      for (; loaded < target; ++loaded) load_row(loaded);
+    }
+    __syncthreads();
+    if (col < wu.i0 || col >= wu.i1) continue;
+    const int sj = j % RB;
+    // x derivatives (along the row, neighbours are other threads' columns)
+    auto xa = [&](int f) {
+      return d_line<ORD, T>(col, n, [&](int m) { return ring[sj][f][m - wu.cl0]; });
+    };
+    auto ya = [&](int f) {
+      return d_line<ORD, T>(j, n, [&](int m) { return ring[m % RB][f][t]; });
+    };
+    const T dxke = xa(RF_KE), dyke = ya(RF_KE);
+    const T dxv = xa(RF_V), dyu = ya(RF_U);
+    const T dxgu = xa(RF_GU), dygv = ya(RF_GV);
+    const T J = ring[sj][RF_J][t];
+    T rJ;
+    if constexpr (sizeof(T) == 8) {
+      rJ = I.metric[MRJ * fs + pbase + (long long)j * P + col];
+    } else {
+      rJ = I.ghs / J;
+    }
+    const T gx = dxke * I.ghs, gy = dyke * I.ghs;
+    const T zeta = (dxv - dyu) * rJ;
+    const T dv = (dxgu + dygv) * rJ;
+    const long long idx = pbase + (long long)j * P + col;
+    const bool bnd = (col == 0) | (col == n - 1) | (j == 0) | (j == n - 1);
+    if (bnd) {
+      T* E = I.edge + (long long)wu.panel * 16 * n;
+      const T vals[4] = {gx, gy, zeta, dv};
+      if (col == 0)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) E[(SIDE_L * 4 + e) * n + j] = vals[e];
+      if (col == n - 1)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) E[(SIDE_R * 4 + e) * n + j] = vals[e];
+      if (j == 0)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) E[(SIDE_B * 4 + e) * n + col] = vals[e];
+      if (j == n - 1)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) E[(SIDE_T * 4 + e) * n + col] = vals[e];
+      continue;
+    }
+    const T f = I.metric[MF * fs + idx];
+    T kh, ku, kv;
+    node_tendency<T>(gx, gy, zeta, dv, f, J, ring[sj][RF_UT][t], ring[sj][RF_VT][t], kh, ku, kv);
+    stage_epilogue<T>(I, mode, idx, kh, ku, kv);
+  }
+  (void)NE;
+}
+
+template <class T, int ORD>
+constexpr size_t stage_smem_bytes() {
+  return sizeof(T) * (2 * Ord<ORD>::RMAX + 1) * RF_N * STAGE_BW;
+}
+
+template <class T, int ORD>
+cudaError_t launch_stage_ord(const InstDev<T>& one, const InstDev<T>* many, const WorkUnit* units,
+                             int nunits, int mode, cudaStream_t st) {
+  constexpr size_t smem = stage_smem_bytes<T, ORD>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(stage_kernel<T, ORD>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (nunits <= 0) return cudaSuccess;
+  stage_kernel<T, ORD><<<nunits, STAGE_BW, smem, st>>>(one, many, units, mode);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Cube-edge syncs at one panel-boundary node (p, i, j): returns the synced
+// gx, gy (covariant gradient), zeta and div.  E points at the edge buffer of
+// the instance; ring values come from the neighbour panels' entries.
+// ---------------------------------------------------------------------------
+template <class T>
+struct EdgeView {
+  const T* E;
+  int n;
+  __device__ __forceinline__ T get(int p, int side, int v, int k) const {
+    return E[((long long)(p * 4 + side) * 4 + v) * n + k];
+  }
+};
+
+template <class T>
+__device__ __forceinline__ void ring_scalar(const EdgeView<T>& ev, const Topology& tp, int p,
+                                            int side, int v, int k, T& out) {
+  const EdgeLink L = tp.link[p][side];
+  const int kk = L.rev ? ev.n - 1 - k : k;
+  out = ev.get(L.q, L.side_q, v, kk);
+}
+
+template <class T>
+__device__ __forceinline__ void ring_vector(const EdgeView<T>& ev, const Topology& tp, int p,
+                                            int side, int k, T& rx, T& ry) {
+  const EdgeLink L = tp.link[p][side];
+  const int kk = L.rev ? ev.n - 1 - k : k;
+  const T gxq = ev.get(L.q, L.side_q, EV_GX, kk), gyq = ev.get(L.q, L.side_q, EV_GY, kk);
+  if (L.dim_i) { rx = T(L.istep) * gxq; ry = T(L.jstep) * gyq; }
+  else { rx = T(L.jstep) * gyq; ry = T(L.istep) * gxq; }
+}
+
+// Scalar sync of value slot v at node (p,i,j) (halo_Ah_scalar_sync_mod.f90:38-93).
+template <class T>
+__device__ T sync_scalar_node(const EdgeView<T>& ev, const Topology& tp, int p, int i, int j,
+                              int v, T own) {
+  const int e = ev.n - 1;
+  T a, b;
+  if (i == 0 && j == 0) { ring_scalar(ev, tp, p, SIDE_L, v, 0, a); ring_scalar(ev, tp, p, SIDE_B, v, 0, b); return (own + a + b) / T(3.0); }
+  if (i == e && j == 0) { ring_scalar(ev, tp, p, SIDE_R, v, 0, a); ring_scalar(ev, tp, p, SIDE_B, v, e, b); return (own + a + b) / T(3.0); }
+  if (i == 0 && j == e) { ring_scalar(ev, tp, p, SIDE_L, v, e, a); ring_scalar(ev, tp, p, SIDE_T, v, 0, b); return (own + a + b) / T(3.0); }
+  if (i == e && j == e) { ring_scalar(ev, tp, p, SIDE_R, v, e, a); ring_scalar(ev, tp, p, SIDE_T, v, e, b); return (own + a + b) / T(3.0); }
+  if (i == 0) { ring_scalar(ev, tp, p, SIDE_L, v, j, a); return T(0.5) * (a + own); }
+  if (i == e) { ring_scalar(ev, tp, p, SIDE_R, v, j, a); return T(0.5) * (own + a); }
+  if (j == 0) { ring_scalar(ev, tp, p, SIDE_B, v, i, a); return T(0.5) * (own + a); }
+  ring_scalar(ev, tp, p, SIDE_T, v, i, a);
+  return T(0.5) * (own + a);
+}
+
+// Covariant vector sync at node (p,i,j): syncronize_grad_on_edges with U = gy,
+// V = gx (ecs_Ah_vec_sync_mod.f90:52, 62-125).  qw = qb|qt|ql|qr (n each).
+template <class T>
+__device__ void sync_vector_node(const EdgeView<T>& ev, const Topology& tp, const double* qw,
+                                 int p, int i, int j, T& gx, T& gy) {
+  const int n = ev.n, e = n - 1;
+  const double* qb = qw;
+  const double* qt = qw + n;
+  const double* ql = qw + 2 * n;
+  const double* qr = qw + 3 * n;
+  T V = gx, U = gy;
+  T rx, ry, sx, sy;
+  if (i == 0 && j == 0) {
+    ring_vector(ev, tp, p, SIDE_L, 0, rx, ry); ring_vector(ev, tp, p, SIDE_B, 0, sx, sy);
+    gy = (U + ry + sy + T(qb[0]) * sx) / T(3.0);
+    gx = (V + rx + sx + T(ql[0]) * ry) / T(3.0);
+  } else if (i == e && j == 0) {
+    ring_vector(ev, tp, p, SIDE_R, 0, rx, ry); ring_vector(ev, tp, p, SIDE_B, e, sx, sy);
+    gy = (U + ry + sy + T(qb[e]) * sx) / T(3.0);
+    gx = (V + rx + sx + T(qr[0]) * ry) / T(3.0);
+  } else if (i == 0 && j == e) {
+    ring_vector(ev, tp, p, SIDE_L, e, rx, ry); ring_vector(ev, tp, p, SIDE_T, 0, sx, sy);
+    gy = (U + ry + sy + T(qt[0]) * sx) / T(3.0);
+    gx = (V + rx + sx + T(ql[e]) * ry) / T(3.0);
+  } else if (i == e && j == e) {
+    ring_vector(ev, tp, p, SIDE_R, e, rx, ry); ring_vector(ev, tp, p, SIDE_T, e, sx, sy);
+    gy = (U + ry + sy + T(qt[e]) * sx) / T(3.0);
+    gx = (V + rx + sx + T(qr[e]) * ry) / T(3.0);
+  } else if (i == 0) {
+    ring_vector(ev, tp, p, SIDE_L, j, rx, ry);
+    gy = T(0.5) * (ry + U);
+    gx = T(0.5) * (V + rx + T(ql[j]) * ry);
+  } else if (i == e) {
+    ring_vector(ev, tp, p, SIDE_R, j, rx, ry);
+    gy = T(0.5) * (U + ry);
+    gx = T(0.5) * (V + rx + T(qr[j]) * ry);
+  } else if (j == 0) {
+    ring_vector(ev, tp, p, SIDE_B, i, sx, sy);
+    gx = T(0.5) * (sx + V);
+    gy = T(0.5) * (sy + U + T(qb[i]) * sx);
+  } else {
+    ring_vector(ev, tp, p, SIDE_T, i, sx, sy);
+    gx = T(0.5) * (V + sx);
+    gy = T(0.5) * (U + sy + T(qt[i]) * sx);
+  }
+}
+
+// boundary node b of a panel (0 <= b < 4n-4) -> (i, j); bottom and top rows
+// own the corners.
+__device__ __forceinline__ void boundary_node(int b, int n, int& i, int& j) {
+  if (b < n) { i = b; j = 0; }
+  else if (b < 2 * n) { i = b - n; j = n - 1; }
+  else if (b < 3 * n - 2) { i = 0; j = b - 2 * n + 1; }
+  else { i = n - 1; j = b - (3 * n - 2) + 1; }
+}
+
+// ---------------------------------------------------------------------------
+// Edge kernel: finishes every panel-boundary node of every instance.
+// blockIdx.y = instance, x covers 6*(4n-4) nodes.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void edge_kernel(InstDev<T> one, const InstDev<T>* many, Topology tp, int mode) {
+  const InstDev<T>& I = many ? many[blockIdx.y] : one;
+  const int n = I.n, nb = 4 * n - 4;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 6 * nb) return;
+  const int p = g / nb;
+  int i, j;
+  boundary_node(g - p * nb, n, i, j);
+  const EdgeView<T> ev{I.edge, n};
+  // own pre-sync values: read from a side the node lies on
+  int side, k;
+  if (j == 0) { side = SIDE_B; k = i; }
+  else if (j == n - 1) { side = SIDE_T; k = i; }
+  else if (i == 0) { side = SIDE_L; k = j; }
+  else { side = SIDE_R; k = j; }
+  T gx = ev.get(p, side, EV_GX, k), gy = ev.get(p, side, EV_GY, k);
+  const T zo = ev.get(p, side, EV_ZETA, k), dvo = ev.get(p, side, EV_DIV, k);
+  sync_vector_node<T>(ev, tp, I.qw, p, i, j, gx, gy);
+  const T zeta = sync_scalar_node<T>(ev, tp, p, i, j, EV_ZETA, zo);
+  const T dv = sync_scalar_node<T>(ev, tp, p, i, j, EV_DIV, dvo);
+
+  const long long fs = I.fs;
+  const long long idx = (long long)p * I.ps + (long long)j * I.P + i;
+  const T u = I.in[fs + idx], v = I.in[2 * fs + idx];
+  const T q1 = I.metric[MQI1 * fs + idx], q2 = I.metric[MQI2 * fs + idx],
+          q3 = I.metric[MQI3 * fs + idx];
+  const T ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
+  const T J = I.metric[MJ * fs + idx], f = I.metric[MF * fs + idx];
+  T kh, ku, kv;
+  node_tendency<T>(gx, gy, zeta, dv, f, J, ut, vt, kh, ku, kv);
+  stage_epilogue<T>(I, mode, idx, kh, ku, kv);
+}
+
+}  // namespace swm

@@ -1,0 +1,187 @@
+"""Seeded synthetic initial states on the cubed sphere (host, FP64, numpy).
+
+These stand in for the reference's analytic test cases (Williamson TS2-type
+balanced zonal flow, test_fields_mod.f90:826-859; Galewsky-type barotropic
+jet, barotropic_inst_mod.f90:236-284) with seeded perturbations:
+
+* balanced_zonal(N, seed, lmax): u = u0 cos(lat) with u0 ~ U[20, 40] m/s,
+  h from the balance relation with area-mean depth 5960 m, plus a random
+  spherical-harmonic height perturbation of degrees 1..lmax with amplitude
+  spectrum l^-3, rescaled to 10 m area-weighted RMS.  The associated Legendre
+  recursion follows random_friction_mod.f90:136-178 (fully normalised P_lm).
+* unstable_jet(N, seed): a Gaussian jet in latitude with peak 80 m/s and
+  seeded centre/width, its balanced height integrated with 3-point Gauss
+  quadrature as barotropic_inst_mod.f90:236-284 does, plus a seeded 120 m
+  height bump.
+
+Velocities are returned as covariant components on the unit-sphere basis
+(u = V.a1, v = V.a2), the representation the reference stores
+(test_fields_mod.f90:283-319).  Arrays have shape (6, N+1, N+1).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# panel frames of the six cube faces (ex, ey, inward normal)
+_EX = np.array([[-1, 0, 0], [0, 0, -1], [1, 0, 0], [0, 0, 1], [1, 0, 0], [1, 0, 0]], float)
+_EY = np.array([[0, 1, 0], [0, 1, 0], [0, 1, 0], [0, 1, 0], [0, 0, 1], [0, 0, -1]], float)
+_EN = np.array([[0, 0, 1], [-1, 0, 0], [0, 0, -1], [1, 0, 0], [0, 1, 0], [0, -1, 0]], float)
+
+MEAN_DEPTH = 5960.0
+
+
+def ecs_geometry(N: int) -> dict:
+    """Node positions r (unit sphere), covariant basis a1, a2 and Jacobian J
+    of the equiangular cubed sphere (ecs_metric_mod.f90:326-478)."""
+    n = N + 1
+    hx = (0.5 * math.pi) / N
+    al = -0.25 * math.pi + hx * np.arange(n)
+    ta = np.tan(al)[None, :]       # i direction
+    tb = np.tan(al)[:, None]       # j direction
+    s2 = 1.0 + ta * ta + tb * tb
+    sg = np.sqrt(s2)
+    p15 = s2 ** 1.5
+    one = np.ones_like(s2)
+    rp = np.stack([ta * one / sg, tb * one / sg, one / sg], -1)
+    a1p = np.stack([(1 + ta * ta) * (1 + tb * tb) / p15, -ta * tb * (1 + ta * ta) / p15,
+                    -ta * (1 + ta * ta) * one / p15], -1)
+    a2p = np.stack([-ta * tb * (1 + tb * tb) / p15, (1 + ta * ta) * (1 + tb * tb) / p15,
+                    -tb * (1 + tb * tb) * one / p15], -1)
+    J = (1 + ta * ta) * (1 + tb * tb) / (sg * sg * sg)
+
+    def face(v):
+        return (v[None, ..., 0:1] * _EX[:, None, None, :] + v[None, ..., 1:2] * _EY[:, None, None, :]
+                - v[None, ..., 2:3] * _EN[:, None, None, :])
+
+    return dict(r=face(rp), a1=face(a1p), a2=face(a2p), J=np.broadcast_to(J, (6, n, n)).copy(),
+                hx=hx, n=n, N=N)
+
+
+def _legendre_all(lmax: int, x: np.ndarray) -> dict:
+    """Fully normalised associated Legendre functions P_lm(x), 0<=m<=l<=lmax,
+    by the recursion of random_friction_mod.f90:136-178."""
+    P = {}
+    for m in range(lmax + 1):
+        if m == 0:
+            P[(0, 0)] = np.full_like(x, math.sqrt(0.5))
+        else:
+            c = -math.sqrt((2.0 * m + 1.0) / (2.0 * max(m, 1)))
+            P[(m, m)] = c * np.sqrt(1.0 - x * x) * P[(m - 1, m - 1)]
+        if m < lmax:
+            P[(m + 1, m)] = math.sqrt(2.0 * m + 3.0) * x * P[(m, m)]
+        for k in range(m + 2, lmax + 1):
+            c1 = math.sqrt((2.0 * k + 1.0) * (2.0 * k - 1.0) / (1.0 * (k + m) * (k - m)))
+            c2 = -math.sqrt((2.0 * k + 1.0) * (k - m - 1.0) * (k + m - 1.0)
+                            / ((2.0 * k - 3.0) * (k + m) * (k - m)))
+            P[(k, m)] = c1 * x * P[(k - 1, m)] + c2 * P[(k - 2, m)]
+    return P
+
+
+def _covariant(geo, V):
+    return (np.einsum("pjic,pjic->pji", V, geo["a1"]).copy(),
+            np.einsum("pjic,pjic->pji", V, geo["a2"]).copy())
+
+
+def _area_rms(f, J):
+    return math.sqrt(float(np.sum(J * f * f) / np.sum(J)))
+
+
+def harmonic_perturbation(geo, seed: int, lmax: int, rms: float = 10.0) -> np.ndarray:
+    """Random real spherical-harmonic field, degrees 1..lmax, spectrum l^-3,
+    scaled to the given area-weighted RMS."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    r = geo["r"]
+    x = r[..., 2]                                  # sin(latitude) about the z axis
+    lam = np.arctan2(r[..., 1], r[..., 0])
+    P = _legendre_all(lmax, x)
+    f = np.zeros_like(x)
+    for l in range(1, lmax + 1):
+        amp = float(l) ** -3
+        for m in range(0, l + 1):
+            a, b = rng.standard_normal(2)
+            if m == 0:
+                f += amp * a * P[(l, 0)] / math.sqrt(2.0 * math.pi)
+            else:
+                f += amp * P[(l, m)] * (a * np.cos(m * lam) + b * np.sin(m * lam)) / math.sqrt(2.0 * math.pi)
+    return f * (rms / _area_rms(f, geo["J"]))
+
+
+def balanced_zonal(N: int, seed: int, lmax: int, radius=6.371e6, grav=9.80616, omega=7.292e-5,
+                   pert_rms: float = 10.0):
+    """Balanced zonal flow u = u0 cos(lat) + seeded height perturbation.
+    Returns (h, u, v, info)."""
+    geo = ecs_geometry(N)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    u0 = float(rng.uniform(20.0, 40.0))
+    r = geo["r"]
+    k = np.array([0.0, 0.0, 1.0])
+    V = u0 * np.cross(k, r)                        # u0 cos(lat) e_lambda
+    sphi = r[..., 2]
+    c = (radius * omega * u0 + 0.5 * u0 * u0) / grav
+    H0 = MEAN_DEPTH + c / 3.0                      # area mean of sin^2 = 1/3
+    h = H0 - c * sphi * sphi
+    if pert_rms > 0.0 and lmax > 0:
+        h = h + harmonic_perturbation(geo, seed + 7919, lmax, pert_rms)
+    u, v = _covariant(geo, V)
+    return h, u, v, dict(u0=u0, H0=H0, seed=seed, lmax=lmax)
+
+
+def _jet_u(phi, umax, phic, width):
+    return umax * np.exp(-((phi - phic) / width) ** 2)
+
+
+def unstable_jet(N: int, seed: int, radius=6.371e6, grav=9.80616, omega=7.292e-5,
+                 umax: float = 80.0, bump: float = 120.0, nq: int = 4096):
+    """Gaussian zonal jet (peak umax) in balance, plus a seeded height bump."""
+    geo = ecs_geometry(N)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    phic = float(rng.uniform(math.pi / 6, math.pi / 3))
+    width = float(rng.uniform(0.08, 0.14))
+    lam_b = float(rng.uniform(-math.pi, math.pi))
+    phi_b = phic + float(rng.uniform(-0.05, 0.05))
+    # balance: dh/dphi = -(u^2 tan(phi) + 2 omega a sin(phi) u) / g, Gauss 3-pt
+    xq = np.array([-math.sqrt(0.6), 0.0, math.sqrt(0.6)])
+    wq = np.array([5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0])
+    edges = np.linspace(-0.5 * math.pi, 0.5 * math.pi, nq + 1)
+    dphi = edges[1] - edges[0]
+    H = np.zeros(nq + 1)
+    for jq in range(nq):
+        ph = edges[jq] + 0.5 * dphi + 0.5 * dphi * xq
+        u = _jet_u(ph, umax, phic, width)
+        rhs = -(u * u * np.tan(ph) + 2.0 * omega * radius * np.sin(ph) * u) / grav
+        H[jq + 1] = H[jq] + 0.5 * dphi * float(np.sum(wq * rhs))
+    r = geo["r"]
+    phi = np.arcsin(np.clip(r[..., 2], -1.0, 1.0))
+    lam = np.arctan2(r[..., 1], r[..., 0])
+    hz = np.interp(phi, edges, H)
+    hz = hz - float(np.sum(geo["J"] * hz) / np.sum(geo["J"])) + MEAN_DEPTH
+    dl = np.angle(np.exp(1j * (lam - lam_b)))
+    h = hz + bump * np.cos(phi) * np.exp(-(dl / (1.0 / 3.0)) ** 2) * np.exp(-((phi - phi_b) / (1.0 / 15.0)) ** 2)
+    k = np.array([0.0, 0.0, 1.0])
+    kxr = np.cross(k, r)
+    cphi = np.maximum(np.linalg.norm(kxr, axis=-1), 1e-14)
+    V = (_jet_u(phi, umax, phic, width) / cphi)[..., None] * kxr
+    u, v = _covariant(geo, V)
+    return h, u, v, dict(phic=phic, width=width, lam_b=lam_b, phi_b=phi_b, seed=seed)
+
+
+# The benchmark configurations: (N, sbp_order, dt [s], steps, generator args)
+CONFIGS = {
+    1: dict(N=48, sbp_order=42, dt=900.0, steps=96, seed=1, lmax=16, kind="zonal"),
+    2: dict(N=384, sbp_order=42, dt=120.0, steps=7200, seed=2, lmax=64, kind="zonal"),
+    4: dict(N=192, sbp_order=42, dt=300.0, steps=240, seed=3, lmax=16, kind="zonal"),
+    5: dict(N=1024, sbp_order=63, dt=45.0, steps=9600, seed=5, kind="jet"),
+}
+
+
+def config_state(cfg: int, N: int | None = None, seed: int | None = None):
+    """Initial (h, u, v, info) of benchmark configuration cfg (optionally at
+    another resolution, for reduced-size parity runs)."""
+    c = CONFIGS[cfg]
+    N = c["N"] if N is None else N
+    seed = c["seed"] if seed is None else seed
+    if c["kind"] == "jet":
+        return unstable_jet(N, seed)
+    return balanced_zonal(N, seed, c["lmax"])

@@ -1,0 +1,206 @@
+/*
+ * swm_gpu.h -- C-ABI of the GB300 shallow-water hot path.
+ *
+ * Drop-in boundary for the reference's Fortran plugin surface
+ * (vvshashkin/cubedsphere_sbp_swm).  Every entry point below names the
+ * reference interface it replaces (file:line inside the reference project).
+ * A Fortran caller binds these with iso_c_binding; Python/C++ callers use
+ * plain pointers and sizes.  No torch or CUDA types appear in the signatures.
+ *
+ * Conventions
+ *  - Every function returns SWM_OK (0) or a negative SWM_E_* code; the
+ *    message of the last failure is swm_last_error(ctx) (or
+ *    swm_last_error(NULL) for failures without a context).  Nothing aborts,
+ *    traps or exits: the reference's parcomm_global%abort paths
+ *    (parallel/parcomm_mod.f90:73-83) become error codes.
+ *  - Host arrays use the reference layout of one tile per panel: for each of
+ *    the 6 panels an (N+1) x (N+1) FP64 array p(1:N+1, 1:N+1) with i (alpha)
+ *    fastest, panels stored one after another (6*(N+1)^2 doubles).  N is the
+ *    number of cells per panel edge as in the reference namelist
+ *    (domain/config_domain_mod.f90), so panel edge nodes are duplicated on
+ *    both panels exactly as in the reference Ah grid.
+ *  - Device memory belongs to the context; every call is ordered on the
+ *    context's CUDA stream.  A context is not thread-safe (the reference
+ *    operators are not re-entrant either: they share work fields).
+ */
+#ifndef SWM_GPU_H
+#define SWM_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWM_OK             0
+#define SWM_E_INVALID     -1  /* bad argument, size or handle */
+#define SWM_E_UNSUPPORTED -2  /* unknown operator / scheme name or option */
+#define SWM_E_CUDA        -3  /* CUDA runtime failure */
+#define SWM_E_NOMEM       -4  /* device or host allocation failed */
+#define SWM_E_DEVICE      -5  /* a kernel raised its device error flag */
+
+/* Arithmetic of the hot path. */
+#define SWM_FP64_PLAIN 0   /* FP64 end to end; parity path (1e-12 rel. L2/step) */
+#define SWM_FP32_FUSED 1   /* FP32 stencils, compensated RK4 stage sums, FP64
+                              metric precompute and FP64 global integrals */
+
+typedef struct swm_ctx swm_ctx;      /* domain + operator + time scheme */
+typedef struct swm_state swm_state;  /* stvec_swm_t: (h, u, v) on the device */
+typedef struct swm_field swm_field;  /* grid_field_t: one FP64 field */
+
+/* Model configuration: the &domain, &metric and &shallow_water_model keys
+ * the hot path needs (domain/config_domain_mod.f90:26-58,
+ * metric/config_metric_mod.f90:37-63, models/shallow_water/config/
+ * config_swm_mod.f90:8-107).  Physical constants are explicit. */
+typedef struct swm_config {
+  int    N;                 /* cells per panel edge (>= 16) */
+  int    sbp_order;         /* 21, 42, 43 or 63 (SBP d21/d42/d43/d63) */
+  double radius;            /* sphere radius a [m]   (metric "scale") */
+  double grav;              /* gravity g [m s^-2] */
+  double omega;             /* rotation rate [s^-1] */
+  double rotation_axis[3];  /* normalised internally */
+  int    precision;         /* SWM_FP64_PLAIN or SWM_FP32_FUSED */
+  int    device;            /* CUDA device ordinal */
+} swm_config;
+
+/* ---------------------------------------------------------------------- */
+/* Construction                                                            */
+/* ---------------------------------------------------------------------- */
+
+/* create_domain + create_swm_operator + create_timescheme("rk4") in one:
+ * domain/domain_factory_mod.f90:44-136,
+ * models/shallow_water/operator/operator_swm_factory_mod.f90:43-131,
+ * time_schemes/timescheme_factory_mod.f90:42-59.  Uses the operator names
+ * that match cfg->sbp_order (divergence_ahXX_sbp, gradient_ahXX_sbp_ecs,
+ * curl_divergence_ahXX_sbp, coriolis_colocated, KE_colocated,
+ * co2contra_colocated, massflux_colocated, SBP_AhXX_quadrature). */
+int swm_ctx_create(const swm_config* cfg, swm_ctx** out);
+
+/* As swm_ctx_create, with the operator names of the &shallow_water_model
+ * namelist (config_swm_mod.f90:70-104).  Names outside the vector-invariant
+ * Ah-grid family, or div/grad/curl of different SBP orders, return
+ * SWM_E_UNSUPPORTED. */
+int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name,
+                         const char* grad_op_name, const char* curl_op_name,
+                         const char* coriolis_op_name, const char* KE_op_name,
+                         const char* co2contra_op_name,
+                         const char* massflux_op_name,
+                         const char* quadrature_name, swm_ctx** out);
+
+void        swm_ctx_destroy(swm_ctx* ctx);
+const char* swm_last_error(const swm_ctx* ctx);
+int         swm_ctx_synchronize(swm_ctx* ctx);
+/* The context's cudaStream_t, for callers that interleave their own work. */
+void*       swm_ctx_stream(swm_ctx* ctx);
+/* Number of nodes per field, 6*(N+1)^2. */
+size_t      swm_ctx_npts(const swm_ctx* ctx);
+
+/* Orography h_surf (operator_swm_factory_mod.f90:120-121; zero if never set). */
+int swm_set_orography(swm_ctx* ctx, const double* h_surf_host);
+
+/* ---------------------------------------------------------------------- */
+/* State vector: stvec_t (stvec_mod.f90:10-28), stvec_swm_t                 */
+/* (models/shallow_water/stvec/stvec_swm_mod.f90:10-106)                    */
+/* ---------------------------------------------------------------------- */
+int  swm_state_create(swm_ctx* ctx, swm_state** out);   /* create_stvec_swm */
+int  swm_state_create_similar(swm_ctx* ctx, const swm_state* src,
+                              swm_state** out);          /* %create_similar */
+void swm_state_free(swm_state* s);
+int  swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h,
+                      const double* u, const double* v);
+int  swm_state_download(swm_ctx* ctx, const swm_state* s, double* h,
+                        double* u, double* v);
+/* this = s1                       (%assign_s1) */
+int swm_assign_s1(swm_ctx* ctx, swm_state* s, double s1);
+/* this = s1*v1                    (%assign_s1v1) */
+int swm_assign_s1v1(swm_ctx* ctx, swm_state* s, double s1, const swm_state* v1);
+/* this = s1*v1 + s2*v2            (%assign_s1v1s2v2, stvec_swm_mod.f90:38-62) */
+int swm_assign_s1v1s2v2(swm_ctx* ctx, swm_state* s, double s1,
+                        const swm_state* v1, double s2, const swm_state* v2);
+/* this = this + s1*v1             (%update_s1v1, stvec_swm_mod.f90:88-106) */
+int swm_update_s1v1(swm_ctx* ctx, swm_state* s, double s1, const swm_state* v1);
+/* this = this + s1*v1 + s2*v2     (%update_s1v1s2v2, stvec_swm_mod.f90:63-87) */
+int swm_update_s1v1s2v2(swm_ctx* ctx, swm_state* s, double s1,
+                        const swm_state* v1, double s2, const swm_state* v2);
+/* algebraic dot / norm2 over all nodes of h, u, v (%algebraic_dot/norm2) */
+int swm_dot(swm_ctx* ctx, const swm_state* a, const swm_state* b, double* out);
+int swm_norm2(swm_ctx* ctx, const swm_state* a, double* out);
+
+/* ---------------------------------------------------------------------- */
+/* Operator and time scheme                                                */
+/* ---------------------------------------------------------------------- */
+/* vout = A(vin): operator_t%apply (operator_mod.f90:18-25), implemented by
+ * operator_swm_t%apply (operator_swm_mod.f90:61-113) as one fused kernel
+ * pass plus the cube-edge pass. */
+int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin);
+/* Same result through the unfused FP64 per-operator kernels in the
+ * reference's call order (co2contra, massflux, KE, grad+sync, curl+sync,
+ * coriolis, div+sync).  FP64 contexts only. */
+int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin);
+/* nsteps of rk4_t%step (time_schemes/rk4_mod.f90:20-42) on v0, in place,
+ * with the stage combinations folded into the RHS kernels and the step
+ * replayed as a CUDA graph. */
+int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
+/* get_diagnostics (operator_swm_mod.f90:115-155): out[7] = hmin, hmax,
+ * mass, TE, KE, PE, Enstrophy, all FP64 with SBP quadrature. */
+int swm_diagnostics(swm_ctx* ctx, const swm_state* v, double out[7]);
+
+/* ---------------------------------------------------------------------- */
+/* Fields and single operators (grid_field_t, grid_field_mod.f90:7-65)     */
+/* FP64, reference semantics, one kernel pass each (parity mode).          */
+/* ---------------------------------------------------------------------- */
+int  swm_field_create(swm_ctx* ctx, swm_field** out);
+void swm_field_free(swm_field* f);
+int  swm_field_upload(swm_ctx* ctx, swm_field* f, const double* host);
+int  swm_field_download(swm_ctx* ctx, const swm_field* f, double* host);
+
+/* co2contra_colocated%transform (co2contra_colocated_mod.f90:20-60) */
+int swm_op_co2contra(swm_ctx* ctx, swm_field* ut, swm_field* vt,
+                     const swm_field* u, const swm_field* v);
+/* massflux_colocated (massflux_colocated_mod.f90:19-29) */
+int swm_op_massflux(swm_ctx* ctx, swm_field* hu, swm_field* hv,
+                    const swm_field* h, const swm_field* ut,
+                    const swm_field* vt);
+/* KE_colocated (kinetic_energy/KE_colocated_mod.f90:17-48) */
+int swm_op_ke(swm_ctx* ctx, swm_field* ke, const swm_field* u,
+              const swm_field* v, const swm_field* ut, const swm_field* vt);
+/* grad_ah_sbp_t%calc_grad incl. its covariant edge sync
+ * (gradient/grad_ah_sbp_mod.f90:26-90) */
+int swm_op_grad(swm_ctx* ctx, swm_field* gx, swm_field* gy,
+                const swm_field* f);
+/* div_ah_sbp_t%calc_div incl. its scalar sync (div_ah_sbp_mod.f90:24-98);
+ * u, v contravariant */
+int swm_op_div(swm_ctx* ctx, swm_field* div, const swm_field* u,
+               const swm_field* v);
+/* curl_div_based_t%calc_curl (curl/curl_div_based_mod.f90:26-66); u, v
+ * covariant */
+int swm_op_curl(swm_ctx* ctx, swm_field* curl, const swm_field* u,
+                const swm_field* v);
+/* coriolis_colocated%calc_coriolis_vec_inv (coriolis_colocated_mod.f90:61-103) */
+int swm_op_coriolis(swm_ctx* ctx, swm_field* cor_u, swm_field* cor_v,
+                    const swm_field* hu, const swm_field* hv,
+                    const swm_field* h, const swm_field* curl);
+/* halo_t%get_halo_scalar for "Ah_scalar_sync"
+ * (halo/halo_Ah_scalar_sync_mod.f90:20-93) */
+int swm_sync_scalar(swm_ctx* ctx, swm_field* f);
+/* halo_vec_t%get_halo_vector for "ecs_Ah_vec_sync_covariant"
+ * (equiang_cs/ecs_Ah_vec_sync_mod.f90:34-125) */
+int swm_sync_vector_cov(swm_ctx* ctx, swm_field* gx, swm_field* gy);
+/* quadrature_t%mass with the SBP_AhXX quadrature
+ * (quadrature/abstract_quadrature_mod.f90:27-44, sbp_quadrature_mod.f90:21-40) */
+int swm_quadrature_mass(swm_ctx* ctx, const swm_field* f, double* out);
+
+/* ---------------------------------------------------------------------- */
+/* Kernel timing for measurement (no reference counterpart): when enabled,  */
+/* every fused-stage kernel launch is bracketed by CUDA events on the       */
+/* context stream; swm_timing_read returns the summed stage-kernel time     */
+/* [ms] and the number of launches since the last reset.                   */
+/* ---------------------------------------------------------------------- */
+int swm_timing_enable(swm_ctx* ctx, int on);
+int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches,
+                    double* edge_ms, long* edge_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

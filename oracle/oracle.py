@@ -72,6 +72,10 @@ def lib():
         L.orc_golden_quadrature.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_golden_quadrature.restype = ctypes.c_double
         L.orc_golden_rk4_iomega.restype = ctypes.c_double
+        L.orc_vector_test_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
+        L.orc_vector_test_field.restype = ctypes.c_int
+        L.orc_scalar_test_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, _D]
+        L.orc_scalar_test_field.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -175,6 +179,21 @@ class OracleDomain:
         out = np.zeros(7)
         lib().orc_diagnostics(self._h, _p(hs), _p(h), _p(u), _p(v), _p(out))
         return out
+
+    VECTOR_FIELDS = {"solid_rotation": 0, "cross_polar": 1, "xyz_grad": 2, "vsh_curl_free_10": 3}
+    SCALAR_FIELDS = {"xyz": 10, "cross_polar_div": 11, "cross_polar_zeta": 12}
+
+    def vector_test_field(self, kind, level=0, contravariant=False):
+        u, v = self.zeros(), self.zeros()
+        rc = lib().orc_vector_test_field(self._h, self.VECTOR_FIELDS[kind], int(level),
+                                         1 if contravariant else 0, _p(u), _p(v))
+        assert rc == 0
+        return u, v
+
+    def scalar_test_field(self, kind, level=0):
+        f = self.zeros()
+        assert lib().orc_scalar_test_field(self._h, self.SCALAR_FIELDS[kind], int(level), _p(f)) == 0
+        return f
 
     def l2norm(self, f):
         return lib().orc_l2norm(self._h, _p(np.ascontiguousarray(f, dtype=np.float64)))

@@ -786,6 +786,38 @@ void orc_diagnostics(const orc_domain* d, const double* hs, const double* h, con
 double orc_l2norm(const orc_domain* d, const double* f) { return std::sqrt(l2sq(*d, f)); }
 double orc_mass(const orc_domain* d, const double* f) { return mass(*d, f); }
 
+// Analytic test fields of the known-answer tests, one level (0..2):
+// kind 0 solid rotation, 1 cross-polar flow, 2 xyz gradient, 3 VSH curl-free
+// (vectors; contravariant != 0 selects b1/b2 components) and kind 10 xyz,
+// 11 cross-polar divergence, 12 cross-polar vorticity (scalars).
+int orc_vector_test_field(const orc_domain* d, int kind, int level, int contravariant,
+                          double* u, double* v) {
+  std::vector<double> uu, vv;
+  switch (kind) {
+    case 0: set_vector(*d, [level](double x, double y, double z, double w[3]) { field_solid_rotation(level, x, y, z, w); }, contravariant != 0, uu, vv); break;
+    case 1: set_vector(*d, field_cross_polar, contravariant != 0, uu, vv); break;
+    case 2: set_vector(*d, [level](double x, double y, double z, double w[3]) { field_xyz_grad(level, x, y, z, w); }, contravariant != 0, uu, vv); break;
+    case 3: set_vector(*d, field_vsh_curl_free_10, contravariant != 0, uu, vv); break;
+    default: return -1;
+  }
+  std::memcpy(u, uu.data(), sizeof(double) * uu.size());
+  std::memcpy(v, vv.data(), sizeof(double) * vv.size());
+  return 0;
+}
+
+int orc_scalar_test_field(const orc_domain* d, int kind, int level, double* f) {
+  for (int k = 0; k < d->npts(); ++k) {
+    const double x = d->rx[k], y = d->ry[k], z = d->rz[k];
+    switch (kind) {
+      case 10: f[k] = field_xyz(level, x, y, z); break;
+      case 11: f[k] = field_cross_polar_div(x, y, z); break;
+      case 12: f[k] = field_cross_polar_zeta(x, y, z); break;
+      default: return -1;
+    }
+  }
+  return 0;
+}
+
 // test_div (test_diff_ops/test_diffops_mod.f90:71-125), nz = 3
 int orc_golden_div(int N, int order, double out[4]) {
   const double ax[3] = {0, 0, 1};

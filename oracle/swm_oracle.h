@@ -77,6 +77,15 @@ void orc_diagnostics(const orc_domain* d, const double* hs, const double* h,
 double orc_l2norm(const orc_domain* d, const double* f);   /* vec_math_mod.f90:50-90 */
 double orc_mass(const orc_domain* d, const double* f);     /* SBP quadrature */
 
+/* Analytic fields of the known-answer tests (test_fields/test_fields_mod.f90):
+ * vector kinds 0 solid rotation (axis cycles with level), 1 cross-polar flow,
+ * 2 gradient of x/y/z (cycles with level), 3 curl-free VSH; contravariant
+ * selects b1/b2 components, else a1/a2.  Scalar kinds 10 x/y/z (cycles),
+ * 11 cross-polar divergence, 12 cross-polar vorticity.  Returns 0 or -1. */
+int orc_vector_test_field(const orc_domain* d, int kind, int level,
+                          int contravariant, double* u, double* v);
+int orc_scalar_test_field(const orc_domain* d, int kind, int level, double* f);
+
 /* Known-answer tests at (N, nz=3, unit sphere); out receives the values
  * printed by the reference test (4 for div/curl, 2 for grad/co2contra). */
 int orc_golden_div(int N, int sbp_order, double out[4]);
