@@ -189,6 +189,11 @@ def run_gpu_arm(args):
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     value = ws * args.steps / (total_ms / 1e3)
+    if args.quick:  # profiling case: only the timed FP32 steps
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "steps/s",
+                              "ms_per_step": round(ms_per_step, 5), "quick": True}), flush=True)
+        return
 
     # dominant kernel timing (stage kernel), events around every launch
     _, _, _, kt = time_steps("fp32", max(8, min(args.steps, 40)), 2, kernel_timing=True)
@@ -330,6 +335,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--quick", action="store_true",
+                    help="profiling case: time only the FP32 steps, print a short line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

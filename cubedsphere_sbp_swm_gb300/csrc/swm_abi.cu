@@ -401,8 +401,10 @@ void free_ctx(swm_ctx* c) {
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
   for (auto& e : c->ev_stage) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   for (auto& e : c->ev_edge) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  // hsT aliases hs64 in FP64 contexts: free each allocation once
+  void* hsT = (c->hsT == (void*)c->hs64) ? nullptr : c->hsT;
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
-                  c->tmp, c->hs64, c->hsT, c->partial, c->dres, c->units};
+                  c->tmp, c->hs64, hsT, c->partial, c->dres, c->units};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->hres) cudaFreeHost(c->hres);
   if (c->st) cudaStreamDestroy(c->st);
@@ -486,6 +488,7 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     }                                                                                 \
   } while (0)
   CKC(cudaSetDevice(cfg->device), "cudaSetDevice");
+  (void)cudaGetLastError();  // drop a stale, non-sticky error of an earlier caller
   CKC(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking), "stream");
   const size_t fbytes = sizeof(double) * ctx->fs;
   CKC(cudaMalloc(&ctx->m64, NMETRIC * fbytes), "alloc metric");
