@@ -176,6 +176,8 @@ struct swm_ctx {
   double* hs64 = nullptr; void* hsT = nullptr;
   double* partial = nullptr; double* dres = nullptr; double* hres = nullptr;
   WorkUnit* units = nullptr; int nunits = 0;
+  int* derr = nullptr;          // device error flag of the bounded waits
+  int num_sms = 0, ctas_per_sm = 0, stage_cols = 0;
   std::map<std::pair<void*, double>, GraphEntry> graphs;
   long graph_clock = 0;
   bool timing = false;
@@ -203,8 +205,10 @@ int cuda_fail(swm_ctx* c, cudaError_t e, const char* where) {
 
 long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
-// Work units of the fused stage kernel: column strips x row segments.
-bool make_units(const SbpC& s, int n, int threads, std::vector<WorkUnit>& out, std::string& why) {
+// Work units of the fused stage kernel: column strips x row segments, as
+// many as fit on the GPU at once (target_ctas) so no CTA waits for a wave.
+bool make_units(const SbpC& s, int n, int threads, int target_ctas, std::vector<WorkUnit>& out,
+                std::string& why) {
   auto need_lo = [&](int k) {
     if (k < s.ne) return 0;
     if (k >= n - s.ne) return n - s.last[n - 1 - k];
@@ -229,8 +233,9 @@ bool make_units(const SbpC& s, int n, int threads, std::vector<WorkUnit>& out, s
     if (ok) break;
     if (nstrip > n) { why = "work split failed"; return false; }
   }
-  const int seg = 16;
-  const int nseg = (n + seg - 1) / seg;
+  const int min_rows = 8;
+  int nseg = std::max(1, target_ctas / (6 * nstrip));
+  nseg = std::min(nseg, std::max(1, n / min_rows));
   for (int p = 0; p < 6; ++p)
     for (int k = 0; k < nstrip; ++k)
       for (int r = 0; r < nseg; ++r) {
@@ -284,7 +289,8 @@ int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
     CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
-  CK(launch_stage<T>(ctx->order, I, nullptr, ctx->units, ctx->nunits, mode, ctx->st), "stage kernel");
+  CK(launch_stage<T>(ctx->order, I, nullptr, ctx->units, ctx->nunits, mode, ctx->derr, ctx->st),
+     "stage kernel");
   if (ctx->timing) {
     CK(cudaEventRecord(b, ctx->st), "event record");
     ctx->ev_stage.emplace_back(a, b);
@@ -363,9 +369,23 @@ int reduce(swm_ctx* ctx, int kind, const double* a, const double* b, int slot) {
   return SWM_OK;
 }
 
+// After a stream synchronisation: report (and clear) the device error flag a
+// kernel raises when one of its bounded waits expired.
+int check_device_flag(swm_ctx* ctx) {
+  int flag = 0;
+  CK(cudaMemcpy(&flag, ctx->derr, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+  if (flag != 0) {
+    CK(cudaMemset(ctx->derr, 0, sizeof(int)), "clear error flag");
+    return fail(ctx, SWM_E_DEVICE, "a kernel gave up a bounded wait (code " + std::to_string(flag) +
+                                       "); results of the affected calls are invalid");
+  }
+  return SWM_OK;
+}
+
 int fetch_results(swm_ctx* ctx, int count, double* out) {
   CK(cudaMemcpyAsync(ctx->hres, ctx->dres, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->st), "copy results");
   CK(cudaStreamSynchronize(ctx->st), "sync");
+  if (int rc_ = check_device_flag(ctx)) return rc_;
   std::memcpy(out, ctx->hres, sizeof(double) * count);
   return SWM_OK;
 }
@@ -404,7 +424,7 @@ void free_ctx(swm_ctx* c) {
   // hsT aliases hs64 in FP64 contexts: free each allocation once
   void* hsT = (c->hsT == (void*)c->hs64) ? nullptr : c->hsT;
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
-                  c->tmp, c->hs64, hsT, c->partial, c->dres, c->units};
+                  c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->hres) cudaFreeHost(c->hres);
   if (c->st) cudaStreamDestroy(c->st);
@@ -472,11 +492,6 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   std::string why;
   if (!build_topology(ctx->topo, why)) { free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why); }
   std::vector<WorkUnit> units;
-  if (!make_units(kTables[sbp_index(od)], ctx->n, kStageThreads, units, why)) {
-    free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
-  }
-  ctx->nunits = (int)units.size();
-
   cudaError_t e;
 #define CKC(call, where)                                                              \
   do {                                                                                \
@@ -508,10 +523,20 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   CKC(cudaMalloc(&ctx->partial, sizeof(double) * REDUCE_BLOCKS), "alloc");
   CKC(cudaMalloc(&ctx->dres, sizeof(double) * 16), "alloc");
   CKC(cudaMallocHost(&ctx->hres, sizeof(double) * 16), "alloc host");
+  CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od, &ctx->ctas_per_sm, &ctx->stage_cols)
+                                  : prepare_stage<double>(od, &ctx->ctas_per_sm, &ctx->stage_cols),
+      "stage kernel attributes");
+  CKC(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device), "SM count");
+  if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->stage_cols,
+                  std::max(1, ctx->ctas_per_sm) * ctx->num_sms, units, why)) {
+    free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
+  }
+  ctx->nunits = (int)units.size();
+  CKC(cudaMalloc(&ctx->derr, sizeof(int)), "alloc");
+  CKC(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st), "memset");
   CKC(cudaMalloc(&ctx->units, sizeof(WorkUnit) * units.size()), "alloc");
   CKC(cudaMemcpyAsync(ctx->units, units.data(), sizeof(WorkUnit) * units.size(), cudaMemcpyHostToDevice, ctx->st), "copy");
   CKC(launch_geometry(ctx->g64, ctx->N, cfg->radius, cfg->omega, cfg->rotation_axis, ctx->m64, ctx->qw, ctx->st), "geometry");
-  CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od) : prepare_stage<double>(od), "stage kernel attributes");
   if (ctx->prec == SWM_FP32_FUSED) {
     CKC(cudaMalloc(&ctx->m32, sizeof(float) * NMETRIC * ctx->fs), "alloc");
     CKC(launch_to_f32(ctx->m64, ctx->m32, NMETRIC * ctx->fs, ctx->st), "metric to f32");
@@ -554,6 +579,7 @@ void swm_ctx_destroy(swm_ctx* ctx) {
 int swm_ctx_synchronize(swm_ctx* ctx) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   CK(cudaStreamSynchronize(ctx->st), "synchronize");
+  if (int rc_ = check_device_flag(ctx)) return rc_;
   return SWM_OK;
 }
 
@@ -656,6 +682,7 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
     CK(cudaMemcpy2DAsync(dst[c], sizeof(double) * ctx->n, src[c], sizeof(double) * ctx->P,
                          sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToHost, ctx->st), "download");
   CK(cudaStreamSynchronize(ctx->st), "sync");
+  if (int rc_ = check_device_flag(ctx)) return rc_;
   return SWM_OK;
 }
 
@@ -903,6 +930,7 @@ int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
   CK(cudaMemcpy2DAsync(host, sizeof(double) * ctx->n, f->p, sizeof(double) * ctx->P, sizeof(double) * ctx->n,
                        (size_t)6 * ctx->n, cudaMemcpyDeviceToHost, ctx->st), "download");
   CK(cudaStreamSynchronize(ctx->st), "sync");
+  if (int rc_ = check_device_flag(ctx)) return rc_;
   return SWM_OK;
 }
 
@@ -974,6 +1002,7 @@ int swm_timing_enable(swm_ctx* ctx, int on) {
 int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches, double* edge_ms, long* edge_launches) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   CK(cudaStreamSynchronize(ctx->st), "sync");
+  if (int rc_ = check_device_flag(ctx)) return rc_;
   double ts = 0.0, te = 0.0;
   for (auto& e : ctx->ev_stage) { float ms; CK(cudaEventElapsedTime(&ms, e.first, e.second), "elapsed"); ts += ms; }
   for (auto& e : ctx->ev_edge) { float ms; CK(cudaEventElapsedTime(&ms, e.first, e.second), "elapsed"); te += ms; }

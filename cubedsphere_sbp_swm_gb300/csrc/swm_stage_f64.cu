@@ -1,4 +1,6 @@
-// swm_stage_f64.cu -- double instantiation of the fused stage and edge kernels.
+// swm_stage_f64.cu -- double instantiation of the fused stage kernel (plain
+// loads; the FP64 path is bound by the GPU's FP64 rate, not by HBM) and the
+// cube-edge kernel.
 #include "swm_launch.h"
 #include "swm_stage.cuh"
 
@@ -6,7 +8,9 @@ namespace swm {
 
 template <>
 cudaError_t launch_stage<double>(int order, const InstDev<double>& one, const InstDev<double>* many,
-                               const WorkUnit* units, int nunits, int mode, cudaStream_t st) {
+                                 const WorkUnit* units, int nunits, int mode, int* err,
+                                 cudaStream_t st) {
+  (void)err;
   switch (order) {
     case 21: return launch_stage_ord<double, 21>(one, many, units, nunits, mode, st);
     case 42: return launch_stage_ord<double, 42>(one, many, units, nunits, mode, st);
@@ -16,15 +20,32 @@ cudaError_t launch_stage<double>(int order, const InstDev<double>& one, const In
   }
 }
 
+template <class T, int ORD>
+static int v1_occupancy() {
+  int blocks = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_kernel<T, ORD>, STAGE_BW,
+                                                stage_smem_bytes<T, ORD>());
+  return blocks;
+}
+
 template <>
-cudaError_t prepare_stage<double>(int order) {
-  // set the dynamic shared-memory opt-in once, outside any stream capture
-  return launch_stage<double>(order, InstDev<double>{}, nullptr, nullptr, 0, MODE_APPLY, nullptr) ;
+cudaError_t prepare_stage<double>(int order, int* ctas_per_sm, int* cols) {
+  cudaError_t e = launch_stage<double>(order, InstDev<double>{}, nullptr, nullptr, 0, MODE_APPLY,
+                                       nullptr, nullptr);
+  if (e != cudaSuccess) return e;
+  switch (order) {
+    case 21: *ctas_per_sm = v1_occupancy<double, 21>(); break;
+    case 42: *ctas_per_sm = v1_occupancy<double, 42>(); break;
+    case 43: *ctas_per_sm = v1_occupancy<double, 43>(); break;
+    default: *ctas_per_sm = v1_occupancy<double, 63>(); break;
+  }
+  *cols = STAGE_BW;
+  return cudaGetLastError();
 }
 
 template <>
 cudaError_t launch_edge<double>(const InstDev<double>& one, const InstDev<double>* many, int ninst,
-                              int max_n, const Topology& tp, int mode, cudaStream_t st) {
+                                int max_n, const Topology& tp, int mode, cudaStream_t st) {
   const int nodes = 6 * (4 * max_n - 4);
   dim3 grid((nodes + 127) / 128, ninst);
   edge_kernel<double><<<grid, 128, 0, st>>>(one, many, tp, mode);
