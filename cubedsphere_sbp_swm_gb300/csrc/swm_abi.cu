@@ -177,7 +177,8 @@ struct swm_ctx {
   double* partial = nullptr; double* dres = nullptr; double* hres = nullptr;
   WorkUnit* units = nullptr; int nunits = 0;
   int* derr = nullptr;          // device error flag of the bounded waits
-  int num_sms = 0, ctas_per_sm = 0, stage_cols = 0;
+  int num_sms = 0;
+  StageShape shape{};           // launch shape of the fused stage kernel
   std::map<std::pair<void*, double>, GraphEntry> graphs;
   long graph_clock = 0;
   bool timing = false;
@@ -282,14 +283,70 @@ InstDev<T> base_inst(swm_ctx* c) {
   return I;
 }
 
+// cuTensorMapEncodeTiled, resolved once through the runtime's driver entry
+// point query (no link-time dependency on libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// 3-D map (column, row of the 6n panel rows, field) over nfields pitched
+// fields starting at base; box {boxw, rps, boxf}.
+template <class T>
+bool encode_fields(swm_ctx* c, CUtensorMap* m, const void* base, int nfields, int boxf) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !base) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)c->P, (cuuint64_t)6 * c->n, (cuuint64_t)nfields};
+  const cuuint64_t strides[2] = {(cuuint64_t)c->P * sizeof(T), (cuuint64_t)c->fs * sizeof(T)};
+  const cuuint32_t box[3] = {(cuuint32_t)c->shape.boxw, (cuuint32_t)c->shape.rps, (cuuint32_t)boxf};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+            const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps of one stage launch on instance I in mode `mode`.
+template <class T>
+int make_maps(swm_ctx* ctx, const InstDev<T>& I, int mode, StageMaps* m) {
+  std::memset(m, 0, sizeof(*m));
+  if (!ctx->shape.tma) return SWM_OK;
+  bool ok = encode_fields<T>(ctx, &m->met, I.metric, NMETRIC, 4);
+  ok = ok && encode_fields<T>(ctx, &m->metf, I.metric, NMETRIC, ctx->shape.nf);
+  ok = ok && encode_fields<T>(ctx, &m->in, I.in, 3, 3);
+  if (!ok) return fail(ctx, SWM_E_CUDA, "cuTensorMapEncodeTiled failed");
+  m->base = m->acc = m->lo = m->hs = m->met;
+  const T* b = (sizeof(T) == 4 && mode == MODE_RK4) ? I.base_out : I.base;
+  if (b && !encode_fields<T>(ctx, &m->base, b, 3, 3)) return fail(ctx, SWM_E_CUDA, "tensor map (base)");
+  if (I.acc && !encode_fields<T>(ctx, &m->acc, I.acc, 3, 3)) return fail(ctx, SWM_E_CUDA, "tensor map (acc)");
+  if (I.base_lo && !encode_fields<T>(ctx, &m->lo, I.base_lo, 3, 3)) return fail(ctx, SWM_E_CUDA, "tensor map (lo)");
+  if (I.hs && !encode_fields<T>(ctx, &m->hs, I.hs, 1, 1)) return fail(ctx, SWM_E_CUDA, "tensor map (hs)");
+  return SWM_OK;
+}
+
 template <class T>
 int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
+  StageMaps maps;
+  if (int rc = make_maps<T>(ctx, I, mode, &maps)) return rc;
   cudaEvent_t a = nullptr, b = nullptr;
   if (ctx->timing) {
     CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
-  CK(launch_stage<T>(ctx->order, I, nullptr, ctx->units, ctx->nunits, mode, ctx->derr, ctx->st),
+  CK(launch_stage<T>(ctx->order, &maps, I, nullptr, ctx->units, ctx->nunits, mode, ctx->derr,
+                     ctx->st),
      "stage kernel");
   if (ctx->timing) {
     CK(cudaEventRecord(b, ctx->st), "event record");
@@ -523,12 +580,16 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   CKC(cudaMalloc(&ctx->partial, sizeof(double) * REDUCE_BLOCKS), "alloc");
   CKC(cudaMalloc(&ctx->dres, sizeof(double) * 16), "alloc");
   CKC(cudaMallocHost(&ctx->hres, sizeof(double) * 16), "alloc host");
-  CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od, &ctx->ctas_per_sm, &ctx->stage_cols)
-                                  : prepare_stage<double>(od, &ctx->ctas_per_sm, &ctx->stage_cols),
+  CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od, &ctx->shape)
+                                  : prepare_stage<double>(od, &ctx->shape),
       "stage kernel attributes");
+  if (ctx->shape.tma && !encode_tiled()) {
+    free_ctx(ctx);
+    return fail(nullptr, SWM_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  }
   CKC(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device), "SM count");
-  if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->stage_cols,
-                  std::max(1, ctx->ctas_per_sm) * ctx->num_sms, units, why)) {
+  if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->shape.cols,
+                  std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms, units, why)) {
     free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
   }
   ctx->nunits = (int)units.size();

@@ -10,10 +10,32 @@
 //            pre-sync values of every panel-boundary node.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace swm {
+
+// TMA tensor maps of one fused-stage launch.  All are 3-D (column, panel row
+// over the 6n rows of all panels, field) over the pitched fields; entries a
+// launch does not use hold a copy of a valid map.
+struct StageMaps {
+  CUtensorMap in;    // stage input state   box {boxw, rps, 3}
+  CUtensorMap met;   // metric J, Qi1..3    box {boxw, rps, 4}
+  CUtensorMap metf;  // metric f (+rJ)      box {boxw, rps, 1 | 2}
+  CUtensorMap base;  // RK base state       box {boxw, rps, 3}
+  CUtensorMap acc;   // RK running sum      box {boxw, rps, 3}
+  CUtensorMap lo;    // FP32 state low part box {boxw, rps, 3}
+  CUtensorMap hs;    // orography           box {boxw, rps, 1}
+};
+
+// Launch shape of the fused stage kernel of one precision and SBP order.
+struct StageShape {
+  int ctas_per_sm;   // resident CTAs per SM
+  int cols;          // columns one CTA reads (threads of its consumer warps)
+  int tma;           // 1: TMA-pipelined kernel (needs StageMaps)
+  int boxw, rps, nf; // TMA box: columns, rows per stage, metric f fields
+};
 
 constexpr int MAXNE = 6;   // closure rows
 constexpr int MAXNW = 9;   // closure width

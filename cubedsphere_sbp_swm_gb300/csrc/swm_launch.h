@@ -6,16 +6,17 @@
 
 namespace swm {
 
-// Fused stage kernel over nunits work units (one CTA each); err is the
+// Fused stage kernel over nunits work units (one CTA each).  maps describes
+// the buffers of this launch to the TMA unit (TMA kernels only); err is the
 // device error flag raised by an expired bounded wait.
 template <class T>
-cudaError_t launch_stage(int order, const InstDev<T>& one, const InstDev<T>* many,
-                         const WorkUnit* units, int nunits, int mode, int* err, cudaStream_t st);
-// Sets the launch attributes of the stage kernel of one SBP order; called at
-// context creation, outside any stream capture.  Returns the resident CTAs
-// per SM through *ctas_per_sm and the columns one CTA can read through *cols.
+cudaError_t launch_stage(int order, const StageMaps* maps, const InstDev<T>& one,
+                         const InstDev<T>* many, const WorkUnit* units, int nunits, int mode,
+                         int* err, cudaStream_t st);
+// Sets the launch attributes of the stage kernel of one SBP order (called at
+// context creation, outside any stream capture) and returns its shape.
 template <class T>
-cudaError_t prepare_stage(int order, int* ctas_per_sm, int* cols);
+cudaError_t prepare_stage(int order, StageShape* shape);
 // Cube-edge kernel over ninst instances whose largest edge has max_n nodes.
 template <class T>
 cudaError_t launch_edge(const InstDev<T>& one, const InstDev<T>* many, int ninst, int max_n,

@@ -5,33 +5,40 @@
 
 namespace swm {
 
-constexpr int kNstF32 = 6;  // pipeline depth (rows in flight per CTA)
+constexpr int kRpsF32 = 2;  // rows per pipeline stage
+constexpr int kNstF32 = 3;  // pipeline stages
 
 template <>
-cudaError_t launch_stage<float>(int order, const InstDev<float>& one, const InstDev<float>* many,
-                                const WorkUnit* units, int nunits, int mode, int* err,
-                                cudaStream_t st) {
+cudaError_t launch_stage<float>(int order, const StageMaps* maps, const InstDev<float>& one,
+                                const InstDev<float>* many, const WorkUnit* units, int nunits,
+                                int mode, int* err, cudaStream_t st) {
+  static const StageMaps kNone{};
+  const StageMaps& m = maps ? *maps : kNone;
   switch (order) {
-    case 21: return launch_stage_tma_ord<float, 21, kNstF32>(one, many, units, nunits, mode, err, st);
-    case 42: return launch_stage_tma_ord<float, 42, kNstF32>(one, many, units, nunits, mode, err, st);
-    case 43: return launch_stage_tma_ord<float, 43, kNstF32>(one, many, units, nunits, mode, err, st);
-    case 63: return launch_stage_tma_ord<float, 63, kNstF32>(one, many, units, nunits, mode, err, st);
+    case 21: return launch_stage_tma_ord<float, 21, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
+    case 42: return launch_stage_tma_ord<float, 42, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
+    case 43: return launch_stage_tma_ord<float, 43, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
+    case 63: return launch_stage_tma_ord<float, 63, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <>
-cudaError_t prepare_stage<float>(int order, int* ctas_per_sm, int* cols) {
-  cudaError_t e = launch_stage<float>(order, InstDev<float>{}, nullptr, nullptr, 0, MODE_APPLY,
-                                      nullptr, nullptr);
+cudaError_t prepare_stage<float>(int order, StageShape* shape) {
+  cudaError_t e = launch_stage<float>(order, nullptr, InstDev<float>{}, nullptr, nullptr, 0,
+                                      MODE_APPLY, nullptr, nullptr);
   if (e != cudaSuccess) return e;
   switch (order) {
-    case 21: *ctas_per_sm = stage_tma_occupancy<float, 21, kNstF32>(); break;
-    case 42: *ctas_per_sm = stage_tma_occupancy<float, 42, kNstF32>(); break;
-    case 43: *ctas_per_sm = stage_tma_occupancy<float, 43, kNstF32>(); break;
-    default: *ctas_per_sm = stage_tma_occupancy<float, 63, kNstF32>(); break;
+    case 21: shape->ctas_per_sm = stage_tma_occupancy<float, 21, kRpsF32, kNstF32>(); break;
+    case 42: shape->ctas_per_sm = stage_tma_occupancy<float, 42, kRpsF32, kNstF32>(); break;
+    case 43: shape->ctas_per_sm = stage_tma_occupancy<float, 43, kRpsF32, kNstF32>(); break;
+    default: shape->ctas_per_sm = stage_tma_occupancy<float, 63, kRpsF32, kNstF32>(); break;
   }
-  *cols = TMA_CONS;
+  shape->cols = TMA_CONS;
+  shape->tma = 1;
+  shape->boxw = TmaLayout<float, 42, kRpsF32, kNstF32>::BOXW;
+  shape->rps = kRpsF32;
+  shape->nf = TmaLayout<float, 42, kRpsF32, kNstF32>::NF;
   return cudaGetLastError();
 }
 

@@ -7,10 +7,11 @@
 namespace swm {
 
 template <>
-cudaError_t launch_stage<double>(int order, const InstDev<double>& one, const InstDev<double>* many,
-                                 const WorkUnit* units, int nunits, int mode, int* err,
-                                 cudaStream_t st) {
+cudaError_t launch_stage<double>(int order, const StageMaps* maps, const InstDev<double>& one,
+                                 const InstDev<double>* many, const WorkUnit* units, int nunits,
+                                 int mode, int* err, cudaStream_t st) {
   (void)err;
+  (void)maps;
   switch (order) {
     case 21: return launch_stage_ord<double, 21>(one, many, units, nunits, mode, st);
     case 42: return launch_stage_ord<double, 42>(one, many, units, nunits, mode, st);
@@ -29,9 +30,10 @@ static int v1_occupancy() {
 }
 
 template <>
-cudaError_t prepare_stage<double>(int order, int* ctas_per_sm, int* cols) {
-  cudaError_t e = launch_stage<double>(order, InstDev<double>{}, nullptr, nullptr, 0, MODE_APPLY,
-                                       nullptr, nullptr);
+cudaError_t prepare_stage<double>(int order, StageShape* shape) {
+  cudaError_t e = launch_stage<double>(order, nullptr, InstDev<double>{}, nullptr, nullptr, 0,
+                                       MODE_APPLY, nullptr, nullptr);
+  int* ctas_per_sm = &shape->ctas_per_sm;
   if (e != cudaSuccess) return e;
   switch (order) {
     case 21: *ctas_per_sm = v1_occupancy<double, 21>(); break;
@@ -39,7 +41,9 @@ cudaError_t prepare_stage<double>(int order, int* ctas_per_sm, int* cols) {
     case 43: *ctas_per_sm = v1_occupancy<double, 43>(); break;
     default: *ctas_per_sm = v1_occupancy<double, 63>(); break;
   }
-  *cols = STAGE_BW;
+  shape->cols = STAGE_BW;
+  shape->tma = 0;
+  shape->boxw = shape->rps = shape->nf = 0;
   return cudaGetLastError();
 }
 
