@@ -5,9 +5,6 @@
 
 namespace swm {
 
-constexpr int kRpsF32 = 2;  // rows per pipeline stage
-constexpr int kNstF32 = 3;  // pipeline stages
-
 template <>
 cudaError_t launch_stage<float>(int order, const StageMaps* maps, const InstDev<float>& one,
                                 const InstDev<float>* many, const WorkUnit* units, int nunits,
@@ -15,30 +12,30 @@ cudaError_t launch_stage<float>(int order, const StageMaps* maps, const InstDev<
   static const StageMaps kNone{};
   const StageMaps& m = maps ? *maps : kNone;
   switch (order) {
-    case 21: return launch_stage_tma_ord<float, 21, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
-    case 42: return launch_stage_tma_ord<float, 42, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
-    case 43: return launch_stage_tma_ord<float, 43, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
-    case 63: return launch_stage_tma_ord<float, 63, kRpsF32, kNstF32>(m, one, many, units, nunits, mode, err, st);
+    case 21: return launch_stage_tma_ord<float, 21>(m, one, many, units, nunits, mode, err, st);
+    case 42: return launch_stage_tma_ord<float, 42>(m, one, many, units, nunits, mode, err, st);
+    case 43: return launch_stage_tma_ord<float, 43>(m, one, many, units, nunits, mode, err, st);
+    case 63: return launch_stage_tma_ord<float, 63>(m, one, many, units, nunits, mode, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <>
 cudaError_t prepare_stage<float>(int order, StageShape* shape) {
-  cudaError_t e = launch_stage<float>(order, nullptr, InstDev<float>{}, nullptr, nullptr, 0,
-                                      MODE_APPLY, nullptr, nullptr);
-  if (e != cudaSuccess) return e;
+  cudaError_t e;
   switch (order) {
-    case 21: shape->ctas_per_sm = stage_tma_occupancy<float, 21, kRpsF32, kNstF32>(); break;
-    case 42: shape->ctas_per_sm = stage_tma_occupancy<float, 42, kRpsF32, kNstF32>(); break;
-    case 43: shape->ctas_per_sm = stage_tma_occupancy<float, 43, kRpsF32, kNstF32>(); break;
-    default: shape->ctas_per_sm = stage_tma_occupancy<float, 63, kRpsF32, kNstF32>(); break;
+    case 21: e = prepare_stage_tma_ord<float, 21>(&shape->ctas_per_sm); break;
+    case 42: e = prepare_stage_tma_ord<float, 42>(&shape->ctas_per_sm); break;
+    case 43: e = prepare_stage_tma_ord<float, 43>(&shape->ctas_per_sm); break;
+    case 63: e = prepare_stage_tma_ord<float, 63>(&shape->ctas_per_sm); break;
+    default: return cudaErrorInvalidValue;
   }
+  if (e != cudaSuccess) return e;
   shape->cols = TMA_CONS;
   shape->tma = 1;
-  shape->boxw = TmaLayout<float, 42, kRpsF32, kNstF32>::BOXW;
-  shape->rps = kRpsF32;
-  shape->nf = TmaLayout<float, 42, kRpsF32, kNstF32>::NF;
+  shape->boxw = TmaLayout<float, 42>::BOXW;
+  shape->rps = TmaLayout<float, 42>::RPS;
+  shape->nf = TmaLayout<float, 42>::NF;
   return cudaGetLastError();
 }
 

@@ -10,6 +10,8 @@
 // behind -- completing on an mbarrier.  Four consumer warps (one thread per
 // column) turn each landed row into the derived stencil fields (KE, u, v,
 // J h ut, J h vt in a shared-memory ring) and finish one row per landed row.
+// Interior nodes take a branch-free path with the interior stencil; the SBP
+// boundary closures and the panel-edge bookkeeping run on a separate path.
 // Every mbarrier wait is bounded: on expiry the kernel raises the device
 // error flag, stops waiting, still passes every barrier, and drains its
 // copies before exit.
@@ -86,14 +88,18 @@ constexpr int TMA_THREADS = TMA_CONS + 32;        // + one producer warp
 enum { W_KE = 0, W_U, W_V, W_GU, W_GV, NW_FIELDS };   // stencil (wide) ring
 enum { N_UT = 0, N_VT, N_J, NN_FIELDS };              // own-node (narrow) ring
 
-template <class T, int ORD, int RPS, int NST>
+constexpr int pow2_at_least(int v) { return v <= 1 ? 1 : 2 * pow2_at_least((v + 1) / 2); }
+
+template <class T, int ORD>
 struct TmaLayout {
+  static constexpr int RPS = 2;              // rows per pipeline stage
+  static constexpr int NST = 2;              // pipeline stages
   static constexpr int RMAX = Ord<ORD>::RMAX;
-  static constexpr int RBW = 2 * RMAX + 2;   // written row r, read rows r-2RMAX..r
-  static constexpr int RBN = RMAX + 2;       // written row r, read at row r+RMAX
+  static constexpr int RBW = pow2_at_least(2 * RMAX + 2);  // rows r-2RMAX..r live
+  static constexpr int RBN = pow2_at_least(RMAX + 2);      // row r read at r+RMAX
   static constexpr int ALIGN = 16 / (int)sizeof(T);
   static constexpr int BOXW = TMA_CONS + ALIGN;  // columns per box (16-byte multiple)
-  static constexpr int NF = sizeof(T) == 8 ? 2 : 1;  // f (+ rJ)
+  static constexpr int NF = 2;                   // metric f, rJ of the finished rows
   static constexpr size_t r128(size_t b) { return (b + 127) / 128 * 128; }
   static constexpr size_t row_bytes = sizeof(T) * BOXW * RPS;  // one field, RPS rows
   static constexpr size_t b_in = r128(3 * row_bytes), b_met = r128(4 * row_bytes),
@@ -110,12 +116,21 @@ struct TmaLayout {
   static_assert(BOXW <= 256 && RPS <= 256, "TMA box limits");
 };
 
-template <class T, int ORD, int RPS, int NST>
+template <class T, int ORD, int MODE>
 __global__ void __launch_bounds__(TMA_THREADS)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
-                     const InstDev<T>* many, const WorkUnit* units, int mode, int* err) {
-  using L = TmaLayout<T, ORD, RPS, NST>;
-  constexpr int RMAX = L::RMAX, RBW = L::RBW, RBN = L::RBN, BOXW = L::BOXW, AL = L::ALIGN;
+                     const InstDev<T>* many, const WorkUnit* units, int* err) {
+  using L = TmaLayout<T, ORD>;
+  constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, BOXW = L::BOXW, AL = L::ALIGN;
+  constexpr int MW = L::RBW - 1, MN = L::RBN - 1;
+  constexpr int RSW = NW_FIELDS * TMA_CONS, RSN = NN_FIELDS * TMA_CONS;  // ring slot strides
+  constexpr int NE = Ord<ORD>::NE;
+  constexpr bool FP32 = sizeof(T) == 4;
+  constexpr bool needB = MODE == MODE_RK1 || MODE == MODE_RK2 || MODE == MODE_RK3 ||
+                         (FP32 && MODE == MODE_RK4);
+  constexpr bool needA = MODE == MODE_RK2 || MODE == MODE_RK3 || MODE == MODE_RK4;
+  constexpr bool needL = FP32 && MODE == MODE_RK4;
+
   extern __shared__ unsigned char smem_dyn[];
   // 128-byte aligned base (TMA tensor destinations)
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -130,18 +145,11 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const WorkUnit wu = units[blockIdx.x];
   const InstDev<T>& I = many ? many[wu.inst] : one;
   const int n = I.n, P = I.P;
-  const long long fs = I.fs;
-  const long long pbase = (long long)wu.panel * I.ps;
+  const int rl0 = wu.rl0, rl1 = wu.rl1, j0u = wu.j0, j1u = wu.j1;
   const int tid = threadIdx.x;
   const int cal = wu.cl0 & ~(AL - 1);         // 16-byte aligned box start column
-  const int off = wu.cl0 - cal;
   const int prow = wu.panel * n;              // row of this panel in the (6n)-row tensors
-  const int nch = (wu.j1 + RMAX - wu.rl0 + RPS - 1) / RPS;
-  const bool fp32 = sizeof(T) == 4;
-  const bool needB = mode == MODE_RK1 || mode == MODE_RK2 || mode == MODE_RK3 ||
-                     (fp32 && mode == MODE_RK4);
-  const bool needA = mode == MODE_RK2 || mode == MODE_RK3 || mode == MODE_RK4;
-  const bool needL = fp32 && mode == MODE_RK4;
+  const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
   const bool hasHs = I.hs != nullptr;
 
   if (tid == 0) {
@@ -167,9 +175,9 @@ __global__ void __launch_bounds__(TMA_THREADS)
           atomicExch(err, 1);
           break;
         }
-        const int r0 = wu.rl0 + c * RPS, j0 = r0 - RMAX;
-        const bool in_any = r0 < wu.rl1;
-        const bool out_any = j0 + RPS > wu.j0 && j0 < wu.j1;
+        const int r0 = rl0 + c * RPS, j0 = r0 - RMAX;
+        const bool in_any = r0 < rl1;
+        const bool out_any = j0 + RPS > j0u && j0 < j1u;
         uint32_t tx = 0;
         if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * (uint32_t)L::row_bytes;
         if (out_any)
@@ -203,67 +211,83 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const int col = wu.cl0 + t;
   const bool ld = col < wu.cl1;
   const bool own = col >= wu.i0 && col < wu.i1;
-  const int x = t + off;                   // column inside a box row
-  const T grav = I.grav;
+  const bool xint = col >= NE && col < n - NE;   // interior stencil along the row
+  const int x = t + (wu.cl0 - cal);               // column inside a box row
+  const T grav = I.grav, ghs = I.ghs, c_in = I.c_in, c_acc = I.c_acc;
+  const int fs = (int)I.fs;
+  const int gcol = (int)((long long)wu.panel * I.ps) + col;  // node (col, 0) of this panel
+  T* const outp = I.out;
+  T* const accp = I.acc;
+  T* const bop = I.base_out;
+  T* const blp = I.base_lo;
   for (int c = 0; c < nch; ++c) {
     const int s = c % NST;
     const uint32_t ph = (uint32_t)(c / NST) & 1u;
     bool ok = true;
     if (!*abort_flag) ok = mbar_wait_bounded(&full[s], ph, kWaitLimitNs);
     if (!ok) { *abort_flag = 1; atomicExch(err, 3); }
-    const unsigned char* sb = stg + (size_t)s * L::stage;
-    // element (field f, box row q) of a box at byte offset o
+    const T* sb = reinterpret_cast<const T*>(stg + (size_t)s * L::stage);
+    // element (field f, box row q) of the box at byte offset o
     auto bx = [&](size_t o, int f, int q) {
-      return reinterpret_cast<const T*>(sb + o)[(f * RPS + q) * BOXW + x];
+      return sb[o / sizeof(T) + (f * RPS + q) * BOXW + x];
     };
-#pragma unroll 1
+#pragma unroll
     for (int q = 0; q < RPS; ++q) {
-      const int r = wu.rl0 + c * RPS + q, j = r - RMAX;
-      if (ok && r < wu.rl1 && ld) {
+      const int r = rl0 + c * RPS + q, j = r - RMAX;
+      if (ok && r < rl1 && ld) {
         const T h = bx(L::o_in, 0, q), u = bx(L::o_in, 1, q), v = bx(L::o_in, 2, q);
         const T J = bx(L::o_met, 0, q);
         const T q1 = bx(L::o_met, 1, q), q2 = bx(L::o_met, 2, q), q3 = bx(L::o_met, 3, q);
         const T ut = q1 * u + q2 * v;
         const T vt = q2 * u + q3 * v;
-        T ke = (u * ut + v * vt) / T(2.0);
+        T ke = (u * ut + v * vt) * T(0.5);
         ke = ke + grav * h;
         if (hasHs) ke = ke + grav * bx(L::o_hs, 0, q);
-        T* w = wide + (size_t)(r % RBW) * NW_FIELDS * TMA_CONS;
-        w[W_KE * TMA_CONS + t] = ke;
-        w[W_U * TMA_CONS + t] = u;
-        w[W_V * TMA_CONS + t] = v;
-        w[W_GU * TMA_CONS + t] = J * (h * ut);
-        w[W_GV * TMA_CONS + t] = J * (h * vt);
-        T* nr = narrow + (size_t)(r % RBN) * NN_FIELDS * TMA_CONS;
-        nr[N_UT * TMA_CONS + t] = ut;
-        nr[N_VT * TMA_CONS + t] = vt;
-        nr[N_J * TMA_CONS + t] = J;
+        T* w = wide + (r & MW) * RSW + t;
+        w[W_KE * TMA_CONS] = ke;
+        w[W_U * TMA_CONS] = u;
+        w[W_V * TMA_CONS] = v;
+        w[W_GU * TMA_CONS] = J * (h * ut);
+        w[W_GV * TMA_CONS] = J * (h * vt);
+        T* nr = narrow + (r & MN) * RSN + t;
+        nr[N_UT * TMA_CONS] = ut;
+        nr[N_VT * TMA_CONS] = vt;
+        nr[N_J * TMA_CONS] = J;
       }
       consumers_sync();
-      if (*abort_flag || !own || j < wu.j0 || j >= wu.j1) continue;
-      const T* wj = wide + (size_t)(j % RBW) * NW_FIELDS * TMA_CONS;
-      auto xa = [&](int f) {
-        return d_line<ORD, T>(col, n, [&](int m) { return wj[f * TMA_CONS + (m - wu.cl0)]; });
-      };
-      auto ya = [&](int f) {
-        return d_line<ORD, T>(j, n, [&](int m) {
-          return wide[(size_t)(m % RBW) * NW_FIELDS * TMA_CONS + f * TMA_CONS + t];
-        });
-      };
-      const T dxke = xa(W_KE), dyke = ya(W_KE);
-      const T dxv = xa(W_V), dyu = ya(W_U);
-      const T dxgu = xa(W_GU), dygv = ya(W_GV);
-      const T* nj = narrow + (size_t)(j % RBN) * NN_FIELDS * TMA_CONS;
-      const T J = nj[N_J * TMA_CONS + t];
-      T rJ;
-      if constexpr (sizeof(T) == 8) rJ = bx(L::o_metf, 1, q);
-      else rJ = I.ghs / J;
-      const T gx = dxke * I.ghs, gy = dyke * I.ghs;
+      if (*abort_flag || !own || j < j0u || j >= j1u) continue;
+      const T* wj = wide + (j & MW) * RSW + t;      // this thread's column in row j
+      T dxke, dyke, dxv, dyu, dxgu, dygv;
+      const bool yint = j >= NE && j < n - NE;
+      if (xint && yint) {
+        auto X = [&](int f) {
+          return d_interior<ORD, T>([&](int o) { return wj[f * TMA_CONS + o]; });
+        };
+        auto Y = [&](int f) {
+          return d_interior<ORD, T>(
+              [&](int o) { return wide[((j + o) & MW) * RSW + f * TMA_CONS + t]; });
+        };
+        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
+        dyke = Y(W_KE); dyu = Y(W_U); dygv = Y(W_GV);
+      } else {
+        auto X = [&](int f) {
+          return d_line<ORD, T>(col, n, [&](int m) { return wj[f * TMA_CONS + (m - col)]; });
+        };
+        auto Y = [&](int f) {
+          return d_line<ORD, T>(j, n,
+                                [&](int m) { return wide[(m & MW) * RSW + f * TMA_CONS + t]; });
+        };
+        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
+        dyke = Y(W_KE); dyu = Y(W_U); dygv = Y(W_GV);
+      }
+      const T* nj = narrow + (j & MN) * RSN + t;
+      const T J = nj[N_J * TMA_CONS];
+      const T rJ = bx(L::o_metf, 1, q);
+      const T gx = dxke * ghs, gy = dyke * ghs;
       const T zeta = (dxv - dyu) * rJ;
       const T dv = (dxgu + dygv) * rJ;
-      const long long idx = pbase + (long long)j * P + col;
-      if ((col == 0) | (col == n - 1) | (j == 0) | (j == n - 1)) {
-        T* E = I.edge + (long long)wu.panel * 16 * n;
+      if (!(xint && yint) && ((col == 0) | (col == n - 1) | (j == 0) | (j == n - 1))) {
+        T* E = I.edge + wu.panel * 16 * n;
         const T vals[4] = {gx, gy, zeta, dv};
         if (col == 0)
 #pragma unroll
@@ -280,39 +304,40 @@ __global__ void __launch_bounds__(TMA_THREADS)
         continue;
       }
       T kk[3];
-      node_tendency<T>(gx, gy, zeta, dv, bx(L::o_metf, 0, q), J, nj[N_UT * TMA_CONS + t],
-                       nj[N_VT * TMA_CONS + t], kk[0], kk[1], kk[2]);
+      node_tendency<T>(gx, gy, zeta, dv, bx(L::o_metf, 0, q), J, nj[N_UT * TMA_CONS],
+                       nj[N_VT * TMA_CONS], kk[0], kk[1], kk[2]);
+      const int g = gcol + j * P;
 #pragma unroll
       for (int cc = 0; cc < 3; ++cc) {
-        const long long o = cc * fs + idx;
-        if (mode == MODE_APPLY) {
-          I.out[o] = kk[cc];
-        } else if constexpr (sizeof(T) == 8) {
-          if (mode == MODE_RK1) {
+        const int o = cc * fs + g;
+        if constexpr (MODE == MODE_APPLY) {
+          outp[o] = kk[cc];
+        } else if constexpr (!FP32) {
+          if constexpr (MODE == MODE_RK1) {
             const T b = bx(L::o_base, cc, q);
-            I.out[o] = T(1.0) * b + I.c_in * kk[cc];
-            I.acc[o] = b + I.c_acc * kk[cc];
-          } else if (mode == MODE_RK4) {
-            I.base_out[o] = bx(L::o_acc, cc, q) + I.c_acc * kk[cc];
+            outp[o] = T(1.0) * b + c_in * kk[cc];
+            accp[o] = b + c_acc * kk[cc];
+          } else if constexpr (MODE == MODE_RK4) {
+            bop[o] = bx(L::o_acc, cc, q) + c_acc * kk[cc];
           } else {
-            I.out[o] = T(1.0) * bx(L::o_base, cc, q) + I.c_in * kk[cc];
-            I.acc[o] = bx(L::o_acc, cc, q) + I.c_acc * kk[cc];
+            outp[o] = T(1.0) * bx(L::o_base, cc, q) + c_in * kk[cc];
+            accp[o] = bx(L::o_acc, cc, q) + c_acc * kk[cc];
           }
         } else {
-          if (mode == MODE_RK1) {
-            I.out[o] = bx(L::o_base, cc, q) + I.c_in * kk[cc];
-            I.acc[o] = I.c_acc * kk[cc];
-          } else if (mode == MODE_RK4) {
-            const T d = bx(L::o_acc, cc, q) + I.c_acc * kk[cc];
+          if constexpr (MODE == MODE_RK1) {
+            outp[o] = bx(L::o_base, cc, q) + c_in * kk[cc];
+            accp[o] = c_acc * kk[cc];
+          } else if constexpr (MODE == MODE_RK4) {
+            const T d = bx(L::o_acc, cc, q) + c_acc * kk[cc];
             const T hi = bx(L::o_base, cc, q), lo = bx(L::o_lo, cc, q);
             const T tt = lo + d;
             const T sm = hi + tt;
             const T bb = sm - hi;
-            I.base_out[o] = sm;
-            I.base_lo[o] = (hi - (sm - bb)) + (tt - bb);
+            bop[o] = sm;
+            blp[o] = (hi - (sm - bb)) + (tt - bb);
           } else {
-            I.out[o] = bx(L::o_base, cc, q) + I.c_in * kk[cc];
-            I.acc[o] = bx(L::o_acc, cc, q) + I.c_acc * kk[cc];
+            outp[o] = bx(L::o_base, cc, q) + c_in * kk[cc];
+            accp[o] = bx(L::o_acc, cc, q) + c_acc * kk[cc];
           }
         }
       }
@@ -322,30 +347,48 @@ __global__ void __launch_bounds__(TMA_THREADS)
   }
 }
 
-template <class T, int ORD, int RPS, int NST>
-cudaError_t launch_stage_tma_ord(const StageMaps& maps, const InstDev<T>& one,
-                                 const InstDev<T>* many, const WorkUnit* units, int nunits,
-                                 int mode, int* err, cudaStream_t st) {
-  constexpr size_t smem = TmaLayout<T, ORD, RPS, NST>::bytes;
+template <class T, int ORD, int MODE>
+cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
+                                  const InstDev<T>* many, const WorkUnit* units, int nunits,
+                                  int* err, cudaStream_t st) {
+  constexpr size_t smem = TmaLayout<T, ORD>::bytes;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, RPS, NST>,
+    cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   if (nunits <= 0) return cudaSuccess;
-  stage_tma_kernel<T, ORD, RPS, NST><<<nunits, TMA_THREADS, smem, st>>>(maps, one, many, units,
-                                                                         mode, err);
+  stage_tma_kernel<T, ORD, MODE><<<nunits, TMA_THREADS, smem, st>>>(maps, one, many, units, err);
   return cudaGetLastError();
 }
 
-template <class T, int ORD, int RPS, int NST>
-int stage_tma_occupancy() {
-  int blocks = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_tma_kernel<T, ORD, RPS, NST>,
-                                                TMA_THREADS, TmaLayout<T, ORD, RPS, NST>::bytes);
-  return blocks;
+template <class T, int ORD>
+cudaError_t launch_stage_tma_ord(const StageMaps& maps, const InstDev<T>& one,
+                                 const InstDev<T>* many, const WorkUnit* units, int nunits,
+                                 int mode, int* err, cudaStream_t st) {
+  switch (mode) {
+    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY>(maps, one, many, units, nunits, err, st);
+    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1>(maps, one, many, units, nunits, err, st);
+    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2>(maps, one, many, units, nunits, err, st);
+    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3>(maps, one, many, units, nunits, err, st);
+    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4>(maps, one, many, units, nunits, err, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// configure every mode; returns resident CTAs per SM
+template <class T, int ORD>
+cudaError_t prepare_stage_tma_ord(int* ctas_per_sm) {
+  static const StageMaps kNone{};
+  for (int m = MODE_APPLY; m <= MODE_RK4; ++m) {
+    cudaError_t e = launch_stage_tma_ord<T, ORD>(kNone, InstDev<T>{}, nullptr, nullptr, 0, m,
+                                                 nullptr, nullptr);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      ctas_per_sm, stage_tma_kernel<T, ORD, MODE_RK2>, TMA_THREADS, TmaLayout<T, ORD>::bytes);
 }
 
 }  // namespace swm
