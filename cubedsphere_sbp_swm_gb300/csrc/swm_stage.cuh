@@ -377,32 +377,68 @@ __device__ __forceinline__ void boundary_node(int b, int n, int& i, int& j) {
 template <class T>
 __global__ void edge_kernel(InstDev<T> one, const InstDev<T>* many, Topology tp, int mode) {
   const InstDev<T>& I = many ? many[blockIdx.y] : one;
-  const int n = I.n, nb = 4 * n - 4;
+  const int n = I.n, nb = 4 * n - 4, e = n - 1;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= 6 * nb) return;
   const int p = g / nb;
   int i, j;
   boundary_node(g - p * nb, n, i, j);
-  const EdgeView<T> ev{I.edge, n};
-  // own pre-sync values: read from a side the node lies on
-  int side, k;
-  if (j == 0) { side = SIDE_B; k = i; }
-  else if (j == n - 1) { side = SIDE_T; k = i; }
-  else if (i == 0) { side = SIDE_L; k = j; }
-  else { side = SIDE_R; k = j; }
-  T gx = ev.get(p, side, EV_GX, k), gy = ev.get(p, side, EV_GY, k);
-  const T zo = ev.get(p, side, EV_ZETA, k), dvo = ev.get(p, side, EV_DIV, k);
-  sync_vector_node<T>(ev, tp, I.qw, p, i, j, gx, gy);
-  const T zeta = sync_scalar_node<T>(ev, tp, p, i, j, EV_ZETA, zo);
-  const T dv = sync_scalar_node<T>(ev, tp, p, i, j, EV_DIV, dvo);
-
+  // The node lies on a left/right side (lr), a bottom/top side (bt), or both
+  // (cube corner).  Every address below is known before any load, so all
+  // loads of the node issue together.
+  const bool lr = (i == 0) | (i == e), bt = (j == 0) | (j == e);
+  const int sLR = i == 0 ? SIDE_L : SIDE_R, sBT = j == 0 ? SIDE_B : SIDE_T;
+  const EdgeLink LL = tp.link[p][sLR], LB = tp.link[p][sBT];
+  const T* E = I.edge;
+  auto at = [&](int q, int s, int v, int k) { return E[((q * 4 + s) * 4 + v) * n + k]; };
+  const int so = lr ? sLR : sBT, ko = lr ? j : i;          // own values
+  const int kl = LL.rev ? e - j : j, kb = LB.rev ? e - i : i;  // neighbour positions
+  T own[4], nl[4], nbt[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    own[v] = at(p, so, v, ko);
+    nl[v] = lr ? at(LL.q, LL.side_q, v, kl) : T(0);
+    nbt[v] = bt ? at(LB.q, LB.side_q, v, kb) : T(0);
+  }
+  const double* qw = I.qw;
+  const T qlr = lr ? T(qw[(i == 0 ? 2 : 3) * n + j]) : T(0);   // ql / qr at j
+  const T qbt = bt ? T(qw[(j == 0 ? 0 : 1) * n + i]) : T(0);   // qb / qt at i
   const long long fs = I.fs;
   const long long idx = (long long)p * I.ps + (long long)j * I.P + i;
   const T u = I.in[fs + idx], v = I.in[2 * fs + idx];
   const T q1 = I.metric[MQI1 * fs + idx], q2 = I.metric[MQI2 * fs + idx],
           q3 = I.metric[MQI3 * fs + idx];
-  const T ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
   const T J = I.metric[MJ * fs + idx], f = I.metric[MF * fs + idx];
+
+  // neighbour vectors in this panel's frame (pack_to_buf_vec component map)
+  auto rot = [](const EdgeLink& L, T gxq, T gyq, T& rx, T& ry) {
+    if (L.dim_i) { rx = T(L.istep) * gxq; ry = T(L.jstep) * gyq; }
+    else { rx = T(L.jstep) * gyq; ry = T(L.istep) * gxq; }
+  };
+  T rx, ry, sx, sy;
+  rot(LL, nl[EV_GX], nl[EV_GY], rx, ry);
+  rot(LB, nbt[EV_GX], nbt[EV_GY], sx, sy);
+  const T U = own[EV_GY], V = own[EV_GX];
+  T gx, gy, zeta, dv;
+  if (lr && bt) {
+    // cube corner: 3-way averages (halo_Ah_scalar_sync_mod.f90:56-85,
+    // ecs_Ah_vec_sync_mod.f90:77-100)
+    gy = (U + ry + sy + qbt * sx) / T(3.0);
+    gx = (V + rx + sx + qlr * ry) / T(3.0);
+    zeta = (own[EV_ZETA] + nl[EV_ZETA] + nbt[EV_ZETA]) / T(3.0);
+    dv = (own[EV_DIV] + nl[EV_DIV] + nbt[EV_DIV]) / T(3.0);
+  } else if (lr) {
+    gy = T(0.5) * (U + ry);
+    gx = T(0.5) * (V + rx + qlr * ry);
+    zeta = T(0.5) * (own[EV_ZETA] + nl[EV_ZETA]);
+    dv = T(0.5) * (own[EV_DIV] + nl[EV_DIV]);
+  } else {
+    gx = T(0.5) * (V + sx);
+    gy = T(0.5) * (U + sy + qbt * sx);
+    zeta = T(0.5) * (own[EV_ZETA] + nbt[EV_ZETA]);
+    dv = T(0.5) * (own[EV_DIV] + nbt[EV_DIV]);
+  }
+  const T ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
   T kh, ku, kv;
   node_tendency<T>(gx, gy, zeta, dv, f, J, ut, vt, kh, ku, kv);
   stage_epilogue<T>(I, mode, idx, kh, ku, kv);

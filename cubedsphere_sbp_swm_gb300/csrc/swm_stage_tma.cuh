@@ -90,10 +90,17 @@ enum { N_UT = 0, N_VT, N_J, NN_FIELDS };              // own-node (narrow) ring
 
 constexpr int pow2_at_least(int v) { return v <= 1 ? 1 : 2 * pow2_at_least((v + 1) / 2); }
 
+#ifndef SWM_TMA_RPS
+#define SWM_TMA_RPS 2
+#endif
+#ifndef SWM_TMA_NST
+#define SWM_TMA_NST 2
+#endif
+
 template <class T, int ORD>
 struct TmaLayout {
-  static constexpr int RPS = 2;              // rows per pipeline stage
-  static constexpr int NST = 2;              // pipeline stages
+  static constexpr int RPS = SWM_TMA_RPS;    // rows per pipeline stage
+  static constexpr int NST = SWM_TMA_NST;    // pipeline stages
   static constexpr int RMAX = Ord<ORD>::RMAX;
   static constexpr int RBW = pow2_at_least(2 * RMAX + 2);  // rows r-2RMAX..r live
   static constexpr int RBN = pow2_at_least(RMAX + 2);      // row r read at r+RMAX
