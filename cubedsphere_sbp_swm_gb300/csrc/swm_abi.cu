@@ -274,6 +274,7 @@ template <class T>
 InstDev<T> base_inst(swm_ctx* c) {
   InstDev<T> I{};
   I.n = c->n; I.P = c->P; I.ps = c->ps; I.fs = c->fs;
+  I.boxw = c->shape.boxw;
   I.metric = (c->prec == SWM_FP32_FUSED) ? (const T*)(const void*)c->m32 : (const T*)(const void*)c->m64;
   I.qw = c->qw;
   I.hs = (const T*)c->hsT;
@@ -593,6 +594,20 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
   }
   ctx->nunits = (int)units.size();
+  if (ctx->shape.tma) {
+    // narrowest TMA box that covers every unit's columns from its aligned start
+    const int al = 16 / ctx->elt;
+    int bw = al;
+    for (const WorkUnit& w : units) {
+      const int cal = w.cl0 & ~(al - 1);
+      bw = std::max(bw, (w.cl1 - cal + al - 1) / al * al);
+    }
+    if (bw > ctx->shape.boxw) {
+      free_ctx(ctx);
+      return fail(nullptr, SWM_E_INVALID, "work split exceeds the TMA box");
+    }
+    ctx->shape.boxw = bw;
+  }
   CKC(cudaMalloc(&ctx->derr, sizeof(int)), "alloc");
   CKC(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st), "memset");
   CKC(cudaMalloc(&ctx->units, sizeof(WorkUnit) * units.size()), "alloc");

@@ -157,6 +157,7 @@ struct WorkUnit {
 template <class T>
 struct InstDev {
   int n, P;
+  int boxw;                   // TMA box width (columns) of this instance's strips
   long long ps, fs;           // panel stride n*P, field stride 6*n*P
   const T* metric;            // NMETRIC fields
   const double* qw;           // sync weights qb, qt, ql, qr (4*n, FP64)

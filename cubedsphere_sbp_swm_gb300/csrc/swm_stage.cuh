@@ -126,6 +126,48 @@ __device__ __forceinline__ void stage_epilogue(const InstDev<T>& I, int mode, lo
   }
 }
 
+// The same epilogue with the RK inputs already loaded: rb = base (FP32 RK4:
+// the state's high part), ra = running sum, rl = state's low part.
+template <class T>
+__device__ __forceinline__ void stage_epilogue_pre(const InstDev<T>& I, int mode, long long idx,
+                                                   T kh, T ku, T kv, const T* rb, const T* ra,
+                                                   const T* rl) {
+  const long long fs = I.fs;
+  const T kk[3] = {kh, ku, kv};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const long long o = c * fs + idx;
+    if (mode == MODE_APPLY) {
+      I.out[o] = kk[c];
+    } else if (sizeof(T) == 8) {
+      if (mode == MODE_RK1) {
+        I.out[o] = T(1.0) * rb[c] + I.c_in * kk[c];
+        I.acc[o] = rb[c] + I.c_acc * kk[c];
+      } else if (mode == MODE_RK4) {
+        I.base_out[o] = ra[c] + I.c_acc * kk[c];
+      } else {
+        I.out[o] = T(1.0) * rb[c] + I.c_in * kk[c];
+        I.acc[o] = ra[c] + I.c_acc * kk[c];
+      }
+    } else {
+      if (mode == MODE_RK1) {
+        I.out[o] = rb[c] + I.c_in * kk[c];
+        I.acc[o] = I.c_acc * kk[c];
+      } else if (mode == MODE_RK4) {
+        const T d = ra[c] + I.c_acc * kk[c];
+        const T t = rl[c] + d;
+        const T s = rb[c] + t;
+        const T bb = s - rb[c];
+        I.base_out[o] = s;
+        I.base_lo[o] = (rb[c] - (s - bb)) + (t - bb);
+      } else {
+        I.out[o] = rb[c] + I.c_in * kk[c];
+        I.acc[o] = ra[c] + I.c_acc * kk[c];
+      }
+    }
+  }
+}
+
 // Coriolis + tendency at a node, given the synced gx, gy, zeta, div.
 // cor_u = (f+zeta)*hv/h*J with hv/h = vt (coriolis_colocated_mod.f90:93-100).
 template <class T>
@@ -409,6 +451,20 @@ __global__ void edge_kernel(InstDev<T> one, const InstDev<T>* many, Topology tp,
   const T q1 = I.metric[MQI1 * fs + idx], q2 = I.metric[MQI2 * fs + idx],
           q3 = I.metric[MQI3 * fs + idx];
   const T J = I.metric[MJ * fs + idx], f = I.metric[MF * fs + idx];
+  // RK inputs of the node, loaded with everything else
+  const bool fp32 = sizeof(T) == 4;
+  const bool needB = mode == MODE_RK1 || mode == MODE_RK2 || mode == MODE_RK3 ||
+                     (fp32 && mode == MODE_RK4);
+  const bool needA = mode == MODE_RK2 || mode == MODE_RK3 || mode == MODE_RK4;
+  const bool needL = fp32 && mode == MODE_RK4;
+  const T* bsrc = mode == MODE_RK4 ? I.base_out : I.base;
+  T rb[3], ra[3], rlo[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    rb[c] = needB ? bsrc[c * fs + idx] : T(0);
+    ra[c] = needA ? I.acc[c * fs + idx] : T(0);
+    rlo[c] = needL ? I.base_lo[c * fs + idx] : T(0);
+  }
 
   // neighbour vectors in this panel's frame (pack_to_buf_vec component map)
   auto rot = [](const EdgeLink& L, T gxq, T gyq, T& rx, T& ry) {
@@ -441,7 +497,7 @@ __global__ void edge_kernel(InstDev<T> one, const InstDev<T>* many, Topology tp,
   const T ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
   T kh, ku, kv;
   node_tendency<T>(gx, gy, zeta, dv, f, J, ut, vt, kh, ku, kv);
-  stage_epilogue<T>(I, mode, idx, kh, ku, kv);
+  stage_epilogue_pre<T>(I, mode, idx, kh, ku, kv, rb, ra, rlo);
 }
 
 }  // namespace swm

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(TMA_THREADS)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
                      const InstDev<T>* many, const WorkUnit* units, int* err) {
   using L = TmaLayout<T, ORD>;
-  constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, BOXW = L::BOXW, AL = L::ALIGN;
+  constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, AL = L::ALIGN;
   constexpr int MW = L::RBW - 1, MN = L::RBN - 1;
   constexpr int RSW = NW_FIELDS * TMA_CONS, RSN = NN_FIELDS * TMA_CONS;  // ring slot strides
   constexpr int NE = Ord<ORD>::NE;
@@ -158,6 +158,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const int prow = wu.panel * n;              // row of this panel in the (6n)-row tensors
   const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
   const bool hasHs = I.hs != nullptr;
+  const int bw = I.boxw;                                   // box width (columns)
+  const uint32_t rowb = (uint32_t)(bw * RPS * (int)sizeof(T));  // one field, RPS rows
 
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
@@ -186,10 +188,9 @@ __global__ void __launch_bounds__(TMA_THREADS)
         const bool in_any = r0 < rl1;
         const bool out_any = j0 + RPS > j0u && j0 < j1u;
         uint32_t tx = 0;
-        if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * (uint32_t)L::row_bytes;
+        if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * rowb;
         if (out_any)
-          tx += (uint32_t)(L::NF + (needB ? 3 : 0) + (needA ? 3 : 0) + (needL ? 3 : 0)) *
-                (uint32_t)L::row_bytes;
+          tx += (uint32_t)(L::NF + (needB ? 3 : 0) + (needA ? 3 : 0) + (needL ? 3 : 0)) * rowb;
         unsigned char* sb = stg + (size_t)s * L::stage;
         mbar_arrive_expect_tx(&full[s], tx);
         if (in_any) {
@@ -220,6 +221,25 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const bool own = col >= wu.i0 && col < wu.i1;
   const bool xint = col >= NE && col < n - NE;   // interior stencil along the row
   const int x = t + (wu.cl0 - cal);               // column inside a box row
+  // A boundary-closure column keeps its closure row in registers: taps at
+  // columns xs + m with coefficients cx[m] (the right block is the mirrored,
+  // sign-flipped left block), so the closure needs no per-row table lookups.
+  constexpr int NW = Ord<ORD>::NW;
+  T cx[NW];
+  int xs = 0;
+  if (!xint && own) {
+    const bool left = col < NE;
+    const int rr = left ? col : n - 1 - col;
+    const int last = c_sbp[Ord<ORD>::idx].last[rr];
+    xs = left ? 0 : n - NW;
+#pragma unroll
+    for (int m = 0; m < NW; ++m) {
+      // left: tap m at column m; right: tap at column n-NW+m <- mirrored index NW-1-m
+      const int mm = left ? m : NW - 1 - m;
+      const double cq = mm < last ? c_sbp[Ord<ORD>::idx].Ql[rr * MAXNW + mm] : 0.0;
+      cx[m] = T(left ? cq : -cq);
+    }
+  }
   const T grav = I.grav, ghs = I.ghs, c_in = I.c_in, c_acc = I.c_acc;
   const int fs = (int)I.fs;
   const int gcol = (int)((long long)wu.panel * I.ps) + col;  // node (col, 0) of this panel
@@ -236,7 +256,7 @@ __global__ void __launch_bounds__(TMA_THREADS)
     const T* sb = reinterpret_cast<const T*>(stg + (size_t)s * L::stage);
     // element (field f, box row q) of the box at byte offset o
     auto bx = [&](size_t o, int f, int q) {
-      return sb[o / sizeof(T) + (f * RPS + q) * BOXW + x];
+      return sb[o / sizeof(T) + (f * RPS + q) * bw + x];
     };
 #pragma unroll
     for (int q = 0; q < RPS; ++q) {
@@ -265,26 +285,32 @@ __global__ void __launch_bounds__(TMA_THREADS)
       if (*abort_flag || !own || j < j0u || j >= j1u) continue;
       const T* wj = wide + (j & MW) * RSW + t;      // this thread's column in row j
       T dxke, dyke, dxv, dyu, dxgu, dygv;
-      const bool yint = j >= NE && j < n - NE;
-      if (xint && yint) {
+      const bool yint = j >= NE && j < n - NE;   // uniform across the CTA
+      if (xint) {
         auto X = [&](int f) {
           return d_interior<ORD, T>([&](int o) { return wj[f * TMA_CONS + o]; });
         };
+        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
+      } else {
+        auto X = [&](int f) {
+          T a = T(0);
+#pragma unroll
+          for (int m = 0; m < NW; ++m) a += cx[m] * wj[f * TMA_CONS + (xs + m - col)];
+          return a;
+        };
+        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
+      }
+      if (yint) {
         auto Y = [&](int f) {
           return d_interior<ORD, T>(
               [&](int o) { return wide[((j + o) & MW) * RSW + f * TMA_CONS + t]; });
         };
-        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
         dyke = Y(W_KE); dyu = Y(W_U); dygv = Y(W_GV);
       } else {
-        auto X = [&](int f) {
-          return d_line<ORD, T>(col, n, [&](int m) { return wj[f * TMA_CONS + (m - col)]; });
-        };
         auto Y = [&](int f) {
           return d_line<ORD, T>(j, n,
                                 [&](int m) { return wide[(m & MW) * RSW + f * TMA_CONS + t]; });
         };
-        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
         dyke = Y(W_KE); dyu = Y(W_U); dygv = Y(W_GV);
       }
       const T* nj = narrow + (j & MN) * RSN + t;
