@@ -346,8 +346,8 @@ int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
     CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
-  CK(launch_stage<T>(ctx->order, &maps, I, nullptr, ctx->units, ctx->nunits, mode, ctx->derr,
-                     ctx->st),
+  CK(launch_stage<T>(ctx->order, &maps, I, nullptr, ctx->units, ctx->nunits, mode,
+                     ctx->shape.boxw, ctx->derr, ctx->st),
      "stage kernel");
   if (ctx->timing) {
     CK(cudaEventRecord(b, ctx->st), "event record");
@@ -589,16 +589,17 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     return fail(nullptr, SWM_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   }
   CKC(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device), "SM count");
-  if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->shape.cols,
-                  std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms, units, why)) {
-    free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
-  }
-  ctx->nunits = (int)units.size();
   if (ctx->shape.tma) {
-    // narrowest TMA box that covers every unit's columns from its aligned start
+    // the column strips alone fix the narrowest TMA box covering every
+    // strip from its aligned start; the box fixes shared memory and so the
+    // resident CTAs per SM, which sets the number of row segments
+    std::vector<WorkUnit> strips;
+    if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->shape.cols, 1, strips, why)) {
+      free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
+    }
     const int al = 16 / ctx->elt;
     int bw = al;
-    for (const WorkUnit& w : units) {
+    for (const WorkUnit& w : strips) {
       const int cal = w.cl0 & ~(al - 1);
       bw = std::max(bw, (w.cl1 - cal + al - 1) / al * al);
     }
@@ -607,7 +608,14 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
       return fail(nullptr, SWM_E_INVALID, "work split exceeds the TMA box");
     }
     ctx->shape.boxw = bw;
+    ctx->shape.ctas_per_sm = ctx->prec == SWM_FP32_FUSED ? stage_occupancy<float>(od, bw)
+                                                         : stage_occupancy<double>(od, bw);
   }
+  if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->shape.cols,
+                  std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms, units, why)) {
+    free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
+  }
+  ctx->nunits = (int)units.size();
   CKC(cudaMalloc(&ctx->derr, sizeof(int)), "alloc");
   CKC(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st), "memset");
   CKC(cudaMalloc(&ctx->units, sizeof(WorkUnit) * units.size()), "alloc");

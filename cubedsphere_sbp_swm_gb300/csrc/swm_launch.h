@@ -7,16 +7,21 @@
 namespace swm {
 
 // Fused stage kernel over nunits work units (one CTA each).  maps describes
-// the buffers of this launch to the TMA unit (TMA kernels only); err is the
-// device error flag raised by an expired bounded wait.
+// the buffers of this launch to the TMA unit and boxw is the widest TMA box
+// of the instances (TMA kernels only); err is the device error flag raised
+// by an expired bounded wait.
 template <class T>
 cudaError_t launch_stage(int order, const StageMaps* maps, const InstDev<T>& one,
                          const InstDev<T>* many, const WorkUnit* units, int nunits, int mode,
-                         int* err, cudaStream_t st);
+                         int boxw, int* err, cudaStream_t st);
 // Sets the launch attributes of the stage kernel of one SBP order (called at
-// context creation, outside any stream capture) and returns its shape.
+// context creation, outside any stream capture) and returns its shape; the
+// shape's boxw is the widest box the kernel supports.
 template <class T>
 cudaError_t prepare_stage(int order, StageShape* shape);
+// Resident stage-kernel CTAs per SM when the TMA box is boxw columns wide.
+template <class T>
+int stage_occupancy(int order, int boxw);
 // Cube-edge kernel over ninst instances whose largest edge has max_n nodes.
 template <class T>
 cudaError_t launch_edge(const InstDev<T>& one, const InstDev<T>* many, int ninst, int max_n,

@@ -9,8 +9,9 @@ namespace swm {
 template <>
 cudaError_t launch_stage<double>(int order, const StageMaps* maps, const InstDev<double>& one,
                                  const InstDev<double>* many, const WorkUnit* units, int nunits,
-                                 int mode, int* err, cudaStream_t st) {
+                                 int mode, int boxw, int* err, cudaStream_t st) {
   (void)err;
+  (void)boxw;
   (void)maps;
   switch (order) {
     case 21: return launch_stage_ord<double, 21>(one, many, units, nunits, mode, st);
@@ -32,7 +33,7 @@ static int v1_occupancy() {
 template <>
 cudaError_t prepare_stage<double>(int order, StageShape* shape) {
   cudaError_t e = launch_stage<double>(order, nullptr, InstDev<double>{}, nullptr, nullptr, 0,
-                                       MODE_APPLY, nullptr, nullptr);
+                                       MODE_APPLY, 0, nullptr, nullptr);
   int* ctas_per_sm = &shape->ctas_per_sm;
   if (e != cudaSuccess) return e;
   switch (order) {
@@ -45,6 +46,17 @@ cudaError_t prepare_stage<double>(int order, StageShape* shape) {
   shape->tma = 0;
   shape->boxw = shape->rps = shape->nf = 0;
   return cudaGetLastError();
+}
+
+template <>
+int stage_occupancy<double>(int order, int boxw) {
+  (void)boxw;
+  switch (order) {
+    case 21: return v1_occupancy<double, 21>();
+    case 42: return v1_occupancy<double, 42>();
+    case 43: return v1_occupancy<double, 43>();
+    default: return v1_occupancy<double, 63>();
+  }
 }
 
 template <>

@@ -8,10 +8,13 @@
 // cp.async.bulk.tensor.3d copies -- the state rows and metric rows the
 // stencils need next, plus the RK inputs of the rows being finished RMAX
 // behind -- completing on an mbarrier.  Four consumer warps (one thread per
-// column) turn each landed row into the derived stencil fields (KE, u, v,
-// J h ut, J h vt in a shared-memory ring) and finish one row per landed row.
-// Interior nodes take a branch-free path with the interior stencil; the SBP
-// boundary closures and the panel-edge bookkeeping run on a separate path.
+// column) turn each landed row into the derived stencil fields and finish
+// the row RMAX behind it.  Each thread derives every row of its own column,
+// so the y stencils read a register window of the last 2*RMAX+1 rows; only
+// the values other threads need along a row (KE, v, J h ut) and the
+// thread's own (ut, vt, J) of the row being finished go through a small
+// shared-memory ring.  Boundary-closure columns keep their closure row in
+// registers; closure rows of the y stencil are compile-time cases.
 // Every mbarrier wait is bounded: on expiry the kernel raises the device
 // error flag, stops waiting, still passes every barrier, and drains its
 // copies before exit.
@@ -85,53 +88,99 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legal w
 constexpr int TMA_CONS = 128;                     // consumer threads, one per column
 constexpr int TMA_THREADS = TMA_CONS + 32;        // + one producer warp
 
-enum { W_KE = 0, W_U, W_V, W_GU, W_GV, NW_FIELDS };   // stencil (wide) ring
-enum { N_UT = 0, N_VT, N_J, NN_FIELDS };              // own-node (narrow) ring
 
-constexpr int pow2_at_least(int v) { return v <= 1 ? 1 : 2 * pow2_at_least((v + 1) / 2); }
 
 #ifndef SWM_TMA_RPS
 #define SWM_TMA_RPS 2
 #endif
 #ifndef SWM_TMA_NST
-#define SWM_TMA_NST 2
+#define SWM_TMA_NST 3
 #endif
+
+// x-ring fields: what other threads read along the row (KE, v, J h ut) and
+// what the owning thread reads RMAX rows later (ut, vt, J)
+enum { X_KE = 0, X_V, X_GU, X_UT, X_VT, X_J, NX_FIELDS };
 
 template <class T, int ORD>
 struct TmaLayout {
   static constexpr int RPS = SWM_TMA_RPS;    // rows per pipeline stage
   static constexpr int NST = SWM_TMA_NST;    // pipeline stages
   static constexpr int RMAX = Ord<ORD>::RMAX;
-  static constexpr int RBW = pow2_at_least(2 * RMAX + 2);  // rows r-2RMAX..r live
-  static constexpr int RBN = pow2_at_least(RMAX + 2);      // row r read at r+RMAX
+  static constexpr int WS = 2 * RMAX + 1;    // y window (registers): rows j-RMAX..j+RMAX
+  static constexpr int RBX = RMAX + 2;       // x-ring rows: row r written, read at r+RMAX
   static constexpr int ALIGN = 16 / (int)sizeof(T);
-  static constexpr int BOXW = TMA_CONS + ALIGN;  // columns per box (16-byte multiple)
-  static constexpr int NF = 2;                   // metric f, rJ of the finished rows
-  static constexpr size_t r128(size_t b) { return (b + 127) / 128 * 128; }
-  static constexpr size_t row_bytes = sizeof(T) * BOXW * RPS;  // one field, RPS rows
-  static constexpr size_t b_in = r128(3 * row_bytes), b_met = r128(4 * row_bytes),
-                          b_metf = r128(NF * row_bytes), b_rk = r128(3 * row_bytes),
-                          b_hs = r128(row_bytes);
-  static constexpr size_t o_in = 0, o_met = o_in + b_in, o_metf = o_met + b_met,
-                          o_base = o_metf + b_metf, o_acc = o_base + b_rk, o_lo = o_acc + b_rk,
-                          o_hs = o_lo + b_rk, stage = o_hs + b_hs;
+  static constexpr int BOXW_MAX = TMA_CONS + ALIGN;  // widest box (16-byte multiple)
+  static constexpr int NF = 2;               // metric f, rJ of the finished rows
   static constexpr size_t head = 256;        // mbarriers + abort flag
-  static constexpr size_t wide = sizeof(T) * RBW * NW_FIELDS * TMA_CONS;
-  static constexpr size_t narrow = sizeof(T) * RBN * NN_FIELDS * TMA_CONS;
-  static constexpr size_t bytes = 128 + head + r128(wide) + r128(narrow) + NST * stage;
+  static constexpr size_t xring = sizeof(T) * RBX * NX_FIELDS * TMA_CONS;
+  __host__ __device__ static constexpr size_t r128(size_t b) { return (b + 127) / 128 * 128; }
+  // stage layout for a box width bw: in(3) met(4) metf(2) base(3) acc(3) lo(3) hs(1)
+  struct Stage {
+    size_t o_in, o_met, o_metf, o_base, o_acc, o_lo, o_hs, bytes;
+  };
+  __host__ __device__ static constexpr Stage stage(int bw) {
+    const size_t rb = sizeof(T) * (size_t)bw * RPS;
+    Stage s{};
+    s.o_in = 0;
+    s.o_met = s.o_in + r128(3 * rb);
+    s.o_metf = s.o_met + r128(4 * rb);
+    s.o_base = s.o_metf + r128(NF * rb);
+    s.o_acc = s.o_base + r128(3 * rb);
+    s.o_lo = s.o_acc + r128(3 * rb);
+    s.o_hs = s.o_lo + r128(3 * rb);
+    s.bytes = s.o_hs + r128(rb);
+    return s;
+  }
+  __host__ __device__ static constexpr size_t smem_bytes(int bw) {
+    return 128 + head + r128(xring) + NST * stage(bw).bytes;
+  }
   static_assert(2 * NST * 8 + 16 <= head, "barrier area");
-  static_assert(BOXW <= 256 && RPS <= 256, "TMA box limits");
+  static_assert(BOXW_MAX <= 256 && RPS <= 256, "TMA box limits");
 };
+
+// y derivative at row j from the register window w (w[i] holds row j-RMAX+i)
+template <int ORD, class T, int WS>
+__device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
+  constexpr int NE = Ord<ORD>::NE, RMAX = Ord<ORD>::RMAX, ID = Ord<ORD>::idx, NW = Ord<ORD>::NW;
+  if (j >= NE && j < n - NE) return d_interior<ORD, T>([&](int o) { return w[RMAX + o]; });
+  T acc = T(0);
+  if (j < NE) {
+#pragma unroll
+    for (int J = 0; J < NE; ++J) {
+      if (j == J) {
+#pragma unroll
+        for (int m = 0; m < NW; ++m) {
+          const int idx = m - J + RMAX;  // row m
+          if (m < c_sbp[ID].last[J] && idx >= 0 && idx < WS)
+            acc += T(c_sbp[ID].Ql[J * MAXNW + m]) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int R = 0; R < NE; ++R) {
+      if (n - 1 - j == R) {
+#pragma unroll
+        for (int m = NW - 1; m >= 0; --m) {
+          const int idx = R - m + RMAX;  // row n-1-m
+          if (m < c_sbp[ID].last[R] && idx >= 0 && idx < WS)
+            acc += T(-c_sbp[ID].Ql[R * MAXNW + m]) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
+        }
+      }
+    }
+  }
+  return acc;
+}
 
 template <class T, int ORD, int MODE>
 __global__ void __launch_bounds__(TMA_THREADS)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
                      const InstDev<T>* many, const WorkUnit* units, int* err) {
   using L = TmaLayout<T, ORD>;
-  constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, AL = L::ALIGN;
-  constexpr int MW = L::RBW - 1, MN = L::RBN - 1;
-  constexpr int RSW = NW_FIELDS * TMA_CONS, RSN = NN_FIELDS * TMA_CONS;  // ring slot strides
-  constexpr int NE = Ord<ORD>::NE;
+  constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, AL = L::ALIGN, WS = L::WS,
+                RBX = L::RBX;
+  constexpr int XS = NX_FIELDS * TMA_CONS;   // x-ring slot stride
+  constexpr int NE = Ord<ORD>::NE, NW = Ord<ORD>::NW;
   constexpr bool FP32 = sizeof(T) == 4;
   constexpr bool needB = MODE == MODE_RK1 || MODE == MODE_RK2 || MODE == MODE_RK3 ||
                          (FP32 && MODE == MODE_RK4);
@@ -145,9 +194,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + NST;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 2 * NST * 8);
-  T* wide = reinterpret_cast<T*>(smem + L::head);
-  T* narrow = reinterpret_cast<T*>(smem + L::head + L::r128(L::wide));
-  unsigned char* stg = smem + L::head + L::r128(L::wide) + L::r128(L::narrow);
+  T* xring = reinterpret_cast<T*>(smem + L::head);
+  unsigned char* stg = smem + L::head + L::r128(L::xring);
 
   const WorkUnit wu = units[blockIdx.x];
   const InstDev<T>& I = many ? many[wu.inst] : one;
@@ -158,7 +206,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const int prow = wu.panel * n;              // row of this panel in the (6n)-row tensors
   const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
   const bool hasHs = I.hs != nullptr;
-  const int bw = I.boxw;                                   // box width (columns)
+  const int bw = I.boxw;                      // box width (columns)
+  const typename L::Stage SL = L::stage(bw);
   const uint32_t rowb = (uint32_t)(bw * RPS * (int)sizeof(T));  // one field, RPS rows
 
   if (tid == 0) {
@@ -191,18 +240,18 @@ __global__ void __launch_bounds__(TMA_THREADS)
         if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * rowb;
         if (out_any)
           tx += (uint32_t)(L::NF + (needB ? 3 : 0) + (needA ? 3 : 0) + (needL ? 3 : 0)) * rowb;
-        unsigned char* sb = stg + (size_t)s * L::stage;
+        unsigned char* sb = stg + (size_t)s * SL.bytes;
         mbar_arrive_expect_tx(&full[s], tx);
         if (in_any) {
-          tma_load_3d(sb + L::o_in, &maps.in, cal, prow + r0, 0, &full[s]);
-          tma_load_3d(sb + L::o_met, &maps.met, cal, prow + r0, MJ, &full[s]);
-          if (hasHs) tma_load_3d(sb + L::o_hs, &maps.hs, cal, prow + r0, 0, &full[s]);
+          tma_load_3d(sb + SL.o_in, &maps.in, cal, prow + r0, 0, &full[s]);
+          tma_load_3d(sb + SL.o_met, &maps.met, cal, prow + r0, MJ, &full[s]);
+          if (hasHs) tma_load_3d(sb + SL.o_hs, &maps.hs, cal, prow + r0, 0, &full[s]);
         }
         if (out_any) {
-          tma_load_3d(sb + L::o_metf, &maps.metf, cal, prow + j0, MF, &full[s]);
-          if (needB) tma_load_3d(sb + L::o_base, &maps.base, cal, prow + j0, 0, &full[s]);
-          if (needA) tma_load_3d(sb + L::o_acc, &maps.acc, cal, prow + j0, 0, &full[s]);
-          if (needL) tma_load_3d(sb + L::o_lo, &maps.lo, cal, prow + j0, 0, &full[s]);
+          tma_load_3d(sb + SL.o_metf, &maps.metf, cal, prow + j0, MF, &full[s]);
+          if (needB) tma_load_3d(sb + SL.o_base, &maps.base, cal, prow + j0, 0, &full[s]);
+          if (needA) tma_load_3d(sb + SL.o_acc, &maps.acc, cal, prow + j0, 0, &full[s]);
+          if (needL) tma_load_3d(sb + SL.o_lo, &maps.lo, cal, prow + j0, 0, &full[s]);
         }
         issued = c + 1;
       }
@@ -223,10 +272,11 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const int x = t + (wu.cl0 - cal);               // column inside a box row
   // A boundary-closure column keeps its closure row in registers: taps at
   // columns xs + m with coefficients cx[m] (the right block is the mirrored,
-  // sign-flipped left block), so the closure needs no per-row table lookups.
-  constexpr int NW = Ord<ORD>::NW;
+  // sign-flipped left block).
   T cx[NW];
   int xs = 0;
+#pragma unroll
+  for (int m = 0; m < NW; ++m) cx[m] = T(0);
   if (!xint && own) {
     const bool left = col < NE;
     const int rr = left ? col : n - 1 - col;
@@ -234,7 +284,6 @@ __global__ void __launch_bounds__(TMA_THREADS)
     xs = left ? 0 : n - NW;
 #pragma unroll
     for (int m = 0; m < NW; ++m) {
-      // left: tap m at column m; right: tap at column n-NW+m <- mirrored index NW-1-m
       const int mm = left ? m : NW - 1 - m;
       const double cq = mm < last ? c_sbp[Ord<ORD>::idx].Ql[rr * MAXNW + mm] : 0.0;
       cx[m] = T(left ? cq : -cq);
@@ -247,13 +296,18 @@ __global__ void __launch_bounds__(TMA_THREADS)
   T* const accp = I.acc;
   T* const bop = I.base_out;
   T* const blp = I.base_lo;
+  // y windows of the derived fields this thread needs along its column
+  T yke[WS], yu[WS], ygv[WS];
+#pragma unroll
+  for (int i = 0; i < WS; ++i) { yke[i] = T(0); yu[i] = T(0); ygv[i] = T(0); }
+
   for (int c = 0; c < nch; ++c) {
     const int s = c % NST;
     const uint32_t ph = (uint32_t)(c / NST) & 1u;
     bool ok = true;
     if (!*abort_flag) ok = mbar_wait_bounded(&full[s], ph, kWaitLimitNs);
     if (!ok) { *abort_flag = 1; atomicExch(err, 3); }
-    const T* sb = reinterpret_cast<const T*>(stg + (size_t)s * L::stage);
+    const T* sb = reinterpret_cast<const T*>(stg + (size_t)s * SL.bytes);
     // element (field f, box row q) of the box at byte offset o
     auto bx = [&](size_t o, int f, int q) {
       return sb[o / sizeof(T) + (f * RPS + q) * bw + x];
@@ -261,65 +315,58 @@ __global__ void __launch_bounds__(TMA_THREADS)
 #pragma unroll
     for (int q = 0; q < RPS; ++q) {
       const int r = rl0 + c * RPS + q, j = r - RMAX;
+      T ke = T(0), u = T(0), gv = T(0);
       if (ok && r < rl1 && ld) {
-        const T h = bx(L::o_in, 0, q), u = bx(L::o_in, 1, q), v = bx(L::o_in, 2, q);
-        const T J = bx(L::o_met, 0, q);
-        const T q1 = bx(L::o_met, 1, q), q2 = bx(L::o_met, 2, q), q3 = bx(L::o_met, 3, q);
+        const T h = bx(SL.o_in, 0, q);
+        u = bx(SL.o_in, 1, q);
+        const T v = bx(SL.o_in, 2, q);
+        const T J = bx(SL.o_met, 0, q);
+        const T q1 = bx(SL.o_met, 1, q), q2 = bx(SL.o_met, 2, q), q3 = bx(SL.o_met, 3, q);
         const T ut = q1 * u + q2 * v;
         const T vt = q2 * u + q3 * v;
-        T ke = (u * ut + v * vt) * T(0.5);
+        ke = (u * ut + v * vt) * T(0.5);
         ke = ke + grav * h;
-        if (hasHs) ke = ke + grav * bx(L::o_hs, 0, q);
-        T* w = wide + (r & MW) * RSW + t;
-        w[W_KE * TMA_CONS] = ke;
-        w[W_U * TMA_CONS] = u;
-        w[W_V * TMA_CONS] = v;
-        w[W_GU * TMA_CONS] = J * (h * ut);
-        w[W_GV * TMA_CONS] = J * (h * vt);
-        T* nr = narrow + (r & MN) * RSN + t;
-        nr[N_UT * TMA_CONS] = ut;
-        nr[N_VT * TMA_CONS] = vt;
-        nr[N_J * TMA_CONS] = J;
+        if (hasHs) ke = ke + grav * bx(SL.o_hs, 0, q);
+        gv = J * (h * vt);
+        T* xw = xring + (r % RBX) * XS + t;
+        xw[X_KE * TMA_CONS] = ke;
+        xw[X_V * TMA_CONS] = v;
+        xw[X_GU * TMA_CONS] = J * (h * ut);
+        xw[X_UT * TMA_CONS] = ut;
+        xw[X_VT * TMA_CONS] = vt;
+        xw[X_J * TMA_CONS] = J;
       }
+      // push row r into the window: w[i] holds row r-2RMAX+i = j-RMAX+i
+#pragma unroll
+      for (int i = 0; i < WS - 1; ++i) { yke[i] = yke[i + 1]; yu[i] = yu[i + 1]; ygv[i] = ygv[i + 1]; }
+      yke[WS - 1] = ke; yu[WS - 1] = u; ygv[WS - 1] = gv;
       consumers_sync();
       if (*abort_flag || !own || j < j0u || j >= j1u) continue;
-      const T* wj = wide + (j & MW) * RSW + t;      // this thread's column in row j
-      T dxke, dyke, dxv, dyu, dxgu, dygv;
-      const bool yint = j >= NE && j < n - NE;   // uniform across the CTA
+      const T* xr = xring + (j % RBX) * XS + t;      // row j, this thread's column
+      T dxke, dxv, dxgu;
       if (xint) {
-        auto X = [&](int f) {
-          return d_interior<ORD, T>([&](int o) { return wj[f * TMA_CONS + o]; });
-        };
-        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
+        dxke = d_interior<ORD, T>([&](int o) { return xr[X_KE * TMA_CONS + o]; });
+        dxv = d_interior<ORD, T>([&](int o) { return xr[X_V * TMA_CONS + o]; });
+        dxgu = d_interior<ORD, T>([&](int o) { return xr[X_GU * TMA_CONS + o]; });
       } else {
-        auto X = [&](int f) {
-          T a = T(0);
+        dxke = T(0); dxv = T(0); dxgu = T(0);
 #pragma unroll
-          for (int m = 0; m < NW; ++m) a += cx[m] * wj[f * TMA_CONS + (xs + m - col)];
-          return a;
-        };
-        dxke = X(W_KE); dxv = X(W_V); dxgu = X(W_GU);
+        for (int m = 0; m < NW; ++m) {
+          const int o = xs + m - col;
+          dxke += cx[m] * xr[X_KE * TMA_CONS + o];
+          dxv += cx[m] * xr[X_V * TMA_CONS + o];
+          dxgu += cx[m] * xr[X_GU * TMA_CONS + o];
+        }
       }
-      if (yint) {
-        auto Y = [&](int f) {
-          return d_interior<ORD, T>(
-              [&](int o) { return wide[((j + o) & MW) * RSW + f * TMA_CONS + t]; });
-        };
-        dyke = Y(W_KE); dyu = Y(W_U); dygv = Y(W_GV);
-      } else {
-        auto Y = [&](int f) {
-          return d_line<ORD, T>(j, n,
-                                [&](int m) { return wide[(m & MW) * RSW + f * TMA_CONS + t]; });
-        };
-        dyke = Y(W_KE); dyu = Y(W_U); dygv = Y(W_GV);
-      }
-      const T* nj = narrow + (j & MN) * RSN + t;
-      const T J = nj[N_J * TMA_CONS];
-      const T rJ = bx(L::o_metf, 1, q);
+      const T dyke = ydiff<ORD, T, WS>(yke, j, n);
+      const T dyu = ydiff<ORD, T, WS>(yu, j, n);
+      const T dygv = ydiff<ORD, T, WS>(ygv, j, n);
+      const T J = xr[X_J * TMA_CONS];
+      const T rJ = bx(SL.o_metf, 1, q);
       const T gx = dxke * ghs, gy = dyke * ghs;
       const T zeta = (dxv - dyu) * rJ;
       const T dv = (dxgu + dygv) * rJ;
-      if (!(xint && yint) && ((col == 0) | (col == n - 1) | (j == 0) | (j == n - 1))) {
+      if ((col == 0) | (col == n - 1) | (j == 0) | (j == n - 1)) {
         T* E = I.edge + wu.panel * 16 * n;
         const T vals[4] = {gx, gy, zeta, dv};
         if (col == 0)
@@ -337,8 +384,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
         continue;
       }
       T kk[3];
-      node_tendency<T>(gx, gy, zeta, dv, bx(L::o_metf, 0, q), J, nj[N_UT * TMA_CONS],
-                       nj[N_VT * TMA_CONS], kk[0], kk[1], kk[2]);
+      node_tendency<T>(gx, gy, zeta, dv, bx(SL.o_metf, 0, q), J, xr[X_UT * TMA_CONS],
+                       xr[X_VT * TMA_CONS], kk[0], kk[1], kk[2]);
       const int g = gcol + j * P;
 #pragma unroll
       for (int cc = 0; cc < 3; ++cc) {
@@ -347,30 +394,30 @@ __global__ void __launch_bounds__(TMA_THREADS)
           outp[o] = kk[cc];
         } else if constexpr (!FP32) {
           if constexpr (MODE == MODE_RK1) {
-            const T b = bx(L::o_base, cc, q);
+            const T b = bx(SL.o_base, cc, q);
             outp[o] = T(1.0) * b + c_in * kk[cc];
             accp[o] = b + c_acc * kk[cc];
           } else if constexpr (MODE == MODE_RK4) {
-            bop[o] = bx(L::o_acc, cc, q) + c_acc * kk[cc];
+            bop[o] = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
           } else {
-            outp[o] = T(1.0) * bx(L::o_base, cc, q) + c_in * kk[cc];
-            accp[o] = bx(L::o_acc, cc, q) + c_acc * kk[cc];
+            outp[o] = T(1.0) * bx(SL.o_base, cc, q) + c_in * kk[cc];
+            accp[o] = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
           }
         } else {
           if constexpr (MODE == MODE_RK1) {
-            outp[o] = bx(L::o_base, cc, q) + c_in * kk[cc];
+            outp[o] = bx(SL.o_base, cc, q) + c_in * kk[cc];
             accp[o] = c_acc * kk[cc];
           } else if constexpr (MODE == MODE_RK4) {
-            const T d = bx(L::o_acc, cc, q) + c_acc * kk[cc];
-            const T hi = bx(L::o_base, cc, q), lo = bx(L::o_lo, cc, q);
+            const T d = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
+            const T hi = bx(SL.o_base, cc, q), lo = bx(SL.o_lo, cc, q);
             const T tt = lo + d;
             const T sm = hi + tt;
             const T bb = sm - hi;
             bop[o] = sm;
             blp[o] = (hi - (sm - bb)) + (tt - bb);
           } else {
-            outp[o] = bx(L::o_base, cc, q) + c_in * kk[cc];
-            accp[o] = bx(L::o_acc, cc, q) + c_acc * kk[cc];
+            outp[o] = bx(SL.o_base, cc, q) + c_in * kk[cc];
+            accp[o] = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
           }
         }
       }
@@ -383,45 +430,55 @@ __global__ void __launch_bounds__(TMA_THREADS)
 template <class T, int ORD, int MODE>
 cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
                                   const InstDev<T>* many, const WorkUnit* units, int nunits,
-                                  int* err, cudaStream_t st) {
-  constexpr size_t smem = TmaLayout<T, ORD>::bytes;
+                                  int boxw, int* err, cudaStream_t st) {
+  using L = TmaLayout<T, ORD>;
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, MODE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L::smem_bytes(L::BOXW_MAX));
     if (e != cudaSuccess) return e;
     configured = true;
   }
   if (nunits <= 0) return cudaSuccess;
-  stage_tma_kernel<T, ORD, MODE><<<nunits, TMA_THREADS, smem, st>>>(maps, one, many, units, err);
+  stage_tma_kernel<T, ORD, MODE><<<nunits, TMA_THREADS, L::smem_bytes(boxw), st>>>(maps, one, many,
+                                                                                    units, err);
   return cudaGetLastError();
 }
 
 template <class T, int ORD>
 cudaError_t launch_stage_tma_ord(const StageMaps& maps, const InstDev<T>& one,
                                  const InstDev<T>* many, const WorkUnit* units, int nunits,
-                                 int mode, int* err, cudaStream_t st) {
+                                 int mode, int boxw, int* err, cudaStream_t st) {
   switch (mode) {
-    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY>(maps, one, many, units, nunits, err, st);
-    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1>(maps, one, many, units, nunits, err, st);
-    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2>(maps, one, many, units, nunits, err, st);
-    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3>(maps, one, many, units, nunits, err, st);
-    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4>(maps, one, many, units, nunits, err, st);
+    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY>(maps, one, many, units, nunits, boxw, err, st);
+    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1>(maps, one, many, units, nunits, boxw, err, st);
+    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2>(maps, one, many, units, nunits, boxw, err, st);
+    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3>(maps, one, many, units, nunits, boxw, err, st);
+    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4>(maps, one, many, units, nunits, boxw, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
-// configure every mode; returns resident CTAs per SM
+// configure every mode (outside any capture)
 template <class T, int ORD>
-cudaError_t prepare_stage_tma_ord(int* ctas_per_sm) {
+cudaError_t prepare_stage_tma_ord() {
   static const StageMaps kNone{};
   for (int m = MODE_APPLY; m <= MODE_RK4; ++m) {
     cudaError_t e = launch_stage_tma_ord<T, ORD>(kNone, InstDev<T>{}, nullptr, nullptr, 0, m,
-                                                 nullptr, nullptr);
+                                                 TmaLayout<T, ORD>::BOXW_MAX, nullptr, nullptr);
     if (e != cudaSuccess) return e;
   }
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      ctas_per_sm, stage_tma_kernel<T, ORD, MODE_RK2>, TMA_THREADS, TmaLayout<T, ORD>::bytes);
+  return cudaSuccess;
+}
+
+// resident CTAs per SM at box width bw
+template <class T, int ORD>
+int stage_tma_occupancy(int bw) {
+  int blocks = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_tma_kernel<T, ORD, MODE_RK2>,
+                                                TMA_THREADS, TmaLayout<T, ORD>::smem_bytes(bw));
+  return blocks;
 }
 
 }  // namespace swm
