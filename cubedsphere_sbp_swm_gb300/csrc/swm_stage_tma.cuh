@@ -172,6 +172,46 @@ __device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
   return acc;
 }
 
+// RK stage epilogue of one field at global offset o: k is the tendency, sc
+// points at this field's row of the stage (base at +eb, running sum at +ea,
+// FP32 low part at +el).
+template <class T, int MODE>
+__device__ __forceinline__ void rk_store(T* outp, T* accp, T* bop, T* blp, int o, T k, const T* sc,
+                                         int eb, int ea, int el, int fstride, T c_in, T c_acc) {
+  (void)fstride;
+  constexpr bool FP32 = sizeof(T) == 4;
+  if constexpr (MODE == MODE_APPLY) {
+    outp[o] = k;
+  } else if constexpr (!FP32) {
+    if constexpr (MODE == MODE_RK1) {
+      const T b = sc[eb];
+      outp[o] = T(1.0) * b + c_in * k;
+      accp[o] = b + c_acc * k;
+    } else if constexpr (MODE == MODE_RK4) {
+      bop[o] = sc[ea] + c_acc * k;
+    } else {
+      outp[o] = T(1.0) * sc[eb] + c_in * k;
+      accp[o] = sc[ea] + c_acc * k;
+    }
+  } else {
+    if constexpr (MODE == MODE_RK1) {
+      outp[o] = sc[eb] + c_in * k;
+      accp[o] = c_acc * k;
+    } else if constexpr (MODE == MODE_RK4) {
+      const T d = sc[ea] + c_acc * k;
+      const T hi = sc[eb], lo = sc[el];
+      const T tt = lo + d;
+      const T sm = hi + tt;
+      const T bb = sm - hi;
+      bop[o] = sm;
+      blp[o] = (hi - (sm - bb)) + (tt - bb);
+    } else {
+      outp[o] = sc[eb] + c_in * k;
+      accp[o] = sc[ea] + c_acc * k;
+    }
+  }
+}
+
 template <class T, int ORD, int MODE>
 __global__ void __launch_bounds__(TMA_THREADS)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
@@ -207,7 +247,12 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
   const bool hasHs = I.hs != nullptr;
   const int bw = I.boxw;                      // box width (columns)
-  const typename L::Stage SL = L::stage(bw);
+  // stage layout as plain scalars (element offsets of the boxes in a stage)
+  const size_t st_bytes = L::stage(bw).bytes;
+  const int e_in = (int)(L::stage(bw).o_in / sizeof(T)), e_met = (int)(L::stage(bw).o_met / sizeof(T)),
+            e_metf = (int)(L::stage(bw).o_metf / sizeof(T)), e_base = (int)(L::stage(bw).o_base / sizeof(T)),
+            e_acc = (int)(L::stage(bw).o_acc / sizeof(T)), e_lo = (int)(L::stage(bw).o_lo / sizeof(T)),
+            e_hs = (int)(L::stage(bw).o_hs / sizeof(T));
   const uint32_t rowb = (uint32_t)(bw * RPS * (int)sizeof(T));  // one field, RPS rows
 
   if (tid == 0) {
@@ -240,18 +285,18 @@ __global__ void __launch_bounds__(TMA_THREADS)
         if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * rowb;
         if (out_any)
           tx += (uint32_t)(L::NF + (needB ? 3 : 0) + (needA ? 3 : 0) + (needL ? 3 : 0)) * rowb;
-        unsigned char* sb = stg + (size_t)s * SL.bytes;
+        T* sb = reinterpret_cast<T*>(stg + (size_t)s * st_bytes);
         mbar_arrive_expect_tx(&full[s], tx);
         if (in_any) {
-          tma_load_3d(sb + SL.o_in, &maps.in, cal, prow + r0, 0, &full[s]);
-          tma_load_3d(sb + SL.o_met, &maps.met, cal, prow + r0, MJ, &full[s]);
-          if (hasHs) tma_load_3d(sb + SL.o_hs, &maps.hs, cal, prow + r0, 0, &full[s]);
+          tma_load_3d(sb + e_in, &maps.in, cal, prow + r0, 0, &full[s]);
+          tma_load_3d(sb + e_met, &maps.met, cal, prow + r0, MJ, &full[s]);
+          if (hasHs) tma_load_3d(sb + e_hs, &maps.hs, cal, prow + r0, 0, &full[s]);
         }
         if (out_any) {
-          tma_load_3d(sb + SL.o_metf, &maps.metf, cal, prow + j0, MF, &full[s]);
-          if (needB) tma_load_3d(sb + SL.o_base, &maps.base, cal, prow + j0, 0, &full[s]);
-          if (needA) tma_load_3d(sb + SL.o_acc, &maps.acc, cal, prow + j0, 0, &full[s]);
-          if (needL) tma_load_3d(sb + SL.o_lo, &maps.lo, cal, prow + j0, 0, &full[s]);
+          tma_load_3d(sb + e_metf, &maps.metf, cal, prow + j0, MF, &full[s]);
+          if (needB) tma_load_3d(sb + e_base, &maps.base, cal, prow + j0, 0, &full[s]);
+          if (needA) tma_load_3d(sb + e_acc, &maps.acc, cal, prow + j0, 0, &full[s]);
+          if (needL) tma_load_3d(sb + e_lo, &maps.lo, cal, prow + j0, 0, &full[s]);
         }
         issued = c + 1;
       }
@@ -307,26 +352,24 @@ __global__ void __launch_bounds__(TMA_THREADS)
     bool ok = true;
     if (!*abort_flag) ok = mbar_wait_bounded(&full[s], ph, kWaitLimitNs);
     if (!ok) { *abort_flag = 1; atomicExch(err, 3); }
-    const T* sb = reinterpret_cast<const T*>(stg + (size_t)s * SL.bytes);
-    // element (field f, box row q) of the box at byte offset o
-    auto bx = [&](size_t o, int f, int q) {
-      return sb[o / sizeof(T) + (f * RPS + q) * bw + x];
-    };
+    // this thread's column in the stage; element (field f, box row q) of the
+    // box at element offset e is sx[e + (f * RPS + q) * bw]
+    const T* sx = reinterpret_cast<const T*>(stg + (size_t)s * st_bytes) + x;
 #pragma unroll
     for (int q = 0; q < RPS; ++q) {
       const int r = rl0 + c * RPS + q, j = r - RMAX;
       T ke = T(0), u = T(0), gv = T(0);
       if (ok && r < rl1 && ld) {
-        const T h = bx(SL.o_in, 0, q);
-        u = bx(SL.o_in, 1, q);
-        const T v = bx(SL.o_in, 2, q);
-        const T J = bx(SL.o_met, 0, q);
-        const T q1 = bx(SL.o_met, 1, q), q2 = bx(SL.o_met, 2, q), q3 = bx(SL.o_met, 3, q);
+        const T h = sx[e_in + (0 * RPS + q) * bw];
+        u = sx[e_in + (1 * RPS + q) * bw];
+        const T v = sx[e_in + (2 * RPS + q) * bw];
+        const T J = sx[e_met + (0 * RPS + q) * bw];
+        const T q1 = sx[e_met + (1 * RPS + q) * bw], q2 = sx[e_met + (2 * RPS + q) * bw], q3 = sx[e_met + (3 * RPS + q) * bw];
         const T ut = q1 * u + q2 * v;
         const T vt = q2 * u + q3 * v;
         ke = (u * ut + v * vt) * T(0.5);
         ke = ke + grav * h;
-        if (hasHs) ke = ke + grav * bx(SL.o_hs, 0, q);
+        if (hasHs) ke = ke + grav * sx[e_hs + (0 * RPS + q) * bw];
         gv = J * (h * vt);
         T* xw = xring + (r % RBX) * XS + t;
         xw[X_KE * TMA_CONS] = ke;
@@ -362,7 +405,7 @@ __global__ void __launch_bounds__(TMA_THREADS)
       const T dyu = ydiff<ORD, T, WS>(yu, j, n);
       const T dygv = ydiff<ORD, T, WS>(ygv, j, n);
       const T J = xr[X_J * TMA_CONS];
-      const T rJ = bx(SL.o_metf, 1, q);
+      const T rJ = sx[e_metf + (1 * RPS + q) * bw];
       const T gx = dxke * ghs, gy = dyke * ghs;
       const T zeta = (dxv - dyu) * rJ;
       const T dv = (dxgu + dygv) * rJ;
@@ -383,44 +426,14 @@ __global__ void __launch_bounds__(TMA_THREADS)
           for (int e = 0; e < 4; ++e) E[(SIDE_T * 4 + e) * n + col] = vals[e];
         continue;
       }
-      T kk[3];
-      node_tendency<T>(gx, gy, zeta, dv, bx(SL.o_metf, 0, q), J, xr[X_UT * TMA_CONS],
-                       xr[X_VT * TMA_CONS], kk[0], kk[1], kk[2]);
+      T k0, k1, k2;
+      node_tendency<T>(gx, gy, zeta, dv, sx[e_metf + (0 * RPS + q) * bw], J, xr[X_UT * TMA_CONS],
+                       xr[X_VT * TMA_CONS], k0, k1, k2);
       const int g = gcol + j * P;
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) {
-        const int o = cc * fs + g;
-        if constexpr (MODE == MODE_APPLY) {
-          outp[o] = kk[cc];
-        } else if constexpr (!FP32) {
-          if constexpr (MODE == MODE_RK1) {
-            const T b = bx(SL.o_base, cc, q);
-            outp[o] = T(1.0) * b + c_in * kk[cc];
-            accp[o] = b + c_acc * kk[cc];
-          } else if constexpr (MODE == MODE_RK4) {
-            bop[o] = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
-          } else {
-            outp[o] = T(1.0) * bx(SL.o_base, cc, q) + c_in * kk[cc];
-            accp[o] = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
-          }
-        } else {
-          if constexpr (MODE == MODE_RK1) {
-            outp[o] = bx(SL.o_base, cc, q) + c_in * kk[cc];
-            accp[o] = c_acc * kk[cc];
-          } else if constexpr (MODE == MODE_RK4) {
-            const T d = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
-            const T hi = bx(SL.o_base, cc, q), lo = bx(SL.o_lo, cc, q);
-            const T tt = lo + d;
-            const T sm = hi + tt;
-            const T bb = sm - hi;
-            bop[o] = sm;
-            blp[o] = (hi - (sm - bb)) + (tt - bb);
-          } else {
-            outp[o] = bx(SL.o_base, cc, q) + c_in * kk[cc];
-            accp[o] = bx(SL.o_acc, cc, q) + c_acc * kk[cc];
-          }
-        }
-      }
+      const int qb = q * bw;
+      rk_store<T, MODE>(outp, accp, bop, blp, g, k0, sx + qb, e_base, e_acc, e_lo, RPS * bw, c_in, c_acc);
+      rk_store<T, MODE>(outp, accp, bop, blp, fs + g, k1, sx + qb + RPS * bw, e_base, e_acc, e_lo, RPS * bw, c_in, c_acc);
+      rk_store<T, MODE>(outp, accp, bop, blp, 2 * fs + g, k2, sx + qb + 2 * RPS * bw, e_base, e_acc, e_lo, RPS * bw, c_in, c_acc);
     }
     __syncwarp();
     if ((t & 31) == 0) mbar_arrive(&empty[s]);
