@@ -20,6 +20,9 @@ SWM_E_DEVICE = -5
 SWM_FP64_PLAIN = 0
 SWM_FP32_FUSED = 1
 
+# largest N that swm_sync_scalar_static accepts
+SWM_SYNC_STATIC_MAX_N = 1024
+
 # every entry point of include/swm_gpu.h
 EXPORTS = (
     "swm_ctx_create", "swm_ctx_create_named", "swm_ctx_destroy", "swm_last_error",
@@ -31,7 +34,7 @@ EXPORTS = (
     "swm_field_free", "swm_field_upload", "swm_field_download", "swm_op_co2contra",
     "swm_op_massflux", "swm_op_ke", "swm_op_grad", "swm_op_div", "swm_op_curl",
     "swm_op_coriolis", "swm_sync_scalar", "swm_sync_vector_cov", "swm_quadrature_mass",
-    "swm_timing_enable", "swm_timing_read",
+    "swm_timing_enable", "swm_timing_read", "swm_sync_scalar_static",
 )
 
 
@@ -123,6 +126,7 @@ def load(build_if_missing: bool = True):
     sig("swm_timing_enable", I, VP, I)
     sig("swm_timing_read", I, VP, _D, ctypes.POINTER(ctypes.c_long), _D,
         ctypes.POINTER(ctypes.c_long))
+    sig("swm_sync_scalar_static", I, VP, VP)
     _lib = L
     return L
 

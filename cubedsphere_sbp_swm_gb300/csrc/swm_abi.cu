@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <set>
 #include <string>
 #include <utility>
@@ -487,6 +488,31 @@ void free_ctx(swm_ctx* c) {
   if (c->hres) cudaFreeHost(c->hres);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
+}
+
+// Edge scratch of swm_sync_scalar_static: the context edge-buffer layout
+// (6 panels x 4 sides x 4 value slots x n) for n <= SWM_SYNC_STATIC_MAX_N + 1,
+// part of the module image so that no call allocates it.
+constexpr int kStaticSyncScratch = 6 * 4 * 4 * (SWM_SYNC_STATIC_MAX_N + 1);
+static __device__ __align__(256) double g_sync_scratch[kStaticSyncScratch];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_sync_scratch on the context's device, looked up once
+// per device (the device is current: the caller has just selected it).
+int static_sync_scratch(swm_ctx* ctx, double** out) {
+  const int dev = ctx->cfg.device;
+  if (dev < 0 || dev >= kMaxDevices) return fail(ctx, SWM_E_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_sync_scratch), "static scratch address");
+    g_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return SWM_OK;
 }
 
 }  // namespace
@@ -1074,6 +1100,23 @@ int swm_quadrature_mass(swm_ctx* ctx, const swm_field* f, double* out) {
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
   if (int rc = reduce(ctx, 1, f->p, nullptr, 0)) return rc;
   return fetch_results(ctx, 1, out);
+}
+
+// ---------------------------------------------------------------- static scratch
+int swm_sync_scalar_static(swm_ctx* ctx, swm_field* f) {
+  CHECK_FIELDS(f);
+  if (ctx->N > SWM_SYNC_STATIC_MAX_N) {
+    char m[160];
+    std::snprintf(m, sizeof m,
+                  "swm_sync_scalar_static: N=%d exceeds the static scratch limit N<=%d "
+                  "(swm_sync_scalar has no limit)",
+                  ctx->N, SWM_SYNC_STATIC_MAX_N);
+    return fail(ctx, SWM_E_INVALID, m);
+  }
+  double* scratch = nullptr;
+  if (int rc = static_sync_scratch(ctx, &scratch)) return rc;
+  CK(launch_sync_scalar(ctx->g64, ctx->topo, f->p, scratch, ctx->st), "sync");
+  return SWM_OK;
 }
 
 // ---------------------------------------------------------------- timing

@@ -200,6 +200,30 @@ int swm_timing_enable(swm_ctx* ctx, int on);
 int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches,
                     double* edge_ms, long* edge_launches);
 
+/* ---------------------------------------------------------------------- */
+/* Scalar cube-edge sync with static scratch (no counterpart in the        */
+/* reference; same result as swm_sync_scalar).                             */
+/*                                                                          */
+/* For callers that must not have device memory allocated on their behalf: */
+/* a host model that hands a fixed device budget to its own pool at        */
+/* start-up, or one that cannot afford the device-wide synchronisation a   */
+/* cudaMalloc/cudaFree brings.  The edge scratch is a fixed array in the   */
+/* library's device image (reserved when the library's module loads), not  */
+/* a buffer of the context; the call itself allocates nothing.             */
+/*  - Limit: N <= SWM_SYNC_STATIC_MAX_N (scratch 6*4*4*(N+1) doubles,        */
+/*    769 KiB at the limit); a larger N is rejected with SWM_E_INVALID.     */
+/*  - The first call on each device looks up the scratch address on that   */
+/*    device (cudaGetSymbolAddress); make that first call before any stream */
+/*    capture begins.                                                        */
+/*  - No scratch value has to start at zero: every slot the sync reads is   */
+/*    written by the same call first.                                        */
+/*  - All calls on one device share the scratch: calls that overlap in time */
+/*    (different streams or contexts on the same device) race; calls on one */
+/*    stream are ordered and safe.                                          */
+/* ---------------------------------------------------------------------- */
+#define SWM_SYNC_STATIC_MAX_N 1024
+int swm_sync_scalar_static(swm_ctx* ctx, swm_field* f);
+
 #ifdef __cplusplus
 }
 #endif
