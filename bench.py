@@ -1,14 +1,20 @@
 #!/usr/bin/env python
 """Benchmark of the shallow-water RK4 hot path on GB300.
 
-Workload: 6 panels x 385^2 nodes (N=384), SBP 4/2 operators, RK4 with
-dt = 120 s, seeded balanced zonal flow plus a degree<=64 spherical-harmonic
-height perturbation (synthetic; the reference's own test cases are analytic
-and produce no checked-in data).  One "step" is one RK4 step of the whole
-state.  The headline value is the FP32 fused form (compensated stage sums,
-FP64 metric precompute); the FP64 plain path is measured beside it.
+Default workload: 6 panels x 385^2 nodes (N=384), SBP 4/2 operators, RK4
+with dt = 120 s, seeded balanced zonal flow plus a degree<=64
+spherical-harmonic height perturbation (synthetic; the reference's own test
+cases are analytic and produce no checked-in data).  One "step" is one RK4
+step of the whole state.  The headline value is the FP32 fused form
+(compensated stage sums, FP64 metric precompute); the FP64 plain path is
+measured beside it, and the FP32 state is compared with the FP64 state after
+10 simulated days.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+                  [--workload n384_d42|n1024_d63]
+
+n1024_d63 is the large single instance: 6 x 1025^2 nodes, SBP 6/3, dt = 45 s,
+balanced flow plus a barotropically unstable jet.
 
 Multi-GPU runs (torchrun) are independent replicas, one per GPU: the path
 does not shard across GPUs here (all six panels live on one GPU).
@@ -17,7 +23,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -29,12 +34,28 @@ sys.path.insert(0, ROOT)
 
 METRIC = ("RK4 steps/s at 6×384² (FP32 form vs FP64 plain), "
           "adjoint/forward time ratio")
-N_BENCH, ORDER, DT = 384, 42, 120.0
 L2_FLUSH_BYTES = 256 << 20          # > 129 MB L2
-# Algorithmic HBM bytes per node per RK4 step (4 stage launches), see DESIGN:
-#  FP32 compensated: 77 words x 4 B; FP64 plain: 68 + 4 (rJ) words x 8 B.
-BYTES_PER_NODE_STEP = {"fp32": 77 * 4, "fp64": 72 * 8}
+# Algorithmic HBM words per node per RK4 step (4 stage launches; 3 state
+# words, 5 metric words J, Qi1, Qi2, Qi3, f):
+#   FP64 plain 68 = 14 + 20 + 20 + 14;
+#   FP32 compensated 77 = 14 + 20 + 20 + 23 (stage 4 also reads the low part
+#   of the state pair).  The derived 1/(J hx a) field the kernels read is not
+#   counted.
+BYTES_PER_NODE_STEP = {"fp32": 77 * 4, "fp64": 68 * 8}
 KERNELS_PER_STEP = 8                # 4 x (stage kernel + cube-edge kernel)
+
+# acc_dt: time step of the FP32-vs-FP64 accuracy run.  The workloads' own
+# time steps (Courant number c*dt/(a*hx) = 1.11 with c = sqrt(g*5960 m)) lie
+# beyond the RK4 stability limit of the undiffused SBP scheme: the FP64 state
+# turns non-finite within 6 simulated hours.  Courant 0.84 (N=384, 90 s) and
+# 0.74 (N=1024 d63, 30 s) stay stable over the full simulated period.  The
+# per-step work, and so steps/s, does not depend on dt.
+WORKLOADS = {
+    "n384_d42": dict(N=384, order=42, dt=120.0, cfg=2, days=10.0, acc_dt=90.0,
+                     desc="6 panels x 385^2 nodes (N=384), SBP 4/2 (d42), RK4 dt=120 s"),
+    "n1024_d63": dict(N=1024, order=63, dt=45.0, cfg=5, days=5.0, acc_dt=30.0,
+                      desc="6 panels x 1025^2 nodes (N=1024), SBP 6/3 (d63), RK4 dt=45 s"),
+}
 
 
 def _dist():
@@ -53,10 +74,10 @@ def _measured_peak():
         return 6800.0, "fallback"
 
 
-def _profile_traffic():
+def _profile_traffic(workload):
     """Per-launch DRAM traffic of the stage kernel from the committed ncu
     summary (profiles/), or None."""
-    path = os.path.join(ROOT, "profiles", "stage_kernel_fp32_n384.md")
+    path = os.path.join(ROOT, "profiles", f"stage_kernel_fp32_{workload}.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -119,18 +140,61 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _state(cfg_N):
+def _state(w):
     from cubedsphere_sbp_swm_gb300 import initial
-    h, u, v, info = initial.balanced_zonal(cfg_N, 2, 64)
-    return h, u, v, info
+    return initial.config_state(w["cfg"])
+
+
+def _data_desc(w, info):
+    if w["cfg"] == 5:
+        return ("synthetic: seeded balanced zonal flow + Gaussian jet (peak 80 m/s) + 120 m "
+                "height bump")
+    return ("synthetic: seeded balanced zonal flow u0=%.2f m/s + Y_lm (l<=64) height "
+            "perturbation, 10 m RMS" % info["u0"])
+
+
+def accuracy_vs_fp64(w, h, u, v, local, days):
+    """FP32 fused form against the FP64 plain path (which matches the FP64
+    oracle to 1e-12 per step) after `days` simulated days from the same
+    initial state at the stable time step acc_dt: J-weighted relative L2 and
+    relative Linf of h, u, v and the SBP-quadrature mass drift of both runs."""
+    import numpy as np
+
+    import cubedsphere_sbp_swm_gb300 as swm
+    from cubedsphere_sbp_swm_gb300 import initial
+
+    dt = w["acc_dt"]
+    nsteps = int(round(days * 86400.0 / dt))
+    J = initial.ecs_geometry(w["N"])["J"]
+    res, drift = {}, {}
+    for prec in ("fp64", "fp32"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=w["N"], sbp_order=w["order"], precision=prec, device=local))
+        s = op.create_stvec()
+        s.upload(h, u, v)
+        m0 = op.get_diagnostics(s)["mass"]
+        swm.RK4().step(s, op, dt, nsteps)
+        res[prec] = s.download()
+        drift[prec] = (op.get_diagnostics(s)["mass"] - m0) / m0
+        del s, op
+    out = {"days": days, "dt_s": dt, "steps": nsteps, "reference": "FP64 plain GPU path",
+           "note": "the workload dt (Courant 1.11) is beyond the RK4 stability limit of the "
+                   "undiffused scheme (FP64 state non-finite within 6 simulated hours); this run "
+                   "uses the stable dt_s"}
+    for name, a, b in zip("huv", res["fp32"], res["fp64"]):
+        out[f"{name}_rel_l2"] = float(np.sqrt(np.sum(J * (a - b) ** 2) / np.sum(J * b * b)))
+        out[f"{name}_rel_linf"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    out["mass_drift_fp32"] = drift["fp32"]
+    out["mass_drift_fp64"] = drift["fp64"]
+    return out
 
 
 def run_gpu_arm(args):
-    import numpy as np
     import torch
 
     import cubedsphere_sbp_swm_gb300 as swm
 
+    w = WORKLOADS[args.workload]
+    N, ORDER, DT = w["N"], w["order"], w["dt"]
     ws, rank, local = _dist()
     if ws > 1:
         import torch.distributed as dist
@@ -138,11 +202,11 @@ def run_gpu_arm(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    h, u, v, info = _state(N_BENCH)
+    h, u, v, info = _state(w)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     def time_steps(prec, steps, warmup, kernel_timing=False):
-        op = swm.OperatorSWM(swm.ModelConfig(N=N_BENCH, sbp_order=ORDER, precision=prec, device=local))
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=ORDER, precision=prec, device=local))
         s = op.create_stvec()
         s.upload(h, u, v)
         ts = swm.RK4()
@@ -182,6 +246,8 @@ def run_gpu_arm(args):
     with ClockSampler(uuid) as clk:
         op32, s32, ms32, _ = time_steps("fp32", args.steps, args.warmup)
     clocks = clk.summary()
+    import numpy as np
+    finite = bool(all(np.isfinite(a).all() for a in s32.download()))
     total_ms = sum(ms32)
     if ws > 1:
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
@@ -192,25 +258,27 @@ def run_gpu_arm(args):
     if args.quick:  # profiling case: only the timed FP32 steps
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "steps/s",
-                              "ms_per_step": round(ms_per_step, 5), "quick": True}), flush=True)
+                              "ms_per_step": round(ms_per_step, 5), "quick": True,
+                              "workload": args.workload}), flush=True)
         return
 
     # dominant kernel timing (stage kernel), events around every launch
     _, _, _, kt = time_steps("fp32", max(8, min(args.steps, 40)), 2, kernel_timing=True)
     stage_ms, stage_n, edge_ms, edge_n = kt
-    npts = 6 * (N_BENCH + 1) ** 2
+    npts = 6 * (N + 1) ** 2
     bytes_per_launch = BYTES_PER_NODE_STEP["fp32"] * npts / 4.0
     achieved = bytes_per_launch / (stage_ms / stage_n / 1e3) / 1e9
     peak, peak_kind = _measured_peak()
-    traffic = _profile_traffic()
+    traffic = _profile_traffic(args.workload)
 
     # FP64 plain path beside it
     op64, s64, ms64, _ = time_steps("fp64", max(10, args.steps // 2), args.warmup)
     fp64_ms = sum(ms64) / len(ms64)
     _, _, _, kt64 = time_steps("fp64", 10, 2, kernel_timing=True)
+    del op64, s64
 
     # end to end through the C-ABI with host (pinned) buffers
-    pin = [torch.empty((6, N_BENCH + 1, N_BENCH + 1), dtype=torch.float64, pin_memory=True) for _ in range(6)]
+    pin = [torch.empty((6, N + 1, N + 1), dtype=torch.float64, pin_memory=True) for _ in range(6)]
     for t_, a_ in zip(pin[:3], (h, u, v)):
         t_.numpy()[...] = a_
     hin = [t_.numpy() for t_ in pin[:3]]
@@ -232,22 +300,27 @@ def run_gpu_arm(args):
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_val = ws * e2e_steps / float(t.item())
+    del s32, op32
+
+    # FP32 form against the FP64 plain path over the workload's simulated days
+    acc = None
+    if rank == 0 and not args.no_accuracy:
+        acc = accuracy_vs_fp64(w, h, u, v, local, w["days"] if args.days is None else args.days)
 
     # CPU baseline: the oracle (C++ restatement) on the host cores, rank 0
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline_sample(h, u, v, budget_s=args.cpu_budget)
+        cpu = cpu_baseline_sample(w, h, u, v, budget_s=args.cpu_budget)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded balanced zonal flow u0=%.2f m/s + Y_lm (l<=64) height "
-                    "perturbation, 10 m RMS" % info["u0"],
-            "config": {"workload": "6 panels x 385^2 nodes (N=384), SBP 4/2 (d42), RK4 dt=120 s, "
-                                   "FP32 fused form (compensated stage sums, FP64 metric precompute)",
-                       "N": N_BENCH, "sbp": "d42", "dt_s": DT, "nodes_per_field": npts,
+            "data": _data_desc(w, info),
+            "config": {"workload": w["desc"] + ", FP32 fused form (compensated stage sums, FP64 "
+                                               "metric precompute)",
+                       "N": N, "sbp": "d%d" % ORDER, "dt_s": DT, "nodes_per_field": npts,
                        "l2": "256 MB buffer written between timed steps",
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "e2e": {"value": round(e2e_val, 3), "unit": "steps/s",
@@ -255,7 +328,7 @@ def run_gpu_arm(args):
                     "path": "swm_state_upload (pinned FP64 host) + swm_rk4_step + swm_state_download"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "kernel": "stage_kernel<float,42>", "peak_source": peak_kind,
+                         "kernel": "stage_tma_kernel<float,%d,mode>" % ORDER, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "avg_launch_us": round(stage_ms / stage_n * 1e3, 3),
                          "edge_kernel_avg_us": round(edge_ms / max(edge_n, 1) * 1e3, 3)},
@@ -265,7 +338,10 @@ def run_gpu_arm(args):
             "fp32_over_fp64": round((1e3 / ms_per_step) / (1e3 / fp64_ms), 3),
             "clocks": clocks,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "state_finite_after_timed_steps": finite,
         }
+        if acc:
+            line["accuracy_fp32_vs_fp64"] = acc
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -274,51 +350,52 @@ def run_gpu_arm(args):
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline_sample(h, u, v, budget_s=15.0, min_steps=1, max_steps=50):
+def cpu_baseline_sample(w, h, u, v, budget_s=15.0, min_steps=1, max_steps=50):
     """Time RK4 steps of the FP64 oracle with all host threads on a bounded
-    sample (whole N=384 steps until the time budget is used)."""
+    sample (whole steps of the workload until the time budget is used)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the CPU restatement of the reference (checker / baseline)
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    od = oracle.OracleDomain(N_BENCH, ORDER)
+    od = oracle.OracleDomain(w["N"], w["order"])
     hh, uu, vv = h.copy(), u.copy(), v.copy()
-    hh, uu, vv = od.rk4(hh, uu, vv, DT, 1)            # warm-up
+    hh, uu, vv = od.rk4(hh, uu, vv, w["dt"], 1)            # warm-up
     steps, t0 = 0, time.perf_counter()
     while steps < max_steps and (steps < min_steps or time.perf_counter() - t0 < budget_s):
-        hh, uu, vv = od.rk4(hh, uu, vv, DT, 1)
+        hh, uu, vv = od.rk4(hh, uu, vv, w["dt"], 1)
         steps += 1
     dt = time.perf_counter() - t0
     return {"value": round(steps / dt, 4), "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} RK4 steps of the N=384 FP64 oracle (C++ restatement of the reference), "
-                      f"OpenMP over panel rows"}
+            "sample": f"{steps} RK4 steps of the N={w['N']} d{w['order']} FP64 oracle (C++ restatement "
+                      f"of the reference), OpenMP over panel rows"}
 
 
 def run_reference_arm(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    h, u, v, info = _state(N_BENCH)
+    w = WORKLOADS[args.workload]
+    h, u, v, info = _state(w)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    od = oracle.OracleDomain(N_BENCH, ORDER)
+    od = oracle.OracleDomain(w["N"], w["order"])
     for _ in range(args.warmup):
-        h, u, v = od.rk4(h, u, v, DT, 1)
+        h, u, v = od.rk4(h, u, v, w["dt"], 1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        h, u, v = od.rk4(h, u, v, DT, 1)
+        h, u, v = od.rk4(h, u, v, w["dt"], 1)
     el = time.perf_counter() - t0
     val = args.steps / el
     line = {
         "metric": METRIC, "value": round(val, 4), "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-        "data": "synthetic: seeded balanced zonal flow + Y_lm (l<=64) height perturbation",
-        "config": {"workload": "6 panels x 385^2 nodes (N=384), SBP 4/2 (d42), RK4 dt=120 s, FP64",
-                   "N": N_BENCH, "sbp": "d42", "dt_s": DT},
+        "data": _data_desc(w, info),
+        "config": {"workload": w["desc"] + ", FP64", "N": w["N"], "sbp": "d%d" % w["order"],
+                   "dt_s": w["dt"]},
         "cpu_baseline": {"value": round(val, 4), "unit": "steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} RK4 steps of the FP64 C++ restatement of the reference "
                                    "(the Fortran/MPI reference has no compiler on this image)"},
@@ -333,7 +410,12 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--workload", default="n384_d42", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP32-vs-FP64 run over the workload's simulated days")
+    ap.add_argument("--days", type=float, default=None,
+                    help="simulated days of the accuracy run (default: the workload's)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--quick", action="store_true",
                     help="profiling case: time only the FP32 steps, print a short line")
