@@ -27,7 +27,7 @@ from ._abi import SWM_FP32_FUSED, SWM_FP64_PLAIN, SwmError
 __all__ = [
     "ModelConfig", "OperatorSWM", "StvecSWM", "GridField", "RK4", "HaloAhScalarSync",
     "EcsAhVecSyncCovariant", "create_timescheme", "create_halo_procedure",
-    "create_vector_halo_procedure", "SwmError", "EARTH",
+    "create_vector_halo_procedure", "Ensemble", "SwmError", "EARTH",
 ]
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -331,6 +331,98 @@ class EcsAhVecSyncCovariant:
 
     def get_halo_vector(self, u: GridField, v: GridField, halo_width: int = 0):
         self.op._check(self.op._L.swm_sync_vector_cov(self.op._h, u._h, v._h))
+
+
+class Ensemble:
+    """Independent members (own N, initial state and time step each; shared
+    SBP order, constants and precision) advanced together: one RK4 step of
+    all members is one CUDA graph with one stage-kernel and one edge-kernel
+    launch per RK stage.  No reference counterpart (the reference runs one
+    instance per job)."""
+
+    def __init__(self, config: ModelConfig, member_N, member_dt):
+        member_N = [int(x) for x in member_N]
+        member_dt = [float(x) for x in member_dt]
+        if len(member_N) != len(member_dt):
+            raise ValueError("member_N and member_dt differ in length")
+        self._L = _abi.load()
+        self.config = config
+        self.member_N = member_N
+        self.member_dt = member_dt
+        Ns = (ctypes.c_int * len(member_N))(*member_N)
+        dts = (ctypes.c_double * len(member_dt))(*member_dt)
+        h = ctypes.c_void_p()
+        rc = self._L.swm_ensemble_create(ctypes.byref(config.c_struct()), len(member_N), Ns, dts,
+                                         ctypes.byref(h))
+        _abi.check_ensemble(rc, None)
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.swm_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.member_N)
+
+    def _check(self, rc):
+        _abi.check_ensemble(rc, self._h)
+
+    def shape(self, m):
+        n = self.member_N[m] + 1
+        return (6, n, n)
+
+    def upload(self, m, h, u, v):
+        sh = self.shape(m)
+        h, u, v = (_host(a, sh) for a in (h, u, v))
+        self._check(self._L.swm_ensemble_upload(self._h, int(m), _ptr(h), _ptr(u), _ptr(v)))
+
+    def download(self, m):
+        out = tuple(np.empty(self.shape(m)) for _ in range(3))
+        self._check(self._L.swm_ensemble_download(self._h, int(m), *(_ptr(a) for a in out)))
+        return out
+
+    def get_diagnostics(self, m) -> dict:
+        out = np.zeros(7)
+        self._check(self._L.swm_ensemble_diagnostics(self._h, int(m), _ptr(out)))
+        return dict(zip(DIAG_KEYS, out.tolist()))
+
+    def step(self, nsteps: int = 1):
+        self._check(self._L.swm_ensemble_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        self._check(self._L.swm_ensemble_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return self._L.swm_ensemble_stream(self._h) or 0
+
+    def member(self, m):
+        """(context handle, state handle) of member m, for single-instance calls."""
+        c, s = ctypes.c_void_p(), ctypes.c_void_p()
+        self._check(self._L.swm_ensemble_member(self._h, int(m), ctypes.byref(c), ctypes.byref(s)))
+        return c, s
+
+    def set_shape(self, seg_rows: int, grid: int):
+        self._check(self._L.swm_ensemble_set_shape(self._h, int(seg_rows), int(grid)))
+
+    def get_shape(self) -> dict:
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.swm_ensemble_get_shape(self._h, ctypes.byref(a), ctypes.byref(b),
+                                                   ctypes.byref(c)))
+        return {"seg_rows": a.value, "grid": b.value, "units": c.value}
+
+    def tune(self, steps: int = 5) -> dict:
+        a, b, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._check(self._L.swm_ensemble_tune(self._h, int(steps), ctypes.byref(a), ctypes.byref(b),
+                                              ctypes.byref(ms)))
+        return {"seg_rows": a.value, "grid": b.value, "ms_per_step": ms.value}
 
 
 def create_timescheme(name: str) -> RK4:

@@ -35,6 +35,10 @@ EXPORTS = (
     "swm_op_massflux", "swm_op_ke", "swm_op_grad", "swm_op_div", "swm_op_curl",
     "swm_op_coriolis", "swm_sync_scalar", "swm_sync_vector_cov", "swm_quadrature_mass",
     "swm_timing_enable", "swm_timing_read", "swm_sync_scalar_static",
+    "swm_ensemble_create", "swm_ensemble_destroy", "swm_ensemble_last_error", "swm_ensemble_size",
+    "swm_ensemble_member", "swm_ensemble_upload", "swm_ensemble_download",
+    "swm_ensemble_diagnostics", "swm_ensemble_step", "swm_ensemble_synchronize",
+    "swm_ensemble_stream", "swm_ensemble_set_shape", "swm_ensemble_get_shape", "swm_ensemble_tune",
 )
 
 
@@ -127,6 +131,21 @@ def load(build_if_missing: bool = True):
     sig("swm_timing_read", I, VP, _D, ctypes.POINTER(ctypes.c_long), _D,
         ctypes.POINTER(ctypes.c_long))
     sig("swm_sync_scalar_static", I, VP, VP)
+    IP = ctypes.POINTER(ctypes.c_int)
+    sig("swm_ensemble_create", I, ctypes.POINTER(SwmConfig), I, IP, _D, PP)
+    sig("swm_ensemble_destroy", None, VP)
+    sig("swm_ensemble_last_error", C, VP)
+    sig("swm_ensemble_size", I, VP)
+    sig("swm_ensemble_member", I, VP, I, PP, PP)
+    sig("swm_ensemble_upload", I, VP, I, _D, _D, _D)
+    sig("swm_ensemble_download", I, VP, I, _D, _D, _D)
+    sig("swm_ensemble_diagnostics", I, VP, I, _D)
+    sig("swm_ensemble_step", I, VP, I)
+    sig("swm_ensemble_synchronize", I, VP)
+    sig("swm_ensemble_stream", VP, VP)
+    sig("swm_ensemble_set_shape", I, VP, I, I)
+    sig("swm_ensemble_get_shape", I, VP, IP, IP, IP)
+    sig("swm_ensemble_tune", I, VP, I, IP, IP, _D)
     _lib = L
     return L
 
@@ -134,4 +153,10 @@ def load(build_if_missing: bool = True):
 def check(rc: int, ctx=None) -> None:
     if rc != SWM_OK:
         msg = load().swm_last_error(ctx)
+        raise SwmError(rc, msg.decode() if msg else "")
+
+
+def check_ensemble(rc: int, ens=None) -> None:
+    if rc != SWM_OK:
+        msg = load().swm_ensemble_last_error(ens)
         raise SwmError(rc, msg.decode() if msg else "")

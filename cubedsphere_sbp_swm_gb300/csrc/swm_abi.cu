@@ -5,6 +5,7 @@
 #include "swm_launch.h"
 #include "swm_ops.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -208,9 +209,10 @@ int cuda_fail(swm_ctx* c, cudaError_t e, const char* where) {
 long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
 // Work units of the fused stage kernel: column strips x row segments, as
-// many as fit on the GPU at once (target_ctas) so no CTA waits for a wave.
+// many as fit on the GPU at once (target_ctas) so no CTA waits for a wave,
+// or exactly nseg_fixed row segments per strip when that is > 0.
 bool make_units(const SbpC& s, int n, int threads, int target_ctas, std::vector<WorkUnit>& out,
-                std::string& why) {
+                std::string& why, int nseg_fixed = 0) {
   auto need_lo = [&](int k) {
     if (k < s.ne) return 0;
     if (k >= n - s.ne) return n - s.last[n - 1 - k];
@@ -238,6 +240,7 @@ bool make_units(const SbpC& s, int n, int threads, int target_ctas, std::vector<
   const int min_rows = 8;
   int nseg = std::max(1, target_ctas / (6 * nstrip));
   nseg = std::min(nseg, std::max(1, n / min_rows));
+  if (nseg_fixed > 0) nseg = std::min(nseg_fixed, n);
   for (int p = 0; p < 6; ++p)
     for (int k = 0; k < nstrip; ++k)
       for (int r = 0; r < nseg; ++r) {
@@ -348,7 +351,7 @@ int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
   CK(launch_stage<T>(ctx->order, &maps, I, nullptr, ctx->units, ctx->nunits, mode,
-                     ctx->shape.boxw, ctx->derr, ctx->st),
+                     ctx->shape.boxw, 0, ctx->derr, ctx->st),
      "stage kernel");
   if (ctx->timing) {
     CK(cudaEventRecord(b, ctx->st), "event record");
@@ -1142,6 +1145,370 @@ int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches, double
   ctx->ev_stage.clear();
   ctx->ev_edge.clear();
   return SWM_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Ensembles: independent instances (each with its own N, initial state and
+// time step) advanced together.  Every member is a full context (geometry,
+// buffers, diagnostics); the ensemble adds one table of instances and tensor
+// maps per RK stage, the work units of all members in one list, and one
+// CUDA graph of the RK4 step: per stage one persistent stage-kernel launch
+// and one edge-kernel launch for all members.
+// ===========================================================================
+struct swm_ensemble {
+  int nmem = 0, order = 42, prec = SWM_FP32_FUSED, device = 0;
+  std::vector<swm_ctx*> mem;
+  std::vector<swm_state*> state;
+  std::vector<double> dt;
+  cudaStream_t st = nullptr;
+  int boxw = 0, max_n = 0, num_sms = 0, occ = 0, cols = 0;
+  StageMaps* dmaps = nullptr;        // [4 stages][nmem]
+  void* dinst = nullptr;             // InstDev<T> [4 stages][nmem]
+  WorkUnit* dunits = nullptr;
+  int nunits = 0, cap_units = 0;
+  int seg_rows = 0;                  // rows per work unit (0: whole panel height)
+  int grid = 0;                      // persistent CTAs (0: one CTA per unit)
+  cudaGraphExec_t graph = nullptr;
+  std::string err;
+};
+
+namespace {
+
+int efail(swm_ensemble* e, int code, const std::string& msg) {
+  if (e) e->err = msg; else g_err = msg;
+  return code;
+}
+#define ECK(call, where)                                                              \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return efail(ens, e_ == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,   \
+                   std::string(where) + ": " + cudaGetErrorString(e_));               \
+  } while (0)
+#define EMEM(call)                                                                    \
+  do {                                                                                \
+    if (int rc_ = (call)) return efail(ens, rc_, mem_err(ens));                        \
+  } while (0)
+
+std::string mem_err(swm_ensemble* ens) {
+  for (swm_ctx* c : ens->mem)
+    if (c && !c->err.empty()) return c->err;
+  return g_err;
+}
+
+// Work units of every member: `seg_rows` rows per unit (0: one segment per
+// strip), largest units first so the persistent CTAs finish together.
+int ens_units(swm_ensemble* ens, int seg_rows) {
+  std::vector<WorkUnit> all;
+  std::string why;
+  for (int m = 0; m < ens->nmem; ++m) {
+    const swm_ctx* c = ens->mem[m];
+    const int nseg = seg_rows > 0 ? std::max(1, (c->n + seg_rows - 1) / seg_rows) : 1;
+    std::vector<WorkUnit> u;
+    if (!make_units(kTables[sbp_index(c->order)], c->n, ens->cols, 1, u, why, nseg))
+      return efail(ens, SWM_E_INVALID, why);
+    for (WorkUnit& w : u) { w.inst = (int16_t)m; all.push_back(w); }
+  }
+  std::stable_sort(all.begin(), all.end(), [](const WorkUnit& a, const WorkUnit& b) {
+    return (a.rl1 - a.rl0) * (a.cl1 - a.cl0) > (b.rl1 - b.rl0) * (b.cl1 - b.cl0);
+  });
+  if ((int)all.size() > ens->cap_units) {
+    if (ens->dunits) cudaFree(ens->dunits);
+    ens->dunits = nullptr;
+    ens->cap_units = 0;
+    ECK(cudaMalloc(&ens->dunits, sizeof(WorkUnit) * all.size()), "alloc units");
+    ens->cap_units = (int)all.size();
+  }
+  ECK(cudaMemcpy(ens->dunits, all.data(), sizeof(WorkUnit) * all.size(), cudaMemcpyHostToDevice),
+      "copy units");
+  ens->nunits = (int)all.size();
+  ens->seg_rows = seg_rows;
+  return SWM_OK;
+}
+
+// Instance and tensor-map tables of the four RK stages (the member time
+// steps are in the stage coefficients).
+template <class T>
+int ens_tables(swm_ensemble* ens) {
+  const int M = ens->nmem;
+  std::vector<InstDev<T>> inst(4 * M);
+  std::vector<StageMaps> maps(4 * M);
+  for (int m = 0; m < M; ++m) {
+    swm_ctx* c = ens->mem[m];
+    swm_state* s = ens->state[m];
+    const double dt = ens->dt[m];
+    T* v0 = (T*)s->hi;
+    T* ya = (T*)c->ya;
+    T* yb = (T*)c->yb;
+    T* acc = (T*)c->acc;
+    for (int i = 0; i < 4; ++i) {
+      InstDev<T> I = base_inst<T>(c);
+      I.acc = acc;
+      switch (i) {   // the stage coefficients of enqueue_rk4 (rk4_mod.f90:20-42)
+        case 0: I.in = v0; I.base = v0; I.out = ya; I.c_in = (T)(0.5 * dt); I.c_acc = (T)(dt / 6.0); break;
+        case 1: I.in = ya; I.base = v0; I.out = yb; I.c_in = (T)(0.5 * dt); I.c_acc = (T)(dt / 3.0); break;
+        case 2: I.in = yb; I.base = v0; I.out = ya; I.c_in = (T)dt; I.c_acc = (T)(dt / 3.0); break;
+        default:
+          I.in = ya; I.base = v0; I.out = nullptr; I.base_out = v0;
+          I.base_lo = s->lo ? (T*)(void*)s->lo : nullptr; I.c_acc = (T)(dt / 6.0);
+      }
+      if (int rc = make_maps<T>(c, I, MODE_RK1 + i, &maps[i * M + m])) return efail(ens, rc, c->err);
+      I.maps = c->shape.tma ? ens->dmaps + i * M + m : nullptr;
+      inst[i * M + m] = I;
+    }
+  }
+  ECK(cudaMemcpy(ens->dmaps, maps.data(), sizeof(StageMaps) * maps.size(), cudaMemcpyHostToDevice),
+      "copy maps");
+  ECK(cudaMemcpy(ens->dinst, inst.data(), sizeof(InstDev<T>) * inst.size(), cudaMemcpyHostToDevice),
+      "copy instances");
+  return SWM_OK;
+}
+
+// Capture one ensemble RK4 step into ens->graph.
+template <class T>
+int ens_capture(swm_ensemble* ens) {
+  if (ens->graph) { cudaGraphExecDestroy(ens->graph); ens->graph = nullptr; }
+  const InstDev<T>* I = (const InstDev<T>*)ens->dinst;
+  const Topology& tp = ens->mem[0]->topo;
+  int* derr = ens->mem[0]->derr;
+  cudaGraph_t g;
+  ECK(cudaStreamBeginCapture(ens->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
+    e = launch_stage<T>(ens->order, nullptr, InstDev<T>{}, I + i * ens->nmem, ens->dunits,
+                        ens->nunits, MODE_RK1 + i, ens->boxw, ens->grid, derr, ens->st);
+    if (e == cudaSuccess)
+      e = launch_edge<T>(InstDev<T>{}, I + i * ens->nmem, ens->nmem, ens->max_n, tp, MODE_RK1 + i,
+                         ens->st);
+  }
+  cudaError_t ec = cudaStreamEndCapture(ens->st, &g);
+  if (e != cudaSuccess) { if (ec == cudaSuccess) cudaGraphDestroy(g); ECK(e, "ensemble stage launch"); }
+  ECK(ec, "end capture");
+  cudaError_t ei = cudaGraphInstantiate(&ens->graph, g, 0);
+  cudaGraphDestroy(g);
+  ECK(ei, "graph instantiate");
+  return SWM_OK;
+}
+
+int ens_rebuild(swm_ensemble* ens, int seg_rows, int grid) {
+  if (int rc = ens_units(ens, seg_rows)) return rc;
+  ens->grid = grid;
+  const bool f32 = ens->prec == SWM_FP32_FUSED;
+  if (int rc = f32 ? ens_tables<float>(ens) : ens_tables<double>(ens)) return rc;
+  return f32 ? ens_capture<float>(ens) : ens_capture<double>(ens);
+}
+
+int ens_check_member(swm_ensemble* ens, int m) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  if (m < 0 || m >= ens->nmem) return efail(ens, SWM_E_INVALID, "member index out of range");
+  cudaSetDevice(ens->device);
+  ECK(cudaStreamSynchronize(ens->st), "sync");
+  return SWM_OK;
+}
+
+void free_ensemble(swm_ensemble* ens) {
+  if (!ens) return;
+  cudaSetDevice(ens->device);
+  if (ens->st) cudaStreamSynchronize(ens->st);
+  if (ens->graph) cudaGraphExecDestroy(ens->graph);
+  if (ens->dmaps) cudaFree(ens->dmaps);
+  if (ens->dinst) cudaFree(ens->dinst);
+  if (ens->dunits) cudaFree(ens->dunits);
+  for (size_t m = 0; m < ens->mem.size(); ++m) {
+    if (m < ens->state.size() && ens->state[m]) swm_state_free(ens->state[m]);
+    swm_ctx_destroy(ens->mem[m]);
+  }
+  if (ens->st) cudaStreamDestroy(ens->st);
+  delete ens;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_ensemble_create(const swm_config* base, int nmembers, const int* member_N,
+                        const double* member_dt, swm_ensemble** out) {
+  swm_ensemble* ens = nullptr;
+  if (!base || !member_N || !member_dt || !out) return efail(nullptr, SWM_E_INVALID, "null argument");
+  if (nmembers < 1 || nmembers > 32767) return efail(nullptr, SWM_E_INVALID, "member count out of range");
+  for (int m = 0; m < nmembers; ++m)
+    if (!(member_dt[m] > 0.0)) return efail(nullptr, SWM_E_INVALID, "member time steps must be positive");
+  ens = new swm_ensemble();
+  ens->nmem = nmembers;
+  ens->order = base->sbp_order;
+  ens->prec = base->precision;
+  ens->device = base->device;
+  ens->dt.assign(member_dt, member_dt + nmembers);
+  auto bail = [&](int rc, const std::string& msg) {
+    free_ensemble(ens);
+    return efail(nullptr, rc, msg);
+  };
+  for (int m = 0; m < nmembers; ++m) {
+    swm_config c = *base;
+    c.N = member_N[m];
+    swm_ctx* ctx = nullptr;
+    if (int rc = swm_ctx_create(&c, &ctx)) return bail(rc, "member " + std::to_string(m) + ": " + g_err);
+    ens->mem.push_back(ctx);
+    swm_state* s = nullptr;
+    if (int rc = swm_state_create(ctx, &s)) return bail(rc, ctx->err);
+    ens->state.push_back(s);
+    ens->max_n = std::max(ens->max_n, ctx->n);
+    ens->boxw = std::max(ens->boxw, ctx->shape.boxw);
+    ens->cols = ctx->shape.cols;
+    ens->num_sms = ctx->num_sms;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&ens->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ens->dmaps, sizeof(StageMaps) * 4 * nmembers);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&ens->dinst, (ens->prec == SWM_FP32_FUSED ? sizeof(InstDev<float>) : sizeof(InstDev<double>)) *
+                                    4 * nmembers);
+  if (e != cudaSuccess)
+    return bail(e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
+                std::string("ensemble alloc: ") + cudaGetErrorString(e));
+  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw)
+                                         : stage_occupancy<double>(ens->order, ens->boxw);
+  // default tile shape: whole-panel strips on persistent CTAs (FP32) or one
+  // CTA per unit of 64 rows (FP64); swm_ensemble_tune measures the others
+  const bool f32 = ens->prec == SWM_FP32_FUSED;
+  if (int rc = ens_rebuild(ens, f32 ? 0 : 64, f32 ? std::max(1, ens->occ) * ens->num_sms : 0))
+    return bail(rc, ens->err);
+  *out = ens;
+  return SWM_OK;
+}
+
+void swm_ensemble_destroy(swm_ensemble* ens) { free_ensemble(ens); }
+
+const char* swm_ensemble_last_error(const swm_ensemble* ens) {
+  return ens ? ens->err.c_str() : g_err.c_str();
+}
+
+int swm_ensemble_size(const swm_ensemble* ens) { return ens ? ens->nmem : 0; }
+
+int swm_ensemble_member(swm_ensemble* ens, int m, swm_ctx** ctx, swm_state** state) {
+  if (int rc = ens_check_member(ens, m)) return rc;
+  if (ctx) *ctx = ens->mem[m];
+  if (state) *state = ens->state[m];
+  return SWM_OK;
+}
+
+int swm_ensemble_upload(swm_ensemble* ens, int m, const double* h, const double* u, const double* v) {
+  if (int rc = ens_check_member(ens, m)) return rc;
+  EMEM(swm_state_upload(ens->mem[m], ens->state[m], h, u, v));
+  ECK(cudaStreamSynchronize(ens->mem[m]->st), "sync");
+  return SWM_OK;
+}
+
+int swm_ensemble_download(swm_ensemble* ens, int m, double* h, double* u, double* v) {
+  if (int rc = ens_check_member(ens, m)) return rc;
+  EMEM(swm_state_download(ens->mem[m], ens->state[m], h, u, v));
+  return SWM_OK;
+}
+
+int swm_ensemble_diagnostics(swm_ensemble* ens, int m, double out[7]) {
+  if (int rc = ens_check_member(ens, m)) return rc;
+  EMEM(swm_diagnostics(ens->mem[m], ens->state[m], out));
+  return SWM_OK;
+}
+
+int swm_ensemble_step(swm_ensemble* ens, int nsteps) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  if (nsteps < 0) return efail(ens, SWM_E_INVALID, "nsteps must be >= 0");
+  cudaSetDevice(ens->device);
+  for (int k = 0; k < nsteps; ++k) ECK(cudaGraphLaunch(ens->graph, ens->st), "graph launch");
+  return SWM_OK;
+}
+
+int swm_ensemble_synchronize(swm_ensemble* ens) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  cudaSetDevice(ens->device);
+  ECK(cudaStreamSynchronize(ens->st), "sync");
+  EMEM(check_device_flag(ens->mem[0]));
+  return SWM_OK;
+}
+
+void* swm_ensemble_stream(swm_ensemble* ens) { return ens ? (void*)ens->st : nullptr; }
+
+int swm_ensemble_set_shape(swm_ensemble* ens, int seg_rows, int grid) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  if (seg_rows < 0 || grid < 0) return efail(ens, SWM_E_INVALID, "tile shape must be >= 0");
+  cudaSetDevice(ens->device);
+  ECK(cudaStreamSynchronize(ens->st), "sync");
+  return ens_rebuild(ens, seg_rows, grid);
+}
+
+int swm_ensemble_get_shape(const swm_ensemble* ens, int* seg_rows, int* grid, int* nunits) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  if (seg_rows) *seg_rows = ens->seg_rows;
+  if (grid) *grid = ens->grid;
+  if (nunits) *nunits = ens->nunits;
+  return SWM_OK;
+}
+
+int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid_out,
+                      double* ms_per_step_out) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  if (steps < 1) return efail(ens, SWM_E_INVALID, "steps must be >= 1");
+  cudaSetDevice(ens->device);
+  ECK(cudaStreamSynchronize(ens->st), "sync");
+  // the trial steps advance the members: keep their states and restore them
+  const int M = ens->nmem;
+  std::vector<void*> keep(M, nullptr);
+  std::vector<size_t> hib(M), lob(M);
+  int rc = SWM_OK;
+  for (int m = 0; m < M && rc == SWM_OK; ++m) {
+    swm_ctx* c = ens->mem[m];
+    hib[m] = (size_t)c->elt * 3 * c->fs;
+    lob[m] = ens->state[m]->lo ? sizeof(float) * 3 * c->fs : 0;
+    if (cudaMalloc(&keep[m], hib[m] + lob[m]) != cudaSuccess) { rc = efail(ens, SWM_E_NOMEM, "tune: alloc"); break; }
+    cudaMemcpyAsync(keep[m], ens->state[m]->hi, hib[m], cudaMemcpyDeviceToDevice, ens->st);
+    if (lob[m]) cudaMemcpyAsync((char*)keep[m] + hib[m], ens->state[m]->lo, lob[m], cudaMemcpyDeviceToDevice, ens->st);
+  }
+  auto restore = [&]() {
+    for (int m = 0; m < M; ++m) {
+      if (!keep[m]) continue;
+      cudaMemcpyAsync(ens->state[m]->hi, keep[m], hib[m], cudaMemcpyDeviceToDevice, ens->st);
+      if (lob[m]) cudaMemcpyAsync(ens->state[m]->lo, (char*)keep[m] + hib[m], lob[m], cudaMemcpyDeviceToDevice, ens->st);
+    }
+  };
+  const int segs[] = {0, 192, 128, 96, 64, 48, 32, 24, 16};
+  const int persistent = std::max(1, ens->occ) * ens->num_sms;
+  const int grids[] = {persistent, 0};
+  double best = 1e30;
+  int best_seg = ens->seg_rows, best_grid = ens->grid;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (rc == SWM_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess))
+    rc = efail(ens, SWM_E_CUDA, "tune: events");
+  for (int si = 0; si < (int)(sizeof(segs) / sizeof(segs[0])) && rc == SWM_OK; ++si) {
+    if (segs[si] > 0 && segs[si] >= ens->max_n) continue;
+    for (int gi = 0; gi < 2 && rc == SWM_OK; ++gi) {
+      if (ens->prec != SWM_FP32_FUSED && grids[gi] != 0) continue;  // FP64 kernel: one CTA per unit
+      if ((rc = ens_rebuild(ens, segs[si], grids[gi]))) break;
+      cudaGraphLaunch(ens->graph, ens->st);                          // warm-up
+      cudaEventRecord(a, ens->st);
+      for (int k = 0; k < steps; ++k) cudaGraphLaunch(ens->graph, ens->st);
+      cudaEventRecord(b, ens->st);
+      if (cudaEventSynchronize(b) != cudaSuccess) { rc = efail(ens, SWM_E_CUDA, "tune: sync"); break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      restore();
+      if (ms / steps < best) { best = ms / steps; best_seg = segs[si]; best_grid = grids[gi]; }
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  restore();
+  cudaStreamSynchronize(ens->st);
+  for (void* p : keep) if (p) cudaFree(p);
+  if (rc == SWM_OK) rc = ens_rebuild(ens, best_seg, best_grid);
+  if (rc == SWM_OK) {
+    EMEM(check_device_flag(ens->mem[0]));
+    if (seg_rows_out) *seg_rows_out = best_seg;
+    if (grid_out) *grid_out = best_grid;
+    if (ms_per_step_out) *ms_per_step_out = best;
+  }
+  return rc;
 }
 
 }  // extern "C"

@@ -169,6 +169,7 @@ struct InstDev {
   T* base_lo;                 // FP32 RK4 final stage: S_lo; S_hi is written via base_out
   T* base_out;                // final stage: new state (FP64 v0 / FP32 S_hi)
   T* edge;                    // edge buffer (6*4*4*n)
+  const StageMaps* maps;      // TMA maps of this instance (batched launches; else null)
   T c_in;                     // stage coefficient for the next stage state
   T c_acc;                    // stage coefficient for the running sum
   T ghs;                      // 1 / (hx * a)

@@ -6,14 +6,16 @@
 
 namespace swm {
 
-// Fused stage kernel over nunits work units (one CTA each).  maps describes
-// the buffers of this launch to the TMA unit and boxw is the widest TMA box
-// of the instances (TMA kernels only); err is the device error flag raised
-// by an expired bounded wait.
+// Fused stage kernel over nunits work units.  maps describes the buffers of
+// a one-instance launch to the TMA unit (batched instances carry their own
+// maps in InstDev::maps) and boxw is the widest TMA box of the instances
+// (TMA kernels only); grid > 0 runs the TMA kernel persistently on that many
+// CTAs (0: one CTA per unit); err is the device error flag raised by an
+// expired bounded wait.
 template <class T>
 cudaError_t launch_stage(int order, const StageMaps* maps, const InstDev<T>& one,
                          const InstDev<T>* many, const WorkUnit* units, int nunits, int mode,
-                         int boxw, int* err, cudaStream_t st);
+                         int boxw, int grid, int* err, cudaStream_t st);
 // Sets the launch attributes of the stage kernel of one SBP order (called at
 // context creation, outside any stream capture) and returns its shape; the
 // shape's boxw is the widest box the kernel supports.

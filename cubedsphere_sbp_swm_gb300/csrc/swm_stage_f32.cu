@@ -8,14 +8,14 @@ namespace swm {
 template <>
 cudaError_t launch_stage<float>(int order, const StageMaps* maps, const InstDev<float>& one,
                                 const InstDev<float>* many, const WorkUnit* units, int nunits,
-                                int mode, int boxw, int* err, cudaStream_t st) {
+                                int mode, int boxw, int grid, int* err, cudaStream_t st) {
   static const StageMaps kNone{};
   const StageMaps& m = maps ? *maps : kNone;
   switch (order) {
-    case 21: return launch_stage_tma_ord<float, 21>(m, one, many, units, nunits, mode, boxw, err, st);
-    case 42: return launch_stage_tma_ord<float, 42>(m, one, many, units, nunits, mode, boxw, err, st);
-    case 43: return launch_stage_tma_ord<float, 43>(m, one, many, units, nunits, mode, boxw, err, st);
-    case 63: return launch_stage_tma_ord<float, 63>(m, one, many, units, nunits, mode, boxw, err, st);
+    case 21: return launch_stage_tma_ord<float, 21>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 42: return launch_stage_tma_ord<float, 42>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 43: return launch_stage_tma_ord<float, 43>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 63: return launch_stage_tma_ord<float, 63>(m, one, many, units, nunits, mode, boxw, grid, err, st);
     default: return cudaErrorInvalidValue;
   }
 }

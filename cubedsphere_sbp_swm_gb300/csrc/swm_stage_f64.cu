@@ -9,8 +9,9 @@ namespace swm {
 template <>
 cudaError_t launch_stage<double>(int order, const StageMaps* maps, const InstDev<double>& one,
                                  const InstDev<double>* many, const WorkUnit* units, int nunits,
-                                 int mode, int boxw, int* err, cudaStream_t st) {
+                                 int mode, int boxw, int grid, int* err, cudaStream_t st) {
   (void)err;
+  (void)grid;
   (void)boxw;
   (void)maps;
   switch (order) {
@@ -33,7 +34,7 @@ static int v1_occupancy() {
 template <>
 cudaError_t prepare_stage<double>(int order, StageShape* shape) {
   cudaError_t e = launch_stage<double>(order, nullptr, InstDev<double>{}, nullptr, nullptr, 0,
-                                       MODE_APPLY, 0, nullptr, nullptr);
+                                       MODE_APPLY, 0, 0, nullptr, nullptr);
   int* ctas_per_sm = &shape->ctas_per_sm;
   if (e != cudaSuccess) return e;
   switch (order) {

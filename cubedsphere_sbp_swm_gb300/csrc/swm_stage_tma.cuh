@@ -212,10 +212,37 @@ __device__ __forceinline__ void rk_store(T* outp, T* accp, T* bop, T* blp, int o
   }
 }
 
+// Stage-ring slot layout of one work unit: element offsets of its boxes for
+// the unit's box width bw (the slots themselves are sized for the widest box
+// of the launch).
+struct StageOffsets {
+  int in, met, metf, base, acc, lo, hs;
+};
+template <class L>
+__device__ __forceinline__ StageOffsets stage_offsets(int bw, int esz) {
+  const auto sl = L::stage(bw);
+  return StageOffsets{(int)(sl.o_in / esz), (int)(sl.o_met / esz), (int)(sl.o_metf / esz),
+                      (int)(sl.o_base / esz), (int)(sl.o_acc / esz), (int)(sl.o_lo / esz),
+                      (int)(sl.o_hs / esz)};
+}
+
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                   reinterpret_cast<uint64_t>(m))
+               : "memory");
+}
+
+// Persistent over work units: CTA b runs units b, b + gridDim.x, ...; the
+// pipeline's chunk count (and so every mbarrier phase) runs on across units,
+// so the producer streams the next unit while the consumers finish the last.
+// A unit takes its tensor maps from its instance (InstDev::maps, global
+// memory; batched launches) or from the kernel parameter (one instance).
+// slot_bw is the widest box width of the launch (ring slot size).
 template <class T, int ORD, int MODE>
 __global__ void __launch_bounds__(TMA_THREADS)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
-                     const InstDev<T>* many, const WorkUnit* units, int* err) {
+                     const InstDev<T>* many, const WorkUnit* units, int nunits, int slot_bw,
+                     int* err) {
   using L = TmaLayout<T, ORD>;
   constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, AL = L::ALIGN, WS = L::WS,
                 RBX = L::RBX;
@@ -236,24 +263,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 2 * NST * 8);
   T* xring = reinterpret_cast<T*>(smem + L::head);
   unsigned char* stg = smem + L::head + L::r128(L::xring);
-
-  const WorkUnit wu = units[blockIdx.x];
-  const InstDev<T>& I = many ? many[wu.inst] : one;
-  const int n = I.n, P = I.P;
-  const int rl0 = wu.rl0, rl1 = wu.rl1, j0u = wu.j0, j1u = wu.j1;
+  const size_t st_bytes = L::stage(slot_bw).bytes;   // ring slot stride
   const int tid = threadIdx.x;
-  const int cal = wu.cl0 & ~(AL - 1);         // 16-byte aligned box start column
-  const int prow = wu.panel * n;              // row of this panel in the (6n)-row tensors
-  const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
-  const bool hasHs = I.hs != nullptr;
-  const int bw = I.boxw;                      // box width (columns)
-  // stage layout as plain scalars (element offsets of the boxes in a stage)
-  const size_t st_bytes = L::stage(bw).bytes;
-  const int e_in = (int)(L::stage(bw).o_in / sizeof(T)), e_met = (int)(L::stage(bw).o_met / sizeof(T)),
-            e_metf = (int)(L::stage(bw).o_metf / sizeof(T)), e_base = (int)(L::stage(bw).o_base / sizeof(T)),
-            e_acc = (int)(L::stage(bw).o_acc / sizeof(T)), e_lo = (int)(L::stage(bw).o_lo / sizeof(T)),
-            e_hs = (int)(L::stage(bw).o_hs / sizeof(T));
-  const uint32_t rowb = (uint32_t)(bw * RPS * (int)sizeof(T));  // one field, RPS rows
 
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
@@ -268,40 +279,57 @@ __global__ void __launch_bounds__(TMA_THREADS)
   // ------------------------------------------------------------ producer
   if (tid >= TMA_CONS) {
     if (tid == TMA_CONS) {
-      int issued = 0;
-      for (int c = 0; c < nch; ++c) {
-        const int s = c % NST;
-        const uint32_t ph = (uint32_t)(c / NST) & 1u;
-        if (*abort_flag) break;
-        if (c >= NST && !mbar_wait_bounded(&empty[s], ph ^ 1u, kWaitLimitNs)) {
-          *abort_flag = 1;
-          atomicExch(err, 1);
-          break;
+      int gc = 0;   // chunks issued over all units of this CTA
+      for (int u = blockIdx.x; u < nunits && !*abort_flag; u += gridDim.x) {
+        const WorkUnit wu = units[u];
+        const InstDev<T>& I = many ? many[wu.inst] : one;
+        const StageMaps* M = I.maps ? I.maps : &maps;
+        if (I.maps) {
+          tensormap_acquire(&M->in); tensormap_acquire(&M->met); tensormap_acquire(&M->metf);
+          tensormap_acquire(&M->base); tensormap_acquire(&M->acc); tensormap_acquire(&M->lo);
+          tensormap_acquire(&M->hs);
         }
-        const int r0 = rl0 + c * RPS, j0 = r0 - RMAX;
-        const bool in_any = r0 < rl1;
-        const bool out_any = j0 + RPS > j0u && j0 < j1u;
-        uint32_t tx = 0;
-        if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * rowb;
-        if (out_any)
-          tx += (uint32_t)(L::NF + (needB ? 3 : 0) + (needA ? 3 : 0) + (needL ? 3 : 0)) * rowb;
-        T* sb = reinterpret_cast<T*>(stg + (size_t)s * st_bytes);
-        mbar_arrive_expect_tx(&full[s], tx);
-        if (in_any) {
-          tma_load_3d(sb + e_in, &maps.in, cal, prow + r0, 0, &full[s]);
-          tma_load_3d(sb + e_met, &maps.met, cal, prow + r0, MJ, &full[s]);
-          if (hasHs) tma_load_3d(sb + e_hs, &maps.hs, cal, prow + r0, 0, &full[s]);
+        const int rl0 = wu.rl0, rl1 = wu.rl1, j0u = wu.j0, j1u = wu.j1;
+        const int cal = wu.cl0 & ~(AL - 1);     // 16-byte aligned box start column
+        const int prow = wu.panel * I.n;        // row of this panel in the (6n)-row tensors
+        const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
+        const bool hasHs = I.hs != nullptr;
+        const int bw = I.boxw;
+        const StageOffsets e = stage_offsets<L>(bw, (int)sizeof(T));
+        const uint32_t rowb = (uint32_t)(bw * RPS * (int)sizeof(T));  // one field, RPS rows
+        for (int c = 0; c < nch; ++c, ++gc) {
+          const int s = gc % NST;
+          const uint32_t ph = (uint32_t)(gc / NST) & 1u;
+          if (*abort_flag) break;
+          if (gc >= NST && !mbar_wait_bounded(&empty[s], ph ^ 1u, kWaitLimitNs)) {
+            *abort_flag = 1;
+            atomicExch(err, 1);
+            break;
+          }
+          const int r0 = rl0 + c * RPS, j0 = r0 - RMAX;
+          const bool in_any = r0 < rl1;
+          const bool out_any = j0 + RPS > j0u && j0 < j1u;
+          uint32_t tx = 0;
+          if (in_any) tx += (uint32_t)(3 + 4 + (hasHs ? 1 : 0)) * rowb;
+          if (out_any)
+            tx += (uint32_t)(L::NF + (needB ? 3 : 0) + (needA ? 3 : 0) + (needL ? 3 : 0)) * rowb;
+          T* sb = reinterpret_cast<T*>(stg + (size_t)s * st_bytes);
+          mbar_arrive_expect_tx(&full[s], tx);
+          if (in_any) {
+            tma_load_3d(sb + e.in, &M->in, cal, prow + r0, 0, &full[s]);
+            tma_load_3d(sb + e.met, &M->met, cal, prow + r0, MJ, &full[s]);
+            if (hasHs) tma_load_3d(sb + e.hs, &M->hs, cal, prow + r0, 0, &full[s]);
+          }
+          if (out_any) {
+            tma_load_3d(sb + e.metf, &M->metf, cal, prow + j0, MF, &full[s]);
+            if (needB) tma_load_3d(sb + e.base, &M->base, cal, prow + j0, 0, &full[s]);
+            if (needA) tma_load_3d(sb + e.acc, &M->acc, cal, prow + j0, 0, &full[s]);
+            if (needL) tma_load_3d(sb + e.lo, &M->lo, cal, prow + j0, 0, &full[s]);
+          }
         }
-        if (out_any) {
-          tma_load_3d(sb + e_metf, &maps.metf, cal, prow + j0, MF, &full[s]);
-          if (needB) tma_load_3d(sb + e_base, &maps.base, cal, prow + j0, 0, &full[s]);
-          if (needA) tma_load_3d(sb + e_acc, &maps.acc, cal, prow + j0, 0, &full[s]);
-          if (needL) tma_load_3d(sb + e_lo, &maps.lo, cal, prow + j0, 0, &full[s]);
-        }
-        issued = c + 1;
       }
       // drain: the copies of the last stages must have landed before exit
-      for (int c = max(0, issued - NST); c < issued; ++c)
+      for (int c = max(0, gc - NST); c < gc; ++c)
         if (!mbar_wait_bounded(&full[c % NST], (uint32_t)(c / NST) & 1u, kWaitLimitNs))
           atomicExch(err, 2);
     }
@@ -310,6 +338,21 @@ __global__ void __launch_bounds__(TMA_THREADS)
 
   // ------------------------------------------------------------ consumers
   const int t = tid;
+  int gc = 0;   // chunks consumed over all units of this CTA
+  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+  const WorkUnit wu = units[u];
+  const InstDev<T>& I = many ? many[wu.inst] : one;
+  const int n = I.n, P = I.P;
+  const int rl0 = wu.rl0, rl1 = wu.rl1, j0u = wu.j0, j1u = wu.j1;
+  const int cal = wu.cl0 & ~(AL - 1);
+  const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
+  const bool hasHs = I.hs != nullptr;
+  const int bw = I.boxw;
+  const StageOffsets eo = stage_offsets<L>(bw, (int)sizeof(T));
+  const int e_in = eo.in, e_met = eo.met, e_metf = eo.metf, e_base = eo.base, e_acc = eo.acc,
+            e_lo = eo.lo, e_hs = eo.hs;
+  // every consumer is done with the previous unit's x-ring rows
+  if (u != (int)blockIdx.x) consumers_sync();
   const int col = wu.cl0 + t;
   const bool ld = col < wu.cl1;
   const bool own = col >= wu.i0 && col < wu.i1;
@@ -346,9 +389,9 @@ __global__ void __launch_bounds__(TMA_THREADS)
 #pragma unroll
   for (int i = 0; i < WS; ++i) { yke[i] = T(0); yu[i] = T(0); ygv[i] = T(0); }
 
-  for (int c = 0; c < nch; ++c) {
-    const int s = c % NST;
-    const uint32_t ph = (uint32_t)(c / NST) & 1u;
+  for (int c = 0; c < nch; ++c, ++gc) {
+    const int s = gc % NST;
+    const uint32_t ph = (uint32_t)(gc / NST) & 1u;
     bool ok = true;
     if (!*abort_flag) ok = mbar_wait_bounded(&full[s], ph, kWaitLimitNs);
     if (!ok) { *abort_flag = 1; atomicExch(err, 3); }
@@ -438,12 +481,13 @@ __global__ void __launch_bounds__(TMA_THREADS)
     __syncwarp();
     if ((t & 31) == 0) mbar_arrive(&empty[s]);
   }
+  }  // units
 }
 
 template <class T, int ORD, int MODE>
 cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
                                   const InstDev<T>* many, const WorkUnit* units, int nunits,
-                                  int boxw, int* err, cudaStream_t st) {
+                                  int boxw, int grid, int* err, cudaStream_t st) {
   using L = TmaLayout<T, ORD>;
   static bool configured = false;
   if (!configured) {
@@ -454,21 +498,23 @@ cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
     configured = true;
   }
   if (nunits <= 0) return cudaSuccess;
-  stage_tma_kernel<T, ORD, MODE><<<nunits, TMA_THREADS, L::smem_bytes(boxw), st>>>(maps, one, many,
-                                                                                    units, err);
+  if (boxw < 1 || boxw > L::BOXW_MAX) return cudaErrorInvalidValue;
+  const int g = (grid > 0 && grid < nunits) ? grid : nunits;
+  stage_tma_kernel<T, ORD, MODE><<<g, TMA_THREADS, L::smem_bytes(boxw), st>>>(
+      maps, one, many, units, nunits, boxw, err);
   return cudaGetLastError();
 }
 
 template <class T, int ORD>
 cudaError_t launch_stage_tma_ord(const StageMaps& maps, const InstDev<T>& one,
                                  const InstDev<T>* many, const WorkUnit* units, int nunits,
-                                 int mode, int boxw, int* err, cudaStream_t st) {
+                                 int mode, int boxw, int grid, int* err, cudaStream_t st) {
   switch (mode) {
-    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY>(maps, one, many, units, nunits, boxw, err, st);
-    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1>(maps, one, many, units, nunits, boxw, err, st);
-    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2>(maps, one, many, units, nunits, boxw, err, st);
-    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3>(maps, one, many, units, nunits, boxw, err, st);
-    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4>(maps, one, many, units, nunits, boxw, err, st);
+    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4>(maps, one, many, units, nunits, boxw, grid, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -479,7 +525,7 @@ cudaError_t prepare_stage_tma_ord() {
   static const StageMaps kNone{};
   for (int m = MODE_APPLY; m <= MODE_RK4; ++m) {
     cudaError_t e = launch_stage_tma_ord<T, ORD>(kNone, InstDev<T>{}, nullptr, nullptr, 0, m,
-                                                 TmaLayout<T, ORD>::BOXW_MAX, nullptr, nullptr);
+                                                 TmaLayout<T, ORD>::BOXW_MAX, 0, nullptr, nullptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -88,6 +88,9 @@ def _area_rms(f, J):
     return math.sqrt(float(np.sum(J * f * f) / np.sum(J)))
 
 
+_LEGENDRE_CACHE: dict = {}
+
+
 def harmonic_perturbation(geo, seed: int, lmax: int, rms: float = 10.0) -> np.ndarray:
     """Random real spherical-harmonic field, degrees 1..lmax, spectrum l^-3,
     scaled to the given area-weighted RMS."""
@@ -95,7 +98,13 @@ def harmonic_perturbation(geo, seed: int, lmax: int, rms: float = 10.0) -> np.nd
     r = geo["r"]
     x = r[..., 2]                                  # sin(latitude) about the z axis
     lam = np.arctan2(r[..., 1], r[..., 0])
-    P = _legendre_all(lmax, x)
+    key = (geo["N"], lmax)
+    if _LEGENDRE_CACHE.get("key") != key:      # members of one resolution share it
+        _LEGENDRE_CACHE.clear()
+        _LEGENDRE_CACHE.update(key=key, P=_legendre_all(lmax, x))
+    P = _LEGENDRE_CACHE["P"]
+    cm = [np.cos(m * lam) for m in range(lmax + 1)]
+    sm = [np.sin(m * lam) for m in range(lmax + 1)]
     f = np.zeros_like(x)
     for l in range(1, lmax + 1):
         amp = float(l) ** -3
@@ -104,7 +113,7 @@ def harmonic_perturbation(geo, seed: int, lmax: int, rms: float = 10.0) -> np.nd
             if m == 0:
                 f += amp * a * P[(l, 0)] / math.sqrt(2.0 * math.pi)
             else:
-                f += amp * P[(l, m)] * (a * np.cos(m * lam) + b * np.sin(m * lam)) / math.sqrt(2.0 * math.pi)
+                f += amp * P[(l, m)] * (a * cm[m] + b * sm[m]) / math.sqrt(2.0 * math.pi)
     return f * (rms / _area_rms(f, geo["J"]))
 
 

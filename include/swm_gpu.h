@@ -201,6 +201,48 @@ int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches,
                     double* edge_ms, long* edge_launches);
 
 /* ---------------------------------------------------------------------- */
+/* Ensembles (no counterpart in the reference, which runs one instance per  */
+/* job): independent members, each with its own N, initial state and time   */
+/* step, sharing SBP order, constants and precision.  Each member is a full */
+/* context; an ensemble RK4 step is one CUDA graph with, per RK stage, one  */
+/* stage-kernel launch over the work units of all members (persistent CTAs  */
+/* in the FP32 form) and one edge-kernel launch.  Each member's arithmetic  */
+/* is exactly that of swm_rk4_step on the member alone.                     */
+/* ---------------------------------------------------------------------- */
+typedef struct swm_ensemble swm_ensemble;
+
+/* member_N[m], member_dt[m] for m < nmembers; base gives the rest. */
+int  swm_ensemble_create(const swm_config* base, int nmembers,
+                         const int* member_N, const double* member_dt,
+                         swm_ensemble** out);
+void swm_ensemble_destroy(swm_ensemble* ens);
+const char* swm_ensemble_last_error(const swm_ensemble* ens);
+int  swm_ensemble_size(const swm_ensemble* ens);
+/* Member m's context and state (for single-instance calls on it; call
+ * swm_ensemble_synchronize first). */
+int  swm_ensemble_member(swm_ensemble* ens, int m, swm_ctx** ctx,
+                         swm_state** state);
+/* Host arrays in the layout of swm_state_upload/download (member's N). */
+int  swm_ensemble_upload(swm_ensemble* ens, int m, const double* h,
+                         const double* u, const double* v);
+int  swm_ensemble_download(swm_ensemble* ens, int m, double* h, double* u,
+                           double* v);
+int  swm_ensemble_diagnostics(swm_ensemble* ens, int m, double out[7]);
+/* nsteps RK4 steps of every member (asynchronous on the ensemble stream). */
+int  swm_ensemble_step(swm_ensemble* ens, int nsteps);
+int  swm_ensemble_synchronize(swm_ensemble* ens);
+void* swm_ensemble_stream(swm_ensemble* ens);
+/* Tile shape: rows per work unit (0: whole panel height) and persistent
+ * CTAs of the stage kernel (0: one CTA per work unit). */
+int  swm_ensemble_set_shape(swm_ensemble* ens, int seg_rows, int grid);
+int  swm_ensemble_get_shape(const swm_ensemble* ens, int* seg_rows, int* grid,
+                            int* nunits);
+/* Autotuner: times `steps` ensemble steps for each candidate tile shape,
+ * keeps the fastest and restores the member states. */
+int  swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out,
+                       int* grid_out, double* ms_per_step_out);
+
+/* ---------------------------------------------------------------------- */
 /* Scalar cube-edge sync with static scratch (no counterpart in the        */
 /* reference; same result as swm_sync_scalar).                             */
 /*                                                                          */
