@@ -39,6 +39,9 @@ EXPORTS = (
     "swm_ensemble_member", "swm_ensemble_upload", "swm_ensemble_download",
     "swm_ensemble_diagnostics", "swm_ensemble_step", "swm_ensemble_synchronize",
     "swm_ensemble_stream", "swm_ensemble_set_shape", "swm_ensemble_get_shape", "swm_ensemble_tune",
+    "swm_apply_tl", "swm_apply_ad", "swm_rk4_tl", "swm_rk4_ad", "swm_adjoint_create",
+    "swm_adjoint_destroy", "swm_adjoint_forward", "swm_adjoint_backward", "swm_adjoint_counts",
+    "swm_state_upload_device", "swm_state_download_device", "swm_quadrature_weights",
 )
 
 
@@ -146,6 +149,19 @@ def load(build_if_missing: bool = True):
     sig("swm_ensemble_set_shape", I, VP, I, I)
     sig("swm_ensemble_get_shape", I, VP, IP, IP, IP)
     sig("swm_ensemble_tune", I, VP, I, IP, IP, _D)
+    LP = ctypes.POINTER(ctypes.c_long)
+    sig("swm_apply_tl", I, VP, VP, VP, VP)
+    sig("swm_apply_ad", I, VP, VP, VP, VP)
+    sig("swm_rk4_tl", I, VP, VP, VP, D)
+    sig("swm_rk4_ad", I, VP, VP, VP, D)
+    sig("swm_adjoint_create", I, VP, I, I, D, PP)
+    sig("swm_adjoint_destroy", None, VP)
+    sig("swm_adjoint_forward", I, VP, VP, VP)
+    sig("swm_adjoint_backward", I, VP, VP)
+    sig("swm_adjoint_counts", I, VP, LP, LP, LP)
+    sig("swm_state_upload_device", I, VP, VP, VP, VP, VP)
+    sig("swm_state_download_device", I, VP, VP, VP, VP, VP)
+    sig("swm_quadrature_weights", I, VP, _D)
     _lib = L
     return L
 

@@ -189,6 +189,15 @@ struct swm_ctx {
   // detaches them, so a later swm_state_free / swm_field_free stays safe
   std::set<swm_state*> states;
   std::set<swm_field*> fields;
+  // tangent-linear / adjoint workspace (FP64 contexts, allocated on first
+  // use): 10 work fields, then 7 states of 3 fields; edge buffer of the
+  // vector-sync transpose; transposed SBP table
+  double* adw = nullptr;
+  double* adC = nullptr;
+  SbpT sbpT{};
+  cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
+  const void* ad_key[2] = {nullptr, nullptr};
+  double ad_dt = 0.0;
 };
 
 namespace {
@@ -485,8 +494,9 @@ void free_ctx(swm_ctx* c) {
   for (auto& e : c->ev_edge) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   // hsT aliases hs64 in FP64 contexts: free each allocation once
   void* hsT = (c->hsT == (void*)c->hs64) ? nullptr : c->hsT;
+  if (c->ad_graph) cudaGraphExecDestroy(c->ad_graph);
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
-                  c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr};
+                  c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->hres) cudaFreeHost(c->hres);
   if (c->st) cudaStreamDestroy(c->st);
@@ -1509,6 +1519,411 @@ int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid
     if (ms_per_step_out) *ms_per_step_out = best;
   }
   return rc;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Tangent-linear and adjoint of the FP64 model operator and RK4 step, and
+// the binomially checkpointed gradient of a trajectory (no counterpart in the
+// reference).  The adjoint is the exact transpose of the tangent-linear
+// model of the discrete step in the algebraic inner product of all stored
+// nodes (the one swm_dot computes).
+// ===========================================================================
+namespace {
+
+constexpr int kAdWork = 10, kAdStates = 7;
+
+double* adf(swm_ctx* c, int k) { return c->adw + (long long)k * c->fs; }          // work field
+double* ads(swm_ctx* c, int s) { return adf(c, kAdWork + 3 * s); }                  // work state
+
+SbpT make_sbpT(const SbpC& s) {
+  SbpT t{};
+  int maxlast = 0;
+  for (int r = 0; r < s.ne; ++r) maxlast = std::max(maxlast, s.last[r]);
+  t.ct = std::max(maxlast, s.ne + s.H);
+  t.kr = t.ct + s.H;
+  t.nin = s.nin;
+  t.inshift = s.inshift;
+  for (int m = 0; m < s.nin; ++m) t.qin[m] = s.Qin[m];
+  // D[r][c] near the left end (closure rows, then interior rows)
+  auto D = [&](int r, int c) -> double {
+    if (r < s.ne) return c < s.last[r] ? s.Ql[r * MAXNW + c] : 0.0;
+    const int m = c - r - s.inshift;
+    return (m >= 0 && m < s.nin) ? s.Qin[m] : 0.0;
+  };
+  for (int c = 0; c < t.ct; ++c)
+    for (int r = 0; r < t.kr; ++r) t.t[c * t.kr + r] = D(r, c);
+  return t;
+}
+
+int adjoint_ws(swm_ctx* ctx) {
+  if (ctx->prec != SWM_FP64_PLAIN)
+    return fail(ctx, SWM_E_UNSUPPORTED, "tangent-linear and adjoint need an FP64 (plain) context");
+  if (ctx->adw) return SWM_OK;
+  ctx->sbpT = make_sbpT(kTables[sbp_index(ctx->order)]);
+  if (ctx->n < 2 * ctx->sbpT.kr) return fail(ctx, SWM_E_INVALID, "grid too small for the adjoint");
+  const size_t b = sizeof(double) * (size_t)(kAdWork + 3 * kAdStates) * ctx->fs;
+  CK(cudaMalloc(&ctx->adw, b), "alloc adjoint work");
+  CK(cudaMemsetAsync(ctx->adw, 0, b, ctx->st), "memset");
+  CK(cudaMalloc(&ctx->adC, sizeof(double) * 16 * 6 * ctx->n), "alloc adjoint edge buffer");
+  CK(cudaMemsetAsync(ctx->adC, 0, sizeof(double) * 16 * 6 * ctx->n, ctx->st), "memset");
+  return SWM_OK;
+}
+
+int apply_fused64(swm_ctx* ctx, const double* in, double* out) {
+  InstDev<double> I = base_inst<double>(ctx);
+  I.in = in;
+  I.out = out;
+  return run_stage<double>(ctx, I, MODE_APPLY);
+}
+
+// dk = F'(y) dx
+int tl_apply(swm_ctx* ctx, const double* y, const double* dx, double* dk) {
+  const long long fs = ctx->fs;
+  int rc;
+  if ((rc = op_curl(ctx, y + fs, y + 2 * fs, adf(ctx, 9)))) return rc;            // base zeta
+  CK(launch_tl_pre(ctx->g64, ctx->m64, ctx->cfg.grav, y, dx, adf(ctx, 0), ctx->st), "tl pre");
+  if ((rc = op_grad(ctx, adf(ctx, 0), adf(ctx, 5), adf(ctx, 6)))) return rc;       // dGX, dGY
+  if ((rc = op_curl(ctx, dx + fs, dx + 2 * fs, adf(ctx, 7)))) return rc;          // dZ
+  if ((rc = op_div(ctx, adf(ctx, 1), adf(ctx, 2), adf(ctx, 8)))) return rc;       // dDIV
+  CK(launch_tl_post(ctx->g64, ctx->m64, y, adf(ctx, 9), adf(ctx, 0), adf(ctx, 5), adf(ctx, 6),
+                    adf(ctx, 7), adf(ctx, 8), dk, ctx->st),
+     "tl post");
+  return SWM_OK;
+}
+
+// out = F'(y)^T lk
+int ad_apply(swm_ctx* ctx, const double* y, const double* lk, double* out) {
+  const long long fs = ctx->fs;
+  if (int rc = op_curl(ctx, y + fs, y + 2 * fs, adf(ctx, 9))) return rc;           // base zeta
+  CK(launch_ad_pre(ctx->g64, ctx->m64, y, adf(ctx, 9), lk, adf(ctx, 0), ctx->st), "ad pre");
+  CK(launch_adsync_vector(ctx->g64, ctx->topo, ctx->qw, adf(ctx, 0), adf(ctx, 1), ctx->adC, ctx->st),
+     "ad vector sync");
+  CK(launch_sync_scalar(ctx->g64, ctx->topo, adf(ctx, 2), ctx->edge64, ctx->st), "ad sync");
+  CK(launch_sync_scalar(ctx->g64, ctx->topo, adf(ctx, 3), ctx->edge64, ctx->st), "ad sync");
+  CK(launch_ad_main(ctx->g64, ctx->sbpT, ctx->m64, ctx->ghs, ctx->cfg.grav, y, adf(ctx, 0), out,
+                    ctx->st),
+     "ad main");
+  return SWM_OK;
+}
+
+// dx <- Phi'(x) dx for one RK4 step Phi (rk4_mod.f90:20-42)
+int rk4_tl(swm_ctx* ctx, const double* x, double* dx, double dt) {
+  const long long c = 3 * ctx->fs;
+  double *Y = ads(ctx, 0), *K = ads(ctx, 1), *DK = ads(ctx, 2), *DY = ads(ctx, 3), *ACC = ads(ctx, 4);
+  const cudaStream_t st = ctx->st;
+  int rc;
+  if ((rc = tl_apply(ctx, x, dx, DK))) return rc;
+  CK(launch_axpby(c, 1.0, dx, dt / 6.0, DK, ACC, st), "axpby");
+  CK(launch_axpby(c, 1.0, dx, 0.5 * dt, DK, DY, st), "axpby");
+  if ((rc = apply_fused64(ctx, x, K))) return rc;
+  CK(launch_axpby(c, 1.0, x, 0.5 * dt, K, Y, st), "axpby");
+  if ((rc = tl_apply(ctx, Y, DY, DK))) return rc;
+  CK(launch_axpby(c, 1.0, ACC, dt / 3.0, DK, ACC, st), "axpby");
+  CK(launch_axpby(c, 1.0, dx, 0.5 * dt, DK, DY, st), "axpby");
+  if ((rc = apply_fused64(ctx, Y, K))) return rc;
+  CK(launch_axpby(c, 1.0, x, 0.5 * dt, K, Y, st), "axpby");
+  if ((rc = tl_apply(ctx, Y, DY, DK))) return rc;
+  CK(launch_axpby(c, 1.0, ACC, dt / 3.0, DK, ACC, st), "axpby");
+  CK(launch_axpby(c, 1.0, dx, dt, DK, DY, st), "axpby");
+  if ((rc = apply_fused64(ctx, Y, K))) return rc;
+  CK(launch_axpby(c, 1.0, x, dt, K, Y, st), "axpby");
+  if ((rc = tl_apply(ctx, Y, DY, DK))) return rc;
+  CK(launch_axpby(c, 1.0, ACC, dt / 6.0, DK, dx, st), "axpby");
+  return SWM_OK;
+}
+
+// lx <- Phi'(x)^T lx: recompute the stage states, then run the stages back
+int rk4_ad(swm_ctx* ctx, const double* x, double* lx, double dt) {
+  const long long c = 3 * ctx->fs;
+  double *Y2 = ads(ctx, 0), *Y3 = ads(ctx, 1), *Y4 = ads(ctx, 2), *K = ads(ctx, 3);
+  double *LK = ads(ctx, 4), *MU = ads(ctx, 5), *ACC = ads(ctx, 6);
+  const cudaStream_t st = ctx->st;
+  int rc;
+  if ((rc = apply_fused64(ctx, x, K))) return rc;
+  CK(launch_axpby(c, 1.0, x, 0.5 * dt, K, Y2, st), "axpby");
+  if ((rc = apply_fused64(ctx, Y2, K))) return rc;
+  CK(launch_axpby(c, 1.0, x, 0.5 * dt, K, Y3, st), "axpby");
+  if ((rc = apply_fused64(ctx, Y3, K))) return rc;
+  CK(launch_axpby(c, 1.0, x, dt, K, Y4, st), "axpby");
+  CK(launch_axpby(c, dt / 6.0, lx, 0.0, nullptr, LK, st), "axpby");
+  if ((rc = ad_apply(ctx, Y4, LK, MU))) return rc;
+  CK(launch_axpby(c, 1.0, lx, 1.0, MU, ACC, st), "axpby");
+  CK(launch_axpby(c, dt / 3.0, lx, dt, MU, LK, st), "axpby");
+  if ((rc = ad_apply(ctx, Y3, LK, MU))) return rc;
+  CK(launch_axpby(c, 1.0, ACC, 1.0, MU, ACC, st), "axpby");
+  CK(launch_axpby(c, dt / 3.0, lx, 0.5 * dt, MU, LK, st), "axpby");
+  if ((rc = ad_apply(ctx, Y2, LK, MU))) return rc;
+  CK(launch_axpby(c, 1.0, ACC, 1.0, MU, ACC, st), "axpby");
+  CK(launch_axpby(c, dt / 6.0, lx, 0.5 * dt, MU, LK, st), "axpby");
+  if ((rc = ad_apply(ctx, x, LK, MU))) return rc;
+  CK(launch_axpby(c, 1.0, ACC, 1.0, MU, lx, st), "axpby");
+  return SWM_OK;
+}
+
+// rk4_ad through a CUDA graph captured for the last (x, lx, dt)
+int rk4_ad_graph(swm_ctx* ctx, const double* x, double* lx, double dt) {
+  if (!(ctx->ad_graph && ctx->ad_key[0] == x && ctx->ad_key[1] == lx && ctx->ad_dt == dt)) {
+    if (ctx->ad_graph) { cudaGraphExecDestroy(ctx->ad_graph); ctx->ad_graph = nullptr; }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const int rc = rk4_ad(ctx, x, lx, dt);
+    const cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
+    if (rc) { if (ec == cudaSuccess) cudaGraphDestroy(g); return rc; }
+    CK(ec, "end capture");
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->ad_graph, g, 0);
+    cudaGraphDestroy(g);
+    CK(ei, "graph instantiate");
+    ctx->ad_key[0] = x; ctx->ad_key[1] = lx; ctx->ad_dt = dt;
+  }
+  CK(cudaGraphLaunch(ctx->ad_graph, ctx->st), "graph launch");
+  return SWM_OK;
+}
+
+int check_tl_args(swm_ctx* ctx, const swm_state* a, const swm_state* b, const swm_state* c) {
+  if (int rc = check_state(ctx, a)) return rc;
+  if (int rc = check_state(ctx, b)) return rc;
+  if (c && check_state(ctx, c)) return SWM_E_INVALID;
+  if (a == b || (c && (c == a || c == b)))
+    return fail(ctx, SWM_E_INVALID, "tangent-linear / adjoint calls need distinct states");
+  cudaSetDevice(ctx->cfg.device);
+  return adjoint_ws(ctx);
+}
+
+}  // namespace
+
+// Binomial checkpointing (Griewank's "revolve" recursion) over nsteps RK4
+// steps with nsnap stored states, the initial state included.  The plan is a
+// list of actions on one working state: restore it from a snapshot, advance
+// it k steps, store it in a snapshot, or run the adjoint step at step n (the
+// working state then holds x_n).
+struct swm_adjoint {
+  enum Kind { RESTORE, ADVANCE, STORE, ADJ };
+  struct Act { int kind, arg; };
+  swm_ctx* ctx = nullptr;
+  int nsteps = 0, nsnap = 0;
+  double dt = 0.0;
+  std::vector<swm_state*> slot;
+  swm_state* cur = nullptr;
+  swm_state* lam = nullptr;
+  std::vector<Act> plan;
+  size_t first_adj = 0;
+  bool ready = false;          // forward run done, backward sweep pending
+  long fwd_steps = 0, adj_steps = 0;
+};
+
+namespace {
+
+long long beta(int c, int r) {   // C(c + r, c), saturating
+  long double v = 1.0L;
+  for (int k = 1; k <= c; ++k) { v = v * (r + k) / k; if (v > 4e18L) return (long long)4e18; }
+  return (long long)(v + 0.5L);
+}
+
+void plan_reverse(std::vector<swm_adjoint::Act>& acts, int a, int b, int sa, std::vector<int>& freeslots) {
+  using A = swm_adjoint;
+  if (b - a == 1) { acts.push_back({A::RESTORE, sa}); acts.push_back({A::ADJ, a}); return; }
+  if (freeslots.empty()) {
+    for (int k = b - 1; k >= a; --k) {
+      acts.push_back({A::RESTORE, sa});
+      if (k > a) acts.push_back({A::ADVANCE, k - a});
+      acts.push_back({A::ADJ, k});
+    }
+    return;
+  }
+  const int c = (int)freeslots.size() + 1, l = b - a;
+  int r = 1;
+  while (beta(c, r) < l) ++r;
+  const long long right = std::min<long long>(l - 1, beta(c - 1, r));
+  const int m = b - (int)right;
+  acts.push_back({A::RESTORE, sa});
+  acts.push_back({A::ADVANCE, m - a});
+  const int sm = freeslots.back();
+  freeslots.pop_back();
+  acts.push_back({A::STORE, sm});
+  plan_reverse(acts, m, b, sm, freeslots);
+  freeslots.push_back(sm);
+  plan_reverse(acts, a, m, sa, freeslots);
+}
+
+int copy_state(swm_ctx* ctx, void* dst, const void* src) {
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * 3 * ctx->fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+  return SWM_OK;
+}
+
+int run_action(swm_adjoint* adj, const swm_adjoint::Act& a) {
+  swm_ctx* ctx = adj->ctx;
+  switch (a.kind) {
+    case swm_adjoint::RESTORE: return copy_state(ctx, adj->cur->hi, adj->slot[a.arg]->hi);
+    case swm_adjoint::STORE: return copy_state(ctx, adj->slot[a.arg]->hi, adj->cur->hi);
+    case swm_adjoint::ADVANCE:
+      adj->fwd_steps += a.arg;
+      return swm_rk4_step(ctx, adj->cur, adj->dt, a.arg);
+    default:
+      adj->adj_steps += 1;
+      return rk4_ad_graph(ctx, (const double*)adj->cur->hi, (double*)adj->lam->hi, adj->dt);
+  }
+}
+
+void free_adjoint(swm_adjoint* adj) {
+  if (!adj) return;
+  for (swm_state* s : adj->slot) swm_state_free(s);
+  swm_state_free(adj->cur);
+  swm_state_free(adj->lam);
+  delete adj;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_apply_tl(swm_ctx* ctx, const swm_state* y, const swm_state* dx, swm_state* dk) {
+  if (int rc = check_tl_args(ctx, y, dx, dk)) return rc;
+  return tl_apply(ctx, (const double*)y->hi, (const double*)dx->hi, (double*)dk->hi);
+}
+
+int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk, swm_state* lx) {
+  if (int rc = check_tl_args(ctx, y, lk, lx)) return rc;
+  return ad_apply(ctx, (const double*)y->hi, (const double*)lk->hi, (double*)lx->hi);
+}
+
+int swm_rk4_tl(swm_ctx* ctx, const swm_state* x, swm_state* dx, double dt) {
+  if (int rc = check_tl_args(ctx, x, dx, nullptr)) return rc;
+  return rk4_tl(ctx, (const double*)x->hi, (double*)dx->hi, dt);
+}
+
+int swm_rk4_ad(swm_ctx* ctx, const swm_state* x, swm_state* lx, double dt) {
+  if (int rc = check_tl_args(ctx, x, lx, nullptr)) return rc;
+  return rk4_ad_graph(ctx, (const double*)x->hi, (double*)lx->hi, dt);
+}
+
+int swm_adjoint_create(swm_ctx* ctx, int nsteps, int nsnap, double dt, swm_adjoint** out) {
+  if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
+  if (nsteps < 1 || nsnap < 1 || !(dt > 0.0))
+    return fail(ctx, SWM_E_INVALID, "need nsteps >= 1, nsnap >= 1 and dt > 0");
+  if (ctx->prec != SWM_FP64_PLAIN)
+    return fail(ctx, SWM_E_UNSUPPORTED, "the adjoint needs an FP64 (plain) context");
+  cudaSetDevice(ctx->cfg.device);
+  if (int rc = adjoint_ws(ctx)) return rc;
+  swm_adjoint* adj = new swm_adjoint();
+  adj->ctx = ctx; adj->nsteps = nsteps; adj->nsnap = std::min(nsnap, nsteps); adj->dt = dt;
+  for (int k = 0; k < adj->nsnap; ++k) {
+    swm_state* s = nullptr;
+    if (int rc = swm_state_create(ctx, &s)) { free_adjoint(adj); return rc; }
+    adj->slot.push_back(s);
+  }
+  if (int rc = swm_state_create(ctx, &adj->cur)) { free_adjoint(adj); return rc; }
+  if (int rc = swm_state_create(ctx, &adj->lam)) { free_adjoint(adj); return rc; }
+  std::vector<int> freeslots;
+  for (int k = adj->nsnap - 1; k >= 1; --k) freeslots.push_back(k);
+  plan_reverse(adj->plan, 0, nsteps, 0, freeslots);
+  for (size_t k = 0; k < adj->plan.size(); ++k)
+    if (adj->plan[k].kind == swm_adjoint::ADJ) { adj->first_adj = k; break; }
+  *out = adj;
+  return SWM_OK;
+}
+
+void swm_adjoint_destroy(swm_adjoint* adj) {
+  if (adj && adj->ctx) cudaSetDevice(adj->ctx->cfg.device);
+  free_adjoint(adj);
+}
+
+int swm_adjoint_forward(swm_adjoint* adj, const swm_state* x0, swm_state* xT) {
+  if (!adj) return fail(nullptr, SWM_E_INVALID, "null adjoint");
+  swm_ctx* ctx = adj->ctx;
+  if (int rc = check_state(ctx, x0)) return rc;
+  if (int rc = check_state(ctx, xT)) return rc;
+  cudaSetDevice(ctx->cfg.device);
+  adj->fwd_steps = adj->adj_steps = 0;
+  if (int rc = copy_state(ctx, adj->slot[0]->hi, x0->hi)) return rc;
+  for (size_t k = 0; k < adj->first_adj; ++k)
+    if (int rc = run_action(adj, adj->plan[k])) return rc;
+  // the working state holds x_{T-1}: one more step gives x_T
+  if (int rc = copy_state(ctx, xT->hi, adj->cur->hi)) return rc;
+  if (int rc = swm_rk4_step(ctx, xT, adj->dt, 1)) return rc;
+  adj->fwd_steps += 1;
+  adj->ready = true;
+  return SWM_OK;
+}
+
+int swm_adjoint_backward(swm_adjoint* adj, swm_state* lambda) {
+  if (!adj) return fail(nullptr, SWM_E_INVALID, "null adjoint");
+  swm_ctx* ctx = adj->ctx;
+  if (int rc = check_state(ctx, lambda)) return rc;
+  if (!adj->ready) return fail(ctx, SWM_E_INVALID, "swm_adjoint_backward needs a forward run first");
+  cudaSetDevice(ctx->cfg.device);
+  if (int rc = copy_state(ctx, adj->lam->hi, lambda->hi)) return rc;
+  for (size_t k = adj->first_adj; k < adj->plan.size(); ++k)
+    if (int rc = run_action(adj, adj->plan[k])) return rc;
+  if (int rc = copy_state(ctx, lambda->hi, adj->lam->hi)) return rc;
+  adj->ready = false;
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  return check_device_flag(ctx);
+}
+
+int swm_adjoint_counts(const swm_adjoint* adj, long* forward_steps, long* adjoint_steps,
+                       long* planned_forward_steps) {
+  if (!adj) return fail(nullptr, SWM_E_INVALID, "null adjoint");
+  if (forward_steps) *forward_steps = adj->fwd_steps;
+  if (adjoint_steps) *adjoint_steps = adj->adj_steps;
+  if (planned_forward_steps) {
+    long p = 1;   // the extra step to x_T
+    for (const auto& a : adj->plan) if (a.kind == swm_adjoint::ADVANCE) p += a.arg;
+    *planned_forward_steps = p;
+  }
+  return SWM_OK;
+}
+
+int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const double* u,
+                            const double* v) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
+  cudaSetDevice(ctx->cfg.device);
+  const double* src[3] = {h, u, v};
+  for (int c = 0; c < 3; ++c) {
+    double* dst = ctx->prec == SWM_FP64_PLAIN ? (double*)s->hi + c * ctx->fs : tmpf(ctx, 11 + c);
+    CK(cudaMemcpy2DAsync(dst, sizeof(double) * ctx->P, src[c], sizeof(double) * ctx->n,
+                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToDevice, ctx->st),
+       "device upload");
+    if (ctx->prec == SWM_FP32_FUSED)
+      CK(launch_split_f64(ctx->fs, dst, (float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs, ctx->st), "split");
+  }
+  return SWM_OK;
+}
+
+int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
+  cudaSetDevice(ctx->cfg.device);
+  double* dst[3] = {h, u, v};
+  const double *dh, *du, *dv;
+  if (int rc = state64(ctx, s, &dh, &du, &dv)) return rc;
+  const double* src[3] = {dh, du, dv};
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpy2DAsync(dst[c], sizeof(double) * ctx->n, src[c], sizeof(double) * ctx->P,
+                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToDevice, ctx->st),
+       "device download");
+  return SWM_OK;
+}
+
+int swm_quadrature_weights(swm_ctx* ctx, double* w_host) {
+  if (!ctx || !w_host) return fail(ctx, SWM_E_INVALID, "null argument");
+  cudaSetDevice(ctx->cfg.device);
+  const int n = ctx->n;
+  std::vector<double> A(n), J((size_t)6 * n * n);
+  CK(cudaMemcpy(A.data(), ctx->Aw, sizeof(double) * n, cudaMemcpyDeviceToHost), "copy");
+  CK(cudaMemcpy2D(J.data(), sizeof(double) * n, ctx->m64 + MJ * ctx->fs, sizeof(double) * ctx->P,
+                  sizeof(double) * n, (size_t)6 * n, cudaMemcpyDeviceToHost),
+     "copy");
+  const double hx2 = ctx->hx * ctx->hx;
+  for (int p = 0; p < 6; ++p)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const size_t k = ((size_t)p * n + j) * n + i;
+        w_host[k] = J[k] * hx2 * A[i] * A[j];
+      }
+  return SWM_OK;
 }
 
 }  // extern "C"

@@ -52,6 +52,35 @@ cudaError_t launch_sync_scalar(const FieldGeom& g, const Topology& tp, double* f
 cudaError_t launch_sync_vector(const FieldGeom& g, const Topology& tp, const double* qw,
                                double* gx, double* gy, double* edge, cudaStream_t st);
 
+// Transposed SBP first-derivative operator D^T: t[c*kr + r] = D[r][c] for
+// the columns c < ct next to the left end (rows r < kr); the right end is
+// the sign-flipped mirror and the interior the negated interior stencil
+// (qin, inshift as in SbpC).  Needs n >= 2*kr.
+struct SbpT {
+  int ct, kr, nin, inshift;
+  double t[9 * 12];
+  double qin[7];
+};
+
+// Tangent-linear and adjoint pieces of the FP64 model operator (swm_adjoint.cu).
+// y, dx, dk, lk, out: 3 fields (h, u, v); w: 5 fields (dK, d(h ut), d(h vt),
+// dut, dvt); A: 6 fields.
+cudaError_t launch_tl_pre(const FieldGeom& g, const double* m64, double grav, const double* y,
+                          const double* dx, double* w, cudaStream_t st);
+cudaError_t launch_tl_post(const FieldGeom& g, const double* m64, const double* y,
+                           const double* zeta, const double* w, const double* dgx,
+                           const double* dgy, const double* dz, const double* ddiv, double* dk,
+                           cudaStream_t st);
+cudaError_t launch_ad_pre(const FieldGeom& g, const double* m64, const double* y,
+                          const double* zeta, const double* lk, double* A, cudaStream_t st);
+cudaError_t launch_ad_main(const FieldGeom& g, const SbpT& t, const double* m64, double ghs,
+                           double grav, const double* y, const double* A, double* out,
+                           cudaStream_t st);
+// transpose of the covariant vector sync, in place on (lgx, lgy); C is an
+// edge buffer (6*4*4*n doubles)
+cudaError_t launch_adsync_vector(const FieldGeom& g, const Topology& tp, const double* qw,
+                                 double* lgx, double* lgy, double* C, cudaStream_t st);
+
 // Deterministic FP64 reductions over the valid nodes of a field.
 // kind: 0 sum(a*b), 1 SBP mass sum(a*J*hx^2*Ax*Ay), 2 min(a), 3 max(a),
 //       4 SBP mass of a*b.

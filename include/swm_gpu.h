@@ -201,6 +201,51 @@ int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches,
                     double* edge_ms, long* edge_launches);
 
 /* ---------------------------------------------------------------------- */
+/* Tangent-linear and adjoint of the FP64 model (no counterpart in the      */
+/* reference).  F is the model operator of swm_apply, Phi one RK4 step of   */
+/* swm_rk4_step.  The adjoint is the exact transpose of the tangent-linear  */
+/* model of the discrete operators (SBP stencils with their closures, the    */
+/* cube-edge syncs, RK4) in the algebraic inner product of swm_dot.  FP64    */
+/* contexts only; the first call allocates the context's TL/AD workspace.    */
+/* Arguments must be distinct states of the context.                        */
+/* ---------------------------------------------------------------------- */
+/* dk = F'(y) dx */
+int swm_apply_tl(swm_ctx* ctx, const swm_state* y, const swm_state* dx,
+                 swm_state* dk);
+/* lx = F'(y)^T lk */
+int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk,
+                 swm_state* lx);
+/* dx <- Phi'(x) dx */
+int swm_rk4_tl(swm_ctx* ctx, const swm_state* x, swm_state* dx, double dt);
+/* lx <- Phi'(x)^T lx (recomputes the stage states of x; CUDA graph) */
+int swm_rk4_ad(swm_ctx* ctx, const swm_state* x, swm_state* lx, double dt);
+
+/* Gradient through nsteps RK4 steps with binomial checkpointing: nsnap      */
+/* stored states (x0 included) and recomputation by the revolve recursion.   */
+typedef struct swm_adjoint swm_adjoint;
+int  swm_adjoint_create(swm_ctx* ctx, int nsteps, int nsnap, double dt,
+                        swm_adjoint** out);
+void swm_adjoint_destroy(swm_adjoint* adj);
+/* x_T = Phi^nsteps(x0), storing the first snapshots */
+int  swm_adjoint_forward(swm_adjoint* adj, const swm_state* x0, swm_state* xT);
+/* lambda: in dJ/dx_T, out dJ/dx0 (after swm_adjoint_forward) */
+int  swm_adjoint_backward(swm_adjoint* adj, swm_state* lambda);
+/* RK4 steps run by the last forward + backward, adjoint steps, and the
+ * forward steps the plan needs in total */
+int  swm_adjoint_counts(const swm_adjoint* adj, long* forward_steps,
+                        long* adjoint_steps, long* planned_forward_steps);
+
+/* States from/to DEVICE arrays in the host layout (framework tensors),      */
+/* ordered on the context stream.                                           */
+int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h,
+                            const double* u, const double* v);
+int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h,
+                              double* u, double* v);
+/* SBP quadrature weight of every node (host layout), the weights of
+ * swm_quadrature_mass: J hx^2 A_i A_j (sbp_quadrature_mod.f90:21-40). */
+int swm_quadrature_weights(swm_ctx* ctx, double* w_host);
+
+/* ---------------------------------------------------------------------- */
 /* Ensembles (no counterpart in the reference, which runs one instance per  */
 /* job): independent members, each with its own N, initial state and time   */
 /* step, sharing SBP order, constants and precision.  Each member is a full */
