@@ -252,6 +252,125 @@ def ensemble_leg(local, steps, warmup, peak):
     }
 
 
+# Adjoint workload: N=192, 240 RK4 steps, 16 snapshots, FP64.  The workload's
+# dt = 300 s (Courant 1.39) is past the RK4 stability limit of the undiffused
+# scheme; 150 s (Courant 0.70) is used.
+ADJOINT = dict(N=192, steps=240, dt=150.0, nsnap=16, seed_x0=3, seed_obs=4, ndir=20, eps=1e-6)
+
+
+def adjoint_leg(local):
+    """Cost of the discrete adjoint against the forward model and its
+    checks: J = 1/2 sum w (h_T - h_obs)^2 with SBP quadrature weights w."""
+    import numpy as np
+    import torch
+
+    import cubedsphere_sbp_swm_gb300 as swm
+    from cubedsphere_sbp_swm_gb300 import adjoint as ad
+    from cubedsphere_sbp_swm_gb300 import initial
+
+    c = ADJOINT
+    N, T, dt = c["N"], c["steps"], c["dt"]
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, precision="fp64", device=local))
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.ExternalStream(op.stream, device=dev)
+    rk4 = swm.RK4()
+
+    def st(arrs):
+        s = op.create_stvec()
+        s.upload(*arrs)
+        return s
+
+    def timed(fn):
+        op.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        op.synchronize()
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    x0 = initial.balanced_zonal(N, c["seed_x0"], 16)[:3]
+    s = st(initial.balanced_zonal(N, c["seed_obs"], 16)[:3])
+    rk4.step(s, op, dt, T)
+    hobs = s.download()[0]
+    w = ad.quadrature_weights(op)
+    zeros = np.zeros(op.shape)
+
+    # forward run and a single adjoint step
+    s = st(x0)
+    rk4.step(s, op, dt, 3)
+    s.upload(*x0)
+    fwd_ms = timed(lambda: rk4.step(s, op, dt, T))
+    x = st(x0)
+    lam = st((w, zeros, zeros))
+    ad.rk4_ad(op, x, lam, dt)
+    reps = 20
+    adj_step_ms = timed(lambda: [ad.rk4_ad(op, x, lam, dt) for _ in range(reps)]) / reps
+
+    # checkpointed gradient (forward with snapshots + reverse sweep)
+    run = ad.CheckpointedRK4(op, dt, T, c["nsnap"])
+    sx0, xT = st(x0), op.create_stvec()
+
+    def gradient():
+        f_ms = timed(lambda: run.forward(sx0, xT))
+        hT = xT.download()[0]
+        g = st((w * (hT - hobs), zeros, zeros))
+        b_ms = timed(lambda: run.backward(g))
+        return f_ms + b_ms, g, hT
+
+    gradient()                                   # warm-up: graph captures
+    grad_ms, g, hT = gradient()
+    counts = run.counts()
+    grad = g.download()
+    J0 = 0.5 * float(np.sum(w * (hT - hobs) ** 2))
+
+    # dot-product test over the whole trajectory
+    rng = np.random.default_rng(2024)
+    dx0 = tuple(rng.standard_normal(op.shape) for _ in range(3))
+    lamT = tuple(rng.standard_normal(op.shape) for _ in range(3))
+    xb, d = st(x0), st(dx0)
+    for _ in range(T):
+        ad.rk4_tl(op, xb, d, dt)
+        rk4.step(xb, op, dt, 1)
+    lt = st(lamT)
+    run.forward(sx0, xT)
+    run.backward(lt)
+    dot_a = float(sum(np.sum(p * q) for p, q in zip(d.download(), lamT)))
+    dot_b = float(sum(np.sum(p * q) for p, q in zip(dx0, lt.download())))
+    dot_gap = abs(dot_a - dot_b) / max(abs(dot_a), abs(dot_b))
+
+    # central finite differences of J along seeded directions
+    def cost(arrs):
+        s.upload(*arrs)
+        rk4.step(s, op, dt, T)
+        return 0.5 * float(np.sum(w * (s.download()[0] - hobs) ** 2))
+
+    eps, gaps = c["eps"], []
+    for k in range(c["ndir"]):
+        r = np.random.default_rng(5 + k)
+        dd = tuple(r.standard_normal(op.shape) for _ in range(3))
+        jp = cost([a + eps * b for a, b in zip(x0, dd)])
+        jm = cost([a - eps * b for a, b in zip(x0, dd)])
+        an = float(sum(np.sum(p * q) for p, q in zip(grad, dd)))
+        gaps.append(abs((jp - jm) / (2 * eps) - an) / abs(an))
+    return {
+        "N": N, "steps": T, "dt_s": dt, "snapshots": c["nsnap"], "precision": "fp64",
+        "cost": "J = 1/2 sum_nodes w (h_T - h_obs)^2, w = SBP quadrature weights",
+        "J": J0,
+        "forward_step_ms": round(fwd_ms / T, 5), "adjoint_step_ms": round(adj_step_ms, 5),
+        "adjoint_over_forward_step": round(adj_step_ms / (fwd_ms / T), 3),
+        "forward_run_ms": round(fwd_ms, 3), "gradient_ms": round(grad_ms, 3),
+        "gradient_over_forward_run": round(grad_ms / fwd_ms, 3),
+        "forward_steps_in_gradient": counts["forward_steps"],
+        "adjoint_steps_in_gradient": counts["adjoint_steps"],
+        "dot_product_rel_gap": dot_gap,
+        "fd_directions": c["ndir"], "fd_eps": eps, "fd_max_rel_gap": max(gaps),
+        "note": "the workload's dt = 300 s (Courant 1.39) is past the RK4 stability limit; "
+                "dt = 150 s (Courant 0.70)",
+    }
+
+
 def run_gpu_arm(args):
     import torch
 
@@ -381,6 +500,9 @@ def run_gpu_arm(args):
     ens = None
     if rank == 0 and not args.no_ensemble:
         ens = ensemble_leg(local, max(10, args.steps // 2), args.warmup, peak)
+    adj = None
+    if rank == 0 and not args.no_adjoint:
+        adj = adjoint_leg(local)
 
     # CPU baseline: the oracle (C++ restatement) on the host cores, rank 0
     cpu = None
@@ -419,6 +541,8 @@ def run_gpu_arm(args):
             line["accuracy_fp32_vs_fp64"] = acc
         if ens:
             line["ensemble"] = ens
+        if adj:
+            line["adjoint"] = adj
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -493,13 +617,25 @@ def main():
                     help="skip the FP32-vs-FP64 run over the workload's simulated days")
     ap.add_argument("--no-ensemble", action="store_true",
                     help="skip the 96-member ensemble leg")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the adjoint leg (N=192, 240 steps)")
     ap.add_argument("--days", type=float, default=None,
                     help="simulated days of the accuracy run (default: the workload's)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--quick", action="store_true",
                     help="profiling case: time only the FP32 steps, print a short line")
+    ap.add_argument("--only", choices=("ensemble", "adjoint"), default=None,
+                    help="run one leg alone and print its JSON object")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.only:
+        import torch
+        _, _, local = _dist()
+        torch.cuda.set_device(local)
+        res = (ensemble_leg(local, max(10, args.steps // 2), args.warmup, _measured_peak()[0])
+               if args.only == "ensemble" else adjoint_leg(local))
+        print(json.dumps({args.only: res}), flush=True)
+        return
     if args.impl == "reference":
         run_reference_arm(args)
     else:

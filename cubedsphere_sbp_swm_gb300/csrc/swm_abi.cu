@@ -1562,12 +1562,15 @@ int adjoint_ws(swm_ctx* ctx) {
     return fail(ctx, SWM_E_UNSUPPORTED, "tangent-linear and adjoint need an FP64 (plain) context");
   if (ctx->adw) return SWM_OK;
   ctx->sbpT = make_sbpT(kTables[sbp_index(ctx->order)]);
+  if (ctx->sbpT.ct != adjoint_table_ct(ctx->order))
+    return fail(ctx, SWM_E_UNSUPPORTED, "transposed SBP table does not match the adjoint kernels");
   if (ctx->n < 2 * ctx->sbpT.kr) return fail(ctx, SWM_E_INVALID, "grid too small for the adjoint");
   const size_t b = sizeof(double) * (size_t)(kAdWork + 3 * kAdStates) * ctx->fs;
   CK(cudaMalloc(&ctx->adw, b), "alloc adjoint work");
   CK(cudaMemsetAsync(ctx->adw, 0, b, ctx->st), "memset");
-  CK(cudaMalloc(&ctx->adC, sizeof(double) * 16 * 6 * ctx->n), "alloc adjoint edge buffer");
-  CK(cudaMemsetAsync(ctx->adC, 0, sizeof(double) * 16 * 6 * ctx->n, ctx->st), "memset");
+  // two edge buffers: transposed-sync pulls, base-curl edge values
+  CK(cudaMalloc(&ctx->adC, sizeof(double) * 2 * 16 * 6 * ctx->n), "alloc adjoint edge buffers");
+  CK(cudaMemsetAsync(ctx->adC, 0, sizeof(double) * 2 * 16 * 6 * ctx->n, ctx->st), "memset");
   return SWM_OK;
 }
 
@@ -1593,19 +1596,39 @@ int tl_apply(swm_ctx* ctx, const double* y, const double* dx, double* dk) {
   return SWM_OK;
 }
 
-// out = F'(y)^T lk
-int ad_apply(swm_ctx* ctx, const double* y, const double* lk, double* out) {
-  const long long fs = ctx->fs;
-  if (int rc = op_curl(ctx, y + fs, y + 2 * fs, adf(ctx, 9))) return rc;           // base zeta
-  CK(launch_ad_pre(ctx->g64, ctx->m64, y, adf(ctx, 9), lk, adf(ctx, 0), ctx->st), "ad pre");
-  CK(launch_adsync_vector(ctx->g64, ctx->topo, ctx->qw, adf(ctx, 0), adf(ctx, 1), ctx->adC, ctx->st),
-     "ad vector sync");
-  CK(launch_sync_scalar(ctx->g64, ctx->topo, adf(ctx, 2), ctx->edge64, ctx->st), "ad sync");
-  CK(launch_sync_scalar(ctx->g64, ctx->topo, adf(ctx, 3), ctx->edge64, ctx->st), "ad sync");
-  CK(launch_ad_main(ctx->g64, ctx->sbpT, ctx->m64, ctx->ghs, ctx->cfg.grav, y, adf(ctx, 0), out,
-                    ctx->st),
+// mu_out = F'(y)^T (alpha*lam + beta*mu_in) and acc_out = acc_in + mu_out
+// (mu_in, mu_out, acc_in/acc_out nullable; outputs may alias inputs)
+int ad_stage(swm_ctx* ctx, const double* y, const double* lam, const double* mu_in, double alpha,
+             double beta, double* mu_out, const double* acc_in, double* acc_out) {
+  double* Zedge = ctx->adC + 16LL * 6 * ctx->n;   // edge values of the base curl
+  CK(launch_zeta_pre(ctx->g64, ctx->order, ctx->m64, y, adf(ctx, 9), Zedge, ctx->st), "ad curl");
+  CK(launch_ad_pre(ctx->g64, ctx->topo, ctx->qw, ctx->m64, y, adf(ctx, 9), Zedge, lam, mu_in, alpha,
+                   beta, adf(ctx, 0), ctx->adC, ctx->st),
+     "ad pre");
+  CK(launch_adsync_gather(ctx->g64, ctx->topo, ctx->m64, ctx->adC, adf(ctx, 0), ctx->st), "ad syncs");
+  CK(launch_ad_main(ctx->g64, ctx->order, ctx->sbpT, ctx->m64, ctx->ghs, ctx->cfg.grav, y, adf(ctx, 0),
+                    mu_out, acc_in, acc_out, ctx->st),
      "ad main");
   return SWM_OK;
+}
+
+// out = F'(y)^T lk
+int ad_apply(swm_ctx* ctx, const double* y, const double* lk, double* out) {
+  return ad_stage(ctx, y, lk, nullptr, 1.0, 0.0, out, nullptr, nullptr);
+}
+
+// out = base + c F(in) by the fused stage kernel (RK stage mode; scratch
+// takes its running-sum output)
+int stage_state(swm_ctx* ctx, const double* in, const double* base, double c, double* out,
+                double* scratch) {
+  InstDev<double> I = base_inst<double>(ctx);
+  I.in = in;
+  I.base = base;
+  I.out = out;
+  I.acc = scratch;
+  I.c_in = c;
+  I.c_acc = 0.0;
+  return run_stage<double>(ctx, I, MODE_RK1);
 }
 
 // dx <- Phi'(x) dx for one RK4 step Phi (rk4_mod.f90:20-42)
@@ -1635,31 +1658,18 @@ int rk4_tl(swm_ctx* ctx, const double* x, double* dx, double dt) {
 }
 
 // lx <- Phi'(x)^T lx: recompute the stage states, then run the stages back
+// (the RK combinations are folded into the adjoint kernels)
 int rk4_ad(swm_ctx* ctx, const double* x, double* lx, double dt) {
-  const long long c = 3 * ctx->fs;
   double *Y2 = ads(ctx, 0), *Y3 = ads(ctx, 1), *Y4 = ads(ctx, 2), *K = ads(ctx, 3);
-  double *LK = ads(ctx, 4), *MU = ads(ctx, 5), *ACC = ads(ctx, 6);
-  const cudaStream_t st = ctx->st;
+  double *MU = ads(ctx, 5), *ACC = ads(ctx, 6);
   int rc;
-  if ((rc = apply_fused64(ctx, x, K))) return rc;
-  CK(launch_axpby(c, 1.0, x, 0.5 * dt, K, Y2, st), "axpby");
-  if ((rc = apply_fused64(ctx, Y2, K))) return rc;
-  CK(launch_axpby(c, 1.0, x, 0.5 * dt, K, Y3, st), "axpby");
-  if ((rc = apply_fused64(ctx, Y3, K))) return rc;
-  CK(launch_axpby(c, 1.0, x, dt, K, Y4, st), "axpby");
-  CK(launch_axpby(c, dt / 6.0, lx, 0.0, nullptr, LK, st), "axpby");
-  if ((rc = ad_apply(ctx, Y4, LK, MU))) return rc;
-  CK(launch_axpby(c, 1.0, lx, 1.0, MU, ACC, st), "axpby");
-  CK(launch_axpby(c, dt / 3.0, lx, dt, MU, LK, st), "axpby");
-  if ((rc = ad_apply(ctx, Y3, LK, MU))) return rc;
-  CK(launch_axpby(c, 1.0, ACC, 1.0, MU, ACC, st), "axpby");
-  CK(launch_axpby(c, dt / 3.0, lx, 0.5 * dt, MU, LK, st), "axpby");
-  if ((rc = ad_apply(ctx, Y2, LK, MU))) return rc;
-  CK(launch_axpby(c, 1.0, ACC, 1.0, MU, ACC, st), "axpby");
-  CK(launch_axpby(c, dt / 6.0, lx, 0.5 * dt, MU, LK, st), "axpby");
-  if ((rc = ad_apply(ctx, x, LK, MU))) return rc;
-  CK(launch_axpby(c, 1.0, ACC, 1.0, MU, lx, st), "axpby");
-  return SWM_OK;
+  if ((rc = stage_state(ctx, x, x, 0.5 * dt, Y2, K))) return rc;
+  if ((rc = stage_state(ctx, Y2, x, 0.5 * dt, Y3, K))) return rc;
+  if ((rc = stage_state(ctx, Y3, x, dt, Y4, K))) return rc;
+  if ((rc = ad_stage(ctx, Y4, lx, nullptr, dt / 6.0, 0.0, MU, lx, ACC))) return rc;     // ACC = l + mu4
+  if ((rc = ad_stage(ctx, Y3, lx, MU, dt / 3.0, dt, MU, ACC, ACC))) return rc;          // ACC += mu3
+  if ((rc = ad_stage(ctx, Y2, lx, MU, dt / 3.0, 0.5 * dt, MU, ACC, ACC))) return rc;    // ACC += mu2
+  return ad_stage(ctx, x, lx, MU, dt / 6.0, 0.5 * dt, nullptr, ACC, lx);                // l = ACC + mu1
 }
 
 // rk4_ad through a CUDA graph captured for the last (x, lx, dt)

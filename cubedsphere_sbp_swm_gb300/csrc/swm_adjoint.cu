@@ -41,24 +41,60 @@ __device__ __forceinline__ bool node_of(const FieldGeom& g, Node& o) {
   return true;
 }
 
+// Columns next to each line end that need the transposed closure block (ct)
+// and the rows those columns read (kr), per SBP order:
+// ct = max(max_r last[r], ne + H), kr = ct + H.
+template <int ORD> struct AdOrd;
+template <> struct AdOrd<21> { static constexpr int CT = 2, KR = 3; };
+template <> struct AdOrd<42> { static constexpr int CT = 6, KR = 8; };
+template <> struct AdOrd<43> { static constexpr int CT = 6, KR = 8; };
+template <> struct AdOrd<63> { static constexpr int CT = 9, KR = 12; };
+
 // (D^T f)_c of the 1-D SBP operator along one grid line; F(k) is f at line
 // index k.  Columns near the ends use the transposed closure block, the
 // interior the negated interior stencil (the interior stencil is
 // antisymmetric).
-template <class Get>
+template <int ORD, class Get>
 __device__ __forceinline__ double dT_line(const SbpT& t, int n, int c, Get F) {
+  constexpr int CT = AdOrd<ORD>::CT, KR = AdOrd<ORD>::KR;
   double s = 0.0;
-  if (c < t.ct) {
-    for (int r = 0; r < t.kr; ++r) s += t.t[c * t.kr + r] * F(r);
+  if (c < CT) {
+#pragma unroll
+    for (int r = 0; r < KR; ++r) s += t.t[c * KR + r] * F(r);
     return s;
   }
-  if (c >= n - t.ct) {
+  if (c >= n - CT) {
     const int cc = n - 1 - c;
-    for (int r = 0; r < t.kr; ++r) s += t.t[cc * t.kr + r] * F(n - 1 - r);
+#pragma unroll
+    for (int r = 0; r < KR; ++r) s += t.t[cc * KR + r] * F(n - 1 - r);
     return -s;
   }
-  for (int m = 0; m < t.nin; ++m) s += t.qin[m] * F(c + t.inshift + m);
-  return -s;
+  return -d_interior<ORD, double>([&](int o) { return F(c + o); });
+}
+
+// Pre-sync curl of the base state, rJ (Dx v - Dy u), with the values of the
+// panel-boundary nodes also stored in the EV_ZETA slots of the edge buffer
+// Z (the layout of the forward edge buffer).
+template <int ORD>
+__global__ void zeta_pre_kernel(FieldGeom g, const double* m, const double* y, double* zeta,
+                                double* Z) {
+  Node o;
+  if (!node_of(g, o)) return;
+  const long long fs = g.fs, x = o.x;
+  const int n = g.n, e = n - 1;
+  const long long row = (long long)o.p * g.ps + (long long)o.j * g.P;
+  const long long col = (long long)o.p * g.ps + o.i;
+  const double* u = y + fs;
+  const double* v = y + 2 * fs;
+  const double dxv = d_line<ORD, double>(o.i, n, [&](int k) { return v[row + k]; });
+  const double dyu = d_line<ORD, double>(o.j, n, [&](int k) { return u[col + (long long)k * g.P]; });
+  const double z = (dxv - dyu) * m[MRJ * fs + x];
+  zeta[x] = z;
+  auto put = [&](int side, int k) { Z[((long long)(o.p * 4 + side) * 4 + EV_ZETA) * n + k] = z; };
+  if (o.i == 0) put(SIDE_L, o.j);
+  if (o.i == e) put(SIDE_R, o.j);
+  if (o.j == 0) put(SIDE_B, o.i);
+  if (o.j == e) put(SIDE_T, o.i);
 }
 
 __global__ void tl_pre_kernel(FieldGeom g, const double* m, double grav, const double* y,
@@ -95,68 +131,8 @@ __global__ void tl_post_kernel(FieldGeom g, const double* m, const double* y, co
   dk[2 * fs + x] = -dgy[x] - dz[x] * J * ut - fz * J * dut;
 }
 
-// Cotangents of the synced quantities from the cotangent lk of (k_h, k_u, k_v):
-// A = (lGX, lGY, lDIV, lZ, l_ut part, l_vt part)
-__global__ void ad_pre_kernel(FieldGeom g, const double* m, const double* y, const double* zeta,
-                              const double* lk, double* A) {
-  Node o;
-  if (!node_of(g, o)) return;
-  const long long fs = g.fs, x = o.x;
-  const double u = y[fs + x], v = y[2 * fs + x];
-  const double q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
-  const double J = m[MJ * fs + x], fz = m[MF * fs + x] + zeta[x];
-  const double ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
-  const double lh = lk[x], lu = lk[fs + x], lv = lk[2 * fs + x];
-  A[x] = -lu;
-  A[fs + x] = -lv;
-  A[2 * fs + x] = -lh;
-  A[3 * fs + x] = J * (vt * lu - ut * lv);
-  A[4 * fs + x] = -fz * J * lv;
-  A[5 * fs + x] = fz * J * lu;
-}
-
-// out = F'(y)^T lk from the synced-transposed cotangents A (see ad_pre_kernel)
-__global__ void ad_main_kernel(FieldGeom g, SbpT t, const double* m, double ghs, double grav,
-                               const double* y, const double* A, double* out) {
-  Node o;
-  if (!node_of(g, o)) return;
-  const long long fs = g.fs, x = o.x;
-  const int n = g.n;
-  const long long row = (long long)o.p * g.ps + (long long)o.j * g.P;   // node (0, j)
-  const long long col = (long long)o.p * g.ps + o.i;                     // node (i, 0)
-  const double* A1 = A;
-  const double* A2 = A + fs;
-  const double* A3 = A + 2 * fs;
-  const double* A4 = A + 3 * fs;
-  const double* rJ = m + MRJ * fs;
-  const double dx1 = dT_line(t, n, o.i, [&](int k) { return A1[row + k]; });
-  const double dy2 = dT_line(t, n, o.j, [&](int k) { return A2[col + (long long)k * g.P]; });
-  const double dx3 = dT_line(t, n, o.i, [&](int k) { return rJ[row + k] * A3[row + k]; });
-  const double dy3 = dT_line(t, n, o.j, [&](int k) {
-    const long long q = col + (long long)k * g.P;
-    return rJ[q] * A3[q];
-  });
-  const double dx4 = dT_line(t, n, o.i, [&](int k) { return rJ[row + k] * A4[row + k]; });
-  const double dy4 = dT_line(t, n, o.j, [&](int k) {
-    const long long q = col + (long long)k * g.P;
-    return rJ[q] * A4[q];
-  });
-  const double h = y[x], u = y[fs + x], v = y[2 * fs + x];
-  const double q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
-  const double J = m[MJ * fs + x];
-  const double ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
-  const double lK = ghs * (dx1 + dy2);
-  const double lGu = dx3, lGv = dy3;          // cotangents of J h ut, J h vt
-  const double lut = A[4 * fs + x] + J * h * lGu + 0.5 * u * lK;
-  const double lvt = A[5 * fs + x] + J * h * lGv + 0.5 * v * lK;
-  out[x] = J * (ut * lGu + vt * lGv) + grav * lK;
-  out[fs + x] = -dy4 + 0.5 * ut * lK + q1 * lut + q2 * lvt;
-  out[2 * fs + x] = dx4 + 0.5 * vt * lK + q2 * lut + q3 * lvt;
-}
-
-// Sv^T, pass 1: at every panel-boundary node, pull the cotangent (lgx, lgy)
-// of the node's synced output back onto the raw neighbour values the sync
-// read (ring_vector, component map included) and store it at the reading
+// Sv^T pull of one boundary node: the cotangent of a raw neighbour value
+// read through ring_vector (component map included) goes to the reading
 // node's slot C[p][side][EV_GX|EV_GY][k].
 __device__ __forceinline__ void put_ring(double* C, const Topology& tp, int n, int p, int side,
                                          int k, double lrx, double lry) {
@@ -168,16 +144,13 @@ __device__ __forceinline__ void put_ring(double* C, const Topology& tp, int n, i
   C[((long long)(p * 4 + side) * 4 + EV_GY) * n + k] = lgy;
 }
 
-__global__ void adsync_vec_pull_kernel(FieldGeom g, Topology tp, const double* qw,
-                                       const double* lgx, const double* lgy, double* C) {
-  const int n = g.n, nb = 4 * n - 4, e = n - 1;
-  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6 * nb) return;
-  const int p = gi / nb;
-  int i, j;
-  boundary_node(gi - p * nb, n, i, j);
-  const long long x = (long long)p * g.ps + (long long)j * g.P + i;
-  const double a = lgx[x], b = lgy[x];     // cotangents of the synced gx (V) and gy (U)
+// the pulls of one boundary node (i, j) of panel p: (a, b) are the
+// cotangents of its synced (gx, gy) = (V, U) (syncronize_grad_on_edges,
+// transposed case by case), s1/s2 the two scalar fields
+__device__ __forceinline__ void pull_node(double* C, const Topology& tp, const double* qw, int n,
+                                          int p, int i, int j, double a, double b, double s1,
+                                          double s2) {
+  const int e = n - 1;
   const double* qb = qw;
   const double* qt = qw + n;
   const double* ql = qw + 2 * n;
@@ -204,12 +177,104 @@ __global__ void adsync_vec_pull_kernel(FieldGeom g, Topology tp, const double* q
   } else {
     put_ring(C, tp, n, p, SIDE_T, i, 0.5 * a + 0.5 * qt[i] * b, 0.5 * b);
   }
+  auto putS = [&](int side, int k) {
+    C[((long long)(p * 4 + side) * 4 + EV_ZETA) * n + k] = s1;
+    C[((long long)(p * 4 + side) * 4 + EV_DIV) * n + k] = s2;
+  };
+  if (i == 0) putS(SIDE_L, j);
+  if (i == e) putS(SIDE_R, j);
+  if (j == 0) putS(SIDE_B, i);
+  if (j == e) putS(SIDE_T, i);
 }
 
-// Sv^T, pass 2: a node's input cotangent is its own share of its synced
-// output plus what every copy that read it pulled back (in fixed order).
-__global__ void adsync_vec_gather_kernel(FieldGeom g, Topology tp, const double* C, double* lgx,
-                                         double* lgy) {
+// Cotangents of the synced quantities from lk = alpha*lam + beta*mu (mu
+// nullable) of (k_h, k_u, k_v), with the base curl synced here (zeta holds
+// the pre-sync curl, Z its edge values):
+// A = (lGX, lGY, rJ*lDIV, rJ*lZ, l_ut part, l_vt part); at panel-boundary
+// nodes the raw (unsynced) cotangents are pulled into C for adsync_gather.
+__global__ void ad_pre_kernel(FieldGeom g, Topology tp, const double* qw, const double* m,
+                              const double* y, const double* zeta, const double* Z,
+                              const double* lam, const double* mu, double alpha, double beta,
+                              double* A, double* C) {
+  Node o;
+  if (!node_of(g, o)) return;
+  const long long fs = g.fs, x = o.x;
+  const int n = g.n, e = n - 1;
+  const bool edge = o.i == 0 || o.i == e || o.j == 0 || o.j == e;
+  double z = zeta[x];
+  if (edge) z = sync_scalar_node<double>(EdgeView<double>{Z, n}, tp, o.p, o.i, o.j, EV_ZETA, z);
+  const double u = y[fs + x], v = y[2 * fs + x];
+  const double q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
+  const double J = m[MJ * fs + x], fz = m[MF * fs + x] + z, rJ = m[MRJ * fs + x];
+  const double ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
+  double lh = alpha * lam[x], lu = alpha * lam[fs + x], lv = alpha * lam[2 * fs + x];
+  if (mu) {
+    lh += beta * mu[x];
+    lu += beta * mu[fs + x];
+    lv += beta * mu[2 * fs + x];
+  }
+  const double lz = J * (vt * lu - ut * lv);
+  A[x] = -lu;
+  A[fs + x] = -lv;
+  A[2 * fs + x] = -lh * rJ;
+  A[3 * fs + x] = lz * rJ;
+  A[4 * fs + x] = -fz * J * lv;
+  A[5 * fs + x] = fz * J * lu;
+  if (edge) pull_node(C, tp, qw, n, o.p, o.i, o.j, -lu, -lv, -lh, lz);
+}
+
+// mu = F'(y)^T lk from the synced-transposed cotangents A (ad_pre_kernel +
+// adsync_gather_kernel); also acc_out = acc_in + mu (acc_in/acc_out
+// nullable; acc_out may be acc_in)
+template <int ORD>
+__global__ void ad_main_kernel(FieldGeom g, SbpT t, const double* m, double ghs, double grav,
+                               const double* y, const double* A, double* out,
+                               const double* acc_in, double* acc_out) {
+  Node o;
+  if (!node_of(g, o)) return;
+  const long long fs = g.fs, x = o.x;
+  const int n = g.n;
+  const long long row = (long long)o.p * g.ps + (long long)o.j * g.P;   // node (0, j)
+  const long long col = (long long)o.p * g.ps + o.i;                     // node (i, 0)
+  const double* A1 = A;
+  const double* A2 = A + fs;
+  const double* W3 = A + 2 * fs;
+  const double* W4 = A + 3 * fs;
+  const double dx1 = dT_line<ORD>(t, n, o.i, [&](int k) { return A1[row + k]; });
+  const double dy2 = dT_line<ORD>(t, n, o.j, [&](int k) { return A2[col + (long long)k * g.P]; });
+  const double dx3 = dT_line<ORD>(t, n, o.i, [&](int k) { return W3[row + k]; });
+  const double dy3 = dT_line<ORD>(t, n, o.j, [&](int k) { return W3[col + (long long)k * g.P]; });
+  const double dx4 = dT_line<ORD>(t, n, o.i, [&](int k) { return W4[row + k]; });
+  const double dy4 = dT_line<ORD>(t, n, o.j, [&](int k) { return W4[col + (long long)k * g.P]; });
+  const double h = y[x], u = y[fs + x], v = y[2 * fs + x];
+  const double q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
+  const double J = m[MJ * fs + x];
+  const double ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
+  const double lK = ghs * (dx1 + dy2);
+  const double lGu = dx3, lGv = dy3;          // cotangents of J h ut, J h vt
+  const double lut = A[4 * fs + x] + J * h * lGu + 0.5 * u * lK;
+  const double lvt = A[5 * fs + x] + J * h * lGv + 0.5 * v * lK;
+  const double mh = J * (ut * lGu + vt * lGv) + grav * lK;
+  const double mu_ = -dy4 + 0.5 * ut * lK + q1 * lut + q2 * lvt;
+  const double mv = dx4 + 0.5 * vt * lK + q2 * lut + q3 * lvt;
+  if (out) {
+    out[x] = mh;
+    out[fs + x] = mu_;
+    out[2 * fs + x] = mv;
+  }
+  if (acc_out) {
+    acc_out[x] = acc_in[x] + mh;
+    acc_out[fs + x] = acc_in[fs + x] + mu_;
+    acc_out[2 * fs + x] = acc_in[2 * fs + x] + mv;
+  }
+}
+
+// Pass 2: a node's vector input cotangent is its own share of its synced
+// output plus what every copy that read it pulled back (fixed order); the
+// two scalar fields get the forward scalar sync (its own transpose).
+// s1, s2 are scaled by rJ in the field (A's W3/W4) and raw in C
+__global__ void adsync_gather_kernel(FieldGeom g, Topology tp, const double* m, const double* C,
+                                     double* lgx, double* lgy, double* s1, double* s2) {
   const int n = g.n, nb = 4 * n - 4, e = n - 1;
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= 6 * nb) return;
@@ -230,8 +295,18 @@ __global__ void adsync_vec_gather_kernel(FieldGeom g, Topology tp, const double*
   if (i == e) add(SIDE_R, j);
   if (j == 0) add(SIDE_B, i);
   if (j == e) add(SIDE_T, i);
+  const EdgeView<double> ev{C, n};
+  const double own1 = ev.get(p, i == 0 ? SIDE_L : i == e ? SIDE_R : j == 0 ? SIDE_B : SIDE_T, EV_ZETA,
+                             (i == 0 || i == e) ? j : i);
+  const double own2 = ev.get(p, i == 0 ? SIDE_L : i == e ? SIDE_R : j == 0 ? SIDE_B : SIDE_T, EV_DIV,
+                             (i == 0 || i == e) ? j : i);
+  const double rJ = m[MRJ * g.fs + x];
+  const double z = sync_scalar_node<double>(ev, tp, p, i, j, EV_ZETA, own1);
+  const double d = sync_scalar_node<double>(ev, tp, p, i, j, EV_DIV, own2);
   lgx[x] = ax;
   lgy[x] = ay;
+  s1[x] = z * rJ;
+  s2[x] = d * rJ;
 }
 
 }  // namespace
@@ -250,25 +325,58 @@ cudaError_t launch_tl_post(const FieldGeom& g, const double* m64, const double* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_ad_pre(const FieldGeom& g, const double* m64, const double* y,
-                          const double* zeta, const double* lk, double* A, cudaStream_t st) {
-  ad_pre_kernel<<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, m64, y, zeta, lk, A);
+cudaError_t launch_zeta_pre(const FieldGeom& g, int order, const double* m64, const double* y,
+                            double* zeta, double* Z, cudaStream_t st) {
+  const int nb = nblk(6LL * g.n * g.n);
+  switch (order) {
+    case 21: zeta_pre_kernel<21><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
+    case 42: zeta_pre_kernel<42><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
+    case 43: zeta_pre_kernel<43><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
+    case 63: zeta_pre_kernel<63><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_ad_main(const FieldGeom& g, const SbpT& t, const double* m64, double ghs,
-                           double grav, const double* y, const double* A, double* out,
-                           cudaStream_t st) {
-  ad_main_kernel<<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out);
+cudaError_t launch_ad_pre(const FieldGeom& g, const Topology& tp, const double* qw,
+                          const double* m64, const double* y, const double* zeta, const double* Z,
+                          const double* lam, const double* mu, double alpha, double beta,
+                          double* A, double* C, cudaStream_t st) {
+  ad_pre_kernel<<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, tp, qw, m64, y, zeta, Z, lam, mu, alpha,
+                                                        beta, A, C);
   return cudaGetLastError();
 }
 
-cudaError_t launch_adsync_vector(const FieldGeom& g, const Topology& tp, const double* qw,
-                                 double* lgx, double* lgy, double* C, cudaStream_t st) {
+cudaError_t launch_adsync_gather(const FieldGeom& g, const Topology& tp, const double* m64,
+                                 const double* C, double* A, cudaStream_t st) {
   const int nb = 6 * (4 * g.n - 4);
-  adsync_vec_pull_kernel<<<nblk(nb), TPB, 0, st>>>(g, tp, qw, lgx, lgy, C);
-  adsync_vec_gather_kernel<<<nblk(nb), TPB, 0, st>>>(g, tp, C, lgx, lgy);
+  adsync_gather_kernel<<<nblk(nb), TPB, 0, st>>>(g, tp, m64, C, A, A + g.fs, A + 2 * g.fs,
+                                                  A + 3 * g.fs);
   return cudaGetLastError();
+}
+
+cudaError_t launch_ad_main(const FieldGeom& g, int order, const SbpT& t, const double* m64,
+                           double ghs, double grav, const double* y, const double* A, double* out,
+                           const double* acc_in, double* acc_out, cudaStream_t st) {
+  const int nb = nblk(6LL * g.n * g.n);
+  switch (order) {
+    case 21: ad_main_kernel<21><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 42: ad_main_kernel<42><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 43: ad_main_kernel<43><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 63: ad_main_kernel<63><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+int adjoint_table_ct(int order) {
+  switch (order) {
+    case 21: return AdOrd<21>::CT;
+    case 42: return AdOrd<42>::CT;
+    case 43: return AdOrd<43>::CT;
+    case 63: return AdOrd<63>::CT;
+    default: return -1;
+  }
 }
 
 }  // namespace swm
