@@ -192,8 +192,8 @@ struct swm_ctx {
   // tangent-linear / adjoint workspace (FP64 contexts, allocated on first
   // use): 10 work fields, then 7 states of 3 fields; edge buffer of the
   // vector-sync transpose; transposed SBP table
-  double* adw = nullptr;
-  double* adC = nullptr;
+  void* adw = nullptr;      // elements of the context precision
+  void* adC = nullptr;
   SbpT sbpT{};
   cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
   const void* ad_key[2] = {nullptr, nullptr};
@@ -1534,8 +1534,14 @@ namespace {
 
 constexpr int kAdWork = 10, kAdStates = 7;
 
-double* adf(swm_ctx* c, int k) { return c->adw + (long long)k * c->fs; }          // work field
-double* ads(swm_ctx* c, int s) { return adf(c, kAdWork + 3 * s); }                  // work state
+template <class T = double>
+T* adf(swm_ctx* c, int k) { return (T*)c->adw + (long long)k * c->fs; }           // work field
+template <class T = double>
+T* ads(swm_ctx* c, int s) { return adf<T>(c, kAdWork + 3 * s); }                   // work state
+template <class T>
+const T* metric_of(swm_ctx* c) {
+  return c->prec == SWM_FP32_FUSED ? (const T*)(const void*)c->m32 : (const T*)(const void*)c->m64;
+}
 
 SbpT make_sbpT(const SbpC& s) {
   SbpT t{};
@@ -1557,20 +1563,23 @@ SbpT make_sbpT(const SbpC& s) {
   return t;
 }
 
-int adjoint_ws(swm_ctx* ctx) {
-  if (ctx->prec != SWM_FP64_PLAIN)
-    return fail(ctx, SWM_E_UNSUPPORTED, "tangent-linear and adjoint need an FP64 (plain) context");
+// tl: the caller needs the tangent-linear model (FP64 contexts only); the
+// adjoint runs in either precision
+int adjoint_ws(swm_ctx* ctx, bool tl) {
+  if (tl && ctx->prec != SWM_FP64_PLAIN)
+    return fail(ctx, SWM_E_UNSUPPORTED, "the tangent-linear model needs an FP64 (plain) context");
   if (ctx->adw) return SWM_OK;
   ctx->sbpT = make_sbpT(kTables[sbp_index(ctx->order)]);
   if (ctx->sbpT.ct != adjoint_table_ct(ctx->order))
     return fail(ctx, SWM_E_UNSUPPORTED, "transposed SBP table does not match the adjoint kernels");
   if (ctx->n < 2 * ctx->sbpT.kr) return fail(ctx, SWM_E_INVALID, "grid too small for the adjoint");
-  const size_t b = sizeof(double) * (size_t)(kAdWork + 3 * kAdStates) * ctx->fs;
+  const size_t b = (size_t)ctx->elt * (size_t)(kAdWork + 3 * kAdStates) * ctx->fs;
   CK(cudaMalloc(&ctx->adw, b), "alloc adjoint work");
   CK(cudaMemsetAsync(ctx->adw, 0, b, ctx->st), "memset");
   // two edge buffers: transposed-sync pulls, base-curl edge values
-  CK(cudaMalloc(&ctx->adC, sizeof(double) * 2 * 16 * 6 * ctx->n), "alloc adjoint edge buffers");
-  CK(cudaMemsetAsync(ctx->adC, 0, sizeof(double) * 2 * 16 * 6 * ctx->n, ctx->st), "memset");
+  const size_t eb = (size_t)ctx->elt * 2 * 16 * 6 * ctx->n;
+  CK(cudaMalloc(&ctx->adC, eb), "alloc adjoint edge buffers");
+  CK(cudaMemsetAsync(ctx->adC, 0, eb, ctx->st), "memset");
   return SWM_OK;
 }
 
@@ -1598,37 +1607,41 @@ int tl_apply(swm_ctx* ctx, const double* y, const double* dx, double* dk) {
 
 // mu_out = F'(y)^T (alpha*lam + beta*mu_in) and acc_out = acc_in + mu_out
 // (mu_in, mu_out, acc_in/acc_out nullable; outputs may alias inputs)
-int ad_stage(swm_ctx* ctx, const double* y, const double* lam, const double* mu_in, double alpha,
-             double beta, double* mu_out, const double* acc_in, double* acc_out) {
-  double* Zedge = ctx->adC + 16LL * 6 * ctx->n;   // edge values of the base curl
-  CK(launch_zeta_pre(ctx->g64, ctx->order, ctx->m64, y, adf(ctx, 9), Zedge, ctx->st), "ad curl");
-  CK(launch_ad_pre(ctx->g64, ctx->topo, ctx->qw, ctx->m64, y, adf(ctx, 9), Zedge, lam, mu_in, alpha,
-                   beta, adf(ctx, 0), ctx->adC, ctx->st),
+template <class T>
+int ad_stage(swm_ctx* ctx, const T* y, const T* lam, const T* mu_in, double alpha, double beta,
+             T* mu_out, const T* acc_in, T* acc_out) {
+  T* C = (T*)ctx->adC;
+  T* Zedge = C + 16LL * 6 * ctx->n;   // edge values of the base curl
+  const T* m = metric_of<T>(ctx);
+  CK(launch_zeta_pre<T>(ctx->g, ctx->order, m, y, adf<T>(ctx, 9), Zedge, ctx->st), "ad curl");
+  CK(launch_ad_pre<T>(ctx->g, ctx->topo, ctx->qw, m, y, adf<T>(ctx, 9), Zedge, lam, mu_in, (T)alpha,
+                      (T)beta, adf<T>(ctx, 0), C, ctx->st),
      "ad pre");
-  CK(launch_adsync_gather(ctx->g64, ctx->topo, ctx->m64, ctx->adC, adf(ctx, 0), ctx->st), "ad syncs");
-  CK(launch_ad_main(ctx->g64, ctx->order, ctx->sbpT, ctx->m64, ctx->ghs, ctx->cfg.grav, y, adf(ctx, 0),
-                    mu_out, acc_in, acc_out, ctx->st),
+  CK(launch_adsync_gather<T>(ctx->g, ctx->topo, m, C, adf<T>(ctx, 0), ctx->st), "ad syncs");
+  CK(launch_ad_main<T>(ctx->g, ctx->order, ctx->sbpT, m, (T)ctx->ghs, (T)ctx->cfg.grav, y,
+                       adf<T>(ctx, 0), mu_out, acc_in, acc_out, ctx->st),
      "ad main");
   return SWM_OK;
 }
 
 // out = F'(y)^T lk
-int ad_apply(swm_ctx* ctx, const double* y, const double* lk, double* out) {
-  return ad_stage(ctx, y, lk, nullptr, 1.0, 0.0, out, nullptr, nullptr);
+template <class T>
+int ad_apply(swm_ctx* ctx, const T* y, const T* lk, T* out) {
+  return ad_stage<T>(ctx, y, lk, nullptr, 1.0, 0.0, out, nullptr, nullptr);
 }
 
 // out = base + c F(in) by the fused stage kernel (RK stage mode; scratch
 // takes its running-sum output)
-int stage_state(swm_ctx* ctx, const double* in, const double* base, double c, double* out,
-                double* scratch) {
-  InstDev<double> I = base_inst<double>(ctx);
+template <class T>
+int stage_state(swm_ctx* ctx, const T* in, const T* base, double c, T* out, T* scratch) {
+  InstDev<T> I = base_inst<T>(ctx);
   I.in = in;
   I.base = base;
   I.out = out;
   I.acc = scratch;
-  I.c_in = c;
-  I.c_acc = 0.0;
-  return run_stage<double>(ctx, I, MODE_RK1);
+  I.c_in = (T)c;
+  I.c_acc = T(0);
+  return run_stage<T>(ctx, I, MODE_RK1);
 }
 
 // dx <- Phi'(x) dx for one RK4 step Phi (rk4_mod.f90:20-42)
@@ -1659,26 +1672,28 @@ int rk4_tl(swm_ctx* ctx, const double* x, double* dx, double dt) {
 
 // lx <- Phi'(x)^T lx: recompute the stage states, then run the stages back
 // (the RK combinations are folded into the adjoint kernels)
-int rk4_ad(swm_ctx* ctx, const double* x, double* lx, double dt) {
-  double *Y2 = ads(ctx, 0), *Y3 = ads(ctx, 1), *Y4 = ads(ctx, 2), *K = ads(ctx, 3);
-  double *MU = ads(ctx, 5), *ACC = ads(ctx, 6);
+template <class T>
+int rk4_ad(swm_ctx* ctx, const T* x, T* lx, double dt) {
+  T *Y2 = ads<T>(ctx, 0), *Y3 = ads<T>(ctx, 1), *Y4 = ads<T>(ctx, 2), *K = ads<T>(ctx, 3);
+  T *MU = ads<T>(ctx, 5), *ACC = ads<T>(ctx, 6);
   int rc;
-  if ((rc = stage_state(ctx, x, x, 0.5 * dt, Y2, K))) return rc;
-  if ((rc = stage_state(ctx, Y2, x, 0.5 * dt, Y3, K))) return rc;
-  if ((rc = stage_state(ctx, Y3, x, dt, Y4, K))) return rc;
-  if ((rc = ad_stage(ctx, Y4, lx, nullptr, dt / 6.0, 0.0, MU, lx, ACC))) return rc;     // ACC = l + mu4
-  if ((rc = ad_stage(ctx, Y3, lx, MU, dt / 3.0, dt, MU, ACC, ACC))) return rc;          // ACC += mu3
-  if ((rc = ad_stage(ctx, Y2, lx, MU, dt / 3.0, 0.5 * dt, MU, ACC, ACC))) return rc;    // ACC += mu2
-  return ad_stage(ctx, x, lx, MU, dt / 6.0, 0.5 * dt, nullptr, ACC, lx);                // l = ACC + mu1
+  if ((rc = stage_state<T>(ctx, x, x, 0.5 * dt, Y2, K))) return rc;
+  if ((rc = stage_state<T>(ctx, Y2, x, 0.5 * dt, Y3, K))) return rc;
+  if ((rc = stage_state<T>(ctx, Y3, x, dt, Y4, K))) return rc;
+  if ((rc = ad_stage<T>(ctx, Y4, lx, nullptr, dt / 6.0, 0.0, MU, lx, ACC))) return rc;     // ACC = l + mu4
+  if ((rc = ad_stage<T>(ctx, Y3, lx, MU, dt / 3.0, dt, MU, ACC, ACC))) return rc;          // ACC += mu3
+  if ((rc = ad_stage<T>(ctx, Y2, lx, MU, dt / 3.0, 0.5 * dt, MU, ACC, ACC))) return rc;    // ACC += mu2
+  return ad_stage<T>(ctx, x, lx, MU, dt / 6.0, 0.5 * dt, nullptr, ACC, lx);                // l = ACC + mu1
 }
 
 // rk4_ad through a CUDA graph captured for the last (x, lx, dt)
-int rk4_ad_graph(swm_ctx* ctx, const double* x, double* lx, double dt) {
+int rk4_ad_graph(swm_ctx* ctx, const void* x, void* lx, double dt) {
   if (!(ctx->ad_graph && ctx->ad_key[0] == x && ctx->ad_key[1] == lx && ctx->ad_dt == dt)) {
     if (ctx->ad_graph) { cudaGraphExecDestroy(ctx->ad_graph); ctx->ad_graph = nullptr; }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "begin capture");
-    const int rc = rk4_ad(ctx, x, lx, dt);
+    const int rc = ctx->prec == SWM_FP32_FUSED ? rk4_ad<float>(ctx, (const float*)x, (float*)lx, dt)
+                                               : rk4_ad<double>(ctx, (const double*)x, (double*)lx, dt);
     const cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
     if (rc) { if (ec == cudaSuccess) cudaGraphDestroy(g); return rc; }
     CK(ec, "end capture");
@@ -1691,14 +1706,21 @@ int rk4_ad_graph(swm_ctx* ctx, const double* x, double* lx, double dt) {
   return SWM_OK;
 }
 
-int check_tl_args(swm_ctx* ctx, const swm_state* a, const swm_state* b, const swm_state* c) {
+int check_tl_args(swm_ctx* ctx, const swm_state* a, const swm_state* b, const swm_state* c,
+                  bool tl) {
   if (int rc = check_state(ctx, a)) return rc;
   if (int rc = check_state(ctx, b)) return rc;
   if (c && check_state(ctx, c)) return SWM_E_INVALID;
   if (a == b || (c && (c == a || c == b)))
     return fail(ctx, SWM_E_INVALID, "tangent-linear / adjoint calls need distinct states");
   cudaSetDevice(ctx->cfg.device);
-  return adjoint_ws(ctx);
+  return adjoint_ws(ctx, tl);
+}
+
+// FP32 cotangents live in the high part of the state pair: clear the low part
+int clear_lo(swm_ctx* ctx, swm_state* s) {
+  if (s->lo) CK(cudaMemsetAsync(s->lo, 0, sizeof(float) * 3 * ctx->fs, ctx->st), "memset");
+  return SWM_OK;
 }
 
 }  // namespace
@@ -1757,22 +1779,26 @@ void plan_reverse(std::vector<swm_adjoint::Act>& acts, int a, int b, int sa, std
   plan_reverse(acts, a, m, sa, freeslots);
 }
 
-int copy_state(swm_ctx* ctx, void* dst, const void* src) {
-  CK(cudaMemcpyAsync(dst, src, sizeof(double) * 3 * ctx->fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+int copy_state(swm_ctx* ctx, swm_state* dst, const swm_state* src) {
+  CK(cudaMemcpyAsync(dst->hi, src->hi, (size_t)ctx->elt * 3 * ctx->fs, cudaMemcpyDeviceToDevice, ctx->st),
+     "copy");
+  if (dst->lo && src->lo)
+    CK(cudaMemcpyAsync(dst->lo, src->lo, sizeof(float) * 3 * ctx->fs, cudaMemcpyDeviceToDevice, ctx->st),
+       "copy");
   return SWM_OK;
 }
 
 int run_action(swm_adjoint* adj, const swm_adjoint::Act& a) {
   swm_ctx* ctx = adj->ctx;
   switch (a.kind) {
-    case swm_adjoint::RESTORE: return copy_state(ctx, adj->cur->hi, adj->slot[a.arg]->hi);
-    case swm_adjoint::STORE: return copy_state(ctx, adj->slot[a.arg]->hi, adj->cur->hi);
+    case swm_adjoint::RESTORE: return copy_state(ctx, adj->cur, adj->slot[a.arg]);
+    case swm_adjoint::STORE: return copy_state(ctx, adj->slot[a.arg], adj->cur);
     case swm_adjoint::ADVANCE:
       adj->fwd_steps += a.arg;
       return swm_rk4_step(ctx, adj->cur, adj->dt, a.arg);
     default:
       adj->adj_steps += 1;
-      return rk4_ad_graph(ctx, (const double*)adj->cur->hi, (double*)adj->lam->hi, adj->dt);
+      return rk4_ad_graph(ctx, adj->cur->hi, adj->lam->hi, adj->dt);
   }
 }
 
@@ -1789,33 +1815,36 @@ void free_adjoint(swm_adjoint* adj) {
 extern "C" {
 
 int swm_apply_tl(swm_ctx* ctx, const swm_state* y, const swm_state* dx, swm_state* dk) {
-  if (int rc = check_tl_args(ctx, y, dx, dk)) return rc;
+  if (int rc = check_tl_args(ctx, y, dx, dk, true)) return rc;
   return tl_apply(ctx, (const double*)y->hi, (const double*)dx->hi, (double*)dk->hi);
 }
 
 int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk, swm_state* lx) {
-  if (int rc = check_tl_args(ctx, y, lk, lx)) return rc;
-  return ad_apply(ctx, (const double*)y->hi, (const double*)lk->hi, (double*)lx->hi);
+  if (int rc = check_tl_args(ctx, y, lk, lx, false)) return rc;
+  if (ctx->prec == SWM_FP32_FUSED) {
+    if (int rc = ad_apply<float>(ctx, (const float*)y->hi, (const float*)lk->hi, (float*)lx->hi)) return rc;
+    return clear_lo(ctx, lx);
+  }
+  return ad_apply<double>(ctx, (const double*)y->hi, (const double*)lk->hi, (double*)lx->hi);
 }
 
 int swm_rk4_tl(swm_ctx* ctx, const swm_state* x, swm_state* dx, double dt) {
-  if (int rc = check_tl_args(ctx, x, dx, nullptr)) return rc;
+  if (int rc = check_tl_args(ctx, x, dx, nullptr, true)) return rc;
   return rk4_tl(ctx, (const double*)x->hi, (double*)dx->hi, dt);
 }
 
 int swm_rk4_ad(swm_ctx* ctx, const swm_state* x, swm_state* lx, double dt) {
-  if (int rc = check_tl_args(ctx, x, lx, nullptr)) return rc;
-  return rk4_ad_graph(ctx, (const double*)x->hi, (double*)lx->hi, dt);
+  if (int rc = check_tl_args(ctx, x, lx, nullptr, false)) return rc;
+  if (int rc = rk4_ad_graph(ctx, x->hi, lx->hi, dt)) return rc;
+  return clear_lo(ctx, lx);
 }
 
 int swm_adjoint_create(swm_ctx* ctx, int nsteps, int nsnap, double dt, swm_adjoint** out) {
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
   if (nsteps < 1 || nsnap < 1 || !(dt > 0.0))
     return fail(ctx, SWM_E_INVALID, "need nsteps >= 1, nsnap >= 1 and dt > 0");
-  if (ctx->prec != SWM_FP64_PLAIN)
-    return fail(ctx, SWM_E_UNSUPPORTED, "the adjoint needs an FP64 (plain) context");
   cudaSetDevice(ctx->cfg.device);
-  if (int rc = adjoint_ws(ctx)) return rc;
+  if (int rc = adjoint_ws(ctx, false)) return rc;
   swm_adjoint* adj = new swm_adjoint();
   adj->ctx = ctx; adj->nsteps = nsteps; adj->nsnap = std::min(nsnap, nsteps); adj->dt = dt;
   for (int k = 0; k < adj->nsnap; ++k) {
@@ -1846,11 +1875,11 @@ int swm_adjoint_forward(swm_adjoint* adj, const swm_state* x0, swm_state* xT) {
   if (int rc = check_state(ctx, xT)) return rc;
   cudaSetDevice(ctx->cfg.device);
   adj->fwd_steps = adj->adj_steps = 0;
-  if (int rc = copy_state(ctx, adj->slot[0]->hi, x0->hi)) return rc;
+  if (int rc = copy_state(ctx, adj->slot[0], x0)) return rc;
   for (size_t k = 0; k < adj->first_adj; ++k)
     if (int rc = run_action(adj, adj->plan[k])) return rc;
   // the working state holds x_{T-1}: one more step gives x_T
-  if (int rc = copy_state(ctx, xT->hi, adj->cur->hi)) return rc;
+  if (int rc = copy_state(ctx, xT, adj->cur)) return rc;
   if (int rc = swm_rk4_step(ctx, xT, adj->dt, 1)) return rc;
   adj->fwd_steps += 1;
   adj->ready = true;
@@ -1863,10 +1892,11 @@ int swm_adjoint_backward(swm_adjoint* adj, swm_state* lambda) {
   if (int rc = check_state(ctx, lambda)) return rc;
   if (!adj->ready) return fail(ctx, SWM_E_INVALID, "swm_adjoint_backward needs a forward run first");
   cudaSetDevice(ctx->cfg.device);
-  if (int rc = copy_state(ctx, adj->lam->hi, lambda->hi)) return rc;
+  if (int rc = copy_state(ctx, adj->lam, lambda)) return rc;
   for (size_t k = adj->first_adj; k < adj->plan.size(); ++k)
     if (int rc = run_action(adj, adj->plan[k])) return rc;
-  if (int rc = copy_state(ctx, lambda->hi, adj->lam->hi)) return rc;
+  if (int rc = copy_state(ctx, lambda, adj->lam)) return rc;
+  if (int rc = clear_lo(ctx, lambda)) return rc;
   adj->ready = false;
   CK(cudaStreamSynchronize(ctx->st), "sync");
   return check_device_flag(ctx);

@@ -1,6 +1,7 @@
-// swm_adjoint.cu -- tangent-linear (TL) and adjoint (AD) kernels of the FP64
-// vector-invariant model operator F (operator_swm_mod.f90:61-113), for the
-// discrete adjoint of the RK4 step.  No counterpart in the reference.
+// swm_adjoint.cu -- tangent-linear (TL, FP64) and adjoint (AD, FP64 or FP32)
+// kernels of the vector-invariant model operator F (operator_swm_mod.f90:
+// 61-113), for the discrete adjoint of the RK4 step.  No counterpart in the
+// reference.
 //
 // With base state y = (h, u, v), ut = Qi11 u + Qi12 v, vt = Qi12 u + Qi22 v,
 // K = (u ut + v vt)/2 + g (h + hs), the operator is
@@ -54,41 +55,40 @@ template <> struct AdOrd<63> { static constexpr int CT = 9, KR = 12; };
 // index k.  Columns near the ends use the transposed closure block, the
 // interior the negated interior stencil (the interior stencil is
 // antisymmetric).
-template <int ORD, class Get>
-__device__ __forceinline__ double dT_line(const SbpT& t, int n, int c, Get F) {
+template <int ORD, class T, class Get>
+__device__ __forceinline__ T dT_line(const SbpT& t, int n, int c, Get F) {
   constexpr int CT = AdOrd<ORD>::CT, KR = AdOrd<ORD>::KR;
-  double s = 0.0;
+  T s = T(0);
   if (c < CT) {
 #pragma unroll
-    for (int r = 0; r < KR; ++r) s += t.t[c * KR + r] * F(r);
+    for (int r = 0; r < KR; ++r) s += T(t.t[c * KR + r]) * F(r);
     return s;
   }
   if (c >= n - CT) {
     const int cc = n - 1 - c;
 #pragma unroll
-    for (int r = 0; r < KR; ++r) s += t.t[cc * KR + r] * F(n - 1 - r);
+    for (int r = 0; r < KR; ++r) s += T(t.t[cc * KR + r]) * F(n - 1 - r);
     return -s;
   }
-  return -d_interior<ORD, double>([&](int o) { return F(c + o); });
+  return -d_interior<ORD, T>([&](int o) { return F(c + o); });
 }
 
 // Pre-sync curl of the base state, rJ (Dx v - Dy u), with the values of the
 // panel-boundary nodes also stored in the EV_ZETA slots of the edge buffer
 // Z (the layout of the forward edge buffer).
-template <int ORD>
-__global__ void zeta_pre_kernel(FieldGeom g, const double* m, const double* y, double* zeta,
-                                double* Z) {
+template <class T, int ORD>
+__global__ void zeta_pre_kernel(FieldGeom g, const T* m, const T* y, T* zeta, T* Z) {
   Node o;
   if (!node_of(g, o)) return;
   const long long fs = g.fs, x = o.x;
   const int n = g.n, e = n - 1;
   const long long row = (long long)o.p * g.ps + (long long)o.j * g.P;
   const long long col = (long long)o.p * g.ps + o.i;
-  const double* u = y + fs;
-  const double* v = y + 2 * fs;
-  const double dxv = d_line<ORD, double>(o.i, n, [&](int k) { return v[row + k]; });
-  const double dyu = d_line<ORD, double>(o.j, n, [&](int k) { return u[col + (long long)k * g.P]; });
-  const double z = (dxv - dyu) * m[MRJ * fs + x];
+  const T* u = y + fs;
+  const T* v = y + 2 * fs;
+  const T dxv = d_line<ORD, T>(o.i, n, [&](int k) { return v[row + k]; });
+  const T dyu = d_line<ORD, T>(o.j, n, [&](int k) { return u[col + (long long)k * g.P]; });
+  const T z = (dxv - dyu) * m[MRJ * fs + x];
   zeta[x] = z;
   auto put = [&](int side, int k) { Z[((long long)(o.p * 4 + side) * 4 + EV_ZETA) * n + k] = z; };
   if (o.i == 0) put(SIDE_L, o.j);
@@ -134,12 +134,13 @@ __global__ void tl_post_kernel(FieldGeom g, const double* m, const double* y, co
 // Sv^T pull of one boundary node: the cotangent of a raw neighbour value
 // read through ring_vector (component map included) goes to the reading
 // node's slot C[p][side][EV_GX|EV_GY][k].
-__device__ __forceinline__ void put_ring(double* C, const Topology& tp, int n, int p, int side,
-                                         int k, double lrx, double lry) {
+template <class T>
+__device__ __forceinline__ void put_ring(T* C, const Topology& tp, int n, int p, int side,
+                                         int k, T lrx, T lry) {
   const EdgeLink L = tp.link[p][side];
-  double lgx, lgy;
-  if (L.dim_i) { lgx = L.istep * lrx; lgy = L.jstep * lry; }
-  else { lgy = L.jstep * lrx; lgx = L.istep * lry; }
+  T lgx, lgy;
+  if (L.dim_i) { lgx = T(L.istep) * lrx; lgy = T(L.jstep) * lry; }
+  else { lgy = T(L.jstep) * lrx; lgx = T(L.istep) * lry; }
   C[((long long)(p * 4 + side) * 4 + EV_GX) * n + k] = lgx;
   C[((long long)(p * 4 + side) * 4 + EV_GY) * n + k] = lgy;
 }
@@ -147,35 +148,35 @@ __device__ __forceinline__ void put_ring(double* C, const Topology& tp, int n, i
 // the pulls of one boundary node (i, j) of panel p: (a, b) are the
 // cotangents of its synced (gx, gy) = (V, U) (syncronize_grad_on_edges,
 // transposed case by case), s1/s2 the two scalar fields
-__device__ __forceinline__ void pull_node(double* C, const Topology& tp, const double* qw, int n,
-                                          int p, int i, int j, double a, double b, double s1,
-                                          double s2) {
+template <class T>
+__device__ __forceinline__ void pull_node(T* C, const Topology& tp, const double* qw, int n,
+                                          int p, int i, int j, T a, T b, T s1, T s2) {
   const int e = n - 1;
   const double* qb = qw;
   const double* qt = qw + n;
   const double* ql = qw + 2 * n;
   const double* qr = qw + 3 * n;
-  const double t3 = 1.0 / 3.0;
+  const T t3 = T(1.0 / 3.0), hf = T(0.5);
   if (i == 0 && j == 0) {
-    put_ring(C, tp, n, p, SIDE_L, 0, a * t3, b * t3 + ql[0] * a * t3);
-    put_ring(C, tp, n, p, SIDE_B, 0, a * t3 + qb[0] * b * t3, b * t3);
+    put_ring(C, tp, n, p, SIDE_L, 0, a * t3, b * t3 + T(ql[0]) * a * t3);
+    put_ring(C, tp, n, p, SIDE_B, 0, a * t3 + T(qb[0]) * b * t3, b * t3);
   } else if (i == e && j == 0) {
-    put_ring(C, tp, n, p, SIDE_R, 0, a * t3, b * t3 + qr[0] * a * t3);
-    put_ring(C, tp, n, p, SIDE_B, e, a * t3 + qb[e] * b * t3, b * t3);
+    put_ring(C, tp, n, p, SIDE_R, 0, a * t3, b * t3 + T(qr[0]) * a * t3);
+    put_ring(C, tp, n, p, SIDE_B, e, a * t3 + T(qb[e]) * b * t3, b * t3);
   } else if (i == 0 && j == e) {
-    put_ring(C, tp, n, p, SIDE_L, e, a * t3, b * t3 + ql[e] * a * t3);
-    put_ring(C, tp, n, p, SIDE_T, 0, a * t3 + qt[0] * b * t3, b * t3);
+    put_ring(C, tp, n, p, SIDE_L, e, a * t3, b * t3 + T(ql[e]) * a * t3);
+    put_ring(C, tp, n, p, SIDE_T, 0, a * t3 + T(qt[0]) * b * t3, b * t3);
   } else if (i == e && j == e) {
-    put_ring(C, tp, n, p, SIDE_R, e, a * t3, b * t3 + qr[e] * a * t3);
-    put_ring(C, tp, n, p, SIDE_T, e, a * t3 + qt[e] * b * t3, b * t3);
+    put_ring(C, tp, n, p, SIDE_R, e, a * t3, b * t3 + T(qr[e]) * a * t3);
+    put_ring(C, tp, n, p, SIDE_T, e, a * t3 + T(qt[e]) * b * t3, b * t3);
   } else if (i == 0) {
-    put_ring(C, tp, n, p, SIDE_L, j, 0.5 * a, 0.5 * b + 0.5 * ql[j] * a);
+    put_ring(C, tp, n, p, SIDE_L, j, hf * a, hf * b + hf * T(ql[j]) * a);
   } else if (i == e) {
-    put_ring(C, tp, n, p, SIDE_R, j, 0.5 * a, 0.5 * b + 0.5 * qr[j] * a);
+    put_ring(C, tp, n, p, SIDE_R, j, hf * a, hf * b + hf * T(qr[j]) * a);
   } else if (j == 0) {
-    put_ring(C, tp, n, p, SIDE_B, i, 0.5 * a + 0.5 * qb[i] * b, 0.5 * b);
+    put_ring(C, tp, n, p, SIDE_B, i, hf * a + hf * T(qb[i]) * b, hf * b);
   } else {
-    put_ring(C, tp, n, p, SIDE_T, i, 0.5 * a + 0.5 * qt[i] * b, 0.5 * b);
+    put_ring(C, tp, n, p, SIDE_T, i, hf * a + hf * T(qt[i]) * b, hf * b);
   }
   auto putS = [&](int side, int k) {
     C[((long long)(p * 4 + side) * 4 + EV_ZETA) * n + k] = s1;
@@ -192,28 +193,28 @@ __device__ __forceinline__ void pull_node(double* C, const Topology& tp, const d
 // the pre-sync curl, Z its edge values):
 // A = (lGX, lGY, rJ*lDIV, rJ*lZ, l_ut part, l_vt part); at panel-boundary
 // nodes the raw (unsynced) cotangents are pulled into C for adsync_gather.
-__global__ void ad_pre_kernel(FieldGeom g, Topology tp, const double* qw, const double* m,
-                              const double* y, const double* zeta, const double* Z,
-                              const double* lam, const double* mu, double alpha, double beta,
-                              double* A, double* C) {
+template <class T>
+__global__ void ad_pre_kernel(FieldGeom g, Topology tp, const double* qw, const T* m, const T* y,
+                              const T* zeta, const T* Z, const T* lam, const T* mu, T alpha,
+                              T beta, T* A, T* C) {
   Node o;
   if (!node_of(g, o)) return;
   const long long fs = g.fs, x = o.x;
   const int n = g.n, e = n - 1;
   const bool edge = o.i == 0 || o.i == e || o.j == 0 || o.j == e;
-  double z = zeta[x];
-  if (edge) z = sync_scalar_node<double>(EdgeView<double>{Z, n}, tp, o.p, o.i, o.j, EV_ZETA, z);
-  const double u = y[fs + x], v = y[2 * fs + x];
-  const double q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
-  const double J = m[MJ * fs + x], fz = m[MF * fs + x] + z, rJ = m[MRJ * fs + x];
-  const double ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
-  double lh = alpha * lam[x], lu = alpha * lam[fs + x], lv = alpha * lam[2 * fs + x];
+  T z = zeta[x];
+  if (edge) z = sync_scalar_node<T>(EdgeView<T>{Z, n}, tp, o.p, o.i, o.j, EV_ZETA, z);
+  const T u = y[fs + x], v = y[2 * fs + x];
+  const T q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
+  const T J = m[MJ * fs + x], fz = m[MF * fs + x] + z, rJ = m[MRJ * fs + x];
+  const T ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
+  T lh = alpha * lam[x], lu = alpha * lam[fs + x], lv = alpha * lam[2 * fs + x];
   if (mu) {
     lh += beta * mu[x];
     lu += beta * mu[fs + x];
     lv += beta * mu[2 * fs + x];
   }
-  const double lz = J * (vt * lu - ut * lv);
+  const T lz = J * (vt * lu - ut * lv);
   A[x] = -lu;
   A[fs + x] = -lv;
   A[2 * fs + x] = -lh * rJ;
@@ -226,37 +227,36 @@ __global__ void ad_pre_kernel(FieldGeom g, Topology tp, const double* qw, const 
 // mu = F'(y)^T lk from the synced-transposed cotangents A (ad_pre_kernel +
 // adsync_gather_kernel); also acc_out = acc_in + mu (acc_in/acc_out
 // nullable; acc_out may be acc_in)
-template <int ORD>
-__global__ void ad_main_kernel(FieldGeom g, SbpT t, const double* m, double ghs, double grav,
-                               const double* y, const double* A, double* out,
-                               const double* acc_in, double* acc_out) {
+template <class T, int ORD>
+__global__ void ad_main_kernel(FieldGeom g, SbpT t, const T* m, T ghs, T grav, const T* y,
+                               const T* A, T* out, const T* acc_in, T* acc_out) {
   Node o;
   if (!node_of(g, o)) return;
   const long long fs = g.fs, x = o.x;
   const int n = g.n;
   const long long row = (long long)o.p * g.ps + (long long)o.j * g.P;   // node (0, j)
   const long long col = (long long)o.p * g.ps + o.i;                     // node (i, 0)
-  const double* A1 = A;
-  const double* A2 = A + fs;
-  const double* W3 = A + 2 * fs;
-  const double* W4 = A + 3 * fs;
-  const double dx1 = dT_line<ORD>(t, n, o.i, [&](int k) { return A1[row + k]; });
-  const double dy2 = dT_line<ORD>(t, n, o.j, [&](int k) { return A2[col + (long long)k * g.P]; });
-  const double dx3 = dT_line<ORD>(t, n, o.i, [&](int k) { return W3[row + k]; });
-  const double dy3 = dT_line<ORD>(t, n, o.j, [&](int k) { return W3[col + (long long)k * g.P]; });
-  const double dx4 = dT_line<ORD>(t, n, o.i, [&](int k) { return W4[row + k]; });
-  const double dy4 = dT_line<ORD>(t, n, o.j, [&](int k) { return W4[col + (long long)k * g.P]; });
-  const double h = y[x], u = y[fs + x], v = y[2 * fs + x];
-  const double q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
-  const double J = m[MJ * fs + x];
-  const double ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
-  const double lK = ghs * (dx1 + dy2);
-  const double lGu = dx3, lGv = dy3;          // cotangents of J h ut, J h vt
-  const double lut = A[4 * fs + x] + J * h * lGu + 0.5 * u * lK;
-  const double lvt = A[5 * fs + x] + J * h * lGv + 0.5 * v * lK;
-  const double mh = J * (ut * lGu + vt * lGv) + grav * lK;
-  const double mu_ = -dy4 + 0.5 * ut * lK + q1 * lut + q2 * lvt;
-  const double mv = dx4 + 0.5 * vt * lK + q2 * lut + q3 * lvt;
+  const T* A1 = A;
+  const T* A2 = A + fs;
+  const T* W3 = A + 2 * fs;
+  const T* W4 = A + 3 * fs;
+  const T dx1 = dT_line<ORD, T>(t, n, o.i, [&](int k) { return A1[row + k]; });
+  const T dy2 = dT_line<ORD, T>(t, n, o.j, [&](int k) { return A2[col + (long long)k * g.P]; });
+  const T dx3 = dT_line<ORD, T>(t, n, o.i, [&](int k) { return W3[row + k]; });
+  const T dy3 = dT_line<ORD, T>(t, n, o.j, [&](int k) { return W3[col + (long long)k * g.P]; });
+  const T dx4 = dT_line<ORD, T>(t, n, o.i, [&](int k) { return W4[row + k]; });
+  const T dy4 = dT_line<ORD, T>(t, n, o.j, [&](int k) { return W4[col + (long long)k * g.P]; });
+  const T h = y[x], u = y[fs + x], v = y[2 * fs + x];
+  const T q1 = m[MQI1 * fs + x], q2 = m[MQI2 * fs + x], q3 = m[MQI3 * fs + x];
+  const T J = m[MJ * fs + x];
+  const T ut = q1 * u + q2 * v, vt = q2 * u + q3 * v;
+  const T lK = ghs * (dx1 + dy2);
+  const T lGu = dx3, lGv = dy3;          // cotangents of J h ut, J h vt
+  const T lut = A[4 * fs + x] + J * h * lGu + T(0.5) * u * lK;
+  const T lvt = A[5 * fs + x] + J * h * lGv + T(0.5) * v * lK;
+  const T mh = J * (ut * lGu + vt * lGv) + grav * lK;
+  const T mu_ = -dy4 + T(0.5) * ut * lK + q1 * lut + q2 * lvt;
+  const T mv = dx4 + T(0.5) * vt * lK + q2 * lut + q3 * lvt;
   if (out) {
     out[x] = mh;
     out[fs + x] = mu_;
@@ -273,8 +273,9 @@ __global__ void ad_main_kernel(FieldGeom g, SbpT t, const double* m, double ghs,
 // output plus what every copy that read it pulled back (fixed order); the
 // two scalar fields get the forward scalar sync (its own transpose).
 // s1, s2 are scaled by rJ in the field (A's W3/W4) and raw in C
-__global__ void adsync_gather_kernel(FieldGeom g, Topology tp, const double* m, const double* C,
-                                     double* lgx, double* lgy, double* s1, double* s2) {
+template <class T>
+__global__ void adsync_gather_kernel(FieldGeom g, Topology tp, const T* m, const T* C, T* lgx,
+                                     T* lgy, T* s1, T* s2) {
   const int n = g.n, nb = 4 * n - 4, e = n - 1;
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= 6 * nb) return;
@@ -283,8 +284,8 @@ __global__ void adsync_gather_kernel(FieldGeom g, Topology tp, const double* m, 
   boundary_node(gi - p * nb, n, i, j);
   const long long x = (long long)p * g.ps + (long long)j * g.P + i;
   const bool corner = (i == 0 || i == e) && (j == 0 || j == e);
-  const double own = corner ? 1.0 / 3.0 : 0.5;
-  double ax = own * lgx[x], ay = own * lgy[x];
+  const T own = corner ? T(1.0 / 3.0) : T(0.5);
+  T ax = own * lgx[x], ay = own * lgy[x];
   auto add = [&](int side, int k) {
     const EdgeLink L = tp.link[p][side];
     const int kk = L.rev ? n - 1 - k : k;
@@ -295,14 +296,14 @@ __global__ void adsync_gather_kernel(FieldGeom g, Topology tp, const double* m, 
   if (i == e) add(SIDE_R, j);
   if (j == 0) add(SIDE_B, i);
   if (j == e) add(SIDE_T, i);
-  const EdgeView<double> ev{C, n};
-  const double own1 = ev.get(p, i == 0 ? SIDE_L : i == e ? SIDE_R : j == 0 ? SIDE_B : SIDE_T, EV_ZETA,
+  const EdgeView<T> ev{C, n};
+  const T own1 = ev.get(p, i == 0 ? SIDE_L : i == e ? SIDE_R : j == 0 ? SIDE_B : SIDE_T, EV_ZETA,
                              (i == 0 || i == e) ? j : i);
-  const double own2 = ev.get(p, i == 0 ? SIDE_L : i == e ? SIDE_R : j == 0 ? SIDE_B : SIDE_T, EV_DIV,
+  const T own2 = ev.get(p, i == 0 ? SIDE_L : i == e ? SIDE_R : j == 0 ? SIDE_B : SIDE_T, EV_DIV,
                              (i == 0 || i == e) ? j : i);
-  const double rJ = m[MRJ * g.fs + x];
-  const double z = sync_scalar_node<double>(ev, tp, p, i, j, EV_ZETA, own1);
-  const double d = sync_scalar_node<double>(ev, tp, p, i, j, EV_DIV, own2);
+  const T rJ = m[MRJ * g.fs + x];
+  const T z = sync_scalar_node<T>(ev, tp, p, i, j, EV_ZETA, own1);
+  const T d = sync_scalar_node<T>(ev, tp, p, i, j, EV_DIV, own2);
   lgx[x] = ax;
   lgy[x] = ay;
   s1[x] = z * rJ;
@@ -325,49 +326,66 @@ cudaError_t launch_tl_post(const FieldGeom& g, const double* m64, const double* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_zeta_pre(const FieldGeom& g, int order, const double* m64, const double* y,
-                            double* zeta, double* Z, cudaStream_t st) {
+template <class T>
+cudaError_t launch_zeta_pre(const FieldGeom& g, int order, const T* m, const T* y, T* zeta, T* Z,
+                            cudaStream_t st) {
   const int nb = nblk(6LL * g.n * g.n);
   switch (order) {
-    case 21: zeta_pre_kernel<21><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
-    case 42: zeta_pre_kernel<42><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
-    case 43: zeta_pre_kernel<43><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
-    case 63: zeta_pre_kernel<63><<<nb, TPB, 0, st>>>(g, m64, y, zeta, Z); break;
+    case 21: zeta_pre_kernel<T, 21><<<nb, TPB, 0, st>>>(g, m, y, zeta, Z); break;
+    case 42: zeta_pre_kernel<T, 42><<<nb, TPB, 0, st>>>(g, m, y, zeta, Z); break;
+    case 43: zeta_pre_kernel<T, 43><<<nb, TPB, 0, st>>>(g, m, y, zeta, Z); break;
+    case 63: zeta_pre_kernel<T, 63><<<nb, TPB, 0, st>>>(g, m, y, zeta, Z); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_ad_pre(const FieldGeom& g, const Topology& tp, const double* qw,
-                          const double* m64, const double* y, const double* zeta, const double* Z,
-                          const double* lam, const double* mu, double alpha, double beta,
-                          double* A, double* C, cudaStream_t st) {
-  ad_pre_kernel<<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, tp, qw, m64, y, zeta, Z, lam, mu, alpha,
-                                                        beta, A, C);
+template <class T>
+cudaError_t launch_ad_pre(const FieldGeom& g, const Topology& tp, const double* qw, const T* m,
+                          const T* y, const T* zeta, const T* Z, const T* lam, const T* mu, T alpha,
+                          T beta, T* A, T* C, cudaStream_t st) {
+  ad_pre_kernel<T><<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, tp, qw, m, y, zeta, Z, lam, mu, alpha,
+                                                           beta, A, C);
   return cudaGetLastError();
 }
 
-cudaError_t launch_adsync_gather(const FieldGeom& g, const Topology& tp, const double* m64,
-                                 const double* C, double* A, cudaStream_t st) {
+template <class T>
+cudaError_t launch_adsync_gather(const FieldGeom& g, const Topology& tp, const T* m, const T* C,
+                                 T* A, cudaStream_t st) {
   const int nb = 6 * (4 * g.n - 4);
-  adsync_gather_kernel<<<nblk(nb), TPB, 0, st>>>(g, tp, m64, C, A, A + g.fs, A + 2 * g.fs,
-                                                  A + 3 * g.fs);
+  adsync_gather_kernel<T><<<nblk(nb), TPB, 0, st>>>(g, tp, m, C, A, A + g.fs, A + 2 * g.fs,
+                                                     A + 3 * g.fs);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ad_main(const FieldGeom& g, int order, const SbpT& t, const double* m64,
-                           double ghs, double grav, const double* y, const double* A, double* out,
-                           const double* acc_in, double* acc_out, cudaStream_t st) {
+template <class T>
+cudaError_t launch_ad_main(const FieldGeom& g, int order, const SbpT& t, const T* m, T ghs, T grav,
+                           const T* y, const T* A, T* out, const T* acc_in, T* acc_out,
+                           cudaStream_t st) {
   const int nb = nblk(6LL * g.n * g.n);
   switch (order) {
-    case 21: ad_main_kernel<21><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
-    case 42: ad_main_kernel<42><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
-    case 43: ad_main_kernel<43><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
-    case 63: ad_main_kernel<63><<<nb, TPB, 0, st>>>(g, t, m64, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 21: ad_main_kernel<T, 21><<<nb, TPB, 0, st>>>(g, t, m, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 42: ad_main_kernel<T, 42><<<nb, TPB, 0, st>>>(g, t, m, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 43: ad_main_kernel<T, 43><<<nb, TPB, 0, st>>>(g, t, m, ghs, grav, y, A, out, acc_in, acc_out); break;
+    case 63: ad_main_kernel<T, 63><<<nb, TPB, 0, st>>>(g, t, m, ghs, grav, y, A, out, acc_in, acc_out); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
+
+#define SWM_AD_INSTANTIATE(T)                                                                    \
+  template cudaError_t launch_zeta_pre<T>(const FieldGeom&, int, const T*, const T*, T*, T*,      \
+                                          cudaStream_t);                                          \
+  template cudaError_t launch_ad_pre<T>(const FieldGeom&, const Topology&, const double*,        \
+                                        const T*, const T*, const T*, const T*, const T*,        \
+                                        const T*, T, T, T*, T*, cudaStream_t);                   \
+  template cudaError_t launch_adsync_gather<T>(const FieldGeom&, const Topology&, const T*,      \
+                                               const T*, T*, cudaStream_t);                      \
+  template cudaError_t launch_ad_main<T>(const FieldGeom&, int, const SbpT&, const T*, T, T,     \
+                                         const T*, const T*, T*, const T*, T*, cudaStream_t);
+SWM_AD_INSTANTIATE(float)
+SWM_AD_INSTANTIATE(double)
+#undef SWM_AD_INSTANTIATE
 
 int adjoint_table_ct(int order) {
   switch (order) {

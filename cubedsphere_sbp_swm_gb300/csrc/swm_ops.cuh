@@ -71,25 +71,29 @@ cudaError_t launch_tl_post(const FieldGeom& g, const double* m64, const double* 
                            const double* zeta, const double* w, const double* dgx,
                            const double* dgy, const double* dz, const double* ddiv, double* dk,
                            cudaStream_t st);
-// Adjoint stage pieces (order = SBP order of the context):
+// Adjoint stage pieces, FP64 or FP32 (order = SBP order of the context;
+// m = metric of the element type; qw = FP64 sync weights):
 // zeta = pre-sync curl rJ (Dx v - Dy u) of the state y, boundary values also
 // into the EV_ZETA slots of the edge buffer Z;
-cudaError_t launch_zeta_pre(const FieldGeom& g, int order, const double* m64, const double* y,
-                            double* zeta, double* Z, cudaStream_t st);
+template <class T>
+cudaError_t launch_zeta_pre(const FieldGeom& g, int order, const T* m, const T* y, T* zeta, T* Z,
+                            cudaStream_t st);
 // A (6 fields) from lk = alpha*lam + beta*mu (mu nullable), boundary
 // cotangents pulled into the edge buffer C;
-cudaError_t launch_ad_pre(const FieldGeom& g, const Topology& tp, const double* qw,
-                          const double* m64, const double* y, const double* zeta, const double* Z,
-                          const double* lam, const double* mu, double alpha, double beta,
-                          double* A, double* C, cudaStream_t st);
+template <class T>
+cudaError_t launch_ad_pre(const FieldGeom& g, const Topology& tp, const double* qw, const T* m,
+                          const T* y, const T* zeta, const T* Z, const T* lam, const T* mu, T alpha,
+                          T beta, T* A, T* C, cudaStream_t st);
 // the transposed cube-edge syncs of A's first four fields from C;
-cudaError_t launch_adsync_gather(const FieldGeom& g, const Topology& tp, const double* m64,
-                                 const double* C, double* A, cudaStream_t st);
+template <class T>
+cudaError_t launch_adsync_gather(const FieldGeom& g, const Topology& tp, const T* m, const T* C,
+                                 T* A, cudaStream_t st);
 // out = F'(y)^T lk (out nullable); acc_out = acc_in + out (both nullable,
 // may alias)
-cudaError_t launch_ad_main(const FieldGeom& g, int order, const SbpT& t, const double* m64,
-                           double ghs, double grav, const double* y, const double* A, double* out,
-                           const double* acc_in, double* acc_out, cudaStream_t st);
+template <class T>
+cudaError_t launch_ad_main(const FieldGeom& g, int order, const SbpT& t, const T* m, T ghs, T grav,
+                           const T* y, const T* A, T* out, const T* acc_in, T* acc_out,
+                           cudaStream_t st);
 // transposed-table width of an SBP order (must match make_sbpT)
 int adjoint_table_ct(int order);
 

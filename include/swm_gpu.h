@@ -201,13 +201,16 @@ int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches,
                     double* edge_ms, long* edge_launches);
 
 /* ---------------------------------------------------------------------- */
-/* Tangent-linear and adjoint of the FP64 model (no counterpart in the      */
+/* Tangent-linear and adjoint of the model (no counterpart in the           */
 /* reference).  F is the model operator of swm_apply, Phi one RK4 step of   */
 /* swm_rk4_step.  The adjoint is the exact transpose of the tangent-linear  */
 /* model of the discrete operators (SBP stencils with their closures, the    */
-/* cube-edge syncs, RK4) in the algebraic inner product of swm_dot.  FP64    */
-/* contexts only; the first call allocates the context's TL/AD workspace.    */
-/* Arguments must be distinct states of the context.                        */
+/* cube-edge syncs, RK4) in the algebraic inner product of swm_dot.  The     */
+/* tangent-linear calls need an FP64 context; the adjoint calls run in both  */
+/* precisions (FP32 contexts: FP32 arithmetic, cotangents in the high part   */
+/* of the state pair, low part cleared).  The first call allocates the       */
+/* context's TL/AD workspace.  Arguments must be distinct states of the      */
+/* context.                                                                 */
 /* ---------------------------------------------------------------------- */
 /* dk = F'(y) dx */
 int swm_apply_tl(swm_ctx* ctx, const swm_state* y, const swm_state* dx,

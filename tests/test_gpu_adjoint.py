@@ -192,9 +192,50 @@ def test_torch_autograd_matches_direct(setup):
         assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
 
 
-def test_fp32_context_is_rejected():
+def test_fp32_context_rejects_the_tangent_linear_model():
     op = swm.OperatorSWM(swm.ModelConfig(N=N, precision="fp32"))
     s = op.create_stvec()
     with pytest.raises(swm.SwmError) as e:
-        ad.rk4_ad(op, s, op.create_stvec(), DT)
+        ad.rk4_tl(op, s, op.create_stvec(), DT)
     assert e.value.code == swm._abi.SWM_E_UNSUPPORTED
+
+
+def _rel(a, b):
+    return float(np.sqrt(sum(np.sum((x - y) ** 2) for x, y in zip(a, b)) /
+                         sum(np.sum(y * y) for y in b)))
+
+
+@pytest.mark.parametrize("order", [42, 63])
+def test_fp32_adjoint_step_matches_fp64(order):
+    """One FP32 adjoint step against the FP64 one on the same base state and
+    cotangent: relative L2 <= 1e-4 (FP32 stencil arithmetic)."""
+    x0 = initial.balanced_zonal(N, 3, 16)[:3]
+    rng = np.random.default_rng(21)
+    lam = tuple(rng.standard_normal((6, N + 1, N + 1)) for _ in range(3))
+    out = {}
+    for prec in ("fp64", "fp32"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=order, precision=prec))
+        lx = _stvec(op, lam)
+        ad.rk4_ad(op, _stvec(op, x0), lx, DT)
+        out[prec] = lx.download()
+    assert _rel(out["fp32"], out["fp64"]) <= 1e-4
+
+
+def test_fp32_checkpointed_gradient_matches_fp64():
+    """Gradient of J over 20 steps with 4 snapshots, FP32 against FP64:
+    relative L2 of the gradient <= 1e-3."""
+    x0 = initial.balanced_zonal(N, 3, 16)[:3]
+    grads = {}
+    for prec in ("fp64", "fp32"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, precision=prec))
+        w = ad.quadrature_weights(op)
+        hobs = _trajectory(op, initial.balanced_zonal(N, 4, 16)[:3], T)[T][0]
+        run = ad.CheckpointedRK4(op, DT, T, 4)
+        xT = op.create_stvec()
+        run.forward(_stvec(op, x0), xT)
+        hT = xT.download()[0]
+        lam = _stvec(op, (w * (hT - hobs), np.zeros(op.shape), np.zeros(op.shape)))
+        run.backward(lam)
+        grads[prec] = lam.download()
+        assert run.counts()["adjoint_steps"] == T
+    assert _rel(grads["fp32"], grads["fp64"]) <= 1e-3
