@@ -354,6 +354,44 @@ def adjoint_leg(local):
         jm = cost([a - eps * b for a, b in zip(x0, dd)])
         an = float(sum(np.sum(p * q) for p, q in zip(grad, dd)))
         gaps.append(abs((jp - jm) / (2 * eps) - an) / abs(an))
+
+    # the same gradient in the FP32 form: cost against the FP32 forward step,
+    # and its gradient against the FP64 one
+    op32 = swm.OperatorSWM(swm.ModelConfig(N=N, precision="fp32", device=local))
+    st32 = torch.cuda.ExternalStream(op32.stream, device=dev)
+
+    def timed32(fn):
+        op32.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st32)
+        fn()
+        b.record(st32)
+        op32.synchronize()
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def st_32(arrs):
+        v = op32.create_stvec()
+        v.upload(*arrs)
+        return v
+
+    s32 = st_32(x0)
+    rk4.step(s32, op32, dt, 3)
+    s32.upload(*x0)
+    fwd32_ms = timed32(lambda: rk4.step(s32, op32, dt, T))
+    x32, lam32 = st_32(x0), st_32((w, zeros, zeros))
+    ad.rk4_ad(op32, x32, lam32, dt)
+    adj32_ms = timed32(lambda: [ad.rk4_ad(op32, x32, lam32, dt) for _ in range(reps)]) / reps
+    run32 = ad.CheckpointedRK4(op32, dt, T, c["nsnap"])
+    sx32, xT32 = st_32(x0), op32.create_stvec()
+    for _ in range(2):                               # warm-up, then timed
+        f32_ms = timed32(lambda: run32.forward(sx32, xT32))
+        hT32 = xT32.download()[0]
+        g32 = st_32((w * (hT32 - hobs), zeros, zeros))
+        b32_ms = timed32(lambda: run32.backward(g32))
+    grad32 = g32.download()
+    gerr32 = float(np.sqrt(sum(np.sum((p - q) ** 2) for p, q in zip(grad32, grad)) /
+                           sum(np.sum(q * q) for q in grad)))
     return {
         "N": N, "steps": T, "dt_s": dt, "snapshots": c["nsnap"], "precision": "fp64",
         "cost": "J = 1/2 sum_nodes w (h_T - h_obs)^2, w = SBP quadrature weights",
@@ -366,6 +404,11 @@ def adjoint_leg(local):
         "adjoint_steps_in_gradient": counts["adjoint_steps"],
         "dot_product_rel_gap": dot_gap,
         "fd_directions": c["ndir"], "fd_eps": eps, "fd_max_rel_gap": max(gaps),
+        "fp32": {"forward_step_ms": round(fwd32_ms / T, 5), "adjoint_step_ms": round(adj32_ms, 5),
+                 "adjoint_over_forward_step": round(adj32_ms / (fwd32_ms / T), 3),
+                 "forward_run_ms": round(fwd32_ms, 3), "gradient_ms": round(f32_ms + b32_ms, 3),
+                 "gradient_over_forward_run": round((f32_ms + b32_ms) / fwd32_ms, 3),
+                 "gradient_rel_l2_vs_fp64": gerr32},
         "note": "the workload's dt = 300 s (Courant 1.39) is past the RK4 stability limit; "
                 "dt = 150 s (Courant 0.70)",
     }
