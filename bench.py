@@ -565,7 +565,7 @@ def run_gpu_arm(args):
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "e2e": {"value": round(e2e_val, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,
-                    "path": "swm_state_upload (pinned FP64 host) + swm_rk4_step + swm_state_download"},
+                    "path": "swm_state_upload (pinned FP64 host arrays, read in place over the host link) + swm_rk4_step + swm_state_download (written in place)"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "kernel": "stage_tma_kernel<float,%d,mode>" % ORDER, "peak_source": peak_kind,

@@ -316,6 +316,43 @@ EncodeTiledFn encode_tiled() {
   return fn;
 }
 
+// Device address of a host array of `bytes` bytes that kernels may read and
+// write in place, or nullptr.  Only an array whose first and last byte lie in
+// the same page-locked CUDA allocation (cudaHostAlloc / cudaMallocHost /
+// cudaHostRegister, same buffer id) mapped for the current device qualifies;
+// pageable memory and anything the driver does not describe answer nullptr.
+typedef CUresult (*PtrAttrsFn)(unsigned, CUpointer_attribute*, void**, CUdeviceptr);
+void* mapped_host(const void* p, size_t bytes) {
+  static PtrAttrsFn fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    void* q = nullptr;
+    cudaDriverEntryPointQueryResult r;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttributes", &q, 12000, cudaEnableDefault,
+                                         &r) == cudaSuccess &&
+        r == cudaDriverEntryPointSuccess)
+      fn = (PtrAttrsFn)q;
+    looked = true;
+  }
+  if (!fn || !p || bytes == 0) return nullptr;
+  CUpointer_attribute at[3] = {CU_POINTER_ATTRIBUTE_MEMORY_TYPE, CU_POINTER_ATTRIBUTE_DEVICE_POINTER,
+                               CU_POINTER_ATTRIBUTE_BUFFER_ID};
+  unsigned mt[2] = {0, 0};
+  CUdeviceptr dp[2] = {0, 0};
+  unsigned long long id[2] = {0, 0};
+  for (int e = 0; e < 2; ++e) {
+    void* out[3] = {&mt[e], &dp[e], &id[e]};
+    const char* a = (const char*)p + (e ? bytes - 1 : 0);
+    if (fn(3, at, out, (CUdeviceptr)a) != CUDA_SUCCESS) {
+      cudaGetLastError();
+      return nullptr;
+    }
+  }
+  if (mt[0] != CU_MEMORYTYPE_HOST || mt[1] != CU_MEMORYTYPE_HOST) return nullptr;
+  if (!dp[0] || dp[1] - dp[0] != bytes - 1 || id[0] == 0 || id[0] != id[1]) return nullptr;
+  return (void*)dp[0];
+}
+
 // 3-D map (column, row of the 6n panel rows, field) over nfields pitched
 // fields starting at base; box {boxw, rps, boxf}.
 template <class T>
@@ -431,6 +468,66 @@ int state64(swm_ctx* ctx, const swm_state* s, const double** h, const double** u
                            d + c * ctx->g64.fs, ctx->st), "join");
   }
   *h = d; *u = d + ctx->g64.fs; *v = d + 2 * ctx->g64.fs;
+  return SWM_OK;
+}
+
+// Whole-state transfers between packed FP64 arrays (6*n*n values per field,
+// host or device) and a state.  One kernel scatters the packed fields into
+// the pitched state (splitting them into the FP32 pair) and reads device
+// arrays and page-locked host arrays in place, the latter over the
+// host-device link; pageable host data first moves as one contiguous copy
+// per field into the work fields 11..13.  Downloads run the mirror image.
+int put_packed(swm_ctx* ctx, swm_state* s, const double* const src[3], cudaMemcpyKind kind) {
+  const size_t bytes = sizeof(double) * 6 * (size_t)ctx->n * ctx->n;
+  PackedFields pf;
+  for (int c = 0; c < 3; ++c) {
+    pf.f[c] = const_cast<double*>(src[c]);
+    if (kind != cudaMemcpyHostToDevice) continue;
+    if (void* d = mapped_host(src[c], bytes)) {
+      pf.f[c] = (double*)d;
+    } else {
+      pf.f[c] = tmpf(ctx, 11 + c);
+      CK(cudaMemcpyAsync(pf.f[c], src[c], bytes, cudaMemcpyHostToDevice, ctx->st), "upload");
+    }
+  }
+  CK(launch_unpack_state(ctx->g64, 3, pf, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr,
+                         ctx->st),
+     "unpack");
+  return SWM_OK;
+}
+
+// one packed FP64 host field into a pitched FP64 field
+int put_field(swm_ctx* ctx, double* dst, const double* host) {
+  const size_t bytes = sizeof(double) * 6 * (size_t)ctx->n * ctx->n;
+  PackedFields pf{{(double*)mapped_host(host, bytes), nullptr, nullptr}};
+  if (!pf.f[0]) {
+    pf.f[0] = tmpf(ctx, 11);
+    CK(cudaMemcpyAsync(pf.f[0], host, bytes, cudaMemcpyHostToDevice, ctx->st), "upload");
+  }
+  CK(launch_unpack_state(ctx->g64, 1, pf, dst, nullptr, ctx->st), "unpack");
+  return SWM_OK;
+}
+
+int get_packed(swm_ctx* ctx, const swm_state* s, double* const dst[3], cudaMemcpyKind kind) {
+  const size_t bytes = sizeof(double) * 6 * (size_t)ctx->n * ctx->n;
+  bool staged[3] = {false, false, false};
+  PackedFields pf;
+  for (int c = 0; c < 3; ++c) {
+    pf.f[c] = dst[c];
+    if (kind != cudaMemcpyDeviceToHost) continue;
+    if (void* d = mapped_host(dst[c], bytes)) {
+      pf.f[c] = (double*)d;
+    } else {
+      pf.f[c] = tmpf(ctx, 11 + c);
+      staged[c] = true;
+    }
+  }
+  CK(launch_pack_state(ctx->g64, 3, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr, pf,
+                       ctx->st),
+     "pack");
+  for (int c = 0; c < 3; ++c)
+    if (staged[c])
+      CK(cudaMemcpyAsync(dst[c], pf.f[c], bytes, cudaMemcpyDeviceToHost, ctx->st), "download");
   return SWM_OK;
 }
 
@@ -716,8 +813,7 @@ int swm_set_orography(swm_ctx* ctx, const double* hs) {
     CK(cudaMalloc(&ctx->hs64, sizeof(double) * ctx->fs), "alloc");
     CK(cudaMemsetAsync(ctx->hs64, 0, sizeof(double) * ctx->fs, ctx->st), "memset");
   }
-  CK(cudaMemcpy2DAsync(ctx->hs64, sizeof(double) * ctx->P, hs, sizeof(double) * ctx->n,
-                       sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyHostToDevice, ctx->st), "upload");
+  if (int rc = put_field(ctx, ctx->hs64, hs)) return rc;
   if (ctx->prec == SWM_FP32_FUSED) {
     if (!ctx->hsT) CK(cudaMalloc(&ctx->hsT, sizeof(float) * ctx->fs), "alloc");
     CK(launch_to_f32(ctx->hs64, (float*)ctx->hsT, ctx->fs, ctx->st), "to f32");
@@ -783,14 +879,7 @@ int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* 
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
   cudaSetDevice(ctx->cfg.device);
   const double* src[3] = {h, u, v};
-  for (int c = 0; c < 3; ++c) {
-    double* dst = ctx->prec == SWM_FP64_PLAIN ? (double*)s->hi + c * ctx->fs : tmpf(ctx, 11 + c);
-    CK(cudaMemcpy2DAsync(dst, sizeof(double) * ctx->P, src[c], sizeof(double) * ctx->n,
-                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyHostToDevice, ctx->st), "upload");
-    if (ctx->prec == SWM_FP32_FUSED)
-      CK(launch_split_f64(ctx->fs, dst, (float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs, ctx->st), "split");
-  }
-  return SWM_OK;
+  return put_packed(ctx, s, src, cudaMemcpyHostToDevice);
 }
 
 int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
@@ -798,12 +887,7 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
   cudaSetDevice(ctx->cfg.device);
   double* dst[3] = {h, u, v};
-  const double *dh, *du, *dv;
-  if (int rc = state64(ctx, s, &dh, &du, &dv)) return rc;
-  const double* src[3] = {dh, du, dv};
-  for (int c = 0; c < 3; ++c)
-    CK(cudaMemcpy2DAsync(dst[c], sizeof(double) * ctx->n, src[c], sizeof(double) * ctx->P,
-                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToHost, ctx->st), "download");
+  if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
   CK(cudaStreamSynchronize(ctx->st), "sync");
   if (int rc_ = check_device_flag(ctx)) return rc_;
   return SWM_OK;
@@ -1041,17 +1125,19 @@ int swm_field_upload(swm_ctx* ctx, swm_field* f, const double* host) {
   if (int rc = check_field(ctx, f)) return rc;
   if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
   cudaSetDevice(ctx->cfg.device);
-  CK(cudaMemcpy2DAsync(f->p, sizeof(double) * ctx->P, host, sizeof(double) * ctx->n, sizeof(double) * ctx->n,
-                       (size_t)6 * ctx->n, cudaMemcpyHostToDevice, ctx->st), "upload");
-  return SWM_OK;
+  return put_field(ctx, f->p, host);
 }
 
 int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
   if (int rc = check_field(ctx, f)) return rc;
   if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
   cudaSetDevice(ctx->cfg.device);
-  CK(cudaMemcpy2DAsync(host, sizeof(double) * ctx->n, f->p, sizeof(double) * ctx->P, sizeof(double) * ctx->n,
-                       (size_t)6 * ctx->n, cudaMemcpyDeviceToHost, ctx->st), "download");
+  const size_t bytes = sizeof(double) * 6 * (size_t)ctx->n * ctx->n;
+  PackedFields pf{{(double*)mapped_host(host, bytes), nullptr, nullptr}};
+  const bool staged = !pf.f[0];
+  if (staged) pf.f[0] = tmpf(ctx, 11);
+  CK(launch_pack_state(ctx->g64, 1, f->p, nullptr, pf, ctx->st), "pack");
+  if (staged) CK(cudaMemcpyAsync(host, pf.f[0], bytes, cudaMemcpyDeviceToHost, ctx->st), "download");
   CK(cudaStreamSynchronize(ctx->st), "sync");
   if (int rc_ = check_device_flag(ctx)) return rc_;
   return SWM_OK;
@@ -1921,15 +2007,7 @@ int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const d
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
   cudaSetDevice(ctx->cfg.device);
   const double* src[3] = {h, u, v};
-  for (int c = 0; c < 3; ++c) {
-    double* dst = ctx->prec == SWM_FP64_PLAIN ? (double*)s->hi + c * ctx->fs : tmpf(ctx, 11 + c);
-    CK(cudaMemcpy2DAsync(dst, sizeof(double) * ctx->P, src[c], sizeof(double) * ctx->n,
-                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToDevice, ctx->st),
-       "device upload");
-    if (ctx->prec == SWM_FP32_FUSED)
-      CK(launch_split_f64(ctx->fs, dst, (float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs, ctx->st), "split");
-  }
-  return SWM_OK;
+  return put_packed(ctx, s, src, cudaMemcpyDeviceToDevice);
 }
 
 int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
@@ -1937,14 +2015,7 @@ int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, doubl
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
   cudaSetDevice(ctx->cfg.device);
   double* dst[3] = {h, u, v};
-  const double *dh, *du, *dv;
-  if (int rc = state64(ctx, s, &dh, &du, &dv)) return rc;
-  const double* src[3] = {dh, du, dv};
-  for (int c = 0; c < 3; ++c)
-    CK(cudaMemcpy2DAsync(dst[c], sizeof(double) * ctx->n, src[c], sizeof(double) * ctx->P,
-                         sizeof(double) * ctx->n, (size_t)6 * ctx->n, cudaMemcpyDeviceToDevice, ctx->st),
-       "device download");
-  return SWM_OK;
+  return get_packed(ctx, s, dst, cudaMemcpyDeviceToDevice);
 }
 
 int swm_quadrature_weights(swm_ctx* ctx, double* w_host) {

@@ -370,6 +370,43 @@ __global__ void join_kernel(long long count, const float* hi, const float* lo, d
   d[k] = (double)hi[k] + (double)lo[k];
 }
 
+// Packed <-> pitched state fields.  Block b handles one row of one field
+// (b = (c*6 + p)*n + j); packed fields hold 6*n*n contiguous values in
+// (panel, j, i) order, the state fields n*P pitched rows per panel.
+template <class T>
+__global__ void unpack_kernel(FieldGeom g, PackedFields src, T* hi, float* lo) {
+  const int n = g.n;
+  const long long b = blockIdx.x;
+  const int c = (int)(b / (6LL * n));
+  const long long row = b - (long long)c * 6 * n;        // p*n + j
+  const double* s = src.f[c] + row * n;
+  const long long o = c * g.fs + row * g.P;              // p*ps + j*P (ps = n*P)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = s[i];
+    if constexpr (sizeof(T) == 8) {
+      hi[o + i] = x;
+    } else {
+      const float h = (float)x;
+      hi[o + i] = h;
+      lo[o + i] = (float)(x - (double)h);
+    }
+  }
+}
+
+template <class T>
+__global__ void pack_kernel(FieldGeom g, const T* hi, const float* lo, PackedFields dst) {
+  const int n = g.n;
+  const long long b = blockIdx.x;
+  const int c = (int)(b / (6LL * n));
+  const long long row = b - (long long)c * 6 * n;
+  double* d = dst.f[c] + row * n;
+  const long long o = c * g.fs + row * g.P;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if constexpr (sizeof(T) == 8) d[i] = hi[o + i];
+    else d[i] = (double)hi[o + i] + (double)lo[o + i];
+  }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -495,6 +532,24 @@ cudaError_t launch_split_f64(long long count, const double* src, float* hi, floa
 cudaError_t launch_join_f32pair(long long count, const float* hi, const float* lo, double* dst,
                                 cudaStream_t st) {
   join_kernel<<<nblk(count), TPB, 0, st>>>(count, hi, lo, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_state(const FieldGeom& g, int nf, const PackedFields& src, void* hi,
+                                float* lo, cudaStream_t st) {
+  if (nf < 1 || nf > 3) return cudaErrorInvalidValue;
+  const unsigned blocks = (unsigned)(nf * 6LL * g.n);
+  if (lo) unpack_kernel<float><<<blocks, 128, 0, st>>>(g, src, (float*)hi, lo);
+  else unpack_kernel<double><<<blocks, 128, 0, st>>>(g, src, (double*)hi, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_state(const FieldGeom& g, int nf, const void* hi, const float* lo,
+                              const PackedFields& dst, cudaStream_t st) {
+  if (nf < 1 || nf > 3) return cudaErrorInvalidValue;
+  const unsigned blocks = (unsigned)(nf * 6LL * g.n);
+  if (lo) pack_kernel<float><<<blocks, 128, 0, st>>>(g, (const float*)hi, lo, dst);
+  else pack_kernel<double><<<blocks, 128, 0, st>>>(g, (const double*)hi, nullptr, dst);
   return cudaGetLastError();
 }
 

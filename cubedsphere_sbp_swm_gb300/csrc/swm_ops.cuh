@@ -123,5 +123,16 @@ cudaError_t launch_split_f64(long long count, const double* src, float* hi, floa
                              cudaStream_t st);
 cudaError_t launch_join_f32pair(long long count, const float* hi, const float* lo, double* dst,
                                 cudaStream_t st);
+// Packed FP64 fields (6*n*n values each, panel-major, row-major inside a
+// panel) <-> nf pitched state fields at field stride fs.  lo == nullptr: the
+// state is FP64 (hi holds doubles); otherwise hi/lo are the FP32 pair, split
+// on unpack and summed in FP64 on pack.
+struct PackedFields {
+  double* f[3];
+};
+cudaError_t launch_unpack_state(const FieldGeom& g, int nf, const PackedFields& src, void* hi,
+                                float* lo, cudaStream_t st);
+cudaError_t launch_pack_state(const FieldGeom& g, int nf, const void* hi, const float* lo,
+                              const PackedFields& dst, cudaStream_t st);
 
 }  // namespace swm
