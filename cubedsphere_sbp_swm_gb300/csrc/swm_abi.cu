@@ -177,6 +177,7 @@ struct swm_ctx {
   double* tmp = nullptr;   // 14 FP64 work fields (g64)
   double* hs64 = nullptr; void* hsT = nullptr;
   double* partial = nullptr; double* dres = nullptr; double* hres = nullptr;
+  int* herr = nullptr;      // page-locked copy of the device error flag
   WorkUnit* units = nullptr; int nunits = 0;
   int* derr = nullptr;          // device error flag of the bounded waits
   int num_sms = 0;
@@ -537,13 +538,17 @@ int reduce(swm_ctx* ctx, int kind, const double* a, const double* b, int slot) {
   return SWM_OK;
 }
 
-// After a stream synchronisation: report (and clear) the device error flag a
-// kernel raises when one of its bounded waits expired.
-int check_device_flag(swm_ctx* ctx) {
-  int flag = 0;
-  CK(cudaMemcpy(&flag, ctx->derr, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+// Synchronise stream st and report (and clear) the device error flag a
+// kernel raises when one of its bounded waits expired; the flag is read by a
+// copy queued on st behind the work it guards.
+int sync_check(swm_ctx* ctx, cudaStream_t st) {
+  CK(cudaMemcpyAsync(ctx->herr, ctx->derr, sizeof(int), cudaMemcpyDeviceToHost, st), "read error flag");
+  CK(cudaStreamSynchronize(st), "sync");
+  const int flag = *ctx->herr;
   if (flag != 0) {
-    CK(cudaMemset(ctx->derr, 0, sizeof(int)), "clear error flag");
+    *ctx->herr = 0;
+    CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st), "clear error flag");
+    CK(cudaStreamSynchronize(st), "sync");
     return fail(ctx, SWM_E_DEVICE, "a kernel gave up a bounded wait (code " + std::to_string(flag) +
                                        "); results of the affected calls are invalid");
   }
@@ -552,8 +557,7 @@ int check_device_flag(swm_ctx* ctx) {
 
 int fetch_results(swm_ctx* ctx, int count, double* out) {
   CK(cudaMemcpyAsync(ctx->hres, ctx->dres, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->st), "copy results");
-  CK(cudaStreamSynchronize(ctx->st), "sync");
-  if (int rc_ = check_device_flag(ctx)) return rc_;
+  if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   std::memcpy(out, ctx->hres, sizeof(double) * count);
   return SWM_OK;
 }
@@ -596,6 +600,7 @@ void free_ctx(swm_ctx* c) {
                   c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (c->hres) cudaFreeHost(c->hres);
+  if (c->herr) cudaFreeHost(c->herr);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -717,6 +722,8 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   CKC(cudaMalloc(&ctx->partial, sizeof(double) * REDUCE_BLOCKS), "alloc");
   CKC(cudaMalloc(&ctx->dres, sizeof(double) * 16), "alloc");
   CKC(cudaMallocHost(&ctx->hres, sizeof(double) * 16), "alloc host");
+  CKC(cudaMallocHost(&ctx->herr, sizeof(int)), "alloc host");
+  *ctx->herr = 0;
   CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od, &ctx->shape)
                                   : prepare_stage<double>(od, &ctx->shape),
       "stage kernel attributes");
@@ -798,8 +805,7 @@ void swm_ctx_destroy(swm_ctx* ctx) {
 
 int swm_ctx_synchronize(swm_ctx* ctx) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
-  CK(cudaStreamSynchronize(ctx->st), "synchronize");
-  if (int rc_ = check_device_flag(ctx)) return rc_;
+  if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   return SWM_OK;
 }
 
@@ -888,8 +894,7 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
   cudaSetDevice(ctx->cfg.device);
   double* dst[3] = {h, u, v};
   if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
-  CK(cudaStreamSynchronize(ctx->st), "sync");
-  if (int rc_ = check_device_flag(ctx)) return rc_;
+  if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   return SWM_OK;
 }
 
@@ -1138,8 +1143,7 @@ int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
   if (staged) pf.f[0] = tmpf(ctx, 11);
   CK(launch_pack_state(ctx->g64, 1, f->p, nullptr, pf, ctx->st), "pack");
   if (staged) CK(cudaMemcpyAsync(host, pf.f[0], bytes, cudaMemcpyDeviceToHost, ctx->st), "download");
-  CK(cudaStreamSynchronize(ctx->st), "sync");
-  if (int rc_ = check_device_flag(ctx)) return rc_;
+  if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   return SWM_OK;
 }
 
@@ -1227,8 +1231,7 @@ int swm_timing_enable(swm_ctx* ctx, int on) {
 
 int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches, double* edge_ms, long* edge_launches) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
-  CK(cudaStreamSynchronize(ctx->st), "sync");
-  if (int rc_ = check_device_flag(ctx)) return rc_;
+  if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   double ts = 0.0, te = 0.0;
   for (auto& e : ctx->ev_stage) { float ms; CK(cudaEventElapsedTime(&ms, e.first, e.second), "elapsed"); ts += ms; }
   for (auto& e : ctx->ev_edge) { float ms; CK(cudaEventElapsedTime(&ms, e.first, e.second), "elapsed"); te += ms; }
@@ -1519,8 +1522,7 @@ int swm_ensemble_step(swm_ensemble* ens, int nsteps) {
 int swm_ensemble_synchronize(swm_ensemble* ens) {
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   cudaSetDevice(ens->device);
-  ECK(cudaStreamSynchronize(ens->st), "sync");
-  EMEM(check_device_flag(ens->mem[0]));
+  EMEM(sync_check(ens->mem[0], ens->st));
   return SWM_OK;
 }
 
@@ -1599,7 +1601,7 @@ int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid
   for (void* p : keep) if (p) cudaFree(p);
   if (rc == SWM_OK) rc = ens_rebuild(ens, best_seg, best_grid);
   if (rc == SWM_OK) {
-    EMEM(check_device_flag(ens->mem[0]));
+    EMEM(sync_check(ens->mem[0], ens->st));
     if (seg_rows_out) *seg_rows_out = best_seg;
     if (grid_out) *grid_out = best_grid;
     if (ms_per_step_out) *ms_per_step_out = best;
@@ -1984,8 +1986,7 @@ int swm_adjoint_backward(swm_adjoint* adj, swm_state* lambda) {
   if (int rc = copy_state(ctx, lambda, adj->lam)) return rc;
   if (int rc = clear_lo(ctx, lambda)) return rc;
   adj->ready = false;
-  CK(cudaStreamSynchronize(ctx->st), "sync");
-  return check_device_flag(ctx);
+  return sync_check(ctx, ctx->st);
 }
 
 int swm_adjoint_counts(const swm_adjoint* adj, long* forward_steps, long* adjoint_steps,

@@ -370,41 +370,53 @@ __global__ void join_kernel(long long count, const float* hi, const float* lo, d
   d[k] = (double)hi[k] + (double)lo[k];
 }
 
-// Packed <-> pitched state fields.  Block b handles one row of one field
-// (b = (c*6 + p)*n + j); packed fields hold 6*n*n contiguous values in
-// (panel, j, i) order, the state fields n*P pitched rows per panel.
+// Packed <-> pitched state fields.  Thread k handles packed value k of the
+// nf fields (k = c*6*n*n + (p*n + j)*n + i), so a warp touches 32
+// consecutive packed doubles: whole 128-byte lines of the packed side, which
+// may sit in host memory behind the host-device link.  The state fields hold
+// n*P pitched rows per panel (ps = n*P).  Indices fit 32 bits for n <= 8191.
+__device__ __forceinline__ void packed_index(const FieldGeom& g, unsigned k, unsigned& c,
+                                             unsigned& r, long long& o) {
+  const unsigned n = (unsigned)g.n, nn6 = 6u * n * n;
+  c = k / nn6;
+  r = k - c * nn6;
+  const unsigned row = r / n;
+  o = (long long)c * g.fs + (long long)row * g.P + (r - row * n);
+}
+
+__device__ __forceinline__ double* field_of(const PackedFields& pf, unsigned c) {
+  return c == 0 ? pf.f[0] : (c == 1 ? pf.f[1] : pf.f[2]);
+}
+
 template <class T>
-__global__ void unpack_kernel(FieldGeom g, PackedFields src, T* hi, float* lo) {
-  const int n = g.n;
-  const long long b = blockIdx.x;
-  const int c = (int)(b / (6LL * n));
-  const long long row = b - (long long)c * 6 * n;        // p*n + j
-  const double* s = src.f[c] + row * n;
-  const long long o = c * g.fs + row * g.P;              // p*ps + j*P (ps = n*P)
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double x = s[i];
-    if constexpr (sizeof(T) == 8) {
-      hi[o + i] = x;
-    } else {
-      const float h = (float)x;
-      hi[o + i] = h;
-      lo[o + i] = (float)(x - (double)h);
-    }
+__global__ void unpack_kernel(FieldGeom g, unsigned total, PackedFields src, T* hi, float* lo) {
+  const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  unsigned c, r;
+  long long o;
+  packed_index(g, k, c, r, o);
+  const double x = field_of(src, c)[r];
+  if constexpr (sizeof(T) == 8) {
+    hi[o] = x;
+  } else {
+    const float h = (float)x;
+    hi[o] = h;
+    lo[o] = (float)(x - (double)h);
   }
 }
 
 template <class T>
-__global__ void pack_kernel(FieldGeom g, const T* hi, const float* lo, PackedFields dst) {
-  const int n = g.n;
-  const long long b = blockIdx.x;
-  const int c = (int)(b / (6LL * n));
-  const long long row = b - (long long)c * 6 * n;
-  double* d = dst.f[c] + row * n;
-  const long long o = c * g.fs + row * g.P;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    if constexpr (sizeof(T) == 8) d[i] = hi[o + i];
-    else d[i] = (double)hi[o + i] + (double)lo[o + i];
-  }
+__global__ void pack_kernel(FieldGeom g, unsigned total, const T* hi, const float* lo,
+                            PackedFields dst) {
+  const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  unsigned c, r;
+  long long o;
+  packed_index(g, k, c, r, o);
+  double x;
+  if constexpr (sizeof(T) == 8) x = hi[o];
+  else x = (double)hi[o] + (double)lo[o];
+  field_of(dst, c)[r] = x;
 }
 
 }  // namespace
@@ -537,19 +549,19 @@ cudaError_t launch_join_f32pair(long long count, const float* hi, const float* l
 
 cudaError_t launch_unpack_state(const FieldGeom& g, int nf, const PackedFields& src, void* hi,
                                 float* lo, cudaStream_t st) {
-  if (nf < 1 || nf > 3) return cudaErrorInvalidValue;
-  const unsigned blocks = (unsigned)(nf * 6LL * g.n);
-  if (lo) unpack_kernel<float><<<blocks, 128, 0, st>>>(g, src, (float*)hi, lo);
-  else unpack_kernel<double><<<blocks, 128, 0, st>>>(g, src, (double*)hi, nullptr);
+  if (nf < 1 || nf > 3 || g.n > 8191) return cudaErrorInvalidValue;
+  const unsigned total = (unsigned)(nf * 6LL * g.n * g.n);
+  if (lo) unpack_kernel<float><<<nblk(total), TPB, 0, st>>>(g, total, src, (float*)hi, lo);
+  else unpack_kernel<double><<<nblk(total), TPB, 0, st>>>(g, total, src, (double*)hi, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pack_state(const FieldGeom& g, int nf, const void* hi, const float* lo,
                               const PackedFields& dst, cudaStream_t st) {
-  if (nf < 1 || nf > 3) return cudaErrorInvalidValue;
-  const unsigned blocks = (unsigned)(nf * 6LL * g.n);
-  if (lo) pack_kernel<float><<<blocks, 128, 0, st>>>(g, (const float*)hi, lo, dst);
-  else pack_kernel<double><<<blocks, 128, 0, st>>>(g, (const double*)hi, nullptr, dst);
+  if (nf < 1 || nf > 3 || g.n > 8191) return cudaErrorInvalidValue;
+  const unsigned total = (unsigned)(nf * 6LL * g.n * g.n);
+  if (lo) pack_kernel<float><<<nblk(total), TPB, 0, st>>>(g, total, (const float*)hi, lo, dst);
+  else pack_kernel<double><<<nblk(total), TPB, 0, st>>>(g, total, (const double*)hi, nullptr, dst);
   return cudaGetLastError();
 }
 
