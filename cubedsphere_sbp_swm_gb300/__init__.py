@@ -25,7 +25,8 @@ from . import _abi
 from ._abi import SWM_FP32_FUSED, SWM_FP64_PLAIN, SwmError
 
 __all__ = [
-    "ModelConfig", "OperatorSWM", "StvecSWM", "GridField", "RK4", "HaloAhScalarSync",
+    "ModelConfig", "OperatorSWM", "StvecSWM", "GridField", "RK4", "OperatorSWMDiff",
+    "ExplicitEul1", "HaloAhScalarSync",
     "EcsAhVecSyncCovariant", "create_timescheme", "create_halo_procedure",
     "create_vector_halo_procedure", "Ensemble", "SwmError", "EARTH",
 ]
@@ -154,6 +155,16 @@ class OperatorSWM:
 
     def apply_unfused(self, vout: "StvecSWM", vin: "StvecSWM"):
         self._check(self._L.swm_apply_unfused(self._h, vout._h, vin._h))
+
+    def laplace(self, out: "GridField", f: "GridField", narrow_order: int = 42):
+        """out = L(f): the narrow-stencil SBP Laplacian laplace_ah_sbp42_narrow /
+        laplace_ah_sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58), edge-synced."""
+        self._check(self._L.swm_laplace(self._h, out._h, f._h, int(narrow_order)))
+
+    def model_step(self, v0: "StvecSWM", dt: float, nsteps: int = 1):
+        """nsteps of the drivers' time step (ts2_mod.f90:143-146): RK4, then the
+        diffusion step when an OperatorSWMDiff is attached to this operator."""
+        self._check(self._L.swm_model_step(self._h, v0._h, float(dt), int(nsteps)))
 
     def get_diagnostics(self, v: "StvecSWM") -> dict:
         out = np.zeros(7)
@@ -313,6 +324,35 @@ class RK4:
         operator._check(operator._L.swm_rk4_step(operator._h, v0._h, float(dt), int(nsteps)))
 
 
+class OperatorSWMDiff:
+    """operator_swm_diff_t (models/shallow_water/operator/operator_swm_diff_mod.f90
+    :25-46), created like create_swm_diff_operator
+    (operator_swm_diff_factory_mod.f90:27-30) from the namelist's
+    hordiff_uv_name / uv_diff_coeff / hordiff_h_name / h_diff_coeff.  It lives
+    on the model operator's context (its grid, stream and work fields)."""
+
+    def __init__(self, op: OperatorSWM, hordiff_uv_name: str = "hordiff_vec_xyz_Ah_sbp_42_narrow",
+                 uv_diff_coeff: float = 0.03,
+                 hordiff_h_name: str = "hordiff_scalar_Ah_sbp_42_narrow",
+                 h_diff_coeff: float = 0.01):
+        self.op = op
+        op._check(op._L.swm_diffusion_set(op._h, hordiff_uv_name.encode(), float(uv_diff_coeff),
+                                          hordiff_h_name.encode(), float(h_diff_coeff)))
+
+    def apply(self, vout: StvecSWM, vin: StvecSWM):
+        """vout = D(vin)."""
+        self.op._check(self.op._L.swm_apply_diffusion(self.op._h, vout._h, vin._h))
+
+
+class ExplicitEul1:
+    """explicit_Eul1_t (time_schemes/explicit_Eul1_mod.f90:20-30) for the
+    diffusion operator: v0 += dt * D(v0), replayed as a CUDA graph."""
+
+    def step(self, v0: StvecSWM, operator: OperatorSWMDiff, dt: float, nsteps: int = 1):
+        op = operator.op
+        op._check(op._L.swm_diffusion_step(op._h, v0._h, float(dt), int(nsteps)))
+
+
 class HaloAhScalarSync:
     """halo_t "Ah_scalar_sync" (halo/halo_Ah_scalar_sync_mod.f90)."""
 
@@ -425,11 +465,14 @@ class Ensemble:
         return {"seg_rows": a.value, "grid": b.value, "ms_per_step": ms.value}
 
 
-def create_timescheme(name: str) -> RK4:
-    """timescheme factory (time_schemes/timescheme_factory_mod.f90:13-59);
-    the GPU hot path provides "rk4"."""
+def create_timescheme(name: str):
+    """timescheme factory (time_schemes/timescheme_factory_mod.f90:13-59):
+    "rk4" for the model operator, "explicit_Eul1" for the diffusion
+    operator (the drivers' diff_time_scheme)."""
     if name == "rk4":
         return RK4()
+    if name == "explicit_Eul1":
+        return ExplicitEul1()
     raise SwmError(_abi.SWM_E_UNSUPPORTED, f"unsupported time scheme: {name}")
 
 

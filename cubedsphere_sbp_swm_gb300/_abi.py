@@ -42,6 +42,8 @@ EXPORTS = (
     "swm_apply_tl", "swm_apply_ad", "swm_rk4_tl", "swm_rk4_ad", "swm_adjoint_create",
     "swm_adjoint_destroy", "swm_adjoint_forward", "swm_adjoint_backward", "swm_adjoint_counts",
     "swm_state_upload_device", "swm_state_download_device", "swm_quadrature_weights",
+    "swm_diffusion_set", "swm_apply_diffusion", "swm_diffusion_step", "swm_model_step",
+    "swm_laplace",
 )
 
 
@@ -115,6 +117,11 @@ def load(build_if_missing: bool = True):
     sig("swm_apply", I, VP, VP, VP)
     sig("swm_apply_unfused", I, VP, VP, VP)
     sig("swm_rk4_step", I, VP, VP, D, I)
+    sig("swm_diffusion_set", I, VP, C, D, C, D)
+    sig("swm_apply_diffusion", I, VP, VP, VP)
+    sig("swm_diffusion_step", I, VP, VP, D, I)
+    sig("swm_model_step", I, VP, VP, D, I)
+    sig("swm_laplace", I, VP, VP, VP, I)
     sig("swm_diagnostics", I, VP, VP, _D)
     sig("swm_field_create", I, VP, PP)
     sig("swm_field_free", None, VP)

@@ -12,6 +12,7 @@
 #include <map>
 #include <mutex>
 #include <set>
+#include <tuple>
 #include <string>
 #include <utility>
 #include <vector>
@@ -182,7 +183,9 @@ struct swm_ctx {
   int* derr = nullptr;          // device error flag of the bounded waits
   int num_sms = 0;
   StageShape shape{};           // launch shape of the fused stage kernel
-  std::map<std::pair<void*, double>, GraphEntry> graphs;
+  // CUDA graphs of whole steps, keyed by (state, dt, kind): kind 0 RK4 step,
+  // 1 RK4 step + diffusion step, 2 diffusion step
+  std::map<std::tuple<void*, double, int>, GraphEntry> graphs;
   long graph_clock = 0;
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_stage, ev_edge;
@@ -196,6 +199,15 @@ struct swm_ctx {
   void* adw = nullptr;      // elements of the context precision
   void* adC = nullptr;
   SbpT sbpT{};
+  // hyperdiffusion split step (swm_diffusion_set): narrow Laplacian orders
+  // of the (u, v) and h operators (0: not configured), coefficients, the
+  // coefficient tables per order ([0] 4/2, [1] 6/3), the Cartesian basis
+  // vectors (6 fields) and 19 FP64 work fields, all allocated on first use
+  int diff_uv = 0, diff_h = 0;
+  double diff_uv_coeff = 0.0, diff_h_coeff = 0.0;
+  NarrowTables ntab[2] = {};
+  double* b12 = nullptr;
+  double* dw = nullptr;
   cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
   const void* ad_key[2] = {nullptr, nullptr};
   double ad_dt = 0.0;
@@ -599,6 +611,10 @@ void free_ctx(swm_ctx* c) {
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
                   c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
+  for (NarrowTables& t : c->ntab)
+    for (double* p : {t.cx, t.cy, t.clx, t.cly}) if (p) cudaFree(p);
+  if (c->b12) cudaFree(c->b12);
+  if (c->dw) cudaFree(c->dw);
   if (c->hres) cudaFreeHost(c->hres);
   if (c->herr) cudaFreeHost(c->herr);
   if (c->st) cudaStreamDestroy(c->st);
@@ -870,7 +886,7 @@ void swm_state_free(swm_state* s) {
     cudaSetDevice(c->cfg.device);
     cudaStreamSynchronize(c->st);
     for (auto it = c->graphs.begin(); it != c->graphs.end();) {
-      if (it->first.first == (void*)s) { cudaGraphExecDestroy(it->second.exec); it = c->graphs.erase(it); }
+      if (std::get<0>(it->first) == (void*)s) { cudaGraphExecDestroy(it->second.exec); it = c->graphs.erase(it); }
       else ++it;
     }
     if (s->hi) cudaFree(s->hi);
@@ -1033,19 +1049,16 @@ int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   return SWM_OK;
 }
 
-int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
-  if (int rc = check_state(ctx, v0)) return rc;
-  if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
-  if (nsteps == 0) return SWM_OK;
-  cudaSetDevice(ctx->cfg.device);
-  if (ctx->timing) {
-    for (int k = 0; k < nsteps; ++k) {
-      int rc = ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);
-      if (rc) return rc;
-    }
-    return SWM_OK;
-  }
-  const auto key = std::make_pair((void*)v0, dt);
+}  // extern "C"
+
+namespace {
+
+// Run nsteps replays of the CUDA graph of `enqueue` for (state, dt, kind),
+// capturing it on first use (at most 8 graphs per context, least recently
+// used evicted).
+template <class F>
+int graph_steps(swm_ctx* ctx, swm_state* v0, double dt, int kind, int nsteps, F enqueue) {
+  const auto key = std::make_tuple((void*)v0, dt, kind);
   auto it = ctx->graphs.find(key);
   if (it == ctx->graphs.end()) {
     if (ctx->graphs.size() >= 8) {
@@ -1057,7 +1070,7 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
     }
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "begin capture");
-    int rc = ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);
+    int rc = enqueue();
     cudaError_t ec = cudaStreamEndCapture(ctx->st, &graph);
     if (rc) { if (ec == cudaSuccess) cudaGraphDestroy(graph); return rc; }
     CK(ec, "end capture");
@@ -1070,6 +1083,233 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
   it->second.use = ++ctx->graph_clock;
   for (int k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(it->second.exec, ctx->st), "graph launch");
   return SWM_OK;
+}
+
+int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
+  return ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);
+}
+
+// ------------------------------------------------------- hyperdiffusion
+// Names of operator_swm_diff's operators (hordiff_factory_mod.f90:27-40)
+// that this library provides: the narrow-Laplacian ones of the Ah grid.
+int hordiff_uv_order(const char* name) {
+  if (!name) return 0;
+  if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_42_narrow")) return 42;
+  if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_63_narrow")) return 63;
+  return 0;
+}
+int hordiff_h_order(const char* name) {
+  if (!name) return 0;
+  if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_42_narrow")) return 42;
+  if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_63_narrow")) return 63;
+  return 0;
+}
+
+constexpr int kDiffWork = 19;   // F 4, L 4, d1x 4, d1y 4, tendencies 3
+
+// Workspace, basis vectors and the coefficient tables of order `narrow`
+// (outside any capture: allocates on first use).
+int diffusion_ws(swm_ctx* ctx, int narrow) {
+  const FieldGeom& g = ctx->g64;
+  if (ctx->n < 2 * narrow_rows(narrow))
+    return fail(ctx, SWM_E_INVALID, "grid too small for the narrow Laplacian closures");
+  if (!ctx->dw) {
+    CK(cudaMalloc(&ctx->dw, sizeof(double) * kDiffWork * g.fs), "alloc");
+    CK(cudaMemsetAsync(ctx->dw, 0, sizeof(double) * kDiffWork * g.fs, ctx->st), "memset");
+  }
+  if (!ctx->b12) {
+    CK(cudaMalloc(&ctx->b12, sizeof(double) * 6 * g.fs), "alloc");
+    CK(cudaMemsetAsync(ctx->b12, 0, sizeof(double) * 6 * g.fs, ctx->st), "memset");
+    CK(launch_basis(g, ctx->hx, ctx->b12, ctx->st), "basis");
+  }
+  NarrowTables& t = ctx->ntab[narrow == 63 ? 1 : 0];
+  if (!t.cx) {
+    const size_t nw = (size_t)narrow_width(narrow) * g.fs;
+    const size_t ncl = (size_t)narrow_closure_count(narrow, ctx->n);
+    NarrowTables nt{narrow, nullptr, nullptr, nullptr, nullptr};
+    cudaError_t e = cudaMalloc(&nt.cx, sizeof(double) * nw);
+    if (e == cudaSuccess) e = cudaMalloc(&nt.cy, sizeof(double) * nw);
+    if (e == cudaSuccess) e = cudaMalloc(&nt.clx, sizeof(double) * ncl);
+    if (e == cudaSuccess) e = cudaMalloc(&nt.cly, sizeof(double) * ncl);
+    if (e == cudaSuccess) e = launch_narrow_tables(g, nt, ctx->m64, ctx->st);
+    if (e != cudaSuccess) {
+      for (double* p : {nt.cx, nt.cy, nt.clx, nt.cly}) if (p) cudaFree(p);
+      return fail(ctx, e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
+                  std::string("diffusion tables: ") + cudaGetErrorString(e));
+    }
+    t = nt;
+  }
+  return SWM_OK;
+}
+
+// Synced Laplacian of nf FP64 fields src -> dst (laplace_Ah_sbp42_narrow_mod
+// .f90:23-58); work fields d1x, d1y of the diffusion workspace.
+int laplace_fields(swm_ctx* ctx, int narrow, int nf, const double* src, double* dst) {
+  const FieldGeom& g = ctx->g64;
+  double* D1X = ctx->dw + 8 * g.fs;
+  double* D1Y = ctx->dw + 12 * g.fs;
+  CK(launch_laplace_presync(g, ctx->ntab[narrow == 63 ? 1 : 0], nf, src, g.fs, ctx->m64,
+                            ctx->hx * ctx->cfg.radius, D1X, D1Y, dst, ctx->st),
+     "laplace");
+  for (int c = 0; c < nf; ++c)
+    CK(launch_sync_scalar(g, ctx->topo, dst + c * g.fs, ctx->edge64, ctx->st), "laplace sync");
+  return SWM_OK;
+}
+
+// Diffusion tendencies of the FP64 fields (h, u, v) into (th, tu, tv)
+// (operator_swm_diff_mod.f90:25-46): the xyz-vector operator on (u, v)
+// (hordiff_colocated_mod.f90:41-58) and the scalar one on h
+// (hordiff_scalar_mod.f90:33-53), each -(c^4) L(L(.)) with
+// c = coeff*radius*hx (hordiff_factory_mod.f90:183).
+int enqueue_diffusion_tend(swm_ctx* ctx, const double* h, const double* u, const double* v,
+                           double* th, double* tu, double* tv) {
+  const FieldGeom& g = ctx->g64;
+  const long long fs = g.fs;
+  double* F = ctx->dw;
+  double* L = ctx->dw + 4 * fs;
+  CK(cudaMemcpyAsync(F, h, sizeof(double) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+  CK(launch_to_cart(g, ctx->b12, u, v, F + fs, ctx->st), "to cart");
+  if (ctx->diff_uv == ctx->diff_h) {
+    if (int rc = laplace_fields(ctx, ctx->diff_h, 4, F, L)) return rc;
+    if (int rc = laplace_fields(ctx, ctx->diff_h, 4, L, F)) return rc;
+  } else {
+    if (int rc = laplace_fields(ctx, ctx->diff_h, 1, F, L)) return rc;
+    if (int rc = laplace_fields(ctx, ctx->diff_h, 1, L, F)) return rc;
+    if (int rc = laplace_fields(ctx, ctx->diff_uv, 3, F + fs, L + fs)) return rc;
+    if (int rc = laplace_fields(ctx, ctx->diff_uv, 3, L + fs, F + fs)) return rc;
+  }
+  auto coeff4 = [&](double coeff) {
+    const double dc = coeff * ctx->cfg.radius * ctx->hx;
+    const double dc2 = dc * dc;
+    return -1.0 * (dc2 * dc2);
+  };
+  CK(launch_diff_tendency(g, ctx->b12, coeff4(ctx->diff_uv_coeff), F + fs, tu, tv,
+                          coeff4(ctx->diff_h_coeff), F, th, ctx->st),
+     "tendency");
+  CK(launch_sync_vector(g, ctx->topo, ctx->qw, tu, tv, ctx->edge64, ctx->st), "vector sync");
+  return SWM_OK;
+}
+
+// One explicit Euler step of the diffusion operator (explicit_Eul1_mod.f90:
+// 20-30): v0 = v0 + dt * D(v0).
+int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
+  const long long fs = ctx->g64.fs;
+  double* T = ctx->dw + 16 * fs;
+  const double *h, *u, *v;
+  if (int rc = state64(ctx, v0, &h, &u, &v)) return rc;
+  if (int rc = enqueue_diffusion_tend(ctx, h, u, v, T, T + fs, T + 2 * fs)) return rc;
+  if (ctx->prec == SWM_FP64_PLAIN) {
+    double* x = (double*)v0->hi;
+    CK(launch_axpby(3 * fs, 1.0, x, dt, T, x, ctx->st), "update");
+  } else {
+    CK(launch_pair_axpy(3 * fs, dt, T, (float*)v0->hi, v0->lo, ctx->st), "update");
+  }
+  return SWM_OK;
+}
+
+int diffusion_ready(swm_ctx* ctx) {
+  if (!ctx->diff_uv) return fail(ctx, SWM_E_INVALID, "diffusion is not configured (swm_diffusion_set)");
+  if (int rc = diffusion_ws(ctx, ctx->diff_uv)) return rc;
+  return diffusion_ws(ctx, ctx->diff_h);
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  if (int rc = check_state(ctx, v0)) return rc;
+  if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
+  if (nsteps == 0) return SWM_OK;
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->timing) {
+    for (int k = 0; k < nsteps; ++k)
+      if (int rc = enqueue_rk4_any(ctx, v0, dt)) return rc;
+    return SWM_OK;
+  }
+  return graph_steps(ctx, v0, dt, 0, nsteps, [&] { return enqueue_rk4_any(ctx, v0, dt); });
+}
+
+int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
+                      const char* hordiff_h_name, double h_diff_coeff) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  const int uv = hordiff_uv_order(hordiff_uv_name), h = hordiff_h_order(hordiff_h_name);
+  if (!uv || !h)
+    return fail(ctx, SWM_E_UNSUPPORTED,
+                std::string("unsupported hordiff operator: ") +
+                    (!uv ? (hordiff_uv_name ? hordiff_uv_name : "(null)")
+                         : (hordiff_h_name ? hordiff_h_name : "(null)")));
+  if (!std::isfinite(uv_diff_coeff) || !std::isfinite(h_diff_coeff))
+    return fail(ctx, SWM_E_INVALID, "bad diffusion coefficient");
+  cudaSetDevice(ctx->cfg.device);
+  const int old_uv = ctx->diff_uv, old_h = ctx->diff_h;
+  const double old_cu = ctx->diff_uv_coeff, old_ch = ctx->diff_h_coeff;
+  ctx->diff_uv = uv; ctx->diff_h = h;
+  ctx->diff_uv_coeff = uv_diff_coeff; ctx->diff_h_coeff = h_diff_coeff;
+  if (int rc = diffusion_ready(ctx)) {
+    ctx->diff_uv = old_uv; ctx->diff_h = old_h;
+    ctx->diff_uv_coeff = old_cu; ctx->diff_h_coeff = old_ch;
+    return rc;
+  }
+  // captured graphs hold the old coefficients
+  for (auto it = ctx->graphs.begin(); it != ctx->graphs.end();) {
+    if (std::get<2>(it->first) != 0) { cudaGraphExecDestroy(it->second.exec); it = ctx->graphs.erase(it); }
+    else ++it;
+  }
+  return SWM_OK;
+}
+
+int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  if (int rc = check_state(ctx, vout)) return rc;
+  if (int rc = check_state(ctx, vin)) return rc;
+  if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
+  cudaSetDevice(ctx->cfg.device);
+  if (int rc = diffusion_ready(ctx)) return rc;
+  const long long fs = ctx->g64.fs;
+  const double *h, *u, *v;
+  if (int rc = state64(ctx, vin, &h, &u, &v)) return rc;
+  if (ctx->prec == SWM_FP64_PLAIN) {
+    double* o = (double*)vout->hi;
+    return enqueue_diffusion_tend(ctx, h, u, v, o, o + fs, o + 2 * fs);
+  }
+  double* T = ctx->dw + 16 * fs;
+  if (int rc = enqueue_diffusion_tend(ctx, h, u, v, T, T + fs, T + 2 * fs)) return rc;
+  CK(launch_split_f64(3 * fs, T, (float*)vout->hi, vout->lo, ctx->st), "split");
+  return SWM_OK;
+}
+
+int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  if (int rc = check_state(ctx, v0)) return rc;
+  if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
+  cudaSetDevice(ctx->cfg.device);
+  if (int rc = diffusion_ready(ctx)) return rc;
+  if (nsteps == 0) return SWM_OK;
+  return graph_steps(ctx, v0, dt, 2, nsteps, [&] { return enqueue_diffusion_step(ctx, v0, dt); });
+}
+
+int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  if (int rc = check_state(ctx, v0)) return rc;
+  if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
+  cudaSetDevice(ctx->cfg.device);
+  if (!ctx->diff_uv) return swm_rk4_step(ctx, v0, dt, nsteps);
+  if (int rc = diffusion_ready(ctx)) return rc;
+  if (nsteps == 0) return SWM_OK;
+  return graph_steps(ctx, v0, dt, 1, nsteps, [&] {
+    if (int rc = enqueue_rk4_any(ctx, v0, dt)) return rc;
+    return enqueue_diffusion_step(ctx, v0, dt);
+  });
+}
+
+int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_order) {
+  if (int rc = check_field(ctx, out)) return rc;
+  if (int rc = check_field(ctx, in)) return rc;
+  if (narrow_order != 42 && narrow_order != 63)
+    return fail(ctx, SWM_E_UNSUPPORTED, "narrow Laplacian order must be 42 or 63");
+  cudaSetDevice(ctx->cfg.device);
+  if (int rc = diffusion_ws(ctx, narrow_order)) return rc;
+  double* F = ctx->dw;   // the input may be the output
+  CK(cudaMemcpyAsync(F, in->p, sizeof(double) * ctx->g64.fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+  return laplace_fields(ctx, narrow_order, 1, F, out->p);
 }
 
 int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {

@@ -94,6 +94,23 @@ __device__ void b2p(double a, double b, double v[3]) {
   v[2] = -tb * (ta * ta / (1.0 + tb * tb) + 1.0) / s;
 }
 
+// Cartesian contravariant basis vectors b1, b2 of every node, mapped from
+// the prototype face to panel p (mesh_factory_mod.f90:131-132 with
+// ecs_metric_mod.f90 calculate_b1/b2): 6 fields b1x b1y b1z b2x b2y b2z.
+__global__ void basis_kernel(FieldGeom g, double hx, double* b) {
+  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= 6LL * g.n * g.n) return;
+  const NodeIx k = node_of(g, gi);
+  const double al = -0.25 * kPi + k.i * hx, be = -0.25 * kPi + k.j * hx;
+  double v1[3], v2[3];
+  b1p(al, be, v1);
+  b2p(al, be, v2);
+  for (int c = 0; c < 3; ++c) {
+    b[c * g.fs + k.idx] = c_ex[k.p][c] * v1[0] + c_ey[k.p][c] * v1[1] - c_n[k.p][c] * v1[2];
+    b[(3 + c) * g.fs + k.idx] = c_ex[k.p][c] * v2[0] + c_ey[k.p][c] * v2[1] - c_n[k.p][c] * v2[2];
+  }
+}
+
 // Covariant-vector sync weights: dot products of the basis vectors of the
 // two panels across each edge (ecs_Ah_vec_sync_factory_mod.f90:97-144).
 __global__ void sync_weights_kernel(int n, double hx, double* qw) {
@@ -431,6 +448,11 @@ cudaError_t launch_geometry(const FieldGeom& g, int N, double radius, double ome
   geometry_kernel<<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, hx, radius, omega, axis[0] / an,
                                                           axis[1] / an, axis[2] / an, m64);
   sync_weights_kernel<<<nblk(g.n), TPB, 0, st>>>(g.n, hx, qw);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_basis(const FieldGeom& g, double hx, double* b, cudaStream_t st) {
+  basis_kernel<<<nblk(6LL * g.n * g.n), TPB, 0, st>>>(g, hx, b);
   return cudaGetLastError();
 }
 

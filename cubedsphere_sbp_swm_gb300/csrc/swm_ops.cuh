@@ -16,6 +16,8 @@ struct FieldGeom {
 // fields of fs doubles) and sync weights qb|qt|ql|qr into qw (4n doubles).
 cudaError_t launch_geometry(const FieldGeom& g, int N, double radius, double omega,
                             const double axis[3], double* m64, double* qw, cudaStream_t st);
+// Cartesian contravariant basis vectors: 6 fields b1x b1y b1z b2x b2y b2z
+cudaError_t launch_basis(const FieldGeom& g, double hx, double* b, cudaStream_t st);
 // FP64 -> FP32 copy of nfields fields
 cudaError_t launch_to_f32(const double* src, float* dst, long long count, cudaStream_t st);
 
@@ -134,5 +136,36 @@ cudaError_t launch_unpack_state(const FieldGeom& g, int nf, const PackedFields& 
                                 float* lo, cudaStream_t st);
 cudaError_t launch_pack_state(const FieldGeom& g, int nf, const void* hi, const float* lo,
                               const PackedFields& dst, cudaStream_t st);
+
+// Hyperdiffusion (swm_diffusion.cu): narrow-stencil SBP Laplacians of order
+// narrow = 42 or 63.  Per-context coefficient tables of one order: interior
+// stencil coefficients (narrow_width fields each for x and y, g64) and the
+// closure rows (narrow_closure_count values each for x and y).
+struct NarrowTables {
+  int narrow;
+  double *cx, *cy, *clx, *cly;
+};
+int narrow_rows(int narrow);
+int narrow_cols(int narrow);
+int narrow_width(int narrow);
+long long narrow_closure_count(int narrow, int n);
+cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables& t, const double* m,
+                                 cudaStream_t st);
+// pre-sync Laplacian of nf fields f (stride fstride) into out (stride g.fs);
+// d1x, d1y: nf work fields each; hs = hx * radius
+cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables& t, int nf,
+                                   const double* f, long long fstride, const double* m, double hs,
+                                   double* d1x, double* d1y, double* out, cudaStream_t st);
+// cart (3 fields) = b1*u + b2*v; b12 from launch_basis
+cudaError_t launch_to_cart(const FieldGeom& g, const double* b12, const double* u, const double* v,
+                           double* cart, cudaStream_t st);
+// tu, tv = projections of cuv*L (3 Cartesian fields) on b1, b2 (skipped when
+// tu is null); th = ch*Lh (skipped when th is null)
+cudaError_t launch_diff_tendency(const FieldGeom& g, const double* b12, double cuv, const double* L,
+                                 double* tu, double* tv, double ch, const double* Lh, double* th,
+                                 cudaStream_t st);
+// FP32 (hi, lo) += dt * t, over count elements
+cudaError_t launch_pair_axpy(long long count, double dt, const double* t, float* hi, float* lo,
+                             cudaStream_t st);
 
 }  // namespace swm

@@ -141,6 +141,41 @@ int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin);
  * with the stage combinations folded into the RHS kernels and the step
  * replayed as a CUDA graph. */
 int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
+
+/* ---------------------------------------------------------------------- */
+/* Hyperdiffusion split step                                              */
+/* ---------------------------------------------------------------------- */
+/* The reference drivers follow every RK4 step with one explicit Euler step
+ * of operator_swm_diff_t (operator_swm_diff_mod.f90:25-46; ts2_mod.f90:
+ * 143-146, barotropic_inst_mod.f90:163-168).  swm_diffusion_set takes the
+ * namelist's hordiff_uv_name / uv_diff_coeff / hordiff_h_name /
+ * h_diff_coeff (config_swm_mod.f90:24-27, operator_swm_diff_factory_mod.f90
+ * :27-30).  Supported names: "hordiff_vec_xyz_Ah_sbp_42_narrow" and
+ * "hordiff_vec_xyz_Ah_sbp_63_narrow" for (u, v); "hordiff_scalar_Ah_sbp_42_
+ * narrow" and "hordiff_scalar_Ah_sbp_63_narrow" for h
+ * (hordiff_factory_mod.f90:27-40); others give SWM_E_UNSUPPORTED.  The
+ * operator is -(c^4) L(L(.)) with L the narrow-stencil SBP Laplacian and
+ * c = coeff*radius*hx, on h and on the Cartesian components of the
+ * velocity.  Computed in FP64 in both precisions (FP32 contexts join the
+ * state, and update the (hi, lo) pair in FP64). */
+int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
+                      const char* hordiff_h_name, double h_diff_coeff);
+/* vout = D(vin): operator_swm_diff_t%apply (operator_swm_diff_mod.f90:
+ * 25-46). */
+int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin);
+/* nsteps of explicit_Eul1_t%step (explicit_Eul1_mod.f90:20-30) with the
+ * diffusion operator: v0 += dt * D(v0); one CUDA graph per step. */
+int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
+/* nsteps of the drivers' time step (ts2_mod.f90:143-146): rk4_t%step then
+ * the diffusion step, both as one CUDA graph per step; without
+ * swm_diffusion_set the same as swm_rk4_step. */
+int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
+/* out = L(in): laplace_operator_t%calc_laplace of laplace_ah_sbp42_narrow /
+ * laplace_ah_sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58,
+ * laplace_factory_mod.f90:179-250) on FP64 fields, edge-synced; out may be
+ * in.  narrow_order = 42 or 63. */
+int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_order);
+
 /* get_diagnostics (operator_swm_mod.f90:115-155): out[7] = hmin, hmax,
  * mass, TE, KE, PE, Enstrophy, all FP64 with SBP quadrature. */
 int swm_diagnostics(swm_ctx* ctx, const swm_state* v, double out[7]);

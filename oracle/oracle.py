@@ -29,7 +29,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB_PATH) or (
         os.path.getmtime(_LIB_PATH) < max(
             os.path.getmtime(os.path.join(_HERE, f))
-            for f in ("swm_oracle.cpp", "swm_oracle.h", "Makefile")
+            for f in ("swm_oracle.cpp", "swm_oracle.h", "Makefile",
+                      "../cubedsphere_sbp_swm_gb300/csrc/swm_narrow_tables.h")
         )
     ):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -76,6 +77,15 @@ def lib():
         L.orc_vector_test_field.restype = ctypes.c_int
         L.orc_scalar_test_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, _D]
         L.orc_scalar_test_field.restype = ctypes.c_int
+        for name, args in (("orc_laplace", [vp, ctypes.c_int, _D, _D]),
+                           ("orc_hordiff_scalar", [vp, ctypes.c_int, ctypes.c_double, _D, _D]),
+                           ("orc_hordiff_vec_xyz", [vp, ctypes.c_int, ctypes.c_double] + [_D] * 4),
+                           ("orc_diffusion_apply", [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                    ctypes.c_double] + [_D] * 6),
+                           ("orc_diffusion_step", [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                   ctypes.c_double, _D, _D, _D, ctypes.c_double])):
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -179,6 +189,38 @@ class OracleDomain:
         out = np.zeros(7)
         lib().orc_diagnostics(self._h, _p(hs), _p(h), _p(u), _p(v), _p(out))
         return out
+
+    # hyperdiffusion (narrow = 42 or 63: the narrow Laplacian's SBP order)
+    def laplace(self, f, narrow=42):
+        out = self.zeros()
+        assert lib().orc_laplace(self._h, int(narrow), _p(np.ascontiguousarray(f)), _p(out)) == 0
+        return out
+
+    def hordiff_scalar(self, f, coeff, narrow=42):
+        out = self.zeros()
+        assert lib().orc_hordiff_scalar(self._h, int(narrow), float(coeff),
+                                        _p(np.ascontiguousarray(f)), _p(out)) == 0
+        return out
+
+    def hordiff_vec_xyz(self, u, v, coeff, narrow=42):
+        ut, vt = self.zeros(), self.zeros()
+        assert lib().orc_hordiff_vec_xyz(self._h, int(narrow), float(coeff),
+                                         _p(np.ascontiguousarray(u)), _p(np.ascontiguousarray(v)),
+                                         _p(ut), _p(vt)) == 0
+        return ut, vt
+
+    def diffusion_apply(self, h, u, v, uv_coeff, h_coeff, uv_narrow=42, h_narrow=42):
+        th, tu, tv = self.zeros(), self.zeros(), self.zeros()
+        assert lib().orc_diffusion_apply(self._h, int(uv_narrow), float(uv_coeff), int(h_narrow),
+                                         float(h_coeff), *(_p(np.ascontiguousarray(a)) for a in (h, u, v)),
+                                         _p(th), _p(tu), _p(tv)) == 0
+        return th, tu, tv
+
+    def diffusion_step(self, h, u, v, dt, uv_coeff, h_coeff, uv_narrow=42, h_narrow=42):
+        h, u, v = (np.array(a, dtype=np.float64, order="C") for a in (h, u, v))
+        assert lib().orc_diffusion_step(self._h, int(uv_narrow), float(uv_coeff), int(h_narrow),
+                                        float(h_coeff), _p(h), _p(u), _p(v), float(dt)) == 0
+        return h, u, v
 
     VECTOR_FIELDS = {"solid_rotation": 0, "cross_polar": 1, "xyz_grad": 2, "vsh_curl_free_10": 3}
     SCALAR_FIELDS = {"xyz": 10, "cross_polar_div": 11, "cross_polar_zeta": 12}

@@ -11,6 +11,7 @@
 // floating-point reductions).
 
 #include "swm_oracle.h"
+#include "../cubedsphere_sbp_swm_gb300/csrc/swm_narrow_tables.h"
 
 #include <algorithm>
 #include <cmath>
@@ -692,6 +693,130 @@ void set_vector(const orc_domain& d, Gen gen, bool contravariant, std::vector<do
   }
 }
 
+// ---------------------------------------------------------------------------
+// Hyperdiffusion: the diffusion operator of the split step
+// (models/shallow_water/operator/operator_swm_diff_mod.f90:25-46).
+// ---------------------------------------------------------------------------
+using swm::NarrowD2;
+
+const NarrowD2& narrow_table(int order) { return order == 63 ? swm::kNarrow63 : swm::kNarrow42; }
+
+// Narrow variable-coefficient second derivative D2^(b) at node k of a line of
+// n values f with coefficients b (stride st): closure rows near either end
+// (laplace_Ah_sbp42_narrow_mod.f90:128-274, the right end 275-421 counts the
+// nodes from that end), interior stencil (lines 229-246; 6/3: the di_*
+// formulas, laplace_Ah_sbp63_narrow_mod.f90:861-881).
+double d2_point(const NarrowD2& T, const double* f, const double* b, int n, int st, int k) {
+  if (k < T.rows || k >= n - T.rows) {
+    const bool left = k < T.rows;
+    const int r = left ? k : n - 1 - k;
+    auto at = [&](const double* a, int m) { return a[(left ? m : n - 1 - m) * st]; };
+    double acc = 0.0;
+    for (int c = 0; c < T.cols; ++c) {
+      double m = 0.0;
+      for (int q = 0; q < T.nb; ++q) m += T.c[r][c][q] * at(b, q);
+      acc += m * at(f, c);
+    }
+    return T.rowscale[r] * acc;
+  }
+  const int w = 2 * T.hw + 1;
+  double acc = 0.0;
+  for (int o = 0; o < w; ++o) {
+    double cf = 0.0;
+    for (int q = 0; q < w; ++q) cf += T.in[o][q] * b[(k + q - T.hw) * st];
+    acc += cf * f[(k + o - T.hw) * st];
+  }
+  return acc;
+}
+
+// laplace_Ah_sbp{42,63}_narrow calc_laplace (laplace_Ah_sbp42_narrow_mod.f90:
+// 23-58): first derivatives times J*Qi12 (calc_tile_d1x_d1y, 60-93), the
+// narrow D2 along x with b = J*Qi11 and along y with b = J*Qi22, the
+// cross-derivative boundary fluxes on the x rows (717-743), the mixed terms
+// D_y(d1f_x) + D_x(d1f_y) (745-752), division by (hx*scale)^2 and by J, then
+// the Ah scalar sync.  The first derivatives use the SBP operator of the
+// same order (laplace_factory_mod.f90:179-214).
+void laplace_narrow(const orc_domain& d, int narrow, const double* f, double* out) {
+  const NarrowD2& T = narrow_table(narrow);
+  const Sbp s1 = make_sbp(narrow);
+  const int n = d.n, np = d.npts();
+  std::vector<double> bx(np), by(np), d1x(np), d1y(np);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int k = 0; k < np; ++k) {
+    bx[k] = d.Qi1[k] * d.J[k];
+    by[k] = d.Qi3[k] * d.J[k];
+  }
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int pj = 0; pj < 6 * n; ++pj) {
+    const int p = pj / n, j = pj % n;
+    const double* F = f + p * n * n;
+    for (int i = 0; i < n; ++i) {
+      const int id = p * n * n + j * n + i;
+      d1x[id] = sbp_point(s1, F + j * n, n, 1, i) * d.J[id] * d.Qi2[id];
+      d1y[id] = sbp_point(s1, F + i, n, n, j) * d.J[id] * d.Qi2[id];
+    }
+  }
+  const double hs = d.hx * d.scale;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int pj = 0; pj < 6 * n; ++pj) {
+    const int p = pj / n, j = pj % n;
+    const int o = p * n * n;
+    for (int i = 0; i < n; ++i) {
+      const int id = o + j * n + i;
+      double d2x = d2_point(T, f + o + j * n, &bx[o + j * n], n, 1, i);
+      const double d2y = d2_point(T, f + o + i, &by[o + i], n, n, j);
+      if (i == 0) d2x = d2x - 0.5 * (T.penalty * (-2.0 * d1y[id]));
+      if (i == n - 1) d2x = d2x - 0.5 * (T.penalty * (2.0 * d1y[id]));
+      if (j == 0) d2x = d2x - 0.5 * (T.penalty * (-2.0 * d1x[id]));
+      if (j == n - 1) d2x = d2x - 0.5 * (T.penalty * (2.0 * d1x[id]));
+      const double d2yx = sbp_point(s1, &d1x[o + i], n, n, j);
+      const double d2xy = sbp_point(s1, &d1y[o + j * n], n, 1, i);
+      double v = 1.0 * d2x + 1.0 * d2y;
+      v = v + 1.0 * d2xy + 1.0 * d2yx;
+      v = v / (hs * hs);
+      out[id] = v / d.J[id];
+    }
+  }
+  sync_scalar(d, out);
+}
+
+// hordiff_scalar_t%calc_diff with diff_order 2 (hordiff_scalar_mod.f90:33-53;
+// coefficient hordiff_coeff*scale*hx, hordiff_factory_mod.f90:157-188):
+// out = -(c^4) * lap(lap(f)).
+void hordiff_scalar(const orc_domain& d, int narrow, double coeff, const double* f, double* out) {
+  const int np = d.npts();
+  std::vector<double> t(np), t2(np);
+  laplace_narrow(d, narrow, f, t.data());
+  laplace_narrow(d, narrow, t.data(), t2.data());
+  const double dc = coeff * d.scale * d.hx;
+  const double dc2 = dc * dc;
+  const double c = -1.0 * (dc2 * dc2);
+  for (int k = 0; k < np; ++k) out[k] = c * t2[k];
+}
+
+// hordiff_colocated_xyz_t%calc_diff_vec (hordiff_colocated_mod.f90:41-58):
+// the Cartesian vector b1*u + b2*v (vec_math_mod.f90:107-126), the scalar
+// operator on each Cartesian component, the projections onto b1 and b2
+// (vec_math_mod.f90:128-160) and the covariant vector sync.
+void hordiff_vec_xyz(const orc_domain& d, int narrow, double coeff, const double* u,
+                     const double* v, double* ut, double* vt) {
+  const int np = d.npts();
+  std::vector<double> c[3], t[3];
+  for (int a = 0; a < 3; ++a) { c[a].assign(np, 0.0); t[a].assign(np, 0.0); }
+  for (int k = 0; k < np; ++k)
+    for (int a = 0; a < 3; ++a) c[a][k] = d.b1[3 * k + a] * u[k] + d.b2[3 * k + a] * v[k];
+  for (int a = 0; a < 3; ++a) hordiff_scalar(d, narrow, coeff, c[a].data(), t[a].data());
+  for (int k = 0; k < np; ++k) {
+    ut[k] = t[0][k] * d.b1[3 * k] + t[1][k] * d.b1[3 * k + 1] + t[2][k] * d.b1[3 * k + 2];
+    vt[k] = t[0][k] * d.b2[3 * k] + t[1][k] * d.b2[3 * k + 1] + t[2][k] * d.b2[3 * k + 2];
+  }
+  sync_vector_cov(d, ut, vt);
+}
+
+bool narrow_ok(const orc_domain& d, int narrow) {
+  return (narrow == 42 || narrow == 63) && d.n >= 2 * narrow_table(narrow).rows;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -781,6 +906,49 @@ void orc_diagnostics(const orc_domain* d, const double* hs, const double* h, con
   }
   out[0] = hmin; out[1] = hmax; out[2] = mass(*d, h);
   out[3] = ke + pen; out[4] = ke; out[5] = pen; out[6] = mass(*d, cu.data());
+}
+
+// Hyperdiffusion pieces (operator_swm_diff_mod.f90:25-46,
+// explicit_Eul1_mod.f90:20-30); narrow = 42 or 63 selects
+// laplace_ah_sbp42_narrow or laplace_ah_sbp63_narrow.  -1 on a bad order or
+// a grid too small for the closures.
+int orc_laplace(const orc_domain* d, int narrow, const double* f, double* out) {
+  if (!narrow_ok(*d, narrow)) return -1;
+  laplace_narrow(*d, narrow, f, out);
+  return 0;
+}
+int orc_hordiff_scalar(const orc_domain* d, int narrow, double coeff, const double* f, double* out) {
+  if (!narrow_ok(*d, narrow)) return -1;
+  hordiff_scalar(*d, narrow, coeff, f, out);
+  return 0;
+}
+int orc_hordiff_vec_xyz(const orc_domain* d, int narrow, double coeff, const double* u,
+                        const double* v, double* ut, double* vt) {
+  if (!narrow_ok(*d, narrow)) return -1;
+  hordiff_vec_xyz(*d, narrow, coeff, u, v, ut, vt);
+  return 0;
+}
+int orc_diffusion_apply(const orc_domain* d, int uv_narrow, double uv_coeff, int h_narrow,
+                        double h_coeff, const double* h, const double* u, const double* v,
+                        double* th, double* tu, double* tv) {
+  if (!narrow_ok(*d, uv_narrow) || !narrow_ok(*d, h_narrow)) return -1;
+  hordiff_vec_xyz(*d, uv_narrow, uv_coeff, u, v, tu, tv);
+  hordiff_scalar(*d, h_narrow, h_coeff, h, th);
+  return 0;
+}
+int orc_diffusion_step(const orc_domain* d, int uv_narrow, double uv_coeff, int h_narrow,
+                       double h_coeff, double* h, double* u, double* v, double dt) {
+  const int np = d->npts();
+  std::vector<double> th(np), tu(np), tv(np);
+  if (int rc = orc_diffusion_apply(d, uv_narrow, uv_coeff, h_narrow, h_coeff, h, u, v, th.data(),
+                                   tu.data(), tv.data()))
+    return rc;
+  for (int k = 0; k < np; ++k) {
+    h[k] = h[k] + dt * th[k];
+    u[k] = u[k] + dt * tu[k];
+    v[k] = v[k] + dt * tv[k];
+  }
+  return 0;
 }
 
 double orc_l2norm(const orc_domain* d, const double* f) { return std::sqrt(l2sq(*d, f)); }

@@ -74,6 +74,21 @@ void orc_rk4(const orc_domain* d, const double* hs, double* h, double* u,
 /* out[7] = hmin, hmax, mass, TE, KE, PE, Enstrophy (operator_swm_mod.f90:115-155) */
 void orc_diagnostics(const orc_domain* d, const double* hs, const double* h,
                      const double* u, const double* v, double out[7]);
+/* Hyperdiffusion (operator_swm_diff_mod.f90:25-46): narrow = 42 or 63 picks
+ * laplace_ah_sbp42_narrow / laplace_ah_sbp63_narrow; coefficients as the
+ * namelist's uv_diff_coeff / h_diff_coeff.  Return 0, or -1 for a bad order
+ * or a grid too small for the closures. */
+int orc_laplace(const orc_domain* d, int narrow, const double* f, double* out);
+int orc_hordiff_scalar(const orc_domain* d, int narrow, double coeff, const double* f,
+                       double* out);
+int orc_hordiff_vec_xyz(const orc_domain* d, int narrow, double coeff, const double* u,
+                        const double* v, double* ut, double* vt);
+int orc_diffusion_apply(const orc_domain* d, int uv_narrow, double uv_coeff, int h_narrow,
+                        double h_coeff, const double* h, const double* u, const double* v,
+                        double* th, double* tu, double* tv);
+/* explicit_Eul1 step (explicit_Eul1_mod.f90:20-30) of the diffusion operator */
+int orc_diffusion_step(const orc_domain* d, int uv_narrow, double uv_coeff, int h_narrow,
+                       double h_coeff, double* h, double* u, double* v, double dt);
 double orc_l2norm(const orc_domain* d, const double* f);   /* vec_math_mod.f90:50-90 */
 double orc_mass(const orc_domain* d, const double* f);     /* SBP quadrature */
 

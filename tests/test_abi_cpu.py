@@ -57,7 +57,8 @@ def test_bad_sizes_are_rejected():
 
 
 def test_unknown_time_scheme_and_halo():
+    assert isinstance(swm.create_timescheme("explicit_Eul1"), swm.ExplicitEul1)
     with pytest.raises(swm.SwmError):
-        swm.create_timescheme("explicit_Eul1")
+        swm.create_timescheme("ars343")
     with pytest.raises(swm.SwmError):
         swm.create_halo_procedure(None, "ECS_O")

@@ -1,0 +1,147 @@
+"""Hyperdiffusion split step on the GPU against the CPU oracle.
+
+The FP64 GPU path follows the oracle's arithmetic (same coefficient tables,
+same evaluation order up to the summation of the closure rows), so the bar is
+a J-weighted relative L2 difference <= 1e-12 per field for the narrow
+Laplacian, the diffusion operator (operator_swm_diff_mod.f90:25-46) and the
+drivers' time step of RK4 followed by one explicit Euler diffusion step
+(ts2_mod.f90:143-146).  The FP32 context runs the diffusion in FP64 on the
+joined state; its model steps stay within 1e-5 of the FP64 ones."""
+import numpy as np
+import pytest
+
+import cubedsphere_sbp_swm_gb300 as swm
+from cubedsphere_sbp_swm_gb300 import _abi, initial
+import oracle
+from gpu_helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+UV = {42: "hordiff_vec_xyz_Ah_sbp_42_narrow", 63: "hordiff_vec_xyz_Ah_sbp_63_narrow"}
+H = {42: "hordiff_scalar_Ah_sbp_42_narrow", 63: "hordiff_scalar_Ah_sbp_63_narrow"}
+
+
+def _state(N, seed=5):
+    h, u, v, _ = initial.balanced_zonal(N, 2, 16)
+    rng = np.random.default_rng(seed)
+    od = oracle.OracleDomain(N, 42)
+    h = od.sync_scalar(h + 20.0 * rng.standard_normal(h.shape))
+    u, v = od.sync_vector_cov(u + 2.0 * rng.standard_normal(u.shape),
+                              v + 2.0 * rng.standard_normal(v.shape))
+    return h, u, v
+
+
+@pytest.mark.parametrize("narrow,N", [(42, 32), (63, 32), (63, 48)])
+def test_laplace_matches_oracle(narrow, N):
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    od = oracle.OracleDomain(N, 42)
+    J = od.geometry()["J"]
+    rng = np.random.default_rng(narrow + N)
+    f = od.sync_scalar(_state(N)[0] + 5.0 * rng.standard_normal(op.shape))
+    fi, fo = op.create_field(), op.create_field()
+    fi.upload(f)
+    op.laplace(fo, fi, narrow)
+    ref = od.laplace(f, narrow)
+    assert rel_l2(fo.download(), ref, J) <= 1e-12
+    op.laplace(fi, fi, narrow)   # in place
+    assert rel_l2(fi.download(), ref, J) <= 1e-12
+
+
+@pytest.mark.parametrize("uv_narrow,h_narrow", [(42, 42), (63, 63), (63, 42)])
+def test_diffusion_operator_matches_oracle(uv_narrow, h_narrow):
+    N = 32
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    dop = swm.OperatorSWMDiff(op, UV[uv_narrow], 0.03, H[h_narrow], 0.01)
+    od = oracle.OracleDomain(N, 42)
+    J = od.geometry()["J"]
+    h, u, v = _state(N)
+    x, t = op.create_stvec(), op.create_stvec()
+    x.upload(h, u, v)
+    dop.apply(t, x)
+    ref = od.diffusion_apply(h, u, v, 0.03, 0.01, uv_narrow, h_narrow)
+    for a, b in zip(t.download(), ref):
+        assert rel_l2(a, b, J) <= 1e-12
+
+
+@pytest.mark.parametrize("order", [42, 63])
+def test_model_step_matches_oracle(order):
+    N, dt, steps = 32, 600.0, 3
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=order, precision="fp64"))
+    swm.OperatorSWMDiff(op, UV[order], 0.03, H[order], 0.01)
+    od = oracle.OracleDomain(N, order)
+    J = od.geometry()["J"]
+    h, u, v = _state(N)
+    x = op.create_stvec()
+    x.upload(h, u, v)
+    op.model_step(x, dt, steps)
+    for _ in range(steps):
+        h, u, v = od.rk4(h, u, v, dt)
+        h, u, v = od.diffusion_step(h, u, v, dt, 0.03, 0.01, order, order)
+    for a, b in zip(x.download(), (h, u, v)):
+        assert rel_l2(a, b, J) <= 1e-12
+
+
+def test_euler_scheme_and_model_step_agree():
+    """ExplicitEul1 after RK4 gives the model step's state bit for bit."""
+    N, dt = 32, 600.0
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    dop = swm.OperatorSWMDiff(op)
+    h, u, v = _state(N)
+    a, b = op.create_stvec(), op.create_stvec()
+    a.upload(h, u, v)
+    b.upload(h, u, v)
+    rk4, eul = swm.create_timescheme("rk4"), swm.create_timescheme("explicit_Eul1")
+    for _ in range(2):
+        rk4.step(a, op, dt)
+        eul.step(a, dop, dt)
+    op.model_step(b, dt, 2)
+    for x, y in zip(a.download(), b.download()):
+        assert np.array_equal(x, y)
+
+
+def test_fp32_model_step_tracks_fp64():
+    N, dt, steps = 48, 600.0, 10
+    res = {}
+    for prec in ("fp64", "fp32"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision=prec))
+        swm.OperatorSWMDiff(op)
+        x = op.create_stvec()
+        x.upload(*_state(N))
+        op.model_step(x, dt, steps)
+        res[prec] = x.download()
+    J = oracle.OracleDomain(N, 42).geometry()["J"]
+    for a, b in zip(res["fp32"], res["fp64"]):
+        assert rel_l2(a, b, J) <= 1e-5
+
+
+def test_diffusion_conserves_mass_at_scale():
+    N = 192
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    dop = swm.OperatorSWMDiff(op)
+    x, t = op.create_stvec(), op.create_stvec()
+    x.upload(*_state(N))
+    dop.apply(t, x)
+    th = t.download()[0]
+    w = np.zeros(op.shape)
+    op._check(op._L.swm_quadrature_weights(op._h, w.ctypes.data_as(_abi._D)))
+    assert abs(np.sum(w * th)) <= 1e-11 * np.sum(w * np.abs(th))
+    assert np.sum(w * th * x.download()[0]) < 0
+
+
+def test_errors():
+    op = swm.OperatorSWM(swm.ModelConfig(N=32, sbp_order=42, precision="fp64"))
+    x, t = op.create_stvec(), op.create_stvec()
+    with pytest.raises(swm.SwmError) as e:
+        op._check(op._L.swm_apply_diffusion(op._h, t._h, x._h))   # not configured
+    assert e.value.code == _abi.SWM_E_INVALID
+    with pytest.raises(swm.SwmError) as e:
+        swm.OperatorSWMDiff(op, "hordiff_c_biharm_div", 0.03, H[42], 0.01)
+    assert e.value.code == _abi.SWM_E_UNSUPPORTED
+    with pytest.raises(swm.SwmError) as e:
+        swm.create_timescheme("explicit_Eul2")
+    assert e.value.code == _abi.SWM_E_UNSUPPORTED
+    small = swm.OperatorSWM(swm.ModelConfig(N=16, sbp_order=42, precision="fp64"))
+    with pytest.raises(swm.SwmError) as e:   # 17 nodes < 2 x 9 closure rows
+        swm.OperatorSWMDiff(small, UV[63], 0.03, H[63], 0.01)
+    assert e.value.code == _abi.SWM_E_INVALID
+    swm.OperatorSWMDiff(small, UV[42], 0.03, H[42], 0.01)
