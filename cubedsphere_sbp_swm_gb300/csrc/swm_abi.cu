@@ -205,9 +205,9 @@ struct swm_ctx {
   // vectors (6 fields) and 19 FP64 work fields, all allocated on first use
   int diff_uv = 0, diff_h = 0;
   double diff_uv_coeff = 0.0, diff_h_coeff = 0.0;
-  NarrowTables ntab[2] = {};
-  double* b12 = nullptr;
-  double* dw = nullptr;
+  void* ntab[2][4] = {};    // cx, cy, clx, cly (context precision)
+  void* b12 = nullptr;
+  void* dw = nullptr;
   cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
   const void* ad_key[2] = {nullptr, nullptr};
   double ad_dt = 0.0;
@@ -464,6 +464,12 @@ int check_field(swm_ctx* ctx, const swm_field* f) {
 
 double* tmpf(swm_ctx* c, int k) { return c->tmp + (long long)k * c->g64.fs; }
 
+// metric fields of the context precision (NMETRIC fields)
+template <class T>
+const T* metric_of(swm_ctx* c) {
+  return c->prec == SWM_FP32_FUSED ? (const T*)(const void*)c->m32 : (const T*)(const void*)c->m64;
+}
+
 // FP64 view of a state: the state itself (FP64) or its joined copy in the
 // work fields 11..13 (FP32).
 int state64(swm_ctx* ctx, const swm_state* s, const double** h, const double** u, const double** v) {
@@ -611,8 +617,8 @@ void free_ctx(swm_ctx* c) {
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
                   c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
-  for (NarrowTables& t : c->ntab)
-    for (double* p : {t.cx, t.cy, t.clx, t.cly}) if (p) cudaFree(p);
+  for (auto& t : c->ntab)
+    for (void* p : t) if (p) cudaFree(p);
   if (c->b12) cudaFree(c->b12);
   if (c->dw) cudaFree(c->dw);
   if (c->hres) cudaFreeHost(c->hres);
@@ -1107,102 +1113,131 @@ int hordiff_h_order(const char* name) {
 
 constexpr int kDiffWork = 19;   // F 4, L 4, d1x 4, d1y 4, tendencies 3
 
-// Workspace, basis vectors and the coefficient tables of order `narrow`
-// (outside any capture: allocates on first use).
+template <class T>
+NarrowTables<T> narrow_tables(swm_ctx* ctx, int narrow) {
+  void* const* t = ctx->ntab[narrow == 63 ? 1 : 0];
+  return NarrowTables<T>{narrow, (T*)t[0], (T*)t[1], (T*)t[2], (T*)t[3]};
+}
+template <class T> T* dwork(swm_ctx* ctx, int field) { return (T*)ctx->dw + field * ctx->g64.fs; }
+
+// Workspace, basis vectors and the coefficient tables of order `narrow`, in
+// the context precision (outside any capture: allocates on first use).
 int diffusion_ws(swm_ctx* ctx, int narrow) {
   const FieldGeom& g = ctx->g64;
+  const size_t elt = (size_t)ctx->elt;
   if (ctx->n < 2 * narrow_rows(narrow))
     return fail(ctx, SWM_E_INVALID, "grid too small for the narrow Laplacian closures");
   if (!ctx->dw) {
-    CK(cudaMalloc(&ctx->dw, sizeof(double) * kDiffWork * g.fs), "alloc");
-    CK(cudaMemsetAsync(ctx->dw, 0, sizeof(double) * kDiffWork * g.fs, ctx->st), "memset");
+    CK(cudaMalloc(&ctx->dw, elt * kDiffWork * g.fs), "alloc");
+    CK(cudaMemsetAsync(ctx->dw, 0, elt * kDiffWork * g.fs, ctx->st), "memset");
   }
   if (!ctx->b12) {
-    CK(cudaMalloc(&ctx->b12, sizeof(double) * 6 * g.fs), "alloc");
-    CK(cudaMemsetAsync(ctx->b12, 0, sizeof(double) * 6 * g.fs, ctx->st), "memset");
-    CK(launch_basis(g, ctx->hx, ctx->b12, ctx->st), "basis");
+    CK(cudaMalloc(&ctx->b12, elt * 6 * g.fs), "alloc");
+    CK(cudaMemsetAsync(ctx->b12, 0, elt * 6 * g.fs, ctx->st), "memset");
+    if (ctx->prec == SWM_FP64_PLAIN) {
+      CK(launch_basis(g, ctx->hx, (double*)ctx->b12, ctx->st), "basis");
+    } else {
+      double* b64 = tmpf(ctx, 0);   // 6 FP64 work fields
+      CK(cudaMemsetAsync(b64, 0, sizeof(double) * 6 * g.fs, ctx->st), "memset");
+      CK(launch_basis(g, ctx->hx, b64, ctx->st), "basis");
+      CK(launch_f64_to_f32(6 * g.fs, b64, (float*)ctx->b12, ctx->st), "basis f32");
+    }
   }
-  NarrowTables& t = ctx->ntab[narrow == 63 ? 1 : 0];
-  if (!t.cx) {
+  void** t = ctx->ntab[narrow == 63 ? 1 : 0];
+  if (!t[0]) {
     const size_t nw = (size_t)narrow_width(narrow) * g.fs;
     const size_t ncl = (size_t)narrow_closure_count(narrow, ctx->n);
-    NarrowTables nt{narrow, nullptr, nullptr, nullptr, nullptr};
-    cudaError_t e = cudaMalloc(&nt.cx, sizeof(double) * nw);
-    if (e == cudaSuccess) e = cudaMalloc(&nt.cy, sizeof(double) * nw);
-    if (e == cudaSuccess) e = cudaMalloc(&nt.clx, sizeof(double) * ncl);
-    if (e == cudaSuccess) e = cudaMalloc(&nt.cly, sizeof(double) * ncl);
-    if (e == cudaSuccess) e = launch_narrow_tables(g, nt, ctx->m64, ctx->st);
+    void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaError_t e = cudaMalloc(&p[0], elt * nw);
+    if (e == cudaSuccess) e = cudaMalloc(&p[1], elt * nw);
+    if (e == cudaSuccess) e = cudaMalloc(&p[2], elt * ncl);
+    if (e == cudaSuccess) e = cudaMalloc(&p[3], elt * ncl);
+    if (e == cudaSuccess) {
+      if (ctx->prec == SWM_FP64_PLAIN)
+        e = launch_narrow_tables<double>(
+            g, NarrowTables<double>{narrow, (double*)p[0], (double*)p[1], (double*)p[2], (double*)p[3]},
+            ctx->m64, ctx->st);
+      else
+        e = launch_narrow_tables<float>(
+            g, NarrowTables<float>{narrow, (float*)p[0], (float*)p[1], (float*)p[2], (float*)p[3]},
+            ctx->m64, ctx->st);
+    }
     if (e != cudaSuccess) {
-      for (double* p : {nt.cx, nt.cy, nt.clx, nt.cly}) if (p) cudaFree(p);
+      for (void* q : p) if (q) cudaFree(q);
       return fail(ctx, e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
                   std::string("diffusion tables: ") + cudaGetErrorString(e));
     }
-    t = nt;
+    for (int k = 0; k < 4; ++k) t[k] = p[k];
   }
   return SWM_OK;
 }
 
-// Synced Laplacian of nf FP64 fields src -> dst (laplace_Ah_sbp42_narrow_mod
+// Synced Laplacian of nf fields src -> dst (laplace_Ah_sbp42_narrow_mod
 // .f90:23-58); work fields d1x, d1y of the diffusion workspace.
-int laplace_fields(swm_ctx* ctx, int narrow, int nf, const double* src, double* dst) {
+template <class T>
+int laplace_fields(swm_ctx* ctx, int narrow, int nf, const T* src, T* dst) {
   const FieldGeom& g = ctx->g64;
-  double* D1X = ctx->dw + 8 * g.fs;
-  double* D1Y = ctx->dw + 12 * g.fs;
-  CK(launch_laplace_presync(g, ctx->ntab[narrow == 63 ? 1 : 0], nf, src, g.fs, ctx->m64,
-                            ctx->hx * ctx->cfg.radius, D1X, D1Y, dst, ctx->st),
+  CK(launch_laplace_presync<T>(g, narrow_tables<T>(ctx, narrow), nf, src, metric_of<T>(ctx),
+                               ctx->hx * ctx->cfg.radius, dwork<T>(ctx, 8), dwork<T>(ctx, 12), dst,
+                               ctx->st),
      "laplace");
-  for (int c = 0; c < nf; ++c)
-    CK(launch_sync_scalar(g, ctx->topo, dst + c * g.fs, ctx->edge64, ctx->st), "laplace sync");
+  T* edge = sizeof(T) == 8 ? (T*)ctx->edge64 : (T*)ctx->edge;
+  CK(launch_sync_fields<T>(g, ctx->topo, nf, dst, edge, ctx->st), "laplace sync");
   return SWM_OK;
 }
 
-// Diffusion tendencies of the FP64 fields (h, u, v) into (th, tu, tv)
+// Diffusion tendencies of the fields (h, u, v) into (th, tu, tv)
 // (operator_swm_diff_mod.f90:25-46): the xyz-vector operator on (u, v)
 // (hordiff_colocated_mod.f90:41-58) and the scalar one on h
 // (hordiff_scalar_mod.f90:33-53), each -(c^4) L(L(.)) with
 // c = coeff*radius*hx (hordiff_factory_mod.f90:183).
-int enqueue_diffusion_tend(swm_ctx* ctx, const double* h, const double* u, const double* v,
-                           double* th, double* tu, double* tv) {
+template <class T>
+int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* th, T* tu, T* tv) {
   const FieldGeom& g = ctx->g64;
   const long long fs = g.fs;
-  double* F = ctx->dw;
-  double* L = ctx->dw + 4 * fs;
-  CK(cudaMemcpyAsync(F, h, sizeof(double) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
-  CK(launch_to_cart(g, ctx->b12, u, v, F + fs, ctx->st), "to cart");
+  T* F = dwork<T>(ctx, 0);
+  T* L = dwork<T>(ctx, 4);
+  CK(cudaMemcpyAsync(F, h, sizeof(T) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+  CK(launch_to_cart<T>(g, (const T*)ctx->b12, u, v, F + fs, ctx->st), "to cart");
   if (ctx->diff_uv == ctx->diff_h) {
-    if (int rc = laplace_fields(ctx, ctx->diff_h, 4, F, L)) return rc;
-    if (int rc = laplace_fields(ctx, ctx->diff_h, 4, L, F)) return rc;
+    if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 4, F, L)) return rc;
+    if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 4, L, F)) return rc;
   } else {
-    if (int rc = laplace_fields(ctx, ctx->diff_h, 1, F, L)) return rc;
-    if (int rc = laplace_fields(ctx, ctx->diff_h, 1, L, F)) return rc;
-    if (int rc = laplace_fields(ctx, ctx->diff_uv, 3, F + fs, L + fs)) return rc;
-    if (int rc = laplace_fields(ctx, ctx->diff_uv, 3, L + fs, F + fs)) return rc;
+    if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 1, F, L)) return rc;
+    if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 1, L, F)) return rc;
+    if (int rc = laplace_fields<T>(ctx, ctx->diff_uv, 3, F + fs, L + fs)) return rc;
+    if (int rc = laplace_fields<T>(ctx, ctx->diff_uv, 3, L + fs, F + fs)) return rc;
   }
   auto coeff4 = [&](double coeff) {
     const double dc = coeff * ctx->cfg.radius * ctx->hx;
     const double dc2 = dc * dc;
     return -1.0 * (dc2 * dc2);
   };
-  CK(launch_diff_tendency(g, ctx->b12, coeff4(ctx->diff_uv_coeff), F + fs, tu, tv,
-                          coeff4(ctx->diff_h_coeff), F, th, ctx->st),
+  CK(launch_diff_tendency<T>(g, (const T*)ctx->b12, coeff4(ctx->diff_uv_coeff), F + fs, tu, tv,
+                             coeff4(ctx->diff_h_coeff), F, th, ctx->st),
      "tendency");
-  CK(launch_sync_vector(g, ctx->topo, ctx->qw, tu, tv, ctx->edge64, ctx->st), "vector sync");
+  T* edge = sizeof(T) == 8 ? (T*)ctx->edge64 : (T*)ctx->edge;
+  CK(launch_sync_vector_t<T>(g, ctx->topo, ctx->qw, tu, tv, edge, ctx->st), "vector sync");
   return SWM_OK;
 }
 
 // One explicit Euler step of the diffusion operator (explicit_Eul1_mod.f90:
-// 20-30): v0 = v0 + dt * D(v0).
+// 20-30): v0 = v0 + dt * D(v0).  FP32 contexts take the tendency of the
+// high part in FP32 and update the (hi, lo) pair in FP64.
 int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
   const long long fs = ctx->g64.fs;
-  double* T = ctx->dw + 16 * fs;
-  const double *h, *u, *v;
-  if (int rc = state64(ctx, v0, &h, &u, &v)) return rc;
-  if (int rc = enqueue_diffusion_tend(ctx, h, u, v, T, T + fs, T + 2 * fs)) return rc;
   if (ctx->prec == SWM_FP64_PLAIN) {
     double* x = (double*)v0->hi;
+    double* T = dwork<double>(ctx, 16);
+    if (int rc = enqueue_diffusion_tend<double>(ctx, x, x + fs, x + 2 * fs, T, T + fs, T + 2 * fs))
+      return rc;
     CK(launch_axpby(3 * fs, 1.0, x, dt, T, x, ctx->st), "update");
   } else {
-    CK(launch_pair_axpy(3 * fs, dt, T, (float*)v0->hi, v0->lo, ctx->st), "update");
+    const float* x = (const float*)v0->hi;
+    float* T = dwork<float>(ctx, 16);
+    if (int rc = enqueue_diffusion_tend<float>(ctx, x, x + fs, x + 2 * fs, T, T + fs, T + 2 * fs))
+      return rc;
+    CK(launch_pair_axpy<float>(3 * fs, dt, T, (float*)v0->hi, v0->lo, ctx->st), "update");
   }
   return SWM_OK;
 }
@@ -1266,16 +1301,15 @@ int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   cudaSetDevice(ctx->cfg.device);
   if (int rc = diffusion_ready(ctx)) return rc;
   const long long fs = ctx->g64.fs;
-  const double *h, *u, *v;
-  if (int rc = state64(ctx, vin, &h, &u, &v)) return rc;
   if (ctx->prec == SWM_FP64_PLAIN) {
+    const double* x = (const double*)vin->hi;
     double* o = (double*)vout->hi;
-    return enqueue_diffusion_tend(ctx, h, u, v, o, o + fs, o + 2 * fs);
+    return enqueue_diffusion_tend<double>(ctx, x, x + fs, x + 2 * fs, o, o + fs, o + 2 * fs);
   }
-  double* T = ctx->dw + 16 * fs;
-  if (int rc = enqueue_diffusion_tend(ctx, h, u, v, T, T + fs, T + 2 * fs)) return rc;
-  CK(launch_split_f64(3 * fs, T, (float*)vout->hi, vout->lo, ctx->st), "split");
-  return SWM_OK;
+  const float* x = (const float*)vin->hi;
+  float* o = (float*)vout->hi;
+  CK(cudaMemsetAsync(vout->lo, 0, sizeof(float) * 3 * fs, ctx->st), "memset");
+  return enqueue_diffusion_tend<float>(ctx, x, x + fs, x + 2 * fs, o, o + fs, o + 2 * fs);
 }
 
 int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
@@ -1305,11 +1339,13 @@ int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_or
   if (int rc = check_field(ctx, in)) return rc;
   if (narrow_order != 42 && narrow_order != 63)
     return fail(ctx, SWM_E_UNSUPPORTED, "narrow Laplacian order must be 42 or 63");
+  if (ctx->prec != SWM_FP64_PLAIN)
+    return fail(ctx, SWM_E_UNSUPPORTED, "swm_laplace works on FP64 contexts");
   cudaSetDevice(ctx->cfg.device);
   if (int rc = diffusion_ws(ctx, narrow_order)) return rc;
-  double* F = ctx->dw;   // the input may be the output
+  double* F = dwork<double>(ctx, 0);   // the input may be the output
   CK(cudaMemcpyAsync(F, in->p, sizeof(double) * ctx->g64.fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
-  return laplace_fields(ctx, narrow_order, 1, F, out->p);
+  return laplace_fields<double>(ctx, narrow_order, 1, F, out->p);
 }
 
 int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
@@ -1866,10 +1902,6 @@ template <class T = double>
 T* adf(swm_ctx* c, int k) { return (T*)c->adw + (long long)k * c->fs; }           // work field
 template <class T = double>
 T* ads(swm_ctx* c, int s) { return adf<T>(c, kAdWork + 3 * s); }                   // work state
-template <class T>
-const T* metric_of(swm_ctx* c) {
-  return c->prec == SWM_FP32_FUSED ? (const T*)(const void*)c->m32 : (const T*)(const void*)c->m64;
-}
 
 SbpT make_sbpT(const SbpC& s) {
   SbpT t{};

@@ -1,4 +1,4 @@
-// swm_diffusion.cu -- the hyperdiffusion split step on the GPU (FP64).
+// swm_diffusion.cu -- the hyperdiffusion split step on the GPU.
 //
 // The reference's drivers follow every RK4 step with one explicit Euler step
 // of a diffusion operator (ts2_mod.f90:143-146,
@@ -9,10 +9,11 @@
 //
 // The narrow second-derivative operators have variable coefficients
 // b = J*Qi11 (x) and J*Qi22 (y), which depend on the grid only, so the
-// per-node stencil coefficients are built once per context: the interior
-// stencil (2*hw+1 coefficients per node and direction) as fields, the
-// closure rows (rows x cols per line end) as small tables.  A Laplacian is
-// then two passes over the fields it is applied to:
+// per-node stencil coefficients are built once per context (in FP64, stored
+// in the element type): the interior stencil (2*hw+1 coefficients per node
+// and direction) as fields, the closure rows (rows x cols per line end) as
+// small tables.  A Laplacian is then two passes over the fields it is
+// applied to:
 //   1. d1x = D1x(f)*J*Qi12, d1y = D1y(f)*J*Qi12 (SBP first derivative of the
 //      same order);
 //   2. the narrow D2 in x and y from the precomputed coefficients, the
@@ -21,8 +22,13 @@
 // followed by the Ah scalar edge sync.  Every pass handles nf fields per
 // node so the coefficient loads are shared by h and the three Cartesian
 // velocity components.
+//
+// Element type T: double for FP64 contexts; float for FP32 contexts (the
+// tendency is small next to the state, which stays a compensated pair
+// updated in FP64).  GB300's FP64 rate bounds the FP64 passes.
 #include "swm_narrow_tables.h"
 #include "swm_ops.cuh"
+#include "swm_stage.cuh"
 
 namespace swm {
 namespace {
@@ -40,50 +46,35 @@ struct NarrowShape {
   static constexpr int nb = NARROW == 63 ? kNarrow63.nb : kNarrow42.nb;
   static constexpr int hw = NARROW == 63 ? kNarrow63.hw : kNarrow42.hw;
   static constexpr int w = 2 * hw + 1;
-  static constexpr int sbp = NARROW == 63 ? 3 : 1;   // index of the D1 operator in c_sbp
 };
+
+// Node kernels run on a 2-D grid: blockIdx.y = panel row p*n + j, x over the
+// columns i (RTPB threads per block).
+constexpr int RTPB = 128;
+inline dim3 row_grid(const FieldGeom& g) { return dim3((g.n + RTPB - 1) / RTPB, 6 * g.n); }
 
 struct Node {
   int p, i, j;
   long long idx;   // pitched index
 };
-__device__ __forceinline__ Node node_at(const FieldGeom& g, long long gi) {
-  Node r;
-  const long long nn = (long long)g.n * g.n;
-  r.p = (int)(gi / nn);
-  const long long rem = gi - (long long)r.p * nn;
-  r.j = (int)(rem / g.n);
-  r.i = (int)(rem - (long long)r.j * g.n);
+// false for the padding threads past the last column
+__device__ __forceinline__ bool node_here(const FieldGeom& g, Node& r) {
+  r.i = blockIdx.x * RTPB + threadIdx.x;
+  const int row = blockIdx.y;
+  r.p = row / g.n;
+  r.j = row - r.p * g.n;
   r.idx = (long long)r.p * g.ps + (long long)r.j * g.P + r.i;
-  return r;
-}
-
-// SBP first derivative at k of a line read through fa (sbp_operator_mod.f90:
-// 152-228: left closure, interior, mirrored right closure).
-template <class FA>
-__device__ __forceinline__ double d1_line(int id, int k, int n, FA fa) {
-  const SbpC& s = c_sbp[id];
-  double acc = 0.0;
-  if (k < s.ne) {
-    for (int m = 0; m < s.last[k]; ++m) acc += s.Ql[k * MAXNW + m] * fa(m);
-  } else if (k >= n - s.ne) {
-    const int r = n - 1 - k;
-    for (int m = s.last[r] - 1; m >= 0; --m) acc += (-s.Ql[r * MAXNW + m]) * fa(n - 1 - m);
-  } else {
-    for (int t = 0; t < s.nin; ++t) acc += s.Qin[t] * fa(k + s.inshift + t);
-  }
-  return acc;
+  return r.i < g.n;
 }
 
 // Interior stencil coefficients of both directions (zero at closure nodes):
 // cx[o] multiplies f[i+o-hw] of the row, cy[o] f[j+o-hw] of the column.
-template <int NARROW>
-__global__ void narrow_coef_kernel(FieldGeom g, const double* m, double* cx, double* cy) {
+template <class T, int NARROW>
+__global__ void narrow_coef_kernel(FieldGeom g, const double* m, T* cx, T* cy) {
   using S = NarrowShape<NARROW>;
-  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6LL * g.n * g.n) return;
-  const Node k = node_at(g, gi);
-  const NarrowD2& T = c_narrow[S::ni];
+  Node k;
+  if (!node_here(g, k)) return;
+  const NarrowD2& D = c_narrow[S::ni];
   const long long pb = (long long)k.p * g.ps;
   const double* J = m + MJ * g.fs + pb;
   const double* Q1 = m + MQI1 * g.fs + pb;
@@ -96,23 +87,23 @@ __global__ void narrow_coef_kernel(FieldGeom g, const double* m, double* cx, dou
     if (inx)
       for (int q = 0; q < S::w; ++q) {
         const long long a = (long long)k.j * g.P + (k.i + q - S::hw);
-        ax += T.in[o][q] * (Q1[a] * J[a]);
+        ax += D.in[o][q] * (Q1[a] * J[a]);
       }
     if (iny)
       for (int q = 0; q < S::w; ++q) {
         const long long a = (long long)(k.j + q - S::hw) * g.P + k.i;
-        ay += T.in[o][q] * (Q3[a] * J[a]);
+        ay += D.in[o][q] * (Q3[a] * J[a]);
       }
-    cx[o * g.fs + k.idx] = ax;
-    cy[o * g.fs + k.idx] = ay;
+    cx[o * g.fs + k.idx] = T(ax);
+    cy[o * g.fs + k.idx] = T(ay);
   }
 }
 
 // Closure rows of both directions: entry ((((p*n + line)*2 + side)*rows + r)
 // *cols + c) holds M[r][c] = sum_q C[r][c][q] b_q for the line's end `side`
-// (nodes counted from that end).
-template <int NARROW>
-__global__ void narrow_closure_kernel(FieldGeom g, const double* m, double* clx, double* cly) {
+// (nodes counted from that end); the row scale is applied after the sum.
+template <class T, int NARROW>
+__global__ void narrow_closure_kernel(FieldGeom g, const double* m, T* clx, T* cly) {
   using S = NarrowShape<NARROW>;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long per = 6LL * g.n * 2 * S::rows * S::cols;
@@ -122,7 +113,7 @@ __global__ void narrow_closure_kernel(FieldGeom g, const double* m, double* clx,
   const int side = (int)((e / ((long long)S::cols * S::rows)) % 2);
   const long long pl = e / (2LL * S::cols * S::rows);
   const int p = (int)(pl / g.n), line = (int)(pl % g.n);
-  const NarrowD2& T = c_narrow[S::ni];
+  const NarrowD2& D = c_narrow[S::ni];
   const long long pb = (long long)p * g.ps;
   const double* J = m + MJ * g.fs + pb;
   const double* Q1 = m + MQI1 * g.fs + pb;
@@ -132,147 +123,196 @@ __global__ void narrow_closure_kernel(FieldGeom g, const double* m, double* clx,
     const int node = side ? g.n - 1 - q : q;
     const long long ax = (long long)line * g.P + node;    // x: along the row `line`
     const long long ay = (long long)node * g.P + line;    // y: along the column `line`
-    mx += T.c[r][c][q] * (Q1[ax] * J[ax]);
-    my += T.c[r][c][q] * (Q3[ay] * J[ay]);
+    mx += D.c[r][c][q] * (Q1[ax] * J[ax]);
+    my += D.c[r][c][q] * (Q3[ay] * J[ay]);
   }
-  clx[e] = mx;
-  cly[e] = my;
+  clx[e] = T(mx);
+  cly[e] = T(my);
 }
 
-// Pass 1: d1x = D1x(f)*J*Qi12, d1y = D1y(f)*J*Qi12 of nf fields
+// Pass 1: d1x = D1x(f)*J*Qi12, d1y = D1y(f)*J*Qi12 of NF fields
 // (laplace_Ah_sbp42_narrow_mod.f90:60-93).
-template <int NARROW>
-__global__ void lap_d1_kernel(FieldGeom g, int nf, const double* f, long long fstride,
-                              const double* m, double* d1x, double* d1y) {
-  using S = NarrowShape<NARROW>;
-  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6LL * g.n * g.n) return;
-  const Node k = node_at(g, gi);
-  const double J = m[MJ * g.fs + k.idx], Q2 = m[MQI2 * g.fs + k.idx];
-  for (int c = 0; c < nf; ++c) {
-    const double* F = f + c * fstride + (long long)k.p * g.ps;
-    const double dx = d1_line(S::sbp, k.i, g.n, [&](int q) { return F[(long long)k.j * g.P + q]; });
-    const double dy = d1_line(S::sbp, k.j, g.n, [&](int q) { return F[(long long)q * g.P + k.i]; });
-    d1x[c * g.fs + k.idx] = dx * J * Q2;
-    d1y[c * g.fs + k.idx] = dy * J * Q2;
+template <class T, int NARROW, int NF>
+__global__ void __launch_bounds__(RTPB) lap_d1_kernel(FieldGeom g, const T* f, const T* mt,
+                                                      T* d1x, T* d1y) {
+  Node k;
+  if (!node_here(g, k)) return;
+  const int o = k.j * g.P + k.i;   // offset inside the panel
+  const long long pb = (long long)k.p * g.ps;
+  const T J = mt[MJ * g.fs + pb + o], Q2 = mt[MQI2 * g.fs + pb + o];
+#pragma unroll
+  for (int c = 0; c < NF; ++c) {
+    const T* F = f + c * g.fs + pb;
+    const T dx = d_line<NARROW, T>(k.i, g.n, [&](int q) { return F[k.j * g.P + q]; });
+    const T dy = d_line<NARROW, T>(k.j, g.n, [&](int q) { return F[q * g.P + k.i]; });
+    d1x[c * g.fs + pb + o] = dx * J * Q2;
+    d1y[c * g.fs + pb + o] = dy * J * Q2;
   }
 }
 
-// Pass 2: the pre-sync Laplacian of nf fields (laplace_Ah_sbp42_narrow_mod.f90
+// Pass 2: the pre-sync Laplacian of NF fields (laplace_Ah_sbp42_narrow_mod.f90
 // :94-763 with the division by J of lines 52-53).
-template <int NARROW>
-__global__ void lap_main_kernel(FieldGeom g, int nf, const double* f, long long fstride,
-                                const double* d1x, const double* d1y, const double* cx,
-                                const double* cy, const double* clx, const double* cly,
-                                const double* m, double hs, double* out) {
+template <class T, int NARROW, int NF>
+__global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f, const T* d1x,
+                                                        const T* d1y, const T* cx, const T* cy,
+                                                        const T* clx, const T* cly, const T* mt,
+                                                        double hs, T* out) {
   using S = NarrowShape<NARROW>;
-  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6LL * g.n * g.n) return;
-  const Node k = node_at(g, gi);
-  const NarrowD2& T = c_narrow[S::ni];
-  const int n = g.n;
+  Node k;
+  if (!node_here(g, k)) return;
+  const NarrowD2& D = c_narrow[S::ni];
+  const int n = g.n, P = g.P;
+  const int o = k.j * P + k.i;
+  const long long pb = (long long)k.p * g.ps;
   const bool clxn = k.i < S::rows || k.i >= n - S::rows;
   const bool clyn = k.j < S::rows || k.j >= n - S::rows;
-  // stencil of this node in x and y: coefficients, first tap, tap step
-  double ax[S::cols], ay[S::cols];
+  // stencil of this node in x and y: coefficients and tap offsets (inside
+  // the panel); the interior uses the first w taps
+  T ax[S::cols], ay[S::cols];
   int x0, xs, y0, ys;
-  double rsx = 1.0, rsy = 1.0;
+  T rsx = T(1), rsy = T(1);
   if (clxn) {
     const int side = k.i < S::rows ? 0 : 1, r = side ? n - 1 - k.i : k.i;
-    const double* M = clx + ((((long long)k.p * n + k.j) * 2 + side) * S::rows + r) * S::cols;
+    const T* M = clx + ((((long long)k.p * n + k.j) * 2 + side) * S::rows + r) * S::cols;
 #pragma unroll
     for (int c = 0; c < S::cols; ++c) ax[c] = M[c];
-    x0 = side ? n - 1 : 0; xs = side ? -1 : 1;
-    rsx = T.rowscale[r];
+    x0 = k.j * P + (side ? n - 1 : 0); xs = side ? -1 : 1;
+    rsx = T(D.rowscale[r]);
   } else {
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + k.idx] : 0.0;
-    x0 = k.i - S::hw; xs = 1;
+    for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
+    x0 = o - S::hw; xs = 1;
   }
   if (clyn) {
     const int side = k.j < S::rows ? 0 : 1, r = side ? n - 1 - k.j : k.j;
-    const double* M = cly + ((((long long)k.p * n + k.i) * 2 + side) * S::rows + r) * S::cols;
+    const T* M = cly + ((((long long)k.p * n + k.i) * 2 + side) * S::rows + r) * S::cols;
 #pragma unroll
     for (int c = 0; c < S::cols; ++c) ay[c] = M[c];
-    y0 = side ? n - 1 : 0; ys = side ? -1 : 1;
-    rsy = T.rowscale[r];
+    y0 = (side ? n - 1 : 0) * P + k.i; ys = side ? -P : P;
+    rsy = T(D.rowscale[r]);
   } else {
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + k.idx] : 0.0;
-    y0 = k.j - S::hw; ys = 1;
+    for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
+    y0 = o - S::hw * P; ys = P;
   }
   const int ntx = clxn ? S::cols : S::w, nty = clyn ? S::cols : S::w;
-  const double J = m[MJ * g.fs + k.idx];
-  const double hs2 = hs * hs;
-  const long long pb = (long long)k.p * g.ps;
-  for (int c = 0; c < nf; ++c) {
-    const double* F = f + c * fstride + pb;
-    double sx = 0.0, sy = 0.0;
+  const T J = mt[MJ * g.fs + pb + o];
+  const T hs2 = T(hs * hs);
+  const T pen = T(D.penalty);
+#pragma unroll
+  for (int c = 0; c < NF; ++c) {
+    const T* F = f + c * g.fs + pb;
+    T sx = T(0), sy = T(0);
 #pragma unroll
     for (int t = 0; t < S::cols; ++t)
-      if (t < ntx) sx += ax[t] * F[(long long)k.j * g.P + (x0 + xs * t)];
+      if (t < ntx) sx += ax[t] * F[x0 + xs * t];
 #pragma unroll
     for (int t = 0; t < S::cols; ++t)
-      if (t < nty) sy += ay[t] * F[(long long)(y0 + ys * t) * g.P + k.i];
-    double d2x = clxn ? rsx * sx : sx;
-    const double d2y = clyn ? rsy * sy : sy;
-    const double* DX = d1x + c * g.fs + pb;
-    const double* DY = d1y + c * g.fs + pb;
-    const long long o = (long long)k.j * g.P + k.i;
-    if (k.i == 0) d2x = d2x - 0.5 * (T.penalty * (-2.0 * DY[o]));
-    if (k.i == n - 1) d2x = d2x - 0.5 * (T.penalty * (2.0 * DY[o]));
-    if (k.j == 0) d2x = d2x - 0.5 * (T.penalty * (-2.0 * DX[o]));
-    if (k.j == n - 1) d2x = d2x - 0.5 * (T.penalty * (2.0 * DX[o]));
-    const double d2yx = d1_line(S::sbp, k.j, n, [&](int q) { return DX[(long long)q * g.P + k.i]; });
-    const double d2xy = d1_line(S::sbp, k.i, n, [&](int q) { return DY[(long long)k.j * g.P + q]; });
-    double v = 1.0 * d2x + 1.0 * d2y;
-    v = v + 1.0 * d2xy + 1.0 * d2yx;
+      if (t < nty) sy += ay[t] * F[y0 + ys * t];
+    T d2x = clxn ? rsx * sx : sx;
+    const T d2y = clyn ? rsy * sy : sy;
+    const T* DX = d1x + c * g.fs + pb;
+    const T* DY = d1y + c * g.fs + pb;
+    if (k.i == 0) d2x = d2x - T(0.5) * (pen * (T(-2) * DY[o]));
+    if (k.i == n - 1) d2x = d2x - T(0.5) * (pen * (T(2) * DY[o]));
+    if (k.j == 0) d2x = d2x - T(0.5) * (pen * (T(-2) * DX[o]));
+    if (k.j == n - 1) d2x = d2x - T(0.5) * (pen * (T(2) * DX[o]));
+    const T d2yx = d_line<NARROW, T>(k.j, n, [&](int q) { return DX[q * P + k.i]; });
+    const T d2xy = d_line<NARROW, T>(k.i, n, [&](int q) { return DY[k.j * P + q]; });
+    T v = d2x + d2y;
+    v = v + d2xy + d2yx;
     v = v / hs2;
-    out[c * g.fs + k.idx] = v / J;
+    out[c * g.fs + pb + o] = v / J;
   }
 }
 
 // Cartesian components of the covariant (u, v): b1*u + b2*v
 // (vec_math_mod.f90:107-126).
-__global__ void to_cart_kernel(FieldGeom g, const double* b, const double* u, const double* v,
-                               double* cart) {
-  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6LL * g.n * g.n) return;
-  const Node k = node_at(g, gi);
-  const double uu = u[k.idx], vv = v[k.idx];
+template <class T>
+__global__ void to_cart_kernel(FieldGeom g, const T* b, const T* u, const T* v, T* cart) {
+  Node k;
+  if (!node_here(g, k)) return;
+  const T uu = u[k.idx], vv = v[k.idx];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
     cart[a * g.fs + k.idx] = b[a * g.fs + k.idx] * uu + b[(3 + a) * g.fs + k.idx] * vv;
 }
 
 // Tendencies of (u, v): the projections of c*L (3 Cartesian fields) on b1
-// and b2 (vec_math_mod.f90:128-160); and, with th != nullptr, the depth
-// tendency ch*Lh.
-__global__ void from_cart_kernel(FieldGeom g, const double* b, double cuv, const double* L,
-                                 double* tu, double* tv, double ch, const double* Lh,
-                                 double* th) {
-  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6LL * g.n * g.n) return;
-  const Node k = node_at(g, gi);
-  if (tu) {
-    double t[3];
+// and b2 (vec_math_mod.f90:128-160); and the depth tendency ch*Lh.
+template <class T>
+__global__ void from_cart_kernel(FieldGeom g, const T* b, T cuv, const T* L, T* tu, T* tv, T ch,
+                                 const T* Lh, T* th) {
+  Node k;
+  if (!node_here(g, k)) return;
+  T t[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) t[a] = cuv * L[a * g.fs + k.idx];
-    tu[k.idx] = t[0] * b[k.idx] + t[1] * b[g.fs + k.idx] + t[2] * b[2 * g.fs + k.idx];
-    tv[k.idx] = t[0] * b[3 * g.fs + k.idx] + t[1] * b[4 * g.fs + k.idx] + t[2] * b[5 * g.fs + k.idx];
-  }
-  if (th) th[k.idx] = ch * Lh[k.idx];
+  for (int a = 0; a < 3; ++a) t[a] = cuv * L[a * g.fs + k.idx];
+  tu[k.idx] = t[0] * b[k.idx] + t[1] * b[g.fs + k.idx] + t[2] * b[2 * g.fs + k.idx];
+  tv[k.idx] = t[0] * b[3 * g.fs + k.idx] + t[1] * b[4 * g.fs + k.idx] + t[2] * b[5 * g.fs + k.idx];
+  th[k.idx] = ch * Lh[k.idx];
 }
 
-// FP32 (hi, lo) pair += dt * t (t FP64), summed in FP64 and split again.
-__global__ void pair_axpy_kernel(long long count, double dt, const double* t, float* hi,
-                                 float* lo) {
+// FP32 (hi, lo) pair += dt * t: the increment joins the low part, then a
+// two-sum renormalises the pair (the compensated update of the RK4 stage
+// epilogue); FP64 tendencies are added in FP64.
+template <class T>
+__global__ void pair_axpy_kernel(long long count, double dt, const T* t, float* hi, float* lo) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  const double y = ((double)hi[k] + (double)lo[k]) + dt * t[k];
-  const float h = (float)y;
-  hi[k] = h;
-  lo[k] = (float)(y - (double)h);
+  if constexpr (sizeof(T) == 4) {
+    const float d = float(dt) * t[k];
+    const float h = hi[k];
+    const float tt = lo[k] + d;
+    const float sm = h + tt;
+    const float bb = sm - h;
+    hi[k] = sm;
+    lo[k] = (h - (sm - bb)) + (tt - bb);
+  } else {
+    const double y = ((double)hi[k] + (double)lo[k]) + dt * (double)t[k];
+    const float h = (float)y;
+    hi[k] = h;
+    lo[k] = (float)(y - (double)h);
+  }
+}
+
+// Ah scalar sync of nf <= 4 fields at once (halo_Ah_scalar_sync_mod.f90:
+// 38-93): field c goes through value slot c of the edge buffer.
+template <class T>
+__global__ void gather_fields_kernel(FieldGeom g, int nf, const T* f, T* E) {
+  const int n = g.n, nb = 4 * n - 4;
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= 6 * nb) return;
+  const int p = gi / nb;
+  int i, j;
+  boundary_node(gi - p * nb, n, i, j);
+  const long long x = (long long)p * g.ps + (long long)j * g.P + i;
+  for (int c = 0; c < nf; ++c) {
+    const T a = f[c * g.fs + x];
+    auto put = [&](int side, int k) { E[((long long)(p * 4 + side) * 4 + c) * n + k] = a; };
+    if (i == 0) put(SIDE_L, j);
+    if (i == n - 1) put(SIDE_R, j);
+    if (j == 0) put(SIDE_B, i);
+    if (j == n - 1) put(SIDE_T, i);
+  }
+}
+
+template <class T>
+__global__ void sync_fields_kernel(FieldGeom g, Topology tp, int nf, const T* E, T* f) {
+  const int n = g.n, nb = 4 * n - 4;
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= 6 * nb) return;
+  const int p = gi / nb;
+  int i, j;
+  boundary_node(gi - p * nb, n, i, j);
+  const long long x = (long long)p * g.ps + (long long)j * g.P + i;
+  const EdgeView<T> ev{E, n};
+  for (int c = 0; c < nf; ++c) f[c * g.fs + x] = sync_scalar_node<T>(ev, tp, p, i, j, c, f[c * g.fs + x]);
+}
+
+__global__ void to_f32_kernel(long long count, const double* s, float* d) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < count) d[k] = (float)s[k];
 }
 
 }  // namespace
@@ -284,52 +324,97 @@ long long narrow_closure_count(int narrow, int n) {
   return 6LL * n * 2 * narrow_rows(narrow) * narrow_cols(narrow);
 }
 
-cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables& t, const double* m,
+template <class T>
+cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, const double* m,
                                  cudaStream_t st) {
-  const long long nodes = 6LL * g.n * g.n, ncl = narrow_closure_count(t.narrow, g.n);
+  const long long ncl = narrow_closure_count(t.narrow, g.n);
   if (t.narrow == 63) {
-    narrow_coef_kernel<63><<<dblk(nodes), DTPB, 0, st>>>(g, m, t.cx, t.cy);
-    narrow_closure_kernel<63><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
+    narrow_coef_kernel<T, 63><<<row_grid(g), RTPB, 0, st>>>(g, m, t.cx, t.cy);
+    narrow_closure_kernel<T, 63><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   } else {
-    narrow_coef_kernel<42><<<dblk(nodes), DTPB, 0, st>>>(g, m, t.cx, t.cy);
-    narrow_closure_kernel<42><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
+    narrow_coef_kernel<T, 42><<<row_grid(g), RTPB, 0, st>>>(g, m, t.cx, t.cy);
+    narrow_closure_kernel<T, 42><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables& t, int nf,
-                                   const double* f, long long fstride, const double* m, double hs,
-                                   double* d1x, double* d1y, double* out, cudaStream_t st) {
-  const long long nodes = 6LL * g.n * g.n;
+template <class T, int NARROW, int NF>
+void laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f, const T* mt, double hs,
+                T* d1x, T* d1y, T* out, cudaStream_t st) {
+  lap_d1_kernel<T, NARROW, NF><<<row_grid(g), RTPB, 0, st>>>(g, f, mt, d1x, d1y);
+  lap_main_kernel<T, NARROW, NF><<<row_grid(g), RTPB, 0, st>>>(g, f, d1x, d1y, t.cx, t.cy, t.clx,
+                                                               t.cly, mt, hs, out);
+}
+
+template <class T>
+cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables<T>& t, int nf,
+                                   const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out,
+                                   cudaStream_t st) {
+  if (nf != 1 && nf != 3 && nf != 4) return cudaErrorInvalidValue;
   if (t.narrow == 63) {
-    lap_d1_kernel<63><<<dblk(nodes), DTPB, 0, st>>>(g, nf, f, fstride, m, d1x, d1y);
-    lap_main_kernel<63><<<dblk(nodes), DTPB, 0, st>>>(g, nf, f, fstride, d1x, d1y, t.cx, t.cy,
-                                                      t.clx, t.cly, m, hs, out);
+    if (nf == 1) laplace_nf<T, 63, 1>(g, t, f, mt, hs, d1x, d1y, out, st);
+    else if (nf == 3) laplace_nf<T, 63, 3>(g, t, f, mt, hs, d1x, d1y, out, st);
+    else laplace_nf<T, 63, 4>(g, t, f, mt, hs, d1x, d1y, out, st);
   } else {
-    lap_d1_kernel<42><<<dblk(nodes), DTPB, 0, st>>>(g, nf, f, fstride, m, d1x, d1y);
-    lap_main_kernel<42><<<dblk(nodes), DTPB, 0, st>>>(g, nf, f, fstride, d1x, d1y, t.cx, t.cy,
-                                                      t.clx, t.cly, m, hs, out);
+    if (nf == 1) laplace_nf<T, 42, 1>(g, t, f, mt, hs, d1x, d1y, out, st);
+    else if (nf == 3) laplace_nf<T, 42, 3>(g, t, f, mt, hs, d1x, d1y, out, st);
+    else laplace_nf<T, 42, 4>(g, t, f, mt, hs, d1x, d1y, out, st);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_to_cart(const FieldGeom& g, const double* b12, const double* u, const double* v,
-                           double* cart, cudaStream_t st) {
-  to_cart_kernel<<<dblk(6LL * g.n * g.n), DTPB, 0, st>>>(g, b12, u, v, cart);
+template <class T>
+cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* u, const T* v, T* cart,
+                           cudaStream_t st) {
+  to_cart_kernel<T><<<row_grid(g), RTPB, 0, st>>>(g, b12, u, v, cart);
   return cudaGetLastError();
 }
 
-cudaError_t launch_diff_tendency(const FieldGeom& g, const double* b12, double cuv, const double* L,
-                                 double* tu, double* tv, double ch, const double* Lh, double* th,
-                                 cudaStream_t st) {
-  from_cart_kernel<<<dblk(6LL * g.n * g.n), DTPB, 0, st>>>(g, b12, cuv, L, tu, tv, ch, Lh, th);
+template <class T>
+cudaError_t launch_diff_tendency(const FieldGeom& g, const T* b12, double cuv, const T* L, T* tu,
+                                 T* tv, double ch, const T* Lh, T* th, cudaStream_t st) {
+  from_cart_kernel<T><<<row_grid(g), RTPB, 0, st>>>(g, b12, T(cuv), L, tu, tv, T(ch), Lh,
+                                                              th);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_axpy(long long count, double dt, const double* t, float* hi, float* lo,
+template <class T>
+cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, float* lo,
                              cudaStream_t st) {
-  pair_axpy_kernel<<<dblk(count), DTPB, 0, st>>>(count, dt, t, hi, lo);
+  pair_axpy_kernel<T><<<dblk(count), DTPB, 0, st>>>(count, dt, t, hi, lo);
   return cudaGetLastError();
 }
+
+template <class T>
+cudaError_t launch_sync_fields(const FieldGeom& g, const Topology& tp, int nf, T* f, T* edge,
+                               cudaStream_t st) {
+  if (nf < 1 || nf > 4) return cudaErrorInvalidValue;
+  const int nb = 6 * (4 * g.n - 4);
+  gather_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, nf, f, edge);
+  sync_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, tp, nf, edge, f);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaStream_t st) {
+  to_f32_kernel<<<dblk(count), DTPB, 0, st>>>(count, s, d);
+  return cudaGetLastError();
+}
+
+#define SWM_DIFF_INSTANTIATE(T)                                                                  \
+  template cudaError_t launch_narrow_tables<T>(const FieldGeom&, const NarrowTables<T>&,         \
+                                               const double*, cudaStream_t);                     \
+  template cudaError_t launch_laplace_presync<T>(const FieldGeom&, const NarrowTables<T>&, int,  \
+                                                 const T*, const T*, double, T*, T*, T*,         \
+                                                 cudaStream_t);                                  \
+  template cudaError_t launch_to_cart<T>(const FieldGeom&, const T*, const T*, const T*, T*,     \
+                                         cudaStream_t);                                          \
+  template cudaError_t launch_diff_tendency<T>(const FieldGeom&, const T*, double, const T*, T*, \
+                                               T*, double, const T*, T*, cudaStream_t);          \
+  template cudaError_t launch_pair_axpy<T>(long long, double, const T*, float*, float*,          \
+                                           cudaStream_t);                                        \
+  template cudaError_t launch_sync_fields<T>(const FieldGeom&, const Topology&, int, T*, T*,      \
+                                             cudaStream_t);
+SWM_DIFF_INSTANTIATE(float)
+SWM_DIFF_INSTANTIATE(double)
 
 }  // namespace swm

@@ -242,8 +242,8 @@ __global__ void axpby_kernel(long long count, double s1, const double* a, double
 }
 
 // gather boundary values of up to two fields into edge slots v0 (and v1)
-__global__ void gather_edge_kernel(FieldGeom g, const double* f0, int v0, const double* f1,
-                                   int v1, double* E) {
+template <class T>
+__global__ void gather_edge_kernel(FieldGeom g, const T* f0, int v0, const T* f1, int v1, T* E) {
   const int n = g.n, nb = 4 * n - 4;
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= 6 * nb) return;
@@ -251,7 +251,7 @@ __global__ void gather_edge_kernel(FieldGeom g, const double* f0, int v0, const 
   int i, j;
   boundary_node(gi - p * nb, n, i, j);
   const long long x = (long long)p * g.ps + (long long)j * g.P + i;
-  const double a = f0[x], b = f1 ? f1[x] : 0.0;
+  const T a = f0[x], b = f1 ? f1[x] : T(0);
   auto put = [&](int side, int k) {
     E[((long long)(p * 4 + side) * 4 + v0) * n + k] = a;
     if (f1) E[((long long)(p * 4 + side) * 4 + v1) * n + k] = b;
@@ -262,7 +262,8 @@ __global__ void gather_edge_kernel(FieldGeom g, const double* f0, int v0, const 
   if (j == n - 1) put(SIDE_T, i);
 }
 
-__global__ void sync_scalar_kernel(FieldGeom g, Topology tp, const double* E, double* f) {
+template <class T>
+__global__ void sync_scalar_kernel(FieldGeom g, Topology tp, const T* E, T* f) {
   const int n = g.n, nb = 4 * n - 4;
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= 6 * nb) return;
@@ -270,12 +271,13 @@ __global__ void sync_scalar_kernel(FieldGeom g, Topology tp, const double* E, do
   int i, j;
   boundary_node(gi - p * nb, n, i, j);
   const long long x = (long long)p * g.ps + (long long)j * g.P + i;
-  const EdgeView<double> ev{E, n};
-  f[x] = sync_scalar_node<double>(ev, tp, p, i, j, EV_ZETA, f[x]);
+  const EdgeView<T> ev{E, n};
+  f[x] = sync_scalar_node<T>(ev, tp, p, i, j, EV_ZETA, f[x]);
 }
 
-__global__ void sync_vector_kernel(FieldGeom g, Topology tp, const double* qw, const double* E,
-                                   double* gx, double* gy) {
+template <class T>
+__global__ void sync_vector_kernel(FieldGeom g, Topology tp, const double* qw, const T* E, T* gx,
+                                   T* gy) {
   const int n = g.n, nb = 4 * n - 4;
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= 6 * nb) return;
@@ -283,9 +285,9 @@ __global__ void sync_vector_kernel(FieldGeom g, Topology tp, const double* qw, c
   int i, j;
   boundary_node(gi - p * nb, n, i, j);
   const long long x = (long long)p * g.ps + (long long)j * g.P + i;
-  const EdgeView<double> ev{E, n};
-  double a = gx[x], b = gy[x];
-  sync_vector_node<double>(ev, tp, qw, p, i, j, a, b);
+  const EdgeView<T> ev{E, n};
+  T a = gx[x], b = gy[x];
+  sync_vector_node<T>(ev, tp, qw, p, i, j, a, b);
   gx[x] = a;
   gy[x] = b;
 }
@@ -517,20 +519,39 @@ cudaError_t launch_axpby(long long count, double s1, const double* a, double s2,
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_sync_scalar_t(const FieldGeom& g, const Topology& tp, T* f, T* edge,
+                                 cudaStream_t st) {
+  const int nb = 6 * (4 * g.n - 4);
+  gather_edge_kernel<T><<<nblk(nb), TPB, 0, st>>>(g, f, EV_ZETA, nullptr, 0, edge);
+  sync_scalar_kernel<T><<<nblk(nb), TPB, 0, st>>>(g, tp, edge, f);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_sync_vector_t(const FieldGeom& g, const Topology& tp, const double* qw, T* gx,
+                                 T* gy, T* edge, cudaStream_t st) {
+  const int nb = 6 * (4 * g.n - 4);
+  gather_edge_kernel<T><<<nblk(nb), TPB, 0, st>>>(g, gx, EV_GX, gy, EV_GY, edge);
+  sync_vector_kernel<T><<<nblk(nb), TPB, 0, st>>>(g, tp, qw, edge, gx, gy);
+  return cudaGetLastError();
+}
+template cudaError_t launch_sync_scalar_t<float>(const FieldGeom&, const Topology&, float*, float*,
+                                                 cudaStream_t);
+template cudaError_t launch_sync_scalar_t<double>(const FieldGeom&, const Topology&, double*,
+                                                  double*, cudaStream_t);
+template cudaError_t launch_sync_vector_t<float>(const FieldGeom&, const Topology&, const double*,
+                                                 float*, float*, float*, cudaStream_t);
+template cudaError_t launch_sync_vector_t<double>(const FieldGeom&, const Topology&, const double*,
+                                                  double*, double*, double*, cudaStream_t);
+
 cudaError_t launch_sync_scalar(const FieldGeom& g, const Topology& tp, double* f, double* edge,
                                cudaStream_t st) {
-  const int nb = 6 * (4 * g.n - 4);
-  gather_edge_kernel<<<nblk(nb), TPB, 0, st>>>(g, f, EV_ZETA, nullptr, 0, edge);
-  sync_scalar_kernel<<<nblk(nb), TPB, 0, st>>>(g, tp, edge, f);
-  return cudaGetLastError();
+  return launch_sync_scalar_t<double>(g, tp, f, edge, st);
 }
 
 cudaError_t launch_sync_vector(const FieldGeom& g, const Topology& tp, const double* qw,
                                double* gx, double* gy, double* edge, cudaStream_t st) {
-  const int nb = 6 * (4 * g.n - 4);
-  gather_edge_kernel<<<nblk(nb), TPB, 0, st>>>(g, gx, EV_GX, gy, EV_GY, edge);
-  sync_vector_kernel<<<nblk(nb), TPB, 0, st>>>(g, tp, qw, edge, gx, gy);
-  return cudaGetLastError();
+  return launch_sync_vector_t<double>(g, tp, qw, gx, gy, edge, st);
 }
 
 cudaError_t launch_reduce(const FieldGeom& g, int kind, const double* a, const double* b,

@@ -53,6 +53,13 @@ cudaError_t launch_sync_scalar(const FieldGeom& g, const Topology& tp, double* f
                                cudaStream_t st);
 cudaError_t launch_sync_vector(const FieldGeom& g, const Topology& tp, const double* qw,
                                double* gx, double* gy, double* edge, cudaStream_t st);
+// the same syncs on fields of either precision (edge buffer of that precision)
+template <class T>
+cudaError_t launch_sync_scalar_t(const FieldGeom& g, const Topology& tp, T* f, T* edge,
+                                 cudaStream_t st);
+template <class T>
+cudaError_t launch_sync_vector_t(const FieldGeom& g, const Topology& tp, const double* qw, T* gx,
+                                 T* gy, T* edge, cudaStream_t st);
 
 // Transposed SBP first-derivative operator D^T: t[c*kr + r] = D[r][c] for
 // the columns c < ct next to the left end (rows r < kr); the right end is
@@ -138,34 +145,46 @@ cudaError_t launch_pack_state(const FieldGeom& g, int nf, const void* hi, const 
                               const PackedFields& dst, cudaStream_t st);
 
 // Hyperdiffusion (swm_diffusion.cu): narrow-stencil SBP Laplacians of order
-// narrow = 42 or 63.  Per-context coefficient tables of one order: interior
-// stencil coefficients (narrow_width fields each for x and y, g64) and the
-// closure rows (narrow_closure_count values each for x and y).
+// narrow = 42 or 63, on fields of element type T.  Per-context coefficient
+// tables of one order: interior stencil coefficients (narrow_width fields
+// each for x and y) and the closure rows (narrow_closure_count values each
+// for x and y), built in FP64.
+template <class T>
 struct NarrowTables {
   int narrow;
-  double *cx, *cy, *clx, *cly;
+  T *cx, *cy, *clx, *cly;
 };
 int narrow_rows(int narrow);
 int narrow_cols(int narrow);
 int narrow_width(int narrow);
 long long narrow_closure_count(int narrow, int n);
-cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables& t, const double* m,
+template <class T>
+cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, const double* m,
                                  cudaStream_t st);
-// pre-sync Laplacian of nf fields f (stride fstride) into out (stride g.fs);
-// d1x, d1y: nf work fields each; hs = hx * radius
-cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables& t, int nf,
-                                   const double* f, long long fstride, const double* m, double hs,
-                                   double* d1x, double* d1y, double* out, cudaStream_t st);
+// pre-sync Laplacian of nf = 1, 3 or 4 fields f into out (all at field
+// stride g.fs); mt: metric of element type T; d1x, d1y: nf work fields
+// each; hs = hx * radius
+template <class T>
+cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables<T>& t, int nf,
+                                   const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out,
+                                   cudaStream_t st);
 // cart (3 fields) = b1*u + b2*v; b12 from launch_basis
-cudaError_t launch_to_cart(const FieldGeom& g, const double* b12, const double* u, const double* v,
-                           double* cart, cudaStream_t st);
-// tu, tv = projections of cuv*L (3 Cartesian fields) on b1, b2 (skipped when
-// tu is null); th = ch*Lh (skipped when th is null)
-cudaError_t launch_diff_tendency(const FieldGeom& g, const double* b12, double cuv, const double* L,
-                                 double* tu, double* tv, double ch, const double* Lh, double* th,
-                                 cudaStream_t st);
+template <class T>
+cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* u, const T* v, T* cart,
+                           cudaStream_t st);
+// tu, tv = projections of cuv*L (3 Cartesian fields) on b1, b2; th = ch*Lh
+template <class T>
+cudaError_t launch_diff_tendency(const FieldGeom& g, const T* b12, double cuv, const T* L, T* tu,
+                                 T* tv, double ch, const T* Lh, T* th, cudaStream_t st);
 // FP32 (hi, lo) += dt * t, over count elements
-cudaError_t launch_pair_axpy(long long count, double dt, const double* t, float* hi, float* lo,
+template <class T>
+cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, float* lo,
                              cudaStream_t st);
+cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaStream_t st);
+// Ah scalar sync of nf <= 4 fields (stride g.fs) in one gather and one sync
+// launch (value slot c of the edge buffer carries field c)
+template <class T>
+cudaError_t launch_sync_fields(const FieldGeom& g, const Topology& tp, int nf, T* f, T* edge,
+                               cudaStream_t st);
 
 }  // namespace swm

@@ -156,8 +156,9 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
  * (hordiff_factory_mod.f90:27-40); others give SWM_E_UNSUPPORTED.  The
  * operator is -(c^4) L(L(.)) with L the narrow-stencil SBP Laplacian and
  * c = coeff*radius*hx, on h and on the Cartesian components of the
- * velocity.  Computed in FP64 in both precisions (FP32 contexts join the
- * state, and update the (hi, lo) pair in FP64). */
+ * velocity.  FP64 contexts compute it in FP64; FP32 contexts compute the
+ * tendency in FP32 from the high part of the state and add it to the
+ * (hi, lo) pair in FP64. */
 int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
                       const char* hordiff_h_name, double h_diff_coeff);
 /* vout = D(vin): operator_swm_diff_t%apply (operator_swm_diff_mod.f90:

@@ -5,8 +5,9 @@ same evaluation order up to the summation of the closure rows), so the bar is
 a J-weighted relative L2 difference <= 1e-12 per field for the narrow
 Laplacian, the diffusion operator (operator_swm_diff_mod.f90:25-46) and the
 drivers' time step of RK4 followed by one explicit Euler diffusion step
-(ts2_mod.f90:143-146).  The FP32 context runs the diffusion in FP64 on the
-joined state; its model steps stay within 1e-5 of the FP64 ones."""
+(ts2_mod.f90:143-146).  The FP32 context computes the diffusion tendency in
+FP32 (within 1e-4 of FP64) and adds it to its compensated state in FP64; its
+model steps stay within 1e-5 of the FP64 ones."""
 import numpy as np
 import pytest
 
@@ -112,6 +113,21 @@ def test_fp32_model_step_tracks_fp64():
     J = oracle.OracleDomain(N, 42).geometry()["J"]
     for a, b in zip(res["fp32"], res["fp64"]):
         assert rel_l2(a, b, J) <= 1e-5
+
+
+def test_fp32_diffusion_tendency_tracks_fp64():
+    N = 48
+    res = {}
+    for prec in ("fp64", "fp32"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision=prec))
+        dop = swm.OperatorSWMDiff(op)
+        x, t = op.create_stvec(), op.create_stvec()
+        x.upload(*_state(N))
+        dop.apply(t, x)
+        res[prec] = t.download()
+    J = oracle.OracleDomain(N, 42).geometry()["J"]
+    for a, b in zip(res["fp32"], res["fp64"]):
+        assert rel_l2(a, b, J) <= 1e-4
 
 
 def test_diffusion_conserves_mass_at_scale():
