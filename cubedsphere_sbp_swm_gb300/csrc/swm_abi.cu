@@ -1177,12 +1177,11 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
 template <class T>
 int laplace_fields(swm_ctx* ctx, int narrow, int nf, const T* src, T* dst) {
   const FieldGeom& g = ctx->g64;
-  CK(launch_laplace_presync<T>(g, narrow_tables<T>(ctx, narrow), nf, src, metric_of<T>(ctx),
-                               ctx->hx * ctx->cfg.radius, dwork<T>(ctx, 8), dwork<T>(ctx, 12), dst,
-                               ctx->st),
-     "laplace");
   T* edge = sizeof(T) == 8 ? (T*)ctx->edge64 : (T*)ctx->edge;
-  CK(launch_sync_fields<T>(g, ctx->topo, nf, dst, edge, ctx->st), "laplace sync");
+  CK(launch_laplace<T>(g, ctx->topo, narrow_tables<T>(ctx, narrow), nf, src, metric_of<T>(ctx),
+                       ctx->hx * ctx->cfg.radius, dwork<T>(ctx, 8), dwork<T>(ctx, 12), dst, edge,
+                       ctx->st),
+     "laplace");
   return SWM_OK;
 }
 

@@ -48,23 +48,24 @@ struct NarrowShape {
   static constexpr int w = 2 * hw + 1;
 };
 
-// Node kernels run on a 2-D grid: blockIdx.y = panel row p*n + j, x over the
-// columns i (RTPB threads per block).
-constexpr int RTPB = 128;
-inline dim3 row_grid(const FieldGeom& g) { return dim3((g.n + RTPB - 1) / RTPB, 6 * g.n); }
+// Node kernels run on 2-D tiles of TX columns x TY rows of the (6n)-row
+// stack of panels, so a block reuses the rows its y-stencils share.
+constexpr int TX = 32, TY = 8, RTPB = TX * TY;
+inline dim3 row_grid(const FieldGeom& g) { return dim3((g.n + TX - 1) / TX, (6 * g.n + TY - 1) / TY); }
+inline dim3 row_block() { return dim3(TX, TY); }
 
 struct Node {
   int p, i, j;
   long long idx;   // pitched index
 };
-// false for the padding threads past the last column
+// false for the threads past the last column or row
 __device__ __forceinline__ bool node_here(const FieldGeom& g, Node& r) {
-  r.i = blockIdx.x * RTPB + threadIdx.x;
-  const int row = blockIdx.y;
+  r.i = blockIdx.x * TX + threadIdx.x;
+  const int row = blockIdx.y * TY + threadIdx.y;
   r.p = row / g.n;
   r.j = row - r.p * g.n;
   r.idx = (long long)r.p * g.ps + (long long)r.j * g.P + r.i;
-  return r.i < g.n;
+  return r.i < g.n && row < 6 * g.n;
 }
 
 // Interior stencil coefficients of both directions (zero at closure nodes):
@@ -156,7 +157,7 @@ template <class T, int NARROW, int NF>
 __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f, const T* d1x,
                                                         const T* d1y, const T* cx, const T* cy,
                                                         const T* clx, const T* cly, const T* mt,
-                                                        double hs, T* out) {
+                                                        double hs, T* out, T* E) {
   using S = NarrowShape<NARROW>;
   Node k;
   if (!node_here(g, k)) return;
@@ -222,7 +223,14 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     T v = d2x + d2y;
     v = v + d2xy + d2yx;
     v = v / hs2;
-    out[c * g.fs + pb + o] = v / J;
+    v = v / J;
+    out[c * g.fs + pb + o] = v;
+    // panel-boundary values also go to value slot c of the edge buffer
+    auto put = [&](int side, int q) { E[((long long)(k.p * 4 + side) * 4 + c) * n + q] = v; };
+    if (k.i == 0) put(SIDE_L, k.j);
+    if (k.i == n - 1) put(SIDE_R, k.j);
+    if (k.j == 0) put(SIDE_B, k.i);
+    if (k.j == n - 1) put(SIDE_T, k.i);
   }
 }
 
@@ -277,26 +285,8 @@ __global__ void pair_axpy_kernel(long long count, double dt, const T* t, float* 
 }
 
 // Ah scalar sync of nf <= 4 fields at once (halo_Ah_scalar_sync_mod.f90:
-// 38-93): field c goes through value slot c of the edge buffer.
-template <class T>
-__global__ void gather_fields_kernel(FieldGeom g, int nf, const T* f, T* E) {
-  const int n = g.n, nb = 4 * n - 4;
-  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= 6 * nb) return;
-  const int p = gi / nb;
-  int i, j;
-  boundary_node(gi - p * nb, n, i, j);
-  const long long x = (long long)p * g.ps + (long long)j * g.P + i;
-  for (int c = 0; c < nf; ++c) {
-    const T a = f[c * g.fs + x];
-    auto put = [&](int side, int k) { E[((long long)(p * 4 + side) * 4 + c) * n + k] = a; };
-    if (i == 0) put(SIDE_L, j);
-    if (i == n - 1) put(SIDE_R, j);
-    if (j == 0) put(SIDE_B, i);
-    if (j == n - 1) put(SIDE_T, i);
-  }
-}
-
+// 38-93): field c comes from value slot c of the edge buffer, which the
+// Laplacian kernel filled with the panel-boundary values.
 template <class T>
 __global__ void sync_fields_kernel(FieldGeom g, Topology tp, int nf, const T* E, T* f) {
   const int n = g.n, nb = 4 * n - 4;
@@ -329,10 +319,10 @@ cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, c
                                  cudaStream_t st) {
   const long long ncl = narrow_closure_count(t.narrow, g.n);
   if (t.narrow == 63) {
-    narrow_coef_kernel<T, 63><<<row_grid(g), RTPB, 0, st>>>(g, m, t.cx, t.cy);
+    narrow_coef_kernel<T, 63><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy);
     narrow_closure_kernel<T, 63><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   } else {
-    narrow_coef_kernel<T, 42><<<row_grid(g), RTPB, 0, st>>>(g, m, t.cx, t.cy);
+    narrow_coef_kernel<T, 42><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy);
     narrow_closure_kernel<T, 42><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   }
   return cudaGetLastError();
@@ -340,40 +330,42 @@ cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, c
 
 template <class T, int NARROW, int NF>
 void laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f, const T* mt, double hs,
-                T* d1x, T* d1y, T* out, cudaStream_t st) {
-  lap_d1_kernel<T, NARROW, NF><<<row_grid(g), RTPB, 0, st>>>(g, f, mt, d1x, d1y);
-  lap_main_kernel<T, NARROW, NF><<<row_grid(g), RTPB, 0, st>>>(g, f, d1x, d1y, t.cx, t.cy, t.clx,
-                                                               t.cly, mt, hs, out);
+                T* d1x, T* d1y, T* out, T* edge, cudaStream_t st) {
+  lap_d1_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(g, f, mt, d1x, d1y);
+  lap_main_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(
+      g, f, d1x, d1y, t.cx, t.cy, t.clx, t.cly, mt, hs, out, edge);
 }
 
 template <class T>
-cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables<T>& t, int nf,
-                                   const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out,
-                                   cudaStream_t st) {
+cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowTables<T>& t, int nf,
+                           const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out, T* edge,
+                           cudaStream_t st) {
   if (nf != 1 && nf != 3 && nf != 4) return cudaErrorInvalidValue;
   if (t.narrow == 63) {
-    if (nf == 1) laplace_nf<T, 63, 1>(g, t, f, mt, hs, d1x, d1y, out, st);
-    else if (nf == 3) laplace_nf<T, 63, 3>(g, t, f, mt, hs, d1x, d1y, out, st);
-    else laplace_nf<T, 63, 4>(g, t, f, mt, hs, d1x, d1y, out, st);
+    if (nf == 1) laplace_nf<T, 63, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else if (nf == 3) laplace_nf<T, 63, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else laplace_nf<T, 63, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
   } else {
-    if (nf == 1) laplace_nf<T, 42, 1>(g, t, f, mt, hs, d1x, d1y, out, st);
-    else if (nf == 3) laplace_nf<T, 42, 3>(g, t, f, mt, hs, d1x, d1y, out, st);
-    else laplace_nf<T, 42, 4>(g, t, f, mt, hs, d1x, d1y, out, st);
+    if (nf == 1) laplace_nf<T, 42, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else if (nf == 3) laplace_nf<T, 42, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else laplace_nf<T, 42, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
   }
+  const int nb = 6 * (4 * g.n - 4);
+  sync_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, tp, nf, edge, out);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* u, const T* v, T* cart,
                            cudaStream_t st) {
-  to_cart_kernel<T><<<row_grid(g), RTPB, 0, st>>>(g, b12, u, v, cart);
+  to_cart_kernel<T><<<row_grid(g), row_block(), 0, st>>>(g, b12, u, v, cart);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_diff_tendency(const FieldGeom& g, const T* b12, double cuv, const T* L, T* tu,
                                  T* tv, double ch, const T* Lh, T* th, cudaStream_t st) {
-  from_cart_kernel<T><<<row_grid(g), RTPB, 0, st>>>(g, b12, T(cuv), L, tu, tv, T(ch), Lh,
+  from_cart_kernel<T><<<row_grid(g), row_block(), 0, st>>>(g, b12, T(cuv), L, tu, tv, T(ch), Lh,
                                                               th);
   return cudaGetLastError();
 }
@@ -385,16 +377,6 @@ cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, 
   return cudaGetLastError();
 }
 
-template <class T>
-cudaError_t launch_sync_fields(const FieldGeom& g, const Topology& tp, int nf, T* f, T* edge,
-                               cudaStream_t st) {
-  if (nf < 1 || nf > 4) return cudaErrorInvalidValue;
-  const int nb = 6 * (4 * g.n - 4);
-  gather_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, nf, f, edge);
-  sync_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, tp, nf, edge, f);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaStream_t st) {
   to_f32_kernel<<<dblk(count), DTPB, 0, st>>>(count, s, d);
   return cudaGetLastError();
@@ -403,17 +385,15 @@ cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaSt
 #define SWM_DIFF_INSTANTIATE(T)                                                                  \
   template cudaError_t launch_narrow_tables<T>(const FieldGeom&, const NarrowTables<T>&,         \
                                                const double*, cudaStream_t);                     \
-  template cudaError_t launch_laplace_presync<T>(const FieldGeom&, const NarrowTables<T>&, int,  \
-                                                 const T*, const T*, double, T*, T*, T*,         \
-                                                 cudaStream_t);                                  \
+  template cudaError_t launch_laplace<T>(const FieldGeom&, const Topology&, const NarrowTables<T>&,\
+                                         int, const T*, const T*, double, T*, T*, T*, T*,        \
+                                         cudaStream_t);                                          \
   template cudaError_t launch_to_cart<T>(const FieldGeom&, const T*, const T*, const T*, T*,     \
                                          cudaStream_t);                                          \
   template cudaError_t launch_diff_tendency<T>(const FieldGeom&, const T*, double, const T*, T*, \
                                                T*, double, const T*, T*, cudaStream_t);          \
   template cudaError_t launch_pair_axpy<T>(long long, double, const T*, float*, float*,          \
-                                           cudaStream_t);                                        \
-  template cudaError_t launch_sync_fields<T>(const FieldGeom&, const Topology&, int, T*, T*,      \
-                                             cudaStream_t);
+                                           cudaStream_t);
 SWM_DIFF_INSTANTIATE(float)
 SWM_DIFF_INSTANTIATE(double)
 

@@ -161,13 +161,13 @@ long long narrow_closure_count(int narrow, int n);
 template <class T>
 cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, const double* m,
                                  cudaStream_t st);
-// pre-sync Laplacian of nf = 1, 3 or 4 fields f into out (all at field
+// Edge-synced Laplacian of nf = 1, 3 or 4 fields f into out (all at field
 // stride g.fs); mt: metric of element type T; d1x, d1y: nf work fields
-// each; hs = hx * radius
+// each; hs = hx * radius; edge: edge buffer of element type T
 template <class T>
-cudaError_t launch_laplace_presync(const FieldGeom& g, const NarrowTables<T>& t, int nf,
-                                   const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out,
-                                   cudaStream_t st);
+cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowTables<T>& t, int nf,
+                           const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out, T* edge,
+                           cudaStream_t st);
 // cart (3 fields) = b1*u + b2*v; b12 from launch_basis
 template <class T>
 cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* u, const T* v, T* cart,
@@ -181,10 +181,6 @@ template <class T>
 cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, float* lo,
                              cudaStream_t st);
 cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaStream_t st);
-// Ah scalar sync of nf <= 4 fields (stride g.fs) in one gather and one sync
-// launch (value slot c of the edge buffer carries field c)
-template <class T>
-cudaError_t launch_sync_fields(const FieldGeom& g, const Topology& tp, int nf, T* f, T* edge,
-                               cudaStream_t st);
+
 
 }  // namespace swm
