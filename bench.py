@@ -546,6 +546,9 @@ def run_gpu_arm(args):
     adj = None
     if rank == 0 and not args.no_adjoint:
         adj = adjoint_leg(local)
+    dif = None
+    if rank == 0 and not args.no_diffusion:
+        dif = diffusion_leg(w, h, u, v, local, max(10, args.steps // 2), args.warmup)
 
     # CPU baseline: the oracle (C++ restatement) on the host cores, rank 0
     cpu = None
@@ -586,12 +589,63 @@ def run_gpu_arm(args):
             line["ensemble"] = ens
         if adj:
             line["adjoint"] = adj
+        if dif:
+            line["model_step_with_diffusion"] = dif
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def diffusion_leg(w, h, u, v, local, steps, warmup):
+    """The drivers' full time step (ts2_mod.f90:143-146): RK4, then one
+    explicit Euler step of the hyperdiffusion operator, with the TS2 scripts'
+    operators and coefficients (narrow-Laplacian order of the workload's SBP
+    order, uv_diff_coeff 0.03, h_diff_coeff 0.01).  Each timed step starts
+    from the initial state, with an L2 flush before it."""
+    import numpy as np
+    import torch
+    import cubedsphere_sbp_swm_gb300 as swm
+    dev = torch.device("cuda", local)
+    narrow = 63 if w["order"] == 63 else 42
+    names = ("hordiff_vec_xyz_Ah_sbp_%d_narrow" % narrow, "hordiff_scalar_Ah_sbp_%d_narrow" % narrow)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    out = {"operators": list(names), "uv_diff_coeff": 0.03, "h_diff_coeff": 0.01, "dt_s": w["dt"]}
+    for prec in ("fp32", "fp64"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=w["N"], sbp_order=w["order"], precision=prec, device=local))
+        dop = swm.OperatorSWMDiff(op, names[0], 0.03, names[1], 0.01)
+        s0, s = op.create_stvec(), op.create_stvec()
+        s0.upload(h, u, v)
+        s.assign_s1v1(1.0, s0)
+        stream = torch.cuda.ExternalStream(op.stream, device=dev)
+        eul, rk4 = swm.ExplicitEul1(), swm.RK4()
+        legs = {"model_step": lambda: op.model_step(s, w["dt"], 1),
+                "diffusion_step": lambda: eul.step(s, dop, w["dt"], 1),
+                "rk4_step": lambda: rk4.step(s, op, w["dt"], 1)}
+        r = {}
+        for name, fn in legs.items():
+            for _ in range(warmup):
+                fn()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(steps)]
+            torch.cuda.synchronize(dev)
+            for a, b in evs:
+                s.assign_s1v1(1.0, s0)
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                a.record(stream)
+                fn()
+                b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+            r[name + "_ms"] = round(ms, 5)
+        r["model_steps_per_s"] = round(1e3 / r["model_step_ms"], 3)
+        r["state_finite"] = bool(all(np.isfinite(a).all() for a in s.download()))
+        out[prec] = r
+        del op, dop
+    return out
 
 
 def cpu_baseline_sample(w, h, u, v, budget_s=15.0, min_steps=1, max_steps=50):
@@ -662,12 +716,14 @@ def main():
                     help="skip the 96-member ensemble leg")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint leg (N=192, 240 steps)")
+    ap.add_argument("--no-diffusion", action="store_true",
+                    help="skip the RK4 + hyperdiffusion model-step leg")
     ap.add_argument("--days", type=float, default=None,
                     help="simulated days of the accuracy run (default: the workload's)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--quick", action="store_true",
                     help="profiling case: time only the FP32 steps, print a short line")
-    ap.add_argument("--only", choices=("ensemble", "adjoint"), default=None,
+    ap.add_argument("--only", choices=("ensemble", "adjoint", "diffusion"), default=None,
                     help="run one leg alone and print its JSON object")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -675,8 +731,14 @@ def main():
         import torch
         _, _, local = _dist()
         torch.cuda.set_device(local)
-        res = (ensemble_leg(local, max(10, args.steps // 2), args.warmup, _measured_peak()[0])
-               if args.only == "ensemble" else adjoint_leg(local))
+        if args.only == "ensemble":
+            res = ensemble_leg(local, max(10, args.steps // 2), args.warmup, _measured_peak()[0])
+        elif args.only == "adjoint":
+            res = adjoint_leg(local)
+        else:
+            w = WORKLOADS[args.workload]
+            h, u, v, _ = _state(w)
+            res = diffusion_leg(w, h, u, v, local, max(10, args.steps // 2), args.warmup)
         print(json.dumps({args.only: res}), flush=True)
         return
     if args.impl == "reference":
