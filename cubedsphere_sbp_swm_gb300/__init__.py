@@ -26,7 +26,7 @@ from ._abi import SWM_FP32_FUSED, SWM_FP64_PLAIN, SwmError
 
 __all__ = [
     "ModelConfig", "OperatorSWM", "StvecSWM", "GridField", "RK4", "OperatorSWMDiff",
-    "ExplicitEul1", "HaloAhScalarSync",
+    "ExplicitEul1", "LatLonRegrid", "LatLonOutputer", "PaneledOutputer", "HaloAhScalarSync",
     "EcsAhVecSyncCovariant", "create_timescheme", "create_halo_procedure",
     "create_vector_halo_procedure", "Ensemble", "SwmError", "EARTH",
 ]
@@ -351,6 +351,82 @@ class ExplicitEul1:
     def step(self, v0: StvecSWM, operator: OperatorSWMDiff, dt: float, nsteps: int = 1):
         op = operator.op
         op._check(op._L.swm_diffusion_step(op._h, v0._h, float(dt), int(nsteps)))
+
+
+class LatLonRegrid:
+    """Lat-lon regrid of the context's Ah fields: create_latlon_regrid and
+    create_latlon_vector_regrid with grid type "Ah"
+    (regridders/regrid_factory_mod.f90:9-190).  Outputs are (Nlat, Nlon)
+    arrays (longitude fastest, latitude from -90 to 90 degrees); vectors come
+    out as (east, north) components."""
+
+    def __init__(self, op: OperatorSWM, Nlon: int, Nlat: int, interp_type: str = "cubic",
+                 components_type: str = "covariant"):
+        self.op, self.Nlon, self.Nlat = op, int(Nlon), int(Nlat)
+        h = ctypes.c_void_p()
+        op._check(op._L.swm_latlon_create(op._h, self.Nlon, self.Nlat, interp_type.encode(),
+                                          components_type.encode(), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.op._L.swm_latlon_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _out(self):
+        return np.empty((self.Nlat, self.Nlon))
+
+    def do_regrid(self, f: "GridField") -> np.ndarray:
+        out = self._out()
+        self.op._check(self.op._L.swm_latlon_regrid_field(self.op._h, self._h, f._h, _ptr(out)))
+        return out
+
+    def do_regrid_vec(self, u: "GridField", v: "GridField"):
+        uo, vo = self._out(), self._out()
+        self.op._check(self.op._L.swm_latlon_regrid_vector(self.op._h, self._h, u._h, v._h,
+                                                          _ptr(uo), _ptr(vo)))
+        return uo, vo
+
+    def regrid_state(self, s: "StvecSWM"):
+        h, u, v = self._out(), self._out(), self._out()
+        self.op._check(self.op._L.swm_latlon_regrid_state(self.op._h, self._h, s._h, _ptr(h),
+                                                          _ptr(u), _ptr(v)))
+        return h, u, v
+
+
+class LatLonOutputer:
+    """latlon_outputer_t and latlon_vec_outputer_t for a state
+    (outputer/latlon_outputer_mod.f90:38-190, created as in
+    outputer_factory_mod.f90:45-218 with cubic interpolation): FP32
+    direct-access records of Nlon*Nlat values."""
+
+    def __init__(self, op: OperatorSWM, Nlat: int, Nlon: int):
+        self.regrid = LatLonRegrid(op, Nlon, Nlat, "cubic", "covariant")
+        self.op = op
+
+    def write(self, s: "StvecSWM", h_file: str | None = "h.dat", u_file: str | None = "u.dat",
+              v_file: str | None = "v.dat", rec_num: int = 1):
+        enc = lambda x: x.encode() if x else None
+        self.op._check(self.op._L.swm_latlon_write(self.op._h, self.regrid._h, s._h, enc(h_file),
+                                                   enc(u_file), enc(v_file), int(rec_num)))
+
+
+class PaneledOutputer:
+    """master_paneled_outputer_t (outputer/master_paneled_outputer_mod.f90:24-77):
+    FP32 direct-access records of the six panels' (N+1)^2 values."""
+
+    def __init__(self, op: OperatorSWM):
+        self.op = op
+
+    def write(self, s: "StvecSWM", component: int, file_name: str, rec_num: int = 1):
+        self.op._check(self.op._L.swm_paneled_write(self.op._h, s._h, int(component),
+                                                    file_name.encode(), int(rec_num)))
 
 
 class HaloAhScalarSync:

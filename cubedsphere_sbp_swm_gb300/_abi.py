@@ -16,6 +16,7 @@ SWM_E_UNSUPPORTED = -2
 SWM_E_CUDA = -3
 SWM_E_NOMEM = -4
 SWM_E_DEVICE = -5
+SWM_E_IO = -6
 
 SWM_FP64_PLAIN = 0
 SWM_FP32_FUSED = 1
@@ -43,7 +44,8 @@ EXPORTS = (
     "swm_adjoint_destroy", "swm_adjoint_forward", "swm_adjoint_backward", "swm_adjoint_counts",
     "swm_state_upload_device", "swm_state_download_device", "swm_quadrature_weights",
     "swm_diffusion_set", "swm_apply_diffusion", "swm_diffusion_step", "swm_model_step",
-    "swm_laplace",
+    "swm_laplace", "swm_latlon_create", "swm_latlon_destroy", "swm_latlon_regrid_field",
+    "swm_latlon_regrid_vector", "swm_latlon_regrid_state", "swm_latlon_write", "swm_paneled_write",
 )
 
 
@@ -122,6 +124,13 @@ def load(build_if_missing: bool = True):
     sig("swm_diffusion_step", I, VP, VP, D, I)
     sig("swm_model_step", I, VP, VP, D, I)
     sig("swm_laplace", I, VP, VP, VP, I)
+    sig("swm_latlon_create", I, VP, I, I, C, C, PP)
+    sig("swm_latlon_destroy", None, VP)
+    sig("swm_latlon_regrid_field", I, VP, VP, VP, _D)
+    sig("swm_latlon_regrid_vector", I, VP, VP, VP, VP, _D, _D)
+    sig("swm_latlon_regrid_state", I, VP, VP, VP, _D, _D, _D)
+    sig("swm_latlon_write", I, VP, VP, VP, C, C, C, I)
+    sig("swm_paneled_write", I, VP, VP, I, C, I)
     sig("swm_diagnostics", I, VP, VP, _D)
     sig("swm_field_create", I, VP, PP)
     sig("swm_field_free", None, VP)

@@ -153,6 +153,20 @@ struct swm_field {
   double* p;
 };
 
+// Lat-lon interpolator of one context (regrid_factory_mod.f90:9-301): device
+// copies of the per-point stencil offsets, weights and rotation, and output
+// buffers of two planes (FP64 and FP32) with their page-locked host copies.
+struct swm_latlon {
+  swm_ctx* ctx;
+  int nlon, nlat, w, contravariant;
+  long long* base;
+  double *wx, *wy, *rot;
+  double* out;
+  float* out32;
+  double* hout;
+  float* hout32;
+};
+
 struct GraphEntry {
   cudaGraphExec_t exec;
   long use;
@@ -193,6 +207,7 @@ struct swm_ctx {
   // detaches them, so a later swm_state_free / swm_field_free stays safe
   std::set<swm_state*> states;
   std::set<swm_field*> fields;
+  std::set<swm_latlon*> latlons;
   // tangent-linear / adjoint workspace (FP64 contexts, allocated on first
   // use): 10 work fields, then 7 states of 3 fields; edge buffer of the
   // vector-sync transpose; transposed SBP table
@@ -597,6 +612,15 @@ int op_grad(swm_ctx* ctx, const double* f, double* gx, double* gy) {
   return SWM_OK;
 }
 
+void release_latlon(swm_latlon* r) {
+  void* dev[] = {r->base, r->wx, r->wy, r->rot, r->out, r->out32};
+  for (void* p : dev) if (p) cudaFree(p);
+  if (r->hout) cudaFreeHost(r->hout);
+  if (r->hout32) cudaFreeHost(r->hout32);
+  r->base = nullptr; r->wx = r->wy = r->rot = r->out = r->hout = nullptr;
+  r->out32 = r->hout32 = nullptr;
+}
+
 void free_ctx(swm_ctx* c) {
   if (!c) return;
   for (swm_state* s : c->states) {
@@ -607,6 +631,10 @@ void free_ctx(swm_ctx* c) {
   for (swm_field* f : c->fields) {
     if (f->p) cudaFree(f->p);
     f->p = nullptr; f->ctx = nullptr;
+  }
+  for (swm_latlon* r : c->latlons) {
+    release_latlon(r);
+    r->ctx = nullptr;
   }
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
   for (auto& e : c->ev_stage) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -2307,6 +2335,219 @@ int swm_quadrature_weights(swm_ctx* ctx, double* w_host) {
         w_host[k] = J[k] * hx2 * A[i] * A[j];
       }
   return SWM_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Lat-lon and paneled output (regridders/, outputer/)
+// ===========================================================================
+namespace {
+
+int check_latlon(swm_ctx* ctx, const swm_latlon* r) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  if (!r || r->ctx != ctx || !r->base) return fail(ctx, SWM_E_INVALID, "latlon interpolator not of this context");
+  return SWM_OK;
+}
+
+LatLonDev latlon_dev(const swm_latlon* r) {
+  return LatLonDev{r->nlon, r->nlat, r->w, r->base, r->wx, r->wy, r->rot};
+}
+
+// Regrid the scalar h (component 0) or the vector (u, v) (components 1, 2)
+// of a state into the interpolator's output planes.
+int latlon_state(swm_ctx* ctx, swm_latlon* r, const swm_state* s, bool vector, bool f32) {
+  const LatLonDev L = latlon_dev(r);
+  const long long fs = ctx->fs;
+  const int nf = vector ? 2 : 1;
+  const long long c0 = vector ? 1 : 0;
+  double* out = f32 ? nullptr : r->out;
+  float* out32 = f32 ? r->out32 : nullptr;
+  if (ctx->prec == SWM_FP64_PLAIN) {
+    const double* x = (const double*)s->hi;
+    CK(launch_latlon<double>(ctx->g64, L, nf, x + c0 * fs, x + (c0 + 1) * fs, nullptr, nullptr, out, out32,
+                             ctx->st),
+       "latlon");
+  } else {
+    const float* x = (const float*)s->hi;
+    CK(launch_latlon<float>(ctx->g64, L, nf, x + c0 * fs, x + (c0 + 1) * fs, s->lo + c0 * fs,
+                            s->lo + (c0 + 1) * fs, out, out32, ctx->st),
+       "latlon");
+  }
+  return SWM_OK;
+}
+
+// Write `count` FP32 values as record rec_num (1-based) of a direct-access
+// file of records of `count` values (the outputers' open(access="direct",
+// recl=count) with 4-byte record units).
+int write_record(swm_ctx* ctx, const char* path, int rec_num, const float* data, size_t count) {
+  if (!path || !*path) return SWM_OK;
+  if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
+  FILE* fp = std::fopen(path, "r+b");
+  if (!fp) fp = std::fopen(path, "w+b");
+  if (!fp) return fail(ctx, SWM_E_IO, std::string("cannot open ") + path);
+  const long long off = (long long)(rec_num - 1) * (long long)count * 4;
+  bool ok = fseeko(fp, (off_t)off, SEEK_SET) == 0 && std::fwrite(data, 4, count, fp) == count;
+  ok = (std::fclose(fp) == 0) && ok;
+  if (!ok) return fail(ctx, SWM_E_IO, std::string("cannot write ") + path);
+  return SWM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_latlon_create(swm_ctx* ctx, int nlon, int nlat, const char* interp_type,
+                      const char* components_type, swm_latlon** out) {
+  if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
+  *out = nullptr;
+  int w = 0, contra = 0;
+  const char* it = interp_type ? interp_type : "cubic";
+  if (!std::strcmp(it, "linear")) w = 2;
+  else if (!std::strcmp(it, "cubic")) w = 4;
+  else return fail(ctx, SWM_E_UNSUPPORTED, std::string("unknown interpolation type: ") + it);
+  const char* ct = components_type ? components_type : "covariant";
+  if (!std::strcmp(ct, "covariant")) contra = 0;
+  else if (!std::strcmp(ct, "contravariant")) contra = 1;
+  else return fail(ctx, SWM_E_UNSUPPORTED, std::string("unknown vector components type: ") + ct);
+  if (nlon < 1 || nlat < 2 || (long long)nlon * nlat > (1LL << 30))
+    return fail(ctx, SWM_E_INVALID, "bad lat-lon grid size");
+  LatLonHost h;
+  if (latlon_setup(ctx->N, nlon, nlat, w, contra, ctx->g64, h))
+    return fail(ctx, SWM_E_INVALID, "lat-lon set-up failed");
+  cudaSetDevice(ctx->cfg.device);
+  swm_latlon* r = new swm_latlon{ctx, nlon, nlat, w, contra, nullptr, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr, nullptr, nullptr};
+  const size_t np = (size_t)nlon * nlat;
+  cudaError_t e = cudaMalloc(&r->base, sizeof(long long) * np);
+  if (e == cudaSuccess) e = cudaMalloc(&r->wx, sizeof(double) * 4 * np);
+  if (e == cudaSuccess) e = cudaMalloc(&r->wy, sizeof(double) * 4 * np);
+  if (e == cudaSuccess) e = cudaMalloc(&r->rot, sizeof(double) * 4 * np);
+  if (e == cudaSuccess) e = cudaMalloc(&r->out, sizeof(double) * 2 * np);
+  if (e == cudaSuccess) e = cudaMalloc(&r->out32, sizeof(float) * 2 * np);
+  if (e == cudaSuccess) e = cudaMallocHost(&r->hout, sizeof(double) * 2 * np);
+  if (e == cudaSuccess) e = cudaMallocHost(&r->hout32, sizeof(float) * 2 * np);
+  if (e == cudaSuccess) e = cudaMemcpy(r->base, h.base.data(), sizeof(long long) * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(r->wx, h.wx.data(), sizeof(double) * 4 * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(r->wy, h.wy.data(), sizeof(double) * 4 * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(r->rot, h.rot.data(), sizeof(double) * 4 * np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    release_latlon(r);
+    delete r;
+    return fail(ctx, e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
+                std::string("latlon: ") + cudaGetErrorString(e));
+  }
+  ctx->latlons.insert(r);
+  *out = r;
+  return SWM_OK;
+}
+
+void swm_latlon_destroy(swm_latlon* r) {
+  if (!r) return;
+  if (r->ctx) {
+    cudaSetDevice(r->ctx->cfg.device);
+    release_latlon(r);
+    r->ctx->latlons.erase(r);
+  }
+  delete r;
+}
+
+int swm_latlon_regrid_field(swm_ctx* ctx, swm_latlon* r, const swm_field* f, double* out) {
+  if (int rc = check_latlon(ctx, r)) return rc;
+  if (int rc = check_field(ctx, f)) return rc;
+  if (!out) return fail(ctx, SWM_E_INVALID, "null output");
+  cudaSetDevice(ctx->cfg.device);
+  const size_t np = (size_t)r->nlon * r->nlat;
+  CK(launch_latlon<double>(ctx->g64, latlon_dev(r), 1, f->p, nullptr, nullptr, nullptr, r->out, nullptr,
+                           ctx->st),
+     "latlon");
+  CK(cudaMemcpyAsync(r->hout, r->out, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+  if (int rc = sync_check(ctx, ctx->st)) return rc;
+  std::memcpy(out, r->hout, sizeof(double) * np);
+  return SWM_OK;
+}
+
+int swm_latlon_regrid_vector(swm_ctx* ctx, swm_latlon* r, const swm_field* u, const swm_field* v,
+                             double* uo, double* vo) {
+  if (int rc = check_latlon(ctx, r)) return rc;
+  if (int rc = check_field(ctx, u)) return rc;
+  if (int rc = check_field(ctx, v)) return rc;
+  if (!uo || !vo) return fail(ctx, SWM_E_INVALID, "null output");
+  cudaSetDevice(ctx->cfg.device);
+  const size_t np = (size_t)r->nlon * r->nlat;
+  CK(launch_latlon<double>(ctx->g64, latlon_dev(r), 2, u->p, v->p, nullptr, nullptr, r->out, nullptr,
+                           ctx->st),
+     "latlon");
+  CK(cudaMemcpyAsync(r->hout, r->out, sizeof(double) * 2 * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+  if (int rc = sync_check(ctx, ctx->st)) return rc;
+  std::memcpy(uo, r->hout, sizeof(double) * np);
+  std::memcpy(vo, r->hout + np, sizeof(double) * np);
+  return SWM_OK;
+}
+
+int swm_latlon_regrid_state(swm_ctx* ctx, swm_latlon* r, const swm_state* s, double* h, double* u,
+                            double* v) {
+  if (int rc = check_latlon(ctx, r)) return rc;
+  if (int rc = check_state(ctx, s)) return rc;
+  cudaSetDevice(ctx->cfg.device);
+  const size_t np = (size_t)r->nlon * r->nlat;
+  if (h) {
+    if (int rc = latlon_state(ctx, r, s, false, false)) return rc;
+    CK(cudaMemcpyAsync(r->hout, r->out, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+    if (int rc = sync_check(ctx, ctx->st)) return rc;
+    std::memcpy(h, r->hout, sizeof(double) * np);
+  }
+  if (u || v) {
+    if (int rc = latlon_state(ctx, r, s, true, false)) return rc;
+    CK(cudaMemcpyAsync(r->hout, r->out, sizeof(double) * 2 * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+    if (int rc = sync_check(ctx, ctx->st)) return rc;
+    if (u) std::memcpy(u, r->hout, sizeof(double) * np);
+    if (v) std::memcpy(v, r->hout + np, sizeof(double) * np);
+  }
+  return SWM_OK;
+}
+
+int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char* h_file,
+                     const char* u_file, const char* v_file, int rec_num) {
+  if (int rc = check_latlon(ctx, r)) return rc;
+  if (int rc = check_state(ctx, s)) return rc;
+  if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
+  cudaSetDevice(ctx->cfg.device);
+  const size_t np = (size_t)r->nlon * r->nlat;
+  if (h_file && *h_file) {
+    if (int rc = latlon_state(ctx, r, s, false, true)) return rc;
+    CK(cudaMemcpyAsync(r->hout32, r->out32, sizeof(float) * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+    if (int rc = sync_check(ctx, ctx->st)) return rc;
+    if (int rc = write_record(ctx, h_file, rec_num, r->hout32, np)) return rc;
+  }
+  if ((u_file && *u_file) || (v_file && *v_file)) {
+    if (int rc = latlon_state(ctx, r, s, true, true)) return rc;
+    CK(cudaMemcpyAsync(r->hout32, r->out32, sizeof(float) * 2 * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+    if (int rc = sync_check(ctx, ctx->st)) return rc;
+    if (int rc = write_record(ctx, u_file, rec_num, r->hout32, np)) return rc;
+    if (int rc = write_record(ctx, v_file, rec_num, r->hout32 + np, np)) return rc;
+  }
+  return SWM_OK;
+}
+
+int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const char* file, int rec_num) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (component < 0 || component > 2 || !file) return fail(ctx, SWM_E_INVALID, "bad component or file");
+  if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
+  cudaSetDevice(ctx->cfg.device);
+  const size_t np = (size_t)6 * ctx->n * ctx->n;
+  PackedFields pf{{tmpf(ctx, 11), nullptr, nullptr}};
+  const long long off = (long long)component * ctx->fs;
+  if (ctx->prec == SWM_FP64_PLAIN)
+    CK(launch_pack_state(ctx->g64, 1, (const double*)s->hi + off, nullptr, pf, ctx->st), "pack");
+  else
+    CK(launch_pack_state(ctx->g64, 1, (const float*)s->hi + off, s->lo + off, pf, ctx->st), "pack");
+  std::vector<double> d(np);
+  CK(cudaMemcpyAsync(d.data(), pf.f[0], sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->st), "copy");
+  if (int rc = sync_check(ctx, ctx->st)) return rc;
+  std::vector<float> f(np);
+  for (size_t k = 0; k < np; ++k) f[k] = (float)d[k];
+  return write_record(ctx, file, rec_num, f.data(), np);
 }
 
 }  // extern "C"

@@ -5,6 +5,8 @@
 
 #include "swm_device.cuh"
 
+#include <vector>
+
 namespace swm {
 
 struct FieldGeom {
@@ -182,5 +184,31 @@ cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, 
                              cudaStream_t st);
 cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaStream_t st);
 
+
+// Lat-lon output (swm_output.cu).  Interpolator of an Nlon x Nlat grid with
+// stencil width w (2 linear, 4 cubic): per point the pitched offset of its
+// stencil's first node, w weights per direction (point-major planes) and
+// the rotation u2u, u2v, v2u, v2v to lat-lon components.
+struct LatLonHost {
+  int nlon = 0, nlat = 0, w = 0;
+  std::vector<long long> base;
+  std::vector<double> wx, wy, rot;   // 4 planes of nlon*nlat each
+};
+struct LatLonDev {
+  int nlon, nlat, w;
+  const long long* base;
+  const double *wx, *wy, *rot;
+};
+// host set-up (regrid_factory_mod.f90:195-299; rotation of 121-160 for
+// covariant or contravariant components); -1 on bad arguments
+int latlon_setup(int N, int nlon, int nlat, int width, int contravariant, const FieldGeom& g,
+                 LatLonHost& h);
+// nf = 1: out = regrid of fa; nf = 2: the vector (fa, fb) regridded and
+// rotated, out = (u plane, v plane).  la/lb: FP32 low parts (nullable);
+// out (FP64) and out32 (FP32) nullable.
+template <class T>
+cudaError_t launch_latlon(const FieldGeom& g, const LatLonDev& L, int nf, const T* fa, const T* fb,
+                          const float* la, const float* lb, double* out, float* out32,
+                          cudaStream_t st);
 
 }  // namespace swm

@@ -38,6 +38,7 @@ extern "C" {
 #define SWM_E_CUDA        -3  /* CUDA runtime failure */
 #define SWM_E_NOMEM       -4  /* device or host allocation failed */
 #define SWM_E_DEVICE      -5  /* a kernel raised its device error flag */
+#define SWM_E_IO          -6  /* an output file could not be opened or written */
 
 /* Arithmetic of the hot path. */
 #define SWM_FP64_PLAIN 0   /* FP64 end to end; parity path (1e-12 rel. L2/step) */
@@ -47,6 +48,7 @@ extern "C" {
 typedef struct swm_ctx swm_ctx;      /* domain + operator + time scheme */
 typedef struct swm_state swm_state;  /* stvec_swm_t: (h, u, v) on the device */
 typedef struct swm_field swm_field;  /* grid_field_t: one FP64 field */
+typedef struct swm_latlon swm_latlon;  /* lat-lon interpolator of a context */
 
 /* Model configuration: the &domain, &metric and &shallow_water_model keys
  * the hot path needs (domain/config_domain_mod.f90:26-58,
@@ -349,6 +351,39 @@ int  swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out,
 /* ---------------------------------------------------------------------- */
 #define SWM_SYNC_STATIC_MAX_N 1024
 int swm_sync_scalar_static(swm_ctx* ctx, swm_field* f);
+
+/* ---------------------------------------------------------------------- */
+/* Lat-lon and paneled output                                             */
+/* ---------------------------------------------------------------------- */
+/* Interpolator of the Ah fields of a context to an Nlon x Nlat lat-lon grid
+ * (lon = i*2pi/Nlon, lat = -pi/2 + j*pi/(Nlat-1)): create_latlon_regrid /
+ * create_latlon_vector_regrid with scalar/vector grid type "Ah"
+ * (regridders/regrid_factory_mod.f90:9-190, 195-299).  interp_type
+ * "linear" or "cubic" (NULL: cubic, the outputers' choice);
+ * components_type "covariant" or "contravariant" (NULL: covariant), the
+ * meaning of the (u, v) it is given.  Outputs have Nlon*Nlat values,
+ * longitude fastest; vectors come out as (east, north) components. */
+int swm_latlon_create(swm_ctx* ctx, int nlon, int nlat, const char* interp_type,
+                      const char* components_type, swm_latlon** out);
+void swm_latlon_destroy(swm_latlon* r);
+/* regrid_t%do_regrid (regrid_to_latlon_mod.f90:54-74) of an FP64 field */
+int swm_latlon_regrid_field(swm_ctx* ctx, swm_latlon* r, const swm_field* f, double* out);
+/* regrid_vec_t%do_regrid (regrid_to_latlon_mod.f90:76-124) of (u, v) */
+int swm_latlon_regrid_vector(swm_ctx* ctx, swm_latlon* r, const swm_field* u, const swm_field* v,
+                             double* uo, double* vo);
+/* h and (u, v) of a state; any output may be NULL */
+int swm_latlon_regrid_state(swm_ctx* ctx, swm_latlon* r, const swm_state* s, double* h, double* u,
+                            double* v);
+/* latlon_outputer_t%write and latlon_vec_outputer_t%write
+ * (outputer/latlon_outputer_mod.f90:38-190): FP32 record rec_num (1-based)
+ * of Nlon*Nlat values into direct-access files (the reference's h.dat,
+ * u.dat, v.dat); a NULL or empty name skips that file. */
+int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char* h_file,
+                     const char* u_file, const char* v_file, int rec_num);
+/* master_paneled_outputer_t%write (outputer/master_paneled_outputer_mod.f90:
+ * 24-77): FP32 record rec_num of 6*(N+1)^2 values (i fastest, then j, then
+ * panel) of state component 0 (h), 1 (u) or 2 (v). */
+int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const char* file, int rec_num);
 
 #ifdef __cplusplus
 }

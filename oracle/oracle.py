@@ -77,6 +77,12 @@ def lib():
         L.orc_vector_test_field.restype = ctypes.c_int
         L.orc_scalar_test_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, _D]
         L.orc_scalar_test_field.restype = ctypes.c_int
+        L.orc_latlon_scalar.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
+        L.orc_latlon_scalar.restype = ctypes.c_int
+        L.orc_latlon_vector.argtypes = [vp] + [ctypes.c_int] * 4 + [_D] * 4
+        L.orc_latlon_vector.restype = ctypes.c_int
+        L.orc_golden_regrid.argtypes = [ctypes.c_int, ctypes.c_int, _D]
+        L.orc_golden_regrid.restype = ctypes.c_int
         for name, args in (("orc_laplace", [vp, ctypes.c_int, _D, _D]),
                            ("orc_hordiff_scalar", [vp, ctypes.c_int, ctypes.c_double, _D, _D]),
                            ("orc_hordiff_vec_xyz", [vp, ctypes.c_int, ctypes.c_double] + [_D] * 4),
@@ -222,6 +228,20 @@ class OracleDomain:
                                         float(h_coeff), _p(h), _p(u), _p(v), float(dt)) == 0
         return h, u, v
 
+    # lat-lon regrid of Ah fields (width 2 linear, 4 cubic); (Nlat, Nlon) arrays
+    def latlon_scalar(self, f, nlon, nlat, width=4):
+        out = np.zeros((nlat, nlon))
+        assert lib().orc_latlon_scalar(self._h, int(nlon), int(nlat), int(width),
+                                       _p(np.ascontiguousarray(f)), _p(out)) == 0
+        return out
+
+    def latlon_vector(self, u, v, nlon, nlat, width=4, contravariant=False):
+        uo, vo = np.zeros((nlat, nlon)), np.zeros((nlat, nlon))
+        assert lib().orc_latlon_vector(self._h, int(nlon), int(nlat), int(width),
+                                       1 if contravariant else 0, _p(np.ascontiguousarray(u)),
+                                       _p(np.ascontiguousarray(v)), _p(uo), _p(vo)) == 0
+        return uo, vo
+
     VECTOR_FIELDS = {"solid_rotation": 0, "cross_polar": 1, "xyz_grad": 2, "vsh_curl_free_10": 3}
     SCALAR_FIELDS = {"xyz": 10, "cross_polar_div": 11, "cross_polar_zeta": 12}
 
@@ -261,6 +281,15 @@ def golden(kind: str, N: int = 32, sbp_order: int = 42):
     if rc != 0:
         raise ValueError(f"oracle golden {kind} failed for order {sbp_order}")
     return out
+
+
+def golden_regrid(kind: str, interp: str) -> np.ndarray:
+    """test_regrid_mod.f90's maximum errors on the Ah grid at N=32: kind
+    "scalar", "covariant" or "contravariant"; interp "linear" or "cubic"."""
+    out = np.zeros(2)
+    k = {"scalar": 0, "covariant": 1, "contravariant": 2}[kind]
+    assert lib().orc_golden_regrid(k, 2 if interp == "linear" else 4, _p(out)) == 0
+    return out[:1] if k == 0 else out
 
 
 def quadrature_error(N: int, sbp_order: int, max_order: int) -> float:

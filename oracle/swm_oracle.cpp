@@ -813,6 +813,127 @@ void hordiff_vec_xyz(const orc_domain& d, int narrow, double coeff, const double
   sync_vector_cov(d, ut, vt);
 }
 
+// ---------------------------------------------------------------------------
+// Lat-lon output of Ah fields: the interpolator of create_latlon_interp
+// (regridders/regrid_factory_mod.f90:195-299), the scalar and vector regrids
+// (regrid_to_latlon_mod.f90:54-124, 126-165) and the ECS map from a point on
+// the sphere to (panel, alpha, beta) (equiang_cs/ecs_metric_mod.f90:480-506).
+// ---------------------------------------------------------------------------
+void cart_to_native(const double r[3], int& panel, double& alpha, double& beta) {
+  panel = 0;
+  double best = 0.0;
+  for (int p = 0; p < 6; ++p) {
+    const double rn = -(r[0] * TN[p][0] + r[1] * TN[p][1] + r[2] * TN[p][2]);
+    if (rn > best) { panel = p; best = rn; }
+  }
+  alpha = std::atan((TEX[panel][0] * r[0] + TEX[panel][1] * r[1] + TEX[panel][2] * r[2]) / best);
+  beta = std::atan((TEY[panel][0] * r[0] + TEY[panel][1] * r[1] + TEY[panel][2] * r[2]) / best);
+}
+
+struct LatLonInterp {
+  int nlon = 0, nlat = 0, w = 0;
+  std::vector<int> panel, xi, yi;      // stencil start (0-based) per point
+  std::vector<double> wx, wy;          // w weights per point
+  std::vector<double> alpha, beta;
+};
+
+// Point (i, j) of the Nlon x Nlat grid: lon = i*2pi/Nlon, lat = -pi/2 + j*pi/(Nlat-1).
+void latlon_point(int nlon, int nlat, int i, int j, double& lat, double& lon) {
+  const double hlon = 2.0 * PI / (double)nlon, hlat = PI / (nlat - 1.0);
+  lat = -0.5 * PI + hlat * j;
+  lon = hlon * i;
+}
+
+LatLonInterp make_latlon_interp(const orc_domain& d, int nlon, int nlat, int w) {
+  LatLonInterp L;
+  L.nlon = nlon; L.nlat = nlat; L.w = w;
+  const int np = nlon * nlat, n = d.n;
+  L.panel.resize(np); L.xi.resize(np); L.yi.resize(np);
+  L.wx.resize((size_t)w * np); L.wy.resize((size_t)w * np);
+  L.alpha.resize(np); L.beta.resize(np);
+  const double alpha0 = -0.25 * PI;
+  for (int j = 0; j < nlat; ++j)
+    for (int i = 0; i < nlon; ++i) {
+      const int q = j * nlon + i;
+      double lat, lon;
+      latlon_point(nlon, nlat, i, j, lat, lon);
+      const double r[3] = {std::cos(lat) * std::cos(lon), std::cos(lat) * std::sin(lon), std::sin(lat)};
+      int p; double a, b;
+      cart_to_native(r, p, a, b);
+      L.panel[q] = p; L.alpha[q] = a; L.beta[q] = b;
+      // 1-based node coordinates, stencil clipped to the panel's nodes 1..n
+      const double zdx = (a - alpha0) / d.hx + 1.0, zdy = (b - alpha0) / d.hx + 1.0;
+      int ir = std::min((int)std::floor(zdx) + w / 2, n);
+      const int x1 = std::max(ir - w + 1, 1);
+      ir = std::min((int)std::floor(zdy) + w / 2, n);
+      const int y1 = std::max(ir - w + 1, 1);
+      L.xi[q] = x1 - 1; L.yi[q] = y1 - 1;
+      const double dx = zdx - x1, dy = zdy - y1;
+      double* WX = &L.wx[(size_t)w * q];
+      double* WY = &L.wy[(size_t)w * q];
+      if (w == 2) {
+        WX[0] = 1.0 - dx; WX[1] = dx;
+        WY[0] = 1.0 - dy; WY[1] = dy;
+      } else {
+        WX[0] = -(dx - 1.0) * (dx - 2.0) * (dx - 3.0) / 6.0;
+        WX[1] = dx * (dx - 2.0) * (dx - 3.0) / 2.0;
+        WX[2] = -dx * (dx - 1.0) * (dx - 3.0) / 2.0;
+        WX[3] = dx * (dx - 1.0) * (dx - 2.0) / 6.0;
+        WY[0] = -(dy - 1.0) * (dy - 2.0) * (dy - 3.0) / 6.0;
+        WY[1] = dy * (dy - 2.0) * (dy - 3.0) / 2.0;
+        WY[2] = -dy * (dy - 1.0) * (dy - 3.0) / 2.0;
+        WY[3] = dy * (dy - 1.0) * (dy - 2.0) / 6.0;
+      }
+    }
+  return L;
+}
+
+// latlon_interpolate (regrid_to_latlon_mod.f90:146-165)
+void latlon_interpolate(const orc_domain& d, const LatLonInterp& L, const double* f, double* out) {
+  const int n = d.n, w = L.w;
+  for (int q = 0; q < L.nlon * L.nlat; ++q) {
+    const double* F = f + (size_t)L.panel[q] * n * n;
+    double acc = 0.0;
+    for (int j1 = 0; j1 < w; ++j1)
+      for (int i1 = 0; i1 < w; ++i1) {
+        const double p = F[(L.yi[q] + j1) * n + (L.xi[q] + i1)];
+        acc = acc + L.wx[(size_t)w * q + i1] * L.wy[(size_t)w * q + j1] * p;
+      }
+    out[q] = acc;
+  }
+}
+
+// Ah vector regrid: both components interpolated, then rotated to the
+// lat-lon (east, north) components with the dot products of the lat-lon
+// unit vectors and b1, b2 (covariant components) or a1, a2 (contravariant)
+// at the point (regrid_factory_mod.f90:121-160, regrid_to_latlon_mod.f90:
+// 126-144).
+void latlon_vector(const orc_domain& d, const LatLonInterp& L, bool contravariant, const double* u,
+                   const double* v, double* uo, double* vo) {
+  latlon_interpolate(d, L, u, uo);
+  latlon_interpolate(d, L, v, vo);
+  for (int j = 0; j < L.nlat; ++j)
+    for (int i = 0; i < L.nlon; ++i) {
+      const int q = j * L.nlon + i;
+      double lat, lon;
+      latlon_point(L.nlon, L.nlat, i, j, lat, lon);
+      const double iv[3] = {-std::sin(lon), std::cos(lon), 0.0};
+      const double jv[3] = {-std::sin(lat) * std::cos(lon), -std::sin(lat) * std::sin(lon), std::cos(lat)};
+      double e1p[3], e2p[3], e1[3], e2[3];
+      if (contravariant) { a1_proto(L.alpha[q], L.beta[q], e1p); a2_proto(L.alpha[q], L.beta[q], e2p); }
+      else { b1_proto(L.alpha[q], L.beta[q], e1p); b2_proto(L.alpha[q], L.beta[q], e2p); }
+      to_face(L.panel[q], e1p, e1);
+      to_face(L.panel[q], e2p, e2);
+      const double u2u = iv[0] * e1[0] + iv[1] * e1[1] + iv[2] * e1[2];
+      const double u2v = jv[0] * e1[0] + jv[1] * e1[1] + jv[2] * e1[2];
+      const double v2u = iv[0] * e2[0] + iv[1] * e2[1] + iv[2] * e2[2];
+      const double v2v = jv[0] * e2[0] + jv[1] * e2[1] + jv[2] * e2[2];
+      const double zu = uo[q], zv = vo[q];
+      uo[q] = u2u * zu + v2u * zv;
+      vo[q] = u2v * zu + v2v * zv;
+    }
+}
+
 bool narrow_ok(const orc_domain& d, int narrow) {
   return (narrow == 42 || narrow == 63) && d.n >= 2 * narrow_table(narrow).rows;
 }
@@ -906,6 +1027,70 @@ void orc_diagnostics(const orc_domain* d, const double* hs, const double* h, con
   }
   out[0] = hmin; out[1] = hmax; out[2] = mass(*d, h);
   out[3] = ke + pen; out[4] = ke; out[5] = pen; out[6] = mass(*d, cu.data());
+}
+
+// Lat-lon regrids of Ah fields: width 2 (linear) or 4 (cubic); out has
+// Nlon*Nlat values, longitude fastest.  -1 on bad arguments.
+int orc_latlon_scalar(const orc_domain* d, int nlon, int nlat, int width, const double* f,
+                      double* out) {
+  if (nlon < 1 || nlat < 2 || (width != 2 && width != 4)) return -1;
+  const LatLonInterp L = make_latlon_interp(*d, nlon, nlat, width);
+  latlon_interpolate(*d, L, f, out);
+  return 0;
+}
+int orc_latlon_vector(const orc_domain* d, int nlon, int nlat, int width, int contravariant,
+                      const double* u, const double* v, double* uo, double* vo) {
+  if (nlon < 1 || nlat < 2 || (width != 2 && width != 4)) return -1;
+  const LatLonInterp L = make_latlon_interp(*d, nlon, nlat, width);
+  latlon_vector(*d, L, contravariant != 0, u, v, uo, vo);
+  return 0;
+}
+
+// The reference's regrid known-answer test (test/test_regrid/
+// test_regrid_mod.f90:16-119) on the Ah grid at N=32, nz=3: the maximum
+// interpolation error of the xyz scalar field (kind 0; out[0]) or of the
+// solid rotation field's lat-lon components (kind 1 covariant, 2
+// contravariant; out[0] u, out[1] v).
+int orc_golden_regrid(int kind, int width, double out[2]) {
+  const int N = 32, nlon = 4 * N, nlat = 2 * N + 1;
+  orc_domain d;
+  const double axis[3] = {0.0, 0.0, 1.0};
+  build(d, N, 42, 1.0, 9.80616, 1.0, axis);
+  const LatLonInterp L = make_latlon_interp(d, nlon, nlat, width);
+  const int npl = nlon * nlat;
+  std::vector<double> a(npl), b(npl);
+  out[0] = out[1] = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    if (kind == 0) {
+      std::vector<double> f(d.npts());
+      for (int q = 0; q < d.npts(); ++q) f[q] = field_xyz(k, d.rx[q], d.ry[q], d.rz[q]);
+      latlon_interpolate(d, L, f.data(), a.data());
+    } else {
+      std::vector<double> u, v;
+      set_vector(d, [k](double x, double y, double z, double w[3]) { field_solid_rotation(k, x, y, z, w); },
+                 kind == 2, u, v);
+      latlon_vector(d, L, kind == 2, u.data(), v.data(), a.data(), b.data());
+    }
+    for (int j = 0; j < nlat; ++j)
+      for (int i = 0; i < nlon; ++i) {
+        const int q = j * nlon + i;
+        double lat, lon;
+        latlon_point(nlon, nlat, i, j, lat, lon);
+        const double x = std::cos(lat) * std::cos(lon), y = std::cos(lat) * std::sin(lon), z = std::sin(lat);
+        if (kind == 0) {
+          out[0] = std::max(out[0], std::fabs(a[q] - field_xyz(k, x, y, z)));
+        } else {
+          double w[3];
+          field_solid_rotation(k, x, y, z, w);
+          const double ut = -std::sin(lon) * w[0] + std::cos(lon) * w[1];
+          const double vt = -std::sin(lat) * std::cos(lon) * w[0] - std::sin(lat) * std::sin(lon) * w[1] +
+                            std::cos(lat) * w[2];
+          out[0] = std::max(out[0], std::fabs(a[q] - ut));
+          out[1] = std::max(out[1], std::fabs(b[q] - vt));
+        }
+      }
+  }
+  return 0;
 }
 
 // Hyperdiffusion pieces (operator_swm_diff_mod.f90:25-46,

@@ -89,6 +89,16 @@ int orc_diffusion_apply(const orc_domain* d, int uv_narrow, double uv_coeff, int
 /* explicit_Eul1 step (explicit_Eul1_mod.f90:20-30) of the diffusion operator */
 int orc_diffusion_step(const orc_domain* d, int uv_narrow, double uv_coeff, int h_narrow,
                        double h_coeff, double* h, double* u, double* v, double dt);
+/* Lat-lon regrid of Ah fields (regridders/regrid_factory_mod.f90,
+ * regrid_to_latlon_mod.f90): width 2 linear, 4 cubic; Nlon*Nlat outputs,
+ * longitude fastest, lat = -pi/2 .. pi/2. */
+int orc_latlon_scalar(const orc_domain* d, int nlon, int nlat, int width, const double* f,
+                      double* out);
+int orc_latlon_vector(const orc_domain* d, int nlon, int nlat, int width, int contravariant,
+                      const double* u, const double* v, double* uo, double* vo);
+/* test_regrid_mod.f90 known-answer values on the Ah grid at N=32: kind 0
+ * scalar, 1 covariant vector, 2 contravariant vector. */
+int orc_golden_regrid(int kind, int width, double out[2]);
 double orc_l2norm(const orc_domain* d, const double* f);   /* vec_math_mod.f90:50-90 */
 double orc_mass(const orc_domain* d, const double* f);     /* SBP quadrature */
 

@@ -104,3 +104,17 @@ def test_discrete_mass_conservation():
     th, tu, tv = d.apply(h, u, v)
     scale = d.mass(np.abs(th)) + 1e-300
     assert abs(d.mass(th)) / scale < 1e-12
+
+
+REGRID = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "regrid_ah_n32.json")))
+
+
+@pytest.mark.parametrize("case", REGRID, ids=lambda c: f"{c['kind']}-{c['components']}-{c['interp']}")
+def test_latlon_regrid_matches_reference(case):
+    """The reference's lat-lon regrid known-answer values (full precision,
+    test_regrid_mod.f90 at N=32, Ah grid): maximum interpolation errors of
+    the xyz scalar field and of the solid rotation field."""
+    kind = case["components"] or "scalar"
+    got = oracle.golden_regrid(kind, case["interp"])
+    ref = np.array(case["values"])
+    assert np.allclose(got, ref, rtol=1e-9, atol=0.0), (got, ref)
