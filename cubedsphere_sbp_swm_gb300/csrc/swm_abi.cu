@@ -973,9 +973,7 @@ static int combine(swm_ctx* ctx, swm_state* s, double s1, const swm_state* a, do
       CK(launch_axpby_f32pair(cnt, 1.0, ohi, olo, s1, (const float*)a->hi, a->lo, ohi, olo, ctx->st), "update");
       if (b) CK(launch_axpby_f32pair(cnt, 1.0, ohi, olo, s2, (const float*)b->hi, b->lo, ohi, olo, ctx->st), "update");
     } else if (!a) {
-      double* d = tmpf(ctx, 11);  // 3 work fields = 3*fs doubles
-      CK(launch_fill(cnt, s1, d, ctx->st), "fill");
-      CK(launch_split_f64(cnt, d, ohi, olo, ctx->st), "split");
+      CK(launch_fill_f32pair(cnt, s1, ohi, olo, ctx->st), "fill");
     } else {
       CK(launch_axpby_f32pair(cnt, s1, (const float*)a->hi, a->lo, s2,
                               b ? (const float*)b->hi : nullptr, b ? b->lo : nullptr, ohi, olo, ctx->st), "assign");

@@ -363,16 +363,54 @@ __global__ void diag_kernel(FieldGeom g, const double* m, double grav, const dou
 // ---------------------------------------------------------------------------
 // FP32 (hi, lo) pair helpers
 // ---------------------------------------------------------------------------
-__global__ void axpby_pair_kernel(long long count, double s1, const float* ahi, const float* alo,
-                                  double s2, const float* bhi, const float* blo, float* ohi,
-                                  float* olo) {
+// FP32 (hi, lo) pairs combined in double-float arithmetic: error-free
+// two-sum and two-product (fmaf), then renormalisation; the coefficients
+// come split into float pairs.  FP32 instructions only (GB300's FP64 rate
+// would bound an FP64 evaluation); about 2^-44 relative accuracy.
+__device__ __forceinline__ void quick_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  e = b - (s - a);
+}
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void df_mul(float xh, float xl, float yh, float yl, float& h, float& l) {
+  const float p = xh * yh;
+  float e = fmaf(xh, yh, -p);
+  e = fmaf(xh, yl, e);
+  e = fmaf(xl, yh, e);
+  quick_two_sum(p, e, h, l);
+}
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float& h, float& l) {
+  float sm, e;
+  two_sum(ah, bh, sm, e);
+  e += al + bl;
+  quick_two_sum(sm, e, h, l);
+}
+
+__global__ void axpby_pair_kernel(long long count, float s1h, float s1l, const float* ahi,
+                                  const float* alo, float s2h, float s2l, const float* bhi,
+                                  const float* blo, float* ohi, float* olo) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  double x = s1 * ((double)ahi[k] + (double)alo[k]);
-  if (bhi) x += s2 * ((double)bhi[k] + (double)blo[k]);
-  const float hi = (float)x;
-  ohi[k] = hi;
-  olo[k] = (float)(x - (double)hi);
+  float h, l;
+  df_mul(s1h, s1l, ahi[k], alo[k], h, l);
+  if (bhi) {
+    float h2, l2;
+    df_mul(s2h, s2l, bhi[k], blo[k], h2, l2);
+    df_add(h, l, h2, l2, h, l);
+  }
+  ohi[k] = h;
+  olo[k] = l;
+}
+
+__global__ void fill_pair_kernel(long long count, float vh, float vl, float* ohi, float* olo) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  ohi[k] = vh;
+  olo[k] = vl;
 }
 
 __global__ void split_kernel(long long count, const double* s, float* hi, float* lo) {
@@ -574,7 +612,17 @@ cudaError_t launch_diag_integrands(const FieldGeom& g, const double* m64, double
 cudaError_t launch_axpby_f32pair(long long count, double s1, const float* ahi, const float* alo,
                                  double s2, const float* bhi, const float* blo, float* ohi,
                                  float* olo, cudaStream_t st) {
-  axpby_pair_kernel<<<nblk(count), TPB, 0, st>>>(count, s1, ahi, alo, s2, bhi, blo, ohi, olo);
+  const float s1h = (float)s1, s1l = (float)(s1 - (double)s1h);
+  const float s2h = (float)s2, s2l = (float)(s2 - (double)s2h);
+  axpby_pair_kernel<<<nblk(count), TPB, 0, st>>>(count, s1h, s1l, ahi, alo, s2h, s2l, bhi, blo, ohi,
+                                                 olo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_f32pair(long long count, double value, float* ohi, float* olo,
+                                cudaStream_t st) {
+  const float vh = (float)value, vl = (float)(value - (double)vh);
+  fill_pair_kernel<<<nblk(count), TPB, 0, st>>>(count, vh, vl, ohi, olo);
   return cudaGetLastError();
 }
 

@@ -125,10 +125,13 @@ cudaError_t launch_diag_integrands(const FieldGeom& g, const double* m64, double
                                    double* ke_v, double* pe, double* ens, cudaStream_t st);
 
 // State combinations for the FP32 compensated representation: out = s1*(a_hi
-// + a_lo) + s2*(b_hi + b_lo) evaluated in FP64 and split into (hi, lo).
+// + a_lo) + s2*(b_hi + b_lo) (b nullable) in double-float arithmetic on FP32
+// instructions; out may alias a or b.  fill: (hi, lo) = value.
 cudaError_t launch_axpby_f32pair(long long count, double s1, const float* ahi, const float* alo,
                                  double s2, const float* bhi, const float* blo, float* ohi,
                                  float* olo, cudaStream_t st);
+cudaError_t launch_fill_f32pair(long long count, double value, float* ohi, float* olo,
+                                cudaStream_t st);
 // FP64 <-> (hi, lo) FP32 pair conversions
 cudaError_t launch_split_f64(long long count, const double* src, float* hi, float* lo,
                              cudaStream_t st);

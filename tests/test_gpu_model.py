@@ -135,6 +135,30 @@ def test_stvec_linear_combinations(cfg1):
     assert abs(a.algebraic_norm2() - np.sqrt(np.sum(h * h) + np.sum(u * u) + np.sum(v * v))) < 1e-9
 
 
+def test_stvec_linear_combinations_fp32_pair(cfg1):
+    """The FP32 (hi, lo) pair algebra (double-float arithmetic on FP32
+    instructions) agrees with FP64 to ~2^-44 relative."""
+    od, J, (h, u, v) = cfg1
+    op = swm.OperatorSWM(swm.ModelConfig(N=48, precision="fp32"))
+    a = _state(op, h, u, v)
+    b = _state(op, 2 * h, -u, 0.5 * v)
+    c = a.create_similar()
+    dt6 = 90.0 / 6.0 * 0.1   # not a float
+    c.assign_s1v1s2v2(dt6, a, -3.0, b)
+    ref = [dt6 * x + -3.0 * y for x, y in zip((h, u, v), (2 * h, -u, 0.5 * v))]
+    for got, r in zip(c.download(), ref):
+        assert np.max(np.abs(got - r)) <= 1e-12 * np.max(np.abs(r))
+    c.update_s1v1(1.0 / 3.0, a)
+    ref = [r + (1.0 / 3.0) * x for r, x in zip(ref, (h, u, v))]
+    for got, r in zip(c.download(), ref):
+        assert np.max(np.abs(got - r)) <= 1e-12 * np.max(np.abs(r))
+    c.assign_s1v1(1.0, a)                       # a copy is exact
+    for got, x in zip(c.download(), a.download()):
+        assert np.array_equal(got, x)
+    c.assign_s1(0.1)
+    assert np.max(np.abs(c.download()[0] - 0.1)) <= 1e-15
+
+
 def test_state_roundtrip_fp32_pair_is_exact_to_fp64_split(cfg1):
     od, J, (h, u, v) = cfg1
     op = swm.OperatorSWM(swm.ModelConfig(N=48, precision="fp32"))
