@@ -424,7 +424,7 @@ int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
     CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
-  CK(launch_stage<T>(ctx->order, &maps, I, nullptr, ctx->units, ctx->nunits, mode,
+  CK(launch_stage<T>(ctx->order, ctx->shape.cols, &maps, I, nullptr, ctx->units, ctx->nunits, mode,
                      ctx->shape.boxw, 0, ctx->derr, ctx->st),
      "stage kernel");
   if (ctx->timing) {
@@ -478,6 +478,50 @@ int check_field(swm_ctx* ctx, const swm_field* f) {
 }
 
 double* tmpf(swm_ctx* c, int k) { return c->tmp + (long long)k * c->g64.fs; }
+
+// Work split of the fused stage kernel for consumer width cols (TMA kernel;
+// the FP64 kernel keeps its own width): the column strips fix the narrowest
+// TMA box that covers every strip from its aligned start; the box fixes the
+// shared memory and so the resident CTAs per SM, which sets the number of
+// row segments.  Replaces the context's units and drops its captured graphs.
+int stage_layout(swm_ctx* ctx, int cols) {
+  std::string why;
+  StageShape sh = ctx->shape;
+  const SbpC& tab = kTables[sbp_index(ctx->order)];
+  if (sh.tma) {
+    const int bmax = ctx->prec == SWM_FP32_FUSED ? stage_boxw_max<float>(cols) : stage_boxw_max<double>(cols);
+    if (bmax <= 0) return fail(ctx, SWM_E_INVALID, "no stage kernel of that width");
+    std::vector<WorkUnit> strips;
+    if (!make_units(tab, ctx->n, cols, 1, strips, why)) return fail(ctx, SWM_E_INVALID, why);
+    const int al = 16 / ctx->elt;
+    int bw = al;
+    for (const WorkUnit& w : strips) {
+      const int cal = w.cl0 & ~(al - 1);
+      bw = std::max(bw, (w.cl1 - cal + al - 1) / al * al);
+    }
+    if (bw > bmax) return fail(ctx, SWM_E_INVALID, "work split exceeds the TMA box");
+    sh.cols = cols;
+    sh.boxw = bw;
+    sh.ctas_per_sm = ctx->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ctx->order, bw, cols)
+                                                 : stage_occupancy<double>(ctx->order, bw, cols);
+  }
+  std::vector<WorkUnit> units;
+  if (!make_units(tab, ctx->n, sh.cols, std::max(1, sh.ctas_per_sm) * ctx->num_sms, units, why))
+    return fail(ctx, SWM_E_INVALID, why);
+  CK(cudaStreamSynchronize(ctx->st), "sync");
+  WorkUnit* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(WorkUnit) * units.size()), "alloc");
+  cudaError_t e = cudaMemcpy(d, units.data(), sizeof(WorkUnit) * units.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); return cuda_fail(ctx, e, "copy units"); }
+  if (ctx->units) cudaFree(ctx->units);
+  ctx->units = d;
+  ctx->nunits = (int)units.size();
+  ctx->shape = sh;
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+  ctx->graphs.clear();
+  if (ctx->ad_graph) { cudaGraphExecDestroy(ctx->ad_graph); ctx->ad_graph = nullptr; }
+  return SWM_OK;
+}
 
 // metric fields of the context precision (NMETRIC fields)
 template <class T>
@@ -740,7 +784,6 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   ctx->g64 = ctx->g;
   std::string why;
   if (!build_topology(ctx->topo, why)) { free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why); }
-  std::vector<WorkUnit> units;
   cudaError_t e;
 #define CKC(call, where)                                                              \
   do {                                                                                \
@@ -782,37 +825,13 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     return fail(nullptr, SWM_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   }
   CKC(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device), "SM count");
-  if (ctx->shape.tma) {
-    // the column strips alone fix the narrowest TMA box covering every
-    // strip from its aligned start; the box fixes shared memory and so the
-    // resident CTAs per SM, which sets the number of row segments
-    std::vector<WorkUnit> strips;
-    if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->shape.cols, 1, strips, why)) {
-      free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
-    }
-    const int al = 16 / ctx->elt;
-    int bw = al;
-    for (const WorkUnit& w : strips) {
-      const int cal = w.cl0 & ~(al - 1);
-      bw = std::max(bw, (w.cl1 - cal + al - 1) / al * al);
-    }
-    if (bw > ctx->shape.boxw) {
-      free_ctx(ctx);
-      return fail(nullptr, SWM_E_INVALID, "work split exceeds the TMA box");
-    }
-    ctx->shape.boxw = bw;
-    ctx->shape.ctas_per_sm = ctx->prec == SWM_FP32_FUSED ? stage_occupancy<float>(od, bw)
-                                                         : stage_occupancy<double>(od, bw);
-  }
-  if (!make_units(kTables[sbp_index(od)], ctx->n, ctx->shape.cols,
-                  std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms, units, why)) {
-    free_ctx(ctx); return fail(nullptr, SWM_E_INVALID, why);
-  }
-  ctx->nunits = (int)units.size();
   CKC(cudaMalloc(&ctx->derr, sizeof(int)), "alloc");
   CKC(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st), "memset");
-  CKC(cudaMalloc(&ctx->units, sizeof(WorkUnit) * units.size()), "alloc");
-  CKC(cudaMemcpyAsync(ctx->units, units.data(), sizeof(WorkUnit) * units.size(), cudaMemcpyHostToDevice, ctx->st), "copy");
+  if (int rc = stage_layout(ctx, ctx->shape.cols)) {
+    why = ctx->err;
+    free_ctx(ctx);
+    return fail(nullptr, rc, why);
+  }
   CKC(launch_geometry(ctx->g64, ctx->N, cfg->radius, cfg->omega, cfg->rotation_axis, ctx->m64, ctx->qw, ctx->st), "geometry");
   if (ctx->prec == SWM_FP32_FUSED) {
     CKC(cudaMalloc(&ctx->m32, sizeof(float) * NMETRIC * ctx->fs), "alloc");
@@ -1677,7 +1696,7 @@ int ens_capture(swm_ensemble* ens) {
   ECK(cudaStreamBeginCapture(ens->st, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
-    e = launch_stage<T>(ens->order, nullptr, InstDev<T>{}, I + i * ens->nmem, ens->dunits,
+    e = launch_stage<T>(ens->order, ens->cols, nullptr, InstDev<T>{}, I + i * ens->nmem, ens->dunits,
                         ens->nunits, MODE_RK1 + i, ens->boxw, ens->grid, derr, ens->st);
     if (e == cudaSuccess)
       e = launch_edge<T>(InstDev<T>{}, I + i * ens->nmem, ens->nmem, ens->max_n, tp, MODE_RK1 + i,
@@ -1767,8 +1786,8 @@ int swm_ensemble_create(const swm_config* base, int nmembers, const int* member_
   if (e != cudaSuccess)
     return bail(e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
                 std::string("ensemble alloc: ") + cudaGetErrorString(e));
-  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw)
-                                         : stage_occupancy<double>(ens->order, ens->boxw);
+  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw, ens->cols)
+                                         : stage_occupancy<double>(ens->order, ens->boxw, ens->cols);
   // default tile shape: whole-panel strips on persistent CTAs (FP32) or one
   // CTA per unit of 64 rows (FP64); swm_ensemble_tune measures the others
   const bool f32 = ens->prec == SWM_FP32_FUSED;
@@ -2546,6 +2565,69 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
   std::vector<float> f(np);
   for (size_t k = 0; k < np; ++k) f[k] = (float)d[k];
   return write_record(ctx, file, rec_num, f.data(), np);
+}
+
+// ------------------------------------------------------------ tuning
+int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
+                   double* ms_out) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (steps < 1 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or steps");
+  cudaSetDevice(ctx->cfg.device);
+  if (!ctx->shape.tma) {   // the FP64 kernel has one width
+    if (cols_out) *cols_out = ctx->shape.cols;
+    if (ms_out) *ms_out = 0.0;
+    return SWM_OK;
+  }
+  swm_state* x = nullptr;
+  if (int rc = swm_state_create_similar(ctx, s, &x)) return rc;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int start = ctx->shape.cols;
+  int best = start, rc = SWM_OK;
+  double best_ms = 1e30;
+  for (int w : kStageWidths) {
+    if (stage_layout(ctx, w) != SWM_OK) continue;   // this width cannot cover the grid
+    std::vector<float> ms;
+    for (int k = -2; k < steps && rc == SWM_OK; ++k) {   // two untimed steps capture the graph
+      rc = copy_state(ctx, x, s);
+      if (rc == SWM_OK && cudaEventRecord(a, ctx->st) != cudaSuccess) rc = cuda_fail(ctx, cudaGetLastError(), "event");
+      if (rc == SWM_OK) rc = swm_rk4_step(ctx, x, dt, 1);
+      if (rc == SWM_OK && cudaEventRecord(b, ctx->st) != cudaSuccess) rc = cuda_fail(ctx, cudaGetLastError(), "event");
+      if (rc == SWM_OK) rc = sync_check(ctx, ctx->st);
+      float t = 0.0f;
+      if (rc == SWM_OK && k >= 0 && cudaEventElapsedTime(&t, a, b) == cudaSuccess) ms.push_back(t);
+    }
+    if (rc != SWM_OK) break;
+    std::sort(ms.begin(), ms.end());
+    const double med = ms.empty() ? 1e30 : ms[ms.size() / 2];
+    if (med < best_ms) { best_ms = med; best = w; }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  swm_state_free(x);
+  const int rc2 = stage_layout(ctx, rc == SWM_OK ? best : start);
+  if (rc != SWM_OK) return rc;
+  if (rc2 != SWM_OK) return rc2;
+  if (cols_out) *cols_out = best;
+  if (ms_out) *ms_out = best_ms;
+  return SWM_OK;
+}
+
+int swm_stage_width(swm_ctx* ctx, int* cols) {
+  if (!ctx || !cols) return fail(ctx, SWM_E_INVALID, "null argument");
+  *cols = ctx->shape.cols;
+  return SWM_OK;
+}
+
+int swm_set_stage_width(swm_ctx* ctx, int cols) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  cudaSetDevice(ctx->cfg.device);
+  if (!ctx->shape.tma) {
+    if (cols == ctx->shape.cols) return SWM_OK;
+    return fail(ctx, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
+  }
+  return stage_layout(ctx, cols);
 }
 
 }  // extern "C"

@@ -1,52 +1,62 @@
-// swm_stage_f32.cu -- float instantiation: the TMA-pipelined fused stage
-// kernel (swm_stage_tma.cuh) and the cube-edge kernel.
+// swm_stage_f32.cu -- float: the dispatch of the TMA-pipelined fused stage
+// kernel (swm_stage_tma.cuh) over its consumer widths (instantiated in
+// swm_stage_f32_w*.cu) and the cube-edge kernel.
 #include "swm_launch.h"
 #include "swm_stage_tma.cuh"
 
 namespace swm {
 
 template <>
-cudaError_t launch_stage<float>(int order, const StageMaps* maps, const InstDev<float>& one,
-                                const InstDev<float>* many, const WorkUnit* units, int nunits,
-                                int mode, int boxw, int grid, int* err, cudaStream_t st) {
+cudaError_t launch_stage<float>(int order, int cols, const StageMaps* maps,
+                                const InstDev<float>& one, const InstDev<float>* many,
+                                const WorkUnit* units, int nunits, int mode, int boxw, int grid,
+                                int* err, cudaStream_t st) {
   static const StageMaps kNone{};
   const StageMaps& m = maps ? *maps : kNone;
-  switch (order) {
-    case 21: return launch_stage_tma_ord<float, 21>(m, one, many, units, nunits, mode, boxw, grid, err, st);
-    case 42: return launch_stage_tma_ord<float, 42>(m, one, many, units, nunits, mode, boxw, grid, err, st);
-    case 43: return launch_stage_tma_ord<float, 43>(m, one, many, units, nunits, mode, boxw, grid, err, st);
-    case 63: return launch_stage_tma_ord<float, 63>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+  switch (cols) {
+    case 96: return stage_f32_launch<96>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 128: return stage_f32_launch<128>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 160: return stage_f32_launch<160>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 192: return stage_f32_launch<192>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <>
-int stage_occupancy<float>(int order, int boxw) {
-  switch (order) {
-    case 21: return stage_tma_occupancy<float, 21>(boxw);
-    case 42: return stage_tma_occupancy<float, 42>(boxw);
-    case 43: return stage_tma_occupancy<float, 43>(boxw);
-    default: return stage_tma_occupancy<float, 63>(boxw);
+int stage_occupancy<float>(int order, int boxw, int cols) {
+  switch (cols) {
+    case 96: return stage_f32_occupancy<96>(order, boxw);
+    case 128: return stage_f32_occupancy<128>(order, boxw);
+    case 160: return stage_f32_occupancy<160>(order, boxw);
+    case 192: return stage_f32_occupancy<192>(order, boxw);
+    default: return 0;
+  }
+}
+
+template <>
+int stage_boxw_max<float>(int cols) {
+  switch (cols) {
+    case 96: return TmaLayout<float, 42, 96>::BOXW_MAX;
+    case 128: return TmaLayout<float, 42, 128>::BOXW_MAX;
+    case 160: return TmaLayout<float, 42, 160>::BOXW_MAX;
+    case 192: return TmaLayout<float, 42, 192>::BOXW_MAX;
+    default: return 0;
   }
 }
 
 template <>
 cudaError_t prepare_stage<float>(int order, StageShape* shape) {
-  cudaError_t e;
-  switch (order) {
-    case 21: e = prepare_stage_tma_ord<float, 21>(); break;
-    case 42: e = prepare_stage_tma_ord<float, 42>(); break;
-    case 43: e = prepare_stage_tma_ord<float, 43>(); break;
-    case 63: e = prepare_stage_tma_ord<float, 63>(); break;
-    default: return cudaErrorInvalidValue;
-  }
+  cudaError_t e = stage_f32_prepare<96>(order);
+  if (e == cudaSuccess) e = stage_f32_prepare<128>(order);
+  if (e == cudaSuccess) e = stage_f32_prepare<160>(order);
+  if (e == cudaSuccess) e = stage_f32_prepare<192>(order);
   if (e != cudaSuccess) return e;
-  shape->cols = TMA_CONS;
+  shape->cols = TMA_CONS_DEFAULT;
   shape->tma = 1;
-  shape->boxw = TmaLayout<float, 42>::BOXW_MAX;
-  shape->rps = TmaLayout<float, 42>::RPS;
-  shape->nf = TmaLayout<float, 42>::NF;
-  shape->ctas_per_sm = stage_occupancy<float>(order, shape->boxw);
+  shape->boxw = stage_boxw_max<float>(shape->cols);
+  shape->rps = TmaLayout<float, 42, TMA_CONS_DEFAULT>::RPS;
+  shape->nf = TmaLayout<float, 42, TMA_CONS_DEFAULT>::NF;
+  shape->ctas_per_sm = stage_occupancy<float>(order, shape->boxw, shape->cols);
   return cudaGetLastError();
 }
 

@@ -7,9 +7,11 @@
 namespace swm {
 
 template <>
-cudaError_t launch_stage<double>(int order, const StageMaps* maps, const InstDev<double>& one,
-                                 const InstDev<double>* many, const WorkUnit* units, int nunits,
-                                 int mode, int boxw, int grid, int* err, cudaStream_t st) {
+cudaError_t launch_stage<double>(int order, int cols, const StageMaps* maps,
+                                 const InstDev<double>& one, const InstDev<double>* many,
+                                 const WorkUnit* units, int nunits, int mode, int boxw, int grid,
+                                 int* err, cudaStream_t st) {
+  (void)cols;
   (void)err;
   (void)grid;
   (void)boxw;
@@ -33,8 +35,8 @@ static int v1_occupancy() {
 
 template <>
 cudaError_t prepare_stage<double>(int order, StageShape* shape) {
-  cudaError_t e = launch_stage<double>(order, nullptr, InstDev<double>{}, nullptr, nullptr, 0,
-                                       MODE_APPLY, 0, 0, nullptr, nullptr);
+  cudaError_t e = launch_stage<double>(order, STAGE_BW, nullptr, InstDev<double>{}, nullptr, nullptr,
+                                       0, MODE_APPLY, 0, 0, nullptr, nullptr);
   int* ctas_per_sm = &shape->ctas_per_sm;
   if (e != cudaSuccess) return e;
   switch (order) {
@@ -50,8 +52,15 @@ cudaError_t prepare_stage<double>(int order, StageShape* shape) {
 }
 
 template <>
-int stage_occupancy<double>(int order, int boxw) {
+int stage_boxw_max<double>(int cols) {
+  (void)cols;
+  return 0;
+}
+
+template <>
+int stage_occupancy<double>(int order, int boxw, int cols) {
   (void)boxw;
+  (void)cols;
   switch (order) {
     case 21: return v1_occupancy<double, 21>();
     case 42: return v1_occupancy<double, 42>();

@@ -80,13 +80,17 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
       : "memory");
 }
-__device__ __forceinline__ void consumers_sync() {  // the 128 consumer threads only
-  asm volatile("bar.sync 1, 128;" ::: "memory");
-}
-
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legal wait
-constexpr int TMA_CONS = 128;                     // consumer threads, one per column
-constexpr int TMA_THREADS = TMA_CONS + 32;        // + one producer warp
+// Consumer threads per CTA (one per column of the unit's strip): a template
+// parameter CONS of the kernel, one of the widths below; a context picks one
+// (default 128, or the fastest for its grid, see swm_tune_stage).  The
+// strip width changes only the work split, not any node's arithmetic.
+constexpr int TMA_CONS_DEFAULT = 128;
+
+template <int CONS>
+__device__ __forceinline__ void consumers_sync() {  // the consumer threads only
+  asm volatile("bar.sync 1, %0;" ::"n"(CONS) : "memory");
+}
 
 
 
@@ -101,7 +105,7 @@ constexpr int TMA_THREADS = TMA_CONS + 32;        // + one producer warp
 // what the owning thread reads RMAX rows later (ut, vt, J)
 enum { X_KE = 0, X_V, X_GU, X_UT, X_VT, X_J, NX_FIELDS };
 
-template <class T, int ORD>
+template <class T, int ORD, int CONS>
 struct TmaLayout {
   static constexpr int RPS = SWM_TMA_RPS;    // rows per pipeline stage
   static constexpr int NST = SWM_TMA_NST;    // pipeline stages
@@ -109,10 +113,10 @@ struct TmaLayout {
   static constexpr int WS = 2 * RMAX + 1;    // y window (registers): rows j-RMAX..j+RMAX
   static constexpr int RBX = RMAX + 2;       // x-ring rows: row r written, read at r+RMAX
   static constexpr int ALIGN = 16 / (int)sizeof(T);
-  static constexpr int BOXW_MAX = TMA_CONS + ALIGN;  // widest box (16-byte multiple)
+  static constexpr int BOXW_MAX = CONS + ALIGN;  // widest box (16-byte multiple)
   static constexpr int NF = 2;               // metric f, rJ of the finished rows
   static constexpr size_t head = 256;        // mbarriers + abort flag
-  static constexpr size_t xring = sizeof(T) * RBX * NX_FIELDS * TMA_CONS;
+  static constexpr size_t xring = sizeof(T) * RBX * NX_FIELDS * CONS;
   __host__ __device__ static constexpr size_t r128(size_t b) { return (b + 127) / 128 * 128; }
   // stage layout for a box width bw: in(3) met(4) metf(2) base(3) acc(3) lo(3) hs(1)
   struct Stage {
@@ -265,15 +269,15 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
 // A unit takes its tensor maps from its instance (InstDev::maps, global
 // memory; batched launches) or from the kernel parameter (one instance).
 // slot_bw is the widest box width of the launch (ring slot size).
-template <class T, int ORD, int MODE>
-__global__ void __launch_bounds__(TMA_THREADS)
+template <class T, int ORD, int MODE, int CONS>
+__global__ void __launch_bounds__(CONS + 32)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
                      const InstDev<T>* many, const WorkUnit* units, int nunits, int slot_bw,
                      int* err) {
-  using L = TmaLayout<T, ORD>;
+  using L = TmaLayout<T, ORD, CONS>;
   constexpr int RMAX = L::RMAX, RPS = L::RPS, NST = L::NST, AL = L::ALIGN, WS = L::WS,
                 RBX = L::RBX;
-  constexpr int XS = NX_FIELDS * TMA_CONS;   // x-ring slot stride
+  constexpr int XS = NX_FIELDS * CONS;   // x-ring slot stride
   constexpr int NE = Ord<ORD>::NE, NW = Ord<ORD>::NW;
   constexpr bool FP32 = sizeof(T) == 4;
   constexpr bool needB = MODE == MODE_RK1 || MODE == MODE_RK2 || MODE == MODE_RK3 ||
@@ -296,7 +300,7 @@ __global__ void __launch_bounds__(TMA_THREADS)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], TMA_CONS / 32);
+      mbar_init(&empty[s], CONS / 32);
     }
     *abort_flag = 0;
     mbar_fence_init();
@@ -304,8 +308,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
   __syncthreads();
 
   // ------------------------------------------------------------ producer
-  if (tid >= TMA_CONS) {
-    if (tid == TMA_CONS) {
+  if (tid >= CONS) {
+    if (tid == CONS) {
       int gc = 0;   // chunks issued over all units of this CTA
       for (int u = blockIdx.x; u < nunits && !*abort_flag; u += gridDim.x) {
         const WorkUnit wu = units[u];
@@ -379,7 +383,7 @@ __global__ void __launch_bounds__(TMA_THREADS)
   const int e_in = eo.in, e_met = eo.met, e_metf = eo.metf, e_base = eo.base, e_acc = eo.acc,
             e_lo = eo.lo, e_hs = eo.hs;
   // every consumer is done with the previous unit's x-ring rows
-  if (u != (int)blockIdx.x) consumers_sync();
+  if (u != (int)blockIdx.x) consumers_sync<CONS>();
   const int col = wu.cl0 + t;
   const bool ld = col < wu.cl1;
   const bool own = col >= wu.i0 && col < wu.i1;
@@ -442,39 +446,39 @@ __global__ void __launch_bounds__(TMA_THREADS)
         if (hasHs) ke = ke + grav * sx[e_hs + (0 * RPS + q) * bw];
         gv = J * (h * vt);
         T* xw = xring + (r % RBX) * XS + t;
-        xw[X_KE * TMA_CONS] = ke;
-        xw[X_V * TMA_CONS] = v;
-        xw[X_GU * TMA_CONS] = J * (h * ut);
-        xw[X_UT * TMA_CONS] = ut;
-        xw[X_VT * TMA_CONS] = vt;
-        xw[X_J * TMA_CONS] = J;
+        xw[X_KE * CONS] = ke;
+        xw[X_V * CONS] = v;
+        xw[X_GU * CONS] = J * (h * ut);
+        xw[X_UT * CONS] = ut;
+        xw[X_VT * CONS] = vt;
+        xw[X_J * CONS] = J;
       }
       // push row r into the window: w[i] holds row r-2RMAX+i = j-RMAX+i
 #pragma unroll
       for (int i = 0; i < WS - 1; ++i) { yke[i] = yke[i + 1]; yu[i] = yu[i + 1]; ygv[i] = ygv[i + 1]; }
       yke[WS - 1] = ke; yu[WS - 1] = u; ygv[WS - 1] = gv;
-      consumers_sync();
+      consumers_sync<CONS>();
       if (*abort_flag || !own || j < j0u || j >= j1u) continue;
       const T* xr = xring + (j % RBX) * XS + t;      // row j, this thread's column
       T dxke, dxv, dxgu;
       if (xint) {
-        dxke = d_interior<ORD, T>([&](int o) { return xr[X_KE * TMA_CONS + o]; });
-        dxv = d_interior<ORD, T>([&](int o) { return xr[X_V * TMA_CONS + o]; });
-        dxgu = d_interior<ORD, T>([&](int o) { return xr[X_GU * TMA_CONS + o]; });
+        dxke = d_interior<ORD, T>([&](int o) { return xr[X_KE * CONS + o]; });
+        dxv = d_interior<ORD, T>([&](int o) { return xr[X_V * CONS + o]; });
+        dxgu = d_interior<ORD, T>([&](int o) { return xr[X_GU * CONS + o]; });
       } else {
         dxke = T(0); dxv = T(0); dxgu = T(0);
 #pragma unroll
         for (int m = 0; m < NW; ++m) {
           const int o = xs + m - col;
-          dxke += cx[m] * xr[X_KE * TMA_CONS + o];
-          dxv += cx[m] * xr[X_V * TMA_CONS + o];
-          dxgu += cx[m] * xr[X_GU * TMA_CONS + o];
+          dxke += cx[m] * xr[X_KE * CONS + o];
+          dxv += cx[m] * xr[X_V * CONS + o];
+          dxgu += cx[m] * xr[X_GU * CONS + o];
         }
       }
       const T dyke = ydiff<ORD, T, WS>(yke, j, n);
       const T dyu = ydiff<ORD, T, WS>(yu, j, n);
       const T dygv = ydiff<ORD, T, WS>(ygv, j, n);
-      const T J = xr[X_J * TMA_CONS];
+      const T J = xr[X_J * CONS];
       const T rJ = sx[e_metf + (1 * RPS + q) * bw];
       const T gx = dxke * ghs, gy = dyke * ghs;
       const T zeta = (dxv - dyu) * rJ;
@@ -497,8 +501,8 @@ __global__ void __launch_bounds__(TMA_THREADS)
         continue;
       }
       T k0, k1, k2;
-      node_tendency<T>(gx, gy, zeta, dv, sx[e_metf + (0 * RPS + q) * bw], J, xr[X_UT * TMA_CONS],
-                       xr[X_VT * TMA_CONS], k0, k1, k2);
+      node_tendency<T>(gx, gy, zeta, dv, sx[e_metf + (0 * RPS + q) * bw], J, xr[X_UT * CONS],
+                       xr[X_VT * CONS], k0, k1, k2);
       const int g = gcol + j * P;
       const int qb = q * bw;
       rk_store<T, MODE>(outp, accp, bop, blp, g, k0, sx + qb, e_base, e_acc, e_lo, RPS * bw, c_in, c_acc);
@@ -511,14 +515,14 @@ __global__ void __launch_bounds__(TMA_THREADS)
   }  // units
 }
 
-template <class T, int ORD, int MODE>
+template <class T, int ORD, int MODE, int CONS>
 cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
                                   const InstDev<T>* many, const WorkUnit* units, int nunits,
                                   int boxw, int grid, int* err, cudaStream_t st) {
-  using L = TmaLayout<T, ORD>;
+  using L = TmaLayout<T, ORD, CONS>;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, MODE>,
+    cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, MODE, CONS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L::smem_bytes(L::BOXW_MAX));
     if (e != cudaSuccess) return e;
@@ -527,44 +531,82 @@ cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
   if (nunits <= 0) return cudaSuccess;
   if (boxw < 1 || boxw > L::BOXW_MAX) return cudaErrorInvalidValue;
   const int g = (grid > 0 && grid < nunits) ? grid : nunits;
-  stage_tma_kernel<T, ORD, MODE><<<g, TMA_THREADS, L::smem_bytes(boxw), st>>>(
+  stage_tma_kernel<T, ORD, MODE, CONS><<<g, CONS + 32, L::smem_bytes(boxw), st>>>(
       maps, one, many, units, nunits, boxw, err);
   return cudaGetLastError();
 }
 
-template <class T, int ORD>
+template <class T, int ORD, int CONS>
 cudaError_t launch_stage_tma_ord(const StageMaps& maps, const InstDev<T>& one,
                                  const InstDev<T>* many, const WorkUnit* units, int nunits,
                                  int mode, int boxw, int grid, int* err, cudaStream_t st) {
   switch (mode) {
-    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 // configure every mode (outside any capture)
-template <class T, int ORD>
+template <class T, int ORD, int CONS>
 cudaError_t prepare_stage_tma_ord() {
   static const StageMaps kNone{};
   for (int m = MODE_APPLY; m <= MODE_RK4; ++m) {
-    cudaError_t e = launch_stage_tma_ord<T, ORD>(kNone, InstDev<T>{}, nullptr, nullptr, 0, m,
-                                                 TmaLayout<T, ORD>::BOXW_MAX, 0, nullptr, nullptr);
+    cudaError_t e = launch_stage_tma_ord<T, ORD, CONS>(kNone, InstDev<T>{}, nullptr, nullptr, 0, m,
+                                                       TmaLayout<T, ORD, CONS>::BOXW_MAX, 0,
+                                                       nullptr, nullptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
 // resident CTAs per SM at box width bw
-template <class T, int ORD>
+template <class T, int ORD, int CONS>
 int stage_tma_occupancy(int bw) {
   int blocks = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_tma_kernel<T, ORD, MODE_RK2>,
-                                                TMA_THREADS, TmaLayout<T, ORD>::smem_bytes(bw));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_tma_kernel<T, ORD, MODE_RK2, CONS>,
+                                                CONS + 32, TmaLayout<T, ORD, CONS>::smem_bytes(bw));
   return blocks;
 }
+
+// The FP32 stage kernel of one consumer width CONS for every SBP order
+// (instantiated by swm_stage_f32_w<CONS>.cu).
+template <int CONS>
+struct StageF32Width {
+  static cudaError_t launch(int order, const StageMaps& m, const InstDev<float>& one,
+                            const InstDev<float>* many, const WorkUnit* units, int nunits,
+                            int mode, int boxw, int grid, int* err, cudaStream_t st) {
+    switch (order) {
+      case 21: return launch_stage_tma_ord<float, 21, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 42: return launch_stage_tma_ord<float, 42, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 43: return launch_stage_tma_ord<float, 43, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 63: return launch_stage_tma_ord<float, 63, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  static int occupancy(int order, int boxw) {
+    switch (order) {
+      case 21: return stage_tma_occupancy<float, 21, CONS>(boxw);
+      case 42: return stage_tma_occupancy<float, 42, CONS>(boxw);
+      case 43: return stage_tma_occupancy<float, 43, CONS>(boxw);
+      default: return stage_tma_occupancy<float, 63, CONS>(boxw);
+    }
+  }
+  static cudaError_t prepare(int order) {
+    switch (order) {
+      case 21: return prepare_stage_tma_ord<float, 21, CONS>();
+      case 42: return prepare_stage_tma_ord<float, 42, CONS>();
+      case 43: return prepare_stage_tma_ord<float, 43, CONS>();
+      case 63: return prepare_stage_tma_ord<float, 63, CONS>();
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  static constexpr int boxw_max() { return TmaLayout<float, 42, CONS>::BOXW_MAX; }
+  static constexpr int rps() { return TmaLayout<float, 42, CONS>::RPS; }
+  static constexpr int nf() { return TmaLayout<float, 42, CONS>::NF; }
+};
 
 }  // namespace swm

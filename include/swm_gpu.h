@@ -385,6 +385,20 @@ int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char
  * panel) of state component 0 (h), 1 (u) or 2 (v). */
 int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const char* file, int rec_num);
 
+/* ---------------------------------------------------------------------- */
+/* Launch-shape tuning (no reference counterpart)                         */
+/* ---------------------------------------------------------------------- */
+/* The FP32 stage kernel comes in consumer widths 96, 128, 160 and 192
+ * columns per CTA; the width changes how the panels are split into work
+ * units, not any node's arithmetic (results are bit-identical).  The best
+ * width depends on the grid: swm_tune_stage times `steps` RK4 steps of dt
+ * per width on a copy of s (s is not changed), keeps the fastest, and
+ * returns it and its median step time.  FP64 contexts have one width. */
+int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
+                   double* ms_out);
+int swm_stage_width(swm_ctx* ctx, int* cols);
+int swm_set_stage_width(swm_ctx* ctx, int cols);
+
 #ifdef __cplusplus
 }
 #endif

@@ -166,3 +166,34 @@ def test_state_roundtrip_fp32_pair_is_exact_to_fp64_split(cfg1):
     gh, gu, gv = s.download()
     # (hi, lo) float pairs carry ~48 significant bits
     assert np.max(np.abs(gh - h) / np.abs(h)) < 1e-13
+
+
+@pytest.mark.parametrize("order,N", [(42, 48), (63, 64), (43, 40)])
+def test_stage_widths_are_bit_identical(order, N):
+    """The FP32 stage kernel's consumer widths split the panels differently
+    but give bit-identical steps; the tuner keeps the input state and picks
+    one of the widths."""
+    h, u, v, _ = initial.balanced_zonal(N, 2, 16)
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=order, precision="fp32"))
+    assert op.stage_width == 128
+    x0 = op.create_stvec()
+    x0.upload(h, u, v)
+    ref = None
+    for w in (96, 128, 160, 192):
+        op.stage_width = w
+        assert op.stage_width == w
+        x = x0.create_similar()
+        x.assign_s1v1(1.0, x0)
+        swm.RK4().step(x, op, 300.0, 3)
+        got = x.download()
+        if ref is None:
+            ref = got
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+    before = x0.download()
+    w, ms = op.tune_stage(x0, 300.0, steps=3)
+    assert w in (96, 128, 160, 192) and ms > 0 and op.stage_width == w
+    for a, b in zip(x0.download(), before):
+        assert np.array_equal(a, b)
+    with pytest.raises(swm.SwmError):
+        op.stage_width = 100
