@@ -431,7 +431,7 @@ def run_gpu_arm(args):
     h, u, v, info = _state(w)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    tuned = {"width": 128}
+    tuned = {"width": 128, "seg_rows": 0, "grid": 0}
 
     def time_steps(prec, steps, warmup, kernel_timing=False):
         """Every timed step starts from the initial state (restored outside
@@ -441,8 +441,8 @@ def run_gpu_arm(args):
         op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=ORDER, precision=prec, device=local))
         s0 = op.create_stvec()
         s0.upload(h, u, v)
-        if prec == "fp32":   # set-up: pick the stage kernel's fastest consumer width
-            tuned["width"], _ = op.tune_stage(s0, DT, 10)
+        if prec == "fp32":   # set-up: pick the stage kernel's fastest launch shape
+            tuned.update(op.tune_stage(s0, DT, 10))
         s = op.create_stvec()
         s.assign_s1v1(1.0, s0)
         ts = swm.RK4()
@@ -569,7 +569,7 @@ def run_gpu_arm(args):
                                                "metric precompute)",
                        "N": N, "sbp": "d%d" % ORDER, "dt_s": DT, "nodes_per_field": npts,
                        "l2": "256 MB buffer written between timed steps",
-                       "stage_width": tuned["width"],
+                       "stage_shape": {k: tuned[k] for k in ("width", "seg_rows", "grid")},
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "e2e": {"value": round(e2e_val, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,

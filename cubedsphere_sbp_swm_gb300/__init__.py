@@ -161,23 +161,24 @@ class OperatorSWM:
         laplace_ah_sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58), edge-synced."""
         self._check(self._L.swm_laplace(self._h, out._h, f._h, int(narrow_order)))
 
-    def tune_stage(self, v: "StvecSWM", dt: float, steps: int = 10):
-        """Time the stage kernel's consumer widths on a copy of v and keep the
-        fastest (bit-identical results); returns (width, median step ms)."""
-        cols, ms = ctypes.c_int(), ctypes.c_double()
-        self._check(self._L.swm_tune_stage(self._h, v._h, float(dt), int(steps),
-                                           ctypes.byref(cols), ctypes.byref(ms)))
-        return cols.value, ms.value
+    def tune_stage(self, v: "StvecSWM", dt: float, steps: int = 10) -> dict:
+        """Time the stage kernel's launch shapes (consumer width, rows per
+        unit, persistent grid) on a copy of v and keep the fastest
+        (bit-identical results)."""
+        c, r, g, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._check(self._L.swm_tune_stage(self._h, v._h, float(dt), int(steps), ctypes.byref(c),
+                                           ctypes.byref(r), ctypes.byref(g), ctypes.byref(ms)))
+        return {"width": c.value, "seg_rows": r.value, "grid": g.value, "ms": ms.value}
 
     @property
-    def stage_width(self) -> int:
-        cols = ctypes.c_int()
-        self._check(self._L.swm_stage_width(self._h, ctypes.byref(cols)))
-        return cols.value
+    def stage_shape(self) -> dict:
+        c, r, g, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.swm_get_stage_shape(self._h, ctypes.byref(c), ctypes.byref(r),
+                                                ctypes.byref(g), ctypes.byref(n)))
+        return {"width": c.value, "seg_rows": r.value, "grid": g.value, "units": n.value}
 
-    @stage_width.setter
-    def stage_width(self, cols: int):
-        self._check(self._L.swm_set_stage_width(self._h, int(cols)))
+    def set_stage_shape(self, width: int = 128, seg_rows: int = 0, grid: int = 0):
+        self._check(self._L.swm_set_stage_shape(self._h, int(width), int(seg_rows), int(grid)))
 
     def model_step(self, v0: "StvecSWM", dt: float, nsteps: int = 1):
         """nsteps of the drivers' time step (ts2_mod.f90:143-146): RK4, then the

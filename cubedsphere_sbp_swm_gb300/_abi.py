@@ -46,7 +46,7 @@ EXPORTS = (
     "swm_diffusion_set", "swm_apply_diffusion", "swm_diffusion_step", "swm_model_step",
     "swm_laplace", "swm_latlon_create", "swm_latlon_destroy", "swm_latlon_regrid_field",
     "swm_latlon_regrid_vector", "swm_latlon_regrid_state", "swm_latlon_write", "swm_paneled_write",
-    "swm_tune_stage", "swm_stage_width", "swm_set_stage_width",
+    "swm_tune_stage", "swm_get_stage_shape", "swm_set_stage_shape",
 )
 
 
@@ -132,9 +132,10 @@ def load(build_if_missing: bool = True):
     sig("swm_latlon_regrid_state", I, VP, VP, VP, _D, _D, _D)
     sig("swm_latlon_write", I, VP, VP, VP, C, C, C, I)
     sig("swm_paneled_write", I, VP, VP, I, C, I)
-    sig("swm_tune_stage", I, VP, VP, D, I, ctypes.POINTER(I), _D)
-    sig("swm_stage_width", I, VP, ctypes.POINTER(I))
-    sig("swm_set_stage_width", I, VP, I)
+    sig("swm_tune_stage", I, VP, VP, D, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), _D)
+    sig("swm_get_stage_shape", I, VP, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
+        ctypes.POINTER(I))
+    sig("swm_set_stage_shape", I, VP, I, I, I)
     sig("swm_diagnostics", I, VP, VP, _D)
     sig("swm_field_create", I, VP, PP)
     sig("swm_field_free", None, VP)

@@ -197,6 +197,8 @@ struct swm_ctx {
   int* derr = nullptr;          // device error flag of the bounded waits
   int num_sms = 0;
   StageShape shape{};           // launch shape of the fused stage kernel
+  int seg_rows = 0;             // rows per work unit (0: from the occupancy)
+  int stage_grid = 0;           // persistent CTAs (0: one CTA per unit)
   // CUDA graphs of whole steps, keyed by (state, dt, kind): kind 0 RK4 step,
   // 1 RK4 step + diffusion step, 2 diffusion step
   std::map<std::tuple<void*, double, int>, GraphEntry> graphs;
@@ -425,7 +427,7 @@ int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
   CK(launch_stage<T>(ctx->order, ctx->shape.cols, &maps, I, nullptr, ctx->units, ctx->nunits, mode,
-                     ctx->shape.boxw, 0, ctx->derr, ctx->st),
+                     ctx->shape.boxw, ctx->stage_grid, ctx->derr, ctx->st),
      "stage kernel");
   if (ctx->timing) {
     CK(cudaEventRecord(b, ctx->st), "event record");
@@ -483,8 +485,10 @@ double* tmpf(swm_ctx* c, int k) { return c->tmp + (long long)k * c->g64.fs; }
 // the FP64 kernel keeps its own width): the column strips fix the narrowest
 // TMA box that covers every strip from its aligned start; the box fixes the
 // shared memory and so the resident CTAs per SM, which sets the number of
-// row segments.  Replaces the context's units and drops its captured graphs.
-int stage_layout(swm_ctx* ctx, int cols) {
+// row segments unless seg_rows > 0 fixes the rows per unit.  grid > 0 runs
+// the kernel persistently on that many CTAs.  Replaces the context's units
+// and drops its captured graphs.
+int stage_layout(swm_ctx* ctx, int cols, int seg_rows = 0, int grid = 0) {
   std::string why;
   StageShape sh = ctx->shape;
   const SbpC& tab = kTables[sbp_index(ctx->order)];
@@ -506,7 +510,8 @@ int stage_layout(swm_ctx* ctx, int cols) {
                                                  : stage_occupancy<double>(ctx->order, bw, cols);
   }
   std::vector<WorkUnit> units;
-  if (!make_units(tab, ctx->n, sh.cols, std::max(1, sh.ctas_per_sm) * ctx->num_sms, units, why))
+  const int nseg = seg_rows > 0 ? (ctx->n + seg_rows - 1) / seg_rows : 0;
+  if (!make_units(tab, ctx->n, sh.cols, std::max(1, sh.ctas_per_sm) * ctx->num_sms, units, why, nseg))
     return fail(ctx, SWM_E_INVALID, why);
   CK(cudaStreamSynchronize(ctx->st), "sync");
   WorkUnit* d = nullptr;
@@ -517,6 +522,8 @@ int stage_layout(swm_ctx* ctx, int cols) {
   ctx->units = d;
   ctx->nunits = (int)units.size();
   ctx->shape = sh;
+  ctx->seg_rows = seg_rows;
+  ctx->stage_grid = grid;
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
   ctx->graphs.clear();
   if (ctx->ad_graph) { cudaGraphExecDestroy(ctx->ad_graph); ctx->ad_graph = nullptr; }
@@ -2569,12 +2576,14 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 
 // ------------------------------------------------------------ tuning
 int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
-                   double* ms_out) {
+                   int* seg_rows_out, int* grid_out, double* ms_out) {
   if (int rc = check_state(ctx, s)) return rc;
   if (steps < 1 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or steps");
   cudaSetDevice(ctx->cfg.device);
-  if (!ctx->shape.tma) {   // the FP64 kernel has one width
+  if (!ctx->shape.tma) {   // the FP64 kernel has one shape
     if (cols_out) *cols_out = ctx->shape.cols;
+    if (seg_rows_out) *seg_rows_out = ctx->seg_rows;
+    if (grid_out) *grid_out = ctx->stage_grid;
     if (ms_out) *ms_out = 0.0;
     return SWM_OK;
   }
@@ -2583,11 +2592,11 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
   cudaEvent_t a = nullptr, b = nullptr;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  const int start = ctx->shape.cols;
-  int best = start, rc = SWM_OK;
+  const int c0 = ctx->shape.cols, r0 = ctx->seg_rows, g0 = ctx->stage_grid;
+  int bc = c0, br = r0, bg = g0, rc = SWM_OK;
   double best_ms = 1e30;
-  for (int w : kStageWidths) {
-    if (stage_layout(ctx, w) != SWM_OK) continue;   // this width cannot cover the grid
+  auto trial = [&](int cols, int seg, int grid) {
+    if (stage_layout(ctx, cols, seg, grid) != SWM_OK) return;   // shape cannot cover the grid
     std::vector<float> ms;
     for (int k = -2; k < steps && rc == SWM_OK; ++k) {   // two untimed steps capture the graph
       rc = copy_state(ctx, x, s);
@@ -2598,36 +2607,53 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
       float t = 0.0f;
       if (rc == SWM_OK && k >= 0 && cudaEventElapsedTime(&t, a, b) == cudaSuccess) ms.push_back(t);
     }
-    if (rc != SWM_OK) break;
+    if (rc != SWM_OK || ms.empty()) return;
     std::sort(ms.begin(), ms.end());
-    const double med = ms.empty() ? 1e30 : ms[ms.size() / 2];
-    if (med < best_ms) { best_ms = med; best = w; }
+    const double med = ms[ms.size() / 2];
+    if (med < best_ms) { best_ms = med; bc = cols; br = seg; bg = grid; }
+  };
+  // widths x rows per unit (0: one wave of units) x one CTA per unit or a
+  // persistent wave of CTAs
+  const int seg_opts[] = {0, 16, 24, 32, 48, 64, 96};
+  for (int w : kStageWidths) {
+    for (int seg : seg_opts) {
+      if (rc != SWM_OK) break;
+      if (seg >= ctx->n) continue;
+      trial(w, seg, 0);
+      if (rc != SWM_OK || seg == 0) continue;
+      const int wave = std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms;
+      if (ctx->shape.cols == w && ctx->nunits > wave) trial(w, seg, wave);
+    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   swm_state_free(x);
-  const int rc2 = stage_layout(ctx, rc == SWM_OK ? best : start);
+  const int rc2 = rc == SWM_OK ? stage_layout(ctx, bc, br, bg) : stage_layout(ctx, c0, r0, g0);
   if (rc != SWM_OK) return rc;
   if (rc2 != SWM_OK) return rc2;
-  if (cols_out) *cols_out = best;
+  if (cols_out) *cols_out = bc;
+  if (seg_rows_out) *seg_rows_out = br;
+  if (grid_out) *grid_out = bg;
   if (ms_out) *ms_out = best_ms;
   return SWM_OK;
 }
 
-int swm_stage_width(swm_ctx* ctx, int* cols) {
-  if (!ctx || !cols) return fail(ctx, SWM_E_INVALID, "null argument");
-  *cols = ctx->shape.cols;
+int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* nunits) {
+  if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  if (cols) *cols = ctx->shape.cols;
+  if (seg_rows) *seg_rows = ctx->seg_rows;
+  if (grid) *grid = ctx->stage_grid;
+  if (nunits) *nunits = ctx->nunits;
   return SWM_OK;
 }
 
-int swm_set_stage_width(swm_ctx* ctx, int cols) {
+int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  if (seg_rows < 0 || grid < 0) return fail(ctx, SWM_E_INVALID, "shape values must be >= 0");
   cudaSetDevice(ctx->cfg.device);
-  if (!ctx->shape.tma) {
-    if (cols == ctx->shape.cols) return SWM_OK;
+  if (!ctx->shape.tma && cols != ctx->shape.cols)
     return fail(ctx, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
-  }
-  return stage_layout(ctx, cols);
+  return stage_layout(ctx, cols, seg_rows, grid);
 }
 
 }  // extern "C"

@@ -388,16 +388,18 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 /* ---------------------------------------------------------------------- */
 /* Launch-shape tuning (no reference counterpart)                         */
 /* ---------------------------------------------------------------------- */
-/* The FP32 stage kernel comes in consumer widths 96, 128, 160 and 192
- * columns per CTA; the width changes how the panels are split into work
- * units, not any node's arithmetic (results are bit-identical).  The best
- * width depends on the grid: swm_tune_stage times `steps` RK4 steps of dt
- * per width on a copy of s (s is not changed), keeps the fastest, and
- * returns it and its median step time.  FP64 contexts have one width. */
+/* The stage kernel's launch shape: the consumer width of the FP32 kernel
+ * (96, 128, 160 or 192 columns per CTA), the rows per work unit (0: enough
+ * units for one wave of CTAs) and the persistent grid (0: one CTA per unit).
+ * The shape changes how the panels are split into work, not any node's
+ * arithmetic (results are bit-identical).  The best shape depends on the
+ * grid: swm_tune_stage times `steps` RK4 steps of dt per candidate on a copy
+ * of s (s is not changed), keeps the fastest and returns it with its median
+ * step time.  FP64 contexts have one width. */
 int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
-                   double* ms_out);
-int swm_stage_width(swm_ctx* ctx, int* cols);
-int swm_set_stage_width(swm_ctx* ctx, int cols);
+                   int* seg_rows_out, int* grid_out, double* ms_out);
+int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* nunits);
+int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid);
 
 #ifdef __cplusplus
 }

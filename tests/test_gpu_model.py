@@ -169,19 +169,21 @@ def test_state_roundtrip_fp32_pair_is_exact_to_fp64_split(cfg1):
 
 
 @pytest.mark.parametrize("order,N", [(42, 48), (63, 64), (43, 40)])
-def test_stage_widths_are_bit_identical(order, N):
-    """The FP32 stage kernel's consumer widths split the panels differently
-    but give bit-identical steps; the tuner keeps the input state and picks
-    one of the widths."""
+def test_stage_shapes_are_bit_identical(order, N):
+    """The FP32 stage kernel's launch shapes (consumer width, rows per unit,
+    persistent grid) split the panels differently but give bit-identical
+    steps; the tuner keeps the input state and picks one of the shapes."""
     h, u, v, _ = initial.balanced_zonal(N, 2, 16)
     op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=order, precision="fp32"))
-    assert op.stage_width == 128
+    assert op.stage_shape["width"] == 128
     x0 = op.create_stvec()
     x0.upload(h, u, v)
     ref = None
-    for w in (96, 128, 160, 192):
-        op.stage_width = w
-        assert op.stage_width == w
+    for w, seg, grid in ((96, 0, 0), (128, 0, 0), (160, 0, 0), (192, 0, 0), (128, 8, 0),
+                         (128, 8, 7), (192, 16, 3)):
+        op.set_stage_shape(w, seg, grid)
+        sh = op.stage_shape
+        assert (sh["width"], sh["seg_rows"], sh["grid"]) == (w, seg, grid)
         x = x0.create_similar()
         x.assign_s1v1(1.0, x0)
         swm.RK4().step(x, op, 300.0, 3)
@@ -191,9 +193,10 @@ def test_stage_widths_are_bit_identical(order, N):
         for a, b in zip(got, ref):
             assert np.array_equal(a, b)
     before = x0.download()
-    w, ms = op.tune_stage(x0, 300.0, steps=3)
-    assert w in (96, 128, 160, 192) and ms > 0 and op.stage_width == w
+    t = op.tune_stage(x0, 300.0, steps=2)
+    assert t["width"] in (96, 128, 160, 192) and t["ms"] > 0
+    assert op.stage_shape["width"] == t["width"]
     for a, b in zip(x0.download(), before):
         assert np.array_equal(a, b)
     with pytest.raises(swm.SwmError):
-        op.stage_width = 100
+        op.set_stage_shape(100)
