@@ -548,16 +548,22 @@ class Ensemble:
         self._check(self._L.swm_ensemble_set_shape(self._h, int(seg_rows), int(grid)))
 
     def get_shape(self) -> dict:
-        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        a, b, c, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._check(self._L.swm_ensemble_get_shape(self._h, ctypes.byref(a), ctypes.byref(b),
                                                    ctypes.byref(c)))
-        return {"seg_rows": a.value, "grid": b.value, "units": c.value}
+        self._check(self._L.swm_ensemble_get_width(self._h, ctypes.byref(w)))
+        return {"seg_rows": a.value, "grid": b.value, "units": c.value, "width": w.value}
+
+    def set_width(self, cols: int):
+        """Consumer width of the members' FP32 stage kernel (96, 128, 160, 192)."""
+        self._check(self._L.swm_ensemble_set_width(self._h, int(cols)))
 
     def tune(self, steps: int = 5) -> dict:
-        a, b, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        a, b, ms, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
         self._check(self._L.swm_ensemble_tune(self._h, int(steps), ctypes.byref(a), ctypes.byref(b),
                                               ctypes.byref(ms)))
-        return {"seg_rows": a.value, "grid": b.value, "ms_per_step": ms.value}
+        self._check(self._L.swm_ensemble_get_width(self._h, ctypes.byref(w)))
+        return {"seg_rows": a.value, "grid": b.value, "width": w.value, "ms_per_step": ms.value}
 
 
 def create_timescheme(name: str):

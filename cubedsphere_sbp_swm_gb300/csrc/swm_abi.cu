@@ -1718,6 +1718,21 @@ int ens_capture(swm_ensemble* ens) {
   return SWM_OK;
 }
 
+// Consumer width of the members' FP32 stage kernel: every member's box and
+// the ensemble's widest box and occupancy follow it.
+int ens_set_width(swm_ensemble* ens, int cols) {
+  int boxw = 0;
+  for (swm_ctx* c : ens->mem) {
+    if (c->shape.cols != cols && stage_layout(c, cols, 0, 0) != SWM_OK) return efail(ens, SWM_E_INVALID, c->err);
+    boxw = std::max(boxw, c->shape.boxw);
+  }
+  ens->cols = cols;
+  ens->boxw = boxw;
+  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw, ens->cols)
+                                         : stage_occupancy<double>(ens->order, ens->boxw, ens->cols);
+  return SWM_OK;
+}
+
 int ens_rebuild(swm_ensemble* ens, int seg_rows, int grid) {
   if (int rc = ens_units(ens, seg_rows)) return rc;
   ens->grid = grid;
@@ -1863,6 +1878,24 @@ int swm_ensemble_set_shape(swm_ensemble* ens, int seg_rows, int grid) {
   return ens_rebuild(ens, seg_rows, grid);
 }
 
+int swm_ensemble_set_width(swm_ensemble* ens, int cols) {
+  if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
+  cudaSetDevice(ens->device);
+  ECK(cudaStreamSynchronize(ens->st), "sync");
+  if (ens->prec != SWM_FP32_FUSED && cols != ens->cols)
+    return efail(ens, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
+  const int grid = ens->grid;
+  if (int rc = ens_set_width(ens, cols)) return rc;
+  // a persistent grid follows the new occupancy
+  return ens_rebuild(ens, ens->seg_rows, grid > 0 ? std::max(1, ens->occ) * ens->num_sms : 0);
+}
+
+int swm_ensemble_get_width(const swm_ensemble* ens, int* cols) {
+  if (!ens || !cols) return efail(nullptr, SWM_E_INVALID, "null argument");
+  *cols = ens->cols;
+  return SWM_OK;
+}
+
 int swm_ensemble_get_shape(const swm_ensemble* ens, int* seg_rows, int* grid, int* nunits) {
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (seg_rows) *seg_rows = ens->seg_rows;
@@ -1898,27 +1931,35 @@ int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid
     }
   };
   const int segs[] = {0, 192, 128, 96, 64, 48, 32, 24, 16};
-  const int persistent = std::max(1, ens->occ) * ens->num_sms;
-  const int grids[] = {persistent, 0};
+  const bool f32 = ens->prec == SWM_FP32_FUSED;
   double best = 1e30;
-  int best_seg = ens->seg_rows, best_grid = ens->grid;
+  int best_seg = ens->seg_rows, best_grid = ens->grid, best_cols = ens->cols;
   cudaEvent_t a = nullptr, b = nullptr;
   if (rc == SWM_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess))
     rc = efail(ens, SWM_E_CUDA, "tune: events");
-  for (int si = 0; si < (int)(sizeof(segs) / sizeof(segs[0])) && rc == SWM_OK; ++si) {
-    if (segs[si] > 0 && segs[si] >= ens->max_n) continue;
-    for (int gi = 0; gi < 2 && rc == SWM_OK; ++gi) {
-      if (ens->prec != SWM_FP32_FUSED && grids[gi] != 0) continue;  // FP64 kernel: one CTA per unit
-      if ((rc = ens_rebuild(ens, segs[si], grids[gi]))) break;
-      cudaGraphLaunch(ens->graph, ens->st);                          // warm-up
-      cudaEventRecord(a, ens->st);
-      for (int k = 0; k < steps; ++k) cudaGraphLaunch(ens->graph, ens->st);
-      cudaEventRecord(b, ens->st);
-      if (cudaEventSynchronize(b) != cudaSuccess) { rc = efail(ens, SWM_E_CUDA, "tune: sync"); break; }
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, a, b);
-      restore();
-      if (ms / steps < best) { best = ms / steps; best_seg = segs[si]; best_grid = grids[gi]; }
+  for (int wi = 0; wi < 4 && rc == SWM_OK; ++wi) {   // consumer widths (FP32 kernel only)
+    const int cols = f32 ? kStageWidths[wi] : ens->cols;
+    if (!f32 && wi > 0) break;
+    if (ens_set_width(ens, cols) != SWM_OK) continue;   // width cannot cover a member
+    const int persistent = std::max(1, ens->occ) * ens->num_sms;
+    const int grids[] = {persistent, 0};
+    for (int si = 0; si < (int)(sizeof(segs) / sizeof(segs[0])) && rc == SWM_OK; ++si) {
+      if (segs[si] > 0 && segs[si] >= ens->max_n) continue;
+      for (int gi = 0; gi < 2 && rc == SWM_OK; ++gi) {
+        if (!f32 && grids[gi] != 0) continue;  // FP64 kernel: one CTA per unit
+        if ((rc = ens_rebuild(ens, segs[si], grids[gi]))) break;
+        cudaGraphLaunch(ens->graph, ens->st);                          // warm-up
+        cudaEventRecord(a, ens->st);
+        for (int k = 0; k < steps; ++k) cudaGraphLaunch(ens->graph, ens->st);
+        cudaEventRecord(b, ens->st);
+        if (cudaEventSynchronize(b) != cudaSuccess) { rc = efail(ens, SWM_E_CUDA, "tune: sync"); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        restore();
+        if (ms / steps < best) {
+          best = ms / steps; best_seg = segs[si]; best_grid = grids[gi]; best_cols = cols;
+        }
+      }
     }
   }
   if (a) cudaEventDestroy(a);
@@ -1926,6 +1967,7 @@ int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid
   restore();
   cudaStreamSynchronize(ens->st);
   for (void* p : keep) if (p) cudaFree(p);
+  if (rc == SWM_OK) rc = ens_set_width(ens, best_cols);
   if (rc == SWM_OK) rc = ens_rebuild(ens, best_seg, best_grid);
   if (rc == SWM_OK) {
     EMEM(sync_check(ens->mem[0], ens->st));

@@ -321,6 +321,10 @@ void* swm_ensemble_stream(swm_ensemble* ens);
 /* Tile shape: rows per work unit (0: whole panel height) and persistent
  * CTAs of the stage kernel (0: one CTA per work unit). */
 int  swm_ensemble_set_shape(swm_ensemble* ens, int seg_rows, int grid);
+/* Consumer width of the members' FP32 stage kernel (96, 128, 160 or 192;
+ * bit-identical results); swm_ensemble_tune also searches it. */
+int  swm_ensemble_set_width(swm_ensemble* ens, int cols);
+int  swm_ensemble_get_width(const swm_ensemble* ens, int* cols);
 int  swm_ensemble_get_shape(const swm_ensemble* ens, int* seg_rows, int* grid,
                             int* nunits);
 /* Autotuner: times `steps` ensemble steps for each candidate tile shape,
