@@ -276,6 +276,17 @@ class StvecSWM:
         self.op._check(self.op._L.swm_state_download(self.op._h, self._h, *(_ptr(a) for a in out)))
         return out
 
+    def save(self, path: str, time: float = 0.0):
+        """Write the state to a restart file (FP64 fields and a header)."""
+        self.op._check(self.op._L.swm_state_save(self.op._h, self._h, str(path).encode(), float(time)))
+
+    def load(self, path: str) -> float:
+        """Read a restart file of the same N; returns the stored model time."""
+        t = ctypes.c_double()
+        self.op._check(self.op._L.swm_state_load(self.op._h, self._h, str(path).encode(),
+                                                 ctypes.byref(t)))
+        return t.value
+
     def assign_s1(self, s1):
         self.op._check(self.op._L.swm_assign_s1(self.op._h, self._h, float(s1)))
 

@@ -47,7 +47,7 @@ EXPORTS = (
     "swm_laplace", "swm_latlon_create", "swm_latlon_destroy", "swm_latlon_regrid_field",
     "swm_latlon_regrid_vector", "swm_latlon_regrid_state", "swm_latlon_write", "swm_paneled_write",
     "swm_tune_stage", "swm_get_stage_shape", "swm_set_stage_shape", "swm_ensemble_set_width",
-    "swm_ensemble_get_width",
+    "swm_ensemble_get_width", "swm_state_save", "swm_state_load",
 )
 
 
@@ -139,6 +139,8 @@ def load(build_if_missing: bool = True):
     sig("swm_set_stage_shape", I, VP, I, I, I)
     sig("swm_ensemble_set_width", I, VP, I)
     sig("swm_ensemble_get_width", I, VP, ctypes.POINTER(I))
+    sig("swm_state_save", I, VP, VP, C, D)
+    sig("swm_state_load", I, VP, VP, C, _D)
     sig("swm_diagnostics", I, VP, VP, _D)
     sig("swm_field_create", I, VP, PP)
     sig("swm_field_free", None, VP)

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -2696,6 +2697,70 @@ int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid) {
   if (!ctx->shape.tma && cols != ctx->shape.cols)
     return fail(ctx, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
   return stage_layout(ctx, cols, seg_rows, grid);
+}
+
+// ------------------------------------------------------- checkpoint / resume
+// State file: a 64-byte header (magic "SWMSTATE", format version, N, SBP
+// order, the writer's precision, the caller's model time) followed by the
+// FP64 fields h, u, v, each 6*(N+1)^2 values in the reference layout (per
+// panel (N+1)^2 values, i fastest).  An FP32 pair is stored as its exact
+// FP64 sum and split again on load, so a round trip restores it.
+struct StateFileHeader {
+  char magic[8];
+  uint32_t version, N, order, precision;
+  double time;
+  uint8_t pad[32];
+};
+static_assert(sizeof(StateFileHeader) == 64, "state file header is 64 bytes");
+
+int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double time) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
+  cudaSetDevice(ctx->cfg.device);
+  const size_t np = (size_t)6 * ctx->n * ctx->n;
+  std::vector<double> buf(3 * np);
+  double* dst[3] = {buf.data(), buf.data() + np, buf.data() + 2 * np};
+  if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
+  if (int rc = sync_check(ctx, ctx->st)) return rc;
+  StateFileHeader hd{};
+  std::memcpy(hd.magic, "SWMSTATE", 8);
+  hd.version = 1; hd.N = (uint32_t)ctx->N; hd.order = (uint32_t)ctx->order;
+  hd.precision = (uint32_t)ctx->prec; hd.time = time;
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return fail(ctx, SWM_E_IO, std::string("cannot open ") + path);
+  bool ok = std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
+            std::fwrite(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+  ok = (std::fclose(fp) == 0) && ok;
+  if (!ok) return fail(ctx, SWM_E_IO, std::string("cannot write ") + path);
+  return SWM_OK;
+}
+
+int swm_state_load(swm_ctx* ctx, swm_state* s, const char* path, double* time) {
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
+  cudaSetDevice(ctx->cfg.device);
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return fail(ctx, SWM_E_IO, std::string("cannot open ") + path);
+  StateFileHeader hd{};
+  const size_t np = (size_t)6 * ctx->n * ctx->n;
+  std::vector<double> buf(3 * np);
+  bool ok = std::fread(&hd, sizeof(hd), 1, fp) == 1;
+  if (ok && (std::memcmp(hd.magic, "SWMSTATE", 8) != 0 || hd.version != 1)) {
+    std::fclose(fp);
+    return fail(ctx, SWM_E_INVALID, std::string(path) + " is not a state file");
+  }
+  if (ok && (int)hd.N != ctx->N) {
+    std::fclose(fp);
+    return fail(ctx, SWM_E_INVALID, "state file N=" + std::to_string(hd.N) + " does not match the context");
+  }
+  ok = ok && std::fread(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+  std::fclose(fp);
+  if (!ok) return fail(ctx, SWM_E_IO, std::string("cannot read ") + path);
+  const double* src[3] = {buf.data(), buf.data() + np, buf.data() + 2 * np};
+  if (int rc = put_packed(ctx, s, src, cudaMemcpyHostToDevice)) return rc;
+  if (int rc = sync_check(ctx, ctx->st)) return rc;   // the host buffer goes out of scope
+  if (time) *time = hd.time;
+  return SWM_OK;
 }
 
 }  // extern "C"

@@ -405,6 +405,19 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
 int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* nunits);
 int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid);
 
+/* ---------------------------------------------------------------------- */
+/* Checkpoint / resume (no reference counterpart: the reference writes no   */
+/* restart files)                                                          */
+/* ---------------------------------------------------------------------- */
+/* A state file holds a 64-byte header (magic "SWMSTATE", version 1, N, SBP
+ * order, the writer's precision, the caller's model time) and the FP64
+ * fields h, u, v in the reference layout (6*(N+1)^2 values each).  Loading
+ * needs the same N; the precision may differ (FP32 pairs round-trip
+ * exactly).  SWM_E_IO on file errors, SWM_E_INVALID on a foreign or
+ * mismatched file. */
+int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double time);
+int swm_state_load(swm_ctx* ctx, swm_state* s, const char* path, double* time);
+
 #ifdef __cplusplus
 }
 #endif
