@@ -5,6 +5,8 @@
 #include "swm_launch.h"
 #include "swm_ops.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -232,6 +234,14 @@ struct swm_ctx {
 };
 
 namespace {
+
+// Named range of a public call for profilers (NVTX; no-op without a tool).
+struct TraceRange {
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
 
 int fail(swm_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg; else g_err = msg;
@@ -958,6 +968,7 @@ void swm_state_free(swm_state* s) {
 }
 
 int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* u, const double* v) {
+  TraceRange trace_("swm_state_upload");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
   cudaSetDevice(ctx->cfg.device);
@@ -966,6 +977,7 @@ int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* 
 }
 
 int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  TraceRange trace_("swm_state_download");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
   cudaSetDevice(ctx->cfg.device);
@@ -1062,6 +1074,7 @@ int swm_norm2(swm_ctx* ctx, const swm_state* a, double* out) {
 
 // ------------------------------------------------------------- operator
 int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  TraceRange trace_("swm_apply");
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
   if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
@@ -1078,6 +1091,7 @@ int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
 }
 
 int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  TraceRange trace_("swm_apply_unfused");
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
   if (ctx->prec != SWM_FP64_PLAIN) return fail(ctx, SWM_E_UNSUPPORTED, "unfused apply is FP64 only");
@@ -1305,6 +1319,7 @@ int diffusion_ready(swm_ctx* ctx) {
 extern "C" {
 
 int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  TraceRange trace_("swm_rk4_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
   if (nsteps == 0) return SWM_OK;
@@ -1347,6 +1362,7 @@ int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_
 }
 
 int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  TraceRange trace_("swm_apply_diffusion");
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
   if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
@@ -1365,6 +1381,7 @@ int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
 }
 
 int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  TraceRange trace_("swm_diffusion_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
   cudaSetDevice(ctx->cfg.device);
@@ -1374,6 +1391,7 @@ int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 }
 
 int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  TraceRange trace_("swm_model_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
   cudaSetDevice(ctx->cfg.device);
@@ -1387,6 +1405,7 @@ int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 }
 
 int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_order) {
+  TraceRange trace_("swm_laplace");
   if (int rc = check_field(ctx, out)) return rc;
   if (int rc = check_field(ctx, in)) return rc;
   if (narrow_order != 42 && narrow_order != 63)
@@ -1401,6 +1420,7 @@ int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_or
 }
 
 int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
+  TraceRange trace_("swm_diagnostics");
   if (int rc = check_state(ctx, s)) return rc;
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
   cudaSetDevice(ctx->cfg.device);
@@ -1855,6 +1875,7 @@ int swm_ensemble_diagnostics(swm_ensemble* ens, int m, double out[7]) {
 }
 
 int swm_ensemble_step(swm_ensemble* ens, int nsteps) {
+  TraceRange trace_("swm_ensemble_step");
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (nsteps < 0) return efail(ens, SWM_E_INVALID, "nsteps must be >= 0");
   cudaSetDevice(ens->device);
@@ -1907,6 +1928,7 @@ int swm_ensemble_get_shape(const swm_ensemble* ens, int* seg_rows, int* grid, in
 
 int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid_out,
                       double* ms_per_step_out) {
+  TraceRange trace_("swm_ensemble_tune");
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (steps < 1) return efail(ens, SWM_E_INVALID, "steps must be >= 1");
   cudaSetDevice(ens->device);
@@ -2269,11 +2291,13 @@ void free_adjoint(swm_adjoint* adj) {
 extern "C" {
 
 int swm_apply_tl(swm_ctx* ctx, const swm_state* y, const swm_state* dx, swm_state* dk) {
+  TraceRange trace_("swm_apply_tl");
   if (int rc = check_tl_args(ctx, y, dx, dk, true)) return rc;
   return tl_apply(ctx, (const double*)y->hi, (const double*)dx->hi, (double*)dk->hi);
 }
 
 int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk, swm_state* lx) {
+  TraceRange trace_("swm_apply_ad");
   if (int rc = check_tl_args(ctx, y, lk, lx, false)) return rc;
   if (ctx->prec == SWM_FP32_FUSED) {
     if (int rc = ad_apply<float>(ctx, (const float*)y->hi, (const float*)lk->hi, (float*)lx->hi)) return rc;
@@ -2283,11 +2307,13 @@ int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk, swm_stat
 }
 
 int swm_rk4_tl(swm_ctx* ctx, const swm_state* x, swm_state* dx, double dt) {
+  TraceRange trace_("swm_rk4_tl");
   if (int rc = check_tl_args(ctx, x, dx, nullptr, true)) return rc;
   return rk4_tl(ctx, (const double*)x->hi, (double*)dx->hi, dt);
 }
 
 int swm_rk4_ad(swm_ctx* ctx, const swm_state* x, swm_state* lx, double dt) {
+  TraceRange trace_("swm_rk4_ad");
   if (int rc = check_tl_args(ctx, x, lx, nullptr, false)) return rc;
   if (int rc = rk4_ad_graph(ctx, x->hi, lx->hi, dt)) return rc;
   return clear_lo(ctx, lx);
@@ -2323,6 +2349,7 @@ void swm_adjoint_destroy(swm_adjoint* adj) {
 }
 
 int swm_adjoint_forward(swm_adjoint* adj, const swm_state* x0, swm_state* xT) {
+  TraceRange trace_("swm_adjoint_forward");
   if (!adj) return fail(nullptr, SWM_E_INVALID, "null adjoint");
   swm_ctx* ctx = adj->ctx;
   if (int rc = check_state(ctx, x0)) return rc;
@@ -2341,6 +2368,7 @@ int swm_adjoint_forward(swm_adjoint* adj, const swm_state* x0, swm_state* xT) {
 }
 
 int swm_adjoint_backward(swm_adjoint* adj, swm_state* lambda) {
+  TraceRange trace_("swm_adjoint_backward");
   if (!adj) return fail(nullptr, SWM_E_INVALID, "null adjoint");
   swm_ctx* ctx = adj->ctx;
   if (int rc = check_state(ctx, lambda)) return rc;
@@ -2370,6 +2398,7 @@ int swm_adjoint_counts(const swm_adjoint* adj, long* forward_steps, long* adjoin
 
 int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const double* u,
                             const double* v) {
+  TraceRange trace_("swm_state_upload_device");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
   cudaSetDevice(ctx->cfg.device);
@@ -2378,6 +2407,7 @@ int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const d
 }
 
 int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  TraceRange trace_("swm_state_download_device");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
   cudaSetDevice(ctx->cfg.device);
@@ -2554,6 +2584,7 @@ int swm_latlon_regrid_vector(swm_ctx* ctx, swm_latlon* r, const swm_field* u, co
 
 int swm_latlon_regrid_state(swm_ctx* ctx, swm_latlon* r, const swm_state* s, double* h, double* u,
                             double* v) {
+  TraceRange trace_("swm_latlon_regrid_state");
   if (int rc = check_latlon(ctx, r)) return rc;
   if (int rc = check_state(ctx, s)) return rc;
   cudaSetDevice(ctx->cfg.device);
@@ -2576,6 +2607,7 @@ int swm_latlon_regrid_state(swm_ctx* ctx, swm_latlon* r, const swm_state* s, dou
 
 int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char* h_file,
                      const char* u_file, const char* v_file, int rec_num) {
+  TraceRange trace_("swm_latlon_write");
   if (int rc = check_latlon(ctx, r)) return rc;
   if (int rc = check_state(ctx, s)) return rc;
   if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
@@ -2598,6 +2630,7 @@ int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char
 }
 
 int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const char* file, int rec_num) {
+  TraceRange trace_("swm_paneled_write");
   if (int rc = check_state(ctx, s)) return rc;
   if (component < 0 || component > 2 || !file) return fail(ctx, SWM_E_INVALID, "bad component or file");
   if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
@@ -2620,6 +2653,7 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 // ------------------------------------------------------------ tuning
 int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
                    int* seg_rows_out, int* grid_out, double* ms_out) {
+  TraceRange trace_("swm_tune_stage");
   if (int rc = check_state(ctx, s)) return rc;
   if (steps < 1 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or steps");
   cudaSetDevice(ctx->cfg.device);
@@ -2714,6 +2748,7 @@ struct StateFileHeader {
 static_assert(sizeof(StateFileHeader) == 64, "state file header is 64 bytes");
 
 int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double time) {
+  TraceRange trace_("swm_state_save");
   if (int rc = check_state(ctx, s)) return rc;
   if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
   cudaSetDevice(ctx->cfg.device);
@@ -2736,6 +2771,7 @@ int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double ti
 }
 
 int swm_state_load(swm_ctx* ctx, swm_state* s, const char* path, double* time) {
+  TraceRange trace_("swm_state_load");
   if (int rc = check_state(ctx, s)) return rc;
   if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
   cudaSetDevice(ctx->cfg.device);
