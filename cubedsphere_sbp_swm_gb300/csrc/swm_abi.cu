@@ -225,7 +225,7 @@ struct swm_ctx {
   // vectors (6 fields) and 19 FP64 work fields, all allocated on first use
   int diff_uv = 0, diff_h = 0;
   double diff_uv_coeff = 0.0, diff_h_coeff = 0.0;
-  void* ntab[2][4] = {};    // cx, cy, clx, cly (context precision)
+  void* ntab[2][5] = {};    // cx, cy, clx, cly, b (context precision)
   void* b12 = nullptr;
   void* dw = nullptr;
   cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
@@ -1183,7 +1183,7 @@ constexpr int kDiffWork = 19;   // F 4, L 4, d1x 4, d1y 4, tendencies 3
 template <class T>
 NarrowTables<T> narrow_tables(swm_ctx* ctx, int narrow) {
   void* const* t = ctx->ntab[narrow == 63 ? 1 : 0];
-  return NarrowTables<T>{narrow, (T*)t[0], (T*)t[1], (T*)t[2], (T*)t[3]};
+  return NarrowTables<T>{narrow, (T*)t[0], (T*)t[1], (T*)t[2], (T*)t[3], (T*)t[4]};
 }
 template <class T> T* dwork(swm_ctx* ctx, int field) { return (T*)ctx->dw + field * ctx->g64.fs; }
 
@@ -1211,22 +1211,28 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
     }
   }
   void** t = ctx->ntab[narrow == 63 ? 1 : 0];
-  if (!t[0]) {
-    const size_t nw = (size_t)narrow_width(narrow) * g.fs;
+  if (!t[2]) {
+    // FP32 contexts form the interior coefficients from the two b fields
+    const bool f64 = ctx->prec == SWM_FP64_PLAIN;
+    const size_t nw = f64 ? (size_t)narrow_width(narrow) * g.fs : 0;
     const size_t ncl = (size_t)narrow_closure_count(narrow, ctx->n);
-    void* p[4] = {nullptr, nullptr, nullptr, nullptr};
-    cudaError_t e = cudaMalloc(&p[0], elt * nw);
-    if (e == cudaSuccess) e = cudaMalloc(&p[1], elt * nw);
+    void* p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaError_t e = cudaSuccess;
+    if (f64) e = cudaMalloc(&p[0], elt * nw);
+    if (f64 && e == cudaSuccess) e = cudaMalloc(&p[1], elt * nw);
     if (e == cudaSuccess) e = cudaMalloc(&p[2], elt * ncl);
     if (e == cudaSuccess) e = cudaMalloc(&p[3], elt * ncl);
+    if (e == cudaSuccess) e = cudaMalloc(&p[4], elt * 2 * g.fs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p[4], 0, elt * 2 * g.fs, ctx->st);
     if (e == cudaSuccess) {
-      if (ctx->prec == SWM_FP64_PLAIN)
+      if (f64)
         e = launch_narrow_tables<double>(
-            g, NarrowTables<double>{narrow, (double*)p[0], (double*)p[1], (double*)p[2], (double*)p[3]},
+            g, NarrowTables<double>{narrow, (double*)p[0], (double*)p[1], (double*)p[2], (double*)p[3],
+                                    (double*)p[4]},
             ctx->m64, ctx->st);
       else
         e = launch_narrow_tables<float>(
-            g, NarrowTables<float>{narrow, (float*)p[0], (float*)p[1], (float*)p[2], (float*)p[3]},
+            g, NarrowTables<float>{narrow, nullptr, nullptr, (float*)p[2], (float*)p[3], (float*)p[4]},
             ctx->m64, ctx->st);
     }
     if (e != cudaSuccess) {
@@ -1234,7 +1240,7 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
       return fail(ctx, e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
                   std::string("diffusion tables: ") + cudaGetErrorString(e));
     }
-    for (int k = 0; k < 4; ++k) t[k] = p[k];
+    for (int k = 0; k < 5; ++k) t[k] = p[k];
   }
   return SWM_OK;
 }

@@ -38,6 +38,21 @@ inline int dblk(long long count) { return (int)((count + DTPB - 1) / DTPB); }
 
 __constant__ NarrowD2 c_narrow[2] = {kNarrow42, kNarrow63};
 
+// Interior stencil matrices of both orders in FP32 ([0] 4/2, [1] 6/3).
+struct NarrowIn32 {
+  float v[2][NARROW_MAXW][NARROW_MAXW];
+};
+constexpr NarrowIn32 make_narrow_in32() {
+  NarrowIn32 t{};
+  for (int o = 0; o < NARROW_MAXW; ++o)
+    for (int q = 0; q < NARROW_MAXW; ++q) {
+      t.v[0][o][q] = float(kNarrow42.in[o][q]);
+      t.v[1][o][q] = float(kNarrow63.in[o][q]);
+    }
+  return t;
+}
+__constant__ NarrowIn32 c_in32 = make_narrow_in32();
+
 template <int NARROW>
 struct NarrowShape {
   static constexpr int ni = NARROW == 63 ? 1 : 0;
@@ -71,7 +86,7 @@ __device__ __forceinline__ bool node_here(const FieldGeom& g, Node& r) {
 // Interior stencil coefficients of both directions (zero at closure nodes):
 // cx[o] multiplies f[i+o-hw] of the row, cy[o] f[j+o-hw] of the column.
 template <class T, int NARROW>
-__global__ void narrow_coef_kernel(FieldGeom g, const double* m, T* cx, T* cy) {
+__global__ void narrow_coef_kernel(FieldGeom g, const double* m, T* cx, T* cy, T* b) {
   using S = NarrowShape<NARROW>;
   Node k;
   if (!node_here(g, k)) return;
@@ -82,6 +97,10 @@ __global__ void narrow_coef_kernel(FieldGeom g, const double* m, T* cx, T* cy) {
   const double* Q3 = m + MQI3 * g.fs + pb;
   const bool inx = k.i >= S::rows && k.i < g.n - S::rows;
   const bool iny = k.j >= S::rows && k.j < g.n - S::rows;
+  const long long a0 = (long long)k.j * g.P + k.i;
+  b[k.idx] = T(Q1[a0] * J[a0]);
+  b[g.fs + k.idx] = T(Q3[a0] * J[a0]);
+  if (!cx) return;
 #pragma unroll
   for (int o = 0; o < S::w; ++o) {
     double ax = 0.0, ay = 0.0;
@@ -156,8 +175,8 @@ __global__ void __launch_bounds__(RTPB) lap_d1_kernel(FieldGeom g, const T* f, c
 template <class T, int NARROW, int NF>
 __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f, const T* d1x,
                                                         const T* d1y, const T* cx, const T* cy,
-                                                        const T* clx, const T* cly, const T* mt,
-                                                        double hs, T* out, T* E) {
+                                                        const T* clx, const T* cly, const T* bco,
+                                                        const T* mt, double hs, T* out, T* E) {
   using S = NarrowShape<NARROW>;
   Node k;
   if (!node_here(g, k)) return;
@@ -180,8 +199,23 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     x0 = k.j * P + (side ? n - 1 : 0); xs = side ? -1 : 1;
     rsx = T(D.rowscale[r]);
   } else {
+    if constexpr (sizeof(T) == 4) {   // from the variable coefficients along the row
+      T bb[S::w];
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
+      for (int q = 0; q < S::w; ++q) bb[q] = bco[pb + o + q - S::hw];
+#pragma unroll
+      for (int c = 0; c < S::cols; ++c) {
+        T acc = T(0);
+        if (c < S::w) {
+#pragma unroll
+          for (int q = 0; q < S::w; ++q) acc += c_in32.v[S::ni][c][q] * bb[q];
+        }
+        ax[c] = acc;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
+    }
     x0 = o - S::hw; xs = 1;
   }
   if (clyn) {
@@ -192,8 +226,23 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     y0 = (side ? n - 1 : 0) * P + k.i; ys = side ? -P : P;
     rsy = T(D.rowscale[r]);
   } else {
+    if constexpr (sizeof(T) == 4) {   // from the variable coefficients along the column
+      T bb[S::w];
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
+      for (int q = 0; q < S::w; ++q) bb[q] = bco[g.fs + pb + o + (q - S::hw) * P];
+#pragma unroll
+      for (int c = 0; c < S::cols; ++c) {
+        T acc = T(0);
+        if (c < S::w) {
+#pragma unroll
+          for (int q = 0; q < S::w; ++q) acc += c_in32.v[S::ni][c][q] * bb[q];
+        }
+        ay[c] = acc;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
+    }
     y0 = o - S::hw * P; ys = P;
   }
   const int ntx = clxn ? S::cols : S::w, nty = clyn ? S::cols : S::w;
@@ -319,10 +368,10 @@ cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, c
                                  cudaStream_t st) {
   const long long ncl = narrow_closure_count(t.narrow, g.n);
   if (t.narrow == 63) {
-    narrow_coef_kernel<T, 63><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy);
+    narrow_coef_kernel<T, 63><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy, t.b);
     narrow_closure_kernel<T, 63><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   } else {
-    narrow_coef_kernel<T, 42><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy);
+    narrow_coef_kernel<T, 42><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy, t.b);
     narrow_closure_kernel<T, 42><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   }
   return cudaGetLastError();
@@ -333,7 +382,7 @@ void laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f, const 
                 T* d1x, T* d1y, T* out, T* edge, cudaStream_t st) {
   lap_d1_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(g, f, mt, d1x, d1y);
   lap_main_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(
-      g, f, d1x, d1y, t.cx, t.cy, t.clx, t.cly, mt, hs, out, edge);
+      g, f, d1x, d1y, t.cx, t.cy, t.clx, t.cly, t.b, mt, hs, out, edge);
 }
 
 template <class T>

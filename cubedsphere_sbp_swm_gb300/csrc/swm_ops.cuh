@@ -152,12 +152,14 @@ cudaError_t launch_pack_state(const FieldGeom& g, int nf, const void* hi, const 
 // Hyperdiffusion (swm_diffusion.cu): narrow-stencil SBP Laplacians of order
 // narrow = 42 or 63, on fields of element type T.  Per-context coefficient
 // tables of one order: interior stencil coefficients (narrow_width fields
-// each for x and y) and the closure rows (narrow_closure_count values each
-// for x and y), built in FP64.
+// each for x and y; FP64 contexts), the variable coefficients (2 fields;
+// FP32 contexts form the interior coefficients from them) and the closure
+// rows (narrow_closure_count values each for x and y), built in FP64.
 template <class T>
 struct NarrowTables {
   int narrow;
   T *cx, *cy, *clx, *cly;
+  T* b;   // the variable coefficients J*Qi11 (field 0) and J*Qi22 (field 1)
 };
 int narrow_rows(int narrow);
 int narrow_cols(int narrow);
