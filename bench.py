@@ -442,7 +442,12 @@ def run_gpu_arm(args):
         s0 = op.create_stvec()
         s0.upload(h, u, v)
         if prec == "fp32":   # set-up: pick the stage kernel's fastest launch shape
-            tuned.update(op.tune_stage(s0, DT, 10))
+            if args.stage_shape:
+                wdt, seg, grd = (int(x) for x in args.stage_shape.split(","))
+                op.set_stage_shape(wdt, seg, grd)
+                tuned.update({"width": wdt, "seg_rows": seg, "grid": grd})
+            else:
+                tuned.update(op.tune_stage(s0, DT, 10))
         s = op.create_stvec()
         s.assign_s1v1(1.0, s0)
         ts = swm.RK4()
@@ -724,6 +729,9 @@ def main():
                     help="skip the 96-member ensemble leg")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint leg (N=192, 240 steps)")
+    ap.add_argument("--stage-shape", default=None,
+                    help="WIDTH,SEG_ROWS,GRID of the FP32 stage kernel instead of tuning it "
+                         "(reproducible profiling runs)")
     ap.add_argument("--no-diffusion", action="store_true",
                     help="skip the RK4 + hyperdiffusion model-step leg")
     ap.add_argument("--days", type=float, default=None,
