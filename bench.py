@@ -443,9 +443,10 @@ def run_gpu_arm(args):
         s0.upload(h, u, v)
         if prec == "fp32":   # set-up: pick the stage kernel's fastest launch shape
             if args.stage_shape:
-                wdt, seg, grd = (int(x) for x in args.stage_shape.split(","))
-                op.set_stage_shape(wdt, seg, grd)
-                tuned.update({"width": wdt, "seg_rows": seg, "grid": grd})
+                parts = args.stage_shape.split(",")
+                wdt, seg, grd = (int(x) for x in parts[:3])
+                op.set_stage_shape(wdt, seg, grd, parts[3] if len(parts) > 3 else "auto")
+                tuned.update(op.stage_shape)
             else:
                 tuned.update(op.tune_stage(s0, DT, 10))
         s = op.create_stvec()
@@ -574,7 +575,7 @@ def run_gpu_arm(args):
                                                "metric precompute)",
                        "N": N, "sbp": "d%d" % ORDER, "dt_s": DT, "nodes_per_field": npts,
                        "l2": "256 MB buffer written between timed steps",
-                       "stage_shape": {k: tuned[k] for k in ("width", "seg_rows", "grid")},
+                       "stage_shape": {k: tuned[k] for k in ("width", "seg_rows", "grid", "box")},
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "e2e": {"value": round(e2e_val, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,
@@ -730,8 +731,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint leg (N=192, 240 steps)")
     ap.add_argument("--stage-shape", default=None,
-                    help="WIDTH,SEG_ROWS,GRID of the FP32 stage kernel instead of tuning it "
-                         "(reproducible profiling runs)")
+                    help="WIDTH,SEG_ROWS,GRID[,BOX] of the FP32 stage kernel instead of tuning it, "
+                         "BOX one of auto, strip, widest (reproducible profiling runs)")
     ap.add_argument("--no-diffusion", action="store_true",
                     help="skip the RK4 + hyperdiffusion model-step leg")
     ap.add_argument("--days", type=float, default=None,

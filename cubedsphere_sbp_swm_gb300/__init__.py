@@ -161,24 +161,37 @@ class OperatorSWM:
         laplace_ah_sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58), edge-synced."""
         self._check(self._L.swm_laplace(self._h, out._h, f._h, int(narrow_order)))
 
+    _BOX_MODES = {"auto": 0, "strip": 1, "widest": 2}
+    _BOX_NAMES = {1: "strip", 2: "widest"}
+
     def tune_stage(self, v: "StvecSWM", dt: float, steps: int = 10) -> dict:
         """Time the stage kernel's launch shapes (consumer width, rows per
-        unit, persistent grid) on a copy of v and keep the fastest
-        (bit-identical results)."""
-        c, r, g, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        unit, persistent grid, TMA box mode) on a copy of v and keep the
+        fastest (bit-identical results)."""
+        c, r, g, b, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         self._check(self._L.swm_tune_stage(self._h, v._h, float(dt), int(steps), ctypes.byref(c),
-                                           ctypes.byref(r), ctypes.byref(g), ctypes.byref(ms)))
-        return {"width": c.value, "seg_rows": r.value, "grid": g.value, "ms": ms.value}
+                                           ctypes.byref(r), ctypes.byref(g), ctypes.byref(b),
+                                           ctypes.byref(ms)))
+        return {"width": c.value, "seg_rows": r.value, "grid": g.value,
+                "box": self._BOX_NAMES[b.value], "ms": ms.value}
 
     @property
     def stage_shape(self) -> dict:
-        c, r, g, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        c, r, g, b, n = (ctypes.c_int() for _ in range(5))
         self._check(self._L.swm_get_stage_shape(self._h, ctypes.byref(c), ctypes.byref(r),
-                                                ctypes.byref(g), ctypes.byref(n)))
-        return {"width": c.value, "seg_rows": r.value, "grid": g.value, "units": n.value}
+                                                ctypes.byref(g), ctypes.byref(b), ctypes.byref(n)))
+        return {"width": c.value, "seg_rows": r.value, "grid": g.value,
+                "box": self._BOX_NAMES[b.value], "units": n.value}
 
-    def set_stage_shape(self, width: int = 128, seg_rows: int = 0, grid: int = 0):
-        self._check(self._L.swm_set_stage_shape(self._h, int(width), int(seg_rows), int(grid)))
+    def set_stage_shape(self, width: int = 128, seg_rows: int = 0, grid: int = 0, box: str = "auto"):
+        """box: "strip" (the narrowest TMA box covering every column strip),
+        "widest" (the width's widest box, compiled in; needs a field pitch of
+        at least that box) or "auto" (the widest where it fits and keeps the
+        resident CTAs per SM)."""
+        if box not in self._BOX_MODES:
+            raise SwmError(_abi.SWM_E_INVALID, f"unknown box mode {box!r}")
+        self._check(self._L.swm_set_stage_shape(self._h, int(width), int(seg_rows), int(grid),
+                                                self._BOX_MODES[box]))
 
     def model_step(self, v0: "StvecSWM", dt: float, nsteps: int = 1):
         """nsteps of the drivers' time step (ts2_mod.f90:143-146): RK4, then the

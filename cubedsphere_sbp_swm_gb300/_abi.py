@@ -133,10 +133,11 @@ def load(build_if_missing: bool = True):
     sig("swm_latlon_regrid_state", I, VP, VP, VP, _D, _D, _D)
     sig("swm_latlon_write", I, VP, VP, VP, C, C, C, I)
     sig("swm_paneled_write", I, VP, VP, I, C, I)
-    sig("swm_tune_stage", I, VP, VP, D, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), _D)
+    sig("swm_tune_stage", I, VP, VP, D, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
+        ctypes.POINTER(I), _D)
     sig("swm_get_stage_shape", I, VP, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
-        ctypes.POINTER(I))
-    sig("swm_set_stage_shape", I, VP, I, I, I)
+        ctypes.POINTER(I), ctypes.POINTER(I))
+    sig("swm_set_stage_shape", I, VP, I, I, I, I)
     sig("swm_ensemble_set_width", I, VP, I)
     sig("swm_ensemble_get_width", I, VP, ctypes.POINTER(I))
     sig("swm_state_save", I, VP, VP, C, D)

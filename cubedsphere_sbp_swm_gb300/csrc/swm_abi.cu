@@ -437,8 +437,8 @@ int run_stage(swm_ctx* ctx, const InstDev<T>& I, int mode) {
     CK(cudaEventCreate(&a), "event"); CK(cudaEventCreate(&b), "event");
     CK(cudaEventRecord(a, ctx->st), "event record");
   }
-  CK(launch_stage<T>(ctx->order, ctx->shape.cols, &maps, I, nullptr, ctx->units, ctx->nunits, mode,
-                     ctx->shape.boxw, ctx->stage_grid, ctx->derr, ctx->st),
+  CK(launch_stage<T>(ctx->order, ctx->shape.cols, ctx->shape.fixbw != 0, &maps, I, nullptr, ctx->units,
+                     ctx->nunits, mode, ctx->shape.boxw, ctx->stage_grid, ctx->derr, ctx->st),
      "stage kernel");
   if (ctx->timing) {
     CK(cudaEventRecord(b, ctx->st), "event record");
@@ -497,9 +497,13 @@ double* tmpf(swm_ctx* c, int k) { return c->tmp + (long long)k * c->g64.fs; }
 // TMA box that covers every strip from its aligned start; the box fixes the
 // shared memory and so the resident CTAs per SM, which sets the number of
 // row segments unless seg_rows > 0 fixes the rows per unit.  grid > 0 runs
-// the kernel persistently on that many CTAs.  Replaces the context's units
-// and drops its captured graphs.
-int stage_layout(swm_ctx* ctx, int cols, int seg_rows = 0, int grid = 0) {
+// the kernel persistently on that many CTAs.  box selects the box mode:
+// SWM_BOX_STRIP (that narrowest box, its width a kernel argument),
+// SWM_BOX_WIDEST (the width's widest box, a compile-time constant of the
+// kernel; needs a pitch of at least that box) or SWM_BOX_AUTO (the widest
+// box where it fits and keeps the resident CTAs per SM).  Replaces the
+// context's units and drops its captured graphs.
+int stage_layout(swm_ctx* ctx, int cols, int seg_rows = 0, int grid = 0, int box = SWM_BOX_AUTO) {
   std::string why;
   StageShape sh = ctx->shape;
   const SbpC& tab = kTables[sbp_index(ctx->order)];
@@ -515,10 +519,19 @@ int stage_layout(swm_ctx* ctx, int cols, int seg_rows = 0, int grid = 0) {
       bw = std::max(bw, (w.cl1 - cal + al - 1) / al * al);
     }
     if (bw > bmax) return fail(ctx, SWM_E_INVALID, "work split exceeds the TMA box");
+    const bool f32 = ctx->prec == SWM_FP32_FUSED;
+    auto occ = [&](int w, bool fixed) {
+      return f32 ? stage_occupancy<float>(ctx->order, w, cols, fixed)
+                 : stage_occupancy<double>(ctx->order, w, cols, fixed);
+    };
+    const bool fits = f32 && bmax <= ctx->P;
+    if (box == SWM_BOX_WIDEST && !fits) return fail(ctx, SWM_E_INVALID, "the widest box exceeds the pitch");
+    const int occ_strip = occ(bw, false);
+    const bool fixed = box == SWM_BOX_WIDEST || (box == SWM_BOX_AUTO && fits && occ(bmax, true) >= occ_strip);
     sh.cols = cols;
-    sh.boxw = bw;
-    sh.ctas_per_sm = ctx->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ctx->order, bw, cols)
-                                                 : stage_occupancy<double>(ctx->order, bw, cols);
+    sh.fixbw = fixed ? 1 : 0;
+    sh.boxw = fixed ? bmax : bw;
+    sh.ctas_per_sm = fixed ? occ(bmax, true) : occ_strip;
   }
   std::vector<WorkUnit> units;
   const int nseg = seg_rows > 0 ? (ctx->n + seg_rows - 1) / seg_rows : 0;
@@ -1617,6 +1630,7 @@ struct swm_ensemble {
   std::vector<double> dt;
   cudaStream_t st = nullptr;
   int boxw = 0, max_n = 0, num_sms = 0, occ = 0, cols = 0;
+  bool fixbw = false;   // every member uses its width's widest (compile-time) box
   StageMaps* dmaps = nullptr;        // [4 stages][nmem]
   void* dinst = nullptr;             // InstDev<T> [4 stages][nmem]
   WorkUnit* dunits = nullptr;
@@ -1730,8 +1744,8 @@ int ens_capture(swm_ensemble* ens) {
   ECK(cudaStreamBeginCapture(ens->st, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
-    e = launch_stage<T>(ens->order, ens->cols, nullptr, InstDev<T>{}, I + i * ens->nmem, ens->dunits,
-                        ens->nunits, MODE_RK1 + i, ens->boxw, ens->grid, derr, ens->st);
+    e = launch_stage<T>(ens->order, ens->cols, ens->fixbw, nullptr, InstDev<T>{}, I + i * ens->nmem,
+                        ens->dunits, ens->nunits, MODE_RK1 + i, ens->boxw, ens->grid, derr, ens->st);
     if (e == cudaSuccess)
       e = launch_edge<T>(InstDev<T>{}, I + i * ens->nmem, ens->nmem, ens->max_n, tp, MODE_RK1 + i,
                          ens->st);
@@ -1745,18 +1759,28 @@ int ens_capture(swm_ensemble* ens) {
   return SWM_OK;
 }
 
+// Box mode, widest box and occupancy of the ensemble's stage launches: the
+// compile-time widest box only when every member's maps use it.
+void ens_box(swm_ensemble* ens) {
+  int boxw = 0;
+  bool fixed = true;
+  for (swm_ctx* c : ens->mem) {
+    boxw = std::max(boxw, c->shape.boxw);
+    fixed = fixed && c->shape.fixbw != 0;
+  }
+  ens->boxw = boxw;
+  ens->fixbw = fixed;
+  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw, ens->cols, fixed)
+                                         : stage_occupancy<double>(ens->order, ens->boxw, ens->cols, fixed);
+}
+
 // Consumer width of the members' FP32 stage kernel: every member's box and
 // the ensemble's widest box and occupancy follow it.
 int ens_set_width(swm_ensemble* ens, int cols) {
-  int boxw = 0;
-  for (swm_ctx* c : ens->mem) {
+  for (swm_ctx* c : ens->mem)
     if (c->shape.cols != cols && stage_layout(c, cols, 0, 0) != SWM_OK) return efail(ens, SWM_E_INVALID, c->err);
-    boxw = std::max(boxw, c->shape.boxw);
-  }
   ens->cols = cols;
-  ens->boxw = boxw;
-  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw, ens->cols)
-                                         : stage_occupancy<double>(ens->order, ens->boxw, ens->cols);
+  ens_box(ens);
   return SWM_OK;
 }
 
@@ -1823,7 +1847,6 @@ int swm_ensemble_create(const swm_config* base, int nmembers, const int* member_
     if (int rc = swm_state_create(ctx, &s)) return bail(rc, ctx->err);
     ens->state.push_back(s);
     ens->max_n = std::max(ens->max_n, ctx->n);
-    ens->boxw = std::max(ens->boxw, ctx->shape.boxw);
     ens->cols = ctx->shape.cols;
     ens->num_sms = ctx->num_sms;
   }
@@ -1835,8 +1858,7 @@ int swm_ensemble_create(const swm_config* base, int nmembers, const int* member_
   if (e != cudaSuccess)
     return bail(e == cudaErrorMemoryAllocation ? SWM_E_NOMEM : SWM_E_CUDA,
                 std::string("ensemble alloc: ") + cudaGetErrorString(e));
-  ens->occ = ens->prec == SWM_FP32_FUSED ? stage_occupancy<float>(ens->order, ens->boxw, ens->cols)
-                                         : stage_occupancy<double>(ens->order, ens->boxw, ens->cols);
+  ens_box(ens);
   // default tile shape: whole-panel strips on persistent CTAs (FP32) or one
   // CTA per unit of 64 rows (FP64); swm_ensemble_tune measures the others
   const bool f32 = ens->prec == SWM_FP32_FUSED;
@@ -2658,16 +2680,20 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 
 // ------------------------------------------------------------ tuning
 int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
-                   int* seg_rows_out, int* grid_out, double* ms_out) {
+                   int* seg_rows_out, int* grid_out, int* box_out, double* ms_out) {
   TraceRange trace_("swm_tune_stage");
   if (int rc = check_state(ctx, s)) return rc;
   if (steps < 1 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or steps");
   cudaSetDevice(ctx->cfg.device);
+  auto report = [&](int c, int r, int g, int b, double ms) {
+    if (cols_out) *cols_out = c;
+    if (seg_rows_out) *seg_rows_out = r;
+    if (grid_out) *grid_out = g;
+    if (box_out) *box_out = b;
+    if (ms_out) *ms_out = ms;
+  };
   if (!ctx->shape.tma) {   // the FP64 kernel has one shape
-    if (cols_out) *cols_out = ctx->shape.cols;
-    if (seg_rows_out) *seg_rows_out = ctx->seg_rows;
-    if (grid_out) *grid_out = ctx->stage_grid;
-    if (ms_out) *ms_out = 0.0;
+    report(ctx->shape.cols, ctx->seg_rows, ctx->stage_grid, SWM_BOX_STRIP, 0.0);
     return SWM_OK;
   }
   swm_state* x = nullptr;
@@ -2676,10 +2702,11 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   const int c0 = ctx->shape.cols, r0 = ctx->seg_rows, g0 = ctx->stage_grid;
-  int bc = c0, br = r0, bg = g0, rc = SWM_OK;
+  const int x0 = ctx->shape.fixbw ? SWM_BOX_WIDEST : SWM_BOX_STRIP;
+  int bc = c0, br = r0, bg = g0, bx = x0, rc = SWM_OK;
   double best_ms = 1e30;
-  auto trial = [&](int cols, int seg, int grid) {
-    if (stage_layout(ctx, cols, seg, grid) != SWM_OK) return;   // shape cannot cover the grid
+  auto trial = [&](int cols, int seg, int grid, int box) {
+    if (stage_layout(ctx, cols, seg, grid, box) != SWM_OK) return;   // shape cannot cover the grid
     std::vector<float> ms;
     for (int k = -2; k < steps && rc == SWM_OK; ++k) {   // two untimed steps capture the graph
       rc = copy_state(ctx, x, s);
@@ -2693,50 +2720,51 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
     if (rc != SWM_OK || ms.empty()) return;
     std::sort(ms.begin(), ms.end());
     const double med = ms[ms.size() / 2];
-    if (med < best_ms) { best_ms = med; bc = cols; br = seg; bg = grid; }
+    if (med < best_ms) { best_ms = med; bc = cols; br = seg; bg = grid; bx = box; }
   };
   // widths x rows per unit (0: one wave of units) x one CTA per unit or a
-  // persistent wave of CTAs
+  // persistent wave of CTAs x both box modes
   const int seg_opts[] = {0, 16, 24, 32, 48, 64, 96};
   for (int w : kStageWidths) {
     for (int seg : seg_opts) {
-      if (rc != SWM_OK) break;
-      if (seg >= ctx->n) continue;
-      trial(w, seg, 0);
-      if (rc != SWM_OK || seg == 0) continue;
-      const int wave = std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms;
-      if (ctx->shape.cols == w && ctx->nunits > wave) trial(w, seg, wave);
+      for (int box : {SWM_BOX_STRIP, SWM_BOX_WIDEST}) {
+        if (rc != SWM_OK) break;
+        if (seg >= ctx->n) continue;
+        trial(w, seg, 0, box);
+        if (rc != SWM_OK || seg == 0) continue;
+        const int wave = std::max(1, ctx->shape.ctas_per_sm) * ctx->num_sms;
+        if (ctx->shape.cols == w && ctx->nunits > wave) trial(w, seg, wave, box);
+      }
     }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   swm_state_free(x);
-  const int rc2 = rc == SWM_OK ? stage_layout(ctx, bc, br, bg) : stage_layout(ctx, c0, r0, g0);
+  const int rc2 = rc == SWM_OK ? stage_layout(ctx, bc, br, bg, bx) : stage_layout(ctx, c0, r0, g0, x0);
   if (rc != SWM_OK) return rc;
   if (rc2 != SWM_OK) return rc2;
-  if (cols_out) *cols_out = bc;
-  if (seg_rows_out) *seg_rows_out = br;
-  if (grid_out) *grid_out = bg;
-  if (ms_out) *ms_out = best_ms;
+  report(bc, br, bg, bx, best_ms);
   return SWM_OK;
 }
 
-int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* nunits) {
+int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* box, int* nunits) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   if (cols) *cols = ctx->shape.cols;
   if (seg_rows) *seg_rows = ctx->seg_rows;
   if (grid) *grid = ctx->stage_grid;
+  if (box) *box = ctx->shape.fixbw ? SWM_BOX_WIDEST : SWM_BOX_STRIP;
   if (nunits) *nunits = ctx->nunits;
   return SWM_OK;
 }
 
-int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid) {
+int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid, int box) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   if (seg_rows < 0 || grid < 0) return fail(ctx, SWM_E_INVALID, "shape values must be >= 0");
+  if (box < SWM_BOX_AUTO || box > SWM_BOX_WIDEST) return fail(ctx, SWM_E_INVALID, "unknown box mode");
   cudaSetDevice(ctx->cfg.device);
   if (!ctx->shape.tma && cols != ctx->shape.cols)
     return fail(ctx, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
-  return stage_layout(ctx, cols, seg_rows, grid);
+  return stage_layout(ctx, cols, seg_rows, grid, ctx->shape.tma ? box : SWM_BOX_AUTO);
 }
 
 // ------------------------------------------------------- checkpoint / resume

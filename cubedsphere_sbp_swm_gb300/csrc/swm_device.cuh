@@ -35,6 +35,7 @@ struct StageShape {
   int cols;          // columns one CTA reads (threads of its consumer warps)
   int tma;           // 1: TMA-pipelined kernel (needs StageMaps)
   int boxw, rps, nf; // TMA box: columns, rows per stage, metric f fields
+  int fixbw;         // 1: every box has the width's widest box width
 };
 
 constexpr int MAXNE = 6;   // closure rows

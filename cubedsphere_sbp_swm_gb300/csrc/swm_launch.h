@@ -12,9 +12,11 @@ namespace swm {
 // (TMA kernels only); grid > 0 runs the TMA kernel persistently on that many
 // CTAs (0: one CTA per unit); err is the device error flag raised by an
 // expired bounded wait.
-// cols: the consumer width of the TMA kernel (one of kStageWidths).
+// cols: the consumer width of the TMA kernel (one of kStageWidths); fixbw:
+// the variant whose boxes all have the width's widest box width (boxw must
+// then equal stage_boxw_max).
 template <class T>
-cudaError_t launch_stage(int order, int cols, const StageMaps* maps, const InstDev<T>& one,
+cudaError_t launch_stage(int order, int cols, bool fixbw, const StageMaps* maps, const InstDev<T>& one,
                          const InstDev<T>* many, const WorkUnit* units, int nunits, int mode,
                          int boxw, int grid, int* err, cudaStream_t st);
 // Sets the launch attributes of the stage kernels of one SBP order, every
@@ -24,7 +26,7 @@ template <class T>
 cudaError_t prepare_stage(int order, StageShape* shape);
 // Resident stage-kernel CTAs per SM when the TMA box is boxw columns wide.
 template <class T>
-int stage_occupancy(int order, int boxw, int cols);
+int stage_occupancy(int order, int boxw, int cols, bool fixbw);
 // Widest TMA box of the kernel of consumer width cols (0: width not built).
 template <class T>
 int stage_boxw_max(int cols);
@@ -33,11 +35,11 @@ int stage_boxw_max(int cols);
 // own translation unit (swm_stage_f32_w<width>.cu).
 constexpr int kStageWidths[4] = {96, 128, 160, 192};
 template <int CONS>
-cudaError_t stage_f32_launch(int order, const StageMaps& m, const InstDev<float>& one,
+cudaError_t stage_f32_launch(int order, bool fixbw, const StageMaps& m, const InstDev<float>& one,
                              const InstDev<float>* many, const WorkUnit* units, int nunits,
                              int mode, int boxw, int grid, int* err, cudaStream_t st);
 template <int CONS>
-int stage_f32_occupancy(int order, int boxw);
+int stage_f32_occupancy(int order, bool fixbw, int boxw);
 template <int CONS>
 cudaError_t stage_f32_prepare(int order);
 // Cube-edge kernel over ninst instances whose largest edge has max_n nodes.

@@ -7,28 +7,28 @@
 namespace swm {
 
 template <>
-cudaError_t launch_stage<float>(int order, int cols, const StageMaps* maps,
+cudaError_t launch_stage<float>(int order, int cols, bool fixbw, const StageMaps* maps,
                                 const InstDev<float>& one, const InstDev<float>* many,
                                 const WorkUnit* units, int nunits, int mode, int boxw, int grid,
                                 int* err, cudaStream_t st) {
   static const StageMaps kNone{};
   const StageMaps& m = maps ? *maps : kNone;
   switch (cols) {
-    case 96: return stage_f32_launch<96>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
-    case 128: return stage_f32_launch<128>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
-    case 160: return stage_f32_launch<160>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
-    case 192: return stage_f32_launch<192>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 96: return stage_f32_launch<96>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 128: return stage_f32_launch<128>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 160: return stage_f32_launch<160>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
+    case 192: return stage_f32_launch<192>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <>
-int stage_occupancy<float>(int order, int boxw, int cols) {
+int stage_occupancy<float>(int order, int boxw, int cols, bool fixbw) {
   switch (cols) {
-    case 96: return stage_f32_occupancy<96>(order, boxw);
-    case 128: return stage_f32_occupancy<128>(order, boxw);
-    case 160: return stage_f32_occupancy<160>(order, boxw);
-    case 192: return stage_f32_occupancy<192>(order, boxw);
+    case 96: return stage_f32_occupancy<96>(order, fixbw, boxw);
+    case 128: return stage_f32_occupancy<128>(order, fixbw, boxw);
+    case 160: return stage_f32_occupancy<160>(order, fixbw, boxw);
+    case 192: return stage_f32_occupancy<192>(order, fixbw, boxw);
     default: return 0;
   }
 }
@@ -56,7 +56,8 @@ cudaError_t prepare_stage<float>(int order, StageShape* shape) {
   shape->boxw = stage_boxw_max<float>(shape->cols);
   shape->rps = TmaLayout<float, 42, TMA_CONS_DEFAULT>::RPS;
   shape->nf = TmaLayout<float, 42, TMA_CONS_DEFAULT>::NF;
-  shape->ctas_per_sm = stage_occupancy<float>(order, shape->boxw, shape->cols);
+  shape->fixbw = 0;
+  shape->ctas_per_sm = stage_occupancy<float>(order, shape->boxw, shape->cols, false);
   return cudaGetLastError();
 }
 

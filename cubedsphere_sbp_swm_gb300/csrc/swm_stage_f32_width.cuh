@@ -10,17 +10,17 @@
 namespace swm {
 
 template <>
-cudaError_t stage_f32_launch<SWM_STAGE_WIDTH>(int order, const StageMaps& m,
+cudaError_t stage_f32_launch<SWM_STAGE_WIDTH>(int order, bool fixbw, const StageMaps& m,
                                               const InstDev<float>& one, const InstDev<float>* many,
                                               const WorkUnit* units, int nunits, int mode, int boxw,
                                               int grid, int* err, cudaStream_t st) {
-  return StageF32Width<SWM_STAGE_WIDTH>::launch(order, m, one, many, units, nunits, mode, boxw,
-                                                grid, err, st);
+  return StageF32Width<SWM_STAGE_WIDTH>::launch(order, fixbw, m, one, many, units, nunits, mode,
+                                                boxw, grid, err, st);
 }
 
 template <>
-int stage_f32_occupancy<SWM_STAGE_WIDTH>(int order, int boxw) {
-  return StageF32Width<SWM_STAGE_WIDTH>::occupancy(order, boxw);
+int stage_f32_occupancy<SWM_STAGE_WIDTH>(int order, bool fixbw, int boxw) {
+  return StageF32Width<SWM_STAGE_WIDTH>::occupancy(order, fixbw, boxw);
 }
 
 template <>

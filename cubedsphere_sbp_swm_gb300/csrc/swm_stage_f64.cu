@@ -7,11 +7,12 @@
 namespace swm {
 
 template <>
-cudaError_t launch_stage<double>(int order, int cols, const StageMaps* maps,
+cudaError_t launch_stage<double>(int order, int cols, bool fixbw, const StageMaps* maps,
                                  const InstDev<double>& one, const InstDev<double>* many,
                                  const WorkUnit* units, int nunits, int mode, int boxw, int grid,
                                  int* err, cudaStream_t st) {
   (void)cols;
+  (void)fixbw;
   (void)err;
   (void)grid;
   (void)boxw;
@@ -35,7 +36,7 @@ static int v1_occupancy() {
 
 template <>
 cudaError_t prepare_stage<double>(int order, StageShape* shape) {
-  cudaError_t e = launch_stage<double>(order, STAGE_BW, nullptr, InstDev<double>{}, nullptr, nullptr,
+  cudaError_t e = launch_stage<double>(order, STAGE_BW, false, nullptr, InstDev<double>{}, nullptr, nullptr,
                                        0, MODE_APPLY, 0, 0, nullptr, nullptr);
   int* ctas_per_sm = &shape->ctas_per_sm;
   if (e != cudaSuccess) return e;
@@ -48,6 +49,7 @@ cudaError_t prepare_stage<double>(int order, StageShape* shape) {
   shape->cols = STAGE_BW;
   shape->tma = 0;
   shape->boxw = shape->rps = shape->nf = 0;
+  shape->fixbw = 0;
   return cudaGetLastError();
 }
 
@@ -58,9 +60,10 @@ int stage_boxw_max<double>(int cols) {
 }
 
 template <>
-int stage_occupancy<double>(int order, int boxw, int cols) {
+int stage_occupancy<double>(int order, int boxw, int cols, bool fixbw) {
   (void)boxw;
   (void)cols;
+  (void)fixbw;
   switch (order) {
     case 21: return v1_occupancy<double, 21>();
     case 42: return v1_occupancy<double, 42>();

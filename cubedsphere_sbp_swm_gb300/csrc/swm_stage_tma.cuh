@@ -269,7 +269,7 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
 // A unit takes its tensor maps from its instance (InstDev::maps, global
 // memory; batched launches) or from the kernel parameter (one instance).
 // slot_bw is the widest box width of the launch (ring slot size).
-template <class T, int ORD, int MODE, int CONS>
+template <class T, int ORD, int MODE, int CONS, bool FIXBW>
 __global__ void __launch_bounds__(CONS + 32)
     stage_tma_kernel(const __grid_constant__ StageMaps maps, InstDev<T> one,
                      const InstDev<T>* many, const WorkUnit* units, int nunits, int slot_bw,
@@ -294,7 +294,10 @@ __global__ void __launch_bounds__(CONS + 32)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 2 * NST * 8);
   T* xring = reinterpret_cast<T*>(smem + L::head);
   unsigned char* stg = smem + L::head + L::r128(L::xring);
-  const size_t st_bytes = L::stage(slot_bw).bytes;   // ring slot stride
+  // FIXBW: every box is the widest one, so every shared-memory offset is a
+  // compile-time constant (fewer address instructions and registers, more
+  // shared memory for narrow strips)
+  const size_t st_bytes = L::stage(FIXBW ? int(L::BOXW_MAX) : slot_bw).bytes;   // ring slot stride
   const int tid = threadIdx.x;
 
   if (tid == 0) {
@@ -325,7 +328,7 @@ __global__ void __launch_bounds__(CONS + 32)
         const int prow = wu.panel * I.n;        // row of this panel in the (6n)-row tensors
         const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
         const bool hasHs = I.hs != nullptr;
-        const int bw = I.boxw;
+        const int bw = FIXBW ? int(L::BOXW_MAX) : I.boxw;
         const StageOffsets e = stage_offsets<L>(bw, (int)sizeof(T));
         const uint32_t rowb = (uint32_t)(bw * RPS * (int)sizeof(T));  // one field, RPS rows
         for (int c = 0; c < nch; ++c, ++gc) {
@@ -378,7 +381,7 @@ __global__ void __launch_bounds__(CONS + 32)
   const int cal = wu.cl0 & ~(AL - 1);
   const int nch = (j1u + RMAX - rl0 + RPS - 1) / RPS;
   const bool hasHs = I.hs != nullptr;
-  const int bw = I.boxw;
+  const int bw = FIXBW ? int(L::BOXW_MAX) : I.boxw;
   const StageOffsets eo = stage_offsets<L>(bw, (int)sizeof(T));
   const int e_in = eo.in, e_met = eo.met, e_metf = eo.metf, e_base = eo.base, e_acc = eo.acc,
             e_lo = eo.lo, e_hs = eo.hs;
@@ -515,98 +518,111 @@ __global__ void __launch_bounds__(CONS + 32)
   }  // units
 }
 
-template <class T, int ORD, int MODE, int CONS>
+template <class T, int ORD, int MODE, int CONS, bool FIXBW>
 cudaError_t launch_stage_tma_mode(const StageMaps& maps, const InstDev<T>& one,
                                   const InstDev<T>* many, const WorkUnit* units, int nunits,
                                   int boxw, int grid, int* err, cudaStream_t st) {
   using L = TmaLayout<T, ORD, CONS>;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, MODE, CONS>,
+    cudaError_t e = cudaFuncSetAttribute(stage_tma_kernel<T, ORD, MODE, CONS, FIXBW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L::smem_bytes(L::BOXW_MAX));
     if (e != cudaSuccess) return e;
     configured = true;
   }
   if (nunits <= 0) return cudaSuccess;
-  if (boxw < 1 || boxw > L::BOXW_MAX) return cudaErrorInvalidValue;
+  if (boxw < 1 || boxw > L::BOXW_MAX || (FIXBW && boxw != L::BOXW_MAX)) return cudaErrorInvalidValue;
   const int g = (grid > 0 && grid < nunits) ? grid : nunits;
-  stage_tma_kernel<T, ORD, MODE, CONS><<<g, CONS + 32, L::smem_bytes(boxw), st>>>(
+  stage_tma_kernel<T, ORD, MODE, CONS, FIXBW><<<g, CONS + 32, L::smem_bytes(boxw), st>>>(
       maps, one, many, units, nunits, boxw, err);
   return cudaGetLastError();
 }
 
-template <class T, int ORD, int CONS>
+template <class T, int ORD, int CONS, bool FIXBW>
 cudaError_t launch_stage_tma_ord(const StageMaps& maps, const InstDev<T>& one,
                                  const InstDev<T>* many, const WorkUnit* units, int nunits,
                                  int mode, int boxw, int grid, int* err, cudaStream_t st) {
   switch (mode) {
-    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
-    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4, CONS>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_APPLY: return launch_stage_tma_mode<T, ORD, MODE_APPLY, CONS, FIXBW>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK1: return launch_stage_tma_mode<T, ORD, MODE_RK1, CONS, FIXBW>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK2: return launch_stage_tma_mode<T, ORD, MODE_RK2, CONS, FIXBW>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK3: return launch_stage_tma_mode<T, ORD, MODE_RK3, CONS, FIXBW>(maps, one, many, units, nunits, boxw, grid, err, st);
+    case MODE_RK4: return launch_stage_tma_mode<T, ORD, MODE_RK4, CONS, FIXBW>(maps, one, many, units, nunits, boxw, grid, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 // configure every mode (outside any capture)
-template <class T, int ORD, int CONS>
+template <class T, int ORD, int CONS, bool FIXBW>
 cudaError_t prepare_stage_tma_ord() {
   static const StageMaps kNone{};
   for (int m = MODE_APPLY; m <= MODE_RK4; ++m) {
-    cudaError_t e = launch_stage_tma_ord<T, ORD, CONS>(kNone, InstDev<T>{}, nullptr, nullptr, 0, m,
-                                                       TmaLayout<T, ORD, CONS>::BOXW_MAX, 0,
-                                                       nullptr, nullptr);
+    cudaError_t e = launch_stage_tma_ord<T, ORD, CONS, FIXBW>(kNone, InstDev<T>{}, nullptr, nullptr,
+                                                              0, m, TmaLayout<T, ORD, CONS>::BOXW_MAX,
+                                                              0, nullptr, nullptr);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
 // resident CTAs per SM at box width bw
-template <class T, int ORD, int CONS>
+template <class T, int ORD, int CONS, bool FIXBW>
 int stage_tma_occupancy(int bw) {
   int blocks = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_tma_kernel<T, ORD, MODE_RK2, CONS>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stage_tma_kernel<T, ORD, MODE_RK2, CONS, FIXBW>,
                                                 CONS + 32, TmaLayout<T, ORD, CONS>::smem_bytes(bw));
   return blocks;
 }
 
-// The FP32 stage kernel of one consumer width CONS for every SBP order
-// (instantiated by swm_stage_f32_w<CONS>.cu).
+// The FP32 stage kernel of one consumer width CONS for every SBP order and
+// both box modes (instantiated by swm_stage_f32_w<CONS>.cu).
 template <int CONS>
 struct StageF32Width {
-  static cudaError_t launch(int order, const StageMaps& m, const InstDev<float>& one,
-                            const InstDev<float>* many, const WorkUnit* units, int nunits,
-                            int mode, int boxw, int grid, int* err, cudaStream_t st) {
+  template <bool FIXBW>
+  static cudaError_t launch_fb(int order, const StageMaps& m, const InstDev<float>& one,
+                               const InstDev<float>* many, const WorkUnit* units, int nunits,
+                               int mode, int boxw, int grid, int* err, cudaStream_t st) {
     switch (order) {
-      case 21: return launch_stage_tma_ord<float, 21, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
-      case 42: return launch_stage_tma_ord<float, 42, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
-      case 43: return launch_stage_tma_ord<float, 43, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
-      case 63: return launch_stage_tma_ord<float, 63, CONS>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 21: return launch_stage_tma_ord<float, 21, CONS, FIXBW>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 42: return launch_stage_tma_ord<float, 42, CONS, FIXBW>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 43: return launch_stage_tma_ord<float, 43, CONS, FIXBW>(m, one, many, units, nunits, mode, boxw, grid, err, st);
+      case 63: return launch_stage_tma_ord<float, 63, CONS, FIXBW>(m, one, many, units, nunits, mode, boxw, grid, err, st);
       default: return cudaErrorInvalidValue;
     }
   }
-  static int occupancy(int order, int boxw) {
+  static cudaError_t launch(int order, bool fixbw, const StageMaps& m, const InstDev<float>& one,
+                            const InstDev<float>* many, const WorkUnit* units, int nunits,
+                            int mode, int boxw, int grid, int* err, cudaStream_t st) {
+    return fixbw ? launch_fb<true>(order, m, one, many, units, nunits, mode, boxw, grid, err, st)
+                 : launch_fb<false>(order, m, one, many, units, nunits, mode, boxw, grid, err, st);
+  }
+  template <bool FIXBW>
+  static int occupancy_fb(int order, int boxw) {
     switch (order) {
-      case 21: return stage_tma_occupancy<float, 21, CONS>(boxw);
-      case 42: return stage_tma_occupancy<float, 42, CONS>(boxw);
-      case 43: return stage_tma_occupancy<float, 43, CONS>(boxw);
-      default: return stage_tma_occupancy<float, 63, CONS>(boxw);
+      case 21: return stage_tma_occupancy<float, 21, CONS, FIXBW>(boxw);
+      case 42: return stage_tma_occupancy<float, 42, CONS, FIXBW>(boxw);
+      case 43: return stage_tma_occupancy<float, 43, CONS, FIXBW>(boxw);
+      default: return stage_tma_occupancy<float, 63, CONS, FIXBW>(boxw);
+    }
+  }
+  static int occupancy(int order, bool fixbw, int boxw) {
+    return fixbw ? occupancy_fb<true>(order, boxw) : occupancy_fb<false>(order, boxw);
+  }
+  template <bool FIXBW>
+  static cudaError_t prepare_fb(int order) {
+    switch (order) {
+      case 21: return prepare_stage_tma_ord<float, 21, CONS, FIXBW>();
+      case 42: return prepare_stage_tma_ord<float, 42, CONS, FIXBW>();
+      case 43: return prepare_stage_tma_ord<float, 43, CONS, FIXBW>();
+      case 63: return prepare_stage_tma_ord<float, 63, CONS, FIXBW>();
+      default: return cudaErrorInvalidValue;
     }
   }
   static cudaError_t prepare(int order) {
-    switch (order) {
-      case 21: return prepare_stage_tma_ord<float, 21, CONS>();
-      case 42: return prepare_stage_tma_ord<float, 42, CONS>();
-      case 43: return prepare_stage_tma_ord<float, 43, CONS>();
-      case 63: return prepare_stage_tma_ord<float, 63, CONS>();
-      default: return cudaErrorInvalidValue;
-    }
+    cudaError_t e = prepare_fb<false>(order);
+    return e == cudaSuccess ? prepare_fb<true>(order) : e;
   }
-  static constexpr int boxw_max() { return TmaLayout<float, 42, CONS>::BOXW_MAX; }
-  static constexpr int rps() { return TmaLayout<float, 42, CONS>::RPS; }
-  static constexpr int nf() { return TmaLayout<float, 42, CONS>::NF; }
 };
 
 }  // namespace swm

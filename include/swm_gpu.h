@@ -394,16 +394,24 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 /* ---------------------------------------------------------------------- */
 /* The stage kernel's launch shape: the consumer width of the FP32 kernel
  * (96, 128, 160 or 192 columns per CTA), the rows per work unit (0: enough
- * units for one wave of CTAs) and the persistent grid (0: one CTA per unit).
+ * units for one wave of CTAs), the persistent grid (0: one CTA per unit) and
+ * the box mode of the FP32 kernel's TMA loads: SWM_BOX_STRIP (the narrowest
+ * box that covers every column strip, its width a kernel argument),
+ * SWM_BOX_WIDEST (the width's widest box, a compile-time constant of the
+ * kernel; needs a field pitch of at least that box) or SWM_BOX_AUTO (the
+ * widest box where it fits and keeps the resident CTAs per SM).
  * The shape changes how the panels are split into work, not any node's
  * arithmetic (results are bit-identical).  The best shape depends on the
  * grid: swm_tune_stage times `steps` RK4 steps of dt per candidate on a copy
  * of s (s is not changed), keeps the fastest and returns it with its median
- * step time.  FP64 contexts have one width. */
+ * step time.  FP64 contexts have one width and ignore the box mode. */
+#define SWM_BOX_AUTO 0
+#define SWM_BOX_STRIP 1
+#define SWM_BOX_WIDEST 2
 int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
-                   int* seg_rows_out, int* grid_out, double* ms_out);
-int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* nunits);
-int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid);
+                   int* seg_rows_out, int* grid_out, int* box_out, double* ms_out);
+int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* box, int* nunits);
+int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid, int box);
 
 /* ---------------------------------------------------------------------- */
 /* Checkpoint / resume (no reference counterpart: the reference writes no   */

@@ -168,22 +168,29 @@ def test_state_roundtrip_fp32_pair_is_exact_to_fp64_split(cfg1):
     assert np.max(np.abs(gh - h) / np.abs(h)) < 1e-13
 
 
-@pytest.mark.parametrize("order,N", [(42, 48), (63, 64), (43, 40)])
+@pytest.mark.parametrize("order,N", [(42, 48), (63, 64), (43, 40), (42, 128), (63, 160)])
 def test_stage_shapes_are_bit_identical(order, N):
     """The FP32 stage kernel's launch shapes (consumer width, rows per unit,
-    persistent grid) split the panels differently but give bit-identical
-    steps; the tuner keeps the input state and picks one of the shapes."""
+    persistent grid, TMA box mode) split the panels differently but give
+    bit-identical steps; the tuner keeps the input state and picks one of the
+    shapes.  The widest box of width w is w + 4 columns and needs a field
+    pitch (N + 1 rounded up to 16) of at least that."""
     h, u, v, _ = initial.balanced_zonal(N, 2, 16)
     op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=order, precision="fp32"))
     assert op.stage_shape["width"] == 128
     x0 = op.create_stvec()
     x0.upload(h, u, v)
     ref = None
-    for w, seg, grid in ((96, 0, 0), (128, 0, 0), (160, 0, 0), (192, 0, 0), (128, 8, 0),
-                         (128, 8, 7), (192, 16, 3)):
-        op.set_stage_shape(w, seg, grid)
+    shapes = [(96, 0, 0, "strip"), (128, 0, 0, "strip"), (160, 0, 0, "strip"), (192, 0, 0, "strip"),
+              (128, 8, 0, "strip"), (128, 8, 7, "strip"), (192, 16, 3, "strip"), (96, 0, 0, "auto")]
+    pitch = (N + 1 + 15) // 16 * 16
+    wide = [w for w in (96, 128, 160, 192) if w + 4 <= pitch]
+    shapes += [(w, 0, 0, "widest") for w in wide] + [(w, 8, 7, "widest") for w in wide[:1]]
+    for w, seg, grid, box in shapes:
+        op.set_stage_shape(w, seg, grid, box)
         sh = op.stage_shape
         assert (sh["width"], sh["seg_rows"], sh["grid"]) == (w, seg, grid)
+        assert sh["box"] == box or box == "auto"
         x = x0.create_similar()
         x.assign_s1v1(1.0, x0)
         swm.RK4().step(x, op, 300.0, 3)
@@ -200,6 +207,12 @@ def test_stage_shapes_are_bit_identical(order, N):
         assert np.array_equal(a, b)
     with pytest.raises(swm.SwmError):
         op.set_stage_shape(100)
+    for w in (96, 128, 160, 192):
+        if w not in wide:
+            with pytest.raises(swm.SwmError):
+                op.set_stage_shape(w, 0, 0, "widest")
+    with pytest.raises(swm.SwmError):
+        op.set_stage_shape(128, 0, 0, "square")
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
