@@ -1191,7 +1191,9 @@ int hordiff_h_order(const char* name) {
   return 0;
 }
 
-constexpr int kDiffWork = 19;   // F 4, L 4, d1x 4, d1y 4, tendencies 3
+// work fields of the diffusion step: F 4, L 4, tendencies 3, and (FP64, for
+// the two-pass Laplacian) d1x 4, d1y 4
+constexpr int kDiffWorkF32 = 11, kDiffWorkF64 = 19;
 
 template <class T>
 NarrowTables<T> narrow_tables(swm_ctx* ctx, int narrow) {
@@ -1208,8 +1210,9 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
   if (ctx->n < 2 * narrow_rows(narrow))
     return fail(ctx, SWM_E_INVALID, "grid too small for the narrow Laplacian closures");
   if (!ctx->dw) {
-    CK(cudaMalloc(&ctx->dw, elt * kDiffWork * g.fs), "alloc");
-    CK(cudaMemsetAsync(ctx->dw, 0, elt * kDiffWork * g.fs, ctx->st), "memset");
+    const size_t nw = ctx->prec == SWM_FP64_PLAIN ? kDiffWorkF64 : kDiffWorkF32;
+    CK(cudaMalloc(&ctx->dw, elt * nw * g.fs), "alloc");
+    CK(cudaMemsetAsync(ctx->dw, 0, elt * nw * g.fs, ctx->st), "memset");
   }
   if (!ctx->b12) {
     CK(cudaMalloc(&ctx->b12, elt * 6 * g.fs), "alloc");
@@ -1259,13 +1262,14 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
 }
 
 // Synced Laplacian of nf fields src -> dst (laplace_Ah_sbp42_narrow_mod
-// .f90:23-58); work fields d1x, d1y of the diffusion workspace.
+// .f90:23-58); src and dst do not overlap; FP64 uses the d1 work fields.
 template <class T>
 int laplace_fields(swm_ctx* ctx, int narrow, int nf, const T* src, T* dst) {
   const FieldGeom& g = ctx->g64;
   T* edge = sizeof(T) == 8 ? (T*)ctx->edge64 : (T*)ctx->edge;
+  T* d1 = sizeof(T) == 8 ? dwork<T>(ctx, kDiffWorkF32) : nullptr;
   CK(launch_laplace<T>(g, ctx->topo, narrow_tables<T>(ctx, narrow), nf, src, metric_of<T>(ctx),
-                       ctx->hx * ctx->cfg.radius, dwork<T>(ctx, 8), dwork<T>(ctx, 12), dst, edge,
+                       ctx->hx * ctx->cfg.radius, d1, d1 ? d1 + 4 * g.fs : nullptr, dst, edge,
                        ctx->st),
      "laplace");
   return SWM_OK;
@@ -1313,13 +1317,13 @@ int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
   const long long fs = ctx->g64.fs;
   if (ctx->prec == SWM_FP64_PLAIN) {
     double* x = (double*)v0->hi;
-    double* T = dwork<double>(ctx, 16);
+    double* T = dwork<double>(ctx, 8);
     if (int rc = enqueue_diffusion_tend<double>(ctx, x, x + fs, x + 2 * fs, T, T + fs, T + 2 * fs))
       return rc;
     CK(launch_axpby(3 * fs, 1.0, x, dt, T, x, ctx->st), "update");
   } else {
     const float* x = (const float*)v0->hi;
-    float* T = dwork<float>(ctx, 16);
+    float* T = dwork<float>(ctx, 8);
     if (int rc = enqueue_diffusion_tend<float>(ctx, x, x + fs, x + 2 * fs, T, T + fs, T + 2 * fs))
       return rc;
     CK(launch_pair_axpy<float>(3 * fs, dt, T, (float*)v0->hi, v0->lo, ctx->st), "update");

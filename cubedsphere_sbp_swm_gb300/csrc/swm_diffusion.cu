@@ -12,16 +12,16 @@
 // per-node stencil coefficients are built once per context (in FP64, stored
 // in the element type): the interior stencil (2*hw+1 coefficients per node
 // and direction) as fields, the closure rows (rows x cols per line end) as
-// small tables.  A Laplacian is then two passes over the fields it is
-// applied to:
-//   1. d1x = D1x(f)*J*Qi12, d1y = D1y(f)*J*Qi12 (SBP first derivative of the
-//      same order);
-//   2. the narrow D2 in x and y from the precomputed coefficients, the
-//      cross-derivative boundary fluxes on the panel edges, the mixed terms
-//      D1y(d1x) + D1x(d1y), division by (hx*a)^2 and by J;
-// followed by the Ah scalar edge sync.  Every pass handles nf fields per
-// node so the coefficient loads are shared by h and the three Cartesian
-// velocity components.
+// small tables (FP32 contexts form the interior coefficients from the two b
+// fields instead).  A Laplacian computes d1x = D1x(f)*J*Qi12 and
+// d1y = D1y(f)*J*Qi12 (SBP first derivative of the same order), then the
+// narrow D2 in x and y, the cross-derivative boundary fluxes on the panel
+// edges, the mixed terms D1y(d1x) + D1x(d1y), division by (hx*a)^2 and by J;
+// followed by the Ah scalar edge sync.  FP32: one tiled pass with the first
+// derivatives in shared memory (lap_tile_kernel); FP64: two passes with the
+// first derivatives in work fields (lap_d1_kernel, lap_main_kernel).  Every
+// pass handles nf fields per node so the coefficient and metric loads are
+// shared by h and the three Cartesian velocity components.
 //
 // Element type T: double for FP64 contexts; float for FP32 contexts (the
 // tendency is small next to the state, which stays a compensated pair
@@ -150,6 +150,240 @@ __global__ void narrow_closure_kernel(FieldGeom g, const double* m, T* clx, T* c
   cly[e] = T(my);
 }
 
+// FP32 Laplacian tiles: a block of LTX x LTY threads computes the pre-sync
+// Laplacian of NF fields on a tile of LTX x LTY nodes of one panel, one node
+// per thread (laplace_Ah_sbp42_narrow_mod.f90:23-763 with the division by J
+// of lines 52-53).  Tiles start at multiples of the tile size; the last one
+// of a line is moved back to end on the panel edge (its nodes overlap the
+// previous tile's and get the same values), so a closure node's stencil stays
+// inside the tile's region: [a0 - R, a0 + len + R) clipped to the panel,
+// widened to the closure columns [0, cols) or [n - cols, n) when the tile
+// holds closure nodes.  The block stages in shared memory, for all NF fields
+// at once:
+//   the fields on the region;
+//   d1x = D1x(f)*J*Qi12 on the tile's columns x the region's rows and
+//   d1y = D1y(f)*J*Qi12 on the region's columns x the tile's rows
+//   (laplace_Ah_sbp42_narrow_mod.f90:60-93);
+// together with J and Qi12 on both d1 areas and (FP32) the variable
+// coefficients b, and then finishes its nodes from shared memory: the narrow
+// D2 in x and y, the cross-derivative boundary fluxes, the mixed terms
+// D1y(d1x) + D1x(d1y), the scaling, and the edge values for the sync.
+constexpr int LTX = 32, LTY = 8, LTPB = LTX * LTY;
+
+template <int NARROW, int NF>
+struct LapTile {
+  using S = NarrowShape<NARROW>;
+  static constexpr int H1 = Ord<NARROW>::H;          // first-derivative interior half width
+  static constexpr int R = S::hw > H1 ? S::hw : H1;  // interior reach
+  // widest region of a tile of length L: L + R on the inner side, and on
+  // the outer side R, or the rest of the closure columns when the tile
+  // starts inside the closure rows.  A row tile (LTY < rows) can also start
+  // inside the closure rows of one end and reach those of the other (small
+  // panels): its region is then the whole line, shorter than 2 rows + LTY - 1.
+  static constexpr int EXT = R + (R > S::rows - 1 ? R : S::rows - 1);
+  static constexpr int RX = LTX + EXT;
+  static constexpr int RY = LTY + (EXT > 2 * S::rows - 2 ? EXT : 2 * S::rows - 2);
+  // shared-memory arrays, in floats: fields, d1x, d1y, then J and Qi12 on
+  // the d1x and d1y areas, then b_x and b_y
+  static constexpr int NDX = RY * LTX, NDY = LTY * RX;
+  static constexpr int OFS_DX = NF * RY * RX, OFS_DY = OFS_DX + NF * NDX;
+  static constexpr int OFS_JX = OFS_DY + NF * NDY, OFS_QX = OFS_JX + NDX;
+  static constexpr int OFS_JY = OFS_QX + NDX, OFS_QY = OFS_JY + NDY;
+  static constexpr int OFS_BX = OFS_QY + NDY, OFS_BY = OFS_BX + NDY;
+  static constexpr size_t bytes = sizeof(float) * (size_t)(OFS_BY + NDX);
+};
+
+// region [lo, hi) of a tile [a0, a0 + len) along a line of n nodes
+template <int NARROW>
+__device__ __forceinline__ void lap_region(int a0, int len, int n, int& lo, int& hi) {
+  using S = NarrowShape<NARROW>;
+  constexpr int R = LapTile<NARROW, 1>::R;
+  lo = max(0, a0 - R);
+  hi = min(n, a0 + len + R);
+  if (a0 < S::rows) {
+    lo = 0;
+    hi = max(hi, min(n, S::cols));
+  }
+  if (a0 + len > n - S::rows) {
+    hi = n;
+    lo = min(lo, max(0, n - S::cols));
+  }
+}
+
+template <int NARROW, int NF>
+__global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty, const float* f,
+                                                           const float* clx, const float* cly,
+                                                           const float* bco, const float* mt,
+                                                           double hs, float* out, float* E) {
+  using T = float;
+  using S = NarrowShape<NARROW>;
+  using LT = LapTile<NARROW, NF>;
+  constexpr int RX = LT::RX, RY = LT::RY;
+  extern __shared__ __align__(16) unsigned char lap_smem[];
+  T* sm = reinterpret_cast<T*>(lap_smem);
+  T(*Fs)[RY][RX] = reinterpret_cast<T(*)[RY][RX]>(sm);
+  T(*DXs)[RY][LTX] = reinterpret_cast<T(*)[RY][LTX]>(sm + LT::OFS_DX);
+  T(*DYs)[LTY][RX] = reinterpret_cast<T(*)[LTY][RX]>(sm + LT::OFS_DY);
+  T(*JXs)[LTX] = reinterpret_cast<T(*)[LTX]>(sm + LT::OFS_JX);
+  T(*QXs)[LTX] = reinterpret_cast<T(*)[LTX]>(sm + LT::OFS_QX);
+  T(*JYs)[RX] = reinterpret_cast<T(*)[RX]>(sm + LT::OFS_JY);
+  T(*QYs)[RX] = reinterpret_cast<T(*)[RX]>(sm + LT::OFS_QY);
+  T(*BXs)[RX] = reinterpret_cast<T(*)[RX]>(sm + LT::OFS_BX);
+  T(*BYs)[LTX] = reinterpret_cast<T(*)[LTX]>(sm + LT::OFS_BY);
+
+  const NarrowD2& D = c_narrow[S::ni];
+  const int n = g.n, P = g.P;
+  const int p = blockIdx.y / nty, ty = blockIdx.y - p * nty;
+  const int tw = min(LTX, n), th = min(LTY, n);
+  const int i0 = min((int)blockIdx.x * LTX, n - tw), j0 = min(ty * LTY, n - th);
+  int xlo, xhi, ylo, yhi;
+  lap_region<NARROW>(i0, tw, n, xlo, xhi);
+  lap_region<NARROW>(j0, th, n, ylo, yhi);
+  const int rx = xhi - xlo, ry = yhi - ylo;
+  const long long pb = (long long)p * g.ps;
+  const int lx = threadIdx.x, ly = threadIdx.y;
+
+  // stage the fields on the region, the metric on the d1 areas and b.
+  // Region rows go to thread rows, region columns to lanes.
+  const T* MJp = mt + MJ * g.fs + pb;
+  const T* MQp = mt + MQI2 * g.fs + pb;
+  for (int y = ly; y < ry; y += LTY) {
+    const long long rowa = (long long)(ylo + y) * P;
+    for (int x = lx; x < rx; x += LTX) {
+#pragma unroll
+      for (int c = 0; c < NF; ++c) Fs[c][y][x] = f[c * g.fs + pb + rowa + xlo + x];
+    }
+    if (lx < tw) {
+      const long long a = rowa + i0 + lx;
+      JXs[y][lx] = MJp[a];
+      QXs[y][lx] = MQp[a];
+      BYs[y][lx] = bco[g.fs + pb + a];
+    }
+  }
+  if (ly < th) {
+    const long long rowa = (long long)(j0 + ly) * P;
+    for (int x = lx; x < rx; x += LTX) {
+      const long long a = rowa + xlo + x;
+      JYs[ly][x] = MJp[a];
+      QYs[ly][x] = MQp[a];
+      BXs[ly][x] = bco[pb + a];
+    }
+  }
+  __syncthreads();
+
+  // d1x on the tile's columns x the region's rows, d1y on the region's
+  // columns x the tile's rows
+  if (lx < tw) {
+    const int i = i0 + lx;
+    for (int y = ly; y < ry; y += LTY) {
+      const T jq = JXs[y][lx], qq = QXs[y][lx];
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const T dx = d_line<NARROW, T>(i, n, [&](int q) { return Fs[c][y][q - xlo]; });
+        DXs[c][y][lx] = dx * jq * qq;
+      }
+    }
+  }
+  if (ly < th) {
+    const int j = j0 + ly;
+    for (int x = lx; x < rx; x += LTX) {
+      const T jq = JYs[ly][x], qq = QYs[ly][x];
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const T dy = d_line<NARROW, T>(j, n, [&](int q) { return Fs[c][q - ylo][x]; });
+        DYs[c][ly][x] = dy * jq * qq;
+      }
+    }
+  }
+  __syncthreads();
+  if (lx >= tw || ly >= th) return;
+
+  const int i = i0 + lx, j = j0 + ly;
+  const int yr = j - ylo, xr = i - xlo;
+  const bool clxn = i < S::rows || i >= n - S::rows;
+  const bool clyn = j < S::rows || j >= n - S::rows;
+  // stencil of this node in x and y: coefficients and tap offsets in the
+  // region; the interior uses the first w taps
+  T ax[S::cols], ay[S::cols];
+  int x0, xs, y0, ys;
+  T rsx = T(1), rsy = T(1);
+  if (clxn) {
+    const int side = i < S::rows ? 0 : 1, r = side ? n - 1 - i : i;
+    const T* M = clx + ((((long long)p * n + j) * 2 + side) * S::rows + r) * S::cols;
+#pragma unroll
+    for (int c = 0; c < S::cols; ++c) ax[c] = M[c];
+    x0 = (side ? n - 1 : 0) - xlo; xs = side ? -1 : 1;
+    rsx = T(D.rowscale[r]);
+  } else {   // from the variable coefficients along the row
+#pragma unroll
+    for (int c = 0; c < S::cols; ++c) {
+      T acc = T(0);
+      if (c < S::w) {
+#pragma unroll
+        for (int q = 0; q < S::w; ++q) acc += c_in32.v[S::ni][c][q] * BXs[ly][xr - S::hw + q];
+      }
+      ax[c] = acc;
+    }
+    x0 = xr - S::hw; xs = 1;
+  }
+  if (clyn) {
+    const int side = j < S::rows ? 0 : 1, r = side ? n - 1 - j : j;
+    const T* M = cly + ((((long long)p * n + i) * 2 + side) * S::rows + r) * S::cols;
+#pragma unroll
+    for (int c = 0; c < S::cols; ++c) ay[c] = M[c];
+    y0 = (side ? n - 1 : 0) - ylo; ys = side ? -1 : 1;
+    rsy = T(D.rowscale[r]);
+  } else {   // from the variable coefficients along the column
+#pragma unroll
+    for (int c = 0; c < S::cols; ++c) {
+      T acc = T(0);
+      if (c < S::w) {
+#pragma unroll
+        for (int q = 0; q < S::w; ++q) acc += c_in32.v[S::ni][c][q] * BYs[yr - S::hw + q][lx];
+      }
+      ay[c] = acc;
+    }
+    y0 = yr - S::hw; ys = 1;
+  }
+  const int ntx = clxn ? S::cols : S::w, nty_ = clyn ? S::cols : S::w;
+  const T J = JXs[yr][lx];
+  const T hs2 = T(hs * hs);
+  const T pen = T(D.penalty);
+#pragma unroll
+  for (int c = 0; c < NF; ++c) {
+    T sx = T(0), sy = T(0);
+#pragma unroll
+    for (int t = 0; t < S::cols; ++t)
+      if (t < ntx) sx += ax[t] * Fs[c][yr][x0 + xs * t];
+#pragma unroll
+    for (int t = 0; t < S::cols; ++t)
+      if (t < nty_) sy += ay[t] * Fs[c][y0 + ys * t][xr];
+    T d2x = clxn ? rsx * sx : sx;
+    const T d2y = clyn ? rsy * sy : sy;
+    const T dxo = DXs[c][yr][lx], dyo = DYs[c][ly][xr];
+    if (i == 0) d2x = d2x - T(0.5) * (pen * (T(-2) * dyo));
+    if (i == n - 1) d2x = d2x - T(0.5) * (pen * (T(2) * dyo));
+    if (j == 0) d2x = d2x - T(0.5) * (pen * (T(-2) * dxo));
+    if (j == n - 1) d2x = d2x - T(0.5) * (pen * (T(2) * dxo));
+    const T d2yx = d_line<NARROW, T>(j, n, [&](int q) { return DXs[c][q - ylo][lx]; });
+    const T d2xy = d_line<NARROW, T>(i, n, [&](int q) { return DYs[c][ly][q - xlo]; });
+    T v = d2x + d2y;
+    v = v + d2xy + d2yx;
+    v = v / hs2;
+    v = v / J;
+    out[c * g.fs + pb + (long long)j * P + i] = v;
+    // panel-boundary values also go to value slot c of the edge buffer
+    auto put = [&](int side, int q) { E[((long long)(p * 4 + side) * 4 + c) * n + q] = v; };
+    if (i == 0) put(SIDE_L, j);
+    if (i == n - 1) put(SIDE_R, j);
+    if (j == 0) put(SIDE_B, i);
+    if (j == n - 1) put(SIDE_T, i);
+  }
+}
+
+// FP64 Laplacian, two passes of one node per thread.  GB300's FP64 rate
+// bounds them, so they compute every first derivative once and keep it in
+// work fields rather than recompute the tile halos of the FP32 kernel.
 // Pass 1: d1x = D1x(f)*J*Qi12, d1y = D1y(f)*J*Qi12 of NF fields
 // (laplace_Ah_sbp42_narrow_mod.f90:60-93).
 template <class T, int NARROW, int NF>
@@ -175,8 +409,8 @@ __global__ void __launch_bounds__(RTPB) lap_d1_kernel(FieldGeom g, const T* f, c
 template <class T, int NARROW, int NF>
 __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f, const T* d1x,
                                                         const T* d1y, const T* cx, const T* cy,
-                                                        const T* clx, const T* cly, const T* bco,
-                                                        const T* mt, double hs, T* out, T* E) {
+                                                        const T* clx, const T* cly, const T* mt,
+                                                        double hs, T* out, T* E) {
   using S = NarrowShape<NARROW>;
   Node k;
   if (!node_here(g, k)) return;
@@ -199,23 +433,8 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     x0 = k.j * P + (side ? n - 1 : 0); xs = side ? -1 : 1;
     rsx = T(D.rowscale[r]);
   } else {
-    if constexpr (sizeof(T) == 4) {   // from the variable coefficients along the row
-      T bb[S::w];
 #pragma unroll
-      for (int q = 0; q < S::w; ++q) bb[q] = bco[pb + o + q - S::hw];
-#pragma unroll
-      for (int c = 0; c < S::cols; ++c) {
-        T acc = T(0);
-        if (c < S::w) {
-#pragma unroll
-          for (int q = 0; q < S::w; ++q) acc += c_in32.v[S::ni][c][q] * bb[q];
-        }
-        ax[c] = acc;
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
-    }
+    for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
     x0 = o - S::hw; xs = 1;
   }
   if (clyn) {
@@ -226,23 +445,8 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     y0 = (side ? n - 1 : 0) * P + k.i; ys = side ? -P : P;
     rsy = T(D.rowscale[r]);
   } else {
-    if constexpr (sizeof(T) == 4) {   // from the variable coefficients along the column
-      T bb[S::w];
 #pragma unroll
-      for (int q = 0; q < S::w; ++q) bb[q] = bco[g.fs + pb + o + (q - S::hw) * P];
-#pragma unroll
-      for (int c = 0; c < S::cols; ++c) {
-        T acc = T(0);
-        if (c < S::w) {
-#pragma unroll
-          for (int q = 0; q < S::w; ++q) acc += c_in32.v[S::ni][c][q] * bb[q];
-        }
-        ay[c] = acc;
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
-    }
+    for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
     y0 = o - S::hw * P; ys = P;
   }
   const int ntx = clxn ? S::cols : S::w, nty = clyn ? S::cols : S::w;
@@ -363,10 +567,47 @@ long long narrow_closure_count(int narrow, int n) {
   return 6LL * n * 2 * narrow_rows(narrow) * narrow_cols(narrow);
 }
 
+template <class T, int NARROW, int NF>
+cudaError_t laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f, const T* mt, double hs,
+                       T* d1x, T* d1y, T* out, T* edge, cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    const int nty = (g.n + LTY - 1) / LTY;
+    const dim3 grid((g.n + LTX - 1) / LTX, 6 * nty), block(LTX, LTY);
+    lap_tile_kernel<NARROW, NF><<<grid, block, LapTile<NARROW, NF>::bytes, st>>>(
+        g, nty, f, t.clx, t.cly, t.b, mt, hs, out, edge);
+  } else {
+    if (!d1x || !d1y) return cudaErrorInvalidValue;
+    lap_d1_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(g, f, mt, d1x, d1y);
+    lap_main_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(
+        g, f, d1x, d1y, t.cx, t.cy, t.clx, t.cly, mt, hs, out, edge);
+  }
+  return cudaGetLastError();
+}
+
+// Shared memory above the default 48 KB for the FP32 Laplacian tiles of one
+// order (set outside any stream capture).
+template <int NARROW>
+cudaError_t prepare_laplace_order() {
+  cudaError_t e = cudaFuncSetAttribute(lap_tile_kernel<NARROW, 1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)LapTile<NARROW, 1>::bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(lap_tile_kernel<NARROW, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)LapTile<NARROW, 3>::bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(lap_tile_kernel<NARROW, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)LapTile<NARROW, 4>::bytes);
+  return e;
+}
+
 template <class T>
 cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, const double* m,
                                  cudaStream_t st) {
   const long long ncl = narrow_closure_count(t.narrow, g.n);
+  if constexpr (sizeof(T) == 4) {
+    cudaError_t e = t.narrow == 63 ? prepare_laplace_order<63>() : prepare_laplace_order<42>();
+    if (e != cudaSuccess) return e;
+  }
   if (t.narrow == 63) {
     narrow_coef_kernel<T, 63><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy, t.b);
     narrow_closure_kernel<T, 63><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
@@ -377,28 +618,22 @@ cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, c
   return cudaGetLastError();
 }
 
-template <class T, int NARROW, int NF>
-void laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f, const T* mt, double hs,
-                T* d1x, T* d1y, T* out, T* edge, cudaStream_t st) {
-  lap_d1_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(g, f, mt, d1x, d1y);
-  lap_main_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(
-      g, f, d1x, d1y, t.cx, t.cy, t.clx, t.cly, t.b, mt, hs, out, edge);
-}
-
 template <class T>
 cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowTables<T>& t, int nf,
                            const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out, T* edge,
                            cudaStream_t st) {
   if (nf != 1 && nf != 3 && nf != 4) return cudaErrorInvalidValue;
+  cudaError_t e;
   if (t.narrow == 63) {
-    if (nf == 1) laplace_nf<T, 63, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else if (nf == 3) laplace_nf<T, 63, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else laplace_nf<T, 63, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    if (nf == 1) e = laplace_nf<T, 63, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else if (nf == 3) e = laplace_nf<T, 63, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else e = laplace_nf<T, 63, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
   } else {
-    if (nf == 1) laplace_nf<T, 42, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else if (nf == 3) laplace_nf<T, 42, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else laplace_nf<T, 42, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    if (nf == 1) e = laplace_nf<T, 42, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else if (nf == 3) e = laplace_nf<T, 42, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    else e = laplace_nf<T, 42, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
   }
+  if (e != cudaSuccess) return e;
   const int nb = 6 * (4 * g.n - 4);
   sync_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, tp, nf, edge, out);
   return cudaGetLastError();

@@ -169,8 +169,10 @@ template <class T>
 cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, const double* m,
                                  cudaStream_t st);
 // Edge-synced Laplacian of nf = 1, 3 or 4 fields f into out (all at field
-// stride g.fs); mt: metric of element type T; d1x, d1y: nf work fields
-// each; hs = hx * radius; edge: edge buffer of element type T
+// stride g.fs, out must not overlap f); mt: metric of element type T;
+// hs = hx * radius; edge: edge buffer of element type T; d1x, d1y: nf work
+// fields each (FP64; FP32 passes null).  The tables' launcher must have run
+// first (it sets the FP32 tile kernel's shared memory).
 template <class T>
 cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowTables<T>& t, int nf,
                            const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out, T* edge,
