@@ -240,6 +240,10 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
   lap_region<NARROW>(i0, tw, n, xlo, xhi);
   lap_region<NARROW>(j0, th, n, ylo, yhi);
   const int rx = xhi - xlo, ry = yhi - ylo;
+  // tiles without closure nodes in a direction take the interior first
+  // derivative there without the per-node closure tests
+  const bool xin = i0 >= S::rows && i0 + tw <= n - S::rows;
+  const bool yin = j0 >= S::rows && j0 + th <= n - S::rows;
   const long long pb = (long long)p * g.ps;
   const int lx = threadIdx.x, ly = threadIdx.y;
 
@@ -279,7 +283,9 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
       const T jq = JXs[y][lx], qq = QXs[y][lx];
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
-        const T dx = d_line<NARROW, T>(i, n, [&](int q) { return Fs[c][y][q - xlo]; });
+        auto fa = [&](int q) { return Fs[c][y][q - xlo]; };
+        const T dx = xin ? d_interior<NARROW, T>([&](int o) { return fa(i + o); })
+                         : d_line<NARROW, T>(i, n, fa);
         DXs[c][y][lx] = dx * jq * qq;
       }
     }
@@ -290,7 +296,9 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
       const T jq = JYs[ly][x], qq = QYs[ly][x];
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
-        const T dy = d_line<NARROW, T>(j, n, [&](int q) { return Fs[c][q - ylo][x]; });
+        auto fa = [&](int q) { return Fs[c][q - ylo][x]; };
+        const T dy = yin ? d_interior<NARROW, T>([&](int o) { return fa(j + o); })
+                         : d_line<NARROW, T>(j, n, fa);
         DYs[c][ly][x] = dy * jq * qq;
       }
     }
@@ -345,19 +353,27 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
     }
     y0 = yr - S::hw; ys = 1;
   }
-  const int ntx = clxn ? S::cols : S::w, nty_ = clyn ? S::cols : S::w;
   const T J = JXs[yr][lx];
   const T hs2 = T(hs * hs);
   const T pen = T(D.penalty);
 #pragma unroll
   for (int c = 0; c < NF; ++c) {
+    // the closure rows read cols taps, the interior w (same order)
     T sx = T(0), sy = T(0);
+    if (clxn) {
 #pragma unroll
-    for (int t = 0; t < S::cols; ++t)
-      if (t < ntx) sx += ax[t] * Fs[c][yr][x0 + xs * t];
+      for (int t = 0; t < S::cols; ++t) sx += ax[t] * Fs[c][yr][x0 + xs * t];
+    } else {
 #pragma unroll
-    for (int t = 0; t < S::cols; ++t)
-      if (t < nty_) sy += ay[t] * Fs[c][y0 + ys * t][xr];
+      for (int t = 0; t < S::w; ++t) sx += ax[t] * Fs[c][yr][x0 + t];
+    }
+    if (clyn) {
+#pragma unroll
+      for (int t = 0; t < S::cols; ++t) sy += ay[t] * Fs[c][y0 + ys * t][xr];
+    } else {
+#pragma unroll
+      for (int t = 0; t < S::w; ++t) sy += ay[t] * Fs[c][y0 + t][xr];
+    }
     T d2x = clxn ? rsx * sx : sx;
     const T d2y = clyn ? rsy * sy : sy;
     const T dxo = DXs[c][yr][lx], dyo = DYs[c][ly][xr];
@@ -365,8 +381,12 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
     if (i == n - 1) d2x = d2x - T(0.5) * (pen * (T(2) * dyo));
     if (j == 0) d2x = d2x - T(0.5) * (pen * (T(-2) * dxo));
     if (j == n - 1) d2x = d2x - T(0.5) * (pen * (T(2) * dxo));
-    const T d2yx = d_line<NARROW, T>(j, n, [&](int q) { return DXs[c][q - ylo][lx]; });
-    const T d2xy = d_line<NARROW, T>(i, n, [&](int q) { return DYs[c][ly][q - xlo]; });
+    auto fdx = [&](int q) { return DXs[c][q - ylo][lx]; };
+    auto fdy = [&](int q) { return DYs[c][ly][q - xlo]; };
+    const T d2yx = yin ? d_interior<NARROW, T>([&](int o) { return fdx(j + o); })
+                       : d_line<NARROW, T>(j, n, fdx);
+    const T d2xy = xin ? d_interior<NARROW, T>([&](int o) { return fdy(i + o); })
+                       : d_line<NARROW, T>(i, n, fdy);
     T v = d2x + d2y;
     v = v + d2xy + d2yx;
     v = v / hs2;

@@ -115,6 +115,25 @@ def test_fp32_model_step_tracks_fp64():
         assert rel_l2(a, b, J) <= 1e-5
 
 
+@pytest.mark.parametrize("N,narrow", [(16, 42), (20, 42), (17, 63), (23, 63), (40, 63)])
+def test_fp32_diffusion_small_panels(N, narrow):
+    """The FP32 Laplacian's tiles at the smallest panels the closures allow,
+    where a row tile starts inside the closure rows of one end and reaches
+    those of the other: the FP32 tendency stays within 1e-4 of FP64."""
+    res = {}
+    for prec in ("fp64", "fp32"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision=prec))
+        dop = swm.OperatorSWMDiff(op, UV[narrow], 0.03, H[narrow], 0.01)
+        x, t = op.create_stvec(), op.create_stvec()
+        x.upload(*_state(N))
+        dop.apply(t, x)
+        res[prec] = t.download()
+    J = oracle.OracleDomain(N, 42).geometry()["J"]
+    for a, b in zip(res["fp32"], res["fp64"]):
+        assert np.all(np.isfinite(a))
+        assert rel_l2(a, b, J) <= 1e-4
+
+
 def test_fp32_diffusion_tendency_tracks_fp64():
     N = 48
     res = {}
