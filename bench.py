@@ -418,6 +418,7 @@ def run_gpu_arm(args):
     import torch
 
     import cubedsphere_sbp_swm_gb300 as swm
+    from cubedsphere_sbp_swm_gb300 import replicas
 
     w = WORKLOADS[args.workload]
     N, ORDER, DT = w["N"], w["order"], w["dt"]
@@ -491,13 +492,9 @@ def run_gpu_arm(args):
     clocks = clk.summary()
     import numpy as np
     finite = bool(all(np.isfinite(a).all() for a in s32.download()))
-    total_ms = sum(ms32)
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    value, total_s = replicas.job_rate(args.steps, sum(ms32) / 1e3, dev)
+    total_ms = total_s * 1e3
     ms_per_step = total_ms / args.steps
-    value = ws * args.steps / (total_ms / 1e3)
     if args.quick:  # profiling case: only the timed FP32 steps
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "steps/s",
@@ -537,12 +534,7 @@ def run_gpu_arm(args):
         s32.upload_async(*hin)
         ts.step(s32, op32, DT, 1)
         s32.download(out=hout)
-    e2e_s = time.perf_counter() - t0
-    e2e_val = ws * e2e_steps / e2e_s
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_val = ws * e2e_steps / float(t.item())
+    e2e_val, _ = replicas.job_rate(e2e_steps, time.perf_counter() - t0, dev)
     del s32, op32
 
     # FP32 form against the FP64 plain path over the workload's simulated days
