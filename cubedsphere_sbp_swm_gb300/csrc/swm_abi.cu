@@ -1275,13 +1275,18 @@ int laplace_fields(swm_ctx* ctx, int narrow, int nf, const T* src, T* dst) {
   return SWM_OK;
 }
 
-// Diffusion tendencies of the fields (h, u, v) into (th, tu, tv)
-// (operator_swm_diff_mod.f90:25-46): the xyz-vector operator on (u, v)
-// (hordiff_colocated_mod.f90:41-58) and the scalar one on h
-// (hordiff_scalar_mod.f90:33-53), each -(c^4) L(L(.)) with
-// c = coeff*radius*hx (hordiff_factory_mod.f90:183).
+// -(c^4) for a diffusion coefficient, c = coeff*radius*hx
+// (hordiff_factory_mod.f90:183)
+double diff_coeff4(const swm_ctx* ctx, double coeff) {
+  const double dc = coeff * ctx->cfg.radius * ctx->hx;
+  const double dc2 = dc * dc;
+  return -1.0 * (dc2 * dc2);
+}
+
+// L(L(.)) of h and of the Cartesian components b1*u + b2*v of the velocity
+// into the work fields 0 (h) and 1..3 (x, y, z).
 template <class T>
-int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* th, T* tu, T* tv) {
+int enqueue_biharmonic(swm_ctx* ctx, const T* h, const T* u, const T* v) {
   const FieldGeom& g = ctx->g64;
   const long long fs = g.fs;
   T* F = dwork<T>(ctx, 0);
@@ -1297,13 +1302,20 @@ int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* 
     if (int rc = laplace_fields<T>(ctx, ctx->diff_uv, 3, F + fs, L + fs)) return rc;
     if (int rc = laplace_fields<T>(ctx, ctx->diff_uv, 3, L + fs, F + fs)) return rc;
   }
-  auto coeff4 = [&](double coeff) {
-    const double dc = coeff * ctx->cfg.radius * ctx->hx;
-    const double dc2 = dc * dc;
-    return -1.0 * (dc2 * dc2);
-  };
-  CK(launch_diff_tendency<T>(g, (const T*)ctx->b12, coeff4(ctx->diff_uv_coeff), F + fs, tu, tv,
-                             coeff4(ctx->diff_h_coeff), F, th, ctx->st),
+  return SWM_OK;
+}
+
+// Diffusion tendencies of the fields (h, u, v) into (th, tu, tv)
+// (operator_swm_diff_mod.f90:25-46): the xyz-vector operator on (u, v)
+// (hordiff_colocated_mod.f90:41-58) and the scalar one on h
+// (hordiff_scalar_mod.f90:33-53), each -(c^4) L(L(.)).
+template <class T>
+int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* th, T* tu, T* tv) {
+  const FieldGeom& g = ctx->g64;
+  if (int rc = enqueue_biharmonic<T>(ctx, h, u, v)) return rc;
+  const T* F = dwork<T>(ctx, 0);
+  CK(launch_diff_tendency<T>(g, (const T*)ctx->b12, diff_coeff4(ctx, ctx->diff_uv_coeff), F + g.fs,
+                             tu, tv, diff_coeff4(ctx, ctx->diff_h_coeff), F, th, ctx->st),
      "tendency");
   T* edge = sizeof(T) == 8 ? (T*)ctx->edge64 : (T*)ctx->edge;
   CK(launch_sync_vector_t<T>(g, ctx->topo, ctx->qw, tu, tv, edge, ctx->st), "vector sync");
@@ -1312,7 +1324,8 @@ int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* 
 
 // One explicit Euler step of the diffusion operator (explicit_Eul1_mod.f90:
 // 20-30): v0 = v0 + dt * D(v0).  FP32 contexts take the tendency of the
-// high part in FP32 and update the (hi, lo) pair in FP64.
+// high part in FP32 and add it to the (hi, lo) pair with a two-sum, fused
+// with the tendency and the sync (launch_diff_update_f32).
 int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
   const long long fs = ctx->g64.fs;
   if (ctx->prec == SWM_FP64_PLAIN) {
@@ -1322,11 +1335,15 @@ int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
       return rc;
     CK(launch_axpby(3 * fs, 1.0, x, dt, T, x, ctx->st), "update");
   } else {
-    const float* x = (const float*)v0->hi;
+    float* x = (float*)v0->hi;
+    if (int rc = enqueue_biharmonic<float>(ctx, x, x + fs, x + 2 * fs)) return rc;
+    const float* F = dwork<float>(ctx, 0);
     float* T = dwork<float>(ctx, 8);
-    if (int rc = enqueue_diffusion_tend<float>(ctx, x, x + fs, x + 2 * fs, T, T + fs, T + 2 * fs))
-      return rc;
-    CK(launch_pair_axpy<float>(3 * fs, dt, T, (float*)v0->hi, v0->lo, ctx->st), "update");
+    CK(launch_diff_update_f32(ctx->g64, ctx->topo, ctx->qw, (const float*)ctx->b12,
+                              diff_coeff4(ctx, ctx->diff_uv_coeff), F + fs,
+                              diff_coeff4(ctx, ctx->diff_h_coeff), F, dt, x, v0->lo, T + fs,
+                              T + 2 * fs, (float*)ctx->edge, ctx->st),
+       "update");
   }
   return SWM_OK;
 }

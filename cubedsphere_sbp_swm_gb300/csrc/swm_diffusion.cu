@@ -534,27 +534,89 @@ __global__ void from_cart_kernel(FieldGeom g, const T* b, T cuv, const T* L, T* 
   th[k.idx] = ch * Lh[k.idx];
 }
 
-// FP32 (hi, lo) pair += dt * t: the increment joins the low part, then a
-// two-sum renormalises the pair (the compensated update of the RK4 stage
-// epilogue); FP64 tendencies are added in FP64.
+// FP32 (hi, lo) pair element k += dt * t: the increment joins the low part,
+// then a two-sum renormalises the pair (the compensated update of the RK4
+// stage epilogue).
+__device__ __forceinline__ void pair_add(double dt, float t, float* hi, float* lo, long long k) {
+  const float d = float(dt) * t;
+  const float h = hi[k];
+  const float tt = lo[k] + d;
+  const float sm = h + tt;
+  const float bb = sm - h;
+  hi[k] = sm;
+  lo[k] = (h - (sm - bb)) + (tt - bb);
+}
+
+// (hi, lo) pair += dt * t over count elements; FP64 tendencies are added in
+// FP64.
 template <class T>
 __global__ void pair_axpy_kernel(long long count, double dt, const T* t, float* hi, float* lo) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   if constexpr (sizeof(T) == 4) {
-    const float d = float(dt) * t[k];
-    const float h = hi[k];
-    const float tt = lo[k] + d;
-    const float sm = h + tt;
-    const float bb = sm - h;
-    hi[k] = sm;
-    lo[k] = (h - (sm - bb)) + (tt - bb);
+    pair_add(dt, t[k], hi, lo, k);
   } else {
     const double y = ((double)hi[k] + (double)lo[k]) + dt * (double)t[k];
     const float h = (float)y;
     hi[k] = h;
     lo[k] = (float)(y - (double)h);
   }
+}
+
+// The FP32 diffusion step's update of the (hi, lo) state, in two launches
+// with the arithmetic of from_cart_kernel, the covariant vector sync and
+// pair_axpy_kernel:
+//   diff_update_kernel: the tendencies (th, tu, tv) of every node; h and the
+//     velocity's inner nodes are added to the pair at once; the velocity's
+//     panel-boundary nodes store their tendencies in (tu, tv) and in the
+//     edge buffer's GX/GY slots;
+//   diff_sync_update_kernel: those nodes' covariant sync
+//     (ecs_Ah_vec_sync_mod.f90:62-125), then their pair update.
+__global__ void diff_update_kernel(FieldGeom g, const float* b, float cuv, const float* L, float ch,
+                                   const float* Lh, double dt, float* hi, float* lo, float* tu,
+                                   float* tv, float* E) {
+  Node k;
+  if (!node_here(g, k)) return;
+  const long long fs = g.fs;
+  float t[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) t[a] = cuv * L[a * fs + k.idx];
+  const float ut = t[0] * b[k.idx] + t[1] * b[fs + k.idx] + t[2] * b[2 * fs + k.idx];
+  const float vt = t[0] * b[3 * fs + k.idx] + t[1] * b[4 * fs + k.idx] + t[2] * b[5 * fs + k.idx];
+  pair_add(dt, ch * Lh[k.idx], hi, lo, k.idx);
+  const int n = g.n;
+  if (k.i > 0 && k.i < n - 1 && k.j > 0 && k.j < n - 1) {
+    pair_add(dt, ut, hi + fs, lo + fs, k.idx);
+    pair_add(dt, vt, hi + 2 * fs, lo + 2 * fs, k.idx);
+    return;
+  }
+  tu[k.idx] = ut;
+  tv[k.idx] = vt;
+  auto put = [&](int side, int q) {
+    E[((long long)(k.p * 4 + side) * 4 + EV_GX) * n + q] = ut;
+    E[((long long)(k.p * 4 + side) * 4 + EV_GY) * n + q] = vt;
+  };
+  if (k.i == 0) put(SIDE_L, k.j);
+  if (k.i == n - 1) put(SIDE_R, k.j);
+  if (k.j == 0) put(SIDE_B, k.i);
+  if (k.j == n - 1) put(SIDE_T, k.i);
+}
+
+__global__ void diff_sync_update_kernel(FieldGeom g, Topology tp, const double* qw, const float* E,
+                                        const float* tu, const float* tv, double dt, float* hi,
+                                        float* lo) {
+  const int n = g.n, nb = 4 * n - 4;
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= 6 * nb) return;
+  const int p = gi / nb;
+  int i, j;
+  boundary_node(gi - p * nb, n, i, j);
+  const long long x = (long long)p * g.ps + (long long)j * g.P + i;
+  const EdgeView<float> ev{E, n};
+  float a = tu[x], c = tv[x];
+  sync_vector_node<float>(ev, tp, qw, p, i, j, a, c);
+  pair_add(dt, a, hi + g.fs, lo + g.fs, x);
+  pair_add(dt, c, hi + 2 * g.fs, lo + 2 * g.fs, x);
 }
 
 // Ah scalar sync of nf <= 4 fields at once (halo_Ah_scalar_sync_mod.f90:
@@ -678,6 +740,17 @@ template <class T>
 cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, float* lo,
                              cudaStream_t st) {
   pair_axpy_kernel<T><<<dblk(count), DTPB, 0, st>>>(count, dt, t, hi, lo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diff_update_f32(const FieldGeom& g, const Topology& tp, const double* qw,
+                                   const float* b12, double cuv, const float* L, double ch,
+                                   const float* Lh, double dt, float* hi, float* lo, float* tu,
+                                   float* tv, float* edge, cudaStream_t st) {
+  diff_update_kernel<<<row_grid(g), row_block(), 0, st>>>(g, b12, float(cuv), L, float(ch), Lh, dt,
+                                                            hi, lo, tu, tv, edge);
+  const int nb = 6 * (4 * g.n - 4);
+  diff_sync_update_kernel<<<dblk(nb), DTPB, 0, st>>>(g, tp, qw, edge, tu, tv, dt, hi, lo);
   return cudaGetLastError();
 }
 

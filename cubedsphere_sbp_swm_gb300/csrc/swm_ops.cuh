@@ -186,6 +186,15 @@ template <class T>
 cudaError_t launch_diff_tendency(const FieldGeom& g, const T* b12, double cuv, const T* L, T* tu,
                                  T* tv, double ch, const T* Lh, T* th, cudaStream_t st);
 // FP32 (hi, lo) += dt * t, over count elements
+// The FP32 diffusion step's state update from the twice-applied Laplacians
+// (L: 3 Cartesian fields, Lh: h): tendencies cuv*L projected on b1, b2 and
+// ch*Lh, the covariant sync of the velocity tendency, and the (hi, lo) pair
+// update by dt, in two launches; tu, tv: work fields for the panel-boundary
+// nodes.
+cudaError_t launch_diff_update_f32(const FieldGeom& g, const Topology& tp, const double* qw,
+                                   const float* b12, double cuv, const float* L, double ch,
+                                   const float* Lh, double dt, float* hi, float* lo, float* tu,
+                                   float* tv, float* edge, cudaStream_t st);
 template <class T>
 cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, float* lo,
                              cudaStream_t st);
