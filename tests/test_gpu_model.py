@@ -1,8 +1,8 @@
 """The fused model operator, RK4 and diagnostics against the FP64 oracle.
 
-Bar (the benchmark spec): the FP64 GPU path matches the FP64 oracle within 1e-12
-relative L2 per step (J-weighted, vec_math_mod.f90:50-90); the FP32 fused
-form reports its error and must stay within the stated bounds."""
+Bar: the FP64 GPU path matches the FP64 oracle within 1e-12 relative L2 per
+step (J-weighted, vec_math_mod.f90:50-90); the FP32 fused form reports its
+error and must stay within the stated bounds."""
 import numpy as np
 import pytest
 
