@@ -111,3 +111,28 @@ def test_member_diagnostics_and_access(states):
     rc = ens._L.swm_ensemble_upload(ens._h, len(MEMBERS), *ptr)     # no such member
     assert rc == swm._abi.SWM_E_INVALID
     assert b"out of range" in ens._L.swm_ensemble_last_error(ens._h)
+
+
+def test_wide_members_match_single_instance():
+    """Members whose field pitch holds the widest TMA box of width 96
+    (N >= 99): the ensemble launches the compile-time box kernel for all of
+    them and still matches each member stepped alone."""
+    wide = [128, 160, 144]
+    sts = [initial.balanced_zonal(N, 2000 + m, 16)[:3] for m, N in enumerate(wide)]
+    ref = []
+    for N, st in zip(wide, sts):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, precision="fp32"))
+        op.set_stage_shape(96, 0, 0, "widest")
+        s = op.create_stvec()
+        s.upload(*st)
+        swm.RK4().step(s, op, _dt(N), 2)
+        ref.append(s.download())
+    ens = swm.Ensemble(swm.ModelConfig(N=wide[0], precision="fp32"), wide, [_dt(N) for N in wide])
+    for m, st in enumerate(sts):
+        ens.upload(m, *st)
+    ens.set_width(96)
+    ens.step(2)
+    ens.synchronize()
+    for m in range(len(wide)):
+        for a, b in zip(ens.download(m), ref[m]):
+            assert np.array_equal(a, b), f"member {m} (N={wide[m]}) differs"
