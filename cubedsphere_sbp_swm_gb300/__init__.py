@@ -579,7 +579,7 @@ class Ensemble:
         return {"seg_rows": a.value, "grid": b.value, "units": c.value, "width": w.value}
 
     def set_width(self, cols: int):
-        """Consumer width of the members' FP32 stage kernel (96, 128, 160, 192)."""
+        """Consumer width of the members' FP32 stage kernel (64, 96, 128, 160, 192)."""
         self._check(self._L.swm_ensemble_set_width(self._h, int(cols)))
 
     def tune(self, steps: int = 5) -> dict:

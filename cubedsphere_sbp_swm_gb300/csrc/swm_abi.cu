@@ -2009,7 +2009,8 @@ int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid
   cudaEvent_t a = nullptr, b = nullptr;
   if (rc == SWM_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess))
     rc = efail(ens, SWM_E_CUDA, "tune: events");
-  for (int wi = 0; wi < 4 && rc == SWM_OK; ++wi) {   // consumer widths (FP32 kernel only)
+  constexpr int kNumWidths = (int)(sizeof(kStageWidths) / sizeof(kStageWidths[0]));
+  for (int wi = 0; wi < kNumWidths && rc == SWM_OK; ++wi) {   // consumer widths (FP32 kernel only)
     const int cols = f32 ? kStageWidths[wi] : ens->cols;
     if (!f32 && wi > 0) break;
     if (ens_set_width(ens, cols) != SWM_OK) continue;   // width cannot cover a member

@@ -33,7 +33,7 @@ int stage_boxw_max(int cols);
 
 // Consumer widths of the FP32 TMA stage kernel; each is instantiated in its
 // own translation unit (swm_stage_f32_w<width>.cu).
-constexpr int kStageWidths[4] = {96, 128, 160, 192};
+constexpr int kStageWidths[5] = {64, 96, 128, 160, 192};
 template <int CONS>
 cudaError_t stage_f32_launch(int order, bool fixbw, const StageMaps& m, const InstDev<float>& one,
                              const InstDev<float>* many, const WorkUnit* units, int nunits,

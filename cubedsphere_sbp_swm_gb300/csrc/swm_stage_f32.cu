@@ -14,6 +14,7 @@ cudaError_t launch_stage<float>(int order, int cols, bool fixbw, const StageMaps
   static const StageMaps kNone{};
   const StageMaps& m = maps ? *maps : kNone;
   switch (cols) {
+    case 64: return stage_f32_launch<64>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
     case 96: return stage_f32_launch<96>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
     case 128: return stage_f32_launch<128>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
     case 160: return stage_f32_launch<160>(order, fixbw, m, one, many, units, nunits, mode, boxw, grid, err, st);
@@ -25,6 +26,7 @@ cudaError_t launch_stage<float>(int order, int cols, bool fixbw, const StageMaps
 template <>
 int stage_occupancy<float>(int order, int boxw, int cols, bool fixbw) {
   switch (cols) {
+    case 64: return stage_f32_occupancy<64>(order, fixbw, boxw);
     case 96: return stage_f32_occupancy<96>(order, fixbw, boxw);
     case 128: return stage_f32_occupancy<128>(order, fixbw, boxw);
     case 160: return stage_f32_occupancy<160>(order, fixbw, boxw);
@@ -36,6 +38,7 @@ int stage_occupancy<float>(int order, int boxw, int cols, bool fixbw) {
 template <>
 int stage_boxw_max<float>(int cols) {
   switch (cols) {
+    case 64: return TmaLayout<float, 42, 64>::BOXW_MAX;
     case 96: return TmaLayout<float, 42, 96>::BOXW_MAX;
     case 128: return TmaLayout<float, 42, 128>::BOXW_MAX;
     case 160: return TmaLayout<float, 42, 160>::BOXW_MAX;
@@ -46,7 +49,8 @@ int stage_boxw_max<float>(int cols) {
 
 template <>
 cudaError_t prepare_stage<float>(int order, StageShape* shape) {
-  cudaError_t e = stage_f32_prepare<96>(order);
+  cudaError_t e = stage_f32_prepare<64>(order);
+  if (e == cudaSuccess) e = stage_f32_prepare<96>(order);
   if (e == cudaSuccess) e = stage_f32_prepare<128>(order);
   if (e == cudaSuccess) e = stage_f32_prepare<160>(order);
   if (e == cudaSuccess) e = stage_f32_prepare<192>(order);

@@ -321,7 +321,7 @@ void* swm_ensemble_stream(swm_ensemble* ens);
 /* Tile shape: rows per work unit (0: whole panel height) and persistent
  * CTAs of the stage kernel (0: one CTA per work unit). */
 int  swm_ensemble_set_shape(swm_ensemble* ens, int seg_rows, int grid);
-/* Consumer width of the members' FP32 stage kernel (96, 128, 160 or 192;
+/* Consumer width of the members' FP32 stage kernel (64, 96, 128, 160 or 192;
  * bit-identical results); swm_ensemble_tune also searches it. */
 int  swm_ensemble_set_width(swm_ensemble* ens, int cols);
 int  swm_ensemble_get_width(const swm_ensemble* ens, int* cols);
@@ -393,7 +393,7 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 /* Launch-shape tuning (no reference counterpart)                         */
 /* ---------------------------------------------------------------------- */
 /* The stage kernel's launch shape: the consumer width of the FP32 kernel
- * (96, 128, 160 or 192 columns per CTA), the rows per work unit (0: enough
+ * (64, 96, 128, 160 or 192 columns per CTA), the rows per work unit (0: enough
  * units for one wave of CTAs), the persistent grid (0: one CTA per unit) and
  * the box mode of the FP32 kernel's TMA loads: SWM_BOX_STRIP (the narrowest
  * box that covers every column strip, its width a kernel argument),

@@ -68,7 +68,7 @@ def test_members_match_single_instance(prec, seg_rows, persistent, states, singl
             assert np.array_equal(a, b), f"member {m} (N={MEMBERS[m]}) differs"
 
 
-@pytest.mark.parametrize("width", [96, 160, 192])
+@pytest.mark.parametrize("width", [64, 96, 160, 192])
 def test_member_widths_match_single_instance(width, states, single):
     ens = _ensemble("fp32", states)
     ens.set_width(width)
@@ -87,7 +87,7 @@ def test_autotuner_keeps_states_and_picks_a_valid_shape(prec, states, single):
     res = ens.tune(steps=2)
     assert res["ms_per_step"] > 0
     assert res["seg_rows"] >= 0 and res["grid"] >= 0
-    assert res["width"] in ((96, 128, 160, 192) if prec == "fp32" else (128,))
+    assert res["width"] in ((64, 96, 128, 160, 192) if prec == "fp32" else (128,))
     sh = ens.get_shape()
     assert sh["seg_rows"] == res["seg_rows"] and sh["width"] == res["width"]
     for m in range(len(MEMBERS)):

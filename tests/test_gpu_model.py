@@ -181,10 +181,10 @@ def test_stage_shapes_are_bit_identical(order, N):
     x0 = op.create_stvec()
     x0.upload(h, u, v)
     ref = None
-    shapes = [(96, 0, 0, "strip"), (128, 0, 0, "strip"), (160, 0, 0, "strip"), (192, 0, 0, "strip"),
+    shapes = [(64, 0, 0, "strip"), (96, 0, 0, "strip"), (128, 0, 0, "strip"), (160, 0, 0, "strip"), (192, 0, 0, "strip"),
               (128, 8, 0, "strip"), (128, 8, 7, "strip"), (192, 16, 3, "strip"), (96, 0, 0, "auto")]
     pitch = (N + 1 + 15) // 16 * 16
-    wide = [w for w in (96, 128, 160, 192) if w + 4 <= pitch]
+    wide = [w for w in (64, 96, 128, 160, 192) if w + 4 <= pitch]
     shapes += [(w, 0, 0, "widest") for w in wide] + [(w, 8, 7, "widest") for w in wide[:1]]
     for w, seg, grid, box in shapes:
         op.set_stage_shape(w, seg, grid, box)
@@ -201,13 +201,13 @@ def test_stage_shapes_are_bit_identical(order, N):
             assert np.array_equal(a, b)
     before = x0.download()
     t = op.tune_stage(x0, 300.0, steps=2)
-    assert t["width"] in (96, 128, 160, 192) and t["ms"] > 0
+    assert t["width"] in (64, 96, 128, 160, 192) and t["ms"] > 0
     assert op.stage_shape["width"] == t["width"]
     for a, b in zip(x0.download(), before):
         assert np.array_equal(a, b)
     with pytest.raises(swm.SwmError):
         op.set_stage_shape(100)
-    for w in (96, 128, 160, 192):
+    for w in (64, 96, 128, 160, 192):
         if w not in wide:
             with pytest.raises(swm.SwmError):
                 op.set_stage_shape(w, 0, 0, "widest")
