@@ -287,17 +287,65 @@ bool make_units(const SbpC& s, int n, int threads, int target_ctas, std::vector<
     if (ok) break;
     if (nstrip > n) { why = "work split failed"; return false; }
   }
-  const int min_rows = 8;
-  int nseg = std::max(1, target_ctas / (6 * nstrip));
-  nseg = std::min(nseg, std::max(1, n / min_rows));
-  if (nseg_fixed > 0) nseg = std::min(nseg_fixed, n);
+  // Row cuts of every strip.  nseg_fixed > 0: that many equal segments.
+  // Otherwise the rows are cut so that every unit of the wave carries about
+  // the same modelled cost, in row-equivalents.  The model is measured per
+  // unit on GB300: a strip on a panel edge costs 1 + kStripEdge per row (its
+  // closure columns make one warp diverge, and the per-row barrier makes the
+  // CTA wait for it); a closure row at a panel end costs 1 + kRowClosure;
+  // every unit adds 0.8 * rmax rows for its halo.
+  std::vector<std::vector<int>> cuts(nstrip);
+  if (nseg_fixed > 0) {
+    const int nseg = std::min(nseg_fixed, n);
+    for (auto& c : cuts)
+      for (int r = 0; r <= nseg; ++r) c.push_back((int)((long long)n * r / nseg));
+  } else {
+    const double kStripEdge = 0.3, kRowClosure = s.ne >= 6 ? 2.0 : 1.0, over = 0.8 * s.rmax;
+    std::vector<double> pre(n + 1, 0.0);
+    for (int j = 0; j < n; ++j)
+      pre[j + 1] = pre[j] + ((j < s.ne || j >= n - s.ne) ? 1.0 + kRowClosure : 1.0);
+    const int max_units = std::max(1, n / std::min(8, n));   // at least 8 rows a unit
+    // units of strip k for a unit cost of at most tau: m units of a strip of
+    // factor f cost f * (pre[n] + m * over) in total
+    auto units_of = [&](int k, double tau) {
+      const double f = (cs[k] == 0 || cs[k + 1] == n) ? 1.0 + kStripEdge : 1.0;
+      const double per = tau - f * over;
+      if (per <= 0.0) return max_units;
+      return std::max(1, std::min(max_units, (int)std::ceil(f * pre[n] / per - 1e-9)));
+    };
+    auto total = [&](double tau) {
+      int t = 0;
+      for (int k = 0; k < nstrip; ++k) t += units_of(k, tau);
+      return 6 * t;
+    };
+    // the smallest unit cost whose units fit the wave
+    double lo = 0.0, hi = (1.0 + kStripEdge) * (pre[n] + over);
+    const int budget = std::max(target_ctas, 6 * nstrip);
+    for (int it = 0; it < 60; ++it) {
+      const double mid = 0.5 * (lo + hi);
+      if (total(mid) <= budget) hi = mid; else lo = mid;
+    }
+    // cut each strip at equal shares of its row cost
+    for (int k = 0; k < nstrip; ++k) {
+      const int m = units_of(k, hi);
+      auto& c = cuts[k];
+      c.assign(1, 0);
+      int j = 0;
+      for (int r = 1; r < m; ++r) {
+        const double want = pre[n] * r / m;
+        while (j < n && pre[j + 1] <= want) ++j;
+        if (j > c.back()) c.push_back(j);
+      }
+      c.push_back(n);
+    }
+  }
   for (int p = 0; p < 6; ++p)
     for (int k = 0; k < nstrip; ++k)
-      for (int r = 0; r < nseg; ++r) {
+      for (size_t r = 0; r + 1 < cuts[k].size(); ++r) {
         WorkUnit w;
         w.inst = 0; w.panel = (int16_t)p;
         w.i0 = (int16_t)cs[k]; w.i1 = (int16_t)cs[k + 1];
-        w.j0 = (int16_t)((long long)n * r / nseg); w.j1 = (int16_t)((long long)n * (r + 1) / nseg);
+        w.j0 = (int16_t)cuts[k][r]; w.j1 = (int16_t)cuts[k][r + 1];
         if (w.j1 <= w.j0) continue;
         int lo = n, hi = 0;
         for (int c = w.i0; c < w.i1; ++c) { lo = std::min(lo, need_lo(c)); hi = std::max(hi, need_hi(c)); }
