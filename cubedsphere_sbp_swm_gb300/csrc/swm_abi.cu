@@ -287,28 +287,45 @@ bool make_units(const SbpC& s, int n, int threads, int target_ctas, std::vector<
     if (ok) break;
     if (nstrip > n) { why = "work split failed"; return false; }
   }
-  // Row cuts of every strip.  nseg_fixed > 0: that many equal segments.
-  // Otherwise the rows are cut so that every unit of the wave carries about
-  // the same modelled cost, in row-equivalents.  The model is measured per
-  // unit on GB300: a strip on a panel edge costs 1 + kStripEdge per row (its
-  // closure columns make one warp diverge, and the per-row barrier makes the
-  // CTA wait for it); a closure row at a panel end costs 1 + kRowClosure;
-  // every unit adds 0.8 * rmax rows for its halo.
+  // Row cuts of every strip, so that units carry about the same modelled
+  // cost in row-equivalents.  The model is measured per unit on GB300: a
+  // strip on a panel edge costs 1 + kStripEdge per row (its closure columns
+  // make one warp diverge, and the per-row barrier makes the CTA wait for
+  // it); a closure row at a panel end costs 1 + kRowClosure; every unit adds
+  // 0.8 * rmax rows for its halo.  nseg_fixed > 0: inner strips get that many
+  // units and edge strips (1 + kStripEdge) times as many when the panel also
+  // has inner strips; otherwise the unit
+  // counts fill one wave of target_ctas.  Each strip is cut at equal shares
+  // of its row cost.
   std::vector<std::vector<int>> cuts(nstrip);
+  const double kStripEdge = 0.3, kRowClosure = s.ne >= 6 ? 2.0 : 1.0, over = 0.8 * s.rmax;
+  std::vector<double> pre(n + 1, 0.0);
+  for (int j = 0; j < n; ++j)
+    pre[j + 1] = pre[j] + ((j < s.ne || j >= n - s.ne) ? 1.0 + kRowClosure : 1.0);
+  auto edge_strip = [&](int k) { return cs[k] == 0 || cs[k + 1] == n; };
+  auto cut_equal = [&](int k, int m) {
+    auto& c = cuts[k];
+    c.assign(1, 0);
+    int j = 0;
+    for (int r = 1; r < m; ++r) {
+      const double want = pre[n] * r / m;
+      while (j < n && pre[j + 1] <= want) ++j;
+      if (j > c.back()) c.push_back(j);
+    }
+    c.push_back(n);
+  };
   if (nseg_fixed > 0) {
-    const int nseg = std::min(nseg_fixed, n);
-    for (auto& c : cuts)
-      for (int r = 0; r <= nseg; ++r) c.push_back((int)((long long)n * r / nseg));
+    // (with no inner strip every strip is an edge strip and none waits)
+    for (int k = 0; k < nstrip; ++k) {
+      const double m = nseg_fixed * (nstrip > 2 && edge_strip(k) ? 1.0 + kStripEdge : 1.0);
+      cut_equal(k, std::max(1, std::min(n, (int)std::lround(m))));
+    }
   } else {
-    const double kStripEdge = 0.3, kRowClosure = s.ne >= 6 ? 2.0 : 1.0, over = 0.8 * s.rmax;
-    std::vector<double> pre(n + 1, 0.0);
-    for (int j = 0; j < n; ++j)
-      pre[j + 1] = pre[j] + ((j < s.ne || j >= n - s.ne) ? 1.0 + kRowClosure : 1.0);
     const int max_units = std::max(1, n / std::min(8, n));   // at least 8 rows a unit
     // units of strip k for a unit cost of at most tau: m units of a strip of
     // factor f cost f * (pre[n] + m * over) in total
     auto units_of = [&](int k, double tau) {
-      const double f = (cs[k] == 0 || cs[k + 1] == n) ? 1.0 + kStripEdge : 1.0;
+      const double f = edge_strip(k) ? 1.0 + kStripEdge : 1.0;
       const double per = tau - f * over;
       if (per <= 0.0) return max_units;
       return std::max(1, std::min(max_units, (int)std::ceil(f * pre[n] / per - 1e-9)));
@@ -325,19 +342,7 @@ bool make_units(const SbpC& s, int n, int threads, int target_ctas, std::vector<
       const double mid = 0.5 * (lo + hi);
       if (total(mid) <= budget) hi = mid; else lo = mid;
     }
-    // cut each strip at equal shares of its row cost
-    for (int k = 0; k < nstrip; ++k) {
-      const int m = units_of(k, hi);
-      auto& c = cuts[k];
-      c.assign(1, 0);
-      int j = 0;
-      for (int r = 1; r < m; ++r) {
-        const double want = pre[n] * r / m;
-        while (j < n && pre[j + 1] <= want) ++j;
-        if (j > c.back()) c.push_back(j);
-      }
-      c.push_back(n);
-    }
+    for (int k = 0; k < nstrip; ++k) cut_equal(k, units_of(k, hi));
   }
   for (int p = 0; p < 6; ++p)
     for (int k = 0; k < nstrip; ++k)
