@@ -46,7 +46,7 @@ EXPORTS = (
     "swm_diffusion_set", "swm_apply_diffusion", "swm_diffusion_step", "swm_model_step",
     "swm_laplace", "swm_latlon_create", "swm_latlon_destroy", "swm_latlon_regrid_field",
     "swm_latlon_regrid_vector", "swm_latlon_regrid_state", "swm_latlon_write", "swm_paneled_write",
-    "swm_tune_stage", "swm_get_stage_shape", "swm_set_stage_shape", "swm_ensemble_set_width",
+    "swm_tune_stage", "swm_get_stage_shape", "swm_set_stage_shape", "swm_work_split", "swm_ensemble_set_width",
     "swm_ensemble_get_width", "swm_state_save", "swm_state_load",
 )
 
@@ -138,6 +138,7 @@ def load(build_if_missing: bool = True):
     sig("swm_get_stage_shape", I, VP, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
         ctypes.POINTER(I), ctypes.POINTER(I))
     sig("swm_set_stage_shape", I, VP, I, I, I, I)
+    sig("swm_work_split", I, I, I, I, I, I, ctypes.POINTER(I), I, ctypes.POINTER(I))
     sig("swm_ensemble_set_width", I, VP, I)
     sig("swm_ensemble_get_width", I, VP, ctypes.POINTER(I))
     sig("swm_state_save", I, VP, VP, C, D)

@@ -2822,6 +2822,29 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
   return SWM_OK;
 }
 
+int swm_work_split(int N, int sbp_order, int cols, int target_units, int seg_rows, int* units_out,
+                   int max_units, int* nunits) {
+  if (!units_out || !nunits) return fail(nullptr, SWM_E_INVALID, "null argument");
+  if (N < 16 || N > 8190 || cols < 32 || target_units < 1 || seg_rows < 0)
+    return fail(nullptr, SWM_E_INVALID, "bad work split arguments");
+  if (sbp_order != 21 && sbp_order != 42 && sbp_order != 43 && sbp_order != 63)
+    return fail(nullptr, SWM_E_UNSUPPORTED, "unknown SBP order");
+  const int n = N + 1;
+  std::vector<WorkUnit> units;
+  std::string why;
+  const int nseg = seg_rows > 0 ? (n + seg_rows - 1) / seg_rows : 0;
+  if (!make_units(kTables[sbp_index(sbp_order)], n, cols, target_units, units, why, nseg))
+    return fail(nullptr, SWM_E_INVALID, why);
+  *nunits = (int)units.size();
+  if ((int)units.size() > max_units) return fail(nullptr, SWM_E_INVALID, "max_units too small");
+  for (size_t k = 0; k < units.size(); ++k) {
+    const WorkUnit& w = units[k];
+    const int v[9] = {w.panel, w.i0, w.i1, w.j0, w.j1, w.cl0, w.cl1, w.rl0, w.rl1};
+    for (int e = 0; e < 9; ++e) units_out[9 * k + e] = v[e];
+  }
+  return SWM_OK;
+}
+
 int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* box, int* nunits) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   if (cols) *cols = ctx->shape.cols;

@@ -412,6 +412,15 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
                    int* seg_rows_out, int* grid_out, int* box_out, double* ms_out);
 int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* box, int* nunits);
 int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid, int box);
+/* The stage kernel's work split for a grid of N cells per panel edge and an
+ * SBP order, with no device work (inspection and tests): consumer width
+ * cols, the units of one wave target_units (seg_rows = 0) or seg_rows rows
+ * per inner-strip unit.  Writes up to max_units units of 9 ints each (panel,
+ * owned columns i0 i1, owned rows j0 j1, read columns cl0 cl1, read rows
+ * rl0 rl1) to units_out and their count to *nunits; SWM_E_INVALID if the
+ * split fails or max_units is too small. */
+int swm_work_split(int N, int sbp_order, int cols, int target_units, int seg_rows, int* units_out,
+                   int max_units, int* nunits);
 
 /* ---------------------------------------------------------------------- */
 /* Checkpoint / resume (no reference counterpart: the reference writes no   */
