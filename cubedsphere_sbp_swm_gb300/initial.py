@@ -21,6 +21,7 @@ Velocities are returned as covariant components on the unit-sphere basis
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
@@ -59,26 +60,6 @@ def ecs_geometry(N: int) -> dict:
                 hx=hx, n=n, N=N)
 
 
-def _legendre_all(lmax: int, x: np.ndarray) -> dict:
-    """Fully normalised associated Legendre functions P_lm(x), 0<=m<=l<=lmax,
-    by the recursion of random_friction_mod.f90:136-178."""
-    P = {}
-    for m in range(lmax + 1):
-        if m == 0:
-            P[(0, 0)] = np.full_like(x, math.sqrt(0.5))
-        else:
-            c = -math.sqrt((2.0 * m + 1.0) / (2.0 * max(m, 1)))
-            P[(m, m)] = c * np.sqrt(1.0 - x * x) * P[(m - 1, m - 1)]
-        if m < lmax:
-            P[(m + 1, m)] = math.sqrt(2.0 * m + 3.0) * x * P[(m, m)]
-        for k in range(m + 2, lmax + 1):
-            c1 = math.sqrt((2.0 * k + 1.0) * (2.0 * k - 1.0) / (1.0 * (k + m) * (k - m)))
-            c2 = -math.sqrt((2.0 * k + 1.0) * (k - m - 1.0) * (k + m - 1.0)
-                            / ((2.0 * k - 3.0) * (k + m) * (k - m)))
-            P[(k, m)] = c1 * x * P[(k - 1, m)] + c2 * P[(k - 2, m)]
-    return P
-
-
 def _covariant(geo, V):
     return (np.einsum("pjic,pjic->pji", V, geo["a1"]).copy(),
             np.einsum("pjic,pjic->pji", V, geo["a2"]).copy())
@@ -88,32 +69,80 @@ def _area_rms(f, J):
     return math.sqrt(float(np.sum(J * f * f) / np.sum(J)))
 
 
-_LEGENDRE_CACHE: dict = {}
+def _harmonic_block(x, lam, A, B, lmax):
+    """sum_m [cos(m lam) S_m + sin(m lam) T_m] over one block of nodes, with
+    S_m = sum_l A[l, m] P_lm(x), T_m = sum_l B[l, m] P_lm(x) and the fully
+    normalised associated Legendre functions P_lm by the recursion of
+    random_friction_mod.f90:136-178 (one order m at a time).  Every node's
+    arithmetic is independent of the blocking; the loops work in place."""
+    s1 = np.sqrt(1.0 - x * x)
+    pmm = np.full_like(x, math.sqrt(0.5))
+    f = np.zeros_like(x)
+    S, T, p1, p2, t, w = (np.empty_like(x) for _ in range(6))
+    for m in range(lmax + 1):
+        if m > 0:
+            np.multiply(pmm, -math.sqrt((2.0 * m + 1.0) / (2.0 * m)), out=t)
+            np.multiply(t, s1, out=pmm)
+        S.fill(0.0)
+        T.fill(0.0)
+        p1[...] = pmm
+        for k in range(m, lmax + 1):
+            if k == m + 1:
+                p2[...] = p1
+                np.multiply(p1, math.sqrt(2.0 * m + 3.0), out=t)
+                np.multiply(t, x, out=p1)
+            elif k > m + 1:
+                c1 = math.sqrt((2.0 * k + 1.0) * (2.0 * k - 1.0) / (1.0 * (k + m) * (k - m)))
+                c2 = -math.sqrt((2.0 * k + 1.0) * (k - m - 1.0) * (k + m - 1.0)
+                                / ((2.0 * k - 3.0) * (k + m) * (k - m)))
+                # p_k = (c1 x) p_{k-1} + c2 p_{k-2}; p2 takes p_{k-1}
+                np.multiply(x, c1, out=t)
+                np.multiply(t, p1, out=t)
+                np.multiply(p2, c2, out=p2)
+                np.add(t, p2, out=t)
+                p2, p1, t = p1, t, p2
+            if k >= 1:
+                np.multiply(p1, A[k, m], out=w)
+                np.add(S, w, out=S)
+                if m > 0:
+                    np.multiply(p1, B[k, m], out=w)
+                    np.add(T, w, out=T)
+        if m == 0:
+            f += S
+        else:
+            f += np.cos(m * lam) * S + np.sin(m * lam) * T
+    return f
 
 
 def harmonic_perturbation(geo, seed: int, lmax: int, rms: float = 10.0) -> np.ndarray:
     """Random real spherical-harmonic field, degrees 1..lmax, spectrum l^-3,
-    scaled to the given area-weighted RMS."""
+    scaled to the given area-weighted RMS.  The coefficients are drawn in
+    degree-major order (l = 1..lmax, m = 0..l, two normals each); the sum is
+    evaluated over blocks of nodes on the host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
     rng = np.random.Generator(np.random.PCG64(seed))
-    r = geo["r"]
-    x = r[..., 2]                                  # sin(latitude) about the z axis
-    lam = np.arctan2(r[..., 1], r[..., 0])
-    key = (geo["N"], lmax)
-    if _LEGENDRE_CACHE.get("key") != key:      # members of one resolution share it
-        _LEGENDRE_CACHE.clear()
-        _LEGENDRE_CACHE.update(key=key, P=_legendre_all(lmax, x))
-    P = _LEGENDRE_CACHE["P"]
-    cm = [np.cos(m * lam) for m in range(lmax + 1)]
-    sm = [np.sin(m * lam) for m in range(lmax + 1)]
-    f = np.zeros_like(x)
+    norm = 1.0 / math.sqrt(2.0 * math.pi)
+    A = np.zeros((lmax + 1, lmax + 1))
+    B = np.zeros((lmax + 1, lmax + 1))
     for l in range(1, lmax + 1):
         amp = float(l) ** -3
         for m in range(0, l + 1):
             a, b = rng.standard_normal(2)
-            if m == 0:
-                f += amp * a * P[(l, 0)] / math.sqrt(2.0 * math.pi)
-            else:
-                f += amp * P[(l, m)] * (a * cm[m] + b * sm[m]) / math.sqrt(2.0 * math.pi)
+            A[l, m] = amp * a * norm
+            B[l, m] = amp * b * norm
+    r = geo["r"]
+    x = np.ascontiguousarray(r[..., 2]).ravel()    # sin(latitude) about the z axis
+    lam = np.arctan2(r[..., 1], r[..., 0]).ravel()
+    f = np.empty_like(x)
+    blk = 131072
+
+    def run(b0):
+        f[b0:b0 + blk] = _harmonic_block(x[b0:b0 + blk], lam[b0:b0 + blk], A, B, lmax)
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(run, range(0, x.size, blk)))
+    f = f.reshape(r.shape[:-1])
     return f * (rms / _area_rms(f, geo["J"]))
 
 

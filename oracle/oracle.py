@@ -191,6 +191,13 @@ class OracleDomain:
         lib().orc_rk4(self._h, _p(hs), _p(h), _p(u), _p(v), float(dt), int(nsteps))
         return h, u, v
 
+    def rk4_inplace(self, h, u, v, dt, nsteps=1, hs=None):
+        """rk4 on the caller's C-contiguous FP64 arrays, updated in place (no
+        copies: the timed CPU baseline uses this)."""
+        for a in (h, u, v):
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] and a.shape == self.shape
+        lib().orc_rk4(self._h, _p(hs), _p(h), _p(u), _p(v), float(dt), int(nsteps))
+
     def diagnostics(self, h, u, v, hs=None):
         out = np.zeros(7)
         lib().orc_diagnostics(self._h, _p(hs), _p(h), _p(u), _p(v), _p(out))

@@ -255,7 +255,21 @@ struct orc_domain {
   std::vector<double> qb, qt, ql, qr;   // covariant sync weights
   std::vector<RingSrc> ring;            // [p][side][k]
   int npts() const { return 6 * n * n; }
+  // Work arrays of the operators and of RK4, allocated on first use and kept
+  // (the reference's operator owns its work fields the same way), so a timed
+  // step does not pay for fresh pages.
+  // The slot table has a fixed size, so references to slots stay valid.
+  static constexpr int kWorkSlots = 24;
+  mutable std::vector<double> ws[kWorkSlots];
+  std::vector<double>& work(int slot, size_t len) const {
+    if (ws[slot].size() != len) ws[slot].assign(len, 0.0);
+    return ws[slot];
+  }
 };
+enum { W_UT = 0, W_VT, W_HU, W_HV, W_KE, W_GX, W_GY, W_CU, W_CORU, W_CORV, W_DV,
+       W_CURL_U, W_CURL_V, W_GU, W_GV, W_K1, W_K2, W_K3, W_K4, W_Y, W_RING, W_RING_U, W_RING_V,
+       W_COUNT };
+static_assert(W_COUNT <= orc_domain::kWorkSlots, "oracle work slots");
 
 namespace {
 
@@ -382,7 +396,7 @@ void exchange_vector(const orc_domain& d, const double* u, const double* v,
 // Scalar edge/corner averaging (halo/halo_Ah_scalar_sync_mod.f90:38-93).
 void sync_scalar(const orc_domain& d, double* f) {
   const int n = d.n;
-  std::vector<double> ring;
+  std::vector<double>& ring = d.work(W_RING, 6 * 4 * n);
   exchange_scalar(d, f, ring);
   for (int p = 0; p < 6; ++p) {
     double* F = f + p * n * n;
@@ -407,7 +421,8 @@ void sync_scalar(const orc_domain& d, double* f) {
 // components swapped (ecs_Ah_vec_sync_mod.f90:34-125): U = gy, V = gx.
 void sync_vector_cov(const orc_domain& d, double* gx, double* gy) {
   const int n = d.n;
-  std::vector<double> rgx, rgy;
+  std::vector<double>& rgx = d.work(W_RING_U, 6 * 4 * n);
+  std::vector<double>& rgy = d.work(W_RING_V, 6 * 4 * n);
   exchange_vector(d, gx, gy, rgx, rgy);
   const double* qb = d.qb.data(); const double* qt = d.qt.data();
   const double* ql = d.ql.data(); const double* qr = d.qr.data();
@@ -470,7 +485,8 @@ void grad(const orc_domain& d, const double* f, double* gx, double* gy) {
 // the scalar sync.  u, v are contravariant components.
 void div(const orc_domain& d, const double* u, const double* v, double* out) {
   const int n = d.n, np = d.npts();
-  std::vector<double> Gu(np), Gv(np);
+  std::vector<double>& Gu = d.work(W_GU, np);
+  std::vector<double>& Gv = d.work(W_GV, np);
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (int k = 0; k < np; ++k) { Gu[k] = d.J[k] * u[k]; Gv[k] = d.J[k] * v[k]; }
   const double hx = d.hx, sc = d.scale;
@@ -492,7 +508,8 @@ void div(const orc_domain& d, const double* u, const double* v, double* out) {
 // curl_div_based (curl/curl_div_based_mod.f90:26-66): div(v/J, -u/J).
 void curl(const orc_domain& d, const double* u, const double* v, double* out) {
   const int np = d.npts();
-  std::vector<double> ut(np), vt(np);
+  std::vector<double>& ut = d.work(W_CURL_U, np);
+  std::vector<double>& vt = d.work(W_CURL_V, np);
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (int k = 0; k < np; ++k) { ut[k] = v[k] / d.J[k]; vt[k] = -u[k] / d.J[k]; }
   div(d, ut.data(), vt.data(), out);
@@ -533,8 +550,17 @@ void coriolis(const orc_domain& d, const double* hu, const double* hv, const dou
 void apply(const orc_domain& d, const double* hs, const double* h, const double* u,
            const double* v, double* th, double* tu, double* tv) {
   const int np = d.npts();
-  std::vector<double> ut(np), vt(np), hu(np), hv(np), KE(np), gx(np), gy(np), cu(np),
-      cor_u(np), cor_v(np), dv(np);
+  std::vector<double>& ut = d.work(W_UT, np);
+  std::vector<double>& vt = d.work(W_VT, np);
+  std::vector<double>& hu = d.work(W_HU, np);
+  std::vector<double>& hv = d.work(W_HV, np);
+  std::vector<double>& KE = d.work(W_KE, np);
+  std::vector<double>& gx = d.work(W_GX, np);
+  std::vector<double>& gy = d.work(W_GY, np);
+  std::vector<double>& cu = d.work(W_CU, np);
+  std::vector<double>& cor_u = d.work(W_CORU, np);
+  std::vector<double>& cor_v = d.work(W_CORV, np);
+  std::vector<double>& dv = d.work(W_DV, np);
   co2contra(d, u, v, ut.data(), vt.data());
   const double g = d.grav;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -561,7 +587,11 @@ void apply(const orc_domain& d, const double* hs, const double* h, const double*
 void rk4(const orc_domain& d, const double* hs, double* h, double* u, double* v, double dt,
          int nsteps) {
   const int np = d.npts();
-  std::vector<double> k1(3 * np), k2(3 * np), k3(3 * np), k4(3 * np), y(3 * np);
+  std::vector<double>& k1 = d.work(W_K1, 3 * (size_t)np);
+  std::vector<double>& k2 = d.work(W_K2, 3 * (size_t)np);
+  std::vector<double>& k3 = d.work(W_K3, 3 * (size_t)np);
+  std::vector<double>& k4 = d.work(W_K4, 3 * (size_t)np);
+  std::vector<double>& y = d.work(W_Y, 3 * (size_t)np);
   double* F0[3] = {h, u, v};
   auto A = [&](std::vector<double>& out, const double* yh, const double* yu, const double* yv) {
     apply(d, hs, yh, yu, yv, &out[0], &out[np], &out[2 * np]);

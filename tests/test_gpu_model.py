@@ -96,9 +96,12 @@ def test_rk4_fp32_fused_error_vs_fp64_oracle(cfg1):
     swm.RK4().step(s, op, 900.0, 96)
     o = od.rk4(h, u, v, 900.0, 96)
     gh, gu, gv = s.download()
-    eh = rel_l2(gh, o[0], J)
-    assert eh < 1e-5, eh
-    assert rel_l2(gu, o[1], J) < 1e-3 and rel_l2(gv, o[2], J) < 1e-3
+    # dt = 900 s is Courant 1.04, past the RK4 stability limit of the
+    # undiffused scheme (the state turns non-finite after ~110 h): growing
+    # modes amplify the FP32 rounding in u and v over the day.  At a stable dt
+    # every field is within 1e-5 (test_gpu_parity_configs.py).
+    errs = [rel_l2(a, b, J) for a, b in zip((gh, gu, gv), o)]
+    assert errs[0] < 1e-5 and max(errs[1:]) < 1e-4, errs
     mass_drift = abs(od.mass(gh) - od.mass(o[0])) / od.mass(o[0])
     assert mass_drift < 1e-6
 
@@ -265,3 +268,27 @@ def test_checkpoint_errors(tmp_path):
     with pytest.raises(swm.SwmError) as e:
         s.load(tmp_path / "missing.bin")
     assert e.value.code == _abi.SWM_E_IO
+
+
+def test_failed_checkpoint_write_keeps_the_previous_file(tmp_path):
+    """A restart file is written beside its path and renamed over it only when
+    complete: a write that fails (here its temporary file cannot be created)
+    reports SWM_E_IO and leaves the previous file loadable."""
+    N = 48
+    h, u, v, _ = initial.balanced_zonal(N, 2, 16)
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    s = op.create_stvec()
+    s.upload(h, u, v)
+    path = tmp_path / "restart.bin"
+    s.save(path, time=60.0)
+    good = s.download()
+    (tmp_path / "restart.bin.tmp").mkdir()      # the temporary file cannot be opened
+    t = s.create_similar()
+    t.assign_s1(1.0)
+    with pytest.raises(swm.SwmError) as e:
+        t.save(path, time=120.0)
+    assert e.value.code == _abi.SWM_E_IO
+    r = s.create_similar()
+    assert r.load(path) == 60.0
+    for a, b in zip(r.download(), good):
+        assert np.array_equal(a, b)
