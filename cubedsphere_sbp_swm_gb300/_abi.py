@@ -84,8 +84,8 @@ def load(build_if_missing: bool = True):
     global _lib
     if _lib is not None:
         return _lib
-    path = os.environ.get("SWM_GB300_LIB") or _build.LIB   # alternative build (tuning)
-    if path == _build.LIB and build_if_missing and not _build.up_to_date():
+    path = _build.LIB
+    if build_if_missing and not _build.up_to_date():
         _build.build()
     if not os.path.exists(path):
         raise OSError(f"libswm_gb300.so not found at {path}: build the CUDA library first")

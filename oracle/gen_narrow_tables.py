@@ -18,7 +18,8 @@ the interior stencil annihilate constants and differentiate x^2 exactly for
 b = 1 (the boundary flux term folded into the first 6/3 row excepted).
 
 usage: python oracle/gen_narrow_tables.py [REFERENCE_ROOT]
-       (default /root/reference; writes the header beside the CUDA sources)
+       (the reference checkout is a required argument; writes the header
+       beside the CUDA sources)
 """
 import os
 import re
@@ -225,7 +226,9 @@ def emit(tables):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python oracle/gen_narrow_tables.py REFERENCE_CHECKOUT")
+    ref = sys.argv[1]
     tables = build(ref)
     for t in tables:
         check(t)

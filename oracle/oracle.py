@@ -67,7 +67,8 @@ def lib():
         for name in ("orc_golden_div", "orc_golden_grad", "orc_golden_curl"):
             getattr(L, name).argtypes = [ctypes.c_int, ctypes.c_int, _D]
             getattr(L, name).restype = ctypes.c_int
-        for name in ("orc_golden_co2contra", "orc_golden_contra2co"):
+        for name in ("orc_golden_co2contra", "orc_golden_contra2co", "orc_golden_coriolis",
+                     "orc_golden_ke"):
             getattr(L, name).argtypes = [ctypes.c_int, _D]
             getattr(L, name).restype = ctypes.c_int
         L.orc_golden_quadrature.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -280,9 +281,12 @@ def golden(kind: str, N: int = 32, sbp_order: int = 42):
     elif kind == "grad":
         out = np.zeros(2)
         rc = L.orc_golden_grad(int(N), int(sbp_order), _p(out))
-    elif kind in ("co2contra", "contra2co"):
+    elif kind in ("co2contra", "contra2co", "coriolis"):
         out = np.zeros(2)
         rc = getattr(L, f"orc_golden_{kind}")(int(N), _p(out))
+    elif kind == "ke":
+        out = np.zeros(4)
+        rc = L.orc_golden_ke(int(N), _p(out))
     else:
         raise ValueError(kind)
     if rc != 0:

@@ -1312,6 +1312,100 @@ static int golden_transform(int N, bool to_contra, double out[2]) {
 int orc_golden_co2contra(int N, double out[2]) { return golden_transform(N, true, out); }
 int orc_golden_contra2co(int N, double out[2]) { return golden_transform(N, false, out); }
 
+// The colocated A grid of the reference's pointwise operator tests
+// (create_domain(domain, "cube", "A", N, nz)): N x N cell-centre points per
+// panel, alpha_i = -pi/4 + (i + 1/2) hx, unit sphere, Omega = 1 about z.  The
+// node's position, covariant / contravariant basis and Jacobian follow
+// ecs_metric_mod.f90:326-478 as on the Ah grid.
+struct AGridNode {
+  double r[3], a1[3], a2[3], b1[3], b2[3], J;
+};
+static AGridNode agrid_node(int N, int p, int i, int j) {
+  const double hx = 0.5 * PI / (double)N;
+  const double al = -0.25 * PI + (i + 0.5) * hx, be = -0.25 * PI + (j + 0.5) * hx;
+  AGridNode g;
+  double v[3];
+  r_proto(al, be, v); to_face(p, v, g.r);
+  a1_proto(al, be, v); to_face(p, v, g.a1);
+  a2_proto(al, be, v); to_face(p, v, g.a2);
+  b1_proto(al, be, v); to_face(p, v, g.b1);
+  b2_proto(al, be, v); to_face(p, v, g.b2);
+  const double ta = std::tan(al), tb = std::tan(be);
+  const double sg = std::sqrt(1.0 + ta * ta + tb * tb);
+  g.J = (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
+  return g;
+}
+static double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// test_coriolis with coriolis_colocated on the A grid (test_diffops_mod.f90:
+// 651-722): cor = calc_coriolis of the contravariant VSH_curl_free_10 field
+// (coriolis_colocated_mod.f90:36-61: cor_u = f vt J, cor_v = -f ut J) against
+// the covariant components of the exact force 2 sin(phi) (v_phi, -v_lam)
+// (test_fields_mod.f90:592-616); nz = 3 identical levels.  out = {sum of
+// the maxabs, sum of the l2 norms} of (cor_u, cor_v) errors.
+int orc_golden_coriolis(int N, double out[2]) {
+  const double hx = 0.5 * PI / (double)N;
+  double mu = 0.0, mv = 0.0, l2u = 0.0, l2v = 0.0;
+  for (int lev = 0; lev < 3; ++lev)
+    for (int p = 0; p < 6; ++p)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          const AGridNode g = agrid_node(N, p, i, j);
+          double V[3];
+          field_vsh_curl_free_10(g.r[0], g.r[1], g.r[2], V);
+          const double ut = dot3(V, g.b1), vt = dot3(V, g.b2);
+          const double f = 2.0 * 1.0 * g.r[2] / std::sqrt(dot3(g.r, g.r));
+          const double cu = f * vt * g.J, cv = -f * ut * g.J;
+          // exact force: lam/phi components of V, rotated and scaled
+          const double lam = std::atan2(g.r[1], g.r[0]);
+          const double phi = std::asin(g.r[2] / std::sqrt(dot3(g.r, g.r)));
+          const double el[3] = {-std::sin(lam), std::cos(lam), 0.0};
+          const double ep[3] = {-std::sin(phi) * std::cos(lam), -std::sin(phi) * std::sin(lam), std::cos(phi)};
+          const double vl = dot3(V, el), vp = dot3(V, ep);
+          const double pc = 2.0 * std::sin(phi);
+          const double fl = pc * vp, fp = -pc * vl;
+          const double F[3] = {fl * el[0] + fp * ep[0], fl * el[1] + fp * ep[1], fl * el[2] + fp * ep[2]};
+          const double eu = cu + (-1.0) * dot3(F, g.a1), ev = cv + (-1.0) * dot3(F, g.a2);
+          mu = std::max(mu, std::fabs(eu));
+          mv = std::max(mv, std::fabs(ev));
+          l2u = l2u + eu * eu * g.J * hx * hx;
+          l2v = l2v + ev * ev * g.J * hx * hx;
+        }
+  out[0] = mu + mv;
+  out[1] = std::sqrt(l2u) + std::sqrt(l2v);
+  return 0;
+}
+
+// test_KE with KE_colocated on the A grid (test_diffops_mod.f90:523-587):
+// KE = (u ut + v vt) / 2 (KE_colocated_mod.f90:41-47) from the covariant and
+// contravariant components of the VSH_curl_free_10 and cross-polar fields,
+// against |V|^2 / 2 (test_fields_mod.f90:804-825); nz = 3.  out = {maxabs,
+// l2} of the VSH error, then of the cross-polar error.
+int orc_golden_ke(int N, double out[4]) {
+  const double hx = 0.5 * PI / (double)N;
+  for (int fld = 0; fld < 2; ++fld) {
+    double m = 0.0, l2 = 0.0;
+    for (int lev = 0; lev < 3; ++lev)
+      for (int p = 0; p < 6; ++p)
+        for (int j = 0; j < N; ++j)
+          for (int i = 0; i < N; ++i) {
+            const AGridNode g = agrid_node(N, p, i, j);
+            double V[3];
+            if (fld == 0) field_vsh_curl_free_10(g.r[0], g.r[1], g.r[2], V);
+            else field_cross_polar(g.r[0], g.r[1], g.r[2], V);
+            const double u = dot3(V, g.a1), v = dot3(V, g.a2);
+            const double ut = dot3(V, g.b1), vt = dot3(V, g.b2);
+            const double ke = (u * ut + v * vt) / 2.0;
+            const double e = ke + (-1.0) * (0.5 * (V[0] * V[0] + V[1] * V[1] + V[2] * V[2]));
+            m = std::max(m, std::fabs(e));
+            l2 = l2 + e * e * g.J * hx * hx;
+          }
+    out[2 * fld] = m;
+    out[2 * fld + 1] = std::sqrt(l2);
+  }
+  return 0;
+}
+
 // test_quadrature (test_quadrature/test_quadrature_mod.f90:18-80)
 double orc_golden_quadrature(int N, int order, int max_order) {
   const double ax[3] = {0, 0, 1};

@@ -118,6 +118,9 @@ int orc_golden_grad(int N, int sbp_order, double out[2]);
 int orc_golden_curl(int N, int sbp_order, double out[4]);
 int orc_golden_co2contra(int N, double out[2]);
 int orc_golden_contra2co(int N, double out[2]);
+/* test_coriolis / test_KE of the colocated operators on the A grid */
+int orc_golden_coriolis(int N, double out[2]);
+int orc_golden_ke(int N, double out[4]);
 /* SBP quadrature exactness (test_quadrature_mod.f90:18-80): returns the
  * largest |exact - numeric| over orders 0..max_order at N. */
 double orc_golden_quadrature(int N, int sbp_order, int max_order);

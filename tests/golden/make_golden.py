@@ -2,9 +2,11 @@
 known-answer file src/test/test_diff_ops/reference_results.txt.
 
 Run once in a container that has the reference checked out:
-    python tests/golden/make_golden.py /root/reference
-The JSON keeps only the Ah-grid (colocated, SBP) entries that pin the hot
-path, each with the line number of the reference file it came from.  The
+    python tests/golden/make_golden.py REFERENCE_CHECKOUT
+The JSON keeps only the entries that pin the hot path -- the Ah-grid SBP
+operators and the colocated pointwise operators (co2contra, contra2co,
+Coriolis, kinetic energy; the last two are tested on the A grid) -- each
+with the line number of the reference file it came from.  The
 values were printed by the reference test with format "(A,4E15.7)", i.e. to
 7 significant digits, from test_diffops_all.f90 at N=32, nz=3.
 """
@@ -22,6 +24,8 @@ KEEP = {
     "curl_divergence_ah43_sbp": ("curl", 43),
     "co2contra_colocated Ah grid": ("co2contra", 42),
     "contra2co_colocated": ("contra2co", 42),
+    "coriolis_colocated": ("coriolis", 42),
+    "KE_colocated": ("ke", 42),
 }
 
 
@@ -44,4 +48,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_CHECKOUT")
+    main(sys.argv[1])

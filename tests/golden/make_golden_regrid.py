@@ -2,7 +2,7 @@
 known-answer file src/test/test_regrid/reference_results.txt.
 
 Run once in a container that has the reference checked out:
-    python tests/golden/make_golden_regrid.py /root/reference
+    python tests/golden/make_golden_regrid.py REFERENCE_CHECKOUT
 The JSON keeps the Ah-grid entries (the grid of the hot path): the maximum
 lat-lon interpolation errors of the xyz scalar field and of the solid
 rotation vector field (covariant and contravariant components), for linear
@@ -44,4 +44,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden_regrid.py REFERENCE_CHECKOUT")
+    main(sys.argv[1])
