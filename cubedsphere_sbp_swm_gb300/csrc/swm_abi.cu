@@ -250,6 +250,13 @@ int fail(swm_ctx* c, int code, const std::string& msg) {
 int cuda_fail(swm_ctx* c, cudaError_t e, const char* where) {
   return fail(c, SWM_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
+// Makes the context's device current; a bad device index is reported here,
+// not later as an unrelated CUDA error.
+#define USE_DEVICE(c)                                                 \
+  do {                                                                \
+    cudaError_t e_ = cudaSetDevice((c)->cfg.device);                  \
+    if (e_ != cudaSuccess) return cuda_fail((c), e_, "set device");   \
+  } while (0)
 #define CK(call, where)                                   \
   do {                                                    \
     cudaError_t e_ = (call);                              \
@@ -967,7 +974,7 @@ size_t swm_ctx_npts(const swm_ctx* ctx) { return ctx ? (size_t)6 * ctx->n * ctx-
 
 int swm_set_orography(swm_ctx* ctx, const double* hs) {
   if (!ctx || !hs) return fail(ctx, SWM_E_INVALID, "null argument");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (!ctx->hs64) {
     CK(cudaMalloc(&ctx->hs64, sizeof(double) * ctx->fs), "alloc");
     CK(cudaMemsetAsync(ctx->hs64, 0, sizeof(double) * ctx->fs, ctx->st), "memset");
@@ -989,7 +996,7 @@ int swm_set_orography(swm_ctx* ctx, const double* hs) {
 // ---------------------------------------------------------------- states
 int swm_state_create(swm_ctx* ctx, swm_state** out) {
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   swm_state* s = new swm_state{ctx, nullptr, nullptr};
   const size_t b = (size_t)ctx->elt * 3 * ctx->fs;
   cudaError_t e = cudaMalloc(&s->hi, b);
@@ -1037,7 +1044,7 @@ int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* 
   TraceRange trace_("swm_state_upload");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const double* src[3] = {h, u, v};
   return put_packed(ctx, s, src, cudaMemcpyHostToDevice);
 }
@@ -1046,7 +1053,7 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
   TraceRange trace_("swm_state_download");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   double* dst[3] = {h, u, v};
   if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
   if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
@@ -1058,7 +1065,7 @@ static int combine(swm_ctx* ctx, swm_state* s, double s1, const swm_state* a, do
   if (int rc = check_state(ctx, s)) return rc;
   if (a && check_state(ctx, a)) return SWM_E_INVALID;
   if (b && check_state(ctx, b)) return SWM_E_INVALID;
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const long long cnt = 3 * ctx->fs;
   if (ctx->prec == SWM_FP64_PLAIN) {
     double* o = (double*)s->hi;
@@ -1109,7 +1116,7 @@ int swm_dot(swm_ctx* ctx, const swm_state* a, const swm_state* b, double* out) {
   if (int rc = check_state(ctx, a)) return rc;
   if (int rc = check_state(ctx, b)) return rc;
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const double *ah, *au, *av, *bh, *bu, *bv;
   if (ctx->prec == SWM_FP32_FUSED) {
     // join a into 11..13 and b into 8..10
@@ -1144,7 +1151,7 @@ int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
   if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (ctx->prec == SWM_FP64_PLAIN) {
     InstDev<double> I = base_inst<double>(ctx);
     I.in = (const double*)vin->hi; I.out = (double*)vout->hi;
@@ -1161,7 +1168,7 @@ int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
   if (ctx->prec != SWM_FP64_PLAIN) return fail(ctx, SWM_E_UNSUPPORTED, "unfused apply is FP64 only");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const long long fs = ctx->fs;
   const double* h = (const double*)vin->hi;
   const double* u = h + fs;
@@ -1416,7 +1423,7 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
   if (nsteps == 0) return SWM_OK;
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (ctx->timing) {
     for (int k = 0; k < nsteps; ++k)
       if (int rc = enqueue_rk4_any(ctx, v0, dt)) return rc;
@@ -1436,7 +1443,7 @@ int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_
                          : (hordiff_h_name ? hordiff_h_name : "(null)")));
   if (!std::isfinite(uv_diff_coeff) || !std::isfinite(h_diff_coeff))
     return fail(ctx, SWM_E_INVALID, "bad diffusion coefficient");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const int old_uv = ctx->diff_uv, old_h = ctx->diff_h;
   const double old_cu = ctx->diff_uv_coeff, old_ch = ctx->diff_h_coeff;
   ctx->diff_uv = uv; ctx->diff_h = h;
@@ -1459,7 +1466,7 @@ int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
   if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (int rc = diffusion_ready(ctx)) return rc;
   const long long fs = ctx->g64.fs;
   if (ctx->prec == SWM_FP64_PLAIN) {
@@ -1477,7 +1484,7 @@ int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
   TraceRange trace_("swm_diffusion_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (int rc = diffusion_ready(ctx)) return rc;
   if (nsteps == 0) return SWM_OK;
   return graph_steps(ctx, v0, dt, 2, nsteps, [&] { return enqueue_diffusion_step(ctx, v0, dt); });
@@ -1487,7 +1494,7 @@ int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
   TraceRange trace_("swm_model_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (!ctx->diff_uv) return swm_rk4_step(ctx, v0, dt, nsteps);
   if (int rc = diffusion_ready(ctx)) return rc;
   if (nsteps == 0) return SWM_OK;
@@ -1505,7 +1512,7 @@ int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_or
     return fail(ctx, SWM_E_UNSUPPORTED, "narrow Laplacian order must be 42 or 63");
   if (ctx->prec != SWM_FP64_PLAIN)
     return fail(ctx, SWM_E_UNSUPPORTED, "swm_laplace works on FP64 contexts");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (int rc = diffusion_ws(ctx, narrow_order)) return rc;
   double* F = dwork<double>(ctx, 0);   // the input may be the output
   CK(cudaMemcpyAsync(F, in->p, sizeof(double) * ctx->g64.fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
@@ -1516,7 +1523,7 @@ int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
   TraceRange trace_("swm_diagnostics");
   if (int rc = check_state(ctx, s)) return rc;
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const double *h, *u, *v;
   if (int rc = state64(ctx, s, &h, &u, &v)) return rc;
   double* z = tmpf(ctx, 0);
@@ -1541,7 +1548,7 @@ int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
 // ---------------------------------------------------------------- fields
 int swm_field_create(swm_ctx* ctx, swm_field** out) {
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   swm_field* f = new swm_field{ctx, nullptr};
   cudaError_t e = cudaMalloc(&f->p, sizeof(double) * ctx->fs);
   if (e == cudaSuccess) e = cudaMemsetAsync(f->p, 0, sizeof(double) * ctx->fs, ctx->st);
@@ -1570,14 +1577,14 @@ void swm_field_free(swm_field* f) {
 int swm_field_upload(swm_ctx* ctx, swm_field* f, const double* host) {
   if (int rc = check_field(ctx, f)) return rc;
   if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   return put_field(ctx, f->p, host);
 }
 
 int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
   if (int rc = check_field(ctx, f)) return rc;
   if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t bytes = sizeof(double) * 6 * (size_t)ctx->n * ctx->n;
   PackedFields pf{{(double*)mapped_host(host, bytes), nullptr, nullptr}};
   const bool staged = !pf.f[0];
@@ -1593,7 +1600,7 @@ int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
     const swm_field* fl_[] = {__VA_ARGS__};                     \
     for (const swm_field* f_ : fl_)                             \
       if (int rc_ = check_field(ctx, f_)) return rc_;           \
-    cudaSetDevice(ctx->cfg.device);                             \
+    USE_DEVICE(ctx);                                            \
   } while (0)
 
 int swm_op_co2contra(swm_ctx* ctx, swm_field* ut, swm_field* vt, const swm_field* u, const swm_field* v) {
@@ -1721,6 +1728,12 @@ int efail(swm_ensemble* e, int code, const std::string& msg) {
   if (e) e->err = msg; else g_err = msg;
   return code;
 }
+#define USE_ENS_DEVICE(en)                                                  \
+  do {                                                                      \
+    cudaError_t e_ = cudaSetDevice((en)->device);                           \
+    if (e_ != cudaSuccess)                                                  \
+      return efail((en), SWM_E_CUDA, std::string("set device: ") + cudaGetErrorString(e_)); \
+  } while (0)
 #define ECK(call, where)                                                              \
   do {                                                                                \
     cudaError_t e_ = (call);                                                          \
@@ -1869,7 +1882,7 @@ int ens_rebuild(swm_ensemble* ens, int seg_rows, int grid) {
 int ens_check_member(swm_ensemble* ens, int m) {
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (m < 0 || m >= ens->nmem) return efail(ens, SWM_E_INVALID, "member index out of range");
-  cudaSetDevice(ens->device);
+  USE_ENS_DEVICE(ens);
   ECK(cudaStreamSynchronize(ens->st), "sync");
   return SWM_OK;
 }
@@ -1980,14 +1993,14 @@ int swm_ensemble_step(swm_ensemble* ens, int nsteps) {
   TraceRange trace_("swm_ensemble_step");
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (nsteps < 0) return efail(ens, SWM_E_INVALID, "nsteps must be >= 0");
-  cudaSetDevice(ens->device);
+  USE_ENS_DEVICE(ens);
   for (int k = 0; k < nsteps; ++k) ECK(cudaGraphLaunch(ens->graph, ens->st), "graph launch");
   return SWM_OK;
 }
 
 int swm_ensemble_synchronize(swm_ensemble* ens) {
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
-  cudaSetDevice(ens->device);
+  USE_ENS_DEVICE(ens);
   EMEM(sync_check(ens->mem[0], ens->st));
   return SWM_OK;
 }
@@ -1997,14 +2010,14 @@ void* swm_ensemble_stream(swm_ensemble* ens) { return ens ? (void*)ens->st : nul
 int swm_ensemble_set_shape(swm_ensemble* ens, int seg_rows, int grid) {
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (seg_rows < 0 || grid < 0) return efail(ens, SWM_E_INVALID, "tile shape must be >= 0");
-  cudaSetDevice(ens->device);
+  USE_ENS_DEVICE(ens);
   ECK(cudaStreamSynchronize(ens->st), "sync");
   return ens_rebuild(ens, seg_rows, grid);
 }
 
 int swm_ensemble_set_width(swm_ensemble* ens, int cols) {
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
-  cudaSetDevice(ens->device);
+  USE_ENS_DEVICE(ens);
   ECK(cudaStreamSynchronize(ens->st), "sync");
   if (ens->prec != SWM_FP32_FUSED && cols != ens->cols)
     return efail(ens, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
@@ -2033,7 +2046,7 @@ int swm_ensemble_tune(swm_ensemble* ens, int steps, int* seg_rows_out, int* grid
   TraceRange trace_("swm_ensemble_tune");
   if (!ens) return efail(nullptr, SWM_E_INVALID, "null ensemble");
   if (steps < 1) return efail(ens, SWM_E_INVALID, "steps must be >= 1");
-  cudaSetDevice(ens->device);
+  USE_ENS_DEVICE(ens);
   ECK(cudaStreamSynchronize(ens->st), "sync");
   // the trial steps advance the members: keep their states and restore them
   const int M = ens->nmem;
@@ -2292,7 +2305,7 @@ int check_tl_args(swm_ctx* ctx, const swm_state* a, const swm_state* b, const sw
   if (c && check_state(ctx, c)) return SWM_E_INVALID;
   if (a == b || (c && (c == a || c == b)))
     return fail(ctx, SWM_E_INVALID, "tangent-linear / adjoint calls need distinct states");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   return adjoint_ws(ctx, tl);
 }
 
@@ -2426,7 +2439,7 @@ int swm_adjoint_create(swm_ctx* ctx, int nsteps, int nsnap, double dt, swm_adjoi
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
   if (nsteps < 1 || nsnap < 1 || !(dt > 0.0))
     return fail(ctx, SWM_E_INVALID, "need nsteps >= 1, nsnap >= 1 and dt > 0");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (int rc = adjoint_ws(ctx, false)) return rc;
   swm_adjoint* adj = new swm_adjoint();
   adj->ctx = ctx; adj->nsteps = nsteps; adj->nsnap = std::min(nsnap, nsteps); adj->dt = dt;
@@ -2457,7 +2470,7 @@ int swm_adjoint_forward(swm_adjoint* adj, const swm_state* x0, swm_state* xT) {
   swm_ctx* ctx = adj->ctx;
   if (int rc = check_state(ctx, x0)) return rc;
   if (int rc = check_state(ctx, xT)) return rc;
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   adj->fwd_steps = adj->adj_steps = 0;
   if (int rc = copy_state(ctx, adj->slot[0], x0)) return rc;
   for (size_t k = 0; k < adj->first_adj; ++k)
@@ -2476,7 +2489,7 @@ int swm_adjoint_backward(swm_adjoint* adj, swm_state* lambda) {
   swm_ctx* ctx = adj->ctx;
   if (int rc = check_state(ctx, lambda)) return rc;
   if (!adj->ready) return fail(ctx, SWM_E_INVALID, "swm_adjoint_backward needs a forward run first");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (int rc = copy_state(ctx, adj->lam, lambda)) return rc;
   for (size_t k = adj->first_adj; k < adj->plan.size(); ++k)
     if (int rc = run_action(adj, adj->plan[k])) return rc;
@@ -2504,7 +2517,7 @@ int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const d
   TraceRange trace_("swm_state_upload_device");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const double* src[3] = {h, u, v};
   return put_packed(ctx, s, src, cudaMemcpyDeviceToDevice);
 }
@@ -2513,14 +2526,14 @@ int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, doubl
   TraceRange trace_("swm_state_download_device");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   double* dst[3] = {h, u, v};
   return get_packed(ctx, s, dst, cudaMemcpyDeviceToDevice);
 }
 
 int swm_quadrature_weights(swm_ctx* ctx, double* w_host) {
   if (!ctx || !w_host) return fail(ctx, SWM_E_INVALID, "null argument");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const int n = ctx->n;
   std::vector<double> A(n), J((size_t)6 * n * n);
   CK(cudaMemcpy(A.data(), ctx->Aw, sizeof(double) * n, cudaMemcpyDeviceToHost), "copy");
@@ -2615,7 +2628,7 @@ int swm_latlon_create(swm_ctx* ctx, int nlon, int nlat, const char* interp_type,
   LatLonHost h;
   if (latlon_setup(ctx->N, nlon, nlat, w, contra, ctx->g64, h))
     return fail(ctx, SWM_E_INVALID, "lat-lon set-up failed");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   swm_latlon* r = new swm_latlon{ctx, nlon, nlat, w, contra, nullptr, nullptr, nullptr, nullptr,
                                  nullptr, nullptr, nullptr, nullptr};
   const size_t np = (size_t)nlon * nlat;
@@ -2656,7 +2669,7 @@ int swm_latlon_regrid_field(swm_ctx* ctx, swm_latlon* r, const swm_field* f, dou
   if (int rc = check_latlon(ctx, r)) return rc;
   if (int rc = check_field(ctx, f)) return rc;
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t np = (size_t)r->nlon * r->nlat;
   CK(launch_latlon<double>(ctx->g64, latlon_dev(r), 1, f->p, nullptr, nullptr, nullptr, r->out, nullptr,
                            ctx->st),
@@ -2673,7 +2686,7 @@ int swm_latlon_regrid_vector(swm_ctx* ctx, swm_latlon* r, const swm_field* u, co
   if (int rc = check_field(ctx, u)) return rc;
   if (int rc = check_field(ctx, v)) return rc;
   if (!uo || !vo) return fail(ctx, SWM_E_INVALID, "null output");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t np = (size_t)r->nlon * r->nlat;
   CK(launch_latlon<double>(ctx->g64, latlon_dev(r), 2, u->p, v->p, nullptr, nullptr, r->out, nullptr,
                            ctx->st),
@@ -2690,7 +2703,7 @@ int swm_latlon_regrid_state(swm_ctx* ctx, swm_latlon* r, const swm_state* s, dou
   TraceRange trace_("swm_latlon_regrid_state");
   if (int rc = check_latlon(ctx, r)) return rc;
   if (int rc = check_state(ctx, s)) return rc;
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t np = (size_t)r->nlon * r->nlat;
   if (h) {
     if (int rc = latlon_state(ctx, r, s, false, false)) return rc;
@@ -2714,7 +2727,7 @@ int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char
   if (int rc = check_latlon(ctx, r)) return rc;
   if (int rc = check_state(ctx, s)) return rc;
   if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t np = (size_t)r->nlon * r->nlat;
   if (h_file && *h_file) {
     if (int rc = latlon_state(ctx, r, s, false, true)) return rc;
@@ -2737,7 +2750,7 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
   if (int rc = check_state(ctx, s)) return rc;
   if (component < 0 || component > 2 || !file) return fail(ctx, SWM_E_INVALID, "bad component or file");
   if (rec_num < 1) return fail(ctx, SWM_E_INVALID, "record numbers start at 1");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t np = (size_t)6 * ctx->n * ctx->n;
   PackedFields pf{{tmpf(ctx, 11), nullptr, nullptr}};
   const long long off = (long long)component * ctx->fs;
@@ -2759,7 +2772,7 @@ int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* 
   TraceRange trace_("swm_tune_stage");
   if (int rc = check_state(ctx, s)) return rc;
   if (steps < 1 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or steps");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   auto report = [&](int c, int r, int g, int b, double ms) {
     if (cols_out) *cols_out = c;
     if (seg_rows_out) *seg_rows_out = r;
@@ -2859,7 +2872,7 @@ int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid, int box)
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   if (seg_rows < 0 || grid < 0) return fail(ctx, SWM_E_INVALID, "shape values must be >= 0");
   if (box < SWM_BOX_AUTO || box > SWM_BOX_WIDEST) return fail(ctx, SWM_E_INVALID, "unknown box mode");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   if (!ctx->shape.tma && cols != ctx->shape.cols)
     return fail(ctx, SWM_E_UNSUPPORTED, "the FP64 stage kernel has a single width");
   return stage_layout(ctx, cols, seg_rows, grid, ctx->shape.tma ? box : SWM_BOX_AUTO);
@@ -2883,7 +2896,7 @@ int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double ti
   TraceRange trace_("swm_state_save");
   if (int rc = check_state(ctx, s)) return rc;
   if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   const size_t np = (size_t)6 * ctx->n * ctx->n;
   std::vector<double> buf(3 * np);
   double* dst[3] = {buf.data(), buf.data() + np, buf.data() + 2 * np};
@@ -2893,12 +2906,23 @@ int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double ti
   std::memcpy(hd.magic, "SWMSTATE", 8);
   hd.version = 1; hd.N = (uint32_t)ctx->N; hd.order = (uint32_t)ctx->order;
   hd.precision = (uint32_t)ctx->prec; hd.time = time;
-  FILE* fp = std::fopen(path, "wb");
-  if (!fp) return fail(ctx, SWM_E_IO, std::string("cannot open ") + path);
+  // Written to path + ".tmp" and renamed over path only when complete, so a
+  // failed or interrupted write leaves an earlier restart file at path intact.
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* fp = std::fopen(tmp.c_str(), "wb");
+  if (!fp) return fail(ctx, SWM_E_IO, "cannot open " + tmp);
   bool ok = std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
             std::fwrite(buf.data(), sizeof(double), buf.size(), fp) == buf.size();
+  ok = (std::fflush(fp) == 0) && ok;
   ok = (std::fclose(fp) == 0) && ok;
-  if (!ok) return fail(ctx, SWM_E_IO, std::string("cannot write ") + path);
+  if (!ok) {
+    std::remove(tmp.c_str());
+    return fail(ctx, SWM_E_IO, std::string("cannot write ") + path);
+  }
+  if (std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return fail(ctx, SWM_E_IO, std::string("cannot rename the restart file to ") + path);
+  }
   return SWM_OK;
 }
 
@@ -2906,7 +2930,7 @@ int swm_state_load(swm_ctx* ctx, swm_state* s, const char* path, double* time) {
   TraceRange trace_("swm_state_load");
   if (int rc = check_state(ctx, s)) return rc;
   if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
-  cudaSetDevice(ctx->cfg.device);
+  USE_DEVICE(ctx);
   FILE* fp = std::fopen(path, "rb");
   if (!fp) return fail(ctx, SWM_E_IO, std::string("cannot open ") + path);
   StateFileHeader hd{};

@@ -426,9 +426,13 @@ __global__ void __launch_bounds__(CONS + 32)
   for (int c = 0; c < nch; ++c, ++gc) {
     const int s = gc % NST;
     const uint32_t ph = (uint32_t)(gc / NST) & 1u;
-    bool ok = true;
-    if (!*abort_flag) ok = mbar_wait_bounded(&full[s], ph, kWaitLimitNs);
-    if (!ok) { *abort_flag = 1; atomicExch(err, 3); }
+    // After an abort nothing of this chunk is read or stored: its copies may
+    // not have landed, and the caller's state stays as it was.
+    bool ok = false;
+    if (!*abort_flag) {
+      ok = mbar_wait_bounded(&full[s], ph, kWaitLimitNs);
+      if (!ok) { *abort_flag = 1; atomicExch(err, 3); }
+    }
     // this thread's column in the stage; element (field f, box row q) of the
     // box at element offset e is sx[e + (f * RPS + q) * bw]
     const T* sx = reinterpret_cast<const T*>(stg + (size_t)s * st_bytes) + x;
