@@ -14,7 +14,13 @@ measured beside it, and the FP32 state is compared with the FP64 state after
                   [--workload n384_d42|n1024_d63]
 
 n1024_d63 is the large single instance: 6 x 1025^2 nodes, SBP 6/3, dt = 45 s,
-balanced flow plus a barotropically unstable jet.
+balanced flow plus a barotropically unstable jet.  The default run also
+measures it beside the headline (key "large_instance").
+
+Every GPU result is stated with its error against the FP64 oracle (the C++
+restatement of the reference) on the same initial state, and the oracle is
+timed on the host cores as the CPU baseline (--impl reference; the default
+run's cpu_baseline leg runs that same measurement in a fresh process).
 
 Multi-GPU runs (torchrun) are independent replicas, one per GPU: the path
 does not shard across GPUs here (all six panels live on one GPU).
@@ -50,10 +56,15 @@ KERNELS_PER_STEP = 8                # 4 x (stage kernel + cube-edge kernel)
 # turns non-finite within 6 simulated hours.  Courant 0.84 (N=384, 90 s) and
 # 0.74 (N=1024 d63, 30 s) stay stable over the full simulated period.  The
 # per-step work, and so steps/s, does not depend on dt.
+# oracle_hours: simulated hours of the run against the FP64 oracle (its CPU
+# cost bounds it); acc_days_extra: the FP32-vs-FP64 GPU run when the workload
+# is measured beside the headline.
 WORKLOADS = {
-    "n384_d42": dict(N=384, order=42, dt=120.0, cfg=2, days=10.0, acc_dt=90.0,
+    "n384_d42": dict(N=384, order=42, dt=120.0, cfg=2, days=10.0, acc_dt=90.0, oracle_hours=24.0,
+                     acc_days_extra=10.0,
                      desc="6 panels x 385^2 nodes (N=384), SBP 4/2 (d42), RK4 dt=120 s"),
-    "n1024_d63": dict(N=1024, order=63, dt=45.0, cfg=5, days=5.0, acc_dt=30.0,
+    "n1024_d63": dict(N=1024, order=63, dt=45.0, cfg=5, days=5.0, acc_dt=30.0, oracle_hours=0.5,
+                      acc_days_extra=1.0,
                       desc="6 panels x 1025^2 nodes (N=1024), SBP 6/3 (d63), RK4 dt=45 s"),
 }
 
@@ -153,11 +164,54 @@ def _data_desc(w, info):
             "perturbation, 10 m RMS" % info["u0"])
 
 
+def accuracy_vs_oracle(w, h, u, v, local, hours):
+    """The FP32 fused form and the FP64 plain path against the FP64 oracle
+    (the C++ restatement of the reference) after `hours` simulated hours from
+    the same initial state at the stable time step acc_dt: J-weighted
+    relative L2 (vec_math_mod.f90:50-90 weighting) and relative Linf of h, u,
+    v, and the SBP-quadrature mass of each run against the oracle's."""
+    import numpy as np
+
+    import cubedsphere_sbp_swm_gb300 as swm
+    from cubedsphere_sbp_swm_gb300 import initial
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker
+
+    dt = w["acc_dt"]
+    nsteps = int(round(hours * 3600.0 / dt))
+    J = initial.ecs_geometry(w["N"])["J"]
+    oracle.set_threads(os.cpu_count() or 1)
+    od = oracle.OracleDomain(w["N"], w["order"])
+    t0 = time.perf_counter()
+    ref = [a.copy() for a in (h, u, v)]
+    od.rk4_inplace(*ref, dt, nsteps)
+    oracle_s = time.perf_counter() - t0
+    m_ref, m0 = od.mass(ref[0]), od.mass(h)
+    out = {"reference": "FP64 oracle (C++ restatement of the reference), same initial state",
+           "hours": hours, "dt_s": dt, "steps": nsteps, "oracle_run_s": round(oracle_s, 2),
+           "oracle_mass_drift": (m_ref - m0) / m0}
+    for prec in ("fp32", "fp64"):
+        op = swm.OperatorSWM(swm.ModelConfig(N=w["N"], sbp_order=w["order"], precision=prec, device=local))
+        s = op.create_stvec()
+        s.upload(h, u, v)
+        swm.RK4().step(s, op, dt, nsteps)
+        got = s.download()
+        del s, op
+        r = {}
+        for name, a, b in zip("huv", got, ref):
+            r[f"{name}_rel_l2"] = float(np.sqrt(np.sum(J * (a - b) ** 2) / np.sum(J * b * b)))
+            r[f"{name}_rel_linf"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+        r["mass_rel_diff_vs_oracle"] = (od.mass(got[0]) - m_ref) / m_ref
+        out[prec] = r
+    return out
+
+
 def accuracy_vs_fp64(w, h, u, v, local, days):
     """FP32 fused form against the FP64 plain path (which matches the FP64
-    oracle to 1e-12 per step) after `days` simulated days from the same
-    initial state at the stable time step acc_dt: J-weighted relative L2 and
-    relative Linf of h, u, v and the SBP-quadrature mass drift of both runs."""
+    oracle to 1e-12 per step; accuracy_vs_oracle checks it over a shorter run)
+    after `days` simulated days from the same initial state at the stable time
+    step acc_dt: J-weighted relative L2 and relative Linf of h, u, v and the
+    SBP-quadrature mass drift of both runs."""
     import numpy as np
 
     import cubedsphere_sbp_swm_gb300 as swm
@@ -176,7 +230,8 @@ def accuracy_vs_fp64(w, h, u, v, local, days):
         res[prec] = s.download()
         drift[prec] = (op.get_diagnostics(s)["mass"] - m0) / m0
         del s, op
-    out = {"days": days, "dt_s": dt, "steps": nsteps, "reference": "FP64 plain GPU path",
+    out = {"days": days, "dt_s": dt, "steps": nsteps,
+           "reference": "FP64 plain GPU path (matches the FP64 oracle to 1e-12 relative L2 per step)",
            "note": "the workload dt (Courant 1.11) is beyond the RK4 stability limit of the "
                    "undiffused scheme (FP64 state non-finite within 6 simulated hours); this run "
                    "uses the stable dt_s"}
@@ -414,27 +469,25 @@ def adjoint_leg(local):
     }
 
 
-def run_gpu_arm(args):
+def single_instance_leg(w, local, steps, warmup, stage_shape=None, state=None, quick=False):
+    """The RK4 step of one workload, FP32 fused form and FP64 plain path:
+    device-timed steps (each from the initial state, L2 flushed before it),
+    CUDA-event timing of the stage kernel, and end-to-end steps through the
+    C-ABI with page-locked host buffers (upload, step, download inside the
+    timed region).  Returns (result dict, FP32 per-step ms list, clocks, info)."""
+    import numpy as np
     import torch
 
     import cubedsphere_sbp_swm_gb300 as swm
     from cubedsphere_sbp_swm_gb300 import replicas
 
-    w = WORKLOADS[args.workload]
     N, ORDER, DT = w["N"], w["order"], w["dt"]
-    ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    h, u, v, info = _state(w)
+    h, u, v, info = state if state is not None else _state(w)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    tuned = {"width": 128, "seg_rows": 0, "grid": 0, "box": "auto"}
 
-    tuned = {"width": 128, "seg_rows": 0, "grid": 0}
-
-    def time_steps(prec, steps, warmup, kernel_timing=False):
+    def time_steps(prec, nsteps, nwarm, kernel_timing=False):
         """Every timed step starts from the initial state (restored outside
         the timed region): at the workload's dt the scheme is past its RK4
         stability limit, and a state left to run for the whole timed region
@@ -443,8 +496,8 @@ def run_gpu_arm(args):
         s0 = op.create_stvec()
         s0.upload(h, u, v)
         if prec == "fp32":   # set-up: pick the stage kernel's fastest launch shape
-            if args.stage_shape:
-                parts = args.stage_shape.split(",")
+            if stage_shape:
+                parts = stage_shape.split(",")
                 wdt, seg, grd = (int(x) for x in parts[:3])
                 op.set_stage_shape(wdt, seg, grd, parts[3] if len(parts) > 3 else "auto")
                 tuned.update(op.stage_shape)
@@ -454,14 +507,14 @@ def run_gpu_arm(args):
         s.assign_s1v1(1.0, s0)
         ts = swm.RK4()
         stream = torch.cuda.ExternalStream(op.stream, device=dev)
-        for _ in range(warmup):
+        for _ in range(nwarm):
             ts.step(s, op, DT, 1)
         op.synchronize()
         if kernel_timing:
             op.timing_enable(True)
             op.timing_read()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(steps)]
+               for _ in range(nsteps)]
         torch.cuda.synchronize(dev)
         for a, b in evs:
             s.assign_s1v1(1.0, s0)                    # on the op stream, before the flush
@@ -477,24 +530,113 @@ def run_gpu_arm(args):
             op.timing_enable(False)
         return op, s, ms, kt
 
+    def e2e(op, s, nsteps):
+        """Steps/s through the C-ABI with host buffers: every step uploads the
+        state from page-locked FP64 host arrays, steps, and downloads it."""
+        pin = [torch.empty((6, N + 1, N + 1), dtype=torch.float64, pin_memory=True) for _ in range(6)]
+        for t_, a_ in zip(pin[:3], (h, u, v)):
+            t_.numpy()[...] = a_
+        hin = [t_.numpy() for t_ in pin[:3]]
+        hout = [t_.numpy() for t_ in pin[3:]]
+        ts = swm.RK4()
+        for _ in range(2):
+            s.upload_async(*hin)
+            ts.step(s, op, DT, 1)
+            s.download(out=hout)
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            s.upload_async(*hin)
+            ts.step(s, op, DT, 1)
+            s.download(out=hout)
+        val, _ = replicas.job_rate(nsteps, time.perf_counter() - t0, dev)
+        return val
+
     uuid = None
     try:
         uuid = str(torch.cuda.get_device_properties(dev).uuid)
     except Exception:
         pass
-
-    # headline: FP32 fused form, graph-replayed steps
-    if ws > 1:
-        torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     with ClockSampler(uuid) as clk:
-        op32, s32, ms32, _ = time_steps("fp32", args.steps, args.warmup)
+        op32, s32, ms32, _ = time_steps("fp32", steps, warmup)
     clocks = clk.summary()
-    import numpy as np
+    if quick:
+        return {}, ms32, clocks, info
     finite = bool(all(np.isfinite(a).all() for a in s32.download()))
+    nsteps_e2e = max(10, steps // 2)
+    e2e32 = e2e(op32, s32, nsteps_e2e)
+    del s32, op32
+
+    # dominant kernel timing (stage kernel), events around every launch
+    _, _, _, kt = time_steps("fp32", max(8, min(steps, 40)), 2, kernel_timing=True)
+    stage_ms, stage_n, edge_ms, edge_n = kt
+    npts = 6 * (N + 1) ** 2
+    bytes_per_launch = BYTES_PER_NODE_STEP["fp32"] * npts / 4.0
+    achieved = bytes_per_launch / (stage_ms / stage_n / 1e3) / 1e9
+    peak, peak_kind = _measured_peak()
+
+    op64, s64, ms64, _ = time_steps("fp64", max(10, steps // 2), warmup)
+    fp64_ms = sum(ms64) / len(ms64)
+    e2e64 = e2e(op64, s64, nsteps_e2e)
+    del op64, s64
+    _, _, _, kt64 = time_steps("fp64", 10, 2, kernel_timing=True)
+    fp32_ms = sum(ms32) / len(ms32)
+    res = {
+        "workload": w["desc"], "N": N, "sbp": "d%d" % ORDER, "dt_s": DT, "nodes_per_field": npts,
+        "fp32": {"steps_per_s": round(1e3 / fp32_ms, 3), "ms_per_step": round(fp32_ms, 5),
+                 "stage_shape": {k: tuned[k] for k in ("width", "seg_rows", "grid", "box")}},
+        "fp64_plain": {"steps_per_s": round(1e3 / fp64_ms, 3), "ms_per_step": round(fp64_ms, 5),
+                       "stage_kernel_avg_us": round(kt64[0] / kt64[1] * 1e3, 3),
+                       "e2e_steps_per_s": round(e2e64, 3)},
+        "fp32_over_fp64": round(fp64_ms / fp32_ms, 3),
+        "e2e": {"value": round(e2e32, 3), "unit": "steps/s",
+                "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,
+                "path": "swm_state_upload (pinned FP64 host arrays, read in place over the host link) "
+                        "+ swm_rk4_step + swm_state_download (written in place)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4),
+                     "traffic": _profile_traffic("n%d_d%d" % (N, ORDER)),
+                     "kernel": "stage_tma_kernel<float,%d,mode,%d>" % (ORDER, tuned["width"]),
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "avg_launch_us": round(stage_ms / stage_n * 1e3, 3)},
+        "launches_per_step": KERNELS_PER_STEP,
+        "state_finite_after_timed_steps": finite,
+    }
+    if edge_n:
+        res["roofline"]["edge_kernel_avg_us"] = round(edge_ms / edge_n * 1e3, 3)
+    return res, ms32, clocks, info
+
+
+def run_gpu_arm(args):
+    import torch
+
+    from cubedsphere_sbp_swm_gb300 import replicas
+
+    w = WORKLOADS[args.workload]
+    N, ORDER, DT = w["N"], w["order"], w["dt"]
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    state = _state(w)
+    h, u, v, info = state
+
+    # CPU baseline first, in a fresh process (the same measurement as
+    # --impl reference), before this process starts its GPU work
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu and not args.quick:
+        cpu = cpu_baseline_subprocess(args)
+
+    if ws > 1:
+        torch.distributed.barrier()
+    head, ms32, clocks, _ = single_instance_leg(w, local, args.steps, args.warmup, args.stage_shape, state,
+                                                quick=args.quick)
     value, total_s = replicas.job_rate(args.steps, sum(ms32) / 1e3, dev)
-    total_ms = total_s * 1e3
-    ms_per_step = total_ms / args.steps
+    ms_per_step = total_s * 1e3 / args.steps
     if args.quick:  # profiling case: only the timed FP32 steps
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "steps/s",
@@ -502,60 +644,31 @@ def run_gpu_arm(args):
                               "workload": args.workload}), flush=True)
         return
 
-    # dominant kernel timing (stage kernel), events around every launch
-    _, _, _, kt = time_steps("fp32", max(8, min(args.steps, 40)), 2, kernel_timing=True)
-    stage_ms, stage_n, edge_ms, edge_n = kt
-    npts = 6 * (N + 1) ** 2
-    bytes_per_launch = BYTES_PER_NODE_STEP["fp32"] * npts / 4.0
-    achieved = bytes_per_launch / (stage_ms / stage_n / 1e3) / 1e9
-    peak, peak_kind = _measured_peak()
-    traffic = _profile_traffic(args.workload)
-
-    # FP64 plain path beside it
-    op64, s64, ms64, _ = time_steps("fp64", max(10, args.steps // 2), args.warmup)
-    fp64_ms = sum(ms64) / len(ms64)
-    _, _, _, kt64 = time_steps("fp64", 10, 2, kernel_timing=True)
-    del op64, s64
-
-    # end to end through the C-ABI with host (pinned) buffers
-    pin = [torch.empty((6, N + 1, N + 1), dtype=torch.float64, pin_memory=True) for _ in range(6)]
-    for t_, a_ in zip(pin[:3], (h, u, v)):
-        t_.numpy()[...] = a_
-    hin = [t_.numpy() for t_ in pin[:3]]
-    hout = [t_.numpy() for t_ in pin[3:]]
-    ts = swm.RK4()
-    e2e_steps = max(10, args.steps // 2)
-    for _ in range(2):
-        s32.upload_async(*hin)
-        ts.step(s32, op32, DT, 1)
-        s32.download(out=hout)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        s32.upload_async(*hin)
-        ts.step(s32, op32, DT, 1)
-        s32.download(out=hout)
-    e2e_val, _ = replicas.job_rate(e2e_steps, time.perf_counter() - t0, dev)
-    del s32, op32
-
-    # FP32 form against the FP64 plain path over the workload's simulated days
-    acc = None
+    acc = acc_or = None
     if rank == 0 and not args.no_accuracy:
         acc = accuracy_vs_fp64(w, h, u, v, local, w["days"] if args.days is None else args.days)
-
+        acc_or = accuracy_vs_oracle(w, h, u, v, local, w["oracle_hours"])
+    large = None
+    if rank == 0 and not args.no_large and args.workload != "n1024_d63":
+        wl = WORKLOADS["n1024_d63"]
+        st_l = _state(wl)
+        large, _, clk_l, _ = single_instance_leg(wl, local, max(10, args.steps // 2), args.warmup, None, st_l)
+        large["clocks"] = clk_l
+        if not args.no_accuracy:
+            large["accuracy_fp32_vs_fp64"] = accuracy_vs_fp64(wl, *st_l[:3], local, wl["acc_days_extra"])
+            large["accuracy_vs_oracle"] = accuracy_vs_oracle(wl, *st_l[:3], local, wl["oracle_hours"])
+        if cpu and "n1024_d63" in cpu.get("rates", {}):
+            large["cpu_oracle"] = cpu["rates"]["n1024_d63"]
+        del st_l
     ens = None
     if rank == 0 and not args.no_ensemble:
-        ens = ensemble_leg(local, max(10, args.steps // 2), args.warmup, peak)
+        ens = ensemble_leg(local, max(10, args.steps // 2), args.warmup, _measured_peak()[0])
     adj = None
     if rank == 0 and not args.no_adjoint:
         adj = adjoint_leg(local)
     dif = None
     if rank == 0 and not args.no_diffusion:
         dif = diffusion_leg(w, h, u, v, local, max(10, args.steps // 2), args.warmup)
-
-    # CPU baseline: the oracle (C++ restatement) on the host cores, rank 0
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline_sample(w, h, u, v, budget_s=args.cpu_budget)
 
     if rank == 0:
         line = {
@@ -565,30 +678,29 @@ def run_gpu_arm(args):
             "data": _data_desc(w, info),
             "config": {"workload": w["desc"] + ", FP32 fused form (compensated stage sums, FP64 "
                                                "metric precompute)",
-                       "N": N, "sbp": "d%d" % ORDER, "dt_s": DT, "nodes_per_field": npts,
+                       "N": N, "sbp": "d%d" % ORDER, "dt_s": DT, "nodes_per_field": head["nodes_per_field"],
                        "l2": "256 MB buffer written between timed steps",
-                       "stage_shape": {k: tuned[k] for k in ("width", "seg_rows", "grid", "box")},
+                       "stage_shape": head["fp32"]["stage_shape"],
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
-            "e2e": {"value": round(e2e_val, 3), "unit": "steps/s",
-                    "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,
-                    "path": "swm_state_upload (pinned FP64 host arrays, read in place over the host link) + swm_rk4_step + swm_state_download (written in place)"},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "kernel": "stage_tma_kernel<float,%d,mode,%d>" % (ORDER, tuned["width"]),
-                         "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "avg_launch_us": round(stage_ms / stage_n * 1e3, 3),
-                         "edge_kernel_avg_us": round(edge_ms / max(edge_n, 1) * 1e3, 3)},
-            "fp64_plain": {"value": round(1e3 / fp64_ms, 3), "unit": "steps/s",
-                           "ms_per_step": round(fp64_ms, 5),
-                           "stage_kernel_avg_us": round(kt64[0] / kt64[1] * 1e3, 3)},
-            "fp32_over_fp64": round((1e3 / ms_per_step) / (1e3 / fp64_ms), 3),
+            "e2e": head["e2e"],
+            "roofline": head["roofline"],
+            "fp64_plain": {"value": head["fp64_plain"]["steps_per_s"], "unit": "steps/s",
+                           "ms_per_step": head["fp64_plain"]["ms_per_step"],
+                           "stage_kernel_avg_us": head["fp64_plain"]["stage_kernel_avg_us"],
+                           "e2e": {"value": head["fp64_plain"]["e2e_steps_per_s"], "unit": "steps/s",
+                                   "h2d_bytes_per_step": head["e2e"]["h2d_bytes_per_step"],
+                                   "d2h_bytes_per_step": head["e2e"]["d2h_bytes_per_step"]}},
+            "fp32_over_fp64": head["fp32_over_fp64"],
             "clocks": clocks,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
-            "state_finite_after_timed_steps": finite,
+            "state_finite_after_timed_steps": head["state_finite_after_timed_steps"],
         }
+        if acc_or:
+            line["accuracy_vs_oracle"] = acc_or
         if acc:
             line["accuracy_fp32_vs_fp64"] = acc
+        if large:
+            line["large_instance"] = large
         if ens:
             line["ensemble"] = ens
         if adj:
@@ -596,7 +708,8 @@ def run_gpu_arm(args):
         if dif:
             line["model_step_with_diffusion"] = dif
         if cpu:
-            line["cpu_baseline"] = cpu
+            line["cpu_baseline"] = cpu["cpu_baseline"]
+            line["cpu_rates"] = cpu["rates"]
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.barrier()
@@ -654,30 +767,50 @@ def diffusion_leg(w, h, u, v, local, steps, warmup):
     return out
 
 
-def cpu_baseline_sample(w, h, u, v, budget_s=15.0, min_steps=1, max_steps=50):
-    """Time RK4 steps of the FP64 oracle with all host threads on a bounded
-    sample (whole steps of the workload until the time budget is used)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the CPU restatement of the reference (checker / baseline)
-    cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
-    od = oracle.OracleDomain(w["N"], w["order"])
-    hh, uu, vv = h.copy(), u.copy(), v.copy()
-    hh, uu, vv = od.rk4(hh, uu, vv, w["dt"], 1)            # warm-up
+def _oracle_rate(od, state, dt, threads, window_s, warm_s, min_steps=1):
+    """Oracle RK4 steps/s with `threads` OpenMP threads: whole steps on the
+    caller's arrays in place, after warm_s seconds of untimed steps, timed
+    over at least window_s seconds."""
+    import oracle
+    oracle.set_threads(threads)
+    h, u, v = (a.copy() for a in state)
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < warm_s:
+        od.rk4_inplace(h, u, v, dt, 1)
     steps, t0 = 0, time.perf_counter()
-    while steps < max_steps and (steps < min_steps or time.perf_counter() - t0 < budget_s):
-        hh, uu, vv = od.rk4(hh, uu, vv, w["dt"], 1)
+    while steps < min_steps or time.perf_counter() - t0 < window_s:
+        od.rk4_inplace(h, u, v, dt, 1)
         steps += 1
-    dt = time.perf_counter() - t0
-    return {"value": round(steps / dt, 4), "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} RK4 steps of the N={w['N']} d{w['order']} FP64 oracle (C++ restatement "
-                      f"of the reference), OpenMP over panel rows"}
+    el = time.perf_counter() - t0
+    return steps / el, steps, el
+
+
+def _cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def run_reference_arm(args):
+    """The reference's CPU path on the host cores: the FP64 oracle (C++
+    restatement of the Fortran reference; the reference itself needs a
+    Fortran compiler and MPI, which neither machine has).  Exactly K timed
+    steps follow W warm-up steps and 2 s of untimed steps; the K-step
+    measurement repeats until the timed window is at least 5 s.  OpenMP
+    threads are pinned to cores (OMP_PROC_BIND=close, OMP_PLACES=cores, set
+    before the runtime loads).  Also reported: the single-thread rate and the
+    N=48 SBP 4/2 configuration's rates, and with --cpu-also the listed
+    workloads' all-thread rates."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
     w = WORKLOADS[args.workload]
     h, u, v, info = _state(w)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -686,26 +819,91 @@ def run_reference_arm(args):
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     od = oracle.OracleDomain(w["N"], w["order"])
+    hh, uu, vv = h.copy(), u.copy(), v.copy()
     for _ in range(args.warmup):
-        h, u, v = od.rk4(h, u, v, w["dt"], 1)
+        od.rk4_inplace(hh, uu, vv, w["dt"], 1)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        h, u, v = od.rk4(h, u, v, w["dt"], 1)
-    el = time.perf_counter() - t0
-    val = args.steps / el
+    while time.perf_counter() - t0 < 2.0:
+        od.rk4_inplace(hh, uu, vv, w["dt"], 1)
+    # the state turns non-finite after a few hours at the workload dt; every
+    # K-step block restarts from the initial state (outside the timed region)
+    el, blocks = 0.0, 0
+    while blocks < 1 or el < 5.0:
+        hh[...], uu[...], vv[...] = h, u, v
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            od.rk4_inplace(hh, uu, vv, w["dt"], 1)
+        el += time.perf_counter() - t0
+        blocks += 1
+    timed = blocks * args.steps
+    val = timed / el
+    rates = {args.workload: {"threads": cores, "steps_per_s": round(val, 4), "timed_steps": timed,
+                             "window_s": round(el, 3)}}
+    r1, n1, e1 = _oracle_rate(od, (h, u, v), w["dt"], 1, 5.0, 1.0)
+    rates[args.workload].update(single_thread_steps_per_s=round(r1, 4), single_thread_steps=n1,
+                                single_thread_window_s=round(e1, 3),
+                                thread_speedup=round(val / r1, 3))
+    # configuration 1: N=48, SBP 4/2, dt = 900 s (the reference's CPU-runnable case)
+    from cubedsphere_sbp_swm_gb300 import initial
+    c1 = initial.CONFIGS[1]
+    st1 = initial.config_state(1)[:3]
+    od1 = oracle.OracleDomain(c1["N"], c1["sbp_order"])
+    ra, na, ea = _oracle_rate(od1, st1, c1["dt"], cores, 5.0, 1.0)
+    rb, nb, eb = _oracle_rate(od1, st1, c1["dt"], 1, 5.0, 1.0)
+    rates["n48_d42"] = {"threads": cores, "steps_per_s": round(ra, 3), "timed_steps": na,
+                        "single_thread_steps_per_s": round(rb, 3), "single_thread_steps": nb,
+                        "dt_s": c1["dt"], "one_day_s": round(c1["steps"] / ra, 3)}
+    for extra in (args.cpu_also or "").split(","):
+        if extra and extra in WORKLOADS and extra not in rates:
+            we = WORKLOADS[extra]
+            ste = _state(we)[:3]
+            ode = oracle.OracleDomain(we["N"], we["order"])
+            re_, ne, ee = _oracle_rate(ode, ste, we["dt"], cores, 5.0, 1.0, min_steps=3)
+            rates[extra] = {"threads": cores, "steps_per_s": round(re_, 4), "timed_steps": ne,
+                            "window_s": round(ee, 3)}
+            del ode, ste
+    sample = (f"{timed} RK4 steps ({blocks} blocks of K={args.steps}, each from the initial state) "
+              f"of the N={w['N']} d{w['order']} FP64 oracle, the C++ restatement of the reference "
+              f"(the Fortran/MPI reference has no compiler on this image); {cores} OpenMP threads "
+              f"pinned to cores, {el:.1f} s window")
     line = {
         "metric": METRIC, "value": round(val, 4), "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": round(el / timed * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
         "data": _data_desc(w, info),
         "config": {"workload": w["desc"] + ", FP64", "N": w["N"], "sbp": "d%d" % w["order"],
                    "dt_s": w["dt"]},
         "cpu_baseline": {"value": round(val, 4), "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} RK4 steps of the FP64 C++ restatement of the reference "
-                                   "(the Fortran/MPI reference has no compiler on this image)"},
+                         "sample": sample},
         "e2e": {"value": round(val, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_rates": rates,
+        "host": {"cpu": _cpu_model(), "nproc": cores,
+                 "omp": {k: os.environ.get(k) for k in ("OMP_PROC_BIND", "OMP_PLACES")}},
+        "reference_fortran": "not measurable: no Fortran compiler or MPI on the build image or the GPU box",
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_subprocess(args):
+    """The reference arm's measurement (run_reference_arm) in a fresh
+    process, so that the default run's cpu_baseline and the reference arm
+    are one procedure: same code, same thread pinning, no GPU process state.
+    Adds the large instance's oracle rate."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+           "--steps", str(args.steps), "--warmup", str(args.warmup), "--workload", args.workload,
+           "--cpu-also", "n1024_d63" if not args.no_large else ""]
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    try:
+        out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env)
+    except (OSError, subprocess.TimeoutExpired) as e:
+        return {"cpu_baseline": {"unavailable": str(e)}, "rates": {}}
+    for line in out.stdout.splitlines()[::-1]:
+        if line.startswith("{"):
+            d = json.loads(line)
+            cb = dict(d["cpu_baseline"])
+            cb["same_procedure_as"] = "bench.py --impl reference"
+            return {"cpu_baseline": cb, "rates": d.get("cpu_rates", {}), "host": d.get("host")}
+    return {"cpu_baseline": {"unavailable": out.stderr[-300:]}, "rates": {}}
 
 
 def main():
@@ -729,7 +927,10 @@ def main():
                     help="skip the RK4 + hyperdiffusion model-step leg")
     ap.add_argument("--days", type=float, default=None,
                     help="simulated days of the accuracy run (default: the workload's)")
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the large single instance (N=1024, SBP 6/3) beside the headline")
+    ap.add_argument("--cpu-also", default="",
+                    help="reference arm: also time these workloads' oracle (comma-separated)")
     ap.add_argument("--quick", action="store_true",
                     help="profiling case: time only the FP32 steps, print a short line")
     ap.add_argument("--only", choices=("ensemble", "adjoint", "diffusion"), default=None,
