@@ -124,9 +124,46 @@ constexpr double kq67 = 3.0 / 4.0, kq68 = -3.0 / 20.0, kq69 = 1.0 / 60.0;
      {kQ63A1, kQ63A2, kQ63A3, kQ63A4, kQ63A5, kQ63A6}},                                        \
   }
 
+// The closure rows in FP32: the left-end rows rounded once at compile time
+// (as a run-time conversion of the double would round them) and the
+// right-end rows already negated, so no FP32 kernel converts a coefficient
+// at run time (conversions from FP64 run on GB300's narrow FP64 pipe).
+struct SbpF {
+  float Ql[MAXNE * MAXNW];
+  float Qr[MAXNE * MAXNW];   // -Ql
+};
+constexpr SbpC kSbpTables[4] = SWM_SBP_TABLES;
+constexpr SbpF make_sbpf(const SbpC& c) {
+  SbpF f{};
+  for (int k = 0; k < MAXNE * MAXNW; ++k) {
+    f.Ql[k] = float(c.Ql[k]);
+    f.Qr[k] = float(-c.Ql[k]);
+  }
+  return f;
+}
+
 #ifdef __CUDACC__
 // every translation unit carries its own initialised copy (no -rdc)
 static __constant__ SbpC c_sbp[4] = SWM_SBP_TABLES;
+static __constant__ SbpF c_sbpf[4] = {make_sbpf(kSbpTables[0]), make_sbpf(kSbpTables[1]),
+                                      make_sbpf(kSbpTables[2]), make_sbpf(kSbpTables[3])};
+
+// Closure coefficient m of left-end row k (sbp_ql) and of right-end row k,
+// counted from the end, with its sign (sbp_qr = -Ql), in the element type.
+template <class T> __device__ __forceinline__ T sbp_ql(int id, int k, int m);
+template <class T> __device__ __forceinline__ T sbp_qr(int id, int k, int m);
+template <> __device__ __forceinline__ float sbp_ql<float>(int id, int k, int m) {
+  return c_sbpf[id].Ql[k * MAXNW + m];
+}
+template <> __device__ __forceinline__ float sbp_qr<float>(int id, int k, int m) {
+  return c_sbpf[id].Qr[k * MAXNW + m];
+}
+template <> __device__ __forceinline__ double sbp_ql<double>(int id, int k, int m) {
+  return c_sbp[id].Ql[k * MAXNW + m];
+}
+template <> __device__ __forceinline__ double sbp_qr<double>(int id, int k, int m) {
+  return -c_sbp[id].Ql[k * MAXNW + m];
+}
 #endif
 
 // index of an SBP order in the table above

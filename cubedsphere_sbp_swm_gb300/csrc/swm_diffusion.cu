@@ -53,6 +53,24 @@ constexpr NarrowIn32 make_narrow_in32() {
 }
 __constant__ NarrowIn32 c_in32 = make_narrow_in32();
 
+// Closure row scales and the flux penalty of both orders in FP32 (rounded at
+// compile time: the FP32 Laplacian converts no coefficient at run time).
+struct NarrowScale32 {
+  float rowscale[2][NARROW_MAXR];
+  float penalty[2];
+};
+constexpr NarrowScale32 make_narrow_scale32() {
+  NarrowScale32 t{};
+  for (int r = 0; r < NARROW_MAXR; ++r) {
+    t.rowscale[0][r] = float(kNarrow42.rowscale[r]);
+    t.rowscale[1][r] = float(kNarrow63.rowscale[r]);
+  }
+  t.penalty[0] = float(kNarrow42.penalty);
+  t.penalty[1] = float(kNarrow63.penalty);
+  return t;
+}
+__constant__ NarrowScale32 c_scale32 = make_narrow_scale32();
+
 template <int NARROW>
 struct NarrowShape {
   static constexpr int ni = NARROW == 63 ? 1 : 0;
@@ -214,7 +232,7 @@ template <int NARROW, int NF>
 __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty, const float* f,
                                                            const float* clx, const float* cly,
                                                            const float* bco, const float* mt,
-                                                           double hs, float* out, float* E) {
+                                                           float hs2, float* out, float* E) {
   using T = float;
   using S = NarrowShape<NARROW>;
   using LT = LapTile<NARROW, NF>;
@@ -231,7 +249,6 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
   T(*BXs)[RX] = reinterpret_cast<T(*)[RX]>(sm + LT::OFS_BX);
   T(*BYs)[LTX] = reinterpret_cast<T(*)[LTX]>(sm + LT::OFS_BY);
 
-  const NarrowD2& D = c_narrow[S::ni];
   const int n = g.n, P = g.P;
   const int p = blockIdx.y / nty, ty = blockIdx.y - p * nty;
   const int tw = min(LTX, n), th = min(LTY, n);
@@ -321,7 +338,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
 #pragma unroll
     for (int c = 0; c < S::cols; ++c) ax[c] = M[c];
     x0 = (side ? n - 1 : 0) - xlo; xs = side ? -1 : 1;
-    rsx = T(D.rowscale[r]);
+    rsx = c_scale32.rowscale[S::ni][r];
   } else {   // from the variable coefficients along the row
 #pragma unroll
     for (int c = 0; c < S::cols; ++c) {
@@ -340,7 +357,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
 #pragma unroll
     for (int c = 0; c < S::cols; ++c) ay[c] = M[c];
     y0 = (side ? n - 1 : 0) - ylo; ys = side ? -1 : 1;
-    rsy = T(D.rowscale[r]);
+    rsy = c_scale32.rowscale[S::ni][r];
   } else {   // from the variable coefficients along the column
 #pragma unroll
     for (int c = 0; c < S::cols; ++c) {
@@ -354,8 +371,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
     y0 = yr - S::hw; ys = 1;
   }
   const T J = JXs[yr][lx];
-  const T hs2 = T(hs * hs);
-  const T pen = T(D.penalty);
+  const T pen = c_scale32.penalty[S::ni];
 #pragma unroll
   for (int c = 0; c < NF; ++c) {
     // the closure rows read cols taps, the interior w (same order)
@@ -537,8 +553,8 @@ __global__ void from_cart_kernel(FieldGeom g, const T* b, T cuv, const T* L, T* 
 // FP32 (hi, lo) pair element k += dt * t: the increment joins the low part,
 // then a two-sum renormalises the pair (the compensated update of the RK4
 // stage epilogue).
-__device__ __forceinline__ void pair_add(double dt, float t, float* hi, float* lo, long long k) {
-  const float d = float(dt) * t;
+__device__ __forceinline__ void pair_add(float dt, float t, float* hi, float* lo, long long k) {
+  const float d = dt * t;
   const float h = hi[k];
   const float tt = lo[k] + d;
   const float sm = h + tt;
@@ -554,7 +570,7 @@ __global__ void pair_axpy_kernel(long long count, double dt, const T* t, float* 
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   if constexpr (sizeof(T) == 4) {
-    pair_add(dt, t[k], hi, lo, k);
+    pair_add(float(dt), t[k], hi, lo, k);
   } else {
     const double y = ((double)hi[k] + (double)lo[k]) + dt * (double)t[k];
     const float h = (float)y;
@@ -573,7 +589,7 @@ __global__ void pair_axpy_kernel(long long count, double dt, const T* t, float* 
 //   diff_sync_update_kernel: those nodes' covariant sync
 //     (ecs_Ah_vec_sync_mod.f90:62-125), then their pair update.
 __global__ void diff_update_kernel(FieldGeom g, const float* b, float cuv, const float* L, float ch,
-                                   const float* Lh, double dt, float* hi, float* lo, float* tu,
+                                   const float* Lh, float dt, float* hi, float* lo, float* tu,
                                    float* tv, float* E) {
   Node k;
   if (!node_here(g, k)) return;
@@ -603,7 +619,7 @@ __global__ void diff_update_kernel(FieldGeom g, const float* b, float cuv, const
 }
 
 __global__ void diff_sync_update_kernel(FieldGeom g, Topology tp, const double* qw, const float* E,
-                                        const float* tu, const float* tv, double dt, float* hi,
+                                        const float* tu, const float* tv, float dt, float* hi,
                                         float* lo) {
   const int n = g.n, nb = 4 * n - 4;
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
@@ -655,8 +671,9 @@ cudaError_t laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f,
   if constexpr (sizeof(T) == 4) {
     const int nty = (g.n + LTY - 1) / LTY;
     const dim3 grid((g.n + LTX - 1) / LTX, 6 * nty), block(LTX, LTY);
+    // (hx a)^2 rounded to FP32 once, as the kernel would round it
     lap_tile_kernel<NARROW, NF><<<grid, block, LapTile<NARROW, NF>::bytes, st>>>(
-        g, nty, f, t.clx, t.cly, t.b, mt, hs, out, edge);
+        g, nty, f, t.clx, t.cly, t.b, mt, float(hs * hs), out, edge);
   } else {
     if (!d1x || !d1y) return cudaErrorInvalidValue;
     lap_d1_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(g, f, mt, d1x, d1y);
@@ -747,10 +764,11 @@ cudaError_t launch_diff_update_f32(const FieldGeom& g, const Topology& tp, const
                                    const float* b12, double cuv, const float* L, double ch,
                                    const float* Lh, double dt, float* hi, float* lo, float* tu,
                                    float* tv, float* edge, cudaStream_t st) {
-  diff_update_kernel<<<row_grid(g), row_block(), 0, st>>>(g, b12, float(cuv), L, float(ch), Lh, dt,
-                                                            hi, lo, tu, tv, edge);
+  // dt enters the FP32 increment rounded to FP32 (once, here)
+  diff_update_kernel<<<row_grid(g), row_block(), 0, st>>>(g, b12, float(cuv), L, float(ch), Lh,
+                                                            float(dt), hi, lo, tu, tv, edge);
   const int nb = 6 * (4 * g.n - 4);
-  diff_sync_update_kernel<<<dblk(nb), DTPB, 0, st>>>(g, tp, qw, edge, tu, tv, dt, hi, lo);
+  diff_sync_update_kernel<<<dblk(nb), DTPB, 0, st>>>(g, tp, qw, edge, tu, tv, float(dt), hi, lo);
   return cudaGetLastError();
 }
 

@@ -55,7 +55,7 @@ __device__ __forceinline__ T d_line(int k, int n, FA fa) {
     const int last = c_sbp[ID].last[k];
 #pragma unroll
     for (int m = 0; m < NW; ++m)
-      if (m < last) acc += T(c_sbp[ID].Ql[k * MAXNW + m]) * fa(m);
+      if (m < last) acc += sbp_ql<T>(ID, k, m) * fa(m);
     return acc;
   } else if (k >= n - NE) {
     const int r = n - 1 - k;
@@ -63,7 +63,7 @@ __device__ __forceinline__ T d_line(int k, int n, FA fa) {
     T acc = T(0);
 #pragma unroll
     for (int m = NW - 1; m >= 0; --m)
-      if (m < last) acc += T(-c_sbp[ID].Ql[r * MAXNW + m]) * fa(n - 1 - m);
+      if (m < last) acc += sbp_qr<T>(ID, r, m) * fa(n - 1 - m);
     return acc;
   }
   return d_interior<ORD, T>([&](int o) { return fa(k + o); });

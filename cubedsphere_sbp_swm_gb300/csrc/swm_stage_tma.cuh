@@ -162,7 +162,7 @@ __device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
 #pragma unroll
       for (int i = 0; i < WS; ++i) {
         const int m = j - RMAX + i;            // panel row of slot i
-        const T c = (m >= 0 && m < last) ? T(c_sbp[ID].Ql[j * MAXNW + m]) : T(0);
+        const T c = (m >= 0 && m < last) ? sbp_ql<T>(ID, j, m) : T(0);
         acc += c * w[i];
       }
     } else {
@@ -171,7 +171,7 @@ __device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
 #pragma unroll
       for (int i = 0; i < WS; ++i) {
         const int m = R + RMAX - i;            // slot i holds panel row n-1-m
-        const T c = (m >= 0 && m < last) ? T(-c_sbp[ID].Ql[R * MAXNW + m]) : T(0);
+        const T c = (m >= 0 && m < last) ? sbp_qr<T>(ID, R, m) : T(0);
         acc += c * w[i];
       }
     }
@@ -183,7 +183,7 @@ __device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
         for (int m = 0; m < NW; ++m) {
           const int idx = m - J + RMAX;  // row m
           if (m < c_sbp[ID].last[J] && idx >= 0 && idx < WS)
-            acc += T(c_sbp[ID].Ql[J * MAXNW + m]) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
+            acc += sbp_ql<T>(ID, J, m) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
         }
       }
     }
@@ -195,7 +195,7 @@ __device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
         for (int m = NW - 1; m >= 0; --m) {
           const int idx = R - m + RMAX;  // row n-1-m
           if (m < c_sbp[ID].last[R] && idx >= 0 && idx < WS)
-            acc += T(-c_sbp[ID].Ql[R * MAXNW + m]) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
+            acc += sbp_qr<T>(ID, R, m) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
         }
       }
     }
@@ -407,8 +407,8 @@ __global__ void __launch_bounds__(CONS + 32)
 #pragma unroll
     for (int m = 0; m < NW; ++m) {
       const int mm = left ? m : NW - 1 - m;
-      const double cq = mm < last ? c_sbp[Ord<ORD>::idx].Ql[rr * MAXNW + mm] : 0.0;
-      cx[m] = T(left ? cq : -cq);
+      cx[m] = mm < last ? (left ? sbp_ql<T>(Ord<ORD>::idx, rr, mm) : sbp_qr<T>(Ord<ORD>::idx, rr, mm))
+                        : T(0);
     }
   }
   const T grav = I.grav, ghs = I.ghs, c_in = I.c_in, c_acc = I.c_acc;
