@@ -28,7 +28,11 @@ template <> struct Ord<42> { static constexpr int idx = 1, NE = 4, NW = 6, H = 2
 template <> struct Ord<43> { static constexpr int idx = 2, NE = 4, NW = 6, H = 2, RMAX = 5; };
 template <> struct Ord<63> { static constexpr int idx = 3, NE = 6, NW = 9, H = 3, RMAX = 5; };
 
-constexpr int STAGE_BW = 128;   // threads per CTA = max columns a unit reads
+// Threads per CTA of the FP64 kernel = the most columns a unit reads.  Two
+// warps: the column strips (own columns + 2*RMAX halo) then fill both warps,
+// and every FP64 instruction runs on nearly full warps (GB300's FP64 pipe is
+// the bound; at 128 threads a strip of N=384 left a warp with 6 live lanes).
+constexpr int STAGE_BW = 64;
 enum { RF_KE = 0, RF_U, RF_V, RF_GU, RF_GV, RF_UT, RF_VT, RF_J, RF_N };
 
 // Interior central difference with the antisymmetric coefficients of the
