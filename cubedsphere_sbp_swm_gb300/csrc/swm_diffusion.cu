@@ -188,6 +188,19 @@ __global__ void narrow_closure_kernel(FieldGeom g, const double* m, T* clx, T* c
 // D1y(d1x) + D1x(d1y), the scaling, and the edge values for the sync.
 constexpr int LTX = 32, LTY = 8, LTPB = LTX * LTY;
 
+// 4-byte asynchronous copy global -> shared (no register round trip: every
+// copy of a thread is in flight at once); cp_async_wait_all waits for this
+// thread's copies, a barrier after it for the block's.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 template <int NARROW, int NF>
 struct LapTile {
   using S = NarrowShape<NARROW>;
@@ -272,24 +285,25 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
     const long long rowa = (long long)(ylo + y) * P;
     for (int x = lx; x < rx; x += LTX) {
 #pragma unroll
-      for (int c = 0; c < NF; ++c) Fs[c][y][x] = f[c * g.fs + pb + rowa + xlo + x];
+      for (int c = 0; c < NF; ++c) cp_async4(&Fs[c][y][x], f + c * g.fs + pb + rowa + xlo + x);
     }
     if (lx < tw) {
       const long long a = rowa + i0 + lx;
-      JXs[y][lx] = MJp[a];
-      QXs[y][lx] = MQp[a];
-      BYs[y][lx] = bco[g.fs + pb + a];
+      cp_async4(&JXs[y][lx], MJp + a);
+      cp_async4(&QXs[y][lx], MQp + a);
+      cp_async4(&BYs[y][lx], bco + g.fs + pb + a);
     }
   }
   if (ly < th) {
     const long long rowa = (long long)(j0 + ly) * P;
     for (int x = lx; x < rx; x += LTX) {
       const long long a = rowa + xlo + x;
-      JYs[ly][x] = MJp[a];
-      QYs[ly][x] = MQp[a];
-      BXs[ly][x] = bco[pb + a];
+      cp_async4(&JYs[ly][x], MJp + a);
+      cp_async4(&QYs[ly][x], MQp + a);
+      cp_async4(&BXs[ly][x], bco + pb + a);
     }
   }
+  cp_async_wait_all();
   __syncthreads();
 
   // d1x on the tile's columns x the region's rows, d1y on the region's
@@ -372,6 +386,8 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
   }
   const T J = JXs[yr][lx];
   const T pen = c_scale32.penalty[S::ni];
+  // one reciprocal of (hx a)^2 J for the NF divisions of the node
+  const T inv = T(1) / (hs2 * J);
 #pragma unroll
   for (int c = 0; c < NF; ++c) {
     // the closure rows read cols taps, the interior w (same order)
@@ -405,8 +421,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
                        : d_line<NARROW, T>(i, n, fdy);
     T v = d2x + d2y;
     v = v + d2xy + d2yx;
-    v = v / hs2;
-    v = v / J;
+    v = v * inv;
     out[c * g.fs + pb + (long long)j * P + i] = v;
     // panel-boundary values also go to value slot c of the edge buffer
     auto put = [&](int side, int q) { E[((long long)(p * 4 + side) * 4 + c) * n + q] = v; };
