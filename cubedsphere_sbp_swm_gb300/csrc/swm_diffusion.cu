@@ -339,6 +339,38 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
 
   const int i = i0 + lx, j = j0 + ly;
   const int yr = j - ylo, xr = i - xlo;
+  if (xin && yin) {
+    // A tile with no closure node and no panel side (most tiles): the same
+    // terms in the same order as below, with every stencil offset known at
+    // compile time and no per-node tests.
+    T ax[S::w], ay[S::w];
+#pragma unroll
+    for (int c = 0; c < S::w; ++c) {
+      T accx = T(0), accy = T(0);
+#pragma unroll
+      for (int q = 0; q < S::w; ++q) {
+        accx += c_in32.v[S::ni][c][q] * BXs[ly][xr - S::hw + q];
+        accy += c_in32.v[S::ni][c][q] * BYs[yr - S::hw + q][lx];
+      }
+      ax[c] = accx;
+      ay[c] = accy;
+    }
+    const T inv = T(1) / (hs2 * JXs[yr][lx]);
+#pragma unroll
+    for (int c = 0; c < NF; ++c) {
+      T sx = T(0), sy = T(0);
+#pragma unroll
+      for (int t = 0; t < S::w; ++t) sx += ax[t] * Fs[c][yr][xr - S::hw + t];
+#pragma unroll
+      for (int t = 0; t < S::w; ++t) sy += ay[t] * Fs[c][yr - S::hw + t][xr];
+      const T d2yx = d_interior<NARROW, T>([&](int o) { return DXs[c][yr + o][lx]; });
+      const T d2xy = d_interior<NARROW, T>([&](int o) { return DYs[c][ly][xr + o]; });
+      T v = sx + sy;
+      v = v + d2xy + d2yx;
+      out[c * g.fs + pb + (long long)j * P + i] = v * inv;
+    }
+    return;
+  }
   const bool clxn = i < S::rows || i >= n - S::rows;
   const bool clyn = j < S::rows || j >= n - S::rows;
   // stencil of this node in x and y: coefficients and tap offsets in the
