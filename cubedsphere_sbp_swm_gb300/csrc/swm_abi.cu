@@ -1351,8 +1351,7 @@ int enqueue_biharmonic(swm_ctx* ctx, const T* h, const T* u, const T* v) {
   const long long fs = g.fs;
   T* F = dwork<T>(ctx, 0);
   T* L = dwork<T>(ctx, 4);
-  CK(cudaMemcpyAsync(F, h, sizeof(T) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
-  CK(launch_to_cart<T>(g, (const T*)ctx->b12, u, v, F + fs, ctx->st), "to cart");
+  CK(launch_to_cart<T>(g, (const T*)ctx->b12, h, u, v, F, F + fs, ctx->st), "to cart");
   if (ctx->diff_uv == ctx->diff_h) {
     if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 4, F, L)) return rc;
     if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 4, L, F)) return rc;

@@ -571,11 +571,13 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
 }
 
 // Cartesian components of the covariant (u, v): b1*u + b2*v
-// (vec_math_mod.f90:107-126).
+// (vec_math_mod.f90:107-126), and a copy of h into h_out (nullable).
 template <class T>
-__global__ void to_cart_kernel(FieldGeom g, const T* b, const T* u, const T* v, T* cart) {
+__global__ void to_cart_kernel(FieldGeom g, const T* b, const T* h, const T* u, const T* v, T* h_out,
+                               T* cart) {
   Node k;
   if (!node_here(g, k)) return;
+  if (h_out) h_out[k.idx] = h[k.idx];
   const T uu = u[k.idx], vv = v[k.idx];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -786,9 +788,9 @@ cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowT
 }
 
 template <class T>
-cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* u, const T* v, T* cart,
-                           cudaStream_t st) {
-  to_cart_kernel<T><<<row_grid(g), row_block(), 0, st>>>(g, b12, u, v, cart);
+cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* h, const T* u, const T* v,
+                           T* h_out, T* cart, cudaStream_t st) {
+  to_cart_kernel<T><<<row_grid(g), row_block(), 0, st>>>(g, b12, h, u, v, h_out, cart);
   return cudaGetLastError();
 }
 
@@ -830,8 +832,8 @@ cudaError_t launch_f64_to_f32(long long count, const double* s, float* d, cudaSt
   template cudaError_t launch_laplace<T>(const FieldGeom&, const Topology&, const NarrowTables<T>&,\
                                          int, const T*, const T*, double, T*, T*, T*, T*,        \
                                          cudaStream_t);                                          \
-  template cudaError_t launch_to_cart<T>(const FieldGeom&, const T*, const T*, const T*, T*,     \
-                                         cudaStream_t);                                          \
+  template cudaError_t launch_to_cart<T>(const FieldGeom&, const T*, const T*, const T*, const T*,\
+                                         T*, T*, cudaStream_t);                                  \
   template cudaError_t launch_diff_tendency<T>(const FieldGeom&, const T*, double, const T*, T*, \
                                                T*, double, const T*, T*, cudaStream_t);          \
   template cudaError_t launch_pair_axpy<T>(long long, double, const T*, float*, float*,          \

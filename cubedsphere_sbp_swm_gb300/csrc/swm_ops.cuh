@@ -178,9 +178,10 @@ cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowT
                            const T* f, const T* mt, double hs, T* d1x, T* d1y, T* out, T* edge,
                            cudaStream_t st);
 // cart (3 fields) = b1*u + b2*v; b12 from launch_basis
+// cart = b1*u + b2*v (3 fields) and, when h_out is given, h_out = h
 template <class T>
-cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* u, const T* v, T* cart,
-                           cudaStream_t st);
+cudaError_t launch_to_cart(const FieldGeom& g, const T* b12, const T* h, const T* u, const T* v,
+                           T* h_out, T* cart, cudaStream_t st);
 // tu, tv = projections of cuv*L (3 Cartesian fields) on b1, b2; th = ch*Lh
 template <class T>
 cudaError_t launch_diff_tendency(const FieldGeom& g, const T* b12, double cuv, const T* L, T* tu,

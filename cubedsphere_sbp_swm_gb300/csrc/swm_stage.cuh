@@ -33,7 +33,11 @@ template <> struct Ord<63> { static constexpr int idx = 3, NE = 6, NW = 9, H = 3
 // and every FP64 instruction runs on nearly full warps (GB300's FP64 pipe is
 // the bound; at 128 threads a strip of N=384 left a warp with 6 live lanes).
 constexpr int STAGE_BW = 64;
-enum { RF_KE = 0, RF_U, RF_V, RF_GU, RF_GV, RF_UT, RF_VT, RF_J, RF_N };
+// Derived fields of the FP64 kernel's row rings: the y ring holds what the
+// y stencils read along a column (2*RMAX+1 rows), the x ring what is read
+// only on the row being finished (RMAX+1 rows: written RMAX rows ahead).
+enum { RY_KE = 0, RY_U, RY_GV, RY_N };
+enum { RX_V = 0, RX_GU, RX_UT, RX_VT, RX_J, RX_N };
 
 // Interior central difference with the antisymmetric coefficients of the
 // order's interior stencil; fm(o) returns the value at offset o.
@@ -185,16 +189,19 @@ __device__ __forceinline__ void node_tendency(T gx, T gy, T zeta, T dv, T f, T J
 
 // ---------------------------------------------------------------------------
 // Fused stage kernel.  One CTA = one work unit (panel strip x row segment);
-// thread t owns column cl0+t.  Rows stream through a shared-memory ring of
-// 2*RMAX+1 rows holding the derived fields, so every input node is read from
-// global memory once per unit.
+// thread t owns column cl0+t.  Rows stream through shared-memory rings of
+// the derived fields (KE, u and J h vt for 2*RMAX+1 rows; v, J h ut, ut, vt
+// and J for RMAX+1 rows), so every input node is read from global memory
+// once per unit.
 // ---------------------------------------------------------------------------
 template <class T, int ORD>
 __global__ void __launch_bounds__(STAGE_BW)
     stage_kernel(InstDev<T> one, const InstDev<T>* many, const WorkUnit* units, int mode) {
-  constexpr int RMAX = Ord<ORD>::RMAX, RB = 2 * RMAX + 1, NE = Ord<ORD>::NE;
+  constexpr int RMAX = Ord<ORD>::RMAX, RB = 2 * RMAX + 1, RX1 = RMAX + 1, NE = Ord<ORD>::NE;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T(*ring)[RF_N][STAGE_BW] = reinterpret_cast<T(*)[RF_N][STAGE_BW]>(smem_raw);
+  T(*yring)[RY_N][STAGE_BW] = reinterpret_cast<T(*)[RY_N][STAGE_BW]>(smem_raw);
+  T(*xring)[RX_N][STAGE_BW] =
+      reinterpret_cast<T(*)[RX_N][STAGE_BW]>(smem_raw + sizeof(T) * RB * RY_N * STAGE_BW);
 
   const WorkUnit wu = units[blockIdx.x];
   const InstDev<T>& I = many ? many[wu.inst] : one;
@@ -218,15 +225,15 @@ __global__ void __launch_bounds__(STAGE_BW)
     T ke = (u * ut + v * vt) / T(2.0);
     ke = ke + grav * h;
     if (I.hs) ke = ke + grav * I.hs[idx];
-    const int s = r % RB;
-    ring[s][RF_KE][t] = ke;
-    ring[s][RF_U][t] = u;
-    ring[s][RF_V][t] = v;
-    ring[s][RF_GU][t] = J * (h * ut);
-    ring[s][RF_GV][t] = J * (h * vt);
-    ring[s][RF_UT][t] = ut;
-    ring[s][RF_VT][t] = vt;
-    ring[s][RF_J][t] = J;
+    const int s = r % RB, sx = r % RX1;
+    yring[s][RY_KE][t] = ke;
+    yring[s][RY_U][t] = u;
+    yring[s][RY_GV][t] = J * (h * vt);
+    xring[sx][RX_V][t] = v;
+    xring[sx][RX_GU][t] = J * (h * ut);
+    xring[sx][RX_UT][t] = ut;
+    xring[sx][RX_VT][t] = vt;
+    xring[sx][RX_J][t] = J;
   };
 
   int loaded = wu.rl0;
@@ -242,18 +249,17 @@ __global__ void __launch_bounds__(STAGE_BW)
     }
     __syncthreads();
     if (col < wu.i0 || col >= wu.i1) continue;
-    const int sj = j % RB;
+    const int sj = j % RB, sxj = j % RX1;
     // x derivatives (along the row, neighbours are other threads' columns)
-    auto xa = [&](int f) {
-      return d_line<ORD, T>(col, n, [&](int m) { return ring[sj][f][m - wu.cl0]; });
-    };
+    const T dxke = d_line<ORD, T>(col, n, [&](int m) { return yring[sj][RY_KE][m - wu.cl0]; });
+    const T dxv = d_line<ORD, T>(col, n, [&](int m) { return xring[sxj][RX_V][m - wu.cl0]; });
+    const T dxgu = d_line<ORD, T>(col, n, [&](int m) { return xring[sxj][RX_GU][m - wu.cl0]; });
+    // y derivatives (along this thread's column)
     auto ya = [&](int f) {
-      return d_line<ORD, T>(j, n, [&](int m) { return ring[m % RB][f][t]; });
+      return d_line<ORD, T>(j, n, [&](int m) { return yring[m % RB][f][t]; });
     };
-    const T dxke = xa(RF_KE), dyke = ya(RF_KE);
-    const T dxv = xa(RF_V), dyu = ya(RF_U);
-    const T dxgu = xa(RF_GU), dygv = ya(RF_GV);
-    const T J = ring[sj][RF_J][t];
+    const T dyke = ya(RY_KE), dyu = ya(RY_U), dygv = ya(RY_GV);
+    const T J = xring[sxj][RX_J][t];
     T rJ;
     if constexpr (sizeof(T) == 8) {
       rJ = I.metric[MRJ * fs + pbase + (long long)j * P + col];
@@ -284,7 +290,7 @@ __global__ void __launch_bounds__(STAGE_BW)
     }
     const T f = I.metric[MF * fs + idx];
     T kh, ku, kv;
-    node_tendency<T>(gx, gy, zeta, dv, f, J, ring[sj][RF_UT][t], ring[sj][RF_VT][t], kh, ku, kv);
+    node_tendency<T>(gx, gy, zeta, dv, f, J, xring[sxj][RX_UT][t], xring[sxj][RX_VT][t], kh, ku, kv);
     stage_epilogue<T>(I, mode, idx, kh, ku, kv);
   }
   (void)NE;
@@ -292,7 +298,7 @@ __global__ void __launch_bounds__(STAGE_BW)
 
 template <class T, int ORD>
 constexpr size_t stage_smem_bytes() {
-  return sizeof(T) * (2 * Ord<ORD>::RMAX + 1) * RF_N * STAGE_BW;
+  return sizeof(T) * ((2 * Ord<ORD>::RMAX + 1) * RY_N + (Ord<ORD>::RMAX + 1) * RX_N) * STAGE_BW;
 }
 
 template <class T, int ORD>
