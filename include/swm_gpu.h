@@ -230,9 +230,9 @@ int swm_quadrature_mass(swm_ctx* ctx, const swm_field* f, double* out);
 
 /* ---------------------------------------------------------------------- */
 /* Kernel timing for measurement (no reference counterpart): when enabled,  */
-/* every fused-stage kernel launch is bracketed by CUDA events on the       */
-/* context stream; swm_timing_read returns the summed stage-kernel time     */
-/* [ms] and the number of launches since the last reset.                   */
+/* every fused-stage and cube-edge kernel launch is bracketed by CUDA       */
+/* events on the context stream; swm_timing_read returns the summed time    */
+/* [ms] and the number of launches of each kind since the last read.        */
 /* ---------------------------------------------------------------------- */
 int swm_timing_enable(swm_ctx* ctx, int on);
 int swm_timing_read(swm_ctx* ctx, double* stage_ms, long* stage_launches,
