@@ -37,7 +37,7 @@ constexpr int STAGE_BW = 64;
 // y stencils read along a column (2*RMAX+1 rows), the x ring what is read
 // only on the row being finished (RMAX+1 rows: written RMAX rows ahead).
 enum { RY_KE = 0, RY_U, RY_GV, RY_N };
-enum { RX_V = 0, RX_GU, RX_UT, RX_VT, RX_J, RX_N };
+enum { RX_V = 0, RX_GU, RX_JUT, RX_JVT, RX_N };
 
 // Interior central difference with the antisymmetric coefficients of the
 // order's interior stencil; fm(o) returns the value at offset o.
@@ -186,6 +186,49 @@ __device__ __forceinline__ void node_tendency(T gx, T gy, T zeta, T dv, T f, T J
   kv = -gy - fz * (J * ut);
   kh = -dv;
 }
+// The same with J*ut and J*vt formed beforehand.
+template <class T>
+__device__ __forceinline__ void node_tendency_j(T gx, T gy, T zeta, T dv, T f, T jut, T jvt,
+                                                T& kh, T& ku, T& kv) {
+  const T fz = f + zeta;
+  ku = -gx + fz * jvt;
+  kv = -gy - fz * jut;
+  kh = -dv;
+}
+
+// SBP derivative times s: interior rows with the interior coefficients
+// pre-multiplied by s (sc[o-1] for offset o), closure rows as d_line * s.
+template <int ORD, class T>
+struct ScaledInterior {
+  T c[Ord<ORD>::H];
+};
+template <int ORD, class T>
+__device__ __forceinline__ ScaledInterior<ORD, T> scaled_interior(T s) {
+  ScaledInterior<ORD, T> r;
+  if constexpr (Ord<ORD>::H == 1) {
+    r.c[0] = T(0.5) * s;
+  } else if constexpr (Ord<ORD>::H == 2) {
+    r.c[0] = T(2.0 / 3.0) * s;
+    r.c[1] = T(-1.0 / 12.0) * s;
+  } else {
+    r.c[0] = T(3.0 / 4.0) * s;
+    r.c[1] = T(-3.0 / 20.0) * s;
+    r.c[2] = T(1.0 / 60.0) * s;
+  }
+  return r;
+}
+template <int ORD, class T, class FA>
+__device__ __forceinline__ T d_line_scaled(int k, int n, FA fa, const ScaledInterior<ORD, T>& sc,
+                                           T s) {
+  constexpr int NE = Ord<ORD>::NE, H = Ord<ORD>::H;
+  if (k >= NE && k < n - NE) {
+    T acc = sc.c[0] * (fa(k + 1) - fa(k - 1));
+#pragma unroll
+    for (int o = 2; o <= H; ++o) acc += sc.c[o - 1] * (fa(k + o) - fa(k - o));
+    return acc;
+  }
+  return d_line<ORD, T>(k, n, fa) * s;
+}
 
 // ---------------------------------------------------------------------------
 // Fused stage kernel.  One CTA = one work unit (panel strip x row segment);
@@ -212,6 +255,9 @@ __global__ void __launch_bounds__(STAGE_BW)
   const int col = wu.cl0 + t;
   const bool load_col = col < wu.cl1;
   const T grav = I.grav;
+  static_assert(sizeof(T) == 8, "the FP32 form runs the TMA kernel");
+  const T ghs = I.ghs;
+  const ScaledInterior<ORD, T> ghs_c = scaled_interior<ORD, T>(ghs);
 
   auto load_row = [&](int r) {
     if (!load_col) return;
@@ -225,15 +271,16 @@ __global__ void __launch_bounds__(STAGE_BW)
     T ke = (u * ut + v * vt) / T(2.0);
     ke = ke + grav * h;
     if (I.hs) ke = ke + grav * I.hs[idx];
+    // J ut and J vt serve the mass flux (times h) and the Coriolis term
+    const T jut = J * ut, jvt = J * vt;
     const int s = r % RB, sx = r % RX1;
     yring[s][RY_KE][t] = ke;
     yring[s][RY_U][t] = u;
-    yring[s][RY_GV][t] = J * (h * vt);
+    yring[s][RY_GV][t] = h * jvt;
     xring[sx][RX_V][t] = v;
-    xring[sx][RX_GU][t] = J * (h * ut);
-    xring[sx][RX_UT][t] = ut;
-    xring[sx][RX_VT][t] = vt;
-    xring[sx][RX_J][t] = J;
+    xring[sx][RX_GU][t] = h * jut;
+    xring[sx][RX_JUT][t] = jut;
+    xring[sx][RX_JVT][t] = jvt;
   };
 
   int loaded = wu.rl0;
@@ -250,23 +297,20 @@ __global__ void __launch_bounds__(STAGE_BW)
     __syncthreads();
     if (col < wu.i0 || col >= wu.i1) continue;
     const int sj = j % RB, sxj = j % RX1;
-    // x derivatives (along the row, neighbours are other threads' columns)
-    const T dxke = d_line<ORD, T>(col, n, [&](int m) { return yring[sj][RY_KE][m - wu.cl0]; });
+    // x derivatives (along the row, neighbours are other threads' columns);
+    // the KE gradient's 1/(hx a) rides in its interior coefficients
+    const T gx = d_line_scaled<ORD, T>(col, n, [&](int m) { return yring[sj][RY_KE][m - wu.cl0]; },
+                                       ghs_c, ghs);
     const T dxv = d_line<ORD, T>(col, n, [&](int m) { return xring[sxj][RX_V][m - wu.cl0]; });
     const T dxgu = d_line<ORD, T>(col, n, [&](int m) { return xring[sxj][RX_GU][m - wu.cl0]; });
     // y derivatives (along this thread's column)
     auto ya = [&](int f) {
       return d_line<ORD, T>(j, n, [&](int m) { return yring[m % RB][f][t]; });
     };
-    const T dyke = ya(RY_KE), dyu = ya(RY_U), dygv = ya(RY_GV);
-    const T J = xring[sxj][RX_J][t];
-    T rJ;
-    if constexpr (sizeof(T) == 8) {
-      rJ = I.metric[MRJ * fs + pbase + (long long)j * P + col];
-    } else {
-      rJ = I.ghs / J;
-    }
-    const T gx = dxke * I.ghs, gy = dyke * I.ghs;
+    const T gy = d_line_scaled<ORD, T>(j, n, [&](int m) { return yring[m % RB][RY_KE][t]; }, ghs_c,
+                                       ghs);
+    const T dyu = ya(RY_U), dygv = ya(RY_GV);
+    const T rJ = I.metric[MRJ * fs + pbase + (long long)j * P + col];
     const T zeta = (dxv - dyu) * rJ;
     const T dv = (dxgu + dygv) * rJ;
     const long long idx = pbase + (long long)j * P + col;
@@ -290,7 +334,7 @@ __global__ void __launch_bounds__(STAGE_BW)
     }
     const T f = I.metric[MF * fs + idx];
     T kh, ku, kv;
-    node_tendency<T>(gx, gy, zeta, dv, f, J, xring[sxj][RX_UT][t], xring[sxj][RX_VT][t], kh, ku, kv);
+    node_tendency_j<T>(gx, gy, zeta, dv, f, xring[sxj][RX_JUT][t], xring[sxj][RX_JVT][t], kh, ku, kv);
     stage_epilogue<T>(I, mode, idx, kh, ku, kv);
   }
   (void)NE;

@@ -426,6 +426,9 @@ __global__ void __launch_bounds__(CONS + 32)
   T yke[WS], yu[WS], ygv[WS];
 #pragma unroll
   for (int i = 0; i < WS; ++i) { yke[i] = T(0); yu[i] = T(0); ygv[i] = T(0); }
+  // x-ring slots of the row being derived (r) and of the row being finished
+  // (j = r - RMAX), counted from the unit's first row
+  int slot_r = 0, slot_j = RBX - RMAX;
 
   for (int c = 0; c < nch; ++c, ++gc) {
     const int s = gc % NST;
@@ -456,7 +459,7 @@ __global__ void __launch_bounds__(CONS + 32)
         ke = ke + grav * h;
         if (hasHs) ke = ke + grav * sx[e_hs + (0 * RPS + q) * bw];
         gv = J * (h * vt);
-        T* xw = xring + (r % RBX) * XS + t;
+        T* xw = xring + slot_r * XS + t;
         xw[X_KE * CONS] = ke;
         xw[X_V * CONS] = v;
         xw[X_GU * CONS] = J * (h * ut);
@@ -469,8 +472,11 @@ __global__ void __launch_bounds__(CONS + 32)
       for (int i = 0; i < WS - 1; ++i) { yke[i] = yke[i + 1]; yu[i] = yu[i + 1]; ygv[i] = ygv[i + 1]; }
       yke[WS - 1] = ke; yu[WS - 1] = u; ygv[WS - 1] = gv;
       consumers_sync<CONS>();
+      const int sj = slot_j;
+      slot_r = slot_r + 1 == RBX ? 0 : slot_r + 1;
+      slot_j = slot_j + 1 == RBX ? 0 : slot_j + 1;
       if (*abort_flag || !own || j < j0u || j >= j1u) continue;
-      const T* xr = xring + (j % RBX) * XS + t;      // row j, this thread's column
+      const T* xr = xring + sj * XS + t;      // row j, this thread's column
       T dxke, dxv, dxgu;
       if (xint) {
         dxke = d_interior<ORD, T>([&](int o) { return xr[X_KE * CONS + o]; });
