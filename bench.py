@@ -531,25 +531,48 @@ def single_instance_leg(w, local, steps, warmup, stage_shape=None, state=None, q
         return op, s, ms, kt
 
     def e2e(op, s, nsteps):
-        """Steps/s through the C-ABI with host buffers: every step uploads the
-        state from page-locked FP64 host arrays, steps, and downloads it."""
-        pin = [torch.empty((6, N + 1, N + 1), dtype=torch.float64, pin_memory=True) for _ in range(6)]
+        """Steps/s through the C-ABI with host buffers: every step moves the
+        state in from page-locked FP64 host arrays, steps it, and moves it
+        back out to page-locked FP64 host arrays.  Returns (pipelined,
+        serial):
+          pipelined: two states take turns; swm_state_upload_async and
+            swm_state_download_async move the arrays with the copy engines
+            (one stream per direction), so one step's download and the next
+            step's upload run under the steps; the clock stops after the
+            last download has landed (swm_ctx_synchronize);
+          serial: swm_state_upload, swm_rk4_step, swm_state_download, one
+            step at a time, each call synchronous."""
+        pin = [torch.empty((6, N + 1, N + 1), dtype=torch.float64, pin_memory=True) for _ in range(9)]
         for t_, a_ in zip(pin[:3], (h, u, v)):
             t_.numpy()[...] = a_
         hin = [t_.numpy() for t_ in pin[:3]]
-        hout = [t_.numpy() for t_ in pin[3:]]
+        outs = [tuple(t_.numpy() for t_ in pin[3:6]), tuple(t_.numpy() for t_ in pin[6:9])]
         ts = swm.RK4()
-        for _ in range(2):
-            s.upload_async(*hin)
-            ts.step(s, op, DT, 1)
-            s.download(out=hout)
+        states = [s, op.create_stvec()]
+
+        def pipelined(n):
+            for k in range(n):
+                st = states[k % 2]
+                st.upload_async(*hin)
+                ts.step(st, op, DT, 1)
+                st.download_async(outs[k % 2])
+            op.synchronize()
+
+        def serial(n):
+            for _ in range(n):
+                s.upload(*hin)
+                ts.step(s, op, DT, 1)
+                s.download(out=outs[0])
+
+        pipelined(4)
         t0 = time.perf_counter()
-        for _ in range(nsteps):
-            s.upload_async(*hin)
-            ts.step(s, op, DT, 1)
-            s.download(out=hout)
+        pipelined(nsteps)
         val, _ = replicas.job_rate(nsteps, time.perf_counter() - t0, dev)
-        return val
+        serial(2)
+        t0 = time.perf_counter()
+        serial(nsteps)
+        val_serial, _ = replicas.job_rate(nsteps, time.perf_counter() - t0, dev)
+        return val, val_serial
 
     uuid = None
     try:
@@ -564,7 +587,7 @@ def single_instance_leg(w, local, steps, warmup, stage_shape=None, state=None, q
         return {}, ms32, clocks, info
     finite = bool(all(np.isfinite(a).all() for a in s32.download()))
     nsteps_e2e = max(10, steps // 2)
-    e2e32 = e2e(op32, s32, nsteps_e2e)
+    e2e32, e2e32_serial = e2e(op32, s32, nsteps_e2e)
     del s32, op32
 
     # dominant kernel timing (stage kernel), events around every launch
@@ -577,7 +600,7 @@ def single_instance_leg(w, local, steps, warmup, stage_shape=None, state=None, q
 
     op64, s64, ms64, _ = time_steps("fp64", max(10, steps // 2), warmup)
     fp64_ms = sum(ms64) / len(ms64)
-    e2e64 = e2e(op64, s64, nsteps_e2e)
+    e2e64, e2e64_serial = e2e(op64, s64, nsteps_e2e)
     del op64, s64
     _, _, _, kt64 = time_steps("fp64", 10, 2, kernel_timing=True)
     fp32_ms = sum(ms32) / len(ms32)
@@ -587,12 +610,18 @@ def single_instance_leg(w, local, steps, warmup, stage_shape=None, state=None, q
                  "stage_shape": {k: tuned[k] for k in ("width", "seg_rows", "grid", "box")}},
         "fp64_plain": {"steps_per_s": round(1e3 / fp64_ms, 3), "ms_per_step": round(fp64_ms, 5),
                        "stage_kernel_avg_us": round(kt64[0] / kt64[1] * 1e3, 3),
-                       "e2e_steps_per_s": round(e2e64, 3)},
+                       "e2e_steps_per_s": round(e2e64, 3),
+                       "e2e_serial_steps_per_s": round(e2e64_serial, 3)},
         "fp32_over_fp64": round(fp64_ms / fp32_ms, 3),
         "e2e": {"value": round(e2e32, 3), "unit": "steps/s",
                 "h2d_bytes_per_step": 3 * npts * 8, "d2h_bytes_per_step": 3 * npts * 8,
-                "path": "swm_state_upload (pinned FP64 host arrays, read in place over the host link) "
-                        "+ swm_rk4_step + swm_state_download (written in place)"},
+                "path": "every step: swm_state_upload_async (pinned FP64 host arrays, copy engine, "
+                        "upload stream) + swm_rk4_step + swm_state_download_async (copy engine, "
+                        "download stream) on two states taking turns, so transfers run under the "
+                        "steps; clock stopped after the last download landed (swm_ctx_synchronize)",
+                "serial_value": round(e2e32_serial, 3),
+                "serial_path": "swm_state_upload (pinned arrays read in place over the host link) "
+                               "+ swm_rk4_step + swm_state_download, one synchronous step at a time"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": _profile_traffic("n%d_d%d" % (N, ORDER)),
@@ -689,7 +718,8 @@ def run_gpu_arm(args):
                            "stage_kernel_avg_us": head["fp64_plain"]["stage_kernel_avg_us"],
                            "e2e": {"value": head["fp64_plain"]["e2e_steps_per_s"], "unit": "steps/s",
                                    "h2d_bytes_per_step": head["e2e"]["h2d_bytes_per_step"],
-                                   "d2h_bytes_per_step": head["e2e"]["d2h_bytes_per_step"]}},
+                                   "d2h_bytes_per_step": head["e2e"]["d2h_bytes_per_step"],
+                                   "serial_value": head["fp64_plain"]["e2e_serial_steps_per_s"]}},
             "fp32_over_fp64": head["fp32_over_fp64"],
             "clocks": clocks,
             "gpu_launches": KERNELS_PER_STEP * args.steps,

@@ -82,6 +82,14 @@ def _host(a, shape) -> np.ndarray:
     return a
 
 
+def _check_c_f64(a, shape):
+    """An array an asynchronous transfer reads or writes after the call
+    returns: no temporary copy may stand in for it."""
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+            and a.shape == shape):
+        raise ValueError(f"asynchronous transfers need C-contiguous float64 arrays of shape {shape}")
+
+
 class OperatorSWM:
     """operator_swm_t on one GPU: domain geometry, the vector-invariant RHS,
     its cube-edge syncs, the fused RK4 driver and FP64 diagnostics."""
@@ -277,16 +285,31 @@ class StvecSWM:
         self.op.synchronize()
 
     def upload_async(self, h, u, v):
-        """Upload from caller-owned (ideally pinned) C-contiguous float64 arrays
-        without synchronising; the arrays must stay alive until the stream
-        reaches the copy."""
-        self.op._check(self.op._L.swm_state_upload(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
+        """Upload from caller-owned C-contiguous float64 arrays
+        (swm_state_upload_async): the copy engine moves them through a
+        device staging buffer on the context's upload stream and the state
+        takes their values for every later call; the arrays must stay
+        unchanged until OperatorSWM.synchronize().  Page-locked arrays let
+        the copy overlap the context's kernels."""
+        for a in (h, u, v):
+            _check_c_f64(a, self.op.shape)
+        self.op._check(self.op._L.swm_state_upload_async(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
 
     def download(self, out=None):
         sh = self.op.shape
         if out is None:
             out = tuple(np.empty(sh) for _ in range(3))
         self.op._check(self.op._L.swm_state_download(self.op._h, self._h, *(_ptr(a) for a in out)))
+        return out
+
+    def download_async(self, out):
+        """Download into caller-owned C-contiguous float64 arrays
+        (swm_state_download_async): the state as the calls queued before
+        leave it, moved by the copy engine on the context's download stream;
+        `out` holds it once OperatorSWM.synchronize() returns."""
+        for a in out:
+            _check_c_f64(a, self.op.shape)
+        self.op._check(self.op._L.swm_state_download_async(self.op._h, self._h, *(_ptr(a) for a in out)))
         return out
 
     def save(self, path: str, time: float = 0.0):

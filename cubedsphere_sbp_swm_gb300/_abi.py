@@ -29,7 +29,8 @@ EXPORTS = (
     "swm_ctx_create", "swm_ctx_create_named", "swm_ctx_destroy", "swm_last_error",
     "swm_ctx_synchronize", "swm_ctx_stream", "swm_ctx_npts", "swm_set_orography",
     "swm_state_create", "swm_state_create_similar", "swm_state_free", "swm_state_upload",
-    "swm_state_download", "swm_assign_s1", "swm_assign_s1v1", "swm_assign_s1v1s2v2",
+    "swm_state_download", "swm_state_upload_async", "swm_state_download_async", "swm_assign_s1",
+    "swm_assign_s1v1", "swm_assign_s1v1s2v2",
     "swm_update_s1v1", "swm_update_s1v1s2v2", "swm_dot", "swm_norm2", "swm_apply",
     "swm_apply_unfused", "swm_rk4_step", "swm_diagnostics", "swm_field_create",
     "swm_field_free", "swm_field_upload", "swm_field_download", "swm_op_co2contra",
@@ -111,6 +112,8 @@ def load(build_if_missing: bool = True):
     sig("swm_state_free", None, VP)
     sig("swm_state_upload", I, VP, VP, _D, _D, _D)
     sig("swm_state_download", I, VP, VP, _D, _D, _D)
+    sig("swm_state_upload_async", I, VP, VP, _D, _D, _D)
+    sig("swm_state_download_async", I, VP, VP, _D, _D, _D)
     sig("swm_assign_s1", I, VP, VP, D)
     sig("swm_assign_s1v1", I, VP, VP, D, VP)
     sig("swm_assign_s1v1s2v2", I, VP, VP, D, VP, D, VP)

@@ -228,6 +228,16 @@ struct swm_ctx {
   void* ntab[2][5] = {};    // cx, cy, clx, cly, b (context precision)
   void* b12 = nullptr;
   void* dw = nullptr;
+  // Asynchronous state transfers (swm_state_upload_async / _download_async),
+  // allocated on first use: the copy engines move packed FP64 states
+  // between the caller's host arrays and device staging buffers on one
+  // stream per direction ([0] host to device, [1] device to host), two
+  // buffers per direction; the context stream unpacks from / packs into
+  // them.  ready[d][k]: buffer k filled; done[d][k]: its consumer finished.
+  cudaStream_t xst[2] = {nullptr, nullptr};
+  double* xbuf[2][2] = {};
+  cudaEvent_t xready[2][2] = {}, xdone[2][2] = {};
+  int xnext[2] = {0, 0};
   cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
   const void* ad_key[2] = {nullptr, nullptr};
   double ad_dt = 0.0;
@@ -786,6 +796,14 @@ void free_ctx(swm_ctx* c) {
   if (c->dw) cudaFree(c->dw);
   if (c->hres) cudaFreeHost(c->hres);
   if (c->herr) cudaFreeHost(c->herr);
+  for (int d = 0; d < 2; ++d) {
+    if (c->xst[d]) { cudaStreamSynchronize(c->xst[d]); cudaStreamDestroy(c->xst[d]); }
+    for (int k = 0; k < 2; ++k) {
+      if (c->xbuf[d][k]) cudaFree(c->xbuf[d][k]);
+      if (c->xready[d][k]) cudaEventDestroy(c->xready[d][k]);
+      if (c->xdone[d][k]) cudaEventDestroy(c->xdone[d][k]);
+    }
+  }
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -965,6 +983,9 @@ void swm_ctx_destroy(swm_ctx* ctx) {
 
 int swm_ctx_synchronize(swm_ctx* ctx) {
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
+  USE_DEVICE(ctx);
+  for (int d = 0; d < 2; ++d)
+    if (ctx->xst[d]) CK(cudaStreamSynchronize(ctx->xst[d]), "sync transfers");
   if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   return SWM_OK;
 }
@@ -1057,6 +1078,84 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
   double* dst[3] = {h, u, v};
   if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
   if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
+  return SWM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Streams, staging buffers and events of the asynchronous transfers of
+// direction d (0: upload, 1: download), created on first use.  The events
+// start recorded, so the first waits on them pass.
+int transfer_ready(swm_ctx* ctx, int d) {
+  if (ctx->xst[d]) return SWM_OK;
+  const size_t bytes = sizeof(double) * 3 * 6 * (size_t)ctx->n * ctx->n;
+  for (int k = 0; k < 2; ++k) {
+    CK(cudaMalloc(&ctx->xbuf[d][k], bytes), "alloc transfer staging");
+    CK(cudaEventCreateWithFlags(&ctx->xready[d][k], cudaEventDisableTiming), "event");
+    CK(cudaEventCreateWithFlags(&ctx->xdone[d][k], cudaEventDisableTiming), "event");
+    CK(cudaEventRecord(ctx->xready[d][k], ctx->st), "event record");
+    CK(cudaEventRecord(ctx->xdone[d][k], ctx->st), "event record");
+  }
+  CK(cudaStreamCreateWithFlags(&ctx->xst[d], cudaStreamNonBlocking), "stream");
+  return SWM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h, const double* u,
+                           const double* v) {
+  TraceRange trace_("swm_state_upload_async");
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
+  USE_DEVICE(ctx);
+  if (int rc = transfer_ready(ctx, 0)) return rc;
+  const size_t np = 6 * (size_t)ctx->n * ctx->n;
+  const int k = ctx->xnext[0];
+  ctx->xnext[0] ^= 1;
+  double* B = ctx->xbuf[0][k];
+  const double* src[3] = {h, u, v};
+  // the copy engine fills buffer k once the unpack that last read it is done
+  CK(cudaStreamWaitEvent(ctx->xst[0], ctx->xdone[0][k], 0), "wait");
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpyAsync(B + c * np, src[c], sizeof(double) * np, cudaMemcpyHostToDevice, ctx->xst[0]),
+       "upload");
+  CK(cudaEventRecord(ctx->xready[0][k], ctx->xst[0]), "event record");
+  CK(cudaStreamWaitEvent(ctx->st, ctx->xready[0][k], 0), "wait");
+  PackedFields pf{{B, B + np, B + 2 * np}};
+  CK(launch_unpack_state(ctx->g64, 3, pf, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr,
+                         ctx->st),
+     "unpack");
+  CK(cudaEventRecord(ctx->xdone[0][k], ctx->st), "event record");
+  return SWM_OK;
+}
+
+int swm_state_download_async(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  TraceRange trace_("swm_state_download_async");
+  if (int rc = check_state(ctx, s)) return rc;
+  if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
+  USE_DEVICE(ctx);
+  if (int rc = transfer_ready(ctx, 1)) return rc;
+  const size_t np = 6 * (size_t)ctx->n * ctx->n;
+  const int k = ctx->xnext[1];
+  ctx->xnext[1] ^= 1;
+  double* B = ctx->xbuf[1][k];
+  double* dst[3] = {h, u, v};
+  // the state is packed into buffer k once the copy that last read it is done
+  CK(cudaStreamWaitEvent(ctx->st, ctx->xdone[1][k], 0), "wait");
+  PackedFields pf{{B, B + np, B + 2 * np}};
+  CK(launch_pack_state(ctx->g64, 3, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr, pf,
+                       ctx->st),
+     "pack");
+  CK(cudaEventRecord(ctx->xready[1][k], ctx->st), "event record");
+  CK(cudaStreamWaitEvent(ctx->xst[1], ctx->xready[1][k], 0), "wait");
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpyAsync(dst[c], B + c * np, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->xst[1]),
+       "download");
+  CK(cudaEventRecord(ctx->xdone[1][k], ctx->xst[1]), "event record");
   return SWM_OK;
 }
 

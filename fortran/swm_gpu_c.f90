@@ -98,6 +98,17 @@ interface
         type(c_ptr), value :: ctx, s
         real(c_double), intent(out) :: h(*), u(*), v(*)
     end function swm_state_download
+    ! The asynchronous transfers read / write the host arrays after the call
+    ! returns, so they take their addresses (c_loc of contiguous target
+    ! arrays): an assumed-size dummy could be a temporary copy.
+    integer(c_int) function swm_state_upload_async(ctx, s, h, u, v) bind(c, name="swm_state_upload_async")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, s, h, u, v
+    end function swm_state_upload_async
+    integer(c_int) function swm_state_download_async(ctx, s, h, u, v) bind(c, name="swm_state_download_async")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, s, h, u, v
+    end function swm_state_download_async
     integer(c_int) function swm_assign_s1(ctx, s, s1) bind(c, name="swm_assign_s1")
         import :: c_int, c_ptr, c_double
         type(c_ptr), value :: ctx, s

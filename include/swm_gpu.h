@@ -112,6 +112,21 @@ int  swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h,
                       const double* u, const double* v);
 int  swm_state_download(swm_ctx* ctx, const swm_state* s, double* h,
                         double* u, double* v);
+/* Asynchronous transfers (no reference counterpart): the same packed host
+ * layout as swm_state_upload / swm_state_download, moved by the copy engines
+ * on two transfer streams of the context (one per direction) through device
+ * staging buffers, so that transfers overlap the context's kernels and each
+ * other.  Both return at once.
+ *   upload_async: s holds the arrays' values for every call queued after
+ *     it; the arrays must stay unchanged until swm_ctx_synchronize returns.
+ *   download_async: copies s as the calls queued before it leave it (s may
+ *     be changed right after the call); the arrays hold the values once
+ *     swm_ctx_synchronize returns.
+ * Page-locked host arrays give the overlap; pageable ones work but block. */
+int  swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h,
+                            const double* u, const double* v);
+int  swm_state_download_async(swm_ctx* ctx, const swm_state* s, double* h,
+                              double* u, double* v);
 /* this = s1                       (%assign_s1) */
 int swm_assign_s1(swm_ctx* ctx, swm_state* s, double s1);
 /* this = s1*v1                    (%assign_s1v1) */

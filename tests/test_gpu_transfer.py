@@ -1,8 +1,10 @@
 """Host <-> device transfers of states and scalar fields through the C-ABI.
 
 Page-locked host arrays are read and written in place by the pack kernels;
-pageable arrays go through a contiguous staging copy.  Both routes must give
-identical device states.  FP64 round trips are exact; the FP32 (hi, lo) pair
+pageable arrays go through a contiguous staging copy; the asynchronous
+transfers (swm_state_upload_async / _download_async) go through device
+staging buffers on the copy engines.  All routes must give identical device
+states.  FP64 round trips are exact; the FP32 (hi, lo) pair
 reproduces an FP64 value x to |x - (hi + lo)| <= 2^-47 |x|
 (hi = fl32(x) loses at most 2^-24 |x|, lo = fl32(x - hi) keeps all but
 2^-24 of that, and the FP64 sum adds at most 2^-53 |x|)."""
@@ -41,8 +43,7 @@ def test_page_locked_and_pageable_routes_agree(prec):
         p[...] = a
     s_pg, s_pin = op.create_stvec(), op.create_stvec()
     s_pg.upload(*x)
-    s_pin.upload_async(*pin_in)
-    op.synchronize()
+    s_pin.upload(*pin_in)   # read in place over the host link
 
     out_pg = s_pg.download()
     keep_out, pin_out = _pinned_views(sh, 3)
@@ -71,7 +72,7 @@ def test_stepped_states_identical_across_routes(prec):
         p[...] = a
     s1, s2 = op.create_stvec(), op.create_stvec()
     s1.upload(h, u, v)
-    s2.upload_async(*pin)
+    s2.upload(*pin)
     ts = swm.RK4()
     ts.step(s1, op, 600.0, 3)
     ts.step(s2, op, 600.0, 3)
@@ -90,3 +91,78 @@ def test_scalar_field_routes_agree():
     f2.upload(pin[0])
     assert np.array_equal(f1.download(), a)
     assert np.array_equal(f2.download(), a)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_async_transfers_match_the_synchronous_route(prec, pinned):
+    """upload_async -> steps -> download_async gives the bytes of upload ->
+    steps -> download, from page-locked and from pageable arrays."""
+    from cubedsphere_sbp_swm_gb300 import initial
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision=prec))
+    h, u, v, _ = initial.balanced_zonal(N, 3, 16)
+    if pinned:
+        keep_in, src = _pinned_views(op.shape, 3)
+        keep_out, dst = _pinned_views(op.shape, 3)
+    else:
+        src = [np.empty(op.shape) for _ in range(3)]
+        dst = [np.empty(op.shape) for _ in range(3)]
+    for p, a in zip(src, (h, u, v)):
+        p[...] = a
+    s_sync, s_async = op.create_stvec(), op.create_stvec()
+    s_sync.upload(h, u, v)
+    s_async.upload_async(*src)
+    ts = swm.RK4()
+    ts.step(s_sync, op, 600.0, 2)
+    ts.step(s_async, op, 600.0, 2)
+    s_async.download_async(tuple(dst))
+    op.synchronize()
+    for a, b in zip(s_sync.download(), dst):
+        assert np.array_equal(a, b)
+
+
+def test_async_pipeline_of_two_states():
+    """The pipelined loop the bench's end-to-end figure runs: two states take
+    turns; each step uploads its input asynchronously, steps and downloads
+    asynchronously, with the next step queued before the last download has
+    landed.  Every output equals the synchronous route's, and a state changed
+    right after download_async does not change what the download returns."""
+    from cubedsphere_sbp_swm_gb300 import initial
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp32"))
+    inputs = [initial.balanced_zonal(N, seed, 16)[:3] for seed in (4, 5, 6, 7, 8)]
+    expect = []
+    ref = op.create_stvec()
+    ts = swm.RK4()
+    for x in inputs:
+        ref.upload(*x)
+        ts.step(ref, op, 600.0, 1)
+        expect.append(ref.download())
+    states = [op.create_stvec(), op.create_stvec()]
+    keeps, outs = [], []
+    for k, x in enumerate(inputs):
+        ki, si = _pinned_views(op.shape, 3)     # every step its own input arrays
+        ko, o = _pinned_views(op.shape, 3)
+        keeps += [ki, ko]
+        outs.append(o)
+        for p, a in zip(si, x):
+            p[...] = a
+        st = states[k % 2]
+        st.upload_async(*si)
+        ts.step(st, op, 600.0, 1)
+        st.download_async(tuple(o))
+        st.assign_s1(-1.0)          # changed right after; the download keeps the stepped state
+    op.synchronize()
+    for e, o in zip(expect, outs):
+        for a, b in zip(e, o):
+            assert np.array_equal(a, b)
+
+
+def test_async_transfers_reject_temporaries():
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    s = op.create_stvec()
+    bad = np.zeros(op.shape, dtype=np.float32)
+    good = np.zeros(op.shape)
+    with pytest.raises(ValueError):
+        s.upload_async(bad, good, good)
+    with pytest.raises(ValueError):
+        s.download_async((good, good, good[:, ::-1]))
