@@ -190,6 +190,7 @@ struct swm_ctx {
   double* qw = nullptr;    // sync weights 4n
   double* Aw = nullptr;    // quadrature weights per line index (n)
   void* edge = nullptr;    // stage edge buffer (context precision)
+  void* edge2 = nullptr;   // second edge buffer of the FP32 diffusion step (allocated on first use)
   double* edge64 = nullptr;
   void* ya = nullptr; void* yb = nullptr; void* acc = nullptr;  // RK work (3 fields)
   double* tmp = nullptr;   // 14 FP64 work fields (g64)
@@ -787,7 +788,7 @@ void free_ctx(swm_ctx* c) {
   // hsT aliases hs64 in FP64 contexts: free each allocation once
   void* hsT = (c->hsT == (void*)c->hs64) ? nullptr : c->hsT;
   if (c->ad_graph) cudaGraphExecDestroy(c->ad_graph);
-  void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge64, c->ya, c->yb, c->acc,
+  void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge2, c->edge64, c->ya, c->yb, c->acc,
                   c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (auto& t : c->ntab)
@@ -1368,6 +1369,8 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
   const size_t elt = (size_t)ctx->elt;
   if (ctx->n < 2 * narrow_rows(narrow))
     return fail(ctx, SWM_E_INVALID, "grid too small for the narrow Laplacian closures");
+  if (ctx->prec == SWM_FP32_FUSED && !ctx->edge2)
+    CK(cudaMalloc(&ctx->edge2, sizeof(float) * 16 * 6 * ctx->n), "alloc");
   if (!ctx->dw) {
     const size_t nw = ctx->prec == SWM_FP64_PLAIN ? kDiffWorkF64 : kDiffWorkF32;
     CK(cudaMalloc(&ctx->dw, elt * nw * g.fs), "alloc");
@@ -1483,7 +1486,9 @@ int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* 
 // One explicit Euler step of the diffusion operator (explicit_Eul1_mod.f90:
 // 20-30): v0 = v0 + dt * D(v0).  FP32 contexts take the tendency of the
 // high part in FP32 and add it to the (hi, lo) pair with a two-sum, fused
-// with the tendency and the sync (launch_diff_update_f32).
+// with the tendency and the sync (launch_diff_update_f32); with the 4/2
+// order for h and the velocity the Laplacians' syncs ride in the next
+// launch's reads (launch_biharmonic_f32).
 int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
   const long long fs = ctx->g64.fs;
   if (ctx->prec == SWM_FP64_PLAIN) {
@@ -1494,13 +1499,27 @@ int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
     CK(launch_axpby(3 * fs, 1.0, x, dt, T, x, ctx->st), "update");
   } else {
     float* x = (float*)v0->hi;
-    if (int rc = enqueue_biharmonic<float>(ctx, x, x + fs, x + 2 * fs)) return rc;
-    const float* F = dwork<float>(ctx, 0);
+    float* F = dwork<float>(ctx, 0);
     float* T = dwork<float>(ctx, 8);
+    const float* edge_in = nullptr;
+    if (ctx->diff_uv == ctx->diff_h && ctx->diff_h == 42) {
+      // the 4/2 order for h and the velocity: two Laplacian launches of the
+      // 4 fields, their syncs folded into the next launch's reads
+      const FieldGeom& g = ctx->g64;
+      CK(launch_to_cart<float>(g, (const float*)ctx->b12, x, x + fs, x + 2 * fs, F, F + fs, ctx->st),
+         "to cart");
+      CK(launch_biharmonic_f32(g, ctx->topo, narrow_tables<float>(ctx, ctx->diff_h), F,
+                               dwork<float>(ctx, 4), metric_of<float>(ctx), ctx->hx * ctx->cfg.radius,
+                               (float*)ctx->edge, (float*)ctx->edge2, ctx->st),
+         "biharmonic");
+      edge_in = (const float*)ctx->edge2;
+    } else if (int rc = enqueue_biharmonic<float>(ctx, x, x + fs, x + 2 * fs)) {
+      return rc;
+    }
     CK(launch_diff_update_f32(ctx->g64, ctx->topo, ctx->qw, (const float*)ctx->b12,
                               diff_coeff4(ctx, ctx->diff_uv_coeff), F + fs,
                               diff_coeff4(ctx, ctx->diff_h_coeff), F, dt, x, v0->lo, T + fs,
-                              T + 2 * fs, (float*)ctx->edge, ctx->st),
+                              T + 2 * fs, (float*)ctx->edge, edge_in, ctx->st),
        "update");
   }
   return SWM_OK;

@@ -241,11 +241,19 @@ __device__ __forceinline__ void lap_region(int a0, int len, int n, int& lo, int&
   }
 }
 
-template <int NARROW, int NF>
+// SYNC_IN: Ein is the edge buffer of the kernel that wrote f, whose
+// panel-side nodes still need their cube-edge scalar sync: the block applies
+// it to the staged values of those nodes (value slot c of Ein for field c),
+// the arithmetic of sync_fields_kernel, so the sync launch is not needed.
+// (A compile-time switch: the code costs registers in the launches that do
+// not need it.)
+template <int NARROW, int NF, bool SYNC_IN = false>
 __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty, const float* f,
                                                            const float* clx, const float* cly,
                                                            const float* bco, const float* mt,
-                                                           float hs2, float* out, float* E) {
+                                                           float hs2, float* out, float* E,
+                                                           const float* Ein,
+                                                           const __grid_constant__ Topology tp) {
   using T = float;
   using S = NarrowShape<NARROW>;
   using LT = LapTile<NARROW, NF>;
@@ -305,6 +313,32 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
   }
   cp_async_wait_all();
   __syncthreads();
+  if (SYNC_IN && (xlo == 0 || xhi == n || ylo == 0 || yhi == n)) {
+    // the region's panel-side nodes: left and right columns, then bottom and
+    // top rows without the corners the columns already took
+    const EdgeView<float> ev{Ein, n};
+    const int tid = ly * LTX + lx;
+    for (int e = tid; e < 2 * (rx + ry); e += LTPB) {
+      int x, y;
+      if (e < ry) {
+        if (xlo != 0) continue;
+        x = 0; y = e;
+      } else if (e < 2 * ry) {
+        if (xhi != n) continue;
+        x = rx - 1; y = e - ry;
+      } else {
+        const bool bottom = e < 2 * ry + rx;
+        if (bottom ? ylo != 0 : yhi != n) continue;
+        x = bottom ? e - 2 * ry : e - 2 * ry - rx;
+        y = bottom ? 0 : ry - 1;
+        if ((x == 0 && xlo == 0) || (x == rx - 1 && xhi == n)) continue;
+      }
+#pragma unroll
+      for (int c = 0; c < NF; ++c)
+        Fs[c][y][x] = sync_scalar_node<float>(ev, tp, p, xlo + x, ylo + y, c, Fs[c][y][x]);
+    }
+    __syncthreads();
+  }
 
   // d1x on the tile's columns x the region's rows, d1y on the region's
   // columns x the tile's rows
@@ -637,19 +671,34 @@ __global__ void pair_axpy_kernel(long long count, double dt, const T* t, float* 
 //     edge buffer's GX/GY slots;
 //   diff_sync_update_kernel: those nodes' covariant sync
 //     (ecs_Ah_vec_sync_mod.f90:62-125), then their pair update.
+//
+// Ein (nullable): the edge buffer of the Laplacian that wrote Lh and L when
+// their panel-side values still need the cube-edge scalar sync (value slot 0
+// for Lh, 1..3 for L), applied here as sync_fields_kernel would.
 __global__ void diff_update_kernel(FieldGeom g, const float* b, float cuv, const float* L, float ch,
                                    const float* Lh, float dt, float* hi, float* lo, float* tu,
-                                   float* tv, float* E) {
+                                   float* tv, float* E, const float* Ein,
+                                   const __grid_constant__ Topology tp) {
   Node k;
   if (!node_here(g, k)) return;
   const long long fs = g.fs;
+  const int n = g.n;
+  const bool side = k.i == 0 || k.i == n - 1 || k.j == 0 || k.j == n - 1;
+  float lv[3], lh = Lh[k.idx];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) lv[a] = L[a * fs + k.idx];
+  if (Ein && side) {
+    const EdgeView<float> ev{Ein, n};
+    lh = sync_scalar_node<float>(ev, tp, k.p, k.i, k.j, 0, lh);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) lv[a] = sync_scalar_node<float>(ev, tp, k.p, k.i, k.j, 1 + a, lv[a]);
+  }
   float t[3];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) t[a] = cuv * L[a * fs + k.idx];
+  for (int a = 0; a < 3; ++a) t[a] = cuv * lv[a];
   const float ut = t[0] * b[k.idx] + t[1] * b[fs + k.idx] + t[2] * b[2 * fs + k.idx];
   const float vt = t[0] * b[3 * fs + k.idx] + t[1] * b[4 * fs + k.idx] + t[2] * b[5 * fs + k.idx];
-  pair_add(dt, ch * Lh[k.idx], hi, lo, k.idx);
-  const int n = g.n;
+  pair_add(dt, ch * lh, hi, lo, k.idx);
   if (k.i > 0 && k.i < n - 1 && k.j > 0 && k.j < n - 1) {
     pair_add(dt, ut, hi + fs, lo + fs, k.idx);
     pair_add(dt, vt, hi + 2 * fs, lo + 2 * fs, k.idx);
@@ -715,15 +764,26 @@ long long narrow_closure_count(int narrow, int n) {
 }
 
 template <class T, int NARROW, int NF>
-cudaError_t laplace_nf(const FieldGeom& g, const NarrowTables<T>& t, const T* f, const T* mt, double hs,
-                       T* d1x, T* d1y, T* out, T* edge, cudaStream_t st) {
+cudaError_t laplace_nf(const FieldGeom& g, const Topology& tp, const NarrowTables<T>& t, const T* f,
+                       const T* mt, double hs, T* d1x, T* d1y, T* out, T* edge, const T* edge_in,
+                       cudaStream_t st) {
   if constexpr (sizeof(T) == 4) {
     const int nty = (g.n + LTY - 1) / LTY;
     const dim3 grid((g.n + LTX - 1) / LTX, 6 * nty), block(LTX, LTY);
     // (hx a)^2 rounded to FP32 once, as the kernel would round it
-    lap_tile_kernel<NARROW, NF><<<grid, block, LapTile<NARROW, NF>::bytes, st>>>(
-        g, nty, f, t.clx, t.cly, t.b, mt, float(hs * hs), out, edge);
+    if constexpr (NARROW == 42 && NF == 4) {
+      if (edge_in) {
+        lap_tile_kernel<NARROW, NF, true><<<grid, block, LapTile<NARROW, NF>::bytes, st>>>(
+            g, nty, f, t.clx, t.cly, t.b, mt, float(hs * hs), out, edge, edge_in, tp);
+        return cudaGetLastError();
+      }
+    } else if (edge_in) {
+      return cudaErrorInvalidValue;
+    }
+      lap_tile_kernel<NARROW, NF><<<grid, block, LapTile<NARROW, NF>::bytes, st>>>(
+          g, nty, f, t.clx, t.cly, t.b, mt, float(hs * hs), out, edge, nullptr, tp);
   } else {
+    if (edge_in) return cudaErrorInvalidValue;   // FP64 inputs are synced by their own launch
     if (!d1x || !d1y) return cudaErrorInvalidValue;
     lap_d1_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(g, f, mt, d1x, d1y);
     lap_main_kernel<T, NARROW, NF><<<row_grid(g), row_block(), 0, st>>>(
@@ -745,6 +805,11 @@ cudaError_t prepare_laplace_order() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(lap_tile_kernel<NARROW, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)LapTile<NARROW, 4>::bytes);
+  if constexpr (NARROW == 42) {   // the folded-sync form serves the 4/2 order only
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(lap_tile_kernel<NARROW, 4, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LapTile<NARROW, 4>::bytes);
+  }
   return e;
 }
 
@@ -773,18 +838,36 @@ cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowT
   if (nf != 1 && nf != 3 && nf != 4) return cudaErrorInvalidValue;
   cudaError_t e;
   if (t.narrow == 63) {
-    if (nf == 1) e = laplace_nf<T, 63, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else if (nf == 3) e = laplace_nf<T, 63, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else e = laplace_nf<T, 63, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    if (nf == 1) e = laplace_nf<T, 63, 1>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+    else if (nf == 3) e = laplace_nf<T, 63, 3>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+    else e = laplace_nf<T, 63, 4>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
   } else {
-    if (nf == 1) e = laplace_nf<T, 42, 1>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else if (nf == 3) e = laplace_nf<T, 42, 3>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
-    else e = laplace_nf<T, 42, 4>(g, t, f, mt, hs, d1x, d1y, out, edge, st);
+    if (nf == 1) e = laplace_nf<T, 42, 1>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+    else if (nf == 3) e = laplace_nf<T, 42, 3>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+    else e = laplace_nf<T, 42, 4>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
   }
   if (e != cudaSuccess) return e;
   const int nb = 6 * (4 * g.n - 4);
   sync_fields_kernel<T><<<dblk(nb), DTPB, 0, st>>>(g, tp, nf, edge, out);
   return cudaGetLastError();
+}
+
+// The biharmonic operator's two FP32 Laplacians of the 4 fields
+// [h, x, y, z] without sync launches: f -> L (panel-side values also to
+// edge_a), then L -> f, whose staging syncs L's panel-side values from
+// edge_a and which writes its own to edge_b.  f's panel-side nodes are left
+// unsynced: the consumer syncs them from edge_b (launch_diff_update_f32).
+// The 4/2 order only: measured on GB300, it saves 2.8% of the FP32
+// diffusion step at N=384 d42, while for 6/3 the folded staging's register
+// spills cost more than the two sync launches (0.77 -> 0.80 ms at N=1024).
+cudaError_t launch_biharmonic_f32(const FieldGeom& g, const Topology& tp,
+                                  const NarrowTables<float>& t, float* f, float* L, const float* mt,
+                                  double hs, float* edge_a, float* edge_b, cudaStream_t st) {
+  if (t.narrow != 42) return cudaErrorInvalidValue;
+  cudaError_t e = laplace_nf<float, 42, 4>(g, tp, t, f, mt, hs, nullptr, nullptr, L, edge_a, nullptr, st);
+  if (e == cudaSuccess)
+    e = laplace_nf<float, 42, 4>(g, tp, t, L, mt, hs, nullptr, nullptr, f, edge_b, edge_a, st);
+  return e;
 }
 
 template <class T>
@@ -812,10 +895,11 @@ cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, 
 cudaError_t launch_diff_update_f32(const FieldGeom& g, const Topology& tp, const double* qw,
                                    const float* b12, double cuv, const float* L, double ch,
                                    const float* Lh, double dt, float* hi, float* lo, float* tu,
-                                   float* tv, float* edge, cudaStream_t st) {
+                                   float* tv, float* edge, const float* edge_in, cudaStream_t st) {
   // dt enters the FP32 increment rounded to FP32 (once, here)
   diff_update_kernel<<<row_grid(g), row_block(), 0, st>>>(g, b12, float(cuv), L, float(ch), Lh,
-                                                            float(dt), hi, lo, tu, tv, edge);
+                                                            float(dt), hi, lo, tu, tv, edge, edge_in,
+                                                            tp);
   const int nb = 6 * (4 * g.n - 4);
   diff_sync_update_kernel<<<dblk(nb), DTPB, 0, st>>>(g, tp, qw, edge, tu, tv, float(dt), hi, lo);
   return cudaGetLastError();

@@ -191,11 +191,20 @@ cudaError_t launch_diff_tendency(const FieldGeom& g, const T* b12, double cuv, c
 // (L: 3 Cartesian fields, Lh: h): tendencies cuv*L projected on b1, b2 and
 // ch*Lh, the covariant sync of the velocity tendency, and the (hi, lo) pair
 // update by dt, in two launches; tu, tv: work fields for the panel-boundary
-// nodes.
+// nodes.  edge_in (nullable): the edge buffer of the Laplacian that wrote
+// Lh (slot 0) and L (slots 1..3) when their panel-side values are not yet
+// synced (launch_biharmonic_f32); edge must be another buffer.
 cudaError_t launch_diff_update_f32(const FieldGeom& g, const Topology& tp, const double* qw,
                                    const float* b12, double cuv, const float* L, double ch,
                                    const float* Lh, double dt, float* hi, float* lo, float* tu,
-                                   float* tv, float* edge, cudaStream_t st);
+                                   float* tv, float* edge, const float* edge_in, cudaStream_t st);
+// The FP32 biharmonic L(L(f)) of the 4 fields [h, x, y, z] of the 4/2
+// narrow order in two tile launches and no sync launch: f is overwritten with the
+// result, whose panel-side values are left for the consumer to sync from
+// edge_b; L is a work area of 4 fields, edge_a another edge buffer.
+cudaError_t launch_biharmonic_f32(const FieldGeom& g, const Topology& tp,
+                                  const NarrowTables<float>& t, float* f, float* L, const float* mt,
+                                  double hs, float* edge_a, float* edge_b, cudaStream_t st);
 template <class T>
 cudaError_t launch_pair_axpy(long long count, double dt, const T* t, float* hi, float* lo,
                              cudaStream_t st);
