@@ -19,11 +19,14 @@
  *     both ways: apply + update_s1v1 (explicit_Eul1_mod.f90:20-30) and the
  *     fused swm_diffusion_step;
  *  6. checks two error paths: a grid that is too small and an unknown
- *     operator name.
+ *     operator name;
+ *  7. moves the input through swm_state_upload_async / _download_async and
+ *     checks the bytes against the synchronous upload / download.
  * OUT receives, in order: the generic RK4 state, the fused RK4 state (3
  * fields each), diagnostics[7], norm2, dot(v0, v0 fused), the generic and the
  * fused diffusion-step states.  Exit status 0 on success; on an ABI error it
- * prints the library's message and exits 2.
+ * prints the library's message and exits 2; 4 if the asynchronous transfers
+ * disagree with the synchronous ones.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -114,6 +117,21 @@ int main(int argc, char** argv) {
   check(swm_state_create_similar(g_ctx, v0, &d2), "create_similar");
   check(swm_state_create_similar(g_ctx, v0, &tend), "create_similar");
   check(swm_state_upload(g_ctx, v0, in, in + np, in + 2 * np), "swm_state_upload");
+
+  /* 7. asynchronous round trip against the synchronous one */
+  {
+    double* a = malloc(3 * np * sizeof(double));
+    check(swm_state_upload_async(g_ctx, y, in, in + np, in + 2 * np), "swm_state_upload_async");
+    check(swm_state_download_async(g_ctx, y, a, a + np, a + 2 * np), "swm_state_download_async");
+    check(swm_assign_s1(g_ctx, y, 0.0), "assign");   /* after the call: does not reach a */
+    check(swm_ctx_synchronize(g_ctx), "synchronize");
+    download(v0, buf, np, "download");
+    if (memcmp(a, buf, 3 * np * sizeof(double)) != 0) {
+      fprintf(stderr, "abi_driver: asynchronous transfers differ from the synchronous ones\n");
+      return 4;
+    }
+    free(a);
+  }
   check(swm_assign_s1v1(g_ctx, vf, 1.0, v0), "copy_to");
   check(swm_assign_s1v1(g_ctx, d1, 1.0, v0), "copy_to");
   check(swm_assign_s1v1(g_ctx, d2, 1.0, v0), "copy_to");
