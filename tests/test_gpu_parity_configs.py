@@ -11,7 +11,14 @@ The FP64 plain path against the FP64 oracle:
 
 The FP32 fused form against the FP64 oracle for SBP 4/2, 4/3 and 6/3, one
 step and 96 steps: h, u and v within 1e-5 relative L2, mass drift within
-1e-6 of the oracle's.
+1e-6 of the oracle's; and one step of each benchmarked configuration: the
+state within 1e-6 (measured: h 3e-8, u and v 3e-7), and the step's
+increment within 0.1, a check of its direction only.  The stage inputs of
+the FP32 form carry the high part of the state, and in these nearly
+balanced flows h (about 6000 m, FP32 ulp 5e-4 m) moves by a few ulp per
+step, so its increment is resolved to a few percent (measured: 3.6% at
+N=384, 1.5% at N=1024; u and v 0.2-0.3%).  The compensated pair keeps what
+the stages cannot resolve, which the state bound checks.
 """
 import os
 
@@ -82,3 +89,20 @@ def test_rk4_fp32_fused_vs_fp64_oracle(order, N, nsteps):
     assert max(errs.values()) < TOL_FP32, errs
     drift = abs(od.mass(gh) - od.mass(oh)) / od.mass(oh)
     assert drift < 1e-6, drift
+
+
+@pytest.mark.parametrize("cfg", [2, 5], ids=["n384_d42_dt120", "n1024_d63_dt45"])
+def test_rk4_fp32_one_step_at_bench_config(cfg):
+    c = initial.CONFIGS[cfg]
+    N, order, dt = c["N"], c["sbp_order"], c["dt"]
+    h, u, v, _ = initial.config_state(cfg)
+    oracle.set_threads(os.cpu_count() or 1)
+    od = oracle.OracleDomain(N, order)
+    J = initial.ecs_geometry(N)["J"]
+    got = _gpu_run(N, order, "fp32", (h, u, v), dt, 1)
+    ref = od.rk4(h, u, v, dt, 1)
+    for name, g, r, x0 in zip("huv", got, ref, (h, u, v)):
+        e = rel_l2(g, r, J)
+        assert e < 1e-6, (name, e)
+        ei = rel_l2(g - x0, r - x0, J)
+        assert ei < 0.1, (name, ei)
