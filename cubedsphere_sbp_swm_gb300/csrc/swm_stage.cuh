@@ -323,19 +323,16 @@ __global__ void __launch_bounds__(STAGE_BW)
     const bool bnd = (col == 0) | (col == n - 1) | (j == 0) | (j == n - 1);
     if (bnd) {
       T* E = I.edge + (long long)wu.panel * 16 * n;
-      const T vals[4] = {gx, gy, zeta, dv};
-      if (col == 0)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) E[(SIDE_L * 4 + e) * n + j] = vals[e];
-      if (col == n - 1)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) E[(SIDE_R * 4 + e) * n + j] = vals[e];
-      if (j == 0)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) E[(SIDE_B * 4 + e) * n + col] = vals[e];
-      if (j == n - 1)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) E[(SIDE_T * 4 + e) * n + col] = vals[e];
+      // the four values one by one (an array of them was kept in local memory
+      // for every node, boundary or not)
+      auto put = [&](int side, int k) {
+        T* e = E + (side * 4) * n + k;
+        e[0] = gx; e[n] = gy; e[2 * n] = zeta; e[3 * n] = dv;
+      };
+      if (col == 0) put(SIDE_L, j);
+      if (col == n - 1) put(SIDE_R, j);
+      if (j == 0) put(SIDE_B, col);
+      if (j == n - 1) put(SIDE_T, col);
       continue;
     }
     const T f = I.metric[MF * fs + idx];

@@ -147,61 +147,32 @@ struct TmaLayout {
 };
 
 // y derivative at row j from the register window w (w[i] holds row j-RMAX+i).
-// Closure rows come in two forms with the same terms in the same order:
-// - per closure row (stencils of reach RMAX <= 3): the row is selected
-//   among the compile-time closure rows;
-// - per window slot (RMAX = 5): every slot with the row's coefficient of that
-//   slot (zero outside the stencil, adding exact zeros), so the wide window
-//   is only ever indexed by compile-time constants and stays in registers.
-// Measured on GB300: the second form is 4.5% faster for SBP 6/3 at N=1024,
-// the first 7% faster for SBP 4/2 at N=384.
+// A closure row takes every window slot with the row's coefficient of that
+// slot (zero outside the stencil, adding exact zeros), so the window is only
+// ever indexed by compile-time constants and stays in registers.  (Selecting
+// among the compile-time closure rows instead, with the taps at their rows,
+// made the compiler keep a 4/2 window in local memory, rewritten every row.)
 template <int ORD, class T, int WS>
 __device__ __forceinline__ T ydiff(const T (&w)[WS], int j, int n) {
-  constexpr int NE = Ord<ORD>::NE, RMAX = Ord<ORD>::RMAX, ID = Ord<ORD>::idx, NW = Ord<ORD>::NW;
+  constexpr int NE = Ord<ORD>::NE, RMAX = Ord<ORD>::RMAX, ID = Ord<ORD>::idx;
   if (j >= NE && j < n - NE) return d_interior<ORD, T>([&](int o) { return w[RMAX + o]; });
   T acc = T(0);
-  if constexpr (RMAX >= 5) {
-    if (j < NE) {
-      const int last = c_sbp[ID].last[j];
+  if (j < NE) {
+    const int last = c_sbp[ID].last[j];
 #pragma unroll
-      for (int i = 0; i < WS; ++i) {
-        const int m = j - RMAX + i;            // panel row of slot i
-        const T c = (m >= 0 && m < last) ? sbp_ql<T>(ID, j, m) : T(0);
-        acc += c * w[i];
-      }
-    } else {
-      const int R = n - 1 - j;
-      const int last = c_sbp[ID].last[R];
-#pragma unroll
-      for (int i = 0; i < WS; ++i) {
-        const int m = R + RMAX - i;            // slot i holds panel row n-1-m
-        const T c = (m >= 0 && m < last) ? sbp_qr<T>(ID, R, m) : T(0);
-        acc += c * w[i];
-      }
-    }
-  } else if (j < NE) {
-#pragma unroll
-    for (int J = 0; J < NE; ++J) {
-      if (j == J) {
-#pragma unroll
-        for (int m = 0; m < NW; ++m) {
-          const int idx = m - J + RMAX;  // row m
-          if (m < c_sbp[ID].last[J] && idx >= 0 && idx < WS)
-            acc += sbp_ql<T>(ID, J, m) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
-        }
-      }
+    for (int i = 0; i < WS; ++i) {
+      const int m = j - RMAX + i;            // panel row of slot i
+      const T c = (m >= 0 && m < last) ? sbp_ql<T>(ID, j, m) : T(0);
+      acc += c * w[i];
     }
   } else {
+    const int R = n - 1 - j;
+    const int last = c_sbp[ID].last[R];
 #pragma unroll
-    for (int R = 0; R < NE; ++R) {
-      if (n - 1 - j == R) {
-#pragma unroll
-        for (int m = NW - 1; m >= 0; --m) {
-          const int idx = R - m + RMAX;  // row n-1-m
-          if (m < c_sbp[ID].last[R] && idx >= 0 && idx < WS)
-            acc += sbp_qr<T>(ID, R, m) * w[idx < 0 ? 0 : (idx >= WS ? WS - 1 : idx)];
-        }
-      }
+    for (int i = 0; i < WS; ++i) {
+      const int m = R + RMAX - i;            // slot i holds panel row n-1-m
+      const T c = (m >= 0 && m < last) ? sbp_qr<T>(ID, R, m) : T(0);
+      acc += c * w[i];
     }
   }
   return acc;
