@@ -29,7 +29,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB_PATH) or (
         os.path.getmtime(_LIB_PATH) < max(
             os.path.getmtime(os.path.join(_HERE, f))
-            for f in ("swm_oracle.cpp", "swm_oracle.h", "Makefile",
+            for f in ("swm_oracle.cpp", "swm_oracle_c.cpp", "swm_oracle.h",
+                      "swm_oracle_common.h", "Makefile",
                       "../cubedsphere_sbp_swm_gb300/csrc/swm_narrow_tables.h")
         )
     ):
@@ -93,6 +94,26 @@ def lib():
                                                    ctypes.c_double, _D, _D, _D, ctypes.c_double])):
             getattr(L, name).argtypes = args
             getattr(L, name).restype = ctypes.c_int
+        # C grid (swm_oracle_c.cpp)
+        L.orcc_create.restype = vp
+        L.orcc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_double, _D]
+        L.orcc_destroy.argtypes = [vp]
+        L.orcc_size.argtypes = [vp, ctypes.c_int]
+        L.orcc_size.restype = ctypes.c_int
+        L.orcc_points.argtypes = [vp, ctypes.c_int] + [_D] * 3
+        L.orcc_metric.argtypes = [vp, ctypes.c_int] + [_D] * 5
+        L.orcc_bases.argtypes = [vp, ctypes.c_int] + [_D] * 4
+        for name, n in (("orcc_co2contra", 4), ("orcc_massflux", 5), ("orcc_ke", 5),
+                        ("orcc_grad", 3), ("orcc_div", 3), ("orcc_curl", 3),
+                        ("orcc_coriolis", 6), ("orcc_apply", 7)):
+            getattr(L, name).argtypes = [vp] + [_D] * n
+        L.orcc_rk4.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int]
+        for name in ("orcc_mass", "orcc_l2norm"):
+            getattr(L, name).argtypes = [vp, ctypes.c_int, _D]
+            getattr(L, name).restype = ctypes.c_double
+        L.orcc_golden.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D]
+        L.orcc_golden.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -270,6 +291,118 @@ class OracleDomain:
 
     def mass(self, f):
         return lib().orc_mass(self._h, _p(np.ascontiguousarray(f, dtype=np.float64)))
+
+
+class OracleCDomain:
+    """FP64 oracle of the C-grid SBP vector-invariant operator
+    (&shallow_water_model_c, sbp_order 21 or 42).  Fields are dense arrays
+    per mesh: h (6, N, N) on the cell centres, u (6, N, N+1) on the x-faces,
+    v (6, N+1, N) on the y-faces, the curl (6, N+1, N+1) on the corners."""
+
+    MESHES = {"p": 0, "u": 1, "v": 2, "q": 3}
+
+    def __init__(self, N, sbp_order=42, radius=6.371e6, grav=9.80616,
+                 omega=7.292e-5, axis=(0.0, 0.0, 1.0)):
+        L = lib()
+        ax = np.asarray(axis, dtype=np.float64)
+        self._h = L.orcc_create(int(N), int(sbp_order), float(radius), float(grav),
+                                float(omega), _p(ax))
+        if not self._h:
+            raise ValueError(f"oracle: unsupported C grid N={N} / sbp_order={sbp_order}")
+        self.N, self.sbp_order = int(N), int(sbp_order)
+        n = self.N
+        self.shapes = {"p": (6, n, n), "u": (6, n, n + 1), "v": (6, n + 1, n), "q": (6, n + 1, n + 1)}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orcc_destroy(self._h)
+            self._h = None
+
+    def zeros(self, mesh):
+        return np.zeros(self.shapes[mesh])
+
+    def points(self, mesh):
+        x, y, z = (self.zeros(mesh) for _ in range(3))
+        lib().orcc_points(self._h, self.MESHES[mesh], _p(x), _p(y), _p(z))
+        return x, y, z
+
+    def metric(self, mesh):
+        out = {k: self.zeros(mesh) for k in ("J", "Qi1", "Qi2", "Qi3", "f")}
+        lib().orcc_metric(self._h, self.MESHES[mesh], *(_p(out[k]) for k in ("J", "Qi1", "Qi2", "Qi3", "f")))
+        return out
+
+    def bases(self, mesh):
+        sh = self.shapes[mesh] + (3,)
+        out = {k: np.zeros(sh) for k in ("a1", "a2", "b1", "b2")}
+        lib().orcc_bases(self._h, self.MESHES[mesh], *(_p(out[k]) for k in ("a1", "a2", "b1", "b2")))
+        return out
+
+    @staticmethod
+    def _c(a):
+        return np.ascontiguousarray(a, dtype=np.float64)
+
+    def co2contra(self, u, v):
+        ut, vt = self.zeros("u"), self.zeros("v")
+        lib().orcc_co2contra(self._h, _p(self._c(u)), _p(self._c(v)), _p(ut), _p(vt))
+        return ut, vt
+
+    def massflux(self, h, ut, vt):
+        hu, hv = self.zeros("u"), self.zeros("v")
+        lib().orcc_massflux(self._h, _p(self._c(h)), _p(self._c(ut)), _p(self._c(vt)), _p(hu), _p(hv))
+        return hu, hv
+
+    def ke(self, u, v, ut, vt):
+        k = self.zeros("p")
+        lib().orcc_ke(self._h, *(_p(self._c(a)) for a in (u, v, ut, vt)), _p(k))
+        return k
+
+    def grad(self, f):
+        gx, gy = self.zeros("u"), self.zeros("v")
+        lib().orcc_grad(self._h, _p(self._c(f)), _p(gx), _p(gy))
+        return gx, gy
+
+    def div(self, hu, hv):
+        d = self.zeros("p")
+        lib().orcc_div(self._h, _p(self._c(hu)), _p(self._c(hv)), _p(d))
+        return d
+
+    def curl(self, u, v):
+        c = self.zeros("q")
+        lib().orcc_curl(self._h, _p(self._c(u)), _p(self._c(v)), _p(c))
+        return c
+
+    def coriolis(self, hu, hv, h, curl):
+        cu, cv = self.zeros("u"), self.zeros("v")
+        lib().orcc_coriolis(self._h, *(_p(self._c(a)) for a in (hu, hv, h, curl)), _p(cu), _p(cv))
+        return cu, cv
+
+    def apply(self, h, u, v, hs=None):
+        th, tu, tv = self.zeros("p"), self.zeros("u"), self.zeros("v")
+        hs_p = None if hs is None else _p(self._c(hs))
+        lib().orcc_apply(self._h, hs_p, *(_p(self._c(a)) for a in (h, u, v)), _p(th), _p(tu), _p(tv))
+        return th, tu, tv
+
+    def rk4(self, h, u, v, dt, nsteps=1, hs=None):
+        h, u, v = (np.array(a, dtype=np.float64, order="C") for a in (h, u, v))
+        hs_p = None if hs is None else _p(self._c(hs))
+        lib().orcc_rk4(self._h, hs_p, _p(h), _p(u), _p(v), float(dt), int(nsteps))
+        return h, u, v
+
+    def mass(self, f, mesh="p"):
+        return lib().orcc_mass(self._h, self.MESHES[mesh], _p(self._c(f)))
+
+    def l2norm(self, f, mesh="p"):
+        return lib().orcc_l2norm(self._h, self.MESHES[mesh], _p(self._c(f)))
+
+
+def golden_c(kind: str, N: int = 32, sbp_order: int = 42) -> np.ndarray:
+    """Values printed by the reference known-answer test of a C-grid
+    operator at (N, nz=3): kind div, grad, curl, coriolis, ke or co2contra."""
+    k = {"div": 0, "grad": 1, "curl": 2, "coriolis": 3, "ke": 4, "co2contra": 5}[kind]
+    out = np.zeros(4)
+    if lib().orcc_golden(k, int(N), int(sbp_order), _p(out)) != 0:
+        raise ValueError(f"oracle C-grid golden {kind} failed for order {sbp_order}")
+    return out[:4] if kind in ("div", "curl", "ke") else out[:2]
 
 
 def golden(kind: str, N: int = 32, sbp_order: int = 42):

@@ -127,6 +127,43 @@ double orc_golden_quadrature(int N, int sbp_order, int max_order);
 /* RK4 amplification test (test_time_steping/test_ts_mod.f90:7-73). */
 double orc_golden_rk4_iomega(void);
 
+/* ---- C grid (swm_oracle_c.cpp): the &shallow_water_model_c operator family
+ * (namelist_swm:80-102), sbp_order 21 or 42, one tile per panel.  Meshes:
+ * 0 p (cell centres, N x N per panel), 1 u (x-faces, (N+1) x N), 2 v
+ * (y-faces, N x (N+1)), 3 q (corners, (N+1) x (N+1)); dense FP64, i fastest,
+ * then j, then panel.  h on p, covariant u on u, v on v, curl on q. */
+typedef struct orcc_domain orcc_domain;
+orcc_domain* orcc_create(int N, int sbp_order, double radius, double grav,
+                         double omega, const double axis[3]);
+void orcc_destroy(orcc_domain* d);
+int  orcc_size(const orcc_domain* d, int mesh);   /* points of a mesh, 6 panels */
+void orcc_points(const orcc_domain* d, int mesh, double* x, double* y, double* z);
+void orcc_metric(const orcc_domain* d, int mesh, double* J, double* Qi1,
+                 double* Qi2, double* Qi3, double* f);
+void orcc_bases(const orcc_domain* d, int mesh, double* a1, double* a2,
+                double* b1, double* b2);
+void orcc_co2contra(const orcc_domain* d, const double* u, const double* v,
+                    double* ut, double* vt);
+void orcc_massflux(const orcc_domain* d, const double* h, const double* ut,
+                   const double* vt, double* hu, double* hv);
+void orcc_ke(const orcc_domain* d, const double* u, const double* v,
+             const double* ut, const double* vt, double* ke);
+void orcc_grad(const orcc_domain* d, const double* f, double* gx, double* gy);
+void orcc_div(const orcc_domain* d, const double* hu, const double* hv, double* out);
+void orcc_curl(const orcc_domain* d, const double* u, const double* v, double* out);
+void orcc_coriolis(const orcc_domain* d, const double* hu, const double* hv,
+                   const double* h, const double* curl, double* cor_u, double* cor_v);
+void orcc_apply(const orcc_domain* d, const double* hs, const double* h,
+                const double* u, const double* v, double* th, double* tu, double* tv);
+void orcc_rk4(const orcc_domain* d, const double* hs, double* h, double* u,
+              double* v, double dt, int nsteps);
+double orcc_mass(const orcc_domain* d, int mesh, const double* f);
+double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
+/* Known-answer tests on the C grid at (N, nz=3, unit sphere): kind 0 div (4
+ * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2).
+ * Returns 0, or -1 for an unknown kind / order. */
+int orcc_golden(int kind, int N, int sbp_order, double* out);
+
 #ifdef __cplusplus
 }
 #endif

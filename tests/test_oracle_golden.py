@@ -107,6 +107,22 @@ def test_discrete_mass_conservation():
     assert abs(d.mass(th)) / scale < 1e-12
 
 
+GOLDEN_C = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "diffops_c_n32.json")))
+
+
+@pytest.mark.parametrize("entry", GOLDEN_C, ids=lambda g: g["name"])
+def test_c_grid_operator_golden_7_digits(entry):
+    """The C-grid SBP operators of the &shallow_water_model_c family
+    (namelist_swm:80-102) against the reference's printed values, to the 7
+    significant digits printed (reference_results.txt, test_diffops_all.f90
+    at N=32, nz=3)."""
+    got = oracle.golden_c(entry["kind"], entry["N"], entry["sbp_order"])
+    want = entry["values"]
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert _fmt7(g) == _fmt7(w), f"{entry['name']}: {g!r} vs {w!r} ({entry['source']})"
+
+
 REGRID = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "regrid_ah_n32.json")))
 
 
