@@ -28,7 +28,7 @@ __all__ = [
     "ModelConfig", "OperatorSWM", "StvecSWM", "GridField", "RK4", "OperatorSWMDiff",
     "ExplicitEul1", "LatLonRegrid", "LatLonOutputer", "PaneledOutputer", "HaloAhScalarSync",
     "EcsAhVecSyncCovariant", "create_timescheme", "create_halo_procedure",
-    "create_vector_halo_procedure", "Ensemble", "SwmError", "EARTH",
+    "create_vector_halo_procedure", "Ensemble", "SwmError", "EARTH", "c_grid_names", "MESHES",
 ]
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -90,9 +90,27 @@ def _check_c_f64(a, shape):
         raise ValueError(f"asynchronous transfers need C-contiguous float64 arrays of shape {shape}")
 
 
+MESHES = {"p": _abi.SWM_MESH_P, "u": _abi.SWM_MESH_U, "v": _abi.SWM_MESH_V, "q": _abi.SWM_MESH_Q}
+
+
+def c_grid_names(sbp_order: int = 42) -> dict:
+    """Operator names of the C-grid family (the &shallow_water_model_c
+    namelist, namelist_swm:80-102) at SBP order 21 or 42."""
+    o = int(sbp_order)
+    return {"div_op_name": f"divergence_c_sbp{o}", "grad_op_name": f"gradient_c_sbp{o}",
+            "curl_op_name": f"curl_c_sbp{o}", "coriolis_op_name": f"coriolis_Cgrid_sbp{o}",
+            "KE_op_name": f"KE_Cgrid_sbp{o}", "co2contra_op_name": f"co2contra_c_sbp{o}",
+            "massflux_op_name": f"massflux_c_sbp{o}", "quadrature_name": f"SBP_C{o}_quadrature"}
+
+
 class OperatorSWM:
     """operator_swm_t on one GPU: domain geometry, the vector-invariant RHS,
-    its cube-edge syncs, the fused RK4 driver and FP64 diagnostics."""
+    its cube-edge syncs, the fused RK4 driver and FP64 diagnostics.
+
+    The staggering follows the operator names: the Ah family (default) keeps
+    h, u, v on the (N+1) x (N+1) nodes; the C family (c_grid_names) keeps h
+    on the N x N cell centres, u on the x-faces and v on the y-faces
+    (shapes in mesh_shape / state_shapes)."""
 
     def __init__(self, config: ModelConfig | None = None, **kw):
         if config is None:
@@ -113,7 +131,19 @@ class OperatorSWM:
         self._h = h
         self.N = config.N
         self.n = config.N + 1
-        self.shape = (6, self.n, self.n)
+        self.staggering = "C" if self._L.swm_ctx_grid(h) == _abi.SWM_GRID_C else "Ah"
+        self._mesh_shapes = {}
+        for name, m in MESHES.items():
+            nx, ny = ctypes.c_int(), ctypes.c_int()
+            _abi.check(self._L.swm_mesh_dims(h, m, ctypes.byref(nx), ctypes.byref(ny)), h)
+            self._mesh_shapes[name] = (6, ny.value, nx.value)
+        # host shape of h, u and v (all (6, N+1, N+1) on the Ah grid)
+        self.state_shapes = tuple(self._mesh_shapes[k] for k in ("p", "u", "v"))
+        self.shape = self._mesh_shapes["p"]
+
+    def mesh_shape(self, mesh: str = "p") -> tuple:
+        """Host array shape (6, ny, nx) of a field on mesh p, u, v or q."""
+        return self._mesh_shapes[mesh]
 
     # lifetime -----------------------------------------------------------
     def close(self):
@@ -149,8 +179,8 @@ class OperatorSWM:
     def create_stvec(self) -> "StvecSWM":
         return StvecSWM(self)
 
-    def create_field(self) -> "GridField":
-        return GridField(self)
+    def create_field(self, mesh: str = "p") -> "GridField":
+        return GridField(self, mesh)
 
     def set_orography(self, hs):
         hs = _host(hs, self.shape)
@@ -279,8 +309,7 @@ class StvecSWM:
         return StvecSWM(self.op, _similar_to=self)
 
     def upload(self, h, u, v):
-        sh = self.op.shape
-        h, u, v = (_host(a, sh) for a in (h, u, v))
+        h, u, v = (_host(a, sh) for a, sh in zip((h, u, v), self.op.state_shapes))
         self.op._check(self.op._L.swm_state_upload(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
         self.op.synchronize()
 
@@ -296,9 +325,8 @@ class StvecSWM:
         self.op._check(self.op._L.swm_state_upload_async(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
 
     def download(self, out=None):
-        sh = self.op.shape
         if out is None:
-            out = tuple(np.empty(sh) for _ in range(3))
+            out = tuple(np.empty(sh) for sh in self.op.state_shapes)
         self.op._check(self.op._L.swm_state_download(self.op._h, self._h, *(_ptr(a) for a in out)))
         return out
 
@@ -352,12 +380,14 @@ class StvecSWM:
 
 
 class GridField:
-    """grid_field_t: one FP64 field on the device."""
+    """grid_field_t: one FP64 field on the device, on mesh p, u, v or q."""
 
-    def __init__(self, op: OperatorSWM):
+    def __init__(self, op: OperatorSWM, mesh: str = "p"):
         self.op = op
+        self.mesh = mesh
+        self.shape = op.mesh_shape(mesh)
         h = ctypes.c_void_p()
-        op._check(op._L.swm_field_create(op._h, ctypes.byref(h)))
+        op._check(op._L.swm_field_create_mesh(op._h, MESHES[mesh], ctypes.byref(h)))
         self._h = h
 
     def close(self):
@@ -372,12 +402,12 @@ class GridField:
             pass
 
     def upload(self, a):
-        a = _host(a, self.op.shape)
+        a = _host(a, self.shape)
         self.op._check(self.op._L.swm_field_upload(self.op._h, self._h, _ptr(a)))
         self.op.synchronize()
 
     def download(self) -> np.ndarray:
-        out = np.empty(self.op.shape)
+        out = np.empty(self.shape)
         self.op._check(self.op._L.swm_field_download(self.op._h, self._h, _ptr(out)))
         return out
 

@@ -21,6 +21,11 @@ SWM_E_IO = -6
 SWM_FP64_PLAIN = 0
 SWM_FP32_FUSED = 1
 
+# staggering of a context and its meshes (swm_ctx_grid, swm_mesh_dims)
+SWM_GRID_AH = 0
+SWM_GRID_C = 1
+SWM_MESH_P, SWM_MESH_U, SWM_MESH_V, SWM_MESH_Q = 0, 1, 2, 3
+
 # largest N that swm_sync_scalar_static accepts
 SWM_SYNC_STATIC_MAX_N = 1024
 
@@ -48,7 +53,8 @@ EXPORTS = (
     "swm_laplace", "swm_latlon_create", "swm_latlon_destroy", "swm_latlon_regrid_field",
     "swm_latlon_regrid_vector", "swm_latlon_regrid_state", "swm_latlon_write", "swm_paneled_write",
     "swm_tune_stage", "swm_get_stage_shape", "swm_set_stage_shape", "swm_work_split", "swm_ensemble_set_width",
-    "swm_ensemble_get_width", "swm_state_save", "swm_state_load",
+    "swm_ensemble_get_width", "swm_state_save", "swm_state_load", "swm_ctx_grid", "swm_mesh_dims",
+    "swm_field_create_mesh",
 )
 
 
@@ -148,6 +154,9 @@ def load(build_if_missing: bool = True):
     sig("swm_state_load", I, VP, VP, C, _D)
     sig("swm_diagnostics", I, VP, VP, _D)
     sig("swm_field_create", I, VP, PP)
+    sig("swm_field_create_mesh", I, VP, I, PP)
+    sig("swm_ctx_grid", I, VP)
+    sig("swm_mesh_dims", I, VP, I, ctypes.POINTER(I), ctypes.POINTER(I))
     sig("swm_field_free", None, VP)
     sig("swm_field_upload", I, VP, VP, _D)
     sig("swm_field_download", I, VP, VP, _D)

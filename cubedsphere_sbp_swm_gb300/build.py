@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas"
               "--expt-relaxed-constexpr"]
 SOURCES = ["swm_abi.cu", "swm_ops.cu", "swm_stage_f64.cu", "swm_stage_f32.cu", "swm_adjoint.cu",
            "swm_diffusion.cu", "swm_output.cu", "swm_stage_f32_w64.cu", "swm_stage_f32_w96.cu", "swm_stage_f32_w128.cu",
-           "swm_stage_f32_w160.cu", "swm_stage_f32_w192.cu"]
+           "swm_stage_f32_w160.cu", "swm_stage_f32_w192.cu", "swm_cgrid.cu"]
 
 
 def _nvcc() -> str:

@@ -2,6 +2,8 @@
 // RK4 time scheme), device states and fields, the fused RK4 driver replayed
 // as a CUDA graph, the unfused FP64 operator path and FP64 diagnostics.
 #include "../../include/swm_gpu.h"
+#include "swm_cgrid.h"
+#include "swm_cube.h"
 #include "swm_launch.h"
 #include "swm_ops.cuh"
 
@@ -29,53 +31,13 @@ thread_local std::string g_err;  // errors without a context
 constexpr double kPi = 3.141592653589793238462643383279502884;
 
 // ---------------------------------------------------------------------------
-// Cube topology on the host: which neighbour side holds the duplicated nodes
-// of each panel side, and the component map of the vector exchange.  Follows
-// transform_index / find_basis_orientation of the reference
-// (topology/cubed_sphere_topology_mod.f90:80-239) and the halo placement of
+// Which neighbour side holds the duplicated nodes of each panel side, and the
+// component map of the vector exchange: the halo placement of
 // parallel/exchange_factory_mod.f90:157-299 (the neighbour's copy of a shared
-// node sits in the 1-wide halo ring).
+// node sits in the 1-wide halo ring), through the index map of swm_cube.h.
 // ---------------------------------------------------------------------------
-const int kEX[6][3] = {{-1, 0, 0}, {0, 0, -1}, {1, 0, 0}, {0, 0, 1}, {1, 0, 0}, {1, 0, 0}};
-const int kEY[6][3] = {{0, 1, 0}, {0, 1, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, -1}};
-const int kN[6][3] = {{0, 0, 1}, {-1, 0, 0}, {0, 0, -1}, {1, 0, 0}, {0, 1, 0}, {0, -1, 0}};
-const int kR[6][3] = {{1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 1, 1}};
-
-int dot3(const int* a, const int* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-
-// frame of target panel pt unfolded across its edge with source panel ps
-void unfolded_frame(int ps, int pt, int nx, int exl[3], int eyl[3], int rl[3], int sh[2]) {
-  const int dr = dot3(kEX[pt], kN[ps]), db = dot3(kEY[pt], kN[ps]);
-  for (int c = 0; c < 3; ++c) {
-    if (dr == -1) { exl[c] = kN[pt][c]; eyl[c] = kEY[pt][c]; rl[c] = kR[pt][c] + kEX[pt][c]; }
-    else if (dr == 1) { exl[c] = -kN[pt][c]; eyl[c] = kEY[pt][c]; rl[c] = kR[pt][c] + kN[pt][c]; }
-    else if (db == 1) { exl[c] = kEX[pt][c]; eyl[c] = -kN[pt][c]; rl[c] = kR[pt][c] + kN[pt][c]; }
-    else if (db == -1) { exl[c] = kEX[pt][c]; eyl[c] = kN[pt][c]; rl[c] = kR[pt][c] + kEY[pt][c]; }
-    else { exl[c] = -kEX[pt][c]; eyl[c] = kEY[pt][c]; rl[c] = kR[pt][c] + kEX[pt][c] + kN[pt][c]; }
-  }
-  if (dr == -1) { sh[0] = nx; sh[1] = 0; }
-  else if (dr == 1) { sh[0] = -nx; sh[1] = 0; }
-  else if (db == 1) { sh[0] = 0; sh[1] = -nx; }
-  else if (db == -1) { sh[0] = 0; sh[1] = nx; }
-  else { sh[0] = 2 * nx; sh[1] = 0; }
-}
-
-void map_index(int ps, int is, int js, int pt, int n, int& it, int& jt) {
-  int exl[3], eyl[3], rl[3], sh[2], d[3];
-  unfolded_frame(ps, pt, n, exl, eyl, rl, sh);
-  for (int c = 0; c < 3; ++c) d[c] = kR[ps][c] - rl[c];
-  it = (is - 1) * dot3(kEX[ps], exl) + (js - 1) * dot3(kEY[ps], exl) + (n - 1) * dot3(d, exl) + 1 + sh[0];
-  jt = (is - 1) * dot3(kEX[ps], eyl) + (js - 1) * dot3(kEY[ps], eyl) + (n - 1) * dot3(d, eyl) + 1 + sh[1];
-}
-
-void orientation(int ps, int pt, int& istep, int& jstep, int& dim_i) {
-  int exl[3], eyl[3], rl[3], sh[2];
-  unfolded_frame(ps, pt, 2, exl, eyl, rl, sh);
-  const int ex_ex = dot3(kEX[ps], exl), ex_ey = dot3(kEY[ps], exl);
-  const int ey_ex = dot3(kEX[ps], eyl), ey_ey = dot3(kEY[ps], eyl);
-  if (ex_ex != 0) { dim_i = 1; istep = ex_ex; jstep = ey_ey; }
-  else { dim_i = 0; istep = ex_ey; jstep = ey_ex; }
-}
+using cube::map_index;
+using cube::orientation;
 
 bool build_topology(Topology& tp, std::string& why) {
   const int n = 9;  // the map is linear along a side; any size resolves it
@@ -91,7 +53,7 @@ bool build_topology(Topology& tp, std::string& why) {
         for (int is = 1; is <= n; ++is) {
           if (is != 1 && is != n && js != 1 && js != n) continue;
           int it, jt;
-          map_index(q, is, js, p, n, it, jt);
+          map_index(q, is, js, p, n, n, it, jt);
           int side = -1, k = -1;
           if (it == 0 && jt >= 1 && jt <= n) { side = SIDE_L; k = jt - 1; }
           else if (it == n + 1 && jt >= 1 && jt <= n) { side = SIDE_R; k = jt - 1; }
@@ -154,6 +116,7 @@ struct swm_state {
 struct swm_field {
   swm_ctx* ctx;
   double* p;
+  int mesh;  // SWM_MESH_*: the staggered mesh of a C-grid field (all one mesh on the Ah grid)
 };
 
 // Lat-lon interpolator of one context (regrid_factory_mod.f90:9-301): device
@@ -240,6 +203,9 @@ struct swm_ctx {
   cudaEvent_t xready[2][2] = {}, xdone[2][2] = {};
   int xnext[2] = {0, 0};
   cudaGraphExec_t ad_graph = nullptr;   // rk4 adjoint step of the last (x, lx, dt)
+  // C-grid contexts (the &shallow_water_model_c operator family): the
+  // staggered-mesh operator; null on the Ah grid
+  CGrid* cg = nullptr;
   const void* ad_key[2] = {nullptr, nullptr};
   double ad_dt = 0.0;
 };
@@ -561,6 +527,42 @@ int check_field(swm_ctx* ctx, const swm_field* f) {
   return SWM_OK;
 }
 
+// Entry points of the Ah-grid path only: refuse a C-grid context.
+#define AH_ONLY(ctx_, what_)                                                              \
+  do {                                                                                    \
+    if ((ctx_) && (ctx_)->cg)                                                             \
+      return fail((ctx_), SWM_E_UNSUPPORTED, std::string(what_) + " is not provided on the C grid"); \
+  } while (0)
+
+// Points per panel row / column of a mesh of the context.
+void mesh_dims(const swm_ctx* ctx, int mesh, int* nx, int* ny) {
+  if (ctx->cg) { cgrid_mesh_dims(ctx->cg, mesh, nx, ny); return; }
+  *nx = ctx->n; *ny = ctx->n;
+}
+
+int sync_check(swm_ctx* ctx, cudaStream_t st);
+
+// Dense host field of a C-grid mesh (i fastest, then j, then panel) to or
+// from its pitched device field: one 2-D copy per panel, then a sync.
+int c_copy(swm_ctx* ctx, int mesh, double* dev, const double* host_in, double* host_out) {
+  int nx, ny;
+  mesh_dims(ctx, mesh, &nx, &ny);
+  const size_t w = sizeof(double) * nx, dp = sizeof(double) * ctx->P;
+  for (int p = 0; p < 6; ++p) {
+    double* d = dev + (long long)p * ctx->ps;
+    if (host_in)
+      CK(cudaMemcpy2DAsync(d, dp, host_in + (size_t)p * nx * ny, w, w, ny, cudaMemcpyHostToDevice, ctx->st), "upload");
+    else
+      CK(cudaMemcpy2DAsync(host_out + (size_t)p * nx * ny, w, d, dp, w, ny, cudaMemcpyDeviceToHost, ctx->st), "download");
+  }
+  return sync_check(ctx, ctx->st);
+}
+int check_mesh(swm_ctx* ctx, const swm_field* f, int mesh, const char* what) {
+  if (ctx->cg && f->mesh != mesh)
+    return fail(ctx, SWM_E_INVALID, std::string(what) + ": field on the wrong C-grid mesh");
+  return SWM_OK;
+}
+
 double* tmpf(swm_ctx* c, int k) { return c->tmp + (long long)k * c->g64.fs; }
 
 // Work split of the fused stage kernel for consumer width cols (TMA kernel;
@@ -788,6 +790,7 @@ void free_ctx(swm_ctx* c) {
   // hsT aliases hs64 in FP64 contexts: free each allocation once
   void* hsT = (c->hsT == (void*)c->hs64) ? nullptr : c->hsT;
   if (c->ad_graph) cudaGraphExecDestroy(c->ad_graph);
+  cgrid_destroy(c->cg);
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge2, c->edge64, c->ya, c->yb, c->acc,
                   c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
@@ -852,23 +855,45 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   if (!cfg || !out) return fail(nullptr, SWM_E_INVALID, "null argument");
   *out = nullptr;
   int od = 0, og = 0, oc = 0, oq = 0;
-  if (!div_op_name || !name_order(div_op_name, "divergence_ah", "_sbp", od))
+  // The C-grid family of &shallow_water_model_c (namelist_swm:80-102), all
+  // operators of one SBP order: divergence_c_sbpNN, gradient_c_sbpNN,
+  // curl_c_sbpNN, coriolis_Cgrid_sbpNN, KE_Cgrid_sbpNN, co2contra_c_sbpNN,
+  // massflux_c_sbpNN, SBP_CNN_quadrature with NN 21 or 42.
+  int cgrid_order = 0;
+  if (div_op_name && std::strncmp(div_op_name, "divergence_c_sbp", 16) == 0) {
+    if (!name_order(div_op_name, "divergence_c_sbp", "", od) || (od != 21 && od != 42))
+      return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported div operator: ") + div_op_name);
+    const std::string o = std::to_string(od);
+    const char* want[7] = {grad_op_name, curl_op_name, coriolis_op_name, KE_op_name, co2contra_op_name,
+                           massflux_op_name, quadrature_name};
+    const std::string need[7] = {"gradient_c_sbp" + o, "curl_c_sbp" + o, "coriolis_Cgrid_sbp" + o, "KE_Cgrid_sbp" + o,
+                                 "co2contra_c_sbp" + o, "massflux_c_sbp" + o, "SBP_C" + o + "_quadrature"};
+    for (int k = 0; k < 7; ++k)
+      if (!want[k] || need[k] != want[k])
+        return fail(nullptr, SWM_E_UNSUPPORTED,
+                    std::string("C-grid family needs ") + need[k] + ", got " + (want[k] ? want[k] : "(null)"));
+    if (cfg->precision != SWM_FP64_PLAIN)
+      return fail(nullptr, SWM_E_UNSUPPORTED, "the C-grid operator family is FP64 only");
+    cgrid_order = od;
+  } else if (!div_op_name || !name_order(div_op_name, "divergence_ah", "_sbp", od))
     return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported div operator: ") + (div_op_name ? div_op_name : "(null)"));
-  if (!grad_op_name || !name_order(grad_op_name, "gradient_ah", "_sbp_ecs", og))
+  if (!cgrid_order && (!grad_op_name || !name_order(grad_op_name, "gradient_ah", "_sbp_ecs", og)))
     return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported grad operator: ") + (grad_op_name ? grad_op_name : "(null)"));
-  if (!curl_op_name || !name_order(curl_op_name, "curl_divergence_ah", "_sbp", oc))
+  if (!cgrid_order && (!curl_op_name || !name_order(curl_op_name, "curl_divergence_ah", "_sbp", oc)))
     return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported curl operator: ") + (curl_op_name ? curl_op_name : "(null)"));
-  if (od == 21 || oc == 21)
-    return fail(nullptr, SWM_E_UNSUPPORTED, "divergence_ah21_sbp does not exist in the operator family");
-  if (od != og || od != oc)
-    return fail(nullptr, SWM_E_UNSUPPORTED, "fused path needs div, grad and curl of one SBP order");
-  auto eq = [](const char* a, const char* b) { return a && std::strcmp(a, b) == 0; };
-  if (!eq(coriolis_op_name, "coriolis_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported coriolis operator");
-  if (!eq(KE_op_name, "KE_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported KE operator");
-  if (!eq(co2contra_op_name, "co2contra_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported co2contra operator");
-  if (!eq(massflux_op_name, "massflux_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported massflux operator");
-  if (!quadrature_name || !name_order(quadrature_name, "SBP_Ah", "_quadrature", oq) || oq == 43)
-    return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported quadrature");
+  if (!cgrid_order) {
+    if (od == 21 || oc == 21)
+      return fail(nullptr, SWM_E_UNSUPPORTED, "divergence_ah21_sbp does not exist in the operator family");
+    if (od != og || od != oc)
+      return fail(nullptr, SWM_E_UNSUPPORTED, "fused path needs div, grad and curl of one SBP order");
+    auto eq = [](const char* a, const char* b) { return a && std::strcmp(a, b) == 0; };
+    if (!eq(coriolis_op_name, "coriolis_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported coriolis operator");
+    if (!eq(KE_op_name, "KE_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported KE operator");
+    if (!eq(co2contra_op_name, "co2contra_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported co2contra operator");
+    if (!eq(massflux_op_name, "massflux_colocated")) return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported massflux operator");
+    if (!quadrature_name || !name_order(quadrature_name, "SBP_Ah", "_quadrature", oq) || oq == 43)
+      return fail(nullptr, SWM_E_UNSUPPORTED, "unsupported quadrature");
+  }
   if (cfg->N < 16 || cfg->N > 8190) return fail(nullptr, SWM_E_INVALID, "N must be in [16, 8190]");
   if (cfg->precision != SWM_FP64_PLAIN && cfg->precision != SWM_FP32_FUSED)
     return fail(nullptr, SWM_E_UNSUPPORTED, "unknown precision");
@@ -927,6 +952,22 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   CKC(cudaMallocHost(&ctx->hres, sizeof(double) * 16), "alloc host");
   CKC(cudaMallocHost(&ctx->herr, sizeof(int)), "alloc host");
   *ctx->herr = 0;
+  CKC(cudaMalloc(&ctx->derr, sizeof(int)), "alloc");
+  CKC(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st), "memset");
+  if (cgrid_order) {
+    // the staggered-mesh operator; the Ah stage kernel, metric and
+    // quadrature weights are not set up
+    ctx->order = cgrid_order;
+    int rc = cgrid_create(ctx->g64, ctx->N, cgrid_order, cfg->radius, cfg->grav, cfg->omega, cfg->rotation_axis,
+                          ctx->st, &ctx->cg, why);
+    if (rc) {
+      free_ctx(ctx);
+      return fail(nullptr, rc == 3 ? SWM_E_NOMEM : rc == 2 ? SWM_E_CUDA : SWM_E_INVALID, why);
+    }
+    CKC(cudaStreamSynchronize(ctx->st), "sync");
+    *out = ctx;
+    return SWM_OK;
+  }
   CKC(ctx->prec == SWM_FP32_FUSED ? prepare_stage<float>(od, &ctx->shape)
                                   : prepare_stage<double>(od, &ctx->shape),
       "stage kernel attributes");
@@ -935,8 +976,6 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     return fail(nullptr, SWM_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   }
   CKC(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device), "SM count");
-  CKC(cudaMalloc(&ctx->derr, sizeof(int)), "alloc");
-  CKC(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st), "memset");
   if (int rc = stage_layout(ctx, ctx->shape.cols)) {
     why = ctx->err;
     free_ctx(ctx);
@@ -994,6 +1033,15 @@ int swm_ctx_synchronize(swm_ctx* ctx) {
 void* swm_ctx_stream(swm_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
 size_t swm_ctx_npts(const swm_ctx* ctx) { return ctx ? (size_t)6 * ctx->n * ctx->n : 0; }
 
+int swm_ctx_grid(const swm_ctx* ctx) { return !ctx ? -1 : ctx->cg ? SWM_GRID_C : SWM_GRID_AH; }
+
+int swm_mesh_dims(const swm_ctx* ctx, int mesh, int* nx, int* ny) {
+  if (!ctx || !nx || !ny) return fail(nullptr, SWM_E_INVALID, "null argument");
+  if (mesh < SWM_MESH_P || mesh > SWM_MESH_Q) return fail(nullptr, SWM_E_INVALID, "unknown mesh");
+  mesh_dims(ctx, mesh, nx, ny);
+  return SWM_OK;
+}
+
 int swm_set_orography(swm_ctx* ctx, const double* hs) {
   if (!ctx || !hs) return fail(ctx, SWM_E_INVALID, "null argument");
   USE_DEVICE(ctx);
@@ -1001,7 +1049,11 @@ int swm_set_orography(swm_ctx* ctx, const double* hs) {
     CK(cudaMalloc(&ctx->hs64, sizeof(double) * ctx->fs), "alloc");
     CK(cudaMemsetAsync(ctx->hs64, 0, sizeof(double) * ctx->fs, ctx->st), "memset");
   }
-  if (int rc = put_field(ctx, ctx->hs64, hs)) return rc;
+  if (ctx->cg) {
+    if (int rc = c_copy(ctx, SWM_MESH_P, ctx->hs64, hs, nullptr)) return rc;
+  } else if (int rc = put_field(ctx, ctx->hs64, hs)) {
+    return rc;
+  }
   if (ctx->prec == SWM_FP32_FUSED) {
     if (!ctx->hsT) CK(cudaMalloc(&ctx->hsT, sizeof(float) * ctx->fs), "alloc");
     CK(launch_to_f32(ctx->hs64, (float*)ctx->hsT, ctx->fs, ctx->st), "to f32");
@@ -1068,6 +1120,11 @@ int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* 
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
   USE_DEVICE(ctx);
   const double* src[3] = {h, u, v};
+  if (ctx->cg) {
+    for (int c = 0; c < 3; ++c)
+      if (int rc = c_copy(ctx, SWM_MESH_P + c, (double*)s->hi + c * ctx->fs, src[c], nullptr)) return rc;
+    return SWM_OK;
+  }
   return put_packed(ctx, s, src, cudaMemcpyHostToDevice);
 }
 
@@ -1077,6 +1134,11 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
   USE_DEVICE(ctx);
   double* dst[3] = {h, u, v};
+  if (ctx->cg) {
+    for (int c = 0; c < 3; ++c)
+      if (int rc = c_copy(ctx, SWM_MESH_P + c, (double*)s->hi + c * ctx->fs, nullptr, dst[c])) return rc;
+    return SWM_OK;
+  }
   if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
   if (int rc_ = sync_check(ctx, ctx->st)) return rc_;
   return SWM_OK;
@@ -1109,6 +1171,7 @@ extern "C" {
 
 int swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h, const double* u,
                            const double* v) {
+  AH_ONLY(ctx, "swm_state_upload_async");
   TraceRange trace_("swm_state_upload_async");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
@@ -1135,6 +1198,7 @@ int swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h, const do
 }
 
 int swm_state_download_async(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  AH_ONLY(ctx, "swm_state_download_async");
   TraceRange trace_("swm_state_download_async");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
@@ -1213,6 +1277,7 @@ int swm_update_s1v1s2v2(swm_ctx* ctx, swm_state* s, double s1, const swm_state* 
 }
 
 int swm_dot(swm_ctx* ctx, const swm_state* a, const swm_state* b, double* out) {
+  AH_ONLY(ctx, "swm_dot");
   if (int rc = check_state(ctx, a)) return rc;
   if (int rc = check_state(ctx, b)) return rc;
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
@@ -1252,6 +1317,11 @@ int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   if (int rc = check_state(ctx, vin)) return rc;
   if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
   USE_DEVICE(ctx);
+  if (ctx->cg) {
+    CK(cgrid_apply(ctx->cg, ctx->topo, ctx->edge64, ctx->hs64, (const double*)vin->hi, (double*)vout->hi, ctx->st),
+       "C-grid apply");
+    return SWM_OK;
+  }
   if (ctx->prec == SWM_FP64_PLAIN) {
     InstDev<double> I = base_inst<double>(ctx);
     I.in = (const double*)vin->hi; I.out = (double*)vout->hi;
@@ -1281,6 +1351,21 @@ int swm_apply_unfused(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
          *cor_u = tmpf(ctx, 8), *cor_v = tmpf(ctx, 9), *dv = tmpf(ctx, 10);
   const FieldGeom& g = ctx->g64;
   cudaStream_t st = ctx->st;
+  if (CGrid* c = ctx->cg) {
+    // the reference's operator sequence, one unfused operator at a time
+    CK(cgrid_co2contra(c, u, v, ut, vt, st), "co2contra");
+    CK(cgrid_massflux(c, h, ut, vt, hu, hv, st), "massflux");
+    CK(cgrid_ke(c, u, v, ut, vt, ke, st), "KE");
+    CK(launch_ke_update(g, ctx->cfg.grav, h, ctx->hs64, ke, st), "KE update");
+    CK(cgrid_grad(c, ke, gx, gy, st), "grad");
+    CK(cgrid_curl(c, ctx->topo, ctx->edge64, u, v, cu, st), "curl");
+    CK(cgrid_coriolis(c, hu, hv, h, cu, cor_u, cor_v, st), "coriolis");
+    CK(launch_axpby(fs, -1.0, gx, 1.0, cor_u, ou, st), "assign");
+    CK(launch_axpby(fs, -1.0, gy, 1.0, cor_v, ov, st), "assign");
+    CK(cgrid_div(c, hu, hv, dv, st), "div");
+    CK(launch_axpby(fs, -1.0, dv, 0.0, nullptr, oh, st), "assign");
+    return SWM_OK;
+  }
   CK(launch_co2contra(g, ctx->m64, u, v, ut, vt, st), "co2contra");
   CK(launch_massflux(g, h, ut, vt, hu, hv, st), "massflux");
   CK(launch_ke(g, u, v, ut, vt, ke, st), "KE");
@@ -1332,6 +1417,10 @@ int graph_steps(swm_ctx* ctx, swm_state* v0, double dt, int kind, int nsteps, F 
 }
 
 int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
+  if (ctx->cg) {
+    CK(cgrid_rk4(ctx->cg, ctx->topo, ctx->edge64, ctx->hs64, (double*)v0->hi, dt, ctx->st), "C-grid RK4 step");
+    return SWM_OK;
+  }
   return ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);
 }
 
@@ -1551,6 +1640,7 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 
 int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
                       const char* hordiff_h_name, double h_diff_coeff) {
+  AH_ONLY(ctx, "swm_diffusion_set");
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   const int uv = hordiff_uv_order(hordiff_uv_name), h = hordiff_h_order(hordiff_h_name);
   if (!uv || !h)
@@ -1579,6 +1669,7 @@ int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_
 }
 
 int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
+  AH_ONLY(ctx, "swm_apply_diffusion");
   TraceRange trace_("swm_apply_diffusion");
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
@@ -1598,6 +1689,7 @@ int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
 }
 
 int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  AH_ONLY(ctx, "swm_diffusion_step");
   TraceRange trace_("swm_diffusion_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
@@ -1608,6 +1700,7 @@ int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 }
 
 int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
+  AH_ONLY(ctx, "swm_model_step");
   TraceRange trace_("swm_model_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
@@ -1622,6 +1715,7 @@ int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 }
 
 int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_order) {
+  AH_ONLY(ctx, "swm_laplace");
   TraceRange trace_("swm_laplace");
   if (int rc = check_field(ctx, out)) return rc;
   if (int rc = check_field(ctx, in)) return rc;
@@ -1637,6 +1731,7 @@ int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_or
 }
 
 int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
+  AH_ONLY(ctx, "swm_diagnostics");
   TraceRange trace_("swm_diagnostics");
   if (int rc = check_state(ctx, s)) return rc;
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
@@ -1663,10 +1758,13 @@ int swm_diagnostics(swm_ctx* ctx, const swm_state* s, double out[7]) {
 }
 
 // ---------------------------------------------------------------- fields
-int swm_field_create(swm_ctx* ctx, swm_field** out) {
+int swm_field_create(swm_ctx* ctx, swm_field** out) { return swm_field_create_mesh(ctx, SWM_MESH_P, out); }
+
+int swm_field_create_mesh(swm_ctx* ctx, int mesh, swm_field** out) {
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
+  if (mesh < SWM_MESH_P || mesh > SWM_MESH_Q) return fail(ctx, SWM_E_INVALID, "unknown mesh");
   USE_DEVICE(ctx);
-  swm_field* f = new swm_field{ctx, nullptr};
+  swm_field* f = new swm_field{ctx, nullptr, mesh};
   cudaError_t e = cudaMalloc(&f->p, sizeof(double) * ctx->fs);
   if (e == cudaSuccess) e = cudaMemsetAsync(f->p, 0, sizeof(double) * ctx->fs, ctx->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
@@ -1695,6 +1793,7 @@ int swm_field_upload(swm_ctx* ctx, swm_field* f, const double* host) {
   if (int rc = check_field(ctx, f)) return rc;
   if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
   USE_DEVICE(ctx);
+  if (ctx->cg) return c_copy(ctx, f->mesh, f->p, host, nullptr);
   return put_field(ctx, f->p, host);
 }
 
@@ -1702,6 +1801,7 @@ int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
   if (int rc = check_field(ctx, f)) return rc;
   if (!host) return fail(ctx, SWM_E_INVALID, "null host array");
   USE_DEVICE(ctx);
+  if (ctx->cg) return c_copy(ctx, f->mesh, f->p, nullptr, host);
   const size_t bytes = sizeof(double) * 6 * (size_t)ctx->n * ctx->n;
   PackedFields pf{{(double*)mapped_host(host, bytes), nullptr, nullptr}};
   const bool staged = !pf.f[0];
@@ -1722,43 +1822,96 @@ int swm_field_download(swm_ctx* ctx, const swm_field* f, double* host) {
 
 int swm_op_co2contra(swm_ctx* ctx, swm_field* ut, swm_field* vt, const swm_field* u, const swm_field* v) {
   CHECK_FIELDS(ut, vt, u, v);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)ut, SWM_MESH_U), std::make_pair((const swm_field*)vt, SWM_MESH_V),
+                    std::make_pair(u, SWM_MESH_U), std::make_pair(v, SWM_MESH_V)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "co2contra")) return rc;
+    CK(cgrid_co2contra(ctx->cg, u->p, v->p, ut->p, vt->p, ctx->st), "co2contra");
+    return SWM_OK;
+  }
   CK(launch_co2contra(ctx->g64, ctx->m64, u->p, v->p, ut->p, vt->p, ctx->st), "co2contra");
   return SWM_OK;
 }
 int swm_op_massflux(swm_ctx* ctx, swm_field* hu, swm_field* hv, const swm_field* h, const swm_field* ut, const swm_field* vt) {
   CHECK_FIELDS(hu, hv, h, ut, vt);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)hu, SWM_MESH_U), std::make_pair((const swm_field*)hv, SWM_MESH_V),
+                    std::make_pair(h, SWM_MESH_P), std::make_pair(ut, SWM_MESH_U), std::make_pair(vt, SWM_MESH_V)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "massflux")) return rc;
+    CK(cgrid_massflux(ctx->cg, h->p, ut->p, vt->p, hu->p, hv->p, ctx->st), "massflux");
+    return SWM_OK;
+  }
   CK(launch_massflux(ctx->g64, h->p, ut->p, vt->p, hu->p, hv->p, ctx->st), "massflux");
   return SWM_OK;
 }
 int swm_op_ke(swm_ctx* ctx, swm_field* ke, const swm_field* u, const swm_field* v, const swm_field* ut, const swm_field* vt) {
   CHECK_FIELDS(ke, u, v, ut, vt);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)ke, SWM_MESH_P), std::make_pair(u, SWM_MESH_U),
+                    std::make_pair(v, SWM_MESH_V), std::make_pair(ut, SWM_MESH_U), std::make_pair(vt, SWM_MESH_V)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "KE")) return rc;
+    CK(cgrid_ke(ctx->cg, u->p, v->p, ut->p, vt->p, ke->p, ctx->st), "KE");
+    return SWM_OK;
+  }
   CK(launch_ke(ctx->g64, u->p, v->p, ut->p, vt->p, ke->p, ctx->st), "KE");
   return SWM_OK;
 }
 int swm_op_grad(swm_ctx* ctx, swm_field* gx, swm_field* gy, const swm_field* f) {
   CHECK_FIELDS(gx, gy, f);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)gx, SWM_MESH_U), std::make_pair((const swm_field*)gy, SWM_MESH_V),
+                    std::make_pair(f, SWM_MESH_P)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "grad")) return rc;
+    CK(cgrid_grad(ctx->cg, f->p, gx->p, gy->p, ctx->st), "grad");
+    return SWM_OK;
+  }
   return op_grad(ctx, f->p, gx->p, gy->p);
 }
 int swm_op_div(swm_ctx* ctx, swm_field* div, const swm_field* u, const swm_field* v) {
   CHECK_FIELDS(div, u, v);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)div, SWM_MESH_P), std::make_pair(u, SWM_MESH_U),
+                    std::make_pair(v, SWM_MESH_V)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "div")) return rc;
+    CK(cgrid_div(ctx->cg, u->p, v->p, div->p, ctx->st), "div");
+    return SWM_OK;
+  }
   return op_div(ctx, u->p, v->p, div->p);
 }
 int swm_op_curl(swm_ctx* ctx, swm_field* curl, const swm_field* u, const swm_field* v) {
   CHECK_FIELDS(curl, u, v);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)curl, SWM_MESH_Q), std::make_pair(u, SWM_MESH_U),
+                    std::make_pair(v, SWM_MESH_V)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "curl")) return rc;
+    CK(cgrid_curl(ctx->cg, ctx->topo, ctx->edge64, u->p, v->p, curl->p, ctx->st), "curl");
+    return SWM_OK;
+  }
   return op_curl(ctx, u->p, v->p, curl->p);
 }
 int swm_op_coriolis(swm_ctx* ctx, swm_field* cor_u, swm_field* cor_v, const swm_field* hu, const swm_field* hv,
                     const swm_field* h, const swm_field* curl) {
   CHECK_FIELDS(cor_u, cor_v, hu, hv, h, curl);
+  if (ctx->cg) {
+    for (auto fm : {std::make_pair((const swm_field*)cor_u, SWM_MESH_U), std::make_pair((const swm_field*)cor_v, SWM_MESH_V),
+                    std::make_pair(hu, SWM_MESH_U), std::make_pair(hv, SWM_MESH_V), std::make_pair(h, SWM_MESH_P),
+                    std::make_pair(curl, SWM_MESH_Q)})
+      if (int rc = check_mesh(ctx, fm.first, fm.second, "coriolis")) return rc;
+    CK(cgrid_coriolis(ctx->cg, hu->p, hv->p, h->p, curl->p, cor_u->p, cor_v->p, ctx->st), "coriolis");
+    return SWM_OK;
+  }
   CK(launch_coriolis(ctx->g64, ctx->m64, hu->p, hv->p, h->p, curl->p, cor_u->p, cor_v->p, ctx->st), "coriolis");
   return SWM_OK;
 }
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f) {
   CHECK_FIELDS(f);
+  // on the C grid the corner mesh is the one with duplicated edge points
+  if (int rc = check_mesh(ctx, f, SWM_MESH_Q, "sync_scalar")) return rc;
   CK(launch_sync_scalar(ctx->g64, ctx->topo, f->p, ctx->edge64, ctx->st), "sync");
   return SWM_OK;
 }
 int swm_sync_vector_cov(swm_ctx* ctx, swm_field* gx, swm_field* gy) {
+  AH_ONLY(ctx, "swm_sync_vector_cov");
   CHECK_FIELDS(gx, gy);
   CK(launch_sync_vector(ctx->g64, ctx->topo, ctx->qw, gx->p, gy->p, ctx->edge64, ctx->st), "sync");
   return SWM_OK;
@@ -1766,12 +1919,17 @@ int swm_sync_vector_cov(swm_ctx* ctx, swm_field* gx, swm_field* gy) {
 int swm_quadrature_mass(swm_ctx* ctx, const swm_field* f, double* out) {
   CHECK_FIELDS(f);
   if (!out) return fail(ctx, SWM_E_INVALID, "null output");
+  if (ctx->cg) {
+    CK(cgrid_mass(ctx->cg, f->mesh, f->p, ctx->dres, ctx->st), "C-grid quadrature");
+    return fetch_results(ctx, 1, out);
+  }
   if (int rc = reduce(ctx, 1, f->p, nullptr, 0)) return rc;
   return fetch_results(ctx, 1, out);
 }
 
 // ---------------------------------------------------------------- static scratch
 int swm_sync_scalar_static(swm_ctx* ctx, swm_field* f) {
+  AH_ONLY(ctx, "swm_sync_scalar_static");
   CHECK_FIELDS(f);
   if (ctx->N > SWM_SYNC_STATIC_MAX_N) {
     char m[160];
@@ -2524,12 +2682,14 @@ void free_adjoint(swm_adjoint* adj) {
 extern "C" {
 
 int swm_apply_tl(swm_ctx* ctx, const swm_state* y, const swm_state* dx, swm_state* dk) {
+  AH_ONLY(ctx, "swm_apply_tl");
   TraceRange trace_("swm_apply_tl");
   if (int rc = check_tl_args(ctx, y, dx, dk, true)) return rc;
   return tl_apply(ctx, (const double*)y->hi, (const double*)dx->hi, (double*)dk->hi);
 }
 
 int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk, swm_state* lx) {
+  AH_ONLY(ctx, "swm_apply_ad");
   TraceRange trace_("swm_apply_ad");
   if (int rc = check_tl_args(ctx, y, lk, lx, false)) return rc;
   if (ctx->prec == SWM_FP32_FUSED) {
@@ -2540,12 +2700,14 @@ int swm_apply_ad(swm_ctx* ctx, const swm_state* y, const swm_state* lk, swm_stat
 }
 
 int swm_rk4_tl(swm_ctx* ctx, const swm_state* x, swm_state* dx, double dt) {
+  AH_ONLY(ctx, "swm_rk4_tl");
   TraceRange trace_("swm_rk4_tl");
   if (int rc = check_tl_args(ctx, x, dx, nullptr, true)) return rc;
   return rk4_tl(ctx, (const double*)x->hi, (double*)dx->hi, dt);
 }
 
 int swm_rk4_ad(swm_ctx* ctx, const swm_state* x, swm_state* lx, double dt) {
+  AH_ONLY(ctx, "swm_rk4_ad");
   TraceRange trace_("swm_rk4_ad");
   if (int rc = check_tl_args(ctx, x, lx, nullptr, false)) return rc;
   if (int rc = rk4_ad_graph(ctx, x->hi, lx->hi, dt)) return rc;
@@ -2553,6 +2715,7 @@ int swm_rk4_ad(swm_ctx* ctx, const swm_state* x, swm_state* lx, double dt) {
 }
 
 int swm_adjoint_create(swm_ctx* ctx, int nsteps, int nsnap, double dt, swm_adjoint** out) {
+  AH_ONLY(ctx, "swm_adjoint_create");
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
   if (nsteps < 1 || nsnap < 1 || !(dt > 0.0))
     return fail(ctx, SWM_E_INVALID, "need nsteps >= 1, nsnap >= 1 and dt > 0");
@@ -2631,6 +2794,7 @@ int swm_adjoint_counts(const swm_adjoint* adj, long* forward_steps, long* adjoin
 
 int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const double* u,
                             const double* v) {
+  AH_ONLY(ctx, "swm_state_upload_device");
   TraceRange trace_("swm_state_upload_device");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
@@ -2640,6 +2804,7 @@ int swm_state_upload_device(swm_ctx* ctx, swm_state* s, const double* h, const d
 }
 
 int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
+  AH_ONLY(ctx, "swm_state_download_device");
   TraceRange trace_("swm_state_download_device");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null device array");
@@ -2649,6 +2814,7 @@ int swm_state_download_device(swm_ctx* ctx, const swm_state* s, double* h, doubl
 }
 
 int swm_quadrature_weights(swm_ctx* ctx, double* w_host) {
+  AH_ONLY(ctx, "swm_quadrature_weights");
   if (!ctx || !w_host) return fail(ctx, SWM_E_INVALID, "null argument");
   USE_DEVICE(ctx);
   const int n = ctx->n;
@@ -2729,6 +2895,7 @@ extern "C" {
 
 int swm_latlon_create(swm_ctx* ctx, int nlon, int nlat, const char* interp_type,
                       const char* components_type, swm_latlon** out) {
+  AH_ONLY(ctx, "swm_latlon_create");
   if (!ctx || !out) return fail(ctx, SWM_E_INVALID, "null argument");
   *out = nullptr;
   int w = 0, contra = 0;
@@ -2863,6 +3030,7 @@ int swm_latlon_write(swm_ctx* ctx, swm_latlon* r, const swm_state* s, const char
 }
 
 int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const char* file, int rec_num) {
+  AH_ONLY(ctx, "swm_paneled_write");
   TraceRange trace_("swm_paneled_write");
   if (int rc = check_state(ctx, s)) return rc;
   if (component < 0 || component > 2 || !file) return fail(ctx, SWM_E_INVALID, "bad component or file");
@@ -2886,6 +3054,7 @@ int swm_paneled_write(swm_ctx* ctx, const swm_state* s, int component, const cha
 // ------------------------------------------------------------ tuning
 int swm_tune_stage(swm_ctx* ctx, const swm_state* s, double dt, int steps, int* cols_out,
                    int* seg_rows_out, int* grid_out, int* box_out, double* ms_out) {
+  AH_ONLY(ctx, "swm_tune_stage");
   TraceRange trace_("swm_tune_stage");
   if (int rc = check_state(ctx, s)) return rc;
   if (steps < 1 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or steps");
@@ -2976,6 +3145,7 @@ int swm_work_split(int N, int sbp_order, int cols, int target_units, int seg_row
 }
 
 int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* box, int* nunits) {
+  AH_ONLY(ctx, "swm_get_stage_shape");
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   if (cols) *cols = ctx->shape.cols;
   if (seg_rows) *seg_rows = ctx->seg_rows;
@@ -2986,6 +3156,7 @@ int swm_get_stage_shape(swm_ctx* ctx, int* cols, int* seg_rows, int* grid, int* 
 }
 
 int swm_set_stage_shape(swm_ctx* ctx, int cols, int seg_rows, int grid, int box) {
+  AH_ONLY(ctx, "swm_set_stage_shape");
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
   if (seg_rows < 0 || grid < 0) return fail(ctx, SWM_E_INVALID, "shape values must be >= 0");
   if (box < SWM_BOX_AUTO || box > SWM_BOX_WIDEST) return fail(ctx, SWM_E_INVALID, "unknown box mode");
@@ -3010,6 +3181,7 @@ struct StateFileHeader {
 static_assert(sizeof(StateFileHeader) == 64, "state file header is 64 bytes");
 
 int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double time) {
+  AH_ONLY(ctx, "swm_state_save");
   TraceRange trace_("swm_state_save");
   if (int rc = check_state(ctx, s)) return rc;
   if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");
@@ -3044,6 +3216,7 @@ int swm_state_save(swm_ctx* ctx, const swm_state* s, const char* path, double ti
 }
 
 int swm_state_load(swm_ctx* ctx, swm_state* s, const char* path, double* time) {
+  AH_ONLY(ctx, "swm_state_load");
   TraceRange trace_("swm_state_load");
   if (int rc = check_state(ctx, s)) return rc;
   if (!path || !*path) return fail(ctx, SWM_E_INVALID, "null path");

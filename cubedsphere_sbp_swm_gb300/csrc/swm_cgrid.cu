@@ -1,0 +1,852 @@
+// swm_cgrid.cu -- the C-grid SBP vector-invariant shallow-water operator on
+// the GPU (FP64): metric of the four staggered meshes, cross-halo tables, the
+// five kernels of one right-hand side, the RK4 stage epilogue and the SBP_C
+// quadrature.
+//
+// One right-hand side (operator_swm_mod.f90:61-113 with the C-grid operators)
+// is five passes over the panels plus the corner sync of the curl:
+//   centre_a  p points   J Qi12 times the other covariant component
+//                        interpolated to the centres (co2contra, first half)
+//   faces_a   u, v       contravariant components, mass fluxes h*u^i, J*flux
+//                        and the kinetic-energy densities J u u^i / 2
+//   curl      q points   staggered differences + SAT penalties, then the
+//                        Ah-type edge / corner average
+//   w2uv      u, v       the curl interpolated to the faces
+//   centre_b  p points   kinetic energy + g (h + hs), the divergence with its
+//                        SAT penalties (h tendency), the Coriolis terms
+//   faces_b   u, v       gradient with its SAT penalties + the Coriolis term
+//                        interpolated back (u, v tendencies)
+// The neighbours' points the SBP-SAT operators read across a panel edge come
+// straight from the neighbouring panel through a precomputed table (one GPU
+// holds all six panels, so the reference's halo exchange becomes an indexed
+// load).
+#include "swm_cgrid.h"
+#include "swm_cube.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <initializer_list>
+#include <vector>
+
+namespace swm {
+
+namespace {
+
+constexpr double kPiC = 3.141592653589793238462643383279502884;
+constexpr int kHaloDepth = 3;
+constexpr int kMassBlocks = 256;
+constexpr int kMassThreads = 256;
+
+// Staggered 1-D SBP operator (sbp_operator_mod.f90:12-38, sbp_apply
+// 152-228): left closure rows Ql[r*nw + m] over inputs m < last[r]; the
+// right block mirrors them (times rsign); interior stencil Qin over inputs
+// k+inshift .. k+inshift+w-1.  dnx = outputs - inputs.
+struct StagOp {
+  int ne, nw, inshift, dnx;
+  double rsign;
+  int last[4];
+  double Ql[24];
+  double Qin[4];
+};
+
+// The operators and SAT constants of one SBP order.
+struct COps {
+  StagOp wc2i, wi2c, dc2i, di2c;
+  int np;           // boundary projection length
+  double proj[3];   // boundary projection (left)
+  double pen_c[3];  // proj / A_centres: penalty of the divergence (at_center)
+  double a_i0;      // A_interfaces(1): penalty weight of the curl
+  double sq1;       // the gradient's first interface weight (7/18 at 4/2)
+};
+
+// Tables of the staggered operators (sbp_operators_collection_mod.f90:88-193
+// and sbp_factory_mod.f90:38-179): the same numbers as the reference.
+void fill_ops(int order, COps& o) {
+  auto set = [](StagOp& s, int ne, int nw, std::initializer_list<double> q, std::initializer_list<int> last,
+                std::initializer_list<double> in, int inshift, int dnx, double rsign) {
+    s = StagOp{};
+    s.ne = ne; s.nw = nw; s.inshift = inshift; s.dnx = dnx; s.rsign = rsign;
+    int k = 0;
+    for (double x : q) s.Ql[k++] = x;
+    k = 0;
+    for (int x : last) s.last[k++] = x;
+    k = 0;
+    for (double x : in) s.Qin[k++] = x;
+  };
+  o = COps{};
+  if (order == 42) {
+    set(o.wc2i, 4, 5,
+        {1.3630402181345285, -0.17804474904273135, -0.23303115631809243, 0.048035687226327554, 0.0,
+         0.46340770044238916, 0.4765661872892848, 0.15664452409426372, -0.09661841182593758, 0.0,
+         0.07545241951434666, 0.44794495248229815, 0.37775283649236274, 0.09884979151099299, 0.0,
+         -0.04413695843145285, -0.04040344754874627, 0.649837488701711, 0.4980831989686297, -0.06338028169014084},
+        {4, 4, 4, 5}, {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0}, -2, 1, 1.0);
+    set(o.wi2c, 4, 6,
+        {0.4892964885611128, 0.48123107353632727, 0.0696483872440123, -0.040175949341450676, 0.0, 0.0,
+         -0.07913099957454726, 0.6127279550862234, 0.5119370885511979, -0.045534044062872786, 0.0, 0.0,
+         -0.0869982983587545, 0.1691760860218048, 0.3626427230326682, 0.6151794893042863, -0.06, 0.0,
+         0.018680545032460714, -0.10869571330417979, 0.09884979151099299, 0.4911653767607321, 0.5625, -0.0625},
+        {4, 4, 5, 6}, {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0}, -1, -1, 1.0);
+    set(o.dc2i, 4, 5,
+        {-2.0, 3.0, -1.0, 0.0, 0.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0 / 24.0, -9.0 / 8.0, 9.0 / 8.0, -1.0 / 24.0, 0.0,
+         -1.0 / 71.0, 6.0 / 71.0, -83.0 / 71.0, 81.0 / 71.0, -3.0 / 71.0},
+        {3, 2, 4, 5}, {1.0 / 24.0, -9.0 / 8.0, 9.0 / 8.0, -1.0 / 24.0}, -2, 1, -1.0);
+    set(o.di2c, 3, 5,
+        {-79.0 / 78.0, 27.0 / 26.0, -1.0 / 26.0, 1.0 / 78.0, 0.0, 2.0 / 21.0, -9.0 / 7.0, 9.0 / 7.0, -2.0 / 21.0, 0.0,
+         1.0 / 75.0, 0.0, -27.0 / 25.0, 83.0 / 75.0, -1.0 / 25.0},
+        {4, 4, 5}, {1.0 / 24.0, -9.0 / 8.0, 9.0 / 8.0, -1.0 / 24.0}, -1, -1, -1.0);
+    o.np = 3;
+    const double proj[3] = {15.0 / 8.0, -5.0 / 4.0, 3.0 / 8.0};
+    const double ac[3] = {13.0 / 12.0, 7.0 / 8.0, 25.0 / 24.0};
+    for (int k = 0; k < 3; ++k) { o.proj[k] = proj[k]; o.pen_c[k] = proj[k] / ac[k]; }
+    o.a_i0 = 7.0 / 18.0;
+    o.sq1 = 7.0 / 18.0;
+  } else {
+    set(o.wc2i, 1, 1, {1.0}, {1}, {0.5, 0.5}, -1, 1, 1.0);
+    set(o.wi2c, 1, 2, {0.5, 0.5}, {2}, {0.5, 0.5}, 0, -1, 1.0);
+    set(o.dc2i, 1, 2, {-1.0, 1.0}, {2}, {-1.0, 1.0}, -1, 1, -1.0);
+    set(o.di2c, 1, 2, {-1.0, 1.0}, {2}, {-1.0, 1.0}, 0, -1, -1.0);
+    o.np = 2;
+    o.proj[0] = 1.5; o.proj[1] = -0.5;
+    o.pen_c[0] = 1.5 / 1.0; o.pen_c[1] = -0.5 / 1.0;
+    o.a_i0 = 0.5;
+    o.sq1 = 0.5;
+  }
+}
+
+// Metric fields (one pitched field each) and work fields of one context.
+enum { M_JP = 0, M_QI2P, M_FP, M_JU, M_QI1U, M_JV, M_QI3V, M_JQ, M_COUNT };
+enum { W_AP = 0, W_BP, W_UT, W_VT, W_HU, W_HV, W_GU, W_GV, W_KEU, W_KEV, W_CURL, W_FU, W_FV, W_KE,
+       W_CUP, W_CVP, W_COUNT };
+
+// kernel flags
+enum : int {
+  F_CO = 1,        // faces_a: contravariant components from the covariant ones
+  F_MF = 2,        // faces_a: mass fluxes
+  F_G = 4,         // faces_a: J * mass flux
+  F_KE = 8,        // faces_a: kinetic-energy densities; centre_b: kinetic energy
+  F_ADDGH = 16,    // centre_b: + g h + g hs
+  F_DIV = 32,      // centre_b: divergence
+  F_COR = 64,      // centre_b: Coriolis terms at the centres; faces_b: back to the faces
+  F_GRAD = 128,    // faces_b: gradient
+  F_SEP = 256,     // centre_b / faces_b: write the operator's own output, not a tendency
+};
+
+struct CArgs {
+  FieldGeom g;
+  int N, L, flags;
+  double hx, radius, grav;
+  COps ops;
+  const double *Jp, *Qi2p, *fp, *Ju, *Qi1u, *Jv, *Qi3v, *Jq;
+  const int* halo;
+  // inputs
+  const double *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
+  // intermediate and unfused outputs
+  double *Ap, *Bp, *ut, *vt, *hu, *hv, *Gu, *Gv, *KEu, *KEv, *curl, *fu, *fv, *KE, *cup, *cvp;
+  double *o1, *o2;  // unfused outputs of centre_b (div) / faces_b (gx|cor_u, gy|cor_v)
+  // RK4 stage epilogue: mode 0 writes the tendency to tend, 1..4 the stages
+  // of rk4_mod.f90:20-42 (y0, Y, Kb, acc: 3 fields each, fs apart)
+  int mode;
+  double hdt, dt, c3, c6;
+  double *tend, *y0, *Y, *Kb, *acc;
+};
+
+__device__ __forceinline__ long long at(const FieldGeom& g, int p, int i, int j) {
+  return (long long)p * g.ps + (long long)j * g.P + i;
+}
+
+// sbp_apply for output k of nout outputs over a line f with stride st
+template <int W>
+__device__ __forceinline__ double stag_at(const StagOp& s, const double* __restrict__ f, long long st, int nout,
+                                          int k) {
+  double acc = 0.0;
+  if (k >= s.ne && k < nout - s.ne) {
+    const double* b = f + (long long)(k + s.inshift) * st;
+#pragma unroll
+    for (int t = 0; t < W; ++t) acc += s.Qin[t] * b[t * st];
+  } else if (k < s.ne) {
+    for (int m = 0; m < s.last[k]; ++m) acc += s.Ql[k * s.nw + m] * f[m * st];
+  } else {
+    const int nin = nout - s.dnx, r = nout - 1 - k;
+    for (int m = s.last[r] - 1; m >= 0; --m) acc += (s.rsign * s.Ql[r * s.nw + m]) * f[(long long)(nin - 1 - m) * st];
+  }
+  return acc;
+}
+
+// value of a neighbour's point in the cross halo: mesh 0 o, 1 u, 2 v; side 0
+// left, 1 right, 2 bottom, 3 top; depth d >= 1; k along the side.  f is the
+// field of the mesh, g the other component of a C vector.
+__device__ __forceinline__ double halo_at(const CArgs& a, int mesh, int side, int p, int d, int k,
+                                          const double* __restrict__ f, const double* __restrict__ g) {
+  const int c = __ldg(&a.halo[((((mesh * 4 + side) * 6 + p) * kHaloDepth + (d - 1)) * a.L) + k]);
+  const double x = ((c & 2) ? g : f)[c >> 2];
+  return (c & 1) ? -x : x;
+}
+
+__device__ __forceinline__ void rk_put(const CArgs& a, int comp, long long e, double k) {
+  const long long o = (long long)comp * a.g.fs + e;
+  switch (a.mode) {
+    case 0: a.tend[o] = k; break;
+    case 1: a.Kb[o] = k; a.Y[o] = 1.0 * a.y0[o] + a.hdt * k; break;
+    case 2: a.acc[o] = (a.y0[o] + a.c6 * a.Kb[o]) + a.c3 * k; a.Y[o] = 1.0 * a.y0[o] + a.hdt * k; break;
+    case 3: a.Kb[o] = k; a.Y[o] = 1.0 * a.y0[o] + a.dt * k; break;
+    default: a.y0[o] = (a.acc[o] + a.c3 * a.Kb[o]) + a.c6 * k; break;
+  }
+}
+
+#define SWM_C_INDEX(nx_, ny_)                                  \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;        \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;        \
+  const int p = blockIdx.z;                                   \
+  if (i >= (nx_) || j >= (ny_)) return;
+
+// co2contra_c_sbp (co2contra_Cgrid_mod.f90:292-437), first half: the other
+// covariant component interpolated to the centres times J Qi12 there.
+template <int ORD>
+__global__ void __launch_bounds__(256) centre_a_kernel(const __grid_constant__ CArgs a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N, N)
+  const FieldGeom& g = a.g;
+  const long long e = at(g, p, i, j);
+  const double jq = a.Jp[e] * a.Qi2p[e];
+  a.Ap[e] = jq * stag_at<W>(a.ops.wi2c, a.v + at(g, p, i, 0), g.P, N, j);
+  a.Bp[e] = jq * stag_at<W>(a.ops.wi2c, a.u + at(g, p, 0, j), 1, N, i);
+}
+
+// co2contra second half, massflux_c_sbp (massflux_Cgrid_mod.f90:298-358),
+// J * flux (div_c_sbp42_mod.f90:109-143, coriolis_Cgrid_mod.f90:83-97) and
+// the kinetic-energy densities (KE_Cgrid_mod.f90:41-58) on the faces.
+template <int ORD>
+__global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CArgs a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N + 1, N + 1)
+  const FieldGeom& g = a.g;
+  const long long e = at(g, p, i, j);
+  if (j < N) {  // u point
+    double ut;
+    if (a.flags & F_CO) {
+      const double t = stag_at<W>(a.ops.wc2i, a.Ap + at(g, p, 0, j), 1, N + 1, i);
+      ut = a.Qi1u[e] * a.u[e] + t / a.Ju[e];
+      a.ut[e] = ut;
+    } else {
+      ut = a.ut_in ? a.ut_in[e] : 0.0;
+    }
+    if (a.flags & F_MF) {
+      const double hu = ut * stag_at<W>(a.ops.wc2i, a.h + at(g, p, 0, j), 1, N + 1, i);
+      a.hu[e] = hu;
+      if (a.flags & F_G) a.Gu[e] = hu * a.Ju[e];
+    } else if (a.flags & F_G) {
+      a.Gu[e] = a.hu_in[e] * a.Ju[e];
+    }
+    if (a.flags & F_KE) a.KEu[e] = a.Ju[e] * (a.u[e] * ut) / 2.0;
+  }
+  if (i < N) {  // v point
+    double vt;
+    if (a.flags & F_CO) {
+      const double t = stag_at<W>(a.ops.wc2i, a.Bp + at(g, p, i, 0), g.P, N + 1, j);
+      vt = a.Qi3v[e] * a.v[e] + t / a.Jv[e];
+      a.vt[e] = vt;
+    } else {
+      vt = a.vt_in ? a.vt_in[e] : 0.0;
+    }
+    if (a.flags & F_MF) {
+      const double hv = vt * stag_at<W>(a.ops.wc2i, a.h + at(g, p, i, 0), g.P, N + 1, j);
+      a.hv[e] = hv;
+      if (a.flags & F_G) a.Gv[e] = hv * a.Jv[e];
+    } else if (a.flags & F_G) {
+      a.Gv[e] = a.hv_in[e] * a.Jv[e];
+    }
+    if (a.flags & F_KE) a.KEv[e] = a.Jv[e] * (a.v[e] * vt) / 2.0;
+  }
+}
+
+// curl_c_sbp (curl/curl_c_sbp_mod.f90:44-127) before the corner sync: the
+// staggered differences of the covariant components onto the corners, with
+// the SAT penalties on their jumps across the panel edges.
+template <int ORD>
+__global__ void __launch_bounds__(256) curl_kernel(const __grid_constant__ CArgs a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N + 1, N + 1)
+  const FieldGeom& g = a.g;
+  const COps& o = a.ops;
+  const double* vrow = a.v + at(g, p, 0, j);
+  const double* ucol = a.u + at(g, p, i, 0);
+  double dvx = stag_at<W>(o.dc2i, vrow, 1, N + 1, i);
+  if (i == 0) {
+    double dv = 0.0;
+    for (int m = 0; m < o.np; ++m) dv = dv + o.proj[m] * (vrow[m] - halo_at(a, 2, 0, p, m + 1, j, a.v, a.u));
+    dvx = dvx + 0.5 * dv / o.a_i0;
+  }
+  if (i == N) {
+    double dv = 0.0;
+    for (int m = 0; m < o.np; ++m) dv = dv + o.proj[m] * (halo_at(a, 2, 1, p, m + 1, j, a.v, a.u) - vrow[N - 1 - m]);
+    dvx = dvx + 0.5 * dv / o.a_i0;
+  }
+  double duy = stag_at<W>(o.dc2i, ucol, g.P, N + 1, j);
+  if (j == 0) {
+    double du = 0.0;
+    for (int m = 0; m < o.np; ++m) du = du + o.proj[m] * (ucol[(long long)m * g.P] - halo_at(a, 1, 2, p, m + 1, i, a.u, a.v));
+    duy = duy + 0.5 * du / o.a_i0;
+  }
+  if (j == N) {
+    double du = 0.0;
+    for (int m = 0; m < o.np; ++m)
+      du = du + o.proj[m] * (halo_at(a, 1, 3, p, m + 1, i, a.u, a.v) - ucol[(long long)(N - 1 - m) * g.P]);
+    duy = duy + 0.5 * du / o.a_i0;
+  }
+  const long long e = at(g, p, i, j);
+  a.curl[e] = (dvx - duy) / (a.Jq[e] * a.hx * a.radius);
+}
+
+// interp_w2h, first half (interpolator_w2h_mod.f90:25-67): the corner field
+// interpolated along y to the u points and along x to the v points.
+template <int ORD>
+__global__ void __launch_bounds__(256) w2uv_kernel(const __grid_constant__ CArgs a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N + 1, N + 1)
+  const FieldGeom& g = a.g;
+  const long long e = at(g, p, i, j);
+  if (j < N) a.fu[e] = stag_at<W>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
+  if (i < N) a.fv[e] = stag_at<W>(a.ops.wi2c, a.curl_in + at(g, p, 0, j), 1, N, i);
+}
+
+// Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
+// (operator_swm_mod.f90:84-85), the divergence (div_c_sbp42_mod.f90:67-107,
+// div_c2_mod.f90:97-177) and the Coriolis terms at the centres
+// (coriolis_Cgrid_mod.f90:98-118).
+template <int ORD>
+__global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ CArgs a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N, N)
+  const FieldGeom& g = a.g;
+  const COps& o = a.ops;
+  const long long e = at(g, p, i, j);
+  const long long row = at(g, p, 0, j), col = at(g, p, i, 0);
+  if (a.flags & F_KE) {
+    double ke = (stag_at<W>(o.wi2c, a.KEu + row, 1, N, i) + stag_at<W>(o.wi2c, a.KEv + col, g.P, N, j)) / a.Jp[e];
+    if (a.flags & F_ADDGH) ke = ke + a.grav * a.h[e] + a.grav * (a.hs ? a.hs[e] : 0.0);
+    a.KE[e] = ke;
+  }
+  if (a.flags & F_DIV) {
+    double dx, dy;
+    if (ORD == 21) {
+      const double* hu = a.hu_in;
+      const double* hv = a.hv_in;
+      auto u = [&](int ii) { return ii < 0 ? halo_at(a, 1, 0, p, 1, j, hu, hv)
+                                            : ii > N ? halo_at(a, 1, 1, p, 1, j, hu, hv) : hu[row + ii]; };
+      auto v = [&](int jj) { return jj < 0 ? halo_at(a, 2, 2, p, 1, i, hv, hu)
+                                            : jj > N ? halo_at(a, 2, 3, p, 1, i, hv, hu) : hv[col + (long long)jj * g.P]; };
+      auto Ju = [&](int ii) { return a.Ju[row + ii]; };
+      auto Jv = [&](int jj) { return a.Jv[col + (long long)jj * g.P]; };
+      if (i == 0) dx = Ju(1) * u(1) - Ju(0) * (0.25 * u(0) + 0.75 * u(-1));
+      else if (i == 1) dx = Ju(2) * u(2) - Ju(1) * u(1) - 0.25 * Ju(0) * (u(0) - u(-1));
+      else if (i == N - 2) dx = Ju(N - 1) * u(N - 1) - Ju(N - 2) * u(N - 2) + 0.25 * Ju(N) * (u(N) - u(N + 1));
+      else if (i == N - 1) dx = Ju(N) * (0.75 * u(N + 1) + 0.25 * u(N)) - Ju(N - 1) * u(N - 1);
+      else dx = Ju(i + 1) * u(i + 1) - Ju(i) * u(i);
+      if (j == 0) dy = Jv(1) * v(1) - Jv(0) * (0.25 * v(0) + 0.75 * v(-1));
+      else if (j == 1) dy = Jv(2) * v(2) - Jv(1) * v(1) - 0.25 * Jv(0) * (v(0) - v(-1));
+      else if (j == N - 2) dy = Jv(N - 1) * v(N - 1) - Jv(N - 2) * v(N - 2) + 0.25 * Jv(N) * (v(N) - v(N + 1));
+      else if (j == N - 1) dy = Jv(N) * (0.75 * v(N + 1) + 0.25 * v(N)) - Jv(N - 1) * v(N - 1);
+      else dy = Jv(j + 1) * v(j + 1) - Jv(j) * v(j);
+    } else {
+      const double* gu = a.Gu;
+      const double* gv = a.Gv;
+      dx = stag_at<W>(o.di2c, gu + row, 1, N, i);
+      dy = stag_at<W>(o.di2c, gv + col, g.P, N, j);
+      if (i < o.np) dx = dx + 0.5 * o.pen_c[i] * (gu[row] - halo_at(a, 1, 0, p, 1, j, gu, gv));
+      if (i >= N - o.np) dx = dx + 0.5 * o.pen_c[N - 1 - i] * (halo_at(a, 1, 1, p, 1, j, gu, gv) - gu[row + N]);
+      if (j < o.np) dy = dy + 0.5 * o.pen_c[j] * (gv[col] - halo_at(a, 2, 2, p, 1, i, gv, gu));
+      if (j >= N - o.np)
+        dy = dy + 0.5 * o.pen_c[N - 1 - j] * (halo_at(a, 2, 3, p, 1, i, gv, gu) - gv[col + (long long)N * g.P]);
+    }
+    const double dv = (dx + dy) / (a.Jp[e] * a.hx * a.radius);
+    if (a.flags & F_SEP) a.o1[e] = dv;
+    else rk_put(a, 0, e, -1.0 * dv);
+  }
+  if (a.flags & F_COR) {
+    const double gup = stag_at<W>(o.wi2c, a.Gu + row, 1, N, i);
+    const double gvp = stag_at<W>(o.wi2c, a.Gv + col, g.P, N, j);
+    const double fuh = stag_at<W>(o.wi2c, a.fu + row, 1, N, i);
+    const double fvh = stag_at<W>(o.wi2c, a.fv + col, g.P, N, j);
+    const double cp = 0.5 * fuh + 0.5 * fvh;
+    const double hh = a.h[e];
+    a.cup[e] = (a.fp[e] + cp) * gvp / hh;
+    a.cvp[e] = -(a.fp[e] + cp) * gup / hh;
+  }
+}
+
+// covariant gradient of the centre field f at face i (gradient_c_sbp42,
+// grad_c_sbp42_mod.f90:44-139; gradient_c_sbp21, grad_c2_ecs_mod.f90:234-293)
+// along a line: F(k) for 0 <= k < N from the panel, else the o halo.
+template <int ORD, class Fn>
+__device__ __forceinline__ double grad_line(const CArgs& a, int N, int i, Fn F) {
+  const COps& o = a.ops;
+  if (ORD == 21) {
+    const double hs = a.hx * a.radius;
+    if (i == 0) return (0.5 * F(1) + 0.5 * F(0) - 1.5 * F(-1) + 0.5 * F(-2)) / hs;
+    if (i == N) return (-0.5 * F(N - 2) - 0.5 * F(N - 1) + 1.5 * F(N) - 0.5 * F(N + 1)) / hs;
+    return (F(i) - F(i - 1)) / hs;
+  } else {
+    const StagOp& D = o.dc2i;
+    const double dx1 = 1.0 / (a.radius * a.hx);
+    if (i <= 3) {
+      double s = 0.0;
+      for (int m = 0; m < D.last[i]; ++m) s += D.Ql[i * D.nw + m] * F(m);
+      double gv = s * dx1;
+      if (i == 0) {
+        const double dh =
+            (o.proj[0] * (F(0) - F(-1)) + o.proj[1] * (F(1) - F(-2)) + o.proj[2] * (F(2) - F(-3))) * dx1;
+        gv = gv + 0.5 * dh / o.sq1;
+      }
+      return gv;
+    }
+    if (i <= N - 4) {
+      double s = 0.0;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) s += F(i - 2 + t) * D.Qin[t];
+      return s * dx1;
+    }
+    const int r = N - i;
+    double s = 0.0;
+    for (int m = 0; m < D.last[r]; ++m) s += D.Ql[r * D.nw + m] * F(N - 1 - m);
+    double gv = -s * dx1;
+    if (i == N) {
+      const double dh =
+          (o.proj[0] * (F(N) - F(N - 1)) + o.proj[1] * (F(N + 1) - F(N - 2)) + o.proj[2] * (F(N + 2) - F(N - 3))) * dx1;
+      gv = gv + 0.5 * dh / o.sq1;
+    }
+    return gv;
+  }
+}
+
+// Face pass: the gradient of the kinetic energy and the Coriolis term
+// interpolated from the centres (interpolator_p2uv_mod.f90:98-115), combined
+// into the u, v tendencies (operator_swm_mod.f90:95-96).
+template <int ORD>
+__global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CArgs a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N + 1, N + 1)
+  const FieldGeom& g = a.g;
+  const long long e = at(g, p, i, j);
+  const double* f = a.ke_in;
+  if (j < N) {  // u point
+    double gx = 0.0, cu = 0.0;
+    if (a.flags & F_GRAD) {
+      const double* rowp = f + at(g, p, 0, j);
+      gx = grad_line<ORD>(a, N, i, [&](int k) {
+        return k < 0 ? halo_at(a, 0, 0, p, -k, j, f, f) : k >= N ? halo_at(a, 0, 1, p, k - N + 1, j, f, f) : rowp[k];
+      });
+    }
+    if (a.flags & F_COR) cu = stag_at<W>(a.ops.wc2i, a.cup + at(g, p, 0, j), 1, N + 1, i);
+    if (a.flags & F_SEP) a.o1[e] = (a.flags & F_GRAD) ? gx : cu;
+    else rk_put(a, 1, e, -1.0 * gx + 1.0 * cu);
+  }
+  if (i < N) {  // v point
+    double gy = 0.0, cv = 0.0;
+    if (a.flags & F_GRAD) {
+      const double* colp = f + at(g, p, i, 0);
+      gy = grad_line<ORD>(a, N, j, [&](int k) {
+        return k < 0 ? halo_at(a, 0, 2, p, -k, i, f, f)
+                     : k >= N ? halo_at(a, 0, 3, p, k - N + 1, i, f, f) : colp[(long long)k * g.P];
+      });
+    }
+    if (a.flags & F_COR) cv = stag_at<W>(a.ops.wc2i, a.cvp + at(g, p, i, 0), g.P, N + 1, j);
+    if (a.flags & F_SEP) a.o2[e] = (a.flags & F_GRAD) ? gy : cv;
+    else rk_put(a, 2, e, -1.0 * gy + 1.0 * cv);
+  }
+}
+
+// SBP_C quadrature (quadrature_factory_mod.f90:90-160, sbp_quadrature_mod.f90:
+// 21-40): sum of f J hx^2 Ax(i) Ay(j) over a mesh, in fixed-order partials.
+__global__ void __launch_bounds__(kMassThreads) mass_partial_kernel(FieldGeom g, int nx, int ny, const double* f,
+                                                                     const double* J, const double* ax,
+                                                                     const double* ay, double hx2, double* part) {
+  __shared__ double sh[kMassThreads];
+  const long long total = 6LL * nx * ny;
+  double acc = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx);
+    const long long r = k / nx;
+    const int j = (int)(r % ny), p = (int)(r / ny);
+    const long long e = (long long)p * g.ps + (long long)j * g.P + i;
+    acc += f[e] * J[e] * hx2 * ax[i] * ay[j];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void mass_final_kernel(const double* part, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) s += part[k];
+    *out = s;
+  }
+}
+
+}  // namespace
+
+struct CGrid {
+  FieldGeom g{};
+  int N = 0, order = 42, L = 0;
+  double hx = 0.0, radius = 1.0, grav = 9.80616;
+  COps ops{};
+  double* met = nullptr;   // M_COUNT fields
+  double* wk = nullptr;    // W_COUNT fields
+  double* rk = nullptr;    // Y, Kb, acc: 3 fields each
+  int* halo = nullptr;
+  double* wts = nullptr;   // quadrature weights: centres (N), interfaces (N+1)
+  double* part = nullptr;  // kMassBlocks partial sums
+  double* metric(int k) const { return met + (long long)k * g.fs; }
+  double* work(int k) const { return wk + (long long)k * g.fs; }
+};
+
+namespace {
+
+CArgs base_args(const CGrid* c) {
+  CArgs a{};
+  a.g = c->g; a.N = c->N; a.L = c->L;
+  a.hx = c->hx; a.radius = c->radius; a.grav = c->grav;
+  a.ops = c->ops;
+  a.Jp = c->metric(M_JP); a.Qi2p = c->metric(M_QI2P); a.fp = c->metric(M_FP);
+  a.Ju = c->metric(M_JU); a.Qi1u = c->metric(M_QI1U);
+  a.Jv = c->metric(M_JV); a.Qi3v = c->metric(M_QI3V); a.Jq = c->metric(M_JQ);
+  a.halo = c->halo;
+  a.Ap = c->work(W_AP); a.Bp = c->work(W_BP); a.ut = c->work(W_UT); a.vt = c->work(W_VT);
+  a.hu = c->work(W_HU); a.hv = c->work(W_HV); a.Gu = c->work(W_GU); a.Gv = c->work(W_GV);
+  a.KEu = c->work(W_KEU); a.KEv = c->work(W_KEV); a.curl = c->work(W_CURL);
+  a.fu = c->work(W_FU); a.fv = c->work(W_FV); a.KE = c->work(W_KE);
+  a.cup = c->work(W_CUP); a.cvp = c->work(W_CVP);
+  return a;
+}
+
+dim3 grid_for(int nx, int ny) { return dim3((nx + 31) / 32, (ny + 7) / 8, 6); }
+const dim3 kBlock(32, 8, 1);
+
+#define SWM_C_LAUNCH(name, kern, nx, ny)                                                              \
+  cudaError_t name(const CGrid* c, const CArgs& a, cudaStream_t st) {                                 \
+    if (c->order == 42) kern<42><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                             \
+    else kern<21><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                                            \
+    return cudaGetLastError();                                                                         \
+  }
+SWM_C_LAUNCH(run_centre_a, centre_a_kernel, c->N, c->N)
+SWM_C_LAUNCH(run_faces_a, faces_a_kernel, c->N + 1, c->N + 1)
+SWM_C_LAUNCH(run_curl, curl_kernel, c->N + 1, c->N + 1)
+SWM_C_LAUNCH(run_w2uv, w2uv_kernel, c->N + 1, c->N + 1)
+SWM_C_LAUNCH(run_centre_b, centre_b_kernel, c->N, c->N)
+SWM_C_LAUNCH(run_faces_b, faces_b_kernel, c->N + 1, c->N + 1)
+#undef SWM_C_LAUNCH
+
+#define CKE(call)                               \
+  do {                                          \
+    cudaError_t e_ = (call);                    \
+    if (e_ != cudaSuccess) return e_;           \
+  } while (0)
+
+// One right-hand side of the state (h, u, v) with the epilogue of a.mode.
+cudaError_t rhs(const CGrid* c, const Topology& tp, double* edge, CArgs a, const double* in, cudaStream_t st) {
+  const long long fs = c->g.fs;
+  a.h = in; a.u = in + fs; a.v = in + 2 * fs;
+  a.flags = F_CO | F_MF | F_G | F_KE;
+  CKE(run_centre_a(c, a, st));
+  CKE(run_faces_a(c, a, st));
+  CKE(run_curl(c, a, st));
+  CKE(launch_sync_scalar(c->g, tp, a.curl, edge, st));
+  a.curl_in = a.curl;
+  CKE(run_w2uv(c, a, st));
+  a.hu_in = a.hu; a.hv_in = a.hv;
+  a.flags = F_KE | F_ADDGH | F_DIV | F_COR;
+  CKE(run_centre_b(c, a, st));
+  a.ke_in = a.KE;
+  a.flags = F_GRAD | F_COR;
+  return run_faces_b(c, a, st);
+}
+
+// ------------------------------------------------------------------ host
+// ECS metric on the prototype face (ecs_metric_mod.f90:326-478) and the
+// panel frame (ecs_proto2realface with the identity rotation).
+void metric_at(double al, double be, double& J, double& qi1, double& qi2, double& qi3) {
+  const double ta = std::tan(al), tb = std::tan(be);
+  const double sg = std::sqrt(1.0 + ta * ta + tb * tb);
+  J = (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
+  qi1 = sg * sg / (1.0 + ta * ta);
+  qi2 = sg * sg * ta * tb / ((1.0 + ta * ta) * (1.0 + tb * tb));
+  qi3 = sg * sg / (1.0 + tb * tb);
+}
+
+double coriolis_at(int p, double al, double be, double omega, const double ax[3]) {
+  const double ta = std::tan(al), tb = std::tan(be);
+  const double d = std::sqrt(1.0 + ta * ta + tb * tb);
+  const double v[3] = {ta / d, tb / d, 1.0 / d};
+  double w[3];
+  for (int k = 0; k < 3; ++k) w[k] = cube::kEX[p][k] * v[0] + cube::kEY[p][k] * v[1] - cube::kN[p][k] * v[2];
+  const double nn = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  const double pr = (ax[0] * w[0] + ax[1] * w[1] + ax[2] * w[2]) / nn;
+  return 2.0 * omega * pr;  // calc_coriolis_parameter (coriolis_factory_mod.f90:151-172)
+}
+
+// Cross-halo table of mesh T (0 o, 1 u, 2 v): create_o_points_halo_exchange
+// and create_symm_halo_vec_exchange_U/V_points (exchange_factory_mod.f90:13-
+// 156, 317-617) with the component swap and signs of buffer_mod.f90:278-475,
+// for the halo points the C-grid SBP operators read: left / right layers
+// along the panel rows, bottom / top layers along the columns, depth 1..3.
+// The neighbour's points are placed with the receiving mesh's point counts,
+// so the duplicated edge faces of u (v) fill the first x (y) layer.
+bool build_halo(int N, const FieldGeom& g, std::vector<int>& tab, std::string& why) {
+  const int L = N + 1;
+  const int dims[3][2] = {{N, N}, {N + 1, N}, {N, N + 1}};
+  tab.assign((size_t)3 * 4 * 6 * kHaloDepth * L, -1);
+  for (int T = 0; T < 3; ++T) {
+    const int nx = dims[T][0], ny = dims[T][1];
+    for (int p = 0; p < 6; ++p)
+      for (int q = 0; q < 6; ++q) {
+        if (q == p) continue;
+        int istep, jstep, dim_i;
+        cube::orientation(p, q, istep, jstep, dim_i);  // (receiver, sender)
+        const bool swap = T != 0 && !dim_i;
+        const int S = swap ? 3 - T : T;
+        int sign = 1;
+        if (T == 1) sign = dim_i ? istep : jstep;
+        if (T == 2) sign = dim_i ? jstep : istep;
+        const int snx = dims[S][0], sny = dims[S][1];
+        for (int js = 1; js <= sny; ++js)
+          for (int is = 1; is <= snx; ++is) {
+            int it, jt;
+            cube::map_index(q, is, js, p, nx, ny, it, jt);
+            int s = -1, d = 0, k = 0;
+            if (it <= 0 && it > -kHaloDepth && jt >= 1 && jt <= ny) { s = 0; d = 1 - it; k = jt - 1; }
+            else if (it > nx && it <= nx + kHaloDepth && jt >= 1 && jt <= ny) { s = 1; d = it - nx; k = jt - 1; }
+            else if (jt <= 0 && jt > -kHaloDepth && it >= 1 && it <= nx) { s = 2; d = 1 - jt; k = it - 1; }
+            else if (jt > ny && jt <= ny + kHaloDepth && it >= 1 && it <= nx) { s = 3; d = jt - ny; k = it - 1; }
+            if (s < 0) continue;
+            const long long src = (long long)q * g.ps + (long long)(js - 1) * g.P + (is - 1);
+            if (src * 4 + 3 > INT32_MAX) { why = "C-grid halo table: field too large"; return false; }
+            tab[((((size_t)T * 4 + s) * 6 + p) * kHaloDepth + (d - 1)) * L + k] =
+                (int)(src * 4 + (swap ? 2 : 0) + (sign < 0 ? 1 : 0));
+          }
+      }
+    for (int p = 0; p < 6; ++p)
+      for (int s = 0; s < 4; ++s)
+        for (int d = 1; d <= kHaloDepth; ++d)
+          for (int k = 0; k < (s < 2 ? ny : nx); ++k)
+            if (tab[((((size_t)T * 4 + s) * 6 + p) * kHaloDepth + (d - 1)) * L + k] < 0) {
+              why = "C-grid halo table: a halo point without a sender";
+              return false;
+            }
+  }
+  return true;
+}
+
+}  // namespace
+
+int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
+                 cudaStream_t st, CGrid** out, std::string& why) {
+  *out = nullptr;
+  if (order != 21 && order != 42) { why = "C-grid SBP order must be 21 or 42"; return 1; }
+  if (N < 12) { why = "C grid needs N >= 12"; return 1; }
+  CGrid* c = new CGrid;
+  c->g = g; c->N = N; c->order = order; c->L = N + 1;
+  c->hx = (0.25 * kPiC - (-0.25 * kPiC)) / (double)N;
+  c->radius = radius; c->grav = grav;
+  fill_ops(order, c->ops);
+  const double an = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+  const double ax[3] = {axis[0] / an, axis[1] / an, axis[2] / an};
+  std::vector<int> tab;
+  if (!build_halo(N, g, tab, why)) { delete c; return 1; }
+  std::vector<double> w(2 * (size_t)N + 1, 1.0);
+  {
+    // SBP_C42 / SBP_C21 edge weights (D42_A_centers / _interfaces, D21_*)
+    const std::vector<double> ec = order == 42 ? std::vector<double>{13.0 / 12.0, 7.0 / 8.0, 25.0 / 24.0, 1.0}
+                                               : std::vector<double>{1.0, 1.0};
+    const std::vector<double> ei = order == 42 ? std::vector<double>{7.0 / 18.0, 9.0 / 8.0, 1.0, 71.0 / 72.0, 1.0}
+                                               : std::vector<double>{0.5, 1.0};
+    auto fill = [](double* a, int n, const std::vector<double>& e) {
+      const int ne = (int)e.size();
+      for (int k = 0; k < std::min(ne, n); ++k) a[k] = e[k];
+      for (int k = std::max(n - ne, 0); k < n; ++k) a[k] = e[n - 1 - k];
+    };
+    fill(w.data(), N, ec);
+    fill(w.data() + N, N + 1, ei);
+  }
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t x) { if (e == cudaSuccess) e = x; return e == cudaSuccess; };
+  const size_t fb = sizeof(double) * g.fs;
+  ok(cudaMalloc(&c->met, M_COUNT * fb));
+  ok(cudaMalloc(&c->wk, W_COUNT * fb));
+  ok(cudaMalloc(&c->rk, 9 * fb));
+  ok(cudaMalloc(&c->halo, sizeof(int) * tab.size()));
+  ok(cudaMalloc(&c->wts, sizeof(double) * w.size()));
+  ok(cudaMalloc(&c->part, sizeof(double) * kMassBlocks));
+  if (e == cudaSuccess) {
+    // metric of the four meshes (mesh_factory_mod.f90:25-133: alpha =
+    // alpha0 + (i - 1 + shift_i) hx, shift 1/2 at centres, 0 on faces and
+    // corners), one field at a time through a host buffer
+    std::vector<double> hm(g.fs, 0.0);
+    for (int k = 0; k < M_COUNT && e == cudaSuccess; ++k) {
+      std::fill(hm.begin(), hm.end(), 0.0);
+      const bool ci = k <= M_FP || (k >= M_JV && k <= M_QI3V);  // centred in alpha
+      const bool cj = k <= M_QI1U;                              // centred in beta
+      const int nx = ci ? N : N + 1, ny = cj ? N : N + 1;
+      for (int p = 0; p < 6; ++p)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) {
+            const double al = -0.25 * kPiC + (i + (ci ? 0.5 : 0.0)) * c->hx;
+            const double be = -0.25 * kPiC + (j + (cj ? 0.5 : 0.0)) * c->hx;
+            double J, q1, q2, q3, x;
+            metric_at(al, be, J, q1, q2, q3);
+            switch (k) {
+              case M_QI2P: x = q2; break;
+              case M_FP: x = coriolis_at(p, al, be, omega, ax); break;
+              case M_QI1U: x = q1; break;
+              case M_QI3V: x = q3; break;
+              default: x = J; break;
+            }
+            hm[(size_t)p * g.ps + (size_t)j * g.P + i] = x;
+          }
+      ok(cudaMemcpy(c->met + (size_t)k * g.fs, hm.data(), fb, cudaMemcpyHostToDevice));
+    }
+    ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
+    ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
+    ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->wts, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaStreamSynchronize(st));  // the host buffers go out of scope
+  }
+  if (e != cudaSuccess) {
+    why = std::string("C-grid setup: ") + cudaGetErrorString(e);
+    cgrid_destroy(c);
+    return e == cudaErrorMemoryAllocation ? 3 : 2;
+  }
+  *out = c;
+  return 0;
+}
+
+void cgrid_destroy(CGrid* c) {
+  if (!c) return;
+  for (void* p : {(void*)c->met, (void*)c->wk, (void*)c->rk, (void*)c->halo, (void*)c->wts, (void*)c->part})
+    if (p) cudaFree(p);
+  delete c;
+}
+
+int cgrid_order(const CGrid* c) { return c->order; }
+
+void cgrid_mesh_dims(const CGrid* c, int mesh, int* nx, int* ny) {
+  const int N = c->N;
+  *nx = (mesh == CMESH_U || mesh == CMESH_Q) ? N + 1 : N;
+  *ny = (mesh == CMESH_V || mesh == CMESH_Q) ? N + 1 : N;
+}
+
+cudaError_t cgrid_co2contra(CGrid* c, const double* u, const double* v, double* ut, double* vt, cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.u = u; a.v = v; a.ut = ut; a.vt = vt;
+  a.flags = F_CO;
+  CKE(run_centre_a(c, a, st));
+  return run_faces_a(c, a, st);
+}
+
+cudaError_t cgrid_massflux(CGrid* c, const double* h, const double* ut, const double* vt, double* hu, double* hv,
+                           cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.h = h; a.ut_in = ut; a.vt_in = vt; a.hu = hu; a.hv = hv;
+  a.flags = F_MF;
+  return run_faces_a(c, a, st);
+}
+
+cudaError_t cgrid_ke(CGrid* c, const double* u, const double* v, const double* ut, const double* vt, double* ke,
+                     cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.u = u; a.v = v; a.ut_in = ut; a.vt_in = vt; a.KE = ke;
+  a.flags = F_KE;
+  CKE(run_faces_a(c, a, st));
+  return run_centre_b(c, a, st);
+}
+
+cudaError_t cgrid_grad(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.ke_in = f; a.o1 = gx; a.o2 = gy;
+  a.flags = F_GRAD | F_SEP;
+  return run_faces_b(c, a, st);
+}
+
+cudaError_t cgrid_div(CGrid* c, const double* hu, const double* hv, double* div, cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.hu_in = hu; a.hv_in = hv; a.o1 = div;
+  if (c->order == 42) {
+    a.flags = F_G;
+    CKE(run_faces_a(c, a, st));
+  }
+  a.flags = F_DIV | F_SEP;
+  return run_centre_b(c, a, st);
+}
+
+cudaError_t cgrid_curl(CGrid* c, const Topology& tp, double* edge, const double* u, const double* v, double* curl,
+                       cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.u = u; a.v = v; a.curl = curl;
+  CKE(run_curl(c, a, st));
+  return launch_sync_scalar(c->g, tp, curl, edge, st);
+}
+
+cudaError_t cgrid_coriolis(CGrid* c, const double* hu, const double* hv, const double* h, const double* curl,
+                           double* cor_u, double* cor_v, cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.hu_in = hu; a.hv_in = hv; a.h = h; a.curl_in = curl;
+  a.flags = F_G;
+  CKE(run_faces_a(c, a, st));
+  CKE(run_w2uv(c, a, st));
+  a.flags = F_COR;
+  CKE(run_centre_b(c, a, st));
+  a.o1 = cor_u; a.o2 = cor_v;
+  a.flags = F_COR | F_SEP;
+  return run_faces_b(c, a, st);
+}
+
+cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double* hs, const double* in, double* out,
+                        cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.hs = hs;
+  a.mode = 0;
+  a.tend = out;
+  return rhs(c, tp, edge, a, in, st);
+}
+
+cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* hs, double* y0, double dt,
+                      cudaStream_t st) {
+  CArgs a = base_args(c);
+  a.hs = hs;
+  a.dt = dt; a.hdt = 0.5 * dt; a.c6 = dt / 6.0; a.c3 = dt / 3.0;
+  a.y0 = y0;
+  a.Y = c->rk;
+  a.Kb = c->rk + 3 * c->g.fs;
+  a.acc = c->rk + 6 * c->g.fs;
+  for (int s = 1; s <= 4; ++s) {
+    a.mode = s;
+    CKE(rhs(c, tp, edge, a, s == 1 ? y0 : a.Y, st));
+  }
+  return cudaSuccess;
+}
+
+cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st) {
+  int nx, ny;
+  cgrid_mesh_dims(c, mesh, &nx, &ny);
+  const double* J = c->metric(mesh == CMESH_P ? M_JP : mesh == CMESH_U ? M_JU : mesh == CMESH_V ? M_JV : M_JQ);
+  const double* wc = c->wts;
+  const double* wi = c->wts + c->N;
+  const double* ax = (mesh == CMESH_U || mesh == CMESH_Q) ? wi : wc;
+  const double* ay = (mesh == CMESH_V || mesh == CMESH_Q) ? wi : wc;
+  mass_partial_kernel<<<kMassBlocks, kMassThreads, 0, st>>>(c->g, nx, ny, f, J, ax, ay, c->hx * c->hx, c->part);
+  mass_final_kernel<<<1, 32, 0, st>>>(c->part, kMassBlocks, result);
+  return cudaGetLastError();
+}
+
+}  // namespace swm

@@ -1,0 +1,62 @@
+// swm_cgrid.h -- the C-grid SBP vector-invariant operator family on the GPU
+// (the reference's &shallow_water_model_c, namelist_swm:80-102: divergence_c,
+// gradient_c, curl_c, coriolis_Cgrid, KE_Cgrid, co2contra_c, massflux_c and
+// the SBP_C quadrature at SBP order 21 or 42), FP64.
+//
+// Fields use the context's pitched layout (FieldGeom): element (p, j, i) at
+// p*ps + j*P + i, each mesh occupying the leading rows / columns of the
+// (N+1) x P panel slab:
+//   mesh p (cell centres)  i < N,   j < N       h, kinetic energy, divergence
+//   mesh u (x-faces)       i <= N,  j < N       covariant / contravariant u
+//   mesh v (y-faces)       i < N,   j <= N      covariant / contravariant v
+//   mesh q (corners)       i <= N,  j <= N      curl (the Ah node layout)
+// Points outside a field's mesh are never written and stay as allocated.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "swm_ops.cuh"
+
+namespace swm {
+
+enum CMesh { CMESH_P = 0, CMESH_U = 1, CMESH_V = 2, CMESH_Q = 3 };
+
+struct CGrid;
+
+// Builds the metric of the four meshes, the cross-halo tables of the
+// one-tile-per-panel exchanges and the work fields; order 21 or 42.
+int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega,
+                 const double axis[3], cudaStream_t st, CGrid** out, std::string& why);
+void cgrid_destroy(CGrid* c);
+int cgrid_order(const CGrid* c);
+// points per panel row (nx) and rows (ny) of a mesh
+void cgrid_mesh_dims(const CGrid* c, int mesh, int* nx, int* ny);
+
+// Unfused operators of the reference's plugin interface.  Each enqueues on
+// st; tp / edge are the context's topology and edge buffer (corner sync).
+cudaError_t cgrid_co2contra(CGrid* c, const double* u, const double* v, double* ut, double* vt,
+                            cudaStream_t st);
+cudaError_t cgrid_massflux(CGrid* c, const double* h, const double* ut, const double* vt, double* hu,
+                           double* hv, cudaStream_t st);
+cudaError_t cgrid_ke(CGrid* c, const double* u, const double* v, const double* ut, const double* vt,
+                     double* ke, cudaStream_t st);
+cudaError_t cgrid_grad(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st);
+cudaError_t cgrid_div(CGrid* c, const double* hu, const double* hv, double* div, cudaStream_t st);
+cudaError_t cgrid_curl(CGrid* c, const Topology& tp, double* edge, const double* u, const double* v,
+                       double* curl, cudaStream_t st);
+cudaError_t cgrid_coriolis(CGrid* c, const double* hu, const double* hv, const double* h,
+                           const double* curl, double* cor_u, double* cor_v, cudaStream_t st);
+
+// operator_swm_t%apply (vector-invariant form): tendencies (th, tu, tv) of
+// the state (h, u, v); each state is 3 fields spaced g.fs apart.  hs nullable.
+cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double* hs, const double* in,
+                        double* out, cudaStream_t st);
+// One rk4_t%step of the state y0 in place (rk4_mod.f90:20-42).
+cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* hs, double* y0,
+                      double dt, cudaStream_t st);
+// SBP_C quadrature of one field of a mesh into *result (device pointer).
+cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
+
+}  // namespace swm

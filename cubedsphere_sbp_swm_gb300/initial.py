@@ -33,14 +33,20 @@ _EN = np.array([[0, 0, 1], [-1, 0, 0], [0, 0, -1], [1, 0, 0], [0, 1, 0], [0, -1,
 MEAN_DEPTH = 5960.0
 
 
-def ecs_geometry(N: int) -> dict:
-    """Node positions r (unit sphere), covariant basis a1, a2 and Jacobian J
-    of the equiangular cubed sphere (ecs_metric_mod.f90:326-478)."""
+def ecs_geometry(N: int, mesh: str = "ah") -> dict:
+    """Point positions r (unit sphere), covariant basis a1, a2 and Jacobian J
+    of the equiangular cubed sphere (ecs_metric_mod.f90:326-478).  mesh "ah"
+    (or "q") is the (N+1) x (N+1) node / corner mesh; the C-grid meshes are
+    "p" (N x N cell centres), "u" (x-faces) and "v" (y-faces), with the
+    half-cell shifts of mesh_factory_mod.f90:34-41."""
     n = N + 1
     hx = (0.5 * math.pi) / N
-    al = -0.25 * math.pi + hx * np.arange(n)
+    si = 0.5 if mesh in ("p", "v") else 0.0
+    sj = 0.5 if mesh in ("p", "u") else 0.0
+    al = -0.25 * math.pi + hx * (np.arange(N if si else n) + si)
+    be = -0.25 * math.pi + hx * (np.arange(N if sj else n) + sj)
     ta = np.tan(al)[None, :]       # i direction
-    tb = np.tan(al)[:, None]       # j direction
+    tb = np.tan(be)[:, None]       # j direction
     s2 = 1.0 + ta * ta + tb * tb
     sg = np.sqrt(s2)
     p15 = s2 ** 1.5
@@ -56,7 +62,7 @@ def ecs_geometry(N: int) -> dict:
         return (v[None, ..., 0:1] * _EX[:, None, None, :] + v[None, ..., 1:2] * _EY[:, None, None, :]
                 - v[None, ..., 2:3] * _EN[:, None, None, :])
 
-    return dict(r=face(rp), a1=face(a1p), a2=face(a2p), J=np.broadcast_to(J, (6, n, n)).copy(),
+    return dict(r=face(rp), a1=face(a1p), a2=face(a2p), J=np.broadcast_to(J, (6,) + J.shape).copy(),
                 hx=hx, n=n, N=N)
 
 
@@ -163,6 +169,25 @@ def balanced_zonal(N: int, seed: int, lmax: int, radius=6.371e6, grav=9.80616, o
     if pert_rms > 0.0 and lmax > 0:
         h = h + harmonic_perturbation(geo, seed + 7919, lmax, pert_rms)
     u, v = _covariant(geo, V)
+    return h, u, v, dict(u0=u0, H0=H0, seed=seed, lmax=lmax)
+
+
+def balanced_zonal_c(N: int, seed: int, lmax: int, radius=6.371e6, grav=9.80616, omega=7.292e-5,
+                     pert_rms: float = 10.0):
+    """balanced_zonal on the C grid: h on the N x N cell centres, covariant u
+    on the x-faces and v on the y-faces.  Returns (h, u, v, info)."""
+    gp, gu, gv = (ecs_geometry(N, m) for m in ("p", "u", "v"))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    u0 = float(rng.uniform(20.0, 40.0))
+    k = np.array([0.0, 0.0, 1.0])
+    sphi = gp["r"][..., 2]
+    c = (radius * omega * u0 + 0.5 * u0 * u0) / grav
+    H0 = MEAN_DEPTH + c / 3.0
+    h = H0 - c * sphi * sphi
+    if pert_rms > 0.0 and lmax > 0:
+        h = h + harmonic_perturbation(gp, seed + 7919, lmax, pert_rms)
+    u = np.einsum("pjic,pjic->pji", u0 * np.cross(k, gu["r"]), gu["a1"]).copy()
+    v = np.einsum("pjic,pjic->pji", u0 * np.cross(k, gv["r"]), gv["a2"]).copy()
     return h, u, v, dict(u0=u0, H0=H0, seed=seed, lmax=lmax)
 
 

@@ -79,9 +79,21 @@ typedef struct swm_config {
 int swm_ctx_create(const swm_config* cfg, swm_ctx** out);
 
 /* As swm_ctx_create, with the operator names of the &shallow_water_model
- * namelist (config_swm_mod.f90:70-104).  Names outside the vector-invariant
- * Ah-grid family, or div/grad/curl of different SBP orders, return
- * SWM_E_UNSUPPORTED. */
+ * namelist (config_swm_mod.f90:70-104).  Two operator families:
+ *   Ah grid (staggering "Ah"): divergence_ahXX_sbp, gradient_ahXX_sbp_ecs,
+ *     curl_divergence_ahXX_sbp (XX 42, 43, 63), coriolis_colocated,
+ *     KE_colocated, co2contra_colocated, massflux_colocated,
+ *     SBP_AhXX_quadrature; FP64 or the FP32 fused form;
+ *   C grid (staggering "C", the &shallow_water_model_c namelist,
+ *     namelist_swm:80-102): divergence_c_sbpNN, gradient_c_sbpNN,
+ *     curl_c_sbpNN, coriolis_Cgrid_sbpNN, KE_Cgrid_sbpNN,
+ *     co2contra_c_sbpNN, massflux_c_sbpNN, SBP_CNN_quadrature with NN 21 or
+ *     42, one order throughout; FP64 only.  h lives on the cell centres, u
+ *     on the x-faces, v on the y-faces (domain_factory_mod.f90:108-112).
+ * Other names, or operators of different SBP orders, return
+ * SWM_E_UNSUPPORTED.  A C-grid context provides the state algebra, apply,
+ * the RK4 step, orography, fields and the single operators below; the other
+ * entry points return SWM_E_UNSUPPORTED on it. */
 int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name,
                          const char* grad_op_name, const char* curl_op_name,
                          const char* coriolis_op_name, const char* KE_op_name,
@@ -94,8 +106,22 @@ const char* swm_last_error(const swm_ctx* ctx);
 int         swm_ctx_synchronize(swm_ctx* ctx);
 /* The context's cudaStream_t, for callers that interleave their own work. */
 void*       swm_ctx_stream(swm_ctx* ctx);
-/* Number of nodes per field, 6*(N+1)^2. */
+/* Number of nodes per field, 6*(N+1)^2 (the Ah grid; see swm_mesh_dims). */
 size_t      swm_ctx_npts(const swm_ctx* ctx);
+
+/* Staggering of a context and its meshes (mesh_p, mesh_u, mesh_v, mesh_q of
+ * domain_t).  On the Ah grid all four are the (N+1) x (N+1) node mesh; on
+ * the C grid p is N x N cell centres, u (N+1) x N x-faces, v N x (N+1)
+ * y-faces, q (N+1) x (N+1) corners.  Host arrays of a mesh are 6 panels of
+ * ny rows of nx points, i fastest. */
+#define SWM_GRID_AH 0
+#define SWM_GRID_C  1
+#define SWM_MESH_P 0
+#define SWM_MESH_U 1
+#define SWM_MESH_V 2
+#define SWM_MESH_Q 3
+int swm_ctx_grid(const swm_ctx* ctx);                      /* SWM_GRID_* or -1 */
+int swm_mesh_dims(const swm_ctx* ctx, int mesh, int* nx, int* ny);
 
 /* Orography h_surf (operator_swm_factory_mod.f90:120-121; zero if never set). */
 int swm_set_orography(swm_ctx* ctx, const double* h_surf_host);
@@ -202,7 +228,9 @@ int swm_diagnostics(swm_ctx* ctx, const swm_state* v, double out[7]);
 /* Fields and single operators (grid_field_t, grid_field_mod.f90:7-65)     */
 /* FP64, reference semantics, one kernel pass each (parity mode).          */
 /* ---------------------------------------------------------------------- */
-int  swm_field_create(swm_ctx* ctx, swm_field** out);
+int  swm_field_create(swm_ctx* ctx, swm_field** out);   /* on mesh p */
+/* a field on one of the context's meshes (create_grid_field on mesh_p/u/v/q) */
+int  swm_field_create_mesh(swm_ctx* ctx, int mesh, swm_field** out);
 void swm_field_free(swm_field* f);
 int  swm_field_upload(swm_ctx* ctx, swm_field* f, const double* host);
 int  swm_field_download(swm_ctx* ctx, const swm_field* f, double* host);

@@ -112,6 +112,10 @@ def lib():
         for name in ("orcc_mass", "orcc_l2norm"):
             getattr(L, name).argtypes = [vp, ctypes.c_int, _D]
             getattr(L, name).restype = ctypes.c_double
+        L.orcc_vector_test_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
+        L.orcc_vector_test_field.restype = ctypes.c_int
+        L.orcc_scalar_test_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D]
+        L.orcc_scalar_test_field.restype = ctypes.c_int
         L.orcc_golden.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D]
         L.orcc_golden.restype = ctypes.c_int
         _lib = L
@@ -387,6 +391,21 @@ class OracleCDomain:
         hs_p = None if hs is None else _p(self._c(hs))
         lib().orcc_rk4(self._h, hs_p, _p(h), _p(u), _p(v), float(dt), int(nsteps))
         return h, u, v
+
+    VECTOR_FIELDS = {"solid_rotation": 0, "cross_polar": 1, "xyz_grad": 2, "vsh_curl_free_10": 3}
+    SCALAR_FIELDS = {"xyz": 10, "cross_polar_div": 11, "cross_polar_zeta": 12}
+
+    def vector_test_field(self, kind, level=0, contravariant=False):
+        u, v = self.zeros("u"), self.zeros("v")
+        assert lib().orcc_vector_test_field(self._h, self.VECTOR_FIELDS[kind], int(level),
+                                            1 if contravariant else 0, _p(u), _p(v)) == 0
+        return u, v
+
+    def scalar_test_field(self, kind, level=0, mesh="p"):
+        f = self.zeros(mesh)
+        assert lib().orcc_scalar_test_field(self._h, self.SCALAR_FIELDS[kind], int(level),
+                                            self.MESHES[mesh], _p(f)) == 0
+        return f
 
     def mass(self, f, mesh="p"):
         return lib().orcc_mass(self._h, self.MESHES[mesh], _p(self._c(f)))

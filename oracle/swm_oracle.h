@@ -159,6 +159,14 @@ void orcc_rk4(const orcc_domain* d, const double* hs, double* h, double* u,
               double* v, double dt, int nsteps);
 double orcc_mass(const orcc_domain* d, int mesh, const double* f);
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
+/* Analytic test fields on the C meshes: vector kinds 0 solid rotation (axis
+ * cycles with level), 1 cross-polar, 2 gradient of x/y/z, 3 curl-free VSH (u
+ * on mesh u, v on mesh v); scalar kinds 10 x/y/z, 11 cross-polar divergence,
+ * 12 cross-polar vorticity on the given mesh.  Return 0 or -1. */
+int orcc_vector_test_field(const orcc_domain* d, int kind, int level,
+                           int contravariant, double* u, double* v);
+int orcc_scalar_test_field(const orcc_domain* d, int kind, int level, int mesh,
+                           double* f);
 /* Known-answer tests on the C grid at (N, nz=3, unit sphere): kind 0 div (4
  * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2).
  * Returns 0, or -1 for an unknown kind / order. */

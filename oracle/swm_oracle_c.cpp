@@ -778,6 +778,40 @@ double orcc_l2norm(const orcc_domain* d, int mesh, const double* f) {
   return std::sqrt(l2sq(d->m[mesh], d->hx, f));
 }
 
+// Analytic fields of the known-answer tests on the C meshes (as
+// orc_vector_test_field / orc_scalar_test_field on the Ah grid): vector kinds
+// 0 solid rotation (axis cycles with level), 1 cross-polar flow, 2 gradient
+// of x/y/z (cycles), 3 curl-free VSH; u on the u mesh, v on the v mesh.
+// Scalar kinds 10 x/y/z (cycles), 11 cross-polar divergence, 12 cross-polar
+// vorticity, on the given mesh.
+int orcc_vector_test_field(const orcc_domain* d, int kind, int level, int contravariant, double* u, double* v) {
+  std::vector<double> a, b;
+  const bool ct = contravariant != 0;
+  switch (kind) {
+    case 0: set_vector(*d, [level](double x, double y, double z, double w[3]) { field_solid_rotation(level, x, y, z, w); }, ct, a, b); break;
+    case 1: set_vector(*d, field_cross_polar, ct, a, b); break;
+    case 2: set_vector(*d, [level](double x, double y, double z, double w[3]) { field_xyz_grad(level, x, y, z, w); }, ct, a, b); break;
+    case 3: set_vector(*d, field_vsh_curl_free_10, ct, a, b); break;
+    default: return -1;
+  }
+  std::copy(a.begin(), a.end(), u);
+  std::copy(b.begin(), b.end(), v);
+  return 0;
+}
+
+int orcc_scalar_test_field(const orcc_domain* d, int kind, int level, int mesh, double* f) {
+  if (mesh < 0 || mesh > 3) return -1;
+  const Mesh& M = d->m[mesh];
+  for (int k = 0; k < M.size(); ++k) {
+    const double x = M.rx[k], y = M.ry[k], z = M.rz[k];
+    if (kind == 10) f[k] = field_xyz(level, x, y, z);
+    else if (kind == 11) f[k] = field_cross_polar_div(x, y, z);
+    else if (kind == 12) f[k] = field_cross_polar_zeta(x, y, z);
+    else return -1;
+  }
+  return 0;
+}
+
 // The reference's known-answer tests on the C grid at N, nz = 3 identical
 // levels apart from the solid-rotation axis (test_diff_ops/
 // test_diffops_mod.f90): kind 0 test_div (71-125), 1 test_grad (127-178),
