@@ -21,6 +21,8 @@ integer(c_int), parameter :: SWM_OK = 0, SWM_E_INVALID = -1, SWM_E_UNSUPPORTED =
 integer(c_int), parameter :: SWM_FP64_PLAIN = 0, SWM_FP32_FUSED = 1
 integer(c_int), parameter :: SWM_BOX_AUTO = 0, SWM_BOX_STRIP = 1, SWM_BOX_WIDEST = 2
 integer(c_int), parameter :: SWM_SYNC_STATIC_MAX_N = 1024
+integer(c_int), parameter :: SWM_GRID_AH = 0, SWM_GRID_C = 1
+integer(c_int), parameter :: SWM_MESH_P = 0, SWM_MESH_U = 1, SWM_MESH_V = 2, SWM_MESH_Q = 3
 
 ! struct swm_config
 type, bind(c) :: swm_config
@@ -67,6 +69,16 @@ interface
         import :: c_size_t, c_ptr
         type(c_ptr), value :: ctx
     end function swm_ctx_npts
+    integer(c_int) function swm_ctx_grid(ctx) bind(c, name="swm_ctx_grid")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx
+    end function swm_ctx_grid
+    integer(c_int) function swm_mesh_dims(ctx, mesh, nx, ny) bind(c, name="swm_mesh_dims")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx
+        integer(c_int), value :: mesh
+        integer(c_int), intent(out) :: nx, ny
+    end function swm_mesh_dims
     integer(c_int) function swm_set_orography(ctx, h_surf) bind(c, name="swm_set_orography")
         import :: c_int, c_ptr, c_double
         type(c_ptr), value :: ctx
@@ -202,6 +214,12 @@ interface
         type(c_ptr), value :: ctx
         type(c_ptr), intent(out) :: f
     end function swm_field_create
+    integer(c_int) function swm_field_create_mesh(ctx, mesh, f) bind(c, name="swm_field_create_mesh")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx
+        integer(c_int), value :: mesh
+        type(c_ptr), intent(out) :: f
+    end function swm_field_create_mesh
     subroutine swm_field_free(f) bind(c, name="swm_field_free")
         import :: c_ptr
         type(c_ptr), value :: f
