@@ -328,9 +328,12 @@ __global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ C
   const COps& o = a.ops;
   const long long e = at(g, p, i, j);
   const long long row = at(g, p, 0, j), col = at(g, p, i, 0);
+  // h of this point, read before the RK epilogue of stages 2 and 3 writes
+  // the new h in place over it
+  const double hh = (a.flags & (F_ADDGH | F_COR)) ? a.h[e] : 0.0;
   if (a.flags & F_KE) {
     double ke = (stag_at<W>(o.wi2c, a.KEu + row, 1, N, i) + stag_at<W>(o.wi2c, a.KEv + col, g.P, N, j)) / a.Jp[e];
-    if (a.flags & F_ADDGH) ke = ke + a.grav * a.h[e] + a.grav * (a.hs ? a.hs[e] : 0.0);
+    if (a.flags & F_ADDGH) ke = ke + a.grav * hh + a.grav * (a.hs ? a.hs[e] : 0.0);
     a.KE[e] = ke;
   }
   if (a.flags & F_DIV) {
@@ -375,7 +378,6 @@ __global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ C
     const double fuh = stag_at<W>(o.wi2c, a.fu + row, 1, N, i);
     const double fvh = stag_at<W>(o.wi2c, a.fv + col, g.P, N, j);
     const double cp = 0.5 * fuh + 0.5 * fvh;
-    const double hh = a.h[e];
     a.cup[e] = (a.fp[e] + cp) * gvp / hh;
     a.cvp[e] = -(a.fp[e] + cp) * gup / hh;
   }
@@ -820,6 +822,11 @@ cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double
   return rhs(c, tp, edge, a, in, st);
 }
 
+// Stage 1 reads y0 and writes Y; stages 2 and 3 read Y and write Y in place;
+// stage 4 reads Y and writes y0.  In place is safe: the passes that read the
+// stage input at neighbouring points (centre_a, faces_a, curl) run before the
+// two that write it (centre_b, faces_b), and those read only their own point
+// of it, before writing it.
 cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* hs, double* y0, double dt,
                       cudaStream_t st) {
   CArgs a = base_args(c);
