@@ -698,6 +698,9 @@ def run_gpu_arm(args):
     dif = None
     if rank == 0 and not args.no_diffusion:
         dif = diffusion_leg(w, h, u, v, local, max(10, args.steps // 2), args.warmup)
+    cg = None
+    if rank == 0 and not args.no_cgrid:
+        cg = cgrid_leg(local, max(10, args.steps // 2), args.warmup, cpu=not args.no_cpu)
 
     if rank == 0:
         line = {
@@ -737,6 +740,8 @@ def run_gpu_arm(args):
             line["adjoint"] = adj
         if dif:
             line["model_step_with_diffusion"] = dif
+        if cg:
+            line["c_grid"] = cg
         if cpu:
             line["cpu_baseline"] = cpu["cpu_baseline"]
             line["cpu_rates"] = cpu["rates"]
@@ -795,6 +800,105 @@ def diffusion_leg(w, h, u, v, local, steps, warmup):
         out[prec] = r
         del op, dop
     return out
+
+
+# The C-grid SBP family (&shallow_water_model_c) at N=384, SBP 4/2, FP64:
+# six passes per RK4 stage (centre_a, faces_a, curl + its corner sync,
+# w2uv, centre_b, faces_b).  Algorithmic HBM words per point and stage of
+# those passes (inputs and outputs of each pass, metric included):
+#   centre_a 6 + faces_a 17 + curl 4 + w2uv 3 + centre_b 13 + faces_b 3,
+#   plus the stage epilogues of the three state components (2, 4, 2 and 3
+#   words in stages 1..4): 4 x 46 + 3 x 11 = 217 words per point and step.
+CGRID_WORDS_PER_POINT_STEP = 217
+CGRID_LAUNCHES_PER_STEP = 32          # 4 x (6 passes + 2 corner-sync kernels)
+
+
+def cgrid_leg(local, steps, warmup, cpu=True):
+    """The C-grid operator family's RK4 step (FP64) on a seeded balanced
+    zonal flow at N=384, dt = 37.5 s (Courant number 0.4: the 4/2 C-grid
+    scheme's RK4 limit is near 0.6): device-timed steps with an L2 flush
+    before each, end-to-end steps through the C-ABI with page-locked host
+    arrays, parity against the FP64 oracle after two steps, and the oracle's
+    own rate on the host cores."""
+    import numpy as np
+    import torch
+
+    import cubedsphere_sbp_swm_gb300 as swm
+    from cubedsphere_sbp_swm_gb300 import initial
+
+    N, ORDER, DT = 384, 42, 37.5
+    dev = torch.device("cuda", local)
+    h, u, v, _ = initial.balanced_zonal_c(N, 11, 24)
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=ORDER, names=swm.c_grid_names(ORDER), device=local))
+    s0, s = op.create_stvec(), op.create_stvec()
+    s0.upload(h, u, v)
+    s.assign_s1v1(1.0, s0)
+    stream = torch.cuda.ExternalStream(op.stream, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    ts = swm.RK4()
+    for _ in range(warmup):
+        ts.step(s, op, DT, 1)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize(dev)
+    for a, b in evs:
+        s.assign_s1v1(1.0, s0)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a.record(stream)
+        ts.step(s, op, DT, 1)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+    # end to end: upload from / download to page-locked host arrays, every step
+    pins = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True) for a in (h, u, v) for _ in range(2)]
+    hin = [pins[2 * k].numpy() for k in range(3)]
+    hout = tuple(pins[2 * k + 1].numpy() for k in range(3))
+    for t_, a_ in zip(hin, (h, u, v)):
+        t_[...] = a_
+    for _ in range(2):
+        s.upload(*hin); ts.step(s, op, DT, 1); s.download(out=hout)
+    n_e2e = max(10, steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        s.upload(*hin)
+        ts.step(s, op, DT, 1)
+        s.download(out=hout)
+    e2e = n_e2e / (time.perf_counter() - t0)
+    nbytes = sum(a.size for a in (h, u, v)) * 8
+    # parity after two steps against the oracle (and its rate)
+    s.upload(h, u, v)
+    ts.step(s, op, DT, 2)
+    got = s.download()
+    res = {"workload": "C-grid SBP 4/2 vector-invariant family (&shallow_water_model_c operators), "
+                       "N=384 (6 x 384^2 centres, 6 x 385 x 384 faces per velocity component), FP64",
+           "operators": swm.c_grid_names(ORDER), "dt_s": DT,
+           "value": round(1e3 / ms, 3), "unit": "steps/s", "ms_per_step": round(ms, 5),
+           "launches_per_step": CGRID_LAUNCHES_PER_STEP,
+           "e2e": {"value": round(e2e, 3), "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+                   "d2h_bytes_per_step": nbytes,
+                   "path": "swm_state_upload (page-locked arrays) + swm_rk4_step + swm_state_download, "
+                           "one synchronous step at a time"}}
+    npts = 6 * N * N
+    peak, peak_kind = _measured_peak()
+    achieved = CGRID_WORDS_PER_POINT_STEP * 8 * npts / (ms / 1e3) / 1e9
+    res["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                       "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                       "algorithmic_bytes_per_step": CGRID_WORDS_PER_POINT_STEP * 8 * npts,
+                       "scope": "whole RK4 step (32 launches)"}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle  # the checker and the timed CPU baseline
+        od = oracle.OracleCDomain(N, ORDER)
+        threads = os.cpu_count() or 1
+        oracle.set_threads(threads)
+        t0 = time.perf_counter()
+        want = od.rk4(h, u, v, DT, 2)
+        el = time.perf_counter() - t0
+        rel = max(float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(got, want))
+        res["parity_vs_oracle_2_steps_max_rel_l2"] = rel
+        res["cpu_oracle"] = {"value": round(2 / el, 4), "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": "2 RK4 steps of the same state at N=384 (C-grid oracle)"}
+    return res
 
 
 def _oracle_rate(od, state, dt, threads, window_s, warm_s, min_steps=1):
@@ -963,7 +1067,9 @@ def main():
                     help="reference arm: also time these workloads' oracle (comma-separated)")
     ap.add_argument("--quick", action="store_true",
                     help="profiling case: time only the FP32 steps, print a short line")
-    ap.add_argument("--only", choices=("ensemble", "adjoint", "diffusion"), default=None,
+    ap.add_argument("--no-cgrid", action="store_true",
+                    help="skip the C-grid operator family's RK4 leg")
+    ap.add_argument("--only", choices=("ensemble", "adjoint", "diffusion", "cgrid"), default=None,
                     help="run one leg alone and print its JSON object")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -975,6 +1081,8 @@ def main():
             res = ensemble_leg(local, max(10, args.steps // 2), args.warmup, _measured_peak()[0])
         elif args.only == "adjoint":
             res = adjoint_leg(local)
+        elif args.only == "cgrid":
+            res = cgrid_leg(local, max(10, args.steps // 2), args.warmup, cpu=not args.no_cpu)
         else:
             w = WORKLOADS[args.workload]
             h, u, v, _ = _state(w)

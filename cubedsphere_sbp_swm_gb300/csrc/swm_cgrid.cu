@@ -11,7 +11,7 @@
 //                        and the kinetic-energy densities J u u^i / 2
 //   curl      q points   staggered differences + SAT penalties, then the
 //                        Ah-type edge / corner average
-//   w2uv      u, v       the curl interpolated to the faces
+//   w2uv      u          the curl interpolated to the x-faces
 //   centre_b  p points   kinetic energy + g (h + hs), the divergence with its
 //                        SAT penalties (h tendency), the Coriolis terms
 //   faces_b   u, v       gradient with its SAT penalties + the Coriolis term
@@ -116,8 +116,15 @@ void fill_ops(int order, COps& o) {
 }
 
 // Metric fields (one pitched field each) and work fields of one context.
-enum { M_JP = 0, M_QI2P, M_FP, M_JU, M_QI1U, M_JV, M_QI3V, M_JQ, M_COUNT };
-enum { W_AP = 0, W_BP, W_UT, W_VT, W_HU, W_HV, W_GU, W_GV, W_KEU, W_KEV, W_CURL, W_FU, W_FV, W_KE,
+// GB300's FP64 pipe is narrow, so the divisions of the operators are taken
+// once on the host: reciprocal fields 1/J and 1/(J hx a), and J Qi12.
+enum { M_JP = 0, M_QI2P, M_FP, M_RJP, M_RJPHA, M_JQI2P,  // centres
+       M_JU, M_QI1U, M_RJU,                              // x-faces
+       M_JV, M_QI3V, M_RJV,                              // y-faces
+       M_JQ, M_RJQHA,                                    // corners
+       M_COUNT };
+constexpr int kMetricMesh[M_COUNT] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 2, 2, 2, 3, 3};
+enum { W_AP = 0, W_BP, W_UT, W_VT, W_HU, W_HV, W_GU, W_GV, W_KEU, W_KEV, W_CURL, W_FU, W_KE,
        W_CUP, W_CVP, W_COUNT };
 
 // kernel flags
@@ -137,13 +144,14 @@ struct CArgs {
   FieldGeom g;
   int N, L, flags;
   double hx, radius, grav;
+  double dx1;  // 1 / (a hx), the gradient's scale
   COps ops;
-  const double *Jp, *Qi2p, *fp, *Ju, *Qi1u, *Jv, *Qi3v, *Jq;
+  const double *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha;
   const int* halo;
   // inputs
   const double *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
   // intermediate and unfused outputs
-  double *Ap, *Bp, *ut, *vt, *hu, *hv, *Gu, *Gv, *KEu, *KEv, *curl, *fu, *fv, *KE, *cup, *cvp;
+  double *Ap, *Bp, *ut, *vt, *hu, *hv, *Gu, *Gv, *KEu, *KEv, *curl, *fu, *KE, *cup, *cvp;
   double *o1, *o2;  // unfused outputs of centre_b (div) / faces_b (gx|cor_u, gy|cor_v)
   // RK4 stage epilogue: mode 0 writes the tendency to tend, 1..4 the stages
   // of rk4_mod.f90:20-42 (y0, Y, Kb, acc: 3 fields each, fs apart)
@@ -152,24 +160,25 @@ struct CArgs {
   double *tend, *y0, *Y, *Kb, *acc;
 };
 
-__device__ __forceinline__ long long at(const FieldGeom& g, int p, int i, int j) {
-  return (long long)p * g.ps + (long long)j * g.P + i;
+// element offset within a field (fields stay below 2^31 elements)
+__device__ __forceinline__ int at(const FieldGeom& g, int p, int i, int j) {
+  return p * (int)g.ps + j * g.P + i;
 }
 
 // sbp_apply for output k of nout outputs over a line f with stride st
 template <int W>
-__device__ __forceinline__ double stag_at(const StagOp& s, const double* __restrict__ f, long long st, int nout,
+__device__ __forceinline__ double stag_at(const StagOp& s, const double* __restrict__ f, int st, int nout,
                                           int k) {
   double acc = 0.0;
   if (k >= s.ne && k < nout - s.ne) {
-    const double* b = f + (long long)(k + s.inshift) * st;
+    const double* b = f + (k + s.inshift) * st;
 #pragma unroll
     for (int t = 0; t < W; ++t) acc += s.Qin[t] * b[t * st];
   } else if (k < s.ne) {
     for (int m = 0; m < s.last[k]; ++m) acc += s.Ql[k * s.nw + m] * f[m * st];
   } else {
     const int nin = nout - s.dnx, r = nout - 1 - k;
-    for (int m = s.last[r] - 1; m >= 0; --m) acc += (s.rsign * s.Ql[r * s.nw + m]) * f[(long long)(nin - 1 - m) * st];
+    for (int m = s.last[r] - 1; m >= 0; --m) acc += (s.rsign * s.Ql[r * s.nw + m]) * f[(nin - 1 - m) * st];
   }
   return acc;
 }
@@ -184,8 +193,8 @@ __device__ __forceinline__ double halo_at(const CArgs& a, int mesh, int side, in
   return (c & 1) ? -x : x;
 }
 
-__device__ __forceinline__ void rk_put(const CArgs& a, int comp, long long e, double k) {
-  const long long o = (long long)comp * a.g.fs + e;
+__device__ __forceinline__ void rk_put(const CArgs& a, int comp, int e, double k) {
+  const int o = comp * (int)a.g.fs + e;
   switch (a.mode) {
     case 0: a.tend[o] = k; break;
     case 1: a.Kb[o] = k; a.Y[o] = 1.0 * a.y0[o] + a.hdt * k; break;
@@ -209,8 +218,8 @@ __global__ void __launch_bounds__(256) centre_a_kernel(const __grid_constant__ C
   const int N = a.N;
   SWM_C_INDEX(N, N)
   const FieldGeom& g = a.g;
-  const long long e = at(g, p, i, j);
-  const double jq = a.Jp[e] * a.Qi2p[e];
+  const int e = at(g, p, i, j);
+  const double jq = a.JQi2p[e];
   a.Ap[e] = jq * stag_at<W>(a.ops.wi2c, a.v + at(g, p, i, 0), g.P, N, j);
   a.Bp[e] = jq * stag_at<W>(a.ops.wi2c, a.u + at(g, p, 0, j), 1, N, i);
 }
@@ -224,12 +233,12 @@ __global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CA
   const int N = a.N;
   SWM_C_INDEX(N + 1, N + 1)
   const FieldGeom& g = a.g;
-  const long long e = at(g, p, i, j);
+  const int e = at(g, p, i, j);
   if (j < N) {  // u point
     double ut;
     if (a.flags & F_CO) {
       const double t = stag_at<W>(a.ops.wc2i, a.Ap + at(g, p, 0, j), 1, N + 1, i);
-      ut = a.Qi1u[e] * a.u[e] + t / a.Ju[e];
+      ut = a.Qi1u[e] * a.u[e] + t * a.rJu[e];
       a.ut[e] = ut;
     } else {
       ut = a.ut_in ? a.ut_in[e] : 0.0;
@@ -241,13 +250,13 @@ __global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CA
     } else if (a.flags & F_G) {
       a.Gu[e] = a.hu_in[e] * a.Ju[e];
     }
-    if (a.flags & F_KE) a.KEu[e] = a.Ju[e] * (a.u[e] * ut) / 2.0;
+    if (a.flags & F_KE) a.KEu[e] = a.Ju[e] * (a.u[e] * ut) * 0.5;
   }
   if (i < N) {  // v point
     double vt;
     if (a.flags & F_CO) {
       const double t = stag_at<W>(a.ops.wc2i, a.Bp + at(g, p, i, 0), g.P, N + 1, j);
-      vt = a.Qi3v[e] * a.v[e] + t / a.Jv[e];
+      vt = a.Qi3v[e] * a.v[e] + t * a.rJv[e];
       a.vt[e] = vt;
     } else {
       vt = a.vt_in ? a.vt_in[e] : 0.0;
@@ -259,7 +268,7 @@ __global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CA
     } else if (a.flags & F_G) {
       a.Gv[e] = a.hv_in[e] * a.Jv[e];
     }
-    if (a.flags & F_KE) a.KEv[e] = a.Jv[e] * (a.v[e] * vt) / 2.0;
+    if (a.flags & F_KE) a.KEv[e] = a.Jv[e] * (a.v[e] * vt) * 0.5;
   }
 }
 
@@ -289,30 +298,31 @@ __global__ void __launch_bounds__(256) curl_kernel(const __grid_constant__ CArgs
   double duy = stag_at<W>(o.dc2i, ucol, g.P, N + 1, j);
   if (j == 0) {
     double du = 0.0;
-    for (int m = 0; m < o.np; ++m) du = du + o.proj[m] * (ucol[(long long)m * g.P] - halo_at(a, 1, 2, p, m + 1, i, a.u, a.v));
+    for (int m = 0; m < o.np; ++m) du = du + o.proj[m] * (ucol[m * g.P] - halo_at(a, 1, 2, p, m + 1, i, a.u, a.v));
     duy = duy + 0.5 * du / o.a_i0;
   }
   if (j == N) {
     double du = 0.0;
     for (int m = 0; m < o.np; ++m)
-      du = du + o.proj[m] * (halo_at(a, 1, 3, p, m + 1, i, a.u, a.v) - ucol[(long long)(N - 1 - m) * g.P]);
+      du = du + o.proj[m] * (halo_at(a, 1, 3, p, m + 1, i, a.u, a.v) - ucol[(N - 1 - m) * g.P]);
     duy = duy + 0.5 * du / o.a_i0;
   }
-  const long long e = at(g, p, i, j);
-  a.curl[e] = (dvx - duy) / (a.Jq[e] * a.hx * a.radius);
+  const int e = at(g, p, i, j);
+  a.curl[e] = (dvx - duy) * a.rJqha[e];
 }
 
 // interp_w2h, first half (interpolator_w2h_mod.f90:25-67): the corner field
-// interpolated along y to the u points and along x to the v points.
+// interpolated along y to the u points.  The reference averages two
+// tensor-product interpolations to the centres, x after y and y after x;
+// the 1-D operators act on different indices, so both are the same linear
+// map and one of them is evaluated (the results agree to round-off).
 template <int ORD>
 __global__ void __launch_bounds__(256) w2uv_kernel(const __grid_constant__ CArgs a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
-  SWM_C_INDEX(N + 1, N + 1)
+  SWM_C_INDEX(N + 1, N)
   const FieldGeom& g = a.g;
-  const long long e = at(g, p, i, j);
-  if (j < N) a.fu[e] = stag_at<W>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
-  if (i < N) a.fv[e] = stag_at<W>(a.ops.wi2c, a.curl_in + at(g, p, 0, j), 1, N, i);
+  a.fu[at(g, p, i, j)] = stag_at<W>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
 }
 
 // Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
@@ -326,13 +336,13 @@ __global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ C
   SWM_C_INDEX(N, N)
   const FieldGeom& g = a.g;
   const COps& o = a.ops;
-  const long long e = at(g, p, i, j);
-  const long long row = at(g, p, 0, j), col = at(g, p, i, 0);
+  const int e = at(g, p, i, j);
+  const int row = at(g, p, 0, j), col = at(g, p, i, 0);
   // h of this point, read before the RK epilogue of stages 2 and 3 writes
   // the new h in place over it
   const double hh = (a.flags & (F_ADDGH | F_COR)) ? a.h[e] : 0.0;
   if (a.flags & F_KE) {
-    double ke = (stag_at<W>(o.wi2c, a.KEu + row, 1, N, i) + stag_at<W>(o.wi2c, a.KEv + col, g.P, N, j)) / a.Jp[e];
+    double ke = (stag_at<W>(o.wi2c, a.KEu + row, 1, N, i) + stag_at<W>(o.wi2c, a.KEv + col, g.P, N, j)) * a.rJp[e];
     if (a.flags & F_ADDGH) ke = ke + a.grav * hh + a.grav * (a.hs ? a.hs[e] : 0.0);
     a.KE[e] = ke;
   }
@@ -344,9 +354,9 @@ __global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ C
       auto u = [&](int ii) { return ii < 0 ? halo_at(a, 1, 0, p, 1, j, hu, hv)
                                             : ii > N ? halo_at(a, 1, 1, p, 1, j, hu, hv) : hu[row + ii]; };
       auto v = [&](int jj) { return jj < 0 ? halo_at(a, 2, 2, p, 1, i, hv, hu)
-                                            : jj > N ? halo_at(a, 2, 3, p, 1, i, hv, hu) : hv[col + (long long)jj * g.P]; };
+                                            : jj > N ? halo_at(a, 2, 3, p, 1, i, hv, hu) : hv[col + jj * g.P]; };
       auto Ju = [&](int ii) { return a.Ju[row + ii]; };
-      auto Jv = [&](int jj) { return a.Jv[col + (long long)jj * g.P]; };
+      auto Jv = [&](int jj) { return a.Jv[col + jj * g.P]; };
       if (i == 0) dx = Ju(1) * u(1) - Ju(0) * (0.25 * u(0) + 0.75 * u(-1));
       else if (i == 1) dx = Ju(2) * u(2) - Ju(1) * u(1) - 0.25 * Ju(0) * (u(0) - u(-1));
       else if (i == N - 2) dx = Ju(N - 1) * u(N - 1) - Ju(N - 2) * u(N - 2) + 0.25 * Ju(N) * (u(N) - u(N + 1));
@@ -366,20 +376,19 @@ __global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ C
       if (i >= N - o.np) dx = dx + 0.5 * o.pen_c[N - 1 - i] * (halo_at(a, 1, 1, p, 1, j, gu, gv) - gu[row + N]);
       if (j < o.np) dy = dy + 0.5 * o.pen_c[j] * (gv[col] - halo_at(a, 2, 2, p, 1, i, gv, gu));
       if (j >= N - o.np)
-        dy = dy + 0.5 * o.pen_c[N - 1 - j] * (halo_at(a, 2, 3, p, 1, i, gv, gu) - gv[col + (long long)N * g.P]);
+        dy = dy + 0.5 * o.pen_c[N - 1 - j] * (halo_at(a, 2, 3, p, 1, i, gv, gu) - gv[col + N * g.P]);
     }
-    const double dv = (dx + dy) / (a.Jp[e] * a.hx * a.radius);
+    const double dv = (dx + dy) * a.rJpha[e];
     if (a.flags & F_SEP) a.o1[e] = dv;
     else rk_put(a, 0, e, -1.0 * dv);
   }
   if (a.flags & F_COR) {
     const double gup = stag_at<W>(o.wi2c, a.Gu + row, 1, N, i);
     const double gvp = stag_at<W>(o.wi2c, a.Gv + col, g.P, N, j);
-    const double fuh = stag_at<W>(o.wi2c, a.fu + row, 1, N, i);
-    const double fvh = stag_at<W>(o.wi2c, a.fv + col, g.P, N, j);
-    const double cp = 0.5 * fuh + 0.5 * fvh;
-    a.cup[e] = (a.fp[e] + cp) * gvp / hh;
-    a.cvp[e] = -(a.fp[e] + cp) * gup / hh;
+    const double cp = stag_at<W>(o.wi2c, a.fu + row, 1, N, i);  // the curl at the centre
+    const double q = (a.fp[e] + cp) / hh;  // one division per point
+    a.cup[e] = q * gvp;
+    a.cvp[e] = -q * gup;
   }
 }
 
@@ -390,13 +399,13 @@ template <int ORD, class Fn>
 __device__ __forceinline__ double grad_line(const CArgs& a, int N, int i, Fn F) {
   const COps& o = a.ops;
   if (ORD == 21) {
-    const double hs = a.hx * a.radius;
-    if (i == 0) return (0.5 * F(1) + 0.5 * F(0) - 1.5 * F(-1) + 0.5 * F(-2)) / hs;
-    if (i == N) return (-0.5 * F(N - 2) - 0.5 * F(N - 1) + 1.5 * F(N) - 0.5 * F(N + 1)) / hs;
-    return (F(i) - F(i - 1)) / hs;
+    const double dx1 = a.dx1;
+    if (i == 0) return (0.5 * F(1) + 0.5 * F(0) - 1.5 * F(-1) + 0.5 * F(-2)) * dx1;
+    if (i == N) return (-0.5 * F(N - 2) - 0.5 * F(N - 1) + 1.5 * F(N) - 0.5 * F(N + 1)) * dx1;
+    return (F(i) - F(i - 1)) * dx1;
   } else {
     const StagOp& D = o.dc2i;
-    const double dx1 = 1.0 / (a.radius * a.hx);
+    const double dx1 = a.dx1;
     if (i <= 3) {
       double s = 0.0;
       for (int m = 0; m < D.last[i]; ++m) s += D.Ql[i * D.nw + m] * F(m);
@@ -436,7 +445,7 @@ __global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CA
   const int N = a.N;
   SWM_C_INDEX(N + 1, N + 1)
   const FieldGeom& g = a.g;
-  const long long e = at(g, p, i, j);
+  const int e = at(g, p, i, j);
   const double* f = a.ke_in;
   if (j < N) {  // u point
     double gx = 0.0, cu = 0.0;
@@ -456,7 +465,7 @@ __global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CA
       const double* colp = f + at(g, p, i, 0);
       gy = grad_line<ORD>(a, N, j, [&](int k) {
         return k < 0 ? halo_at(a, 0, 2, p, -k, i, f, f)
-                     : k >= N ? halo_at(a, 0, 3, p, k - N + 1, i, f, f) : colp[(long long)k * g.P];
+                     : k >= N ? halo_at(a, 0, 3, p, k - N + 1, i, f, f) : colp[k * g.P];
       });
     }
     if (a.flags & F_COR) cv = stag_at<W>(a.ops.wc2i, a.cvp + at(g, p, i, 0), g.P, N + 1, j);
@@ -521,14 +530,17 @@ CArgs base_args(const CGrid* c) {
   a.g = c->g; a.N = c->N; a.L = c->L;
   a.hx = c->hx; a.radius = c->radius; a.grav = c->grav;
   a.ops = c->ops;
-  a.Jp = c->metric(M_JP); a.Qi2p = c->metric(M_QI2P); a.fp = c->metric(M_FP);
-  a.Ju = c->metric(M_JU); a.Qi1u = c->metric(M_QI1U);
-  a.Jv = c->metric(M_JV); a.Qi3v = c->metric(M_QI3V); a.Jq = c->metric(M_JQ);
+  a.dx1 = 1.0 / (c->radius * c->hx);
+  a.Jp = c->metric(M_JP); a.fp = c->metric(M_FP); a.rJp = c->metric(M_RJP);
+  a.rJpha = c->metric(M_RJPHA); a.JQi2p = c->metric(M_JQI2P);
+  a.Ju = c->metric(M_JU); a.Qi1u = c->metric(M_QI1U); a.rJu = c->metric(M_RJU);
+  a.Jv = c->metric(M_JV); a.Qi3v = c->metric(M_QI3V); a.rJv = c->metric(M_RJV);
+  a.rJqha = c->metric(M_RJQHA);
   a.halo = c->halo;
   a.Ap = c->work(W_AP); a.Bp = c->work(W_BP); a.ut = c->work(W_UT); a.vt = c->work(W_VT);
   a.hu = c->work(W_HU); a.hv = c->work(W_HV); a.Gu = c->work(W_GU); a.Gv = c->work(W_GV);
   a.KEu = c->work(W_KEU); a.KEv = c->work(W_KEV); a.curl = c->work(W_CURL);
-  a.fu = c->work(W_FU); a.fv = c->work(W_FV); a.KE = c->work(W_KE);
+  a.fu = c->work(W_FU); a.KE = c->work(W_KE);
   a.cup = c->work(W_CUP); a.cvp = c->work(W_CVP);
   return a;
 }
@@ -545,7 +557,7 @@ const dim3 kBlock(32, 8, 1);
 SWM_C_LAUNCH(run_centre_a, centre_a_kernel, c->N, c->N)
 SWM_C_LAUNCH(run_faces_a, faces_a_kernel, c->N + 1, c->N + 1)
 SWM_C_LAUNCH(run_curl, curl_kernel, c->N + 1, c->N + 1)
-SWM_C_LAUNCH(run_w2uv, w2uv_kernel, c->N + 1, c->N + 1)
+SWM_C_LAUNCH(run_w2uv, w2uv_kernel, c->N + 1, c->N)
 SWM_C_LAUNCH(run_centre_b, centre_b_kernel, c->N, c->N)
 SWM_C_LAUNCH(run_faces_b, faces_b_kernel, c->N + 1, c->N + 1)
 #undef SWM_C_LAUNCH
@@ -697,8 +709,9 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     std::vector<double> hm(g.fs, 0.0);
     for (int k = 0; k < M_COUNT && e == cudaSuccess; ++k) {
       std::fill(hm.begin(), hm.end(), 0.0);
-      const bool ci = k <= M_FP || (k >= M_JV && k <= M_QI3V);  // centred in alpha
-      const bool cj = k <= M_QI1U;                              // centred in beta
+      const int mesh = kMetricMesh[k];
+      const bool ci = mesh == 0 || mesh == 2;  // centred in alpha
+      const bool cj = mesh == 0 || mesh == 1;  // centred in beta
       const int nx = ci ? N : N + 1, ny = cj ? N : N + 1;
       for (int p = 0; p < 6; ++p)
         for (int j = 0; j < ny; ++j)
@@ -707,9 +720,13 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
             const double be = -0.25 * kPiC + (j + (cj ? 0.5 : 0.0)) * c->hx;
             double J, q1, q2, q3, x;
             metric_at(al, be, J, q1, q2, q3);
+            const double jha = J * c->hx * radius;
             switch (k) {
               case M_QI2P: x = q2; break;
               case M_FP: x = coriolis_at(p, al, be, omega, ax); break;
+              case M_RJP: case M_RJU: case M_RJV: x = 1.0 / J; break;
+              case M_RJPHA: case M_RJQHA: x = 1.0 / jha; break;
+              case M_JQI2P: x = J * q2; break;
               case M_QI1U: x = q1; break;
               case M_QI3V: x = q3; break;
               default: x = J; break;
