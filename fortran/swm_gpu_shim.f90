@@ -292,7 +292,9 @@ function gpu_algebraic_dot(this, other, domain) result(dot_product)
     dot_product = r
 end function gpu_algebraic_dot
 
-! h, u, v: the reference's tile arrays, (N+1) x (N+1) x 6 in panel order
+! h, u, v: the reference's tile arrays in panel order, (N+1) x (N+1) x 6 on the
+! Ah grid; on the C grid h is N x N x 6, u (N+1) x N x 6, v N x (N+1) x 6
+! (swm_mesh_dims)
 subroutine gpu_upload(this, h, u, v)
     class(stvec_swm_gpu_t), intent(inout) :: this
     real(kind=8),           intent(in)    :: h(:,:,:), u(:,:,:), v(:,:,:)
