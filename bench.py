@@ -829,26 +829,36 @@ def cgrid_leg(local, steps, warmup, cpu=True):
     N, ORDER, DT = 384, 42, 37.5
     dev = torch.device("cuda", local)
     h, u, v, _ = initial.balanced_zonal_c(N, 11, 24)
-    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=ORDER, names=swm.c_grid_names(ORDER), device=local))
-    s0, s = op.create_stvec(), op.create_stvec()
-    s0.upload(h, u, v)
-    s.assign_s1v1(1.0, s0)
-    stream = torch.cuda.ExternalStream(op.stream, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     ts = swm.RK4()
-    for _ in range(warmup):
-        ts.step(s, op, DT, 1)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    torch.cuda.synchronize(dev)
-    for a, b in evs:
+
+    def timed(prec):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=ORDER, names=swm.c_grid_names(ORDER),
+                                             precision=prec, device=local))
+        s0, s = op.create_stvec(), op.create_stvec()
+        s0.upload(h, u, v)
         s.assign_s1v1(1.0, s0)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        a.record(stream)
-        ts.step(s, op, DT, 1)
-        b.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+        stream = torch.cuda.ExternalStream(op.stream, device=dev)
+        for _ in range(warmup):
+            ts.step(s, op, DT, 1)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize(dev)
+        for a, b in evs:
+            s.assign_s1v1(1.0, s0)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a.record(stream)
+            ts.step(s, op, DT, 1)
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        return op, s, sum(a.elapsed_time(b) for a, b in evs) / steps
+
+    op32, s32, ms32 = timed("fp32")
+    s32.upload(h, u, v)
+    ts.step(s32, op32, DT, 2)
+    got32 = s32.download()
+    del op32, s32
+    op, s, ms = timed("fp64")
     # end to end: upload from / download to page-locked host arrays, every step
     pins = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True) for a in (h, u, v) for _ in range(2)]
     hin = [pins[2 * k].numpy() for k in range(3)]
@@ -873,6 +883,8 @@ def cgrid_leg(local, steps, warmup, cpu=True):
                        "N=384 (6 x 384^2 centres, 6 x 385 x 384 faces per velocity component), FP64",
            "operators": swm.c_grid_names(ORDER), "dt_s": DT,
            "value": round(1e3 / ms, 3), "unit": "steps/s", "ms_per_step": round(ms, 5),
+           "fp32_form": {"value": round(1e3 / ms32, 3), "unit": "steps/s", "ms_per_step": round(ms32, 5),
+                         "note": "FP32 passes, FP32 (hi, lo) state pair, two-sum RK accumulation"},
            "launches_per_step": CGRID_LAUNCHES_PER_STEP,
            "e2e": {"value": round(e2e, 3), "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                    "d2h_bytes_per_step": nbytes,
@@ -896,6 +908,8 @@ def cgrid_leg(local, steps, warmup, cpu=True):
         el = time.perf_counter() - t0
         rel = max(float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(got, want))
         res["parity_vs_oracle_2_steps_max_rel_l2"] = rel
+        res["fp32_form"]["error_vs_oracle_2_steps_max_rel_l2"] = max(
+            float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(got32, want))
         res["cpu_oracle"] = {"value": round(2 / el, 4), "unit": "steps/s", "cores": threads, "kind": "port",
                              "sample": "2 RK4 steps of the same state at N=384 (C-grid oracle)"}
     return res

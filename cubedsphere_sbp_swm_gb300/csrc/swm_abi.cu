@@ -872,8 +872,6 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
       if (!want[k] || need[k] != want[k])
         return fail(nullptr, SWM_E_UNSUPPORTED,
                     std::string("C-grid family needs ") + need[k] + ", got " + (want[k] ? want[k] : "(null)"));
-    if (cfg->precision != SWM_FP64_PLAIN)
-      return fail(nullptr, SWM_E_UNSUPPORTED, "the C-grid operator family is FP64 only");
     cgrid_order = od;
   } else if (!div_op_name || !name_order(div_op_name, "divergence_ah", "_sbp", od))
     return fail(nullptr, SWM_E_UNSUPPORTED, std::string("unsupported div operator: ") + (div_op_name ? div_op_name : "(null)"));
@@ -959,7 +957,7 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     // quadrature weights are not set up
     ctx->order = cgrid_order;
     int rc = cgrid_create(ctx->g64, ctx->N, cgrid_order, cfg->radius, cfg->grav, cfg->omega, cfg->rotation_axis,
-                          ctx->st, &ctx->cg, why);
+                          ctx->prec == SWM_FP32_FUSED, ctx->st, &ctx->cg, why);
     if (rc) {
       free_ctx(ctx);
       return fail(nullptr, rc == 3 ? SWM_E_NOMEM : rc == 2 ? SWM_E_CUDA : SWM_E_INVALID, why);
@@ -1121,9 +1119,16 @@ int swm_state_upload(swm_ctx* ctx, swm_state* s, const double* h, const double* 
   USE_DEVICE(ctx);
   const double* src[3] = {h, u, v};
   if (ctx->cg) {
-    for (int c = 0; c < 3; ++c)
-      if (int rc = c_copy(ctx, SWM_MESH_P + c, (double*)s->hi + c * ctx->fs, src[c], nullptr)) return rc;
-    return SWM_OK;
+    for (int c = 0; c < 3; ++c) {
+      if (ctx->prec == SWM_FP64_PLAIN) {
+        if (int rc = c_copy(ctx, SWM_MESH_P + c, (double*)s->hi + c * ctx->fs, src[c], nullptr)) return rc;
+      } else {  // FP64 values through a device field, split into the (hi, lo) pair
+        double* t = tmpf(ctx, 11);
+        if (int rc = c_copy(ctx, SWM_MESH_P + c, t, src[c], nullptr)) return rc;
+        CK(launch_split_f64(ctx->fs, t, (float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs, ctx->st), "split");
+      }
+    }
+    return sync_check(ctx, ctx->st);
   }
   return put_packed(ctx, s, src, cudaMemcpyHostToDevice);
 }
@@ -1135,8 +1140,15 @@ int swm_state_download(swm_ctx* ctx, const swm_state* s, double* h, double* u, d
   USE_DEVICE(ctx);
   double* dst[3] = {h, u, v};
   if (ctx->cg) {
-    for (int c = 0; c < 3; ++c)
-      if (int rc = c_copy(ctx, SWM_MESH_P + c, (double*)s->hi + c * ctx->fs, nullptr, dst[c])) return rc;
+    for (int c = 0; c < 3; ++c) {
+      if (ctx->prec == SWM_FP64_PLAIN) {
+        if (int rc = c_copy(ctx, SWM_MESH_P + c, (double*)s->hi + c * ctx->fs, nullptr, dst[c])) return rc;
+      } else {  // the (hi, lo) pair joined into FP64
+        double* t = tmpf(ctx, 11);
+        CK(launch_join_f32pair(ctx->fs, (const float*)s->hi + c * ctx->fs, s->lo + c * ctx->fs, t, ctx->st), "join");
+        if (int rc = c_copy(ctx, SWM_MESH_P + c, t, nullptr, dst[c])) return rc;
+      }
+    }
     return SWM_OK;
   }
   if (int rc = get_packed(ctx, s, dst, cudaMemcpyDeviceToHost)) return rc;
@@ -1318,8 +1330,15 @@ int swm_apply(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   if (vout == vin) return fail(ctx, SWM_E_INVALID, "apply needs distinct in/out states");
   USE_DEVICE(ctx);
   if (ctx->cg) {
-    CK(cgrid_apply(ctx->cg, ctx->topo, ctx->edge64, ctx->hs64, (const double*)vin->hi, (double*)vout->hi, ctx->st),
-       "C-grid apply");
+    if (ctx->prec == SWM_FP64_PLAIN) {
+      CK(cgrid_apply(ctx->cg, ctx->topo, ctx->edge64, ctx->hs64, (const double*)vin->hi, (double*)vout->hi, ctx->st),
+         "C-grid apply");
+    } else {  // tendencies of the high part, in FP32
+      CK(cudaMemsetAsync(vout->lo, 0, sizeof(float) * 3 * ctx->fs, ctx->st), "memset");
+      CK(cgrid_apply32(ctx->cg, ctx->topo, (float*)ctx->edge, (const float*)ctx->hsT, (const float*)vin->hi,
+                       (float*)vout->hi, ctx->st),
+         "C-grid apply");
+    }
     return SWM_OK;
   }
   if (ctx->prec == SWM_FP64_PLAIN) {
@@ -1418,7 +1437,12 @@ int graph_steps(swm_ctx* ctx, swm_state* v0, double dt, int kind, int nsteps, F 
 
 int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
   if (ctx->cg) {
-    CK(cgrid_rk4(ctx->cg, ctx->topo, ctx->edge64, ctx->hs64, (double*)v0->hi, dt, ctx->st), "C-grid RK4 step");
+    if (ctx->prec == SWM_FP64_PLAIN)
+      CK(cgrid_rk4(ctx->cg, ctx->topo, ctx->edge64, ctx->hs64, (double*)v0->hi, dt, ctx->st), "C-grid RK4 step");
+    else
+      CK(cgrid_rk4_32(ctx->cg, ctx->topo, (float*)ctx->edge, (const float*)ctx->hsT, (float*)v0->hi, v0->lo, dt,
+                      ctx->st),
+         "C-grid RK4 step");
     return SWM_OK;
   }
   return ctx->prec == SWM_FP64_PLAIN ? enqueue_rk4<double>(ctx, v0, dt) : enqueue_rk4<float>(ctx, v0, dt);

@@ -42,23 +42,48 @@ constexpr int kMassThreads = 256;
 // 152-228): left closure rows Ql[r*nw + m] over inputs m < last[r]; the
 // right block mirrors them (times rsign); interior stencil Qin over inputs
 // k+inshift .. k+inshift+w-1.  dnx = outputs - inputs.
-struct StagOp {
+template <class T>
+struct StagOpT {
   int ne, nw, inshift, dnx;
-  double rsign;
+  T rsign;
   int last[4];
-  double Ql[24];
-  double Qin[4];
+  T Ql[24];
+  T Qin[4];
 };
 
-// The operators and SAT constants of one SBP order.
-struct COps {
-  StagOp wc2i, wi2c, dc2i, di2c;
-  int np;           // boundary projection length
-  double proj[3];   // boundary projection (left)
-  double pen_c[3];  // proj / A_centres: penalty of the divergence (at_center)
-  double a_i0;      // A_interfaces(1): penalty weight of the curl
-  double sq1;       // the gradient's first interface weight (7/18 at 4/2)
+// The operators and SAT constants of one SBP order, in the arithmetic type
+// of the kernels (FP32 copies rounded once on the host).
+template <class T>
+struct COpsT {
+  StagOpT<T> wc2i, wi2c, dc2i, di2c;
+  int np;      // boundary projection length
+  T proj[3];   // boundary projection (left)
+  T pen_c[3];  // proj / A_centres: penalty of the divergence (at_center)
+  T a_i0;      // A_interfaces(1): penalty weight of the curl
+  T sq1;       // the gradient's first interface weight (7/18 at 4/2)
 };
+using StagOp = StagOpT<double>;
+using COps = COpsT<double>;
+
+template <class T>
+StagOpT<T> stag_cast(const StagOp& s) {
+  StagOpT<T> r{};
+  r.ne = s.ne; r.nw = s.nw; r.inshift = s.inshift; r.dnx = s.dnx; r.rsign = T(s.rsign);
+  for (int k = 0; k < 4; ++k) { r.last[k] = s.last[k]; r.Qin[k] = T(s.Qin[k]); }
+  for (int k = 0; k < 24; ++k) r.Ql[k] = T(s.Ql[k]);
+  return r;
+}
+
+template <class T>
+COpsT<T> ops_cast(const COps& o) {
+  COpsT<T> r{};
+  r.wc2i = stag_cast<T>(o.wc2i); r.wi2c = stag_cast<T>(o.wi2c);
+  r.dc2i = stag_cast<T>(o.dc2i); r.di2c = stag_cast<T>(o.di2c);
+  r.np = o.np;
+  for (int k = 0; k < 3; ++k) { r.proj[k] = T(o.proj[k]); r.pen_c[k] = T(o.pen_c[k]); }
+  r.a_i0 = T(o.a_i0); r.sq1 = T(o.sq1);
+  return r;
+}
 
 // Tables of the staggered operators (sbp_operators_collection_mod.f90:88-193
 // and sbp_factory_mod.f90:38-179): the same numbers as the reference.
@@ -140,24 +165,26 @@ enum : int {
   F_SEP = 256,     // centre_b / faces_b: write the operator's own output, not a tendency
 };
 
-struct CArgs {
+template <class T>
+struct CArgsT {
   FieldGeom g;
   int N, L, flags;
-  double hx, radius, grav;
-  double dx1;  // 1 / (a hx), the gradient's scale
-  COps ops;
-  const double *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha;
+  T hx, radius, grav;
+  T dx1;  // 1 / (a hx), the gradient's scale
+  COpsT<T> ops;
+  const T *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha;
   const int* halo;
   // inputs
-  const double *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
+  const T *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
   // intermediate and unfused outputs
-  double *Ap, *Bp, *ut, *vt, *hu, *hv, *Gu, *Gv, *KEu, *KEv, *curl, *fu, *KE, *cup, *cvp;
-  double *o1, *o2;  // unfused outputs of centre_b (div) / faces_b (gx|cor_u, gy|cor_v)
+  T *Ap, *Bp, *ut, *vt, *hu, *hv, *Gu, *Gv, *KEu, *KEv, *curl, *fu, *KE, *cup, *cvp;
+  T *o1, *o2;  // unfused outputs of centre_b (div) / faces_b (gx|cor_u, gy|cor_v)
   // RK4 stage epilogue: mode 0 writes the tendency to tend, 1..4 the stages
-  // of rk4_mod.f90:20-42 (y0, Y, Kb, acc: 3 fields each, fs apart)
+  // of rk4_mod.f90:20-42 (y0, Y, Kb, acc: 3 fields each, fs apart; FP32:
+  // y0 / lo the state pair, acc the running increment, no Kb)
   int mode;
-  double hdt, dt, c3, c6;
-  double *tend, *y0, *Y, *Kb, *acc;
+  T hdt, dt, c3, c6;
+  T *tend, *y0, *Y, *Kb, *acc, *lo;
 };
 
 // element offset within a field (fields stay below 2^31 elements)
@@ -166,12 +193,12 @@ __device__ __forceinline__ int at(const FieldGeom& g, int p, int i, int j) {
 }
 
 // sbp_apply for output k of nout outputs over a line f with stride st
-template <int W>
-__device__ __forceinline__ double stag_at(const StagOp& s, const double* __restrict__ f, int st, int nout,
+template <int W, class T>
+__device__ __forceinline__ T stag_at(const StagOpT<T>& s, const T* __restrict__ f, int st, int nout,
                                           int k) {
-  double acc = 0.0;
+  T acc = T(0.0);
   if (k >= s.ne && k < nout - s.ne) {
-    const double* b = f + (k + s.inshift) * st;
+    const T* b = f + (k + s.inshift) * st;
 #pragma unroll
     for (int t = 0; t < W; ++t) acc += s.Qin[t] * b[t * st];
   } else if (k < s.ne) {
@@ -186,21 +213,47 @@ __device__ __forceinline__ double stag_at(const StagOp& s, const double* __restr
 // value of a neighbour's point in the cross halo: mesh 0 o, 1 u, 2 v; side 0
 // left, 1 right, 2 bottom, 3 top; depth d >= 1; k along the side.  f is the
 // field of the mesh, g the other component of a C vector.
-__device__ __forceinline__ double halo_at(const CArgs& a, int mesh, int side, int p, int d, int k,
-                                          const double* __restrict__ f, const double* __restrict__ g) {
+template <class T>
+__device__ __forceinline__ T halo_at(const CArgsT<T>& a, int mesh, int side, int p, int d, int k,
+                                          const T* __restrict__ f, const T* __restrict__ g) {
   const int c = __ldg(&a.halo[((((mesh * 4 + side) * 6 + p) * kHaloDepth + (d - 1)) * a.L) + k]);
-  const double x = ((c & 2) ? g : f)[c >> 2];
+  const T x = ((c & 2) ? g : f)[c >> 2];
   return (c & 1) ? -x : x;
 }
 
-__device__ __forceinline__ void rk_put(const CArgs& a, int comp, int e, double k) {
+template <class T>
+__device__ __forceinline__ void rk_put(const CArgsT<T>& a, int comp, int e, T k) {
   const int o = comp * (int)a.g.fs + e;
-  switch (a.mode) {
-    case 0: a.tend[o] = k; break;
-    case 1: a.Kb[o] = k; a.Y[o] = 1.0 * a.y0[o] + a.hdt * k; break;
-    case 2: a.acc[o] = (a.y0[o] + a.c6 * a.Kb[o]) + a.c3 * k; a.Y[o] = 1.0 * a.y0[o] + a.hdt * k; break;
-    case 3: a.Kb[o] = k; a.Y[o] = 1.0 * a.y0[o] + a.dt * k; break;
-    default: a.y0[o] = (a.acc[o] + a.c3 * a.Kb[o]) + a.c6 * k; break;
+  if constexpr (sizeof(T) == 8) {
+    // FP64: the reference's order, y = 1*y0 + c k and
+    // y0 = (y0 + dt/6 k1 + dt/3 k2) + dt/3 k3 + dt/6 k4
+    switch (a.mode) {
+      case 0: a.tend[o] = k; break;
+      case 1: a.Kb[o] = k; a.Y[o] = T(1.0) * a.y0[o] + a.hdt * k; break;
+      case 2: a.acc[o] = (a.y0[o] + a.c6 * a.Kb[o]) + a.c3 * k; a.Y[o] = T(1.0) * a.y0[o] + a.hdt * k; break;
+      case 3: a.Kb[o] = k; a.Y[o] = T(1.0) * a.y0[o] + a.dt * k; break;
+      default: a.y0[o] = (a.acc[o] + a.c3 * a.Kb[o]) + a.c6 * k; break;
+    }
+  } else {
+    // FP32 compensated form (as on the Ah grid): the stage increments add up
+    // apart from the state, and the last stage adds them to the (hi, lo)
+    // state pair with an exact two-sum
+    switch (a.mode) {
+      case 0: a.tend[o] = k; break;
+      case 1: a.Y[o] = a.y0[o] + a.hdt * k; a.acc[o] = a.c6 * k; break;
+      case 2: a.Y[o] = a.y0[o] + a.hdt * k; a.acc[o] = a.acc[o] + a.c3 * k; break;
+      case 3: a.Y[o] = a.y0[o] + a.dt * k; a.acc[o] = a.acc[o] + a.c3 * k; break;
+      default: {
+        const T d = a.acc[o] + a.c6 * k;
+        const T hi = a.y0[o], lo = a.lo[o];
+        const T t = lo + d;
+        const T s = hi + t;
+        const T bb = s - hi;
+        a.y0[o] = s;
+        a.lo[o] = (hi - (s - bb)) + (t - bb);
+        break;
+      }
+    }
   }
 }
 
@@ -212,100 +265,100 @@ __device__ __forceinline__ void rk_put(const CArgs& a, int comp, int e, double k
 
 // co2contra_c_sbp (co2contra_Cgrid_mod.f90:292-437), first half: the other
 // covariant component interpolated to the centres times J Qi12 there.
-template <int ORD>
-__global__ void __launch_bounds__(256) centre_a_kernel(const __grid_constant__ CArgs a) {
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) centre_a_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N, N)
   const FieldGeom& g = a.g;
   const int e = at(g, p, i, j);
-  const double jq = a.JQi2p[e];
-  a.Ap[e] = jq * stag_at<W>(a.ops.wi2c, a.v + at(g, p, i, 0), g.P, N, j);
-  a.Bp[e] = jq * stag_at<W>(a.ops.wi2c, a.u + at(g, p, 0, j), 1, N, i);
+  const T jq = a.JQi2p[e];
+  a.Ap[e] = jq * stag_at<W, T>(a.ops.wi2c, a.v + at(g, p, i, 0), g.P, N, j);
+  a.Bp[e] = jq * stag_at<W, T>(a.ops.wi2c, a.u + at(g, p, 0, j), 1, N, i);
 }
 
 // co2contra second half, massflux_c_sbp (massflux_Cgrid_mod.f90:298-358),
 // J * flux (div_c_sbp42_mod.f90:109-143, coriolis_Cgrid_mod.f90:83-97) and
 // the kinetic-energy densities (KE_Cgrid_mod.f90:41-58) on the faces.
-template <int ORD>
-__global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CArgs a) {
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N + 1, N + 1)
   const FieldGeom& g = a.g;
   const int e = at(g, p, i, j);
   if (j < N) {  // u point
-    double ut;
+    T ut;
     if (a.flags & F_CO) {
-      const double t = stag_at<W>(a.ops.wc2i, a.Ap + at(g, p, 0, j), 1, N + 1, i);
+      const T t = stag_at<W, T>(a.ops.wc2i, a.Ap + at(g, p, 0, j), 1, N + 1, i);
       ut = a.Qi1u[e] * a.u[e] + t * a.rJu[e];
       a.ut[e] = ut;
     } else {
-      ut = a.ut_in ? a.ut_in[e] : 0.0;
+      ut = a.ut_in ? a.ut_in[e] : T(0.0);
     }
     if (a.flags & F_MF) {
-      const double hu = ut * stag_at<W>(a.ops.wc2i, a.h + at(g, p, 0, j), 1, N + 1, i);
+      const T hu = ut * stag_at<W, T>(a.ops.wc2i, a.h + at(g, p, 0, j), 1, N + 1, i);
       a.hu[e] = hu;
       if (a.flags & F_G) a.Gu[e] = hu * a.Ju[e];
     } else if (a.flags & F_G) {
       a.Gu[e] = a.hu_in[e] * a.Ju[e];
     }
-    if (a.flags & F_KE) a.KEu[e] = a.Ju[e] * (a.u[e] * ut) * 0.5;
+    if (a.flags & F_KE) a.KEu[e] = a.Ju[e] * (a.u[e] * ut) * T(0.5);
   }
   if (i < N) {  // v point
-    double vt;
+    T vt;
     if (a.flags & F_CO) {
-      const double t = stag_at<W>(a.ops.wc2i, a.Bp + at(g, p, i, 0), g.P, N + 1, j);
+      const T t = stag_at<W, T>(a.ops.wc2i, a.Bp + at(g, p, i, 0), g.P, N + 1, j);
       vt = a.Qi3v[e] * a.v[e] + t * a.rJv[e];
       a.vt[e] = vt;
     } else {
-      vt = a.vt_in ? a.vt_in[e] : 0.0;
+      vt = a.vt_in ? a.vt_in[e] : T(0.0);
     }
     if (a.flags & F_MF) {
-      const double hv = vt * stag_at<W>(a.ops.wc2i, a.h + at(g, p, i, 0), g.P, N + 1, j);
+      const T hv = vt * stag_at<W, T>(a.ops.wc2i, a.h + at(g, p, i, 0), g.P, N + 1, j);
       a.hv[e] = hv;
       if (a.flags & F_G) a.Gv[e] = hv * a.Jv[e];
     } else if (a.flags & F_G) {
       a.Gv[e] = a.hv_in[e] * a.Jv[e];
     }
-    if (a.flags & F_KE) a.KEv[e] = a.Jv[e] * (a.v[e] * vt) * 0.5;
+    if (a.flags & F_KE) a.KEv[e] = a.Jv[e] * (a.v[e] * vt) * T(0.5);
   }
 }
 
 // curl_c_sbp (curl/curl_c_sbp_mod.f90:44-127) before the corner sync: the
 // staggered differences of the covariant components onto the corners, with
 // the SAT penalties on their jumps across the panel edges.
-template <int ORD>
-__global__ void __launch_bounds__(256) curl_kernel(const __grid_constant__ CArgs a) {
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) curl_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N + 1, N + 1)
   const FieldGeom& g = a.g;
-  const COps& o = a.ops;
-  const double* vrow = a.v + at(g, p, 0, j);
-  const double* ucol = a.u + at(g, p, i, 0);
-  double dvx = stag_at<W>(o.dc2i, vrow, 1, N + 1, i);
+  const COpsT<T>& o = a.ops;
+  const T* vrow = a.v + at(g, p, 0, j);
+  const T* ucol = a.u + at(g, p, i, 0);
+  T dvx = stag_at<W, T>(o.dc2i, vrow, 1, N + 1, i);
   if (i == 0) {
-    double dv = 0.0;
+    T dv = T(0.0);
     for (int m = 0; m < o.np; ++m) dv = dv + o.proj[m] * (vrow[m] - halo_at(a, 2, 0, p, m + 1, j, a.v, a.u));
-    dvx = dvx + 0.5 * dv / o.a_i0;
+    dvx = dvx + T(0.5) * dv / o.a_i0;
   }
   if (i == N) {
-    double dv = 0.0;
+    T dv = T(0.0);
     for (int m = 0; m < o.np; ++m) dv = dv + o.proj[m] * (halo_at(a, 2, 1, p, m + 1, j, a.v, a.u) - vrow[N - 1 - m]);
-    dvx = dvx + 0.5 * dv / o.a_i0;
+    dvx = dvx + T(0.5) * dv / o.a_i0;
   }
-  double duy = stag_at<W>(o.dc2i, ucol, g.P, N + 1, j);
+  T duy = stag_at<W, T>(o.dc2i, ucol, g.P, N + 1, j);
   if (j == 0) {
-    double du = 0.0;
+    T du = T(0.0);
     for (int m = 0; m < o.np; ++m) du = du + o.proj[m] * (ucol[m * g.P] - halo_at(a, 1, 2, p, m + 1, i, a.u, a.v));
-    duy = duy + 0.5 * du / o.a_i0;
+    duy = duy + T(0.5) * du / o.a_i0;
   }
   if (j == N) {
-    double du = 0.0;
+    T du = T(0.0);
     for (int m = 0; m < o.np; ++m)
       du = du + o.proj[m] * (halo_at(a, 1, 3, p, m + 1, i, a.u, a.v) - ucol[(N - 1 - m) * g.P]);
-    duy = duy + 0.5 * du / o.a_i0;
+    duy = duy + T(0.5) * du / o.a_i0;
   }
   const int e = at(g, p, i, j);
   a.curl[e] = (dvx - duy) * a.rJqha[e];
@@ -316,77 +369,77 @@ __global__ void __launch_bounds__(256) curl_kernel(const __grid_constant__ CArgs
 // tensor-product interpolations to the centres, x after y and y after x;
 // the 1-D operators act on different indices, so both are the same linear
 // map and one of them is evaluated (the results agree to round-off).
-template <int ORD>
-__global__ void __launch_bounds__(256) w2uv_kernel(const __grid_constant__ CArgs a) {
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) w2uv_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N + 1, N)
   const FieldGeom& g = a.g;
-  a.fu[at(g, p, i, j)] = stag_at<W>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
+  a.fu[at(g, p, i, j)] = stag_at<W, T>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
 }
 
 // Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
 // (operator_swm_mod.f90:84-85), the divergence (div_c_sbp42_mod.f90:67-107,
 // div_c2_mod.f90:97-177) and the Coriolis terms at the centres
 // (coriolis_Cgrid_mod.f90:98-118).
-template <int ORD>
-__global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ CArgs a) {
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N, N)
   const FieldGeom& g = a.g;
-  const COps& o = a.ops;
+  const COpsT<T>& o = a.ops;
   const int e = at(g, p, i, j);
   const int row = at(g, p, 0, j), col = at(g, p, i, 0);
   // h of this point, read before the RK epilogue of stages 2 and 3 writes
   // the new h in place over it
-  const double hh = (a.flags & (F_ADDGH | F_COR)) ? a.h[e] : 0.0;
+  const T hh = (a.flags & (F_ADDGH | F_COR)) ? a.h[e] : T(0.0);
   if (a.flags & F_KE) {
-    double ke = (stag_at<W>(o.wi2c, a.KEu + row, 1, N, i) + stag_at<W>(o.wi2c, a.KEv + col, g.P, N, j)) * a.rJp[e];
-    if (a.flags & F_ADDGH) ke = ke + a.grav * hh + a.grav * (a.hs ? a.hs[e] : 0.0);
+    T ke = (stag_at<W, T>(o.wi2c, a.KEu + row, 1, N, i) + stag_at<W, T>(o.wi2c, a.KEv + col, g.P, N, j)) * a.rJp[e];
+    if (a.flags & F_ADDGH) ke = ke + a.grav * hh + a.grav * (a.hs ? a.hs[e] : T(0.0));
     a.KE[e] = ke;
   }
   if (a.flags & F_DIV) {
-    double dx, dy;
+    T dx, dy;
     if (ORD == 21) {
-      const double* hu = a.hu_in;
-      const double* hv = a.hv_in;
+      const T* hu = a.hu_in;
+      const T* hv = a.hv_in;
       auto u = [&](int ii) { return ii < 0 ? halo_at(a, 1, 0, p, 1, j, hu, hv)
                                             : ii > N ? halo_at(a, 1, 1, p, 1, j, hu, hv) : hu[row + ii]; };
       auto v = [&](int jj) { return jj < 0 ? halo_at(a, 2, 2, p, 1, i, hv, hu)
                                             : jj > N ? halo_at(a, 2, 3, p, 1, i, hv, hu) : hv[col + jj * g.P]; };
       auto Ju = [&](int ii) { return a.Ju[row + ii]; };
       auto Jv = [&](int jj) { return a.Jv[col + jj * g.P]; };
-      if (i == 0) dx = Ju(1) * u(1) - Ju(0) * (0.25 * u(0) + 0.75 * u(-1));
-      else if (i == 1) dx = Ju(2) * u(2) - Ju(1) * u(1) - 0.25 * Ju(0) * (u(0) - u(-1));
-      else if (i == N - 2) dx = Ju(N - 1) * u(N - 1) - Ju(N - 2) * u(N - 2) + 0.25 * Ju(N) * (u(N) - u(N + 1));
-      else if (i == N - 1) dx = Ju(N) * (0.75 * u(N + 1) + 0.25 * u(N)) - Ju(N - 1) * u(N - 1);
+      if (i == 0) dx = Ju(1) * u(1) - Ju(0) * (T(0.25) * u(0) + T(0.75) * u(-1));
+      else if (i == 1) dx = Ju(2) * u(2) - Ju(1) * u(1) - T(0.25) * Ju(0) * (u(0) - u(-1));
+      else if (i == N - 2) dx = Ju(N - 1) * u(N - 1) - Ju(N - 2) * u(N - 2) + T(0.25) * Ju(N) * (u(N) - u(N + 1));
+      else if (i == N - 1) dx = Ju(N) * (T(0.75) * u(N + 1) + T(0.25) * u(N)) - Ju(N - 1) * u(N - 1);
       else dx = Ju(i + 1) * u(i + 1) - Ju(i) * u(i);
-      if (j == 0) dy = Jv(1) * v(1) - Jv(0) * (0.25 * v(0) + 0.75 * v(-1));
-      else if (j == 1) dy = Jv(2) * v(2) - Jv(1) * v(1) - 0.25 * Jv(0) * (v(0) - v(-1));
-      else if (j == N - 2) dy = Jv(N - 1) * v(N - 1) - Jv(N - 2) * v(N - 2) + 0.25 * Jv(N) * (v(N) - v(N + 1));
-      else if (j == N - 1) dy = Jv(N) * (0.75 * v(N + 1) + 0.25 * v(N)) - Jv(N - 1) * v(N - 1);
+      if (j == 0) dy = Jv(1) * v(1) - Jv(0) * (T(0.25) * v(0) + T(0.75) * v(-1));
+      else if (j == 1) dy = Jv(2) * v(2) - Jv(1) * v(1) - T(0.25) * Jv(0) * (v(0) - v(-1));
+      else if (j == N - 2) dy = Jv(N - 1) * v(N - 1) - Jv(N - 2) * v(N - 2) + T(0.25) * Jv(N) * (v(N) - v(N + 1));
+      else if (j == N - 1) dy = Jv(N) * (T(0.75) * v(N + 1) + T(0.25) * v(N)) - Jv(N - 1) * v(N - 1);
       else dy = Jv(j + 1) * v(j + 1) - Jv(j) * v(j);
     } else {
-      const double* gu = a.Gu;
-      const double* gv = a.Gv;
-      dx = stag_at<W>(o.di2c, gu + row, 1, N, i);
-      dy = stag_at<W>(o.di2c, gv + col, g.P, N, j);
-      if (i < o.np) dx = dx + 0.5 * o.pen_c[i] * (gu[row] - halo_at(a, 1, 0, p, 1, j, gu, gv));
-      if (i >= N - o.np) dx = dx + 0.5 * o.pen_c[N - 1 - i] * (halo_at(a, 1, 1, p, 1, j, gu, gv) - gu[row + N]);
-      if (j < o.np) dy = dy + 0.5 * o.pen_c[j] * (gv[col] - halo_at(a, 2, 2, p, 1, i, gv, gu));
+      const T* gu = a.Gu;
+      const T* gv = a.Gv;
+      dx = stag_at<W, T>(o.di2c, gu + row, 1, N, i);
+      dy = stag_at<W, T>(o.di2c, gv + col, g.P, N, j);
+      if (i < o.np) dx = dx + T(0.5) * o.pen_c[i] * (gu[row] - halo_at(a, 1, 0, p, 1, j, gu, gv));
+      if (i >= N - o.np) dx = dx + T(0.5) * o.pen_c[N - 1 - i] * (halo_at(a, 1, 1, p, 1, j, gu, gv) - gu[row + N]);
+      if (j < o.np) dy = dy + T(0.5) * o.pen_c[j] * (gv[col] - halo_at(a, 2, 2, p, 1, i, gv, gu));
       if (j >= N - o.np)
-        dy = dy + 0.5 * o.pen_c[N - 1 - j] * (halo_at(a, 2, 3, p, 1, i, gv, gu) - gv[col + N * g.P]);
+        dy = dy + T(0.5) * o.pen_c[N - 1 - j] * (halo_at(a, 2, 3, p, 1, i, gv, gu) - gv[col + N * g.P]);
     }
-    const double dv = (dx + dy) * a.rJpha[e];
+    const T dv = (dx + dy) * a.rJpha[e];
     if (a.flags & F_SEP) a.o1[e] = dv;
-    else rk_put(a, 0, e, -1.0 * dv);
+    else rk_put(a, 0, e, -T(1.0) * dv);
   }
   if (a.flags & F_COR) {
-    const double gup = stag_at<W>(o.wi2c, a.Gu + row, 1, N, i);
-    const double gvp = stag_at<W>(o.wi2c, a.Gv + col, g.P, N, j);
-    const double cp = stag_at<W>(o.wi2c, a.fu + row, 1, N, i);  // the curl at the centre
-    const double q = (a.fp[e] + cp) / hh;  // one division per point
+    const T gup = stag_at<W, T>(o.wi2c, a.Gu + row, 1, N, i);
+    const T gvp = stag_at<W, T>(o.wi2c, a.Gv + col, g.P, N, j);
+    const T cp = stag_at<W, T>(o.wi2c, a.fu + row, 1, N, i);  // the curl at the centre
+    const T q = (a.fp[e] + cp) / hh;  // one division per point
     a.cup[e] = q * gvp;
     a.cvp[e] = -q * gup;
   }
@@ -395,42 +448,42 @@ __global__ void __launch_bounds__(256) centre_b_kernel(const __grid_constant__ C
 // covariant gradient of the centre field f at face i (gradient_c_sbp42,
 // grad_c_sbp42_mod.f90:44-139; gradient_c_sbp21, grad_c2_ecs_mod.f90:234-293)
 // along a line: F(k) for 0 <= k < N from the panel, else the o halo.
-template <int ORD, class Fn>
-__device__ __forceinline__ double grad_line(const CArgs& a, int N, int i, Fn F) {
-  const COps& o = a.ops;
+template <int ORD, class T, class Fn>
+__device__ __forceinline__ T grad_line(const CArgsT<T>& a, int N, int i, Fn F) {
+  const COpsT<T>& o = a.ops;
   if (ORD == 21) {
-    const double dx1 = a.dx1;
-    if (i == 0) return (0.5 * F(1) + 0.5 * F(0) - 1.5 * F(-1) + 0.5 * F(-2)) * dx1;
-    if (i == N) return (-0.5 * F(N - 2) - 0.5 * F(N - 1) + 1.5 * F(N) - 0.5 * F(N + 1)) * dx1;
+    const T dx1 = a.dx1;
+    if (i == 0) return (T(0.5) * F(1) + T(0.5) * F(0) - T(1.5) * F(-1) + T(0.5) * F(-2)) * dx1;
+    if (i == N) return (-T(0.5) * F(N - 2) - T(0.5) * F(N - 1) + T(1.5) * F(N) - T(0.5) * F(N + 1)) * dx1;
     return (F(i) - F(i - 1)) * dx1;
   } else {
-    const StagOp& D = o.dc2i;
-    const double dx1 = a.dx1;
+    const StagOpT<T>& D = o.dc2i;
+    const T dx1 = a.dx1;
     if (i <= 3) {
-      double s = 0.0;
+      T s = T(0.0);
       for (int m = 0; m < D.last[i]; ++m) s += D.Ql[i * D.nw + m] * F(m);
-      double gv = s * dx1;
+      T gv = s * dx1;
       if (i == 0) {
-        const double dh =
+        const T dh =
             (o.proj[0] * (F(0) - F(-1)) + o.proj[1] * (F(1) - F(-2)) + o.proj[2] * (F(2) - F(-3))) * dx1;
-        gv = gv + 0.5 * dh / o.sq1;
+        gv = gv + T(0.5) * dh / o.sq1;
       }
       return gv;
     }
     if (i <= N - 4) {
-      double s = 0.0;
+      T s = T(0.0);
 #pragma unroll
       for (int t = 0; t < 4; ++t) s += F(i - 2 + t) * D.Qin[t];
       return s * dx1;
     }
     const int r = N - i;
-    double s = 0.0;
+    T s = T(0.0);
     for (int m = 0; m < D.last[r]; ++m) s += D.Ql[r * D.nw + m] * F(N - 1 - m);
-    double gv = -s * dx1;
+    T gv = -s * dx1;
     if (i == N) {
-      const double dh =
+      const T dh =
           (o.proj[0] * (F(N) - F(N - 1)) + o.proj[1] * (F(N + 1) - F(N - 2)) + o.proj[2] * (F(N + 2) - F(N - 3))) * dx1;
-      gv = gv + 0.5 * dh / o.sq1;
+      gv = gv + T(0.5) * dh / o.sq1;
     }
     return gv;
   }
@@ -439,38 +492,38 @@ __device__ __forceinline__ double grad_line(const CArgs& a, int N, int i, Fn F) 
 // Face pass: the gradient of the kinetic energy and the Coriolis term
 // interpolated from the centres (interpolator_p2uv_mod.f90:98-115), combined
 // into the u, v tendencies (operator_swm_mod.f90:95-96).
-template <int ORD>
-__global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CArgs a) {
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N + 1, N + 1)
   const FieldGeom& g = a.g;
   const int e = at(g, p, i, j);
-  const double* f = a.ke_in;
+  const T* f = a.ke_in;
   if (j < N) {  // u point
-    double gx = 0.0, cu = 0.0;
+    T gx = T(0.0), cu = T(0.0);
     if (a.flags & F_GRAD) {
-      const double* rowp = f + at(g, p, 0, j);
-      gx = grad_line<ORD>(a, N, i, [&](int k) {
+      const T* rowp = f + at(g, p, 0, j);
+      gx = grad_line<ORD, T>(a, N, i, [&](int k) {
         return k < 0 ? halo_at(a, 0, 0, p, -k, j, f, f) : k >= N ? halo_at(a, 0, 1, p, k - N + 1, j, f, f) : rowp[k];
       });
     }
-    if (a.flags & F_COR) cu = stag_at<W>(a.ops.wc2i, a.cup + at(g, p, 0, j), 1, N + 1, i);
+    if (a.flags & F_COR) cu = stag_at<W, T>(a.ops.wc2i, a.cup + at(g, p, 0, j), 1, N + 1, i);
     if (a.flags & F_SEP) a.o1[e] = (a.flags & F_GRAD) ? gx : cu;
-    else rk_put(a, 1, e, -1.0 * gx + 1.0 * cu);
+    else rk_put(a, 1, e, -T(1.0) * gx + T(1.0) * cu);
   }
   if (i < N) {  // v point
-    double gy = 0.0, cv = 0.0;
+    T gy = T(0.0), cv = T(0.0);
     if (a.flags & F_GRAD) {
-      const double* colp = f + at(g, p, i, 0);
-      gy = grad_line<ORD>(a, N, j, [&](int k) {
+      const T* colp = f + at(g, p, i, 0);
+      gy = grad_line<ORD, T>(a, N, j, [&](int k) {
         return k < 0 ? halo_at(a, 0, 2, p, -k, i, f, f)
                      : k >= N ? halo_at(a, 0, 3, p, k - N + 1, i, f, f) : colp[k * g.P];
       });
     }
-    if (a.flags & F_COR) cv = stag_at<W>(a.ops.wc2i, a.cvp + at(g, p, i, 0), g.P, N + 1, j);
+    if (a.flags & F_COR) cv = stag_at<W, T>(a.ops.wc2i, a.cvp + at(g, p, i, 0), g.P, N + 1, j);
     if (a.flags & F_SEP) a.o2[e] = (a.flags & F_GRAD) ? gy : cv;
-    else rk_put(a, 2, e, -1.0 * gy + 1.0 * cv);
+    else rk_put(a, 2, e, -T(1.0) * gy + T(1.0) * cv);
   }
 }
 
@@ -513,7 +566,9 @@ struct CGrid {
   int N = 0, order = 42, L = 0;
   double hx = 0.0, radius = 1.0, grav = 9.80616;
   COps ops{};
+  COpsT<float> ops32{};
   double* met = nullptr;   // M_COUNT fields
+  float* met32 = nullptr;  // their FP32 copies (contexts of the FP32 form)
   double* wk = nullptr;    // W_COUNT fields
   double* rk = nullptr;    // Y, Kb, acc: 3 fields each
   int* halo = nullptr;
@@ -525,23 +580,32 @@ struct CGrid {
 
 namespace {
 
-CArgs base_args(const CGrid* c) {
-  CArgs a{};
+// Kernel arguments in precision T: FP64 metric and work fields, or the
+// FP32 metric copies and the same work buffers read as floats.
+template <class T>
+CArgsT<T> base_args(const CGrid* c) {
+  CArgsT<T> a{};
   a.g = c->g; a.N = c->N; a.L = c->L;
-  a.hx = c->hx; a.radius = c->radius; a.grav = c->grav;
-  a.ops = c->ops;
-  a.dx1 = 1.0 / (c->radius * c->hx);
-  a.Jp = c->metric(M_JP); a.fp = c->metric(M_FP); a.rJp = c->metric(M_RJP);
-  a.rJpha = c->metric(M_RJPHA); a.JQi2p = c->metric(M_JQI2P);
-  a.Ju = c->metric(M_JU); a.Qi1u = c->metric(M_QI1U); a.rJu = c->metric(M_RJU);
-  a.Jv = c->metric(M_JV); a.Qi3v = c->metric(M_QI3V); a.rJv = c->metric(M_RJV);
-  a.rJqha = c->metric(M_RJQHA);
+  a.hx = T(c->hx); a.radius = T(c->radius); a.grav = T(c->grav);
+  if constexpr (sizeof(T) == 8) a.ops = c->ops;
+  else a.ops = c->ops32;
+  a.dx1 = T(1.0 / (c->radius * c->hx));
+  auto M = [&](int k) -> const T* {
+    if constexpr (sizeof(T) == 8) return c->metric(k);
+    else return c->met32 + (long long)k * c->g.fs;
+  };
+  auto Wk = [&](int k) { return reinterpret_cast<T*>(c->work(k)); };
+  a.Jp = M(M_JP); a.fp = M(M_FP); a.rJp = M(M_RJP);
+  a.rJpha = M(M_RJPHA); a.JQi2p = M(M_JQI2P);
+  a.Ju = M(M_JU); a.Qi1u = M(M_QI1U); a.rJu = M(M_RJU);
+  a.Jv = M(M_JV); a.Qi3v = M(M_QI3V); a.rJv = M(M_RJV);
+  a.rJqha = M(M_RJQHA);
   a.halo = c->halo;
-  a.Ap = c->work(W_AP); a.Bp = c->work(W_BP); a.ut = c->work(W_UT); a.vt = c->work(W_VT);
-  a.hu = c->work(W_HU); a.hv = c->work(W_HV); a.Gu = c->work(W_GU); a.Gv = c->work(W_GV);
-  a.KEu = c->work(W_KEU); a.KEv = c->work(W_KEV); a.curl = c->work(W_CURL);
-  a.fu = c->work(W_FU); a.KE = c->work(W_KE);
-  a.cup = c->work(W_CUP); a.cvp = c->work(W_CVP);
+  a.Ap = Wk(W_AP); a.Bp = Wk(W_BP); a.ut = Wk(W_UT); a.vt = Wk(W_VT);
+  a.hu = Wk(W_HU); a.hv = Wk(W_HV); a.Gu = Wk(W_GU); a.Gv = Wk(W_GV);
+  a.KEu = Wk(W_KEU); a.KEv = Wk(W_KEV); a.curl = Wk(W_CURL);
+  a.fu = Wk(W_FU); a.KE = Wk(W_KE);
+  a.cup = Wk(W_CUP); a.cvp = Wk(W_CVP);
   return a;
 }
 
@@ -549,9 +613,10 @@ dim3 grid_for(int nx, int ny) { return dim3((nx + 31) / 32, (ny + 7) / 8, 6); }
 const dim3 kBlock(32, 8, 1);
 
 #define SWM_C_LAUNCH(name, kern, nx, ny)                                                              \
-  cudaError_t name(const CGrid* c, const CArgs& a, cudaStream_t st) {                                 \
-    if (c->order == 42) kern<42><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                             \
-    else kern<21><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                                            \
+  template <class T>                                                                                   \
+  cudaError_t name(const CGrid* c, const CArgsT<T>& a, cudaStream_t st) {                             \
+    if (c->order == 42) kern<42, T><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                          \
+    else kern<21, T><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                                         \
     return cudaGetLastError();                                                                         \
   }
 SWM_C_LAUNCH(run_centre_a, centre_a_kernel, c->N, c->N)
@@ -569,14 +634,15 @@ SWM_C_LAUNCH(run_faces_b, faces_b_kernel, c->N + 1, c->N + 1)
   } while (0)
 
 // One right-hand side of the state (h, u, v) with the epilogue of a.mode.
-cudaError_t rhs(const CGrid* c, const Topology& tp, double* edge, CArgs a, const double* in, cudaStream_t st) {
+template <class T>
+cudaError_t rhs(const CGrid* c, const Topology& tp, T* edge, CArgsT<T> a, const T* in, cudaStream_t st) {
   const long long fs = c->g.fs;
   a.h = in; a.u = in + fs; a.v = in + 2 * fs;
   a.flags = F_CO | F_MF | F_G | F_KE;
   CKE(run_centre_a(c, a, st));
   CKE(run_faces_a(c, a, st));
   CKE(run_curl(c, a, st));
-  CKE(launch_sync_scalar(c->g, tp, a.curl, edge, st));
+  CKE(launch_sync_scalar_t<T>(c->g, tp, a.curl, edge, st));
   a.curl_in = a.curl;
   CKE(run_w2uv(c, a, st));
   a.hu_in = a.hu; a.hv_in = a.hv;
@@ -665,7 +731,7 @@ bool build_halo(int N, const FieldGeom& g, std::vector<int>& tab, std::string& w
 }  // namespace
 
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
-                 cudaStream_t st, CGrid** out, std::string& why) {
+                 bool fp32, cudaStream_t st, CGrid** out, std::string& why) {
   *out = nullptr;
   if (order != 21 && order != 42) { why = "C-grid SBP order must be 21 or 42"; return 1; }
   if (N < 12) { why = "C grid needs N >= 12"; return 1; }
@@ -674,6 +740,7 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   c->hx = (0.25 * kPiC - (-0.25 * kPiC)) / (double)N;
   c->radius = radius; c->grav = grav;
   fill_ops(order, c->ops);
+  c->ops32 = ops_cast<float>(c->ops);
   const double an = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
   const double ax[3] = {axis[0] / an, axis[1] / an, axis[2] / an};
   std::vector<int> tab;
@@ -738,6 +805,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
     ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
     ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
+    if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
+      ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
     ok(cudaMemcpyAsync(c->wts, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st));
     ok(cudaStreamSynchronize(st));  // the host buffers go out of scope
   }
@@ -752,7 +821,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
 
 void cgrid_destroy(CGrid* c) {
   if (!c) return;
-  for (void* p : {(void*)c->met, (void*)c->wk, (void*)c->rk, (void*)c->halo, (void*)c->wts, (void*)c->part})
+  for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->halo, (void*)c->wts,
+                  (void*)c->part})
     if (p) cudaFree(p);
   delete c;
 }
@@ -766,7 +836,7 @@ void cgrid_mesh_dims(const CGrid* c, int mesh, int* nx, int* ny) {
 }
 
 cudaError_t cgrid_co2contra(CGrid* c, const double* u, const double* v, double* ut, double* vt, cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.u = u; a.v = v; a.ut = ut; a.vt = vt;
   a.flags = F_CO;
   CKE(run_centre_a(c, a, st));
@@ -775,7 +845,7 @@ cudaError_t cgrid_co2contra(CGrid* c, const double* u, const double* v, double* 
 
 cudaError_t cgrid_massflux(CGrid* c, const double* h, const double* ut, const double* vt, double* hu, double* hv,
                            cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.h = h; a.ut_in = ut; a.vt_in = vt; a.hu = hu; a.hv = hv;
   a.flags = F_MF;
   return run_faces_a(c, a, st);
@@ -783,7 +853,7 @@ cudaError_t cgrid_massflux(CGrid* c, const double* h, const double* ut, const do
 
 cudaError_t cgrid_ke(CGrid* c, const double* u, const double* v, const double* ut, const double* vt, double* ke,
                      cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.u = u; a.v = v; a.ut_in = ut; a.vt_in = vt; a.KE = ke;
   a.flags = F_KE;
   CKE(run_faces_a(c, a, st));
@@ -791,14 +861,14 @@ cudaError_t cgrid_ke(CGrid* c, const double* u, const double* v, const double* u
 }
 
 cudaError_t cgrid_grad(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.ke_in = f; a.o1 = gx; a.o2 = gy;
   a.flags = F_GRAD | F_SEP;
   return run_faces_b(c, a, st);
 }
 
 cudaError_t cgrid_div(CGrid* c, const double* hu, const double* hv, double* div, cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.hu_in = hu; a.hv_in = hv; a.o1 = div;
   if (c->order == 42) {
     a.flags = F_G;
@@ -810,7 +880,7 @@ cudaError_t cgrid_div(CGrid* c, const double* hu, const double* hv, double* div,
 
 cudaError_t cgrid_curl(CGrid* c, const Topology& tp, double* edge, const double* u, const double* v, double* curl,
                        cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.u = u; a.v = v; a.curl = curl;
   CKE(run_curl(c, a, st));
   return launch_sync_scalar(c->g, tp, curl, edge, st);
@@ -818,7 +888,7 @@ cudaError_t cgrid_curl(CGrid* c, const Topology& tp, double* edge, const double*
 
 cudaError_t cgrid_coriolis(CGrid* c, const double* hu, const double* hv, const double* h, const double* curl,
                            double* cor_u, double* cor_v, cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.hu_in = hu; a.hv_in = hv; a.h = h; a.curl_in = curl;
   a.flags = F_G;
   CKE(run_faces_a(c, a, st));
@@ -832,11 +902,41 @@ cudaError_t cgrid_coriolis(CGrid* c, const double* hu, const double* hv, const d
 
 cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double* hs, const double* in, double* out,
                         cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.hs = hs;
   a.mode = 0;
   a.tend = out;
   return rhs(c, tp, edge, a, in, st);
+}
+
+cudaError_t cgrid_apply32(CGrid* c, const Topology& tp, float* edge, const float* hs, const float* in, float* out,
+                          cudaStream_t st) {
+  if (!c->met32) return cudaErrorInvalidValue;
+  CArgsT<float> a = base_args<float>(c);
+  a.hs = hs;
+  a.mode = 0;
+  a.tend = out;
+  return rhs(c, tp, edge, a, in, st);
+}
+
+// The FP32 form: stage inputs are the state's high part (stage 1) or Y in
+// FP32; the increments add up in acc and the last stage adds them to the
+// (hi, lo) pair with an exact two-sum.  In-place safety as for FP64.
+cudaError_t cgrid_rk4_32(CGrid* c, const Topology& tp, float* edge, const float* hs, float* hi, float* lo, double dt,
+                         cudaStream_t st) {
+  if (!c->met32) return cudaErrorInvalidValue;
+  CArgsT<float> a = base_args<float>(c);
+  a.hs = hs;
+  a.dt = float(dt); a.hdt = float(0.5 * dt); a.c6 = float(dt / 6.0); a.c3 = float(dt / 3.0);
+  a.y0 = hi;
+  a.lo = lo;
+  a.Y = reinterpret_cast<float*>(c->rk);
+  a.acc = a.Y + 3 * c->g.fs;
+  for (int s = 1; s <= 4; ++s) {
+    a.mode = s;
+    CKE(rhs(c, tp, edge, a, s == 1 ? static_cast<const float*>(hi) : a.Y, st));
+  }
+  return cudaSuccess;
 }
 
 // Stage 1 reads y0 and writes Y; stages 2 and 3 read Y and write Y in place;
@@ -846,7 +946,7 @@ cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double
 // of it, before writing it.
 cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* hs, double* y0, double dt,
                       cudaStream_t st) {
-  CArgs a = base_args(c);
+  CArgsT<double> a = base_args<double>(c);
   a.hs = hs;
   a.dt = dt; a.hdt = 0.5 * dt; a.c6 = dt / 6.0; a.c3 = dt / 3.0;
   a.y0 = y0;

@@ -27,8 +27,9 @@ struct CGrid;
 
 // Builds the metric of the four meshes, the cross-halo tables of the
 // one-tile-per-panel exchanges and the work fields; order 21 or 42.
+// fp32: also keep FP32 copies of the metric for the FP32 form's passes.
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega,
-                 const double axis[3], cudaStream_t st, CGrid** out, std::string& why);
+                 const double axis[3], bool fp32, cudaStream_t st, CGrid** out, std::string& why);
 void cgrid_destroy(CGrid* c);
 int cgrid_order(const CGrid* c);
 // points per panel row (nx) and rows (ny) of a mesh
@@ -56,6 +57,13 @@ cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double
 // One rk4_t%step of the state y0 in place (rk4_mod.f90:20-42).
 cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* hs, double* y0,
                       double dt, cudaStream_t st);
+// The FP32 form (contexts created with fp32): the same passes in FP32 on
+// FP32 states; the RK4 step keeps the state as an FP32 (hi, lo) pair and
+// adds the stage increments with an exact two-sum.
+cudaError_t cgrid_apply32(CGrid* c, const Topology& tp, float* edge, const float* hs, const float* in,
+                          float* out, cudaStream_t st);
+cudaError_t cgrid_rk4_32(CGrid* c, const Topology& tp, float* edge, const float* hs, float* hi, float* lo,
+                         double dt, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

@@ -282,10 +282,53 @@ def test_ah_only_entry_points_refuse_c_grid():
         op.get_diagnostics(s)
     assert e.value.code == swm._abi.SWM_E_UNSUPPORTED
     with pytest.raises(swm.SwmError) as e:
-        swm.OperatorSWM(swm.ModelConfig(N=24, sbp_order=42, names=swm.c_grid_names(42), precision="fp32"))
+        s.algebraic_norm2()
     assert e.value.code == swm._abi.SWM_E_UNSUPPORTED
     names = swm.c_grid_names(42)
     names["curl_op_name"] = "curl_c_sbp21"
     with pytest.raises(swm.SwmError) as e:
         swm.OperatorSWM(swm.ModelConfig(N=24, sbp_order=42, names=names))
     assert e.value.code == swm._abi.SWM_E_UNSUPPORTED
+
+
+@pytest.mark.parametrize("order,steps", [(42, 1), (42, 24), (21, 24)])
+def test_fp32_form_rk4_against_fp64_oracle(order, steps):
+    """The FP32 form (FP32 passes, FP32 (hi, lo) state pair with a two-sum
+    RK accumulation) against the FP64 oracle: within 1e-5 relative L2 for
+    h, u and v (the bound of the Ah grid's FP32 form), mass drift within
+    1e-6 of the oracle's."""
+    N = 40
+    op, od = c_op(N, order, precision="fp32"), oracle.OracleCDomain(N, order)
+    h, u, v = _state(N, 7)
+    dt = 600.0 * 24 / N
+    s = op.create_stvec()
+    s.upload(h, u, v)
+    swm.RK4().step(s, op, dt, steps)
+    want = od.rk4(h, u, v, dt, steps)
+    got = s.download()
+    for a, b in zip(got, want):
+        assert _rel(a, b) < 1e-5, _rel(a, b)
+    assert abs(od.mass(got[0]) - od.mass(want[0])) / od.mass(want[0]) < 1e-6
+
+
+def test_fp32_form_state_pair_round_trip_and_apply():
+    """Upload splits FP64 values into the (hi, lo) pair and download joins
+    them back (2^-47 relative); the FP32 apply is within 1e-4 of the FP64
+    oracle's tendencies.  The state is perturbed off balance: the tendencies
+    of a balanced flow are the small difference of large terms, and FP32
+    rounding of those terms is then visible at 1e-4 .. 1e-3 of the result."""
+    N = 24
+    op, od = c_op(N, 42, precision="fp32"), oracle.OracleCDomain(N, 42)
+    h, u, v = _state(N, 5)
+    rng = np.random.default_rng(8)
+    h = h + 20.0 * rng.standard_normal(h.shape)
+    u = u + 2.0 * rng.standard_normal(u.shape)
+    v = v + 2.0 * rng.standard_normal(v.shape)
+    s = op.create_stvec()
+    s.upload(h, u, v)
+    for a, b in zip(s.download(), (h, u, v)):
+        assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)) <= 2.0 ** -47
+    t = s.create_similar()
+    op.apply(t, s)
+    for a, b in zip(t.download(), od.apply(h, u, v)):
+        assert _rel(a, b) < 1e-4, _rel(a, b)
