@@ -897,6 +897,10 @@ def cgrid_leg(local, steps, warmup, cpu=True):
                        "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                        "algorithmic_bytes_per_step": CGRID_WORDS_PER_POINT_STEP * 8 * npts,
                        "scope": "whole RK4 step (32 launches)"}
+    a32 = CGRID_WORDS_PER_POINT_STEP * 4 * npts / (ms32 / 1e3) / 1e9
+    res["fp32_form"]["roofline"] = {"bound": "hbm", "achieved": round(a32, 1), "peak": peak, "unit": "GB/s",
+                                    "frac": round(a32 / peak, 4), "peak_source": peak_kind,
+                                    "algorithmic_bytes_per_step": CGRID_WORDS_PER_POINT_STEP * 4 * npts}
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle  # the checker and the timed CPU baseline
