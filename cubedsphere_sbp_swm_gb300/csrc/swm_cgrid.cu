@@ -489,6 +489,25 @@ __device__ __forceinline__ T grad_line(const CArgsT<T>& a, int N, int i, Fn F) {
   }
 }
 
+// The gradient at an interior face (4 <= i <= N-4 at 4/2, 1 <= i <= N-1 at
+// 2/1), f0 pointing at the centre value F(i), st the stride along the line:
+// the interior rows of grad_line with direct loads, in the same order.
+template <int ORD, class T>
+__device__ __forceinline__ bool grad_interior(int N, int i) {
+  return ORD == 21 ? (i >= 1 && i <= N - 1) : (i >= 4 && i <= N - 4);
+}
+template <int ORD, class T>
+__device__ __forceinline__ T grad_in(const CArgsT<T>& a, const T* __restrict__ f0, int st) {
+  if (ORD == 21) return (f0[0] - f0[-st]) * a.dx1;
+  const T* q = a.ops.dc2i.Qin;
+  T s = T(0.0);
+  s += f0[-2 * st] * q[0];
+  s += f0[-st] * q[1];
+  s += f0[0] * q[2];
+  s += f0[st] * q[3];
+  return s * a.dx1;
+}
+
 // Face pass: the gradient of the kinetic energy and the Coriolis term
 // interpolated from the centres (interpolator_p2uv_mod.f90:98-115), combined
 // into the u, v tendencies (operator_swm_mod.f90:95-96).
@@ -504,9 +523,12 @@ __global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CA
     T gx = T(0.0), cu = T(0.0);
     if (a.flags & F_GRAD) {
       const T* rowp = f + at(g, p, 0, j);
-      gx = grad_line<ORD, T>(a, N, i, [&](int k) {
-        return k < 0 ? halo_at(a, 0, 0, p, -k, j, f, f) : k >= N ? halo_at(a, 0, 1, p, k - N + 1, j, f, f) : rowp[k];
-      });
+      if (grad_interior<ORD, T>(N, i))
+        gx = grad_in<ORD, T>(a, rowp + i, 1);
+      else
+        gx = grad_line<ORD, T>(a, N, i, [&](int k) {
+          return k < 0 ? halo_at(a, 0, 0, p, -k, j, f, f) : k >= N ? halo_at(a, 0, 1, p, k - N + 1, j, f, f) : rowp[k];
+        });
     }
     if (a.flags & F_COR) cu = stag_at<W, T>(a.ops.wc2i, a.cup + at(g, p, 0, j), 1, N + 1, i);
     if (a.flags & F_SEP) a.o1[e] = (a.flags & F_GRAD) ? gx : cu;
@@ -516,10 +538,13 @@ __global__ void __launch_bounds__(256) faces_b_kernel(const __grid_constant__ CA
     T gy = T(0.0), cv = T(0.0);
     if (a.flags & F_GRAD) {
       const T* colp = f + at(g, p, i, 0);
-      gy = grad_line<ORD, T>(a, N, j, [&](int k) {
-        return k < 0 ? halo_at(a, 0, 2, p, -k, i, f, f)
-                     : k >= N ? halo_at(a, 0, 3, p, k - N + 1, i, f, f) : colp[k * g.P];
-      });
+      if (grad_interior<ORD, T>(N, j))
+        gy = grad_in<ORD, T>(a, colp + j * g.P, g.P);
+      else
+        gy = grad_line<ORD, T>(a, N, j, [&](int k) {
+          return k < 0 ? halo_at(a, 0, 2, p, -k, i, f, f)
+                       : k >= N ? halo_at(a, 0, 3, p, k - N + 1, i, f, f) : colp[k * g.P];
+        });
     }
     if (a.flags & F_COR) cv = stag_at<W, T>(a.ops.wc2i, a.cvp + at(g, p, i, 0), g.P, N + 1, j);
     if (a.flags & F_SEP) a.o2[e] = (a.flags & F_GRAD) ? gy : cv;

@@ -332,3 +332,18 @@ def test_fp32_form_state_pair_round_trip_and_apply():
     op.apply(t, s)
     for a, b in zip(t.download(), od.apply(h, u, v)):
         assert _rel(a, b) < 1e-4, _rel(a, b)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-5)])
+def test_bench_configuration_against_oracle(prec, tol):
+    """The C-grid bench workload itself (N=384, SBP 4/2, dt = 37.5 s, the
+    seeded balanced flow of bench.py's c_grid leg): two RK4 steps against
+    the FP64 oracle."""
+    N, dt = 384, 37.5
+    op, od = c_op(N, 42, precision=prec), oracle.OracleCDomain(N, 42)
+    h, u, v, _ = initial.balanced_zonal_c(N, 11, 24)
+    s = op.create_stvec()
+    s.upload(h, u, v)
+    swm.RK4().step(s, op, dt, 2)
+    for a, b in zip(s.download(), od.rk4(h, u, v, dt, 2)):
+        assert _rel(a, b) < tol, _rel(a, b)
