@@ -320,8 +320,8 @@ class StvecSWM:
         takes their values for every later call; the arrays must stay
         unchanged until OperatorSWM.synchronize().  Page-locked arrays let
         the copy overlap the context's kernels."""
-        for a in (h, u, v):
-            _check_c_f64(a, self.op.shape)
+        for a, sh in zip((h, u, v), self.op.state_shapes):
+            _check_c_f64(a, sh)
         self.op._check(self.op._L.swm_state_upload_async(self.op._h, self._h, _ptr(h), _ptr(u), _ptr(v)))
 
     def download(self, out=None):
@@ -335,8 +335,8 @@ class StvecSWM:
         (swm_state_download_async): the state as the calls queued before
         leave it, moved by the copy engine on the context's download stream;
         `out` holds it once OperatorSWM.synchronize() returns."""
-        for a in out:
-            _check_c_f64(a, self.op.shape)
+        for a, sh in zip(out, self.op.state_shapes):
+            _check_c_f64(a, sh)
         self.op._check(self.op._L.swm_state_download_async(self.op._h, self._h, *(_ptr(a) for a in out)))
         return out
 

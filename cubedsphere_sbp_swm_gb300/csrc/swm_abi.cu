@@ -1183,7 +1183,6 @@ extern "C" {
 
 int swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h, const double* u,
                            const double* v) {
-  AH_ONLY(ctx, "swm_state_upload_async");
   TraceRange trace_("swm_state_upload_async");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
@@ -1196,11 +1195,23 @@ int swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h, const do
   const double* src[3] = {h, u, v};
   // the copy engine fills buffer k once the unpack that last read it is done
   CK(cudaStreamWaitEvent(ctx->xst[0], ctx->xdone[0][k], 0), "wait");
-  for (int c = 0; c < 3; ++c)
-    CK(cudaMemcpyAsync(B + c * np, src[c], sizeof(double) * np, cudaMemcpyHostToDevice, ctx->xst[0]),
+  for (int c = 0; c < 3; ++c) {
+    int nx, ny;
+    mesh_dims(ctx, SWM_MESH_P + c, &nx, &ny);   // C grid: the component's own mesh
+    CK(cudaMemcpyAsync(B + c * np, src[c], sizeof(double) * 6 * nx * ny, cudaMemcpyHostToDevice, ctx->xst[0]),
        "upload");
+  }
   CK(cudaEventRecord(ctx->xready[0][k], ctx->xst[0]), "event record");
   CK(cudaStreamWaitEvent(ctx->st, ctx->xready[0][k], 0), "wait");
+  if (ctx->cg) {
+    const bool pair = ctx->prec == SWM_FP32_FUSED;
+    for (int c = 0; c < 3; ++c)
+      CK(cgrid_unpack(ctx->cg, SWM_MESH_P + c, B + c * np,
+                      (char*)s->hi + (size_t)ctx->elt * c * ctx->fs, pair ? s->lo + c * ctx->fs : nullptr, ctx->st),
+         "unpack");
+    CK(cudaEventRecord(ctx->xdone[0][k], ctx->st), "event record");
+    return SWM_OK;
+  }
   PackedFields pf{{B, B + np, B + 2 * np}};
   CK(launch_unpack_state(ctx->g64, 3, pf, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr,
                          ctx->st),
@@ -1210,7 +1221,6 @@ int swm_state_upload_async(swm_ctx* ctx, swm_state* s, const double* h, const do
 }
 
 int swm_state_download_async(swm_ctx* ctx, const swm_state* s, double* h, double* u, double* v) {
-  AH_ONLY(ctx, "swm_state_download_async");
   TraceRange trace_("swm_state_download_async");
   if (int rc = check_state(ctx, s)) return rc;
   if (!h || !u || !v) return fail(ctx, SWM_E_INVALID, "null host array");
@@ -1223,15 +1233,26 @@ int swm_state_download_async(swm_ctx* ctx, const swm_state* s, double* h, double
   double* dst[3] = {h, u, v};
   // the state is packed into buffer k once the copy that last read it is done
   CK(cudaStreamWaitEvent(ctx->st, ctx->xdone[1][k], 0), "wait");
-  PackedFields pf{{B, B + np, B + 2 * np}};
-  CK(launch_pack_state(ctx->g64, 3, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr, pf,
-                       ctx->st),
-     "pack");
+  if (ctx->cg) {
+    const bool pair = ctx->prec == SWM_FP32_FUSED;
+    for (int c = 0; c < 3; ++c)
+      CK(cgrid_pack(ctx->cg, SWM_MESH_P + c, (const char*)s->hi + (size_t)ctx->elt * c * ctx->fs,
+                    pair ? s->lo + c * ctx->fs : nullptr, B + c * np, ctx->st),
+         "pack");
+  } else {
+    PackedFields pf{{B, B + np, B + 2 * np}};
+    CK(launch_pack_state(ctx->g64, 3, s->hi, ctx->prec == SWM_FP32_FUSED ? s->lo : nullptr, pf,
+                         ctx->st),
+       "pack");
+  }
   CK(cudaEventRecord(ctx->xready[1][k], ctx->st), "event record");
   CK(cudaStreamWaitEvent(ctx->xst[1], ctx->xready[1][k], 0), "wait");
-  for (int c = 0; c < 3; ++c)
-    CK(cudaMemcpyAsync(dst[c], B + c * np, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->xst[1]),
+  for (int c = 0; c < 3; ++c) {
+    int nx, ny;
+    mesh_dims(ctx, SWM_MESH_P + c, &nx, &ny);
+    CK(cudaMemcpyAsync(dst[c], B + c * np, sizeof(double) * 6 * nx * ny, cudaMemcpyDeviceToHost, ctx->xst[1]),
        "download");
+  }
   CK(cudaEventRecord(ctx->xdone[1][k], ctx->xst[1]), "event record");
   return SWM_OK;
 }

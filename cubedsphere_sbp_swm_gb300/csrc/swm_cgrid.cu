@@ -576,6 +576,38 @@ __global__ void __launch_bounds__(kMassThreads) mass_partial_kernel(FieldGeom g,
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// A mesh field in the dense host layout (i fastest, then j, then panel) to
+// or from its pitched device field: FP64, or split into / joined from the
+// FP32 (hi, lo) pair as the Ah-grid transfers do.
+__global__ void cunpack_kernel(FieldGeom g, int nx, int ny, const double* __restrict__ src, double* d64,
+                               float* hi, float* lo) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 6LL * nx * ny) return;
+  const int i = (int)(k % nx);
+  const long long r = k / nx;
+  const int j = (int)(r % ny), p = (int)(r / ny);
+  const long long e = (long long)p * g.ps + (long long)j * g.P + i;
+  const double x = src[k];
+  if (lo) {
+    const float h = (float)x;
+    hi[e] = h;
+    lo[e] = (float)(x - (double)h);
+  } else {
+    d64[e] = x;
+  }
+}
+
+__global__ void cpack_kernel(FieldGeom g, int nx, int ny, const double* __restrict__ d64, const float* hi,
+                             const float* lo, double* __restrict__ dst) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 6LL * nx * ny) return;
+  const int i = (int)(k % nx);
+  const long long r = k / nx;
+  const int j = (int)(r % ny), p = (int)(r / ny);
+  const long long e = (long long)p * g.ps + (long long)j * g.P + i;
+  dst[k] = lo ? (double)hi[e] + (double)lo[e] : d64[e];
+}
+
 __global__ void mass_final_kernel(const double* part, int n, double* out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
@@ -983,6 +1015,24 @@ cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* 
     CKE(rhs(c, tp, edge, a, s == 1 ? y0 : a.Y, st));
   }
   return cudaSuccess;
+}
+
+cudaError_t cgrid_unpack(CGrid* c, int mesh, const double* dense, void* field, float* lo, cudaStream_t st) {
+  int nx, ny;
+  cgrid_mesh_dims(c, mesh, &nx, &ny);
+  const long long n = 6LL * nx * ny;
+  cunpack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c->g, nx, ny, dense, lo ? nullptr : (double*)field,
+                                                              lo ? (float*)field : nullptr, lo);
+  return cudaGetLastError();
+}
+
+cudaError_t cgrid_pack(CGrid* c, int mesh, const void* field, const float* lo, double* dense, cudaStream_t st) {
+  int nx, ny;
+  cgrid_mesh_dims(c, mesh, &nx, &ny);
+  const long long n = 6LL * nx * ny;
+  cpack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c->g, nx, ny, lo ? nullptr : (const double*)field,
+                                                            lo ? (const float*)field : nullptr, lo, dense);
+  return cudaGetLastError();
 }
 
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st) {

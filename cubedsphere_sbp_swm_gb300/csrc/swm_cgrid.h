@@ -64,6 +64,11 @@ cudaError_t cgrid_apply32(CGrid* c, const Topology& tp, float* edge, const float
                           float* out, cudaStream_t st);
 cudaError_t cgrid_rk4_32(CGrid* c, const Topology& tp, float* edge, const float* hs, float* hi, float* lo,
                          double dt, cudaStream_t st);
+// A mesh field in the dense host layout (6 panels of ny rows of nx points)
+// to / from its pitched device field: FP64 (lo == nullptr), or the FP32
+// (hi, lo) pair, split from / joined into FP64.
+cudaError_t cgrid_unpack(CGrid* c, int mesh, const double* dense, void* field, float* lo, cudaStream_t st);
+cudaError_t cgrid_pack(CGrid* c, int mesh, const void* field, const float* lo, double* dense, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

@@ -347,3 +347,30 @@ def test_bench_configuration_against_oracle(prec, tol):
     swm.RK4().step(s, op, dt, 2)
     for a, b in zip(s.download(), od.rk4(h, u, v, dt, 2)):
         assert _rel(a, b) < tol, _rel(a, b)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_async_transfers_on_staggered_meshes(prec):
+    """upload_async -> steps -> download_async gives the bytes of the
+    synchronous route on the C grid (each component in its own mesh shape),
+    and a state changed right after download_async does not change what the
+    download returns."""
+    import torch
+    N = 32
+    op = c_op(N, 42, precision=prec)
+    h, u, v = _state(N, 6)
+    pins = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True) for a in (h, u, v) for _ in range(2)]
+    src = [pins[2 * k].numpy() for k in range(3)]
+    dst = tuple(pins[2 * k + 1].numpy() for k in range(3))
+    for p_, a in zip(src, (h, u, v)):
+        p_[...] = a
+    s_sync, s_async = op.create_stvec(), op.create_stvec()
+    s_sync.upload(h, u, v)
+    s_async.upload_async(*src)
+    swm.RK4().step(s_sync, op, 300.0, 2)
+    swm.RK4().step(s_async, op, 300.0, 2)
+    s_async.download_async(dst)
+    s_async.assign_s1(-1.0)
+    op.synchronize()
+    for a, b in zip(s_sync.download(), dst):
+        assert np.array_equal(a, b)
