@@ -163,13 +163,15 @@ enum : int {
   F_COR = 64,      // centre_b: Coriolis terms at the centres; faces_b: back to the faces
   F_GRAD = 128,    // faces_b: gradient
   F_SEP = 256,     // centre_b / faces_b: write the operator's own output, not a tendency
+  F_WUT = 512,     // faces_a: store the contravariant components (unfused co2contra)
+  F_WFLUX = 1024,  // faces_a: store the mass fluxes (unfused massflux; the 2/1 divergence)
 };
 
 template <class T>
 struct CArgsT {
   FieldGeom g;
   int N, L, flags;
-  T hx, radius, grav;
+  T grav;
   T dx1;  // 1 / (a hx), the gradient's scale
   COpsT<T> ops;
   const T *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha;
@@ -292,13 +294,13 @@ __global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CA
     if (a.flags & F_CO) {
       const T t = stag_at<W, T>(a.ops.wc2i, a.Ap + at(g, p, 0, j), 1, N + 1, i);
       ut = a.Qi1u[e] * a.u[e] + t * a.rJu[e];
-      a.ut[e] = ut;
+      if (a.flags & F_WUT) a.ut[e] = ut;
     } else {
       ut = a.ut_in ? a.ut_in[e] : T(0.0);
     }
     if (a.flags & F_MF) {
       const T hu = ut * stag_at<W, T>(a.ops.wc2i, a.h + at(g, p, 0, j), 1, N + 1, i);
-      a.hu[e] = hu;
+      if (a.flags & F_WFLUX) a.hu[e] = hu;
       if (a.flags & F_G) a.Gu[e] = hu * a.Ju[e];
     } else if (a.flags & F_G) {
       a.Gu[e] = a.hu_in[e] * a.Ju[e];
@@ -310,13 +312,13 @@ __global__ void __launch_bounds__(256) faces_a_kernel(const __grid_constant__ CA
     if (a.flags & F_CO) {
       const T t = stag_at<W, T>(a.ops.wc2i, a.Bp + at(g, p, i, 0), g.P, N + 1, j);
       vt = a.Qi3v[e] * a.v[e] + t * a.rJv[e];
-      a.vt[e] = vt;
+      if (a.flags & F_WUT) a.vt[e] = vt;
     } else {
       vt = a.vt_in ? a.vt_in[e] : T(0.0);
     }
     if (a.flags & F_MF) {
       const T hv = vt * stag_at<W, T>(a.ops.wc2i, a.h + at(g, p, i, 0), g.P, N + 1, j);
-      a.hv[e] = hv;
+      if (a.flags & F_WFLUX) a.hv[e] = hv;
       if (a.flags & F_G) a.Gv[e] = hv * a.Jv[e];
     } else if (a.flags & F_G) {
       a.Gv[e] = a.hv_in[e] * a.Jv[e];
@@ -643,7 +645,7 @@ template <class T>
 CArgsT<T> base_args(const CGrid* c) {
   CArgsT<T> a{};
   a.g = c->g; a.N = c->N; a.L = c->L;
-  a.hx = T(c->hx); a.radius = T(c->radius); a.grav = T(c->grav);
+  a.grav = T(c->grav);
   if constexpr (sizeof(T) == 8) a.ops = c->ops;
   else a.ops = c->ops32;
   a.dx1 = T(1.0 / (c->radius * c->hx));
@@ -695,7 +697,7 @@ template <class T>
 cudaError_t rhs(const CGrid* c, const Topology& tp, T* edge, CArgsT<T> a, const T* in, cudaStream_t st) {
   const long long fs = c->g.fs;
   a.h = in; a.u = in + fs; a.v = in + 2 * fs;
-  a.flags = F_CO | F_MF | F_G | F_KE;
+  a.flags = F_CO | F_MF | F_G | F_KE | (c->order == 21 ? F_WFLUX : 0);
   CKE(run_centre_a(c, a, st));
   CKE(run_faces_a(c, a, st));
   CKE(run_curl(c, a, st));
@@ -895,7 +897,7 @@ void cgrid_mesh_dims(const CGrid* c, int mesh, int* nx, int* ny) {
 cudaError_t cgrid_co2contra(CGrid* c, const double* u, const double* v, double* ut, double* vt, cudaStream_t st) {
   CArgsT<double> a = base_args<double>(c);
   a.u = u; a.v = v; a.ut = ut; a.vt = vt;
-  a.flags = F_CO;
+  a.flags = F_CO | F_WUT;
   CKE(run_centre_a(c, a, st));
   return run_faces_a(c, a, st);
 }
@@ -904,7 +906,7 @@ cudaError_t cgrid_massflux(CGrid* c, const double* h, const double* ut, const do
                            cudaStream_t st) {
   CArgsT<double> a = base_args<double>(c);
   a.h = h; a.ut_in = ut; a.vt_in = vt; a.hu = hu; a.hv = hv;
-  a.flags = F_MF;
+  a.flags = F_MF | F_WFLUX;
   return run_faces_a(c, a, st);
 }
 

@@ -374,3 +374,26 @@ def test_async_transfers_on_staggered_meshes(prec):
     op.synchronize()
     for a, b in zip(s_sync.download(), dst):
         assert np.array_equal(a, b)
+
+
+def test_c_grid_argument_errors():
+    """Argument errors come back as SWM_E_INVALID / SWM_E_UNSUPPORTED, with
+    no device work: a grid below the closures' reach, an unknown mesh, a
+    field on the wrong mesh for an operator, the corner sync of a
+    non-corner field."""
+    with pytest.raises(swm.SwmError) as e:
+        c_op(8, 42)
+    assert e.value.code in (swm._abi.SWM_E_INVALID, swm._abi.SWM_E_UNSUPPORTED)
+    op = c_op(24, 42)
+    with pytest.raises(KeyError):
+        op.create_field("w")
+    ut, vt = field(op, "u"), field(op, "v")
+    with pytest.raises(swm.SwmError) as e:
+        op.co2contra(ut, vt, field(op, "p"), field(op, "v"))       # u on the wrong mesh
+    assert e.value.code == swm._abi.SWM_E_INVALID
+    with pytest.raises(swm.SwmError) as e:
+        op._check(op._L.swm_sync_scalar(op._h, field(op, "p")._h))
+    assert e.value.code == swm._abi.SWM_E_INVALID
+    import ctypes
+    f = ctypes.c_void_p()
+    assert op._L.swm_field_create_mesh(op._h, 7, ctypes.byref(f)) == swm._abi.SWM_E_INVALID
