@@ -157,6 +157,22 @@ void orcc_apply(const orcc_domain* d, const double* hs, const double* h,
                 const double* u, const double* v, double* th, double* tu, double* tv);
 void orcc_rk4(const orcc_domain* d, const double* hs, double* h, double* u,
               double* v, double dt, int nsteps);
+/* grad_perp_c_sbp{21,42} of a corner field (u on mesh u, v on mesh v) and the
+ * transform2co of co2contra_c_sbp{21,42}_new, at the domain's SBP order. */
+void orcc_grad_perp(const orcc_domain* d, const double* w, double* gu, double* gv);
+void orcc_contra2co(const orcc_domain* d, const double* ut, const double* vt,
+                    double* u, double* v);
+/* C-grid hyperdiffusion tendency with the 2/1 operators at any domain order:
+ * parts 1 hordiff_c_biharm_div, 2 hordiff_c_biharm_curl, 3
+ * hordiff_c_biharm_curl_div for (u, v); hordiff_scalar_C for h. */
+void orcc_hordiff(const orcc_domain* d, int parts, double uv_coeff, double h_coeff,
+                  const double* h, const double* u, const double* v,
+                  double* th, double* tu, double* tv);
+/* nsteps of the drivers' step: one RK4 step, then one explicit Euler step of
+ * the hyperdiffusion. */
+void orcc_model_step(const orcc_domain* d, const double* hs, double* h, double* u,
+                     double* v, double dt, int nsteps, int parts, double uv_coeff,
+                     double h_coeff);
 double orcc_mass(const orcc_domain* d, int mesh, const double* f);
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
 /* Analytic test fields on the C meshes: vector kinds 0 solid rotation (axis
@@ -168,7 +184,8 @@ int orcc_vector_test_field(const orcc_domain* d, int kind, int level,
 int orcc_scalar_test_field(const orcc_domain* d, int kind, int level, int mesh,
                            double* f);
 /* Known-answer tests on the C grid at (N, nz=3, unit sphere): kind 0 div (4
- * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2).
+ * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2),
+ * 6 contra2co of co2contra_c_sbp*_new (2).
  * Returns 0, or -1 for an unknown kind / order. */
 int orcc_golden(int kind, int N, int sbp_order, double* out);
 

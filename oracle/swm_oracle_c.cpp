@@ -50,6 +50,12 @@ struct Stag {
 
 enum StagId { W21_C2I, W21_I2C, W42_C2I, W42_I2C, D21_C2I, D21_I2C, D42_C2I, D42_I2C };
 
+// The four staggered operators of one SBP order.
+struct Ops {
+  int order = 42;
+  Stag Wc2i, Wi2c, Dc2i, Di2c;
+};
+
 Stag make_stag(StagId id) {
   Stag s;
   switch (id) {
@@ -140,7 +146,7 @@ inline double stag_point(const Stag& s, const double* f, int nout, int st, int k
 struct Mesh {
   int nx = 0, ny = 0;
   double si = 0.5, sj = 0.5;  // shift_i, shift_j of mesh_factory_mod.f90:34-41
-  std::vector<double> J, Qi1, Qi2, Qi3, rx, ry, rz, f, a1, a2, b1, b2;
+  std::vector<double> J, Qi1, Qi2, Qi3, Q1, Q2, Q3, rx, ry, rz, f, a1, a2, b1, b2;
   int size() const { return 6 * nx * ny; }
   int at(int p, int i, int j) const { return (p * ny + j) * nx + i; }
 };
@@ -224,7 +230,8 @@ struct orcc_domain {
   double hx = 0.0, scale = 1.0, grav = 9.80616, omega = 1.0, axis[3] = {0, 0, 1};
   Mesh m[4];               // p, u, v, q
   Halo ho, hu, hv, hq;     // scalar on p, C vector u / v, scalar on q
-  Stag Wc2i, Wi2c, Dc2i, Di2c;
+  Ops ops;    // the operators of the model's SBP order
+  Ops ops21;  // the 2/1 operators of the C-grid hyperdiffusion
   std::vector<double> Ac, Ai;  // quadrature edge weights at centres / interfaces
 };
 
@@ -235,7 +242,7 @@ int nthreads() { return orc_get_threads(); }
 void build_mesh(orcc_domain& d, Mesh& M, int nx, int ny, double si, double sj) {
   M.nx = nx; M.ny = ny; M.si = si; M.sj = sj;
   const int np = M.size();
-  for (auto* v : {&M.J, &M.Qi1, &M.Qi2, &M.Qi3, &M.rx, &M.ry, &M.rz, &M.f}) v->assign(np, 0.0);
+  for (auto* v : {&M.J, &M.Qi1, &M.Qi2, &M.Qi3, &M.Q1, &M.Q2, &M.Q3, &M.rx, &M.ry, &M.rz, &M.f}) v->assign(np, 0.0);
   for (auto* v : {&M.a1, &M.a2, &M.b1, &M.b2}) v->assign(3 * (size_t)np, 0.0);
   for (int p = 0; p < 6; ++p)
     for (int j = 0; j < ny; ++j)
@@ -249,6 +256,11 @@ void build_mesh(orcc_domain& d, Mesh& M, int nx, int ny, double si, double sj) {
         M.Qi1[id] = sg * sg / (1.0 + ta * ta);
         M.Qi2[id] = sg * sg * ta * tb / ((1.0 + ta * ta) * (1.0 + tb * tb));
         M.Qi3[id] = sg * sg / (1.0 + tb * tb);
+        // ecs_Q (ecs_metric_mod.f90:401-419)
+        const double s4 = sg * sg * sg * sg;
+        M.Q1[id] = (1.0 + ta * ta) * (1.0 + ta * ta) * (1.0 + tb * tb) / s4;
+        M.Q2[id] = -(1.0 + ta * ta) * (1.0 + tb * tb) * ta * tb / s4;
+        M.Q3[id] = (1.0 + ta * ta) * (1.0 + tb * tb) * (1.0 + tb * tb) / s4;
         double v[3], w[3];
         r_proto(al, be, v); to_face(p, v, w);
         M.rx[id] = w[0]; M.ry[id] = w[1]; M.rz[id] = w[2];
@@ -280,17 +292,17 @@ void stag_apply(const Stag& s, const Mesh& I, const double* f, const Mesh& O, do
 // covariant component is interpolated to the centres, multiplied by J Qi12
 // there, interpolated to the faces and divided by J.  co2contra_c_sbp21
 // (226-290) is the same chain with the 2nd-order W21 weights.
-void co2contra(const orcc_domain& d, const double* u, const double* v, double* ut, double* vt) {
+void co2contra(const orcc_domain& d, const Ops& o, const double* u, const double* v, double* ut, double* vt) {
   const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2];
   std::vector<double> a(P.size()), b(P.size()), t(U.size()), s(V.size());
-  stag_apply(d.Wi2c, V, v, P, a.data(), 1);
-  stag_apply(d.Wi2c, U, u, P, b.data(), 0);
+  stag_apply(o.Wi2c, V, v, P, a.data(), 1);
+  stag_apply(o.Wi2c, U, u, P, b.data(), 0);
   for (int k = 0; k < P.size(); ++k) {
     a[k] = P.J[k] * P.Qi2[k] * a[k];
     b[k] = P.J[k] * P.Qi2[k] * b[k];
   }
-  stag_apply(d.Wc2i, P, a.data(), U, t.data(), 0);
-  stag_apply(d.Wc2i, P, b.data(), V, s.data(), 1);
+  stag_apply(o.Wc2i, P, a.data(), U, t.data(), 0);
+  stag_apply(o.Wc2i, P, b.data(), V, s.data(), 1);
   for (int k = 0; k < U.size(); ++k) ut[k] = U.Qi1[k] * u[k] + t[k] / U.J[k];
   for (int k = 0; k < V.size(); ++k) vt[k] = V.Qi3[k] * v[k] + s[k] / V.J[k];
 }
@@ -299,9 +311,9 @@ void co2contra(const orcc_domain& d, const double* u, const double* v, double* u
 // h interpolated to the faces times the contravariant velocity.
 void massflux(const orcc_domain& d, const double* h, const double* ut, const double* vt, double* hu, double* hv) {
   const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2];
-  stag_apply(d.Wc2i, P, h, U, hu, 0);
+  stag_apply(d.ops.Wc2i, P, h, U, hu, 0);
   for (int k = 0; k < U.size(); ++k) hu[k] = ut[k] * hu[k];
-  stag_apply(d.Wc2i, P, h, V, hv, 1);
+  stag_apply(d.ops.Wc2i, P, h, V, hv, 1);
   for (int k = 0; k < V.size(); ++k) hv[k] = vt[k] * hv[k];
 }
 
@@ -312,20 +324,20 @@ void kinetic_energy(const orcc_domain& d, const double* u, const double* v, cons
   std::vector<double> ku(U.size()), kv(V.size()), kuh(P.size()), kvh(P.size());
   for (int k = 0; k < U.size(); ++k) ku[k] = U.J[k] * (u[k] * ut[k]) / 2.0;
   for (int k = 0; k < V.size(); ++k) kv[k] = V.J[k] * (v[k] * vt[k]) / 2.0;
-  stag_apply(d.Wi2c, U, ku.data(), P, kuh.data(), 0);
-  stag_apply(d.Wi2c, V, kv.data(), P, kvh.data(), 1);
+  stag_apply(d.ops.Wi2c, U, ku.data(), P, kuh.data(), 0);
+  stag_apply(d.ops.Wi2c, V, kv.data(), P, kvh.data(), 1);
   for (int k = 0; k < P.size(); ++k) ke[k] = (kuh[k] + kvh[k]) / P.J[k];
 }
 
 // ------------------------------------------------------------------ grad
 // gradient_c_sbp42 (gradient/grad_c_sbp42_mod.f90:44-139) with the 3-wide
 // o-point halo; gradient_c_sbp21 (grad_c2_ecs_mod.f90:234-293) with 2.
-void grad(const orcc_domain& d, const double* f, double* gx, double* gy) {
+void grad(const orcc_domain& d, const Ops& o, const double* f, double* gx, double* gy) {
   const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2];
   const int N = d.N;
   const double dx1 = 1.0 / (d.scale * d.hx);
   const double hs = d.hx * d.scale;
-  const Stag& D = d.Dc2i;  // dedge / din of grad_c_sbp42 are D42_staggered_c2i
+  const Stag& D = o.Dc2i;  // dedge / din of grad_c_sbp42 are D42_staggered_c2i
   const double sq1 = 7.0 / 18.0;
   auto F = [&](int p, int i, int j) { return ext(P, d.ho, f, nullptr, p, i, j); };
 #pragma omp parallel for schedule(static) num_threads(nthreads())
@@ -334,7 +346,7 @@ void grad(const orcc_domain& d, const double* f, double* gx, double* gy) {
     for (int j = 0; j < N; ++j)
       for (int i = 0; i <= N; ++i) {
         double g;
-        if (d.order == 21) {
+        if (o.order == 21) {
           if (i == 0) g = (0.5 * F(p, 1, j) + 0.5 * F(p, 0, j) - 1.5 * F(p, -1, j) + 0.5 * F(p, -2, j)) / hs;
           else if (i == N) g = (-0.5 * F(p, N - 2, j) - 0.5 * F(p, N - 1, j) + 1.5 * F(p, N, j) - 0.5 * F(p, N + 1, j)) / hs;
           else g = (F(p, i, j) - F(p, i - 1, j)) / hs;
@@ -371,7 +383,7 @@ void grad(const orcc_domain& d, const double* f, double* gx, double* gy) {
     for (int j = 0; j <= N; ++j)
       for (int i = 0; i < N; ++i) {
         double g;
-        if (d.order == 21) {
+        if (o.order == 21) {
           if (j == 0) g = (0.5 * F(p, i, 1) + 0.5 * F(p, i, 0) - 1.5 * F(p, i, -1) + 0.5 * F(p, i, -2)) / hs;
           else if (j == N) g = (-0.5 * F(p, i, N - 2) - 0.5 * F(p, i, N - 1) + 1.5 * F(p, i, N) - 0.5 * F(p, i, N + 1)) / hs;
           else g = (F(p, i, j) - F(p, i, j - 1)) / hs;
@@ -413,19 +425,19 @@ void grad(const orcc_domain& d, const double* f, double* gx, double* gy) {
 // plus the "at_center" SAT penalty on the jump of the duplicated edge faces
 // (sbp_operator_mod.f90:318-384), divided by J hx a.  divergence_c_sbp21
 // (div_c2_mod.f90:76-177) uses the raw halo values times the local J.
-void div(const orcc_domain& d, const double* hu, const double* hv, double* out) {
+void div(const orcc_domain& d, const Ops& o, const double* hu, const double* hv, double* out) {
   const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2];
   const int N = d.N;
   std::vector<double> gu(U.size()), gv(V.size());
   for (int k = 0; k < U.size(); ++k) gu[k] = hu[k] * U.J[k];
   for (int k = 0; k < V.size(); ++k) gv[k] = hv[k] * V.J[k];
-  const Stag& D = d.Di2c;
+  const Stag& D = o.Di2c;
 #pragma omp parallel for schedule(static) num_threads(nthreads())
   for (int pj = 0; pj < 6 * N; ++pj) {
     const int p = pj / N, j = pj % N;
     for (int i = 0; i < N; ++i) {
       double dx, dy;
-      if (d.order == 21) {
+      if (o.order == 21) {
         auto u = [&](int a, int b) { return ext(U, d.hu, hu, hv, p, a, b); };
         auto v = [&](int a, int b) { return ext(V, d.hv, hv, hu, p, a, b); };
         auto Ju = [&](int a, int b) { return U.J[U.at(p, a, b)]; };
@@ -501,10 +513,10 @@ void sync_q(const orcc_domain& d, double* f) {
 // the covariant components onto the corners, the SAT penalties on the jumps
 // across the panel edges, division by J hx a, then the Ah scalar sync
 // (curl_factory_mod.f90:56-88).
-void curl(const orcc_domain& d, const double* u, const double* v, double* out) {
+void curl(const orcc_domain& d, const Ops& o, const double* u, const double* v, double* out) {
   const Mesh &U = d.m[1], &V = d.m[2], &Q = d.m[3];
   const int N = d.N, nq = N + 1;
-  const Stag& D = d.Dc2i;
+  const Stag& D = o.Dc2i;
   const int np = (int)D.proj.size();
   const double al = D.Aout[0];  // Al_out(1) = Ar_out(end)
 #pragma omp parallel for schedule(static) num_threads(nthreads())
@@ -552,21 +564,153 @@ void coriolis(const orcc_domain& d, const double* hu, const double* hv, const do
   std::vector<double> cup(P.size()), cvp(P.size());
   for (int k = 0; k < U.size(); ++k) gu[k] = U.J[k] * hu[k];
   for (int k = 0; k < V.size(); ++k) gv[k] = V.J[k] * hv[k];
-  stag_apply(d.Wi2c, U, gu.data(), P, gup.data(), 0);
-  stag_apply(d.Wi2c, V, gv.data(), P, gvp.data(), 1);
+  stag_apply(d.ops.Wi2c, U, gu.data(), P, gup.data(), 0);
+  stag_apply(d.ops.Wi2c, V, gv.data(), P, gvp.data(), 1);
   // interp_w2h (interpolator_w2h_mod.f90:25-67)
-  stag_apply(d.Wi2c, Q, cu, V, fv.data(), 0);
-  stag_apply(d.Wi2c, Q, cu, U, fu.data(), 1);
-  stag_apply(d.Wi2c, U, fu.data(), P, fuh.data(), 0);
-  stag_apply(d.Wi2c, V, fv.data(), P, fvh.data(), 1);
+  stag_apply(d.ops.Wi2c, Q, cu, V, fv.data(), 0);
+  stag_apply(d.ops.Wi2c, Q, cu, U, fu.data(), 1);
+  stag_apply(d.ops.Wi2c, U, fu.data(), P, fuh.data(), 0);
+  stag_apply(d.ops.Wi2c, V, fv.data(), P, fvh.data(), 1);
   for (int k = 0; k < P.size(); ++k) {
     cp[k] = 0.5 * fuh[k] + 0.5 * fvh[k];
     cup[k] = (P.f[k] + cp[k]) * gvp[k] / h[k];
     cvp[k] = -(P.f[k] + cp[k]) * gup[k] / h[k];
   }
-  stag_apply(d.Wc2i, P, cup.data(), U, cor_u, 0);
-  stag_apply(d.Wc2i, P, cvp.data(), V, cor_v, 1);
+  stag_apply(d.ops.Wc2i, P, cup.data(), U, cor_u, 0);
+  stag_apply(d.ops.Wc2i, P, cvp.data(), V, cor_v, 1);
   (void)Q;
+}
+
+// ------------------------------------------------------------- grad_perp
+// grad_perp_c_sbp21 / _sbp42 (grad_perp/grad_perp_c_sbp_mod.f90:20-95,
+// grad_perp_factory_mod.f90:24-55): D_staggered_i2c of the corner field w
+// along y onto the x-faces and along x onto the y-faces, each with the
+// "at_center" SAT penalty (sbp_operator_mod.f90:343-391) on the jump between
+// the panel's edge point and the neighbour's copy of it in the first halo
+// layer; gu = -(.) / (a hx J_u), gv = (.) / (a hx J_v).
+void grad_perp(const orcc_domain& d, const Ops& o, const double* w, double* gu, double* gv) {
+  const Mesh &U = d.m[1], &V = d.m[2], &Q = d.m[3];
+  const int N = d.N;
+  const Stag& D = o.Di2c;
+  const int ne = (int)D.proj.size();
+  auto W = [&](int p, int i, int j) { return ext(Q, d.hq, w, nullptr, p, i, j); };
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (int p = 0; p < 6; ++p) {
+    for (int j = 0; j < N; ++j)  // x-faces: along y
+      for (int i = 0; i <= N; ++i) {
+        double g = stag_point(D, &w[Q.at(p, i, 0)], N, Q.nx, j);
+        if (j < ne) g = g + 0.5 * (D.proj[j] / D.Aout[j]) * (W(p, i, 0) - W(p, i, -1));
+        if (j >= N - ne) {
+          const int r = N - 1 - j;
+          g = g + 0.5 * (D.proj[r] / D.Aout[r]) * (W(p, i, N + 1) - W(p, i, N));
+        }
+        const int e = U.at(p, i, j);
+        gu[e] = -g / (d.scale * d.hx * U.J[e]);
+      }
+    for (int j = 0; j <= N; ++j)  // y-faces: along x
+      for (int i = 0; i < N; ++i) {
+        double g = stag_point(D, &w[Q.at(p, 0, j)], N, 1, i);
+        if (i < ne) g = g + 0.5 * (D.proj[i] / D.Aout[i]) * (W(p, 0, j) - W(p, -1, j));
+        if (i >= N - ne) {
+          const int r = N - 1 - i;
+          g = g + 0.5 * (D.proj[r] / D.Aout[r]) * (W(p, N + 1, j) - W(p, N, j));
+        }
+        const int e = V.at(p, i, j);
+        gv[e] = g / (d.scale * d.hx * V.J[e]);
+      }
+  }
+}
+
+// ------------------------------------------------------------- contra2co
+// transform2co of co2contra_c_sbp21_new / _sbp42_new (co2contra/
+// co2contra_Cgrid_mod.f90:135-203, the interpolators interp2d_uv2pvec_C and
+// interp2d_pvec2uv_C of interpolator2d_factory_mod.f90:47-58): the
+// contravariant components interpolated to the centres, times J Q12 there,
+// swapped, interpolated back to the faces, divided by J and added to
+// Q11 u^1 (Q22 u^2).
+void contra2co(const orcc_domain& d, const Ops& o, const double* ut, const double* vt, double* u, double* v) {
+  const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2];
+  std::vector<double> uh(P.size()), vh(P.size()), a(U.size()), b(V.size());
+  stag_apply(o.Wi2c, U, ut, P, uh.data(), 0);
+  stag_apply(o.Wi2c, V, vt, P, vh.data(), 1);
+  for (int k = 0; k < P.size(); ++k) {
+    const double x = uh[k] * P.J[k] * P.Q2[k];
+    const double y = vh[k] * P.J[k] * P.Q2[k];
+    uh[k] = y;
+    vh[k] = x;
+  }
+  stag_apply(o.Wc2i, P, uh.data(), U, a.data(), 0);
+  stag_apply(o.Wc2i, P, vh.data(), V, b.data(), 1);
+  for (int k = 0; k < U.size(); ++k) u[k] = U.Q1[k] * ut[k] + a[k] / U.J[k];
+  for (int k = 0; k < V.size(); ++k) v[k] = V.Q3[k] * vt[k] + b[k] / V.J[k];
+}
+
+// ---------------------------------------------------------- hyperdiffusion
+// diff_coeff^(2 diff_order) with its sign, diff_order 2: -(c^4), c = coeff a hx
+// (hordiff_factory_mod.f90:96-100, 132-136, 243-246).
+double diff_c4(const orcc_domain& d, double coeff) {
+  const double c = coeff * d.scale * d.hx;
+  const double c2 = c * c;
+  return -(c2 * c2);
+}
+
+// The C-grid vector hyperdiffusion (hordiff/hordiff_Cgrid_mod.f90:59-140)
+// with the 2/1 operators of hordiff_factory_mod.f90:53-139.  parts: 1 the
+// divergence part (hordiff_c_biharm_div), 2 the curl part
+// (hordiff_c_biharm_curl), 3 both (hordiff_c_biharm_curl_div):
+//   div part   c4 grad div co2contra grad div co2contra (u, v)
+//   curl part  c4 contra2co grad_perp curl contra2co grad_perp curl (u, v)
+// summed as u_tend = c4 A + 1.0 (c4 B).
+void hordiff_uv(const orcc_domain& d, int parts, double coeff, const double* u, const double* v, double* tu,
+                double* tv) {
+  const Ops& o = d.ops21;
+  const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2], &Q = d.m[3];
+  const double c4 = diff_c4(d, coeff);
+  std::vector<double> ut(U.size()), vt(V.size()), a(U.size()), b(V.size()), dv(P.size()), cq(Q.size());
+  std::vector<double> cu(U.size(), 0.0), cv(V.size(), 0.0);
+  if (parts & 2) {
+    curl(d, o, u, v, cq.data());
+    grad_perp(d, o, cq.data(), ut.data(), vt.data());
+    contra2co(d, o, ut.data(), vt.data(), a.data(), b.data());
+    curl(d, o, a.data(), b.data(), cq.data());
+    grad_perp(d, o, cq.data(), ut.data(), vt.data());
+    contra2co(d, o, ut.data(), vt.data(), a.data(), b.data());
+    for (int k = 0; k < U.size(); ++k) cu[k] = c4 * a[k];
+    for (int k = 0; k < V.size(); ++k) cv[k] = c4 * b[k];
+  }
+  if (parts & 1) {
+    co2contra(d, o, u, v, ut.data(), vt.data());
+    div(d, o, ut.data(), vt.data(), dv.data());
+    grad(d, o, dv.data(), a.data(), b.data());
+    co2contra(d, o, a.data(), b.data(), ut.data(), vt.data());
+    div(d, o, ut.data(), vt.data(), dv.data());
+    grad(d, o, dv.data(), ut.data(), vt.data());
+    if (parts & 2) {
+      for (int k = 0; k < U.size(); ++k) cu[k] = cu[k] + 1.0 * (c4 * ut[k]);
+      for (int k = 0; k < V.size(); ++k) cv[k] = cv[k] + 1.0 * (c4 * vt[k]);
+    } else {
+      for (int k = 0; k < U.size(); ++k) cu[k] = c4 * ut[k];
+      for (int k = 0; k < V.size(); ++k) cv[k] = c4 * vt[k];
+    }
+  }
+  std::copy(cu.begin(), cu.end(), tu);
+  std::copy(cv.begin(), cv.end(), tv);
+}
+
+// hordiff_scalar_C (hordiff/hordiff_scalar_mod.f90:33-53 with
+// divgrad_laplace_c_sbp21, laplace/divgrad_laplace_mod.f90:23-33):
+// th = c4 L(L(h)), L = div co2contra grad.
+void hordiff_h(const orcc_domain& d, double coeff, const double* h, double* th) {
+  const Ops& o = d.ops21;
+  const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2];
+  const double c4 = diff_c4(d, coeff);
+  std::vector<double> f(h, h + P.size()), gx(U.size()), gy(V.size()), gxt(U.size()), gyt(V.size());
+  for (int rep = 0; rep < 2; ++rep) {
+    grad(d, o, f.data(), gx.data(), gy.data());
+    co2contra(d, o, gx.data(), gy.data(), gxt.data(), gyt.data());
+    div(d, o, gxt.data(), gyt.data(), f.data());
+  }
+  for (int k = 0; k < P.size(); ++k) th[k] = c4 * f[k];
 }
 
 // operator_swm_t%apply, vector-invariant branch
@@ -576,16 +720,16 @@ void apply(const orcc_domain& d, const double* hs, const double* h, const double
   const Mesh &P = d.m[0], &U = d.m[1], &V = d.m[2], &Q = d.m[3];
   std::vector<double> ut(U.size()), vt(V.size()), hu(U.size()), hv(V.size()), ke(P.size());
   std::vector<double> gx(U.size()), gy(V.size()), cu(Q.size()), cor_u(U.size()), cor_v(V.size()), dv(P.size());
-  co2contra(d, u, v, ut.data(), vt.data());
+  co2contra(d, d.ops, u, v, ut.data(), vt.data());
   massflux(d, h, ut.data(), vt.data(), hu.data(), hv.data());
   kinetic_energy(d, u, v, ut.data(), vt.data(), ke.data());
   for (int k = 0; k < P.size(); ++k) ke[k] = ke[k] + d.grav * h[k] + d.grav * (hs ? hs[k] : 0.0);
-  grad(d, ke.data(), gx.data(), gy.data());
-  curl(d, u, v, cu.data());
+  grad(d, d.ops, ke.data(), gx.data(), gy.data());
+  curl(d, d.ops, u, v, cu.data());
   coriolis(d, hu.data(), hv.data(), h, cu.data(), cor_u.data(), cor_v.data());
   for (int k = 0; k < U.size(); ++k) tu[k] = -1.0 * gx[k] + 1.0 * cor_u[k];
   for (int k = 0; k < V.size(); ++k) tv[k] = -1.0 * gy[k] + 1.0 * cor_v[k];
-  div(d, hu.data(), hv.data(), dv.data());
+  div(d, d.ops, hu.data(), hv.data(), dv.data());
   for (int k = 0; k < P.size(); ++k) th[k] = -1.0 * dv[k];
 }
 
@@ -622,6 +766,19 @@ void rk4(const orcc_domain& d, const double* hs, double* h, double* u, double* v
         F0[c][m] = x;
       }
   }
+}
+
+// explicit_Eul1_t%step (explicit_Eul1_mod.f90:20-30) of operator_swm_diff_t
+// (operator_swm_diff_mod.f90:25-46): v0 = v0 + dt D(v0).
+void diffusion_step(const orcc_domain& d, int parts, double cuv, double ch, double* h, double* u, double* v,
+                    double dt) {
+  const int n[3] = {d.m[0].size(), d.m[1].size(), d.m[2].size()};
+  std::vector<double> th(n[0]), tu(n[1]), tv(n[2]);
+  hordiff_uv(d, parts, cuv, u, v, tu.data(), tv.data());
+  hordiff_h(d, ch, h, th.data());
+  for (int k = 0; k < n[0]; ++k) h[k] = h[k] + dt * th[k];
+  for (int k = 0; k < n[1]; ++k) u[k] = u[k] + dt * tu[k];
+  for (int k = 0; k < n[2]; ++k) v[k] = v[k] + dt * tv[k];
 }
 
 // SBP_C42 / SBP_C21 quadrature (quadrature_factory_mod.f90:90-160 and
@@ -711,14 +868,17 @@ orcc_domain* create(int N, int order, double radius, double grav, double omega, 
   d->hu = build_halo(d->m[1], d->m[2], 1);
   d->hv = build_halo(d->m[2], d->m[1], 2);
   d->hq = build_halo(d->m[3], d->m[3], 0);
+  d->ops21.order = 21;
+  d->ops21.Wc2i = make_stag(W21_C2I); d->ops21.Wi2c = make_stag(W21_I2C);
+  d->ops21.Dc2i = make_stag(D21_C2I); d->ops21.Di2c = make_stag(D21_I2C);
   if (order == 42) {
-    d->Wc2i = make_stag(W42_C2I); d->Wi2c = make_stag(W42_I2C);
-    d->Dc2i = make_stag(D42_C2I); d->Di2c = make_stag(D42_I2C);
+    d->ops.order = 42;
+    d->ops.Wc2i = make_stag(W42_C2I); d->ops.Wi2c = make_stag(W42_I2C);
+    d->ops.Dc2i = make_stag(D42_C2I); d->ops.Di2c = make_stag(D42_I2C);
     d->Ac = {13.0 / 12.0, 7.0 / 8.0, 25.0 / 24.0, 1.0};
     d->Ai = {7.0 / 18.0, 9.0 / 8.0, 1.0, 71.0 / 72.0, 1.0};
   } else {
-    d->Wc2i = make_stag(W21_C2I); d->Wi2c = make_stag(W21_I2C);
-    d->Dc2i = make_stag(D21_C2I); d->Di2c = make_stag(D21_I2C);
+    d->ops = d->ops21;
     d->Ac = {1.0, 1.0};
     d->Ai = {0.5, 1.0};
   }
@@ -751,7 +911,7 @@ void orcc_bases(const orcc_domain* d, int mesh, double* a1, double* a2, double* 
 }
 
 void orcc_co2contra(const orcc_domain* d, const double* u, const double* v, double* ut, double* vt) {
-  co2contra(*d, u, v, ut, vt);
+  co2contra(*d, d->ops, u, v, ut, vt);
 }
 void orcc_massflux(const orcc_domain* d, const double* h, const double* ut, const double* vt, double* hu, double* hv) {
   massflux(*d, h, ut, vt, hu, hv);
@@ -759,9 +919,9 @@ void orcc_massflux(const orcc_domain* d, const double* h, const double* ut, cons
 void orcc_ke(const orcc_domain* d, const double* u, const double* v, const double* ut, const double* vt, double* ke) {
   kinetic_energy(*d, u, v, ut, vt, ke);
 }
-void orcc_grad(const orcc_domain* d, const double* f, double* gx, double* gy) { grad(*d, f, gx, gy); }
-void orcc_div(const orcc_domain* d, const double* hu, const double* hv, double* out) { div(*d, hu, hv, out); }
-void orcc_curl(const orcc_domain* d, const double* u, const double* v, double* out) { curl(*d, u, v, out); }
+void orcc_grad(const orcc_domain* d, const double* f, double* gx, double* gy) { grad(*d, d->ops, f, gx, gy); }
+void orcc_div(const orcc_domain* d, const double* hu, const double* hv, double* out) { div(*d, d->ops, hu, hv, out); }
+void orcc_curl(const orcc_domain* d, const double* u, const double* v, double* out) { curl(*d, d->ops, u, v, out); }
 void orcc_coriolis(const orcc_domain* d, const double* hu, const double* hv, const double* h, const double* cu,
                    double* cor_u, double* cor_v) {
   coriolis(*d, hu, hv, h, cu, cor_u, cor_v);
@@ -772,6 +932,24 @@ void orcc_apply(const orcc_domain* d, const double* hs, const double* h, const d
 }
 void orcc_rk4(const orcc_domain* d, const double* hs, double* h, double* u, double* v, double dt, int nsteps) {
   rk4(*d, hs, h, u, v, dt, nsteps);
+}
+void orcc_grad_perp(const orcc_domain* d, const double* w, double* gu, double* gv) {
+  grad_perp(*d, d->ops, w, gu, gv);
+}
+void orcc_contra2co(const orcc_domain* d, const double* ut, const double* vt, double* u, double* v) {
+  contra2co(*d, d->ops, ut, vt, u, v);
+}
+void orcc_hordiff(const orcc_domain* d, int parts, double uv_coeff, double h_coeff, const double* h, const double* u,
+                  const double* v, double* th, double* tu, double* tv) {
+  hordiff_uv(*d, parts, uv_coeff, u, v, tu, tv);
+  hordiff_h(*d, h_coeff, h, th);
+}
+void orcc_model_step(const orcc_domain* d, const double* hs, double* h, double* u, double* v, double dt, int nsteps,
+                     int parts, double uv_coeff, double h_coeff) {
+  for (int s = 0; s < nsteps; ++s) {
+    rk4(*d, hs, h, u, v, dt, 1);
+    diffusion_step(*d, parts, uv_coeff, h_coeff, h, u, v, dt);
+  }
 }
 double orcc_mass(const orcc_domain* d, int mesh, const double* f) { return mass(*d, mesh, f); }
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f) {
@@ -831,7 +1009,7 @@ int orcc_golden(int kind, int N, int order, double* out) {
       for (int lev = 0; lev < 3; ++lev) {
         set_vector(*d, [lev](double x, double y, double z, double w[3]) { field_solid_rotation(lev, x, y, z, w); },
                    true, u, v);
-        div(*d, u.data(), v.data(), a.data());
+        div(*d, d->ops, u.data(), v.data(), a.data());
         std::vector<double> e(a.begin(), a.begin() + P.size());
         for (double& x : e) x = d->scale * x;
         all.insert(all.end(), e.begin(), e.end());
@@ -841,7 +1019,7 @@ int orcc_golden(int kind, int N, int order, double* out) {
       all.clear(); l2 = 0.0;
       for (int lev = 0; lev < 3; ++lev) {
         set_vector(*d, field_cross_polar, true, u, v);
-        div(*d, u.data(), v.data(), a.data());
+        div(*d, d->ops, u.data(), v.data(), a.data());
         std::vector<double> e(P.size());
         for (int k = 0; k < P.size(); ++k) e[k] = d->scale * a[k] - 1.0 * field_cross_polar_div(P.rx[k], P.ry[k], P.rz[k]);
         all.insert(all.end(), e.begin(), e.end());
@@ -856,7 +1034,7 @@ int orcc_golden(int kind, int N, int order, double* out) {
         for (int k = 0; k < P.size(); ++k) f[k] = field_xyz(lev, P.rx[k], P.ry[k], P.rz[k]);
         set_vector(*d, [lev](double x, double y, double z, double w[3]) { field_xyz_grad(lev, x, y, z, w); }, false,
                    tx, ty);
-        grad(*d, f.data(), c.data(), b.data());
+        grad(*d, d->ops, f.data(), c.data(), b.data());
         for (int k = 0; k < U.size(); ++k) c[k] = d->scale * c[k] - 1.0 * tx[k];
         for (int k = 0; k < V.size(); ++k) b[k] = d->scale * b[k] - 1.0 * ty[k];
         allx.insert(allx.end(), c.begin(), c.end());
@@ -874,7 +1052,7 @@ int orcc_golden(int kind, int N, int order, double* out) {
         for (int lev = 0; lev < 3; ++lev) {
           if (fld == 0) set_vector(*d, field_vsh_curl_free_10, false, u, v);
           else set_vector(*d, field_cross_polar, false, u, v);
-          curl(*d, u.data(), v.data(), a.data());
+          curl(*d, d->ops, u.data(), v.data(), a.data());
           std::vector<double> e(Q.size());
           for (int k = 0; k < Q.size(); ++k) {
             e[k] = d->scale * a[k];
@@ -948,9 +1126,25 @@ int orcc_golden(int kind, int N, int order, double* out) {
       for (int lev = 0; lev < 3; ++lev) {
         set_vector(*d, field_cross_polar, false, u, v);
         set_vector(*d, field_cross_polar, true, ut, vt);
-        co2contra(*d, u.data(), v.data(), c.data(), b.data());
+        co2contra(*d, d->ops, u.data(), v.data(), c.data(), b.data());
         for (int k = 0; k < U.size(); ++k) c[k] = c[k] + (-1.0) * ut[k];
         for (int k = 0; k < V.size(); ++k) b[k] = b[k] + (-1.0) * vt[k];
+        allx.insert(allx.end(), c.begin(), c.end());
+        ally.insert(ally.end(), b.begin(), b.end());
+        l2x += l2sq(U, d->hx, c.data());
+        l2y += l2sq(V, d->hx, b.data());
+      }
+      out[0] = maxabs(allx) + maxabs(ally);
+      out[1] = std::sqrt(l2x) + std::sqrt(l2y);
+      break;
+    }
+    case 6: {  // transform2co of the contravariant cross-polar flow
+      for (int lev = 0; lev < 3; ++lev) {
+        set_vector(*d, field_cross_polar, true, ut, vt);
+        set_vector(*d, field_cross_polar, false, u, v);
+        contra2co(*d, d->ops, ut.data(), vt.data(), c.data(), b.data());
+        for (int k = 0; k < U.size(); ++k) c[k] = c[k] + (-1.0) * u[k];
+        for (int k = 0; k < V.size(); ++k) b[k] = b[k] + (-1.0) * v[k];
         allx.insert(allx.end(), c.begin(), c.end());
         ally.insert(ally.end(), b.begin(), b.end());
         l2x += l2sq(U, d->hx, c.data());

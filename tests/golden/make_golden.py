@@ -9,7 +9,9 @@ operators and the colocated pointwise operators (co2contra, contra2co,
 Coriolis, kinetic energy; the last two are tested on the A grid) -- each
 with the line number of the reference file it came from.  The C-grid file
 keeps the SBP operators of the &shallow_water_model_c family (div, grad,
-curl, Coriolis, KE and co2contra at sbp21 and sbp42).  The
+curl, Coriolis, KE and co2contra at sbp21 and sbp42) and the co2contra /
+contra2co pair of co2contra_c_sbp*_new that the C-grid hyperdiffusion's curl
+part uses.  The
 values were printed by the reference test with format "(A,4E15.7)", i.e. to
 7 significant digits, from test_diffops_all.f90 at N=32, nz=3.
 """
@@ -38,6 +40,8 @@ KEEP_C = {
     "coriolis_Cgrid_sbp21": ("coriolis", 21), "coriolis_Cgrid_sbp42": ("coriolis", 42),
     "KE_Cgrid_sbp21": ("ke", 21), "KE_Cgrid_sbp42": ("ke", 42),
     "co2contra_c_sbp21": ("co2contra", 21), "co2contra_c_sbp42": ("co2contra", 42),
+    "co2contra_c_sbp21_new": ("co2contra", 21), "co2contra_c_sbp42_new": ("co2contra", 42),
+    "contra2co_c_sbp21_new": ("contra2co", 21), "contra2co_c_sbp42_new": ("contra2co", 42),
 }
 
 

@@ -60,3 +60,101 @@ def test_sbp42_more_accurate_than_sbp21():
     assert e42[3] < e21[3]
     g42, g21 = oracle.golden_c("grad", 32, 42), oracle.golden_c("grad", 32, 21)
     assert g42[1] < 0.1 * g21[1]
+
+
+# ---------------------------------------------------------------- hyperdiffusion
+# operator_swm_diff_t with the &shallow_water_model_c names: hordiff_c_biharm_*
+# for (u, v) and hordiff_scalar_C for h, always with the 2/1 operators
+# (hordiff_factory_mod.f90:53-139, 196-247).
+
+def test_hyperdiffusion_uses_the_2_1_operators_at_any_order():
+    """The factory builds the C-grid hyperdiffusion from the sbp21 operators
+    whatever the model's order, so a 4/2 domain gives the same tendency as a
+    2/1 domain bit for bit."""
+    N = 20
+    d21, d42 = oracle.OracleCDomain(N, 21), oracle.OracleCDomain(N, 42)
+    h, u, v, _ = initial.balanced_zonal_c(N, 5, 10)
+    for name in ("hordiff_c_biharm_div", "hordiff_c_biharm_curl", "hordiff_c_biharm_curl_div"):
+        a = d21.hordiff(h, u, v, name)
+        b = d42.hordiff(h, u, v, name)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_hyperdiffusion_matches_the_biharmonic_away_from_panel_edges():
+    """h = z and the solid rotation are l = 1 fields (Laplacian eigenvalue
+    -2/a^2), so the exact tendency is -c^4 (2/a^2)^2 f = -4 coeff^4 hx^4 f.
+    The 2/1 gradient's edge closure leaves the Laplacian O(1) wrong on the
+    edge rows (the reference's own gradient_c_sbp21 error is 7% at N=32), so
+    the comparison starts four rows in, where the error converges."""
+    errs = []
+    for N in (24, 48):
+        d = oracle.OracleCDomain(N, 21)
+        hx = np.pi / 2 / N
+        lam = -4 * 0.03 ** 4 * hx ** 4
+        z = d.scalar_test_field("xyz", 2, "p")
+        u, v = d.vector_test_field("solid_rotation", 0)
+        th, tu, tv = d.hordiff(z, u, v, "hordiff_c_biharm_curl_div", 0.03, 0.03)
+        eh = (th - lam * z).reshape(6, N, N)[:, 4:-4, 4:-4]
+        eu = (tu - lam * u).reshape(6, N, N + 1)[:, 4:-4, 4:-4]
+        ev = (tv - lam * v).reshape(6, N + 1, N)[:, 4:-4, 4:-4]
+        errs.append((np.abs(eh).max() / np.abs(lam * z).max(),
+                     max(np.abs(eu).max(), np.abs(ev).max()) / np.abs(lam * u).max()))
+    assert errs[0][0] < 0.02 and errs[0][1] < 0.05
+    assert errs[1][0] < 0.5 * errs[0][0] and errs[1][1] < 0.5 * errs[0][1]
+
+
+def test_hyperdiffusion_conserves_mass_and_dissipates():
+    """The h part is a divergence, so its SBP_C21 integral vanishes; it is
+    negative semi-definite (<h, D h> < 0), and every vector part lowers the
+    kinetic energy of a rough flow in one explicit Euler step."""
+    N = 24
+    d = oracle.OracleCDomain(N, 21)
+    rng = np.random.default_rng(3)
+    h0, u0, v0, _ = initial.balanced_zonal_c(N, 4, 10)
+    u0 = u0 + rng.standard_normal(u0.shape)
+    v0 = v0 + rng.standard_normal(v0.shape)
+    h = rng.standard_normal(h0.shape)
+    th, _, _ = d.hordiff(h, u0, v0)
+    assert abs(d.mass(th)) / d.mass(np.abs(th)) < 1e-13
+    assert d.mass(h * th) < -0.5 * d.mass(np.abs(h * th))
+
+    def ke(u, v):
+        ut, vt = d.co2contra(u, v)
+        return d.mass(d.ke(u, v, ut, vt))
+
+    k0 = ke(u0, v0)
+    for name in ("hordiff_c_biharm_div", "hordiff_c_biharm_curl", "hordiff_c_biharm_curl_div"):
+        _, tu, tv = d.hordiff(h0, u0, v0, name)
+        assert ke(u0 + 900.0 * tu, v0 + 900.0 * tv) < (1 - 1e-5) * k0
+
+
+@pytest.mark.parametrize("order", [21, 42])
+def test_grad_perp_is_divergence_free(order):
+    """The staggered differences commute, so the divergence of grad_perp of
+    any corner field vanishes to round-off (the mimetic property the curl
+    part of the hyperdiffusion relies on; a sign error in either component
+    would leave 2 D_x D_y w)."""
+    N = 24
+    d = oracle.OracleCDomain(N, order)
+    w = d.scalar_test_field("xyz", 2, "q") + 0.1 * d.scalar_test_field("cross_polar_zeta", 0, "q")
+    gu, gv = d.grad_perp(w)
+    scale = np.abs(gu).max() / (6.371e6 * np.pi / 2 / N)
+    assert np.abs(d.div(gu, gv)).max() < 1e-13 * scale
+
+
+@pytest.mark.parametrize("order", [21, 42])
+def test_model_step_with_hyperdiffusion(order):
+    """A day of the drivers' step (RK4, then the explicit Euler step of the
+    hyperdiffusion with the namelist's coefficients 0.03) keeps the balanced
+    flow balanced.  The mass is kept to round-off at 2/1; at 4/2 the 2/1
+    divergence of the h diffusion is measured with the SBP_C42 quadrature,
+    so it drifts at the 1e-8 level, as in the reference."""
+    N = 24
+    d = oracle.OracleCDomain(N, order)
+    h, u, v, _ = initial.balanced_zonal_c(N, 2, 0, pert_rms=0.0)
+    m0 = d.mass(h)
+    h1, u1, v1 = d.model_step(h, u, v, 600.0, 144)
+    assert np.all(np.isfinite(h1)) and np.all(np.isfinite(u1)) and np.all(np.isfinite(v1))
+    assert np.abs(h1 - h).max() < 0.01 * (h.max() - h.min())
+    assert abs(d.mass(h1) - m0) / m0 < (1e-13 if order == 21 else 1e-7)
