@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass, field
+from typing import Optional
 
 import numpy as np
 
@@ -264,6 +265,14 @@ class OperatorSWM:
         self._check(self._L.swm_op_coriolis(self._h, cor_u._h, cor_v._h, hu._h, hv._h,
                                             h._h, curl._h))
 
+    def calc_grad_perp(self, gu, gv, w):
+        """grad_perp_c_sbp (C grid): w on mesh q, gu on u, gv on v."""
+        self._check(self._L.swm_op_grad_perp(self._h, gu._h, gv._h, w._h))
+
+    def contra2co(self, u, v, ut, vt):
+        """transform2co of co2contra_c_sbp*_new (C grid)."""
+        self._check(self._L.swm_op_contra2co(self._h, u._h, v._h, ut._h, vt._h))
+
     def quadrature_mass(self, f) -> float:
         out = ctypes.c_double()
         self._check(self._L.swm_quadrature_mass(self._h, f._h, ctypes.byref(out)))
@@ -427,10 +436,19 @@ class OperatorSWMDiff:
     hordiff_uv_name / uv_diff_coeff / hordiff_h_name / h_diff_coeff.  It lives
     on the model operator's context (its grid, stream and work fields)."""
 
-    def __init__(self, op: OperatorSWM, hordiff_uv_name: str = "hordiff_vec_xyz_Ah_sbp_42_narrow",
-                 uv_diff_coeff: float = 0.03,
-                 hordiff_h_name: str = "hordiff_scalar_Ah_sbp_42_narrow",
-                 h_diff_coeff: float = 0.01):
+    # the namelist defaults of &shallow_water_model (Ah) and
+    # &shallow_water_model_c (namelist_swm:20-25, 90-94)
+    DEFAULTS = {"Ah": ("hordiff_vec_xyz_Ah_sbp_42_narrow", 0.03, "hordiff_scalar_Ah_sbp_42_narrow", 0.01),
+                "C": ("hordiff_c_biharm_curl_div", 0.03, "hordiff_scalar_C", 0.03)}
+
+    def __init__(self, op: OperatorSWM, hordiff_uv_name: Optional[str] = None,
+                 uv_diff_coeff: Optional[float] = None, hordiff_h_name: Optional[str] = None,
+                 h_diff_coeff: Optional[float] = None):
+        d = self.DEFAULTS[op.staggering]
+        hordiff_uv_name = d[0] if hordiff_uv_name is None else hordiff_uv_name
+        uv_diff_coeff = d[1] if uv_diff_coeff is None else uv_diff_coeff
+        hordiff_h_name = d[2] if hordiff_h_name is None else hordiff_h_name
+        h_diff_coeff = d[3] if h_diff_coeff is None else h_diff_coeff
         self.op = op
         op._check(op._L.swm_diffusion_set(op._h, hordiff_uv_name.encode(), float(uv_diff_coeff),
                                           hordiff_h_name.encode(), float(h_diff_coeff)))

@@ -1484,6 +1484,20 @@ int hordiff_h_order(const char* name) {
   if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_63_narrow")) return 63;
   return 0;
 }
+// ... and the C-grid ones (hordiff_factory_mod.f90:19-36): the parts of the
+// vector hyperdiffusion (1 div, 2 curl, 3 both), and hordiff_scalar_C for h
+// (stored as kHordiffScalarC).
+constexpr int kHordiffScalarC = 21;
+int hordiff_c_parts(const char* name) {
+  if (!name) return 0;
+  if (!std::strcmp(name, "hordiff_c_biharm_div")) return 1;
+  if (!std::strcmp(name, "hordiff_c_biharm_curl")) return 2;
+  if (!std::strcmp(name, "hordiff_c_biharm_curl_div")) return 3;
+  return 0;
+}
+int hordiff_c_h(const char* name) {
+  return name && !std::strcmp(name, "hordiff_scalar_C") ? kHordiffScalarC : 0;
+}
 
 // work fields of the diffusion step: F 4, L 4, tendencies 3, and (FP64, for
 // the two-pass Laplacian) d1x 4, d1y 4
@@ -1625,6 +1639,17 @@ int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* 
 // launch's reads (launch_biharmonic_f32).
 int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
   const long long fs = ctx->g64.fs;
+  if (ctx->cg) {
+    const double cu = diff_coeff4(ctx, ctx->diff_uv_coeff), ch = diff_coeff4(ctx, ctx->diff_h_coeff);
+    if (ctx->prec == SWM_FP64_PLAIN)
+      CK(cgrid_diffusion_step(ctx->cg, ctx->topo, ctx->edge64, ctx->diff_uv, cu, ch, (double*)v0->hi, dt, ctx->st),
+         "C-grid diffusion step");
+    else
+      CK(cgrid_diffusion_step32(ctx->cg, ctx->topo, (float*)ctx->edge, ctx->diff_uv, cu, ch, (float*)v0->hi, v0->lo,
+                                dt, ctx->st),
+         "C-grid diffusion step");
+    return SWM_OK;
+  }
   if (ctx->prec == SWM_FP64_PLAIN) {
     double* x = (double*)v0->hi;
     double* T = dwork<double>(ctx, 8);
@@ -1661,6 +1686,7 @@ int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
 
 int diffusion_ready(swm_ctx* ctx) {
   if (!ctx->diff_uv) return fail(ctx, SWM_E_INVALID, "diffusion is not configured (swm_diffusion_set)");
+  if (ctx->cg) return SWM_OK;  // the C grid's work fields exist from creation
   if (int rc = diffusion_ws(ctx, ctx->diff_uv)) return rc;
   return diffusion_ws(ctx, ctx->diff_h);
 }
@@ -1685,9 +1711,9 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 
 int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
                       const char* hordiff_h_name, double h_diff_coeff) {
-  AH_ONLY(ctx, "swm_diffusion_set");
   if (!ctx) return fail(nullptr, SWM_E_INVALID, "null context");
-  const int uv = hordiff_uv_order(hordiff_uv_name), h = hordiff_h_order(hordiff_h_name);
+  const int uv = ctx->cg ? hordiff_c_parts(hordiff_uv_name) : hordiff_uv_order(hordiff_uv_name);
+  const int h = ctx->cg ? hordiff_c_h(hordiff_h_name) : hordiff_h_order(hordiff_h_name);
   if (!uv || !h)
     return fail(ctx, SWM_E_UNSUPPORTED,
                 std::string("unsupported hordiff operator: ") +
@@ -1714,7 +1740,6 @@ int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_
 }
 
 int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
-  AH_ONLY(ctx, "swm_apply_diffusion");
   TraceRange trace_("swm_apply_diffusion");
   if (int rc = check_state(ctx, vout)) return rc;
   if (int rc = check_state(ctx, vin)) return rc;
@@ -1722,6 +1747,20 @@ int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
   USE_DEVICE(ctx);
   if (int rc = diffusion_ready(ctx)) return rc;
   const long long fs = ctx->g64.fs;
+  if (ctx->cg) {
+    const double cu = diff_coeff4(ctx, ctx->diff_uv_coeff), ch = diff_coeff4(ctx, ctx->diff_h_coeff);
+    if (ctx->prec == SWM_FP64_PLAIN) {
+      CK(cgrid_diffusion(ctx->cg, ctx->topo, ctx->edge64, ctx->diff_uv, cu, ch, (const double*)vin->hi,
+                         (double*)vout->hi, ctx->st),
+         "C-grid diffusion");
+    } else {
+      CK(cudaMemsetAsync(vout->lo, 0, sizeof(float) * 3 * fs, ctx->st), "memset");
+      CK(cgrid_diffusion32(ctx->cg, ctx->topo, (float*)ctx->edge, ctx->diff_uv, cu, ch, (const float*)vin->hi,
+                           (float*)vout->hi, ctx->st),
+         "C-grid diffusion");
+    }
+    return SWM_OK;
+  }
   if (ctx->prec == SWM_FP64_PLAIN) {
     const double* x = (const double*)vin->hi;
     double* o = (double*)vout->hi;
@@ -1734,7 +1773,6 @@ int swm_apply_diffusion(swm_ctx* ctx, swm_state* vout, const swm_state* vin) {
 }
 
 int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
-  AH_ONLY(ctx, "swm_diffusion_step");
   TraceRange trace_("swm_diffusion_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
@@ -1745,7 +1783,6 @@ int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
 }
 
 int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps) {
-  AH_ONLY(ctx, "swm_model_step");
   TraceRange trace_("swm_model_step");
   if (int rc = check_state(ctx, v0)) return rc;
   if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, SWM_E_INVALID, "bad dt or nsteps");
@@ -1946,6 +1983,24 @@ int swm_op_coriolis(swm_ctx* ctx, swm_field* cor_u, swm_field* cor_v, const swm_
     return SWM_OK;
   }
   CK(launch_coriolis(ctx->g64, ctx->m64, hu->p, hv->p, h->p, curl->p, cor_u->p, cor_v->p, ctx->st), "coriolis");
+  return SWM_OK;
+}
+int swm_op_grad_perp(swm_ctx* ctx, swm_field* gu, swm_field* gv, const swm_field* w) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "grad_perp is provided on the C grid only");
+  CHECK_FIELDS(gu, gv, w);
+  for (auto fm : {std::make_pair((const swm_field*)gu, SWM_MESH_U), std::make_pair((const swm_field*)gv, SWM_MESH_V),
+                  std::make_pair(w, SWM_MESH_Q)})
+    if (int rc = check_mesh(ctx, fm.first, fm.second, "grad_perp")) return rc;
+  CK(cgrid_grad_perp(ctx->cg, w->p, gu->p, gv->p, ctx->st), "grad_perp");
+  return SWM_OK;
+}
+int swm_op_contra2co(swm_ctx* ctx, swm_field* u, swm_field* v, const swm_field* ut, const swm_field* vt) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "contra2co is provided on the C grid only");
+  CHECK_FIELDS(u, v, ut, vt);
+  for (auto fm : {std::make_pair((const swm_field*)u, SWM_MESH_U), std::make_pair((const swm_field*)v, SWM_MESH_V),
+                  std::make_pair(ut, SWM_MESH_U), std::make_pair(vt, SWM_MESH_V)})
+    if (int rc = check_mesh(ctx, fm.first, fm.second, "contra2co")) return rc;
+  CK(cgrid_contra2co(ctx->cg, ut->p, vt->p, u->p, v->p, ctx->st), "contra2co");
   return SWM_OK;
 }
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f) {

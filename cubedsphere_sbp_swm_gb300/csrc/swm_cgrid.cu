@@ -142,13 +142,16 @@ void fill_ops(int order, COps& o) {
 
 // Metric fields (one pitched field each) and work fields of one context.
 // GB300's FP64 pipe is narrow, so the divisions of the operators are taken
-// once on the host: reciprocal fields 1/J and 1/(J hx a), and J Qi12.
+// once on the host: reciprocal fields 1/J and 1/(J hx a), and J Qi12.  The
+// covariant metric (J Q12, Q11, Q22) and 1/(J hx a) on the faces serve the
+// contra2co transform and grad_perp of the hyperdiffusion.
 enum { M_JP = 0, M_QI2P, M_FP, M_RJP, M_RJPHA, M_JQI2P,  // centres
        M_JU, M_QI1U, M_RJU,                              // x-faces
        M_JV, M_QI3V, M_RJV,                              // y-faces
        M_JQ, M_RJQHA,                                    // corners
+       M_JQ2P, M_Q1U, M_Q3V, M_RJUHA, M_RJVHA,           // covariant metric, face 1/(J hx a)
        M_COUNT };
-constexpr int kMetricMesh[M_COUNT] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 2, 2, 2, 3, 3};
+constexpr int kMetricMesh[M_COUNT] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 0, 1, 2, 1, 2};
 enum { W_AP = 0, W_BP, W_UT, W_VT, W_HU, W_HV, W_GU, W_GV, W_KEU, W_KEV, W_CURL, W_FU, W_KE,
        W_CUP, W_CVP, W_COUNT };
 
@@ -171,10 +174,11 @@ template <class T>
 struct CArgsT {
   FieldGeom g;
   int N, L, flags;
+  int ord;  // SBP order of ops (21 or 42): the kernels' template argument
   T grav;
   T dx1;  // 1 / (a hx), the gradient's scale
   COpsT<T> ops;
-  const T *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha;
+  const T *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha, *rJuha, *rJvha;
   const int* halo;
   // inputs
   const T *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
@@ -212,7 +216,7 @@ __device__ __forceinline__ T stag_at(const StagOpT<T>& s, const T* __restrict__ 
   return acc;
 }
 
-// value of a neighbour's point in the cross halo: mesh 0 o, 1 u, 2 v; side 0
+// value of a neighbour's point in the cross halo: mesh 0 o, 1 u, 2 v, 3 q; side 0
 // left, 1 right, 2 bottom, 3 top; depth d >= 1; k along the side.  f is the
 // field of the mesh, g the other component of a C vector.
 template <class T>
@@ -378,6 +382,73 @@ __global__ void __launch_bounds__(256) w2uv_kernel(const __grid_constant__ CArgs
   SWM_C_INDEX(N + 1, N)
   const FieldGeom& g = a.g;
   a.fu[at(g, p, i, j)] = stag_at<W, T>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
+}
+
+// grad_perp_c_sbp (grad_perp/grad_perp_c_sbp_mod.f90:20-95): the staggered
+// differences of the corner field w along y onto the x-faces and along x onto
+// the y-faces, each with the "at_center" SAT penalty on the jump between the
+// panel's edge point and the neighbour's copy of it
+// (sbp_operator_mod.f90:343-391); gu = -(.) / (J a hx), gv = (.) / (J a hx).
+template <int ORD, class T>
+__global__ void __launch_bounds__(256) gperp_kernel(const __grid_constant__ CArgsT<T> a) {
+  constexpr int W = ORD == 42 ? 4 : 2;
+  const int N = a.N;
+  SWM_C_INDEX(N + 1, N + 1)
+  const FieldGeom& g = a.g;
+  const COpsT<T>& o = a.ops;
+  const T* w = a.curl_in;
+  const int e = at(g, p, i, j);
+  if (j < N) {  // x-face: along the column i
+    const T* col = w + at(g, p, i, 0);
+    T s = stag_at<W, T>(o.di2c, col, g.P, N, j);
+    if (j < o.np) s = s + T(0.5) * o.pen_c[j] * (col[0] - halo_at(a, 3, 2, p, 1, i, w, w));
+    if (j >= N - o.np) s = s + T(0.5) * o.pen_c[N - 1 - j] * (halo_at(a, 3, 3, p, 1, i, w, w) - col[N * g.P]);
+    a.o1[e] = -s * a.rJuha[e];
+  }
+  if (i < N) {  // y-face: along the row j
+    const T* row = w + at(g, p, 0, j);
+    T s = stag_at<W, T>(o.di2c, row, 1, N, i);
+    if (i < o.np) s = s + T(0.5) * o.pen_c[i] * (row[0] - halo_at(a, 3, 0, p, 1, j, w, w));
+    if (i >= N - o.np) s = s + T(0.5) * o.pen_c[N - 1 - i] * (halo_at(a, 3, 1, p, 1, j, w, w) - row[N]);
+    a.o2[e] = s * a.rJvha[e];
+  }
+}
+
+// Last pass of the hyperdiffusion (hordiff_Cgrid_mod.f90:59-140,
+// hordiff_scalar_mod.f90:33-53): th = c4h L(L(h)); (tu, tv) = c4uv A +
+// 1.0 (c4uv B), A the curl part, B the divergence part (parts 1 B only, 2 A
+// only, 3 both).  mode 0 stores the tendency, 1 the explicit Euler step
+// y + dt t (explicit_Eul1_mod.f90:20-30) in place, 2 the same step on an
+// FP32 (hi, lo) state pair, added in FP64.
+template <class T>
+__global__ void __launch_bounds__(256) diff_combine_kernel(FieldGeom g, int N, int parts, T c4uv, T c4h,
+                                                           const T* __restrict__ Lh, const T* __restrict__ Au,
+                                                           const T* __restrict__ Av, const T* __restrict__ Bu,
+                                                           const T* __restrict__ Bv, int mode, double dt, T* out,
+                                                           float* lo) {
+  SWM_C_INDEX(N + 1, N + 1)
+  const int e = at(g, p, i, j);
+  auto put = [&](int comp, T t) {
+    const long long o = comp * g.fs + e;
+    if (mode == 0) {
+      out[o] = t;
+    } else if (mode == 1) {
+      out[o] = out[o] + T(dt) * t;
+    } else {
+      const double x = ((double)out[o] + (double)lo[o]) + dt * (double)t;
+      const float hi = (float)x;
+      out[o] = T(hi);
+      lo[o] = (float)(x - (double)hi);
+    }
+  };
+  auto mix = [&](T A, T B) {
+    if (parts == 1) return c4uv * B;
+    if (parts == 2) return c4uv * A;
+    return c4uv * A + T(1.0) * (c4uv * B);
+  };
+  if (i < N && j < N) put(0, c4h * Lh[e]);
+  if (j < N) put(1, mix(Au[e], Bu[e]));
+  if (i < N) put(2, mix(Av[e], Bv[e]));
 }
 
 // Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
@@ -626,10 +697,13 @@ struct CGrid {
   double hx = 0.0, radius = 1.0, grav = 9.80616;
   COps ops{};
   COpsT<float> ops32{};
+  COps ops21{};             // the 2/1 operators of the hyperdiffusion (any order)
+  COpsT<float> ops21_32{};
   double* met = nullptr;   // M_COUNT fields
   float* met32 = nullptr;  // their FP32 copies (contexts of the FP32 form)
   double* wk = nullptr;    // W_COUNT fields
   double* rk = nullptr;    // Y, Kb, acc: 3 fields each
+  double* dk = nullptr;    // hyperdiffusion results: L(L(h)), curl part (u, v)
   int* halo = nullptr;
   double* wts = nullptr;   // quadrature weights: centres (N), interfaces (N+1)
   double* part = nullptr;  // kMassBlocks partial sums
@@ -639,26 +713,32 @@ struct CGrid {
 
 namespace {
 
-// Kernel arguments in precision T: FP64 metric and work fields, or the
-// FP32 metric copies and the same work buffers read as floats.
 template <class T>
-CArgsT<T> base_args(const CGrid* c) {
+const T* metric_t(const CGrid* c, int k) {
+  if constexpr (sizeof(T) == 8) return c->metric(k);
+  else return c->met32 + (long long)k * c->g.fs;
+}
+
+// Kernel arguments in precision T: FP64 metric and work fields, or the
+// FP32 metric copies and the same work buffers read as floats.  ord 0: the
+// operators of the context's order; 21: the 2/1 ones.
+template <class T>
+CArgsT<T> base_args(const CGrid* c, int ord = 0) {
   CArgsT<T> a{};
   a.g = c->g; a.N = c->N; a.L = c->L;
   a.grav = T(c->grav);
-  if constexpr (sizeof(T) == 8) a.ops = c->ops;
-  else a.ops = c->ops32;
+  a.ord = ord ? ord : c->order;
+  const bool o21 = a.ord == 21;
+  if constexpr (sizeof(T) == 8) a.ops = o21 ? c->ops21 : c->ops;
+  else a.ops = o21 ? c->ops21_32 : c->ops32;
   a.dx1 = T(1.0 / (c->radius * c->hx));
-  auto M = [&](int k) -> const T* {
-    if constexpr (sizeof(T) == 8) return c->metric(k);
-    else return c->met32 + (long long)k * c->g.fs;
-  };
+  auto M = [&](int k) { return metric_t<T>(c, k); };
   auto Wk = [&](int k) { return reinterpret_cast<T*>(c->work(k)); };
   a.Jp = M(M_JP); a.fp = M(M_FP); a.rJp = M(M_RJP);
   a.rJpha = M(M_RJPHA); a.JQi2p = M(M_JQI2P);
   a.Ju = M(M_JU); a.Qi1u = M(M_QI1U); a.rJu = M(M_RJU);
   a.Jv = M(M_JV); a.Qi3v = M(M_QI3V); a.rJv = M(M_RJV);
-  a.rJqha = M(M_RJQHA);
+  a.rJqha = M(M_RJQHA); a.rJuha = M(M_RJUHA); a.rJvha = M(M_RJVHA);
   a.halo = c->halo;
   a.Ap = Wk(W_AP); a.Bp = Wk(W_BP); a.ut = Wk(W_UT); a.vt = Wk(W_VT);
   a.hu = Wk(W_HU); a.hv = Wk(W_HV); a.Gu = Wk(W_GU); a.Gv = Wk(W_GV);
@@ -674,7 +754,7 @@ const dim3 kBlock(32, 8, 1);
 #define SWM_C_LAUNCH(name, kern, nx, ny)                                                              \
   template <class T>                                                                                   \
   cudaError_t name(const CGrid* c, const CArgsT<T>& a, cudaStream_t st) {                             \
-    if (c->order == 42) kern<42, T><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                          \
+    if (a.ord == 42) kern<42, T><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                             \
     else kern<21, T><<<grid_for(nx, ny), kBlock, 0, st>>>(a);                                         \
     return cudaGetLastError();                                                                         \
   }
@@ -684,6 +764,7 @@ SWM_C_LAUNCH(run_curl, curl_kernel, c->N + 1, c->N + 1)
 SWM_C_LAUNCH(run_w2uv, w2uv_kernel, c->N + 1, c->N)
 SWM_C_LAUNCH(run_centre_b, centre_b_kernel, c->N, c->N)
 SWM_C_LAUNCH(run_faces_b, faces_b_kernel, c->N + 1, c->N + 1)
+SWM_C_LAUNCH(run_gperp, gperp_kernel, c->N + 1, c->N + 1)
 #undef SWM_C_LAUNCH
 
 #define CKE(call)                               \
@@ -715,13 +796,23 @@ cudaError_t rhs(const CGrid* c, const Topology& tp, T* edge, CArgsT<T> a, const 
 // ------------------------------------------------------------------ host
 // ECS metric on the prototype face (ecs_metric_mod.f90:326-478) and the
 // panel frame (ecs_proto2realface with the identity rotation).
-void metric_at(double al, double be, double& J, double& qi1, double& qi2, double& qi3) {
+struct MetricAt {
+  double J, qi1, qi2, qi3, q1, q2, q3;
+};
+MetricAt metric_at(double al, double be) {
   const double ta = std::tan(al), tb = std::tan(be);
   const double sg = std::sqrt(1.0 + ta * ta + tb * tb);
-  J = (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
-  qi1 = sg * sg / (1.0 + ta * ta);
-  qi2 = sg * sg * ta * tb / ((1.0 + ta * ta) * (1.0 + tb * tb));
-  qi3 = sg * sg / (1.0 + tb * tb);
+  const double s4 = sg * sg * sg * sg;
+  MetricAt m;
+  m.J = (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
+  m.qi1 = sg * sg / (1.0 + ta * ta);
+  m.qi2 = sg * sg * ta * tb / ((1.0 + ta * ta) * (1.0 + tb * tb));
+  m.qi3 = sg * sg / (1.0 + tb * tb);
+  // the covariant metric tensor (ecs_Q, ecs_metric_mod.f90:401-419)
+  m.q1 = (1.0 + ta * ta) * (1.0 + ta * ta) * (1.0 + tb * tb) / s4;
+  m.q2 = -(1.0 + ta * ta) * (1.0 + tb * tb) * ta * tb / s4;
+  m.q3 = (1.0 + ta * ta) * (1.0 + tb * tb) * (1.0 + tb * tb) / s4;
+  return m;
 }
 
 double coriolis_at(int p, double al, double be, double omega, const double ax[3]) {
@@ -735,25 +826,28 @@ double coriolis_at(int p, double al, double be, double omega, const double ax[3]
   return 2.0 * omega * pr;  // calc_coriolis_parameter (coriolis_factory_mod.f90:151-172)
 }
 
-// Cross-halo table of mesh T (0 o, 1 u, 2 v): create_o_points_halo_exchange
-// and create_symm_halo_vec_exchange_U/V_points (exchange_factory_mod.f90:13-
-// 156, 317-617) with the component swap and signs of buffer_mod.f90:278-475,
-// for the halo points the C-grid SBP operators read: left / right layers
-// along the panel rows, bottom / top layers along the columns, depth 1..3.
-// The neighbour's points are placed with the receiving mesh's point counts,
-// so the duplicated edge faces of u (v) fill the first x (y) layer.
+// Cross-halo table of mesh T (0 o, 1 u, 2 v, 3 q): create_o_points_halo_
+// exchange, create_symm_halo_vec_exchange_U/V_points and create_xy_points_
+// halo_exchange (exchange_factory_mod.f90:13-156, 317-617) with the component
+// swap and signs of buffer_mod.f90:278-475, for the halo points the C-grid
+// SBP operators read: left / right layers along the panel rows, bottom / top
+// layers along the columns, depth 1..3.  The neighbour's points are placed
+// with the receiving mesh's point counts, so the duplicated edge faces of u
+// (v) fill the first x (y) layer and the duplicated edge points of q its
+// first layers.
+constexpr int kHaloMeshes = 4;
 bool build_halo(int N, const FieldGeom& g, std::vector<int>& tab, std::string& why) {
   const int L = N + 1;
-  const int dims[3][2] = {{N, N}, {N + 1, N}, {N, N + 1}};
-  tab.assign((size_t)3 * 4 * 6 * kHaloDepth * L, -1);
-  for (int T = 0; T < 3; ++T) {
+  const int dims[kHaloMeshes][2] = {{N, N}, {N + 1, N}, {N, N + 1}, {N + 1, N + 1}};
+  tab.assign((size_t)kHaloMeshes * 4 * 6 * kHaloDepth * L, -1);
+  for (int T = 0; T < kHaloMeshes; ++T) {
     const int nx = dims[T][0], ny = dims[T][1];
     for (int p = 0; p < 6; ++p)
       for (int q = 0; q < 6; ++q) {
         if (q == p) continue;
         int istep, jstep, dim_i;
         cube::orientation(p, q, istep, jstep, dim_i);  // (receiver, sender)
-        const bool swap = T != 0 && !dim_i;
+        const bool swap = (T == 1 || T == 2) && !dim_i;
         const int S = swap ? 3 - T : T;
         int sign = 1;
         if (T == 1) sign = dim_i ? istep : jstep;
@@ -787,6 +881,93 @@ bool build_halo(int N, const FieldGeom& g, std::vector<int>& tab, std::string& w
   return true;
 }
 
+// co2contra (to_co false) or the contra2co transform of co2contra_c_sbp*_new
+// (to_co true, co2contra_Cgrid_mod.f90:135-203): the same two passes, with
+// the covariant metric J Q12, Q11, Q22 in place of the inverse one.
+template <class T>
+cudaError_t transform(const CGrid* c, CArgsT<T> a, const T* x, const T* y, T* xo, T* yo, bool to_co,
+                      cudaStream_t st) {
+  if (to_co) {
+    a.JQi2p = metric_t<T>(c, M_JQ2P);
+    a.Qi1u = metric_t<T>(c, M_Q1U);
+    a.Qi3v = metric_t<T>(c, M_Q3V);
+  }
+  a.u = x; a.v = y; a.ut = xo; a.vt = yo;
+  a.flags = F_CO | F_WUT;
+  CKE(run_centre_a(c, a, st));
+  return run_faces_a(c, a, st);
+}
+
+// The C-grid hyperdiffusion of operator_swm_diff_t (operator_swm_diff_mod.f90
+// :25-46) with the 2/1 operators the factory uses at any order
+// (hordiff_factory_mod.f90:53-139, 196-247), on the state in (h, u, v):
+//   curl part  contra2co grad_perp curl contra2co grad_perp curl (u, v)
+//   div part   grad div co2contra grad div co2contra (u, v)
+//   h          L(L(h)), L = div co2contra grad
+// then the combine pass (mode 0 tendency into out, 1 / 2 Euler step on out
+// = the state, 2 with the FP32 low part lo).
+template <class T>
+cudaError_t diffusion(const CGrid* c, const Topology& tp, T* edge, int parts, double c4uv, double c4h, const T* in,
+                      T* out, float* lo, double dt, int mode, cudaStream_t st) {
+  const long long fs = c->g.fs;
+  const CArgsT<T> a = base_args<T>(c, 21);
+  auto Wk = [&](int k) { return reinterpret_cast<T*>(c->work(k)); };
+  T *P1 = Wk(W_KE), *U1 = Wk(W_UT), *V1 = Wk(W_VT), *U2 = Wk(W_HU), *V2 = Wk(W_HV);
+  T *U3 = Wk(W_GU), *V3 = Wk(W_GV), *Q1 = Wk(W_CURL);
+  T* D = reinterpret_cast<T*>(c->dk);
+  T *TH = D, *TU = D + fs, *TV = D + 2 * fs;
+  const T *h = in, *u = in + fs, *v = in + 2 * fs;
+  auto div = [&](const T* x, const T* y, T* o) {
+    CArgsT<T> b = a;
+    b.hu_in = x; b.hv_in = y; b.o1 = o;
+    b.flags = F_DIV | F_SEP;
+    return run_centre_b(c, b, st);
+  };
+  auto grad = [&](const T* f, T* gx, T* gy) {
+    CArgsT<T> b = a;
+    b.ke_in = f; b.o1 = gx; b.o2 = gy;
+    b.flags = F_GRAD | F_SEP;
+    return run_faces_b(c, b, st);
+  };
+  auto curl = [&](const T* x, const T* y, T* q) {
+    CArgsT<T> b = a;
+    b.u = x; b.v = y; b.curl = q;
+    CKE(run_curl(c, b, st));
+    return launch_sync_scalar_t<T>(c->g, tp, q, edge, st);
+  };
+  auto gperp = [&](const T* q, T* gu, T* gv) {
+    CArgsT<T> b = a;
+    b.curl_in = q; b.o1 = gu; b.o2 = gv;
+    return run_gperp(c, b, st);
+  };
+  if (parts & 2) {
+    CKE(curl(u, v, Q1));
+    CKE(gperp(Q1, U1, V1));
+    CKE(transform(c, a, (const T*)U1, (const T*)V1, U2, V2, true, st));
+    CKE(curl(U2, V2, Q1));
+    CKE(gperp(Q1, U1, V1));
+    CKE(transform(c, a, (const T*)U1, (const T*)V1, TU, TV, true, st));
+  }
+  if (parts & 1) {
+    CKE(transform(c, a, u, v, U1, V1, false, st));
+    CKE(div(U1, V1, P1));
+    CKE(grad(P1, U2, V2));
+    CKE(transform(c, a, (const T*)U2, (const T*)V2, U1, V1, false, st));
+    CKE(div(U1, V1, P1));
+    CKE(grad(P1, U3, V3));
+  }
+  const T* f = h;
+  for (int rep = 0; rep < 2; ++rep) {
+    CKE(grad(f, U1, V1));
+    CKE(transform(c, a, (const T*)U1, (const T*)V1, U2, V2, false, st));
+    CKE(div(U2, V2, rep ? TH : P1));
+    f = P1;
+  }
+  diff_combine_kernel<T><<<grid_for(c->N + 1, c->N + 1), kBlock, 0, st>>>(
+      c->g, c->N, parts, T(c4uv), T(c4h), TH, TU, TV, U3, V3, mode, dt, out, lo);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
@@ -800,6 +981,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   c->radius = radius; c->grav = grav;
   fill_ops(order, c->ops);
   c->ops32 = ops_cast<float>(c->ops);
+  fill_ops(21, c->ops21);
+  c->ops21_32 = ops_cast<float>(c->ops21);
   const double an = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
   const double ax[3] = {axis[0] / an, axis[1] / an, axis[2] / an};
   std::vector<int> tab;
@@ -825,6 +1008,7 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   ok(cudaMalloc(&c->met, M_COUNT * fb));
   ok(cudaMalloc(&c->wk, W_COUNT * fb));
   ok(cudaMalloc(&c->rk, 9 * fb));
+  ok(cudaMalloc(&c->dk, 3 * fb));
   ok(cudaMalloc(&c->halo, sizeof(int) * tab.size()));
   ok(cudaMalloc(&c->wts, sizeof(double) * w.size()));
   ok(cudaMalloc(&c->part, sizeof(double) * kMassBlocks));
@@ -844,17 +1028,20 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
           for (int i = 0; i < nx; ++i) {
             const double al = -0.25 * kPiC + (i + (ci ? 0.5 : 0.0)) * c->hx;
             const double be = -0.25 * kPiC + (j + (cj ? 0.5 : 0.0)) * c->hx;
-            double J, q1, q2, q3, x;
-            metric_at(al, be, J, q1, q2, q3);
-            const double jha = J * c->hx * radius;
+            const MetricAt m = metric_at(al, be);
+            const double J = m.J, jha = J * c->hx * radius;
+            double x;
             switch (k) {
-              case M_QI2P: x = q2; break;
+              case M_QI2P: x = m.qi2; break;
               case M_FP: x = coriolis_at(p, al, be, omega, ax); break;
               case M_RJP: case M_RJU: case M_RJV: x = 1.0 / J; break;
-              case M_RJPHA: case M_RJQHA: x = 1.0 / jha; break;
-              case M_JQI2P: x = J * q2; break;
-              case M_QI1U: x = q1; break;
-              case M_QI3V: x = q3; break;
+              case M_RJPHA: case M_RJQHA: case M_RJUHA: case M_RJVHA: x = 1.0 / jha; break;
+              case M_JQI2P: x = J * m.qi2; break;
+              case M_QI1U: x = m.qi1; break;
+              case M_QI3V: x = m.qi3; break;
+              case M_JQ2P: x = J * m.q2; break;
+              case M_Q1U: x = m.q1; break;
+              case M_Q3V: x = m.q3; break;
               default: x = J; break;
             }
             hm[(size_t)p * g.ps + (size_t)j * g.P + i] = x;
@@ -863,6 +1050,7 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     }
     ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
     ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
+    ok(cudaMemsetAsync(c->dk, 0, 3 * fb, st));
     ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
     if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
       ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
@@ -880,8 +1068,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
 
 void cgrid_destroy(CGrid* c) {
   if (!c) return;
-  for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->halo, (void*)c->wts,
-                  (void*)c->part})
+  for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->dk, (void*)c->halo,
+                  (void*)c->wts, (void*)c->part})
     if (p) cudaFree(p);
   delete c;
 }
@@ -1035,6 +1223,40 @@ cudaError_t cgrid_pack(CGrid* c, int mesh, const void* field, const float* lo, d
   cpack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c->g, nx, ny, lo ? nullptr : (const double*)field,
                                                             lo ? (const float*)field : nullptr, lo, dense);
   return cudaGetLastError();
+}
+
+cudaError_t cgrid_grad_perp(CGrid* c, const double* w, double* gu, double* gv, cudaStream_t st) {
+  CArgsT<double> a = base_args<double>(c);
+  a.curl_in = w; a.o1 = gu; a.o2 = gv;
+  return run_gperp(c, a, st);
+}
+
+cudaError_t cgrid_contra2co(CGrid* c, const double* ut, const double* vt, double* u, double* v, cudaStream_t st) {
+  return transform(c, base_args<double>(c), ut, vt, u, v, true, st);
+}
+
+cudaError_t cgrid_diffusion(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,
+                            const double* in, double* out, cudaStream_t st) {
+  if (in == out || parts < 1 || parts > 3) return cudaErrorInvalidValue;
+  return diffusion<double>(c, tp, edge, parts, c4uv, c4h, in, out, nullptr, 0.0, 0, st);
+}
+
+cudaError_t cgrid_diffusion_step(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,
+                                 double* y0, double dt, cudaStream_t st) {
+  if (parts < 1 || parts > 3) return cudaErrorInvalidValue;
+  return diffusion<double>(c, tp, edge, parts, c4uv, c4h, y0, y0, nullptr, dt, 1, st);
+}
+
+cudaError_t cgrid_diffusion32(CGrid* c, const Topology& tp, float* edge, int parts, double c4uv, double c4h,
+                              const float* in, float* out, cudaStream_t st) {
+  if (!c->met32 || in == out || parts < 1 || parts > 3) return cudaErrorInvalidValue;
+  return diffusion<float>(c, tp, edge, parts, c4uv, c4h, in, out, nullptr, 0.0, 0, st);
+}
+
+cudaError_t cgrid_diffusion_step32(CGrid* c, const Topology& tp, float* edge, int parts, double c4uv, double c4h,
+                                   float* hi, float* lo, double dt, cudaStream_t st) {
+  if (!c->met32 || parts < 1 || parts > 3) return cudaErrorInvalidValue;
+  return diffusion<float>(c, tp, edge, parts, c4uv, c4h, hi, hi, lo, dt, 2, st);
 }
 
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st) {

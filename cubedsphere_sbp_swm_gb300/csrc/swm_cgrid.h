@@ -69,6 +69,26 @@ cudaError_t cgrid_rk4_32(CGrid* c, const Topology& tp, float* edge, const float*
 // (hi, lo) pair, split from / joined into FP64.
 cudaError_t cgrid_unpack(CGrid* c, int mesh, const double* dense, void* field, float* lo, cudaStream_t st);
 cudaError_t cgrid_pack(CGrid* c, int mesh, const void* field, const float* lo, double* dense, cudaStream_t st);
+// grad_perp_c_sbp21 / _sbp42 of a corner field (grad_perp_c_sbp_mod.f90:
+// 20-95) and the transform2co of co2contra_c_sbp21_new / _sbp42_new
+// (co2contra_Cgrid_mod.f90:135-203), at the context's order.
+cudaError_t cgrid_grad_perp(CGrid* c, const double* w, double* gu, double* gv, cudaStream_t st);
+cudaError_t cgrid_contra2co(CGrid* c, const double* ut, const double* vt, double* u, double* v, cudaStream_t st);
+// The hyperdiffusion of operator_swm_diff_t with the C-grid names
+// (hordiff_factory_mod.f90:19-36): parts 1 hordiff_c_biharm_div, 2
+// hordiff_c_biharm_curl, 3 hordiff_c_biharm_curl_div for (u, v), and
+// hordiff_scalar_C for h, with the 2/1 operators at any order.  c4uv, c4h:
+// -(c^4) of the two coefficients.  cgrid_diffusion*: the tendency of the
+// state in into out (distinct); cgrid_diffusion_step*: one explicit Euler
+// step in place (FP32: on the (hi, lo) pair, added in FP64).
+cudaError_t cgrid_diffusion(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,
+                            const double* in, double* out, cudaStream_t st);
+cudaError_t cgrid_diffusion_step(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,
+                                 double* y0, double dt, cudaStream_t st);
+cudaError_t cgrid_diffusion32(CGrid* c, const Topology& tp, float* edge, int parts, double c4uv, double c4h,
+                              const float* in, float* out, cudaStream_t st);
+cudaError_t cgrid_diffusion_step32(CGrid* c, const Topology& tp, float* edge, int parts, double c4uv, double c4h,
+                                   float* hi, float* lo, double dt, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

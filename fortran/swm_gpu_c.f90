@@ -262,6 +262,14 @@ interface
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, cor_u, cor_v, hu, hv, h, curl
     end function swm_op_coriolis
+    integer(c_int) function swm_op_grad_perp(ctx, gu, gv, w) bind(c, name="swm_op_grad_perp")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, gu, gv, w
+    end function swm_op_grad_perp
+    integer(c_int) function swm_op_contra2co(ctx, u, v, ut, vt) bind(c, name="swm_op_contra2co")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, u, v, ut, vt
+    end function swm_op_contra2co
     integer(c_int) function swm_sync_scalar(ctx, f) bind(c, name="swm_sync_scalar")
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, f

@@ -193,15 +193,21 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
  * 143-146, barotropic_inst_mod.f90:163-168).  swm_diffusion_set takes the
  * namelist's hordiff_uv_name / uv_diff_coeff / hordiff_h_name /
  * h_diff_coeff (config_swm_mod.f90:24-27, operator_swm_diff_factory_mod.f90
- * :27-30).  Supported names: "hordiff_vec_xyz_Ah_sbp_42_narrow" and
- * "hordiff_vec_xyz_Ah_sbp_63_narrow" for (u, v); "hordiff_scalar_Ah_sbp_42_
- * narrow" and "hordiff_scalar_Ah_sbp_63_narrow" for h
- * (hordiff_factory_mod.f90:27-40); others give SWM_E_UNSUPPORTED.  The
- * operator is -(c^4) L(L(.)) with L the narrow-stencil SBP Laplacian and
- * c = coeff*radius*hx, on h and on the Cartesian components of the
- * velocity.  FP64 contexts compute it in FP64; FP32 contexts compute the
- * tendency in FP32 from the high part of the state and add it to the
- * (hi, lo) pair in FP64. */
+ * :27-30).  Supported names on the Ah grid: "hordiff_vec_xyz_Ah_sbp_42_narrow"
+ * and "hordiff_vec_xyz_Ah_sbp_63_narrow" for (u, v); "hordiff_scalar_Ah_sbp_
+ * 42_narrow" and "hordiff_scalar_Ah_sbp_63_narrow" for h
+ * (hordiff_factory_mod.f90:27-40).  The operator is -(c^4) L(L(.)) with L
+ * the narrow-stencil SBP Laplacian and c = coeff*radius*hx, on h and on the
+ * Cartesian components of the velocity.  On the C grid
+ * (hordiff_factory_mod.f90:19-36, 53-139, 196-247): "hordiff_c_biharm_div",
+ * "hordiff_c_biharm_curl" or "hordiff_c_biharm_curl_div" for (u, v) --
+ * -(c^4) grad div co2contra grad div co2contra and / or -(c^4) contra2co
+ * grad_perp curl contra2co grad_perp curl -- and "hordiff_scalar_C" for h,
+ * -(c^4) L(L(h)) with L = div co2contra grad, all with the sbp21 operators
+ * whatever the context's order.  Other names give SWM_E_UNSUPPORTED.  FP64
+ * contexts compute the tendency in FP64; FP32 contexts compute it in FP32
+ * from the high part of the state and add it to the (hi, lo) pair in
+ * FP64. */
 int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
                       const char* hordiff_h_name, double h_diff_coeff);
 /* vout = D(vin): operator_swm_diff_t%apply (operator_swm_diff_mod.f90:
@@ -261,6 +267,15 @@ int swm_op_curl(swm_ctx* ctx, swm_field* curl, const swm_field* u,
 int swm_op_coriolis(swm_ctx* ctx, swm_field* cor_u, swm_field* cor_v,
                     const swm_field* hu, const swm_field* hv,
                     const swm_field* h, const swm_field* curl);
+/* C grid only: grad_perp_c_sbp21 / _sbp42 (grad_perp/grad_perp_c_sbp_mod.f90
+ * :20-95) of a corner-mesh field w onto the u and v meshes, and the
+ * transform2co of co2contra_c_sbp21_new / _sbp42_new (co2contra/
+ * co2contra_Cgrid_mod.f90:135-203): covariant (u, v) from contravariant
+ * (ut, vt), at the context's SBP order.  SWM_E_UNSUPPORTED on the Ah grid. */
+int swm_op_grad_perp(swm_ctx* ctx, swm_field* gu, swm_field* gv,
+                     const swm_field* w);
+int swm_op_contra2co(swm_ctx* ctx, swm_field* u, swm_field* v,
+                     const swm_field* ut, const swm_field* vt);
 /* halo_t%get_halo_scalar for "Ah_scalar_sync"
  * (halo/halo_Ah_scalar_sync_mod.f90:20-93) */
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f);

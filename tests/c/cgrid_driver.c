@@ -15,11 +15,15 @@
  *     (swm_rk4_step) on a copy;
  *  3. computes the curl of the input velocity on a corner-mesh field and the
  *     SBP_C mass of the input h;
- *  4. checks two refusals: a mixed-order operator set, and the diagnostics
- *     (an Ah-grid entry point).
+ *  4. checks three refusals: a mixed-order operator set, the diagnostics
+ *     (an Ah-grid entry point) and an Ah-grid hyperdiffusion name;
+ *  5. configures the namelist's hyperdiffusion (hordiff_c_biharm_curl_div
+ *     and hordiff_scalar_C, coefficients 0.03) and runs NSTEPS of the
+ *     drivers' step (RK4, then the explicit Euler diffusion step) on the
+ *     input state.
  * OUT receives the generic state, the fused state, the curl field
- * (6 (N+1)^2) and the mass.  Exit status 0 on success, 2 on an ABI error,
- * 3 on a wrong shape or a refusal that did not happen.
+ * (6 (N+1)^2), the mass and the state of step 5.  Exit status 0 on success,
+ * 2 on an ABI error, 3 on a wrong shape or a refusal that did not happen.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -82,7 +86,7 @@ int main(int argc, char** argv) {
   const size_t np = (size_t)6 * N * N, nu = (size_t)6 * (N + 1) * N, nq = (size_t)6 * (N + 1) * (N + 1);
   const size_t ns = np + 2 * nu;
   double* in = malloc(ns * sizeof(double));
-  double* out = malloc((2 * ns + nq + 1) * sizeof(double));
+  double* out = malloc((3 * ns + nq + 1) * sizeof(double));
   FILE* f = fopen(argv[6], "rb");
   if (!f || fread(in, sizeof(double), ns, f) != ns) {
     fprintf(stderr, "cgrid_driver: cannot read %s\n", argv[6]);
@@ -135,13 +139,26 @@ int main(int argc, char** argv) {
       return 3;
     }
   }
+  /* 4c, 5. the hyperdiffusion of &shallow_water_model_c */
+  if (swm_diffusion_set(g_ctx, "hordiff_vec_xyz_Ah_sbp_42_narrow", 0.03, "hordiff_scalar_C", 0.03) !=
+      SWM_E_UNSUPPORTED) {
+    fprintf(stderr, "cgrid_driver: an Ah-grid hyperdiffusion name was accepted\n");
+    return 3;
+  }
+  check(swm_diffusion_set(g_ctx, "hordiff_c_biharm_curl_div", 0.03, "hordiff_scalar_C", 0.03),
+        "swm_diffusion_set");
+  check(swm_state_upload(g_ctx, y, h, u, v), "swm_state_upload");
+  check(swm_model_step(g_ctx, y, dt, nsteps), "swm_model_step");
+  double* md = out + 2 * ns + nq + 1;
+  check(swm_state_download(g_ctx, y, md, md + np, md + np + nu), "download");
+
   swm_field_free(fu); swm_field_free(fv); swm_field_free(fc); swm_field_free(fh);
   swm_state_free(v0); swm_state_free(vf);
   for (int k = 1; k < 6; ++k) swm_state_free(*sim[k]);
   swm_ctx_destroy(g_ctx);
 
   f = fopen(argv[7], "wb");
-  if (!f || fwrite(out, sizeof(double), 2 * ns + nq + 1, f) != 2 * ns + nq + 1) {
+  if (!f || fwrite(out, sizeof(double), 3 * ns + nq + 1, f) != 3 * ns + nq + 1) {
     fprintf(stderr, "cgrid_driver: cannot write %s\n", argv[7]);
     return 1;
   }

@@ -93,9 +93,10 @@ def test_c_driver_matches_oracle(tmp_path, order, prec):
 @pytest.mark.parametrize("order,prec", [(42, 0), (21, 0), (42, 1)], ids=["c42-fp64", "c21-fp64", "c42-fp32"])
 def test_cgrid_c_driver_matches_oracle(tmp_path, order, prec):
     """The C-grid family from plain C: RK4 through the abstract interfaces
-    and fused, the curl on a corner-mesh field and the SBP_C mass, against
-    the C-grid oracle; the refusals of a mixed-order set and of an Ah-grid
-    entry point."""
+    and fused, the curl on a corner-mesh field, the SBP_C mass and the
+    drivers' step with the namelist's hyperdiffusion, against the C-grid
+    oracle; the refusals of a mixed-order set, of an Ah-grid entry point and
+    of an Ah-grid hyperdiffusion name."""
     N, nsteps = 32, 3
     dt = 600.0 * 24 / N
     h, u, v, _ = initial.balanced_zonal_c(N, 4, 12)
@@ -132,3 +133,7 @@ def test_cgrid_c_driver_matches_oracle(tmp_path, order, prec):
         assert rel(g, rr) < tol and rel(f, rr) < tol
     assert rel(curl, od.curl(u, v)) < 1e-12
     assert abs(mass - od.mass(h)) <= 1e-13 * abs(od.mass(h))
+    stepped = state(2 * ns + nq + 1)
+    ref = od.model_step(h, u, v, dt, nsteps, uv_name="hordiff_c_biharm_curl_div", uv_coeff=0.03, h_coeff=0.03)
+    for g, rr in zip(stepped, ref):
+        assert rel(g, rr) < tol

@@ -4,8 +4,9 @@ known answers.
 
 Pins:
 * every C-grid line of reference_results.txt (div, grad, curl, Coriolis, KE,
-  co2contra at sbp21 and sbp42): the GPU operators on the reference test's
-  fields at N=32, nz=3 reproduce the printed values to their 7 digits;
+  co2contra at sbp21 and sbp42, and the co2contra / contra2co pair of
+  co2contra_c_sbp*_new): the GPU operators on the reference test's fields at
+  N=32, nz=3 reproduce the printed values to their 7 digits;
 * each single operator, the fused and the unfused apply and the RK4 step
   against the oracle on a seeded balanced flow (FP64: 1e-12 on states and
   single operators; 1e-10 on tendencies, which carry the cancellation of
@@ -129,6 +130,18 @@ def gpu_golden(kind, order):
             ut, vt = field(op, "u"), field(op, "v")
             op.co2contra(ut, vt, field(op, "u", u), field(op, "v", v))
             ex, ey = ut.download() - tu, vt.download() - tv
+            mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
+            lx, ly = lx + l2sq(od, "u", ex), ly + l2sq(od, "v", ey)
+        out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
+    elif kind == "contra2co":
+        # test_contra2co: transform2co of co2contra_c_sbp*_new
+        mx = my = lx = ly = 0.0
+        for lev in range(3):
+            ut, vt = od.vector_test_field("cross_polar", lev, contravariant=True)
+            tu, tv = od.vector_test_field("cross_polar", lev, contravariant=False)
+            u, v = field(op, "u"), field(op, "v")
+            op.contra2co(u, v, field(op, "u", ut), field(op, "v", vt))
+            ex, ey = u.download() - tu, v.download() - tv
             mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
             lx, ly = lx + l2sq(od, "u", ex), ly + l2sq(od, "v", ey)
         out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
