@@ -811,6 +811,15 @@ def diffusion_leg(w, h, u, v, local, steps, warmup):
 #   words in stages 1..4): 4 x 46 + 3 x 11 = 217 words per point and step.
 CGRID_WORDS_PER_POINT_STEP = 217
 CGRID_LAUNCHES_PER_STEP = 32          # 4 x (6 passes + 2 corner-sync kernels)
+# The namelist's C-grid model step adds one explicit Euler step of the
+# hyperdiffusion (hordiff_c_biharm_curl_div, hordiff_scalar_C; 2/1
+# operators).  Words per point of its passes, inputs + outputs + metric:
+# co2contra / contra2co 15 (centre_a 5 + faces_a 10), div 6, grad 3, curl 4,
+# grad_perp 5; curl part 2 x (4 + 5 + 15), div part 2 x (15 + 6 + 3), h part
+# 2 x (3 + 15 + 6), the combine pass 11 (5 results, state read and written):
+# 48 + 48 + 48 + 11 = 155 words per point.
+CGRID_DIFF_WORDS_PER_POINT_STEP = 155
+CGRID_DIFF_LAUNCHES_PER_STEP = 29     # 24 passes, 2 corner syncs of 2 kernels, combine
 
 
 def cgrid_leg(local, steps, warmup, cpu=True):
@@ -832,15 +841,26 @@ def cgrid_leg(local, steps, warmup, cpu=True):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     ts = swm.RK4()
 
-    def timed(prec):
+    def timed(prec, model=False):
+        """Device-timed steps: RK4 (model False) or the drivers' model step
+        with the namelist's hyperdiffusion (model True)."""
         op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=ORDER, names=swm.c_grid_names(ORDER),
                                              precision=prec, device=local))
+        if model:
+            swm.OperatorSWMDiff(op)  # hordiff_c_biharm_curl_div 0.03, hordiff_scalar_C 0.03
+
+        def step(st, n):
+            if model:
+                op.model_step(st, DT, n)
+            else:
+                ts.step(st, op, DT, n)
+
         s0, s = op.create_stvec(), op.create_stvec()
         s0.upload(h, u, v)
         s.assign_s1v1(1.0, s0)
         stream = torch.cuda.ExternalStream(op.stream, device=dev)
         for _ in range(warmup):
-            ts.step(s, op, DT, 1)
+            step(s, 1)
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         torch.cuda.synchronize(dev)
         for a, b in evs:
@@ -848,7 +868,7 @@ def cgrid_leg(local, steps, warmup, cpu=True):
             with torch.cuda.stream(stream):
                 flush.zero_()
             a.record(stream)
-            ts.step(s, op, DT, 1)
+            step(s, 1)
             b.record(stream)
         torch.cuda.synchronize(dev)
         return op, s, sum(a.elapsed_time(b) for a, b in evs) / steps
@@ -889,6 +909,15 @@ def cgrid_leg(local, steps, warmup, cpu=True):
         serial(n_e2e)
         return pv, n_e2e / (time.perf_counter() - t0)
 
+    # the namelist's model step (RK4 + explicit Euler hyperdiffusion), both
+    # forms, and one step of each for parity
+    model = {}
+    for prec in ("fp32", "fp64"):
+        opm, sm, msm = timed(prec, model=True)
+        sm.upload(h, u, v)
+        opm.model_step(sm, DT, 1)
+        model[prec] = (msm, sm.download())
+        del opm, sm
     op32, s32, ms32 = timed("fp32")
     e2e32, e2e32_serial = e2e_rates(op32, s32)
     s32.upload(h, u, v)
@@ -930,12 +959,38 @@ def cgrid_leg(local, steps, warmup, cpu=True):
     res["fp32_form"]["roofline"] = {"bound": "hbm", "achieved": round(a32, 1), "peak": peak, "unit": "GB/s",
                                     "frac": round(a32 / peak, 4), "peak_source": peak_kind,
                                     "algorithmic_bytes_per_step": CGRID_WORDS_PER_POINT_STEP * 4 * npts}
+    mwords = CGRID_WORDS_PER_POINT_STEP + CGRID_DIFF_WORDS_PER_POINT_STEP
+    mres = {"config": "the namelist's C-grid step (namelist_swm:80-102): RK4, then one explicit Euler step of "
+                      "hordiff_c_biharm_curl_div (0.03) and hordiff_scalar_C (0.03)",
+            "launches_per_step": CGRID_LAUNCHES_PER_STEP + CGRID_DIFF_LAUNCHES_PER_STEP}
+    for prec, elt, key in (("fp64", 8, None), ("fp32", 4, "fp32_form")):
+        msm = model[prec][0]
+        am = mwords * elt * npts / (msm / 1e3) / 1e9
+        r = {"value": round(1e3 / msm, 3), "unit": "steps/s", "ms_per_step": round(msm, 5),
+             "diffusion_ms_per_step": round(msm - (ms if prec == "fp64" else ms32), 5),
+             "roofline": {"bound": "hbm", "achieved": round(am, 1), "peak": peak, "unit": "GB/s",
+                          "frac": round(am / peak, 4), "peak_source": peak_kind,
+                          "algorithmic_bytes_per_step": mwords * elt * npts}}
+        if key:
+            mres[key] = r
+        else:
+            mres.update(r)
+    res["model_step"] = mres
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle  # the checker and the timed CPU baseline
         od = oracle.OracleCDomain(N, ORDER)
         threads = os.cpu_count() or 1
         oracle.set_threads(threads)
+        t0 = time.perf_counter()
+        mwant = od.model_step(h, u, v, DT, 1)
+        mel = time.perf_counter() - t0
+        for prec, key in (("fp64", "parity_vs_oracle_1_step_max_rel_l2"),
+                          ("fp32", "fp32_error_vs_oracle_1_step_max_rel_l2")):
+            mres[key] = max(float(np.linalg.norm(a - b) / np.linalg.norm(b))
+                            for a, b in zip(model[prec][1], mwant))
+        mres["cpu_oracle"] = {"value": round(1 / mel, 4), "unit": "steps/s", "cores": threads, "kind": "port",
+                              "sample": "1 model step of the same state at N=384 (C-grid oracle)"}
         t0 = time.perf_counter()
         want = od.rk4(h, u, v, DT, 2)
         el = time.perf_counter() - t0

@@ -858,7 +858,9 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
   // The C-grid family of &shallow_water_model_c (namelist_swm:80-102), all
   // operators of one SBP order: divergence_c_sbpNN, gradient_c_sbpNN,
   // curl_c_sbpNN, coriolis_Cgrid_sbpNN, KE_Cgrid_sbpNN, co2contra_c_sbpNN,
-  // massflux_c_sbpNN, SBP_CNN_quadrature with NN 21 or 42.
+  // massflux_c_sbpNN, SBP_CNN_quadrature with NN 21 or 42.  co2contra_c_sbpNN_new
+  // (co2contra_Cgrid_mod.f90:66-134: the same interpolate, J Qi12, interpolate
+  // back, divide by J chain through the 2-D interpolators) is the same map.
   int cgrid_order = 0;
   if (div_op_name && std::strncmp(div_op_name, "divergence_c_sbp", 16) == 0) {
     if (!name_order(div_op_name, "divergence_c_sbp", "", od) || (od != 21 && od != 42))
@@ -869,7 +871,7 @@ int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name, const c
     const std::string need[7] = {"gradient_c_sbp" + o, "curl_c_sbp" + o, "coriolis_Cgrid_sbp" + o, "KE_Cgrid_sbp" + o,
                                  "co2contra_c_sbp" + o, "massflux_c_sbp" + o, "SBP_C" + o + "_quadrature"};
     for (int k = 0; k < 7; ++k)
-      if (!want[k] || need[k] != want[k])
+      if (!want[k] || (need[k] != want[k] && !(k == 4 && need[k] + "_new" == want[k])))
         return fail(nullptr, SWM_E_UNSUPPORTED,
                     std::string("C-grid family needs ") + need[k] + ", got " + (want[k] ? want[k] : "(null)"));
     cgrid_order = od;
@@ -1686,7 +1688,10 @@ int enqueue_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt) {
 
 int diffusion_ready(swm_ctx* ctx) {
   if (!ctx->diff_uv) return fail(ctx, SWM_E_INVALID, "diffusion is not configured (swm_diffusion_set)");
-  if (ctx->cg) return SWM_OK;  // the C grid's work fields exist from creation
+  if (ctx->cg) {
+    CK(cgrid_diffusion_prepare(ctx->cg), "C-grid diffusion workspace");
+    return SWM_OK;
+  }
   if (int rc = diffusion_ws(ctx, ctx->diff_uv)) return rc;
   return diffusion_ws(ctx, ctx->diff_h);
 }

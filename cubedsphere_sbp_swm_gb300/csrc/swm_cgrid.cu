@@ -703,7 +703,11 @@ struct CGrid {
   float* met32 = nullptr;  // their FP32 copies (contexts of the FP32 form)
   double* wk = nullptr;    // W_COUNT fields
   double* rk = nullptr;    // Y, Kb, acc: 3 fields each
-  double* dk = nullptr;    // hyperdiffusion results: L(L(h)), curl part (u, v)
+  // hyperdiffusion (allocated on first use): kDiffFields work fields, the two
+  // side streams of its branches and the fork / join events
+  double* dw = nullptr;
+  cudaStream_t bs[2] = {nullptr, nullptr};
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   int* halo = nullptr;
   double* wts = nullptr;   // quadrature weights: centres (N), interfaces (N+1)
   double* part = nullptr;  // kMassBlocks partial sums
@@ -898,71 +902,101 @@ cudaError_t transform(const CGrid* c, CArgsT<T> a, const T* x, const T* y, T* xo
   return run_faces_a(c, a, st);
 }
 
+// Work fields of the hyperdiffusion: the results L(L(h)), the curl part
+// (u, v) and the divergence part (u, v), then per branch (curl, divergence,
+// h) the centre scratch of the transforms (2), two face pairs (4) and one
+// centre or corner field.
+constexpr int kDiffResults = 5, kDiffBranch = 7, kDiffFields = kDiffResults + 3 * kDiffBranch;
+
 // The C-grid hyperdiffusion of operator_swm_diff_t (operator_swm_diff_mod.f90
 // :25-46) with the 2/1 operators the factory uses at any order
 // (hordiff_factory_mod.f90:53-139, 196-247), on the state in (h, u, v):
 //   curl part  contra2co grad_perp curl contra2co grad_perp curl (u, v)
 //   div part   grad div co2contra grad div co2contra (u, v)
 //   h          L(L(h)), L = div co2contra grad
-// then the combine pass (mode 0 tendency into out, 1 / 2 Euler step on out
-// = the state, 2 with the FP32 low part lo).
+// The three chains are independent: they run as three branches (the
+// context stream and two side streams, forked and joined with events, so a
+// captured step becomes a three-branch graph), each on its own work fields.
+// Then the combine pass on the context stream (mode 0 tendency into out, 1 /
+// 2 Euler step on out = the state, 2 with the FP32 low part lo).
 template <class T>
 cudaError_t diffusion(const CGrid* c, const Topology& tp, T* edge, int parts, double c4uv, double c4h, const T* in,
                       T* out, float* lo, double dt, int mode, cudaStream_t st) {
+  if (!c->dw) return cudaErrorInvalidValue;  // cgrid_diffusion_prepare first
   const long long fs = c->g.fs;
-  const CArgsT<T> a = base_args<T>(c, 21);
-  auto Wk = [&](int k) { return reinterpret_cast<T*>(c->work(k)); };
-  T *P1 = Wk(W_KE), *U1 = Wk(W_UT), *V1 = Wk(W_VT), *U2 = Wk(W_HU), *V2 = Wk(W_HV);
-  T *U3 = Wk(W_GU), *V3 = Wk(W_GV), *Q1 = Wk(W_CURL);
-  T* D = reinterpret_cast<T*>(c->dk);
-  T *TH = D, *TU = D + fs, *TV = D + 2 * fs;
+  auto F = [&](int k) { return reinterpret_cast<T*>(c->dw + (long long)k * fs); };
+  T *TH = F(0), *TU = F(1), *TV = F(2), *U3 = F(3), *V3 = F(4);
   const T *h = in, *u = in + fs, *v = in + 2 * fs;
-  auto div = [&](const T* x, const T* y, T* o) {
-    CArgsT<T> b = a;
+  struct Branch {
+    CArgsT<T> a;  // with this branch's transform scratch
+    T *X1, *Y1, *X2, *Y2, *S;
+    cudaStream_t st;
+  };
+  const cudaStream_t side[2] = {c->bs[0], c->bs[1]};
+  auto branch = [&](int b) {
+    const int o = kDiffResults + kDiffBranch * b;
+    Branch r{base_args<T>(c, 21), F(o + 2), F(o + 3), F(o + 4), F(o + 5), F(o + 6), b ? side[b - 1] : st};
+    r.a.Ap = F(o);
+    r.a.Bp = F(o + 1);
+    return r;
+  };
+  auto div = [&](const Branch& B, const T* x, const T* y, T* o) {
+    CArgsT<T> b = B.a;
     b.hu_in = x; b.hv_in = y; b.o1 = o;
     b.flags = F_DIV | F_SEP;
-    return run_centre_b(c, b, st);
+    return run_centre_b(c, b, B.st);
   };
-  auto grad = [&](const T* f, T* gx, T* gy) {
-    CArgsT<T> b = a;
+  auto grad = [&](const Branch& B, const T* f, T* gx, T* gy) {
+    CArgsT<T> b = B.a;
     b.ke_in = f; b.o1 = gx; b.o2 = gy;
     b.flags = F_GRAD | F_SEP;
-    return run_faces_b(c, b, st);
+    return run_faces_b(c, b, B.st);
   };
-  auto curl = [&](const T* x, const T* y, T* q) {
-    CArgsT<T> b = a;
+  auto curl = [&](const Branch& B, const T* x, const T* y, T* q) {
+    CArgsT<T> b = B.a;
     b.u = x; b.v = y; b.curl = q;
-    CKE(run_curl(c, b, st));
-    return launch_sync_scalar_t<T>(c->g, tp, q, edge, st);
+    CKE(run_curl(c, b, B.st));
+    return launch_sync_scalar_t<T>(c->g, tp, q, edge, B.st);
   };
-  auto gperp = [&](const T* q, T* gu, T* gv) {
-    CArgsT<T> b = a;
+  auto gperp = [&](const Branch& B, const T* q, T* gu, T* gv) {
+    CArgsT<T> b = B.a;
     b.curl_in = q; b.o1 = gu; b.o2 = gv;
-    return run_gperp(c, b, st);
+    return run_gperp(c, b, B.st);
   };
+  auto xf = [&](const Branch& B, const T* x, const T* y, T* xo, T* yo, bool to_co) {
+    return transform(c, B.a, x, y, xo, yo, to_co, B.st);
+  };
+  const Branch bc = branch(0), bd = branch(1), bh = branch(2);
+  CKE(cudaEventRecord(c->ev[0], st));
+  CKE(cudaStreamWaitEvent(bd.st, c->ev[0], 0));
+  CKE(cudaStreamWaitEvent(bh.st, c->ev[0], 0));
   if (parts & 2) {
-    CKE(curl(u, v, Q1));
-    CKE(gperp(Q1, U1, V1));
-    CKE(transform(c, a, (const T*)U1, (const T*)V1, U2, V2, true, st));
-    CKE(curl(U2, V2, Q1));
-    CKE(gperp(Q1, U1, V1));
-    CKE(transform(c, a, (const T*)U1, (const T*)V1, TU, TV, true, st));
+    CKE(curl(bc, u, v, bc.S));
+    CKE(gperp(bc, bc.S, bc.X1, bc.Y1));
+    CKE(xf(bc, bc.X1, bc.Y1, bc.X2, bc.Y2, true));
+    CKE(curl(bc, bc.X2, bc.Y2, bc.S));
+    CKE(gperp(bc, bc.S, bc.X1, bc.Y1));
+    CKE(xf(bc, bc.X1, bc.Y1, TU, TV, true));
   }
   if (parts & 1) {
-    CKE(transform(c, a, u, v, U1, V1, false, st));
-    CKE(div(U1, V1, P1));
-    CKE(grad(P1, U2, V2));
-    CKE(transform(c, a, (const T*)U2, (const T*)V2, U1, V1, false, st));
-    CKE(div(U1, V1, P1));
-    CKE(grad(P1, U3, V3));
+    CKE(xf(bd, u, v, bd.X1, bd.Y1, false));
+    CKE(div(bd, bd.X1, bd.Y1, bd.S));
+    CKE(grad(bd, bd.S, bd.X2, bd.Y2));
+    CKE(xf(bd, bd.X2, bd.Y2, bd.X1, bd.Y1, false));
+    CKE(div(bd, bd.X1, bd.Y1, bd.S));
+    CKE(grad(bd, bd.S, U3, V3));
   }
   const T* f = h;
   for (int rep = 0; rep < 2; ++rep) {
-    CKE(grad(f, U1, V1));
-    CKE(transform(c, a, (const T*)U1, (const T*)V1, U2, V2, false, st));
-    CKE(div(U2, V2, rep ? TH : P1));
-    f = P1;
+    CKE(grad(bh, f, bh.X1, bh.Y1));
+    CKE(xf(bh, bh.X1, bh.Y1, bh.X2, bh.Y2, false));
+    CKE(div(bh, bh.X2, bh.Y2, rep ? TH : bh.S));
+    f = bh.S;
   }
+  CKE(cudaEventRecord(c->ev[1], bd.st));
+  CKE(cudaEventRecord(c->ev[2], bh.st));
+  CKE(cudaStreamWaitEvent(st, c->ev[1], 0));
+  CKE(cudaStreamWaitEvent(st, c->ev[2], 0));
   diff_combine_kernel<T><<<grid_for(c->N + 1, c->N + 1), kBlock, 0, st>>>(
       c->g, c->N, parts, T(c4uv), T(c4h), TH, TU, TV, U3, V3, mode, dt, out, lo);
   return cudaGetLastError();
@@ -1008,7 +1042,6 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   ok(cudaMalloc(&c->met, M_COUNT * fb));
   ok(cudaMalloc(&c->wk, W_COUNT * fb));
   ok(cudaMalloc(&c->rk, 9 * fb));
-  ok(cudaMalloc(&c->dk, 3 * fb));
   ok(cudaMalloc(&c->halo, sizeof(int) * tab.size()));
   ok(cudaMalloc(&c->wts, sizeof(double) * w.size()));
   ok(cudaMalloc(&c->part, sizeof(double) * kMassBlocks));
@@ -1050,7 +1083,6 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     }
     ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
     ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
-    ok(cudaMemsetAsync(c->dk, 0, 3 * fb, st));
     ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
     if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
       ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
@@ -1068,9 +1100,13 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
 
 void cgrid_destroy(CGrid* c) {
   if (!c) return;
-  for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->dk, (void*)c->halo,
+  for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->dw, (void*)c->halo,
                   (void*)c->wts, (void*)c->part})
     if (p) cudaFree(p);
+  for (cudaStream_t s : c->bs)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : c->ev)
+    if (e) cudaEventDestroy(e);
   delete c;
 }
 
@@ -1233,6 +1269,25 @@ cudaError_t cgrid_grad_perp(CGrid* c, const double* w, double* gu, double* gv, c
 
 cudaError_t cgrid_contra2co(CGrid* c, const double* ut, const double* vt, double* u, double* v, cudaStream_t st) {
   return transform(c, base_args<double>(c), ut, vt, u, v, true, st);
+}
+
+cudaError_t cgrid_diffusion_prepare(CGrid* c) {
+  if (c->dw) return cudaSuccess;
+  cudaError_t e = cudaMalloc(&c->dw, sizeof(double) * kDiffFields * c->g.fs);
+  if (e == cudaSuccess) e = cudaMemset(c->dw, 0, sizeof(double) * kDiffFields * c->g.fs);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();  // the context stream does not wait on the legacy one
+  for (cudaStream_t& s : c->bs)
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  for (cudaEvent_t& ev : c->ev)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    // leave nothing half made: the next call retries from scratch
+    if (c->dw) cudaFree(c->dw);
+    c->dw = nullptr;
+    for (cudaStream_t& s : c->bs) { if (s) cudaStreamDestroy(s); s = nullptr; }
+    for (cudaEvent_t& ev : c->ev) { if (ev) cudaEventDestroy(ev); ev = nullptr; }
+  }
+  return e;
 }
 
 cudaError_t cgrid_diffusion(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,

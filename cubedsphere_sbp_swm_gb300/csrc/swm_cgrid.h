@@ -80,7 +80,13 @@ cudaError_t cgrid_contra2co(CGrid* c, const double* ut, const double* vt, double
 // hordiff_scalar_C for h, with the 2/1 operators at any order.  c4uv, c4h:
 // -(c^4) of the two coefficients.  cgrid_diffusion*: the tendency of the
 // state in into out (distinct); cgrid_diffusion_step*: one explicit Euler
-// step in place (FP32: on the (hi, lo) pair, added in FP64).
+// step in place (FP32: on the (hi, lo) pair, added in FP64).  The three
+// parts run as three branches (the stream st and two side streams of the
+// context, forked and joined with events).  cgrid_diffusion_prepare
+// allocates their work fields, streams and events; call it once, outside
+// any stream capture, before the others (they return cudaErrorInvalidValue
+// until then).
+cudaError_t cgrid_diffusion_prepare(CGrid* c);
 cudaError_t cgrid_diffusion(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,
                             const double* in, double* out, cudaStream_t st);
 cudaError_t cgrid_diffusion_step(CGrid* c, const Topology& tp, double* edge, int parts, double c4uv, double c4h,

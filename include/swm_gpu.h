@@ -87,13 +87,16 @@ int swm_ctx_create(const swm_config* cfg, swm_ctx** out);
  *   C grid (staggering "C", the &shallow_water_model_c namelist,
  *     namelist_swm:80-102): divergence_c_sbpNN, gradient_c_sbpNN,
  *     curl_c_sbpNN, coriolis_Cgrid_sbpNN, KE_Cgrid_sbpNN,
- *     co2contra_c_sbpNN, massflux_c_sbpNN, SBP_CNN_quadrature with NN 21 or
- *     42, one order throughout; FP64 only.  h lives on the cell centres, u
- *     on the x-faces, v on the y-faces (domain_factory_mod.f90:108-112).
+ *     co2contra_c_sbpNN (or co2contra_c_sbpNN_new, the same map),
+ *     massflux_c_sbpNN, SBP_CNN_quadrature with NN 21 or 42, one order
+ *     throughout; FP64 or the FP32 form (FP32 passes on an FP32 (hi, lo)
+ *     state pair).  h lives on the cell centres, u on the x-faces, v on the
+ *     y-faces (domain_factory_mod.f90:108-112).
  * Other names, or operators of different SBP orders, return
- * SWM_E_UNSUPPORTED.  A C-grid context provides the state algebra, apply,
- * the RK4 step, orography, fields and the single operators below; the other
- * entry points return SWM_E_UNSUPPORTED on it. */
+ * SWM_E_UNSUPPORTED.  A C-grid context provides the state algebra and
+ * transfers, apply, the RK4 step, the hyperdiffusion and the model step,
+ * orography, fields and the single operators below; the other entry points
+ * return SWM_E_UNSUPPORTED on it. */
 int swm_ctx_create_named(const swm_config* cfg, const char* div_op_name,
                          const char* grad_op_name, const char* curl_op_name,
                          const char* coriolis_op_name, const char* KE_op_name,

@@ -159,3 +159,22 @@ def test_diffusion_names_are_per_grid():
     with pytest.raises(swm.SwmError) as e:
         cop._check(cop._L.swm_diffusion_step(cop._h, s._h, 1.0, 1))
     assert e.value.code == swm._abi.SWM_E_INVALID
+
+
+def test_co2contra_new_name_is_the_same_operator():
+    """A namelist may name co2contra_c_sbpNN_new as the model's co2contra
+    operator: the same interpolate / J Qi12 / interpolate back / divide by J
+    map, so the context and its RK4 step are identical."""
+    N = 24
+    names = swm.c_grid_names(42)
+    names["co2contra_op_name"] = "co2contra_c_sbp42_new"
+    a = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, names=names))
+    b = c_op(N, 42)
+    h, u, v = _rough_state(N, 2)
+    sa, sb = a.create_stvec(), b.create_stvec()
+    sa.upload(h, u, v)
+    sb.upload(h, u, v)
+    swm.RK4().step(sa, a, 600.0, 2)
+    swm.RK4().step(sb, b, 600.0, 2)
+    for x, y in zip(sa.download(), sb.download()):
+        assert np.array_equal(x, y)
