@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(256) gperp_kernel(const __grid_constant__ CArg
 // 1.0 (c4uv B), A the curl part, B the divergence part (parts 1 B only, 2 A
 // only, 3 both).  mode 0 stores the tendency, 1 the explicit Euler step
 // y + dt t (explicit_Eul1_mod.f90:20-30) in place, 2 the same step on an
-// FP32 (hi, lo) state pair, added in FP64.
+// FP32 (hi, lo) state pair with an exact two-sum.
 template <class T>
 __global__ void __launch_bounds__(256) diff_combine_kernel(FieldGeom g, int N, int parts, T c4uv, T c4h,
                                                            const T* __restrict__ Lh, const T* __restrict__ Au,
@@ -435,10 +435,16 @@ __global__ void __launch_bounds__(256) diff_combine_kernel(FieldGeom g, int N, i
     } else if (mode == 1) {
       out[o] = out[o] + T(dt) * t;
     } else {
-      const double x = ((double)out[o] + (double)lo[o]) + dt * (double)t;
-      const float hi = (float)x;
-      out[o] = T(hi);
-      lo[o] = (float)(x - (double)hi);
+      // the increment joins the low part, then an exact FP32 two-sum
+      // renormalises the pair (FP64 arithmetic here would make this pass
+      // bound by GB300's narrow FP64 pipe)
+      const float d = float(dt) * float(t);
+      const float h = float(out[o]);
+      const float tt = lo[o] + d;
+      const float sm = h + tt;
+      const float bb = sm - h;
+      out[o] = T(sm);
+      lo[o] = (h - (sm - bb)) + (tt - bb);
     }
   };
   auto mix = [&](T A, T B) {

@@ -80,7 +80,7 @@ cudaError_t cgrid_contra2co(CGrid* c, const double* ut, const double* vt, double
 // hordiff_scalar_C for h, with the 2/1 operators at any order.  c4uv, c4h:
 // -(c^4) of the two coefficients.  cgrid_diffusion*: the tendency of the
 // state in into out (distinct); cgrid_diffusion_step*: one explicit Euler
-// step in place (FP32: on the (hi, lo) pair, added in FP64).  The three
+// step in place (FP32: on the (hi, lo) pair, with an exact two-sum).  The three
 // parts run as three branches (the stream st and two side streams of the
 // context, forked and joined with events).  cgrid_diffusion_prepare
 // allocates their work fields, streams and events; call it once, outside

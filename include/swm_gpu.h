@@ -209,8 +209,8 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
  * -(c^4) L(L(h)) with L = div co2contra grad, all with the sbp21 operators
  * whatever the context's order.  Other names give SWM_E_UNSUPPORTED.  FP64
  * contexts compute the tendency in FP64; FP32 contexts compute it in FP32
- * from the high part of the state and add it to the (hi, lo) pair in
- * FP64. */
+ * from the high part of the state and add dt times it to the (hi, lo) pair
+ * with an exact two-sum. */
 int swm_diffusion_set(swm_ctx* ctx, const char* hordiff_uv_name, double uv_diff_coeff,
                       const char* hordiff_h_name, double h_diff_coeff);
 /* vout = D(vin): operator_swm_diff_t%apply (operator_swm_diff_mod.f90:
