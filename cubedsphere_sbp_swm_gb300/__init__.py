@@ -273,6 +273,19 @@ class OperatorSWM:
         """transform2co of co2contra_c_sbp*_new (C grid)."""
         self._check(self._L.swm_op_contra2co(self._h, u._h, v._h, ut._h, vt._h))
 
+    def calc_grad_a2_ecs(self, gx, gy, f):
+        """gradient_a2_ecs on the cell centres (C grid): gx, gy and f on mesh p."""
+        self._check(self._L.swm_op_grad_a2_ecs(self._h, gx._h, gy._h, f._h))
+
+    def ecs_o_halo(self, f, halo_width: int = 2) -> np.ndarray:
+        """The ECS_O halo of a cell-centre field (C grid): the (6, N+2hw,
+        N+2hw) extended tiles, the reference's 1-based (i, j) at
+        [:, j + hw - 1, i + hw - 1]."""
+        W = self.N + 2 * int(halo_width)
+        out = np.empty((6, W, W))
+        self._check(self._L.swm_halo_ecs_o(self._h, f._h, int(halo_width), _ptr(out)))
+        return out
+
     def quadrature_mass(self, f) -> float:
         out = ctypes.c_double()
         self._check(self._L.swm_quadrature_mass(self._h, f._h, ctypes.byref(out)))

@@ -40,7 +40,8 @@ EXPORTS = (
     "swm_apply_unfused", "swm_rk4_step", "swm_diagnostics", "swm_field_create",
     "swm_field_free", "swm_field_upload", "swm_field_download", "swm_op_co2contra",
     "swm_op_massflux", "swm_op_ke", "swm_op_grad", "swm_op_div", "swm_op_curl",
-    "swm_op_coriolis", "swm_op_grad_perp", "swm_op_contra2co", "swm_sync_scalar", "swm_sync_vector_cov", "swm_quadrature_mass",
+    "swm_op_coriolis", "swm_op_grad_perp", "swm_op_contra2co", "swm_op_grad_a2_ecs", "swm_halo_ecs_o",
+    "swm_sync_scalar", "swm_sync_vector_cov", "swm_quadrature_mass",
     "swm_timing_enable", "swm_timing_read", "swm_sync_scalar_static",
     "swm_ensemble_create", "swm_ensemble_destroy", "swm_ensemble_last_error", "swm_ensemble_size",
     "swm_ensemble_member", "swm_ensemble_upload", "swm_ensemble_download",
@@ -169,6 +170,8 @@ def load(build_if_missing: bool = True):
     sig("swm_op_coriolis", I, VP, VP, VP, VP, VP, VP, VP)
     sig("swm_op_grad_perp", I, VP, VP, VP, VP)
     sig("swm_op_contra2co", I, VP, VP, VP, VP, VP)
+    sig("swm_op_grad_a2_ecs", I, VP, VP, VP, VP)
+    sig("swm_halo_ecs_o", I, VP, VP, I, _D)
     sig("swm_sync_scalar", I, VP, VP)
     sig("swm_sync_vector_cov", I, VP, VP, VP)
     sig("swm_quadrature_mass", I, VP, VP, _D)

@@ -2008,6 +2008,24 @@ int swm_op_contra2co(swm_ctx* ctx, swm_field* u, swm_field* v, const swm_field* 
   CK(cgrid_contra2co(ctx->cg, ut->p, vt->p, u->p, v->p, ctx->st), "contra2co");
   return SWM_OK;
 }
+int swm_op_grad_a2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy, const swm_field* f) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "gradient_a2_ecs needs the cell-centre mesh of the C grid");
+  CHECK_FIELDS(gx, gy, f);
+  for (const swm_field* x : {(const swm_field*)gx, (const swm_field*)gy, f})
+    if (int rc = check_mesh(ctx, x, SWM_MESH_P, "gradient_a2_ecs")) return rc;
+  if (gx == f || gy == f || gx == gy) return fail(ctx, SWM_E_INVALID, "gradient_a2_ecs needs distinct fields");
+  CK(cgrid_grad_a2_ecs(ctx->cg, f->p, gx->p, gy->p, ctx->st), "gradient_a2_ecs");
+  return SWM_OK;
+}
+int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "the ECS_O halo needs the cell-centre mesh of the C grid");
+  CHECK_FIELDS(f);
+  if (int rc = check_mesh(ctx, f, SWM_MESH_P, "ECS_O halo")) return rc;
+  if (halo_width < 1 || halo_width > 2) return fail(ctx, SWM_E_INVALID, "ECS_O halo width must be 1 or 2");
+  if (!ext) return fail(ctx, SWM_E_INVALID, "null output");
+  CK(cgrid_ecs_o_halo(ctx->cg, f->p, halo_width, ext, ctx->st), "ECS_O halo");
+  return SWM_OK;
+}
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f) {
   CHECK_FIELDS(f);
   // on the C grid the corner mesh is the one with duplicated edge points

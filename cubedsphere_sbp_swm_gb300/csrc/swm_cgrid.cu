@@ -34,7 +34,7 @@ namespace swm {
 namespace {
 
 constexpr double kPiC = 3.141592653589793238462643383279502884;
-constexpr int kHaloDepth = 3;
+constexpr int kHaloDepth = 5;  // 3 for the SBP operators, 5 for the ECS_O corner formulas
 constexpr int kMassBlocks = 256;
 constexpr int kMassThreads = 256;
 
@@ -180,6 +180,10 @@ struct CArgsT {
   COpsT<T> ops;
   const T *Jp, *fp, *rJp, *rJpha, *JQi2p, *Ju, *Qi1u, *rJu, *Jv, *Qi3v, *rJv, *rJqha, *rJuha, *rJvha;
   const int* halo;
+  // ECS_O halo: cubic weights [row 0..1][position -1..N+2][4], stencil bases, hx a
+  const double* ecs_w;
+  const int* ecs_ind;
+  double hxa;
   // inputs
   const T *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
   // intermediate and unfused outputs
@@ -457,6 +461,123 @@ __global__ void __launch_bounds__(256) diff_combine_kernel(FieldGeom g, int N, i
   if (i < N) put(2, mix(Av[e], Bv[e]));
 }
 
+// ------------------------------------------------------------------ ECS_O
+// The ECS_O scalar halo of a cell-centre field (equiang_cs/ecs_halo_mod.f90:
+// 95-475), evaluated where it is read instead of stored: (i1, j1) are the
+// reference's 1-based tile indices, a halo point lies within two rows of the
+// panel.  ecs_x is the neighbour's value the 'full' o-point exchange places
+// there (exactly one of i1, j1 outside [1, N]).
+__device__ __forceinline__ double ecs_x(const CArgsT<double>& a, const double* f, int p, int i1, int j1) {
+  const int N = a.N;
+  if (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) return f[at(a.g, p, i1 - 1, j1 - 1)];
+  int side, d, k;
+  if (i1 < 1) { side = 0; d = 1 - i1; k = j1 - 1; }
+  else if (i1 > N) { side = 1; d = i1 - N; k = j1 - 1; }
+  else if (j1 < 1) { side = 2; d = 1 - j1; k = i1 - 1; }
+  else { side = 3; d = j1 - N; k = i1 - 1; }
+  const int c = __ldg(&a.halo[(((0 * 4 + side) * 6 + p) * kHaloDepth + (d - 1)) * a.L + k]);
+  return f[c >> 2];
+}
+
+__device__ __forceinline__ double ecs_wt(const CArgsT<double>& a, int m, int i, int r) {
+  return __ldg(&a.ecs_w[((r - 1) * (a.N + 4) + (i + 1)) * 4 + (m + 1)]);
+}
+
+// The six corner values of corner c (1 at (0,0), 2 at (N+1,0), 3 at
+// (N+1,N+1), 4 at (0,N+1)) from ecs_halo_1corner (ecs_halo_mod.f90:179-260):
+// k = 0..5 at the corner-relative points (0,1), (1,0), (0,0), (-1,0), (0,-1),
+// (-1,-1), the last three for width 2 only.
+__device__ double ecs_corner(const CArgsT<double>& a, const double* f, int p, int c, int k) {
+  const int N = a.N;
+  const int ist = (c == 1 || c == 2) ? N + 1 : 0, jst = c >= 2 ? N + 1 : 0;
+  const int idr = (c == 1 || c == 2) ? -1 : 1, jdr = c >= 2 ? -1 : 1;
+  auto fc = [&](int i, int j) { return ecs_x(a, f, p, ist + idr * i, jst + jdr * j); };
+  // the weights of corner 1, mirrored for the corners at i = N+1
+  auto pw = [&](int m, int i, int r) { return idr == 1 ? ecs_wt(a, m, i, r) : ecs_wt(a, 1 - m, N + 1 - i, r); };
+  const double zw = pw(-1, 1, 1), zw2 = zw * zw, zw3 = zw2 * zw;
+  const double z0 = pw(0, 1, 1), z1 = pw(1, 1, 1), z2 = pw(2, 1, 1);
+  double zx = z0 * fc(0, 1) + z1 * fc(0, 2) + z2 * fc(0, 3);
+  double zy = z0 * fc(1, 0) + z1 * fc(1, -1) + z2 * fc(1, -2);
+  double zz = z0 * fc(1, 1) + z1 * fc(2, 1) + z2 * fc(3, 1);
+  if (k == 0) return (zx + zw * zy + zw2 * zz) / (1.0 - zw3);
+  const double zfy1 = (zy + zw * zz + zw2 * zx) / (1.0 - zw3);
+  zx = z0 * fc(1, 0) + z1 * fc(2, 0) + z2 * fc(3, 0);
+  zy = z0 * fc(0, 1) + z1 * fc(-1, 1) + z2 * fc(-2, 1);
+  zz = z0 * fc(1, 1) + z1 * fc(1, 2) + z2 * fc(1, 3);
+  if (k == 1) return (zx + zw * zy + zw2 * zz) / (1.0 - zw3);
+  const double zfy2 = (zy + zw * zz + zw2 * zx) / (1.0 - zw3);
+  if (k == 2) {
+    const double zff1 = pw(-1, 1, 2) * fc(2, 0) + pw(0, 1, 2) * fc(2, -1) + pw(1, 1, 2) * fc(2, -2) + pw(2, 1, 2) * fc(2, -3);
+    const double zff2 = pw(-1, 1, 2) * fc(0, 2) + pw(0, 1, 2) * fc(-1, 2) + pw(1, 1, 2) * fc(-2, 2) + pw(2, 1, 2) * fc(-3, 2);
+    return 0.5 * (pw(-1, 0, 1) * zff1 + pw(0, 0, 1) * zfy1 + pw(1, 0, 1) * fc(0, 1) + pw(2, 0, 1) * fc(0, 2) +
+                  pw(-1, 0, 1) * zff2 + pw(0, 0, 1) * zfy2 + pw(1, 0, 1) * fc(1, 0) + pw(2, 0, 1) * fc(2, 0));
+  }
+  const double zff1 = pw(-1, 2, 1) * fc(1, 0) + pw(0, 2, 1) * fc(1, -1) + pw(1, 2, 1) * fc(1, -2) + pw(2, 2, 1) * fc(1, -3);
+  const double zff2 = pw(-1, 2, 1) * fc(0, 1) + pw(0, 2, 1) * fc(-1, 1) + pw(1, 2, 1) * fc(-2, 1) + pw(2, 2, 1) * fc(-3, 1);
+  if (k == 3) return pw(-1, 0, 2) * zff1 + pw(0, 0, 2) * fc(-1, 1) + pw(1, 0, 2) * fc(-1, 2) + pw(2, 0, 2) * fc(-1, 3);
+  if (k == 4) return pw(-1, 0, 2) * zff2 + pw(0, 0, 2) * fc(1, -1) + pw(1, 0, 2) * fc(2, -1) + pw(2, 0, 2) * fc(3, -1);
+  const double zff11 = pw(-1, 2, 2) * fc(2, -1) + pw(0, 2, 2) * fc(2, -2) + pw(1, 2, 2) * fc(2, -3) + pw(2, 2, 2) * fc(2, -4);
+  const double zff22 = pw(-1, 2, 2) * fc(-1, 2) + pw(0, 2, 2) * fc(-2, 2) + pw(1, 2, 2) * fc(-3, 2) + pw(2, 2, 2) * fc(-4, 2);
+  return 0.5 * (pw(-1, -1, 2) * zff11 + pw(0, -1, 2) * zff1 + pw(1, -1, 2) * fc(-1, 1) + pw(2, -1, 2) * fc(-1, 2) +
+                pw(-1, -1, 2) * zff22 + pw(0, -1, 2) * zff2 + pw(1, -1, 2) * fc(1, -1) + pw(2, -1, 2) * fc(2, -1));
+}
+
+// The ECS_O value at the halo point (i1, j1) of a halo of width hw (1 or 2):
+// a corner value where the point is one of its corner's special points, else
+// the cubic interpolation along the edge (ecs_ext_halo_1e) of row r.
+__device__ double ecs_o_at(const CArgsT<double>& a, const double* f, int p, int i1, int j1, int hw) {
+  const int N = a.N;
+  const int ci[6] = {0, 1, 0, -1, 0, -1}, cj[6] = {1, 0, 0, 0, -1, -1};
+  for (int c = 0; c < 4; ++c) {
+    const int ist = (c == 1 || c == 2) ? N + 1 : 0, jst = c >= 2 ? N + 1 : 0;
+    const int idr = (c == 1 || c == 2) ? -1 : 1, jdr = c >= 2 ? -1 : 1;
+    const int ri = idr * (i1 - ist), rj = jdr * (j1 - jst);
+    for (int k = 0; k < (hw > 1 ? 6 : 3); ++k)
+      if (ri == ci[k] && rj == cj[k]) return ecs_corner(a, f, p, c, k);
+  }
+  int r, pos;
+  bool along_i;
+  if (j1 < 1) { r = 1 - j1; pos = i1; along_i = true; }
+  else if (j1 > N) { r = j1 - N; pos = i1; along_i = true; }
+  else if (i1 < 1) { r = 1 - i1; pos = j1; along_i = false; }
+  else { r = i1 - N; pos = j1; along_i = false; }
+  const int b = __ldg(&a.ecs_ind[(r - 1) * (N + 4) + (pos + 1)]);
+  auto G = [&](int k) { return along_i ? ecs_x(a, f, p, k, j1) : ecs_x(a, f, p, i1, k); };
+  double s = ecs_wt(a, -1, pos, r) * G(b - 1);
+  s = s + ecs_wt(a, 0, pos, r) * G(b);
+  s = s + ecs_wt(a, 1, pos, r) * G(b + 1);
+  s = s + ecs_wt(a, 2, pos, r) * G(b + 2);
+  return s;
+}
+
+// gradient_a2_ecs (gradient/grad_a2_mod.f90:19-69): the central difference of
+// the cell values with the ECS_O halo of width 1 at the panel edges, gx, gy
+// covariant at the centres.
+__global__ void __launch_bounds__(256) grad_a2_kernel(const __grid_constant__ CArgsT<double> a) {
+  const int N = a.N;
+  SWM_C_INDEX(N, N)
+  const double* f = a.ke_in;
+  auto E = [&](int i1, int j1) {
+    return (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) ? f[at(a.g, p, i1 - 1, j1 - 1)] : ecs_o_at(a, f, p, i1, j1, 1);
+  };
+  const int i1 = i + 1, j1 = j + 1, e = at(a.g, p, i, j);
+  a.o1[e] = 0.5 * (E(i1 + 1, j1) - E(i1 - 1, j1)) / a.hxa;
+  a.o2[e] = 0.5 * (E(i1, j1 + 1) - E(i1, j1 - 1)) / a.hxa;
+}
+
+// The extended tiles of the ECS_O halo of width hw: ext[p][j][i] for the
+// 1-based (i - hw + 1, j - hw + 1), width N + 2 hw.
+__global__ void __launch_bounds__(256) ecs_ext_kernel(const __grid_constant__ CArgsT<double> a, int hw,
+                                                      double* ext) {
+  const int N = a.N, W = N + 2 * hw;
+  SWM_C_INDEX(W, W)
+  const int i1 = i + 1 - hw, j1 = j + 1 - hw;
+  const double* f = a.ke_in;
+  const double v = (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) ? f[at(a.g, p, i1 - 1, j1 - 1)]
+                                                              : ecs_o_at(a, f, p, i1, j1, hw);
+  ext[((long long)p * W + j) * W + i] = v;
+}
+
 // Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
 // (operator_swm_mod.f90:84-85), the divergence (div_c_sbp42_mod.f90:67-107,
 // div_c2_mod.f90:97-177) and the Coriolis terms at the centres
@@ -715,6 +836,10 @@ struct CGrid {
   cudaStream_t bs[2] = {nullptr, nullptr};
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   int* halo = nullptr;
+  double* ecs_w = nullptr;  // ECS_O weights [2][N+4][4]
+  int* ecs_ind = nullptr;   // ECS_O stencil bases [2][N+4]
+  double* ext = nullptr;    // extended tiles of swm_halo_ecs_o (allocated on first use)
+  int ext_hw = 0;
   double* wts = nullptr;   // quadrature weights: centres (N), interfaces (N+1)
   double* part = nullptr;  // kMassBlocks partial sums
   double* metric(int k) const { return met + (long long)k * g.fs; }
@@ -750,6 +875,7 @@ CArgsT<T> base_args(const CGrid* c, int ord = 0) {
   a.Jv = M(M_JV); a.Qi3v = M(M_QI3V); a.rJv = M(M_RJV);
   a.rJqha = M(M_RJQHA); a.rJuha = M(M_RJUHA); a.rJvha = M(M_RJVHA);
   a.halo = c->halo;
+  a.ecs_w = c->ecs_w; a.ecs_ind = c->ecs_ind; a.hxa = c->hx * c->radius;
   a.Ap = Wk(W_AP); a.Bp = Wk(W_BP); a.ut = Wk(W_UT); a.vt = Wk(W_VT);
   a.hu = Wk(W_HU); a.hv = Wk(W_HV); a.Gu = Wk(W_GU); a.Gv = Wk(W_GV);
   a.KEu = Wk(W_KEU); a.KEv = Wk(W_KEV); a.curl = Wk(W_CURL);
@@ -1008,6 +1134,34 @@ cudaError_t diffusion(const CGrid* c, const Topology& tp, T* edge, int parts, do
   return cudaGetLastError();
 }
 
+// Weights of the ECS_O halo (equiang_cs/ecs_halo_factory_mod.f90:164-196,
+// init_halo_interp) for rows 1, 2 and positions -1..N+2: the virtual point's
+// angle on the neighbour's grid line, atan(tan(alpha_i) / tan(pi/4 +
+// (r - 1/2) hx)), its stencil base and the four cubic Lagrange weights.
+// False if a stencil the edges use would leave the panel.
+bool build_ecs_weights(int N, double hx, std::vector<double>& w, std::vector<int>& ind) {
+  const int ni = N + 4;
+  w.assign((size_t)2 * ni * 4, 0.0);
+  ind.assign((size_t)2 * ni, 0);
+  for (int r = 1; r <= 2; ++r)
+    for (int i = -1; i <= N + 2; ++i) {
+      const double zb = 0.25 * kPiC + (r - 0.5) * hx;
+      double za = -0.25 * kPiC + (i - 0.5) * hx;
+      za = std::atan(std::tan(za) / std::tan(zb));
+      const int b = (int)std::floor((za + 0.25 * kPiC - 0.5 * hx) / hx) + 1;
+      const double x = (za + 0.25 * kPiC) / hx - (b - 0.5);
+      double* q = &w[((size_t)(r - 1) * ni + (i + 1)) * 4];
+      q[0] = -x * (x - 1.0) * (x - 2.0) / 6.0;
+      q[1] = (x + 1.0) * (x - 1.0) * (x - 2.0) / 2.0;
+      q[2] = -(x + 1.0) * x * (x - 2.0) / 2.0;
+      q[3] = (x + 1.0) * x * (x - 1.0) / 6.0;
+      ind[(size_t)(r - 1) * ni + (i + 1)] = b;
+      const bool used = r == 1 ? (i >= 2 && i <= N - 1) : (i >= 1 && i <= N);
+      if (used && (b - 1 < 1 || b + 2 > N)) return false;
+    }
+  return true;
+}
+
 }  // namespace
 
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
@@ -1027,6 +1181,9 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   const double ax[3] = {axis[0] / an, axis[1] / an, axis[2] / an};
   std::vector<int> tab;
   if (!build_halo(N, g, tab, why)) { delete c; return 1; }
+  std::vector<double> ew;
+  std::vector<int> eind;
+  if (!build_ecs_weights(N, c->hx, ew, eind)) { why = "ECS_O halo stencils leave the panel"; delete c; return 1; }
   std::vector<double> w(2 * (size_t)N + 1, 1.0);
   {
     // SBP_C42 / SBP_C21 edge weights (D42_A_centers / _interfaces, D21_*)
@@ -1049,6 +1206,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   ok(cudaMalloc(&c->wk, W_COUNT * fb));
   ok(cudaMalloc(&c->rk, 9 * fb));
   ok(cudaMalloc(&c->halo, sizeof(int) * tab.size()));
+  ok(cudaMalloc(&c->ecs_w, sizeof(double) * ew.size()));
+  ok(cudaMalloc(&c->ecs_ind, sizeof(int) * eind.size()));
   ok(cudaMalloc(&c->wts, sizeof(double) * w.size()));
   ok(cudaMalloc(&c->part, sizeof(double) * kMassBlocks));
   if (e == cudaSuccess) {
@@ -1090,6 +1249,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
     ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
     ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->ecs_w, ew.data(), sizeof(double) * ew.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->ecs_ind, eind.data(), sizeof(int) * eind.size(), cudaMemcpyHostToDevice, st));
     if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
       ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
     ok(cudaMemcpyAsync(c->wts, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st));
@@ -1107,7 +1268,7 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
 void cgrid_destroy(CGrid* c) {
   if (!c) return;
   for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->dw, (void*)c->halo,
-                  (void*)c->wts, (void*)c->part})
+                  (void*)c->ecs_w, (void*)c->ecs_ind, (void*)c->ext, (void*)c->wts, (void*)c->part})
     if (p) cudaFree(p);
   for (cudaStream_t s : c->bs)
     if (s) cudaStreamDestroy(s);
@@ -1318,6 +1479,34 @@ cudaError_t cgrid_diffusion_step32(CGrid* c, const Topology& tp, float* edge, in
                                    float* hi, float* lo, double dt, cudaStream_t st) {
   if (!c->met32 || parts < 1 || parts > 3) return cudaErrorInvalidValue;
   return diffusion<float>(c, tp, edge, parts, c4uv, c4h, hi, hi, lo, dt, 2, st);
+}
+
+cudaError_t cgrid_grad_a2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st) {
+  CArgsT<double> a = base_args<double>(c);
+  a.ke_in = f; a.o1 = gx; a.o2 = gy;
+  grad_a2_kernel<<<grid_for(c->N, c->N), kBlock, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t cgrid_ecs_o_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st) {
+  if (halo_width < 1 || halo_width > 2) return cudaErrorInvalidValue;
+  const int W = c->N + 2 * halo_width;
+  const size_t bytes = sizeof(double) * 6 * (size_t)W * W;
+  if (c->ext_hw < halo_width) {
+    // the scratch of the widest halo asked for (a synchronous call)
+    CKE(cudaStreamSynchronize(st));
+    if (c->ext) cudaFree(c->ext);
+    c->ext = nullptr;
+    c->ext_hw = 0;
+    CKE(cudaMalloc(&c->ext, bytes));
+    c->ext_hw = halo_width;
+  }
+  CArgsT<double> a = base_args<double>(c);
+  a.ke_in = f;
+  ecs_ext_kernel<<<grid_for(W, W), kBlock, 0, st>>>(a, halo_width, c->ext);
+  CKE(cudaGetLastError());
+  CKE(cudaMemcpyAsync(ext_host, c->ext, bytes, cudaMemcpyDeviceToHost, st));
+  return cudaStreamSynchronize(st);
 }
 
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st) {

@@ -95,6 +95,13 @@ cudaError_t cgrid_diffusion32(CGrid* c, const Topology& tp, float* edge, int par
                               const float* in, float* out, cudaStream_t st);
 cudaError_t cgrid_diffusion_step32(CGrid* c, const Topology& tp, float* edge, int parts, double c4uv, double c4h,
                                    float* hi, float* lo, double dt, cudaStream_t st);
+// The ECS_O scalar halo of a cell-centre field (equiang_cs/ecs_halo_mod.f90:
+// 95-475, create_halo_procedure "ECS_O") and gradient_a2_ecs (gradient/
+// grad_a2_mod.f90:19-69) on the centre mesh, which is the A grid's mesh.
+// cgrid_ecs_o_halo: the extended tiles (6 x (N+2hw)^2, hw 1 or 2, row-major)
+// into host memory, synchronously.
+cudaError_t cgrid_grad_a2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st);
+cudaError_t cgrid_ecs_o_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

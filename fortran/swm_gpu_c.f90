@@ -270,6 +270,16 @@ interface
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, u, v, ut, vt
     end function swm_op_contra2co
+    integer(c_int) function swm_op_grad_a2_ecs(ctx, gx, gy, f) bind(c, name="swm_op_grad_a2_ecs")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, gx, gy, f
+    end function swm_op_grad_a2_ecs
+    integer(c_int) function swm_halo_ecs_o(ctx, f, halo_width, ext) bind(c, name="swm_halo_ecs_o")
+        import :: c_int, c_ptr, c_double
+        type(c_ptr), value :: ctx, f
+        integer(c_int), value :: halo_width
+        real(c_double), intent(out) :: ext(*)
+    end function swm_halo_ecs_o
     integer(c_int) function swm_sync_scalar(ctx, f) bind(c, name="swm_sync_scalar")
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, f

@@ -279,6 +279,19 @@ int swm_op_grad_perp(swm_ctx* ctx, swm_field* gu, swm_field* gv,
                      const swm_field* w);
 int swm_op_contra2co(swm_ctx* ctx, swm_field* u, swm_field* v,
                      const swm_field* ut, const swm_field* vt);
+/* C grid only, on its cell-centre mesh (the A grid's points): the ECS_O
+ * scalar halo (halo_t%get_halo_scalar for "ECS_O", equiang_cs/ecs_halo_mod.f90
+ * :95-475 with the weights of ecs_halo_factory_mod.f90:164-196) and
+ * gradient_a2_ecs (gradient/grad_a2_mod.f90:19-69: the central difference of
+ * the cell values with that halo, covariant gx, gy at the centres).
+ * swm_halo_ecs_o writes, synchronously, the extended tiles of halo width 1 or
+ * 2 to host memory: 6 panels of (N+2hw) x (N+2hw) doubles, row-major, the
+ * reference's 1-based (i, j) at row j + hw - 1, column i + hw - 1.
+ * SWM_E_UNSUPPORTED on the Ah grid. */
+int swm_op_grad_a2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy,
+                       const swm_field* f);
+int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width,
+                   double* ext);
 /* halo_t%get_halo_scalar for "Ah_scalar_sync"
  * (halo/halo_Ah_scalar_sync_mod.f90:20-93) */
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f);

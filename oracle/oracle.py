@@ -110,6 +110,9 @@ def lib():
             getattr(L, name).argtypes = [vp] + [_D] * n
         L.orcc_rk4.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int]
         L.orcc_grad_perp.argtypes = [vp, _D, _D, _D]
+        L.orcc_ecs_o_halo.argtypes = [vp, _D, ctypes.c_int, _D]
+        L.orcc_ecs_o_halo.restype = ctypes.c_int
+        L.orcc_grad_a2_ecs.argtypes = [vp, _D, _D, _D]
         L.orcc_contra2co.argtypes = [vp, _D, _D, _D, _D]
         L.orcc_hordiff.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double] + [_D] * 6
         L.orcc_model_step.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -280,36 +283,6 @@ class OracleDomain:
                                        _p(np.ascontiguousarray(v)), _p(uo), _p(vo)) == 0
         return uo, vo
 
-    def grad_perp(self, w):
-        gu, gv = self.zeros("u"), self.zeros("v")
-        lib().orcc_grad_perp(self._h, _p(self._c(w)), _p(gu), _p(gv))
-        return gu, gv
-
-    def contra2co(self, ut, vt):
-        u, v = self.zeros("u"), self.zeros("v")
-        lib().orcc_contra2co(self._h, _p(self._c(ut)), _p(self._c(vt)), _p(u), _p(v))
-        return u, v
-
-    # hordiff_uv_name of the C grid -> the parts of the vector hyperdiffusion
-    HORDIFF_UV = {"hordiff_c_biharm_div": 1, "hordiff_c_biharm_curl": 2, "hordiff_c_biharm_curl_div": 3}
-
-    def hordiff(self, h, u, v, uv_name="hordiff_c_biharm_curl_div", uv_coeff=0.03, h_coeff=0.03):
-        """Tendency of operator_swm_diff_t%apply with the C-grid operators."""
-        th, tu, tv = self.zeros("p"), self.zeros("u"), self.zeros("v")
-        lib().orcc_hordiff(self._h, self.HORDIFF_UV[uv_name], float(uv_coeff), float(h_coeff),
-                           *(_p(self._c(a)) for a in (h, u, v)), _p(th), _p(tu), _p(tv))
-        return th, tu, tv
-
-    def model_step(self, h, u, v, dt, nsteps=1, hs=None, uv_name="hordiff_c_biharm_curl_div",
-                   uv_coeff=0.03, h_coeff=0.03):
-        """nsteps of one RK4 step followed by one explicit Euler step of the
-        hyperdiffusion."""
-        h, u, v = (np.array(a, dtype=np.float64, order="C") for a in (h, u, v))
-        hs_p = None if hs is None else _p(self._c(hs))
-        lib().orcc_model_step(self._h, hs_p, _p(h), _p(u), _p(v), float(dt), int(nsteps),
-                              self.HORDIFF_UV[uv_name], float(uv_coeff), float(h_coeff))
-        return h, u, v
-
     VECTOR_FIELDS = {"solid_rotation": 0, "cross_polar": 1, "xyz_grad": 2, "vsh_curl_free_10": 3}
     SCALAR_FIELDS = {"xyz": 10, "cross_polar_div": 11, "cross_polar_zeta": 12}
 
@@ -432,6 +405,20 @@ class OracleCDomain:
         lib().orcc_grad_perp(self._h, _p(self._c(w)), _p(gu), _p(gv))
         return gu, gv
 
+    def ecs_o_halo(self, f, halo_width=2):
+        """The ECS_O halo of a cell-centre field: (6, N+2hw, N+2hw) extended
+        tiles, 1-based (i, j) of the reference at [j + hw - 1, i + hw - 1]."""
+        W = self.N + 2 * int(halo_width)
+        e = np.zeros((6, W, W))
+        assert lib().orcc_ecs_o_halo(self._h, _p(self._c(f)), int(halo_width), _p(e)) == 0
+        return e
+
+    def grad_a2_ecs(self, f):
+        """gradient_a2_ecs at the cell centres (covariant gx, gy, both p-shaped)."""
+        gx, gy = self.zeros("p"), self.zeros("p")
+        lib().orcc_grad_a2_ecs(self._h, _p(self._c(f)), _p(gx), _p(gy))
+        return gx, gy
+
     def contra2co(self, ut, vt):
         u, v = self.zeros("u"), self.zeros("v")
         lib().orcc_contra2co(self._h, _p(self._c(ut)), _p(self._c(vt)), _p(u), _p(v))
@@ -482,8 +469,10 @@ class OracleCDomain:
 def golden_c(kind: str, N: int = 32, sbp_order: int = 42) -> np.ndarray:
     """Values printed by the reference known-answer test of a C-grid
     operator at (N, nz=3): kind div, grad, curl, coriolis, ke, co2contra or
-    contra2co (the transform2co of co2contra_c_sbp*_new)."""
-    k = {"div": 0, "grad": 1, "curl": 2, "coriolis": 3, "ke": 4, "co2contra": 5, "contra2co": 6}[kind]
+    contra2co (the transform2co of co2contra_c_sbp*_new), or grad_a2_ecs
+    (gradient_a2_ecs on the A grid's cell centres, with the ECS_O halo)."""
+    k = {"div": 0, "grad": 1, "curl": 2, "coriolis": 3, "ke": 4, "co2contra": 5, "contra2co": 6,
+         "grad_a2_ecs": 7}[kind]
     out = np.zeros(4)
     if lib().orcc_golden(k, int(N), int(sbp_order), _p(out)) != 0:
         raise ValueError(f"oracle C-grid golden {kind} failed for order {sbp_order}")

@@ -173,6 +173,12 @@ void orcc_hordiff(const orcc_domain* d, int parts, double uv_coeff, double h_coe
 void orcc_model_step(const orcc_domain* d, const double* hs, double* h, double* u,
                      double* v, double dt, int nsteps, int parts, double uv_coeff,
                      double h_coeff);
+/* The ECS_O scalar halo (create_halo_procedure "ECS_O") of a cell-centre
+ * field, width 1 or 2: ext receives per panel the extended (N+2hw)^2 tile,
+ * row-major; returns 0 or -1.  gradient_a2_ecs: its central-difference
+ * gradient at the cell centres (the A grid's points). */
+int orcc_ecs_o_halo(const orcc_domain* d, const double* f, int halo_width, double* ext);
+void orcc_grad_a2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy);
 double orcc_mass(const orcc_domain* d, int mesh, const double* f);
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
 /* Analytic test fields on the C meshes: vector kinds 0 solid rotation (axis
@@ -185,7 +191,7 @@ int orcc_scalar_test_field(const orcc_domain* d, int kind, int level, int mesh,
                            double* f);
 /* Known-answer tests on the C grid at (N, nz=3, unit sphere): kind 0 div (4
  * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2),
- * 6 contra2co of co2contra_c_sbp*_new (2).
+ * 6 contra2co of co2contra_c_sbp*_new (2), 7 gradient_a2_ecs (2).
  * Returns 0, or -1 for an unknown kind / order. */
 int orcc_golden(int kind, int N, int sbp_order, double* out);
 

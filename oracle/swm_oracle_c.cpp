@@ -154,7 +154,7 @@ struct Mesh {
 // Halo slot of panel p, side s (0 left i<0, 1 right i>=nx, 2 bottom j<0,
 // 3 top j>=ny), depth d = 1..kDepth, along-side index k: the sender's dense
 // index, whether the sender value is the other vector component, and the sign.
-constexpr int kDepth = 3;
+constexpr int kDepth = 5;  // 3 for the C-grid operators, 5 for the ECS_O corner formulas
 struct HaloSrc {
   int idx = -1;
   bool other = false;
@@ -232,7 +232,10 @@ struct orcc_domain {
   Halo ho, hu, hv, hq;     // scalar on p, C vector u / v, scalar on q
   Ops ops;    // the operators of the model's SBP order
   Ops ops21;  // the 2/1 operators of the C-grid hyperdiffusion
-  std::vector<double> Ac, Ai;  // quadrature edge weights at centres / interfaces
+  std::vector<double> Ac, Ai;
+  // ECS_O halo: cubic weights [row 0..1][position -1..N+2][4] and stencil bases
+  std::vector<double> ecs_w;
+  std::vector<int> ecs_ind;  // quadrature edge weights at centres / interfaces
 };
 
 namespace {
@@ -713,6 +716,137 @@ void hordiff_h(const orcc_domain& d, double coeff, const double* h, double* th) 
   for (int k = 0; k < P.size(); ++k) th[k] = c4 * f[k];
 }
 
+// ------------------------------------------------------------------ ECS_O
+// Weights of the ECS_O halo (equiang_cs/ecs_halo_factory_mod.f90:164-196,
+// init_halo_interp): the virtual point at position i (1-based, -1..N+2) of
+// halo row r (1, 2) lies on the neighbour panel's grid line r at the angle
+// atan(tan(alpha_i) / tan(pi/4 + (r - 1/2) hx)); ind is the neighbour cell
+// below it and the four cubic Lagrange weights take the neighbour's points
+// ind-1 .. ind+2.  Returns false if a stencil used by the edge interpolation
+// would leave the panel (never for N >= 12).
+bool build_ecs_weights(orcc_domain& d) {
+  const int N = d.N, ni = N + 4;
+  d.ecs_w.assign((size_t)2 * ni * 4, 0.0);
+  d.ecs_ind.assign((size_t)2 * ni, 0);
+  for (int r = 1; r <= 2; ++r)
+    for (int i = -1; i <= N + 2; ++i) {
+      const double zb = 0.25 * PI + (r - 0.5) * d.hx;
+      double za = -0.25 * PI + (i - 0.5) * d.hx;
+      const double zx = std::tan(za) / std::tan(zb);
+      za = std::atan(zx);
+      const int ind = (int)std::floor((za + 0.25 * PI - 0.5 * d.hx) / d.hx) + 1;
+      const double x = (za + 0.25 * PI) / d.hx - (ind - 0.5);
+      double* w = &d.ecs_w[((size_t)(r - 1) * ni + (i + 1)) * 4];
+      w[0] = -x * (x - 1.0) * (x - 2.0) / 6.0;
+      w[1] = (x + 1.0) * (x - 1.0) * (x - 2.0) / 2.0;
+      w[2] = -(x + 1.0) * x * (x - 2.0) / 2.0;
+      w[3] = (x + 1.0) * x * (x - 1.0) / 6.0;
+      d.ecs_ind[(size_t)(r - 1) * ni + (i + 1)] = ind;
+      const bool used = r == 1 ? (i >= 2 && i <= N - 1) : (i >= 1 && i <= N);
+      if (used && (ind - 1 < 1 || ind + 2 > N)) return false;
+    }
+  return true;
+}
+
+// ECS_O halo of width hw (1 or 2) of one panel (ecs_halo_mod.f90:95-475 after
+// the 'full' o-point exchange): E is the extended panel, 1-based (i, j) in
+// [1-hw, N+hw]^2, row-major with width N + 2 hw.  The interior is f; the
+// cross halos are the exchanged neighbour values interpolated along each
+// edge (ecs_ext_halo_1e; the first row leaves its two end points to the
+// corners); the points next to and in each cube corner come from the corner
+// formulas of ecs_halo_1corner on the exchanged values.  No formula reads the
+// exchange's corner regions, which the one-tile-per-panel exchange leaves
+// unfilled.
+void ecs_o_panel(const orcc_domain& d, const double* f, int p, int hw, double* E) {
+  const Mesh& P = d.m[0];
+  const int N = d.N, W = N + 2 * hw, ni = N + 4;
+  auto X = [&](int i1, int j1) { return ext(P, d.ho, f, nullptr, p, i1 - 1, j1 - 1); };
+  auto out = [&](int i1, int j1) -> double& { return E[(size_t)(j1 - 1 + hw) * W + (i1 - 1 + hw)]; };
+  auto w = [&](int m, int i, int r) { return d.ecs_w[((size_t)(r - 1) * ni + (i + 1)) * 4 + (m + 1)]; };
+  auto ind = [&](int i, int r) { return d.ecs_ind[(size_t)(r - 1) * ni + (i + 1)]; };
+  for (int j = 1; j <= N; ++j)
+    for (int i = 1; i <= N; ++i) out(i, j) = f[P.at(p, i - 1, j - 1)];
+  // corners first, from the exchanged values (ecs_halo_corners)
+  const int ist[4] = {0, N + 1, N + 1, 0}, idr[4] = {1, -1, -1, 1};
+  const int jst[4] = {0, 0, N + 1, N + 1}, jdr[4] = {1, 1, -1, -1};
+  double cs[4][6] = {};
+  for (int c = 0; c < 4; ++c) {
+    auto fc = [&](int i, int j) { return X(ist[c] + idr[c] * i, jst[c] + jdr[c] * j); };
+    // the weights of corner 1, mirrored for the corners at i = N+1
+    auto pw = [&](int m, int i, int r) { return idr[c] == 1 ? w(m, i, r) : w(1 - m, N + 1 - i, r); };
+    const double zw = pw(-1, 1, 1), zw2 = zw * zw, zw3 = zw2 * zw;
+    const double z0 = pw(0, 1, 1), z1 = pw(1, 1, 1), z2 = pw(2, 1, 1);
+    double* q = cs[c];
+    double zx = z0 * fc(0, 1) + z1 * fc(0, 2) + z2 * fc(0, 3);
+    double zy = z0 * fc(1, 0) + z1 * fc(1, -1) + z2 * fc(1, -2);
+    double zz = z0 * fc(1, 1) + z1 * fc(2, 1) + z2 * fc(3, 1);
+    q[0] = (zx + zw * zy + zw2 * zz) / (1.0 - zw3);
+    const double zfy1 = (zy + zw * zz + zw2 * zx) / (1.0 - zw3);
+    zx = z0 * fc(1, 0) + z1 * fc(2, 0) + z2 * fc(3, 0);
+    zy = z0 * fc(0, 1) + z1 * fc(-1, 1) + z2 * fc(-2, 1);
+    zz = z0 * fc(1, 1) + z1 * fc(1, 2) + z2 * fc(1, 3);
+    q[1] = (zx + zw * zy + zw2 * zz) / (1.0 - zw3);
+    const double zfy2 = (zy + zw * zz + zw2 * zx) / (1.0 - zw3);
+    double zff1 = pw(-1, 1, 2) * fc(2, 0) + pw(0, 1, 2) * fc(2, -1) + pw(1, 1, 2) * fc(2, -2) + pw(2, 1, 2) * fc(2, -3);
+    double zff2 = pw(-1, 1, 2) * fc(0, 2) + pw(0, 1, 2) * fc(-1, 2) + pw(1, 1, 2) * fc(-2, 2) + pw(2, 1, 2) * fc(-3, 2);
+    q[2] = 0.5 * (pw(-1, 0, 1) * zff1 + pw(0, 0, 1) * zfy1 + pw(1, 0, 1) * fc(0, 1) + pw(2, 0, 1) * fc(0, 2) +
+                  pw(-1, 0, 1) * zff2 + pw(0, 0, 1) * zfy2 + pw(1, 0, 1) * fc(1, 0) + pw(2, 0, 1) * fc(2, 0));
+    if (hw > 1) {
+      zff1 = pw(-1, 2, 1) * fc(1, 0) + pw(0, 2, 1) * fc(1, -1) + pw(1, 2, 1) * fc(1, -2) + pw(2, 2, 1) * fc(1, -3);
+      const double zff11 =
+          pw(-1, 2, 2) * fc(2, -1) + pw(0, 2, 2) * fc(2, -2) + pw(1, 2, 2) * fc(2, -3) + pw(2, 2, 2) * fc(2, -4);
+      zff2 = pw(-1, 2, 1) * fc(0, 1) + pw(0, 2, 1) * fc(-1, 1) + pw(1, 2, 1) * fc(-2, 1) + pw(2, 2, 1) * fc(-3, 1);
+      const double zff22 =
+          pw(-1, 2, 2) * fc(-1, 2) + pw(0, 2, 2) * fc(-2, 2) + pw(1, 2, 2) * fc(-3, 2) + pw(2, 2, 2) * fc(-4, 2);
+      q[3] = pw(-1, 0, 2) * zff1 + pw(0, 0, 2) * fc(-1, 1) + pw(1, 0, 2) * fc(-1, 2) + pw(2, 0, 2) * fc(-1, 3);
+      q[4] = pw(-1, 0, 2) * zff2 + pw(0, 0, 2) * fc(1, -1) + pw(1, 0, 2) * fc(2, -1) + pw(2, 0, 2) * fc(3, -1);
+      q[5] = 0.5 * (pw(-1, -1, 2) * zff11 + pw(0, -1, 2) * zff1 + pw(1, -1, 2) * fc(-1, 1) + pw(2, -1, 2) * fc(-1, 2) +
+                    pw(-1, -1, 2) * zff22 + pw(0, -1, 2) * zff2 + pw(1, -1, 2) * fc(1, -1) + pw(2, -1, 2) * fc(2, -1));
+    }
+  }
+  // edges: rows r = 1..hw of each cross halo (ecs_halo_edges_x / _y)
+  for (int r = 1; r <= hw; ++r)
+    for (int i = (r == 1 ? 2 : 1); i <= (r == 1 ? N - 1 : N); ++i) {
+      const int b = ind(i, r);
+      auto itp = [&](auto G) {
+        double s = w(-1, i, r) * G(b - 1);
+        s = s + w(0, i, r) * G(b);
+        s = s + w(1, i, r) * G(b + 1);
+        s = s + w(2, i, r) * G(b + 2);
+        return s;
+      };
+      out(i, 1 - r) = itp([&](int k) { return X(k, 1 - r); });
+      out(i, N + r) = itp([&](int k) { return X(k, N + r); });
+      out(1 - r, i) = itp([&](int k) { return X(1 - r, k); });
+      out(N + r, i) = itp([&](int k) { return X(N + r, k); });
+    }
+  // corner points (ecs_halo_corners_put): corner-relative (0,1), (1,0), (0,0),
+  // and for hw 2 (-1,0), (0,-1), (-1,-1)
+  const int ci[6] = {0, 1, 0, -1, 0, -1}, cj[6] = {1, 0, 0, 0, -1, -1};
+  for (int c = 0; c < 4; ++c)
+    for (int k = 0; k < (hw > 1 ? 6 : 3); ++k) out(ist[c] + idr[c] * ci[k], jst[c] + jdr[c] * cj[k]) = cs[c][k];
+}
+
+// gradient_a2_ecs (gradient/grad_a2_mod.f90:19-69 with grad_factory_mod.f90:
+// 105-121): the ECS_O halo of width 1, then central differences of the cell
+// values, gx = 0.5 (f(i+1) - f(i-1)) / (hx a), covariant, at the centres.
+void grad_a2_ecs(const orcc_domain& d, const double* f, double* gx, double* gy) {
+  const Mesh& P = d.m[0];
+  const int N = d.N, hw = 1, W = N + 2;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (int p = 0; p < 6; ++p) {
+    std::vector<double> E((size_t)W * W, 0.0);
+    ecs_o_panel(d, f, p, hw, E.data());
+    auto e = [&](int i1, int j1) { return E[(size_t)j1 * W + i1]; };  // 0-based extended
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        const int ii = i + 1, jj = j + 1;
+        gx[P.at(p, i, j)] = 0.5 * (e(ii + 1, jj) - e(ii - 1, jj)) / (d.hx * d.scale);
+        gy[P.at(p, i, j)] = 0.5 * (e(ii, jj + 1) - e(ii, jj - 1)) / (d.hx * d.scale);
+      }
+  }
+}
+
 // operator_swm_t%apply, vector-invariant branch
 // (models/shallow_water/operator/operator_swm_mod.f90:61-113).
 void apply(const orcc_domain& d, const double* hs, const double* h, const double* u, const double* v, double* th,
@@ -868,6 +1002,10 @@ orcc_domain* create(int N, int order, double radius, double grav, double omega, 
   d->hu = build_halo(d->m[1], d->m[2], 1);
   d->hv = build_halo(d->m[2], d->m[1], 2);
   d->hq = build_halo(d->m[3], d->m[3], 0);
+  if (!build_ecs_weights(*d)) {
+    delete d;
+    return nullptr;
+  }
   d->ops21.order = 21;
   d->ops21.Wc2i = make_stag(W21_C2I); d->ops21.Wi2c = make_stag(W21_I2C);
   d->ops21.Dc2i = make_stag(D21_C2I); d->ops21.Di2c = make_stag(D21_I2C);
@@ -951,6 +1089,13 @@ void orcc_model_step(const orcc_domain* d, const double* hs, double* h, double* 
     diffusion_step(*d, parts, uv_coeff, h_coeff, h, u, v, dt);
   }
 }
+int orcc_ecs_o_halo(const orcc_domain* d, const double* f, int halo_width, double* ext) {
+  if (halo_width < 1 || halo_width > 2) return -1;
+  const size_t W = (size_t)d->N + 2 * halo_width;
+  for (int p = 0; p < 6; ++p) ecs_o_panel(*d, f, p, halo_width, ext + p * W * W);
+  return 0;
+}
+void orcc_grad_a2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy) { grad_a2_ecs(*d, f, gx, gy); }
 double orcc_mass(const orcc_domain* d, int mesh, const double* f) { return mass(*d, mesh, f); }
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f) {
   return std::sqrt(l2sq(d->m[mesh], d->hx, f));
@@ -1149,6 +1294,32 @@ int orcc_golden(int kind, int N, int order, double* out) {
         ally.insert(ally.end(), b.begin(), b.end());
         l2x += l2sq(U, d->hx, c.data());
         l2y += l2sq(V, d->hx, b.data());
+      }
+      out[0] = maxabs(allx) + maxabs(ally);
+      out[1] = std::sqrt(l2x) + std::sqrt(l2y);
+      break;
+    }
+    case 7: {  // gradient_a2_ecs of x, y, z on the cell centres (the A grid's points)
+      std::vector<double> f(P.size()), tx(P.size()), ty(P.size()), gx(P.size()), gy(P.size());
+      for (int lev = 0; lev < 3; ++lev) {
+        for (int k = 0; k < P.size(); ++k) {
+          f[k] = field_xyz(lev, P.rx[k], P.ry[k], P.rz[k]);
+          double W3[3];
+          field_xyz_grad(lev, P.rx[k], P.ry[k], P.rz[k], W3);
+          const double* a1 = &P.a1[3 * k];
+          const double* a2 = &P.a2[3 * k];
+          tx[k] = W3[0] * a1[0] + W3[1] * a1[1] + W3[2] * a1[2];
+          ty[k] = W3[0] * a2[0] + W3[1] * a2[1] + W3[2] * a2[2];
+        }
+        grad_a2_ecs(*d, f.data(), gx.data(), gy.data());
+        for (int k = 0; k < P.size(); ++k) {
+          gx[k] = d->scale * gx[k] - 1.0 * tx[k];
+          gy[k] = d->scale * gy[k] - 1.0 * ty[k];
+        }
+        allx.insert(allx.end(), gx.begin(), gx.end());
+        ally.insert(ally.end(), gy.begin(), gy.end());
+        l2x += l2sq(P, d->hx, gx.data());
+        l2y += l2sq(P, d->hx, gy.data());
       }
       out[0] = maxabs(allx) + maxabs(ally);
       out[1] = std::sqrt(l2x) + std::sqrt(l2y);

@@ -11,7 +11,8 @@ with the line number of the reference file it came from.  The C-grid file
 keeps the SBP operators of the &shallow_water_model_c family (div, grad,
 curl, Coriolis, KE and co2contra at sbp21 and sbp42) and the co2contra /
 contra2co pair of co2contra_c_sbp*_new that the C-grid hyperdiffusion's curl
-part uses.  The
+part uses, and gradient_a2_ecs, whose only halo is the interpolating ECS_O
+halo of the cell centres.  The
 values were printed by the reference test with format "(A,4E15.7)", i.e. to
 7 significant digits, from test_diffops_all.f90 at N=32, nz=3.
 """
@@ -42,6 +43,9 @@ KEEP_C = {
     "co2contra_c_sbp21": ("co2contra", 21), "co2contra_c_sbp42": ("co2contra", 42),
     "co2contra_c_sbp21_new": ("co2contra", 21), "co2contra_c_sbp42_new": ("co2contra", 42),
     "contra2co_c_sbp21_new": ("contra2co", 21), "contra2co_c_sbp42_new": ("contra2co", 42),
+    # the A grid's central-difference gradient on the cell centres, which pins
+    # the ECS_O halo (the sbp_order entry only selects the oracle domain)
+    "gradient_a2_ecs": ("grad_a2_ecs", 42),
 }
 
 

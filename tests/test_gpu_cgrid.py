@@ -5,8 +5,9 @@ known answers.
 Pins:
 * every C-grid line of reference_results.txt (div, grad, curl, Coriolis, KE,
   co2contra at sbp21 and sbp42, and the co2contra / contra2co pair of
-  co2contra_c_sbp*_new): the GPU operators on the reference test's fields at
-  N=32, nz=3 reproduce the printed values to their 7 digits;
+  co2contra_c_sbp*_new, and gradient_a2_ecs with its ECS_O halo): the GPU
+  operators on the reference test's fields at N=32, nz=3 reproduce the
+  printed values to their 7 digits;
 * each single operator, the fused and the unfused apply and the RK4 step
   against the oracle on a seeded balanced flow (FP64: 1e-12 on states and
   single operators; 1e-10 on tendencies, which carry the cancellation of
@@ -132,6 +133,22 @@ def gpu_golden(kind, order):
             ex, ey = ut.download() - tu, vt.download() - tv
             mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
             lx, ly = lx + l2sq(od, "u", ex), ly + l2sq(od, "v", ey)
+        out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
+    elif kind == "grad_a2_ecs":
+        # test_grad for gradient_a2_ecs on the A grid's cell centres
+        mx = my = lx = ly = 0.0
+        x, y, z = od.points("p")
+        r = np.stack([x, y, z], -1)
+        b = od.bases("p")
+        for lev in range(3):
+            f = od.scalar_test_field("xyz", lev, "p")
+            W = np.eye(3)[lev] - r[..., lev:lev + 1] * r
+            tx, ty = np.sum(W * b["a1"], -1), np.sum(W * b["a2"], -1)
+            gx, gy = field(op, "p"), field(op, "p")
+            op.calc_grad_a2_ecs(gx, gy, field(op, "p", f))
+            ex, ey = gx.download() - tx, gy.download() - ty
+            mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
+            lx, ly = lx + l2sq(od, "p", ex), ly + l2sq(od, "p", ey)
         out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
     elif kind == "contra2co":
         # test_contra2co: transform2co of co2contra_c_sbp*_new
@@ -410,3 +427,41 @@ def test_c_grid_argument_errors():
     import ctypes
     f = ctypes.c_void_p()
     assert op._L.swm_field_create_mesh(op._h, 7, ctypes.byref(f)) == swm._abi.SWM_E_INVALID
+
+
+@pytest.mark.parametrize("hw", [1, 2])
+def test_ecs_o_halo_and_grad_a2_ecs_match_oracle(hw):
+    """The ECS_O halo of a random cell-centre field (every edge row, corner
+    point and in-corner point of width hw) and gradient_a2_ecs against the
+    oracle."""
+    N = 40
+    op, od = c_op(N, 42), oracle.OracleCDomain(N, 42)
+    f = np.random.default_rng(hw).standard_normal(od.shapes["p"])
+    fp = field(op, "p", f)
+    E, Eo = op.ecs_o_halo(fp, hw), od.ecs_o_halo(f, hw)
+    assert E.shape == (6, N + 2 * hw, N + 2 * hw)
+    assert np.abs(E - Eo).max() <= 1e-14 * np.abs(Eo).max()
+    gx, gy = field(op, "p"), field(op, "p")
+    op.calc_grad_a2_ecs(gx, gy, fp)
+    gxo, gyo = od.grad_a2_ecs(f)
+    assert _rel(gx.download(), gxo) < 1e-13 and _rel(gy.download(), gyo) < 1e-13
+
+
+def test_ecs_o_argument_errors():
+    """Width outside 1..2, a field off the centre mesh and the Ah grid are
+    refused."""
+    op = c_op(24, 42)
+    with pytest.raises(swm.SwmError) as e:
+        op.ecs_o_halo(field(op, "p"), 3)
+    assert e.value.code == swm._abi.SWM_E_INVALID
+    with pytest.raises(swm.SwmError) as e:
+        op.ecs_o_halo(field(op, "u"), 1)
+    assert e.value.code == swm._abi.SWM_E_INVALID
+    with pytest.raises(swm.SwmError) as e:
+        op.calc_grad_a2_ecs(field(op, "u"), field(op, "p"), field(op, "p"))
+    assert e.value.code == swm._abi.SWM_E_INVALID
+    aop = swm.OperatorSWM(swm.ModelConfig(N=24))
+    f = aop.create_field()
+    with pytest.raises(swm.SwmError) as e:
+        aop.calc_grad_a2_ecs(f, f, f)
+    assert e.value.code == swm._abi.SWM_E_UNSUPPORTED

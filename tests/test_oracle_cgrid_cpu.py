@@ -158,3 +158,59 @@ def test_model_step_with_hyperdiffusion(order):
     assert np.all(np.isfinite(h1)) and np.all(np.isfinite(u1)) and np.all(np.isfinite(v1))
     assert np.abs(h1 - h).max() < 0.01 * (h.max() - h.min())
     assert abs(d.mass(h1) - m0) / m0 < (1e-13 if order == 21 else 1e-7)
+
+
+# ------------------------------------------------------------------- ECS_O
+# The interpolating ECS_O halo of the cell centres (equiang_cs/ecs_halo_mod.f90
+# :95-475).  Its width-1 form is pinned by gradient_a2_ecs's known answer
+# (test_oracle_golden.py); the reference's own halo test prints its errors
+# without known answers, so the width-2 form is checked here against the
+# exact field at the virtual points.
+
+def _extended_points(N, hw):
+    """Cartesian points of the extended panel grid lines, (6, W, W, 3)."""
+    import math
+    hx = 0.5 * math.pi / N
+    a = -0.25 * math.pi + hx * (np.arange(1 - hw, N + hw + 1) - 0.5)
+    ta, tb = np.tan(a)[None, :], np.tan(a)[:, None]
+    sg = np.sqrt(1 + ta * ta + tb * tb)
+    one = np.ones_like(sg)
+    rp = np.stack([ta * one / sg, tb * one / sg, one / sg], -1)
+    return (rp[None, ..., 0:1] * initial._EX[:, None, None, :] + rp[None, ..., 1:2] * initial._EY[:, None, None, :]
+            - rp[None, ..., 2:3] * initial._EN[:, None, None, :])
+
+
+@pytest.mark.parametrize("hw", [1, 2])
+def test_ecs_o_halo_is_fourth_order(hw):
+    """Edge rows, the points next to each cube corner and the points inside
+    it all converge at fourth order to the exact field (errors fall by more
+    than 12x per doubling of N); the interior is the field itself."""
+    errs = []
+    for N in (24, 48):
+        od = oracle.OracleCDomain(N, 42, radius=1.0)
+        r = _extended_points(N, hw)
+        e = 0.0
+        for lev in range(3):
+            f = od.scalar_test_field("xyz", lev, "p")
+            E = od.ecs_o_halo(f, hw)
+            assert np.array_equal(E[:, hw:hw + N, hw:hw + N], f.reshape(6, N, N))
+            e = max(e, float(np.abs(E - r[..., lev]).max()))
+        errs.append(e)
+    assert errs[0] < 3e-6 and errs[1] < errs[0] / 12.0, errs
+
+
+def test_grad_a2_ecs_is_second_order():
+    """gradient_a2_ecs converges at second order to the exact covariant
+    gradient of x on the unit sphere."""
+    errs = []
+    for N in (24, 48):
+        od = oracle.OracleCDomain(N, 42, radius=1.0)
+        f = od.scalar_test_field("xyz", 0, "p")
+        gx, gy = od.grad_a2_ecs(f)
+        x, y, z = od.points("p")
+        r = np.stack([x, y, z], -1)
+        W = np.array([1.0, 0.0, 0.0]) - r[..., 0:1] * r
+        b = od.bases("p")
+        tx, ty = np.sum(W * b["a1"], -1), np.sum(W * b["a2"], -1)
+        errs.append(max(np.abs(gx - tx).max(), np.abs(gy - ty).max()))
+    assert errs[1] < errs[0] / 3.5, errs
