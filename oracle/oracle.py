@@ -113,6 +113,9 @@ def lib():
         L.orcc_ecs_o_halo.argtypes = [vp, _D, ctypes.c_int, _D]
         L.orcc_ecs_o_halo.restype = ctypes.c_int
         L.orcc_grad_a2_ecs.argtypes = [vp, _D, _D, _D]
+        L.orcc_ecs_a_vec_halo.argtypes = [vp, _D, _D, ctypes.c_int, _D, _D]
+        L.orcc_ecs_a_vec_halo.restype = ctypes.c_int
+        L.orcc_div_a2_ecs.argtypes = [vp, _D, _D, _D]
         L.orcc_contra2co.argtypes = [vp, _D, _D, _D, _D]
         L.orcc_hordiff.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double] + [_D] * 6
         L.orcc_model_step.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -419,6 +422,21 @@ class OracleCDomain:
         lib().orcc_grad_a2_ecs(self._h, _p(self._c(f)), _p(gx), _p(gy))
         return gx, gy
 
+    def ecs_a_vec_halo(self, u, v, halo_width=2):
+        """The ecs_A_vec halo of contravariant (u, v) at the cell centres:
+        two (6, N+2hw, N+2hw) arrays laid out as ecs_o_halo."""
+        W = self.N + 2 * int(halo_width)
+        eu, ev = np.zeros((6, W, W)), np.zeros((6, W, W))
+        assert lib().orcc_ecs_a_vec_halo(self._h, _p(self._c(u)), _p(self._c(v)), int(halo_width),
+                                         _p(eu), _p(ev)) == 0
+        return eu, ev
+
+    def div_a2_ecs(self, u, v):
+        """divergence_a2_ecs of contravariant (u, v) at the cell centres."""
+        d = self.zeros("p")
+        lib().orcc_div_a2_ecs(self._h, _p(self._c(u)), _p(self._c(v)), _p(d))
+        return d
+
     def contra2co(self, ut, vt):
         u, v = self.zeros("u"), self.zeros("v")
         lib().orcc_contra2co(self._h, _p(self._c(ut)), _p(self._c(vt)), _p(u), _p(v))
@@ -472,11 +490,11 @@ def golden_c(kind: str, N: int = 32, sbp_order: int = 42) -> np.ndarray:
     contra2co (the transform2co of co2contra_c_sbp*_new), or grad_a2_ecs
     (gradient_a2_ecs on the A grid's cell centres, with the ECS_O halo)."""
     k = {"div": 0, "grad": 1, "curl": 2, "coriolis": 3, "ke": 4, "co2contra": 5, "contra2co": 6,
-         "grad_a2_ecs": 7}[kind]
+         "grad_a2_ecs": 7, "div_a2_ecs": 8}[kind]
     out = np.zeros(4)
     if lib().orcc_golden(k, int(N), int(sbp_order), _p(out)) != 0:
         raise ValueError(f"oracle C-grid golden {kind} failed for order {sbp_order}")
-    return out[:4] if kind in ("div", "curl", "ke") else out[:2]
+    return out[:4] if kind in ("div", "curl", "ke", "div_a2_ecs") else out[:2]
 
 
 def golden(kind: str, N: int = 32, sbp_order: int = 42):

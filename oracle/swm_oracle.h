@@ -179,6 +179,11 @@ void orcc_model_step(const orcc_domain* d, const double* hs, double* h, double* 
  * gradient at the cell centres (the A grid's points). */
 int orcc_ecs_o_halo(const orcc_domain* d, const double* f, int halo_width, double* ext);
 void orcc_grad_a2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy);
+/* The ecs_A_vec halo of contravariant (u, v) at the cell centres (width 1 or
+ * 2, the same layout as orcc_ecs_o_halo) and divergence_a2_ecs. */
+int orcc_ecs_a_vec_halo(const orcc_domain* d, const double* u, const double* v, int halo_width,
+                        double* eu, double* ev);
+void orcc_div_a2_ecs(const orcc_domain* d, const double* u, const double* v, double* out);
 double orcc_mass(const orcc_domain* d, int mesh, const double* f);
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
 /* Analytic test fields on the C meshes: vector kinds 0 solid rotation (axis
@@ -191,7 +196,8 @@ int orcc_scalar_test_field(const orcc_domain* d, int kind, int level, int mesh,
                            double* f);
 /* Known-answer tests on the C grid at (N, nz=3, unit sphere): kind 0 div (4
  * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2),
- * 6 contra2co of co2contra_c_sbp*_new (2), 7 gradient_a2_ecs (2).
+ * 6 contra2co of co2contra_c_sbp*_new (2), 7 gradient_a2_ecs (2), 8
+ * divergence_a2_ecs (4).
  * Returns 0, or -1 for an unknown kind / order. */
 int orcc_golden(int kind, int N, int sbp_order, double* out);
 

@@ -230,12 +230,15 @@ struct orcc_domain {
   double hx = 0.0, scale = 1.0, grav = 9.80616, omega = 1.0, axis[3] = {0, 0, 1};
   Mesh m[4];               // p, u, v, q
   Halo ho, hu, hv, hq;     // scalar on p, C vector u / v, scalar on q
+  Halo hau, hav;           // A vector (both components on p): u / v
   Ops ops;    // the operators of the model's SBP order
   Ops ops21;  // the 2/1 operators of the C-grid hyperdiffusion
   std::vector<double> Ac, Ai;
   // ECS_O halo: cubic weights [row 0..1][position -1..N+2][4] and stencil bases
   std::vector<double> ecs_w;
-  std::vector<int> ecs_ind;  // quadrature edge weights at centres / interfaces
+  std::vector<int> ecs_ind;
+  // ecs_A_vec: the 2x2 maps [edge 0..3][depth 1..kDepth][position 1..N][4]
+  std::vector<double> ecs_tm;  // quadrature edge weights at centres / interfaces
 };
 
 namespace {
@@ -757,15 +760,16 @@ bool build_ecs_weights(orcc_domain& d) {
 // formulas of ecs_halo_1corner on the exchanged values.  No formula reads the
 // exchange's corner regions, which the one-tile-per-panel exchange leaves
 // unfilled.
-void ecs_o_panel(const orcc_domain& d, const double* f, int p, int hw, double* E) {
-  const Mesh& P = d.m[0];
+// X(i1, j1) gives the exchanged value at a halo point (and the field inside
+// the panel); the vector halo passes its edge-transformed components.
+template <class Xf>
+void ecs_o_panel_x(const orcc_domain& d, Xf X, int hw, double* E) {
   const int N = d.N, W = N + 2 * hw, ni = N + 4;
-  auto X = [&](int i1, int j1) { return ext(P, d.ho, f, nullptr, p, i1 - 1, j1 - 1); };
   auto out = [&](int i1, int j1) -> double& { return E[(size_t)(j1 - 1 + hw) * W + (i1 - 1 + hw)]; };
   auto w = [&](int m, int i, int r) { return d.ecs_w[((size_t)(r - 1) * ni + (i + 1)) * 4 + (m + 1)]; };
   auto ind = [&](int i, int r) { return d.ecs_ind[(size_t)(r - 1) * ni + (i + 1)]; };
   for (int j = 1; j <= N; ++j)
-    for (int i = 1; i <= N; ++i) out(i, j) = f[P.at(p, i - 1, j - 1)];
+    for (int i = 1; i <= N; ++i) out(i, j) = X(i, j);
   // corners first, from the exchanged values (ecs_halo_corners)
   const int ist[4] = {0, N + 1, N + 1, 0}, idr[4] = {1, -1, -1, 1};
   const int jst[4] = {0, 0, N + 1, N + 1}, jdr[4] = {1, 1, -1, -1};
@@ -827,6 +831,11 @@ void ecs_o_panel(const orcc_domain& d, const double* f, int p, int hw, double* E
     for (int k = 0; k < (hw > 1 ? 6 : 3); ++k) out(ist[c] + idr[c] * ci[k], jst[c] + jdr[c] * cj[k]) = cs[c][k];
 }
 
+void ecs_o_panel(const orcc_domain& d, const double* f, int p, int hw, double* E) {
+  const Mesh& P = d.m[0];
+  ecs_o_panel_x(d, [&](int i1, int j1) { return ext(P, d.ho, f, nullptr, p, i1 - 1, j1 - 1); }, hw, E);
+}
+
 // gradient_a2_ecs (gradient/grad_a2_mod.f90:19-69 with grad_factory_mod.f90:
 // 105-121): the ECS_O halo of width 1, then central differences of the cell
 // values, gx = 0.5 (f(i+1) - f(i-1)) / (hx a), covariant, at the centres.
@@ -844,6 +853,93 @@ void grad_a2_ecs(const orcc_domain& d, const double* f, double* gx, double* gy) 
         gx[P.at(p, i, j)] = 0.5 * (e(ii + 1, jj) - e(ii - 1, jj)) / (d.hx * d.scale);
         gy[P.at(p, i, j)] = 0.5 * (e(ii, jj + 1) - e(ii, jj - 1)) / (d.hx * d.scale);
       }
+  }
+}
+
+// ---------------------------------------------------------------- ecs_A_vec
+// The maps of the A-grid vector halo (equiang_cs/ecs_halo_vec_a_factory_mod.f90
+// :108-170, init_transform_matrix): at position i and depth j of edge e
+// (bottom, top, left, right), the neighbour's exchanged contravariant
+// components (already turned to this panel's axes by the exchange) live at the
+// neighbour's point (alpha_s, beta_s); rotated into this panel's frame, its
+// basis vectors a1s, a2s are projected on this panel's extended dual basis
+// b1t, b2t at the same point: TM = [a1s.b1t, a2s.b1t; a1s.b2t, a2s.b2t].
+void build_ecs_tm(orcc_domain& d) {
+  const int N = d.N;
+  d.ecs_tm.assign((size_t)4 * kDepth * N * 4, 0.0);
+  const int ab_shift[4] = {0, 0, 1, 1}, b_sign[4] = {1, -1, 1, -1};
+  auto rot = [](int e, const double v[3], double o[3]) {
+    switch (e) {
+      case 0: o[0] = v[0]; o[1] = -v[2]; o[2] = v[1]; break;
+      case 1: o[0] = v[0]; o[1] = v[2]; o[2] = -v[1]; break;
+      case 2: o[0] = -v[2]; o[1] = v[1]; o[2] = v[0]; break;
+      default: o[0] = v[2]; o[1] = v[1]; o[2] = -v[0]; break;
+    }
+  };
+  auto dot = [](const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  for (int e = 0; e < 4; ++e)
+    for (int j = 1; j <= kDepth; ++j)
+      for (int i = 1; i <= N; ++i) {
+        const double al = -0.25 * PI + (i - 0.5) * d.hx;
+        const double be = b_sign[e] * (0.25 * PI - (j - 0.5) * d.hx);
+        const double as = ab_shift[e] ? be : al, bs = ab_shift[e] ? al : be;
+        double v[3], a1s[3], a2s[3], r[3], b1t[3], b2t[3];
+        a1_proto(as, bs, v); rot(e, v, a1s);
+        a2_proto(as, bs, v); rot(e, v, a2s);
+        r_proto(as, bs, v); rot(e, v, r);
+        const double at = std::atan(r[0] / r[2]), bt = std::atan(r[1] / r[2]);
+        b1_proto(at, bt, b1t);
+        b2_proto(at, bt, b2t);
+        double* T = &d.ecs_tm[(((size_t)e * kDepth + (j - 1)) * N + (i - 1)) * 4];
+        T[0] = dot(a1s, b1t); T[1] = dot(a2s, b1t); T[2] = dot(a1s, b2t); T[3] = dot(a2s, b2t);
+      }
+}
+
+// The ecs_A_vec halo of width hw (ecs_halo_vec_a_mod.f90:34-158): the 'full'
+// vector exchange, the maps TM on the exchanged rows, then the ECS_O
+// interpolation of each component.  Contravariant components at the centres.
+void ecs_a_vec_panel(const orcc_domain& d, const double* u, const double* v, int p, int hw, double* Eu, double* Ev) {
+  const Mesh& P = d.m[0];
+  const int N = d.N;
+  auto XV = [&](int c, int i1, int j1) -> double {
+    if (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) return (c == 0 ? u : v)[P.at(p, i1 - 1, j1 - 1)];
+    int e, dd, pos;
+    if (j1 < 1) { e = 0; dd = 1 - j1; pos = i1; }
+    else if (j1 > N) { e = 1; dd = j1 - N; pos = i1; }
+    else if (i1 < 1) { e = 2; dd = 1 - i1; pos = j1; }
+    else { e = 3; dd = i1 - N; pos = j1; }
+    const double eu = ext(P, d.hau, u, v, p, i1 - 1, j1 - 1), ev = ext(P, d.hav, v, u, p, i1 - 1, j1 - 1);
+    const double* T = &d.ecs_tm[(((size_t)e * kDepth + (dd - 1)) * N + (pos - 1)) * 4];
+    return c == 0 ? T[0] * eu + T[1] * ev : T[2] * eu + T[3] * ev;
+  };
+  ecs_o_panel_x(d, [&](int i1, int j1) { return XV(0, i1, j1); }, hw, Eu);
+  ecs_o_panel_x(d, [&](int i1, int j1) { return XV(1, i1, j1); }, hw, Ev);
+}
+
+// divergence_a2_ecs (divergence/div_a2_mod.f90:19-72 with div_factory_mod.f90:
+// 90-112): the ecs_A_vec halo of width 1, then the central difference of J u^i
+// over 2 J hx a, J on the extended grid lines beyond the edges.
+void div_a2_ecs(const orcc_domain& d, const double* u, const double* v, double* out) {
+  const Mesh& P = d.m[0];
+  const int N = d.N, hw = 1, W = N + 2;
+  auto Jx = [&](int i1, int j1) {
+    const double al = -0.25 * PI + ((i1 - 1) + 0.5) * d.hx, be = -0.25 * PI + ((j1 - 1) + 0.5) * d.hx;
+    const double ta = std::tan(al), tb = std::tan(be);
+    const double sg = std::sqrt(1.0 + ta * ta + tb * tb);
+    return (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
+  };
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (int p = 0; p < 6; ++p) {
+    std::vector<double> Eu((size_t)W * W, 0.0), Ev((size_t)W * W, 0.0);
+    ecs_a_vec_panel(d, u, v, p, hw, Eu.data(), Ev.data());
+    auto eu = [&](int i1, int j1) { return Eu[(size_t)j1 * W + i1]; };  // 0-based extended = 1-based + 0
+    auto ev = [&](int i1, int j1) { return Ev[(size_t)j1 * W + i1]; };
+    for (int j1 = 1; j1 <= N; ++j1)
+      for (int i1 = 1; i1 <= N; ++i1)
+        out[P.at(p, i1 - 1, j1 - 1)] =
+            (Jx(i1 + 1, j1) * eu(i1 + 1, j1) - Jx(i1 - 1, j1) * eu(i1 - 1, j1) + Jx(i1, j1 + 1) * ev(i1, j1 + 1) -
+             Jx(i1, j1 - 1) * ev(i1, j1 - 1)) /
+            (2.0 * Jx(i1, j1) * d.hx * d.scale);
   }
 }
 
@@ -1006,6 +1102,9 @@ orcc_domain* create(int N, int order, double radius, double grav, double omega, 
     delete d;
     return nullptr;
   }
+  d->hau = build_halo(d->m[0], d->m[0], 1);
+  d->hav = build_halo(d->m[0], d->m[0], 2);
+  build_ecs_tm(*d);
   d->ops21.order = 21;
   d->ops21.Wc2i = make_stag(W21_C2I); d->ops21.Wi2c = make_stag(W21_I2C);
   d->ops21.Dc2i = make_stag(D21_C2I); d->ops21.Di2c = make_stag(D21_I2C);
@@ -1096,6 +1195,14 @@ int orcc_ecs_o_halo(const orcc_domain* d, const double* f, int halo_width, doubl
   return 0;
 }
 void orcc_grad_a2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy) { grad_a2_ecs(*d, f, gx, gy); }
+int orcc_ecs_a_vec_halo(const orcc_domain* d, const double* u, const double* v, int halo_width, double* eu,
+                        double* ev) {
+  if (halo_width < 1 || halo_width > 2) return -1;
+  const size_t W = (size_t)d->N + 2 * halo_width;
+  for (int p = 0; p < 6; ++p) ecs_a_vec_panel(*d, u, v, p, halo_width, eu + p * W * W, ev + p * W * W);
+  return 0;
+}
+void orcc_div_a2_ecs(const orcc_domain* d, const double* u, const double* v, double* out) { div_a2_ecs(*d, u, v, out); }
 double orcc_mass(const orcc_domain* d, int mesh, const double* f) { return mass(*d, mesh, f); }
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f) {
   return std::sqrt(l2sq(d->m[mesh], d->hx, f));
@@ -1297,6 +1404,36 @@ int orcc_golden(int kind, int N, int order, double* out) {
       }
       out[0] = maxabs(allx) + maxabs(ally);
       out[1] = std::sqrt(l2x) + std::sqrt(l2y);
+      break;
+    }
+    case 8: {  // divergence_a2_ecs of the contravariant solid rotation and cross-polar flow at the centres
+      std::vector<double> ua(P.size()), va(P.size()), dv(P.size());
+      auto setp = [&](auto gen) {
+        for (int k = 0; k < P.size(); ++k) {
+          double W3[3];
+          gen(P.rx[k], P.ry[k], P.rz[k], W3);
+          const double* b1 = &P.b1[3 * k];
+          const double* b2 = &P.b2[3 * k];
+          ua[k] = W3[0] * b1[0] + W3[1] * b1[1] + W3[2] * b1[2];
+          va[k] = W3[0] * b2[0] + W3[1] * b2[1] + W3[2] * b2[2];
+        }
+      };
+      for (int fld = 0; fld < 2; ++fld) {
+        all.clear(); l2 = 0.0;
+        for (int lev = 0; lev < 3; ++lev) {
+          if (fld == 0) setp([lev](double x, double y, double z, double w[3]) { field_solid_rotation(lev, x, y, z, w); });
+          else setp(field_cross_polar);
+          div_a2_ecs(*d, ua.data(), va.data(), dv.data());
+          std::vector<double> e(P.size());
+          for (int k = 0; k < P.size(); ++k) {
+            e[k] = d->scale * dv[k];
+            if (fld == 1) e[k] = e[k] - 1.0 * field_cross_polar_div(P.rx[k], P.ry[k], P.rz[k]);
+          }
+          all.insert(all.end(), e.begin(), e.end());
+          l2 += l2sq(P, d->hx, e.data());
+        }
+        out[2 * fld] = maxabs(all); out[2 * fld + 1] = std::sqrt(l2);
+      }
       break;
     }
     case 7: {  // gradient_a2_ecs of x, y, z on the cell centres (the A grid's points)

@@ -11,8 +11,8 @@ with the line number of the reference file it came from.  The C-grid file
 keeps the SBP operators of the &shallow_water_model_c family (div, grad,
 curl, Coriolis, KE and co2contra at sbp21 and sbp42) and the co2contra /
 contra2co pair of co2contra_c_sbp*_new that the C-grid hyperdiffusion's curl
-part uses, and gradient_a2_ecs, whose only halo is the interpolating ECS_O
-halo of the cell centres.  The
+part uses, and gradient_a2_ecs and divergence_a2_ecs, whose halos are the
+interpolating ECS_O and ecs_A_vec halos of the cell centres.  The
 values were printed by the reference test with format "(A,4E15.7)", i.e. to
 7 significant digits, from test_diffops_all.f90 at N=32, nz=3.
 """
@@ -46,6 +46,8 @@ KEEP_C = {
     # the A grid's central-difference gradient on the cell centres, which pins
     # the ECS_O halo (the sbp_order entry only selects the oracle domain)
     "gradient_a2_ecs": ("grad_a2_ecs", 42),
+    # the A grid's divergence, which pins the ecs_A_vec halo
+    "divergence_a2_ecs": ("div_a2_ecs", 42),
 }
 
 

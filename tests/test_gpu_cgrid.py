@@ -23,6 +23,7 @@ import pytest
 import cubedsphere_sbp_swm_gb300 as swm
 import oracle
 from cubedsphere_sbp_swm_gb300 import initial
+from analytic_fields import cross_polar as _cross_polar, vsh_curl_free_10 as _vsh_curl_free_10
 from gpu_helpers import fmt7
 
 pytestmark = pytest.mark.gpu
@@ -163,27 +164,6 @@ def gpu_golden(kind, order):
             lx, ly = lx + l2sq(od, "u", ex), ly + l2sq(od, "v", ey)
         out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
     return out
-
-
-def _cross_polar(r):
-    # cross_polar_flow_generator (test_fields_mod.f90), unit sphere
-    x, y, z = r[..., 0], r[..., 1], r[..., 2]
-    r2 = x * x + y * y + z * z
-    cphi, sphi = np.sqrt((x * x + y * y) / r2), z / np.sqrt(r2)
-    rho = np.maximum(np.sqrt(x * x + y * y), np.float32(1e-14))
-    clam, slam = x / rho, np.where(x * x + y * y == 0.0, 1.0, y / rho)
-    u = sphi * (sphi * sphi - 3.0 * cphi * cphi) * slam - 0.5 * cphi
-    w = sphi * sphi * clam
-    return np.stack([-slam * u - sphi * clam * w, clam * u - sphi * slam * w, cphi * w], -1)
-
-
-def _vsh_curl_free_10(r):
-    x, y, z = r[..., 0], r[..., 1], r[..., 2]
-    lam = np.arctan2(y, x)
-    phi = np.arctan2(z, np.sqrt(x * x + y * y))
-    lam = lam + np.pi * (1.0 - np.where(lam >= 0.0, 1.0, -1.0))
-    vp = -np.cos(phi)
-    return np.stack([-np.sin(phi) * np.cos(lam) * vp, -np.sin(phi) * np.sin(lam) * vp, np.cos(phi) * vp], -1)
 
 
 @pytest.mark.parametrize("entry", GOLDEN_C, ids=lambda g: g["name"])

@@ -214,3 +214,50 @@ def test_grad_a2_ecs_is_second_order():
         tx, ty = np.sum(W * b["a1"], -1), np.sum(W * b["a2"], -1)
         errs.append(max(np.abs(gx - tx).max(), np.abs(gy - ty).max()))
     assert errs[1] < errs[0] / 3.5, errs
+
+
+def _extended_duals(N, hw):
+    """Points and dual basis vectors b1, b2 of the extended panel grid lines."""
+    r = _extended_points(N, hw)
+    import math
+    hx = 0.5 * math.pi / N
+    a = -0.25 * math.pi + hx * (np.arange(1 - hw, N + hw + 1) - 0.5)
+    ta, tb = np.tan(a)[None, :], np.tan(a)[:, None]
+    p15 = (1 + ta * ta + tb * tb) ** 1.5
+    one = np.ones_like(p15)
+    a1p = np.stack([(1 + ta * ta) * (1 + tb * tb) / p15, -ta * tb * (1 + ta * ta) / p15,
+                    -ta * (1 + ta * ta) * one / p15], -1)
+    a2p = np.stack([-ta * tb * (1 + tb * tb) / p15, (1 + ta * ta) * (1 + tb * tb) / p15,
+                    -tb * (1 + tb * tb) * one / p15], -1)
+
+    def face(v):
+        return (v[None, ..., 0:1] * initial._EX[:, None, None, :] + v[None, ..., 1:2] * initial._EY[:, None, None, :]
+                - v[None, ..., 2:3] * initial._EN[:, None, None, :])
+
+    a1, a2 = face(a1p), face(a2p)
+    g11, g12, g22 = (a1 * a1).sum(-1), (a1 * a2).sum(-1), (a2 * a2).sum(-1)
+    det = g11 * g22 - g12 * g12
+    b1 = (g22[..., None] * a1 - g12[..., None] * a2) / det[..., None]
+    b2 = (-g12[..., None] * a1 + g11[..., None] * a2) / det[..., None]
+    return r, b1, b2
+
+
+@pytest.mark.parametrize("hw", [1, 2])
+def test_ecs_a_vec_halo_is_fourth_order(hw):
+    """The ecs_A_vec halo of the contravariant cross-polar flow against its
+    exact contravariant components on the extended grid lines: fourth-order
+    convergence, interior untouched."""
+    from analytic_fields import cross_polar as _cross_polar
+    errs = []
+    for N in (24, 48):
+        od = oracle.OracleCDomain(N, 42, radius=1.0)
+        r, b1, b2 = _extended_duals(N, hw)
+        Vx = _cross_polar(r)
+        x, y, z = od.points("p")
+        b = od.bases("p")
+        Vp = _cross_polar(np.stack([x, y, z], -1))
+        u, v = np.sum(Vp * b["b1"], -1), np.sum(Vp * b["b2"], -1)
+        eu, ev = od.ecs_a_vec_halo(u, v, hw)
+        assert np.array_equal(eu[:, hw:hw + N, hw:hw + N], u.reshape(6, N, N))
+        errs.append(max(np.abs(eu - np.sum(Vx * b1, -1)).max(), np.abs(ev - np.sum(Vx * b2, -1)).max()))
+    assert errs[0] < 1e-4 and errs[1] < errs[0] / 12.0, errs
