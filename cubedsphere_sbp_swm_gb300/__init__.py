@@ -286,6 +286,19 @@ class OperatorSWM:
         self._check(self._L.swm_halo_ecs_o(self._h, f._h, int(halo_width), _ptr(out)))
         return out
 
+    def calc_div_a2_ecs(self, div, u, v):
+        """divergence_a2_ecs on the cell centres (C grid): contravariant u, v
+        and div on mesh p."""
+        self._check(self._L.swm_op_div_a2_ecs(self._h, div._h, u._h, v._h))
+
+    def ecs_a_vec_halo(self, u, v, halo_width: int = 2):
+        """The ecs_A_vec halo of contravariant (u, v) on the cell centres (C
+        grid): two extended-tile arrays laid out as ecs_o_halo's."""
+        W = self.N + 2 * int(halo_width)
+        eu, ev = np.empty((6, W, W)), np.empty((6, W, W))
+        self._check(self._L.swm_halo_ecs_a_vec(self._h, u._h, v._h, int(halo_width), _ptr(eu), _ptr(ev)))
+        return eu, ev
+
     def quadrature_mass(self, f) -> float:
         out = ctypes.c_double()
         self._check(self._L.swm_quadrature_mass(self._h, f._h, ctypes.byref(out)))

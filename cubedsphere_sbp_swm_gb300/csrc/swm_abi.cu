@@ -2026,6 +2026,26 @@ int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext
   CK(cgrid_ecs_o_halo(ctx->cg, f->p, halo_width, ext, ctx->st), "ECS_O halo");
   return SWM_OK;
 }
+int swm_op_div_a2_ecs(swm_ctx* ctx, swm_field* div, const swm_field* u, const swm_field* v) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "divergence_a2_ecs needs the cell-centre mesh of the C grid");
+  CHECK_FIELDS(div, u, v);
+  for (const swm_field* x : {(const swm_field*)div, u, v})
+    if (int rc = check_mesh(ctx, x, SWM_MESH_P, "divergence_a2_ecs")) return rc;
+  if (div == u || div == v) return fail(ctx, SWM_E_INVALID, "divergence_a2_ecs needs an output distinct from its inputs");
+  CK(cgrid_div_a2_ecs(ctx->cg, u->p, v->p, div->p, ctx->st), "divergence_a2_ecs");
+  return SWM_OK;
+}
+int swm_halo_ecs_a_vec(swm_ctx* ctx, const swm_field* u, const swm_field* v, int halo_width, double* ext_u,
+                       double* ext_v) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "the ecs_A_vec halo needs the cell-centre mesh of the C grid");
+  CHECK_FIELDS(u, v);
+  for (const swm_field* x : {u, v})
+    if (int rc = check_mesh(ctx, x, SWM_MESH_P, "ecs_A_vec halo")) return rc;
+  if (halo_width < 1 || halo_width > 2) return fail(ctx, SWM_E_INVALID, "ecs_A_vec halo width must be 1 or 2");
+  if (!ext_u || !ext_v) return fail(ctx, SWM_E_INVALID, "null output");
+  CK(cgrid_ecs_a_vec_halo(ctx->cg, u->p, v->p, halo_width, ext_u, ext_v, ctx->st), "ecs_A_vec halo");
+  return SWM_OK;
+}
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f) {
   CHECK_FIELDS(f);
   // on the C grid the corner mesh is the one with duplicated edge points

@@ -184,6 +184,10 @@ struct CArgsT {
   const double* ecs_w;
   const int* ecs_ind;
   double hxa;
+  // ecs_A_vec: the maps [edge][depth][position][4]; J on the first ring
+  // beyond each edge [edge][position] (bottom, top, left, right)
+  const double* ecs_tm;
+  const double* ecs_jr;
   // inputs
   const T *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
   // intermediate and unfused outputs
@@ -487,11 +491,12 @@ __device__ __forceinline__ double ecs_wt(const CArgsT<double>& a, int m, int i, 
 // (N+1,N+1), 4 at (0,N+1)) from ecs_halo_1corner (ecs_halo_mod.f90:179-260):
 // k = 0..5 at the corner-relative points (0,1), (1,0), (0,0), (-1,0), (0,-1),
 // (-1,-1), the last three for width 2 only.
-__device__ double ecs_corner(const CArgsT<double>& a, const double* f, int p, int c, int k) {
+template <class XF>
+__device__ double ecs_corner(const CArgsT<double>& a, XF X, int c, int k) {
   const int N = a.N;
   const int ist = (c == 1 || c == 2) ? N + 1 : 0, jst = c >= 2 ? N + 1 : 0;
   const int idr = (c == 1 || c == 2) ? -1 : 1, jdr = c >= 2 ? -1 : 1;
-  auto fc = [&](int i, int j) { return ecs_x(a, f, p, ist + idr * i, jst + jdr * j); };
+  auto fc = [&](int i, int j) { return X(ist + idr * i, jst + jdr * j); };
   // the weights of corner 1, mirrored for the corners at i = N+1
   auto pw = [&](int m, int i, int r) { return idr == 1 ? ecs_wt(a, m, i, r) : ecs_wt(a, 1 - m, N + 1 - i, r); };
   const double zw = pw(-1, 1, 1), zw2 = zw * zw, zw3 = zw2 * zw;
@@ -524,8 +529,11 @@ __device__ double ecs_corner(const CArgsT<double>& a, const double* f, int p, in
 
 // The ECS_O value at the halo point (i1, j1) of a halo of width hw (1 or 2):
 // a corner value where the point is one of its corner's special points, else
-// the cubic interpolation along the edge (ecs_ext_halo_1e) of row r.
-__device__ double ecs_o_at(const CArgsT<double>& a, const double* f, int p, int i1, int j1, int hw) {
+// the cubic interpolation along the edge (ecs_ext_halo_1e) of row r.  X(i1,
+// j1) gives the exchanged values (the vector halo passes its mapped
+// components).
+template <class XF>
+__device__ double ecs_o_at_x(const CArgsT<double>& a, XF X, int i1, int j1, int hw) {
   const int N = a.N;
   const int ci[6] = {0, 1, 0, -1, 0, -1}, cj[6] = {1, 0, 0, 0, -1, -1};
   for (int c = 0; c < 4; ++c) {
@@ -533,7 +541,7 @@ __device__ double ecs_o_at(const CArgsT<double>& a, const double* f, int p, int 
     const int idr = (c == 1 || c == 2) ? -1 : 1, jdr = c >= 2 ? -1 : 1;
     const int ri = idr * (i1 - ist), rj = jdr * (j1 - jst);
     for (int k = 0; k < (hw > 1 ? 6 : 3); ++k)
-      if (ri == ci[k] && rj == cj[k]) return ecs_corner(a, f, p, c, k);
+      if (ri == ci[k] && rj == cj[k]) return ecs_corner(a, X, c, k);
   }
   int r, pos;
   bool along_i;
@@ -542,12 +550,41 @@ __device__ double ecs_o_at(const CArgsT<double>& a, const double* f, int p, int 
   else if (i1 < 1) { r = 1 - i1; pos = j1; along_i = false; }
   else { r = i1 - N; pos = j1; along_i = false; }
   const int b = __ldg(&a.ecs_ind[(r - 1) * (N + 4) + (pos + 1)]);
-  auto G = [&](int k) { return along_i ? ecs_x(a, f, p, k, j1) : ecs_x(a, f, p, i1, k); };
+  auto G = [&](int k) { return along_i ? X(k, j1) : X(i1, k); };
   double s = ecs_wt(a, -1, pos, r) * G(b - 1);
   s = s + ecs_wt(a, 0, pos, r) * G(b);
   s = s + ecs_wt(a, 1, pos, r) * G(b + 1);
   s = s + ecs_wt(a, 2, pos, r) * G(b + 2);
   return s;
+}
+
+__device__ __forceinline__ double ecs_o_at(const CArgsT<double>& a, const double* f, int p, int i1, int j1, int hw) {
+  return ecs_o_at_x(a, [&](int x, int y) { return ecs_x(a, f, p, x, y); }, i1, j1, hw);
+}
+
+// The A-grid vector halo's exchanged component c (0 u, 1 v) at (i1, j1): the
+// 'full' vector exchange (the neighbour's components turned to this panel's
+// axes, tables 4 and 5), then the map TM of its edge, depth and position
+// (ecs_halo_vec_a_mod.f90:55-156).  Contravariant components.
+__device__ __forceinline__ double ecs_vx(const CArgsT<double>& a, const double* u, const double* v, int p, int c,
+                                         int i1, int j1) {
+  const int N = a.N;
+  if (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) return (c == 0 ? u : v)[at(a.g, p, i1 - 1, j1 - 1)];
+  int e, d, k;
+  if (j1 < 1) { e = 0; d = 1 - j1; k = i1; }
+  else if (j1 > N) { e = 1; d = j1 - N; k = i1; }
+  else if (i1 < 1) { e = 2; d = 1 - i1; k = j1; }
+  else { e = 3; d = i1 - N; k = j1; }
+  const int side = e == 0 ? 2 : e == 1 ? 3 : e == 2 ? 0 : 1;
+  const double eu = halo_at(a, 4, side, p, d, k - 1, u, v);
+  const double ev = halo_at(a, 5, side, p, d, k - 1, v, u);
+  const double* T = a.ecs_tm + (((e * kHaloDepth) + (d - 1)) * N + (k - 1)) * 4;
+  return c == 0 ? __ldg(T) * eu + __ldg(T + 1) * ev : __ldg(T + 2) * eu + __ldg(T + 3) * ev;
+}
+
+__device__ __forceinline__ double ecs_v_at(const CArgsT<double>& a, const double* u, const double* v, int p, int c,
+                                           int i1, int j1, int hw) {
+  return ecs_o_at_x(a, [&](int x, int y) { return ecs_vx(a, u, v, p, c, x, y); }, i1, j1, hw);
 }
 
 // gradient_a2_ecs (gradient/grad_a2_mod.f90:19-69): the central difference of
@@ -576,6 +613,39 @@ __global__ void __launch_bounds__(256) ecs_ext_kernel(const __grid_constant__ CA
   const double v = (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) ? f[at(a.g, p, i1 - 1, j1 - 1)]
                                                               : ecs_o_at(a, f, p, i1, j1, hw);
   ext[((long long)p * W + j) * W + i] = v;
+}
+
+// divergence_a2_ecs (divergence/div_a2_mod.f90:19-72): the ecs_A_vec halo of
+// width 1, then (J u(i+1) - J u(i-1) + J v(j+1) - J v(j-1)) / (2 J hx a) with
+// J on the extended grid lines beyond the edges.
+__global__ void __launch_bounds__(256) div_a2_kernel(const __grid_constant__ CArgsT<double> a) {
+  const int N = a.N;
+  SWM_C_INDEX(N, N)
+  const double *u = a.u, *v = a.v;
+  const int i1 = i + 1, j1 = j + 1;
+  auto in = [&](int x, int y) { return x >= 1 && x <= N && y >= 1 && y <= N; };
+  auto J = [&](int x, int y) {
+    if (in(x, y)) return a.Jp[at(a.g, p, x - 1, y - 1)];
+    const int e = y < 1 ? 0 : y > N ? 1 : x < 1 ? 2 : 3;
+    return __ldg(&a.ecs_jr[e * N + ((e < 2 ? x : y) - 1)]);
+  };
+  auto U = [&](int x, int y) { return in(x, y) ? u[at(a.g, p, x - 1, y - 1)] : ecs_v_at(a, u, v, p, 0, x, y, 1); };
+  auto V = [&](int x, int y) { return in(x, y) ? v[at(a.g, p, x - 1, y - 1)] : ecs_v_at(a, u, v, p, 1, x, y, 1); };
+  a.o1[at(a.g, p, i, j)] = (J(i1 + 1, j1) * U(i1 + 1, j1) - J(i1 - 1, j1) * U(i1 - 1, j1) +
+                            J(i1, j1 + 1) * V(i1, j1 + 1) - J(i1, j1 - 1) * V(i1, j1 - 1)) /
+                           (2.0 * J(i1, j1) * a.hxa);
+}
+
+// The extended tiles of the ecs_A_vec halo of width hw (both components).
+__global__ void __launch_bounds__(256) ecs_vec_ext_kernel(const __grid_constant__ CArgsT<double> a, int hw,
+                                                          double* eu, double* ev) {
+  const int N = a.N, W = N + 2 * hw;
+  SWM_C_INDEX(W, W)
+  const int i1 = i + 1 - hw, j1 = j + 1 - hw;
+  const bool in = i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N;
+  const long long o = ((long long)p * W + j) * W + i;
+  eu[o] = in ? a.u[at(a.g, p, i1 - 1, j1 - 1)] : ecs_v_at(a, a.u, a.v, p, 0, i1, j1, hw);
+  ev[o] = in ? a.v[at(a.g, p, i1 - 1, j1 - 1)] : ecs_v_at(a, a.u, a.v, p, 1, i1, j1, hw);
 }
 
 // Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
@@ -838,7 +908,9 @@ struct CGrid {
   int* halo = nullptr;
   double* ecs_w = nullptr;  // ECS_O weights [2][N+4][4]
   int* ecs_ind = nullptr;   // ECS_O stencil bases [2][N+4]
-  double* ext = nullptr;    // extended tiles of swm_halo_ecs_o (allocated on first use)
+  double* ecs_tm = nullptr;  // ecs_A_vec maps [4][kHaloDepth][N][4]
+  double* ecs_jr = nullptr;  // J on the first ring beyond each edge [4][N]
+  double* ext = nullptr;    // extended tiles of the halo entry points (allocated on first use)
   int ext_hw = 0;
   double* wts = nullptr;   // quadrature weights: centres (N), interfaces (N+1)
   double* part = nullptr;  // kMassBlocks partial sums
@@ -876,6 +948,7 @@ CArgsT<T> base_args(const CGrid* c, int ord = 0) {
   a.rJqha = M(M_RJQHA); a.rJuha = M(M_RJUHA); a.rJvha = M(M_RJVHA);
   a.halo = c->halo;
   a.ecs_w = c->ecs_w; a.ecs_ind = c->ecs_ind; a.hxa = c->hx * c->radius;
+  a.ecs_tm = c->ecs_tm; a.ecs_jr = c->ecs_jr;
   a.Ap = Wk(W_AP); a.Bp = Wk(W_BP); a.ut = Wk(W_UT); a.vt = Wk(W_VT);
   a.hu = Wk(W_HU); a.hv = Wk(W_HV); a.Gu = Wk(W_GU); a.Gv = Wk(W_GV);
   a.KEu = Wk(W_KEU); a.KEv = Wk(W_KEV); a.curl = Wk(W_CURL);
@@ -971,10 +1044,13 @@ double coriolis_at(int p, double al, double be, double omega, const double ax[3]
 // with the receiving mesh's point counts, so the duplicated edge faces of u
 // (v) fill the first x (y) layer and the duplicated edge points of q its
 // first layers.
-constexpr int kHaloMeshes = 4;
+// Tables 4 and 5 are the u and v components of an A-grid vector, both on the
+// centres (the 'full' vector exchange of create_o_points_halo_exchange, with
+// the same component swap and signs).
+constexpr int kHaloMeshes = 6;
 bool build_halo(int N, const FieldGeom& g, std::vector<int>& tab, std::string& why) {
   const int L = N + 1;
-  const int dims[kHaloMeshes][2] = {{N, N}, {N + 1, N}, {N, N + 1}, {N + 1, N + 1}};
+  const int dims[kHaloMeshes][2] = {{N, N}, {N + 1, N}, {N, N + 1}, {N + 1, N + 1}, {N, N}, {N, N}};
   tab.assign((size_t)kHaloMeshes * 4 * 6 * kHaloDepth * L, -1);
   for (int T = 0; T < kHaloMeshes; ++T) {
     const int nx = dims[T][0], ny = dims[T][1];
@@ -983,11 +1059,12 @@ bool build_halo(int N, const FieldGeom& g, std::vector<int>& tab, std::string& w
         if (q == p) continue;
         int istep, jstep, dim_i;
         cube::orientation(p, q, istep, jstep, dim_i);  // (receiver, sender)
-        const bool swap = (T == 1 || T == 2) && !dim_i;
-        const int S = swap ? 3 - T : T;
+        const bool vec = T == 1 || T == 2 || T == 4 || T == 5;
+        const bool first = T == 1 || T == 4;  // the u component
+        const bool swap = vec && !dim_i;
+        const int S = !swap ? T : T == 1 ? 2 : T == 2 ? 1 : T == 4 ? 5 : 4;
         int sign = 1;
-        if (T == 1) sign = dim_i ? istep : jstep;
-        if (T == 2) sign = dim_i ? jstep : istep;
+        if (vec) sign = first ? (dim_i ? istep : jstep) : (dim_i ? jstep : istep);
         const int snx = dims[S][0], sny = dims[S][1];
         for (int js = 1; js <= sny; ++js)
           for (int is = 1; is <= snx; ++is) {
@@ -1162,6 +1239,74 @@ bool build_ecs_weights(int N, double hx, std::vector<double>& w, std::vector<int
   return true;
 }
 
+// The equiangular gnomonic map on the prototype face: the point r = (X, Y,
+// 1) / sigma with X = tan(alpha), Y = tan(beta), sigma^2 = 1 + X^2 + Y^2, the
+// covariant basis a1 = dr/dalpha, a2 = dr/dbeta and the contravariant basis
+// b1, b2 from the inverse metric (the same geometry as ecs_metric_mod.f90:
+// 326-478).
+struct EcsFrame {
+  double r[3], a1[3], a2[3], b1[3], b2[3];
+};
+EcsFrame ecs_frame(double al, double be) {
+  const double X = std::tan(al), Y = std::tan(be);
+  const double s2 = 1.0 + X * X + Y * Y, sg = std::sqrt(s2), s3 = s2 * sg;
+  const double ca = (1.0 + X * X) / s3, cb = (1.0 + Y * Y) / s3;
+  const double qi1 = s2 / (1.0 + X * X), qi2 = s2 * X * Y / ((1.0 + X * X) * (1.0 + Y * Y)), qi3 = s2 / (1.0 + Y * Y);
+  EcsFrame f;
+  const double r[3] = {X / sg, Y / sg, 1.0 / sg};
+  const double a1[3] = {ca * (1.0 + Y * Y), -ca * X * Y, -ca * X};
+  const double a2[3] = {-cb * X * Y, cb * (1.0 + X * X), -cb * Y};
+  for (int k = 0; k < 3; ++k) {
+    f.r[k] = r[k]; f.a1[k] = a1[k]; f.a2[k] = a2[k];
+    f.b1[k] = qi1 * a1[k] + qi2 * a2[k];
+    f.b2[k] = qi2 * a1[k] + qi3 * a2[k];
+  }
+  return f;
+}
+
+// The maps of the A-grid vector halo (ecs_halo_vec_a_factory_mod.f90:108-170):
+// for edge e (bottom, top, left, right), depth d and position i, the
+// neighbour's point in the canonical placement across that edge (a rotation
+// of the prototype face about a coordinate axis), its covariant basis turned
+// into this face's frame, projected on this face's contravariant basis at the
+// same point of the extended grid.  Also J on the first ring beyond each edge.
+void build_ecs_vec_tables(int N, double hx, std::vector<double>& tm, std::vector<double>& jr) {
+  tm.assign((size_t)4 * kHaloDepth * N * 4, 0.0);
+  jr.assign((size_t)4 * N, 0.0);
+  const int ab_shift[4] = {0, 0, 1, 1}, b_sign[4] = {1, -1, 1, -1};
+  auto rot = [](int e, const double* v, double* o) {
+    switch (e) {
+      case 0: o[0] = v[0]; o[1] = -v[2]; o[2] = v[1]; break;   // about x, edge 1
+      case 1: o[0] = v[0]; o[1] = v[2]; o[2] = -v[1]; break;   // about x, edge 2
+      case 2: o[0] = -v[2]; o[1] = v[1]; o[2] = v[0]; break;   // about y, edge 3
+      default: o[0] = v[2]; o[1] = v[1]; o[2] = -v[0]; break;  // about y, edge 4
+    }
+  };
+  auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  for (int e = 0; e < 4; ++e)
+    for (int d = 1; d <= kHaloDepth; ++d)
+      for (int i = 1; i <= N; ++i) {
+        const double al = -0.25 * kPiC + (i - 0.5) * hx;
+        const double be = b_sign[e] * (0.25 * kPiC - (d - 0.5) * hx);
+        const EcsFrame S = ab_shift[e] ? ecs_frame(be, al) : ecs_frame(al, be);
+        double a1s[3], a2s[3], r[3];
+        rot(e, S.a1, a1s);
+        rot(e, S.a2, a2s);
+        rot(e, S.r, r);
+        const EcsFrame T = ecs_frame(std::atan(r[0] / r[2]), std::atan(r[1] / r[2]));
+        double* q = &tm[(((size_t)e * kHaloDepth + (d - 1)) * N + (i - 1)) * 4];
+        q[0] = dot(a1s, T.b1); q[1] = dot(a2s, T.b1); q[2] = dot(a1s, T.b2); q[3] = dot(a2s, T.b2);
+      }
+  for (int k = 1; k <= N; ++k) {
+    const double in = -0.25 * kPiC + ((k - 1) + 0.5) * hx;
+    const double lo = -0.25 * kPiC + (-1 + 0.5) * hx, hi = -0.25 * kPiC + (N + 0.5) * hx;
+    jr[0 * N + (k - 1)] = metric_at(in, lo).J;
+    jr[1 * N + (k - 1)] = metric_at(in, hi).J;
+    jr[2 * N + (k - 1)] = metric_at(lo, in).J;
+    jr[3 * N + (k - 1)] = metric_at(hi, in).J;
+  }
+}
+
 }  // namespace
 
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
@@ -1184,6 +1329,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   std::vector<double> ew;
   std::vector<int> eind;
   if (!build_ecs_weights(N, c->hx, ew, eind)) { why = "ECS_O halo stencils leave the panel"; delete c; return 1; }
+  std::vector<double> etm, ejr;
+  build_ecs_vec_tables(N, c->hx, etm, ejr);
   std::vector<double> w(2 * (size_t)N + 1, 1.0);
   {
     // SBP_C42 / SBP_C21 edge weights (D42_A_centers / _interfaces, D21_*)
@@ -1208,6 +1355,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   ok(cudaMalloc(&c->halo, sizeof(int) * tab.size()));
   ok(cudaMalloc(&c->ecs_w, sizeof(double) * ew.size()));
   ok(cudaMalloc(&c->ecs_ind, sizeof(int) * eind.size()));
+  ok(cudaMalloc(&c->ecs_tm, sizeof(double) * etm.size()));
+  ok(cudaMalloc(&c->ecs_jr, sizeof(double) * ejr.size()));
   ok(cudaMalloc(&c->wts, sizeof(double) * w.size()));
   ok(cudaMalloc(&c->part, sizeof(double) * kMassBlocks));
   if (e == cudaSuccess) {
@@ -1251,6 +1400,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->ecs_w, ew.data(), sizeof(double) * ew.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->ecs_ind, eind.data(), sizeof(int) * eind.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->ecs_tm, etm.data(), sizeof(double) * etm.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->ecs_jr, ejr.data(), sizeof(double) * ejr.size(), cudaMemcpyHostToDevice, st));
     if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
       ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
     ok(cudaMemcpyAsync(c->wts, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st));
@@ -1268,7 +1419,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
 void cgrid_destroy(CGrid* c) {
   if (!c) return;
   for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->dw, (void*)c->halo,
-                  (void*)c->ecs_w, (void*)c->ecs_ind, (void*)c->ext, (void*)c->wts, (void*)c->part})
+                  (void*)c->ecs_w, (void*)c->ecs_ind, (void*)c->ecs_tm, (void*)c->ecs_jr, (void*)c->ext,
+                  (void*)c->wts, (void*)c->part})
     if (p) cudaFree(p);
   for (cudaStream_t s : c->bs)
     if (s) cudaStreamDestroy(s);
@@ -1488,25 +1640,53 @@ cudaError_t cgrid_grad_a2_ecs(CGrid* c, const double* f, double* gx, double* gy,
   return cudaGetLastError();
 }
 
+// Scratch for the extended tiles of two fields of the widest halo asked for
+// (the halo entry points are synchronous).
+cudaError_t ext_scratch(CGrid* c, int halo_width, cudaStream_t st) {
+  if (c->ext_hw >= halo_width) return cudaSuccess;
+  const int W = c->N + 2 * halo_width;
+  CKE(cudaStreamSynchronize(st));
+  if (c->ext) cudaFree(c->ext);
+  c->ext = nullptr;
+  c->ext_hw = 0;
+  CKE(cudaMalloc(&c->ext, sizeof(double) * 2 * 6 * (size_t)W * W));
+  c->ext_hw = halo_width;
+  return cudaSuccess;
+}
+
 cudaError_t cgrid_ecs_o_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st) {
   if (halo_width < 1 || halo_width > 2) return cudaErrorInvalidValue;
   const int W = c->N + 2 * halo_width;
   const size_t bytes = sizeof(double) * 6 * (size_t)W * W;
-  if (c->ext_hw < halo_width) {
-    // the scratch of the widest halo asked for (a synchronous call)
-    CKE(cudaStreamSynchronize(st));
-    if (c->ext) cudaFree(c->ext);
-    c->ext = nullptr;
-    c->ext_hw = 0;
-    CKE(cudaMalloc(&c->ext, bytes));
-    c->ext_hw = halo_width;
-  }
+  CKE(ext_scratch(c, halo_width, st));
   CArgsT<double> a = base_args<double>(c);
   a.ke_in = f;
   ecs_ext_kernel<<<grid_for(W, W), kBlock, 0, st>>>(a, halo_width, c->ext);
   CKE(cudaGetLastError());
   CKE(cudaMemcpyAsync(ext_host, c->ext, bytes, cudaMemcpyDeviceToHost, st));
   return cudaStreamSynchronize(st);
+}
+
+cudaError_t cgrid_ecs_a_vec_halo(CGrid* c, const double* u, const double* v, int halo_width, double* eu_host,
+                                 double* ev_host, cudaStream_t st) {
+  if (halo_width < 1 || halo_width > 2) return cudaErrorInvalidValue;
+  const int W = c->N + 2 * halo_width;
+  const size_t n = 6 * (size_t)W * W;
+  CKE(ext_scratch(c, halo_width, st));
+  CArgsT<double> a = base_args<double>(c);
+  a.u = u; a.v = v;
+  ecs_vec_ext_kernel<<<grid_for(W, W), kBlock, 0, st>>>(a, halo_width, c->ext, c->ext + n);
+  CKE(cudaGetLastError());
+  CKE(cudaMemcpyAsync(eu_host, c->ext, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  CKE(cudaMemcpyAsync(ev_host, c->ext + n, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  return cudaStreamSynchronize(st);
+}
+
+cudaError_t cgrid_div_a2_ecs(CGrid* c, const double* u, const double* v, double* div, cudaStream_t st) {
+  CArgsT<double> a = base_args<double>(c);
+  a.u = u; a.v = v; a.o1 = div;
+  div_a2_kernel<<<grid_for(c->N, c->N), kBlock, 0, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st) {

@@ -102,6 +102,12 @@ cudaError_t cgrid_diffusion_step32(CGrid* c, const Topology& tp, float* edge, in
 // into host memory, synchronously.
 cudaError_t cgrid_grad_a2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st);
 cudaError_t cgrid_ecs_o_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st);
+// The ecs_A_vec halo of contravariant (u, v) on the centres (equiang_cs/
+// ecs_halo_vec_a_mod.f90:34-158) into two host arrays laid out as above, and
+// divergence_a2_ecs (divergence/div_a2_mod.f90:19-72).
+cudaError_t cgrid_ecs_a_vec_halo(CGrid* c, const double* u, const double* v, int halo_width, double* eu_host,
+                                 double* ev_host, cudaStream_t st);
+cudaError_t cgrid_div_a2_ecs(CGrid* c, const double* u, const double* v, double* div, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

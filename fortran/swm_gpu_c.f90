@@ -280,6 +280,16 @@ interface
         integer(c_int), value :: halo_width
         real(c_double), intent(out) :: ext(*)
     end function swm_halo_ecs_o
+    integer(c_int) function swm_op_div_a2_ecs(ctx, div, u, v) bind(c, name="swm_op_div_a2_ecs")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, div, u, v
+    end function swm_op_div_a2_ecs
+    integer(c_int) function swm_halo_ecs_a_vec(ctx, u, v, halo_width, ext_u, ext_v) bind(c, name="swm_halo_ecs_a_vec")
+        import :: c_int, c_ptr, c_double
+        type(c_ptr), value :: ctx, u, v
+        integer(c_int), value :: halo_width
+        real(c_double), intent(out) :: ext_u(*), ext_v(*)
+    end function swm_halo_ecs_a_vec
     integer(c_int) function swm_sync_scalar(ctx, f) bind(c, name="swm_sync_scalar")
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, f

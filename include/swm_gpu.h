@@ -292,6 +292,16 @@ int swm_op_grad_a2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy,
                        const swm_field* f);
 int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width,
                    double* ext);
+/* The same for A-grid vectors (contravariant u, v on the cell centres): the
+ * ecs_A_vec halo (halo_vec_t%get_halo_vector for "ecs_A_vec",
+ * equiang_cs/ecs_halo_vec_a_mod.f90:34-158 with the maps of
+ * ecs_halo_vec_a_factory_mod.f90:108-170; both extended tiles, laid out as
+ * swm_halo_ecs_o's) and divergence_a2_ecs (divergence/div_a2_mod.f90:19-72:
+ * the J-weighted central difference with that halo). */
+int swm_op_div_a2_ecs(swm_ctx* ctx, swm_field* div, const swm_field* u,
+                      const swm_field* v);
+int swm_halo_ecs_a_vec(swm_ctx* ctx, const swm_field* u, const swm_field* v,
+                       int halo_width, double* ext_u, double* ext_v);
 /* halo_t%get_halo_scalar for "Ah_scalar_sync"
  * (halo/halo_Ah_scalar_sync_mod.f90:20-93) */
 int swm_sync_scalar(swm_ctx* ctx, swm_field* f);

@@ -23,3 +23,10 @@ def vsh_curl_free_10(r):
     lam = lam + np.pi * (1.0 - np.where(lam >= 0.0, 1.0, -1.0))
     vp = -np.cos(phi)
     return np.stack([-np.sin(phi) * np.cos(lam) * vp, -np.sin(phi) * np.sin(lam) * vp, np.cos(phi) * vp], -1)
+
+
+def solid_rotation(r, level):
+    """solid_rotation_field_generator: the rotation about the coordinate
+    axis of the level (x, y, z for levels 0, 1, 2), axis x r."""
+    ax = np.eye(3)[level]
+    return np.cross(np.broadcast_to(ax, r.shape), r)

@@ -23,7 +23,8 @@ import pytest
 import cubedsphere_sbp_swm_gb300 as swm
 import oracle
 from cubedsphere_sbp_swm_gb300 import initial
-from analytic_fields import cross_polar as _cross_polar, vsh_curl_free_10 as _vsh_curl_free_10
+from analytic_fields import cross_polar as _cross_polar, solid_rotation as _solid_rotation
+from analytic_fields import vsh_curl_free_10 as _vsh_curl_free_10
 from gpu_helpers import fmt7
 
 pytestmark = pytest.mark.gpu
@@ -151,6 +152,23 @@ def gpu_golden(kind, order):
             mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
             lx, ly = lx + l2sq(od, "p", ex), ly + l2sq(od, "p", ey)
         out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
+    elif kind == "div_a2_ecs":
+        # test_div for divergence_a2_ecs on the A grid's cell centres
+        x, y, z = od.points("p")
+        r = np.stack([x, y, z], -1)
+        b = od.bases("p")
+        for fld in ("solid_rotation", "cross_polar"):
+            m, l2 = 0.0, 0.0
+            for lev in range(3):
+                V = _solid_rotation(r, lev) if fld == "solid_rotation" else _cross_polar(r)
+                uu, vv = np.sum(V * b["b1"], -1), np.sum(V * b["b2"], -1)
+                d = field(op, "p")
+                op.calc_div_a2_ecs(d, field(op, "p", uu), field(op, "p", vv))
+                e = d.download()
+                if fld == "cross_polar":
+                    e = e - od.scalar_test_field("cross_polar_div", 0, "p")
+                m, l2 = max(m, np.abs(e).max()), l2 + l2sq(od, "p", e)
+            out += [m, np.sqrt(l2)]
     elif kind == "contra2co":
         # test_contra2co: transform2co of co2contra_c_sbp*_new
         mx = my = lx = ly = 0.0
@@ -445,3 +463,22 @@ def test_ecs_o_argument_errors():
     with pytest.raises(swm.SwmError) as e:
         aop.calc_grad_a2_ecs(f, f, f)
     assert e.value.code == swm._abi.SWM_E_UNSUPPORTED
+
+
+@pytest.mark.parametrize("hw", [1, 2])
+def test_ecs_a_vec_halo_and_div_a2_ecs_match_oracle(hw):
+    """The ecs_A_vec halo of random contravariant components (every halo
+    point of width hw, through the vector exchange, the edge maps and the
+    ECS_O interpolation) and divergence_a2_ecs against the oracle."""
+    N = 40
+    op, od = c_op(N, 42), oracle.OracleCDomain(N, 42)
+    rng = np.random.default_rng(10 + hw)
+    u, v = rng.standard_normal(od.shapes["p"]), rng.standard_normal(od.shapes["p"])
+    fu, fv = field(op, "p", u), field(op, "p", v)
+    eu, ev = op.ecs_a_vec_halo(fu, fv, hw)
+    eo_u, eo_v = od.ecs_a_vec_halo(u, v, hw)
+    assert np.abs(eu - eo_u).max() <= 1e-14 * np.abs(eo_u).max()
+    assert np.abs(ev - eo_v).max() <= 1e-14 * np.abs(eo_v).max()
+    d = field(op, "p")
+    op.calc_div_a2_ecs(d, fu, fv)
+    assert _rel(d.download(), od.div_a2_ecs(u, v)) < 1e-13
