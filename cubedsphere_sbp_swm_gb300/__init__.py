@@ -286,6 +286,10 @@ class OperatorSWM:
         self._check(self._L.swm_halo_ecs_o(self._h, f._h, int(halo_width), _ptr(out)))
         return out
 
+    def calc_grad_c2_ecs(self, gx, gy, f):
+        """gradient_c2_ecs (C grid): f on mesh p, gx on u, gy on v."""
+        self._check(self._L.swm_op_grad_c2_ecs(self._h, gx._h, gy._h, f._h))
+
     def calc_div_a2_ecs(self, div, u, v):
         """divergence_a2_ecs on the cell centres (C grid): contravariant u, v
         and div on mesh p."""

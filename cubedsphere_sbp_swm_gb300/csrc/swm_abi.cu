@@ -2026,6 +2026,15 @@ int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext
   CK(cgrid_ecs_o_halo(ctx->cg, f->p, halo_width, ext, ctx->st), "ECS_O halo");
   return SWM_OK;
 }
+int swm_op_grad_c2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy, const swm_field* f) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "gradient_c2_ecs is provided on the C grid only");
+  CHECK_FIELDS(gx, gy, f);
+  for (auto fm : {std::make_pair((const swm_field*)gx, SWM_MESH_U), std::make_pair((const swm_field*)gy, SWM_MESH_V),
+                  std::make_pair(f, SWM_MESH_P)})
+    if (int rc = check_mesh(ctx, fm.first, fm.second, "gradient_c2_ecs")) return rc;
+  CK(cgrid_grad_c2_ecs(ctx->cg, f->p, gx->p, gy->p, ctx->st), "gradient_c2_ecs");
+  return SWM_OK;
+}
 int swm_op_div_a2_ecs(swm_ctx* ctx, swm_field* div, const swm_field* u, const swm_field* v) {
   if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "divergence_a2_ecs needs the cell-centre mesh of the C grid");
   CHECK_FIELDS(div, u, v);

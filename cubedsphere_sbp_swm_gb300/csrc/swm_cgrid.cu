@@ -602,6 +602,21 @@ __global__ void __launch_bounds__(256) grad_a2_kernel(const __grid_constant__ CA
   a.o2[e] = 0.5 * (E(i1, j1 + 1) - E(i1, j1 - 1)) / a.hxa;
 }
 
+// gradient_c2_ecs (gradient/grad_c2_ecs_mod.f90:95-144): the first
+// differences of the cell values onto the faces, with the ECS_O halo of width
+// 1 beyond the panel edges; gx on the x-faces, gy on the y-faces.
+__global__ void __launch_bounds__(256) grad_c2_kernel(const __grid_constant__ CArgsT<double> a) {
+  const int N = a.N;
+  SWM_C_INDEX(N + 1, N + 1)
+  const double* f = a.ke_in;
+  auto E = [&](int i1, int j1) {
+    return (i1 >= 1 && i1 <= N && j1 >= 1 && j1 <= N) ? f[at(a.g, p, i1 - 1, j1 - 1)] : ecs_o_at(a, f, p, i1, j1, 1);
+  };
+  const int i1 = i + 1, j1 = j + 1, e = at(a.g, p, i, j);
+  if (j < N) a.o1[e] = (E(i1, j1) - E(i1 - 1, j1)) / a.hxa;
+  if (i < N) a.o2[e] = (E(i1, j1) - E(i1, j1 - 1)) / a.hxa;
+}
+
 // The extended tiles of the ECS_O halo of width hw: ext[p][j][i] for the
 // 1-based (i - hw + 1, j - hw + 1), width N + 2 hw.
 __global__ void __launch_bounds__(256) ecs_ext_kernel(const __grid_constant__ CArgsT<double> a, int hw,
@@ -1680,6 +1695,13 @@ cudaError_t cgrid_ecs_a_vec_halo(CGrid* c, const double* u, const double* v, int
   CKE(cudaMemcpyAsync(eu_host, c->ext, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   CKE(cudaMemcpyAsync(ev_host, c->ext + n, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   return cudaStreamSynchronize(st);
+}
+
+cudaError_t cgrid_grad_c2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st) {
+  CArgsT<double> a = base_args<double>(c);
+  a.ke_in = f; a.o1 = gx; a.o2 = gy;
+  grad_c2_kernel<<<grid_for(c->N + 1, c->N + 1), kBlock, 0, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t cgrid_div_a2_ecs(CGrid* c, const double* u, const double* v, double* div, cudaStream_t st) {

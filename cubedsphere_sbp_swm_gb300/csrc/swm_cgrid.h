@@ -108,6 +108,9 @@ cudaError_t cgrid_ecs_o_halo(CGrid* c, const double* f, int halo_width, double* 
 cudaError_t cgrid_ecs_a_vec_halo(CGrid* c, const double* u, const double* v, int halo_width, double* eu_host,
                                  double* ev_host, cudaStream_t st);
 cudaError_t cgrid_div_a2_ecs(CGrid* c, const double* u, const double* v, double* div, cudaStream_t st);
+// gradient_c2_ecs (gradient/grad_c2_ecs_mod.f90:33-51, 95-144): f on the
+// centres, gx on the x-faces, gy on the y-faces, with the ECS_O halo.
+cudaError_t cgrid_grad_c2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

@@ -284,6 +284,10 @@ interface
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, div, u, v
     end function swm_op_div_a2_ecs
+    integer(c_int) function swm_op_grad_c2_ecs(ctx, gx, gy, f) bind(c, name="swm_op_grad_c2_ecs")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, gx, gy, f
+    end function swm_op_grad_c2_ecs
     integer(c_int) function swm_halo_ecs_a_vec(ctx, u, v, halo_width, ext_u, ext_v) bind(c, name="swm_halo_ecs_a_vec")
         import :: c_int, c_ptr, c_double
         type(c_ptr), value :: ctx, u, v

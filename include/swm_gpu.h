@@ -300,6 +300,11 @@ int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width,
  * the J-weighted central difference with that halo). */
 int swm_op_div_a2_ecs(swm_ctx* ctx, swm_field* div, const swm_field* u,
                       const swm_field* v);
+/* gradient_c2_ecs (gradient/grad_c2_ecs_mod.f90:33-51, 95-144): the C grid's
+ * second-order gradient with the ECS_O halo; f on mesh p, gx on mesh u, gy on
+ * mesh v.  C grid only. */
+int swm_op_grad_c2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy,
+                       const swm_field* f);
 int swm_halo_ecs_a_vec(swm_ctx* ctx, const swm_field* u, const swm_field* v,
                        int halo_width, double* ext_u, double* ext_v);
 /* halo_t%get_halo_scalar for "Ah_scalar_sync"

@@ -116,6 +116,7 @@ def lib():
         L.orcc_ecs_a_vec_halo.argtypes = [vp, _D, _D, ctypes.c_int, _D, _D]
         L.orcc_ecs_a_vec_halo.restype = ctypes.c_int
         L.orcc_div_a2_ecs.argtypes = [vp, _D, _D, _D]
+        L.orcc_grad_c2_ecs.argtypes = [vp, _D, _D, _D]
         L.orcc_contra2co.argtypes = [vp, _D, _D, _D, _D]
         L.orcc_hordiff.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double] + [_D] * 6
         L.orcc_model_step.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -431,6 +432,12 @@ class OracleCDomain:
                                          _p(eu), _p(ev)) == 0
         return eu, ev
 
+    def grad_c2_ecs(self, f):
+        """gradient_c2_ecs: gx on the x-faces, gy on the y-faces."""
+        gx, gy = self.zeros("u"), self.zeros("v")
+        lib().orcc_grad_c2_ecs(self._h, _p(self._c(f)), _p(gx), _p(gy))
+        return gx, gy
+
     def div_a2_ecs(self, u, v):
         """divergence_a2_ecs of contravariant (u, v) at the cell centres."""
         d = self.zeros("p")
@@ -490,7 +497,7 @@ def golden_c(kind: str, N: int = 32, sbp_order: int = 42) -> np.ndarray:
     contra2co (the transform2co of co2contra_c_sbp*_new), or grad_a2_ecs
     (gradient_a2_ecs on the A grid's cell centres, with the ECS_O halo)."""
     k = {"div": 0, "grad": 1, "curl": 2, "coriolis": 3, "ke": 4, "co2contra": 5, "contra2co": 6,
-         "grad_a2_ecs": 7, "div_a2_ecs": 8}[kind]
+         "grad_a2_ecs": 7, "div_a2_ecs": 8, "grad_c2_ecs": 9}[kind]
     out = np.zeros(4)
     if lib().orcc_golden(k, int(N), int(sbp_order), _p(out)) != 0:
         raise ValueError(f"oracle C-grid golden {kind} failed for order {sbp_order}")

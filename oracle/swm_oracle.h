@@ -184,6 +184,9 @@ void orcc_grad_a2_ecs(const orcc_domain* d, const double* f, double* gx, double*
 int orcc_ecs_a_vec_halo(const orcc_domain* d, const double* u, const double* v, int halo_width,
                         double* eu, double* ev);
 void orcc_div_a2_ecs(const orcc_domain* d, const double* u, const double* v, double* out);
+/* gradient_c2_ecs: the ECS_O halo of width 1, then first differences of the
+ * cell values onto the faces (gx on mesh u, gy on mesh v). */
+void orcc_grad_c2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy);
 double orcc_mass(const orcc_domain* d, int mesh, const double* f);
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
 /* Analytic test fields on the C meshes: vector kinds 0 solid rotation (axis
@@ -197,7 +200,7 @@ int orcc_scalar_test_field(const orcc_domain* d, int kind, int level, int mesh,
 /* Known-answer tests on the C grid at (N, nz=3, unit sphere): kind 0 div (4
  * values), 1 grad (2), 2 curl (4), 3 Coriolis (2), 4 KE (4), 5 co2contra (2),
  * 6 contra2co of co2contra_c_sbp*_new (2), 7 gradient_a2_ecs (2), 8
- * divergence_a2_ecs (4).
+ * divergence_a2_ecs (4), 9 gradient_c2_ecs (2).
  * Returns 0, or -1 for an unknown kind / order. */
 int orcc_golden(int kind, int N, int sbp_order, double* out);
 

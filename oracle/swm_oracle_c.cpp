@@ -856,6 +856,25 @@ void grad_a2_ecs(const orcc_domain& d, const double* f, double* gx, double* gy) 
   }
 }
 
+// gradient_c2_ecs (gradient/grad_c2_ecs_mod.f90:33-51, 95-144 with
+// grad_factory_mod.f90:44-57): the ECS_O halo of width 1, then the first
+// differences of the cell values onto the faces, gx = (f(i) - f(i-1)) / (hx a)
+// on the x-faces, gy likewise on the y-faces; covariant.
+void grad_c2_ecs(const orcc_domain& d, const double* f, double* gx, double* gy) {
+  const Mesh &U = d.m[1], &V = d.m[2];
+  const int N = d.N, W = N + 2;
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (int p = 0; p < 6; ++p) {
+    std::vector<double> E((size_t)W * W, 0.0);
+    ecs_o_panel(d, f, p, 1, E.data());
+    auto e = [&](int i1, int j1) { return E[(size_t)j1 * W + i1]; };  // 1-based, hw 1
+    for (int j1 = 1; j1 <= N; ++j1)
+      for (int i1 = 1; i1 <= N + 1; ++i1) gx[U.at(p, i1 - 1, j1 - 1)] = (e(i1, j1) - e(i1 - 1, j1)) / (d.hx * d.scale);
+    for (int j1 = 1; j1 <= N + 1; ++j1)
+      for (int i1 = 1; i1 <= N; ++i1) gy[V.at(p, i1 - 1, j1 - 1)] = (e(i1, j1) - e(i1, j1 - 1)) / (d.hx * d.scale);
+  }
+}
+
 // ---------------------------------------------------------------- ecs_A_vec
 // The maps of the A-grid vector halo (equiang_cs/ecs_halo_vec_a_factory_mod.f90
 // :108-170, init_transform_matrix): at position i and depth j of edge e
@@ -1203,6 +1222,7 @@ int orcc_ecs_a_vec_halo(const orcc_domain* d, const double* u, const double* v, 
   return 0;
 }
 void orcc_div_a2_ecs(const orcc_domain* d, const double* u, const double* v, double* out) { div_a2_ecs(*d, u, v, out); }
+void orcc_grad_c2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy) { grad_c2_ecs(*d, f, gx, gy); }
 double orcc_mass(const orcc_domain* d, int mesh, const double* f) { return mass(*d, mesh, f); }
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f) {
   return std::sqrt(l2sq(d->m[mesh], d->hx, f));
@@ -1397,6 +1417,24 @@ int orcc_golden(int kind, int N, int order, double* out) {
         contra2co(*d, d->ops, ut.data(), vt.data(), c.data(), b.data());
         for (int k = 0; k < U.size(); ++k) c[k] = c[k] + (-1.0) * u[k];
         for (int k = 0; k < V.size(); ++k) b[k] = b[k] + (-1.0) * v[k];
+        allx.insert(allx.end(), c.begin(), c.end());
+        ally.insert(ally.end(), b.begin(), b.end());
+        l2x += l2sq(U, d->hx, c.data());
+        l2y += l2sq(V, d->hx, b.data());
+      }
+      out[0] = maxabs(allx) + maxabs(ally);
+      out[1] = std::sqrt(l2x) + std::sqrt(l2y);
+      break;
+    }
+    case 9: {  // gradient_c2_ecs of x, y, z onto the faces
+      std::vector<double> f(P.size()), tx, ty;
+      for (int lev = 0; lev < 3; ++lev) {
+        for (int k = 0; k < P.size(); ++k) f[k] = field_xyz(lev, P.rx[k], P.ry[k], P.rz[k]);
+        set_vector(*d, [lev](double x, double y, double z, double w[3]) { field_xyz_grad(lev, x, y, z, w); }, false,
+                   tx, ty);
+        grad_c2_ecs(*d, f.data(), c.data(), b.data());
+        for (int k = 0; k < U.size(); ++k) c[k] = d->scale * c[k] - 1.0 * tx[k];
+        for (int k = 0; k < V.size(); ++k) b[k] = d->scale * b[k] - 1.0 * ty[k];
         allx.insert(allx.end(), c.begin(), c.end());
         ally.insert(ally.end(), b.begin(), b.end());
         l2x += l2sq(U, d->hx, c.data());

@@ -48,6 +48,8 @@ KEEP_C = {
     "gradient_a2_ecs": ("grad_a2_ecs", 42),
     # the A grid's divergence, which pins the ecs_A_vec halo
     "divergence_a2_ecs": ("div_a2_ecs", 42),
+    # the C grid's second-order gradient, with the ECS_O halo
+    "gradient_c2_ecs": ("grad_c2_ecs", 42),
 }
 
 

@@ -136,6 +136,17 @@ def gpu_golden(kind, order):
             mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
             lx, ly = lx + l2sq(od, "u", ex), ly + l2sq(od, "v", ey)
         out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
+    elif kind == "grad_c2_ecs":
+        mx = my = lx = ly = 0.0
+        for lev in range(3):
+            f = od.scalar_test_field("xyz", lev, "p")
+            tx, ty = od.vector_test_field("xyz_grad", lev, contravariant=False)
+            gx, gy = field(op, "u"), field(op, "v")
+            op.calc_grad_c2_ecs(gx, gy, field(op, "p", f))
+            ex, ey = gx.download() - tx, gy.download() - ty
+            mx, my = max(mx, np.abs(ex).max()), max(my, np.abs(ey).max())
+            lx, ly = lx + l2sq(od, "u", ex), ly + l2sq(od, "v", ey)
+        out = [mx + my, np.sqrt(lx) + np.sqrt(ly)]
     elif kind == "grad_a2_ecs":
         # test_grad for gradient_a2_ecs on the A grid's cell centres
         mx = my = lx = ly = 0.0
@@ -443,6 +454,10 @@ def test_ecs_o_halo_and_grad_a2_ecs_match_oracle(hw):
     op.calc_grad_a2_ecs(gx, gy, fp)
     gxo, gyo = od.grad_a2_ecs(f)
     assert _rel(gx.download(), gxo) < 1e-13 and _rel(gy.download(), gyo) < 1e-13
+    gu, gv = field(op, "u"), field(op, "v")
+    op.calc_grad_c2_ecs(gu, gv, fp)
+    guo, gvo = od.grad_c2_ecs(f)
+    assert _rel(gu.download(), guo) < 1e-13 and _rel(gv.download(), gvo) < 1e-13
 
 
 def test_ecs_o_argument_errors():
