@@ -1,17 +1,18 @@
 // swm_cgrid.cu -- the C-grid SBP vector-invariant shallow-water operator on
-// the GPU (FP64): metric of the four staggered meshes, cross-halo tables, the
-// five kernels of one right-hand side, the RK4 stage epilogue and the SBP_C
-// quadrature.
+// the GPU (FP64 and the FP32 form): metric of the four staggered meshes,
+// cross-halo tables, the six passes of one right-hand side, the RK4 stage
+// epilogue, the SBP_C quadrature, the hyperdiffusion and the ECS halos of the
+// cell centres.
 //
 // One right-hand side (operator_swm_mod.f90:61-113 with the C-grid operators)
-// is five passes over the panels plus the corner sync of the curl:
+// is six passes over the panels:
 //   centre_a  p points   J Qi12 times the other covariant component
 //                        interpolated to the centres (co2contra, first half)
 //   faces_a   u, v       contravariant components, mass fluxes h*u^i, J*flux
 //                        and the kinetic-energy densities J u u^i / 2
-//   curl      q points   staggered differences + SAT penalties, then the
-//                        Ah-type edge / corner average
-//   w2uv      u          the curl interpolated to the x-faces
+//   curl      q points   staggered differences + SAT penalties
+//   w2uv      u          the curl, with its Ah-type edge / corner average
+//                        taken as it is read, interpolated to the x-faces
 //   centre_b  p points   kinetic energy + g (h + hs), the divergence with its
 //                        SAT penalties (h tendency), the Coriolis terms
 //   faces_b   u, v       gradient with its SAT penalties + the Coriolis term
@@ -168,6 +169,7 @@ enum : int {
   F_SEP = 256,     // centre_b / faces_b: write the operator's own output, not a tendency
   F_WUT = 512,     // faces_a: store the contravariant components (unfused co2contra)
   F_WFLUX = 1024,  // faces_a: store the mass fluxes (unfused massflux; the 2/1 divergence)
+  F_QSYNC = 2048,  // w2uv: the curl is unsynced; average its edge and corner copies as it is read
 };
 
 template <class T>
@@ -204,6 +206,22 @@ struct CArgsT {
 // element offset within a field (fields stay below 2^31 elements)
 __device__ __forceinline__ int at(const FieldGeom& g, int p, int i, int j) {
   return p * (int)g.ps + j * g.P + i;
+}
+
+// sbp_apply for output k of nout outputs over a line read through F(m)
+template <int W, class T, class Fn>
+__device__ __forceinline__ T stag_at_f(const StagOpT<T>& s, Fn F, int nout, int k) {
+  T acc = T(0.0);
+  if (k >= s.ne && k < nout - s.ne) {
+#pragma unroll
+    for (int t = 0; t < W; ++t) acc += s.Qin[t] * F(k + s.inshift + t);
+  } else if (k < s.ne) {
+    for (int m = 0; m < s.last[k]; ++m) acc += s.Ql[k * s.nw + m] * F(m);
+  } else {
+    const int nin = nout - s.dnx, r = nout - 1 - k;
+    for (int m = s.last[r] - 1; m >= 0; --m) acc += (s.rsign * s.Ql[r * s.nw + m]) * F(nin - 1 - m);
+  }
+  return acc;
 }
 
 // sbp_apply for output k of nout outputs over a line f with stride st
@@ -383,13 +401,41 @@ __global__ void __launch_bounds__(256) curl_kernel(const __grid_constant__ CArgs
 // tensor-product interpolations to the centres, x after y and y after x;
 // the 1-D operators act on different indices, so both are the same linear
 // map and one of them is evaluated (the results agree to round-off).
+//
+// With F_QSYNC the curl comes straight from curl_kernel, unsynced, and its
+// edge and corner points are averaged with the neighbours' copies here, as
+// they are read: the Ah-type sync of the corner mesh
+// (halo/halo_Ah_scalar_sync_mod.f90:38-93, in the order of the sync kernel),
+// with the copies from the corner mesh's cross-halo table.  That saves the
+// sync's two launches per stage in the fused step, where this pass is the
+// curl's only reader.
+template <class T>
+__device__ __forceinline__ T curl_synced(const CArgsT<T>& a, int p, int i, int j) {
+  const int N = a.N;
+  const T* c = a.curl_in;
+  const T own = c[at(a.g, p, i, j)];
+  if (i > 0 && i < N && j > 0 && j < N) return own;
+  auto H = [&](int side, int k) { return halo_at(a, 3, side, p, 1, k, c, c); };
+  if (i == 0 && j == 0) return (own + H(0, 0) + H(2, 0)) / T(3.0);
+  if (i == N && j == 0) return (own + H(1, 0) + H(2, N)) / T(3.0);
+  if (i == 0 && j == N) return (own + H(0, N) + H(3, 0)) / T(3.0);
+  if (i == N && j == N) return (own + H(1, N) + H(3, N)) / T(3.0);
+  if (i == 0) return T(0.5) * (H(0, j) + own);
+  if (i == N) return T(0.5) * (own + H(1, j));
+  if (j == 0) return T(0.5) * (own + H(2, i));
+  return T(0.5) * (own + H(3, i));
+}
+
 template <int ORD, class T>
 __global__ void __launch_bounds__(256) w2uv_kernel(const __grid_constant__ CArgsT<T> a) {
   constexpr int W = ORD == 42 ? 4 : 2;
   const int N = a.N;
   SWM_C_INDEX(N + 1, N)
   const FieldGeom& g = a.g;
-  a.fu[at(g, p, i, j)] = stag_at<W, T>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
+  if (a.flags & F_QSYNC)
+    a.fu[at(g, p, i, j)] = stag_at_f<W, T>(a.ops.wi2c, [&](int m) { return curl_synced(a, p, i, m); }, N, j);
+  else
+    a.fu[at(g, p, i, j)] = stag_at<W, T>(a.ops.wi2c, a.curl_in + at(g, p, i, 0), g.P, N, j);
 }
 
 // grad_perp_c_sbp (grad_perp/grad_perp_c_sbp_mod.f90:20-95): the staggered
@@ -999,15 +1045,16 @@ SWM_C_LAUNCH(run_gperp, gperp_kernel, c->N + 1, c->N + 1)
 
 // One right-hand side of the state (h, u, v) with the epilogue of a.mode.
 template <class T>
-cudaError_t rhs(const CGrid* c, const Topology& tp, T* edge, CArgsT<T> a, const T* in, cudaStream_t st) {
+cudaError_t rhs(const CGrid* c, CArgsT<T> a, const T* in, cudaStream_t st) {
   const long long fs = c->g.fs;
   a.h = in; a.u = in + fs; a.v = in + 2 * fs;
   a.flags = F_CO | F_MF | F_G | F_KE | (c->order == 21 ? F_WFLUX : 0);
   CKE(run_centre_a(c, a, st));
   CKE(run_faces_a(c, a, st));
   CKE(run_curl(c, a, st));
-  CKE(launch_sync_scalar_t<T>(c->g, tp, a.curl, edge, st));
+  // the corner sync of the curl rides in w2uv's reads (its only reader here)
   a.curl_in = a.curl;
+  a.flags = F_QSYNC;
   CKE(run_w2uv(c, a, st));
   a.hu_in = a.hu; a.hv_in = a.hv;
   a.flags = F_KE | F_ADDGH | F_DIV | F_COR;
@@ -1523,7 +1570,7 @@ cudaError_t cgrid_apply(CGrid* c, const Topology& tp, double* edge, const double
   a.hs = hs;
   a.mode = 0;
   a.tend = out;
-  return rhs(c, tp, edge, a, in, st);
+  return rhs(c, a, in, st);
 }
 
 cudaError_t cgrid_apply32(CGrid* c, const Topology& tp, float* edge, const float* hs, const float* in, float* out,
@@ -1533,7 +1580,7 @@ cudaError_t cgrid_apply32(CGrid* c, const Topology& tp, float* edge, const float
   a.hs = hs;
   a.mode = 0;
   a.tend = out;
-  return rhs(c, tp, edge, a, in, st);
+  return rhs(c, a, in, st);
 }
 
 // The FP32 form: stage inputs are the state's high part (stage 1) or Y in
@@ -1551,7 +1598,7 @@ cudaError_t cgrid_rk4_32(CGrid* c, const Topology& tp, float* edge, const float*
   a.acc = a.Y + 3 * c->g.fs;
   for (int s = 1; s <= 4; ++s) {
     a.mode = s;
-    CKE(rhs(c, tp, edge, a, s == 1 ? static_cast<const float*>(hi) : a.Y, st));
+    CKE(rhs(c, a, s == 1 ? static_cast<const float*>(hi) : a.Y, st));
   }
   return cudaSuccess;
 }
@@ -1572,7 +1619,7 @@ cudaError_t cgrid_rk4(CGrid* c, const Topology& tp, double* edge, const double* 
   a.acc = c->rk + 6 * c->g.fs;
   for (int s = 1; s <= 4; ++s) {
     a.mode = s;
-    CKE(rhs(c, tp, edge, a, s == 1 ? y0 : a.Y, st));
+    CKE(rhs(c, a, s == 1 ? y0 : a.Y, st));
   }
   return cudaSuccess;
 }
