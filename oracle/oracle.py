@@ -117,6 +117,10 @@ def lib():
         L.orcc_ecs_a_vec_halo.restype = ctypes.c_int
         L.orcc_div_a2_ecs.argtypes = [vp, _D, _D, _D]
         L.orcc_grad_c2_ecs.argtypes = [vp, _D, _D, _D]
+        L.orcc_ecs_xy_halo.argtypes = [vp, _D, ctypes.c_int, _D]
+        L.orcc_ecs_xy_halo.restype = ctypes.c_int
+        L.orcc_laplace_ch.argtypes = [vp, ctypes.c_int, _D, _D]
+        L.orcc_laplace_ch.restype = ctypes.c_int
         L.orcc_contra2co.argtypes = [vp, _D, _D, _D, _D]
         L.orcc_hordiff.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double] + [_D] * 6
         L.orcc_model_step.argtypes = [vp, _D, _D, _D, _D, ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -431,6 +435,19 @@ class OracleCDomain:
         assert lib().orcc_ecs_a_vec_halo(self._h, _p(self._c(u)), _p(self._c(v)), int(halo_width),
                                          _p(eu), _p(ev)) == 0
         return eu, ev
+
+    def ecs_xy_halo(self, f, halo_width=3):
+        """The ECS_xy halo of a corner-mesh field: (6, n+2hw, n+2hw), n = N+1."""
+        W = self.N + 1 + 2 * int(halo_width)
+        e = np.zeros((6, W, W))
+        assert lib().orcc_ecs_xy_halo(self._h, _p(self._c(f)), int(halo_width), _p(e)) == 0
+        return e
+
+    def laplace_ch(self, f, order=4):
+        """laplace_ch_halo2 / laplace_ch_halo4 of a corner-mesh field."""
+        out = self.zeros("q")
+        assert lib().orcc_laplace_ch(self._h, int(order), _p(self._c(f)), _p(out)) == 0
+        return out
 
     def grad_c2_ecs(self, f):
         """gradient_c2_ecs: gx on the x-faces, gy on the y-faces."""

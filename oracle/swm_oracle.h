@@ -187,6 +187,11 @@ void orcc_div_a2_ecs(const orcc_domain* d, const double* u, const double* v, dou
 /* gradient_c2_ecs: the ECS_O halo of width 1, then first differences of the
  * cell values onto the faces (gx on mesh u, gy on mesh v). */
 void orcc_grad_c2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy);
+/* The ECS_xy halo of a corner (node) mesh field, width 1..4: per panel the
+ * extended (N+1+2hw)^2 tile, row-major; returns 0 or -1.  laplace_ch_halo2 /
+ * laplace_ch_halo4 (order 2 / 4) of a corner-mesh field, edge-synced. */
+int orcc_ecs_xy_halo(const orcc_domain* d, const double* f, int halo_width, double* ext);
+int orcc_laplace_ch(const orcc_domain* d, int order, const double* f, double* out);
 double orcc_mass(const orcc_domain* d, int mesh, const double* f);
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f);
 /* Analytic test fields on the C meshes: vector kinds 0 solid rotation (axis

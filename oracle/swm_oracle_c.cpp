@@ -238,7 +238,10 @@ struct orcc_domain {
   std::vector<double> ecs_w;
   std::vector<int> ecs_ind;
   // ecs_A_vec: the 2x2 maps [edge 0..3][depth 1..kDepth][position 1..N][4]
-  std::vector<double> ecs_tm;  // quadrature edge weights at centres / interfaces
+  std::vector<double> ecs_tm;
+  // ECS_xy: cubic weights [row 0..kXyRows-1][position 1-kXyRows..n+kXyRows][4], bases
+  std::vector<double> xy_w;
+  std::vector<int> xy_ind;  // quadrature edge weights at centres / interfaces
 };
 
 namespace {
@@ -962,6 +965,195 @@ void div_a2_ecs(const orcc_domain& d, const double* u, const double* v, double* 
   }
 }
 
+// ------------------------------------------------------------------ ECS_xy
+// The ECS_xy halo of the corner (node) mesh, the Ah grid's points
+// (equiang_cs/ecs_halo_xy_mod.f90:38-217 with ecs_halo_factory_mod.f90:198-
+// 228, init_halo_xy_interp): n = N+1 nodes a side, the exchange places the
+// neighbour's copy of the shared edge row in the first halo layer, so halo row
+// r is interpolated from the neighbour's row r + 1 layers out.  Widths up to
+// kXyRows (the exchange is kDepth deep).
+constexpr int kXyRows = kDepth - 1;
+
+void build_xy_weights(orcc_domain& d) {
+  const int n = d.N + 1, ni = n + 2 * kXyRows;
+  d.xy_w.assign((size_t)kXyRows * ni * 4, 0.0);
+  d.xy_ind.assign((size_t)kXyRows * ni, 0);
+  for (int r = 1; r <= kXyRows; ++r)
+    for (int i = 1 - kXyRows; i <= n + kXyRows; ++i) {
+      const double zb = 0.25 * PI + r * d.hx;
+      double za = -0.25 * PI + (i - 1.0) * d.hx;
+      za = std::atan(std::tan(za) / std::tan(zb));
+      const int b = std::min(std::max(2, (int)std::floor((za + 0.25 * PI) / d.hx) + 1), n - 2);
+      const double x = (za + 0.25 * PI) / d.hx - (b - 1.0);
+      double* w = &d.xy_w[((size_t)(r - 1) * ni + (i - 1 + kXyRows)) * 4];
+      w[0] = -x * (x - 1.0) * (x - 2.0) / 6.0;
+      w[1] = (x + 1.0) * (x - 1.0) * (x - 2.0) / 2.0;
+      w[2] = -(x + 1.0) * x * (x - 2.0) / 2.0;
+      w[3] = (x + 1.0) * x * (x - 1.0) / 6.0;
+      d.xy_ind[(size_t)(r - 1) * ni + (i - 1 + kXyRows)] = b;
+    }
+}
+
+// One panel's ECS_xy halo of width hw on the extended tile E ((n+2hw)^2,
+// row-major, the reference's 1-based (i, j) at row j+hw-1, column i+hw-1).
+// The reference works in place; each step's inputs are restated here from
+// the exchanged values X:
+//  - the cube-corner nodes become the average of their three copies, and the
+//    corner diagonal (1-r, 1-r) the average of the two strips' points r+1
+//    layers out next to the corner, which also stand in for those points;
+//  - the other edge nodes become the average with their duplicate;
+//  - halo row r of an edge is the cubic interpolation (ecs_ext_halo_1e of the
+//    xy module) of the neighbour's row r+1 layers out, whose end points are
+//    the corner diagonals, at positions max(1-hw, 2-r) .. min(n+hw, n+r-1).
+void ecs_xy_panel(const orcc_domain& d, const double* f, int p, int hw, double* E) {
+  const Mesh& Q = d.m[3];
+  const int n = d.N + 1, W = n + 2 * hw, ni = n + 2 * kXyRows;
+  auto X = [&](int i1, int j1) { return ext(Q, d.hq, f, nullptr, p, i1 - 1, j1 - 1); };
+  auto out = [&](int i1, int j1) -> double& { return E[(size_t)(j1 - 1 + hw) * W + (i1 - 1 + hw)]; };
+  auto w = [&](int m, int i, int r) { return d.xy_w[((size_t)(r - 1) * ni + (i - 1 + kXyRows)) * 4 + (m + 1)]; };
+  auto ind = [&](int i, int r) { return d.xy_ind[(size_t)(r - 1) * ni + (i - 1 + kXyRows)]; };
+  for (int j = 1; j <= n; ++j)
+    for (int i = 1; i <= n; ++i) out(i, j) = X(i, j);
+  // corner diagonals of corners 1..4 (at (1,1), (n,1), (n,n), (1,n))
+  std::vector<double> dg(4 * (size_t)(hw + 1), 0.0);
+  auto D = [&](int c, int r) -> double& { return dg[(size_t)c * (hw + 1) + r]; };
+  for (int r = 1; r <= hw; ++r) {
+    D(0, r) = 0.5 * (X(-r, 1) + X(1, -r));
+    D(1, r) = 0.5 * (X(n + r + 1, 1) + X(n, -r));
+    D(2, r) = 0.5 * (X(n + r + 1, n) + X(n, n + r + 1));
+    D(3, r) = 0.5 * (X(1, n + r + 1) + X(-r, n));
+  }
+  // the panel's edge nodes: corners from three copies, the rest from two
+  out(1, 1) = (X(1, 1) + X(1, 0) + X(0, 1)) / 3.0;
+  out(n, 1) = (X(n, 1) + X(n, 0) + X(n + 1, 1)) / 3.0;
+  out(n, n) = (X(n, n) + X(n, n + 1) + X(n + 1, n)) / 3.0;
+  out(1, n) = (X(1, n) + X(0, n) + X(1, n + 1)) / 3.0;
+  for (int k = 2; k <= n - 1; ++k) {
+    out(k, 1) = 0.5 * (X(k, 1) + X(k, 0));
+    out(k, n) = 0.5 * (X(k, n) + X(k, n + 1));
+    out(1, k) = 0.5 * (X(1, k) + X(0, k));
+    out(n, k) = 0.5 * (X(n, k) + X(n + 1, k));
+  }
+  // halo rows: the source row with its corner-diagonal end points
+  for (int r = 1; r <= hw; ++r) {
+    const int lo = std::max(1 - hw, 2 - r), hi = std::min(n + hw, n + r - 1);
+    auto S1 = [&](int k) { return k == 1 ? D(0, r) : k == n ? D(1, r) : X(k, -r); };         // bottom
+    auto S2 = [&](int k) { return k == 1 ? D(3, r) : k == n ? D(2, r) : X(k, n + r + 1); };  // top
+    auto S3 = [&](int k) { return k == 1 ? D(0, r) : k == n ? D(3, r) : X(-r, k); };         // left
+    auto S4 = [&](int k) { return k == 1 ? D(1, r) : k == n ? D(2, r) : X(n + r + 1, k); };  // right
+    for (int k = lo; k <= hi; ++k) {
+      const int b = ind(k, r);
+      auto itp = [&](auto S) {
+        double s = w(-1, k, r) * S(b - 1);
+        s = s + w(0, k, r) * S(b);
+        s = s + w(1, k, r) * S(b + 1);
+        s = s + w(2, k, r) * S(b + 2);
+        return s;
+      };
+      out(k, 1 - r) = itp(S1);
+      out(k, n + r) = itp(S2);
+      out(1 - r, k) = itp(S3);
+      out(n + r, k) = itp(S4);
+    }
+    out(1 - r, 1 - r) = D(0, r);
+    out(n + r, 1 - r) = D(1, r);
+    out(n + r, n + r) = D(2, r);
+    out(1 - r, n + r) = D(3, r);
+  }
+}
+
+// laplace_ch_halo2 / laplace_ch_halo4 (laplace/laplace_ch_halo_mod.f90:15-179
+// with laplace_factory_mod.f90:110-126): on the node mesh with the ECS_xy
+// halo (width 1 / 3), the divergence of the contravariant gradient at second
+// / fourth order, then the Ah-type edge sync.  The metric is the ECS metric at
+// the nodes and at the half-shifted points (mesh_y at (i+1/2, j), mesh_x at
+// (i, j+1/2)), extended beyond the edges.
+void laplace_ch(const orcc_domain& d, int order, const double* f, double* out) {
+  const Mesh& Q = d.m[3];
+  const int N = d.N, n = N + 1, hw = order == 2 ? 1 : 3, W = n + 2 * hw;
+  const double hx = d.hx, a = d.scale;
+  struct Mt { double J, qi1, qi2, qi3; };
+  auto met = [&](double si, double sj) {  // 1-based node coordinates, may be fractional / outside
+    const double al = -0.25 * PI + (si - 1.0) * hx, be = -0.25 * PI + (sj - 1.0) * hx;
+    const double ta = std::tan(al), tb = std::tan(be);
+    const double sg = std::sqrt(1.0 + ta * ta + tb * tb);
+    Mt m;
+    m.J = (1.0 + ta * ta) * (1.0 + tb * tb) / (sg * sg * sg);
+    m.qi1 = sg * sg / (1.0 + ta * ta);
+    m.qi2 = sg * sg * ta * tb / ((1.0 + ta * ta) * (1.0 + tb * tb));
+    m.qi3 = sg * sg / (1.0 + tb * tb);
+    return m;
+  };
+  std::vector<double> raw(Q.size());
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (int p = 0; p < 6; ++p) {
+    std::vector<double> E((size_t)W * W, 0.0);
+    ecs_xy_panel(d, f, p, hw, E.data());
+    auto F = [&](int i1, int j1) { return E[(size_t)(j1 - 1 + hw) * W + (i1 - 1 + hw)]; };
+    auto xy = [&](int i1, int j1) { return met(i1, j1); };
+    auto my = [&](int i1, int j1) { return met(i1 + 0.5, j1); };  // mesh_y: (i+1/2, j)
+    auto mx = [&](int i1, int j1) { return met(i1, j1 + 0.5); };  // mesh_x: (i, j+1/2)
+    for (int j = 1; j <= n; ++j)
+      for (int i = 1; i <= n; ++i) {
+        double v;
+        if (order == 2) {
+          auto gx = [&](int ii, int jj) { return (F(ii + 1, jj) - F(ii, jj)) / (hx * a); };
+          auto gy = [&](int ii, int jj) { return (F(ii, jj + 1) - F(ii, jj)) / (hx * a); };
+          auto gxt = [&](int ii, int jj) {
+            const double gh0 = 0.5 * (gy(ii, jj - 1) + gy(ii, jj)) * xy(ii, jj).qi2 * xy(ii, jj).J;
+            const double gh1 = 0.5 * (gy(ii + 1, jj - 1) + gy(ii + 1, jj)) * xy(ii + 1, jj).qi2 * xy(ii + 1, jj).J;
+            return my(ii, jj).qi1 * gx(ii, jj) + 0.5 * (gh0 + gh1) / my(ii, jj).J;
+          };
+          // the reference's own index pairing in gyt's second term: Qi12 at
+          // (i+1, j) times J at (i, j+1) (laplace_ch_halo_mod.f90:87).  It
+          // makes the order-2 operator converge at first order; with both at
+          // (i, j+1) it would be second order.  Kept, for parity.
+          auto gyt = [&](int ii, int jj) {
+            const double gh0 = 0.5 * (gx(ii - 1, jj) + gx(ii, jj)) * xy(ii, jj).qi2 * xy(ii, jj).J;
+            const double gh1 = 0.5 * (gx(ii - 1, jj + 1) + gx(ii, jj + 1)) * xy(ii + 1, jj).qi2 * xy(ii, jj + 1).J;
+            return mx(ii, jj).qi3 * gy(ii, jj) + 0.5 * (gh0 + gh1) / mx(ii, jj).J;
+          };
+          v = (my(i, j).J * gxt(i, j) - my(i - 1, j).J * gxt(i - 1, j) + mx(i, j).J * gyt(i, j) -
+               mx(i, j - 1).J * gyt(i, j - 1)) /
+              (xy(i, j).J * hx * a);
+        } else {
+          auto gx = [&](int ii, int jj) {
+            return (-F(ii + 2, jj) + 27.0 * F(ii + 1, jj) - 27.0 * F(ii, jj) + F(ii - 1, jj)) / (24.0 * hx * a);
+          };
+          auto gy = [&](int ii, int jj) {
+            return (-F(ii, jj + 2) + 27.0 * F(ii, jj + 1) - 27.0 * F(ii, jj) + F(ii, jj - 1)) / (24.0 * hx * a);
+          };
+          auto gxh = [&](int ii, int jj) {
+            return (-gx(ii - 2, jj) + 9.0 * gx(ii - 1, jj) + 9.0 * gx(ii, jj) - gx(ii + 1, jj)) / 16.0 * xy(ii, jj).qi2 *
+                   xy(ii, jj).J;
+          };
+          auto gyh = [&](int ii, int jj) {
+            return (-gy(ii, jj - 2) + 9.0 * gy(ii, jj - 1) + 9.0 * gy(ii, jj) - gy(ii, jj + 1)) / 16.0 * xy(ii, jj).qi2 *
+                   xy(ii, jj).J;
+          };
+          auto gxt = [&](int ii, int jj) {
+            return my(ii, jj).qi1 * gx(ii, jj) +
+                   (-gyh(ii + 2, jj) + 9.0 * gyh(ii + 1, jj) + 9.0 * gyh(ii, jj) - gyh(ii - 1, jj)) / (16.0 * my(ii, jj).J);
+          };
+          auto gyt = [&](int ii, int jj) {
+            return mx(ii, jj).qi3 * gy(ii, jj) +
+                   (-gxh(ii, jj + 2) + 9.0 * gxh(ii, jj + 1) + 9.0 * gxh(ii, jj) - gxh(ii, jj - 1)) / (16.0 * mx(ii, jj).J);
+          };
+          const double dx = (-my(i + 1, j).J * gxt(i + 1, j) + 27.0 * my(i, j).J * gxt(i, j) -
+                             27.0 * my(i - 1, j).J * gxt(i - 1, j) + my(i - 2, j).J * gxt(i - 2, j)) /
+                            24.0;
+          const double dy = (-mx(i, j + 1).J * gyt(i, j + 1) + 27.0 * mx(i, j).J * gyt(i, j) -
+                             27.0 * mx(i, j - 1).J * gyt(i, j - 1) + mx(i, j - 2).J * gyt(i, j - 2)) /
+                            24.0;
+          v = (dx / hx + dy / hx) / (xy(i, j).J * a);
+        }
+        raw[Q.at(p, i - 1, j - 1)] = v;
+      }
+  }
+  std::copy(raw.begin(), raw.end(), out);
+  sync_q(d, out);
+}
+
 // operator_swm_t%apply, vector-invariant branch
 // (models/shallow_water/operator/operator_swm_mod.f90:61-113).
 void apply(const orcc_domain& d, const double* hs, const double* h, const double* u, const double* v, double* th,
@@ -1124,6 +1316,7 @@ orcc_domain* create(int N, int order, double radius, double grav, double omega, 
   d->hau = build_halo(d->m[0], d->m[0], 1);
   d->hav = build_halo(d->m[0], d->m[0], 2);
   build_ecs_tm(*d);
+  build_xy_weights(*d);
   d->ops21.order = 21;
   d->ops21.Wc2i = make_stag(W21_C2I); d->ops21.Wi2c = make_stag(W21_I2C);
   d->ops21.Dc2i = make_stag(D21_C2I); d->ops21.Di2c = make_stag(D21_I2C);
@@ -1223,6 +1416,17 @@ int orcc_ecs_a_vec_halo(const orcc_domain* d, const double* u, const double* v, 
 }
 void orcc_div_a2_ecs(const orcc_domain* d, const double* u, const double* v, double* out) { div_a2_ecs(*d, u, v, out); }
 void orcc_grad_c2_ecs(const orcc_domain* d, const double* f, double* gx, double* gy) { grad_c2_ecs(*d, f, gx, gy); }
+int orcc_ecs_xy_halo(const orcc_domain* d, const double* f, int halo_width, double* ext) {
+  if (halo_width < 1 || halo_width > kXyRows) return -1;
+  const size_t W = (size_t)d->N + 1 + 2 * halo_width;
+  for (int p = 0; p < 6; ++p) ecs_xy_panel(*d, f, p, halo_width, ext + p * W * W);
+  return 0;
+}
+int orcc_laplace_ch(const orcc_domain* d, int order, const double* f, double* out) {
+  if (order != 2 && order != 4) return -1;
+  laplace_ch(*d, order, f, out);
+  return 0;
+}
 double orcc_mass(const orcc_domain* d, int mesh, const double* f) { return mass(*d, mesh, f); }
 double orcc_l2norm(const orcc_domain* d, int mesh, const double* f) {
   return std::sqrt(l2sq(d->m[mesh], d->hx, f));

@@ -261,3 +261,51 @@ def test_ecs_a_vec_halo_is_fourth_order(hw):
         assert np.array_equal(eu[:, hw:hw + N, hw:hw + N], u.reshape(6, N, N))
         errs.append(max(np.abs(eu - np.sum(Vx * b1, -1)).max(), np.abs(ev - np.sum(Vx * b2, -1)).max()))
     assert errs[0] < 1e-4 and errs[1] < errs[0] / 12.0, errs
+
+
+# ------------------------------------------------------------------ ECS_xy
+def _extended_nodes(N, hw):
+    """Cartesian points of the extended node grid lines, (6, W, W, 3)."""
+    import math
+    hx = 0.5 * math.pi / N
+    a = -0.25 * math.pi + hx * (np.arange(1 - hw, N + 2 + hw) - 1.0)
+    ta, tb = np.tan(a)[None, :], np.tan(a)[:, None]
+    sg = np.sqrt(1 + ta * ta + tb * tb)
+    one = np.ones_like(sg)
+    rp = np.stack([ta * one / sg, tb * one / sg, one / sg], -1)
+    return (rp[None, ..., 0:1] * initial._EX[:, None, None, :] + rp[None, ..., 1:2] * initial._EY[:, None, None, :]
+            - rp[None, ..., 2:3] * initial._EN[:, None, None, :])
+
+
+@pytest.mark.parametrize("hw", [1, 3])
+def test_ecs_xy_halo_is_fourth_order(hw):
+    """The ECS_xy halo of the node (corner) mesh: every extended point of a
+    smooth field, the synced panel edges included, converges at fourth order
+    to the exact values (the reference's halo test prints these errors with
+    no known answers)."""
+    errs = []
+    for N in (24, 48):
+        od = oracle.OracleCDomain(N, 42, radius=1.0)
+        r = _extended_nodes(N, hw)
+        e = 0.0
+        for lev in range(3):
+            E = od.ecs_xy_halo(od.scalar_test_field("xyz", lev, "q"), hw)
+            e = max(e, float(np.abs(E - r[..., lev]).max()))
+        errs.append(e)
+    assert errs[0] < 2e-6 and errs[1] < errs[0] / 12.0, errs
+
+
+@pytest.mark.parametrize("order,rate", [(2, 1.9), (4, 3.5)])
+def test_laplace_ch_halo_converges(order, rate):
+    """laplace_ch_halo2 / laplace_ch_halo4 on z (an l = 1 field, eigenvalue
+    -2/a^2): the 4th-order operator converges at second order (the halo's
+    fourth-order error over h^2 at the edges), the 2nd-order one at first
+    order (the reference's index pairing in one metric term)."""
+    a = 6.371e6
+    errs = []
+    for N in (24, 48):
+        od = oracle.OracleCDomain(N, 42)
+        z = od.scalar_test_field("xyz", 2, "q")
+        errs.append(float(np.abs(od.laplace_ch(z, order) - (-2 / a ** 2) * z).max() * a ** 2 / 2))
+    assert errs[0] / errs[1] > rate, errs
+    assert errs[0] < (0.03 if order == 2 else 1e-4)
