@@ -290,6 +290,18 @@ class OperatorSWM:
         """gradient_c2_ecs (C grid): f on mesh p, gx on u, gy on v."""
         self._check(self._L.swm_op_grad_c2_ecs(self._h, gx._h, gy._h, f._h))
 
+    def ecs_xy_halo(self, f, halo_width: int = 3) -> np.ndarray:
+        """The ECS_xy halo of a corner-mesh field (C grid): (6, n+2hw, n+2hw)
+        extended tiles, n = N+1, laid out as ecs_o_halo's."""
+        W = self.N + 1 + 2 * int(halo_width)
+        out = np.empty((6, W, W))
+        self._check(self._L.swm_halo_ecs_xy(self._h, f._h, int(halo_width), _ptr(out)))
+        return out
+
+    def laplace_ch(self, out, f, order: int = 4):
+        """laplace_ch_halo2 / laplace_ch_halo4 of a corner-mesh field (C grid)."""
+        self._check(self._L.swm_laplace_ch(self._h, out._h, f._h, int(order)))
+
     def calc_div_a2_ecs(self, div, u, v):
         """divergence_a2_ecs on the cell centres (C grid): contravariant u, v
         and div on mesh p."""

@@ -41,7 +41,7 @@ EXPORTS = (
     "swm_field_free", "swm_field_upload", "swm_field_download", "swm_op_co2contra",
     "swm_op_massflux", "swm_op_ke", "swm_op_grad", "swm_op_div", "swm_op_curl",
     "swm_op_coriolis", "swm_op_grad_perp", "swm_op_contra2co", "swm_op_grad_a2_ecs", "swm_halo_ecs_o",
-    "swm_op_div_a2_ecs", "swm_halo_ecs_a_vec", "swm_op_grad_c2_ecs",
+    "swm_op_div_a2_ecs", "swm_halo_ecs_a_vec", "swm_op_grad_c2_ecs", "swm_halo_ecs_xy", "swm_laplace_ch",
     "swm_sync_scalar", "swm_sync_vector_cov", "swm_quadrature_mass",
     "swm_timing_enable", "swm_timing_read", "swm_sync_scalar_static",
     "swm_ensemble_create", "swm_ensemble_destroy", "swm_ensemble_last_error", "swm_ensemble_size",
@@ -175,6 +175,8 @@ def load(build_if_missing: bool = True):
     sig("swm_halo_ecs_o", I, VP, VP, I, _D)
     sig("swm_op_div_a2_ecs", I, VP, VP, VP, VP)
     sig("swm_op_grad_c2_ecs", I, VP, VP, VP, VP)
+    sig("swm_halo_ecs_xy", I, VP, VP, I, _D)
+    sig("swm_laplace_ch", I, VP, VP, VP, I)
     sig("swm_halo_ecs_a_vec", I, VP, VP, VP, I, _D, _D)
     sig("swm_sync_scalar", I, VP, VP)
     sig("swm_sync_vector_cov", I, VP, VP, VP)

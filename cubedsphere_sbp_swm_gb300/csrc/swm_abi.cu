@@ -2026,6 +2026,24 @@ int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext
   CK(cgrid_ecs_o_halo(ctx->cg, f->p, halo_width, ext, ctx->st), "ECS_O halo");
   return SWM_OK;
 }
+int swm_halo_ecs_xy(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "the ECS_xy halo needs the corner mesh of the C grid");
+  CHECK_FIELDS(f);
+  if (int rc = check_mesh(ctx, f, SWM_MESH_Q, "ECS_xy halo")) return rc;
+  if (halo_width < 1 || halo_width > 4) return fail(ctx, SWM_E_INVALID, "ECS_xy halo width must be 1..4");
+  if (!ext) return fail(ctx, SWM_E_INVALID, "null output");
+  CK(cgrid_ecs_xy_halo(ctx->cg, f->p, halo_width, ext, ctx->st), "ECS_xy halo");
+  return SWM_OK;
+}
+int swm_laplace_ch(swm_ctx* ctx, swm_field* out, const swm_field* in, int order) {
+  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "laplace_ch_halo needs the corner mesh of the C grid");
+  CHECK_FIELDS(out, in);
+  for (const swm_field* x : {(const swm_field*)out, in})
+    if (int rc = check_mesh(ctx, x, SWM_MESH_Q, "laplace_ch_halo")) return rc;
+  if (order != 2 && order != 4) return fail(ctx, SWM_E_INVALID, "laplace_ch_halo order must be 2 or 4");
+  CK(cgrid_laplace_ch(ctx->cg, ctx->topo, ctx->edge64, order, in->p, out->p, ctx->st), "laplace_ch_halo");
+  return SWM_OK;
+}
 int swm_op_grad_c2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy, const swm_field* f) {
   if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "gradient_c2_ecs is provided on the C grid only");
   CHECK_FIELDS(gx, gy, f);

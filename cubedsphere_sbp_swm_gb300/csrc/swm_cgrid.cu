@@ -190,6 +190,10 @@ struct CArgsT {
   // beyond each edge [edge][position] (bottom, top, left, right)
   const double* ecs_tm;
   const double* ecs_jr;
+  // ECS_xy: cubic weights [row 0..kXyRows-1][position 1-kXyRows..n+kXyRows][4], bases
+  const double* xy_w;
+  const int* xy_ind;
+  double hx0, rad;  // hx and the radius
   // inputs
   const T *h, *u, *v, *hs, *ut_in, *vt_in, *hu_in, *hv_in, *ke_in, *curl_in;
   // intermediate and unfused outputs
@@ -709,6 +713,163 @@ __global__ void __launch_bounds__(256) ecs_vec_ext_kernel(const __grid_constant_
   ev[o] = in ? a.v[at(a.g, p, i1 - 1, j1 - 1)] : ecs_v_at(a, a.u, a.v, p, 1, i1, j1, hw);
 }
 
+// ------------------------------------------------------------------ ECS_xy
+// The ECS_xy halo of the corner (node) mesh, the Ah grid's points
+// (equiang_cs/ecs_halo_xy_mod.f90:38-217): n = N+1 nodes a side; the
+// exchange places the neighbour's copy of the shared edge row in the first
+// halo layer, so halo row r comes from the neighbour's row r+1 layers out.
+// The reference works in place; each value is restated from the exchanged
+// values here (the same steps as the oracle's ecs_xy_panel).
+constexpr int kXyRows = kHaloDepth - 1;
+
+__device__ __forceinline__ double xy_x(const CArgsT<double>& a, const double* f, int p, int i1, int j1) {
+  const int n = a.N + 1;
+  if (i1 >= 1 && i1 <= n && j1 >= 1 && j1 <= n) return f[at(a.g, p, i1 - 1, j1 - 1)];
+  int side, d, k;
+  if (i1 < 1) { side = 0; d = 1 - i1; k = j1 - 1; }
+  else if (i1 > n) { side = 1; d = i1 - n; k = j1 - 1; }
+  else if (j1 < 1) { side = 2; d = 1 - j1; k = i1 - 1; }
+  else { side = 3; d = j1 - n; k = i1 - 1; }
+  return halo_at(a, 3, side, p, d, k, f, f);
+}
+
+// The extended value at (i1, j1) of the ECS_xy halo of width hw: the panel's
+// edge nodes averaged with their copies (three at the cube corners), the
+// corner diagonals from the two strips beyond the duplicates, and the halo
+// rows interpolated from the neighbour's rows with the diagonals at their ends.
+__device__ double xy_at(const CArgsT<double>& a, const double* f, int p, int i1, int j1, int hw) {
+  const int n = a.N + 1, ni = n + 2 * kXyRows;
+  auto X = [&](int x, int y) { return xy_x(a, f, p, x, y); };
+  const bool in_i = i1 >= 1 && i1 <= n, in_j = j1 >= 1 && j1 <= n;
+  if (in_i && in_j) {
+    const bool ei = i1 == 1 || i1 == n, ej = j1 == 1 || j1 == n;
+    if (!ei && !ej) return X(i1, j1);
+    if (i1 == 1 && j1 == 1) return (X(1, 1) + X(1, 0) + X(0, 1)) / 3.0;
+    if (i1 == n && j1 == 1) return (X(n, 1) + X(n, 0) + X(n + 1, 1)) / 3.0;
+    if (i1 == n && j1 == n) return (X(n, n) + X(n, n + 1) + X(n + 1, n)) / 3.0;
+    if (i1 == 1 && j1 == n) return (X(1, n) + X(0, n) + X(1, n + 1)) / 3.0;
+    if (j1 == 1) return 0.5 * (X(i1, 1) + X(i1, 0));
+    if (j1 == n) return 0.5 * (X(i1, n) + X(i1, n + 1));
+    if (i1 == 1) return 0.5 * (X(1, j1) + X(0, j1));
+    return 0.5 * (X(n, j1) + X(n + 1, j1));
+  }
+  auto D = [&](int c, int r) {
+    if (c == 0) return 0.5 * (X(-r, 1) + X(1, -r));
+    if (c == 1) return 0.5 * (X(n + r + 1, 1) + X(n, -r));
+    if (c == 2) return 0.5 * (X(n + r + 1, n) + X(n, n + r + 1));
+    return 0.5 * (X(1, n + r + 1) + X(-r, n));
+  };
+  for (int r = 1; r <= hw; ++r) {
+    if (i1 == 1 - r && j1 == 1 - r) return D(0, r);
+    if (i1 == n + r && j1 == 1 - r) return D(1, r);
+    if (i1 == n + r && j1 == n + r) return D(2, r);
+    if (i1 == 1 - r && j1 == n + r) return D(3, r);
+  }
+  auto lo = [&](int r) { return max(1 - hw, 2 - r); };
+  auto hi = [&](int r) { return min(n + hw, n + r - 1); };
+  auto itp = [&](int r, int k, auto S) {
+    const int b = __ldg(&a.xy_ind[(r - 1) * ni + (k - 1 + kXyRows)]);
+    const double* w = a.xy_w + ((r - 1) * ni + (k - 1 + kXyRows)) * 4;
+    double s = __ldg(w) * S(b - 1);
+    s = s + __ldg(w + 1) * S(b);
+    s = s + __ldg(w + 2) * S(b + 1);
+    s = s + __ldg(w + 3) * S(b + 2);
+    return s;
+  };
+  if (j1 < 1 && i1 >= lo(1 - j1) && i1 <= hi(1 - j1)) {
+    const int r = 1 - j1;
+    return itp(r, i1, [&](int k) { return k == 1 ? D(0, r) : k == n ? D(1, r) : X(k, -r); });
+  }
+  if (j1 > n && i1 >= lo(j1 - n) && i1 <= hi(j1 - n)) {
+    const int r = j1 - n;
+    return itp(r, i1, [&](int k) { return k == 1 ? D(3, r) : k == n ? D(2, r) : X(k, n + r + 1); });
+  }
+  if (i1 < 1) {
+    const int r = 1 - i1;
+    return itp(r, j1, [&](int k) { return k == 1 ? D(0, r) : k == n ? D(3, r) : X(-r, k); });
+  }
+  const int r = i1 - n;
+  return itp(r, j1, [&](int k) { return k == 1 ? D(1, r) : k == n ? D(2, r) : X(n + r + 1, k); });
+}
+
+// The extended tiles of the ECS_xy halo of width hw (W = n + 2 hw).
+__global__ void __launch_bounds__(256) xy_ext_kernel(const __grid_constant__ CArgsT<double> a, int hw, double* ext) {
+  const int n = a.N + 1, W = n + 2 * hw;
+  SWM_C_INDEX(W, W)
+  ext[((long long)p * W + j) * W + i] = xy_at(a, a.ke_in, p, i + 1 - hw, j + 1 - hw, hw);
+}
+
+// laplace_ch_halo2 / laplace_ch_halo4 (laplace/laplace_ch_halo_mod.f90:15-179)
+// on the extended tiles of the ECS_xy halo (width 1 / 3), before the edge
+// sync.  mt holds the ECS metric (J, Qi11, Qi12, Qi22) of the extended node
+// grid at the nodes, at (i+1/2, j) and at (i, j+1/2): three tables of
+// (n + 2 kXyRows)^2 points, panel-independent.
+template <int ORDER>
+__global__ void __launch_bounds__(256) laplace_ch_kernel(const __grid_constant__ CArgsT<double> a, const double* ext,
+                                                         const double* mt, double* out) {
+  constexpr int hw = ORDER == 2 ? 1 : 3;
+  const int n = a.N + 1, W = n + 2 * hw, M = n + 2 * kXyRows;
+  SWM_C_INDEX(n, n)
+  const double hx = a.hx0, sc = a.rad;
+  const double* E = ext + (long long)p * W * W;
+  auto F = [&](int x, int y) { return E[(y - 1 + hw) * W + (x - 1 + hw)]; };
+  auto T = [&](int t, int x, int y, int c) { return __ldg(&mt[(((long long)t * M + (y - 1 + kXyRows)) * M + (x - 1 + kXyRows)) * 4 + c]); };
+  auto Jxy = [&](int x, int y) { return T(0, x, y, 0); };
+  auto Q2xy = [&](int x, int y) { return T(0, x, y, 2); };
+  auto Jy = [&](int x, int y) { return T(1, x, y, 0); };    // mesh_y: (i+1/2, j)
+  auto Q1y = [&](int x, int y) { return T(1, x, y, 1); };
+  auto Jx = [&](int x, int y) { return T(2, x, y, 0); };    // mesh_x: (i, j+1/2)
+  auto Q3x = [&](int x, int y) { return T(2, x, y, 3); };
+  const int i1 = i + 1, j1 = j + 1;
+  double v;
+  if (ORDER == 2) {
+    auto gx = [&](int x, int y) { return (F(x + 1, y) - F(x, y)) / (hx * sc); };
+    auto gy = [&](int x, int y) { return (F(x, y + 1) - F(x, y)) / (hx * sc); };
+    auto gxt = [&](int x, int y) {
+      const double gh0 = 0.5 * (gy(x, y - 1) + gy(x, y)) * Q2xy(x, y) * Jxy(x, y);
+      const double gh1 = 0.5 * (gy(x + 1, y - 1) + gy(x + 1, y)) * Q2xy(x + 1, y) * Jxy(x + 1, y);
+      return Q1y(x, y) * gx(x, y) + 0.5 * (gh0 + gh1) / Jy(x, y);
+    };
+    // the reference's pairing: Qi12 at (i+1, j) with J at (i, j+1)
+    // (laplace_ch_halo_mod.f90:87), kept for parity
+    auto gyt = [&](int x, int y) {
+      const double gh0 = 0.5 * (gx(x - 1, y) + gx(x, y)) * Q2xy(x, y) * Jxy(x, y);
+      const double gh1 = 0.5 * (gx(x - 1, y + 1) + gx(x, y + 1)) * Q2xy(x + 1, y) * Jxy(x, y + 1);
+      return Q3x(x, y) * gy(x, y) + 0.5 * (gh0 + gh1) / Jx(x, y);
+    };
+    v = (Jy(i1, j1) * gxt(i1, j1) - Jy(i1 - 1, j1) * gxt(i1 - 1, j1) + Jx(i1, j1) * gyt(i1, j1) -
+         Jx(i1, j1 - 1) * gyt(i1, j1 - 1)) /
+        (Jxy(i1, j1) * hx * sc);
+  } else {
+    auto gx = [&](int x, int y) {
+      return (-F(x + 2, y) + 27.0 * F(x + 1, y) - 27.0 * F(x, y) + F(x - 1, y)) / (24.0 * hx * sc);
+    };
+    auto gy = [&](int x, int y) {
+      return (-F(x, y + 2) + 27.0 * F(x, y + 1) - 27.0 * F(x, y) + F(x, y - 1)) / (24.0 * hx * sc);
+    };
+    auto gxh = [&](int x, int y) {
+      return (-gx(x - 2, y) + 9.0 * gx(x - 1, y) + 9.0 * gx(x, y) - gx(x + 1, y)) / 16.0 * Q2xy(x, y) * Jxy(x, y);
+    };
+    auto gyh = [&](int x, int y) {
+      return (-gy(x, y - 2) + 9.0 * gy(x, y - 1) + 9.0 * gy(x, y) - gy(x, y + 1)) / 16.0 * Q2xy(x, y) * Jxy(x, y);
+    };
+    auto gxt = [&](int x, int y) {
+      return Q1y(x, y) * gx(x, y) + (-gyh(x + 2, y) + 9.0 * gyh(x + 1, y) + 9.0 * gyh(x, y) - gyh(x - 1, y)) / (16.0 * Jy(x, y));
+    };
+    auto gyt = [&](int x, int y) {
+      return Q3x(x, y) * gy(x, y) + (-gxh(x, y + 2) + 9.0 * gxh(x, y + 1) + 9.0 * gxh(x, y) - gxh(x, y - 1)) / (16.0 * Jx(x, y));
+    };
+    const double dx = (-Jy(i1 + 1, j1) * gxt(i1 + 1, j1) + 27.0 * Jy(i1, j1) * gxt(i1, j1) -
+                       27.0 * Jy(i1 - 1, j1) * gxt(i1 - 1, j1) + Jy(i1 - 2, j1) * gxt(i1 - 2, j1)) /
+                      24.0;
+    const double dy = (-Jx(i1, j1 + 1) * gyt(i1, j1 + 1) + 27.0 * Jx(i1, j1) * gyt(i1, j1) -
+                       27.0 * Jx(i1, j1 - 1) * gyt(i1, j1 - 1) + Jx(i1, j1 - 2) * gyt(i1, j1 - 2)) /
+                      24.0;
+    v = (dx / hx + dy / hx) / (Jxy(i1, j1) * sc);
+  }
+  out[at(a.g, p, i, j)] = v;
+}
+
 // Centre pass: the kinetic energy (KE_Cgrid_mod.f90:60-75) plus g (h + hs)
 // (operator_swm_mod.f90:84-85), the divergence (div_c_sbp42_mod.f90:67-107,
 // div_c2_mod.f90:97-177) and the Coriolis terms at the centres
@@ -973,6 +1134,10 @@ struct CGrid {
   double* ecs_jr = nullptr;  // J on the first ring beyond each edge [4][N]
   double* ext = nullptr;    // extended tiles of the halo entry points (allocated on first use)
   int ext_hw = 0;
+  double* xy_w = nullptr;   // ECS_xy weights [kXyRows][n + 2 kXyRows][4]
+  int* xy_ind = nullptr;    // ECS_xy stencil bases
+  double* xy_ext = nullptr; // ECS_xy extended tiles (width up to kXyRows, on first use)
+  double* xy_mt = nullptr;  // metric tables of laplace_ch (on first use)
   double* wts = nullptr;   // quadrature weights: centres (N), interfaces (N+1)
   double* part = nullptr;  // kMassBlocks partial sums
   double* metric(int k) const { return met + (long long)k * g.fs; }
@@ -1010,6 +1175,7 @@ CArgsT<T> base_args(const CGrid* c, int ord = 0) {
   a.halo = c->halo;
   a.ecs_w = c->ecs_w; a.ecs_ind = c->ecs_ind; a.hxa = c->hx * c->radius;
   a.ecs_tm = c->ecs_tm; a.ecs_jr = c->ecs_jr;
+  a.xy_w = c->xy_w; a.xy_ind = c->xy_ind; a.hx0 = c->hx; a.rad = c->radius;
   a.Ap = Wk(W_AP); a.Bp = Wk(W_BP); a.ut = Wk(W_UT); a.vt = Wk(W_VT);
   a.hu = Wk(W_HU); a.hv = Wk(W_HV); a.Gu = Wk(W_GU); a.Gv = Wk(W_GV);
   a.KEu = Wk(W_KEU); a.KEv = Wk(W_KEV); a.curl = Wk(W_CURL);
@@ -1369,6 +1535,30 @@ void build_ecs_vec_tables(int N, double hx, std::vector<double>& tm, std::vector
   }
 }
 
+// Weights of the ECS_xy halo (ecs_halo_factory_mod.f90:198-228,
+// init_halo_xy_interp) for rows 1..kXyRows and positions 1-kXyRows ..
+// n+kXyRows: the node's angle on the neighbour's grid line r layers out, the
+// stencil base clamped to [2, n-2] and the cubic Lagrange weights.
+void build_xy_weights(int N, double hx, std::vector<double>& w, std::vector<int>& ind) {
+  const int n = N + 1, ni = n + 2 * kXyRows;
+  w.assign((size_t)kXyRows * ni * 4, 0.0);
+  ind.assign((size_t)kXyRows * ni, 0);
+  for (int r = 1; r <= kXyRows; ++r)
+    for (int i = 1 - kXyRows; i <= n + kXyRows; ++i) {
+      const double zb = 0.25 * kPiC + r * hx;
+      double za = -0.25 * kPiC + (i - 1.0) * hx;
+      za = std::atan(std::tan(za) / std::tan(zb));
+      const int b = std::min(std::max(2, (int)std::floor((za + 0.25 * kPiC) / hx) + 1), n - 2);
+      const double x = (za + 0.25 * kPiC) / hx - (b - 1.0);
+      double* q = &w[((size_t)(r - 1) * ni + (i - 1 + kXyRows)) * 4];
+      q[0] = -x * (x - 1.0) * (x - 2.0) / 6.0;
+      q[1] = (x + 1.0) * (x - 1.0) * (x - 2.0) / 2.0;
+      q[2] = -(x + 1.0) * x * (x - 2.0) / 2.0;
+      q[3] = (x + 1.0) * x * (x - 1.0) / 6.0;
+      ind[(size_t)(r - 1) * ni + (i - 1 + kXyRows)] = b;
+    }
+}
+
 }  // namespace
 
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
@@ -1393,6 +1583,9 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   if (!build_ecs_weights(N, c->hx, ew, eind)) { why = "ECS_O halo stencils leave the panel"; delete c; return 1; }
   std::vector<double> etm, ejr;
   build_ecs_vec_tables(N, c->hx, etm, ejr);
+  std::vector<double> xyw;
+  std::vector<int> xyind;
+  build_xy_weights(N, c->hx, xyw, xyind);
   std::vector<double> w(2 * (size_t)N + 1, 1.0);
   {
     // SBP_C42 / SBP_C21 edge weights (D42_A_centers / _interfaces, D21_*)
@@ -1419,6 +1612,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   ok(cudaMalloc(&c->ecs_ind, sizeof(int) * eind.size()));
   ok(cudaMalloc(&c->ecs_tm, sizeof(double) * etm.size()));
   ok(cudaMalloc(&c->ecs_jr, sizeof(double) * ejr.size()));
+  ok(cudaMalloc(&c->xy_w, sizeof(double) * xyw.size()));
+  ok(cudaMalloc(&c->xy_ind, sizeof(int) * xyind.size()));
   ok(cudaMalloc(&c->wts, sizeof(double) * w.size()));
   ok(cudaMalloc(&c->part, sizeof(double) * kMassBlocks));
   if (e == cudaSuccess) {
@@ -1464,6 +1659,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     ok(cudaMemcpyAsync(c->ecs_ind, eind.data(), sizeof(int) * eind.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->ecs_tm, etm.data(), sizeof(double) * etm.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->ecs_jr, ejr.data(), sizeof(double) * ejr.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->xy_w, xyw.data(), sizeof(double) * xyw.size(), cudaMemcpyHostToDevice, st));
+    ok(cudaMemcpyAsync(c->xy_ind, xyind.data(), sizeof(int) * xyind.size(), cudaMemcpyHostToDevice, st));
     if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
       ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
     ok(cudaMemcpyAsync(c->wts, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st));
@@ -1482,7 +1679,8 @@ void cgrid_destroy(CGrid* c) {
   if (!c) return;
   for (void* p : {(void*)c->met, (void*)c->met32, (void*)c->wk, (void*)c->rk, (void*)c->dw, (void*)c->halo,
                   (void*)c->ecs_w, (void*)c->ecs_ind, (void*)c->ecs_tm, (void*)c->ecs_jr, (void*)c->ext,
-                  (void*)c->wts, (void*)c->part})
+                  (void*)c->xy_w, (void*)c->xy_ind, (void*)c->xy_ext, (void*)c->xy_mt, (void*)c->wts,
+                  (void*)c->part})
     if (p) cudaFree(p);
   for (cudaStream_t s : c->bs)
     if (s) cudaStreamDestroy(s);
@@ -1742,6 +1940,61 @@ cudaError_t cgrid_ecs_a_vec_halo(CGrid* c, const double* u, const double* v, int
   CKE(cudaMemcpyAsync(eu_host, c->ext, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   CKE(cudaMemcpyAsync(ev_host, c->ext + n, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   return cudaStreamSynchronize(st);
+}
+
+// The ECS_xy extended tiles of width up to kXyRows, and the metric tables of
+// laplace_ch (both allocated on first use; these entry points are synchronous
+// on the host or enqueue after a one-time set-up).
+cudaError_t xy_prepare(CGrid* c, bool metric, cudaStream_t st) {
+  const int n = c->N + 1, W = n + 2 * kXyRows, M = n + 2 * kXyRows;
+  if (!c->xy_ext) {
+    CKE(cudaStreamSynchronize(st));
+    CKE(cudaMalloc(&c->xy_ext, sizeof(double) * 6 * (size_t)W * W));
+  }
+  if (metric && !c->xy_mt) {
+    // J, Qi11, Qi12, Qi22 at the nodes, at (i+1/2, j) and at (i, j+1/2) of
+    // the extended node grid (1-based i, j from 1-kXyRows to n+kXyRows)
+    std::vector<double> t((size_t)3 * M * M * 4);
+    for (int k = 0; k < 3; ++k)
+      for (int y = 1 - kXyRows; y <= n + kXyRows; ++y)
+        for (int x = 1 - kXyRows; x <= n + kXyRows; ++x) {
+          const double si = k == 1 ? x + 0.5 : x, sj = k == 2 ? y + 0.5 : y;
+          const MetricAt m = metric_at(-0.25 * kPiC + (si - 1.0) * c->hx, -0.25 * kPiC + (sj - 1.0) * c->hx);
+          double* q = &t[(((size_t)k * M + (y - 1 + kXyRows)) * M + (x - 1 + kXyRows)) * 4];
+          q[0] = m.J; q[1] = m.qi1; q[2] = m.qi2; q[3] = m.qi3;
+        }
+    CKE(cudaStreamSynchronize(st));
+    CKE(cudaMalloc(&c->xy_mt, sizeof(double) * t.size()));
+    CKE(cudaMemcpy(c->xy_mt, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice));
+  }
+  return cudaSuccess;
+}
+
+cudaError_t cgrid_ecs_xy_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st) {
+  if (halo_width < 1 || halo_width > kXyRows) return cudaErrorInvalidValue;
+  CKE(xy_prepare(c, false, st));
+  const int W = c->N + 1 + 2 * halo_width;
+  CArgsT<double> a = base_args<double>(c);
+  a.ke_in = f;
+  xy_ext_kernel<<<grid_for(W, W), kBlock, 0, st>>>(a, halo_width, c->xy_ext);
+  CKE(cudaGetLastError());
+  CKE(cudaMemcpyAsync(ext_host, c->xy_ext, sizeof(double) * 6 * (size_t)W * W, cudaMemcpyDeviceToHost, st));
+  return cudaStreamSynchronize(st);
+}
+
+cudaError_t cgrid_laplace_ch(CGrid* c, const Topology& tp, double* edge, int order, const double* f, double* out,
+                             cudaStream_t st) {
+  if (order != 2 && order != 4) return cudaErrorInvalidValue;
+  CKE(xy_prepare(c, true, st));
+  const int hw = order == 2 ? 1 : 3, n = c->N + 1, W = n + 2 * hw;
+  CArgsT<double> a = base_args<double>(c);
+  a.ke_in = f;
+  xy_ext_kernel<<<grid_for(W, W), kBlock, 0, st>>>(a, hw, c->xy_ext);
+  CKE(cudaGetLastError());
+  if (order == 2) laplace_ch_kernel<2><<<grid_for(n, n), kBlock, 0, st>>>(a, c->xy_ext, c->xy_mt, out);
+  else laplace_ch_kernel<4><<<grid_for(n, n), kBlock, 0, st>>>(a, c->xy_ext, c->xy_mt, out);
+  CKE(cudaGetLastError());
+  return launch_sync_scalar(c->g, tp, out, edge, st);  // the Ah scalar sync (laplace_factory_mod.f90:124)
 }
 
 cudaError_t cgrid_grad_c2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st) {

@@ -111,6 +111,13 @@ cudaError_t cgrid_div_a2_ecs(CGrid* c, const double* u, const double* v, double*
 // gradient_c2_ecs (gradient/grad_c2_ecs_mod.f90:33-51, 95-144): f on the
 // centres, gx on the x-faces, gy on the y-faces, with the ECS_O halo.
 cudaError_t cgrid_grad_c2_ecs(CGrid* c, const double* f, double* gx, double* gy, cudaStream_t st);
+// The ECS_xy halo of a corner-mesh (Ah node) field (equiang_cs/
+// ecs_halo_xy_mod.f90:38-217), width 1..4, its extended (N+1+2hw)^2 tiles to
+// host memory (synchronous); and laplace_ch_halo2 / laplace_ch_halo4
+// (laplace/laplace_ch_halo_mod.f90:15-179) of a corner-mesh field, edge-synced.
+cudaError_t cgrid_ecs_xy_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st);
+cudaError_t cgrid_laplace_ch(CGrid* c, const Topology& tp, double* edge, int order, const double* f, double* out,
+                             cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

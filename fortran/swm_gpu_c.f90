@@ -288,6 +288,17 @@ interface
         import :: c_int, c_ptr
         type(c_ptr), value :: ctx, gx, gy, f
     end function swm_op_grad_c2_ecs
+    integer(c_int) function swm_halo_ecs_xy(ctx, f, halo_width, ext) bind(c, name="swm_halo_ecs_xy")
+        import :: c_int, c_ptr, c_double
+        type(c_ptr), value :: ctx, f
+        integer(c_int), value :: halo_width
+        real(c_double), intent(out) :: ext(*)
+    end function swm_halo_ecs_xy
+    integer(c_int) function swm_laplace_ch(ctx, out, in, order) bind(c, name="swm_laplace_ch")
+        import :: c_int, c_ptr
+        type(c_ptr), value :: ctx, out, in
+        integer(c_int), value :: order
+    end function swm_laplace_ch
     integer(c_int) function swm_halo_ecs_a_vec(ctx, u, v, halo_width, ext_u, ext_v) bind(c, name="swm_halo_ecs_a_vec")
         import :: c_int, c_ptr, c_double
         type(c_ptr), value :: ctx, u, v

@@ -305,6 +305,17 @@ int swm_op_div_a2_ecs(swm_ctx* ctx, swm_field* div, const swm_field* u,
  * mesh v.  C grid only. */
 int swm_op_grad_c2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy,
                        const swm_field* f);
+/* C grid only, on its corner mesh (the Ah grid's nodes): the ECS_xy halo
+ * (halo_t%get_halo_scalar for "ECS_xy", equiang_cs/ecs_halo_xy_mod.f90:38-217
+ * with the weights of ecs_halo_factory_mod.f90:198-228; width 1..4; the
+ * extended (N+1+2hw)^2 tiles to host memory as swm_halo_ecs_o writes them,
+ * the panel's edge nodes synced) and laplace_ch_halo2 / laplace_ch_halo4
+ * (laplace/laplace_ch_halo_mod.f90:15-179, laplace_factory_mod.f90:110-126:
+ * with that halo of width 1 / 3, then the Ah scalar sync); order 2 or 4;
+ * out may be in. */
+int swm_halo_ecs_xy(swm_ctx* ctx, const swm_field* f, int halo_width,
+                    double* ext);
+int swm_laplace_ch(swm_ctx* ctx, swm_field* out, const swm_field* in, int order);
 int swm_halo_ecs_a_vec(swm_ctx* ctx, const swm_field* u, const swm_field* v,
                        int halo_width, double* ext_u, double* ext_v);
 /* halo_t%get_halo_scalar for "Ah_scalar_sync"

@@ -497,3 +497,31 @@ def test_ecs_a_vec_halo_and_div_a2_ecs_match_oracle(hw):
     d = field(op, "p")
     op.calc_div_a2_ecs(d, fu, fv)
     assert _rel(d.download(), od.div_a2_ecs(u, v)) < 1e-13
+
+
+@pytest.mark.parametrize("hw", [1, 3])
+def test_ecs_xy_halo_matches_oracle(hw):
+    """The ECS_xy halo of a random corner-mesh field (its synced edges, the
+    corner diagonals and every halo row of width hw) against the oracle."""
+    N = 40
+    op, od = c_op(N, 42), oracle.OracleCDomain(N, 42)
+    f = np.random.default_rng(20 + hw).standard_normal(od.shapes["q"])
+    E, Eo = op.ecs_xy_halo(field(op, "q", f), hw), od.ecs_xy_halo(f, hw)
+    assert E.shape == (6, N + 1 + 2 * hw, N + 1 + 2 * hw)
+    assert np.abs(E - Eo).max() <= 1e-14 * np.abs(Eo).max()
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_laplace_ch_halo_matches_oracle(order):
+    """laplace_ch_halo2 / laplace_ch_halo4 of a smooth and of a random
+    corner-mesh field against the oracle, in place as well."""
+    N = 40
+    op, od = c_op(N, 42), oracle.OracleCDomain(N, 42)
+    rng = np.random.default_rng(order)
+    for f in (od.scalar_test_field("xyz", 2, "q") * 1e3, rng.standard_normal(od.shapes["q"])):
+        fin, fo = field(op, "q", f), field(op, "q")
+        op.laplace_ch(fo, fin, order)
+        want = od.laplace_ch(f, order)
+        assert _rel(fo.download(), want) < 1e-12, _rel(fo.download(), want)
+        op.laplace_ch(fin, fin, order)
+        assert _rel(fin.download(), want) < 1e-12
