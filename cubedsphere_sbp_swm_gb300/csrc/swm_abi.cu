@@ -206,6 +206,9 @@ struct swm_ctx {
   // C-grid contexts (the &shallow_water_model_c operator family): the
   // staggered-mesh operator; null on the Ah grid
   CGrid* cg = nullptr;
+  // Ah contexts with a laplace_ch_halo4 hyperdiffusion: the corner-mesh
+  // tables of the ECS_xy halo (the node mesh is the corner mesh)
+  CGrid* xyg = nullptr;
   const void* ad_key[2] = {nullptr, nullptr};
   double ad_dt = 0.0;
 };
@@ -791,6 +794,7 @@ void free_ctx(swm_ctx* c) {
   void* hsT = (c->hsT == (void*)c->hs64) ? nullptr : c->hsT;
   if (c->ad_graph) cudaGraphExecDestroy(c->ad_graph);
   cgrid_destroy(c->cg);
+  cgrid_destroy(c->xyg);
   void* ptrs[] = {c->m64, c->m32, c->qw, c->Aw, c->edge, c->edge2, c->edge64, c->ya, c->yb, c->acc,
                   c->tmp, c->hs64, hsT, c->partial, c->dres, c->units, c->derr, c->adw, c->adC};
   for (void* p : ptrs) if (p) cudaFree(p);
@@ -1474,16 +1478,22 @@ int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
 // ------------------------------------------------------- hyperdiffusion
 // Names of operator_swm_diff's operators (hordiff_factory_mod.f90:27-40)
 // that this library provides: the narrow-Laplacian ones of the Ah grid.
+// kLapCh4: laplace_ch_halo4 with the ECS_xy halo (hordiff_factory_mod.f90:
+// 33-34, 39-40, 196-223: "hordiff_scalar_Ah" and "hordiff_vec_xyz_Ah"), FP64
+// contexts.
+constexpr int kLapCh4 = 4;
 int hordiff_uv_order(const char* name) {
   if (!name) return 0;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_42_narrow")) return 42;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_63_narrow")) return 63;
+  if (!std::strcmp(name, "hordiff_vec_xyz_Ah")) return kLapCh4;
   return 0;
 }
 int hordiff_h_order(const char* name) {
   if (!name) return 0;
   if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_42_narrow")) return 42;
   if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_63_narrow")) return 63;
+  if (!std::strcmp(name, "hordiff_scalar_Ah")) return kLapCh4;
   return 0;
 }
 // ... and the C-grid ones (hordiff_factory_mod.f90:19-36): the parts of the
@@ -1514,10 +1524,25 @@ template <class T> T* dwork(swm_ctx* ctx, int field) { return (T*)ctx->dw + fiel
 
 // Workspace, basis vectors and the coefficient tables of order `narrow`, in
 // the context precision (outside any capture: allocates on first use).
+// The corner-mesh tables of a context: the C grid's own, or on the Ah grid
+// (whose node mesh is the corner mesh) the tables-only object made on first
+// use.
+CGrid* node_tables(swm_ctx* ctx, int* rc) {
+  *rc = SWM_OK;
+  if (ctx->cg) return ctx->cg;
+  if (!ctx->xyg) {
+    std::string why;
+    const int e = cgrid_create_tables(ctx->g64, ctx->N, ctx->cfg.radius, ctx->st, &ctx->xyg, why);
+    if (e) { *rc = fail(ctx, e == 3 ? SWM_E_NOMEM : SWM_E_CUDA, why); return nullptr; }
+  }
+  return ctx->xyg;
+}
 int diffusion_ws(swm_ctx* ctx, int narrow) {
   const FieldGeom& g = ctx->g64;
   const size_t elt = (size_t)ctx->elt;
-  if (ctx->n < 2 * narrow_rows(narrow))
+  if (narrow == kLapCh4 && ctx->prec != SWM_FP64_PLAIN)
+    return fail(ctx, SWM_E_UNSUPPORTED, "hordiff_scalar_Ah / hordiff_vec_xyz_Ah run on FP64 contexts");
+  if (narrow != kLapCh4 && ctx->n < 2 * narrow_rows(narrow))
     return fail(ctx, SWM_E_INVALID, "grid too small for the narrow Laplacian closures");
   if (ctx->prec == SWM_FP32_FUSED && !ctx->edge2)
     CK(cudaMalloc(&ctx->edge2, sizeof(float) * 16 * 6 * ctx->n), "alloc");
@@ -1537,6 +1562,15 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
       CK(launch_basis(g, ctx->hx, b64, ctx->st), "basis");
       CK(launch_f64_to_f32(6 * g.fs, b64, (float*)ctx->b12, ctx->st), "basis f32");
     }
+  }
+  if (narrow == kLapCh4) {
+    // the corner-mesh tables, the ECS_xy scratch and the metric tables, made
+    // here, outside any capture
+    int rc;
+    CGrid* q = node_tables(ctx, &rc);
+    if (!q) return rc;
+    CK(cgrid_laplace_ch_prepare(q, ctx->st), "laplace_ch tables");
+    return SWM_OK;
   }
   void** t = ctx->ntab[narrow == 63 ? 1 : 0];
   if (!t[2]) {
@@ -1578,6 +1612,17 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
 template <class T>
 int laplace_fields(swm_ctx* ctx, int narrow, int nf, const T* src, T* dst) {
   const FieldGeom& g = ctx->g64;
+  if (narrow == kLapCh4) {
+    if constexpr (sizeof(T) == 8) {
+      for (int k = 0; k < nf; ++k)
+        CK(cgrid_laplace_ch(ctx->xyg, ctx->topo, ctx->edge64, 4, src + (long long)k * g.fs,
+                            dst + (long long)k * g.fs, ctx->st),
+           "laplace_ch_halo4");
+      return SWM_OK;
+    } else {
+      return fail(ctx, SWM_E_UNSUPPORTED, "laplace_ch_halo4 runs on FP64 contexts");
+    }
+  }
   T* edge = sizeof(T) == 8 ? (T*)ctx->edge64 : (T*)ctx->edge;
   T* d1 = sizeof(T) == 8 ? dwork<T>(ctx, kDiffWorkF32) : nullptr;
   CK(launch_laplace<T>(g, ctx->topo, narrow_tables<T>(ctx, narrow), nf, src, metric_of<T>(ctx),
@@ -2027,21 +2072,25 @@ int swm_halo_ecs_o(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext
   return SWM_OK;
 }
 int swm_halo_ecs_xy(swm_ctx* ctx, const swm_field* f, int halo_width, double* ext) {
-  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "the ECS_xy halo needs the corner mesh of the C grid");
   CHECK_FIELDS(f);
   if (int rc = check_mesh(ctx, f, SWM_MESH_Q, "ECS_xy halo")) return rc;
   if (halo_width < 1 || halo_width > 4) return fail(ctx, SWM_E_INVALID, "ECS_xy halo width must be 1..4");
   if (!ext) return fail(ctx, SWM_E_INVALID, "null output");
-  CK(cgrid_ecs_xy_halo(ctx->cg, f->p, halo_width, ext, ctx->st), "ECS_xy halo");
+  int rc;
+  CGrid* q = node_tables(ctx, &rc);
+  if (!q) return rc;
+  CK(cgrid_ecs_xy_halo(q, f->p, halo_width, ext, ctx->st), "ECS_xy halo");
   return SWM_OK;
 }
 int swm_laplace_ch(swm_ctx* ctx, swm_field* out, const swm_field* in, int order) {
-  if (ctx && !ctx->cg) return fail(ctx, SWM_E_UNSUPPORTED, "laplace_ch_halo needs the corner mesh of the C grid");
   CHECK_FIELDS(out, in);
   for (const swm_field* x : {(const swm_field*)out, in})
     if (int rc = check_mesh(ctx, x, SWM_MESH_Q, "laplace_ch_halo")) return rc;
   if (order != 2 && order != 4) return fail(ctx, SWM_E_INVALID, "laplace_ch_halo order must be 2 or 4");
-  CK(cgrid_laplace_ch(ctx->cg, ctx->topo, ctx->edge64, order, in->p, out->p, ctx->st), "laplace_ch_halo");
+  int rc;
+  CGrid* q = node_tables(ctx, &rc);
+  if (!q) return rc;
+  CK(cgrid_laplace_ch(q, ctx->topo, ctx->edge64, order, in->p, out->p, ctx->st), "laplace_ch_halo");
   return SWM_OK;
 }
 int swm_op_grad_c2_ecs(swm_ctx* ctx, swm_field* gx, swm_field* gy, const swm_field* f) {

@@ -1148,8 +1148,8 @@ namespace {
 
 template <class T>
 const T* metric_t(const CGrid* c, int k) {
-  if constexpr (sizeof(T) == 8) return c->metric(k);
-  else return c->met32 + (long long)k * c->g.fs;
+  if constexpr (sizeof(T) == 8) return c->met ? c->metric(k) : nullptr;
+  else return c->met32 ? c->met32 + (long long)k * c->g.fs : nullptr;
 }
 
 // Kernel arguments in precision T: FP64 metric and work fields, or the
@@ -1166,7 +1166,7 @@ CArgsT<T> base_args(const CGrid* c, int ord = 0) {
   else a.ops = o21 ? c->ops21_32 : c->ops32;
   a.dx1 = T(1.0 / (c->radius * c->hx));
   auto M = [&](int k) { return metric_t<T>(c, k); };
-  auto Wk = [&](int k) { return reinterpret_cast<T*>(c->work(k)); };
+  auto Wk = [&](int k) { return c->wk ? reinterpret_cast<T*>(c->work(k)) : nullptr; };
   a.Jp = M(M_JP); a.fp = M(M_FP); a.rJp = M(M_RJP);
   a.rJpha = M(M_RJPHA); a.JQi2p = M(M_JQI2P);
   a.Ju = M(M_JU); a.Qi1u = M(M_QI1U); a.rJu = M(M_RJU);
@@ -1561,8 +1561,12 @@ void build_xy_weights(int N, double hx, std::vector<double>& w, std::vector<int>
 
 }  // namespace
 
-int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
-                 bool fp32, cudaStream_t st, CGrid** out, std::string& why) {
+namespace {
+
+// tables_only: the cross-halo tables and ECS weights alone (no metric, work
+// or RK fields), for the ECS halos of another grid's context.
+int create_impl(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
+                bool fp32, bool tables_only, cudaStream_t st, CGrid** out, std::string& why) {
   *out = nullptr;
   if (order != 21 && order != 42) { why = "C-grid SBP order must be 21 or 42"; return 1; }
   if (N < 12) { why = "C grid needs N >= 12"; return 1; }
@@ -1604,9 +1608,11 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   cudaError_t e = cudaSuccess;
   auto ok = [&](cudaError_t x) { if (e == cudaSuccess) e = x; return e == cudaSuccess; };
   const size_t fb = sizeof(double) * g.fs;
-  ok(cudaMalloc(&c->met, M_COUNT * fb));
-  ok(cudaMalloc(&c->wk, W_COUNT * fb));
-  ok(cudaMalloc(&c->rk, 9 * fb));
+  if (!tables_only) {
+    ok(cudaMalloc(&c->met, M_COUNT * fb));
+    ok(cudaMalloc(&c->wk, W_COUNT * fb));
+    ok(cudaMalloc(&c->rk, 9 * fb));
+  }
   ok(cudaMalloc(&c->halo, sizeof(int) * tab.size()));
   ok(cudaMalloc(&c->ecs_w, sizeof(double) * ew.size()));
   ok(cudaMalloc(&c->ecs_ind, sizeof(int) * eind.size()));
@@ -1620,8 +1626,8 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     // metric of the four meshes (mesh_factory_mod.f90:25-133: alpha =
     // alpha0 + (i - 1 + shift_i) hx, shift 1/2 at centres, 0 on faces and
     // corners), one field at a time through a host buffer
-    std::vector<double> hm(g.fs, 0.0);
-    for (int k = 0; k < M_COUNT && e == cudaSuccess; ++k) {
+    std::vector<double> hm(tables_only ? 0 : g.fs, 0.0);
+    for (int k = 0; k < (tables_only ? 0 : M_COUNT) && e == cudaSuccess; ++k) {
       std::fill(hm.begin(), hm.end(), 0.0);
       const int mesh = kMetricMesh[k];
       const bool ci = mesh == 0 || mesh == 2;  // centred in alpha
@@ -1652,8 +1658,10 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
           }
       ok(cudaMemcpy(c->met + (size_t)k * g.fs, hm.data(), fb, cudaMemcpyHostToDevice));
     }
-    ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
-    ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
+    if (!tables_only) {
+      ok(cudaMemsetAsync(c->wk, 0, W_COUNT * fb, st));
+      ok(cudaMemsetAsync(c->rk, 0, 9 * fb, st));
+    }
     ok(cudaMemcpyAsync(c->halo, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->ecs_w, ew.data(), sizeof(double) * ew.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->ecs_ind, eind.data(), sizeof(int) * eind.size(), cudaMemcpyHostToDevice, st));
@@ -1661,7 +1669,7 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
     ok(cudaMemcpyAsync(c->ecs_jr, ejr.data(), sizeof(double) * ejr.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->xy_w, xyw.data(), sizeof(double) * xyw.size(), cudaMemcpyHostToDevice, st));
     ok(cudaMemcpyAsync(c->xy_ind, xyind.data(), sizeof(int) * xyind.size(), cudaMemcpyHostToDevice, st));
-    if (fp32 && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
+    if (fp32 && !tables_only && ok(cudaMalloc(&c->met32, sizeof(float) * M_COUNT * g.fs)))
       ok(launch_to_f32(c->met, c->met32, (long long)M_COUNT * g.fs, st));  // rounded once
     ok(cudaMemcpyAsync(c->wts, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st));
     ok(cudaStreamSynchronize(st));  // the host buffers go out of scope
@@ -1673,6 +1681,18 @@ int cgrid_create(const FieldGeom& g, int N, int order, double radius, double gra
   }
   *out = c;
   return 0;
+}
+
+}  // namespace
+
+int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega, const double axis[3],
+                 bool fp32, cudaStream_t st, CGrid** out, std::string& why) {
+  return create_impl(g, N, order, radius, grav, omega, axis, fp32, false, st, out, why);
+}
+
+int cgrid_create_tables(const FieldGeom& g, int N, double radius, cudaStream_t st, CGrid** out, std::string& why) {
+  const double axis[3] = {0.0, 0.0, 1.0};
+  return create_impl(g, N, 42, radius, 0.0, 0.0, axis, false, true, st, out, why);
 }
 
 void cgrid_destroy(CGrid* c) {
@@ -1969,6 +1989,8 @@ cudaError_t xy_prepare(CGrid* c, bool metric, cudaStream_t st) {
   }
   return cudaSuccess;
 }
+
+cudaError_t cgrid_laplace_ch_prepare(CGrid* c, cudaStream_t st) { return xy_prepare(c, true, st); }
 
 cudaError_t cgrid_ecs_xy_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st) {
   if (halo_width < 1 || halo_width > kXyRows) return cudaErrorInvalidValue;

@@ -30,6 +30,10 @@ struct CGrid;
 // fp32: also keep FP32 copies of the metric for the FP32 form's passes.
 int cgrid_create(const FieldGeom& g, int N, int order, double radius, double grav, double omega,
                  const double axis[3], bool fp32, cudaStream_t st, CGrid** out, std::string& why);
+// Only the cross-halo tables and ECS weights of the four meshes (the same
+// field layout), for the ECS_xy halo and laplace_ch of an Ah-grid context,
+// whose node mesh is the corner mesh.
+int cgrid_create_tables(const FieldGeom& g, int N, double radius, cudaStream_t st, CGrid** out, std::string& why);
 void cgrid_destroy(CGrid* c);
 int cgrid_order(const CGrid* c);
 // points per panel row (nx) and rows (ny) of a mesh
@@ -118,6 +122,9 @@ cudaError_t cgrid_grad_c2_ecs(CGrid* c, const double* f, double* gx, double* gy,
 cudaError_t cgrid_ecs_xy_halo(CGrid* c, const double* f, int halo_width, double* ext_host, cudaStream_t st);
 cudaError_t cgrid_laplace_ch(CGrid* c, const Topology& tp, double* edge, int order, const double* f, double* out,
                              cudaStream_t st);
+// The scratch and metric tables cgrid_laplace_ch allocates on first use, made
+// ahead (outside any stream capture).
+cudaError_t cgrid_laplace_ch_prepare(CGrid* c, cudaStream_t st);
 // SBP_C quadrature of one field of a mesh into *result (device pointer).
 cudaError_t cgrid_mass(CGrid* c, int mesh, const double* f, double* result, cudaStream_t st);
 

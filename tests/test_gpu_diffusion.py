@@ -180,3 +180,85 @@ def test_errors():
         swm.OperatorSWMDiff(small, UV[63], 0.03, H[63], 0.01)
     assert e.value.code == _abi.SWM_E_INVALID
     swm.OperatorSWMDiff(small, UV[42], 0.03, H[42], 0.01)
+
+
+# ----------------------------------------------------------- laplace_ch_halo4
+# hordiff_scalar_Ah / hordiff_vec_xyz_Ah (hordiff_factory_mod.f90:33-40,
+# 196-223): the same diffusion pipeline with laplace_ch_halo4 and its ECS_xy
+# halo as L; the Ah node mesh is the C-grid oracle's corner mesh.
+
+def test_laplace_ch_on_ah_nodes_matches_oracle():
+    N = 32
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    oc = oracle.OracleCDomain(N, 42)
+    f = np.random.default_rng(3).standard_normal((6, N + 1, N + 1))
+    for order in (2, 4):
+        a, b = op.create_field(), op.create_field()
+        a.upload(f)
+        op.laplace_ch(b, a, order)
+        want = oc.laplace_ch(f, order)
+        assert np.linalg.norm(b.download() - want) <= 1e-12 * np.linalg.norm(want)
+    E = op.ecs_xy_halo(a, 3)
+    assert np.abs(E - oc.ecs_xy_halo(f, 3)).max() <= 1e-14 * np.abs(f).max()
+
+
+def test_hordiff_scalar_ah_tendency_matches_oracle():
+    """The h tendency of hordiff_scalar_Ah: -(c^4) L(L(h)), c = coeff a hx,
+    L = laplace_ch_halo4 (the oracle's, on the node mesh)."""
+    N, coeff = 32, 0.01
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    oc = oracle.OracleCDomain(N, 42)
+    dop = swm.OperatorSWMDiff(op, "hordiff_vec_xyz_Ah_sbp_42_narrow", 0.03, "hordiff_scalar_Ah", coeff)
+    h, u, v = _state(N)
+    vin = op.create_stvec()
+    vin.upload(h, u, v)
+    vout = vin.create_similar()
+    dop.apply(vout, vin)
+    c = coeff * 6.371e6 * (0.5 * np.pi / N)
+    want = -((c * c) * (c * c)) * oc.laplace_ch(oc.laplace_ch(h, 4), 4)
+    got = vout.download()[0]
+    assert np.linalg.norm(got - want) <= 1e-11 * np.linalg.norm(want)
+
+
+def test_hordiff_vec_xyz_ah_damps_a_solid_rotation_at_the_exact_rate():
+    """A solid rotation is an l = 1 field in each Cartesian component, so the
+    Cartesian tendency is -4 coeff^4 hx^4 times it; the xyz operator returns
+    its projections on b1 and b2 (hordiff_colocated_mod.f90:41-58, kept as
+    the reference has it), and the laplace_ch_halo4 pipeline gets there at
+    second order four nodes in from the panel edges.  Nearer the edges the
+    reference's operator is O(1) off at every resolution: L(L(.)) of its
+    Laplacian is about 3% off within two nodes of an edge (the C-grid
+    oracle gives the same), and the edge nodes pass contravariant
+    projections through the covariant vector sync
+    (ecs_Ah_vec_sync_covariant)."""
+    errs = []
+    for N in (24, 48):
+        op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+        dop = swm.OperatorSWMDiff(op, "hordiff_vec_xyz_Ah", 0.03, "hordiff_scalar_Ah", 0.03)
+        g = initial.ecs_geometry(N, "ah")
+        W = np.cross(np.broadcast_to(np.array([0.0, 0.0, 1.0]), g["r"].shape), g["r"]) * 20.0
+        u, v = np.sum(W * g["a1"], -1), np.sum(W * g["a2"], -1)
+        h = np.full(u.shape, 5000.0)
+        vin = op.create_stvec()
+        vin.upload(h, u, v)
+        vout = vin.create_similar()
+        dop.apply(vout, vin)
+        _, tu, tv = vout.download()
+        lam = -4.0 * 0.03 ** 4 * (0.5 * np.pi / N) ** 4
+        a1, a2 = g["a1"], g["a2"]
+        g11, g12, g22 = (a1 * a1).sum(-1), (a1 * a2).sum(-1), (a2 * a2).sum(-1)
+        det = g11 * g22 - g12 * g12
+        b1 = (g22[..., None] * a1 - g12[..., None] * a2) / det[..., None]
+        b2 = (-g12[..., None] * a1 + g11[..., None] * a2) / det[..., None]
+        uc, vc = np.sum(W * b1, -1), np.sum(W * b2, -1)
+        inner = (slice(None), slice(4, -4), slice(4, -4))
+        errs.append(max(np.abs(tu - lam * uc)[inner].max(), np.abs(tv - lam * vc)[inner].max()) /
+                    np.abs(lam * uc).max())
+    assert errs[0] < 1e-3 and errs[1] < errs[0] / 2.5, errs
+
+
+def test_laplace_ch_names_need_fp64():
+    op = swm.OperatorSWM(swm.ModelConfig(N=24, sbp_order=42, precision="fp32"))
+    with pytest.raises(swm.SwmError) as e:
+        swm.OperatorSWMDiff(op, "hordiff_vec_xyz_Ah", 0.03, "hordiff_scalar_Ah", 0.01)
+    assert e.value.code == _abi.SWM_E_UNSUPPORTED
