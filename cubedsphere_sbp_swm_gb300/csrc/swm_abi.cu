@@ -1479,14 +1479,16 @@ int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
 // Names of operator_swm_diff's operators (hordiff_factory_mod.f90:27-40)
 // that this library provides: the narrow-Laplacian ones of the Ah grid.
 // kLapCh4: laplace_ch_halo4 with the ECS_xy halo (hordiff_factory_mod.f90:
-// 33-34, 39-40, 196-223: "hordiff_scalar_Ah" and "hordiff_vec_xyz_Ah"), FP64
-// contexts.
-constexpr int kLapCh4 = 4;
+// 33-34, 37-40, 196-223: "hordiff_scalar_Ah" and "hordiff_vec_xyz_Ah");
+// kLapChCov: the same Laplacian on the covariant components as scalars
+// ("hordiff_vec_Ah", hordiff_colocated_mod.f90:25-39).  FP64 contexts.
+constexpr int kLapCh4 = 4, kLapChCov = 5;
 int hordiff_uv_order(const char* name) {
   if (!name) return 0;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_42_narrow")) return 42;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_63_narrow")) return 63;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah")) return kLapCh4;
+  if (!std::strcmp(name, "hordiff_vec_Ah")) return kLapChCov;
   return 0;
 }
 int hordiff_h_order(const char* name) {
@@ -1540,9 +1542,10 @@ CGrid* node_tables(swm_ctx* ctx, int* rc) {
 int diffusion_ws(swm_ctx* ctx, int narrow) {
   const FieldGeom& g = ctx->g64;
   const size_t elt = (size_t)ctx->elt;
-  if (narrow == kLapCh4 && ctx->prec != SWM_FP64_PLAIN)
-    return fail(ctx, SWM_E_UNSUPPORTED, "hordiff_scalar_Ah / hordiff_vec_xyz_Ah run on FP64 contexts");
-  if (narrow != kLapCh4 && ctx->n < 2 * narrow_rows(narrow))
+  const bool ch = narrow == kLapCh4 || narrow == kLapChCov;
+  if (ch && ctx->prec != SWM_FP64_PLAIN)
+    return fail(ctx, SWM_E_UNSUPPORTED, "hordiff_scalar_Ah / hordiff_vec_Ah / hordiff_vec_xyz_Ah run on FP64 contexts");
+  if (!ch && ctx->n < 2 * narrow_rows(narrow))
     return fail(ctx, SWM_E_INVALID, "grid too small for the narrow Laplacian closures");
   if (ctx->prec == SWM_FP32_FUSED && !ctx->edge2)
     CK(cudaMalloc(&ctx->edge2, sizeof(float) * 16 * 6 * ctx->n), "alloc");
@@ -1563,7 +1566,7 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
       CK(launch_f64_to_f32(6 * g.fs, b64, (float*)ctx->b12, ctx->st), "basis f32");
     }
   }
-  if (narrow == kLapCh4) {
+  if (ch) {
     // the corner-mesh tables, the ECS_xy scratch and the metric tables, made
     // here, outside any capture
     int rc;
@@ -1668,6 +1671,31 @@ int enqueue_biharmonic(swm_ctx* ctx, const T* h, const T* u, const T* v) {
 template <class T>
 int enqueue_diffusion_tend(swm_ctx* ctx, const T* h, const T* u, const T* v, T* th, T* tu, T* tv) {
   const FieldGeom& g = ctx->g64;
+  if (ctx->diff_uv == kLapChCov) {
+    // hordiff_vec_Ah (hordiff_colocated_mod.f90:25-39): u and v diffused as
+    // scalars, -(c^4) L(L(.)), then the covariant vector sync; h with its own
+    // operator
+    if constexpr (sizeof(T) == 8) {
+      const long long fs = g.fs;
+      T* F = dwork<T>(ctx, 0);
+      T* L = dwork<T>(ctx, 4);
+      CK(cudaMemcpyAsync(F, h, sizeof(T) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+      CK(cudaMemcpyAsync(F + fs, u, sizeof(T) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+      CK(cudaMemcpyAsync(F + 2 * fs, v, sizeof(T) * fs, cudaMemcpyDeviceToDevice, ctx->st), "copy");
+      if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 1, F, L)) return rc;
+      if (int rc = laplace_fields<T>(ctx, ctx->diff_h, 1, L, F)) return rc;
+      if (int rc = laplace_fields<T>(ctx, kLapCh4, 2, F + fs, L + fs)) return rc;
+      if (int rc = laplace_fields<T>(ctx, kLapCh4, 2, L + fs, F + fs)) return rc;
+      const double ch = diff_coeff4(ctx, ctx->diff_h_coeff), cu = diff_coeff4(ctx, ctx->diff_uv_coeff);
+      CK(launch_axpby(fs, ch, F, 0.0, F, th, ctx->st), "tendency");
+      CK(launch_axpby(fs, cu, F + fs, 0.0, F + fs, tu, ctx->st), "tendency");
+      CK(launch_axpby(fs, cu, F + 2 * fs, 0.0, F + 2 * fs, tv, ctx->st), "tendency");
+      CK(launch_sync_vector_t<T>(g, ctx->topo, ctx->qw, tu, tv, (T*)ctx->edge64, ctx->st), "vector sync");
+      return SWM_OK;
+    } else {
+      return fail(ctx, SWM_E_UNSUPPORTED, "hordiff_vec_Ah runs on FP64 contexts");
+    }
+  }
   if (int rc = enqueue_biharmonic<T>(ctx, h, u, v)) return rc;
   const T* F = dwork<T>(ctx, 0);
   CK(launch_diff_tendency<T>(g, (const T*)ctx->b12, diff_coeff4(ctx, ctx->diff_uv_coeff), F + g.fs,

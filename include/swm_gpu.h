@@ -203,7 +203,9 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
  * the narrow-stencil SBP Laplacian and c = coeff*radius*hx, on h and on the
  * Cartesian components of the velocity.  "hordiff_vec_xyz_Ah" and
  * "hordiff_scalar_Ah" (hordiff_factory_mod.f90:33-40, 196-223) are the same
- * with L = laplace_ch_halo4 and its ECS_xy halo, on FP64 contexts.  On the C grid
+ * with L = laplace_ch_halo4 and its ECS_xy halo, and "hordiff_vec_Ah" that L
+ * on the covariant components as scalars, then the covariant vector sync;
+ * these three on FP64 contexts.  On the C grid
  * (hordiff_factory_mod.f90:19-36, 53-139, 196-247): "hordiff_c_biharm_div",
  * "hordiff_c_biharm_curl" or "hordiff_c_biharm_curl_div" for (u, v) --
  * -(c^4) grad div co2contra grad div co2contra and / or -(c^4) contra2co

@@ -262,3 +262,28 @@ def test_laplace_ch_names_need_fp64():
     with pytest.raises(swm.SwmError) as e:
         swm.OperatorSWMDiff(op, "hordiff_vec_xyz_Ah", 0.03, "hordiff_scalar_Ah", 0.01)
     assert e.value.code == _abi.SWM_E_UNSUPPORTED
+
+
+def test_hordiff_vec_ah_matches_oracle():
+    """hordiff_vec_Ah (hordiff_colocated_mod.f90:25-39): each covariant
+    component diffused as a scalar, -(c^4) L(L(.)) with laplace_ch_halo4,
+    then the covariant vector sync; h by hordiff_scalar_Ah."""
+    N, cuv, chh = 32, 0.03, 0.01
+    op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
+    oc, od = oracle.OracleCDomain(N, 42), oracle.OracleDomain(N, 42)
+    dop = swm.OperatorSWMDiff(op, "hordiff_vec_Ah", cuv, "hordiff_scalar_Ah", chh)
+    h, u, v = _state(N)
+    vin = op.create_stvec()
+    vin.upload(h, u, v)
+    vout = vin.create_similar()
+    dop.apply(vout, vin)
+    hx = 0.5 * np.pi / N
+
+    def c4(coeff):
+        c = coeff * 6.371e6 * hx
+        return -((c * c) * (c * c))
+
+    LL = lambda f: oc.laplace_ch(oc.laplace_ch(f, 4), 4)
+    tu, tv = od.sync_vector_cov(c4(cuv) * LL(u), c4(cuv) * LL(v))
+    for got, want in zip(vout.download(), (c4(chh) * LL(h), tu, tv)):
+        assert np.linalg.norm(got - want) <= 1e-11 * np.linalg.norm(want)
