@@ -196,8 +196,9 @@ class OperatorSWM:
         self._check(self._L.swm_apply_unfused(self._h, vout._h, vin._h))
 
     def laplace(self, out: "GridField", f: "GridField", narrow_order: int = 42):
-        """out = L(f): the narrow-stencil SBP Laplacian laplace_ah_sbp42_narrow /
-        laplace_ah_sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58), edge-synced."""
+        """out = L(f): the narrow-stencil SBP Laplacian laplace_ah_sbp21_narrow /
+        _sbp42_narrow / _sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58,
+        laplace_Ah_sbp21_narrow_mod.f90:23-243), edge-synced."""
         self._check(self._L.swm_laplace(self._h, out._h, f._h, int(narrow_order)))
 
     _BOX_MODES = {"auto": 0, "strip": 1, "widest": 2}

@@ -189,7 +189,7 @@ struct swm_ctx {
   // vectors (6 fields) and 19 FP64 work fields, all allocated on first use
   int diff_uv = 0, diff_h = 0;
   double diff_uv_coeff = 0.0, diff_h_coeff = 0.0;
-  void* ntab[2][5] = {};    // cx, cy, clx, cly, b (context precision)
+  void* ntab[3][5] = {};    // per narrow order (4/2, 6/3, 2/1): cx, cy, clx, cly, b (context precision)
   void* b12 = nullptr;
   void* dw = nullptr;
   // Asynchronous state transfers (swm_state_upload_async / _download_async),
@@ -1477,7 +1477,8 @@ int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
 
 // ------------------------------------------------------- hyperdiffusion
 // Names of operator_swm_diff's operators (hordiff_factory_mod.f90:27-40)
-// that this library provides: the narrow-Laplacian ones of the Ah grid.
+// that this library provides: the narrow-Laplacian ones of the Ah grid
+// (SBP 2/1, 4/2 and 6/3).
 // kLapCh4: laplace_ch_halo4 with the ECS_xy halo (hordiff_factory_mod.f90:
 // 33-34, 37-40, 196-223: "hordiff_scalar_Ah" and "hordiff_vec_xyz_Ah");
 // kLapChCov: the same Laplacian on the covariant components as scalars
@@ -1485,6 +1486,7 @@ int enqueue_rk4_any(swm_ctx* ctx, swm_state* v0, double dt) {
 constexpr int kLapCh4 = 4, kLapChCov = 5;
 int hordiff_uv_order(const char* name) {
   if (!name) return 0;
+  if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_21_narrow")) return 21;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_42_narrow")) return 42;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah_sbp_63_narrow")) return 63;
   if (!std::strcmp(name, "hordiff_vec_xyz_Ah")) return kLapCh4;
@@ -1493,6 +1495,7 @@ int hordiff_uv_order(const char* name) {
 }
 int hordiff_h_order(const char* name) {
   if (!name) return 0;
+  if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_21_narrow")) return 21;
   if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_42_narrow")) return 42;
   if (!std::strcmp(name, "hordiff_scalar_Ah_sbp_63_narrow")) return 63;
   if (!std::strcmp(name, "hordiff_scalar_Ah")) return kLapCh4;
@@ -1519,7 +1522,7 @@ constexpr int kDiffWorkF32 = 11, kDiffWorkF64 = 19;
 
 template <class T>
 NarrowTables<T> narrow_tables(swm_ctx* ctx, int narrow) {
-  void* const* t = ctx->ntab[narrow == 63 ? 1 : 0];
+  void* const* t = ctx->ntab[narrow == 63 ? 1 : narrow == 21 ? 2 : 0];
   return NarrowTables<T>{narrow, (T*)t[0], (T*)t[1], (T*)t[2], (T*)t[3], (T*)t[4]};
 }
 template <class T> T* dwork(swm_ctx* ctx, int field) { return (T*)ctx->dw + field * ctx->g64.fs; }
@@ -1575,7 +1578,7 @@ int diffusion_ws(swm_ctx* ctx, int narrow) {
     CK(cgrid_laplace_ch_prepare(q, ctx->st), "laplace_ch tables");
     return SWM_OK;
   }
-  void** t = ctx->ntab[narrow == 63 ? 1 : 0];
+  void** t = ctx->ntab[narrow == 63 ? 1 : narrow == 21 ? 2 : 0];
   if (!t[2]) {
     // FP32 contexts form the interior coefficients from the two b fields
     const bool f64 = ctx->prec == SWM_FP64_PLAIN;
@@ -1879,8 +1882,8 @@ int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_or
   TraceRange trace_("swm_laplace");
   if (int rc = check_field(ctx, out)) return rc;
   if (int rc = check_field(ctx, in)) return rc;
-  if (narrow_order != 42 && narrow_order != 63)
-    return fail(ctx, SWM_E_UNSUPPORTED, "narrow Laplacian order must be 42 or 63");
+  if (narrow_order != 21 && narrow_order != 42 && narrow_order != 63)
+    return fail(ctx, SWM_E_UNSUPPORTED, "narrow Laplacian order must be 21, 42 or 63");
   if (ctx->prec != SWM_FP64_PLAIN)
     return fail(ctx, SWM_E_UNSUPPORTED, "swm_laplace works on FP64 contexts");
   USE_DEVICE(ctx);

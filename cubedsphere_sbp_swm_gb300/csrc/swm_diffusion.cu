@@ -4,8 +4,9 @@
 // of a diffusion operator (ts2_mod.f90:143-146,
 // operator_swm_diff_mod.f90:25-46): the biharmonic -(c^4) L(L(h)) of the
 // depth and of the three Cartesian components of the velocity, with L the
-// narrow-stencil SBP Laplacian of order 4/2 or 6/3
-// (laplace_Ah_sbp42_narrow_mod.f90:23-763 and its 6/3 twin).
+// narrow-stencil SBP Laplacian of order 4/2, 6/3 or 2/1
+// (laplace_Ah_sbp42_narrow_mod.f90:23-763, its 6/3 twin and
+// laplace_Ah_sbp21_narrow_mod.f90:23-243).
 //
 // The narrow second-derivative operators have variable coefficients
 // b = J*Qi11 (x) and J*Qi22 (y), which depend on the grid only, so the
@@ -36,49 +37,52 @@ namespace {
 constexpr int DTPB = 256;
 inline int dblk(long long count) { return (int)((count + DTPB - 1) / DTPB); }
 
-__constant__ NarrowD2 c_narrow[2] = {kNarrow42, kNarrow63};
+// table index of an order: [0] 4/2, [1] 6/3, [2] 2/1
+constexpr int narrow_index(int narrow) { return narrow == 63 ? 1 : narrow == 21 ? 2 : 0; }
+constexpr NarrowD2 kNarrowAll[3] = {kNarrow42, kNarrow63, kNarrow21};
+__constant__ NarrowD2 c_narrow[3] = {kNarrow42, kNarrow63, kNarrow21};
 
-// Interior stencil matrices of both orders in FP32 ([0] 4/2, [1] 6/3).
+// Interior stencil matrices of the three orders in FP32.
 struct NarrowIn32 {
-  float v[2][NARROW_MAXW][NARROW_MAXW];
+  float v[3][NARROW_MAXW][NARROW_MAXW];
 };
 constexpr NarrowIn32 make_narrow_in32() {
   NarrowIn32 t{};
   for (int o = 0; o < NARROW_MAXW; ++o)
-    for (int q = 0; q < NARROW_MAXW; ++q) {
-      t.v[0][o][q] = float(kNarrow42.in[o][q]);
-      t.v[1][o][q] = float(kNarrow63.in[o][q]);
-    }
+    for (int q = 0; q < NARROW_MAXW; ++q)
+      for (int x = 0; x < 3; ++x) t.v[x][o][q] = float(kNarrowAll[x].in[o][q]);
   return t;
 }
 __constant__ NarrowIn32 c_in32 = make_narrow_in32();
 
-// Closure row scales and the flux penalty of both orders in FP32 (rounded at
-// compile time: the FP32 Laplacian converts no coefficient at run time).
+// Closure row scales and the flux penalty of the three orders in FP32
+// (rounded at compile time: the FP32 Laplacian converts no coefficient at run
+// time).
 struct NarrowScale32 {
-  float rowscale[2][NARROW_MAXR];
-  float penalty[2];
+  float rowscale[3][NARROW_MAXR];
+  float penalty[3];
 };
 constexpr NarrowScale32 make_narrow_scale32() {
   NarrowScale32 t{};
-  for (int r = 0; r < NARROW_MAXR; ++r) {
-    t.rowscale[0][r] = float(kNarrow42.rowscale[r]);
-    t.rowscale[1][r] = float(kNarrow63.rowscale[r]);
+  for (int x = 0; x < 3; ++x) {
+    for (int r = 0; r < NARROW_MAXR; ++r) t.rowscale[x][r] = float(kNarrowAll[x].rowscale[r]);
+    t.penalty[x] = float(kNarrowAll[x].penalty);
   }
-  t.penalty[0] = float(kNarrow42.penalty);
-  t.penalty[1] = float(kNarrow63.penalty);
   return t;
 }
 __constant__ NarrowScale32 c_scale32 = make_narrow_scale32();
 
 template <int NARROW>
 struct NarrowShape {
-  static constexpr int ni = NARROW == 63 ? 1 : 0;
-  static constexpr int rows = NARROW == 63 ? kNarrow63.rows : kNarrow42.rows;
-  static constexpr int cols = NARROW == 63 ? kNarrow63.cols : kNarrow42.cols;
-  static constexpr int nb = NARROW == 63 ? kNarrow63.nb : kNarrow42.nb;
-  static constexpr int hw = NARROW == 63 ? kNarrow63.hw : kNarrow42.hw;
+  static constexpr int ni = narrow_index(NARROW);
+  static constexpr int rows = kNarrowAll[ni].rows;
+  static constexpr int cols = kNarrowAll[ni].cols;
+  static constexpr int nb = kNarrowAll[ni].nb;
+  static constexpr int hw = kNarrowAll[ni].hw;
   static constexpr int w = 2 * hw + 1;
+  // stencil taps a node keeps: a closure row's cols or the interior's w
+  // (2/1: 2 and 3)
+  static constexpr int taps = cols > w ? cols : w;
 };
 
 // Node kernels run on 2-D tiles of TX columns x TY rows of the (6n)-row
@@ -409,7 +413,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
   const bool clyn = j < S::rows || j >= n - S::rows;
   // stencil of this node in x and y: coefficients and tap offsets in the
   // region; the interior uses the first w taps
-  T ax[S::cols], ay[S::cols];
+  T ax[S::taps], ay[S::taps];
   int x0, xs, y0, ys;
   T rsx = T(1), rsy = T(1);
   if (clxn) {
@@ -421,7 +425,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
     rsx = c_scale32.rowscale[S::ni][r];
   } else {   // from the variable coefficients along the row
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) {
+    for (int c = 0; c < S::taps; ++c) {
       T acc = T(0);
       if (c < S::w) {
 #pragma unroll
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(LTPB, 4) lap_tile_kernel(FieldGeom g, int nty,
     rsy = c_scale32.rowscale[S::ni][r];
   } else {   // from the variable coefficients along the column
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) {
+    for (int c = 0; c < S::taps; ++c) {
       T acc = T(0);
       if (c < S::w) {
 #pragma unroll
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
   const bool clyn = k.j < S::rows || k.j >= n - S::rows;
   // stencil of this node in x and y: coefficients and tap offsets (inside
   // the panel); the interior uses the first w taps
-  T ax[S::cols], ay[S::cols];
+  T ax[S::taps], ay[S::taps];
   int x0, xs, y0, ys;
   T rsx = T(1), rsy = T(1);
   if (clxn) {
@@ -551,7 +555,7 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     rsx = T(D.rowscale[r]);
   } else {
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
+    for (int c = 0; c < S::taps; ++c) ax[c] = c < S::w ? cx[c * g.fs + pb + o] : T(0);
     x0 = o - S::hw; xs = 1;
   }
   if (clyn) {
@@ -563,7 +567,7 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     rsy = T(D.rowscale[r]);
   } else {
 #pragma unroll
-    for (int c = 0; c < S::cols; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
+    for (int c = 0; c < S::taps; ++c) ay[c] = c < S::w ? cy[c * g.fs + pb + o] : T(0);
     y0 = o - S::hw * P; ys = P;
   }
   const int ntx = clxn ? S::cols : S::w, nty = clyn ? S::cols : S::w;
@@ -575,10 +579,10 @@ __global__ void __launch_bounds__(RTPB) lap_main_kernel(FieldGeom g, const T* f,
     const T* F = f + c * g.fs + pb;
     T sx = T(0), sy = T(0);
 #pragma unroll
-    for (int t = 0; t < S::cols; ++t)
+    for (int t = 0; t < S::taps; ++t)
       if (t < ntx) sx += ax[t] * F[x0 + xs * t];
 #pragma unroll
-    for (int t = 0; t < S::cols; ++t)
+    for (int t = 0; t < S::taps; ++t)
       if (t < nty) sy += ay[t] * F[y0 + ys * t];
     T d2x = clxn ? rsx * sx : sx;
     const T d2y = clyn ? rsy * sy : sy;
@@ -756,9 +760,9 @@ __global__ void to_f32_kernel(long long count, const double* s, float* d) {
 
 }  // namespace
 
-int narrow_rows(int narrow) { return narrow == 63 ? kNarrow63.rows : kNarrow42.rows; }
-int narrow_cols(int narrow) { return narrow == 63 ? kNarrow63.cols : kNarrow42.cols; }
-int narrow_width(int narrow) { return narrow == 63 ? 2 * kNarrow63.hw + 1 : 2 * kNarrow42.hw + 1; }
+int narrow_rows(int narrow) { return kNarrowAll[narrow_index(narrow)].rows; }
+int narrow_cols(int narrow) { return kNarrowAll[narrow_index(narrow)].cols; }
+int narrow_width(int narrow) { return 2 * kNarrowAll[narrow_index(narrow)].hw + 1; }
 long long narrow_closure_count(int narrow, int n) {
   return 6LL * n * 2 * narrow_rows(narrow) * narrow_cols(narrow);
 }
@@ -818,12 +822,17 @@ cudaError_t launch_narrow_tables(const FieldGeom& g, const NarrowTables<T>& t, c
                                  cudaStream_t st) {
   const long long ncl = narrow_closure_count(t.narrow, g.n);
   if constexpr (sizeof(T) == 4) {
-    cudaError_t e = t.narrow == 63 ? prepare_laplace_order<63>() : prepare_laplace_order<42>();
+    cudaError_t e = t.narrow == 63   ? prepare_laplace_order<63>()
+                    : t.narrow == 21 ? prepare_laplace_order<21>()
+                                     : prepare_laplace_order<42>();
     if (e != cudaSuccess) return e;
   }
   if (t.narrow == 63) {
     narrow_coef_kernel<T, 63><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy, t.b);
     narrow_closure_kernel<T, 63><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
+  } else if (t.narrow == 21) {
+    narrow_coef_kernel<T, 21><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy, t.b);
+    narrow_closure_kernel<T, 21><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
   } else {
     narrow_coef_kernel<T, 42><<<row_grid(g), row_block(), 0, st>>>(g, m, t.cx, t.cy, t.b);
     narrow_closure_kernel<T, 42><<<dblk(ncl), DTPB, 0, st>>>(g, m, t.clx, t.cly);
@@ -841,6 +850,10 @@ cudaError_t launch_laplace(const FieldGeom& g, const Topology& tp, const NarrowT
     if (nf == 1) e = laplace_nf<T, 63, 1>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
     else if (nf == 3) e = laplace_nf<T, 63, 3>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
     else e = laplace_nf<T, 63, 4>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+  } else if (t.narrow == 21) {
+    if (nf == 1) e = laplace_nf<T, 21, 1>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+    else if (nf == 3) e = laplace_nf<T, 21, 3>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
+    else e = laplace_nf<T, 21, 4>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
   } else {
     if (nf == 1) e = laplace_nf<T, 42, 1>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);
     else if (nf == 3) e = laplace_nf<T, 42, 3>(g, tp, t, f, mt, hs, d1x, d1y, out, edge, nullptr, st);

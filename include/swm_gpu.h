@@ -196,10 +196,9 @@ int swm_rk4_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
  * 143-146, barotropic_inst_mod.f90:163-168).  swm_diffusion_set takes the
  * namelist's hordiff_uv_name / uv_diff_coeff / hordiff_h_name /
  * h_diff_coeff (config_swm_mod.f90:24-27, operator_swm_diff_factory_mod.f90
- * :27-30).  Supported names on the Ah grid: "hordiff_vec_xyz_Ah_sbp_42_narrow"
- * and "hordiff_vec_xyz_Ah_sbp_63_narrow" for (u, v); "hordiff_scalar_Ah_sbp_
- * 42_narrow" and "hordiff_scalar_Ah_sbp_63_narrow" for h
- * (hordiff_factory_mod.f90:27-40).  The operator is -(c^4) L(L(.)) with L
+ * :27-30).  Supported names on the Ah grid: "hordiff_vec_xyz_Ah_sbp_NN_narrow"
+ * for (u, v) and "hordiff_scalar_Ah_sbp_NN_narrow" for h, NN = 21, 42 or 63
+ * (hordiff_factory_mod.f90:27-46).  The operator is -(c^4) L(L(.)) with L
  * the narrow-stencil SBP Laplacian and c = coeff*radius*hx, on h and on the
  * Cartesian components of the velocity.  "hordiff_vec_xyz_Ah" and
  * "hordiff_scalar_Ah" (hordiff_factory_mod.f90:33-40, 196-223) are the same
@@ -227,10 +226,10 @@ int swm_diffusion_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
  * the diffusion step, both as one CUDA graph per step; without
  * swm_diffusion_set the same as swm_rk4_step. */
 int swm_model_step(swm_ctx* ctx, swm_state* v0, double dt, int nsteps);
-/* out = L(in): laplace_operator_t%calc_laplace of laplace_ah_sbp42_narrow /
- * laplace_ah_sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58,
- * laplace_factory_mod.f90:179-250) on FP64 fields, edge-synced; out may be
- * in.  narrow_order = 42 or 63. */
+/* out = L(in): laplace_operator_t%calc_laplace of laplace_ah_sbp21_narrow /
+ * _sbp42_narrow / _sbp63_narrow (laplace_Ah_sbp42_narrow_mod.f90:23-58,
+ * laplace_Ah_sbp21_narrow_mod.f90:23-243, laplace_factory_mod.f90:179-250)
+ * on FP64 fields, edge-synced; out may be in.  narrow_order = 21, 42 or 63. */
 int swm_laplace(swm_ctx* ctx, swm_field* out, const swm_field* in, int narrow_order);
 
 /* get_diagnostics (operator_swm_mod.f90:115-155): out[7] = hmin, hmax,

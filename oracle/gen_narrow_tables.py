@@ -1,5 +1,6 @@
 """Generate swm_narrow_tables.h: the coefficient tables of the narrow-stencil
-variable-coefficient SBP second-derivative operators of orders 4/2 and 6/3.
+variable-coefficient SBP second-derivative operators of orders 4/2, 6/3 and
+2/1.
 
 These are tables of published constants: closure row r of the operator
 D2^(b) near a boundary is  (D2 f)_r = s_r * sum_c M[r][c] f_c  with
@@ -10,7 +11,12 @@ derived independently of their construction, so they are read from the
 reference's own source (differential_operators/horizontal/laplace/
 laplace_Ah_sbp42_narrow_mod.f90:128-274 and laplace_Ah_sbp63_narrow_mod.f90:
 11-481, 600-880) and written out as C++ constant expressions in the same
-literal form (each literal and quotient rounds to the same double).
+literal form (each literal and quotient rounds to the same double).  The 2/1
+operator (laplace_Ah_sbp21_narrow_mod.f90:125-195) has no literals to read:
+its closure row is (b_1 + b_2)(f_2 - f_1) and its interior stencil the
+face-averaged ((b_i + b_{i+1})/2 (f_{i+1} - f_i) - (b_{i-1} + b_i)/2
+(f_i - f_{i-1})), with the boundary flux weight 2 (lines 200-225); the script
+states these directly.
 
 The script checks what it extracts: the four closure blocks of each file
 (x left/right, y left/right) carry identical formulas; every closure row and
@@ -149,6 +155,12 @@ def build(ref):
     Wc = {o: {q: s + params[v] for q, (s, v) in row.items()} for o, row in W.items()}
     tables.append(dict(order=63, rows=9, hw=3, rowscale={r: "1.0" for r in range(1, 10)},
                        C=C, W=Wc, penalty="43200.0/13649"))
+
+    # --- 2/1: cc = -(b_1 + b_2), cp = b_1 + b_2 at the closure row; interior
+    # cm = (b_m + b_c)/2, cc = -(b_m + 2 b_c + b_p)/2, cp = (b_p + b_c)/2
+    C = {(1, 1, 1): "-1.0", (1, 1, 2): "-1.0", (1, 2, 1): "1.0", (1, 2, 2): "1.0"}
+    W = {0: {0: "1.0/2", 1: "1.0/2"}, 1: {0: "-1.0/2", 1: "-1.0", 2: "-1.0/2"}, 2: {1: "1.0/2", 2: "1.0/2"}}
+    tables.append(dict(order=21, rows=1, hw=1, rowscale={1: "1.0"}, C=C, W=W, penalty="2.0"))
     return tables
 
 
@@ -161,7 +173,7 @@ def check(t):
         m2 = s * sum(v * (c - r) ** 2 for (rr, c, k), v in val.items() if rr == r)
         if not (t["order"] == 63 and r == 1):
             assert abs(m0) < Fraction(1, 10 ** 12), (t["order"], r, float(m0))
-        if t["order"] == 42 or r > 1:
+        if t["order"] != 63 or r > 1:
             assert abs(m2 - 2) < Fraction(1, 10 ** 9), (t["order"], r, float(m2))
     wv = {(o, q): exact(v) for o, row in t["W"].items() for q, v in row.items()}
     assert abs(sum(wv.values())) < Fraction(1, 10 ** 14)
@@ -172,8 +184,9 @@ def emit(tables):
     L = ["// swm_narrow_tables.h -- generated by oracle/gen_narrow_tables.py; do not edit.",
          "//",
          "// Narrow-stencil variable-coefficient SBP second-derivative operators of",
-         "// orders 4/2 and 6/3, as the reference states them",
-         "// (laplace_Ah_sbp42_narrow_mod.f90:128-274, laplace_Ah_sbp63_narrow_mod.f90:11-481).",
+         "// orders 4/2, 6/3 and 2/1, as the reference states them",
+         "// (laplace_Ah_sbp42_narrow_mod.f90:128-274, laplace_Ah_sbp63_narrow_mod.f90:11-481,",
+         "// laplace_Ah_sbp21_narrow_mod.f90:125-195).",
          "// Closure row r (0-based from the boundary) of D2^(b):",
          "//   (D2 f)_r = rowscale[r] * sum_c (sum_k c[r][c][k] * b_k) * f_c",
          "// Interior node i:",
@@ -186,7 +199,7 @@ def emit(tables):
          "constexpr int NARROW_MAXR = 9, NARROW_MAXC = 12, NARROW_MAXW = 7;",
          "",
          "struct NarrowD2 {",
-         "  int order;      // 42 or 63",
+         "  int order;      // 42, 63 or 21",
          "  int rows;       // closure rows at each end",
          "  int cols;       // nodes a closure row reads",
          "  int nb;         // coefficient nodes a closure row reads",

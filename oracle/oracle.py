@@ -245,7 +245,7 @@ class OracleDomain:
         lib().orc_diagnostics(self._h, _p(hs), _p(h), _p(u), _p(v), _p(out))
         return out
 
-    # hyperdiffusion (narrow = 42 or 63: the narrow Laplacian's SBP order)
+    # hyperdiffusion (narrow = 21, 42 or 63: the narrow Laplacian's SBP order)
     def laplace(self, f, narrow=42):
         out = self.zeros()
         assert lib().orc_laplace(self._h, int(narrow), _p(np.ascontiguousarray(f)), _p(out)) == 0

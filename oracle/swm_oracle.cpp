@@ -576,7 +576,9 @@ void set_vector(const orc_domain& d, Gen gen, bool contravariant, std::vector<do
 // ---------------------------------------------------------------------------
 using swm::NarrowD2;
 
-const NarrowD2& narrow_table(int order) { return order == 63 ? swm::kNarrow63 : swm::kNarrow42; }
+const NarrowD2& narrow_table(int order) {
+  return order == 63 ? swm::kNarrow63 : order == 21 ? swm::kNarrow21 : swm::kNarrow42;
+}
 
 // Narrow variable-coefficient second derivative D2^(b) at node k of a line of
 // n values f with coefficients b (stride st): closure rows near either end
@@ -606,8 +608,8 @@ double d2_point(const NarrowD2& T, const double* f, const double* b, int n, int 
   return acc;
 }
 
-// laplace_Ah_sbp{42,63}_narrow calc_laplace (laplace_Ah_sbp42_narrow_mod.f90:
-// 23-58): first derivatives times J*Qi12 (calc_tile_d1x_d1y, 60-93), the
+// laplace_Ah_sbp{42,63,21}_narrow calc_laplace (laplace_Ah_sbp42_narrow_mod.f90:
+// 23-58, laplace_Ah_sbp21_narrow_mod.f90:23-243): first derivatives times J*Qi12 (calc_tile_d1x_d1y, 60-93), the
 // narrow D2 along x with b = J*Qi11 and along y with b = J*Qi22, the
 // cross-derivative boundary fluxes on the x rows (717-743), the mixed terms
 // D_y(d1f_x) + D_x(d1f_y) (745-752), division by (hx*scale)^2 and by J, then
@@ -812,7 +814,7 @@ void latlon_vector(const orc_domain& d, const LatLonInterp& L, bool contravarian
 }
 
 bool narrow_ok(const orc_domain& d, int narrow) {
-  return (narrow == 42 || narrow == 63) && d.n >= 2 * narrow_table(narrow).rows;
+  return (narrow == 21 || narrow == 42 || narrow == 63) && d.n >= 2 * narrow_table(narrow).rows;
 }
 
 }  // namespace

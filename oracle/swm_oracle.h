@@ -74,8 +74,8 @@ void orc_rk4(const orc_domain* d, const double* hs, double* h, double* u,
 /* out[7] = hmin, hmax, mass, TE, KE, PE, Enstrophy (operator_swm_mod.f90:115-155) */
 void orc_diagnostics(const orc_domain* d, const double* hs, const double* h,
                      const double* u, const double* v, double out[7]);
-/* Hyperdiffusion (operator_swm_diff_mod.f90:25-46): narrow = 42 or 63 picks
- * laplace_ah_sbp42_narrow / laplace_ah_sbp63_narrow; coefficients as the
+/* Hyperdiffusion (operator_swm_diff_mod.f90:25-46): narrow = 21, 42 or 63
+ * picks laplace_ah_sbp21_narrow / _sbp42_narrow / _sbp63_narrow; coefficients as the
  * namelist's uv_diff_coeff / h_diff_coeff.  Return 0, or -1 for a bad order
  * or a grid too small for the closures. */
 int orc_laplace(const orc_domain* d, int narrow, const double* f, double* out);

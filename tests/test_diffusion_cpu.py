@@ -1,5 +1,5 @@
 """Hyperdiffusion in the CPU oracle: the narrow-stencil SBP Laplacians of
-orders 4/2 and 6/3 and the biharmonic diffusion operator built on them
+orders 4/2, 6/3 and 2/1 and the biharmonic diffusion operator built on them
 (operator_swm_diff_mod.f90:25-46).
 
 The reference holds no golden values for these operators (its Laplacian test
@@ -9,8 +9,8 @@ pinned by properties that a wrong coefficient, sign or scaling breaks:
 - the spherical harmonic Y_2^2 = cos(2 lambda) cos^2(phi) is an eigenfunction
   of the unit-sphere Laplacian with eigenvalue -6 (the reference's own test
   field, test_diffops_mod.f90:180-229): the interior error converges at the
-  interior order (4 / 6), the quadrature-RMS error at about the closure
-  order (2 / 3);
+  interior order (4 / 6 / 2), the quadrature-RMS error at about the closure
+  order (2 / 3) plus one half (2/1: first-order closure rows, rate 1.5);
 - L is symmetric and negative definite in the SBP quadrature inner product
   (relative asymmetry <= 1e-13);
 - so the diffusion operator conserves mass (quadrature sum of D h ~ 0) and
@@ -20,7 +20,7 @@ import pytest
 
 import oracle as O
 
-NARROW = (42, 63)
+NARROW = (21, 42, 63)
 
 
 def _ylm22(d):
@@ -44,8 +44,10 @@ def test_laplacian_of_a_constant_vanishes(narrow):
     assert np.abs(L).max() < 1e-14
 
 
-@pytest.mark.parametrize("narrow,interior_rate,rms_rate", [(42, 14.0, 3.5), (63, 30.0, 6.0)])
-def test_spherical_harmonic_eigenvalue_and_convergence(narrow, interior_rate, rms_rate):
+@pytest.mark.parametrize("narrow,i_max,r_max,interior_rate,rms_rate",
+                         [(42, 4e-5, 3e-3, 14.0, 3.5), (63, 4e-5, 3e-3, 30.0, 6.0),
+                          (21, 1e-2, 1.2e-2, 3.8, 2.6)])
+def test_spherical_harmonic_eigenvalue_and_convergence(narrow, i_max, r_max, interior_rate, rms_rate):
     errs = []
     for N in (32, 64):
         d = _dom(N, narrow)
@@ -54,7 +56,7 @@ def test_spherical_harmonic_eigenvalue_and_convergence(narrow, interior_rate, rm
         w = 10
         errs.append((e[:, w:-w, w:-w].max(), np.sqrt(d.mass(e * e) / d.mass(np.ones_like(e)))))
     (i32, r32), (i64, r64) = errs
-    assert r32 < 3e-3 and i32 < 4e-5
+    assert r32 < r_max and i32 < i_max
     assert i32 / i64 > interior_rate
     assert r32 / r64 > rms_rate
 
@@ -83,7 +85,7 @@ def test_biharmonic_is_minus_c4_laplacian_squared(narrow):
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("uv_narrow,h_narrow", [(42, 42), (63, 63), (63, 42)])
+@pytest.mark.parametrize("uv_narrow,h_narrow", [(42, 42), (63, 63), (63, 42), (21, 21)])
 def test_diffusion_conserves_mass_and_dissipates(uv_narrow, h_narrow):
     from cubedsphere_sbp_swm_gb300 import initial
     N = 32

@@ -18,8 +18,8 @@ from gpu_helpers import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-UV = {42: "hordiff_vec_xyz_Ah_sbp_42_narrow", 63: "hordiff_vec_xyz_Ah_sbp_63_narrow"}
-H = {42: "hordiff_scalar_Ah_sbp_42_narrow", 63: "hordiff_scalar_Ah_sbp_63_narrow"}
+UV = {k: "hordiff_vec_xyz_Ah_sbp_%d_narrow" % k for k in (21, 42, 63)}
+H = {k: "hordiff_scalar_Ah_sbp_%d_narrow" % k for k in (21, 42, 63)}
 
 
 def _state(N, seed=5):
@@ -32,7 +32,7 @@ def _state(N, seed=5):
     return h, u, v
 
 
-@pytest.mark.parametrize("narrow,N", [(42, 32), (63, 32), (63, 48)])
+@pytest.mark.parametrize("narrow,N", [(42, 32), (63, 32), (63, 48), (21, 32), (21, 9)])
 def test_laplace_matches_oracle(narrow, N):
     op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
     od = oracle.OracleDomain(N, 42)
@@ -48,7 +48,7 @@ def test_laplace_matches_oracle(narrow, N):
     assert rel_l2(fi.download(), ref, J) <= 1e-12
 
 
-@pytest.mark.parametrize("uv_narrow,h_narrow", [(42, 42), (63, 63), (63, 42)])
+@pytest.mark.parametrize("uv_narrow,h_narrow", [(42, 42), (63, 63), (63, 42), (21, 21), (42, 21)])
 def test_diffusion_operator_matches_oracle(uv_narrow, h_narrow):
     N = 32
     op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
@@ -64,11 +64,13 @@ def test_diffusion_operator_matches_oracle(uv_narrow, h_narrow):
         assert rel_l2(a, b, J) <= 1e-12
 
 
-@pytest.mark.parametrize("order", [42, 63])
-def test_model_step_matches_oracle(order):
+@pytest.mark.parametrize("order,narrow", [(42, 42), (63, 63), (42, 21)])
+def test_model_step_matches_oracle(order, narrow):
+    """The 2/1 hyperdiffusion runs after the 4/2 model operator (the Ah
+    model operator's orders are 4/2, 4/3 and 6/3)."""
     N, dt, steps = 32, 600.0, 3
     op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=order, precision="fp64"))
-    swm.OperatorSWMDiff(op, UV[order], 0.03, H[order], 0.01)
+    swm.OperatorSWMDiff(op, UV[narrow], 0.03, H[narrow], 0.01)
     od = oracle.OracleDomain(N, order)
     J = od.geometry()["J"]
     h, u, v = _state(N)
@@ -77,7 +79,7 @@ def test_model_step_matches_oracle(order):
     op.model_step(x, dt, steps)
     for _ in range(steps):
         h, u, v = od.rk4(h, u, v, dt)
-        h, u, v = od.diffusion_step(h, u, v, dt, 0.03, 0.01, order, order)
+        h, u, v = od.diffusion_step(h, u, v, dt, 0.03, 0.01, narrow, narrow)
     for a, b in zip(x.download(), (h, u, v)):
         assert rel_l2(a, b, J) <= 1e-12
 
@@ -115,7 +117,7 @@ def test_fp32_model_step_tracks_fp64():
         assert rel_l2(a, b, J) <= 1e-5
 
 
-@pytest.mark.parametrize("N,narrow", [(16, 42), (20, 42), (17, 63), (23, 63), (40, 63)])
+@pytest.mark.parametrize("N,narrow", [(16, 42), (20, 42), (17, 63), (23, 63), (40, 63), (8, 21), (40, 21)])
 def test_fp32_diffusion_small_panels(N, narrow):
     """The FP32 Laplacian's tiles at the smallest panels the closures allow,
     where a row tile starts inside the closure rows of one end and reaches
