@@ -32,7 +32,7 @@ def _state(N, seed=5):
     return h, u, v
 
 
-@pytest.mark.parametrize("narrow,N", [(42, 32), (63, 32), (63, 48), (21, 32), (21, 9)])
+@pytest.mark.parametrize("narrow,N", [(42, 32), (63, 32), (63, 48), (21, 32), (21, 17)])
 def test_laplace_matches_oracle(narrow, N):
     op = swm.OperatorSWM(swm.ModelConfig(N=N, sbp_order=42, precision="fp64"))
     od = oracle.OracleDomain(N, 42)
@@ -117,7 +117,7 @@ def test_fp32_model_step_tracks_fp64():
         assert rel_l2(a, b, J) <= 1e-5
 
 
-@pytest.mark.parametrize("N,narrow", [(16, 42), (20, 42), (17, 63), (23, 63), (40, 63), (8, 21), (40, 21)])
+@pytest.mark.parametrize("N,narrow", [(16, 42), (20, 42), (17, 63), (23, 63), (40, 63), (16, 21), (40, 21)])
 def test_fp32_diffusion_small_panels(N, narrow):
     """The FP32 Laplacian's tiles at the smallest panels the closures allow,
     where a row tile starts inside the closure rows of one end and reaches
